@@ -1,0 +1,318 @@
+#!/usr/bin/env python3
+"""Particle-substeps/s of the explicit MLS/APIC step on the 340,489-particle pour.
+
+One bench step = one 1/60 s frame = 432 substeps of Solver.step on the reference
+pour geometry (default GlassProfile filled to 80 %, 192^3 grid on a 0.7 m domain,
+honey eta 10 Pa s, rho 1420, K 9e5, separable floor, domain walls, a tilting
+source glass and a receiver). Inputs are seeded synthetic (cup_fill lattice with
+seeded jitter); no dataset is involved.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the reference's algorithm on the host cores instead:
+the CPU restatement in oracle/ (Warp, the reference's runtime, is not installed),
+all host threads, a bounded sample of the same frame per step.
+
+Under torchrun (N > 1) every rank runs an independent replica of the scene on its
+own GPU (the path has no cross-GPU exchange); value sums all ranks' work over the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+METRIC = "particle-substeps/s on 340k pour"
+UNIT = "particle-substeps/s"
+# algorithmic bytes per unit (particle-substep): x, v, C, F read + write (192 B) and
+# mass + volume read (8 B); grid traffic per active node (56 B) is attributed to the
+# grid kernel, not the particle pass this roofline line describes
+BYTES_PER_PARTICLE_SUBSTEP = 200.0
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["pour", "pour_hb", "dam"], default="pour")
+    ap.add_argument("--n-grid", type=int, default=192)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region (read-only queries)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [c.strip() for c in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(name: str, n_grid: int, solver_cls, **kw):
+    """Returns (solver, frame(i) callable, particles, substeps per step, description)."""
+    from mpm_engine_gb300 import newtonian
+    from mpm_engine_gb300.scenes import dam_break_lattice, pour_scene
+    if name in ("pour", "pour_hb"):
+        mat = None
+        if name == "pour_hb":
+            mat = newtonian(eta=0.0, density=1400.0, bulk_modulus=9.0e5).with_yield(50.0).with_powerlaw(K=20.0, n=0.6)
+        s, src, rcv, traj, S, dt = pour_scene(solver_cls, n_grid=n_grid, material=mat, **kw)
+
+        def frame(i, s=s):
+            t = i / 60.0
+            c, q, v, w = traj.command(t, 1.0 / 60.0)
+            s.set_cup(src, center=c, quat=q, velocity=v, omega=w)
+            s.step(dt, S)
+
+        desc = {"workload": f"pour_{'honey' if name == 'pour' else 'herschel_bulkley'}_{n_grid}^3",
+                "particles": s.n_particles, "substeps_per_step": S, "dt": dt, "grid_lim": 0.7}
+        return s, frame, s.n_particles, S, desc
+    if name == "dam":
+        # dam break: 8 particles per cell over [0.05,0.4]x[0.05,0.6]x[0.05,0.95] of the unit cube,
+        # Newtonian water (eta 1e-2, rho 1000, K 1e4), six sticky planes 3 dx inside the faces
+        from mpm_engine_gb300.solver import GridConfig
+        pos, vol = dam_break_lattice(n_grid, 1.0)
+        s = solver_cls(grid=GridConfig(n_grid=n_grid, grid_lim=1.0), **kw).load_particles(pos, vol)
+        s.set_material(newtonian(eta=1.0e-2, density=1000.0, bulk_modulus=1.0e4), g=[0.0, 0.0, -9.8])
+        dx = 1.0 / n_grid
+        for axis in range(3):
+            for val, nrm in ((3 * dx, 1.0), (1.0 - 3 * dx, -1.0)):
+                p, q = [0.0] * 3, [0.0] * 3
+                p[axis], q[axis] = val, nrm
+                s.add_plane(tuple(p), tuple(q), "sticky")
+        s.add_domain_walls()
+        S, dt = 100, 1.0e-4
+
+        def frame(i, s=s):
+            s.step(dt, S)
+
+        desc = {"workload": f"dam_break_{n_grid}^3", "particles": s.n_particles, "substeps_per_step": S, "dt": dt,
+                "grid_lim": 1.0}
+        return s, frame, s.n_particles, S, desc
+    raise SystemExit(f"unknown workload {name}")
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    """CPU arm: the oracle restatement of the reference step, all host threads."""
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    from oracle.oracle import OracleSolver, build
+    build()
+    threads = os.cpu_count() or 1
+    s, frame, n, S, desc = build_workload(args.workload, args.n_grid, OracleSolver, threads=threads)
+    # bounded sample per step: calibrate substeps so the whole run stays within minutes
+    t0 = time.perf_counter()
+    s.step(s_dt(desc), 1)
+    per = time.perf_counter() - t0
+    m = max(1, min(S, int(args.cpu_seconds / max(per, 1e-6) / max(args.steps + args.warmup, 1))))
+    for _ in range(args.warmup):
+        s.step(s_dt(desc), m)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.step(s_dt(desc), m)
+    el = time.perf_counter() - t0
+    value = n * m * args.steps / el
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {**desc, "sample_substeps_per_step": m, "l2": "n/a (host CPU)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{m} substeps of the {desc['workload']} scene per step (CPU restatement "
+                                       f"of the reference step, not Warp)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def s_dt(desc):
+    return desc["dt"]
+
+
+def cpu_baseline(st, desc, seconds: float):
+    from oracle.oracle import OracleSolver, build
+    build()
+    threads = os.cpu_count() or 1
+    o = OracleSolver.from_state(st, int(desc["workload"].split("_")[-1].split("^")[0]), desc["grid_lim"],
+                                threads=threads)
+    t0 = time.perf_counter()
+    o.step(desc["dt"], 1)
+    per = time.perf_counter() - t0
+    m = max(1, int(seconds / max(per, 1e-6)))
+    t0 = time.perf_counter()
+    o.step(desc["dt"], m)
+    el = time.perf_counter() - t0
+    n = len(st["x"])
+    return {"value": n * m / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{m} substeps of the {desc['workload']} frame state after warm-up "
+                      f"({n} particles; CPU restatement of the reference step, not Warp)"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from mpm_engine_gb300 import Solver
+    from mpm_engine_gb300.build import build_native
+    build_native()
+
+    s, frame, n, S, desc = build_workload(args.workload, args.n_grid, Solver, device=f"cuda:{local}")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")   # 256 MB > L2
+    for i in range(args.warmup):
+        frame(i)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    launches0 = s.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record()
+        frame(args.warmup + k)
+        ev[k][1].record()
+    torch.cuda.synchronize()
+    launches = s.launch_count() - launches0
+    clk = clocks.stop()
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    if dist:
+        t = torch.tensor([total_ms], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * n * S * args.steps / (total_ms / 1e3)
+    ms_per_step = total_ms / args.steps
+
+    # dominant kernel duration: one frame with per-phase CUDA events (live launches)
+    s.profile = True
+    s._eng.lib.gbmpm_profile(s._eng.h, None, None, 1)
+    frame(args.warmup + args.steps)
+    import ctypes as C
+    msv = (C.c_double * 6)()
+    cnt = (C.c_int64 * 6)()
+    s._eng.lib.gbmpm_profile(s._eng.h, msv, cnt, 0)
+    s.profile = False
+    fused_ms = msv[2] / max(cnt[2], 1)
+    grid_ms = msv[3] / max(cnt[3], 1)
+    peak, peak_kind = peaks()
+    achieved = n * BYTES_PER_PARTICLE_SUBSTEP / (fused_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "k_particles (fused G2P2G)", "kernel_ms": fused_ms,
+                "grid_kernel_ms": grid_ms, "peak_kind": peak_kind}
+
+    e2e = None
+    if not args.no_e2e:
+        xh = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+        vh = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+        out = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+        xh.copy_(s.x_torch())
+        vh.copy_(s.v_torch())
+        torch.cuda.synchronize()
+        reps = max(2, min(args.steps, 5))
+        t0 = time.perf_counter()
+        for k in range(reps):
+            s.set_x(xh)
+            s.set_v(vh)
+            frame(args.warmup + args.steps + 1 + k)
+            s.x_into(out)
+            torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        e2e = {"value": world * n * S * reps / el, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 12,
+               "d2h_bytes_per_step": n * 12}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(s.export_state(), desc, args.cpu_seconds)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {**desc, "l2": "256 MB buffer written between timed steps", "parallelism":
+                           "replicas" if world > 1 else "single"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "clocks": clk}
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

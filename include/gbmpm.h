@@ -1,0 +1,218 @@
+/*
+ * gbmpm.h - C ABI of the GB300 MLS/APIC material-point engine.
+ *
+ * One explicit MLS/APIC substep (quadratic B-spline G2P, return mapping and
+ * Kirchhoff stress, P2G, grid update with collider boundary conditions) runs as
+ * hand-written sm_103a CUDA kernels behind these entry points. Every pointer in
+ * gbmpm_particles / gbmpm_grid is a device pointer owned by the caller (the
+ * Python host layer keeps them in PyTorch CUDA tensors and passes data_ptr()).
+ * No entry point takes a torch type; all take plain pointers, sizes and a
+ * cudaStream_t passed as void*.
+ *
+ * Reference interface replaced (warpmpm, Python over NVIDIA Warp):
+ *   gbmpm_engine_create/destroy   MPM_Simulator_WARP.__init__/initialize
+ *                                 (src/warpmpm/kernels/mpm_solver_warp.py:213-504)
+ *   gbmpm_bind                    load_initial_data_from_torch + the state struct
+ *                                 (mpm_solver_warp.py:565-621, kernels/warp_utils.py:23-157)
+ *   gbmpm_set_model               set_parameters_dict / finalize_mu_lam
+ *                                 (mpm_solver_warp.py:634-805)
+ *   gbmpm_set_colliders           add_surface_collider, set_velocity_on_cuboid,
+ *                                 add_revolved_sdf_collider, add_bounding_box,
+ *                                 add_sdf_collider and their pose setters
+ *                                 (mpm_solver_warp.py:1880-2285, 2287-2380, 2621-2814)
+ *   gbmpm_get_colliders           reading back integrated poses (param.point/rot/quat)
+ *   gbmpm_tick                    p2g2p_fused_tick / p2g2p (mpm_solver_warp.py:1092-1546)
+ *   gbmpm_guard                   Solver._update_grid_box edge guard (core/solver.py:485-518)
+ *   gbmpm_wrench / _reset_wrench  cup_wrench, sdf_wrench, tool_force and their resets
+ *                                 (core/solver.py:295-313, 348-361, 415-427)
+ *   gbmpm_sort_particles          Solver._sort_particles + permute_particles
+ *                                 (core/solver.py:454-467, mpm_solver_warp.py:1548-1619)
+ *   gbmpm_rebuild_active_blocks   rebuild_active_blocks (mpm_solver_warp.py:989-1026)
+ *   gbmpm_compute_R / _cov        compute_R_from_F / compute_cov_from_F
+ *                                 (kernels/mpm_utils.py:1234-1285)
+ *   gbmpm_profile                 Solver.profile_report timings (core/solver.py:469-483)
+ *
+ * Return value of every int entry point: GBMPM_OK (0) or a gbmpm_status code;
+ * gbmpm_last_error() gives a one-line message for the calling thread.
+ */
+#ifndef GBMPM_H
+#define GBMPM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBMPM_MAX_MATERIALS 16
+#define GBMPM_MAX_COLLIDERS 32
+#define GBMPM_MAX_SUBSTEPS 8192
+
+typedef enum {
+    GBMPM_OK = 0,
+    GBMPM_ERR_ARG = 1,          /* bad argument (the Python layer raises ValueError) */
+    GBMPM_ERR_CUDA = 2,         /* CUDA runtime error (RuntimeError) */
+    GBMPM_ERR_STATE = 3,        /* called before gbmpm_bind / gbmpm_set_model */
+    GBMPM_ERR_BOUNDS = 4,       /* a kernel bounds check tripped (RuntimeError) */
+    GBMPM_ERR_UNSUPPORTED = 5   /* feature not built (NotImplementedError) */
+} gbmpm_status;
+
+/* Device status word bits, set by kernels, read with gbmpm_guard. */
+#define GBMPM_FLAG_STENCIL_OOB   1u   /* a particle's 3x3x3 stencil left the grid: access skipped */
+#define GBMPM_FLAG_NONFINITE     2u   /* a non-finite particle position was seen */
+#define GBMPM_FLAG_LIST_OVERFLOW 4u   /* the active-block list overflowed (cannot happen by size) */
+
+/* Material ids, pinned by the reference (mpm_solver_warp.py:14-19). */
+enum {
+    GBMPM_MAT_JELLY = 0, GBMPM_MAT_METAL = 1, GBMPM_MAT_SAND = 2, GBMPM_MAT_PLASTICINE = 5,
+    GBMPM_MAT_FLUID = 6, GBMPM_MAT_STATIONARY = 7, GBMPM_MAT_RIGID = 8, GBMPM_MAT_MU_I = 9,
+    GBMPM_MAT_NEWTONIAN = 10, GBMPM_MAT_MU_I_PHI = 11, GBMPM_MAT_TAB_VISCOUS = 12,
+    GBMPM_MAT_TAB_MU_I = 13
+};
+
+/* Particle state, reference layout (warp_utils.py:88-135): vec3 = 3 floats,
+ * mat33 = 9 floats row-major, one record per particle, contiguous. */
+typedef struct {
+    int32_t n;
+    float *x, *v;                       /* [n][3] */
+    float *C, *F, *F_trial, *L, *stress; /* [n][9] */
+    float *mass, *vol, *density, *Jp;   /* [n] */
+    float *mu, *lam, *yield_stress;     /* [n] per-particle model arrays (mpm_solver_warp.py:277-279) */
+    int32_t *material, *selection;      /* [n] */
+    float *cov, *init_cov;              /* [n][6] upper triangle xx,xy,xz,yy,yz,zz, or NULL */
+} gbmpm_particles;
+
+/* Dense n^3 grid, index ((ix*n)+iy)*n+iz (Warp 3-D array order).
+ * mv: scatter target, per node {m*vx, m*vy, m*vz, m}; all zero between substeps.
+ * v : grid velocity after the update and boundary conditions, {vx, vy, vz, 0}.  */
+typedef struct {
+    int32_t n_grid;
+    float *mv;                          /* [n^3][4] */
+    float *v;                           /* [n^3][4] */
+} gbmpm_grid;
+
+/* Model: scalars plus per-material-type tables (MPMModelStruct, warp_utils.py:23-85). */
+typedef struct {
+    int32_t n_grid;
+    float grid_lim, dx, inv_dx;
+    float gravity[3];
+    float rpic_damping;                 /* 0 = APIC, < -0.001 = PIC */
+    float grid_v_damping_scale;         /* applied only when < 1 */
+    int32_t periodic_x;
+    int32_t update_cov_with_F;          /* advect cov each substep (cov_mode "step") */
+    uint32_t material_mask;             /* bit i set when any particle may carry material i */
+    float E[GBMPM_MAX_MATERIALS], nu[GBMPM_MAX_MATERIALS], bulk[GBMPM_MAX_MATERIALS];
+    float hardening[GBMPM_MAX_MATERIALS], xi[GBMPM_MAX_MATERIALS];
+    float plastic_viscosity[GBMPM_MAX_MATERIALS], softening[GBMPM_MAX_MATERIALS];
+    float alpha[GBMPM_MAX_MATERIALS];
+    float muI_mu_s[GBMPM_MAX_MATERIALS], muI_delta_mu[GBMPM_MAX_MATERIALS];
+    float muI_I0[GBMPM_MAX_MATERIALS], muI_d[GBMPM_MAX_MATERIALS];
+    float muI_rho_s[GBMPM_MAX_MATERIALS], muI_phi_init[GBMPM_MAX_MATERIALS];
+    float muI_phi_chi[GBMPM_MAX_MATERIALS];
+    const float *eta_table;             /* eta_table_n samples; device pointer for the CUDA library */
+    int32_t eta_table_n;
+    float eta_table_smin, eta_table_smax;
+} gbmpm_model;
+
+/* Collider kinds (grid boundary conditions, applied in list order per node). */
+enum {
+    GBMPM_COLLIDER_PLANE = 0,   /* add_plane: surface 0 sticky, 1 slip, 2 separable, 11 cut */
+    GBMPM_COLLIDER_BOX = 1,     /* add_box: kinematic velocity overwrite + impulse */
+    GBMPM_COLLIDER_CUP = 2,     /* add_cup: analytic revolved-SDF glass, force + torque */
+    GBMPM_COLLIDER_WALLS = 3,   /* add_domain_walls: 3-cell shells at the six faces */
+    GBMPM_COLLIDER_SDF = 4      /* add_sdf_collider: trilinear voxel SDF, force + torque */
+};
+
+typedef struct {
+    int32_t kind;
+    int32_t surface_type;       /* plane / sdf surface type */
+    int32_t reset;              /* box legacy reset flag */
+    int32_t sdf_res;
+    float start_time, end_time;
+    float point[3];             /* plane point | box, cup or sdf centre (fp32, as in the Warp struct) */
+    float normal[3];            /* plane unit normal */
+    float size[3];              /* box half extents */
+    float velocity[3];
+    float omega[3];
+    float rot[9];               /* cup local->world rotation, row-major fp32 */
+    float quat[4];              /* sdf body->world rotation, x y z w */
+    float friction;
+    float outer_radius, inner_radius, half_height, inner_floor_z, fillet_radius;
+    float sticky_depth, contact_band;
+    float sdf_origin[3];
+    float sdf_cell, band;
+    const float *sdf_val;       /* [res^3] (device pointer for the CUDA library) */
+    const float *sdf_grad;      /* [res^3][3] */
+    double rot64[9];            /* cup: float64 rotation shadow (mpm_solver_warp.py:2227-2254) */
+} gbmpm_collider;
+
+/* gbmpm_tick flags */
+#define GBMPM_TICK_FUSED   1    /* fused G2P2G pipeline (Solver.fused) */
+#define GBMPM_TICK_GRAPH   2    /* replay the tick as one captured CUDA graph when possible */
+#define GBMPM_TICK_PROFILE 4    /* per-phase CUDA-event timing, live launches */
+
+#define GBMPM_NUM_PHASES 6      /* stress, p2g, g2p2g_fused, grid_update, g2p, guard */
+
+typedef struct gbmpm_engine gbmpm_engine;
+
+const char *gbmpm_last_error(void);
+const char *gbmpm_phase_name(int32_t phase);
+
+/* Lifecycle. create selects the current CUDA device; destroy frees engine-owned
+ * scratch (collider tables, block lists, sort scratch), never caller buffers. */
+int gbmpm_engine_create(gbmpm_engine **out);
+void gbmpm_engine_destroy(gbmpm_engine *e);
+
+/* Bind caller-owned device buffers. Pointers must stay valid and stable until
+ * the next bind (captured CUDA graphs bake them in). */
+int gbmpm_bind(gbmpm_engine *e, const gbmpm_particles *p, const gbmpm_grid *g);
+int gbmpm_set_model(gbmpm_engine *e, const gbmpm_model *m);
+
+/* Replace the collider list. Wrench accumulators of indices that already
+ * existed are kept; new indices start at zero. */
+int gbmpm_set_colliders(gbmpm_engine *e, const gbmpm_collider *c, int32_t n);
+/* Copy the engine's current collider records (poses integrated by ticks). */
+int gbmpm_get_colliders(gbmpm_engine *e, gbmpm_collider *c, int32_t n);
+
+/* Advance `substeps` substeps of size dt. *time is the simulation clock in
+ * float64 (Python float in the reference); it advances by dt per substep. */
+int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps,
+               int32_t flags, void *stream);
+
+/* Edge guard: out = {min x, min y, min z, max x, max y, max z, max |v_i|}
+ * over all particles, and *status = the device status word (then cleared).
+ * Synchronizes the stream. */
+int gbmpm_guard(gbmpm_engine *e, float out[7], uint32_t *status, void *stream);
+
+/* Reaction impulse accumulated since the last reset: {fx, fy, fz, tx, ty, tz}. */
+int gbmpm_wrench(gbmpm_engine *e, int32_t collider, double out[6], void *stream);
+int gbmpm_reset_wrench(gbmpm_engine *e, int32_t collider, void *stream);
+
+/* Block-key sort: key = ((bx*nb + by)*nb + bz), b = floor(x/dx - 0.5) >> 2 in
+ * float64, nb = (n_grid >> 2) + 2; stable; skipped when keys are already
+ * non-decreasing (*sorted_out = 0). On a sort every per-particle array (and
+ * perm_out, when not NULL, the int32 permutation) is rewritten in place. */
+int gbmpm_sort_particles(gbmpm_engine *e, double dx, int32_t *sorted_out,
+                         int32_t *perm_out, void *stream);
+
+/* Active 4^3 blocks: mark (fp32 truncation), dilate by one block, compact.
+ * counts = {current, union with previous}. Synchronizes the stream. */
+int gbmpm_rebuild_active_blocks(gbmpm_engine *e, int32_t counts[2], void *stream);
+
+/* Exports: R_out[n][9] receives R^T of the polar rotation of F_trial;
+ * cov_out[n][6] receives F_trial * init_cov * F_trial^T. */
+int gbmpm_compute_R(gbmpm_engine *e, float *R_out, void *stream);
+int gbmpm_compute_cov(gbmpm_engine *e, float *cov_out, void *stream);
+
+/* Per-phase device milliseconds accumulated while GBMPM_TICK_PROFILE was set. */
+int gbmpm_profile(gbmpm_engine *e, double ms_out[GBMPM_NUM_PHASES],
+                  int64_t count_out[GBMPM_NUM_PHASES], int32_t reset);
+
+/* Number of kernels this engine has launched (graph replays count each node). */
+int64_t gbmpm_launch_count(gbmpm_engine *e);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBMPM_H */

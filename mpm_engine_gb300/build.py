@@ -1,0 +1,51 @@
+"""In-tree build of the native library (nvcc, sm_103a only).
+
+Outputs mpm_engine_gb300/_build/libgbmpm.so. The build is a single nvcc call;
+nothing is installed into site-packages.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+PACKAGE_DIR = Path(__file__).resolve().parent
+REPO = PACKAGE_DIR.parent
+CSRC = PACKAGE_DIR / "csrc"
+OUT_DIR = PACKAGE_DIR / "_build"
+GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
+
+
+def nvcc_path() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found (CUDA toolkit required to build libgbmpm.so)")
+
+
+def sources() -> list[Path]:
+    return sorted(CSRC.glob("*.cu"))
+
+
+def build_native(verbose: bool = False, force: bool = False) -> Path:
+    OUT_DIR.mkdir(parents=True, exist_ok=True)
+    out = OUT_DIR / "libgbmpm.so"
+    deps = sources() + sorted(CSRC.glob("*.cuh")) + [REPO / "include" / "gbmpm.h"]
+    if out.exists() and not force and all(out.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return out
+    cmd = [nvcc_path(), GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+           "-I", str(REPO / "include"), "-o", str(out)] + [str(s) for s in sources()]
+    if verbose:
+        cmd.insert(1, "-Xptxas=-v")
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("nvcc failed:\n" + res.stdout + res.stderr)
+    if verbose:
+        print(res.stdout + res.stderr)
+    return out
+
+
+if __name__ == "__main__":
+    import sys
+    print(build_native(verbose="-v" in sys.argv, force="-f" in sys.argv))

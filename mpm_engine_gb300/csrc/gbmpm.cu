@@ -1,0 +1,1754 @@
+// gbmpm.cu - the GB300 MLS/APIC substep: particle kernels, grid kernel, block
+// sort, exports, and the C ABI declared in include/gbmpm.h.
+//
+// Data layout in HBM
+//   particles: the reference's per-particle records (x vec3, F mat33 row-major,
+//              ...), caller-owned (PyTorch tensors), read and written in place.
+//   grid:      mv[n^3] float4 {m vx, m vy, m vz, m}, the scatter target, kept
+//              all-zero between substeps; v[n^3] float4 {vx, vy, vz, 0}, the
+//              updated grid velocity the gather reads.
+//   blocks:    one int flag per 4^3 node block plus two block lists. A particle
+//              pass appends each block its stencils touch (first toucher wins the
+//              flag); the grid pass that follows visits exactly those blocks,
+//              updates, applies the colliders, and clears mv and the flags. The
+//              grid update therefore costs O(active nodes), with no host-side
+//              box and no per-substep host round trip.
+//
+// One tick of S substeps is S+1 particle passes and S grid passes (the
+// reference's fused schedule, mpm_solver_warp.py:1379-1546), replayed as a
+// single CUDA graph. Collider poses for every substep are integrated on the host
+// in float64 once per tick (the reference's modify_bc callables) and uploaded as
+// one table, so the graph needs no host work between substeps.
+
+#include "../../include/gbmpm.h"
+#include "svd3.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace gbmpm {
+
+// ------------------------------------------------------------ constants ----
+constexpr int kMaxCol = GBMPM_MAX_COLLIDERS;
+constexpr int kParticleThreads = 128;
+constexpr int kGridThreads = 256;
+
+enum PassMode : int {
+    PASS_G2P = 1,        // gather from grid v, advect, C, L, F_trial
+    PASS_STRESS = 2,     // return map + Kirchhoff stress
+    PASS_P2G = 4,        // scatter into grid mv, mark blocks
+    PASS_STORE_ALL = 8,  // also store stress (last stress of the tick)
+    PASS_STORE_VC = 16,  // store v and C after the gather
+    PASS_RESET_LISTS = 32
+};
+
+struct MatTables {
+    float E[16], nu[16], bulk[16], hardening[16], xi[16], pv[16], softening[16], alpha[16];
+    float mu_s[16], dmu[16], I0[16], d[16], rho_s[16], phi_init[16], phi_chi[16];
+};
+
+struct PK {
+    float *x, *v, *C, *F, *Ft, *L, *S;
+    const float *mass, *vol;
+    float *Jp, *mu, *lam, *ys;
+    const int *mat, *sel;
+    float *cov;
+    int n;
+    const float4 *gv;
+    float4 *gmv;
+    int ng;
+    float dx, inv_dx, dt, rpic;
+    int periodic_x, update_cov;
+    const MatTables *tab;
+    const float *eta;
+    int eta_n;
+    float eta_smin, eta_smax;
+    int *blk_flag, *blk_list, *blk_count;
+    int bd;
+    unsigned *status;
+};
+
+// Per-substep collider pose record, built on the host each tick.
+struct PoseRec {
+    float p[3];
+    int mode;     // 0 inactive, 1 live, 2 box reset-zero
+    float r[9];   // cup rotation
+    float q[4];   // sdf quaternion
+    float pad[2];
+};
+
+struct ColDev {
+    int kind, surface, sdf_res, pad0;
+    float normal[3], size[3], vel[3], omega[3];
+    float friction, outer_r, inner_r, half_h, floor_z, fillet, sticky, band_c;
+    float origin[3], cell, band;
+    const float *sdf_val, *sdf_grad;
+};
+
+struct GK {
+    float4 *gmv;
+    float4 *gv;
+    int ng;
+    float dx, dt;
+    float g[3];
+    float damp;
+    int ncol;
+    const ColDev *cols;
+    const PoseRec *poses;   // [ncol] for this substep
+    double *wrench;         // [ncol][6]
+    int *blk_flag, *blk_list, *blk_count_read, *blk_count_reset;
+    int bd;
+};
+
+// ------------------------------------------------------------- helpers -----
+__device__ __forceinline__ void mat_load(const float *p, float (&m)[9]) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) m[i] = p[i];
+}
+__device__ __forceinline__ void mat_store(float *p, const float (&m)[9]) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) p[i] = m[i];
+}
+__device__ __forceinline__ void mm(const float *a, const float *b, float *c) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            c[3 * i + j] = a[3 * i] * b[j] + a[3 * i + 1] * b[3 + j] + a[3 * i + 2] * b[6 + j];
+}
+// c = a * b^T
+__device__ __forceinline__ void mmT(const float *a, const float *b, float *c) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            c[3 * i + j] = a[3 * i] * b[3 * j] + a[3 * i + 1] * b[3 * j + 1] + a[3 * i + 2] * b[3 * j + 2];
+}
+__device__ __forceinline__ float det3(const float *m) {
+    return m[0] * (m[4] * m[8] - m[5] * m[7]) + m[1] * (m[5] * m[6] - m[3] * m[8]) +
+           m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+// U diag(d) V^T
+__device__ __forceinline__ void udvt(const float *U, float d0, float d1, float d2, const float *V, float *out) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            out[3 * i + j] = U[3 * i] * d0 * V[3 * j] + U[3 * i + 1] * d1 * V[3 * j + 1] + U[3 * i + 2] * d2 * V[3 * j + 2];
+}
+
+__device__ __forceinline__ void set_status(unsigned *st, unsigned bit) { atomicOr(st, bit); }
+
+// ------------------------------------------------------- material laws -----
+// Kirchhoff stress of the viscous laws (mpm_utils.py:17-85)
+__device__ __forceinline__ void dev_rate(const float *L, float *Dd, float &gd) {
+    float D[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) D[3 * i + j] = 0.5f * (L[3 * i + j] + L[3 * j + i]);
+    float trd = (D[0] + D[4] + D[8]) / 3.0f;
+    float dd = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        Dd[i] = D[i] - ((i % 4 == 0) ? trd : 0.0f);
+        dd += Dd[i] * Dd[i];
+    }
+    gd = sqrtf(2.0f * dd + 0.02f * 0.02f);
+}
+
+__device__ __forceinline__ float eos_pressure(float J, float bulk) { return -bulk * (powf(J, -1.1f) - 1.0f); }
+
+__device__ __forceinline__ float table_lerp(const float *tab, int n, float smin, float smax, float s) {
+    float idx = (s - smin) / (smax - smin) * (float)(n - 1);
+    idx = fminf(fmaxf(idx, 0.0f), (float)(n - 1) - 1.0e-6f);
+    int i0 = (int)floorf(idx);
+    float fr = idx - (float)i0;
+    return tab[i0] * (1.0f - fr) + tab[i0 + 1] * fr;
+}
+
+// Hencky stress U diag(2 mu eps + lam tr eps) U^T (mpm_utils.py:228-243)
+__device__ __forceinline__ void stress_hencky(const float *U, const float *sig, float mu, float lam, float *out) {
+    float e0 = logf(fmaxf(sig[0], 1e-6f)), e1 = logf(fmaxf(sig[1], 1e-6f)), e2 = logf(fmaxf(sig[2], 1e-6f));
+    float tr = e0 + e1 + e2;
+    udvt(U, 2.0f * mu * e0 + lam * tr, 2.0f * mu * e1 + lam * tr, 2.0f * mu * e2 + lam * tr, U, out);
+}
+
+// the 48-step bisection on g(gdp) = tau_bar - G dt gdp - mu(I) p (mpm_utils.py:300-312)
+template <bool TAB>
+__device__ __forceinline__ float mu_i_bisect(float tbK, float G, float dt, float pK, float Ic, float mu_s, float dmu,
+                                             float I0, const PK &k) {
+    float lo = 0.0f, hi = tbK / (G * dt);
+    for (int it = 0; it < 48; ++it) {
+        float mid = 0.5f * (lo + hi);
+        float Im = mid * Ic;
+        float mu_mid;
+        if (!TAB) mu_mid = mu_s + dmu * Im / (Im + I0);
+        else mu_mid = table_lerp(k.eta, k.eta_n, k.eta_smin, k.eta_smax, logf(fmaxf(Im, 1e-12f)) * 0.43429448190325176f);
+        float g = tbK - G * dt * mid - mu_mid * pK;
+        if (g > 0.0f) lo = mid; else hi = mid;
+    }
+    return 0.5f * (lo + hi);
+}
+
+// Return map F_trial -> F and Kirchhoff stress for one particle
+// (stress_update_particle, mpm_utils.py:1056-1149).
+template <bool SOLIDS>
+__device__ __forceinline__ void stress_update(const PK &k, int p, int mat, const float *Ft, const float *L, float *F,
+                                              float *S) {
+    const MatTables &T = *k.tab;
+    if (!SOLIDS || mat == 6 || mat == 10 || mat == 12 || mat == 7 || mat == 8) {
+        float J;
+        if (mat == 7 || mat == 8) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) F[i] = (i % 4 == 0) ? 1.0f : 0.0f;
+            J = 1.0f;
+        } else {
+            float Jt = det3(Ft);
+            float Jc = powf(Jt, 1.0f / 3.0f);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) F[i] = (i % 4 == 0) ? Jc : 0.0f;
+            J = Jc * Jc * Jc;
+        }
+        if (mat == 7 || mat == 8) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) S[i] = 0.0f;
+            return;
+        }
+        float pr = eos_pressure(J, T.bulk[mat]);
+        if (mat == 6) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) S[i] = (i % 4 == 0) ? J * pr : 0.0f;
+            return;
+        }
+        float Dd[9], gd;
+        dev_rate(L, Dd, gd);
+        float eta_app;
+        if (mat == 10) eta_app = T.pv[mat] + k.ys[p] / gd + T.hardening[mat] * powf(gd, T.softening[mat] - 1.0f);
+        else eta_app = table_lerp(k.eta, k.eta_n, k.eta_smin, k.eta_smax, logf(gd) * 0.43429448190325176f);
+        float two_eta = 2.0f * eta_app;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) S[i] = J * (((i % 4 == 0) ? pr : 0.0f) + two_eta * Dd[i]);
+        return;
+    }
+    if constexpr (SOLIDS) {
+        float U[9], V[9], sig[3];
+        float mu = k.mu[p], lam = k.lam[p];
+        // ---- return mapping
+        if (mat == 1 || mat == 5) {  // von Mises (mpm_utils.py:127-225)
+            svd3(Ft, U, sig, V);
+            float e0 = logf(fmaxf(sig[0], 0.01f)), e1 = logf(fmaxf(sig[1], 0.01f)), e2 = logf(fmaxf(sig[2], 0.01f));
+            float tr = e0 + e1 + e2;
+            float temp = tr / 3.0f;
+            float t0 = 2.0f * mu * e0 + lam * tr, t1 = 2.0f * mu * e1 + lam * tr, t2 = 2.0f * mu * e2 + lam * tr;
+            float st = (t0 + t1 + t2) / 3.0f;
+            float c0 = t0 - st, c1 = t1 - st, c2 = t2 - st;
+            float y = k.ys[p];
+            bool done = false;
+            if (sqrtf(c0 * c0 + c1 * c1 + c2 * c2) > y) {
+                if (mat == 5 && y <= 0.0f) {
+#pragma unroll
+                    for (int i = 0; i < 9; ++i) F[i] = Ft[i];
+                    done = true;
+                } else {
+                    float h0 = e0 - temp, h1 = e1 - temp, h2 = e2 - temp;
+                    float hn = sqrtf(h0 * h0 + h1 * h1 + h2 * h2) + 1e-6f;
+                    float dg = hn - y / (2.0f * mu);
+                    float r = dg / hn;
+                    e0 -= r * h0; e1 -= r * h1; e2 -= r * h2;
+                    if (mat == 5) {
+                        float rh0 = r * h0, rh1 = r * h1, rh2 = r * h2;
+                        y = y - T.softening[mat] * sqrtf(rh0 * rh0 + rh1 * rh1 + rh2 * rh2);
+                        if (y <= 0.0f) { mu = 0.0f; lam = 0.0f; k.mu[p] = 0.0f; k.lam[p] = 0.0f; }
+                    }
+                    udvt(U, expf(e0), expf(e1), expf(e2), V, F);
+                    if (T.hardening[mat] > 0.5f) y = y + 2.0f * mu * T.xi[mat] * dg;
+                    k.ys[p] = y;
+                    done = true;
+                }
+            }
+            if (!done) {
+#pragma unroll
+                for (int i = 0; i < 9; ++i) F[i] = Ft[i];
+            }
+        } else if (mat == 2) {  // Drucker-Prager sand (mpm_utils.py:543-580)
+            svd3(Ft, U, sig, V);
+            float e0 = logf(fmaxf(fabsf(sig[0]), 1e-14f)), e1 = logf(fmaxf(fabsf(sig[1]), 1e-14f)),
+                  e2 = logf(fmaxf(fabsf(sig[2]), 1e-14f));
+            float tr = e0 + e1 + e2;
+            float h0 = e0 - tr / 3.0f, h1 = e1 - tr / 3.0f, h2 = e2 - tr / 3.0f;
+            float hn = sqrtf(h0 * h0 + h1 * h1 + h2 * h2);
+            float dg = hn + (3.0f * lam + 2.0f * mu) / (2.0f * mu) * tr * T.alpha[mat];
+            if (dg <= 0.0f) {
+#pragma unroll
+                for (int i = 0; i < 9; ++i) F[i] = Ft[i];
+            } else if (tr > 0.0f) {
+                udvt(U, 1.0f, 1.0f, 1.0f, V, F);
+            } else {
+                float r = dg / hn;
+                udvt(U, expf(e0 - h0 * r), expf(e1 - h1 * r), expf(e2 - h2 * r), V, F);
+            }
+        } else if (mat == 9 || mat == 13 || mat == 11) {  // mu(I) family (mpm_utils.py:246-522)
+            svd3(Ft, U, sig, V);
+            float s0 = fmaxf(fabsf(sig[0]), 1e-6f), s1 = fmaxf(fabsf(sig[1]), 1e-6f), s2 = fmaxf(fabsf(sig[2]), 1e-6f);
+            float e0 = logf(s0), e1 = logf(s1), e2 = logf(s2);
+            float tr = e0 + e1 + e2;
+            float mean = tr / 3.0f;
+            float d0 = e0 - mean, d1 = e1 - mean, d2 = e2 - mean;
+            float dn = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+            float J = s0 * s1 * s2;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) F[i] = Ft[i];
+            if (mat != 11) {
+                if (tr >= 0.0f) {
+                    udvt(U, 1.0f, 1.0f, 1.0f, V, F);
+                } else {
+                    float pK = -(2.0f * mu / 3.0f + lam) * tr;
+                    float tbK = 2.0f * mu * dn / sqrtf(2.0f);
+                    float pC = pK / J;
+                    float thr = (mat == 13) ? k.eta[0] : T.mu_s[mat];
+                    if (tbK > thr * pK) {
+                        float Ic = T.d[mat] * sqrtf(T.rho_s[mat] / pC);
+                        float gdp = (mat == 13) ? mu_i_bisect<true>(tbK, mu, k.dt, pK, Ic, 0, 0, 0, k)
+                                                : mu_i_bisect<false>(tbK, mu, k.dt, pK, Ic, T.mu_s[mat], T.dmu[mat],
+                                                                     T.I0[mat], k);
+                        float sc = (tbK - mu * k.dt * gdp) / fmaxf(tbK, 1e-20f);
+                        udvt(U, expf(d0 * sc + mean), expf(d1 * sc + mean), expf(d2 * sc + mean), V, F);
+                    }
+                }
+            } else {
+                float Jr = k.Jp[p];
+                if (Jr < 0.5f) Jr = 1.0f;
+                float K = T.E[mat] / (3.0f * (1.0f - 2.0f * T.nu[mat]));
+                float pc = fmaxf(K * (Jr / fmaxf(J, 1e-6f) - 1.0f), 0.0f);
+                float jp_new = Jr;
+                if (pc <= 0.0f) {
+                    float si = expf(mean);
+                    udvt(U, si, si, si, V, F);
+                } else {
+                    float pK = pc * J;
+                    float tbK = 2.0f * mu * dn / sqrtf(2.0f);
+                    if (tbK > T.mu_s[mat] * pK) {
+                        float Ic = T.d[mat] * sqrtf(T.rho_s[mat] / pc);
+                        float gdp = mu_i_bisect<false>(tbK, mu, k.dt, pK, Ic, T.mu_s[mat], T.dmu[mat], T.I0[mat], k);
+                        float Ir = gdp * Ic;
+                        float dgam = fminf(8.0f * gdp * k.dt, 1.0f);
+                        float jcs = 1.0f / fmaxf(1.0f - T.phi_chi[mat] * Ir / (Ir + T.I0[mat]), 1e-3f);
+                        jp_new = Jr + dgam * (jcs - Jr);
+                        float sc = (tbK - mu * k.dt * gdp) / fmaxf(tbK, 1e-20f);
+                        udvt(U, expf(d0 * sc + mean), expf(d1 * sc + mean), expf(d2 * sc + mean), V, F);
+                    }
+                }
+                k.Jp[p] = jp_new;
+            }
+        } else {  // jelly (0) and any unknown id: F = F_trial
+#pragma unroll
+            for (int i = 0; i < 9; ++i) F[i] = Ft[i];
+        }
+        // ---- stress of the returned F
+        float J = det3(F);
+        svd3(F, U, sig, V);
+        if (mat == 0 || mat == 5) {  // FCR (mpm_utils.py:8-15)
+            float R[9], FR[9];
+            mmT(U, V, R);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) FR[i] = 2.0f * mu * (F[i] - R[i]);
+            mmT(FR, F, S);
+            float dl = lam * J * (J - 1.0f);
+            S[0] += dl; S[4] += dl; S[8] += dl;
+        } else if (mat == 1 || mat == 9 || mat == 13) {
+            stress_hencky(U, sig, mu, lam, S);
+        } else if (mat == 2) {  // Drucker-Prager stress (mpm_utils.py:109-124)
+            float l0 = logf(sig[0]), l1 = logf(sig[1]), l2 = logf(sig[2]);
+            float ls = l0 + l1 + l2;
+            float c0 = (2.0f * mu * l0 + lam * ls) / sig[0];
+            float c1 = (2.0f * mu * l1 + lam * ls) / sig[1];
+            float c2 = (2.0f * mu * l2 + lam * ls) / sig[2];
+            float T1[9];
+            udvt(U, c0, c1, c2, V, T1);
+            mmT(T1, F, S);
+        } else if (mat == 11) {  // mu(I)-Phi(I) stress (mpm_utils.py:525-540)
+            float Jr = k.Jp[p];
+            if (Jr < 0.5f) Jr = 1.0f;
+            float K = T.E[mat] / (3.0f * (1.0f - 2.0f * T.nu[mat]));
+            float pc = fmaxf(K * (Jr / fmaxf(J, 1e-6f) - 1.0f), 0.0f);
+            float s0 = fmaxf(sig[0], 1e-6f), s1 = fmaxf(sig[1], 1e-6f), s2 = fmaxf(sig[2], 1e-6f);
+            float e0 = logf(s0), e1 = logf(s1), e2 = logf(s2);
+            float Jc = s0 * s1 * s2;
+            float mean = (e0 + e1 + e2) / 3.0f;
+            float iso = -pc * Jc;
+            udvt(U, 2.0f * mu * (e0 - mean) + iso, 2.0f * mu * (e1 - mean) + iso, 2.0f * mu * (e2 - mean) + iso, U, S);
+        } else {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) S[i] = 0.0f;
+        }
+        // symmetrize (mpm_utils.py:1148)
+        float s01 = 0.5f * (S[1] + S[3]), s02 = 0.5f * (S[2] + S[6]), s12 = 0.5f * (S[5] + S[7]);
+        S[1] = S[3] = s01; S[2] = S[6] = s02; S[5] = S[7] = s12;
+    }
+}
+
+// ------------------------------------------------------ particle pass ------
+struct Stencil {
+    int b[3];
+    float fx[3];
+    float w[3][3], dw[3][3];
+};
+
+__device__ __forceinline__ void stencil(const float *x, float inv_dx, Stencil &s) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float gp = x[a] * inv_dx;
+        s.b[a] = (int)floorf(gp - 0.5f);
+        float fx = gp - (float)s.b[a];
+        s.fx[a] = fx;
+        float wa = 1.5f - fx, wb = fx - 1.0f, wc = fx - 0.5f;
+        s.w[a][0] = 0.5f * (wa * wa);
+        s.w[a][1] = 0.75f - wb * wb;
+        s.w[a][2] = 0.5f * (wc * wc);
+        s.dw[a][0] = fx - 1.5f;
+        s.dw[a][1] = -2.0f * wb;
+        s.dw[a][2] = wc;
+    }
+}
+
+// true when the 3x3x3 stencil lies inside the grid (x wraps when periodic)
+__device__ __forceinline__ bool stencil_ok(const Stencil &s, int ng, int periodic_x) {
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (a == 0 && periodic_x) continue;
+        ok = ok && s.b[a] >= 0 && s.b[a] + 2 < ng;
+    }
+    return ok;
+}
+
+__device__ __forceinline__ int wrap(int i, int n) { return ((i % n) + n) % n; }
+
+__device__ __forceinline__ void mark_block(const PK &k, int bx, int by, int bz) {
+    int b = (bx * k.bd + by) * k.bd + bz;
+    if (k.blk_flag[b] == 0 && atomicExch(&k.blk_flag[b], 1) == 0) {
+        int i = atomicAdd(k.blk_count, 1);
+        k.blk_list[i] = b;
+    }
+}
+
+// One kernel serves every particle pass of the schedule; `mode` selects the
+// stages (G2P, STRESS, P2G) so the fused interior pass is G2P|STRESS|P2G, the
+// tick prologue STRESS|P2G and the epilogue G2P.
+template <bool SOLIDS>
+__global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) {
+    if ((mode & PASS_RESET_LISTS) && blockIdx.x == 0 && threadIdx.x == 0) {
+        k.blk_count[0] = 0;
+        k.blk_count[1] = 0;
+    }
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= k.n) return;
+    if (k.sel && k.sel[p] != 0) return;
+    const int mat = k.mat[p];
+    float x[3] = {k.x[3 * p], k.x[3 * p + 1], k.x[3 * p + 2]};
+    float v[3], C[9], L[9], Ft[9];
+    bool gathered = false;
+    if ((mode & PASS_G2P) && mat != 7 && mat != 8) {
+        Stencil s;
+        stencil(x, k.inv_dx, s);
+        if (!stencil_ok(s, k.ng, k.periodic_x)) {
+            set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
+            return;
+        }
+        float nv[3] = {0.f, 0.f, 0.f};
+        float nC[9], nL[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) { nC[i] = 0.f; nL[i] = 0.f; }
+        const float c4 = k.inv_dx * 4.0f;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            int ix = s.b[0] + i;
+            if (k.periodic_x) ix = wrap(ix, k.ng);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                float wij = s.w[0][i] * s.w[1][j];
+                float dwi_j = s.dw[0][i] * s.w[1][j];
+                float wi_dj = s.w[0][i] * s.dw[1][j];
+                const float4 *row = k.gv + ((size_t)ix * k.ng + (s.b[1] + j)) * k.ng + s.b[2];
+#pragma unroll
+                for (int kk = 0; kk < 3; ++kk) {
+                    float4 g = __ldg(row + kk);
+                    float wt = wij * s.w[2][kk];
+                    float dp0 = (float)i - s.fx[0], dp1 = (float)j - s.fx[1], dp2 = (float)kk - s.fx[2];
+                    float gx = dwi_j * s.w[2][kk] * k.inv_dx;
+                    float gy = wi_dj * s.w[2][kk] * k.inv_dx;
+                    float gz = wij * s.dw[2][kk] * k.inv_dx;
+                    float cw = wt * c4;
+                    float gvv[3] = {g.x, g.y, g.z};
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        nv[a] += gvv[a] * wt;
+                        float ga = gvv[a] * cw;
+                        nC[3 * a + 0] += ga * dp0;
+                        nC[3 * a + 1] += ga * dp1;
+                        nC[3 * a + 2] += ga * dp2;
+                        nL[3 * a + 0] += gvv[a] * gx;
+                        nL[3 * a + 1] += gvv[a] * gy;
+                        nL[3 * a + 2] += gvv[a] * gz;
+                    }
+                }
+            }
+        }
+        float xn[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) { v[a] = nv[a]; xn[a] = x[a] + k.dt * nv[a]; }
+        if (k.periodic_x) {
+            float lx = (float)k.ng * k.dx;
+            if (xn[0] < 0.0f) xn[0] += lx;
+            if (xn[0] >= lx) xn[0] -= lx;
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) x[a] = xn[a];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) { C[i] = nC[i]; L[i] = nL[i]; }
+        float Fo[9], A[9];
+        mat_load(k.F + 9 * (size_t)p, Fo);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) A[i] = ((i % 4 == 0) ? 1.0f : 0.0f) + L[i] * k.dt;
+        mm(A, Fo, Ft);
+        if (k.update_cov && k.cov) {
+            float *c6 = k.cov + 6 * (size_t)p;
+            float cn[9] = {c6[0], c6[1], c6[2], c6[1], c6[3], c6[4], c6[2], c6[4], c6[5]};
+            float a1[9], a2[9];
+            mm(L, cn, a1);
+            mmT(cn, L, a2);
+            c6[0] = cn[0] + k.dt * (a1[0] + a2[0]);
+            c6[1] = cn[1] + k.dt * (a1[1] + a2[1]);
+            c6[2] = cn[2] + k.dt * (a1[2] + a2[2]);
+            c6[3] = cn[4] + k.dt * (a1[4] + a2[4]);
+            c6[4] = cn[5] + k.dt * (a1[5] + a2[5]);
+            c6[5] = cn[8] + k.dt * (a1[8] + a2[8]);
+        }
+        gathered = true;
+        float *xo = k.x + 3 * (size_t)p;
+        xo[0] = x[0]; xo[1] = x[1]; xo[2] = x[2];
+        if (!(mode & (PASS_STRESS | PASS_P2G)) || (mode & PASS_STORE_VC)) {
+            float *vo = k.v + 3 * (size_t)p;
+            vo[0] = v[0]; vo[1] = v[1]; vo[2] = v[2];
+            mat_store(k.C + 9 * (size_t)p, C);
+        }
+        if (!(mode & PASS_STRESS)) {
+            mat_store(k.L + 9 * (size_t)p, L);
+            mat_store(k.Ft + 9 * (size_t)p, Ft);
+        }
+    }
+    float S[9];
+    if (mode & PASS_STRESS) {
+        if (!gathered) {
+            mat_load(k.Ft + 9 * (size_t)p, Ft);
+            mat_load(k.L + 9 * (size_t)p, L);
+        }
+        float Fn[9];
+        stress_update<SOLIDS>(k, p, mat, Ft, L, Fn, S);
+        mat_store(k.F + 9 * (size_t)p, Fn);
+        if (mode & PASS_STORE_ALL) mat_store(k.S + 9 * (size_t)p, S);
+    }
+    if (mode & PASS_P2G) {
+        if (!(mode & PASS_STRESS)) mat_load(k.S + 9 * (size_t)p, S);
+        if (!gathered) {
+            const float *vi = k.v + 3 * (size_t)p;
+            v[0] = vi[0]; v[1] = vi[1]; v[2] = vi[2];
+            mat_load(k.C + 9 * (size_t)p, C);
+        }
+        Stencil s;
+        stencil(x, k.inv_dx, s);
+        if (!stencil_ok(s, k.ng, k.periodic_x)) {
+            set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
+            return;
+        }
+        if (k.rpic != 0.0f) {
+            float Cn[9];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                    Cn[3 * i + j] = (1.0f - k.rpic) * C[3 * i + j] + k.rpic / 2.0f * (C[3 * i + j] - C[3 * j + i]);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) C[i] = (k.rpic < -0.001f) ? 0.0f : Cn[i];
+        }
+        const float m = k.mass[p];
+        const float fs = -k.vol[p] * k.dt * k.inv_dx;   // stress term scale
+        float A[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) A[i] = fs * S[i];
+        // affine momentum m (v + C dpos dx): precompute m v - m C fx dx and m C dx
+        float mCdx[9], base[3];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) mCdx[i] = m * C[i] * k.dx;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            base[a] = m * v[a] - (mCdx[3 * a] * s.fx[0] + mCdx[3 * a + 1] * s.fx[1] + mCdx[3 * a + 2] * s.fx[2]);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            int ix = s.b[0] + i;
+            if (k.periodic_x) ix = wrap(ix, k.ng);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                float wij = s.w[0][i] * s.w[1][j];
+                float dwi_j = s.dw[0][i] * s.w[1][j];
+                float wi_dj = s.w[0][i] * s.dw[1][j];
+                float4 *row = k.gmv + ((size_t)ix * k.ng + (s.b[1] + j)) * k.ng + s.b[2];
+#pragma unroll
+                for (int kk = 0; kk < 3; ++kk) {
+                    float wt = wij * s.w[2][kk];
+                    float gx = dwi_j * s.w[2][kk], gy = wi_dj * s.w[2][kk], gz = wij * s.dw[2][kk];
+                    float mom[3];
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        float aff = base[a] + mCdx[3 * a] * (float)i + mCdx[3 * a + 1] * (float)j + mCdx[3 * a + 2] * (float)kk;
+                        mom[a] = wt * aff + (A[3 * a] * gx + A[3 * a + 1] * gy + A[3 * a + 2] * gz);
+                    }
+                    atomicAdd(row + kk, make_float4(mom[0], mom[1], mom[2], wt * m));
+                }
+            }
+        }
+        // blocks spanned by the stencil
+        int bx0 = s.b[0] >> 2, bx1 = (s.b[0] + 2) >> 2;
+        int by0 = s.b[1] >> 2, by1 = (s.b[1] + 2) >> 2;
+        int bz0 = s.b[2] >> 2, bz1 = (s.b[2] + 2) >> 2;
+        if (k.periodic_x) {
+            // wrapped x nodes: mark the blocks of the wrapped indices
+            for (int i = 0; i < 3; ++i) {
+                int bxi = wrap(s.b[0] + i, k.ng) >> 2;
+                for (int by = by0; by <= by1; ++by)
+                    for (int bz = bz0; bz <= bz1; ++bz) mark_block(k, bxi, by, bz);
+            }
+        } else {
+            for (int bx = bx0; bx <= bx1; ++bx)
+                for (int by = by0; by <= by1; ++by)
+                    for (int bz = bz0; bz <= bz1; ++bz) mark_block(k, bx, by, bz);
+        }
+        if (!gathered || (mode & PASS_STORE_VC)) {
+            // v and C are state only for particles the gather skipped
+        }
+    }
+}
+
+// -------------------------------------------------------- grid pass --------
+// capped_cylinder_sdf / revolved_glass_sdf (mpm_solver_warp.py:29-57)
+__device__ __forceinline__ float capped_cyl(float r, float z, float rad, float z0, float z1) {
+    float zc = 0.5f * (z0 + z1), hh = 0.5f * (z1 - z0);
+    float dr = r - rad, dz = fabsf(z - zc) - hh;
+    float dro = fmaxf(dr, 0.0f), dzo = fmaxf(dz, 0.0f);
+    return sqrtf(dro * dro + dzo * dzo) + fminf(fmaxf(dr, dz), 0.0f);
+}
+__device__ __forceinline__ float glass_sdf(float l0, float l1, float l2, const ColDev &c) {
+    float r = sqrtf(l0 * l0 + l1 * l1);
+    float d_outer = capped_cyl(r, l2, c.outer_r, -c.half_h, c.half_h);
+    float d_cav = capped_cyl(r, l2, c.inner_r - c.fillet, c.floor_z + c.fillet, c.half_h + c.outer_r) - c.fillet;
+    return fmaxf(d_outer, -d_cav);
+}
+__device__ __forceinline__ float trilerp(const float *vals, int res, float f0, float f1, float f2, int stride,
+                                         int comp) {
+    float fi = fminf(fmaxf(f0, 0.0f), (float)res - 1.0001f);
+    float fj = fminf(fmaxf(f1, 0.0f), (float)res - 1.0001f);
+    float fk = fminf(fmaxf(f2, 0.0f), (float)res - 1.0001f);
+    int i = (int)floorf(fi), j = (int)floorf(fj), kk = (int)floorf(fk);
+    float tx = fi - (float)i, ty = fj - (float)j, tz = fk - (float)kk;
+    auto at = [&](int a, int b, int c) { return __ldg(vals + ((((size_t)a * res + b) * res + c) * stride + comp)); };
+    float c00 = at(i, j, kk) * (1.0f - tx) + at(i + 1, j, kk) * tx;
+    float c01 = at(i, j, kk + 1) * (1.0f - tx) + at(i + 1, j, kk + 1) * tx;
+    float c10 = at(i, j + 1, kk) * (1.0f - tx) + at(i + 1, j + 1, kk) * tx;
+    float c11 = at(i, j + 1, kk + 1) * (1.0f - tx) + at(i + 1, j + 1, kk + 1) * tx;
+    float c0 = c00 * (1.0f - ty) + c10 * ty;
+    float c1 = c01 * (1.0f - ty) + c11 * ty;
+    return c0 * (1.0f - tz) + c1 * tz;
+}
+// quaternion rotation x(2w^2-1) +/- 2w (q x x) + 2 q (q . x)
+__device__ __forceinline__ void qrot(const float *q, const float *x, float *out, bool inv) {
+    float w = q[3];
+    float c = 2.0f * w * w - 1.0f;
+    float cx = q[1] * x[2] - q[2] * x[1], cy = q[2] * x[0] - q[0] * x[2], cz = q[0] * x[1] - q[1] * x[0];
+    float d = q[0] * x[0] + q[1] * x[1] + q[2] * x[2];
+    float sgn = inv ? -2.0f * w : 2.0f * w;
+    out[0] = x[0] * c + cx * sgn + q[0] * d * 2.0f;
+    out[1] = x[1] * c + cy * sgn + q[1] * d * 2.0f;
+    out[2] = x[2] * c + cz * sgn + q[2] * d * 2.0f;
+}
+
+// Applies collider c to node (gx,gy,gz) of mass m (> 0); adds the reaction
+// impulse and torque into acc[6].
+__device__ __forceinline__ void collide(const ColDev &c, const PoseRec &P, int gx, int gy, int gz, float m,
+                                        float *v, const GK &k, float *acc) {
+    const float dx = k.dx;
+    switch (c.kind) {
+    case GBMPM_COLLIDER_PLANE: {  // mpm_solver_warp.py:1929-1992
+        float o0 = (float)gx * dx - P.p[0], o1 = (float)gy * dx - P.p[1], o2 = (float)gz * dx - P.p[2];
+        float dp = o0 * c.normal[0] + o1 * c.normal[1] + o2 * c.normal[2];
+        if (dp < 0.0f) {
+            if (c.surface == 0) {
+                v[0] = v[1] = v[2] = 0.0f;
+            } else if (c.surface == 11) {
+                if ((float)gz * dx < 0.4f || (float)gz * dx > 0.53f) { v[0] = v[1] = v[2] = 0.0f; }
+                else { v[0] *= 0.3f; v[1] = 0.0f; v[2] *= 0.3f; }
+            } else {
+                float nc = v[0] * c.normal[0] + v[1] * c.normal[1] + v[2] * c.normal[2];
+                float sub = (c.surface == 1) ? nc : fminf(nc, 0.0f);
+                float w0 = v[0] - sub * c.normal[0], w1 = v[1] - sub * c.normal[1], w2 = v[2] - sub * c.normal[2];
+                float len = sqrtf(w0 * w0 + w1 * w1 + w2 * w2);
+                if (nc < 0.0f && len > 1e-20f) {
+                    float sc = fmaxf(0.0f, len + nc * c.friction) / len;
+                    w0 *= sc; w1 *= sc; w2 *= sc;
+                }
+                v[0] = w0; v[1] = w1; v[2] = w2;
+            }
+        }
+        return;
+    }
+    case GBMPM_COLLIDER_BOX: {  // mpm_solver_warp.py:2053-2088
+        if (P.mode == 2) { v[0] = v[1] = v[2] = 0.0f; return; }
+        float o0 = (float)gx * dx - P.p[0], o1 = (float)gy * dx - P.p[1], o2 = (float)gz * dx - P.p[2];
+        if (fabsf(o0) < c.size[0] && fabsf(o1) < c.size[1] && fabsf(o2) < c.size[2]) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) { acc[a] += m * (v[a] - c.vel[a]); v[a] = c.vel[a]; }
+        }
+        return;
+    }
+    case GBMPM_COLLIDER_CUP: {  // mpm_solver_warp.py:2161-2225
+        float rel[3] = {(float)gx * dx - P.p[0], (float)gy * dx - P.p[1], (float)gz * dx - P.p[2]};
+        const float *R = P.r;
+        float l0 = R[0] * rel[0] + R[3] * rel[1] + R[6] * rel[2];
+        float l1 = R[1] * rel[0] + R[4] * rel[1] + R[7] * rel[2];
+        float l2 = R[2] * rel[0] + R[5] * rel[1] + R[8] * rel[2];
+        float sdf = glass_sdf(l0, l1, l2, c);
+        if (sdf < c.band_c) {
+            float vs[3] = {c.vel[0] + (c.omega[1] * rel[2] - c.omega[2] * rel[1]),
+                           c.vel[1] + (c.omega[2] * rel[0] - c.omega[0] * rel[2]),
+                           c.vel[2] + (c.omega[0] * rel[1] - c.omega[1] * rel[0])};
+            float vn_[3] = {vs[0], vs[1], vs[2]};
+            if (sdf > -c.sticky) {
+                vn_[0] = v[0]; vn_[1] = v[1]; vn_[2] = v[2];
+                float h = 0.25f * dx;
+                float n0 = glass_sdf(l0 + h, l1, l2, c) - glass_sdf(l0 - h, l1, l2, c);
+                float n1 = glass_sdf(l0, l1 + h, l2, c) - glass_sdf(l0, l1 - h, l2, c);
+                float n2 = glass_sdf(l0, l1, l2 + h, c) - glass_sdf(l0, l1, l2 - h, c);
+                float nl = sqrtf(n0 * n0 + n1 * n1 + n2 * n2);
+                if (nl > 1.0e-12f) {
+                    n0 /= nl; n1 /= nl; n2 /= nl;
+                    float n[3] = {R[0] * n0 + R[1] * n1 + R[2] * n2, R[3] * n0 + R[4] * n1 + R[5] * n2,
+                                  R[6] * n0 + R[7] * n1 + R[8] * n2};
+                    float vr[3] = {v[0] - vs[0], v[1] - vs[1], v[2] - vs[2]};
+                    float vn = vr[0] * n[0] + vr[1] * n[1] + vr[2] * n[2];
+                    if (vn < 0.0f) {
+                        float vt[3] = {vr[0] - vn * n[0], vr[1] - vn * n[1], vr[2] - vn * n[2]};
+                        float vtl = sqrtf(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
+                        if (vtl > 1.0e-20f) {
+                            float sc = fmaxf(vtl + c.friction * vn, 0.0f) / vtl;
+                            vt[0] *= sc; vt[1] *= sc; vt[2] *= sc;
+                        }
+                        vn_[0] = vs[0] + vt[0]; vn_[1] = vs[1] + vt[1]; vn_[2] = vs[2] + vt[2];
+                    }
+                }
+            }
+            float imp[3] = {m * (v[0] - vn_[0]), m * (v[1] - vn_[1]), m * (v[2] - vn_[2])};
+            acc[0] += imp[0]; acc[1] += imp[1]; acc[2] += imp[2];
+            acc[3] += rel[1] * imp[2] - rel[2] * imp[1];
+            acc[4] += rel[2] * imp[0] - rel[0] * imp[2];
+            acc[5] += rel[0] * imp[1] - rel[1] * imp[0];
+            v[0] = vn_[0]; v[1] = vn_[1]; v[2] = vn_[2];
+        }
+        return;
+    }
+    case GBMPM_COLLIDER_WALLS: {  // mpm_solver_warp.py:2294-2359
+        const int pad = 3;
+        const int n = k.ng;
+        if (gx < pad && v[0] < 0) v[0] = 0.0f;
+        if (gx >= n - pad && v[0] > 0) v[0] = 0.0f;
+        if (gy < pad && v[1] < 0) v[1] = 0.0f;
+        if (gy >= n - pad && v[1] > 0) v[1] = 0.0f;
+        if (gz < pad && v[2] < 0) v[2] = 0.0f;
+        if (gz >= n - pad && v[2] > 0) v[2] = 0.0f;
+        return;
+    }
+    case GBMPM_COLLIDER_SDF: {  // mpm_solver_warp.py:2680-2736
+        float rel[3] = {(float)gx * dx - P.p[0], (float)gy * dx - P.p[1], (float)gz * dx - P.p[2]};
+        float body[3];
+        qrot(P.q, rel, body, true);
+        float f0 = (body[0] - c.origin[0]) / c.cell, f1 = (body[1] - c.origin[1]) / c.cell,
+              f2 = (body[2] - c.origin[2]) / c.cell;
+        float rf = (float)c.sdf_res - 1.0f;
+        if (!(f0 >= 0.0f && f1 >= 0.0f && f2 >= 0.0f && f0 <= rf && f1 <= rf && f2 <= rf)) return;
+        float sd = trilerp(c.sdf_val, c.sdf_res, f0, f1, f2, 1, 0);
+        if (sd <= c.band) {
+            float g[3] = {trilerp(c.sdf_grad, c.sdf_res, f0, f1, f2, 3, 0), trilerp(c.sdf_grad, c.sdf_res, f0, f1, f2, 3, 1),
+                          trilerp(c.sdf_grad, c.sdf_res, f0, f1, f2, 3, 2)};
+            float gl = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+            if (gl > 1.0e-12f) {
+                g[0] /= gl; g[1] /= gl; g[2] /= gl;
+                float n[3];
+                qrot(P.q, g, n, false);
+                float vs[3] = {c.vel[0] + (c.omega[1] * rel[2] - c.omega[2] * rel[1]),
+                               c.vel[1] + (c.omega[2] * rel[0] - c.omega[0] * rel[2]),
+                               c.vel[2] + (c.omega[0] * rel[1] - c.omega[1] * rel[0])};
+                float vr[3] = {v[0] - vs[0], v[1] - vs[1], v[2] - vs[2]};
+                float vn = vr[0] * n[0] + vr[1] * n[1] + vr[2] * n[2];
+                float nv[3] = {v[0], v[1], v[2]};
+                if (c.surface == 0) {
+                    nv[0] = vs[0]; nv[1] = vs[1]; nv[2] = vs[2];
+                } else if (c.surface == 1) {
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) nv[a] = vs[a] + (vr[a] - vn * n[a]);
+                } else if (vn < 0.0f) {
+                    float vt[3] = {vr[0] - vn * n[0], vr[1] - vn * n[1], vr[2] - vn * n[2]};
+                    float tl = sqrtf(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
+                    if (tl > 1.0e-12f) {
+                        float sc = fmaxf(0.0f, tl + c.friction * vn) / tl;
+                        vt[0] *= sc; vt[1] *= sc; vt[2] *= sc;
+                    }
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) nv[a] = vs[a] + vt[a];
+                }
+                float imp[3] = {m * (v[0] - nv[0]), m * (v[1] - nv[1]), m * (v[2] - nv[2])};
+                acc[0] += imp[0]; acc[1] += imp[1]; acc[2] += imp[2];
+                acc[3] += rel[1] * imp[2] - rel[2] * imp[1];
+                acc[4] += rel[2] * imp[0] - rel[0] * imp[2];
+                acc[5] += rel[0] * imp[1] - rel[1] * imp[0];
+                v[0] = nv[0]; v[1] = nv[1]; v[2] = nv[2];
+            }
+        }
+        return;
+    }
+    default: return;
+    }
+}
+
+// Grid pass over the active-block list: normalize + gravity (mpm_utils.py:927-941),
+// damping (:1287-1295), every collider in list order, then clear the scatter
+// target and the block flags for the next particle pass.
+__global__ void __launch_bounds__(kGridThreads) k_grid(GK k) {
+    __shared__ ColDev s_cols[kMaxCol];
+    __shared__ PoseRec s_pose[kMaxCol];
+    __shared__ float s_acc[kMaxCol][6];
+    const int t = threadIdx.x;
+    for (int i = t; i < k.ncol; i += blockDim.x) { s_cols[i] = k.cols[i]; s_pose[i] = k.poses[i]; }
+    for (int i = t; i < k.ncol * 6; i += blockDim.x) s_acc[i / 6][i % 6] = 0.0f;
+    if (blockIdx.x == 0 && t == 0) *k.blk_count_reset = 0;
+    __syncthreads();
+    const int count = *k.blk_count_read;
+    const int per = blockDim.x / 64;
+    const int lane = t & 31;
+    for (int item = blockIdx.x * per + t / 64; item < count; item += gridDim.x * per) {
+        bool valid = true;
+        int b = k.blk_list[item];
+        int bz = b % k.bd, r = b / k.bd, by = r % k.bd, bx = r / k.bd;
+        int cell = t & 63;
+        int gx = bx * 4 + (cell >> 4), gy = by * 4 + ((cell >> 2) & 3), gz = bz * 4 + (cell & 3);
+        valid = valid && gx < k.ng && gy < k.ng && gz < k.ng;
+        float m = 0.0f;
+        float v[3] = {0.f, 0.f, 0.f};
+        size_t id = 0;
+        if (valid) {
+            id = ((size_t)gx * k.ng + gy) * k.ng + gz;
+            float4 mv = k.gmv[id];
+            m = mv.w;
+            if (m > 1e-15f) {
+                float inv = 1.0f / m;
+                v[0] = mv.x * inv + k.dt * k.g[0];
+                v[1] = mv.y * inv + k.dt * k.g[1];
+                v[2] = mv.z * inv + k.dt * k.g[2];
+            }
+            if (k.damp < 1.0f) { v[0] *= k.damp; v[1] *= k.damp; v[2] *= k.damp; }
+        }
+        for (int c = 0; c < k.ncol; ++c) {
+            float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (valid && m > 0.0f && s_pose[c].mode != 0) collide(s_cols[c], s_pose[c], gx, gy, gz, m, v, k, acc);
+            int kind = s_cols[c].kind;
+            if (kind == GBMPM_COLLIDER_BOX || kind == GBMPM_COLLIDER_CUP || kind == GBMPM_COLLIDER_SDF) {
+                bool any = __any_sync(0xffffffffu, acc[0] != 0.f || acc[1] != 0.f || acc[2] != 0.f || acc[3] != 0.f ||
+                                                       acc[4] != 0.f || acc[5] != 0.f);
+                if (any) {
+#pragma unroll
+                    for (int a = 0; a < 6; ++a) {
+                        float x = acc[a];
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+                        if (lane == 0) atomicAdd(&s_acc[c][a], x);
+                    }
+                }
+            }
+        }
+        if (valid) {
+            k.gv[id] = make_float4(v[0], v[1], v[2], 0.0f);
+            k.gmv[id] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (cell == 0) k.blk_flag[b] = 0;
+        }
+    }
+    __syncthreads();
+    for (int i = t; i < k.ncol * 6; i += blockDim.x) {
+        float a = s_acc[i / 6][i % 6];
+        if (a != 0.0f) atomicAdd(&k.wrench[i], (double)a);
+    }
+}
+
+// ------------------------------------------------- guard / reductions ------
+__device__ __forceinline__ float warp_min(float x) {
+    for (int o = 16; o > 0; o >>= 1) x = fminf(x, __shfl_xor_sync(0xffffffffu, x, o));
+    return x;
+}
+__device__ __forceinline__ float warp_max(float x) {
+    for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+    return x;
+}
+__device__ __forceinline__ void atomic_min_f(float *a, float v) {
+    if (v >= 0.0f) atomicMin((int *)a, __float_as_int(v));
+    else atomicMax((unsigned *)a, __float_as_uint(v));
+}
+__device__ __forceinline__ void atomic_max_f(float *a, float v) {
+    if (v >= 0.0f) atomicMax((int *)a, __float_as_int(v));
+    else atomicMin((unsigned *)a, __float_as_uint(v));
+}
+
+__global__ void k_guard_init(float *out) {
+    if (threadIdx.x < 3) out[threadIdx.x] = INFINITY;
+    else if (threadIdx.x < 6) out[threadIdx.x] = -INFINITY;
+    else if (threadIdx.x == 6) out[6] = 0.0f;
+}
+
+__global__ void k_guard(const float *x, const float *v, int n, float *out, unsigned *status) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY}, vm = 0.0f;
+    bool bad = false;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            float xa = x[3 * p + a];
+            if (!isfinite(xa)) bad = true;
+            lo[a] = fminf(lo[a], xa);
+            hi[a] = fmaxf(hi[a], xa);
+            vm = fmaxf(vm, fabsf(v[3 * p + a]));
+        }
+    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(status, GBMPM_FLAG_NONFINITE);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { lo[a] = warp_min(lo[a]); hi[a] = warp_max(hi[a]); }
+    vm = warp_max(vm);
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) { atomic_min_f(out + a, lo[a]); atomic_max_f(out + 3 + a, hi[a]); }
+        atomic_max_f(out + 6, vm);
+    }
+}
+
+// ------------------------------------------------------- block sort --------
+// key = ((bx nb + by) nb + bz), b = floor(x/dx - 0.5) >> 2 in float64
+// (core/solver.py:458-465). The pass stores the signed key, flags any descent
+// (the reference skips the permutation when keys are already non-decreasing)
+// and reduces min/max so the radix sort only walks the bits the keys span.
+__global__ void k_sort_keys(const float *x, int n, double dx, long long nb, long long *keys, int *idx,
+                            int *unsorted, long long *kminmax) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    long long key = 0;
+    bool valid = p < n;
+    if (valid) {
+        long long b[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) b[a] = ((long long)floor((double)x[3 * p + a] / dx - 0.5)) >> 2;
+        key = (b[0] * nb + b[1]) * nb + b[2];
+        keys[p] = key;
+        idx[p] = p;
+        if (p > 0) {
+            long long bp[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) bp[a] = ((long long)floor((double)x[3 * (p - 1) + a] / dx - 0.5)) >> 2;
+            long long kp = (bp[0] * nb + bp[1]) * nb + bp[2];
+            if (kp > key) *unsorted = 1;
+        }
+    }
+    long long lo = valid ? key : LLONG_MAX, hi = valid ? key : LLONG_MIN;
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) { atomicMin(&kminmax[0], lo); atomicMax(&kminmax[1], hi); }
+}
+
+__global__ void k_sort_minmax_init(long long *kminmax) {
+    kminmax[0] = LLONG_MAX;
+    kminmax[1] = LLONG_MIN;
+}
+
+// signed key -> unsigned offset from the minimum (order preserving)
+__global__ void k_sort_rebase(const long long *keys, int n, const long long *kminmax, unsigned long long *out) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) out[p] = (unsigned long long)(keys[p] - kminmax[0]);
+}
+
+constexpr int kRadixBits = 8;
+constexpr int kRadixBins = 1 << kRadixBits;
+constexpr int kSortTile = 4096;          // elements per tile
+constexpr int kSortThreads = 256;        // 16 rounds of 256 elements
+
+// per-tile digit histogram, stored bin-major: hist[bin * ntiles + tile]
+__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned long long *keys, int n, int shift,
+                                                             unsigned *hist, int ntiles) {
+    __shared__ unsigned h[kRadixBins];
+    for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    int base = blockIdx.x * kSortTile;
+    for (int i = threadIdx.x; i < kSortTile; i += blockDim.x) {
+        int e = base + i;
+        if (e < n) atomicAdd(&h[(keys[e] >> shift) & (kRadixBins - 1)], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) hist[(size_t)i * ntiles + blockIdx.x] = h[i];
+}
+
+// exclusive scan of hist in place, one CTA: each thread scans a contiguous
+// chunk, the chunk totals are scanned in shared memory, then chunks are rebased
+__global__ void __launch_bounds__(1024) k_radix_scan(unsigned *hist, int total) {
+    __shared__ unsigned s[1024];
+    const int t = threadIdx.x;
+    const int chunk = (total + 1023) / 1024;
+    const int beg = min(t * chunk, total), end = min(beg + chunk, total);
+    unsigned sum = 0;
+    for (int i = beg; i < end; ++i) sum += hist[i];
+    s[t] = sum;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        unsigned v = t >= off ? s[t - off] : 0;
+        __syncthreads();
+        s[t] += v;
+        __syncthreads();
+    }
+    unsigned run = s[t] - sum;
+    for (int i = beg; i < end; ++i) {
+        unsigned v = hist[i];
+        hist[i] = run;
+        run += v;
+    }
+}
+
+// stable scatter: elements of a tile are ranked in index order per digit
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned long long *keys_in, const int *idx_in,
+                                                                unsigned long long *keys_out, int *idx_out, int n,
+                                                                int shift, const unsigned *hist, int ntiles) {
+    __shared__ unsigned offs[kRadixBins];
+    __shared__ unsigned warp_cnt[kSortThreads / 32][kRadixBins];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) offs[i] = hist[(size_t)i * ntiles + blockIdx.x];
+    int base = blockIdx.x * kSortTile;
+    for (int round = 0; round < kSortTile / kSortThreads; ++round) {
+        for (int i = threadIdx.x; i < (kSortThreads / 32) * kRadixBins; i += blockDim.x)
+            (&warp_cnt[0][0])[i] = 0;
+        __syncthreads();
+        int e = base + round * kSortThreads + threadIdx.x;
+        bool valid = e < n;
+        unsigned long long key = valid ? keys_in[e] : 0ull;
+        unsigned d = valid ? (unsigned)((key >> shift) & (kRadixBins - 1)) : 0xffffffffu;
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        int rank_in_warp = __popc(peers & ((1u << lane) - 1u));
+        int leader = 31 - __clz(peers);
+        if (valid && lane == leader) warp_cnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            unsigned before = 0;
+            for (int w = 0; w < warp; ++w) before += warp_cnt[w][d];
+            unsigned pos = offs[d] + before + rank_in_warp;
+            keys_out[pos] = key;
+            idx_out[pos] = idx_in[e];
+        }
+        __syncthreads();
+        for (int b2 = threadIdx.x; b2 < kRadixBins; b2 += blockDim.x) {
+            unsigned tot = 0;
+            for (int w = 0; w < kSortThreads / 32; ++w) tot += warp_cnt[w][b2];
+            offs[b2] += tot;
+        }
+        __syncthreads();
+    }
+}
+
+template <int W>
+__global__ void k_gather_rows(const float *src, const int *perm, float *dst, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float *s = src + (size_t)perm[i] * W;
+    float *d = dst + (size_t)i * W;
+#pragma unroll
+    for (int a = 0; a < W; ++a) d[a] = s[a];
+}
+
+// ------------------------------------------------- active blocks ----------
+// blocks_mark / blocks_dilate / blocks_compact (mpm_utils.py:1506-1544)
+__global__ void k_blocks_mark(const float *x, int n, float inv_dx, int bd, int *raw) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int b[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        int v = (int)(x[3 * p + a] * inv_dx - 0.5f);
+        b[a] = min(max(v >> 2, 0), bd - 1);
+    }
+    raw[((size_t)b[0] * bd + b[1]) * bd + b[2]] = 1;
+}
+__global__ void k_blocks_dilate(const int *raw, int bd, int *cur, const int *prev, int *counts) {
+    int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= bd * bd * bd) return;
+    int z = id % bd, r = id / bd, y = r % bd, x = r / bd;
+    int on = 0;
+    for (int i = -1; i <= 1; ++i)
+        for (int j = -1; j <= 1; ++j)
+            for (int kk = -1; kk <= 1; ++kk) {
+                int xi = min(max(x + i, 0), bd - 1), yj = min(max(y + j, 0), bd - 1), zk = min(max(z + kk, 0), bd - 1);
+                if (raw[((size_t)xi * bd + yj) * bd + zk] == 1) on = 1;
+            }
+    cur[id] = on;
+    if (on) atomicAdd(&counts[0], 1);
+    if (on || prev[id] == 1) atomicAdd(&counts[1], 1);
+}
+
+// ----------------------------------------------------------- exports -------
+__global__ void k_compute_R(const float *Ft, int n, float *R_out) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float F[9], U[9], V[9], s[3], R[9];
+    mat_load(Ft + 9 * (size_t)p, F);
+    svd3(F, U, s, V);
+    if (det3(U) < 0.0f) { U[2] = -U[2]; U[5] = -U[5]; U[8] = -U[8]; }
+    if (det3(V) < 0.0f) { V[2] = -V[2]; V[5] = -V[5]; V[8] = -V[8]; }
+    mmT(U, V, R);
+    float *o = R_out + 9 * (size_t)p;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) o[3 * i + j] = R[3 * j + i];
+}
+__global__ void k_compute_cov(const float *Ft, const float *c0, int n, float *out) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float F[9], I0[9], T[9], r[9];
+    mat_load(Ft + 9 * (size_t)p, F);
+    const float *c = c0 + 6 * (size_t)p;
+    I0[0] = c[0]; I0[1] = c[1]; I0[2] = c[2];
+    I0[3] = c[1]; I0[4] = c[3]; I0[5] = c[4];
+    I0[6] = c[2]; I0[7] = c[4]; I0[8] = c[5];
+    mm(F, I0, T);
+    mmT(T, F, r);
+    float *o = out + 6 * (size_t)p;
+    o[0] = r[0]; o[1] = r[1]; o[2] = r[2]; o[3] = r[4]; o[4] = r[5]; o[5] = r[8];
+}
+
+}  // namespace gbmpm
+
+// ====================================================================== host
+using namespace gbmpm;
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+#define GB_CUDA(call)                                                                            \
+    do {                                                                                         \
+        cudaError_t _e = (call);                                                                 \
+        if (_e != cudaSuccess)                                                                   \
+            return fail(GBMPM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));     \
+    } while (0)
+
+const char *kPhaseNames[GBMPM_NUM_PHASES] = {"compute_stress_from_F_trial", "p2g", "g2p2g_fused",
+                                             "grid_update+BC", "g2p", "guard"};
+
+template <class T>
+struct DevBuf {
+    T *ptr = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= n && ptr) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc(&ptr, std::max<size_t>(want, 1) * sizeof(T));
+        if (e == cudaSuccess) n = want;
+        return e;
+    }
+    void release() { if (ptr) cudaFree(ptr); ptr = nullptr; n = 0; }
+};
+}  // namespace
+
+struct gbmpm_engine {
+    int device = 0;
+    gbmpm_particles P{};
+    gbmpm_grid G{};
+    gbmpm_model M{};
+    bool bound = false, modeled = false;
+    std::vector<gbmpm_collider> cols;
+    // device scratch
+    DevBuf<MatTables> d_tab;
+    DevBuf<ColDev> d_cols;
+    DevBuf<PoseRec> d_pose;
+    DevBuf<double> d_wrench;
+    DevBuf<int> d_flag, d_list, d_count;
+    DevBuf<unsigned> d_status;
+    DevBuf<float> d_guard;
+    DevBuf<unsigned long long> d_keys[2];
+    DevBuf<long long> d_skeys, d_kminmax;
+    DevBuf<int> d_idx[2];
+    DevBuf<unsigned> d_hist;
+    DevBuf<int> d_flagbuf;
+    DevBuf<float> d_tmp;
+    DevBuf<int> d_braw, d_bcur, d_bprev, d_bcount;
+    PoseRec *h_pose = nullptr;
+    size_t h_pose_cap = 0;
+    cudaEvent_t pose_done = nullptr;
+    int bd = 0;
+    int num_sms = 148;
+    // graph cache
+    cudaGraphExec_t graph = nullptr;
+    int g_substeps = -1, g_flags = -1;
+    double g_dt = 0.0;
+    cudaStream_t g_stream = nullptr;
+    bool dirty = true;
+    // profiling
+    double prof_ms[GBMPM_NUM_PHASES] = {0};
+    int64_t prof_n[GBMPM_NUM_PHASES] = {0};
+    int64_t launches = 0;
+};
+
+namespace {
+
+PK make_pk(gbmpm_engine *e, float dt, int list) {
+    PK k{};
+    const gbmpm_particles &P = e->P;
+    k.x = P.x; k.v = P.v; k.C = P.C; k.F = P.F; k.Ft = P.F_trial; k.L = P.L; k.S = P.stress;
+    k.mass = P.mass; k.vol = P.vol; k.Jp = P.Jp; k.mu = P.mu; k.lam = P.lam; k.ys = P.yield_stress;
+    k.mat = P.material; k.sel = P.selection; k.cov = P.cov; k.n = P.n;
+    k.gv = reinterpret_cast<const float4 *>(e->G.v);
+    k.gmv = reinterpret_cast<float4 *>(e->G.mv);
+    k.ng = e->G.n_grid;
+    k.dx = e->M.dx; k.inv_dx = e->M.inv_dx; k.dt = dt; k.rpic = e->M.rpic_damping;
+    k.periodic_x = e->M.periodic_x; k.update_cov = e->M.update_cov_with_F && P.cov;
+    k.tab = e->d_tab.ptr; k.eta = e->M.eta_table; k.eta_n = e->M.eta_table_n;
+    k.eta_smin = e->M.eta_table_smin; k.eta_smax = e->M.eta_table_smax;
+    k.blk_flag = e->d_flag.ptr;
+    k.bd = e->bd;
+    size_t nb = (size_t)e->bd * e->bd * e->bd;
+    k.blk_list = e->d_list.ptr + (size_t)list * nb;
+    k.blk_count = e->d_count.ptr + list;
+    k.status = e->d_status.ptr;
+    return k;
+}
+
+bool has_solids(const gbmpm_model &m) {
+    const uint32_t fluid = (1u << 6) | (1u << 7) | (1u << 8) | (1u << 10) | (1u << 12);
+    return (m.material_mask & ~fluid) != 0;
+}
+
+void launch_particles(gbmpm_engine *e, const PK &k, int mode, cudaStream_t s) {
+    int grid = (k.n + kParticleThreads - 1) / kParticleThreads;
+    if (grid == 0) grid = 1;
+    if (has_solids(e->M)) k_particles<true><<<grid, kParticleThreads, 0, s>>>(k, mode);
+    else k_particles<false><<<grid, kParticleThreads, 0, s>>>(k, mode);
+    e->launches++;
+}
+
+void launch_grid(gbmpm_engine *e, float dt, int substep, int list, cudaStream_t s) {
+    GK g{};
+    g.gmv = reinterpret_cast<float4 *>(e->G.mv);
+    g.gv = reinterpret_cast<float4 *>(e->G.v);
+    g.ng = e->G.n_grid;
+    g.dx = e->M.dx; g.dt = dt;
+    g.g[0] = e->M.gravity[0]; g.g[1] = e->M.gravity[1]; g.g[2] = e->M.gravity[2];
+    g.damp = e->M.grid_v_damping_scale;
+    g.ncol = (int)e->cols.size();
+    g.cols = e->d_cols.ptr;
+    g.poses = e->d_pose.ptr + (size_t)substep * std::max<int>(1, g.ncol);
+    g.wrench = e->d_wrench.ptr;
+    g.blk_flag = e->d_flag.ptr;
+    size_t nb = (size_t)e->bd * e->bd * e->bd;
+    g.blk_list = e->d_list.ptr + (size_t)list * nb;
+    g.blk_count_read = e->d_count.ptr + list;
+    g.blk_count_reset = e->d_count.ptr + (list ^ 1);
+    g.bd = e->bd;
+    int grid = e->num_sms * 8;
+    k_grid<<<grid, kGridThreads, 0, s>>>(g);
+    e->launches++;
+}
+
+ColDev to_dev(const gbmpm_collider &c) {
+    ColDev d{};
+    d.kind = c.kind; d.surface = c.surface_type; d.sdf_res = c.sdf_res;
+    for (int a = 0; a < 3; ++a) {
+        d.normal[a] = c.normal[a]; d.size[a] = c.size[a]; d.vel[a] = c.velocity[a]; d.omega[a] = c.omega[a];
+        d.origin[a] = c.sdf_origin[a];
+    }
+    d.friction = c.friction; d.outer_r = c.outer_radius; d.inner_r = c.inner_radius; d.half_h = c.half_height;
+    d.floor_z = c.inner_floor_z; d.fillet = c.fillet_radius; d.sticky = c.sticky_depth; d.band_c = c.contact_band;
+    d.cell = c.sdf_cell; d.band = c.band; d.sdf_val = c.sdf_val; d.sdf_grad = c.sdf_grad;
+    return d;
+}
+
+// Host pose integration for one substep: the reference's modify_bc callables
+// (mpm_solver_warp.py:2090-2096, 2227-2254, 2749-2760) on float64 values read
+// from the fp32 struct and rounded back.
+void integrate_pose(gbmpm_collider &c, double time, double dt) {
+    if (!(time >= (double)c.start_time && time < (double)c.end_time)) return;
+    if (c.kind == GBMPM_COLLIDER_BOX || c.kind == GBMPM_COLLIDER_CUP || c.kind == GBMPM_COLLIDER_SDF)
+        for (int i = 0; i < 3; ++i) c.point[i] = (float)((double)c.point[i] + dt * (double)c.velocity[i]);
+    if (c.kind == GBMPM_COLLIDER_CUP) {
+        double w[3] = {c.omega[0], c.omega[1], c.omega[2]};
+        double wn = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        double ang = wn * dt;
+        if (ang > 1.0e-12) {
+            double ax[3] = {w[0] / wn, w[1] / wn, w[2] / wn};
+            double K[3][3] = {{0.0, -ax[2], ax[1]}, {ax[2], 0.0, -ax[0]}, {-ax[1], ax[0], 0.0}};
+            double s = std::sin(ang), cc = 1.0 - std::cos(ang);
+            double Ri[3][3], Rn[3][3];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    double k2 = K[i][0] * K[0][j] + K[i][1] * K[1][j] + K[i][2] * K[2][j];
+                    Ri[i][j] = ((i == j) ? 1.0 : 0.0) + s * K[i][j] + cc * k2;
+                }
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j)
+                    Rn[i][j] = Ri[i][0] * c.rot64[j] + Ri[i][1] * c.rot64[3 + j] + Ri[i][2] * c.rot64[6 + j];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) { c.rot64[3 * i + j] = Rn[i][j]; c.rot[3 * i + j] = (float)Rn[i][j]; }
+        }
+    }
+    if (c.kind == GBMPM_COLLIDER_SDF) {
+        double w[3] = {c.omega[0], c.omega[1], c.omega[2]};
+        double sp = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        if (!(sp * dt < 1e-12)) {
+            double q[4] = {c.quat[0], c.quat[1], c.quat[2], c.quat[3]};
+            double half = 0.5 * sp * dt, sh = std::sin(half);
+            double d[4] = {w[0] / sp * sh, w[1] / sp * sh, w[2] / sp * sh, std::cos(half)};
+            double r[4] = {d[3] * q[0] + d[0] * q[3] + d[1] * q[2] - d[2] * q[1],
+                           d[3] * q[1] - d[0] * q[2] + d[1] * q[3] + d[2] * q[0],
+                           d[3] * q[2] + d[0] * q[1] - d[1] * q[0] + d[2] * q[3],
+                           d[3] * q[3] - d[0] * q[0] - d[1] * q[1] - d[2] * q[2]};
+            double nr = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3]);
+            for (int i = 0; i < 4; ++i) c.quat[i] = (float)(r[i] / nr);
+        }
+    }
+}
+
+// Builds the [S][ncol] pose table for a tick and advances the host collider
+// records and clock exactly as S calls of _apply_grid_bc + time += dt would.
+void build_pose_table(gbmpm_engine *e, double &time, double dt, int S) {
+    int nc = (int)e->cols.size();
+    int stride = std::max(1, nc);
+    float dtf = (float)dt;
+    for (int s = 0; s < S; ++s) {
+        float tf = (float)time;
+        for (int c = 0; c < nc; ++c) {
+            gbmpm_collider &col = e->cols[c];
+            PoseRec &r = e->h_pose[(size_t)s * stride + c];
+            std::memset(&r, 0, sizeof r);
+            bool live = tf >= col.start_time && tf < col.end_time;
+            if (col.kind == GBMPM_COLLIDER_BOX && !live && col.reset == 1)
+                r.mode = (tf < col.end_time + 15.0f * dtf) ? 2 : 0;
+            else r.mode = live ? 1 : 0;
+            for (int a = 0; a < 3; ++a) r.p[a] = col.point[a];
+            for (int a = 0; a < 9; ++a) r.r[a] = col.rot[a];
+            for (int a = 0; a < 4; ++a) r.q[a] = col.quat[a];
+        }
+        for (int c = 0; c < nc; ++c) integrate_pose(e->cols[c], time, dt);
+        time = time + dt;
+    }
+}
+
+int check_ready(gbmpm_engine *e) {
+    if (!e) return fail(GBMPM_ERR_ARG, "null engine");
+    if (!e->bound) return fail(GBMPM_ERR_STATE, "buffers not bound (call gbmpm_bind)");
+    if (!e->modeled) return fail(GBMPM_ERR_STATE, "model not set (call gbmpm_set_model)");
+    return GBMPM_OK;
+}
+
+// Records the launches of one tick on stream s.
+void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, cudaStream_t s, bool profile) {
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (profile) { cudaEventCreate(&ev0); cudaEventCreate(&ev1); }
+    auto timed = [&](int phase, auto fn) {
+        if (!profile) { fn(); return; }
+        cudaEventRecord(ev0, s);
+        fn();
+        cudaEventRecord(ev1, s);
+        cudaEventSynchronize(ev1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev0, ev1);
+        e->prof_ms[phase] += ms;
+        e->prof_n[phase] += 1;
+    };
+    for (int sub = 0; sub < S; ++sub) {
+        int list = sub & 1;
+        PK k = make_pk(e, dtf, list);
+        bool last_stress = fused ? (sub == S - 1) : true;
+        if (!fused || sub == 0) {
+            int mode = PASS_STRESS | PASS_P2G | (last_stress ? PASS_STORE_ALL : 0);
+            timed(0, [&] { launch_particles(e, k, mode, s); });
+        } else {
+            int mode = PASS_G2P | PASS_STRESS | PASS_P2G | (last_stress ? PASS_STORE_ALL : 0);
+            timed(2, [&] { launch_particles(e, k, mode, s); });
+        }
+        timed(3, [&] { launch_grid(e, dtf, sub, list, s); });
+        if (!fused) timed(4, [&] { launch_particles(e, k, PASS_G2P | PASS_RESET_LISTS, s); });
+    }
+    if (fused) {
+        PK k = make_pk(e, dtf, 0);
+        timed(4, [&] { launch_particles(e, k, PASS_G2P | PASS_RESET_LISTS, s); });
+    }
+    if (profile) { cudaEventDestroy(ev0); cudaEventDestroy(ev1); }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gbmpm_last_error(void) { return g_err.c_str(); }
+
+const char *gbmpm_phase_name(int32_t phase) {
+    if (phase < 0 || phase >= GBMPM_NUM_PHASES) return "";
+    return kPhaseNames[phase];
+}
+
+int gbmpm_engine_create(gbmpm_engine **out) {
+    if (!out) return fail(GBMPM_ERR_ARG, "null out");
+    gbmpm_engine *e = new gbmpm_engine();
+    if (cudaGetDevice(&e->device) != cudaSuccess) { delete e; return fail(GBMPM_ERR_CUDA, "no CUDA device"); }
+    cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, e->device);
+    if (cudaEventCreateWithFlags(&e->pose_done, cudaEventDisableTiming) != cudaSuccess) {
+        delete e;
+        return fail(GBMPM_ERR_CUDA, "event create failed");
+    }
+    *out = e;
+    return GBMPM_OK;
+}
+
+void gbmpm_engine_destroy(gbmpm_engine *e) {
+    if (!e) return;
+    cudaDeviceSynchronize();
+    if (e->graph) cudaGraphExecDestroy(e->graph);
+    if (e->pose_done) cudaEventDestroy(e->pose_done);
+    if (e->h_pose) cudaFreeHost(e->h_pose);
+    e->d_tab.release(); e->d_cols.release(); e->d_pose.release(); e->d_wrench.release();
+    e->d_flag.release(); e->d_list.release(); e->d_count.release(); e->d_status.release();
+    e->d_guard.release(); e->d_keys[0].release(); e->d_keys[1].release(); e->d_skeys.release(); e->d_kminmax.release(); e->d_idx[0].release();
+    e->d_idx[1].release(); e->d_hist.release(); e->d_flagbuf.release(); e->d_tmp.release();
+    e->d_braw.release(); e->d_bcur.release(); e->d_bprev.release(); e->d_bcount.release();
+    delete e;
+}
+
+int gbmpm_bind(gbmpm_engine *e, const gbmpm_particles *p, const gbmpm_grid *g) {
+    if (!e || !p || !g) return fail(GBMPM_ERR_ARG, "null argument");
+    if (p->n < 0 || g->n_grid < 4) return fail(GBMPM_ERR_ARG, "bad sizes");
+    if (p->n > 0 && (!p->x || !p->v || !p->C || !p->F || !p->F_trial || !p->L || !p->stress || !p->mass ||
+                     !p->vol || !p->Jp || !p->mu || !p->lam || !p->yield_stress || !p->material))
+        return fail(GBMPM_ERR_ARG, "a required particle buffer is NULL");
+    if (!g->mv || !g->v) return fail(GBMPM_ERR_ARG, "grid buffers are NULL");
+    e->P = *p;
+    e->G = *g;
+    e->bd = (g->n_grid + 3) / 4;
+    size_t nb = (size_t)e->bd * e->bd * e->bd;
+    GB_CUDA(e->d_flag.ensure(nb));
+    GB_CUDA(e->d_list.ensure(2 * nb));
+    GB_CUDA(e->d_count.ensure(2));
+    GB_CUDA(e->d_status.ensure(1));
+    GB_CUDA(e->d_guard.ensure(8));
+    GB_CUDA(cudaMemset(e->d_flag.ptr, 0, nb * sizeof(int)));
+    GB_CUDA(cudaMemset(e->d_count.ptr, 0, 2 * sizeof(int)));
+    GB_CUDA(cudaMemset(e->d_status.ptr, 0, sizeof(unsigned)));
+    size_t nn = (size_t)g->n_grid * g->n_grid * g->n_grid;
+    GB_CUDA(cudaMemset(g->mv, 0, nn * 16));
+    GB_CUDA(cudaMemset(g->v, 0, nn * 16));
+    e->bound = true;
+    e->dirty = true;
+    return GBMPM_OK;
+}
+
+int gbmpm_set_model(gbmpm_engine *e, const gbmpm_model *m) {
+    if (!e || !m) return fail(GBMPM_ERR_ARG, "null argument");
+    if (m->eta_table_n < 2 || !m->eta_table) return fail(GBMPM_ERR_ARG, "eta_table needs >= 2 samples");
+    if (e->bound && m->n_grid != e->G.n_grid) return fail(GBMPM_ERR_ARG, "model n_grid differs from bound grid");
+    e->M = *m;
+    MatTables t;
+    std::memcpy(t.E, m->E, sizeof t.E); std::memcpy(t.nu, m->nu, sizeof t.nu);
+    std::memcpy(t.bulk, m->bulk, sizeof t.bulk); std::memcpy(t.hardening, m->hardening, sizeof t.hardening);
+    std::memcpy(t.xi, m->xi, sizeof t.xi); std::memcpy(t.pv, m->plastic_viscosity, sizeof t.pv);
+    std::memcpy(t.softening, m->softening, sizeof t.softening); std::memcpy(t.alpha, m->alpha, sizeof t.alpha);
+    std::memcpy(t.mu_s, m->muI_mu_s, sizeof t.mu_s); std::memcpy(t.dmu, m->muI_delta_mu, sizeof t.dmu);
+    std::memcpy(t.I0, m->muI_I0, sizeof t.I0); std::memcpy(t.d, m->muI_d, sizeof t.d);
+    std::memcpy(t.rho_s, m->muI_rho_s, sizeof t.rho_s); std::memcpy(t.phi_init, m->muI_phi_init, sizeof t.phi_init);
+    std::memcpy(t.phi_chi, m->muI_phi_chi, sizeof t.phi_chi);
+    GB_CUDA(e->d_tab.ensure(1));
+    GB_CUDA(cudaMemcpy(e->d_tab.ptr, &t, sizeof t, cudaMemcpyHostToDevice));
+    e->modeled = true;
+    e->dirty = true;
+    return GBMPM_OK;
+}
+
+int gbmpm_set_colliders(gbmpm_engine *e, const gbmpm_collider *c, int32_t n) {
+    if (!e || (n > 0 && !c)) return fail(GBMPM_ERR_ARG, "null argument");
+    if (n < 0 || n > kMaxCol) return fail(GBMPM_ERR_ARG, "collider count out of range (max 32)");
+    for (int i = 0; i < n; ++i) {
+        if (c[i].kind < 0 || c[i].kind > GBMPM_COLLIDER_SDF) return fail(GBMPM_ERR_ARG, "unknown collider kind");
+        if (c[i].kind == GBMPM_COLLIDER_SDF && (!c[i].sdf_val || !c[i].sdf_grad || c[i].sdf_res < 2))
+            return fail(GBMPM_ERR_ARG, "sdf collider without a field");
+    }
+    size_t old = e->cols.size();
+    e->cols.assign(c, c + n);
+    std::vector<ColDev> d(std::max(1, n));
+    for (int i = 0; i < n; ++i) d[i] = to_dev(c[i]);
+    GB_CUDA(e->d_cols.ensure(d.size()));
+    GB_CUDA(cudaMemcpy(e->d_cols.ptr, d.data(), d.size() * sizeof(ColDev), cudaMemcpyHostToDevice));
+    if (e->d_wrench.n < (size_t)kMaxCol * 6) {
+        std::vector<double> keep(e->d_wrench.n);
+        if (e->d_wrench.ptr && e->d_wrench.n)
+            GB_CUDA(cudaMemcpy(keep.data(), e->d_wrench.ptr, keep.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        GB_CUDA(e->d_wrench.ensure((size_t)kMaxCol * 6));
+        GB_CUDA(cudaMemset(e->d_wrench.ptr, 0, (size_t)kMaxCol * 6 * sizeof(double)));
+        if (!keep.empty())
+            GB_CUDA(cudaMemcpy(e->d_wrench.ptr, keep.data(), keep.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    if ((size_t)n > old)
+        GB_CUDA(cudaMemset(e->d_wrench.ptr + old * 6, 0, (n - old) * 6 * sizeof(double)));
+    e->dirty = true;
+    return GBMPM_OK;
+}
+
+int gbmpm_get_colliders(gbmpm_engine *e, gbmpm_collider *c, int32_t n) {
+    if (!e || (n > 0 && !c)) return fail(GBMPM_ERR_ARG, "null argument");
+    if (n != (int)e->cols.size()) return fail(GBMPM_ERR_ARG, "collider count mismatch");
+    std::copy(e->cols.begin(), e->cols.end(), c);
+    return GBMPM_OK;
+}
+
+int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32_t flags, void *stream) {
+    int rc = check_ready(e);
+    if (rc) return rc;
+    if (!time || substeps < 1 || substeps > GBMPM_MAX_SUBSTEPS || !(dt > 0.0))
+        return fail(GBMPM_ERR_ARG, "bad tick arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (e->P.n == 0) {
+        for (int i = 0; i < substeps; ++i) *time += dt;
+        return GBMPM_OK;
+    }
+    const int nc = (int)e->cols.size();
+    const size_t need = (size_t)substeps * std::max(1, nc);
+    // pose table: host integration in float64, one upload per tick
+    if (e->h_pose_cap < need) {
+        if (e->h_pose) { cudaEventSynchronize(e->pose_done); cudaFreeHost(e->h_pose); }
+        e->h_pose = nullptr;
+        GB_CUDA(cudaMallocHost(&e->h_pose, need * sizeof(PoseRec)));
+        e->h_pose_cap = need;
+    }
+    PoseRec *old_dev = e->d_pose.ptr;
+    GB_CUDA(e->d_pose.ensure(need));
+    if (e->d_pose.ptr != old_dev) e->dirty = true;
+    GB_CUDA(cudaEventSynchronize(e->pose_done));
+    build_pose_table(e, *time, dt, substeps);
+    GB_CUDA(cudaMemcpyAsync(e->d_pose.ptr, e->h_pose, need * sizeof(PoseRec), cudaMemcpyHostToDevice, s));
+    GB_CUDA(cudaEventRecord(e->pose_done, s));
+    const bool fused = (flags & GBMPM_TICK_FUSED) != 0;
+    const bool profile = (flags & GBMPM_TICK_PROFILE) != 0;
+    const bool use_graph = (flags & GBMPM_TICK_GRAPH) && !profile;
+    const float dtf = (float)dt;
+    if (!use_graph) {
+        record_tick(e, dtf, substeps, fused, s, profile);
+        GB_CUDA(cudaGetLastError());
+        return GBMPM_OK;
+    }
+    bool reuse = e->graph && !e->dirty && e->g_substeps == substeps && e->g_flags == flags && e->g_dt == dt &&
+                 e->g_stream == s;
+    if (!reuse) {
+        if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
+        cudaStream_t cap;
+        GB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaGraph_t g = nullptr;
+        GB_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        int64_t before = e->launches;
+        record_tick(e, dtf, substeps, fused, cap, false);
+        e->launches = before;
+        cudaError_t ce = cudaStreamEndCapture(cap, &g);
+        cudaStreamDestroy(cap);
+        if (ce != cudaSuccess) return fail(GBMPM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+        ce = cudaGraphInstantiate(&e->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) { e->graph = nullptr; return fail(GBMPM_ERR_CUDA, "graph instantiate failed"); }
+        e->g_substeps = substeps; e->g_flags = flags; e->g_dt = dt; e->g_stream = s;
+        e->dirty = false;
+    }
+    GB_CUDA(cudaGraphLaunch(e->graph, s));
+    e->launches += (int64_t)substeps * (fused ? 2 : 3) + (fused ? 1 : 0);
+    return GBMPM_OK;
+}
+
+int gbmpm_guard(gbmpm_engine *e, float out[7], uint32_t *status, void *stream) {
+    if (!e || !out) return fail(GBMPM_ERR_ARG, "null argument");
+    if (!e->bound) return fail(GBMPM_ERR_STATE, "buffers not bound");
+    cudaStream_t s = (cudaStream_t)stream;
+    k_guard_init<<<1, 32, 0, s>>>(e->d_guard.ptr);
+    if (e->P.n > 0) {
+        int grid = std::min((e->P.n + 255) / 256, e->num_sms * 4);
+        k_guard<<<grid, 256, 0, s>>>(e->P.x, e->P.v, e->P.n, e->d_guard.ptr, e->d_status.ptr);
+    }
+    e->launches += 2;
+    float h[8];
+    unsigned st = 0;
+    GB_CUDA(cudaMemcpyAsync(h, e->d_guard.ptr, 7 * sizeof(float), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaMemcpyAsync(&st, e->d_status.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaMemsetAsync(e->d_status.ptr, 0, sizeof(unsigned), s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < 7; ++i) out[i] = h[i];
+    if (status) *status = st;
+    return GBMPM_OK;
+}
+
+int gbmpm_wrench(gbmpm_engine *e, int32_t collider, double out[6], void *stream) {
+    if (!e || !out) return fail(GBMPM_ERR_ARG, "null argument");
+    if (collider < 0 || collider >= (int)e->cols.size()) return fail(GBMPM_ERR_ARG, "collider index out of range");
+    cudaStream_t s = (cudaStream_t)stream;
+    GB_CUDA(cudaMemcpyAsync(out, e->d_wrench.ptr + 6 * collider, 6 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    return GBMPM_OK;
+}
+
+int gbmpm_reset_wrench(gbmpm_engine *e, int32_t collider, void *stream) {
+    if (!e) return fail(GBMPM_ERR_ARG, "null argument");
+    if (collider < 0 || collider >= (int)e->cols.size()) return fail(GBMPM_ERR_ARG, "collider index out of range");
+    GB_CUDA(cudaMemsetAsync(e->d_wrench.ptr + 6 * collider, 0, 6 * sizeof(double), (cudaStream_t)stream));
+    return GBMPM_OK;
+}
+
+int gbmpm_sort_particles(gbmpm_engine *e, double dx, int32_t *sorted_out, int32_t *perm_out, void *stream) {
+    if (!e || !(dx > 0.0)) return fail(GBMPM_ERR_ARG, "bad argument");
+    if (!e->bound) return fail(GBMPM_ERR_STATE, "buffers not bound");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int n = e->P.n;
+    if (sorted_out) *sorted_out = 0;
+    if (n < 2) return GBMPM_OK;
+    GB_CUDA(e->d_keys[0].ensure(n)); GB_CUDA(e->d_keys[1].ensure(n));
+    GB_CUDA(e->d_skeys.ensure(n));
+    GB_CUDA(e->d_idx[0].ensure(n)); GB_CUDA(e->d_idx[1].ensure(n));
+    GB_CUDA(e->d_flagbuf.ensure(1));
+    GB_CUDA(e->d_kminmax.ensure(2));
+    const int ntiles = (n + kSortTile - 1) / kSortTile;
+    GB_CUDA(e->d_hist.ensure((size_t)ntiles * kRadixBins));
+    GB_CUDA(cudaMemsetAsync(e->d_flagbuf.ptr, 0, sizeof(int), s));
+    k_sort_minmax_init<<<1, 1, 0, s>>>(e->d_kminmax.ptr);
+    long long nb = (long long)(e->G.n_grid >> 2) + 2;
+    k_sort_keys<<<(n + 255) / 256, 256, 0, s>>>(e->P.x, n, dx, nb, e->d_skeys.ptr, e->d_idx[0].ptr,
+                                                  e->d_flagbuf.ptr, e->d_kminmax.ptr);
+    e->launches += 2;
+    int unsorted = 0;
+    long long mm[2];
+    GB_CUDA(cudaMemcpyAsync(&unsorted, e->d_flagbuf.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaMemcpyAsync(mm, e->d_kminmax.ptr, 2 * sizeof(long long), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    if (!unsorted) return GBMPM_OK;
+    k_sort_rebase<<<(n + 255) / 256, 256, 0, s>>>(e->d_skeys.ptr, n, e->d_kminmax.ptr, e->d_keys[0].ptr);
+    e->launches++;
+    unsigned long long span = (unsigned long long)(mm[1] - mm[0]);
+    int bits = 0;
+    while (bits < 64 && (span >> bits) != 0ull) ++bits;
+    int cur = 0;
+    for (int shift = 0; shift < bits; shift += kRadixBits) {
+        k_radix_hist<<<ntiles, kSortThreads, 0, s>>>(e->d_keys[cur].ptr, n, shift, e->d_hist.ptr, ntiles);
+        k_radix_scan<<<1, 1024, 0, s>>>(e->d_hist.ptr, ntiles * kRadixBins);
+        k_radix_scatter<<<ntiles, kSortThreads, 0, s>>>(e->d_keys[cur].ptr, e->d_idx[cur].ptr, e->d_keys[cur ^ 1].ptr,
+                                                         e->d_idx[cur ^ 1].ptr, n, shift, e->d_hist.ptr, ntiles);
+        e->launches += 3;
+        cur ^= 1;
+    }
+    const int *perm = e->d_idx[cur].ptr;
+    GB_CUDA(e->d_tmp.ensure((size_t)9 * n));
+    float *tmp = e->d_tmp.ptr;
+    const gbmpm_particles &P = e->P;
+    int g = (n + 255) / 256;
+    auto permute = [&](float *a, int w) -> cudaError_t {
+        if (!a) return cudaSuccess;
+        switch (w) {
+        case 1: k_gather_rows<1><<<g, 256, 0, s>>>(a, perm, tmp, n); break;
+        case 3: k_gather_rows<3><<<g, 256, 0, s>>>(a, perm, tmp, n); break;
+        case 6: k_gather_rows<6><<<g, 256, 0, s>>>(a, perm, tmp, n); break;
+        default: k_gather_rows<9><<<g, 256, 0, s>>>(a, perm, tmp, n); break;
+        }
+        e->launches++;
+        return cudaMemcpyAsync(a, tmp, (size_t)w * n * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    };
+    float *v3[] = {P.x, P.v};
+    for (float *a : v3) GB_CUDA(permute(a, 3));
+    float *m9[] = {P.F, P.F_trial, P.stress, P.C, P.L};
+    for (float *a : m9) GB_CUDA(permute(a, 9));
+    float *f1[] = {P.vol, P.mass, P.density, P.Jp, P.mu, P.lam, P.yield_stress};
+    for (float *a : f1) GB_CUDA(permute(a, 1));
+    float *c6[] = {P.init_cov, P.cov};
+    for (float *a : c6) GB_CUDA(permute(a, 6));
+    int *i1[] = {P.selection, P.material};
+    for (int *a : i1) GB_CUDA(permute(reinterpret_cast<float *>(a), 1));
+    if (perm_out) GB_CUDA(cudaMemcpyAsync(perm_out, perm, (size_t)n * sizeof(int), cudaMemcpyDeviceToDevice, s));
+    if (sorted_out) *sorted_out = 1;
+    return GBMPM_OK;
+}
+
+int gbmpm_rebuild_active_blocks(gbmpm_engine *e, int32_t counts[2], void *stream) {
+    if (!e || !counts) return fail(GBMPM_ERR_ARG, "null argument");
+    if (!e->bound || !e->modeled) return fail(GBMPM_ERR_STATE, "engine not ready");
+    cudaStream_t s = (cudaStream_t)stream;
+    size_t nb = (size_t)e->bd * e->bd * e->bd;
+    bool fresh = e->d_bcur.n < nb;
+    GB_CUDA(e->d_braw.ensure(nb)); GB_CUDA(e->d_bcur.ensure(nb)); GB_CUDA(e->d_bprev.ensure(nb));
+    GB_CUDA(e->d_bcount.ensure(2));
+    if (fresh) {
+        GB_CUDA(cudaMemsetAsync(e->d_bcur.ptr, 0, nb * sizeof(int), s));
+    }
+    std::swap(e->d_bcur, e->d_bprev);
+    GB_CUDA(cudaMemsetAsync(e->d_braw.ptr, 0, nb * sizeof(int), s));
+    GB_CUDA(cudaMemsetAsync(e->d_bcount.ptr, 0, 2 * sizeof(int), s));
+    if (e->P.n > 0)
+        k_blocks_mark<<<(e->P.n + 255) / 256, 256, 0, s>>>(e->P.x, e->P.n, e->M.inv_dx, e->bd, e->d_braw.ptr);
+    k_blocks_dilate<<<(int)((nb + 255) / 256), 256, 0, s>>>(e->d_braw.ptr, e->bd, e->d_bcur.ptr, e->d_bprev.ptr,
+                                                            e->d_bcount.ptr);
+    e->launches += 2;
+    GB_CUDA(cudaMemcpyAsync(counts, e->d_bcount.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    return GBMPM_OK;
+}
+
+int gbmpm_compute_R(gbmpm_engine *e, float *R_out, void *stream) {
+    if (!e || !R_out) return fail(GBMPM_ERR_ARG, "null argument");
+    if (!e->bound) return fail(GBMPM_ERR_STATE, "buffers not bound");
+    if (e->P.n == 0) return GBMPM_OK;
+    k_compute_R<<<(e->P.n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(e->P.F_trial, e->P.n, R_out);
+    e->launches++;
+    GB_CUDA(cudaGetLastError());
+    return GBMPM_OK;
+}
+
+int gbmpm_compute_cov(gbmpm_engine *e, float *cov_out, void *stream) {
+    if (!e || !cov_out) return fail(GBMPM_ERR_ARG, "null argument");
+    if (!e->bound || !e->P.init_cov) return fail(GBMPM_ERR_STATE, "no init_cov bound");
+    if (e->P.n == 0) return GBMPM_OK;
+    k_compute_cov<<<(e->P.n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(e->P.F_trial, e->P.init_cov, e->P.n,
+                                                                          cov_out);
+    e->launches++;
+    GB_CUDA(cudaGetLastError());
+    return GBMPM_OK;
+}
+
+int gbmpm_profile(gbmpm_engine *e, double ms_out[GBMPM_NUM_PHASES], int64_t count_out[GBMPM_NUM_PHASES],
+                  int32_t reset) {
+    if (!e) return fail(GBMPM_ERR_ARG, "null engine");
+    for (int i = 0; i < GBMPM_NUM_PHASES; ++i) {
+        if (ms_out) ms_out[i] = e->prof_ms[i];
+        if (count_out) count_out[i] = e->prof_n[i];
+        if (reset) { e->prof_ms[i] = 0; e->prof_n[i] = 0; }
+    }
+    return GBMPM_OK;
+}
+
+int64_t gbmpm_launch_count(gbmpm_engine *e) { return e ? e->launches : 0; }
+
+}  // extern "C"

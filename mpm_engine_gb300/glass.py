@@ -1,0 +1,150 @@
+"""Open-top glass geometry: profile, signed distance, fill lattice, quaternion helpers.
+
+Same public behaviour as warpmpm.colliders.glass (src/warpmpm/colliders/glass.py):
+`GlassProfile` (defaults 0.089 m outer radius, 0.020 m wall, 0.24 m height, 0.050 m
+base, 0.012 m fillet), the revolved SDF `glass_sdf_local` that the cup collider
+kernel evaluates, and `cup_fill`, whose jittered lattice defines the 340,489-particle
+pour at 192^3 / grid_lim 0.7. Quaternions here are w x y z.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+
+def quat_to_mat(q) -> np.ndarray:
+    """Rotation matrix (float64) of a w x y z quaternion."""
+    w, x, y, z = (float(c) for c in q)
+    return np.array([
+        [1.0 - 2.0 * (y * y + z * z), 2.0 * (x * y - z * w), 2.0 * (x * z + y * w)],
+        [2.0 * (x * y + z * w), 1.0 - 2.0 * (x * x + z * z), 2.0 * (y * z - x * w)],
+        [2.0 * (x * z - y * w), 2.0 * (y * z + x * w), 1.0 - 2.0 * (x * x + y * y)],
+    ], dtype=np.float64)
+
+
+def quat_mul(a, b) -> np.ndarray:
+    aw, ax, ay, az = (float(c) for c in a)
+    bw, bx, by, bz = (float(c) for c in b)
+    return np.array([aw * bw - ax * bx - ay * by - az * bz,
+                     aw * bx + ax * bw + ay * bz - az * by,
+                     aw * by - ax * bz + ay * bw + az * bx,
+                     aw * bz + ax * by - ay * bx + az * bw], dtype=np.float64)
+
+
+def quat_from_axis_angle(axis, angle: float) -> np.ndarray:
+    a = np.asarray(axis, dtype=np.float64)
+    a = a / max(float(np.linalg.norm(a)), 1e-12)
+    h = 0.5 * float(angle)
+    return np.concatenate([[np.cos(h)], np.sin(h) * a])
+
+
+def angular_velocity_between(q0, q1, dt: float) -> np.ndarray:
+    """World-frame angular velocity taking w x y z quaternion q0 to q1 over dt."""
+    d = quat_mul(np.asarray(q1, dtype=np.float64), np.array([q0[0], -q0[1], -q0[2], -q0[3]], dtype=np.float64))
+    d = d / np.linalg.norm(d)
+    if d[0] < 0.0:
+        d = -d
+    s = float(np.linalg.norm(d[1:]))
+    if s < 1e-9:
+        return np.zeros(3)
+    return d[1:] / s * (2.0 * np.arctan2(s, float(d[0])) / dt)
+
+
+def world_to_local(points, pos, quat) -> np.ndarray:
+    return (np.asarray(points, dtype=np.float64) - np.asarray(pos, dtype=np.float64)) @ quat_to_mat(quat)
+
+
+@dataclass(frozen=True)
+class GlassProfile:
+    outer_radius: float = 0.089
+    inner_radius: float = 0.069
+    height: float = 0.24
+    base_thickness: float = 0.050
+    fillet_radius: float = 0.012
+
+    def __post_init__(self):
+        if not 0.0 < self.inner_radius < self.outer_radius:
+            raise ValueError("need 0 < inner_radius < outer_radius")
+        if not 0.0 < self.base_thickness < self.height:
+            raise ValueError("need 0 < base_thickness < height")
+        if not 0.0 <= self.fillet_radius < self.inner_radius:
+            raise ValueError("need 0 <= fillet_radius < inner_radius")
+
+    @property
+    def half_height(self) -> float:
+        return 0.5 * self.height
+
+    @property
+    def inner_floor_z(self) -> float:
+        return self.base_thickness - 0.5 * self.height
+
+    @property
+    def rim_z(self) -> float:
+        return 0.5 * self.height
+
+    @property
+    def wall_thickness(self) -> float:
+        return self.outer_radius - self.inner_radius
+
+    def inner_radius_at_z(self, z) -> np.ndarray:
+        """Cavity radius against local z, including the quarter-circle floor fillet."""
+        z = np.asarray(z, dtype=np.float64)
+        fr = self.fillet_radius
+        r = np.full_like(z, self.inner_radius)
+        if fr > 0.0:
+            zc = self.inner_floor_z + fr
+            in_fillet = (z >= self.inner_floor_z) & (z < zc)
+            dz = z[in_fillet] - zc
+            r[in_fillet] = self.inner_radius - fr + np.sqrt(np.maximum(fr * fr - dz * dz, 0.0))
+            r = np.where(z < self.inner_floor_z, self.inner_radius - fr, r)
+        return r
+
+
+def _capped_cylinder(r, z, radius, z0, z1):
+    zc, hh = 0.5 * (z0 + z1), 0.5 * (z1 - z0)
+    dr = r - radius
+    dz = np.abs(z - zc) - hh
+    a, b = np.maximum(dr, 0.0), np.maximum(dz, 0.0)
+    return np.sqrt(a * a + b * b) + np.minimum(np.maximum(dr, dz), 0.0)
+
+
+def glass_sdf_local(points_local, profile: GlassProfile):
+    """Signed distance (float64, negative inside the glass material) in the local frame:
+    outer capped cylinder minus the fillet-dilated, rim-extended cavity cylinder."""
+    p = np.asarray(points_local, dtype=np.float64)
+    r = np.linalg.norm(p[..., :2], axis=-1)
+    z = p[..., 2]
+    fr = profile.fillet_radius
+    outer = _capped_cylinder(r, z, profile.outer_radius, -profile.half_height, profile.half_height)
+    cavity = _capped_cylinder(r, z, profile.inner_radius - fr, profile.inner_floor_z + fr,
+                              profile.half_height + profile.outer_radius) - fr
+    return np.maximum(outer, -cavity)
+
+
+def cup_fill(profile: GlassProfile, h: float, fill_fraction: float = 0.80, clearance: float | None = None,
+             floor_clearance: float | None = None, brim_clearance: float = 0.006, seed: int = 0):
+    """Jittered lattice (spacing h, +-h/4 uniform jitter from default_rng(seed)) filling
+    the cavity to `fill_fraction` of its usable height. Returns local-frame
+    (pos[N,3] float32, vol[N] float32)."""
+    clearance = h if clearance is None else clearance
+    floor_clearance = h if floor_clearance is None else floor_clearance
+    usable = profile.rim_z - profile.inner_floor_z - brim_clearance - floor_clearance
+    fill_h = fill_fraction * usable
+    if fill_h <= 0:
+        raise ValueError("fill height is non-positive; check clearances")
+    z0 = profile.inner_floor_z + floor_clearance
+    r_max = profile.inner_radius - clearance
+    xs = np.arange(-r_max + 0.5 * h, r_max, h)
+    zs = np.arange(z0 + 0.5 * h, z0 + fill_h, h)
+    lattice = np.stack(np.meshgrid(xs, xs, zs, indexing="ij"), axis=-1).reshape(-1, 3)
+    lattice = lattice + np.random.default_rng(seed).uniform(-0.25 * h, 0.25 * h, size=lattice.shape)
+    rad = np.linalg.norm(lattice[:, :2], axis=1)
+    z = lattice[:, 2]
+    keep = (rad < profile.inner_radius_at_z(z) - clearance) & (z >= z0) & (z <= z0 + fill_h)
+    pos = lattice[keep].astype(np.float32)
+    return pos, np.full(len(pos), h ** 3, dtype=np.float32)
+
+
+__all__ = ["GlassProfile", "angular_velocity_between", "cup_fill", "glass_sdf_local", "quat_from_axis_angle", "quat_mul", "quat_to_mat",
+           "world_to_local"]

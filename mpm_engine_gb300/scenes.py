@@ -1,0 +1,106 @@
+"""Scene builders used by tests and benchmarks (warpmpm.scenes, src/warpmpm/scenes.py:10-34),
+plus the synthetic workloads the benchmark runs (dam break, pour)."""
+from __future__ import annotations
+
+import numpy as np
+
+from .materials import Material, newtonian
+
+
+def dough(eta: float = 40.0, tau_y: float = 200.0) -> Material:
+    """Bingham preset of the squeeze-flow study: newtonian(eta) with a yield stress."""
+    return newtonian(eta=eta, density=1000.0).with_yield(tau_y)
+
+
+def block(grid, size=(0.12, 0.05, 0.06), center=None, ppc: int = 2, seed: int = 0):
+    """Jittered particle box resting 3 cells above the domain floor.
+    Returns (pos[N,3] float32, vol[N] float32, floor_z)."""
+    dx = grid.dx
+    floor = 3 * dx
+    h = dx / ppc
+    cx = grid.grid_lim * 0.5 if center is None else center[0]
+    cy = grid.grid_lim * 0.5 if center is None else center[1]
+    sx, sy, sz = size
+    axes = (np.arange(cx - 0.5 * sx + 0.5 * h, cx + 0.5 * sx, h),
+            np.arange(cy - 0.5 * sy + 0.5 * h, cy + 0.5 * sy, h),
+            np.arange(floor + 0.5 * h, floor + sz, h))
+    pts = np.stack(np.meshgrid(*axes, indexing="ij"), axis=-1).reshape(-1, 3)
+    pts = pts + np.random.default_rng(seed).uniform(-0.25 * h, 0.25 * h, size=pts.shape)
+    pos = pts.astype(np.float32)
+    return pos, np.full(len(pos), h ** 3, dtype=np.float32), floor
+
+
+def dam_break_lattice(n_grid: int = 64, grid_lim: float = 1.0, lo=(0.05, 0.05, 0.05), hi=(0.4, 0.6, 0.95),
+                      seed: int = 0):
+    """Dam-break fill: 8 particles per cell (spacing dx/2) over the box [lo, hi] with
+    +-h/4 seeded jitter. At 64^3 on the unit cube this is 362,250 particles."""
+    dx = grid_lim / n_grid
+    h = 0.5 * dx
+    axes = [np.arange(lo[a] + 0.5 * h, hi[a], h) for a in range(3)]
+    pts = np.stack(np.meshgrid(*axes, indexing="ij"), axis=-1).reshape(-1, 3)
+    pts = pts + np.random.default_rng(seed).uniform(-0.25 * h, 0.25 * h, size=pts.shape)
+    pos = pts.astype(np.float32)
+    return pos, np.full(len(pos), h ** 3, dtype=np.float32)
+
+
+# ---- the 340,489-particle pour (examples/pour_franka.py:73-116, 266-291, 341-365) ----
+POUR_GRID_LIM = 0.7
+POUR_SOURCE = (0.22, 0.50, 0.34)       # source glass centre in the MPM domain (scripted stand-in for the arm)
+POUR_RECEIVER = (0.46, 0.38, 0.14)     # receiver glass resting on the floor
+POUR_FLOOR_Z = 0.02
+HONEY = dict(eta=10.0, density=1420.0, bulk_modulus=9.0e5)
+
+
+def pour_substeps(liq: dict, dx: float, dt_tick: float = 1.0 / 60.0, cfl: float = 0.28) -> int:
+    """Acoustic CFL plus the explicit-viscosity bound (examples/pour_franka.py:98-110)."""
+    c = float(np.sqrt(1.1 * liq["bulk_modulus"] / liq["density"]))
+    acoustic = c / (cfl * dx)
+    viscous = 6.0 * liq["eta"] / (liq["density"] * dx * dx)
+    return int(np.ceil(dt_tick * max(acoustic, viscous)))
+
+
+class PourTrajectory:
+    """Scripted source-glass pose: upright, then a smoothstep tilt of `angle_deg`
+    over `duration` s toward the receiver, then hold (w x y z quaternions)."""
+
+    def __init__(self, angle_deg: float = 115.0, start: float = 0.1, duration: float = 1.2):
+        from .glass import quat_from_axis_angle
+        d = np.array(POUR_RECEIVER[:2]) - np.array(POUR_SOURCE[:2])
+        self.axis = np.array([-d[1], d[0], 0.0]) / np.linalg.norm(d)   # z x d: tips the rim toward d
+        self.angle, self.start, self.duration = np.deg2rad(angle_deg), start, duration
+        self._q = quat_from_axis_angle
+
+    def quat(self, t: float):
+        u = min(max((t - self.start) / self.duration, 0.0), 1.0)
+        return self._q(self.axis, self.angle * u * u * (3.0 - 2.0 * u))
+
+    def command(self, t: float, dt_tick: float):
+        """(center, quat, velocity, omega) for the control tick starting at t."""
+        from .glass import angular_velocity_between
+        q0, q1 = self.quat(t), self.quat(t + dt_tick)
+        return POUR_SOURCE, q0, (0.0, 0.0, 0.0), angular_velocity_between(q0, q1, dt_tick)
+
+
+def pour_scene(solver_cls, n_grid: int = 192, material=None, **solver_kw):
+    """The reference pour geometry: default GlassProfile filled to 80 % with cup_fill at
+    h = dx/2 (340,489 particles at 192^3, grid_lim 0.7), a separable floor (mu 0.3),
+    domain walls, a source and a receiver glass (friction 0.05). Returns
+    (solver, source handle, receiver handle, trajectory, substeps per 1/60 s frame, dt)."""
+    from .glass import GlassProfile, cup_fill
+    from .solver import GridConfig
+    prof = GlassProfile()
+    grid = GridConfig(n_grid=n_grid, grid_lim=POUR_GRID_LIM)
+    pos_local, vol = cup_fill(prof, grid.dx / 2, fill_fraction=0.80)
+    pos = (pos_local + np.asarray(POUR_SOURCE)).astype(np.float32)
+    s = solver_cls(grid=grid, **solver_kw).load_particles(pos, vol)
+    s.set_material(material if material is not None else newtonian(**HONEY))
+    s.add_plane((0, 0, POUR_FLOOR_Z), (0, 0, 1), "separate", friction=0.3)
+    s.add_domain_walls()
+    traj = PourTrajectory()
+    src = s.add_cup(prof, POUR_SOURCE, tuple(traj.quat(0.0)), friction=0.05)
+    rcv = s.add_cup(prof, POUR_RECEIVER, (1.0, 0.0, 0.0, 0.0), friction=0.05)
+    substeps = pour_substeps(HONEY, grid.dx)
+    return s, src, rcv, traj, substeps, (1.0 / 60.0) / substeps
+
+
+__all__ = ["HONEY", "PourTrajectory", "block", "dam_break_lattice", "dough", "pour_scene", "pour_substeps"]

@@ -1,0 +1,892 @@
+"""Drop-in replacement of warpmpm's typed `Solver` (src/warpmpm/core/solver.py:47-642).
+
+Same constructor fields, method names, argument meaning, return values and
+exceptions. Particle and grid state are PyTorch CUDA tensors owned by the
+solver; the substep runs in libgbmpm.so (hand-written sm_103a kernels) through
+the C ABI of include/gbmpm.h, given the tensors' device pointers. There is no
+Warp, no Triton and no CPU path: a solver whose device is not CUDA, or whose
+native library is missing, raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import warnings
+from dataclasses import dataclass, field
+from typing import Any
+
+import numpy as np
+
+from . import _abi, host
+from .glass import quat_to_mat
+from .materials import material_id
+
+_COV6_IDX = ((0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2))
+_DEVICE_ANNOUNCED = False
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _cov_to_six(cov: np.ndarray) -> np.ndarray:
+    """(N, 6) upper-triangle or (N, 3, 3) symmetric -> (N, 6) float32 xx, xy, xz, yy, yz, zz."""
+    cov = np.asarray(cov)
+    if cov.ndim == 2 and cov.shape[1] == 6:
+        return np.ascontiguousarray(cov, dtype=np.float32)
+    if cov.ndim == 3 and cov.shape[1:] == (3, 3):
+        return np.ascontiguousarray(np.stack([cov[:, i, j] for i, j in _COV6_IDX], axis=1), dtype=np.float32)
+    raise ValueError(f"cov must be (N, 6) or (N, 3, 3), got shape {cov.shape}")
+
+
+@dataclass
+class GridConfig:
+    n_grid: int = 64
+    grid_lim: float = 0.4  # cubic domain edge, metres
+
+    @property
+    def dx(self) -> float:
+        return self.grid_lim / self.n_grid
+
+
+class _Engine:
+    """Owner of one native engine handle."""
+
+    def __init__(self):
+        self.lib = _abi.load()
+        h = C.c_void_p()
+        _abi.check(self.lib.gbmpm_engine_create(C.byref(h)), "gbmpm_engine_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.gbmpm_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _DeviceArray:
+    """Minimal stand-in for the wp.array handles tests reach through `_sim`."""
+
+    def __init__(self, t):
+        self._t = t
+
+    def numpy(self):
+        return self._t.detach().cpu().numpy()
+
+    @property
+    def ptr(self) -> int:
+        return self._t.data_ptr()
+
+    @property
+    def shape(self):
+        return tuple(self._t.shape)
+
+    def zero_(self):
+        self._t.zero_()
+
+
+class _StateView:
+    def __init__(self, s: Solver):
+        self._s = s
+
+    def __getattr__(self, name):
+        t = self._s._t
+        key = name[len("particle_"):] if name.startswith("particle_") else None
+        if key in t:
+            return _DeviceArray(t[key])
+        raise AttributeError(name)
+
+
+class _ModelView:
+    def __init__(self, s: Solver):
+        self._s = s
+
+    @property
+    def mu(self):
+        return _DeviceArray(self._s._t["mu"])
+
+    @property
+    def lam(self):
+        return _DeviceArray(self._s._t["lam"])
+
+    @property
+    def yield_stress(self):
+        return _DeviceArray(self._s._t["yield_stress"])
+
+    def _get(self, name):
+        return getattr(self._s._model, name)
+
+    def _set(self, name, value):
+        setattr(self._s._model, name, value)
+        self._s._model_dirty = True
+
+    grid_v_damping_scale = property(lambda self: self._get("grid_v_damping_scale"),
+                                    lambda self, v: self._set("grid_v_damping_scale", host.f32(v)))
+    rpic_damping = property(lambda self: self._get("rpic_damping"),
+                            lambda self, v: self._set("rpic_damping", host.f32(v)))
+    periodic_x = property(lambda self: self._get("periodic_x"), lambda self, v: self._set("periodic_x", int(v)))
+    n_grid = property(lambda self: self._get("n_grid"))
+    dx = property(lambda self: self._get("dx"))
+    inv_dx = property(lambda self: self._get("inv_dx"))
+    cdf_mask_off = 0
+
+
+class _SimShim:
+    """The parts of MPM_Simulator_WARP that tests and scripts touch through
+    `Solver._sim` (mpm_solver_warp.py), mapped onto this engine."""
+
+    def __init__(self, s: Solver):
+        self._s = s
+        self.mpm_state = _StateView(s)
+        self.mpm_model = _ModelView(s)
+        self.use_cuda_graph = os.environ.get("WARPMPM_NO_CUDA_GRAPH", "") != "1" and \
+            os.environ.get("GBMPM_NO_CUDA_GRAPH", "") != "1"
+        self.restrict_bc = True
+        self.restrict_grid = True
+        self.pre_p2g_operations = []
+        self.particle_velocity_modifiers = []
+        self.n_rigid_bodies = 0
+        self.profile = False
+        self.time_profile: dict = {}
+        self._block_counts = None
+
+    @property
+    def n_particles(self) -> int:
+        return self._s._n
+
+    @property
+    def time(self) -> float:
+        return self._s._time
+
+    def rebuild_active_blocks(self, device=None):
+        self._s._rebuild_active_blocks()
+
+    def active_block_fraction(self) -> float:
+        if self._block_counts is None:
+            return 1.0
+        bd = (self._s.grid.n_grid + 3) // 4
+        return self._block_counts[0] / float(bd ** 3)
+
+    def _import(self, key, tensor, shape):
+        torch = _torch()
+        src = tensor.detach().reshape(shape).to(device=self._s._t[key].device, dtype=self._s._t[key].dtype)
+        self._s._t[key].copy_(src)
+        torch.cuda.synchronize()
+
+    def import_particle_x_from_torch(self, t, clone=True, device=None):
+        if t is not None:
+            self._import("x", t, (-1, 3))
+
+    def import_particle_v_from_torch(self, t, clone=True, device=None):
+        if t is not None:
+            self._import("v", t, (-1, 3))
+
+    def import_particle_F_from_torch(self, t, clone=True, device=None):
+        if t is not None:
+            self._import("F", t, (-1, 3, 3))
+
+    def import_particle_C_from_torch(self, t, clone=True, device=None):
+        if t is not None:
+            self._import("C", t, (-1, 3, 3))
+
+    def export_particle_x_to_torch(self):
+        return self._s._t["x"]
+
+    def export_particle_v_to_torch(self):
+        return self._s._t["v"]
+
+    def export_particle_F_to_torch(self):
+        return self._s._t["F"].reshape(-1, 9)
+
+    def export_particle_stress_to_torch(self):
+        return self._s._t["stress"].reshape(-1, 9)
+
+
+@dataclass
+class Solver:
+    """One scene on one GPU. Field meanings follow warpmpm.Solver."""
+
+    grid: GridConfig = field(default_factory=GridConfig)
+    device: str = "auto"
+    guard_interval: int = 1
+    sparse: bool = False
+    fused: bool = True
+    sort_interval: int = 0
+    profile: bool = False
+    inversion_policy: str = "warn"
+    periodic_x: bool = False
+    _sim: Any = field(default=None, init=False, repr=False)
+    _step: int = field(default=0, init=False, repr=False)
+    _tick: int = field(default=0, init=False, repr=False)
+    _vol0: Any = field(default=None, init=False, repr=False)
+
+    def __post_init__(self) -> None:
+        if self.inversion_policy not in {"warn", "raise", "nan"}:
+            raise ValueError("inversion_policy must be 'warn', 'raise', or 'nan'")
+        self._eng = None
+        self._t: dict = {}
+        self._n = 0
+        self._time = 0.0
+        self._model = None
+        self._model_dirty = True
+        self._cols: list = []          # engine collider records (engine copy is authoritative)
+        self._handles: list = []       # reference handle -> engine collider index (None: extra wall slots)
+        self._cols_dirty = True
+        self._keep: list = []          # tensors referenced by collider records
+        self._mat_current = 0
+        self._sdf_guard: dict = {}
+        self._rigid_surfaces: list = []
+        self._update_cov = False
+
+    # ------------------------------------------------------------------ setup
+    def _resolve_device(self) -> None:
+        torch = _torch()
+        if self.device == "auto":
+            self.device = "cuda:0" if torch.cuda.is_available() else "cpu"
+            global _DEVICE_ANNOUNCED
+            if not _DEVICE_ANNOUNCED:
+                _DEVICE_ANNOUNCED = True
+                print(f"mpm_engine_gb300: device auto -> {self.device}")
+        if not str(self.device).startswith("cuda"):
+            raise RuntimeError(f"mpm_engine_gb300 runs on CUDA devices only (device={self.device!r}); "
+                               f"there is no CPU path")
+        if not torch.cuda.is_available():
+            raise RuntimeError("CUDA is not available: mpm_engine_gb300 has no CPU path")
+
+    def load_particles(self, pos: np.ndarray, vol: np.ndarray, cov: np.ndarray | None = None,
+                       cov_mode: str = "step") -> Solver:
+        """Load positions (N,3) and volumes (N,); optional per-particle covariance (N,6)
+        or (N,3,3), advected each substep ("step") or rebuilt from F at export ("from_F")."""
+        torch = _torch()
+        self._resolve_device()
+        _abi.load()
+        dev = torch.device(self.device)
+        torch.cuda.set_device(dev)
+        pos = np.asarray(pos)
+        n = len(pos)
+        self._n = n
+        self._vol0 = np.asarray(vol).astype(np.float32).copy()
+        cov6 = None
+        if cov is not None:
+            if cov_mode not in ("step", "from_F"):
+                raise ValueError(f"cov_mode must be 'step' or 'from_F', got {cov_mode!r}")
+            cov6 = _cov_to_six(cov)
+            if cov6.shape[0] != n:
+                raise ValueError(f"cov has {cov6.shape[0]} rows, expected {n}")
+        f = dict(device=dev, dtype=torch.float32)
+        eye = torch.eye(3, **f).expand(n, 3, 3).contiguous()
+        t = {
+            "x": torch.from_numpy(np.ascontiguousarray(pos, dtype=np.float32)).to(dev),
+            "v": torch.zeros(n, 3, **f), "C": torch.zeros(n, 3, 3, **f), "F": eye.clone(),
+            "F_trial": eye.clone(), "L": torch.zeros(n, 3, 3, **f), "stress": torch.zeros(n, 3, 3, **f),
+            "R": torch.zeros(n, 3, 3, **f),
+            "vol": torch.from_numpy(self._vol0.copy()).to(dev), "mass": torch.zeros(n, **f),
+            "density": torch.zeros(n, **f), "Jp": torch.zeros(n, **f), "mu": torch.zeros(n, **f),
+            "lam": torch.zeros(n, **f), "yield_stress": torch.zeros(n, **f),
+            "material": torch.zeros(n, device=dev, dtype=torch.int32),
+            "selection": torch.zeros(n, device=dev, dtype=torch.int32),
+            "init_cov": None, "cov": None,
+        }
+        if cov6 is not None:
+            t["init_cov"] = torch.from_numpy(cov6).to(dev)
+            t["cov"] = t["init_cov"].clone() if cov_mode == "step" else torch.zeros_like(t["init_cov"])
+        ng = int(self.grid.n_grid)
+        t["grid_mv"] = torch.zeros(ng * ng * ng, 4, **f)
+        t["grid_v"] = torch.zeros(ng * ng * ng, 4, **f)
+        t["perm"] = torch.zeros(max(n, 1), device=dev, dtype=torch.int32)
+        t["eta_table"] = torch.zeros(2, **f)
+        self._t = t
+        self._update_cov = cov6 is not None and cov_mode == "step"
+        self._model = host.default_model(ng, self.grid.grid_lim)
+        self._model.periodic_x = 1 if self.periodic_x else 0
+        self._model.update_cov_with_F = 1 if self._update_cov else 0
+        self._model.eta_table = t["eta_table"].data_ptr()
+        self._eng = _Engine()
+        self._bind()
+        self._model_dirty = True
+        self._sim = _SimShim(self)
+        return self
+
+    def _ptr(self, key) -> int | None:
+        tt = self._t.get(key)
+        return None if tt is None else tt.data_ptr()
+
+    def _bind(self) -> None:
+        p = _abi.Particles()
+        p.n = self._n
+        for k in ("x", "v", "C", "F", "F_trial", "L", "stress", "mass", "vol", "density", "Jp", "mu", "lam",
+                  "yield_stress", "material", "selection", "cov", "init_cov"):
+            setattr(p, k, self._ptr(k))
+        g = _abi.Grid()
+        g.n_grid = int(self.grid.n_grid)
+        g.mv = self._ptr("grid_mv")
+        g.v = self._ptr("grid_v")
+        lib = self._eng.lib
+        _abi.check(lib.gbmpm_bind(self._eng.h, C.byref(p), C.byref(g)), "gbmpm_bind")
+
+    def _stream(self) -> int:
+        return _torch().cuda.current_stream().cuda_stream
+
+    def _require_loaded(self) -> None:
+        if self._eng is None:
+            raise RuntimeError("load_particles must be called first")
+
+    # -------------------------------------------------------------- materials
+    def _apply_params(self, kw: dict, lo: int | None = None, hi: int | None = None) -> None:
+        """set_parameters_dict (whole scene) or set_parameters_for_particles ([lo, hi))."""
+        torch = _torch()
+        t, m = self._t, self._model
+        ranged = lo is not None
+        sl = slice(lo, hi) if ranged else slice(None)
+        if "material" in kw:
+            mid = material_id(kw["material"])
+            t["material"][sl] = mid
+            if ranged:
+                m.material_mask |= 1 << mid
+            else:
+                self._mat_current = mid
+                m.material_mask = 1 << mid
+            mat = mid
+        else:
+            mat = self._mat_current
+        host.apply_type_params(m, mat, kw)
+        if "yield_stress" in kw:
+            t["yield_stress"][sl] = float(kw["yield_stress"])
+        if "eta_table" in kw:
+            tab = np.asarray(kw["eta_table"], dtype=np.float32).reshape(-1)
+            t["eta_table"] = torch.from_numpy(tab.copy()).to(t["x"].device)
+            m.eta_table = t["eta_table"].data_ptr()
+            m.eta_table_n = int(tab.shape[0])
+        if "eta_table_smin" in kw:
+            m.eta_table_smin = host.f32(kw["eta_table_smin"])
+        if "eta_table_smax" in kw:
+            m.eta_table_smax = host.f32(kw["eta_table_smax"])
+        if "g" in kw and not ranged:
+            g = kw["g"]
+            m.gravity[:] = (host.f32(g[0]), host.f32(g[1]), host.f32(g[2]))
+        if "density" in kw:
+            t["density"][sl] = float(kw["density"])
+            t["mass"][sl] = t["density"][sl] * t["vol"][sl]
+        if "E" in kw or "nu" in kw:
+            if ranged:
+                # the range path computes in float64 from the fp32 table values (:1774-1783)
+                E_val, nu_val = float(m.E[mat]), float(m.nu[mat])
+                t["mu"][sl] = E_val / (2.0 * (1.0 + nu_val))
+                t["lam"][sl] = E_val * nu_val / ((1.0 + nu_val) * (1.0 - 2.0 * nu_val))
+            else:
+                self._finalize_mu_lam()
+        if "rpic_damping" in kw:
+            m.rpic_damping = host.f32(kw["rpic_damping"])
+        if "grid_v_damping_scale" in kw:
+            m.grid_v_damping_scale = host.f32(kw["grid_v_damping_scale"])
+        if "additional_material_params" in kw:
+            raise NotImplementedError("regional additional_material_params are not supported")
+        self._model_dirty = True
+
+    def _finalize_mu_lam(self) -> None:
+        torch = _torch()
+        t, m = self._t, self._model
+        dev = t["x"].device
+        E = torch.tensor(list(m.E), device=dev, dtype=torch.float32)
+        nu = torch.tensor(list(m.nu), device=dev, dtype=torch.float32)
+        idx = t["material"].long()
+        Ep, nup = E[idx], nu[idx]
+        t["mu"].copy_(Ep / (2.0 * (1.0 + nup)))
+        t["lam"].copy_(Ep * nup / ((1.0 + nup) * (1.0 - 2.0 * nup)))
+
+    def set_material(self, material, **overrides: float) -> Solver:
+        """A Material (or material name) applied to every particle; gravity defaults
+        to (0, 0, -9.81) unless overridden."""
+        self._require_loaded()
+        if hasattr(material, "resolve"):
+            name, params = material.resolve()
+        else:
+            name, params = str(material), {}
+        params = {**params, **overrides}
+        self._apply_params({"material": name, "g": [0.0, 0.0, -9.81], **params})
+        self._finalize_mu_lam()
+        return self
+
+    def set_material_range(self, start: int, end: int, material, **overrides) -> Solver:
+        """Material for particles [start, end); per-type parameters are shared by id."""
+        self._require_loaded()
+        if hasattr(material, "resolve"):
+            name, params = material.resolve()
+        else:
+            name, params = str(material), {}
+        if name in ("tabulated_viscous", "tabulated_mu_i"):
+            raise NotImplementedError("tabulated materials are global-only (one eta table on the model); "
+                                      "use set_material")
+        self._apply_params({"material": name, **params, **overrides}, lo=int(start), hi=int(end))
+        return self
+
+    def finalize_rigid_bodies(self) -> Solver:
+        raise NotImplementedError("rigid bodies are not part of this engine")
+
+    # -------------------------------------------------------------- colliders
+    def _add_collider(self, rec, slots: int = 1) -> int:
+        idx = len(self._cols)
+        self._cols.append(rec)
+        first = len(self._handles)
+        self._handles.append(idx)
+        for _ in range(slots - 1):
+            self._handles.append(None)
+        self._cols_dirty = True
+        return first
+
+    def _pull_colliders(self) -> None:
+        """Bring the engine's integrated poses into the host records."""
+        if self._cols_dirty or not self._cols:
+            return
+        arr = (_abi.Collider * len(self._cols))()
+        _abi.check(self._eng.lib.gbmpm_get_colliders(self._eng.h, arr, len(self._cols)), "gbmpm_get_colliders")
+        self._cols = [arr[i] for i in range(len(self._cols))]
+
+    def _push_colliders(self) -> None:
+        if not self._cols_dirty:
+            return
+        arr = (_abi.Collider * max(1, len(self._cols)))(*self._cols)
+        _abi.check(self._eng.lib.gbmpm_set_colliders(self._eng.h, arr, len(self._cols)), "gbmpm_set_colliders")
+        self._cols_dirty = False
+
+    def _col(self, handle: int):
+        if handle < 0 or handle >= len(self._handles) or self._handles[handle] is None:
+            raise IndexError(f"no collider with handle {handle}")
+        self._pull_colliders()
+        return self._handles[handle]
+
+    def add_plane(self, point, normal, surface: str = "sticky", friction: float = 0.0,
+                  restitution: float = 0.0) -> Solver:
+        """Half-space boundary behind `point` along `normal` (sticky / slip / separable)."""
+        self._require_loaded()
+        rec = host.plane_collider(point, normal, surface, friction)
+        if restitution != 0.0:
+            if not (0.0 < restitution <= 1.0):
+                raise ValueError("restitution must be between 0 (exclusive) and 1 (inclusive).")
+            self._rigid_surfaces.append((tuple(point), tuple(normal), friction, restitution))
+        self._pull_colliders()
+        self._add_collider(rec)
+        return self
+
+    def add_box(self, center, half_size, velocity=(0.0, 0.0, 0.0), start_time: float = 0.0,
+                end_time: float = 1.0e9) -> int:
+        """Kinematic axis-aligned box imposing its velocity on covered nodes; returns a handle."""
+        self._require_loaded()
+        self._pull_colliders()
+        return self._add_collider(host.box_collider(center, half_size, velocity, start_time, end_time))
+
+    def set_box(self, handle: int, center=None, velocity=None) -> Solver:
+        """Start-of-tick centre and per-tick velocity (the box sweeps center -> center + dt*v)."""
+        i = self._col(handle)
+        c = self._cols[i]
+        if center is not None:
+            host._vec(c.point, center)
+        if velocity is not None:
+            host._vec(c.velocity, velocity)
+        self._cols_dirty = True
+        return self
+
+    def add_cup(self, profile, center, quat=(1.0, 0.0, 0.0, 0.0), velocity=(0.0, 0.0, 0.0),
+                omega=(0.0, 0.0, 0.0), friction: float = 0.05, sticky_cells: float = 1.5,
+                contact_cells: float = 0.5, start_time: float = 0.0, end_time: float = 1.0e9) -> int:
+        """Kinematic open-top glass (analytic revolved SDF, quat w x y z); returns a handle."""
+        self._require_loaded()
+        sticky_depth = min(sticky_cells * self.grid.dx, 0.45 * profile.wall_thickness)
+        rec = host.cup_collider(center, quat_to_mat(quat), velocity, omega, profile.outer_radius,
+                                profile.inner_radius, profile.half_height, profile.inner_floor_z,
+                                profile.fillet_radius, friction, sticky_depth, contact_cells * self.grid.dx,
+                                start_time, end_time)
+        self._pull_colliders()
+        return self._add_collider(rec)
+
+    def set_cup(self, handle: int, center=None, quat=None, velocity=None, omega=None) -> Solver:
+        i = self._col(handle)
+        c = self._cols[i]
+        if center is not None:
+            host._vec(c.point, center)
+        if quat is not None:
+            host.set_rotation(c, quat_to_mat(quat))
+        if velocity is not None:
+            host._vec(c.velocity, velocity)
+        if omega is not None:
+            host._vec(c.omega, omega)
+        self._cols_dirty = True
+        return self
+
+    def _wrench(self, handle: int) -> np.ndarray:
+        i = self._col(handle)
+        self._push_colliders()
+        out = (C.c_double * 6)()
+        _abi.check(self._eng.lib.gbmpm_wrench(self._eng.h, i, out, self._stream()), "gbmpm_wrench")
+        return np.array(out[:], dtype=float)
+
+    def _reset_wrench(self, handle: int) -> None:
+        i = self._col(handle)
+        self._push_colliders()
+        _abi.check(self._eng.lib.gbmpm_reset_wrench(self._eng.h, i, self._stream()), "gbmpm_reset_wrench")
+
+    def reset_cup_wrench(self, handle: int) -> Solver:
+        self._reset_wrench(handle)
+        return self
+
+    def cup_wrench(self, handle: int, dt: float) -> dict:
+        """Accumulated reaction impulse / dt: {'force': (3,), 'torque': (3,)} (torque about the cup centre)."""
+        w = self._wrench(handle)
+        return {"force": w[:3] / dt, "torque": w[3:] / dt}
+
+    def add_domain_walls(self, start_time: float = 0.0, end_time: float = 1.0e9) -> Solver:
+        """Zero outward velocity in a three-cell band at each domain face."""
+        self._require_loaded()
+        self._pull_colliders()
+        self._add_collider(host.walls_collider(start_time, end_time), slots=6)
+        return self
+
+    def add_sdf_collider(self, sdf, center, quat=(0.0, 0.0, 0.0, 1.0), velocity=(0.0, 0.0, 0.0),
+                         omega=(0.0, 0.0, 0.0), band=None, surface: str = "separable", friction: float = 0.4,
+                         start_time: float = 0.0, end_time: float = 1.0e9) -> int:
+        """Moving signed-distance-field collider (geometry.SDFData, quat x y z w); returns a handle."""
+        self._require_loaded()
+        torch = _torch()
+        res = int(np.asarray(sdf.values).shape[0])
+        if band is None:
+            band = float(self._model.dx)
+        surface_id = host.SDF_SURFACES[surface]
+        bmin = host.sdf_boundary_min(sdf.values)
+        if band >= bmin:
+            raise ValueError(
+                f"SDF collider contact band ({band * 1e3:.1f} mm) reaches or exceeds the SDF "
+                f"grid margin ({bmin * 1e3:.1f} mm): near-surface space outside the "
+                f"stored grid would get no collision. Rebuild the SDF with more margin_cells "
+                f"or reduce band.")
+        dev = self._t["x"].device
+        val = torch.from_numpy(np.ascontiguousarray(sdf.values, dtype=np.float32)).to(dev)
+        grad = torch.from_numpy(np.ascontiguousarray(sdf.grads, dtype=np.float32)).to(dev)
+        self._keep += [val, grad]
+        rec = host.sdf_collider(val.data_ptr(), grad.data_ptr(), res, sdf.origin, sdf.cell, center, quat,
+                                velocity, omega, band, surface_id, friction, start_time, end_time)
+        self._pull_colliders()
+        h = self._add_collider(rec)
+        self._sdf_guard[h] = {"r_max": host.sdf_r_max(sdf.origin, sdf.cell, res), "band": float(band),
+                              "warned": False}
+        return h
+
+    def set_sdf_pose(self, handle: int, center=None, quat=None, velocity=None, omega=None) -> Solver:
+        i = self._col(handle)
+        c = self._cols[i]
+        guard = self._sdf_guard.get(handle)
+        if guard is not None and not guard["warned"]:
+            jump = 0.0
+            if center is not None:
+                jump += float(np.linalg.norm(np.array([float(center[k]) - c.point[k] for k in range(3)])))
+            if quat is not None:
+                dot = abs(sum(float(quat[k]) * c.quat[k] for k in range(4)))
+                jump += 2.0 * float(np.arccos(min(1.0, dot))) * guard["r_max"]
+            if jump > guard["band"]:
+                guard["warned"] = True
+                warnings.warn(
+                    f"set_sdf_pose jumped the collider surface by up to {jump * 1e3:.2f} mm in one tick, more "
+                    f"than the contact band ({guard['band'] * 1e3:.2f} mm): material inside the swept region "
+                    f"can be tunnelled through. Drive the pose in smaller per-tick steps (or via "
+                    f"velocity/omega).", RuntimeWarning, stacklevel=2)
+        if center is not None:
+            host._vec(c.point, center)
+        if quat is not None:
+            host._vec(c.quat, quat)
+        if velocity is not None:
+            host._vec(c.velocity, velocity)
+        if omega is not None:
+            host._vec(c.omega, omega)
+        self._cols_dirty = True
+        return self
+
+    def reset_sdf_force(self, handle: int) -> Solver:
+        self._reset_wrench(handle)
+        return self
+
+    def sdf_wrench(self, handle: int, dt: float) -> dict:
+        w = self._wrench(handle)
+        return {"force": w[:3] / dt, "torque": w[3:] / dt}
+
+    def add_cdf_collider(self, cdf, center, quat=(0.0, 0.0, 0.0, 1.0), velocity=(0.0, 0.0, 0.0),
+                         omega=(0.0, 0.0, 0.0), band=None, surface: str = "separable", friction: float = 0.4,
+                         start_time: float = 0.0, end_time: float = 1.0e9) -> int:
+        if self.periodic_x:
+            raise NotImplementedError("CDF colliders do not wrap the periodic x axis")
+        raise NotImplementedError("CPIC thin-boundary (CDF) colliders are not built in this engine")
+
+    def reset_tool_force(self, handle: int) -> Solver:
+        self._reset_wrench(handle)
+        return self
+
+    def tool_force(self, handle: int, dt: float) -> np.ndarray:
+        """Box reaction force: accumulated sum of m (v_free - v_box) / dt."""
+        return self._wrench(handle)[:3] / dt
+
+    # ------------------------------------------------------------------- step
+    def _sync_engine(self) -> None:
+        lib, h = self._eng.lib, self._eng.h
+        if self._model_dirty:
+            self._model.update_cov_with_F = 1 if self._update_cov else 0
+            _abi.check(lib.gbmpm_set_model(h, C.byref(self._model)), "gbmpm_set_model")
+            self._model_dirty = False
+        self._push_colliders()
+
+    def _sdf_tunnel_check(self, dt: float) -> None:
+        for handle, guard in self._sdf_guard.items():
+            if guard["warned"]:
+                continue
+            c = self._cols[self._handles[handle]]
+            speed = float(np.hypot(np.hypot(c.velocity[0], c.velocity[1]), c.velocity[2])) + \
+                float(np.linalg.norm([c.omega[0], c.omega[1], c.omega[2]])) * guard["r_max"]
+            live = c.start_time <= self._time < c.end_time
+            if live and speed * dt > guard["band"]:
+                guard["warned"] = True
+                warnings.warn(
+                    f"SDF collider surface sweeps {speed * dt * 1e3:.2f} mm per substep, more than the contact "
+                    f"band ({guard['band'] * 1e3:.2f} mm): fast material can tunnel through. Reduce dt, "
+                    f"velocity/omega, or raise band (and the SDF margin).", RuntimeWarning, stacklevel=3)
+
+    def step(self, dt: float, substeps: int = 1) -> Solver:
+        """Advance `substeps` substeps of size dt (one control tick)."""
+        self._require_loaded()
+        if self._tick % max(1, self.guard_interval) == 0:
+            self._update_grid_box(dt, substeps)
+        if self.sort_interval and self._tick % self.sort_interval == 0:
+            self._sort_particles()
+        if self.sparse:
+            self._rebuild_active_blocks()
+        self._sim.profile = self.profile
+        self._tick += 1
+        self._pull_colliders()
+        if self._sdf_guard:
+            self._sdf_tunnel_check(dt)
+        self._sync_engine()
+        flags = 0
+        if self.fused and not self.sparse:
+            flags |= _abi.TICK_FUSED
+        if self.profile:
+            flags |= _abi.TICK_PROFILE
+        elif self._sim.use_cuda_graph:
+            flags |= _abi.TICK_GRAPH
+        t = C.c_double(self._time)
+        _abi.check(self._eng.lib.gbmpm_tick(self._eng.h, C.byref(t), float(dt), int(substeps), flags,
+                                            self._stream()), "gbmpm_tick")
+        self._time = t.value
+        self._step += substeps
+        return self
+
+    def _rebuild_active_blocks(self) -> None:
+        self._sync_engine()
+        counts = (C.c_int32 * 2)()
+        _abi.check(self._eng.lib.gbmpm_rebuild_active_blocks(self._eng.h, counts, self._stream()),
+                   "gbmpm_rebuild_active_blocks")
+        self._sim._block_counts = (int(counts[0]), int(counts[1]))
+
+    def _sort_particles(self) -> bool:
+        """Stable block-key sort (4^3 blocks of the stencil base, float64 keys); skipped
+        when already ordered. Returns True when particles were permuted."""
+        self._require_loaded()
+        flag = C.c_int32(0)
+        perm = self._t["perm"]
+        _abi.check(self._eng.lib.gbmpm_sort_particles(self._eng.h, float(self.grid.dx), C.byref(flag),
+                                                      perm.data_ptr(), self._stream()), "gbmpm_sort_particles")
+        if not flag.value:
+            return False
+        p = perm[: self._n].cpu().numpy().astype(np.int64)
+        self._vol0 = self._vol0[p]
+        return True
+
+    def profile_report(self) -> str:
+        """Per-phase device time collected while profile=True (CUDA events, live launches)."""
+        if self._eng is None:
+            return "profile_report: no samples (set solver.profile = True and step)"
+        ms = (C.c_double * _abi.NUM_PHASES)()
+        cnt = (C.c_int64 * _abi.NUM_PHASES)()
+        _abi.check(self._eng.lib.gbmpm_profile(self._eng.h, ms, cnt, 0), "gbmpm_profile")
+        rows = [(self._eng.lib.gbmpm_phase_name(i).decode(), ms[i] / 1000.0, cnt[i])
+                for i in range(_abi.NUM_PHASES) if cnt[i]]
+        if not rows:
+            return "profile_report: no samples (set solver.profile = True and step)"
+        timed = sum(r[1] for r in rows)
+        rows.sort(key=lambda r: -r[1])
+        lines = [f"substep profile over {self._step} substeps (timed device work {timed:.1f}s; "
+                 f"live launches + per-phase sync):"]
+        for name, tot, n in rows:
+            lines.append(f"  {name:<28s} {tot:7.1f}s  {tot / max(n, 1) * 1000:8.3f} ms/substep"
+                         f"  {tot / timed * 100:5.1f}%")
+        return "\n".join(lines)
+
+    def _update_grid_box(self, dt: float, substeps: int) -> None:
+        """Edge guard once per control tick (core/solver.py:485-518), reduced on the device."""
+        out = (C.c_float * 7)()
+        st = C.c_uint32(0)
+        _abi.check(self._eng.lib.gbmpm_guard(self._eng.h, out, C.byref(st), self._stream()), "gbmpm_guard")
+        if st.value & _abi.FLAG_STENCIL_OOB:
+            raise RuntimeError("a particle's P2G stencil left the grid during the previous tick; the kernels "
+                               "skipped it. Enlarge grid_lim or add a bounding box / wall collider.")
+        dx, lim = self.grid.dx, self.grid.grid_lim
+        lo = np.array(out[0:3], dtype=np.float32)
+        hi = np.array(out[3:6], dtype=np.float32)
+        if self.periodic_x:
+            gmin, gmax = float(lo[1:].min()), float(hi[1:].max())
+        else:
+            gmin, gmax = float(lo.min()), float(hi.max())
+        if gmin < 1.5 * dx or gmax > lim - 2.5 * dx:
+            raise RuntimeError(host.grid_guard_message(gmin, gmax, lim, dx))
+
+    # ---------------------------------------------------------------- imports
+    def _import_rows(self, key: str, data) -> None:
+        torch = _torch()
+        if isinstance(data, torch.Tensor):
+            # a (pinned) host or device tensor: stream-ordered copy into the existing buffer
+            self._t[key].copy_(data.reshape(-1, 3), non_blocking=True)
+            return
+        self._t[key].copy_(torch.from_numpy(np.ascontiguousarray(data, dtype=np.float32)).reshape(-1, 3))
+        torch.cuda.synchronize()
+
+    def set_x(self, pos) -> Solver:
+        """Copy positions into the existing device buffer (pointers stay stable)."""
+        self._import_rows("x", pos)
+        return self
+
+    def set_v(self, vel) -> Solver:
+        self._import_rows("v", vel)
+        return self
+
+    def x_into(self, out) -> None:
+        """Stream-ordered copy of the positions into a caller (pinned host) tensor."""
+        out.copy_(self._t["x"], non_blocking=True)
+
+    # ---------------------------------------------------------------- exports
+    def x(self) -> np.ndarray:
+        return self._t["x"].cpu().numpy()
+
+    def v(self) -> np.ndarray:
+        return self._t["v"].cpu().numpy()
+
+    def F(self) -> np.ndarray:
+        return self._t["F"].cpu().numpy().reshape(-1, 3, 3)
+
+    def stress(self) -> np.ndarray:
+        return self._t["stress"].cpu().numpy().reshape(-1, 3, 3)
+
+    def L(self) -> np.ndarray:
+        """Velocity gradient L_ij = dv_i/dx_j from the most recent gather."""
+        return self._t["L"].cpu().numpy().reshape(-1, 3, 3)
+
+    def C(self) -> np.ndarray:
+        return self._t["C"].cpu().numpy().reshape(-1, 3, 3)
+
+    def inverted_count(self) -> int:
+        J = np.linalg.det(self.F())
+        return int(np.count_nonzero(~np.isfinite(J) | (J <= 0.0)))
+
+    def _checked_jacobian(self) -> np.ndarray:
+        if self.inversion_policy not in {"warn", "raise", "nan"}:
+            raise ValueError("inversion_policy must be 'warn', 'raise', or 'nan'")
+        J = np.linalg.det(self.F())
+        bad = ~np.isfinite(J) | (J <= 0.0)
+        n = int(np.count_nonzero(bad))
+        if not n:
+            return J
+        message = (f"{n} particles have non-finite or non-positive det(F); current volume "
+                   "and Cauchy stress are undefined for an inverted configuration")
+        if self.inversion_policy == "raise":
+            raise RuntimeError(message)
+        if self.inversion_policy == "warn":
+            if not getattr(self, "_warned_inverted", False):
+                self._warned_inverted = True
+                warnings.warn(f"{message}; using |det(F)| for compatibility. Set inversion_policy='raise' to "
+                              "reject or 'nan' to mark these particles.", RuntimeWarning, stacklevel=3)
+            out = np.abs(J)
+            out[~np.isfinite(out)] = np.nan
+            return out
+        J = J.copy()
+        J[bad] = np.nan
+        return J
+
+    def vol(self) -> np.ndarray:
+        return self._vol0 * self._checked_jacobian()
+
+    def cauchy(self) -> np.ndarray:
+        """Cauchy stress = Kirchhoff / det(F) under the inversion policy."""
+        J = self._checked_jacobian()
+        if self.inversion_policy == "warn":
+            J = np.clip(J, 1e-9, None)
+        return self.stress() / J[:, None, None]
+
+    def _cov_tensor(self):
+        if self._t.get("cov") is None:
+            raise ValueError("no covariance was loaded (load_particles(cov=...))")
+        if not self._update_cov:
+            _abi.check(self._eng.lib.gbmpm_compute_cov(self._eng.h, self._t["cov"].data_ptr(), self._stream()),
+                       "gbmpm_compute_cov")
+        return self._t["cov"]
+
+    def cov(self) -> np.ndarray:
+        return self._cov_tensor().cpu().numpy().reshape(-1, 6)
+
+    def _R_tensor(self):
+        _abi.check(self._eng.lib.gbmpm_compute_R(self._eng.h, self._t["R"].data_ptr(), self._stream()),
+                   "gbmpm_compute_R")
+        return self._t["R"]
+
+    def R(self) -> np.ndarray:
+        """Polar rotation R of F (the kernel stores R^T; this returns R)."""
+        return np.transpose(self._R_tensor().cpu().numpy().reshape(-1, 3, 3), (0, 2, 1))
+
+    def x_torch(self):
+        return self._t["x"]
+
+    def v_torch(self):
+        return self._t["v"]
+
+    def F_torch(self):
+        return self._t["F"].reshape(-1, 3, 3)
+
+    def cov_torch(self):
+        return self._cov_tensor().reshape(-1, 6)
+
+    def R_torch(self):
+        return self._R_tensor().reshape(-1, 3, 3).transpose(1, 2)
+
+    @property
+    def n_particles(self) -> int:
+        return 0 if self._eng is None else self._n
+
+    @property
+    def time(self) -> float:
+        return self._time
+
+    def launch_count(self) -> int:
+        return 0 if self._eng is None else int(self._eng.lib.gbmpm_launch_count(self._eng.h))
+
+    # ------------------------------------------------------------ test access
+    def export_state(self) -> dict:
+        """Host copies of the engine inputs (particles, model, colliders, clock) used to
+        replay the same scene elsewhere."""
+        self._pull_colliders()
+        out = {k: (None if v is None else v.detach().cpu().numpy().copy())
+               for k, v in self._t.items() if k in ("x", "v", "C", "F", "F_trial", "L", "stress", "mass", "vol",
+                                                    "density", "Jp", "mu", "lam", "yield_stress", "material",
+                                                    "selection", "cov", "init_cov")}
+        model = _abi.Model()
+        C.memmove(C.byref(model), C.byref(self._model), C.sizeof(_abi.Model))
+        out["model"] = model
+        out["eta_table"] = self._t["eta_table"].cpu().numpy().copy()
+        cols = []
+        for rec in self._cols:
+            r = _abi.Collider()
+            C.memmove(C.byref(r), C.byref(rec), C.sizeof(_abi.Collider))
+            cols.append(r)
+        out["colliders"] = cols
+        out["sdf_host"] = {t.data_ptr(): t.cpu().numpy().copy() for t in self._keep}
+        out["time"] = self._time
+        return out

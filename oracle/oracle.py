@@ -1,0 +1,341 @@
+"""Python driver of the CPU oracle (mpm_oracle.cpp) - test infrastructure only.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, as the checker and as the timed CPU restatement. The product
+(mpm_engine_gb300) never imports it.
+
+`OracleSolver` mirrors the host side of warpmpm's Solver on numpy arrays (the
+parameter and collider conventions come from mpm_engine_gb300.host) and steps
+through gbmpm_oracle_tick. `OracleSolver.from_state` replays a scene exported
+from the GPU Solver, so both run the same inputs.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent
+if str(REPO) not in sys.path:
+    sys.path.insert(0, str(REPO))
+
+from mpm_engine_gb300 import _abi, host  # noqa: E402
+from mpm_engine_gb300.glass import quat_to_mat  # noqa: E402
+from mpm_engine_gb300.materials import material_id  # noqa: E402
+
+LIB = HERE / "_build" / "libmpm_oracle.so"
+SRC = HERE / "mpm_oracle.cpp"
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """g++ recipe: fp contraction off so every product and sum rounds as written."""
+    LIB.parent.mkdir(parents=True, exist_ok=True)
+    deps = [SRC, REPO / "include" / "gbmpm.h"]
+    if LIB.exists() and not force and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return LIB
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           "-I", str(REPO / "include"), "-o", str(LIB), str(SRC)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + res.stdout + res.stderr)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB.exists():
+        build()
+    lib = C.CDLL(str(LIB))
+    P = C.POINTER
+    lib.gbmpm_oracle_tick.restype = C.c_int
+    lib.gbmpm_oracle_tick.argtypes = [P(_abi.Particles), P(_abi.Model), P(_abi.Collider), C.c_int32, C.c_void_p,
+                                      P(C.c_double), C.c_double, C.c_int32, C.c_int32, C.c_int32]
+    lib.gbmpm_oracle_svd3.argtypes = [C.c_void_p] * 4
+    lib.gbmpm_oracle_glass_sdf.restype = C.c_float
+    lib.gbmpm_oracle_glass_sdf.argtypes = [P(_abi.Collider), C.c_void_p]
+    lib.gbmpm_oracle_integrate_pose.argtypes = [P(_abi.Collider), C.c_double, C.c_double]
+    lib.gbmpm_oracle_sort_perm.restype = C.c_int32
+    lib.gbmpm_oracle_sort_perm.argtypes = [C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.c_void_p]
+    lib.gbmpm_oracle_blocks.argtypes = [C.c_void_p, C.c_int32, C.c_float, C.c_int32, C.c_void_p, C.c_void_p,
+                                        C.c_void_p]
+    lib.gbmpm_oracle_R.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
+    lib.gbmpm_oracle_cov.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
+    lib.gbmpm_oracle_last_error.restype = C.c_char_p
+    lib.gbmpm_oracle_abi_layout.argtypes = [C.c_void_p]
+    _lib = lib
+    return lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def abi_layout() -> list[int]:
+    out = np.zeros(10, np.int64)
+    load().gbmpm_oracle_abi_layout(_p(out))
+    return [int(v) for v in out]
+
+
+def svd3(F: np.ndarray):
+    lib = load()
+    F = np.ascontiguousarray(F, dtype=np.float32).reshape(3, 3)
+    U = np.zeros((3, 3), np.float32)
+    V = np.zeros((3, 3), np.float32)
+    s = np.zeros(3, np.float32)
+    lib.gbmpm_oracle_svd3(_p(F), _p(U), _p(s), _p(V))
+    return U, s, V
+
+
+def sort_perm(x: np.ndarray, dx: float, n_grid: int):
+    lib = load()
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    keys = np.zeros(len(x), np.int64)
+    perm = np.arange(len(x), dtype=np.int32)
+    moved = lib.gbmpm_oracle_sort_perm(_p(x), len(x), float(dx), int(n_grid), _p(keys), _p(perm))
+    return bool(moved), perm, keys
+
+
+def blocks(x: np.ndarray, inv_dx: float, n_grid: int, prev: np.ndarray | None = None):
+    lib = load()
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    bd = (n_grid + 3) // 4
+    cur = np.zeros(bd ** 3, np.int32)
+    counts = np.zeros(2, np.int32)
+    lib.gbmpm_oracle_blocks(_p(x), len(x), float(inv_dx), int(n_grid),
+                            None if prev is None else _p(np.ascontiguousarray(prev, np.int32)), _p(cur), _p(counts))
+    return cur, counts
+
+
+_KEYS = ("x", "v", "C", "F", "F_trial", "L", "stress", "mass", "vol", "density", "Jp", "mu", "lam", "yield_stress",
+         "material", "selection", "cov", "init_cov")
+
+
+class OracleSolver:
+    """numpy twin of mpm_engine_gb300.Solver's host side, stepping the C++ oracle."""
+
+    def __init__(self, n_grid: int = 64, grid_lim: float = 0.4, fused: bool = True, threads: int = 1,
+                 periodic_x: bool = False, grid=None, **_ignored):
+        if grid is not None:
+            n_grid, grid_lim = grid.n_grid, grid.grid_lim
+        self.n_grid, self.grid_lim = int(n_grid), float(grid_lim)
+        self.dx = self.grid_lim / self.n_grid
+        self.fused = fused
+        self.threads = threads
+        self.a: dict = {}
+        self.model = host.default_model(self.n_grid, self.grid_lim)
+        self.model.periodic_x = 1 if periodic_x else 0
+        self.eta_table = np.zeros(2, np.float32)
+        self.model.eta_table = _p(self.eta_table)
+        self.cols: list = []
+        self.handles: list = []
+        self.sdf_arrays: list = []
+        self.time = 0.0
+        self.mat_current = 0
+        self.wrench = np.zeros((0, 6), np.float32)
+
+    # ----------------------------------------------------------------- setup
+    def load_particles(self, pos, vol, cov=None, cov_mode="step"):
+        n = len(pos)
+        eye = np.tile(np.eye(3, dtype=np.float32), (n, 1, 1))
+        z = lambda *s: np.zeros(s, np.float32)  # noqa: E731
+        self.a = {"x": np.ascontiguousarray(pos, np.float32).reshape(n, 3).copy(), "v": z(n, 3), "C": z(n, 3, 3),
+                  "F": eye.copy(), "F_trial": eye.copy(), "L": z(n, 3, 3), "stress": z(n, 3, 3),
+                  "mass": z(n), "vol": np.asarray(vol, np.float32).copy(), "density": z(n), "Jp": z(n),
+                  "mu": z(n), "lam": z(n), "yield_stress": z(n), "material": np.zeros(n, np.int32),
+                  "selection": np.zeros(n, np.int32), "cov": None, "init_cov": None}
+        if cov is not None:
+            c6 = np.ascontiguousarray(cov, np.float32).reshape(n, 6)
+            self.a["init_cov"] = c6.copy()
+            self.a["cov"] = c6.copy() if cov_mode == "step" else np.zeros_like(c6)
+            self.model.update_cov_with_F = 1 if cov_mode == "step" else 0
+        return self
+
+    def _apply(self, kw, lo=None, hi=None):
+        a, m = self.a, self.model
+        ranged = lo is not None
+        sl = slice(lo, hi) if ranged else slice(None)
+        if "material" in kw:
+            mid = material_id(kw["material"])
+            a["material"][sl] = mid
+            if ranged:
+                m.material_mask |= 1 << mid
+            else:
+                self.mat_current = mid
+                m.material_mask = 1 << mid
+            mat = mid
+        else:
+            mat = self.mat_current
+        host.apply_type_params(m, mat, kw)
+        if "yield_stress" in kw:
+            a["yield_stress"][sl] = np.float32(kw["yield_stress"])
+        if "eta_table" in kw:
+            self.eta_table = np.asarray(kw["eta_table"], np.float32).reshape(-1).copy()
+            m.eta_table = _p(self.eta_table)
+            m.eta_table_n = len(self.eta_table)
+        if "eta_table_smin" in kw:
+            m.eta_table_smin = host.f32(kw["eta_table_smin"])
+        if "eta_table_smax" in kw:
+            m.eta_table_smax = host.f32(kw["eta_table_smax"])
+        if "g" in kw and not ranged:
+            m.gravity[:] = tuple(host.f32(g) for g in kw["g"])
+        if "density" in kw:
+            a["density"][sl] = np.float32(kw["density"])
+            a["mass"][sl] = a["density"][sl] * a["vol"][sl]
+        if "E" in kw or "nu" in kw:
+            if ranged:
+                E, nu = float(m.E[mat]), float(m.nu[mat])
+                a["mu"][sl] = E / (2.0 * (1.0 + nu))
+                a["lam"][sl] = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+            else:
+                self._mu_lam()
+        if "rpic_damping" in kw:
+            m.rpic_damping = host.f32(kw["rpic_damping"])
+        if "grid_v_damping_scale" in kw:
+            m.grid_v_damping_scale = host.f32(kw["grid_v_damping_scale"])
+
+    def _mu_lam(self):
+        idx = self.a["material"]
+        mu, lam = host.mu_lam_from_E_nu_f32(np.array(self.model.E[:], np.float32)[idx],
+                                            np.array(self.model.nu[:], np.float32)[idx])
+        self.a["mu"][:] = mu
+        self.a["lam"][:] = lam
+
+    def set_material(self, material, **overrides):
+        name, params = material.resolve() if hasattr(material, "resolve") else (str(material), {})
+        self._apply({"material": name, "g": [0.0, 0.0, -9.81], **params, **overrides})
+        self._mu_lam()
+        return self
+
+    def set_material_range(self, start, end, material, **overrides):
+        name, params = material.resolve() if hasattr(material, "resolve") else (str(material), {})
+        self._apply({"material": name, **params, **overrides}, lo=int(start), hi=int(end))
+        return self
+
+    def _add(self, rec, slots=1):
+        self.cols.append(rec)
+        first = len(self.handles)
+        self.handles.append(len(self.cols) - 1)
+        self.handles.extend([None] * (slots - 1))
+        self.wrench = np.zeros((len(self.cols), 6), np.float32)
+        return first
+
+    def add_plane(self, point, normal, surface="sticky", friction=0.0, restitution=0.0):
+        self._add(host.plane_collider(point, normal, surface, friction))
+        return self
+
+    def add_box(self, center, half_size, velocity=(0.0, 0.0, 0.0), start_time=0.0, end_time=1.0e9):
+        return self._add(host.box_collider(center, half_size, velocity, start_time, end_time))
+
+    def add_cup(self, profile, center, quat=(1.0, 0.0, 0.0, 0.0), velocity=(0.0, 0.0, 0.0), omega=(0.0, 0.0, 0.0),
+                friction=0.05, sticky_cells=1.5, contact_cells=0.5, start_time=0.0, end_time=1.0e9):
+        sticky = min(sticky_cells * self.dx, 0.45 * profile.wall_thickness)
+        return self._add(host.cup_collider(center, quat_to_mat(quat), velocity, omega, profile.outer_radius,
+                                           profile.inner_radius, profile.half_height, profile.inner_floor_z,
+                                           profile.fillet_radius, friction, sticky, contact_cells * self.dx,
+                                           start_time, end_time))
+
+    def set_cup(self, handle, center=None, quat=None, velocity=None, omega=None):
+        c = self.cols[self.handles[handle]]
+        if center is not None:
+            host._vec(c.point, center)
+        if quat is not None:
+            host.set_rotation(c, quat_to_mat(quat))
+        if velocity is not None:
+            host._vec(c.velocity, velocity)
+        if omega is not None:
+            host._vec(c.omega, omega)
+        return self
+
+    def set_box(self, handle, center=None, velocity=None):
+        c = self.cols[self.handles[handle]]
+        if center is not None:
+            host._vec(c.point, center)
+        if velocity is not None:
+            host._vec(c.velocity, velocity)
+        return self
+
+    def add_domain_walls(self, start_time=0.0, end_time=1.0e9):
+        self._add(host.walls_collider(start_time, end_time), slots=6)
+        return self
+
+    def add_sdf_collider(self, sdf, center, quat=(0.0, 0.0, 0.0, 1.0), velocity=(0.0, 0.0, 0.0),
+                         omega=(0.0, 0.0, 0.0), band=None, surface="separable", friction=0.4, start_time=0.0,
+                         end_time=1.0e9):
+        val = np.ascontiguousarray(sdf.values, np.float32)
+        grad = np.ascontiguousarray(sdf.grads, np.float32)
+        self.sdf_arrays += [val, grad]
+        band = float(self.model.dx) if band is None else band
+        return self._add(host.sdf_collider(_p(val), _p(grad), val.shape[0], sdf.origin, sdf.cell, center, quat,
+                                           velocity, omega, band, host.SDF_SURFACES[surface], friction,
+                                           start_time, end_time))
+
+    def wrench_of(self, handle, dt):
+        w = self.wrench[self.handles[handle]].astype(float)
+        return {"force": w[:3] / dt, "torque": w[3:] / dt}
+
+    def reset_wrench(self, handle):
+        self.wrench[self.handles[handle]] = 0.0
+
+    # ------------------------------------------------------------ from GPU
+    @classmethod
+    def from_state(cls, st: dict, n_grid: int, grid_lim: float, fused: bool = True, threads: int = 1):
+        o = cls(n_grid, grid_lim, fused=fused, threads=threads)
+        o.a = {k: (None if st.get(k) is None else np.ascontiguousarray(st[k]).copy()) for k in _KEYS}
+        C.memmove(C.byref(o.model), C.byref(st["model"]), C.sizeof(_abi.Model))
+        o.eta_table = np.ascontiguousarray(st["eta_table"], np.float32).copy()
+        o.model.eta_table = _p(o.eta_table)
+        for rec in st["colliders"]:
+            r = _abi.Collider()
+            C.memmove(C.byref(r), C.byref(rec), C.sizeof(_abi.Collider))
+            if r.kind == _abi.COLLIDER_SDF:
+                val = np.ascontiguousarray(st["sdf_host"][rec.sdf_val], np.float32)
+                grad = np.ascontiguousarray(st["sdf_host"][rec.sdf_grad], np.float32)
+                o.sdf_arrays += [val, grad]
+                r.sdf_val, r.sdf_grad = _p(val), _p(grad)
+            o.cols.append(r)
+            o.handles.append(len(o.cols) - 1)
+        o.wrench = np.zeros((len(o.cols), 6), np.float32)
+        o.time = float(st["time"])
+        return o
+
+    # ------------------------------------------------------------------ step
+    def _particles(self):
+        p = _abi.Particles()
+        p.n = len(self.a["x"])
+        for k in _KEYS:
+            setattr(p, k, _p(self.a[k]))
+        return p
+
+    def step(self, dt, substeps=1):
+        lib = load()
+        p = self._particles()
+        arr = (_abi.Collider * max(1, len(self.cols)))(*self.cols)
+        t = C.c_double(self.time)
+        rc = lib.gbmpm_oracle_tick(C.byref(p), C.byref(self.model), arr, len(self.cols), _p(self.wrench),
+                                   C.byref(t), float(dt), int(substeps), 1 if self.fused else 0, int(self.threads))
+        if rc != 0:
+            raise RuntimeError(f"oracle tick failed ({rc}): {lib.gbmpm_oracle_last_error().decode()}")
+        self.cols = [arr[i] for i in range(len(self.cols))]
+        self.time = t.value
+        return self
+
+    def x(self):
+        return self.a["x"]
+
+    def v(self):
+        return self.a["v"]
+
+    def F(self):
+        return self.a["F"]
+
+    @property
+    def n_particles(self):
+        return len(self.a["x"])

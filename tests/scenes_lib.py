@@ -1,0 +1,125 @@
+"""Small scenes shared by the oracle physics gates and the GPU parity tests.
+
+Each builder takes a solver class with the warpmpm.Solver surface
+(mpm_engine_gb300.Solver or oracle.oracle.OracleSolver) and returns the loaded
+scene plus whatever the test reads back.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from mpm_engine_gb300 import GlassProfile, GridConfig, cup_fill, newtonian
+from mpm_engine_gb300.materials import elastic, granular, tabulated_viscous, vonmises
+from mpm_engine_gb300.scenes import block, dough
+
+SMALL_CUP = GlassProfile(outer_radius=0.05, inner_radius=0.04, height=0.12, base_thickness=0.02,
+                         fillet_radius=0.006)
+
+
+def make(cls, n_grid, grid_lim, **kw):
+    """Instantiate either solver flavour with the same grid."""
+    if cls.__name__ == "OracleSolver":
+        return cls(n_grid=n_grid, grid_lim=grid_lim, fused=kw.get("fused", True),
+                   periodic_x=kw.get("periodic_x", False))
+    return cls(grid=GridConfig(n_grid=n_grid, grid_lim=grid_lim), **kw)
+
+
+def blob(n=2000, seed=0, lo=0.15, size=0.10):
+    rng = np.random.default_rng(seed)
+    pts = (rng.random((n, 3), dtype=np.float32) * size + lo).astype(np.float32)
+    return pts, np.full(n, 1.0e-7, np.float32)
+
+
+MATERIALS = {
+    "newtonian": lambda: newtonian(eta=2.0, density=1000.0, bulk_modulus=2.0e5),
+    "herschel_bulkley": lambda: newtonian(eta=0.0, density=1400.0, bulk_modulus=2.0e5).with_yield(50.0)
+    .with_powerlaw(K=20.0, n=0.6),
+    "bingham": lambda: dough(),
+    "jelly": lambda: elastic(E=5.0e4, nu=0.3, density=800.0),
+    "metal": lambda: vonmises(E=1.0e5, nu=0.3, yield_stress=2.0e3, density=1200.0),
+    "metal_hardening": lambda: vonmises(E=1.0e5, nu=0.3, yield_stress=5.0e2, hardening_xi=0.5, density=1200.0),
+    "mu_i": lambda: granular(mu_s=0.38, delta_mu=0.26, I0=0.28, density=2500.0, E=1e5, nu=0.3),
+    "mu_i_phi": lambda: granular(mu_s=0.38, delta_mu=0.26, I0=0.28, density=2500.0, E=1e5, nu=0.3)
+    .with_dilatancy(phi_init=0.6, chi=0.2),
+    "tabulated": lambda: tabulated_viscous([8.0, 4.0, 2.0, 1.0, 0.5], smin=-1.0, smax=2.0, bulk_modulus=2.0e5),
+    "sand": "sand",
+    "water": "fluid",
+    "plasticine": "plasticine",
+}
+
+# extra per-type parameters for the fork names used as plain strings
+NAME_PARAMS = {
+    "sand": dict(E=1.0e5, nu=0.3, density=1600.0, friction_angle=30.0),
+    "fluid": dict(density=1000.0, bulk_modulus=2.0e5),
+    "plasticine": dict(E=1.0e5, nu=0.3, density=1200.0, yield_stress=1.0e3, softening=0.1, hardening=0.0),
+}
+
+
+def blob_scene(cls, material_key, n_grid=48, grid_lim=0.4, fused=True, cup=False, box=False, n=2000, **kw):
+    """A falling blob on a separable floor with domain walls (the fused-pipeline test
+    scene, tests/test_fused_pipeline.py:27-56), optionally with a moving cup or a
+    descending plate."""
+    pts, vol = blob(n=n)
+    s = make(cls, n_grid, grid_lim, fused=fused, **kw).load_particles(pts, vol)
+    mat = MATERIALS[material_key]
+    if isinstance(mat, str):
+        s.set_material(mat, **NAME_PARAMS[mat])
+    else:
+        s.set_material(mat())
+    dx = grid_lim / n_grid
+    s.add_plane((0, 0, 3 * dx), (0, 0, 1), "separate", friction=0.3)
+    s.add_domain_walls()
+    h = None
+    if cup:
+        h = s.add_cup(SMALL_CUP, np.array([0.2, 0.2, 3 * dx + 0.001]))
+        s.set_cup(h, center=np.array([0.2, 0.2, 3 * dx + 0.001]), quat=(1.0, 0.0, 0.0, 0.0),
+                  velocity=(0.02, 0.0, 0.0), omega=(0.0, 0.0, 0.3))
+    if box:
+        h = s.add_box((0.2, 0.2, 0.27), (0.08, 0.08, 0.01), velocity=(0.0, 0.0, -0.5))
+    return s, h
+
+
+def water_in_cup(cls, n_grid=40, grid_lim=0.35, fill=0.5):
+    """A cup of water on the floor (tests/test_pour.py:25-37)."""
+    dx = grid_lim / n_grid
+    h = dx / 2
+    pos_local, vol = cup_fill(GlassProfile(), h, fill_fraction=fill)
+    cup_pos = np.array([0.5 * grid_lim, 0.5 * grid_lim, 0.16])
+    s = make(cls, n_grid, grid_lim).load_particles((pos_local + cup_pos).astype(np.float32), vol)
+    s.set_material(newtonian(eta=1.0e-3, density=1000.0, bulk_modulus=9.0e5))
+    s.add_plane((0, 0, 3 * dx), (0, 0, 1), "separate", friction=0.3)
+    s.add_domain_walls()
+    return s, cup_pos, vol, h
+
+
+def dam_break(cls, n_grid=32, grid_lim=1.0, hi=(0.4, 0.6, 0.95)):
+    """Dam-break fill at 8 particles per cell with six sticky planes 3 dx inside the
+    faces plus domain walls, Newtonian water (eta 1e-2, rho 1000, K 1e4)."""
+    from mpm_engine_gb300.scenes import dam_break_lattice
+    pos, vol = dam_break_lattice(n_grid, grid_lim, hi=hi)
+    s = make(cls, n_grid, grid_lim).load_particles(pos, vol)
+    s.set_material(newtonian(eta=1.0e-2, density=1000.0, bulk_modulus=1.0e4), g=[0.0, 0.0, -9.8])
+    add_sticky_box(s, n_grid, grid_lim)
+    s.add_domain_walls()
+    return s
+
+
+def add_sticky_box(s, n_grid, grid_lim):
+    dx = grid_lim / n_grid
+    lo, hi = 3 * dx, grid_lim - 3 * dx
+    for axis in range(3):
+        p = [0.0, 0.0, 0.0]
+        nrm = [0.0, 0.0, 0.0]
+        p[axis], nrm[axis] = lo, 1.0
+        s.add_plane(tuple(p), tuple(nrm), "sticky")
+        p[axis], nrm[axis] = hi, -1.0
+        s.add_plane(tuple(p), tuple(nrm), "sticky")
+
+
+def free_blob(cls, n_grid=40):
+    grid = GridConfig(n_grid=n_grid, grid_lim=0.4)
+    pos, vol, _ = block(grid, size=(0.08, 0.05, 0.05), ppc=2)
+    pos[:, 2] += grid.grid_lim * 0.5 - pos[:, 2].mean()
+    s = make(cls, n_grid, 0.4).load_particles(pos, vol)
+    s.set_material(dough())
+    return s

@@ -1,0 +1,97 @@
+"""Drop-in behaviour of Solver on the GPU: guards, imports, exports, handles and
+the error conventions of warpmpm.Solver (core/solver.py)."""
+import numpy as np
+import pytest
+
+from scenes_lib import blob_scene, free_blob
+
+pytestmark = pytest.mark.gpu
+
+
+def test_edge_guard_raises_runtime_error(cuda):
+    """tests/test_restricted_launch.py:68-79: particles near the edge are rejected."""
+    from mpm_engine_gb300 import GridConfig, Solver
+    pos = np.array([[0.005, 0.2, 0.2], [0.2, 0.2, 0.2]], np.float32)
+    s = Solver(grid=GridConfig(40, 0.4)).load_particles(pos, np.full(2, 1e-7, np.float32))
+    s.set_material("jelly", E=1e4, nu=0.3, density=1000.0)
+    with pytest.raises(RuntimeError, match="out of bounds"):
+        s.step(1e-4, 1)
+
+
+def test_set_x_copies_in_place_and_pointers_are_stable(cuda):
+    """tests/test_state_import.py:13-33."""
+    from mpm_engine_gb300 import Solver
+    s, _ = blob_scene(Solver, "newtonian")
+    ptr = s._sim.mpm_state.particle_x.ptr
+    x = s.x() + 0.001
+    s.set_x(x)
+    assert s._sim.mpm_state.particle_x.ptr == ptr
+    np.testing.assert_array_equal(s.x(), x.astype(np.float32))
+    v = np.full_like(x, 0.1)
+    s.set_v(v)
+    np.testing.assert_array_equal(s.v(), v)
+
+
+def test_torch_exports_alias_device_memory(cuda):
+    from mpm_engine_gb300 import Solver
+    s, _ = blob_scene(Solver, "jelly")
+    s.step(2e-4, 3)
+    assert s.x_torch().data_ptr() == s._t["x"].data_ptr()
+    assert s.F_torch().shape == (s.n_particles, 3, 3)
+    assert s.x_torch().is_cuda
+
+
+def test_inversion_policies(cuda):
+    """tests/test_engine.py:76-98."""
+    import torch
+    from mpm_engine_gb300 import Solver
+    s = free_blob(Solver, 24)
+    F = s.F()
+    F[0, 0, 0] = -1.0
+    s._sim.import_particle_F_from_torch(torch.from_numpy(F))
+    with pytest.warns(RuntimeWarning, match=r"using \|det\(F\)\|"):
+        assert np.isfinite(s.vol()).all()
+    s.inversion_policy = "raise"
+    with pytest.raises(RuntimeError, match=r"det\(F\)"):
+        s.vol()
+    s.inversion_policy = "nan"
+    assert np.isnan(s.vol()[0]) and np.isfinite(s.vol()[1:]).all()
+
+
+def test_handles_follow_reference_numbering(cuda):
+    from mpm_engine_gb300 import GlassProfile, Solver
+    s, _ = blob_scene(Solver, "newtonian")     # plane (0) + domain walls (1..6)
+    h = s.add_cup(GlassProfile(), (0.2, 0.2, 0.2))
+    assert h == 7
+    b = s.add_box((0.2, 0.2, 0.3), (0.05, 0.05, 0.01))
+    assert b == 8
+    with pytest.raises(IndexError):
+        s.cup_wrench(3, 1.0)
+
+
+def test_profile_report_lists_phases(cuda):
+    from mpm_engine_gb300 import Solver
+    s, _ = blob_scene(Solver, "newtonian", profile=True)
+    s.step(2e-4, 4)
+    rep = s.profile_report()
+    assert "g2p2g_fused" in rep and "grid_update" in rep
+
+
+def test_material_range_and_mu_lam(cuda):
+    from mpm_engine_gb300 import Solver, elastic, vonmises
+    s, _ = blob_scene(Solver, "jelly")
+    s.set_material_range(0, 100, vonmises(E=2e5, nu=0.25, yield_stress=1e3))
+    mat = s._t["material"].cpu().numpy()
+    assert (mat[:100] == 1).all() and (mat[100:] == 0).all()
+    mu = s._sim.mpm_model.mu.numpy()
+    np.testing.assert_allclose(mu[:100], 2e5 / (2 * 1.25), rtol=1e-6)
+    np.testing.assert_allclose(mu[100:], 5e4 / 2.6, rtol=1e-6)
+    with pytest.raises(NotImplementedError):
+        s.set_material_range(0, 10, __import__("mpm_engine_gb300").tabulated_viscous([1.0, 2.0]))
+
+
+def test_cdf_collider_is_reported_missing(cuda):
+    from mpm_engine_gb300 import Solver
+    s, _ = blob_scene(Solver, "newtonian")
+    with pytest.raises(NotImplementedError):
+        s.add_cdf_collider(None, (0, 0, 0))

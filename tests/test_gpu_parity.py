@@ -1,0 +1,196 @@
+"""CUDA engine (through the C ABI) against the CPU oracle on identical inputs.
+
+Tolerances (the engine's parity contract): x, v, C and F within 1e-5 relative per
+substep and 1e-3 after 1000 substeps; collider wrenches within 1e-4 relative;
+particle mass unchanged. "Relative" is max|gpu - oracle| / (max|oracle| + floor)
+per field, with the floors below standing for the field's natural scale. The two
+sides differ only in fp32 rounding order (float atomics, FMA contraction).
+"""
+import numpy as np
+import pytest
+
+from scenes_lib import MATERIALS, blob_scene, dam_break, free_blob
+
+pytestmark = pytest.mark.gpu
+
+FLOOR = {"x": 1e-6, "v": 1e-6, "C": 1e-4, "F": 1e-6}
+
+
+def rel_err(a, b, floor):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.abs(a - b).max() / (np.abs(b).max() + floor))
+
+
+def fields_gpu(s):
+    return {"x": s.x(), "v": s.v(), "C": s.C(), "F": s.F()}
+
+
+def fields_oracle(o):
+    return {"x": o.a["x"], "v": o.a["v"], "C": o.a["C"], "F": o.a["F"]}
+
+
+def assert_close(s, o, tol, what=""):
+    g, r = fields_gpu(s), fields_oracle(o)
+    errs = {k: rel_err(g[k], r[k], FLOOR[k]) for k in g}
+    bad = {k: e for k, e in errs.items() if not e <= tol}
+    assert not bad, f"{what}: relative errors {errs} exceed {tol}"
+    return errs
+
+
+def pair(cuda, oracle_lib, builder, *args, fused=True, **kw):
+    from mpm_engine_gb300 import Solver
+    s, h = builder(Solver, *args, fused=fused, **kw)
+    o = oracle_lib.OracleSolver.from_state(s.export_state(), s.grid.n_grid, s.grid.grid_lim, fused=fused)
+    return s, o, h
+
+
+@pytest.mark.parametrize("key", sorted(MATERIALS))
+def test_per_substep_parity_all_materials(cuda, oracle_lib, key):
+    s, o, _ = pair(cuda, oracle_lib, blob_scene, key)
+    dt = 2.0e-4
+    for i in range(4):
+        s.step(dt, 1)
+        o.step(dt, 1)
+        assert_close(s, o, 1e-5, f"{key} substep {i}")
+    s.step(dt, 8)
+    o.step(dt, 8)
+    assert_close(s, o, 1e-5, f"{key} after a fused 8-substep tick")
+    np.testing.assert_array_equal(s._t["mass"].cpu().numpy(), o.a["mass"])
+
+
+def test_parity_split_pipeline(cuda, oracle_lib):
+    s, o, _ = pair(cuda, oracle_lib, blob_scene, "metal", fused=False)
+    for _ in range(3):
+        s.step(2.0e-4, 4)
+        o.step(2.0e-4, 4)
+        assert_close(s, o, 1e-5, "split")
+
+
+def test_cup_wrench_parity(cuda, oracle_lib):
+    s, o, h = pair(cuda, oracle_lib, blob_scene, "newtonian", cup=True)
+    dt, n = 2.0e-4, 6
+    for _ in range(5):
+        s.reset_cup_wrench(h)
+        o.reset_wrench(h)
+        s.step(dt, n)
+        o.step(dt, n)
+        assert_close(s, o, 1e-5, "cup scene")
+        wg, wo = s.cup_wrench(h, dt * n), o.wrench_of(h, dt * n)
+        for k in ("force", "torque"):
+            assert rel_err(wg[k], wo[k], 1e-9) < 1e-4, (k, wg[k], wo[k])
+
+
+def test_box_tool_force_parity(cuda, oracle_lib):
+    s, o, h = pair(cuda, oracle_lib, blob_scene, "jelly", box=True)
+    dt, n = 2.0e-4, 5
+    for _ in range(6):
+        s.reset_tool_force(h)
+        o.reset_wrench(h)
+        s.step(dt, n)
+        o.step(dt, n)
+        fg, fo = s.tool_force(h, dt * n), o.wrench_of(h, dt * n)["force"]
+        assert rel_err(fg, fo, 1e-9) < 1e-4, (fg, fo)
+    assert_close(s, o, 1e-5, "box scene")
+
+
+def test_long_horizon_1000_substeps(cuda, oracle_lib):
+    from mpm_engine_gb300 import Solver
+    s, o = None, None
+    s, _ = blob_scene(Solver, "herschel_bulkley")
+    o = oracle_lib.OracleSolver.from_state(s.export_state(), s.grid.n_grid, s.grid.grid_lim)
+    for _ in range(10):
+        s.step(1.0e-4, 100)
+        o.step(1.0e-4, 100)
+    errs = assert_close(s, o, 1e-3, "1000 substeps")
+    print("1000-substep relative errors", errs)
+
+
+def test_dam_break_momentum_and_mass(cuda, oracle_lib):
+    from mpm_engine_gb300 import Solver
+    s = dam_break(Solver, n_grid=32)
+    o = oracle_lib.OracleSolver.from_state(s.export_state(), 32, 1.0)
+    m = s._t["mass"].cpu().numpy().astype(np.float64)
+    for _ in range(5):
+        s.step(1.0e-4, 20)
+        o.step(1.0e-4, 20)
+    assert_close(s, o, 1e-4, "dam break 100 substeps")
+    pg = (m[:, None] * s.v()).sum(0)
+    po = (m[:, None] * o.a["v"].astype(np.float64)).sum(0)
+    assert np.abs(pg - po).max() <= 1e-5 * np.abs(po).max() + 1e-12
+    np.testing.assert_array_equal(s._t["mass"].cpu().numpy(), o.a["mass"])
+
+
+def test_graph_replay_equals_live_launches(cuda):
+    from mpm_engine_gb300 import Solver
+    outs = []
+    for graph in (True, False):
+        s, _ = blob_scene(Solver, "newtonian")
+        s._sim.use_cuda_graph = graph
+        for _ in range(3):
+            s.step(2.0e-4, 8)
+        outs.append(s.x())
+    np.testing.assert_allclose(outs[0], outs[1], rtol=1e-5, atol=1e-7)
+
+
+def test_free_fall_gates_on_gpu(cuda):
+    """tests/test_engine.py:51-73 on the engine."""
+    from mpm_engine_gb300 import Solver
+    s = free_blob(Solver)
+    dt, n = 2.0e-5, 100
+    s.step(dt, n)
+    expect = -9.81 * dt * n
+    assert abs(float(s.v()[:, 2].mean()) - expect) < 0.05 * abs(expect)
+    s.step(dt, 105)
+    assert abs(float(np.abs(np.linalg.det(s.F())).mean()) - 1.0) < 5e-3
+
+
+def test_sort_bit_exact_against_oracle(cuda, oracle_lib):
+    from mpm_engine_gb300 import Solver
+    s, _ = blob_scene(Solver, "newtonian", n=5000)
+    s.step(2.0e-4, 10)
+    x0 = s.x().copy()
+    vol0 = s._vol0.copy()
+    fields = {k: s._t[k].cpu().numpy().copy() for k in ("v", "F", "C", "mass", "material")}
+    moved_ref, perm_ref, _ = oracle_lib.sort_perm(x0, s.grid.dx, s.grid.n_grid)
+    assert moved_ref
+    assert s._sort_particles()
+    perm = s._t["perm"].cpu().numpy()[: s.n_particles]
+    np.testing.assert_array_equal(perm, perm_ref)
+    np.testing.assert_array_equal(s.x(), x0[perm_ref])
+    np.testing.assert_array_equal(s._vol0, vol0[perm_ref])
+    for k, a in fields.items():
+        np.testing.assert_array_equal(s._t[k].cpu().numpy(), a[perm_ref])
+    assert not s._sort_particles()  # already ordered: skipped
+
+
+def test_active_block_counts_match_oracle(cuda, oracle_lib):
+    from mpm_engine_gb300 import Solver
+    s, _ = blob_scene(Solver, "newtonian", sparse=True)
+    prev = None
+    for _ in range(3):
+        s.step(2.0e-4, 5)
+        cur, counts = oracle_lib.blocks(s.x(), float(s._model.inv_dx), s.grid.n_grid, prev)
+        prev = cur
+    s._rebuild_active_blocks()
+    cur, counts = oracle_lib.blocks(s.x(), float(s._model.inv_dx), s.grid.n_grid, prev)
+    assert s._sim._block_counts == (int(counts[0]), int(counts[1]))
+
+
+def test_R_and_cov_exports_match_oracle(cuda, oracle_lib):
+    from mpm_engine_gb300 import Solver
+    from scenes_lib import MATERIALS, blob
+    pts, vol = blob(n=1500)
+    cov = np.tile(np.array([1e-6, 0, 0, 1e-6, 0, 1e-6], np.float32), (len(pts), 1))
+    s = Solver(grid=__import__("mpm_engine_gb300").GridConfig(48, 0.4)).load_particles(pts, vol, cov=cov,
+                                                                                     cov_mode="from_F")
+    s.set_material(MATERIALS["jelly"]())
+    s.add_plane((0, 0, 0.025), (0, 0, 1), "sticky")
+    s.step(2.0e-4, 20)
+    Ft = s._t["F_trial"].cpu().numpy().reshape(-1, 9)
+    R_ref = np.zeros_like(Ft)
+    oracle_lib.load().gbmpm_oracle_R(Ft.ctypes.data, len(Ft), R_ref.ctypes.data)
+    np.testing.assert_allclose(s.R(), np.transpose(R_ref.reshape(-1, 3, 3), (0, 2, 1)), atol=2e-5)
+    c_ref = np.zeros((len(Ft), 6), np.float32)
+    oracle_lib.load().gbmpm_oracle_cov(Ft.ctypes.data, cov.ctypes.data, len(Ft), c_ref.ctypes.data)
+    np.testing.assert_allclose(s.cov(), c_ref, rtol=1e-5, atol=1e-12)
