@@ -150,8 +150,10 @@ typedef struct {
 #define GBMPM_TICK_FUSED   1    /* fused G2P2G pipeline (Solver.fused) */
 #define GBMPM_TICK_GRAPH   2    /* replay the tick as one captured CUDA graph when possible */
 #define GBMPM_TICK_PROFILE 4    /* per-phase CUDA-event timing, live launches */
+#define GBMPM_TICK_REORDER 8    /* run the tick on a block-sorted working copy with shared-memory
+                                   grid tiles (results equal up to float summation order) */
 
-#define GBMPM_NUM_PHASES 6      /* stress, p2g, g2p2g_fused, grid_update, g2p, guard */
+#define GBMPM_NUM_PHASES 6      /* stress, p2g, g2p2g_fused, grid_update, g2p, sort+gather/scatter */
 
 typedef struct gbmpm_engine gbmpm_engine;
 

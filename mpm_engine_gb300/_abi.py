@@ -28,6 +28,7 @@ FLAG_LIST_OVERFLOW = 4
 TICK_FUSED = 1
 TICK_GRAPH = 2
 TICK_PROFILE = 4
+TICK_REORDER = 8
 
 COLLIDER_PLANE = 0
 COLLIDER_BOX = 1

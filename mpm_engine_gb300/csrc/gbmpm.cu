@@ -440,9 +440,171 @@ __device__ __forceinline__ void mark_block(const PK &k, int bx, int by, int bz) 
     }
 }
 
+// ---- building blocks shared by the direct and the tiled particle kernels ----
+
+// G2P for one particle (g2p_particle, mpm_utils.py:944-1043) with the grid
+// velocity supplied by `fetch(ix, iy, iz)` (global memory or a shared tile).
+template <class Fetch>
+__device__ __forceinline__ void g2p_core(const PK &k, const Stencil &s, Fetch fetch, float *v, float *C, float *L) {
+    float nv[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int i = 0; i < 9; ++i) { C[i] = 0.f; L[i] = 0.f; }
+    const float c4 = k.inv_dx * 4.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            float wij = s.w[0][i] * s.w[1][j];
+            float dwi_j = s.dw[0][i] * s.w[1][j];
+            float wi_dj = s.w[0][i] * s.dw[1][j];
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk) {
+                float4 g = fetch(i, j, kk);
+                float wt = wij * s.w[2][kk];
+                float dp0 = (float)i - s.fx[0], dp1 = (float)j - s.fx[1], dp2 = (float)kk - s.fx[2];
+                float gx = dwi_j * s.w[2][kk] * k.inv_dx;
+                float gy = wi_dj * s.w[2][kk] * k.inv_dx;
+                float gz = wij * s.dw[2][kk] * k.inv_dx;
+                float cw = wt * c4;
+                float gvv[3] = {g.x, g.y, g.z};
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    nv[a] += gvv[a] * wt;
+                    float ga = gvv[a] * cw;
+                    C[3 * a + 0] += ga * dp0;
+                    C[3 * a + 1] += ga * dp1;
+                    C[3 * a + 2] += ga * dp2;
+                    L[3 * a + 0] += gvv[a] * gx;
+                    L[3 * a + 1] += gvv[a] * gy;
+                    L[3 * a + 2] += gvv[a] * gz;
+                }
+            }
+        }
+    }
+    v[0] = nv[0]; v[1] = nv[1]; v[2] = nv[2];
+}
+
+// advection, F_trial and covariance after the gather
+__device__ __forceinline__ void g2p_finish(const PK &k, int p, float *x, const float *v, const float *L, float *Ft) {
+    float xn[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) xn[a] = x[a] + k.dt * v[a];
+    if (k.periodic_x) {
+        float lx = (float)k.ng * k.dx;
+        if (xn[0] < 0.0f) xn[0] += lx;
+        if (xn[0] >= lx) xn[0] -= lx;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) x[a] = xn[a];
+    float Fo[9], A[9];
+    mat_load(k.F + 9 * (size_t)p, Fo);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) A[i] = ((i % 4 == 0) ? 1.0f : 0.0f) + L[i] * k.dt;
+    mm(A, Fo, Ft);
+    if (k.update_cov && k.cov) {
+        float *c6 = k.cov + 6 * (size_t)p;
+        float cn[9] = {c6[0], c6[1], c6[2], c6[1], c6[3], c6[4], c6[2], c6[4], c6[5]};
+        float a1[9], a2[9];
+        mm(L, cn, a1);
+        mmT(cn, L, a2);
+        c6[0] = cn[0] + k.dt * (a1[0] + a2[0]);
+        c6[1] = cn[1] + k.dt * (a1[1] + a2[1]);
+        c6[2] = cn[2] + k.dt * (a1[2] + a2[2]);
+        c6[3] = cn[4] + k.dt * (a1[4] + a2[4]);
+        c6[4] = cn[5] + k.dt * (a1[5] + a2[5]);
+        c6[5] = cn[8] + k.dt * (a1[8] + a2[8]);
+    }
+}
+
+// P2G for one particle (p2g_particle, mpm_utils.py:819-916): every node
+// contribution {m v_i, m} goes through `deposit(i, j, kk, float4)`.
+template <class Deposit>
+__device__ __forceinline__ void p2g_core(const PK &k, const Stencil &s, int p, const float *v, const float *Cin,
+                                         const float *S, Deposit deposit) {
+    float C[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) C[i] = Cin[i];
+    if (k.rpic != 0.0f) {
+        float Cn[9];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                Cn[3 * i + j] = (1.0f - k.rpic) * C[3 * i + j] + k.rpic / 2.0f * (C[3 * i + j] - C[3 * j + i]);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) C[i] = (k.rpic < -0.001f) ? 0.0f : Cn[i];
+    }
+    const float m = k.mass[p];
+    const float fs = -k.vol[p] * k.dt * k.inv_dx;
+    float A[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) A[i] = fs * S[i];
+    float mCdx[9], base[3];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) mCdx[i] = m * C[i] * k.dx;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        base[a] = m * v[a] - (mCdx[3 * a] * s.fx[0] + mCdx[3 * a + 1] * s.fx[1] + mCdx[3 * a + 2] * s.fx[2]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            float wij = s.w[0][i] * s.w[1][j];
+            float dwi_j = s.dw[0][i] * s.w[1][j];
+            float wi_dj = s.w[0][i] * s.dw[1][j];
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk) {
+                float wt = wij * s.w[2][kk];
+                float gx = dwi_j * s.w[2][kk], gy = wi_dj * s.w[2][kk], gz = wij * s.dw[2][kk];
+                float mom[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    float aff = base[a] + mCdx[3 * a] * (float)i + mCdx[3 * a + 1] * (float)j + mCdx[3 * a + 2] * (float)kk;
+                    mom[a] = wt * aff + (A[3 * a] * gx + A[3 * a + 1] * gy + A[3 * a + 2] * gz);
+                }
+                deposit(i, j, kk, make_float4(mom[0], mom[1], mom[2], wt * m));
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void mark_stencil_blocks(const PK &k, const Stencil &s) {
+    int by0 = s.b[1] >> 2, by1 = (s.b[1] + 2) >> 2;
+    int bz0 = s.b[2] >> 2, bz1 = (s.b[2] + 2) >> 2;
+    if (k.periodic_x) {
+        for (int i = 0; i < 3; ++i) {
+            int bxi = wrap(s.b[0] + i, k.ng) >> 2;
+            for (int by = by0; by <= by1; ++by)
+                for (int bz = bz0; bz <= bz1; ++bz) mark_block(k, bxi, by, bz);
+        }
+    } else {
+        int bx0 = s.b[0] >> 2, bx1 = (s.b[0] + 2) >> 2;
+        for (int bx = bx0; bx <= bx1; ++bx)
+            for (int by = by0; by <= by1; ++by)
+                for (int bz = bz0; bz <= bz1; ++bz) mark_block(k, bx, by, bz);
+    }
+}
+
+__device__ __forceinline__ void global_deposit_all(const PK &k, const Stencil &s, int p, const float *v,
+                                                   const float *C, const float *S) {
+    p2g_core(k, s, p, v, C, S, [&](int i, int j, int kk, float4 val) {
+        int ix = s.b[0] + i;
+        if (k.periodic_x) ix = wrap(ix, k.ng);
+        atomicAdd(k.gmv + ((size_t)ix * k.ng + (s.b[1] + j)) * k.ng + (s.b[2] + kk), val);
+    });
+    mark_stencil_blocks(k, s);
+}
+
+__device__ __forceinline__ float4 global_fetch(const PK &k, const Stencil &s, int i, int j, int kk) {
+    int ix = s.b[0] + i;
+    if (k.periodic_x) ix = wrap(ix, k.ng);
+    return __ldg(k.gv + ((size_t)ix * k.ng + (s.b[1] + j)) * k.ng + (s.b[2] + kk));
+}
+
+// ---- direct kernel: one thread per particle, global gather and atomics ------
 // One kernel serves every particle pass of the schedule; `mode` selects the
-// stages (G2P, STRESS, P2G) so the fused interior pass is G2P|STRESS|P2G, the
-// tick prologue STRESS|P2G and the epilogue G2P.
+// stages (G2P, STRESS, P2G): the fused interior pass is G2P|STRESS|P2G, the tick
+// prologue STRESS|P2G and the epilogue G2P.
 template <bool SOLIDS>
 __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) {
     if ((mode & PASS_RESET_LISTS) && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -454,7 +616,7 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
     if (k.sel && k.sel[p] != 0) return;
     const int mat = k.mat[p];
     float x[3] = {k.x[3 * p], k.x[3 * p + 1], k.x[3 * p + 2]};
-    float v[3], C[9], L[9], Ft[9];
+    float v[3], C[9], L[9], Ft[9], S[9];
     bool gathered = false;
     if ((mode & PASS_G2P) && mat != 7 && mat != 8) {
         Stencil s;
@@ -463,76 +625,11 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
             set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
             return;
         }
-        float nv[3] = {0.f, 0.f, 0.f};
-        float nC[9], nL[9];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) { nC[i] = 0.f; nL[i] = 0.f; }
-        const float c4 = k.inv_dx * 4.0f;
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            int ix = s.b[0] + i;
-            if (k.periodic_x) ix = wrap(ix, k.ng);
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                float wij = s.w[0][i] * s.w[1][j];
-                float dwi_j = s.dw[0][i] * s.w[1][j];
-                float wi_dj = s.w[0][i] * s.dw[1][j];
-                const float4 *row = k.gv + ((size_t)ix * k.ng + (s.b[1] + j)) * k.ng + s.b[2];
-#pragma unroll
-                for (int kk = 0; kk < 3; ++kk) {
-                    float4 g = __ldg(row + kk);
-                    float wt = wij * s.w[2][kk];
-                    float dp0 = (float)i - s.fx[0], dp1 = (float)j - s.fx[1], dp2 = (float)kk - s.fx[2];
-                    float gx = dwi_j * s.w[2][kk] * k.inv_dx;
-                    float gy = wi_dj * s.w[2][kk] * k.inv_dx;
-                    float gz = wij * s.dw[2][kk] * k.inv_dx;
-                    float cw = wt * c4;
-                    float gvv[3] = {g.x, g.y, g.z};
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) {
-                        nv[a] += gvv[a] * wt;
-                        float ga = gvv[a] * cw;
-                        nC[3 * a + 0] += ga * dp0;
-                        nC[3 * a + 1] += ga * dp1;
-                        nC[3 * a + 2] += ga * dp2;
-                        nL[3 * a + 0] += gvv[a] * gx;
-                        nL[3 * a + 1] += gvv[a] * gy;
-                        nL[3 * a + 2] += gvv[a] * gz;
-                    }
-                }
-            }
-        }
-        float xn[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) { v[a] = nv[a]; xn[a] = x[a] + k.dt * nv[a]; }
-        if (k.periodic_x) {
-            float lx = (float)k.ng * k.dx;
-            if (xn[0] < 0.0f) xn[0] += lx;
-            if (xn[0] >= lx) xn[0] -= lx;
-        }
-#pragma unroll
-        for (int a = 0; a < 3; ++a) x[a] = xn[a];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) { C[i] = nC[i]; L[i] = nL[i]; }
-        float Fo[9], A[9];
-        mat_load(k.F + 9 * (size_t)p, Fo);
-#pragma unroll
-        for (int i = 0; i < 9; ++i) A[i] = ((i % 4 == 0) ? 1.0f : 0.0f) + L[i] * k.dt;
-        mm(A, Fo, Ft);
-        if (k.update_cov && k.cov) {
-            float *c6 = k.cov + 6 * (size_t)p;
-            float cn[9] = {c6[0], c6[1], c6[2], c6[1], c6[3], c6[4], c6[2], c6[4], c6[5]};
-            float a1[9], a2[9];
-            mm(L, cn, a1);
-            mmT(cn, L, a2);
-            c6[0] = cn[0] + k.dt * (a1[0] + a2[0]);
-            c6[1] = cn[1] + k.dt * (a1[1] + a2[1]);
-            c6[2] = cn[2] + k.dt * (a1[2] + a2[2]);
-            c6[3] = cn[4] + k.dt * (a1[4] + a2[4]);
-            c6[4] = cn[5] + k.dt * (a1[5] + a2[5]);
-            c6[5] = cn[8] + k.dt * (a1[8] + a2[8]);
-        }
+        g2p_core(k, s, [&](int i, int j, int kk) { return global_fetch(k, s, i, j, kk); }, v, C, L);
+        g2p_finish(k, p, x, v, L, Ft);
         gathered = true;
+    }
+    if (gathered) {
         float *xo = k.x + 3 * (size_t)p;
         xo[0] = x[0]; xo[1] = x[1]; xo[2] = x[2];
         if (!(mode & (PASS_STRESS | PASS_P2G)) || (mode & PASS_STORE_VC)) {
@@ -545,7 +642,6 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
             mat_store(k.Ft + 9 * (size_t)p, Ft);
         }
     }
-    float S[9];
     if (mode & PASS_STRESS) {
         if (!gathered) {
             mat_load(k.Ft + 9 * (size_t)p, Ft);
@@ -569,71 +665,239 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
             set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
             return;
         }
-        if (k.rpic != 0.0f) {
-            float Cn[9];
+        global_deposit_all(k, s, p, v, C, S);
+    }
+}
+
+// ---- tiled kernel: block-sorted particles, shared-memory grid tiles ---------
+// Particles arrive sorted by (4^3 block, cell). A CTA owns kTileThreads
+// consecutive particles and maps lane l of warp w to particle l*(T/32)+w, so the
+// lanes of one warp sit in different cells and their shared-memory atomics hit
+// different nodes. The CTA reduces the bounding box of its stencils; when it
+// fits kTileCap nodes the gather reads the grid velocity from a shared copy of
+// that box and the scatter accumulates into a shared tile that is flushed with
+// one vector atomic per touched node. Otherwise the CTA falls back to the direct
+// global path for that stage.
+constexpr int kTileThreads = 256;
+constexpr int kTileCap = 1536;   // nodes; 24 KB as float4
+
+struct TileBox {
+    int lo[3], e[3];
+    int vol;
+    bool fits;
+};
+
+__device__ __forceinline__ void block_box(const int *b, bool valid, TileBox &box, int (*s_red)[6]) {
+    int v[6];
 #pragma unroll
-            for (int i = 0; i < 3; ++i)
+    for (int a = 0; a < 3; ++a) {
+        v[a] = valid ? b[a] : INT_MAX;
+        v[3 + a] = valid ? -b[a] : INT_MAX;   // max as min of negatives
+    }
 #pragma unroll
-                for (int j = 0; j < 3; ++j)
-                    Cn[3 * i + j] = (1.0f - k.rpic) * C[3 * i + j] + k.rpic / 2.0f * (C[3 * i + j] - C[3 * j + i]);
+    for (int a = 0; a < 6; ++a)
+        for (int o = 16; o > 0; o >>= 1) v[a] = min(v[a], __shfl_xor_sync(0xffffffffu, v[a], o));
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
 #pragma unroll
-            for (int i = 0; i < 9; ++i) C[i] = (k.rpic < -0.001f) ? 0.0f : Cn[i];
+        for (int a = 0; a < 6; ++a) s_red[w][a] = v[a];
+    }
+    __syncthreads();
+    int r[6];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) r[a] = INT_MAX;
+    for (int ww = 0; ww < kTileThreads / 32; ++ww)
+#pragma unroll
+        for (int a = 0; a < 6; ++a) r[a] = min(r[a], s_red[ww][a]);
+    __syncthreads();
+    bool any = r[0] != INT_MAX;
+    long long vol = 1;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        box.lo[a] = any ? r[a] : 0;
+        box.e[a] = any ? (-r[3 + a]) - r[a] + 3 : 0;
+        vol *= (long long)box.e[a];
+    }
+    box.vol = any ? (int)min(vol, (long long)INT_MAX) : 0;
+    box.fits = any && vol <= kTileCap;
+}
+
+template <bool SOLIDS>
+__global__ void __launch_bounds__(kTileThreads) k_particles_tiled(PK k, int mode) {
+    __shared__ float4 s_tile[kTileCap];
+    __shared__ int s_red[kTileThreads / 32][6];
+    if ((mode & PASS_RESET_LISTS) && blockIdx.x == 0 && threadIdx.x == 0) {
+        k.blk_count[0] = 0;
+        k.blk_count[1] = 0;
+    }
+    const int t = threadIdx.x;
+    const int slot = (t & 31) * (kTileThreads / 32) + (t >> 5);
+    const int p = blockIdx.x * kTileThreads + slot;
+    bool live = p < k.n && !(k.sel && k.sel[p] != 0);
+    const int mat = live ? k.mat[p] : 0;
+    float x[3] = {0.f, 0.f, 0.f};
+    if (live) { x[0] = k.x[3 * p]; x[1] = k.x[3 * p + 1]; x[2] = k.x[3 * p + 2]; }
+    float v[3] = {0.f, 0.f, 0.f}, C[9], L[9], Ft[9], S[9];
+    bool gathered = false;
+    if (mode & PASS_G2P) {
+        bool want = live && mat != 7 && mat != 8;
+        Stencil s;
+        stencil(x, k.inv_dx, s);
+        if (want && !stencil_ok(s, k.ng, k.periodic_x)) {
+            set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
+            want = false;
+            live = false;
         }
-        const float m = k.mass[p];
-        const float fs = -k.vol[p] * k.dt * k.inv_dx;   // stress term scale
-        float A[9];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) A[i] = fs * S[i];
-        // affine momentum m (v + C dpos dx): precompute m v - m C fx dx and m C dx
-        float mCdx[9], base[3];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) mCdx[i] = m * C[i] * k.dx;
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-            base[a] = m * v[a] - (mCdx[3 * a] * s.fx[0] + mCdx[3 * a + 1] * s.fx[1] + mCdx[3 * a + 2] * s.fx[2]);
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            int ix = s.b[0] + i;
-            if (k.periodic_x) ix = wrap(ix, k.ng);
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                float wij = s.w[0][i] * s.w[1][j];
-                float dwi_j = s.dw[0][i] * s.w[1][j];
-                float wi_dj = s.w[0][i] * s.dw[1][j];
-                float4 *row = k.gmv + ((size_t)ix * k.ng + (s.b[1] + j)) * k.ng + s.b[2];
-#pragma unroll
-                for (int kk = 0; kk < 3; ++kk) {
-                    float wt = wij * s.w[2][kk];
-                    float gx = dwi_j * s.w[2][kk], gy = wi_dj * s.w[2][kk], gz = wij * s.dw[2][kk];
-                    float mom[3];
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) {
-                        float aff = base[a] + mCdx[3 * a] * (float)i + mCdx[3 * a + 1] * (float)j + mCdx[3 * a + 2] * (float)kk;
-                        mom[a] = wt * aff + (A[3 * a] * gx + A[3 * a + 1] * gy + A[3 * a + 2] * gz);
-                    }
-                    atomicAdd(row + kk, make_float4(mom[0], mom[1], mom[2], wt * m));
+        TileBox box;
+        block_box(s.b, want, box, s_red);
+        if (box.fits) {
+            const int e12 = box.e[1] * box.e[2];
+            for (int q = t; q < box.vol; q += kTileThreads) {
+                int qx = q / e12, r = q - qx * e12, qy = r / box.e[2], qz = r - qy * box.e[2];
+                s_tile[q] = __ldg(k.gv + ((size_t)(box.lo[0] + qx) * k.ng + (box.lo[1] + qy)) * k.ng + (box.lo[2] + qz));
+            }
+            __syncthreads();
+            if (want) {
+                const int o0 = s.b[0] - box.lo[0], o1 = s.b[1] - box.lo[1], o2 = s.b[2] - box.lo[2];
+                g2p_core(k, s, [&](int i, int j, int kk) {
+                    return s_tile[((o0 + i) * box.e[1] + (o1 + j)) * box.e[2] + (o2 + kk)];
+                }, v, C, L);
+            }
+            __syncthreads();
+        } else if (want) {
+            g2p_core(k, s, [&](int i, int j, int kk) { return global_fetch(k, s, i, j, kk); }, v, C, L);
+        }
+        if (want) {
+            g2p_finish(k, p, x, v, L, Ft);
+            gathered = true;
+            float *xo = k.x + 3 * (size_t)p;
+            xo[0] = x[0]; xo[1] = x[1]; xo[2] = x[2];
+            if (!(mode & (PASS_STRESS | PASS_P2G)) || (mode & PASS_STORE_VC)) {
+                float *vo = k.v + 3 * (size_t)p;
+                vo[0] = v[0]; vo[1] = v[1]; vo[2] = v[2];
+                mat_store(k.C + 9 * (size_t)p, C);
+            }
+            if (!(mode & PASS_STRESS)) {
+                mat_store(k.L + 9 * (size_t)p, L);
+                mat_store(k.Ft + 9 * (size_t)p, Ft);
+            }
+        }
+    }
+    if ((mode & PASS_STRESS) && live) {
+        if (!gathered) {
+            mat_load(k.Ft + 9 * (size_t)p, Ft);
+            mat_load(k.L + 9 * (size_t)p, L);
+        }
+        float Fn[9];
+        stress_update<SOLIDS>(k, p, mat, Ft, L, Fn, S);
+        mat_store(k.F + 9 * (size_t)p, Fn);
+        if (mode & PASS_STORE_ALL) mat_store(k.S + 9 * (size_t)p, S);
+    }
+    if (mode & PASS_P2G) {
+        if (live) {
+            if (!(mode & PASS_STRESS)) mat_load(k.S + 9 * (size_t)p, S);
+            if (!gathered) {
+                const float *vi = k.v + 3 * (size_t)p;
+                v[0] = vi[0]; v[1] = vi[1]; v[2] = vi[2];
+                mat_load(k.C + 9 * (size_t)p, C);
+            }
+        }
+        Stencil s;
+        stencil(x, k.inv_dx, s);
+        bool want = live;
+        if (want && !stencil_ok(s, k.ng, k.periodic_x)) {
+            set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
+            want = false;
+        }
+        TileBox box;
+        block_box(s.b, want, box, s_red);
+        if (box.fits) {
+            float *f = reinterpret_cast<float *>(s_tile);   // SoA: f[c * kTileCap + node]
+            for (int q = t; q < box.vol; q += kTileThreads) {
+                f[q] = 0.f; f[kTileCap + q] = 0.f; f[2 * kTileCap + q] = 0.f; f[3 * kTileCap + q] = 0.f;
+            }
+            __syncthreads();
+            if (want) {
+                const int o0 = s.b[0] - box.lo[0], o1 = s.b[1] - box.lo[1], o2 = s.b[2] - box.lo[2];
+                p2g_core(k, s, p, v, C, S, [&](int i, int j, int kk, float4 val) {
+                    int q = ((o0 + i) * box.e[1] + (o1 + j)) * box.e[2] + (o2 + kk);
+                    atomicAdd(f + q, val.x);
+                    atomicAdd(f + kTileCap + q, val.y);
+                    atomicAdd(f + 2 * kTileCap + q, val.z);
+                    atomicAdd(f + 3 * kTileCap + q, val.w);
+                });
+            }
+            __syncthreads();
+            const int e12 = box.e[1] * box.e[2];
+            for (int q = t; q < box.vol; q += kTileThreads) {
+                float4 val = make_float4(f[q], f[kTileCap + q], f[2 * kTileCap + q], f[3 * kTileCap + q]);
+                if (val.x != 0.f || val.y != 0.f || val.z != 0.f || val.w != 0.f) {
+                    int qx = q / e12, r = q - qx * e12, qy = r / box.e[2], qz = r - qy * box.e[2];
+                    int gx = box.lo[0] + qx, gy = box.lo[1] + qy, gz = box.lo[2] + qz;
+                    atomicAdd(k.gmv + ((size_t)gx * k.ng + gy) * k.ng + gz, val);
+                    mark_block(k, gx >> 2, gy >> 2, gz >> 2);
                 }
             }
+        } else if (want) {
+            global_deposit_all(k, s, p, v, C, S);
         }
-        // blocks spanned by the stencil
-        int bx0 = s.b[0] >> 2, bx1 = (s.b[0] + 2) >> 2;
-        int by0 = s.b[1] >> 2, by1 = (s.b[1] + 2) >> 2;
-        int bz0 = s.b[2] >> 2, bz1 = (s.b[2] + 2) >> 2;
-        if (k.periodic_x) {
-            // wrapped x nodes: mark the blocks of the wrapped indices
-            for (int i = 0; i < 3; ++i) {
-                int bxi = wrap(s.b[0] + i, k.ng) >> 2;
-                for (int by = by0; by <= by1; ++by)
-                    for (int bz = bz0; bz <= bz1; ++bz) mark_block(k, bxi, by, bz);
-            }
-        } else {
-            for (int bx = bx0; bx <= bx1; ++bx)
-                for (int by = by0; by <= by1; ++by)
-                    for (int bz = bz0; bz <= bz1; ++bz) mark_block(k, bx, by, bz);
-        }
-        if (!gathered || (mode & PASS_STORE_VC)) {
-            // v and C are state only for particles the gather skipped
-        }
+    }
+}
+
+// ---- per-tick working set: block-sorted copy of the particles --------------
+// key = (4^3 block of the stencil base, cell within the block); positions are
+// clamped into the grid so every particle gets a key.
+__global__ void k_cell_keys(const float *x, int n, float inv_dx, int ng, int bd, unsigned long long *keys,
+                            int *idx) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int b[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float g = x[3 * (size_t)p + a] * inv_dx - 0.5f;
+        int c = isfinite(g) ? (int)floorf(fminf(fmaxf(g, 0.0f), (float)(ng - 1))) : 0;
+        b[a] = c;
+    }
+    unsigned blk = (unsigned)(((b[0] >> 2) * bd + (b[1] >> 2)) * bd + (b[2] >> 2));
+    unsigned cell = (unsigned)(((b[0] & 3) << 4) | ((b[1] & 3) << 2) | (b[2] & 3));
+    keys[p] = ((unsigned long long)blk << 6) | cell;
+    idx[p] = p;
+}
+
+struct WsField {
+    float *ext;
+    float *ws;
+    int width;
+    int back;   // copied back to the caller's buffer at the end of the tick
+};
+constexpr int kMaxWsFields = 20;
+struct WsTable {
+    WsField f[kMaxWsFields];
+    int nf;
+};
+
+__global__ void k_ws_gather(WsTable T, const int *perm, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t src = (size_t)perm[i];
+    for (int f = 0; f < T.nf; ++f) {
+        const int w = T.f[f].width;
+        const float *a = T.f[f].ext + src * w;
+        float *b = T.f[f].ws + (size_t)i * w;
+        for (int c = 0; c < w; ++c) b[c] = a[c];
+    }
+}
+
+__global__ void k_ws_scatter(WsTable T, const int *perm, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t dst = (size_t)perm[i];
+    for (int f = 0; f < T.nf; ++f) {
+        if (!T.f[f].back) continue;
+        const int w = T.f[f].width;
+        const float *a = T.f[f].ws + (size_t)i * w;
+        float *b = T.f[f].ext + dst * w;
+        for (int c = 0; c < w; ++c) b[c] = a[c];
     }
 }
 
@@ -1159,7 +1423,7 @@ int fail(int code, const std::string &msg) {
     } while (0)
 
 const char *kPhaseNames[GBMPM_NUM_PHASES] = {"compute_stress_from_F_trial", "p2g", "g2p2g_fused",
-                                             "grid_update+BC", "g2p", "guard"};
+                                             "grid_update+BC", "g2p", "block_sort+gather"};
 
 template <class T>
 struct DevBuf {
@@ -1200,6 +1464,14 @@ struct gbmpm_engine {
     DevBuf<int> d_flagbuf;
     DevBuf<float> d_tmp;
     DevBuf<int> d_braw, d_bcur, d_bprev, d_bcount;
+    // per-tick block-sorted working set
+    DevBuf<float> ws_buf;
+    DevBuf<unsigned long long> ws_keys[2];
+    DevBuf<int> ws_idx[2];
+    DevBuf<unsigned> ws_hist;
+    gbmpm_particles W{};
+    WsTable ws_table{};
+    int ws_n = -1;
     PoseRec *h_pose = nullptr;
     size_t h_pose_cap = 0;
     cudaEvent_t pose_done = nullptr;
@@ -1208,6 +1480,7 @@ struct gbmpm_engine {
     // graph cache
     cudaGraphExec_t graph = nullptr;
     int g_substeps = -1, g_flags = -1;
+    int64_t graph_launches = 0;
     double g_dt = 0.0;
     cudaStream_t g_stream = nullptr;
     bool dirty = true;
@@ -1219,9 +1492,8 @@ struct gbmpm_engine {
 
 namespace {
 
-PK make_pk(gbmpm_engine *e, float dt, int list) {
+PK make_pk(gbmpm_engine *e, const gbmpm_particles &P, float dt, int list) {
     PK k{};
-    const gbmpm_particles &P = e->P;
     k.x = P.x; k.v = P.v; k.C = P.C; k.F = P.F; k.Ft = P.F_trial; k.L = P.L; k.S = P.stress;
     k.mass = P.mass; k.vol = P.vol; k.Jp = P.Jp; k.mu = P.mu; k.lam = P.lam; k.ys = P.yield_stress;
     k.mat = P.material; k.sel = P.selection; k.cov = P.cov; k.n = P.n;
@@ -1246,12 +1518,86 @@ bool has_solids(const gbmpm_model &m) {
     return (m.material_mask & ~fluid) != 0;
 }
 
-void launch_particles(gbmpm_engine *e, const PK &k, int mode, cudaStream_t s) {
-    int grid = (k.n + kParticleThreads - 1) / kParticleThreads;
-    if (grid == 0) grid = 1;
-    if (has_solids(e->M)) k_particles<true><<<grid, kParticleThreads, 0, s>>>(k, mode);
-    else k_particles<false><<<grid, kParticleThreads, 0, s>>>(k, mode);
+void launch_particles(gbmpm_engine *e, const PK &k, int mode, bool tiled, cudaStream_t s) {
+    if (tiled) {
+        int grid = std::max(1, (k.n + kTileThreads - 1) / kTileThreads);
+        if (has_solids(e->M)) k_particles_tiled<true><<<grid, kTileThreads, 0, s>>>(k, mode);
+        else k_particles_tiled<false><<<grid, kTileThreads, 0, s>>>(k, mode);
+    } else {
+        int grid = std::max(1, (k.n + kParticleThreads - 1) / kParticleThreads);
+        if (has_solids(e->M)) k_particles<true><<<grid, kParticleThreads, 0, s>>>(k, mode);
+        else k_particles<false><<<grid, kParticleThreads, 0, s>>>(k, mode);
+    }
     e->launches++;
+}
+
+// Allocates the block-sorted working copy and the table of fields the tick
+// gathers into it and scatters back (only fields a tick writes go back).
+cudaError_t ensure_ws(gbmpm_engine *e) {
+    const gbmpm_particles &P = e->P;
+    const int n = P.n;
+    const bool cov = P.cov && e->M.update_cov_with_F;
+    struct Spec { float *ext; int w; int back; float **dst; };
+    gbmpm_particles &W = e->W;
+    W = P;
+    Spec spec[] = {
+        {P.x, 3, 1, &W.x}, {P.v, 3, 1, &W.v}, {P.C, 9, 1, &W.C}, {P.F, 9, 1, &W.F},
+        {P.F_trial, 9, 1, &W.F_trial}, {P.L, 9, 1, &W.L}, {P.stress, 9, 1, &W.stress},
+        {P.mass, 1, 0, &W.mass}, {P.vol, 1, 0, &W.vol}, {P.Jp, 1, 1, &W.Jp}, {P.mu, 1, 1, &W.mu},
+        {P.lam, 1, 1, &W.lam}, {P.yield_stress, 1, 1, &W.yield_stress},
+        {reinterpret_cast<float *>(P.material), 1, 0, reinterpret_cast<float **>(&W.material)},
+        {reinterpret_cast<float *>(P.selection), 1, 0, reinterpret_cast<float **>(&W.selection)},
+        {cov ? P.cov : nullptr, 6, 1, &W.cov},
+    };
+    size_t total = 0;
+    for (const Spec &sp : spec) if (sp.ext) total += (size_t)sp.w * n;
+    cudaError_t err = e->ws_buf.ensure(total);
+    if (err != cudaSuccess) return err;
+    size_t off = 0;
+    e->ws_table.nf = 0;
+    for (const Spec &sp : spec) {
+        if (!sp.ext) { *sp.dst = nullptr; continue; }
+        float *ws = e->ws_buf.ptr + off;
+        off += (size_t)sp.w * n;
+        *sp.dst = ws;
+        e->ws_table.f[e->ws_table.nf++] = WsField{sp.ext, ws, sp.w, sp.back};
+    }
+    W.density = nullptr;
+    W.init_cov = nullptr;
+    if (!cov) W.cov = nullptr;
+    const int ntiles = (n + kSortTile - 1) / kSortTile;
+    if ((err = e->ws_keys[0].ensure(n)) != cudaSuccess) return err;
+    if ((err = e->ws_keys[1].ensure(n)) != cudaSuccess) return err;
+    if ((err = e->ws_idx[0].ensure(n)) != cudaSuccess) return err;
+    if ((err = e->ws_idx[1].ensure(n)) != cudaSuccess) return err;
+    if ((err = e->ws_hist.ensure((size_t)ntiles * kRadixBins)) != cudaSuccess) return err;
+    e->ws_n = n;
+    return cudaSuccess;
+}
+
+// Records the working-set sort + gather; returns the permutation buffer.
+const int *record_ws_begin(gbmpm_engine *e, cudaStream_t s) {
+    const int n = e->P.n;
+    const int ntiles = (n + kSortTile - 1) / kSortTile;
+    k_cell_keys<<<(n + 255) / 256, 256, 0, s>>>(e->P.x, n, e->M.inv_dx, e->G.n_grid, e->bd, e->ws_keys[0].ptr,
+                                                 e->ws_idx[0].ptr);
+    e->launches++;
+    unsigned long long maxkey = ((unsigned long long)e->bd * e->bd * e->bd << 6) - 1ull;
+    int bits = 0;
+    while ((maxkey >> bits) != 0ull) ++bits;
+    int cur = 0;
+    for (int shift = 0; shift < bits; shift += kRadixBits) {
+        k_radix_hist<<<ntiles, kSortThreads, 0, s>>>(e->ws_keys[cur].ptr, n, shift, e->ws_hist.ptr, ntiles);
+        k_radix_scan<<<1, 1024, 0, s>>>(e->ws_hist.ptr, ntiles * kRadixBins);
+        k_radix_scatter<<<ntiles, kSortThreads, 0, s>>>(e->ws_keys[cur].ptr, e->ws_idx[cur].ptr,
+                                                         e->ws_keys[cur ^ 1].ptr, e->ws_idx[cur ^ 1].ptr, n, shift,
+                                                         e->ws_hist.ptr, ntiles);
+        e->launches += 3;
+        cur ^= 1;
+    }
+    k_ws_gather<<<(n + 255) / 256, 256, 0, s>>>(e->ws_table, e->ws_idx[cur].ptr, n);
+    e->launches++;
+    return e->ws_idx[cur].ptr;
 }
 
 void launch_grid(gbmpm_engine *e, float dt, int substep, int list, cudaStream_t s) {
@@ -1368,7 +1714,7 @@ int check_ready(gbmpm_engine *e) {
 }
 
 // Records the launches of one tick on stream s.
-void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, cudaStream_t s, bool profile) {
+void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cudaStream_t s, bool profile) {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     if (profile) { cudaEventCreate(&ev0); cudaEventCreate(&ev1); }
     auto timed = [&](int phase, auto fn) {
@@ -1382,23 +1728,32 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, cudaStream_t s, 
         e->prof_ms[phase] += ms;
         e->prof_n[phase] += 1;
     };
+    const int *perm = nullptr;
+    if (reorder) timed(5, [&] { perm = record_ws_begin(e, s); });
+    const gbmpm_particles &P = reorder ? e->W : e->P;
     for (int sub = 0; sub < S; ++sub) {
         int list = sub & 1;
-        PK k = make_pk(e, dtf, list);
+        PK k = make_pk(e, P, dtf, list);
         bool last_stress = fused ? (sub == S - 1) : true;
         if (!fused || sub == 0) {
             int mode = PASS_STRESS | PASS_P2G | (last_stress ? PASS_STORE_ALL : 0);
-            timed(0, [&] { launch_particles(e, k, mode, s); });
+            timed(0, [&] { launch_particles(e, k, mode, reorder, s); });
         } else {
             int mode = PASS_G2P | PASS_STRESS | PASS_P2G | (last_stress ? PASS_STORE_ALL : 0);
-            timed(2, [&] { launch_particles(e, k, mode, s); });
+            timed(2, [&] { launch_particles(e, k, mode, reorder, s); });
         }
         timed(3, [&] { launch_grid(e, dtf, sub, list, s); });
-        if (!fused) timed(4, [&] { launch_particles(e, k, PASS_G2P | PASS_RESET_LISTS, s); });
+        if (!fused) timed(4, [&] { launch_particles(e, k, PASS_G2P | PASS_RESET_LISTS, reorder, s); });
     }
     if (fused) {
-        PK k = make_pk(e, dtf, 0);
-        timed(4, [&] { launch_particles(e, k, PASS_G2P | PASS_RESET_LISTS, s); });
+        PK k = make_pk(e, P, dtf, 0);
+        timed(4, [&] { launch_particles(e, k, PASS_G2P | PASS_RESET_LISTS, reorder, s); });
+    }
+    if (reorder) {
+        timed(5, [&] {
+            k_ws_scatter<<<(e->P.n + 255) / 256, 256, 0, s>>>(e->ws_table, perm, e->P.n);
+            e->launches++;
+        });
     }
     if (profile) { cudaEventDestroy(ev0); cudaEventDestroy(ev1); }
 }
@@ -1438,6 +1793,8 @@ void gbmpm_engine_destroy(gbmpm_engine *e) {
     e->d_guard.release(); e->d_keys[0].release(); e->d_keys[1].release(); e->d_skeys.release(); e->d_kminmax.release(); e->d_idx[0].release();
     e->d_idx[1].release(); e->d_hist.release(); e->d_flagbuf.release(); e->d_tmp.release();
     e->d_braw.release(); e->d_bcur.release(); e->d_bprev.release(); e->d_bcount.release();
+    e->ws_buf.release(); e->ws_keys[0].release(); e->ws_keys[1].release(); e->ws_idx[0].release();
+    e->ws_idx[1].release(); e->ws_hist.release();
     delete e;
 }
 
@@ -1465,6 +1822,7 @@ int gbmpm_bind(gbmpm_engine *e, const gbmpm_particles *p, const gbmpm_grid *g) {
     GB_CUDA(cudaMemset(g->v, 0, nn * 16));
     e->bound = true;
     e->dirty = true;
+    e->ws_n = -1;
     return GBMPM_OK;
 }
 
@@ -1485,6 +1843,7 @@ int gbmpm_set_model(gbmpm_engine *e, const gbmpm_model *m) {
     GB_CUDA(e->d_tab.ensure(1));
     GB_CUDA(cudaMemcpy(e->d_tab.ptr, &t, sizeof t, cudaMemcpyHostToDevice));
     e->modeled = true;
+    e->ws_n = -1;
     e->dirty = true;
     return GBMPM_OK;
 }
@@ -1553,10 +1912,15 @@ int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32
     GB_CUDA(cudaEventRecord(e->pose_done, s));
     const bool fused = (flags & GBMPM_TICK_FUSED) != 0;
     const bool profile = (flags & GBMPM_TICK_PROFILE) != 0;
+    const bool reorder = (flags & GBMPM_TICK_REORDER) && !e->M.periodic_x;
+    if (reorder && e->ws_n != e->P.n) {
+        GB_CUDA(ensure_ws(e));
+        e->dirty = true;
+    }
     const bool use_graph = (flags & GBMPM_TICK_GRAPH) && !profile;
     const float dtf = (float)dt;
     if (!use_graph) {
-        record_tick(e, dtf, substeps, fused, s, profile);
+        record_tick(e, dtf, substeps, fused, reorder, s, profile);
         GB_CUDA(cudaGetLastError());
         return GBMPM_OK;
     }
@@ -1569,7 +1933,8 @@ int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32
         cudaGraph_t g = nullptr;
         GB_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
         int64_t before = e->launches;
-        record_tick(e, dtf, substeps, fused, cap, false);
+        record_tick(e, dtf, substeps, fused, reorder, cap, false);
+        e->graph_launches = e->launches - before;
         e->launches = before;
         cudaError_t ce = cudaStreamEndCapture(cap, &g);
         cudaStreamDestroy(cap);
@@ -1581,7 +1946,7 @@ int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32
         e->dirty = false;
     }
     GB_CUDA(cudaGraphLaunch(e->graph, s));
-    e->launches += (int64_t)substeps * (fused ? 2 : 3) + (fused ? 1 : 0);
+    e->launches += e->graph_launches;
     return GBMPM_OK;
 }
 

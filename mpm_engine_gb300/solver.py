@@ -150,6 +150,8 @@ class _SimShim:
             os.environ.get("GBMPM_NO_CUDA_GRAPH", "") != "1"
         self.restrict_bc = True
         self.restrict_grid = True
+        # run each tick on a block-sorted working copy with shared-memory grid tiles
+        self.reorder = os.environ.get("GBMPM_NO_REORDER", "") != "1"
         self.pre_p2g_operations = []
         self.particle_velocity_modifiers = []
         self.n_rigid_bodies = 0
@@ -675,6 +677,8 @@ class Solver:
             flags |= _abi.TICK_PROFILE
         elif self._sim.use_cuda_graph:
             flags |= _abi.TICK_GRAPH
+        if self._sim.reorder:
+            flags |= _abi.TICK_REORDER
         t = C.c_double(self._time)
         _abi.check(self._eng.lib.gbmpm_tick(self._eng.h, C.byref(t), float(dt), int(substeps), flags,
                                             self._stream()), "gbmpm_tick")
@@ -887,6 +891,7 @@ class Solver:
             C.memmove(C.byref(r), C.byref(rec), C.sizeof(_abi.Collider))
             cols.append(r)
         out["colliders"] = cols
+        out["handles"] = list(self._handles)
         out["sdf_host"] = {t.data_ptr(): t.cpu().numpy().copy() for t in self._keep}
         out["time"] = self._time
         return out

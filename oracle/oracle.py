@@ -301,7 +301,7 @@ class OracleSolver:
                 o.sdf_arrays += [val, grad]
                 r.sdf_val, r.sdf_grad = _p(val), _p(grad)
             o.cols.append(r)
-            o.handles.append(len(o.cols) - 1)
+        o.handles = list(st.get("handles", range(len(o.cols))))
         o.wrench = np.zeros((len(o.cols), 6), np.float32)
         o.time = float(st["time"])
         return o

@@ -13,13 +13,19 @@ from scenes_lib import MATERIALS, blob_scene, dam_break, free_blob
 
 pytestmark = pytest.mark.gpu
 
-FLOOR = {"x": 1e-6, "v": 1e-6, "C": 1e-4, "F": 1e-6}
+FLOOR = {"x": 1e-6, "v": 1e-6, "F": 1e-6}
 
 
 def rel_err(a, b, floor):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
     return float(np.abs(a - b).max() / (np.abs(b).max() + floor))
+
+
+def c_floor(o):
+    """C = 4/dx sum_i w_i v_i (x_i - x_p)/dx is a cancelling sum of terms of size
+    4 |v| / dx; its rounding error scales with that term size, not with |C|."""
+    return 4.0 / o.dx * float(np.abs(o.a["v"]).max()) + 1e-12
 
 
 def fields_gpu(s):
@@ -32,7 +38,8 @@ def fields_oracle(o):
 
 def assert_close(s, o, tol, what=""):
     g, r = fields_gpu(s), fields_oracle(o)
-    errs = {k: rel_err(g[k], r[k], FLOOR[k]) for k in g}
+    floors = dict(FLOOR, C=c_floor(o))
+    errs = {k: rel_err(g[k], r[k], floors[k]) for k in g}
     bad = {k: e for k, e in errs.items() if not e <= tol}
     assert not bad, f"{what}: relative errors {errs} exceed {tol}"
     return errs
@@ -45,10 +52,16 @@ def pair(cuda, oracle_lib, builder, *args, fused=True, **kw):
     return s, o, h
 
 
+# explicit-stability step per material on the 48^3 / 0.4 m blob: the yield-stress
+# fluids carry eta_app up to tau_y / 0.02 (the strain-rate regularization), so their
+# viscous limit rho dx^2 / (6 eta) is a few microseconds
+DT = {"bingham": 1.0e-6, "herschel_bulkley": 5.0e-6}
+
+
 @pytest.mark.parametrize("key", sorted(MATERIALS))
 def test_per_substep_parity_all_materials(cuda, oracle_lib, key):
     s, o, _ = pair(cuda, oracle_lib, blob_scene, key)
-    dt = 2.0e-4
+    dt = DT.get(key, 2.0e-4)
     for i in range(4):
         s.step(dt, 1)
         o.step(dt, 1)
@@ -57,6 +70,17 @@ def test_per_substep_parity_all_materials(cuda, oracle_lib, key):
     o.step(dt, 8)
     assert_close(s, o, 1e-5, f"{key} after a fused 8-substep tick")
     np.testing.assert_array_equal(s._t["mass"].cpu().numpy(), o.a["mass"])
+
+
+@pytest.mark.parametrize("key", ["newtonian", "metal", "mu_i"])
+def test_parity_direct_kernel_path(cuda, oracle_lib, key):
+    """The unsorted one-thread-per-particle path (no working-set reorder)."""
+    s, o, _ = pair(cuda, oracle_lib, blob_scene, key)
+    s._sim.reorder = False
+    for _ in range(3):
+        s.step(2.0e-4, 4)
+        o.step(2.0e-4, 4)
+        assert_close(s, o, 1e-5, f"{key} direct path")
 
 
 def test_parity_split_pipeline(cuda, oracle_lib):
@@ -97,7 +121,7 @@ def test_box_tool_force_parity(cuda, oracle_lib):
 def test_long_horizon_1000_substeps(cuda, oracle_lib):
     from mpm_engine_gb300 import Solver
     s, o = None, None
-    s, _ = blob_scene(Solver, "herschel_bulkley")
+    s, _ = blob_scene(Solver, "newtonian")
     o = oracle_lib.OracleSolver.from_state(s.export_state(), s.grid.n_grid, s.grid.grid_lim)
     for _ in range(10):
         s.step(1.0e-4, 100)
@@ -108,7 +132,7 @@ def test_long_horizon_1000_substeps(cuda, oracle_lib):
 
 def test_dam_break_momentum_and_mass(cuda, oracle_lib):
     from mpm_engine_gb300 import Solver
-    s = dam_break(Solver, n_grid=32)
+    s = dam_break(Solver, n_grid=32, hi=(0.4, 0.6, 0.85))
     o = oracle_lib.OracleSolver.from_state(s.export_state(), 32, 1.0)
     m = s._t["mass"].cpu().numpy().astype(np.float64)
     for _ in range(5):
@@ -119,6 +143,20 @@ def test_dam_break_momentum_and_mass(cuda, oracle_lib):
     po = (m[:, None] * o.a["v"].astype(np.float64)).sum(0)
     assert np.abs(pg - po).max() <= 1e-5 * np.abs(po).max() + 1e-12
     np.testing.assert_array_equal(s._t["mass"].cpu().numpy(), o.a["mass"])
+
+
+def test_reordered_tiles_equal_direct_path(cuda):
+    from mpm_engine_gb300 import Solver
+    outs = []
+    for reorder in (True, False):
+        s, h = blob_scene(Solver, "newtonian", cup=True, n=6000)
+        s._sim.reorder = reorder
+        for _ in range(4):
+            s.step(2.0e-4, 8)
+        outs.append((s.x(), s.v(), s.cup_wrench(h, 1.0)["force"]))
+    np.testing.assert_allclose(outs[0][0], outs[1][0], rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(outs[0][1], outs[1][1], rtol=1e-4, atol=1e-6)
+    np.testing.assert_allclose(outs[0][2], outs[1][2], rtol=1e-4)
 
 
 def test_graph_replay_equals_live_launches(cuda):
@@ -165,16 +203,20 @@ def test_sort_bit_exact_against_oracle(cuda, oracle_lib):
 
 
 def test_active_block_counts_match_oracle(cuda, oracle_lib):
+    """rebuild_active_blocks (mpm_solver_warp.py:989-1026): the sparse solver rebuilds
+    from the positions at the start of each tick; counts = {current, union with previous}."""
     from mpm_engine_gb300 import Solver
     s, _ = blob_scene(Solver, "newtonian", sparse=True)
-    prev = None
+    xs = []
     for _ in range(3):
+        xs.append(s.x().copy())
         s.step(2.0e-4, 5)
-        cur, counts = oracle_lib.blocks(s.x(), float(s._model.inv_dx), s.grid.n_grid, prev)
-        prev = cur
+    inv_dx = float(s._model.inv_dx)
+    prev, _ = oracle_lib.blocks(xs[-1], inv_dx, s.grid.n_grid)
     s._rebuild_active_blocks()
-    cur, counts = oracle_lib.blocks(s.x(), float(s._model.inv_dx), s.grid.n_grid, prev)
+    _, counts = oracle_lib.blocks(s.x(), inv_dx, s.grid.n_grid, prev)
     assert s._sim._block_counts == (int(counts[0]), int(counts[1]))
+    assert 0.0 < s._sim.active_block_fraction() < 1.0
 
 
 def test_R_and_cov_exports_match_oracle(cuda, oracle_lib):
