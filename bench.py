@@ -272,9 +272,11 @@ def main():
     grid_ms = msv[3] / max(cnt[3], 1)
     peak, peak_kind = peaks()
     achieved = n * BYTES_PER_PARTICLE_SUBSTEP / (fused_ms / 1e3) / 1e9
+    phases = {s._eng.lib.gbmpm_phase_name(i).decode(): round(msv[i] / max(cnt[i], 1), 5)
+              for i in range(6) if cnt[i]}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "k_particles (fused G2P2G)", "kernel_ms": fused_ms,
-                "grid_kernel_ms": grid_ms, "peak_kind": peak_kind}
+                "traffic": None, "kernel": "k_particles_tiled (fused G2P2G)", "kernel_ms": fused_ms,
+                "grid_kernel_ms": grid_ms, "peak_kind": peak_kind, "phase_ms_per_launch": phases}
 
     e2e = None
     if not args.no_e2e:
