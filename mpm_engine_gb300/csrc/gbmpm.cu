@@ -669,17 +669,23 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
     }
 }
 
-// ---- tiled kernel: block-sorted particles, shared-memory grid tiles ---------
-// Particles arrive sorted by (4^3 block, cell). A CTA owns kTileThreads
-// consecutive particles and maps lane l of warp w to particle l*(T/32)+w, so the
-// lanes of one warp sit in different cells and their shared-memory atomics hit
-// different nodes. The CTA reduces the bounding box of its stencils; when it
-// fits kTileCap nodes the gather reads the grid velocity from a shared copy of
-// that box and the scatter accumulates into a shared tile that is flushed with
-// one vector atomic per touched node. Otherwise the CTA falls back to the direct
-// global path for that stage.
+// ---- tiled kernel: block-sorted particles, shared-memory gather tile, run-wise scatter
+// Particles arrive sorted by (4^3 block, cell); a CTA owns kTileThreads
+// consecutive particles, one per thread.
+//  * Gather: the CTA reduces the bounding box of its stencils; when it holds at
+//    most kGatherCap nodes the grid velocity of that box is copied to shared
+//    memory and the 27-node gathers read it there (neighbouring threads share
+//    nodes, so most reads are broadcasts).
+//  * Scatter: each particle leaves a 25-float record in shared memory. Runs of
+//    consecutive particles whose stencils share the same base node (the same
+//    cell) are scattered together: 27 lanes of a warp take one node each, sum
+//    the run's contributions to that node from broadcast shared reads, and issue
+//    one red.global.add.v4.f32. Global atomics drop from 27 per particle to 27 per
+//    run, and no shared-memory atomics are needed.
 constexpr int kTileThreads = 256;
-constexpr int kTileCap = 1536;   // nodes; 24 KB as float4
+constexpr int kGatherCap = 1536;          // nodes in the shared gather tile (24 KB)
+constexpr int kRec = 25;                  // floats per particle scatter record
+constexpr int kSmemFloats = (kGatherCap * 4 > kTileThreads * kRec) ? kGatherCap * 4 : kTileThreads * kRec;
 
 struct TileBox {
     int lo[3], e[3];
@@ -719,20 +725,31 @@ __device__ __forceinline__ void block_box(const int *b, bool valid, TileBox &box
         vol *= (long long)box.e[a];
     }
     box.vol = any ? (int)min(vol, (long long)INT_MAX) : 0;
-    box.fits = any && vol <= kTileCap;
+    box.fits = any && vol <= kGatherCap;
+}
+
+// quadratic B-spline weight and its derivative for node offset o of one axis
+__device__ __forceinline__ void bspline_o(float fx, int o, float &w, float &dw) {
+    float t0 = 1.5f - fx, t1 = fx - 1.0f, t2 = fx - 0.5f;
+    float w0 = 0.5f * (t0 * t0), w1 = 0.75f - t1 * t1, w2 = 0.5f * (t2 * t2);
+    w = (o == 0) ? w0 : ((o == 1) ? w1 : w2);
+    dw = (o == 0) ? -t0 : ((o == 1) ? -2.0f * t1 : t2);
 }
 
 template <bool SOLIDS>
 __global__ void __launch_bounds__(kTileThreads) k_particles_tiled(PK k, int mode) {
-    __shared__ float4 s_tile[kTileCap];
+    __shared__ __align__(16) float s_mem[kSmemFloats];
+    __shared__ int s_key[kTileThreads];
+    __shared__ int s_seg[kTileThreads + 1];
+    __shared__ int s_wcnt[kTileThreads / 32];
     __shared__ int s_red[kTileThreads / 32][6];
     if ((mode & PASS_RESET_LISTS) && blockIdx.x == 0 && threadIdx.x == 0) {
         k.blk_count[0] = 0;
         k.blk_count[1] = 0;
     }
     const int t = threadIdx.x;
-    const int slot = (t & 31) * (kTileThreads / 32) + (t >> 5);
-    const int p = blockIdx.x * kTileThreads + slot;
+    const int lane = t & 31, warp = t >> 5;
+    const int p = blockIdx.x * kTileThreads + t;
     bool live = p < k.n && !(k.sel && k.sel[p] != 0);
     const int mat = live ? k.mat[p] : 0;
     float x[3] = {0.f, 0.f, 0.f};
@@ -750,6 +767,7 @@ __global__ void __launch_bounds__(kTileThreads) k_particles_tiled(PK k, int mode
         }
         TileBox box;
         block_box(s.b, want, box, s_red);
+        float4 *s_tile = reinterpret_cast<float4 *>(s_mem);
         if (box.fits) {
             const int e12 = box.e[1] * box.e[2];
             for (int q = t; q < box.vol; q += kTileThreads) {
@@ -793,53 +811,92 @@ __global__ void __launch_bounds__(kTileThreads) k_particles_tiled(PK k, int mode
         mat_store(k.F + 9 * (size_t)p, Fn);
         if (mode & PASS_STORE_ALL) mat_store(k.S + 9 * (size_t)p, S);
     }
-    if (mode & PASS_P2G) {
-        if (live) {
-            if (!(mode & PASS_STRESS)) mat_load(k.S + 9 * (size_t)p, S);
-            if (!gathered) {
-                const float *vi = k.v + 3 * (size_t)p;
-                v[0] = vi[0]; v[1] = vi[1]; v[2] = vi[2];
-                mat_load(k.C + 9 * (size_t)p, C);
-            }
+    if (!(mode & PASS_P2G)) return;
+    if (live) {
+        if (!(mode & PASS_STRESS)) mat_load(k.S + 9 * (size_t)p, S);
+        if (!gathered) {
+            const float *vi = k.v + 3 * (size_t)p;
+            v[0] = vi[0]; v[1] = vi[1]; v[2] = vi[2];
+            mat_load(k.C + 9 * (size_t)p, C);
         }
-        Stencil s;
-        stencil(x, k.inv_dx, s);
-        bool want = live;
-        if (want && !stencil_ok(s, k.ng, k.periodic_x)) {
-            set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
-            want = false;
+    }
+    Stencil s;
+    stencil(x, k.inv_dx, s);
+    bool want = live;
+    if (want && !stencil_ok(s, k.ng, k.periodic_x)) {
+        set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
+        want = false;
+    }
+    // ---- scatter record: fx, affine momentum base, m C dx, stress term A, m
+    if (want) {
+        float Cr[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Cr[i] = C[i];
+        if (k.rpic != 0.0f) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                    Cr[3 * i + j] = (k.rpic < -0.001f) ? 0.0f
+                                    : (1.0f - k.rpic) * C[3 * i + j] + k.rpic / 2.0f * (C[3 * i + j] - C[3 * j + i]);
         }
-        TileBox box;
-        block_box(s.b, want, box, s_red);
-        if (box.fits) {
-            float *f = reinterpret_cast<float *>(s_tile);   // SoA: f[c * kTileCap + node]
-            for (int q = t; q < box.vol; q += kTileThreads) {
-                f[q] = 0.f; f[kTileCap + q] = 0.f; f[2 * kTileCap + q] = 0.f; f[3 * kTileCap + q] = 0.f;
-            }
-            __syncthreads();
-            if (want) {
-                const int o0 = s.b[0] - box.lo[0], o1 = s.b[1] - box.lo[1], o2 = s.b[2] - box.lo[2];
-                p2g_core(k, s, p, v, C, S, [&](int i, int j, int kk, float4 val) {
-                    int q = ((o0 + i) * box.e[1] + (o1 + j)) * box.e[2] + (o2 + kk);
-                    atomicAdd(f + q, val.x);
-                    atomicAdd(f + kTileCap + q, val.y);
-                    atomicAdd(f + 2 * kTileCap + q, val.z);
-                    atomicAdd(f + 3 * kTileCap + q, val.w);
-                });
-            }
-            __syncthreads();
-            const int e12 = box.e[1] * box.e[2];
-            for (int q = t; q < box.vol; q += kTileThreads) {
-                float4 val = make_float4(f[q], f[kTileCap + q], f[2 * kTileCap + q], f[3 * kTileCap + q]);
-                if (val.x != 0.f || val.y != 0.f || val.z != 0.f || val.w != 0.f) {
-                    int qx = q / e12, r = q - qx * e12, qy = r / box.e[2], qz = r - qy * box.e[2];
-                    int gx = box.lo[0] + qx, gy = box.lo[1] + qy, gz = box.lo[2] + qz;
-                    atomicAdd(k.gmv + ((size_t)gx * k.ng + gy) * k.ng + gz, val);
-                    mark_block(k, gx >> 2, gy >> 2, gz >> 2);
-                }
-            }
-        } else if (want) {
-            global_deposit_all(k, s, p, v, C, S);
+        const float m = k.mass[p];
+        const float fs = -k.vol[p] * k.dt * k.inv_dx;
+        float *r = s_mem + t * kRec;
+        r[0] = s.fx[0]; r[1] = s.fx[1]; r[2] = s.fx[2];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            float c0 = m * Cr[3 * a] * k.dx, c1 = m * Cr[3 * a + 1] * k.dx, c2 = m * Cr[3 * a + 2] * k.dx;
+            r[3 + a] = m * v[a] - (c0 * s.fx[0] + c1 * s.fx[1] + c2 * s.fx[2]);
+            r[6 + 3 * a] = c0; r[7 + 3 * a] = c1; r[8 + 3 * a] = c2;
+            r[15 + 3 * a] = fs * S[3 * a]; r[16 + 3 * a] = fs * S[3 * a + 1]; r[17 + 3 * a] = fs * S[3 * a + 2];
+        }
+        r[24] = m;
+        s_key[t] = (s.b[0] * k.ng + s.b[1]) * k.ng + s.b[2];
+    } else {
+        s_key[t] = -1 - t;   // a dead slot forms its own, skipped run
+    }
+    __syncthreads();
+    // ---- runs of equal base node: compact the run heads
+    const bool head = (t == 0) || (s_key[t] != s_key[t - 1]);
+    const unsigned bal = __ballot_sync(0xffffffffu, head);
+    if (lane == 0) s_wcnt[warp] = __popc(bal);
+    __syncthreads();
+    int off = 0, total = 0;
+    for (int w = 0; w < kTileThreads / 32; ++w) {
+        int c = s_wcnt[w];
+        if (w < warp) off += c;
+        total += c;
+    }
+    if (head) s_seg[off + __popc(bal & ((1u << lane) - 1u))] = t;
+    if (t == 0) s_seg[total] = kTileThreads;
+    __syncthreads();
+    // ---- 27 lanes per run, one node each
+    const int oi = lane / 9, oj = (lane / 3) % 3, ok = lane % 3;
+    for (int sg = warp; sg < total; sg += kTileThreads / 32) {
+        const int q0 = s_seg[sg], q1 = s_seg[sg + 1];
+        const int key = s_key[q0];
+        if (key < 0 || lane >= 27) continue;
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+        for (int q = q0; q < q1; ++q) {
+            const float *r = s_mem + q * kRec;
+            float wx, dwx, wy, dwy, wz, dwz;
+            bspline_o(r[0], oi, wx, dwx);
+            bspline_o(r[1], oj, wy, dwy);
+            bspline_o(r[2], ok, wz, dwz);
+            const float wt = wx * wy * wz;
+            const float gx = dwx * wy * wz, gy = wx * dwy * wz, gz = wx * wy * dwz;
+            const float fi = (float)oi, fj = (float)oj, fk = (float)ok;
+            a0 += wt * (r[3] + r[6] * fi + r[7] * fj + r[8] * fk) + (r[15] * gx + r[16] * gy + r[17] * gz);
+            a1 += wt * (r[4] + r[9] * fi + r[10] * fj + r[11] * fk) + (r[18] * gx + r[19] * gy + r[20] * gz);
+            a2 += wt * (r[5] + r[12] * fi + r[13] * fj + r[14] * fk) + (r[21] * gx + r[22] * gy + r[23] * gz);
+            a3 += wt * r[24];
+        }
+        if (a0 != 0.f || a1 != 0.f || a2 != 0.f || a3 != 0.f) {
+            const int bz = key % k.ng, rr = key / k.ng, by = rr % k.ng, bx = rr / k.ng;
+            const int gx = bx + oi, gy = by + oj, gz = bz + ok;
+            atomicAdd(k.gmv + ((size_t)gx * k.ng + gy) * k.ng + gz, make_float4(a0, a1, a2, a3));
+            mark_block(k, gx >> 2, gy >> 2, gz >> 2);
         }
     }
 }

@@ -55,12 +55,25 @@ NAME_PARAMS = {
 }
 
 
-def blob_scene(cls, material_key, n_grid=48, grid_lim=0.4, fused=True, cup=False, box=False, n=2000, **kw):
-    """A falling blob on a separable floor with domain walls (the fused-pipeline test
-    scene, tests/test_fused_pipeline.py:27-56), optionally with a moving cup or a
-    descending plate."""
+def spin_velocity(pts, lin=(0.3, 0.1, -0.4), omega=(0.0, 1.0, 3.0)):
+    """A translating, spinning initial velocity field v0 = lin + omega x (x - centroid)."""
+    c = pts.mean(axis=0)
+    return (np.asarray(lin, np.float32) + np.cross(np.asarray(omega, np.float32), pts - c)).astype(np.float32)
+
+
+def blob_scene(cls, material_key, n_grid=48, grid_lim=0.4, fused=True, cup=False, box=False, n=2000, v0=False,
+               **kw):
+    """A blob on a separable floor with domain walls (the fused-pipeline test
+    scene, tests/test_fused_pipeline.py:27-56), optionally thrown with a spinning
+    initial velocity, with a moving cup or a descending plate."""
     pts, vol = blob(n=n)
     s = make(cls, n_grid, grid_lim, fused=fused, **kw).load_particles(pts, vol)
+    if v0:
+        vel = spin_velocity(pts)
+        if cls.__name__ == "OracleSolver":
+            s.a["v"][:] = vel
+        else:
+            s.set_v(vel)
     mat = MATERIALS[material_key]
     if isinstance(mat, str):
         s.set_material(mat, **NAME_PARAMS[mat])
