@@ -210,6 +210,17 @@ int gbmpm_compute_cov(gbmpm_engine *e, float *cov_out, void *stream);
 int gbmpm_profile(gbmpm_engine *e, double ms_out[GBMPM_NUM_PHASES],
                   int64_t count_out[GBMPM_NUM_PHASES], int32_t reset);
 
+/* Edge-guard reduction that allocates nothing (no counterpart in the reference).
+ * For callers that cannot call cudaMalloc: a process whose device memory is owned
+ * by another allocator, or a control loop that must not take cudaMalloc's implicit
+ * synchronization. Same out[7] as gbmpm_guard, over device arrays x, v of [n][3]
+ * floats, plus *nonfinite = 1 when a position is not finite. Scratch is a 33 KB
+ * static device array, so n <= 4194304 (larger n: GBMPM_ERR_ARG). Calls that
+ * overlap on the GPU race on that array. The first call on a device looks up its
+ * address; make it before any stream capture. Synchronizes the stream. */
+int gbmpm_guard_noalloc(const float *x, const float *v, int32_t n, float out[7], int32_t *nonfinite,
+                        void *stream);
+
 /* Number of kernels this engine has launched (graph replays count each node). */
 int64_t gbmpm_launch_count(gbmpm_engine *e);
 

@@ -111,6 +111,8 @@ _SIGNATURES = {
     "gbmpm_compute_R": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "gbmpm_compute_cov": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "gbmpm_profile": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_int32]),
+    "gbmpm_guard_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_float),
+                                      C.POINTER(C.c_int32), C.c_void_p]),
     "gbmpm_launch_count": (C.c_int64, [C.c_void_p]),
 }
 

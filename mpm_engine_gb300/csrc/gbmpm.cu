@@ -2174,3 +2174,141 @@ int gbmpm_profile(gbmpm_engine *e, double ms_out[GBMPM_NUM_PHASES], int64_t coun
 int64_t gbmpm_launch_count(gbmpm_engine *e) { return e ? e->launches : 0; }
 
 }  // extern "C"
+
+// ======================= gbmpm_guard_noalloc: the edge-guard reduction for callers that cannot allocate
+//
+// gbmpm_guard (above) reduces min/max of the particle positions and max |v|
+// into scratch that the engine allocated with cudaMalloc. Some callers cannot
+// allow that: a process whose device memory is entirely owned by another
+// allocator (a framework that reserves the device up front), or a control loop
+// that must never hit cudaMalloc's implicit device synchronization between
+// ticks. gbmpm_guard_noalloc computes the same seven numbers with no engine and
+// no allocation: its scratch is the file-scope array below, reserved when the
+// library is loaded and held by every GPU that loads it until the process exits.
+//
+// Limits and sharing:
+//  * at most kMaxParticles particles per call (larger n is rejected with
+//    GBMPM_ERR_ARG);
+//  * every call uses the same array; calls that overlap on the GPU (two streams,
+//    two threads) race on it and must be serialized by the caller;
+//  * nothing in the array needs to start at zero: each call writes every slot
+//    it later reads.
+//  * the first call on a device looks up the array's device address
+//    (cudaGetSymbolAddress); make that first call before any stream capture.
+
+#include <mutex>
+
+namespace noalloc {
+
+constexpr int kThreads = 256;
+constexpr int kPerThread = 16;
+constexpr int kMaxBlocks = 1024;
+constexpr int kSlot = 8;  // min xyz, max xyz, max |v|, non-finite flag
+constexpr long long kMaxParticles = (long long)kMaxBlocks * kThreads * kPerThread;   // 4,194,304
+
+// per-block partial results, then the final record at slot kMaxBlocks (33 KB)
+static __device__ __align__(256) float g_guard_scratch[(kMaxBlocks + 1) * kSlot];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mutex;
+float *g_scratch_ptr[kMaxDevices] = {nullptr};
+
+__device__ __forceinline__ float wmin(float x) {
+    for (int o = 16; o > 0; o >>= 1) x = fminf(x, __shfl_xor_sync(0xffffffffu, x, o));
+    return x;
+}
+__device__ __forceinline__ float wmax(float x) {
+    for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+    return x;
+}
+
+// one block reduces its contiguous slice of at most kThreads * kPerThread particles
+__global__ void __launch_bounds__(kThreads) k_guard_partials(const float *x, const float *v, int n, float *scratch) {
+    __shared__ float s[kThreads / 32][kSlot];
+    float r[kSlot] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0.0f, 0.0f};
+    const long long begin = (long long)blockIdx.x * kThreads * kPerThread;
+    for (int i = 0; i < kPerThread; ++i) {
+        long long p = begin + (long long)i * kThreads + threadIdx.x;
+        if (p >= n) break;
+        for (int a = 0; a < 3; ++a) {
+            float xa = x[3 * p + a];
+            if (!isfinite(xa)) r[7] = 1.0f;
+            r[a] = fminf(r[a], xa);
+            r[3 + a] = fmaxf(r[3 + a], xa);
+            r[6] = fmaxf(r[6], fabsf(v[3 * p + a]));
+        }
+    }
+    for (int a = 0; a < 3; ++a) { r[a] = wmin(r[a]); r[3 + a] = wmax(r[3 + a]); }
+    r[6] = wmax(r[6]);
+    r[7] = wmax(r[7]);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int a = 0; a < kSlot; ++a) s[w][a] = r[a];
+    __syncthreads();
+    if (threadIdx.x < kSlot) {
+        const int a = threadIdx.x;
+        float acc = s[0][a];
+        for (int ww = 1; ww < kThreads / 32; ++ww)
+            acc = (a < 3) ? fminf(acc, s[ww][a]) : fmaxf(acc, s[ww][a]);
+        scratch[blockIdx.x * kSlot + a] = acc;
+    }
+}
+
+// one block folds the per-block partials into the final record
+__global__ void __launch_bounds__(32) k_guard_final(float *scratch, int nblocks) {
+    const int a = threadIdx.x;
+    if (a >= kSlot) return;
+    float acc = (a < 3) ? INFINITY : ((a < 6) ? -INFINITY : 0.0f);
+    for (int b = 0; b < nblocks; ++b) {
+        float val = scratch[b * kSlot + a];
+        acc = (a < 3) ? fminf(acc, val) : fmaxf(acc, val);
+    }
+    scratch[kMaxBlocks * kSlot + a] = acc;
+}
+
+// device address of the scratch array for the current device, looked up once
+int scratch_for_current_device(float **out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return fail(GBMPM_ERR_CUDA, "no current CUDA device");
+    if (dev < 0 || dev >= kMaxDevices) return fail(GBMPM_ERR_ARG, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if (!g_scratch_ptr[dev]) {
+        float *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_guard_scratch);
+        if (e != cudaSuccess || !ptr) return fail(GBMPM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_scratch_ptr[dev] = ptr;
+    }
+    *out = g_scratch_ptr[dev];
+    return GBMPM_OK;
+}
+
+}  // namespace noalloc
+
+extern "C" {
+
+// out = {min x, min y, min z, max x, max y, max z, max |v_i|} over n particles
+// (device pointers x, v of [n][3] floats), *nonfinite = 1 when any position is
+// not finite. Host out; synchronizes the stream. No allocation of any kind.
+int gbmpm_guard_noalloc(const float *x, const float *v, int32_t n, float out[7], int32_t *nonfinite,
+                        void *stream) {
+    using namespace noalloc;
+    if ((long long)n > kMaxParticles)
+        return fail(GBMPM_ERR_ARG, "gbmpm_guard_noalloc handles at most 4194304 particles per call");
+    if (!out || n < 0 || (n > 0 && (!x || !v))) return fail(GBMPM_ERR_ARG, "bad argument");
+    float *scratch = nullptr;
+    int rc = noalloc::scratch_for_current_device(&scratch);
+    if (rc != GBMPM_OK) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int nblocks = n > 0 ? (int)((n + (long long)kThreads * kPerThread - 1) / ((long long)kThreads * kPerThread)) : 0;
+    if (nblocks > 0) k_guard_partials<<<nblocks, kThreads, 0, s>>>(x, v, n, scratch);
+    k_guard_final<<<1, 32, 0, s>>>(scratch, nblocks);
+    float h[kSlot];
+    cudaError_t e = cudaMemcpyAsync(h, scratch + kMaxBlocks * kSlot, kSlot * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(GBMPM_ERR_CUDA, std::string("gbmpm_guard_noalloc: ") + cudaGetErrorString(e));
+    for (int i = 0; i < 7; ++i) out[i] = h[i];
+    if (nonfinite) *nonfinite = h[7] != 0.0f ? 1 : 0;
+    return GBMPM_OK;
+}
+
+}  // extern "C"
