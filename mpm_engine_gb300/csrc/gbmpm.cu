@@ -29,6 +29,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -444,44 +445,72 @@ __device__ __forceinline__ void mark_block(const PK &k, int bx, int by, int bz) 
 
 // G2P for one particle (g2p_particle, mpm_utils.py:944-1043) with the grid
 // velocity supplied by `fetch(ix, iy, iz)` (global memory or a shared tile).
+// The 27-node sums v = sum w g, C = 4/dx sum w g (x_i - x_p)^T / dx and
+// L = sum g grad(w)^T are evaluated axis by axis (z, then y, then x): the
+// quadratic weights are separable, so the 7 moment sums cost 441 FMAs instead of
+// 27 x 21.
 template <class Fetch>
 __device__ __forceinline__ void g2p_core(const PK &k, const Stencil &s, Fetch fetch, float *v, float *C, float *L) {
-    float nv[3] = {0.f, 0.f, 0.f};
+    float zw[3], zd[3], zg[3];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) { C[i] = 0.f; L[i] = 0.f; }
-    const float c4 = k.inv_dx * 4.0f;
+    for (int kk = 0; kk < 3; ++kk) {
+        zw[kk] = s.w[2][kk];
+        zd[kk] = s.w[2][kk] * ((float)kk - s.fx[2]);
+        zg[kk] = s.dw[2][kk];
+    }
+    float V0[3] = {0.f, 0.f, 0.f}, SX[3] = {0.f, 0.f, 0.f}, SY[3] = {0.f, 0.f, 0.f}, SZ[3] = {0.f, 0.f, 0.f};
+    float GX[3] = {0.f, 0.f, 0.f}, GY[3] = {0.f, 0.f, 0.f}, GZ[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
+        float B0[3] = {0.f, 0.f, 0.f}, BY[3] = {0.f, 0.f, 0.f}, BDY[3] = {0.f, 0.f, 0.f};
+        float BZ[3] = {0.f, 0.f, 0.f}, BDZ[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            float wij = s.w[0][i] * s.w[1][j];
-            float dwi_j = s.dw[0][i] * s.w[1][j];
-            float wi_dj = s.w[0][i] * s.dw[1][j];
+            float A0[3] = {0.f, 0.f, 0.f}, AZ[3] = {0.f, 0.f, 0.f}, ADZ[3] = {0.f, 0.f, 0.f};
 #pragma unroll
             for (int kk = 0; kk < 3; ++kk) {
                 float4 g = fetch(i, j, kk);
-                float wt = wij * s.w[2][kk];
-                float dp0 = (float)i - s.fx[0], dp1 = (float)j - s.fx[1], dp2 = (float)kk - s.fx[2];
-                float gx = dwi_j * s.w[2][kk] * k.inv_dx;
-                float gy = wi_dj * s.w[2][kk] * k.inv_dx;
-                float gz = wij * s.dw[2][kk] * k.inv_dx;
-                float cw = wt * c4;
-                float gvv[3] = {g.x, g.y, g.z};
+                const float gv[3] = {g.x, g.y, g.z};
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
-                    nv[a] += gvv[a] * wt;
-                    float ga = gvv[a] * cw;
-                    C[3 * a + 0] += ga * dp0;
-                    C[3 * a + 1] += ga * dp1;
-                    C[3 * a + 2] += ga * dp2;
-                    L[3 * a + 0] += gvv[a] * gx;
-                    L[3 * a + 1] += gvv[a] * gy;
-                    L[3 * a + 2] += gvv[a] * gz;
+                    A0[a] += zw[kk] * gv[a];
+                    AZ[a] += zd[kk] * gv[a];
+                    ADZ[a] += zg[kk] * gv[a];
                 }
             }
+            const float wy = s.w[1][j], wyd = s.w[1][j] * ((float)j - s.fx[1]), dwy = s.dw[1][j];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                B0[a] += wy * A0[a];
+                BY[a] += wyd * A0[a];
+                BDY[a] += dwy * A0[a];
+                BZ[a] += wy * AZ[a];
+                BDZ[a] += wy * ADZ[a];
+            }
+        }
+        const float wx = s.w[0][i], wxd = s.w[0][i] * ((float)i - s.fx[0]), dwx = s.dw[0][i];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            V0[a] += wx * B0[a];
+            SX[a] += wxd * B0[a];
+            SY[a] += wx * BY[a];
+            SZ[a] += wx * BZ[a];
+            GX[a] += dwx * B0[a];
+            GY[a] += wx * BDY[a];
+            GZ[a] += wx * BDZ[a];
         }
     }
-    v[0] = nv[0]; v[1] = nv[1]; v[2] = nv[2];
+    const float c4 = k.inv_dx * 4.0f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        v[a] = V0[a];
+        C[3 * a + 0] = SX[a] * c4;
+        C[3 * a + 1] = SY[a] * c4;
+        C[3 * a + 2] = SZ[a] * c4;
+        L[3 * a + 0] = GX[a] * k.inv_dx;
+        L[3 * a + 1] = GY[a] * k.inv_dx;
+        L[3 * a + 2] = GZ[a] * k.inv_dx;
+    }
 }
 
 // advection, F_trial and covariance after the gather
@@ -684,7 +713,7 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
 //    run, and no shared-memory atomics are needed.
 constexpr int kTileThreads = 256;
 constexpr int kGatherCap = 1536;          // nodes in the shared gather tile (24 KB)
-constexpr int kRec = 25;                  // floats per particle scatter record
+constexpr int kRec = 40;                  // floats per particle scatter record (10 float4)
 constexpr int kSmemFloats = (kGatherCap * 4 > kTileThreads * kRec) ? kGatherCap * 4 : kTileThreads * kRec;
 
 struct TileBox {
@@ -736,8 +765,8 @@ __device__ __forceinline__ void bspline_o(float fx, int o, float &w, float &dw) 
     dw = (o == 0) ? -t0 : ((o == 1) ? -2.0f * t1 : t2);
 }
 
-template <bool SOLIDS>
-__global__ void __launch_bounds__(kTileThreads) k_particles_tiled(PK k, int mode) {
+template <bool SOLIDS, int MINB>
+__global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, int mode) {
     __shared__ __align__(16) float s_mem[kSmemFloats];
     __shared__ int s_key[kTileThreads];
     __shared__ int s_seg[kTileThreads + 1];
@@ -827,7 +856,8 @@ __global__ void __launch_bounds__(kTileThreads) k_particles_tiled(PK k, int mode
         set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
         want = false;
     }
-    // ---- scatter record: fx, affine momentum base, m C dx, stress term A, m
+    // ---- scatter record: per-axis weights w[3][3] and dw[3][3], the affine momentum
+    // base m v - m C fx dx, m C dx, the stress term A = -vol dt/dx stress, and m
     if (want) {
         float Cr[9];
 #pragma unroll
@@ -842,16 +872,22 @@ __global__ void __launch_bounds__(kTileThreads) k_particles_tiled(PK k, int mode
         }
         const float m = k.mass[p];
         const float fs = -k.vol[p] * k.dt * k.inv_dx;
-        float *r = s_mem + t * kRec;
-        r[0] = s.fx[0]; r[1] = s.fx[1]; r[2] = s.fx[2];
+        float rec[kRec];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int o = 0; o < 3; ++o) { rec[3 * a + o] = s.w[a][o]; rec[9 + 3 * a + o] = s.dw[a][o]; }
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             float c0 = m * Cr[3 * a] * k.dx, c1 = m * Cr[3 * a + 1] * k.dx, c2 = m * Cr[3 * a + 2] * k.dx;
-            r[3 + a] = m * v[a] - (c0 * s.fx[0] + c1 * s.fx[1] + c2 * s.fx[2]);
-            r[6 + 3 * a] = c0; r[7 + 3 * a] = c1; r[8 + 3 * a] = c2;
-            r[15 + 3 * a] = fs * S[3 * a]; r[16 + 3 * a] = fs * S[3 * a + 1]; r[17 + 3 * a] = fs * S[3 * a + 2];
+            rec[18 + a] = m * v[a] - (c0 * s.fx[0] + c1 * s.fx[1] + c2 * s.fx[2]);
+            rec[21 + 3 * a] = c0; rec[22 + 3 * a] = c1; rec[23 + 3 * a] = c2;
+            rec[30 + 3 * a] = fs * S[3 * a]; rec[31 + 3 * a] = fs * S[3 * a + 1]; rec[32 + 3 * a] = fs * S[3 * a + 2];
         }
-        r[24] = m;
+        rec[39] = m;
+        float4 *dst = reinterpret_cast<float4 *>(s_mem + t * kRec);
+#pragma unroll
+        for (int q = 0; q < kRec / 4; ++q) dst[q] = make_float4(rec[4 * q], rec[4 * q + 1], rec[4 * q + 2], rec[4 * q + 3]);
         s_key[t] = (s.b[0] * k.ng + s.b[1]) * k.ng + s.b[2];
     } else {
         s_key[t] = -1 - t;   // a dead slot forms its own, skipped run
@@ -871,32 +907,65 @@ __global__ void __launch_bounds__(kTileThreads) k_particles_tiled(PK k, int mode
     if (head) s_seg[off + __popc(bal & ((1u << lane) - 1u))] = t;
     if (t == 0) s_seg[total] = kTileThreads;
     __syncthreads();
-    // ---- 27 lanes per run, one node each
-    const int oi = lane / 9, oj = (lane / 3) % 3, ok = lane % 3;
+    // ---- runs: lane = (particle group g, node line (i,j)); each lane sums three
+    // nodes k = 0..2 of its line for particles q0+g, q0+g+3, ...; the three groups
+    // are folded with shuffles and lanes 0..8 deposit
+    const int g3 = lane / 9, li = (lane % 9) / 3, lj = lane % 3;
+    const float fi = (float)li, fj = (float)lj;
     for (int sg = warp; sg < total; sg += kTileThreads / 32) {
         const int q0 = s_seg[sg], q1 = s_seg[sg + 1];
         const int key = s_key[q0];
-        if (key < 0 || lane >= 27) continue;
-        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-        for (int q = q0; q < q1; ++q) {
-            const float *r = s_mem + q * kRec;
-            float wx, dwx, wy, dwy, wz, dwz;
-            bspline_o(r[0], oi, wx, dwx);
-            bspline_o(r[1], oj, wy, dwy);
-            bspline_o(r[2], ok, wz, dwz);
-            const float wt = wx * wy * wz;
-            const float gx = dwx * wy * wz, gy = wx * dwy * wz, gz = wx * wy * dwz;
-            const float fi = (float)oi, fj = (float)oj, fk = (float)ok;
-            a0 += wt * (r[3] + r[6] * fi + r[7] * fj + r[8] * fk) + (r[15] * gx + r[16] * gy + r[17] * gz);
-            a1 += wt * (r[4] + r[9] * fi + r[10] * fj + r[11] * fk) + (r[18] * gx + r[19] * gy + r[20] * gz);
-            a2 += wt * (r[5] + r[12] * fi + r[13] * fj + r[14] * fk) + (r[21] * gx + r[22] * gy + r[23] * gz);
-            a3 += wt * r[24];
+        if (key < 0) continue;   // uniform across the warp
+        float acc[3][4];
+#pragma unroll
+        for (int kk = 0; kk < 3; ++kk) acc[kk][0] = acc[kk][1] = acc[kk][2] = acc[kk][3] = 0.f;
+        if (lane < 27) {
+            for (int q = q0 + g3; q < q1; q += 3) {
+                const float *r = s_mem + q * kRec;
+                const float wxi = r[li], wyj = r[3 + lj], dwxi = r[9 + li], dwyj = r[12 + lj];
+                const float u = wxi * wyj, ux = dwxi * wyj, uy = wxi * dwyj;
+                const float wz0 = r[6], wz1 = r[7], wz2 = r[8], dz0 = r[15], dz1 = r[16], dz2 = r[17];
+                const float m = r[39];
+                float P[3], Q[3], R[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    P[a] = u * (r[18 + a] + r[21 + 3 * a] * fi + r[22 + 3 * a] * fj) + r[30 + 3 * a] * ux +
+                           r[31 + 3 * a] * uy;
+                    Q[a] = u * r[23 + 3 * a];
+                    R[a] = u * r[32 + 3 * a];
+                }
+                const float um = u * m;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    acc[0][a] += wz0 * P[a] + dz0 * R[a];
+                    acc[1][a] += wz1 * (P[a] + Q[a]) + dz1 * R[a];
+                    acc[2][a] += wz2 * (P[a] + 2.0f * Q[a]) + dz2 * R[a];
+                }
+                acc[0][3] += wz0 * um;
+                acc[1][3] += wz1 * um;
+                acc[2][3] += wz2 * um;
+            }
         }
-        if (a0 != 0.f || a1 != 0.f || a2 != 0.f || a3 != 0.f) {
+#pragma unroll
+        for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                float x9 = __shfl_down_sync(0xffffffffu, acc[kk][c], 9);
+                float x18 = __shfl_down_sync(0xffffffffu, acc[kk][c], 18);
+                acc[kk][c] += x9 + x18;
+            }
+        if (lane < 9) {
             const int bz = key % k.ng, rr = key / k.ng, by = rr % k.ng, bx = rr / k.ng;
-            const int gx = bx + oi, gy = by + oj, gz = bz + ok;
-            atomicAdd(k.gmv + ((size_t)gx * k.ng + gy) * k.ng + gz, make_float4(a0, a1, a2, a3));
-            mark_block(k, gx >> 2, gy >> 2, gz >> 2);
+            const int gx = bx + li, gy = by + lj;
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk) {
+                if (acc[kk][0] != 0.f || acc[kk][1] != 0.f || acc[kk][2] != 0.f || acc[kk][3] != 0.f) {
+                    const int gz = bz + kk;
+                    atomicAdd(k.gmv + ((size_t)gx * k.ng + gy) * k.ng + gz,
+                              make_float4(acc[kk][0], acc[kk][1], acc[kk][2], acc[kk][3]));
+                    mark_block(k, gx >> 2, gy >> 2, gz >> 2);
+                }
+            }
         }
     }
 }
@@ -1534,6 +1603,7 @@ struct gbmpm_engine {
     cudaEvent_t pose_done = nullptr;
     int bd = 0;
     int num_sms = 148;
+    int tile_occ = 3;       // resident CTAs per SM the tiled particle kernel is compiled for
     // graph cache
     cudaGraphExec_t graph = nullptr;
     int g_substeps = -1, g_flags = -1;
@@ -1578,8 +1648,11 @@ bool has_solids(const gbmpm_model &m) {
 void launch_particles(gbmpm_engine *e, const PK &k, int mode, bool tiled, cudaStream_t s) {
     if (tiled) {
         int grid = std::max(1, (k.n + kTileThreads - 1) / kTileThreads);
-        if (has_solids(e->M)) k_particles_tiled<true><<<grid, kTileThreads, 0, s>>>(k, mode);
-        else k_particles_tiled<false><<<grid, kTileThreads, 0, s>>>(k, mode);
+        const bool solids = has_solids(e->M);
+        if (solids && e->tile_occ >= 3) k_particles_tiled<true, 3><<<grid, kTileThreads, 0, s>>>(k, mode);
+        else if (solids) k_particles_tiled<true, 2><<<grid, kTileThreads, 0, s>>>(k, mode);
+        else if (e->tile_occ >= 3) k_particles_tiled<false, 3><<<grid, kTileThreads, 0, s>>>(k, mode);
+        else k_particles_tiled<false, 2><<<grid, kTileThreads, 0, s>>>(k, mode);
     } else {
         int grid = std::max(1, (k.n + kParticleThreads - 1) / kParticleThreads);
         if (has_solids(e->M)) k_particles<true><<<grid, kParticleThreads, 0, s>>>(k, mode);
@@ -1831,6 +1904,7 @@ int gbmpm_engine_create(gbmpm_engine **out) {
     gbmpm_engine *e = new gbmpm_engine();
     if (cudaGetDevice(&e->device) != cudaSuccess) { delete e; return fail(GBMPM_ERR_CUDA, "no CUDA device"); }
     cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, e->device);
+    if (const char *occ = std::getenv("GBMPM_TILE_OCC")) e->tile_occ = std::atoi(occ);
     if (cudaEventCreateWithFlags(&e->pose_done, cudaEventDisableTiming) != cudaSuccess) {
         delete e;
         return fail(GBMPM_ERR_CUDA, "event create failed");
