@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-scenes", type=int, default=64)
     return ap.parse_args()
 
 
@@ -152,6 +154,43 @@ def build_workload(name: str, n_grid: int, solver_cls, **kw):
                 "grid_lim": 1.0}
         return s, frame, s.n_particles, S, desc
     raise SystemExit(f"unknown workload {name}")
+
+
+def batched_measure(n_scenes: int, ticks: int, substeps: int = 100, dt: float = 1.0e-5, device: str = "cuda:0"):
+    """Batched forward workload: n_scenes seeded dough-squeeze scenes (8k..120k
+    particles, 48^3..128^3 grids, per-scene E, nu, yield, von Mises or elastic,
+    plate at 0.05 m/s). One scene-tick = `substeps` substeps of one scene. The plain
+    path steps the Solvers one after another (the reference's serial rollouts); the
+    batched path advances all scenes in one CUDA graph."""
+    import torch
+    from mpm_engine_gb300 import BatchSolver, Solver
+    from mpm_engine_gb300.scenes import squeeze_batch_specs, squeeze_from_spec
+    specs = squeeze_batch_specs(n_scenes)
+    scenes = [squeeze_from_spec(Solver, sp, device=device)[0] for sp in specs]
+    n_part = sum(sc.n_particles for sc in scenes)
+    batch = BatchSolver(scenes)
+    for sc in scenes:                      # warm-up: capture each scene's own graph
+        sc.step(dt, substeps)
+    batch.step(dt, substeps)               # warm-up: capture the batch graph
+    torch.cuda.synchronize()
+
+    def timed(fn):
+        t0 = time.perf_counter()
+        for _ in range(ticks):
+            fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    t_plain = timed(lambda: [sc.step(dt, substeps) for sc in scenes])
+    launches0 = batch.launch_count()
+    t_batch = timed(lambda: batch.step(dt, substeps))
+    rate_b = n_scenes * ticks / t_batch
+    rate_p = n_scenes * ticks / t_plain
+    return {"metric": "batched forward scene-ticks/s", "unit": f"scene-ticks/s ({substeps} substeps each)",
+            "value": rate_b, "plain_value": rate_p, "speedup_vs_plain": rate_b / rate_p,
+            "scenes": n_scenes, "particles_total": n_part, "ticks": ticks, "dt": dt,
+            "particle_substeps_per_s": n_part * substeps * ticks / t_batch,
+            "gpu_launches": batch.launch_count() - launches0}
 
 
 def dist_setup(args):
@@ -298,6 +337,10 @@ def main():
         e2e = {"value": world * n * S * reps / el, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 12,
                "d2h_bytes_per_step": n * 12}
 
+    batched = None
+    if not args.no_batched:
+        batched = batched_measure(args.batch_scenes, ticks=max(2, min(args.steps, 4)), device=f"cuda:{local}")
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(s.export_state(), desc, args.cpu_seconds)
@@ -309,7 +352,7 @@ def main():
                 "config": {**desc, "l2": "256 MB buffer written between timed steps", "parallelism":
                            "replicas" if world > 1 else "single"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk}
+                "clocks": clk, "batched": batched}
         print(json.dumps(line))
     if dist:
         dist.barrier()

@@ -210,6 +210,20 @@ int gbmpm_compute_cov(gbmpm_engine *e, float *cov_out, void *stream);
 int gbmpm_profile(gbmpm_engine *e, double ms_out[GBMPM_NUM_PHASES],
                   int64_t count_out[GBMPM_NUM_PHASES], int32_t reset);
 
+/* Batched scenes (no counterpart in the reference, whose planners step one
+ * Solver at a time): a batch advances many independent engines in one CUDA graph
+ * whose branches are the scenes' tick chains, so scenes too small to fill the GPU
+ * run concurrently. times[n] are the scenes' clocks. Without GBMPM_TICK_GRAPH the
+ * scenes are recorded one after another on the stream (the serial baseline).
+ * gbmpm_batch_guard runs every scene's edge guard with one synchronization:
+ * out[n][7] and status[n] as in gbmpm_guard. */
+typedef struct gbmpm_batch gbmpm_batch;
+int gbmpm_batch_create(gbmpm_engine *const *engines, int32_t n, gbmpm_batch **out);
+void gbmpm_batch_destroy(gbmpm_batch *b);
+int gbmpm_batch_tick(gbmpm_batch *b, double *times, double dt, int32_t substeps, int32_t flags, void *stream);
+int gbmpm_batch_guard(gbmpm_batch *b, float *out, uint32_t *status, void *stream);
+int64_t gbmpm_batch_launch_count(gbmpm_batch *b);
+
 /* Edge-guard reduction that allocates nothing (no counterpart in the reference).
  * For callers that cannot call cudaMalloc: a process whose device memory is owned
  * by another allocator, or a control loop that must not take cudaMalloc's implicit

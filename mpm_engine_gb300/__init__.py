@@ -14,11 +14,11 @@ from .geometry import SDFData, analytic_sdf, load_sdf, save_sdf
 from .glass import GlassProfile, cup_fill, glass_sdf_local, quat_from_axis_angle, quat_mul, quat_to_mat
 from .materials import Material, elastic, granular, newtonian, tabulated_viscous, vonmises
 from .scenes import block, dam_break_lattice, dough
-from .solver import GridConfig, Solver
+from .solver import BatchSolver, GridConfig, Solver
 
 __version__ = "0.1.0"
 __all__ = [
-    "GlassProfile", "GridConfig", "Material", "SDFData", "Solver", "__version__", "analytic_sdf", "block",
+    "BatchSolver", "GlassProfile", "GridConfig", "Material", "SDFData", "Solver", "__version__", "analytic_sdf", "block",
     "cup_fill", "dam_break_lattice", "dough", "elastic", "glass_sdf_local", "granular", "load_sdf", "newtonian",
     "quat_from_axis_angle", "quat_mul", "quat_to_mat", "save_sdf", "tabulated_viscous", "vonmises",
 ]

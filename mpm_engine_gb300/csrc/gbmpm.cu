@@ -117,6 +117,23 @@ __device__ __forceinline__ void mat_store(float *p, const float (&m)[9]) {
 #pragma unroll
     for (int i = 0; i < 9; ++i) p[i] = m[i];
 }
+// Particle fields are either the caller's records (AoS: W floats per particle)
+// or the engine's working copy (SoA: component c of particle p at c*n + p, so a
+// warp's access to one component is one coalesced line).
+template <bool SOA, int W>
+__device__ __forceinline__ void fld_load(const float *base, int n, int p, float *out) {
+#pragma unroll
+    for (int c = 0; c < W; ++c) out[c] = SOA ? base[(size_t)c * n + p] : base[(size_t)p * W + c];
+}
+template <bool SOA, int W>
+__device__ __forceinline__ void fld_store(float *base, int n, int p, const float *in) {
+#pragma unroll
+    for (int c = 0; c < W; ++c) {
+        if (SOA) base[(size_t)c * n + p] = in[c];
+        else base[(size_t)p * W + c] = in[c];
+    }
+}
+
 __device__ __forceinline__ void mm(const float *a, const float *b, float *c) {
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -514,6 +531,7 @@ __device__ __forceinline__ void g2p_core(const PK &k, const Stencil &s, Fetch fe
 }
 
 // advection, F_trial and covariance after the gather
+template <bool SOA>
 __device__ __forceinline__ void g2p_finish(const PK &k, int p, float *x, const float *v, const float *L, float *Ft) {
     float xn[3];
 #pragma unroll
@@ -526,12 +544,13 @@ __device__ __forceinline__ void g2p_finish(const PK &k, int p, float *x, const f
 #pragma unroll
     for (int a = 0; a < 3; ++a) x[a] = xn[a];
     float Fo[9], A[9];
-    mat_load(k.F + 9 * (size_t)p, Fo);
+    fld_load<SOA, 9>(k.F, k.n, p, Fo);
 #pragma unroll
     for (int i = 0; i < 9; ++i) A[i] = ((i % 4 == 0) ? 1.0f : 0.0f) + L[i] * k.dt;
     mm(A, Fo, Ft);
     if (k.update_cov && k.cov) {
-        float *c6 = k.cov + 6 * (size_t)p;
+        float c6[6];
+        fld_load<SOA, 6>(k.cov, k.n, p, c6);
         float cn[9] = {c6[0], c6[1], c6[2], c6[1], c6[3], c6[4], c6[2], c6[4], c6[5]};
         float a1[9], a2[9];
         mm(L, cn, a1);
@@ -542,6 +561,7 @@ __device__ __forceinline__ void g2p_finish(const PK &k, int p, float *x, const f
         c6[3] = cn[4] + k.dt * (a1[4] + a2[4]);
         c6[4] = cn[5] + k.dt * (a1[5] + a2[5]);
         c6[5] = cn[8] + k.dt * (a1[8] + a2[8]);
+        fld_store<SOA, 6>(k.cov, k.n, p, c6);
     }
 }
 
@@ -655,7 +675,7 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
             return;
         }
         g2p_core(k, s, [&](int i, int j, int kk) { return global_fetch(k, s, i, j, kk); }, v, C, L);
-        g2p_finish(k, p, x, v, L, Ft);
+        g2p_finish<false>(k, p, x, v, L, Ft);
         gathered = true;
     }
     if (gathered) {
@@ -782,7 +802,7 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
     bool live = p < k.n && !(k.sel && k.sel[p] != 0);
     const int mat = live ? k.mat[p] : 0;
     float x[3] = {0.f, 0.f, 0.f};
-    if (live) { x[0] = k.x[3 * p]; x[1] = k.x[3 * p + 1]; x[2] = k.x[3 * p + 2]; }
+    if (live) fld_load<true, 3>(k.x, k.n, p, x);
     float v[3] = {0.f, 0.f, 0.f}, C[9], L[9], Ft[9], S[9];
     bool gathered = false;
     if (mode & PASS_G2P) {
@@ -815,38 +835,35 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
             g2p_core(k, s, [&](int i, int j, int kk) { return global_fetch(k, s, i, j, kk); }, v, C, L);
         }
         if (want) {
-            g2p_finish(k, p, x, v, L, Ft);
+            g2p_finish<true>(k, p, x, v, L, Ft);
             gathered = true;
-            float *xo = k.x + 3 * (size_t)p;
-            xo[0] = x[0]; xo[1] = x[1]; xo[2] = x[2];
+            fld_store<true, 3>(k.x, k.n, p, x);
             if (!(mode & (PASS_STRESS | PASS_P2G)) || (mode & PASS_STORE_VC)) {
-                float *vo = k.v + 3 * (size_t)p;
-                vo[0] = v[0]; vo[1] = v[1]; vo[2] = v[2];
-                mat_store(k.C + 9 * (size_t)p, C);
+                fld_store<true, 3>(k.v, k.n, p, v);
+                fld_store<true, 9>(k.C, k.n, p, C);
             }
             if (!(mode & PASS_STRESS)) {
-                mat_store(k.L + 9 * (size_t)p, L);
-                mat_store(k.Ft + 9 * (size_t)p, Ft);
+                fld_store<true, 9>(k.L, k.n, p, L);
+                fld_store<true, 9>(k.Ft, k.n, p, Ft);
             }
         }
     }
     if ((mode & PASS_STRESS) && live) {
         if (!gathered) {
-            mat_load(k.Ft + 9 * (size_t)p, Ft);
-            mat_load(k.L + 9 * (size_t)p, L);
+            fld_load<true, 9>(k.Ft, k.n, p, Ft);
+            fld_load<true, 9>(k.L, k.n, p, L);
         }
         float Fn[9];
         stress_update<SOLIDS>(k, p, mat, Ft, L, Fn, S);
-        mat_store(k.F + 9 * (size_t)p, Fn);
-        if (mode & PASS_STORE_ALL) mat_store(k.S + 9 * (size_t)p, S);
+        fld_store<true, 9>(k.F, k.n, p, Fn);
+        if (mode & PASS_STORE_ALL) fld_store<true, 9>(k.S, k.n, p, S);
     }
     if (!(mode & PASS_P2G)) return;
     if (live) {
-        if (!(mode & PASS_STRESS)) mat_load(k.S + 9 * (size_t)p, S);
+        if (!(mode & PASS_STRESS)) fld_load<true, 9>(k.S, k.n, p, S);
         if (!gathered) {
-            const float *vi = k.v + 3 * (size_t)p;
-            v[0] = vi[0]; v[1] = vi[1]; v[2] = vi[2];
-            mat_load(k.C + 9 * (size_t)p, C);
+            fld_load<true, 3>(k.v, k.n, p, v);
+            fld_load<true, 9>(k.C, k.n, p, C);
         }
     }
     Stencil s;
@@ -1002,6 +1019,7 @@ struct WsTable {
     int nf;
 };
 
+// caller AoS records -> working-copy SoA components, in block-sorted order
 __global__ void k_ws_gather(WsTable T, const int *perm, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -1009,8 +1027,8 @@ __global__ void k_ws_gather(WsTable T, const int *perm, int n) {
     for (int f = 0; f < T.nf; ++f) {
         const int w = T.f[f].width;
         const float *a = T.f[f].ext + src * w;
-        float *b = T.f[f].ws + (size_t)i * w;
-        for (int c = 0; c < w; ++c) b[c] = a[c];
+        float *b = T.f[f].ws + i;
+        for (int c = 0; c < w; ++c) b[(size_t)c * n] = a[c];
     }
 }
 
@@ -1021,9 +1039,9 @@ __global__ void k_ws_scatter(WsTable T, const int *perm, int n) {
     for (int f = 0; f < T.nf; ++f) {
         if (!T.f[f].back) continue;
         const int w = T.f[f].width;
-        const float *a = T.f[f].ws + (size_t)i * w;
+        const float *a = T.f[f].ws + i;
         float *b = T.f[f].ext + dst * w;
-        for (int c = 0; c < w; ++c) b[c] = a[c];
+        for (int c = 0; c < w; ++c) b[c] = a[(size_t)c * n];
     }
 }
 
@@ -1611,6 +1629,7 @@ struct gbmpm_engine {
     double g_dt = 0.0;
     cudaStream_t g_stream = nullptr;
     bool dirty = true;
+    uint64_t version = 1;   // bumped with every change a captured graph depends on
     // profiling
     double prof_ms[GBMPM_NUM_PHASES] = {0};
     int64_t prof_n[GBMPM_NUM_PHASES] = {0};
@@ -1618,6 +1637,11 @@ struct gbmpm_engine {
 };
 
 namespace {
+
+void mark_dirty(gbmpm_engine *e) {
+    e->dirty = true;
+    e->version++;
+}
 
 PK make_pk(gbmpm_engine *e, const gbmpm_particles &P, float dt, int list) {
     PK k{};
@@ -1952,7 +1976,7 @@ int gbmpm_bind(gbmpm_engine *e, const gbmpm_particles *p, const gbmpm_grid *g) {
     GB_CUDA(cudaMemset(g->mv, 0, nn * 16));
     GB_CUDA(cudaMemset(g->v, 0, nn * 16));
     e->bound = true;
-    e->dirty = true;
+    mark_dirty(e);
     e->ws_n = -1;
     return GBMPM_OK;
 }
@@ -1975,7 +1999,7 @@ int gbmpm_set_model(gbmpm_engine *e, const gbmpm_model *m) {
     GB_CUDA(cudaMemcpy(e->d_tab.ptr, &t, sizeof t, cudaMemcpyHostToDevice));
     e->modeled = true;
     e->ws_n = -1;
-    e->dirty = true;
+    mark_dirty(e);
     return GBMPM_OK;
 }
 
@@ -2004,7 +2028,7 @@ int gbmpm_set_colliders(gbmpm_engine *e, const gbmpm_collider *c, int32_t n) {
     }
     if ((size_t)n > old)
         GB_CUDA(cudaMemset(e->d_wrench.ptr + old * 6, 0, (n - old) * 6 * sizeof(double)));
-    e->dirty = true;
+    mark_dirty(e);
     return GBMPM_OK;
 }
 
@@ -2015,19 +2039,19 @@ int gbmpm_get_colliders(gbmpm_engine *e, gbmpm_collider *c, int32_t n) {
     return GBMPM_OK;
 }
 
-int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32_t flags, void *stream) {
+}  // extern "C"
+
+namespace {
+// Everything a tick needs before its launches: argument checks, the float64 pose
+// table for every substep (uploaded on stream s) and the working-set buffers.
+int prepare_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32_t flags, cudaStream_t s,
+                 bool &reorder) {
     int rc = check_ready(e);
     if (rc) return rc;
     if (!time || substeps < 1 || substeps > GBMPM_MAX_SUBSTEPS || !(dt > 0.0))
         return fail(GBMPM_ERR_ARG, "bad tick arguments");
-    cudaStream_t s = (cudaStream_t)stream;
-    if (e->P.n == 0) {
-        for (int i = 0; i < substeps; ++i) *time += dt;
-        return GBMPM_OK;
-    }
     const int nc = (int)e->cols.size();
     const size_t need = (size_t)substeps * std::max(1, nc);
-    // pose table: host integration in float64, one upload per tick
     if (e->h_pose_cap < need) {
         if (e->h_pose) { cudaEventSynchronize(e->pose_done); cudaFreeHost(e->h_pose); }
         e->h_pose = nullptr;
@@ -2036,18 +2060,33 @@ int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32
     }
     PoseRec *old_dev = e->d_pose.ptr;
     GB_CUDA(e->d_pose.ensure(need));
-    if (e->d_pose.ptr != old_dev) e->dirty = true;
+    if (e->d_pose.ptr != old_dev) mark_dirty(e);
     GB_CUDA(cudaEventSynchronize(e->pose_done));
     build_pose_table(e, *time, dt, substeps);
     GB_CUDA(cudaMemcpyAsync(e->d_pose.ptr, e->h_pose, need * sizeof(PoseRec), cudaMemcpyHostToDevice, s));
     GB_CUDA(cudaEventRecord(e->pose_done, s));
-    const bool fused = (flags & GBMPM_TICK_FUSED) != 0;
-    const bool profile = (flags & GBMPM_TICK_PROFILE) != 0;
-    const bool reorder = (flags & GBMPM_TICK_REORDER) && !e->M.periodic_x;
+    reorder = (flags & GBMPM_TICK_REORDER) && !e->M.periodic_x && e->P.n > 0;
     if (reorder && e->ws_n != e->P.n) {
         GB_CUDA(ensure_ws(e));
-        e->dirty = true;
+        mark_dirty(e);
     }
+    return GBMPM_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32_t flags, void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (e && time && e->bound && e->P.n == 0 && substeps >= 1 && dt > 0.0) {
+        for (int i = 0; i < substeps; ++i) *time += dt;
+        return GBMPM_OK;
+    }
+    bool reorder = false;
+    int rc = prepare_tick(e, time, dt, substeps, flags, s, reorder);
+    if (rc) return rc;
+    const bool fused = (flags & GBMPM_TICK_FUSED) != 0;
+    const bool profile = (flags & GBMPM_TICK_PROFILE) != 0;
     const bool use_graph = (flags & GBMPM_TICK_GRAPH) && !profile;
     const float dtf = (float)dt;
     if (!use_graph) {
@@ -2246,6 +2285,145 @@ int gbmpm_profile(gbmpm_engine *e, double ms_out[GBMPM_NUM_PHASES], int64_t coun
 }
 
 int64_t gbmpm_launch_count(gbmpm_engine *e) { return e ? e->launches : 0; }
+
+}  // extern "C"
+
+// ============================================================ batched scenes
+// A batch advances many independent engines (scenes with their own particles,
+// grid, materials and colliders) in one CUDA graph whose branches are the
+// scenes' tick chains. Small scenes that fill a fraction of the GPU each then run
+// concurrently instead of one after another; there is no data exchange between
+// branches.
+struct gbmpm_batch {
+    std::vector<gbmpm_engine *> engines;
+    std::vector<uint64_t> versions;
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> joins;
+    cudaEvent_t fork = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int g_substeps = -1, g_flags = -1;
+    double g_dt = 0.0;
+    int64_t graph_launches = 0;
+    int64_t launches = 0;
+};
+
+extern "C" {
+
+int gbmpm_batch_create(gbmpm_engine *const *engines, int32_t n, gbmpm_batch **out) {
+    if (!engines || !out || n < 1) return fail(GBMPM_ERR_ARG, "bad batch arguments");
+    gbmpm_batch *b = new gbmpm_batch();
+    int dev0 = engines[0] ? engines[0]->device : -1;
+    for (int i = 0; i < n; ++i) {
+        if (!engines[i] || engines[i]->device != dev0) { delete b; return fail(GBMPM_ERR_ARG, "batch engines must be non-null and on one device"); }
+        b->engines.push_back(engines[i]);
+    }
+    b->versions.assign(n, 0);
+    b->streams.assign(n, nullptr);
+    b->joins.assign(n, nullptr);
+    cudaError_t err = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    for (int i = 0; i < n && err == cudaSuccess; ++i) {
+        err = cudaStreamCreateWithFlags(&b->streams[i], cudaStreamNonBlocking);
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(&b->joins[i], cudaEventDisableTiming);
+    }
+    if (err != cudaSuccess) { gbmpm_batch_destroy(b); return fail(GBMPM_ERR_CUDA, cudaGetErrorString(err)); }
+    *out = b;
+    return GBMPM_OK;
+}
+
+void gbmpm_batch_destroy(gbmpm_batch *b) {
+    if (!b) return;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (cudaStream_t st : b->streams) if (st) cudaStreamDestroy(st);
+    for (cudaEvent_t ev : b->joins) if (ev) cudaEventDestroy(ev);
+    if (b->fork) cudaEventDestroy(b->fork);
+    delete b;
+}
+
+int gbmpm_batch_tick(gbmpm_batch *b, double *times, double dt, int32_t substeps, int32_t flags, void *stream) {
+    if (!b || !times) return fail(GBMPM_ERR_ARG, "bad batch tick arguments");
+    if (flags & GBMPM_TICK_PROFILE) return fail(GBMPM_ERR_UNSUPPORTED, "profiling is per engine (gbmpm_tick)");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int n = (int)b->engines.size();
+    std::vector<char> reorder(n, 0);
+    for (int i = 0; i < n; ++i) {
+        bool r = false;
+        int rc = prepare_tick(b->engines[i], &times[i], dt, substeps, flags, s, r);
+        if (rc) return rc;
+        reorder[i] = r;
+    }
+    const bool fused = (flags & GBMPM_TICK_FUSED) != 0;
+    const float dtf = (float)dt;
+    if (!(flags & GBMPM_TICK_GRAPH)) {
+        for (int i = 0; i < n; ++i)
+            if (b->engines[i]->P.n > 0) record_tick(b->engines[i], dtf, substeps, fused, reorder[i], s, false);
+        GB_CUDA(cudaGetLastError());
+        return GBMPM_OK;
+    }
+    bool reuse = b->graph && b->g_substeps == substeps && b->g_flags == flags && b->g_dt == dt;
+    for (int i = 0; i < n && reuse; ++i) reuse = b->versions[i] == b->engines[i]->version;
+    if (!reuse) {
+        if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+        cudaStream_t cap;
+        GB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaGraph_t g = nullptr;
+        GB_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        GB_CUDA(cudaEventRecord(b->fork, cap));
+        int64_t total = 0;
+        for (int i = 0; i < n; ++i) {
+            gbmpm_engine *e = b->engines[i];
+            GB_CUDA(cudaStreamWaitEvent(b->streams[i], b->fork, 0));
+            if (e->P.n > 0) {
+                int64_t before = e->launches;
+                record_tick(e, dtf, substeps, fused, reorder[i], b->streams[i], false);
+                total += e->launches - before;
+                e->launches = before;
+            }
+            GB_CUDA(cudaEventRecord(b->joins[i], b->streams[i]));
+            GB_CUDA(cudaStreamWaitEvent(cap, b->joins[i], 0));
+        }
+        cudaError_t ce = cudaStreamEndCapture(cap, &g);
+        cudaStreamDestroy(cap);
+        if (ce != cudaSuccess) return fail(GBMPM_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(ce));
+        ce = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) { b->graph = nullptr; return fail(GBMPM_ERR_CUDA, "batch graph instantiate failed"); }
+        for (int i = 0; i < n; ++i) b->versions[i] = b->engines[i]->version;
+        b->g_substeps = substeps; b->g_flags = flags; b->g_dt = dt;
+        b->graph_launches = total;
+    }
+    GB_CUDA(cudaGraphLaunch(b->graph, s));
+    b->launches += b->graph_launches;
+    return GBMPM_OK;
+}
+
+int gbmpm_batch_guard(gbmpm_batch *b, float *out, uint32_t *status, void *stream) {
+    if (!b || !out || !status) return fail(GBMPM_ERR_ARG, "null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int n = (int)b->engines.size();
+    std::vector<float> h(8 * (size_t)n);
+    std::vector<unsigned> st(n);
+    for (int i = 0; i < n; ++i) {
+        gbmpm_engine *e = b->engines[i];
+        if (!e->bound) return fail(GBMPM_ERR_STATE, "batch engine not bound");
+        k_guard_init<<<1, 32, 0, s>>>(e->d_guard.ptr);
+        if (e->P.n > 0) {
+            int grid = std::min((e->P.n + 255) / 256, e->num_sms * 4);
+            k_guard<<<grid, 256, 0, s>>>(e->P.x, e->P.v, e->P.n, e->d_guard.ptr, e->d_status.ptr);
+        }
+        GB_CUDA(cudaMemcpyAsync(&h[8 * (size_t)i], e->d_guard.ptr, 7 * sizeof(float), cudaMemcpyDeviceToHost, s));
+        GB_CUDA(cudaMemcpyAsync(&st[i], e->d_status.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+        GB_CUDA(cudaMemsetAsync(e->d_status.ptr, 0, sizeof(unsigned), s));
+        b->launches += 2;
+    }
+    GB_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < n; ++i) {
+        for (int a = 0; a < 7; ++a) out[7 * i + a] = h[8 * (size_t)i + a];
+        status[i] = st[i];
+    }
+    return GBMPM_OK;
+}
+
+int64_t gbmpm_batch_launch_count(gbmpm_batch *b) { return b ? b->launches : 0; }
 
 }  // extern "C"
 

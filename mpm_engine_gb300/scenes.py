@@ -103,4 +103,59 @@ def pour_scene(solver_cls, n_grid: int = 192, material=None, **solver_kw):
     return s, src, rcv, traj, substeps, (1.0 / 60.0) / substeps
 
 
-__all__ = ["HONEY", "PourTrajectory", "block", "dam_break_lattice", "dough", "pour_scene", "pour_substeps"]
+# ---- batched dough-squeeze scenes ---------------------------------------------------
+def squeeze_scene(solver_cls, n_particles: int, n_grid: int, material, grid_lim: float = 0.3,
+                  plate_speed: float = 0.05, seed: int = 0, **solver_kw):
+    """A cubic block of about `n_particles` (8 per cell, jittered) resting on a sticky
+    floor 3 cells up, squeezed by a kinematic plate descending at `plate_speed`.
+    Returns (solver, plate handle)."""
+    from .solver import GridConfig
+    grid = GridConfig(n_grid=n_grid, grid_lim=grid_lim)
+    dx = grid.dx
+    h = 0.5 * dx
+    side = max(4, int(round((n_particles ** (1.0 / 3.0)))))
+    edge = side * h
+    floor = 3 * dx
+    c = 0.5 * grid_lim
+    ax = np.arange(side) * h + 0.5 * h
+    pts = np.stack(np.meshgrid(ax + c - 0.5 * edge, ax + c - 0.5 * edge, ax + floor, indexing="ij"),
+                   axis=-1).reshape(-1, 3)
+    pts = pts + np.random.default_rng(seed).uniform(-0.25 * h, 0.25 * h, size=pts.shape)
+    s = solver_cls(grid=grid, **solver_kw).load_particles(pts.astype(np.float32), np.full(len(pts), h ** 3, np.float32))
+    s.set_material(material)
+    s.add_plane((0, 0, floor), (0, 0, 1), "sticky")
+    s.add_domain_walls()
+    top = floor + edge
+    plate = s.add_box((c, c, top + 2 * dx), (0.6 * edge + 2 * dx, 0.6 * edge + 2 * dx, dx),
+                      velocity=(0.0, 0.0, -plate_speed))
+    return s, plate
+
+
+def squeeze_batch_specs(n_scenes: int = 64, seed: int = 0):
+    """Seeded scene parameters of the batched forward workload: particle counts
+    log-uniform in [8k, 120k], grids 48^3..128^3, E log-uniform [1e4, 1e6], nu in
+    [0.2, 0.45], yield log-uniform [1e2, 1e4], von Mises or elastic."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n_scenes):
+        specs.append(dict(
+            n_particles=int(np.exp(rng.uniform(np.log(8e3), np.log(120e3)))),
+            n_grid=int(rng.choice([48, 64, 80, 96, 112, 128])),
+            E=float(np.exp(rng.uniform(np.log(1e4), np.log(1e6)))),
+            nu=float(rng.uniform(0.2, 0.45)),
+            yield_stress=float(np.exp(rng.uniform(np.log(1e2), np.log(1e4)))),
+            vonmises=bool(i % 2 == 0),
+            seed=i,
+        ))
+    return specs
+
+
+def squeeze_from_spec(solver_cls, spec: dict, **solver_kw):
+    from .materials import elastic, vonmises
+    mat = (vonmises(E=spec["E"], nu=spec["nu"], yield_stress=spec["yield_stress"], density=1000.0)
+           if spec["vonmises"] else elastic(E=spec["E"], nu=spec["nu"], density=1000.0))
+    return squeeze_scene(solver_cls, spec["n_particles"], spec["n_grid"], mat, seed=spec["seed"], **solver_kw)
+
+
+__all__ = ["HONEY", "PourTrajectory", "block", "dam_break_lattice", "dough", "pour_scene", "pour_substeps",
+           "squeeze_batch_specs", "squeeze_from_spec", "squeeze_scene"]

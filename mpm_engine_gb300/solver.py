@@ -655,6 +655,18 @@ class Solver:
                     f"band ({guard['band'] * 1e3:.2f} mm): fast material can tunnel through. Reduce dt, "
                     f"velocity/omega, or raise band (and the SDF margin).", RuntimeWarning, stacklevel=3)
 
+    def _tick_flags(self) -> int:
+        flags = 0
+        if self.fused and not self.sparse:
+            flags |= _abi.TICK_FUSED
+        if self.profile:
+            flags |= _abi.TICK_PROFILE
+        elif self._sim.use_cuda_graph:
+            flags |= _abi.TICK_GRAPH
+        if self._sim.reorder:
+            flags |= _abi.TICK_REORDER
+        return flags
+
     def step(self, dt: float, substeps: int = 1) -> Solver:
         """Advance `substeps` substeps of size dt (one control tick)."""
         self._require_loaded()
@@ -670,15 +682,7 @@ class Solver:
         if self._sdf_guard:
             self._sdf_tunnel_check(dt)
         self._sync_engine()
-        flags = 0
-        if self.fused and not self.sparse:
-            flags |= _abi.TICK_FUSED
-        if self.profile:
-            flags |= _abi.TICK_PROFILE
-        elif self._sim.use_cuda_graph:
-            flags |= _abi.TICK_GRAPH
-        if self._sim.reorder:
-            flags |= _abi.TICK_REORDER
+        flags = self._tick_flags()
         t = C.c_double(self._time)
         _abi.check(self._eng.lib.gbmpm_tick(self._eng.h, C.byref(t), float(dt), int(substeps), flags,
                                             self._stream()), "gbmpm_tick")
@@ -732,7 +736,10 @@ class Solver:
         out = (C.c_float * 7)()
         st = C.c_uint32(0)
         _abi.check(self._eng.lib.gbmpm_guard(self._eng.h, out, C.byref(st), self._stream()), "gbmpm_guard")
-        if st.value & _abi.FLAG_STENCIL_OOB:
+        self._check_guard(list(out), int(st.value))
+
+    def _check_guard(self, out, status: int) -> None:
+        if status & _abi.FLAG_STENCIL_OOB:
             raise RuntimeError("a particle's P2G stencil left the grid during the previous tick; the kernels "
                                "skipped it. Enlarge grid_lim or add a bounding box / wall collider.")
         dx, lim = self.grid.dx, self.grid.grid_lim
@@ -895,3 +902,78 @@ class Solver:
         out["sdf_host"] = {t.data_ptr(): t.cpu().numpy().copy() for t in self._keep}
         out["time"] = self._time
         return out
+
+
+class BatchSolver:
+    """Many independent scenes advanced together on one GPU.
+
+    Each scene is a loaded `Solver` (its own particles, grid, materials and
+    colliders). `step` runs every scene's edge guard with one synchronization and
+    then advances all scenes in one CUDA graph whose branches are the scenes'
+    ticks, so scenes that each fill only part of the GPU run concurrently. The
+    reference has no counterpart: its planners step one Solver at a time
+    (experiments/shape_planning.py:107). Per-scene block sorting, sparse mode and
+    profiling are not available inside a batch.
+    """
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        if not self.solvers:
+            raise ValueError("BatchSolver needs at least one Solver")
+        for s in self.solvers:
+            s._require_loaded()
+            if s.sort_interval or s.sparse or s.profile:
+                raise ValueError("sort_interval, sparse and profile are per-Solver features; not in a batch")
+        if len({s.fused for s in self.solvers}) != 1:
+            raise ValueError("all scenes of a batch must share the fused setting")
+        self.lib = _abi.load()
+        n = len(self.solvers)
+        hs = (C.c_void_p * n)(*[s._eng.h.value for s in self.solvers])
+        b = C.c_void_p()
+        _abi.check(self.lib.gbmpm_batch_create(hs, n, C.byref(b)), "gbmpm_batch_create")
+        self.h = b
+        self.use_graph = True
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.gbmpm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self):
+        return len(self.solvers)
+
+    def step(self, dt: float, substeps: int = 1) -> BatchSolver:
+        n = len(self.solvers)
+        stream = self.solvers[0]._stream()
+        if any(s._tick % max(1, s.guard_interval) == 0 for s in self.solvers):
+            out = (C.c_float * (7 * n))()
+            st = (C.c_uint32 * n)()
+            _abi.check(self.lib.gbmpm_batch_guard(self.h, out, st, stream), "gbmpm_batch_guard")
+            for i, s in enumerate(self.solvers):
+                if s._tick % max(1, s.guard_interval) == 0:
+                    s._check_guard(list(out[7 * i:7 * i + 7]), int(st[i]))
+        for s in self.solvers:
+            s._pull_colliders()
+            if s._sdf_guard:
+                s._sdf_tunnel_check(dt)
+            s._sync_engine()
+        flags = self.solvers[0]._tick_flags()
+        if not self.use_graph:
+            flags &= ~_abi.TICK_GRAPH
+        times = (C.c_double * n)(*[s._time for s in self.solvers])
+        _abi.check(self.lib.gbmpm_batch_tick(self.h, times, float(dt), int(substeps), flags, stream),
+                   "gbmpm_batch_tick")
+        for i, s in enumerate(self.solvers):
+            s._time = times[i]
+            s._step += substeps
+            s._tick += 1
+        return self
+
+    def launch_count(self) -> int:
+        return int(self.lib.gbmpm_batch_launch_count(self.h))
