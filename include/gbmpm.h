@@ -80,6 +80,7 @@ typedef struct {
     float *mu, *lam, *yield_stress;     /* [n] per-particle model arrays (mpm_solver_warp.py:277-279) */
     int32_t *material, *selection;      /* [n] */
     float *cov, *init_cov;              /* [n][6] upper triangle xx,xy,xz,yy,yz,zz, or NULL */
+    int32_t *cdf_tag;                   /* [n] persisted CPIC side bits (warp_utils.py:124-129), or NULL */
 } gbmpm_particles;
 
 /* Dense n^3 grid, index ((ix*n)+iy)*n+iz (Warp 3-D array order).
@@ -146,6 +147,25 @@ typedef struct {
     double rot64[9];            /* cup: float64 rotation shadow (mpm_solver_warp.py:2227-2254) */
 } gbmpm_collider;
 
+/* CPIC thin-boundary (CDF) collider lane (CDFCollider, kernels/warp_utils.py:261-285).
+ * Up to GBMPM_MAX_CDF lanes; the lane index is the collider handle. */
+#define GBMPM_MAX_CDF 4
+typedef struct {
+    const float *values;        /* [res^3] side-signed distance to the sheet (device pointer for the library) */
+    const float *valid;         /* [res^3] 1 where distance and side are trustworthy */
+    int32_t res;
+    int32_t surface_type;       /* 0 sticky, 1 slip, 2 separable + Coulomb */
+    float origin[3];
+    float cell;
+    float center[3];            /* world position of the body origin */
+    float quat[4];              /* body -> world, x y z w */
+    float velocity[3];
+    float omega[3];
+    float band;
+    float friction;
+    float start_time, end_time;
+} gbmpm_cdf;
+
 /* gbmpm_tick flags */
 #define GBMPM_TICK_FUSED   1    /* fused G2P2G pipeline (Solver.fused) */
 #define GBMPM_TICK_GRAPH   2    /* replay the tick as one captured CUDA graph when possible */
@@ -185,6 +205,21 @@ int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps,
  * over all particles, and *status = the device status word (then cleared).
  * Synchronizes the stream. */
 int gbmpm_guard(gbmpm_engine *e, float out[7], uint32_t *status, void *stream);
+
+/* Replace the CDF lanes (add_cdf_collider / set_cdf_pose, mpm_solver_warp.py:2819-2953).
+ * A lane whose centre or orientation changed is restamped at the next substep.
+ * Scenes with CDF lanes tick with live launches (no graph, no block reorder). */
+int gbmpm_set_cdf(gbmpm_engine *e, const gbmpm_cdf *lanes, int32_t n);
+/* Current lane records (poses integrated by ticks). */
+int gbmpm_get_cdf(gbmpm_engine *e, gbmpm_cdf *lanes, int32_t n);
+/* Blocked-deposit reaction of a lane since the last reset: {fx, fy, fz, tx, ty, tz}
+ * (cdf_wrench, core/solver.py:401-413); the reset clears every lane. */
+int gbmpm_cdf_wrench(gbmpm_engine *e, int32_t lane, double out[6], void *stream);
+int gbmpm_reset_cdf_wrench(gbmpm_engine *e, void *stream);
+/* Node tag and owner-distance grids of the last stamp (grid_cdf_tag, grid_cdf_d,
+ * mpm_solver_warp.py:2906-2915), copied into caller device buffers of n_grid^3
+ * entries (either may be NULL), and the number of stamps so far (_cdf_stamp_count). */
+int gbmpm_cdf_grids(gbmpm_engine *e, int32_t *tag_out, float *d_out, int64_t *stamps, void *stream);
 
 /* Reaction impulse accumulated since the last reset: {fx, fy, fz, tx, ty, tz}. */
 int gbmpm_wrench(gbmpm_engine *e, int32_t collider, double out[6], void *stream);

@@ -49,6 +49,7 @@ class Particles(C.Structure):
         ("mu", C.c_void_p), ("lam", C.c_void_p), ("yield_stress", C.c_void_p),
         ("material", C.c_void_p), ("selection", C.c_void_p),
         ("cov", C.c_void_p), ("init_cov", C.c_void_p),
+        ("cdf_tag", C.c_void_p),
     ]
 
 
@@ -90,6 +91,18 @@ class Collider(C.Structure):
     ]
 
 
+MAX_CDF = 4
+
+
+class Cdf(C.Structure):
+    _fields_ = [
+        ("values", C.c_void_p), ("valid", C.c_void_p), ("res", C.c_int32), ("surface_type", C.c_int32),
+        ("origin", C.c_float * 3), ("cell", C.c_float), ("center", C.c_float * 3), ("quat", C.c_float * 4),
+        ("velocity", C.c_float * 3), ("omega", C.c_float * 3), ("band", C.c_float), ("friction", C.c_float),
+        ("start_time", C.c_float), ("end_time", C.c_float),
+    ]
+
+
 # every entry point include/gbmpm.h declares, with its ctypes signature
 _SIGNATURES = {
     "gbmpm_last_error": (C.c_char_p, []),
@@ -105,6 +118,11 @@ _SIGNATURES = {
     "gbmpm_guard": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.c_void_p]),
     "gbmpm_wrench": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_void_p]),
     "gbmpm_reset_wrench": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gbmpm_set_cdf": (C.c_int, [C.c_void_p, C.POINTER(Cdf), C.c_int32]),
+    "gbmpm_get_cdf": (C.c_int, [C.c_void_p, C.POINTER(Cdf), C.c_int32]),
+    "gbmpm_cdf_wrench": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_void_p]),
+    "gbmpm_reset_cdf_wrench": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gbmpm_cdf_grids": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64), C.c_void_p]),
     "gbmpm_sort_particles": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_int32), C.c_void_p,
                                        C.c_void_p]),
     "gbmpm_rebuild_active_blocks": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p]),

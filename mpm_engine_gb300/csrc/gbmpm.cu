@@ -55,6 +55,14 @@ struct MatTables {
     float mu_s[16], dmu[16], I0[16], d[16], rho_s[16], phi_init[16], phi_chi[16];
 };
 
+// CPIC lane state the transfer passes read (the reference's cdf_lane_* arrays):
+// poses at the current stamp, and pose/rates/surface at the previous one.
+struct CdfLanes {
+    float c_cur[4][3], c_prev[4][3], v_prev[4][3], w_prev[4][3];
+    float fric[4];
+    int type[4];
+};
+
 struct PK {
     float *x, *v, *C, *F, *Ft, *L, *S;
     const float *mass, *vol;
@@ -74,6 +82,14 @@ struct PK {
     int *blk_flag, *blk_list, *blk_count;
     int bd;
     unsigned *status;
+    // CPIC (CDF) colliders; cdf_on == 0 leaves every branch below unused
+    int cdf_on, cnb;
+    const int *ctag, *ctag_prev, *cblock;
+    const float *cd, *cd_prev;
+    int *ptag;
+    double *cwrench;   // [4][6] blocked-deposit reaction
+    float grav[3];
+    CdfLanes lanes;
 };
 
 // Per-substep collider pose record, built on the host each tick.
@@ -650,6 +666,177 @@ __device__ __forceinline__ float4 global_fetch(const PK &k, const Stencil &s, in
     return __ldg(k.gv + ((size_t)ix * k.ng + (s.b[1] + j)) * k.ng + (s.b[2] + kk));
 }
 
+// ---- CPIC (CDF) transfer helpers (mpm_utils.py:648-816) ----------------------
+// Node tags: bit 2l = lane l valid here, bit 2l+1 = the node's side of lane l,
+// bits 8..9 = the lane nearest the node (owner).
+constexpr int kCdfOwnerShift = 8;
+
+// cdf_pair_incompatible: some lane is valid at both ends with opposite sides
+__device__ __forceinline__ bool cdf_incompatible(int pc, int nt) {
+    return ((pc & nt & 0x55) & ((pc ^ nt) >> 1)) != 0;
+}
+
+__device__ __forceinline__ size_t node_id(const PK &k, const Stencil &s, int i, int j, int kk) {
+    return ((size_t)(s.b[0] + i) * k.ng + (s.b[1] + j)) * k.ng + (s.b[2] + kk);
+}
+
+// cdf_stencil_near: a 4^3 block under the stencil holds tags now or at the last stamp
+__device__ __forceinline__ bool cdf_near(const PK &k, const Stencil &s) {
+    for (int bi = s.b[0] >> 2; bi <= (s.b[0] + 2) >> 2; ++bi)
+        for (int bj = s.b[1] >> 2; bj <= (s.b[1] + 2) >> 2; ++bj)
+            for (int bk = s.b[2] >> 2; bk <= (s.b[2] + 2) >> 2; ++bk)
+                if (__ldg(k.cblock + ((size_t)bi * k.cnb + bj) * k.cnb + bk) != 0) return true;
+    return false;
+}
+
+// cdf_particle_tag: per lane, the particle is valid when any stencil node is, and
+// its side is the sign of the weighted signed distance of the valid nodes.
+__device__ int cdf_vote(const PK &k, const Stencil &s, bool prev) {
+    const int *T = prev ? k.ctag_prev : k.ctag;
+    const float *D = prev ? k.cd_prev : k.cd;
+    float votes[4] = {0.f, 0.f, 0.f, 0.f};
+    int seen = 0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            for (int kk = 0; kk < 3; ++kk) {
+                size_t id = node_id(k, s, i, j, kk);
+                int t = T[id];
+                if (t == 0) continue;
+                float w = s.w[0][i] * s.w[1][j] * s.w[2][kk];
+                float dd = D[id];
+#pragma unroll
+                for (int l = 0; l < 4; ++l)
+                    if ((t >> (2 * l)) & 1) {
+                        seen |= 1 << (2 * l);
+                        votes[l] += w * dd * (((t >> (2 * l + 1)) & 1) ? 1.0f : -1.0f);
+                    }
+            }
+    int pc = 0;
+#pragma unroll
+    for (int l = 0; l < 4; ++l)
+        if ((seen >> (2 * l)) & 1) pc |= (1 << (2 * l)) | ((votes[l] >= 0.0f ? 1 : 0) << (2 * l + 1));
+    return pc;
+}
+
+// cdf_persist_tag: a lane the particle already carried keeps its side
+__device__ __forceinline__ int cdf_persist(int old, int fresh) {
+    int pc = 0;
+#pragma unroll
+    for (int l = 0; l < 4; ++l)
+        if ((fresh >> (2 * l)) & 1) {
+            int side_bit = 1 << (2 * l + 1);
+            pc |= (1 << (2 * l)) | (((old >> (2 * l)) & 1) ? (old & side_bit) : (fresh & side_bit));
+        }
+    return pc;
+}
+
+// cdf_particle_ghost: the velocity the particle reads from nodes across the
+// surface. Surface normal and distance come from the owner-lane distance field
+// at the previous stamp; the tangential part follows the surface type (sticky,
+// slip, separable Coulomb with a capped impulse) plus a separation push when the
+// particle sits within 0.05 dx of the surface.
+__device__ void cdf_ghost(const PK &k, const Stencil &s, const float *xp, const float *vp, int pc, const float *grav,
+                          float *ghost) {
+    float d_hat = 0.0f, n_acc[3] = {0.f, 0.f, 0.f}, best_w = 0.0f;
+    int lane_p = 0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            for (int kk = 0; kk < 3; ++kk) {
+                size_t id = node_id(k, s, i, j, kk);
+                int t = k.ctag_prev[id];
+                if (t == 0) continue;
+                int own = (t >> kCdfOwnerShift) & 3;
+                if (((t >> (2 * own)) & 1) == 0) continue;
+                float w = s.w[0][i] * s.w[1][j] * s.w[2][kk];
+                float sgn = ((t >> (2 * own + 1)) & 1) ? 1.0f : -1.0f;
+                float dd = k.cd_prev[id];
+                d_hat += w * sgn * dd;
+                float dw[3] = {s.dw[0][i] * s.w[1][j] * s.w[2][kk], s.w[0][i] * s.dw[1][j] * s.w[2][kk],
+                               s.w[0][i] * s.w[1][j] * s.dw[2][kk]};
+#pragma unroll
+                for (int a = 0; a < 3; ++a) n_acc[a] += dw[a] * k.inv_dx * sgn * dd;
+                if (w > best_w) { best_w = w; lane_p = own; }
+            }
+    float vf[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { vf[a] = vp[a] + grav[a] * k.dt; ghost[a] = vf[a]; }
+    float nl = sqrtf(n_acc[0] * n_acc[0] + n_acc[1] * n_acc[1] + n_acc[2] * n_acc[2]);
+    if (!(nl > 1.0e-12f)) return;
+    const float side = ((pc >> (2 * lane_p + 1)) & 1) ? 1.0f : -1.0f;
+    float n[3], vs[3], vrel[3];
+    const float *cp = k.lanes.c_prev[lane_p], *vl = k.lanes.v_prev[lane_p], *wl = k.lanes.w_prev[lane_p];
+    float rel[3] = {xp[0] - cp[0], xp[1] - cp[1], xp[2] - cp[2]};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) n[a] = n_acc[a] / nl * side;
+    vs[0] = vl[0] + (wl[1] * rel[2] - wl[2] * rel[1]);
+    vs[1] = vl[1] + (wl[2] * rel[0] - wl[0] * rel[2]);
+    vs[2] = vl[2] + (wl[0] * rel[1] - wl[1] * rel[0]);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) vrel[a] = vf[a] - vs[a];
+    const float vn = vrel[0] * n[0] + vrel[1] * n[1] + vrel[2] * n[2];
+    float vt[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) vt[a] = vrel[a] - n[a] * vn;
+    float c = 0.0f;
+    const float d_side = d_hat * side, eps = 0.05f * k.dx;
+    if (d_side < eps) c = fminf((eps - d_side) / k.dt, 0.5f * k.dx / k.dt);
+    const int stype = k.lanes.type[lane_p];
+    if (stype == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) ghost[a] = vs[a] + n[a] * c;
+    } else if (stype == 1) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) ghost[a] = vs[a] + vt[a] + n[a] * c;
+    } else {
+        const float dvn = fmaxf(-vn, 0.0f) + c;
+        const float tl = sqrtf(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
+        if (tl > 1.0e-12f && dvn > 0.0f) {
+            const float sc = fmaxf(0.0f, tl - k.lanes.fric[lane_p] * dvn) / tl;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) vt[a] *= sc;
+        }
+        const float vnp = fmaxf(vn, 0.0f);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) ghost[a] = vs[a] + vt[a] + n[a] * vnp + n[a] * c;
+    }
+}
+
+// P2G with the CPIC mask: deposits into nodes incompatible with the particle are
+// withheld from the grid and added to the owner lane's reaction (force and torque
+// about the lane centre, summed per thread in float64 before one flush per lane).
+__device__ void cdf_deposit_all(const PK &k, const Stencil &s, int p, const float *v, const float *C, const float *S,
+                                int pc) {
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    int acc_own = -1;
+    auto flush = [&]() {
+        if (acc_own < 0) return;
+        double *w = k.cwrench + 6 * acc_own;
+#pragma unroll
+        for (int a = 0; a < 6; ++a) { atomicAdd(w + a, acc[a]); acc[a] = 0.0; }
+    };
+    p2g_core(k, s, p, v, C, S, [&](int i, int j, int kk, float4 val) {
+        size_t id = node_id(k, s, i, j, kk);
+        int nt = __ldg(k.ctag + id);
+        if (cdf_incompatible(pc, nt)) {
+            int own = (nt >> kCdfOwnerShift) & 3;
+            if (own != acc_own) { flush(); acc_own = own; }
+            const float *cc = k.lanes.c_cur[own];
+            float r[3] = {(float)(s.b[0] + i) * k.dx - cc[0], (float)(s.b[1] + j) * k.dx - cc[1],
+                          (float)(s.b[2] + kk) * k.dx - cc[2]};
+            acc[0] += (double)val.x;
+            acc[1] += (double)val.y;
+            acc[2] += (double)val.z;
+            acc[3] += (double)(r[1] * val.z - r[2] * val.y);
+            acc[4] += (double)(r[2] * val.x - r[0] * val.z);
+            acc[5] += (double)(r[0] * val.y - r[1] * val.x);
+            return;
+        }
+        atomicAdd(k.gmv + id, val);
+    });
+    flush();
+    mark_stencil_blocks(k, s);
+}
+
 // ---- direct kernel: one thread per particle, global gather and atomics ------
 // One kernel serves every particle pass of the schedule; `mode` selects the
 // stages (G2P, STRESS, P2G): the fused interior pass is G2P|STRESS|P2G, the tick
@@ -667,6 +854,7 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
     float x[3] = {k.x[3 * p], k.x[3 * p + 1], k.x[3 * p + 2]};
     float v[3], C[9], L[9], Ft[9], S[9];
     bool gathered = false;
+    int ptag = 0;   // CPIC particle tag carried from G2P into P2G
     if ((mode & PASS_G2P) && mat != 7 && mat != 8) {
         Stencil s;
         stencil(x, k.inv_dx, s);
@@ -674,9 +862,28 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
             set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
             return;
         }
-        g2p_core(k, s, [&](int i, int j, int kk) { return global_fetch(k, s, i, j, kk); }, v, C, L);
+        if (k.cdf_on) {
+            int pc = 0;
+            if (cdf_near(k, s)) pc = cdf_persist(k.ptag[p], cdf_vote(k, s, true));
+            k.ptag[p] = pc;
+            ptag = pc;
+        }
+        if (ptag != 0) {
+            const float *vi = k.v + 3 * (size_t)p;
+            const float vp[3] = {vi[0], vi[1], vi[2]};
+            float gh[3];
+            cdf_ghost(k, s, x, vp, ptag, k.grav, gh);
+            const float4 g4 = make_float4(gh[0], gh[1], gh[2], 0.0f);
+            g2p_core(k, s, [&](int i, int j, int kk) {
+                return cdf_incompatible(ptag, k.ctag_prev[node_id(k, s, i, j, kk)]) ? g4 : global_fetch(k, s, i, j, kk);
+            }, v, C, L);
+        } else {
+            g2p_core(k, s, [&](int i, int j, int kk) { return global_fetch(k, s, i, j, kk); }, v, C, L);
+        }
         g2p_finish<false>(k, p, x, v, L, Ft);
         gathered = true;
+    } else if (k.cdf_on && (mode & PASS_P2G)) {
+        ptag = k.ptag[p];
     }
     if (gathered) {
         float *xo = k.x + 3 * (size_t)p;
@@ -714,7 +921,10 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
             set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
             return;
         }
-        global_deposit_all(k, s, p, v, C, S);
+        int pc = 0;
+        if (k.cdf_on && cdf_near(k, s)) pc = cdf_persist(ptag, cdf_vote(k, s, false));
+        if (pc != 0) cdf_deposit_all(k, s, p, v, C, S, pc);
+        else global_deposit_all(k, s, p, v, C, S);
     }
 }
 
@@ -1085,6 +1295,143 @@ __device__ __forceinline__ void qrot(const float *q, const float *x, float *out,
     out[0] = x[0] * c + cx * sgn + q[0] * d * 2.0f;
     out[1] = x[1] * c + cy * sgn + q[1] * d * 2.0f;
     out[2] = x[2] * c + cz * sgn + q[2] * d * 2.0f;
+}
+
+// ---- CPIC (CDF) stamping (mpm_solver_warp.py:94-183) ---------------------------
+// The stamp decides node tags by thresholds on interpolated fields, so its
+// arithmetic is spelled out with round-to-nearest intrinsics: no contraction into
+// FMAs, every operation rounded once, as in the fp32 statement of the algorithm.
+struct CdfBox {
+    int lo[3], hi[3];   // node range [lo, hi)
+};
+
+__device__ __forceinline__ float trilerp_rn(const float *vals, int res, float f0, float f1, float f2) {
+    const float top = (float)res - 1.0001f;
+    float fi = fminf(fmaxf(f0, 0.0f), top), fj = fminf(fmaxf(f1, 0.0f), top), fk = fminf(fmaxf(f2, 0.0f), top);
+    int i = (int)floorf(fi), j = (int)floorf(fj), kk = (int)floorf(fk);
+    float tx = __fsub_rn(fi, (float)i), ty = __fsub_rn(fj, (float)j), tz = __fsub_rn(fk, (float)kk);
+    auto at = [&](int a, int b, int c) { return __ldg(vals + (((size_t)a * res + b) * res + c)); };
+    auto lerp = [](float a, float b, float t) { return __fadd_rn(__fmul_rn(a, __fsub_rn(1.0f, t)), __fmul_rn(b, t)); };
+    float c00 = lerp(at(i, j, kk), at(i + 1, j, kk), tx);
+    float c01 = lerp(at(i, j, kk + 1), at(i + 1, j, kk + 1), tx);
+    float c10 = lerp(at(i, j + 1, kk), at(i + 1, j + 1, kk), tx);
+    float c11 = lerp(at(i, j + 1, kk + 1), at(i + 1, j + 1, kk + 1), tx);
+    return lerp(lerp(c00, c10, ty), lerp(c01, c11, ty), tz);
+}
+
+// inverse quaternion rotation x(2w^2-1) - 2w (q x x) + 2 q (q . x), rounded per operation
+__device__ __forceinline__ void qrot_inv_rn(const float *q, const float *x, float *out) {
+    const float w = q[3];
+    const float c = __fsub_rn(__fmul_rn(__fmul_rn(2.0f, w), w), 1.0f);
+    const float cr[3] = {__fsub_rn(__fmul_rn(q[1], x[2]), __fmul_rn(q[2], x[1])),
+                         __fsub_rn(__fmul_rn(q[2], x[0]), __fmul_rn(q[0], x[2])),
+                         __fsub_rn(__fmul_rn(q[0], x[1]), __fmul_rn(q[1], x[0]))};
+    const float d = __fadd_rn(__fadd_rn(__fmul_rn(q[0], x[0]), __fmul_rn(q[1], x[1])), __fmul_rn(q[2], x[2]));
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float ta = __fmul_rn(x[a], c);
+        float tb = __fmul_rn(__fmul_rn(cr[a], w), 2.0f);
+        float td = __fmul_rn(__fmul_rn(q[a], d), 2.0f);
+        out[a] = __fadd_rn(__fsub_rn(ta, tb), td);
+    }
+}
+
+__device__ __forceinline__ bool box_node(const CdfBox &b, long long idx, int &x, int &y, int &z) {
+    const long long ny = b.hi[1] - b.lo[1], nz = b.hi[2] - b.lo[2];
+    z = b.lo[2] + (int)(idx % nz);
+    long long r = idx / nz;
+    y = b.lo[1] + (int)(r % ny);
+    x = b.lo[0] + (int)(r / ny);
+    return x < b.hi[0];
+}
+
+__device__ __forceinline__ long long box_volume(const CdfBox &b) {
+    return (long long)(b.hi[0] - b.lo[0]) * (b.hi[1] - b.lo[1]) * (b.hi[2] - b.lo[2]);
+}
+
+// cdf_zero_tags over a box
+__global__ void k_cdf_clear(int *tag, float *d, CdfBox b, int ng) {
+    const long long total = box_volume(b);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        int x, y, z;
+        if (!box_node(b, i, x, y, z)) break;
+        size_t id = ((size_t)x * ng + y) * ng + z;
+        tag[id] = 0;
+        d[id] = 1.0e9f;
+    }
+}
+
+// cdf_copy_prev over a box
+__global__ void k_cdf_copy_prev(const int *tag, const float *d, int *tag_prev, float *d_prev, CdfBox b, int ng) {
+    const long long total = box_volume(b);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        int x, y, z;
+        if (!box_node(b, i, x, y, z)) break;
+        size_t id = ((size_t)x * ng + y) * ng + z;
+        tag_prev[id] = tag[id];
+        d_prev[id] = d[id];
+    }
+}
+
+struct CdfStamp {
+    const float *values, *valid;
+    int res, lane, ng;
+    float origin[3], cell, center[3], quat[4], band;
+    float dx;
+    CdfBox box;
+    int *tag;
+    float *d;
+};
+
+// cdf_stamp for one lane: a node within `band` of the surface, where the field is
+// valid, gains the lane's valid bit and side bit; the nearest lane owns the node.
+__global__ void k_cdf_stamp(CdfStamp a) {
+    const long long total = box_volume(a.box);
+    const float rf = (float)a.res - 1.0f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        int x, y, z;
+        if (!box_node(a.box, i, x, y, z)) break;
+        const float rel[3] = {__fsub_rn(__fmul_rn((float)x, a.dx), a.center[0]),
+                              __fsub_rn(__fmul_rn((float)y, a.dx), a.center[1]),
+                              __fsub_rn(__fmul_rn((float)z, a.dx), a.center[2])};
+        float body[3];
+        qrot_inv_rn(a.quat, rel, body);
+        const float f0 = __fdiv_rn(__fsub_rn(body[0], a.origin[0]), a.cell);
+        const float f1 = __fdiv_rn(__fsub_rn(body[1], a.origin[1]), a.cell);
+        const float f2 = __fdiv_rn(__fsub_rn(body[2], a.origin[2]), a.cell);
+        if (f0 < 0.0f || f1 < 0.0f || f2 < 0.0f || f0 > rf || f1 > rf || f2 > rf) continue;
+        if (trilerp_rn(a.valid, a.res, f0, f1, f2) < 0.999f) continue;
+        const float dd = trilerp_rn(a.values, a.res, f0, f1, f2);
+        const float ud = fabsf(dd);
+        if (ud > a.band) continue;
+        const size_t id = ((size_t)x * a.ng + y) * a.ng + z;
+        int t = a.tag[id] | (1 << (2 * a.lane)) | ((dd >= 0.0f ? 1 : 0) << (2 * a.lane + 1));
+        if (ud < a.d[id]) {
+            a.d[id] = ud;
+            t = (t & ~(3 << kCdfOwnerShift)) | (a.lane << kCdfOwnerShift);
+        }
+        a.tag[id] = t;
+    }
+}
+
+// cdf_block_mask over a box of 4^3 blocks: OR of the current and previous tags
+__global__ void k_cdf_block_mask(const int *tag, const int *tag_prev, int *block, CdfBox bb, int nb, int ng) {
+    const long long total = box_volume(bb);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        int bi, bj, bk;
+        if (!box_node(bb, i, bi, bj, bk)) break;
+        int occ = 0;
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b)
+                for (int c = 0; c < 4; ++c) {
+                    int ci = (bi << 2) + a, cj = (bj << 2) + b, ck = (bk << 2) + c;
+                    if (ci < ng && cj < ng && ck < ng) {
+                        size_t id = ((size_t)ci * ng + cj) * ng + ck;
+                        occ |= tag[id] | tag_prev[id];
+                    }
+                }
+        block[((size_t)bi * nb + bj) * nb + bk] = occ;
+    }
 }
 
 // Applies collider c to node (gx,gy,gz) of mass m (> 0); adds the reaction
@@ -1584,6 +1931,39 @@ struct DevBuf {
     }
     void release() { if (ptr) cudaFree(ptr); ptr = nullptr; n = 0; }
 };
+
+// Host bookkeeping of the CPIC lanes (the reference keeps the same on the Python
+// side of MPM_Simulator_WARP): lane records with poses integrated per substep,
+// the lane arrays the transfer passes read, and which boxes need restamping.
+struct CdfHost {
+    int n = 0;
+    gbmpm_cdf rec[GBMPM_MAX_CDF];
+    float c_cur[4][3] = {}, v_cur[4][3] = {}, w_cur[4][3] = {};
+    float c_prev[4][3] = {}, v_prev[4][3] = {}, w_prev[4][3] = {};
+    float fric[4] = {};
+    int type[4] = {};
+    bool dirty[4] = {}, active[4] = {}, has_prev_box[4] = {};
+    int prev_box[4][6] = {};
+    bool stale_set = false;     // tag_prev lags tag inside stale_box
+    int stale_box[6] = {};
+    bool lane_prev_stale = false;
+    int64_t stamps = 0;
+    void sync_lane(int l) {    // _sync_cdf_lane (mpm_solver_warp.py:2883-2905)
+        for (int a = 0; a < 3; ++a) {
+            c_cur[l][a] = rec[l].center[a];
+            v_cur[l][a] = rec[l].velocity[a];
+            w_cur[l][a] = rec[l].omega[a];
+        }
+        fric[l] = rec[l].friction;
+        type[l] = rec[l].surface_type;
+    }
+    void copy_lane_prev() {
+        std::memcpy(c_prev, c_cur, sizeof c_cur);
+        std::memcpy(v_prev, v_cur, sizeof v_cur);
+        std::memcpy(w_prev, w_cur, sizeof w_cur);
+        lane_prev_stale = false;
+    }
+};
 }  // namespace
 
 struct gbmpm_engine {
@@ -1630,6 +2010,13 @@ struct gbmpm_engine {
     cudaStream_t g_stream = nullptr;
     bool dirty = true;
     uint64_t version = 1;   // bumped with every change a captured graph depends on
+    // CPIC (CDF) colliders: lanes, node tag and distance grids (current and as of
+    // the previous stamp), 4^3 occupancy mask, per-lane reaction
+    CdfHost cdf;
+    DevBuf<int> c_tag, c_tag_prev, c_block;
+    DevBuf<float> c_d, c_d_prev;
+    DevBuf<double> c_wrench;
+    int c_ng = 0;
     // profiling
     double prof_ms[GBMPM_NUM_PHASES] = {0};
     int64_t prof_n[GBMPM_NUM_PHASES] = {0};
@@ -1661,6 +2048,22 @@ PK make_pk(gbmpm_engine *e, const gbmpm_particles &P, float dt, int list) {
     k.blk_list = e->d_list.ptr + (size_t)list * nb;
     k.blk_count = e->d_count.ptr + list;
     k.status = e->d_status.ptr;
+    for (int a = 0; a < 3; ++a) k.grav[a] = e->M.gravity[a];
+    if (e->cdf.n > 0 && P.cdf_tag) {
+        const CdfHost &H = e->cdf;
+        k.cdf_on = 1;
+        k.cnb = (e->c_ng + 3) / 4;
+        k.ctag = e->c_tag.ptr; k.ctag_prev = e->c_tag_prev.ptr; k.cblock = e->c_block.ptr;
+        k.cd = e->c_d.ptr; k.cd_prev = e->c_d_prev.ptr;
+        k.ptag = P.cdf_tag;
+        k.cwrench = e->c_wrench.ptr;
+        std::memcpy(k.lanes.c_cur, H.c_cur, sizeof H.c_cur);
+        std::memcpy(k.lanes.c_prev, H.c_prev, sizeof H.c_prev);
+        std::memcpy(k.lanes.v_prev, H.v_prev, sizeof H.v_prev);
+        std::memcpy(k.lanes.w_prev, H.w_prev, sizeof H.w_prev);
+        std::memcpy(k.lanes.fric, H.fric, sizeof H.fric);
+        std::memcpy(k.lanes.type, H.type, sizeof H.type);
+    }
     return k;
 }
 
@@ -1867,8 +2270,171 @@ int check_ready(gbmpm_engine *e) {
     return GBMPM_OK;
 }
 
+// ---- CPIC (CDF) host driver ----------------------------------------------------
+int cdf_grid_blocks(gbmpm_engine *e, long long work) {
+    long long want = (work + 255) / 256;
+    return (int)std::max<long long>(1, std::min<long long>(want, (long long)e->num_sms * 8));
+}
+
+// The lane's grid box: its field's corners posed by centre and quaternion in
+// float64, widened by a 2-node halo and clipped to the grid (cdf_aabb,
+// mpm_solver_warp.py:2884-2895, _grid_box).
+bool cdf_lane_box(const gbmpm_cdf &r, const gbmpm_model &M, int *box) {
+    double qx = r.quat[0], qy = r.quat[1], qz = r.quat[2], qw = r.quat[3];
+    double R[3][3] = {{1 - 2 * (qy * qy + qz * qz), 2 * (qx * qy - qz * qw), 2 * (qx * qz + qy * qw)},
+                      {2 * (qx * qy + qz * qw), 1 - 2 * (qx * qx + qz * qz), 2 * (qy * qz - qx * qw)},
+                      {2 * (qx * qz - qy * qw), 2 * (qy * qz + qx * qw), 1 - 2 * (qx * qx + qy * qy)}};
+    double ext = (r.res - 1) * (double)r.cell;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b)
+            for (int c = 0; c < 2; ++c) {
+                double cr[3] = {(double)r.origin[0] + a * ext, (double)r.origin[1] + b * ext,
+                                (double)r.origin[2] + c * ext};
+                for (int i = 0; i < 3; ++i) {
+                    double p = (double)r.center[i] + R[i][0] * cr[0] + R[i][1] * cr[1] + R[i][2] * cr[2];
+                    lo[i] = std::min(lo[i], p);
+                    hi[i] = std::max(hi[i], p);
+                }
+            }
+    const double dx = (double)M.grid_lim / M.n_grid;
+    for (int i = 0; i < 3; ++i) {
+        int l = std::max(0, (int)std::floor(lo[i] / dx) - 2);
+        int h = std::min(M.n_grid, (int)std::ceil(hi[i] / dx) + 2 + 1);
+        if (h - l <= 0) return false;
+        box[i] = l;
+        box[3 + i] = h;
+    }
+    return true;
+}
+
+CdfBox to_box(const int *b) {
+    CdfBox x;
+    for (int i = 0; i < 3; ++i) { x.lo[i] = b[i]; x.hi[i] = b[3 + i]; }
+    return x;
+}
+
+void cdf_copy_prev_box(gbmpm_engine *e, const int *b, cudaStream_t s) {
+    CdfBox box = to_box(b);
+    long long vol = (long long)(b[3] - b[0]) * (b[4] - b[1]) * (b[5] - b[2]);
+    k_cdf_copy_prev<<<cdf_grid_blocks(e, vol), 256, 0, s>>>(e->c_tag.ptr, e->c_d.ptr, e->c_tag_prev.ptr,
+                                                           e->c_d_prev.ptr, box, e->c_ng);
+    e->launches++;
+}
+
+// Start-of-substep stamp (_stamp_cdf, mpm_solver_warp.py:3040-3098): lanes whose
+// activity window flipped or that moved are restamped over the union of their
+// current and last boxes; every lane restamps inside that box. With lag_prev
+// (fused ticks) the previous grids catch up at the next stamp or before the
+// closing G2P, so the G2P inside a fused pass reads the tags its grid velocities
+// were computed with.
+void cdf_stamp(gbmpm_engine *e, double time, bool lag_prev, cudaStream_t s) {
+    CdfHost &H = e->cdf;
+    if (H.n == 0) return;
+    if (H.stale_set) { cdf_copy_prev_box(e, H.stale_box, s); H.stale_set = false; }
+    for (int l = 0; l < H.n; ++l) {
+        bool act = time >= (double)H.rec[l].start_time && time < (double)H.rec[l].end_time;
+        if (act != H.active[l]) { H.active[l] = act; H.dirty[l] = true; }
+    }
+    bool any = false;
+    for (int l = 0; l < H.n; ++l) any = any || H.dirty[l];
+    if (!any) return;
+    int box[6] = {INT32_MAX, INT32_MAX, INT32_MAX, INT32_MIN, INT32_MIN, INT32_MIN};
+    bool have = false;
+    auto grow = [&](const int *b) {
+        for (int i = 0; i < 3; ++i) { box[i] = std::min(box[i], b[i]); box[3 + i] = std::max(box[3 + i], b[3 + i]); }
+        have = true;
+    };
+    for (int l = 0; l < H.n; ++l) {
+        if (!H.dirty[l]) continue;
+        int b[6];
+        bool ok = cdf_lane_box(H.rec[l], e->M, b);
+        if (ok) grow(b);
+        if (H.has_prev_box[l]) grow(H.prev_box[l]);
+        H.has_prev_box[l] = ok;
+        if (ok) std::memcpy(H.prev_box[l], b, sizeof b);
+    }
+    for (int l = 0; l < H.n; ++l) H.dirty[l] = false;
+    if (!have) return;
+    H.stamps++;
+    const int ng = e->c_ng;
+    long long vol = (long long)(box[3] - box[0]) * (box[4] - box[1]) * (box[5] - box[2]);
+    k_cdf_clear<<<cdf_grid_blocks(e, vol), 256, 0, s>>>(e->c_tag.ptr, e->c_d.ptr, to_box(box), ng);
+    e->launches++;
+    const float tf = (float)time;
+    for (int l = 0; l < H.n; ++l) {
+        const gbmpm_cdf &r = H.rec[l];
+        int lb[6], clip[6];
+        if (!cdf_lane_box(r, e->M, lb)) continue;
+        bool empty = false;
+        for (int i = 0; i < 3; ++i) {
+            clip[i] = std::max(box[i], lb[i]);
+            clip[3 + i] = std::min(box[3 + i], lb[3 + i]);
+            if (clip[3 + i] <= clip[i]) empty = true;
+        }
+        if (empty || tf < r.start_time || tf >= r.end_time) continue;
+        CdfStamp a{};
+        a.values = r.values; a.valid = r.valid; a.res = r.res; a.lane = l; a.ng = ng;
+        for (int i = 0; i < 3; ++i) { a.origin[i] = r.origin[i]; a.center[i] = r.center[i]; }
+        for (int i = 0; i < 4; ++i) a.quat[i] = r.quat[i];
+        a.cell = r.cell; a.band = r.band; a.dx = e->M.dx;
+        a.box = to_box(clip);
+        a.tag = e->c_tag.ptr; a.d = e->c_d.ptr;
+        long long cv = (long long)(clip[3] - clip[0]) * (clip[4] - clip[1]) * (clip[5] - clip[2]);
+        k_cdf_stamp<<<cdf_grid_blocks(e, cv), 256, 0, s>>>(a);
+        e->launches++;
+    }
+    if (lag_prev) { H.stale_set = true; std::memcpy(H.stale_box, box, sizeof box); }
+    else cdf_copy_prev_box(e, box, s);
+    const int nb = (ng + 3) / 4;
+    int bb[6] = {box[0] >> 2, box[1] >> 2, box[2] >> 2, ((box[3] - 1) >> 2) + 1, ((box[4] - 1) >> 2) + 1,
+                 ((box[5] - 1) >> 2) + 1};
+    long long bv = (long long)(bb[3] - bb[0]) * (bb[4] - bb[1]) * (bb[5] - bb[2]);
+    k_cdf_block_mask<<<cdf_grid_blocks(e, bv), 256, 0, s>>>(e->c_tag.ptr, e->c_tag_prev.ptr, e->c_block.ptr,
+                                                           to_box(bb), nb, ng);
+    e->launches++;
+}
+
+// Per-substep lane pose integration (_integrate_cdf_poses, mpm_solver_warp.py:
+// 3107-3148): centre += dt v and quaternion composed with exp(dt w / 2), in
+// float64 from the fp32 record and rounded back.
+void cdf_integrate(gbmpm_engine *e, double time, double dt, bool lag_prev) {
+    CdfHost &H = e->cdf;
+    if (H.n == 0) return;
+    if (lag_prev && H.lane_prev_stale) H.copy_lane_prev();
+    for (int l = 0; l < H.n; ++l) {
+        gbmpm_cdf &r = H.rec[l];
+        if (!(time >= (double)r.start_time && time < (double)r.end_time)) continue;
+        if (r.velocity[0] == 0.0f && r.velocity[1] == 0.0f && r.velocity[2] == 0.0f && r.omega[0] == 0.0f &&
+            r.omega[1] == 0.0f && r.omega[2] == 0.0f)
+            continue;
+        for (int a = 0; a < 3; ++a) r.center[a] = (float)((double)r.center[a] + dt * (double)r.velocity[a]);
+        double w[3] = {r.omega[0], r.omega[1], r.omega[2]};
+        double sp = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        if (!(sp * dt < 1e-12)) {
+            double q[4] = {r.quat[0], r.quat[1], r.quat[2], r.quat[3]};
+            double half = 0.5 * sp * dt, sh = std::sin(half);
+            double d[4] = {w[0] / sp * sh, w[1] / sp * sh, w[2] / sp * sh, std::cos(half)};
+            double o[4] = {d[3] * q[0] + d[0] * q[3] + d[1] * q[2] - d[2] * q[1],
+                           d[3] * q[1] - d[0] * q[2] + d[1] * q[3] + d[2] * q[0],
+                           d[3] * q[2] + d[0] * q[1] - d[1] * q[0] + d[2] * q[3],
+                           d[3] * q[3] - d[0] * q[0] - d[1] * q[1] - d[2] * q[2]};
+            double nr = std::sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2] + o[3] * o[3]);
+            for (int i = 0; i < 4; ++i) r.quat[i] = (float)(o[i] / nr);
+        }
+        H.sync_lane(l);
+        H.dirty[l] = true;
+        H.lane_prev_stale = true;
+    }
+    if (!lag_prev && H.lane_prev_stale) H.copy_lane_prev();
+}
+
 // Records the launches of one tick on stream s.
-void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cudaStream_t s, bool profile) {
+// With CPIC lanes the host stamps and integrates lane poses between the
+// launches (t0 = the tick's start time, dt its float64 substep), so such ticks
+// run live, on the direct kernel.
+void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cudaStream_t s, bool profile,
+                 double t0 = 0.0, double dt = 0.0) {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     if (profile) { cudaEventCreate(&ev0); cudaEventCreate(&ev1); }
     auto timed = [&](int phase, auto fn) {
@@ -1885,21 +2451,35 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
     const int *perm = nullptr;
     if (reorder) timed(5, [&] { perm = record_ws_begin(e, s); });
     const gbmpm_particles &P = reorder ? e->W : e->P;
+    const bool cdf = e->cdf.n > 0 && !reorder;
+    double tc = t0;
     for (int sub = 0; sub < S; ++sub) {
         int list = sub & 1;
+        if (cdf) cdf_stamp(e, tc, fused, s);
         PK k = make_pk(e, P, dtf, list);
         bool last_stress = fused ? (sub == S - 1) : true;
         if (!fused || sub == 0) {
             int mode = PASS_STRESS | PASS_P2G | (last_stress ? PASS_STORE_ALL : 0);
             timed(0, [&] { launch_particles(e, k, mode, reorder, s); });
         } else {
-            int mode = PASS_G2P | PASS_STRESS | PASS_P2G | (last_stress ? PASS_STORE_ALL : 0);
+            // a CPIC ghost velocity starts from the particle's previous velocity
+            int mode = PASS_G2P | PASS_STRESS | PASS_P2G | (last_stress ? PASS_STORE_ALL : 0) |
+                       (cdf ? PASS_STORE_VC : 0);
             timed(2, [&] { launch_particles(e, k, mode, reorder, s); });
         }
         timed(3, [&] { launch_grid(e, dtf, sub, list, s); });
-        if (!fused) timed(4, [&] { launch_particles(e, k, PASS_G2P | PASS_RESET_LISTS, reorder, s); });
+        if (cdf) cdf_integrate(e, tc, dt, fused);
+        tc = tc + dt;
+        if (!fused) {
+            PK kg = make_pk(e, P, dtf, list);
+            timed(4, [&] { launch_particles(e, kg, PASS_G2P | PASS_RESET_LISTS, reorder, s); });
+        }
     }
     if (fused) {
+        if (cdf && e->cdf.stale_set) {
+            cdf_copy_prev_box(e, e->cdf.stale_box, s);
+            e->cdf.stale_set = false;
+        }
         PK k = make_pk(e, P, dtf, 0);
         timed(4, [&] { launch_particles(e, k, PASS_G2P | PASS_RESET_LISTS, reorder, s); });
     }
@@ -1950,6 +2530,8 @@ void gbmpm_engine_destroy(gbmpm_engine *e) {
     e->d_braw.release(); e->d_bcur.release(); e->d_bprev.release(); e->d_bcount.release();
     e->ws_buf.release(); e->ws_keys[0].release(); e->ws_keys[1].release(); e->ws_idx[0].release();
     e->ws_idx[1].release(); e->ws_hist.release();
+    e->c_tag.release(); e->c_tag_prev.release(); e->c_block.release(); e->c_d.release(); e->c_d_prev.release();
+    e->c_wrench.release();
     delete e;
 }
 
@@ -2039,6 +2621,103 @@ int gbmpm_get_colliders(gbmpm_engine *e, gbmpm_collider *c, int32_t n) {
     return GBMPM_OK;
 }
 
+// add_cdf_collider / set_cdf_pose (mpm_solver_warp.py:2819-2981). The first
+// lanes allocate the node grids for the current n_grid; later calls may only
+// append lanes or change existing ones. A lane whose centre or quaternion changed
+// is restamped at the next substep; any pose or rate change refreshes the lane
+// arrays the transfer passes read.
+int gbmpm_set_cdf(gbmpm_engine *e, const gbmpm_cdf *lanes, int32_t n) {
+    if (!e || (n > 0 && !lanes)) return fail(GBMPM_ERR_ARG, "null argument");
+    if (!e->modeled) return fail(GBMPM_ERR_STATE, "model not set (call gbmpm_set_model)");
+    if (e->M.periodic_x) return fail(GBMPM_ERR_UNSUPPORTED, "CDF colliders do not wrap the periodic x axis");
+    CdfHost &H = e->cdf;
+    if (n < H.n || n > GBMPM_MAX_CDF)
+        return fail(GBMPM_ERR_ARG, "CDF lanes can only be added, at most " + std::to_string(GBMPM_MAX_CDF));
+    for (int l = 0; l < n; ++l) {
+        const gbmpm_cdf &r = lanes[l];
+        if (!r.values || !r.valid || r.res < 2 || !(r.cell > 0.0f) || !(r.band > 0.0f))
+            return fail(GBMPM_ERR_ARG, "CDF lane " + std::to_string(l) + ": needs values, valid, res >= 2, cell > 0, band > 0");
+        if (r.surface_type < 0 || r.surface_type > 2)
+            return fail(GBMPM_ERR_ARG, "CDF surface_type must be 0 (sticky), 1 (slip) or 2 (separable)");
+    }
+    if (n > 0 && e->c_ng == 0) {
+        const int ng = e->M.n_grid;
+        const size_t N = (size_t)ng * ng * ng;
+        const int nb = (ng + 3) / 4;
+        GB_CUDA(e->c_tag.ensure(N)); GB_CUDA(e->c_tag_prev.ensure(N));
+        GB_CUDA(e->c_d.ensure(N)); GB_CUDA(e->c_d_prev.ensure(N));
+        GB_CUDA(e->c_block.ensure((size_t)nb * nb * nb));
+        GB_CUDA(e->c_wrench.ensure(6 * GBMPM_MAX_CDF));
+        GB_CUDA(cudaMemset(e->c_tag.ptr, 0, N * sizeof(int)));
+        GB_CUDA(cudaMemset(e->c_tag_prev.ptr, 0, N * sizeof(int)));
+        GB_CUDA(cudaMemset(e->c_block.ptr, 0, (size_t)nb * nb * nb * sizeof(int)));
+        GB_CUDA(cudaMemset(e->c_wrench.ptr, 0, 6 * GBMPM_MAX_CDF * sizeof(double)));
+        e->c_ng = ng;
+        CdfBox all{{0, 0, 0}, {ng, ng, ng}};
+        int blocks = cdf_grid_blocks(e, (long long)N);
+        k_cdf_clear<<<blocks, 256>>>(e->c_tag.ptr, e->c_d.ptr, all, ng);
+        k_cdf_clear<<<blocks, 256>>>(e->c_tag_prev.ptr, e->c_d_prev.ptr, all, ng);
+        e->launches += 2;
+        GB_CUDA(cudaGetLastError());
+        GB_CUDA(cudaDeviceSynchronize());
+    }
+    for (int l = 0; l < n; ++l) {
+        const gbmpm_cdf &r = lanes[l];
+        if (l >= H.n) {
+            H.rec[l] = r;
+            H.dirty[l] = true;
+            H.active[l] = false;   // settled by the first stamp, which restamps the lane anyway
+            H.has_prev_box[l] = false;
+            H.sync_lane(l);
+            continue;
+        }
+        gbmpm_cdf &o = H.rec[l];
+        bool moved = std::memcmp(o.center, r.center, sizeof o.center) != 0 ||
+                     std::memcmp(o.quat, r.quat, sizeof o.quat) != 0;
+        bool synced = std::memcmp(o.velocity, r.velocity, sizeof o.velocity) != 0 ||
+                      std::memcmp(o.omega, r.omega, sizeof o.omega) != 0;
+        o = r;
+        if (moved) H.dirty[l] = true;
+        if (moved || synced) { H.sync_lane(l); H.lane_prev_stale = true; }
+    }
+    H.n = n;
+    return GBMPM_OK;
+}
+
+int gbmpm_get_cdf(gbmpm_engine *e, gbmpm_cdf *lanes, int32_t n) {
+    if (!e || (n > 0 && !lanes)) return fail(GBMPM_ERR_ARG, "null argument");
+    if (n > e->cdf.n) return fail(GBMPM_ERR_ARG, "more lanes requested than set");
+    for (int l = 0; l < n; ++l) lanes[l] = e->cdf.rec[l];
+    return GBMPM_OK;
+}
+
+int gbmpm_cdf_wrench(gbmpm_engine *e, int32_t lane, double out[6], void *stream) {
+    if (!e || !out) return fail(GBMPM_ERR_ARG, "null argument");
+    if (lane < 0 || lane >= e->cdf.n) return fail(GBMPM_ERR_ARG, "CDF lane out of range");
+    cudaStream_t s = (cudaStream_t)stream;
+    GB_CUDA(cudaMemcpyAsync(out, e->c_wrench.ptr + 6 * lane, 6 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    return GBMPM_OK;
+}
+
+int gbmpm_cdf_grids(gbmpm_engine *e, int32_t *tag_out, float *d_out, int64_t *stamps, void *stream) {
+    if (!e) return fail(GBMPM_ERR_ARG, "null argument");
+    if (stamps) *stamps = e->cdf.stamps;
+    if (e->c_ng == 0) return (tag_out || d_out) ? fail(GBMPM_ERR_STATE, "no CDF collider set") : GBMPM_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t N = (size_t)e->c_ng * e->c_ng * e->c_ng;
+    if (tag_out) GB_CUDA(cudaMemcpyAsync(tag_out, e->c_tag.ptr, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    if (d_out) GB_CUDA(cudaMemcpyAsync(d_out, e->c_d.ptr, N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    return GBMPM_OK;
+}
+
+int gbmpm_reset_cdf_wrench(gbmpm_engine *e, void *stream) {
+    if (!e) return fail(GBMPM_ERR_ARG, "null argument");
+    if (e->cdf.n == 0) return GBMPM_OK;
+    GB_CUDA(cudaMemsetAsync(e->c_wrench.ptr, 0, 6 * GBMPM_MAX_CDF * sizeof(double), (cudaStream_t)stream));
+    return GBMPM_OK;
+}
+
 }  // extern "C"
 
 namespace {
@@ -2078,10 +2757,20 @@ extern "C" {
 
 int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32_t flags, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
-    if (e && time && e->bound && e->P.n == 0 && substeps >= 1 && dt > 0.0) {
+    if (e && time && e->bound && e->P.n == 0 && e->cdf.n == 0 && substeps >= 1 && dt > 0.0) {
         for (int i = 0; i < substeps; ++i) *time += dt;
         return GBMPM_OK;
     }
+    const bool cdf = e && e->cdf.n > 0;
+    if (cdf) {
+        int rc = check_ready(e);
+        if (rc) return rc;
+        if (e->c_ng != e->M.n_grid) return fail(GBMPM_ERR_STATE, "CDF grids were sized for another n_grid");
+        if (e->M.periodic_x) return fail(GBMPM_ERR_UNSUPPORTED, "CDF colliders do not wrap the periodic x axis");
+        if (e->P.n > 0 && !e->P.cdf_tag) return fail(GBMPM_ERR_ARG, "CDF colliders need particles.cdf_tag");
+        flags &= ~(GBMPM_TICK_GRAPH | GBMPM_TICK_REORDER);
+    }
+    const double t0 = time ? *time : 0.0;
     bool reorder = false;
     int rc = prepare_tick(e, time, dt, substeps, flags, s, reorder);
     if (rc) return rc;
@@ -2090,7 +2779,7 @@ int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32
     const bool use_graph = (flags & GBMPM_TICK_GRAPH) && !profile;
     const float dtf = (float)dt;
     if (!use_graph) {
-        record_tick(e, dtf, substeps, fused, reorder, s, profile);
+        record_tick(e, dtf, substeps, fused, reorder, s, profile, t0, dt);
         GB_CUDA(cudaGetLastError());
         return GBMPM_OK;
     }
@@ -2221,7 +2910,7 @@ int gbmpm_sort_particles(gbmpm_engine *e, double dx, int32_t *sorted_out, int32_
     for (float *a : f1) GB_CUDA(permute(a, 1));
     float *c6[] = {P.init_cov, P.cov};
     for (float *a : c6) GB_CUDA(permute(a, 6));
-    int *i1[] = {P.selection, P.material};
+    int *i1[] = {P.selection, P.material, P.cdf_tag};
     for (int *a : i1) GB_CUDA(permute(reinterpret_cast<float *>(a), 1));
     if (perm_out) GB_CUDA(cudaMemcpyAsync(perm_out, perm, (size_t)n * sizeof(int), cudaMemcpyDeviceToDevice, s));
     if (sorted_out) *sorted_out = 1;
@@ -2344,6 +3033,9 @@ int gbmpm_batch_tick(gbmpm_batch *b, double *times, double dt, int32_t substeps,
     if (flags & GBMPM_TICK_PROFILE) return fail(GBMPM_ERR_UNSUPPORTED, "profiling is per engine (gbmpm_tick)");
     cudaStream_t s = (cudaStream_t)stream;
     const int n = (int)b->engines.size();
+    for (int i = 0; i < n; ++i)
+        if (b->engines[i]->cdf.n > 0)
+            return fail(GBMPM_ERR_UNSUPPORTED, "scenes with CDF colliders tick alone (gbmpm_tick)");
     std::vector<char> reorder(n, 0);
     for (int i = 0; i < n; ++i) {
         bool r = false;

@@ -27,6 +27,69 @@ class SDFData:
         return int(self.values.shape[0])
 
 
+@dataclass
+class CDFData:
+    """Side-signed distance field around an OPEN oriented sheet for CPIC colliders
+    (warpmpm.geometry.CDFData, src/warpmpm/geometry/mesh_sdf.py:47-76)."""
+    values: np.ndarray      # [res,res,res] signed distance to the sheet (m)
+    valid: np.ndarray       # [res,res,res] 1 where distance and side are trustworthy
+    origin: np.ndarray
+    cell: float
+    band: float             # metres from the sheet within which valid can be 1
+
+    @property
+    def res(self) -> int:
+        return int(self.values.shape[0])
+
+
+def save_cdf(cdf: CDFData, path) -> None:
+    path = Path(path)
+    path.parent.mkdir(parents=True, exist_ok=True)
+    np.savez_compressed(path, values=cdf.values, valid=cdf.valid, origin=cdf.origin, cell=cdf.cell, band=cdf.band)
+
+
+def load_cdf(path) -> CDFData:
+    d = np.load(path)
+    return CDFData(values=d["values"], valid=d["valid"], origin=d["origin"], cell=float(d["cell"]),
+                   band=float(d["band"]))
+
+
+def sheet_cdf(normal: str = "z", size: float = 0.5, res: int = 64, band_cells: float = 3.0,
+              margin_cells: float = 4.0) -> CDFData:
+    """CDF of a square sheet of edge `size` through the body origin with normal +x or +z,
+    on the grid build_surface_cdf uses (mesh_sdf.py:412-480): distance to the sheet,
+    side from its normal, valid within `band` of the sheet and farther than `band`
+    from its open rim."""
+    span = float(size)
+    cell = span / (res - 1 - 2 * margin_cells)
+    band = band_cells * cell
+    L = cell * (res - 1)
+    origin = np.full(3, -0.5 * L)
+    ax = origin[0] + cell * np.arange(res)
+    X, Y, Z = np.meshgrid(ax, ax, ax, indexing="ij")
+    if normal == "x":
+        dn, u, v = X, Y, Z
+    elif normal == "z":
+        dn, u, v = Z, X, Y
+    else:
+        raise ValueError("normal must be 'x' or 'z'")
+    h = 0.5 * size
+    # distance to the square patch and to its rim (the patch boundary)
+    du = np.maximum(np.abs(u) - h, 0.0)
+    dv = np.maximum(np.abs(v) - h, 0.0)
+    dist = np.sqrt(dn * dn + du * du + dv * dv)
+    side = np.where(dn >= 0.0, 1.0, -1.0)
+    eu = np.abs(np.abs(u) - h)
+    ev = np.abs(np.abs(v) - h)
+    inside_u = np.abs(u) <= h
+    inside_v = np.abs(v) <= h
+    rim_u = np.sqrt(dn * dn + eu * eu + np.where(inside_v, 0.0, dv * dv))   # distance to the u = +-h edges
+    rim_v = np.sqrt(dn * dn + ev * ev + np.where(inside_u, 0.0, du * du))
+    rim = np.minimum(rim_u, rim_v)
+    valid = ((dist <= band) & (rim > band)).astype(np.float64)
+    return CDFData(values=side * dist, valid=valid, origin=origin, cell=float(cell), band=float(band))
+
+
 def save_sdf(sdf: SDFData, path) -> None:
     path = Path(path)
     path.parent.mkdir(parents=True, exist_ok=True)
@@ -61,4 +124,4 @@ def analytic_sdf(kind: str, res: int = 48, half_extent=(0.05, 0.05, 0.05), radiu
     return SDFData(values=vals, grads=grads, origin=origin, cell=float(cell), sdf_max=float(vals.max()))
 
 
-__all__ = ["SDFData", "analytic_sdf", "load_sdf", "save_sdf"]
+__all__ = ["CDFData", "SDFData", "analytic_sdf", "load_cdf", "load_sdf", "save_cdf", "save_sdf", "sheet_cdf"]

@@ -192,6 +192,38 @@ def sdf_collider(val_ptr: int, grad_ptr: int, res: int, origin, cell, center, qu
     return c
 
 
+def cdf_lane(values_ptr: int, valid_ptr: int, res: int, origin, cell, center, quat, velocity, omega,
+             band: float, surface_id: int, friction: float, start_time: float, end_time: float) -> _abi.Cdf:
+    """CDFCollider record of add_cdf_collider (mpm_solver_warp.py:2853-2869)."""
+    c = _abi.Cdf()
+    c.values, c.valid, c.res = values_ptr, valid_ptr, int(res)
+    c.surface_type = int(surface_id)
+    _vec(c.origin, origin)
+    c.cell = f32(cell)
+    _vec(c.center, center)
+    _vec(c.quat, quat)
+    _vec(c.velocity, velocity)
+    _vec(c.omega, omega)
+    c.band = f32(band)
+    c.friction = f32(friction)
+    c.start_time, c.end_time = f32(start_time), f32(end_time)
+    return c
+
+
+def cdf_band(built_band: float, dx: float, band=None) -> float:
+    """Runtime band rules of add_cdf_collider (mpm_solver_warp.py:2833-2849)."""
+    import warnings
+    if band is None:
+        band = min(float(built_band), 2.0 * float(dx))
+    if band > float(built_band) + 1e-12:
+        raise ValueError(f"runtime band ({band * 1e3:.1f} mm) exceeds the band the field was built with "
+                         f"({float(built_band) * 1e3:.1f} mm); rebuild the CDF with a larger band_cells.")
+    if band < 1.5 * float(dx):
+        warnings.warn(f"CDF band ({band * 1e3:.1f} mm) is below 1.5 dx ({1.5 * dx * 1e3:.1f} mm): straddling "
+                      f"particle-node pairs can go untagged and the wall can leak.", RuntimeWarning, stacklevel=3)
+    return float(band)
+
+
 def grid_guard_message(lo: float, hi: float, lim: float, dx: float) -> str:
     """Text of the edge-guard RuntimeError (core/solver.py:508-512)."""
     return (f"particles within 2 cells of the grid edge (x in [{lo:.4f}, {hi:.4f}] m, domain [0, {lim}] m, "

@@ -244,6 +244,9 @@ class Solver:
         self._keep: list = []          # tensors referenced by collider records
         self._mat_current = 0
         self._sdf_guard: dict = {}
+        self._cdf: list = []           # CPIC lane records (engine copy is authoritative)
+        self._cdf_guard: dict = {}
+        self._cdf_keep: list = []      # device copies of the lanes' fields
         self._rigid_surfaces: list = []
         self._update_cov = False
 
@@ -294,6 +297,7 @@ class Solver:
             "lam": torch.zeros(n, **f), "yield_stress": torch.zeros(n, **f),
             "material": torch.zeros(n, device=dev, dtype=torch.int32),
             "selection": torch.zeros(n, device=dev, dtype=torch.int32),
+            "cdf_tag": torch.zeros(n, device=dev, dtype=torch.int32),
             "init_cov": None, "cov": None,
         }
         if cov6 is not None:
@@ -324,7 +328,7 @@ class Solver:
         p = _abi.Particles()
         p.n = self._n
         for k in ("x", "v", "C", "F", "F_trial", "L", "stress", "mass", "vol", "density", "Jp", "mu", "lam",
-                  "yield_stress", "material", "selection", "cov", "init_cov"):
+                  "yield_stress", "material", "selection", "cov", "init_cov", "cdf_tag"):
             setattr(p, k, self._ptr(k))
         g = _abi.Grid()
         g.n_grid = int(self.grid.n_grid)
@@ -619,9 +623,128 @@ class Solver:
     def add_cdf_collider(self, cdf, center, quat=(0.0, 0.0, 0.0, 1.0), velocity=(0.0, 0.0, 0.0),
                          omega=(0.0, 0.0, 0.0), band=None, surface: str = "separable", friction: float = 0.4,
                          start_time: float = 0.0, end_time: float = 1.0e9) -> int:
+        """An OPEN oriented surface (geometry.CDFData) as a CPIC thin-boundary collider
+        (core/solver.py:363-386, mpm_solver_warp.py:2819-2881): particle-node transfers
+        across the surface are severed. Returns a lane handle, a separate space from the
+        grid-BC colliders; at most 4 lanes per scene."""
         if self.periodic_x:
             raise NotImplementedError("CDF colliders do not wrap the periodic x axis")
-        raise NotImplementedError("CPIC thin-boundary (CDF) colliders are not built in this engine")
+        self._require_loaded()
+        torch = _torch()
+        lane = len(self._cdf)
+        if lane >= _abi.MAX_CDF:
+            raise ValueError(f"at most {_abi.MAX_CDF} CDF colliders per scene")
+        band = host.cdf_band(cdf.band, float(self._model.dx), band)
+        surface_id = host.SDF_SURFACES[surface]
+        res = int(np.asarray(cdf.values).shape[0])
+        dev = self._t["x"].device
+        val = torch.from_numpy(np.ascontiguousarray(cdf.values, dtype=np.float32)).to(dev)
+        valid = torch.from_numpy(np.ascontiguousarray(cdf.valid, dtype=np.float32)).to(dev)
+        self._cdf_keep += [val, valid]
+        rec = host.cdf_lane(val.data_ptr(), valid.data_ptr(), res, cdf.origin, cdf.cell, center, quat, velocity,
+                            omega, band, surface_id, friction, start_time, end_time)
+        self._cdf_guard[lane] = {"r_max": host.sdf_r_max(cdf.origin, cdf.cell, res), "band": float(band),
+                                 "warned": False}
+        self._sync_engine()
+        self._pull_cdf()
+        self._cdf.append(rec)
+        self._push_cdf()
+        return lane
+
+    def _pull_cdf(self) -> None:
+        n = len(self._cdf)
+        if n == 0:
+            return
+        arr = (_abi.Cdf * n)()
+        _abi.check(self._eng.lib.gbmpm_get_cdf(self._eng.h, arr, n), "gbmpm_get_cdf")
+        self._cdf = [arr[i] for i in range(n)]
+
+    def _push_cdf(self) -> None:
+        n = len(self._cdf)
+        arr = (_abi.Cdf * max(1, n))(*self._cdf)
+        _abi.check(self._eng.lib.gbmpm_set_cdf(self._eng.h, arr, n), "gbmpm_set_cdf")
+
+    def set_cdf_pose(self, handle: int, center=None, quat=None, velocity=None, omega=None) -> Solver:
+        """Start-of-tick pose of a CDF collider (mpm_solver_warp.py:2945-2996); ticks
+        integrate centre and quaternion per substep from velocity and omega. Warns once
+        when a jump sweeps the surface farther than the band."""
+        if not 0 <= handle < len(self._cdf):
+            raise IndexError(f"no CDF collider with handle {handle}")
+        self._pull_cdf()
+        c = self._cdf[handle]
+        guard = self._cdf_guard.get(handle)
+        if guard is not None and not guard["warned"]:
+            jump = 0.0
+            if center is not None:
+                jump += float(np.linalg.norm(np.array([float(center[k]) - c.center[k] for k in range(3)])))
+            if quat is not None:
+                dot = abs(sum(float(quat[k]) * c.quat[k] for k in range(4)))
+                jump += 2.0 * float(np.arccos(min(1.0, dot))) * guard["r_max"]
+            if jump > guard["band"]:
+                guard["warned"] = True
+                warnings.warn(
+                    f"set_cdf_pose jumped the surface by up to {jump * 1e3:.2f} mm in one tick, more than the "
+                    f"band ({guard['band'] * 1e3:.2f} mm): material in the swept region can end up on the wrong "
+                    f"side. Drive the pose in smaller per-tick steps.", RuntimeWarning, stacklevel=2)
+        if center is not None:
+            host._vec(c.center, center)
+        if quat is not None:
+            host._vec(c.quat, quat)
+        if velocity is not None:
+            host._vec(c.velocity, velocity)
+        if omega is not None:
+            host._vec(c.omega, omega)
+        self._push_cdf()
+        return self
+
+    def reset_cdf_wrench(self) -> Solver:
+        """Zero the CDF reaction accumulators of every lane."""
+        if self._cdf:
+            _abi.check(self._eng.lib.gbmpm_reset_cdf_wrench(self._eng.h, self._stream()), "gbmpm_reset_cdf_wrench")
+        return self
+
+    def cdf_grids(self):
+        """(tag, distance) node grids of the last CPIC stamp as host arrays, and the
+        number of stamps so far."""
+        torch = _torch()
+        ng = int(self.grid.n_grid)
+        dev = self._t["x"].device
+        stamps = C.c_int64(0)
+        if not self._cdf:
+            return np.zeros((ng, ng, ng), np.int32), np.zeros((ng, ng, ng), np.float32), 0
+        tag = torch.empty(ng, ng, ng, device=dev, dtype=torch.int32)
+        d = torch.empty(ng, ng, ng, device=dev, dtype=torch.float32)
+        _abi.check(self._eng.lib.gbmpm_cdf_grids(self._eng.h, tag.data_ptr(), d.data_ptr(), C.byref(stamps),
+                                                 self._stream()), "gbmpm_cdf_grids")
+        return tag.cpu().numpy(), d.cpu().numpy(), int(stamps.value)
+
+    def _cdf_tunnel_check(self, dt: float) -> None:
+        """Warn once per lane whose surface sweeps more than its band per substep
+        (mpm_solver_warp.py:3119-3137)."""
+        for lane, c in enumerate(self._cdf):
+            guard = self._cdf_guard[lane]
+            if guard["warned"] or not (c.start_time <= self._time < c.end_time):
+                continue
+            v = [c.velocity[k] for k in range(3)]
+            w = np.array([c.omega[k] for k in range(3)], dtype=float)
+            if v[0] == 0.0 and v[1] == 0.0 and v[2] == 0.0 and not w.any():
+                continue
+            speed = float(np.hypot(np.hypot(v[0], v[1]), v[2])) + float(np.linalg.norm(w)) * guard["r_max"]
+            if speed * dt > guard["band"]:
+                guard["warned"] = True
+                warnings.warn(
+                    f"CDF collider surface sweeps {speed * dt * 1e3:.2f} mm per substep, more than the band "
+                    f"({guard['band'] * 1e3:.2f} mm): material can end up on the wrong side. Reduce dt or the "
+                    f"pose rate, or rebuild with a larger band.", RuntimeWarning, stacklevel=3)
+
+    def cdf_wrench(self, handle: int, dt: float) -> dict:
+        """Reaction the material exerts on a CDF collider, summed from the blocked P2G
+        deposits since the last reset (core/solver.py:401-413): {'force', 'torque'}."""
+        out = (C.c_double * 6)()
+        _abi.check(self._eng.lib.gbmpm_cdf_wrench(self._eng.h, int(handle), out, self._stream()),
+                   "gbmpm_cdf_wrench")
+        w = np.array(out[:], dtype=float)
+        return {"force": w[:3] / dt, "torque": w[3:] / dt}
 
     def reset_tool_force(self, handle: int) -> Solver:
         self._reset_wrench(handle)
@@ -681,6 +804,9 @@ class Solver:
         self._pull_colliders()
         if self._sdf_guard:
             self._sdf_tunnel_check(dt)
+        if self._cdf:
+            self._pull_cdf()
+            self._cdf_tunnel_check(dt)
         self._sync_engine()
         flags = self._tick_flags()
         t = C.c_double(self._time)
@@ -887,7 +1013,7 @@ class Solver:
         out = {k: (None if v is None else v.detach().cpu().numpy().copy())
                for k, v in self._t.items() if k in ("x", "v", "C", "F", "F_trial", "L", "stress", "mass", "vol",
                                                     "density", "Jp", "mu", "lam", "yield_stress", "material",
-                                                    "selection", "cov", "init_cov")}
+                                                    "selection", "cov", "init_cov", "cdf_tag")}
         model = _abi.Model()
         C.memmove(C.byref(model), C.byref(self._model), C.sizeof(_abi.Model))
         out["model"] = model
@@ -900,6 +1026,14 @@ class Solver:
         out["colliders"] = cols
         out["handles"] = list(self._handles)
         out["sdf_host"] = {t.data_ptr(): t.cpu().numpy().copy() for t in self._keep}
+        self._pull_cdf()
+        lanes = []
+        for rec in self._cdf:
+            r = _abi.Cdf()
+            C.memmove(C.byref(r), C.byref(rec), C.sizeof(_abi.Cdf))
+            lanes.append(r)
+        out["cdf_lanes"] = lanes
+        out["cdf_host"] = {t.data_ptr(): t.cpu().numpy().copy() for t in self._cdf_keep}
         out["time"] = self._time
         return out
 

@@ -442,6 +442,55 @@ M3 rm_sand(const M3& Ft, const gbmpm_particles* P, const gbmpm_model* m, int p, 
     return Fe;
 }
 
+// CPIC (CDF) state; its kernels follow the collider section
+constexpr int kOwnerShift = 8;
+constexpr int kOwnerMask = 3 << kOwnerShift;
+
+struct CdfState {
+    int n_grid = 0, nb = 0, n = 0;
+    std::vector<int32_t> tag, tag_prev, block;
+    std::vector<float> d, d_prev;
+    gbmpm_cdf rec[GBMPM_MAX_CDF];
+    float c_cur[4][3] = {}, v_cur[4][3] = {}, w_cur[4][3] = {};
+    float c_prev[4][3] = {}, v_prev[4][3] = {}, w_prev[4][3] = {};
+    float fric[4] = {};
+    int type[4] = {};
+    bool dirty[4] = {}, active[4] = {}, has_prev_box[4] = {};
+    int prev_box[4][6] = {};
+    bool stale_set = false;
+    int stale_box[6] = {};
+    bool lane_prev_stale = false;
+    int stamp_count = 0;
+    void alloc(int ng) {
+        n_grid = ng;
+        nb = (ng + 3) / 4;
+        size_t N = (size_t)ng * ng * ng;
+        tag.assign(N, 0); tag_prev.assign(N, 0);
+        d.assign(N, 1.0e9f); d_prev.assign(N, 1.0e9f);
+        block.assign((size_t)nb * nb * nb, 0);
+    }
+    size_t idx(int x, int y, int z) const { return ((size_t)x * n_grid + y) * n_grid + z; }
+    void sync_lane(int l) {  // _sync_cdf_lane (mpm_solver_warp.py:2883-2905)
+        const gbmpm_cdf& r = rec[l];
+        for (int a = 0; a < 3; ++a) { c_cur[l][a] = r.center[a]; v_cur[l][a] = r.velocity[a]; w_cur[l][a] = r.omega[a]; }
+        fric[l] = r.friction;
+        type[l] = r.surface_type;
+    }
+    void copy_lane_prev() {
+        std::memcpy(c_prev, c_cur, sizeof c_cur);
+        std::memcpy(v_prev, v_cur, sizeof v_cur);
+        std::memcpy(w_prev, w_cur, sizeof w_cur);
+        lane_prev_stale = false;
+    }
+};
+
+inline bool cdf_incompatible(int pc, int nt);
+bool cdf_stencil_near(const CdfState& S, const int* b);
+struct Weights;
+int cdf_particle_tag(const CdfState& S, const Weights& W, bool use_prev);
+int cdf_persist(int old, int fresh);
+V3 cdf_ghost(const CdfState& S, const gbmpm_model* M, float dt, V3 xp, V3 vp, int pc, const Weights& W);
+
 // ----------------------------------------------------- particle stages -----
 struct Weights {
     int base[3];
@@ -500,6 +549,8 @@ struct Ctx {
     float dt;
     bool atomic;   // parallel mode
     int oob;
+    CdfState* cdf = nullptr;     // CPIC lanes (null or n == 0: feature off)
+    float* cdf_wrench = nullptr; // [4][6] blocked-deposit reaction
 };
 
 inline int wrapx(int ix, int n) { return ((ix % n) + n) % n; }
@@ -525,6 +576,9 @@ void p2g_particle(Ctx& c, int p) {
     float mass = P->mass[p], vol = P->vol[p];
     V3 v = load3(P->v + 3 * (size_t)p);
     M3 fs = mscale(stress, -vol);
+    int pc = 0;
+    if (c.cdf && c.cdf->n > 0 && cdf_stencil_near(*c.cdf, W.base))
+        pc = cdf_persist(P->cdf_tag ? P->cdf_tag[p] : 0, cdf_particle_tag(*c.cdf, W, false));
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j)
             for (int k = 0; k < 3; ++k) {
@@ -537,6 +591,27 @@ void p2g_particle(Ctx& c, int p) {
                 V3 add = vadd(vscale(vadd(v, mvmul(C, dpos)), weight * mass), vscale(ef, c.dt));
                 size_t id = G.idx(ix, iy, iz);
                 float dm = weight * mass;
+                if (pc != 0) {
+                    int nt = c.cdf->tag[id];
+                    if (cdf_incompatible(pc, nt)) {   // blocked deposit = reaction on the sheet
+                        int own = (nt >> kOwnerShift) & 3;
+                        V3 xw = mkv((float)ix * M->dx, (float)iy * M->dx, (float)iz * M->dx);
+                        V3 tq = vcross(vsub(xw, load3(c.cdf->c_cur[own])), add);
+                        float* acc = c.cdf_wrench + 6 * own;
+                        for (int a = 0; a < 3; ++a) {
+                            if (c.atomic) {
+#pragma omp atomic
+                                acc[a] += add[a];
+#pragma omp atomic
+                                acc[3 + a] += tq[a];
+                            } else {
+                                acc[a] += add[a];
+                                acc[3 + a] += tq[a];
+                            }
+                        }
+                        continue;
+                    }
+                }
                 if (c.atomic) {
 #pragma omp atomic
                     G.vin[3 * id + 0] += add[0];
@@ -579,6 +654,15 @@ void g2p_particle(Ctx& c, int p) {
         if (a == 0 && M->periodic_x) continue;
         if (W.base[a] < 0 || W.base[a] + 2 >= n) { c.oob = 1; return; }
     }
+    int pc = 0;
+    V3 ghost = mkv(0, 0, 0);
+    if (c.cdf && c.cdf->n > 0) {
+        if (cdf_stencil_near(*c.cdf, W.base))
+            pc = cdf_persist(P->cdf_tag ? P->cdf_tag[p] : 0, cdf_particle_tag(*c.cdf, W, true));
+        if (P->cdf_tag) P->cdf_tag[p] = pc;
+        if (pc != 0)
+            ghost = cdf_ghost(*c.cdf, M, c.dt, load3(P->x + 3 * (size_t)p), load3(P->v + 3 * (size_t)p), pc, W);
+    }
     V3 nv = mkv(0, 0, 0);
     M3 nC = zero33(), nF = zero33();
     for (int i = 0; i < 3; ++i)
@@ -590,6 +674,7 @@ void g2p_particle(Ctx& c, int p) {
                 float weight = W.w[0][i] * W.w[1][j] * W.w[2][k];
                 size_t id = G.idx(ix, iy, iz);
                 V3 gv = load3(&G.vout[3 * id]);
+                if (pc != 0 && cdf_incompatible(pc, c.cdf->tag_prev[id])) gv = ghost;
                 nv = vadd(nv, vscale(gv, weight));
                 nC = madd(nC, mscale(outer(gv, dpos), weight * M->inv_dx * 4.0f));
                 V3 dwt = dweight(W, i, j, k, M->inv_dx);
@@ -917,6 +1002,287 @@ void integrate_pose(gbmpm_collider& c, double time, double dt) {
     }
 }
 
+// ------------------------------------------------------------ CPIC (CDF) -----
+// Thin-boundary colliders: node tag bits (bit 2l valid, 2l+1 side, owner lane in
+// bits 8..9), owner distance, the previous stamp's copies and a 4^3 occupancy
+// mask (mpm_solver_warp.py:94-183, mpm_utils.py:648-816).
+// cdf_pair_incompatible (mpm_utils.py:648-654)
+inline bool cdf_incompatible(int pc, int nt) { return ((pc & nt & 0x55) & ((pc ^ nt) >> 1)) != 0; }
+
+// cdf_stencil_near (mpm_utils.py:657-675)
+bool cdf_stencil_near(const CdfState& S, const int* b) {
+    for (int bi = b[0] >> 2; bi <= (b[0] + 2) >> 2; ++bi)
+        for (int bj = b[1] >> 2; bj <= (b[1] + 2) >> 2; ++bj)
+            for (int bk = b[2] >> 2; bk <= (b[2] + 2) >> 2; ++bk)
+                if (S.block[((size_t)bi * S.nb + bj) * S.nb + bk] != 0) return true;
+    return false;
+}
+
+// cdf_particle_tag (mpm_utils.py:678-713)
+int cdf_particle_tag(const CdfState& S, const Weights& W, bool use_prev) {
+    float votes[4] = {0.f, 0.f, 0.f, 0.f};
+    int seen = 0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            for (int k = 0; k < 3; ++k) {
+                size_t id = S.idx(W.base[0] + i, W.base[1] + j, W.base[2] + k);
+                int t = use_prev ? S.tag_prev[id] : S.tag[id];
+                float dd = use_prev ? S.d_prev[id] : S.d[id];
+                if (t == 0) continue;
+                float weight = W.w[0][i] * W.w[1][j] * W.w[2][k];
+                for (int lane = 0; lane < 4; ++lane)
+                    if ((t >> (2 * lane)) & 1) {
+                        seen |= 1 << (2 * lane);
+                        float sgn = ((t >> (2 * lane + 1)) & 1) ? 1.0f : -1.0f;
+                        votes[lane] = votes[lane] + weight * dd * sgn;
+                    }
+            }
+    int pc = 0;
+    for (int lane = 0; lane < 4; ++lane)
+        if ((seen >> (2 * lane)) & 1) {
+            pc |= 1 << (2 * lane);
+            if (votes[lane] >= 0.0f) pc |= 1 << (2 * lane + 1);
+        }
+    return pc;
+}
+
+// cdf_persist_tag (mpm_utils.py:716-730)
+int cdf_persist(int old, int fresh) {
+    int pc = 0;
+    for (int lane = 0; lane < 4; ++lane)
+        if ((fresh >> (2 * lane)) & 1) {
+            pc |= 1 << (2 * lane);
+            pc |= ((old >> (2 * lane)) & 1) ? (old & (1 << (2 * lane + 1))) : (fresh & (1 << (2 * lane + 1)));
+        }
+    return pc;
+}
+
+// cdf_particle_ghost (mpm_utils.py:733-816)
+V3 cdf_ghost(const CdfState& S, const gbmpm_model* M, float dt, V3 xp, V3 vp, int pc, const Weights& W) {
+    float d_hat = 0.0f;
+    V3 n_acc = mkv(0, 0, 0);
+    float best_w = 0.0f;
+    int lane_p = 0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            for (int k = 0; k < 3; ++k) {
+                size_t id = S.idx(W.base[0] + i, W.base[1] + j, W.base[2] + k);
+                int t = S.tag_prev[id];
+                if (t == 0) continue;
+                int own = (t >> kOwnerShift) & 3;
+                if (((t >> (2 * own)) & 1) == 0) continue;
+                float weight = W.w[0][i] * W.w[1][j] * W.w[2][k];
+                float sgn = ((t >> (2 * own + 1)) & 1) ? 1.0f : -1.0f;
+                float dd = S.d_prev[id];
+                d_hat = d_hat + weight * sgn * dd;
+                V3 dwt = dweight(W, i, j, k, M->inv_dx);
+                n_acc = vadd(n_acc, vscale(vscale(dwt, sgn), dd));
+                if (weight > best_w) { best_w = weight; lane_p = own; }
+            }
+    V3 g = mkv(M->gravity[0], M->gravity[1], M->gravity[2]);
+    V3 v_free = vadd(vp, vscale(g, dt));
+    V3 ghost = v_free;
+    if (vlen(n_acc) > 1.0e-12f) {
+        V3 n_hat = vnormalize(n_acc);
+        float side = ((pc >> (2 * lane_p + 1)) & 1) ? 1.0f : -1.0f;
+        V3 n_par = vscale(n_hat, side);
+        V3 rel = vsub(xp, load3(S.c_prev[lane_p]));
+        V3 v_surf = vadd(load3(S.v_prev[lane_p]), vcross(load3(S.w_prev[lane_p]), rel));
+        V3 v_rel = vsub(v_free, v_surf);
+        float vn = vdot(v_rel, n_par);
+        V3 v_tan = vsub(v_rel, vscale(n_par, vn));
+        float c = 0.0f;
+        float d_side = d_hat * side;
+        float eps = 0.05f * M->dx;
+        if (d_side < eps) c = std::min((eps - d_side) / dt, 0.5f * M->dx / dt);
+        int stype = S.type[lane_p];
+        if (stype == 0) {
+            ghost = vadd(v_surf, vscale(n_par, c));
+        } else if (stype == 1) {
+            ghost = vadd(vadd(v_surf, v_tan), vscale(n_par, c));
+        } else {
+            float dvn = std::max(-vn, 0.0f) + c;
+            float tlen = vlen(v_tan);
+            if (tlen > 1.0e-12f && dvn > 0.0f) {
+                float sc = std::max(0.0f, tlen - S.fric[lane_p] * dvn) / tlen;
+                v_tan = vscale(v_tan, sc);
+            }
+            ghost = vadd(vadd(vadd(v_surf, v_tan), vscale(n_par, std::max(vn, 0.0f))), vscale(n_par, c));
+        }
+    }
+    return ghost;
+}
+
+// the CDF collider's grid box (cdf_aabb, mpm_solver_warp.py:2860-2870 with halo 2)
+bool cdf_lane_box(const gbmpm_cdf& r, const gbmpm_model* M, int* box) {
+    double qx = r.quat[0], qy = r.quat[1], qz = r.quat[2], qw = r.quat[3];
+    double R[3][3] = {{1 - 2 * (qy * qy + qz * qz), 2 * (qx * qy - qz * qw), 2 * (qx * qz + qy * qw)},
+                      {2 * (qx * qy + qz * qw), 1 - 2 * (qx * qx + qz * qz), 2 * (qy * qz - qx * qw)},
+                      {2 * (qx * qz - qy * qw), 2 * (qy * qz + qx * qw), 1 - 2 * (qx * qx + qy * qy)}};
+    double ext = (r.res - 1) * (double)r.cell;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b)
+            for (int c = 0; c < 2; ++c) {
+                double cr[3] = {(double)r.origin[0] + a * ext, (double)r.origin[1] + b * ext, (double)r.origin[2] + c * ext};
+                for (int i = 0; i < 3; ++i) {
+                    double p = (double)r.center[i] + R[i][0] * cr[0] + R[i][1] * cr[1] + R[i][2] * cr[2];
+                    lo[i] = std::min(lo[i], p);
+                    hi[i] = std::max(hi[i], p);
+                }
+            }
+    double dx = (double)M->grid_lim / M->n_grid;   // python float grid_lim / n_grid
+    for (int i = 0; i < 3; ++i) {
+        int l = std::max(0, (int)std::floor(lo[i] / dx) - 2);
+        int h = std::min(M->n_grid, (int)std::ceil(hi[i] / dx) + 2 + 1);
+        if (h - l <= 0) return false;
+        box[i] = l;
+        box[3 + i] = h;   // exclusive
+    }
+    return true;
+}
+
+// cdf_stamp kernel body (mpm_solver_warp.py:146-183) for one lane over a box
+void cdf_stamp_lane(CdfState& S, const gbmpm_model* M, const gbmpm_cdf& r, int lane, float time_f, const int* box) {
+    if (time_f < r.start_time || time_f >= r.end_time) return;
+    float rf = (float)r.res - 1.0f;
+    for (int x = box[0]; x < box[3]; ++x)
+        for (int y = box[1]; y < box[4]; ++y)
+            for (int z = box[2]; z < box[5]; ++z) {
+                V3 xw = mkv((float)x * M->dx, (float)y * M->dx, (float)z * M->dx);
+                V3 rel = vsub(xw, mkv(r.center[0], r.center[1], r.center[2]));
+                V3 body = qrot(r.quat, rel, true);
+                V3 f = mkv((body[0] - r.origin[0]) / r.cell, (body[1] - r.origin[1]) / r.cell,
+                           (body[2] - r.origin[2]) / r.cell);
+                if (f[0] < 0.0f || f[1] < 0.0f || f[2] < 0.0f || f[0] > rf || f[1] > rf || f[2] > rf) continue;
+                float ok = trilerp(r.valid, r.res, f, 1, 0);
+                if (ok < 0.999f) continue;
+                float dd = trilerp(r.values, r.res, f, 1, 0);
+                float ud = std::fabs(dd);
+                if (ud > r.band) continue;
+                int side = dd >= 0.0f ? 1 : 0;
+                size_t id = S.idx(x, y, z);
+                int t = S.tag[id];
+                t = t | (1 << (2 * lane)) | (side << (2 * lane + 1));
+                if (ud < S.d[id]) {
+                    S.d[id] = ud;
+                    t = (t ^ (t & kOwnerMask)) | (lane << kOwnerShift);
+                }
+                S.tag[id] = t;
+            }
+}
+
+void cdf_copy_prev_box(CdfState& S, const int* box) {
+    for (int x = box[0]; x < box[3]; ++x)
+        for (int y = box[1]; y < box[4]; ++y)
+            for (int z = box[2]; z < box[5]; ++z) {
+                size_t id = S.idx(x, y, z);
+                S.tag_prev[id] = S.tag[id];
+                S.d_prev[id] = S.d[id];
+            }
+}
+
+// _stamp_cdf (mpm_solver_warp.py:3040-3098)
+void cdf_stamp(CdfState& S, const gbmpm_model* M, double time, bool lag_prev) {
+    if (S.n == 0) return;
+    if (S.stale_set) { cdf_copy_prev_box(S, S.stale_box); S.stale_set = false; }
+    for (int l = 0; l < S.n; ++l) {
+        bool act = time >= (double)S.rec[l].start_time && time < (double)S.rec[l].end_time;
+        if (act != S.active[l]) { S.active[l] = act; S.dirty[l] = true; }
+    }
+    bool any = false;
+    for (int l = 0; l < S.n; ++l) any = any || S.dirty[l];
+    if (!any) return;
+    // _cdf_dirty_box: union of the dirty lanes' boxes and the boxes of their last stamps
+    int box[6] = {INT32_MAX, INT32_MAX, INT32_MAX, INT32_MIN, INT32_MIN, INT32_MIN};
+    bool have = false;
+    auto grow = [&](const int* b) {
+        for (int i = 0; i < 3; ++i) { box[i] = std::min(box[i], b[i]); box[3 + i] = std::max(box[3 + i], b[3 + i]); }
+        have = true;
+    };
+    for (int l = 0; l < S.n; ++l) {
+        if (!S.dirty[l]) continue;
+        int b[6];
+        bool ok = cdf_lane_box(S.rec[l], M, b);
+        if (ok) grow(b);
+        if (S.has_prev_box[l]) grow(S.prev_box[l]);
+        S.has_prev_box[l] = ok;
+        if (ok) std::memcpy(S.prev_box[l], b, sizeof b);
+    }
+    for (int l = 0; l < S.n; ++l) S.dirty[l] = false;
+    if (!have) return;
+    S.stamp_count++;
+    for (int x = box[0]; x < box[3]; ++x)
+        for (int y = box[1]; y < box[4]; ++y)
+            for (int z = box[2]; z < box[5]; ++z) {
+                size_t id = S.idx(x, y, z);
+                S.tag[id] = 0;
+                S.d[id] = 1.0e9f;
+            }
+    float tf = (float)time;
+    for (int l = 0; l < S.n; ++l) {
+        int lb[6];
+        if (!cdf_lane_box(S.rec[l], M, lb)) continue;
+        int clip[6];
+        bool empty = false;
+        for (int i = 0; i < 3; ++i) {
+            clip[i] = std::max(box[i], lb[i]);
+            clip[3 + i] = std::min(box[3 + i], lb[3 + i]);
+            if (clip[3 + i] <= clip[i]) empty = true;
+        }
+        if (!empty) cdf_stamp_lane(S, M, S.rec[l], l, tf, clip);
+    }
+    if (lag_prev) { S.stale_set = true; std::memcpy(S.stale_box, box, sizeof box); }
+    else cdf_copy_prev_box(S, box);
+    // cdf_block_mask over the blocks of the box (cur OR prev)
+    for (int bi = box[0] >> 2; bi <= (box[3] - 1) >> 2; ++bi)
+        for (int bj = box[1] >> 2; bj <= (box[4] - 1) >> 2; ++bj)
+            for (int bk = box[2] >> 2; bk <= (box[5] - 1) >> 2; ++bk) {
+                int occ = 0;
+                for (int i = 0; i < 4; ++i)
+                    for (int j = 0; j < 4; ++j)
+                        for (int k = 0; k < 4; ++k) {
+                            int ci = (bi << 2) + i, cj = (bj << 2) + j, ck = (bk << 2) + k;
+                            if (ci < S.n_grid && cj < S.n_grid && ck < S.n_grid) {
+                                size_t id = S.idx(ci, cj, ck);
+                                occ = occ | S.tag[id] | S.tag_prev[id];
+                            }
+                        }
+                S.block[((size_t)bi * S.nb + bj) * S.nb + bk] = occ;
+            }
+}
+
+// _integrate_cdf_poses (mpm_solver_warp.py:3107-3148)
+void cdf_integrate(CdfState& S, double time, double dt, bool lag_prev) {
+    if (S.n == 0) return;
+    if (lag_prev && S.lane_prev_stale) S.copy_lane_prev();
+    for (int l = 0; l < S.n; ++l) {
+        gbmpm_cdf& r = S.rec[l];
+        if (!(time >= (double)r.start_time && time < (double)r.end_time)) continue;
+        if (r.velocity[0] == 0.0f && r.velocity[1] == 0.0f && r.velocity[2] == 0.0f && r.omega[0] == 0.0f &&
+            r.omega[1] == 0.0f && r.omega[2] == 0.0f)
+            continue;
+        for (int a = 0; a < 3; ++a) r.center[a] = (float)((double)r.center[a] + dt * (double)r.velocity[a]);
+        double w[3] = {r.omega[0], r.omega[1], r.omega[2]};
+        double sp = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        if (!(sp * dt < 1e-12)) {
+            double q[4] = {r.quat[0], r.quat[1], r.quat[2], r.quat[3]};
+            double half = 0.5 * sp * dt, sh = std::sin(half);
+            double dq[4] = {w[0] / sp * sh, w[1] / sp * sh, w[2] / sp * sh, std::cos(half)};
+            double o[4] = {dq[3] * q[0] + dq[0] * q[3] + dq[1] * q[2] - dq[2] * q[1],
+                           dq[3] * q[1] - dq[0] * q[2] + dq[1] * q[3] + dq[2] * q[0],
+                           dq[3] * q[2] + dq[0] * q[1] - dq[1] * q[0] + dq[2] * q[3],
+                           dq[3] * q[3] - dq[0] * q[0] - dq[1] * q[1] - dq[2] * q[2]};
+            double nr = std::sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2] + o[3] * o[3]);
+            for (int i = 0; i < 4; ++i) r.quat[i] = (float)(o[i] / nr);
+        }
+        S.sync_lane(l);
+        S.dirty[l] = true;
+        S.lane_prev_stale = true;
+    }
+    if (!lag_prev && S.lane_prev_stale) S.copy_lane_prev();
+}
+
 // ---------------------------------------------------------- tick driver -----
 struct Oracle {
     Grid G;
@@ -1037,8 +1403,58 @@ void gbmpm_oracle_integrate_pose(gbmpm_collider* c, double time, double dt) { in
 // One control tick (MPM_Simulator_WARP.p2g2p_fused_tick, mpm_solver_warp.py:1379-1546,
 // or S calls of p2g2p, :1092-1281, when fused == 0). wrench: [ncol][6] fp32
 // accumulators. threads <= 1 runs serially and deterministically.
+// CPIC lane state of one scene (tag grids, lane poses, stamp bookkeeping)
+void* gbmpm_oracle_cdf_new(int32_t n_grid) {
+    CdfState* S = new CdfState();
+    S->alloc(n_grid);
+    return S;
+}
+void gbmpm_oracle_cdf_free(void* st) { delete static_cast<CdfState*>(st); }
+int32_t gbmpm_oracle_cdf_stamp_count(void* st) { return static_cast<CdfState*>(st)->stamp_count; }
+// current node tags and owner distances (grid_cdf_tag / grid_cdf_d), n_grid^3 each
+void gbmpm_oracle_cdf_grids(void* st, int32_t* tag, float* d) {
+    CdfState& S = *static_cast<CdfState*>(st);
+    if (tag) std::memcpy(tag, S.tag.data(), S.tag.size() * sizeof(int32_t));
+    if (d) std::memcpy(d, S.d.data(), S.d.size() * sizeof(float));
+}
+
+// add_cdf_collider / set_cdf_pose (mpm_solver_warp.py:2819-2953): lanes beyond the
+// current count are new; an existing lane whose centre or quaternion changed is
+// marked for restamping, and any pose or rate change refreshes the lane arrays.
+int gbmpm_oracle_cdf_set(void* st, const gbmpm_cdf* lanes, int32_t n, double time) {
+    CdfState& S = *static_cast<CdfState*>(st);
+    if (n < S.n || n > GBMPM_MAX_CDF) { g_err = "lanes can only be added (max 4)"; return GBMPM_ERR_ARG; }
+    for (int l = 0; l < n; ++l) {
+        const gbmpm_cdf& r = lanes[l];
+        if (l >= S.n) {
+            S.rec[l] = r;
+            S.dirty[l] = true;
+            S.active[l] = time >= (double)r.start_time && time < (double)r.end_time;
+            S.has_prev_box[l] = false;
+            S.sync_lane(l);
+            continue;
+        }
+        gbmpm_cdf& o = S.rec[l];
+        bool moved = std::memcmp(o.center, r.center, sizeof o.center) != 0 || std::memcmp(o.quat, r.quat, sizeof o.quat) != 0;
+        bool synced = std::memcmp(o.velocity, r.velocity, sizeof o.velocity) != 0 ||
+                      std::memcmp(o.omega, r.omega, sizeof o.omega) != 0;
+        S.rec[l] = r;
+        if (moved) S.dirty[l] = true;
+        if (moved || synced) { S.sync_lane(l); S.lane_prev_stale = true; }
+    }
+    S.n = n;
+    return GBMPM_OK;
+}
+
+int gbmpm_oracle_cdf_get(void* st, gbmpm_cdf* lanes, int32_t n) {
+    CdfState& S = *static_cast<CdfState*>(st);
+    for (int l = 0; l < n && l < S.n; ++l) lanes[l] = S.rec[l];
+    return GBMPM_OK;
+}
+
 int gbmpm_oracle_tick(const gbmpm_particles* P, const gbmpm_model* M, gbmpm_collider* cols, int32_t ncol,
-                      float* wrench, double* time, double dt, int32_t substeps, int32_t fused, int32_t threads) {
+                      float* wrench, double* time, double dt, int32_t substeps, int32_t fused, int32_t threads,
+                      void* cdf_state, float* cdf_wrench) {
     if (!P || !M || !time || substeps < 1) { g_err = "bad argument"; return GBMPM_ERR_ARG; }
     bool par = threads > 1;
 #ifdef _OPENMP
@@ -1050,12 +1466,21 @@ int gbmpm_oracle_tick(const gbmpm_particles* P, const gbmpm_model* M, gbmpm_coll
     G.resize(M->n_grid);
     float dtf = (float)dt;
     Ctx c{P, M, &G, dtf, par, 0};
+    CdfState* S = static_cast<CdfState*>(cdf_state);
+    if (S && S->n > 0) {
+        if (S->n_grid != M->n_grid) { g_err = "cdf state grid differs from the model"; return GBMPM_ERR_ARG; }
+        c.cdf = S;
+        c.cdf_wrench = cdf_wrench;
+    } else {
+        S = nullptr;
+    }
     const int n = P->n;
     auto sel = [&](int p) { return !P->selection || P->selection[p] == 0; };
     int prev_lo[3], prev_hi[3];
     for (int s = 0; s < substeps; ++s) {
         float tf = (float)*time;
         for (int a = 0; a < 3; ++a) { prev_lo[a] = G.lo[a]; prev_hi[a] = G.hi[a]; }
+        if (S) cdf_stamp(*S, M, *time, fused != 0);
         if (!fused || s == 0) {
             // zero_grid over the previous touched box, stress, p2g
             if (prev_hi[0] > prev_lo[0]) zero_box(G, prev_lo, prev_hi, true, true);
@@ -1078,6 +1503,7 @@ int gbmpm_oracle_tick(const gbmpm_particles* P, const gbmpm_model* M, gbmpm_coll
         }
         grid_update(G, M, cols, ncol, wrench, tf, dtf, par);
         for (int k = 0; k < ncol; ++k) integrate_pose(cols[k], *time, dt);
+        if (S) cdf_integrate(*S, *time, dt, fused != 0);
         *time = *time + dt;
         if (!fused) {
             par_for(n, par, [&](int p) {
@@ -1088,6 +1514,7 @@ int gbmpm_oracle_tick(const gbmpm_particles* P, const gbmpm_model* M, gbmpm_coll
         }
     }
     if (fused) {
+        if (S && S->stale_set) { cdf_copy_prev_box(*S, S->stale_box); S->stale_set = false; }
         par_for(n, par, [&](int p) {
             if (!sel(p)) return;
             int mat = P->material[p];

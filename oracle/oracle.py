@@ -57,7 +57,16 @@ def load():
     P = C.POINTER
     lib.gbmpm_oracle_tick.restype = C.c_int
     lib.gbmpm_oracle_tick.argtypes = [P(_abi.Particles), P(_abi.Model), P(_abi.Collider), C.c_int32, C.c_void_p,
-                                      P(C.c_double), C.c_double, C.c_int32, C.c_int32, C.c_int32]
+                                      P(C.c_double), C.c_double, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                      C.c_void_p]
+    lib.gbmpm_oracle_cdf_new.restype = C.c_void_p
+    lib.gbmpm_oracle_cdf_new.argtypes = [C.c_int32]
+    lib.gbmpm_oracle_cdf_free.argtypes = [C.c_void_p]
+    lib.gbmpm_oracle_cdf_stamp_count.restype = C.c_int32
+    lib.gbmpm_oracle_cdf_stamp_count.argtypes = [C.c_void_p]
+    lib.gbmpm_oracle_cdf_set.argtypes = [C.c_void_p, P(_abi.Cdf), C.c_int32, C.c_double]
+    lib.gbmpm_oracle_cdf_get.argtypes = [C.c_void_p, P(_abi.Cdf), C.c_int32]
+    lib.gbmpm_oracle_cdf_grids.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     lib.gbmpm_oracle_svd3.argtypes = [C.c_void_p] * 4
     lib.gbmpm_oracle_glass_sdf.restype = C.c_float
     lib.gbmpm_oracle_glass_sdf.argtypes = [P(_abi.Collider), C.c_void_p]
@@ -115,7 +124,7 @@ def blocks(x: np.ndarray, inv_dx: float, n_grid: int, prev: np.ndarray | None = 
 
 
 _KEYS = ("x", "v", "C", "F", "F_trial", "L", "stress", "mass", "vol", "density", "Jp", "mu", "lam", "yield_stress",
-         "material", "selection", "cov", "init_cov")
+         "material", "selection", "cov", "init_cov", "cdf_tag")
 
 
 class OracleSolver:
@@ -140,6 +149,15 @@ class OracleSolver:
         self.time = 0.0
         self.mat_current = 0
         self.wrench = np.zeros((0, 6), np.float32)
+        self.cdf_lanes: list = []
+        self.cdf_arrays: list = []
+        self.cdf_state = None
+        self.cdf_wrench_acc = np.zeros((4, 6), np.float32)
+
+    def __del__(self):
+        if getattr(self, "cdf_state", None):
+            load().gbmpm_oracle_cdf_free(self.cdf_state)
+            self.cdf_state = None
 
     # ----------------------------------------------------------------- setup
     def load_particles(self, pos, vol, cov=None, cov_mode="step"):
@@ -150,7 +168,8 @@ class OracleSolver:
                   "F": eye.copy(), "F_trial": eye.copy(), "L": z(n, 3, 3), "stress": z(n, 3, 3),
                   "mass": z(n), "vol": np.asarray(vol, np.float32).copy(), "density": z(n), "Jp": z(n),
                   "mu": z(n), "lam": z(n), "yield_stress": z(n), "material": np.zeros(n, np.int32),
-                  "selection": np.zeros(n, np.int32), "cov": None, "init_cov": None}
+                  "selection": np.zeros(n, np.int32), "cov": None, "init_cov": None,
+                  "cdf_tag": np.zeros(n, np.int32)}
         if cov is not None:
             c6 = np.ascontiguousarray(cov, np.float32).reshape(n, 6)
             self.a["init_cov"] = c6.copy()
@@ -277,6 +296,71 @@ class OracleSolver:
                                            velocity, omega, band, host.SDF_SURFACES[surface], friction,
                                            start_time, end_time))
 
+    def _push_cdf(self):
+        lib = load()
+        if self.cdf_state is None:
+            self.cdf_state = lib.gbmpm_oracle_cdf_new(self.n_grid)
+        arr = (_abi.Cdf * max(1, len(self.cdf_lanes)))(*self.cdf_lanes)
+        rc = lib.gbmpm_oracle_cdf_set(self.cdf_state, arr, len(self.cdf_lanes), float(self.time))
+        if rc != 0:
+            raise ValueError(lib.gbmpm_oracle_last_error().decode())
+
+    def _pull_cdf(self):
+        if self.cdf_state is None or not self.cdf_lanes:
+            return
+        arr = (_abi.Cdf * len(self.cdf_lanes))()
+        load().gbmpm_oracle_cdf_get(self.cdf_state, arr, len(self.cdf_lanes))
+        self.cdf_lanes = [arr[i] for i in range(len(self.cdf_lanes))]
+
+    def add_cdf_collider(self, cdf, center, quat=(0.0, 0.0, 0.0, 1.0), velocity=(0.0, 0.0, 0.0),
+                         omega=(0.0, 0.0, 0.0), band=None, surface="separable", friction=0.4, start_time=0.0,
+                         end_time=1.0e9):
+        if len(self.cdf_lanes) >= _abi.MAX_CDF:
+            raise ValueError("at most 4 CDF colliders per scene")
+        band = host.cdf_band(cdf.band, self.dx, band)
+        vals = np.ascontiguousarray(cdf.values, np.float32)
+        valid = np.ascontiguousarray(cdf.valid, np.float32)
+        self.cdf_arrays += [vals, valid]
+        self._pull_cdf()
+        self.cdf_lanes.append(host.cdf_lane(_p(vals), _p(valid), vals.shape[0], cdf.origin, cdf.cell, center, quat,
+                                            velocity, omega, band, host.SDF_SURFACES[surface], friction,
+                                            start_time, end_time))
+        self._push_cdf()
+        return len(self.cdf_lanes) - 1
+
+    def set_cdf_pose(self, handle, center=None, quat=None, velocity=None, omega=None):
+        self._pull_cdf()
+        c = self.cdf_lanes[handle]
+        if center is not None:
+            host._vec(c.center, center)
+        if quat is not None:
+            host._vec(c.quat, quat)
+        if velocity is not None:
+            host._vec(c.velocity, velocity)
+        if omega is not None:
+            host._vec(c.omega, omega)
+        self._push_cdf()
+        return self
+
+    def reset_cdf_wrench(self):
+        self.cdf_wrench_acc[:] = 0.0
+        return self
+
+    def cdf_grids(self):
+        """(tag, distance) node grids of the last stamp and the number of stamps so far."""
+        ng = self.n_grid
+        tag = np.zeros((ng, ng, ng), np.int32)
+        d = np.zeros((ng, ng, ng), np.float32)
+        if self.cdf_state is None:
+            return tag, d, 0
+        lib = load()
+        lib.gbmpm_oracle_cdf_grids(self.cdf_state, _p(tag), _p(d))
+        return tag, d, int(lib.gbmpm_oracle_cdf_stamp_count(self.cdf_state))
+
+    def cdf_wrench(self, handle, dt):
+        w = self.cdf_wrench_acc[handle].astype(float)
+        return {"force": w[:3] / dt, "torque": w[3:] / dt}
+
     def wrench_of(self, handle, dt):
         w = self.wrench[self.handles[handle]].astype(float)
         return {"force": w[:3] / dt, "torque": w[3:] / dt}
@@ -304,6 +388,18 @@ class OracleSolver:
         o.handles = list(st.get("handles", range(len(o.cols))))
         o.wrench = np.zeros((len(o.cols), 6), np.float32)
         o.time = float(st["time"])
+        if o.a.get("cdf_tag") is None:
+            o.a["cdf_tag"] = np.zeros(len(o.a["x"]), np.int32)
+        for rec in st.get("cdf_lanes", []):
+            r = _abi.Cdf()
+            C.memmove(C.byref(r), C.byref(rec), C.sizeof(_abi.Cdf))
+            vals = np.ascontiguousarray(st["cdf_host"][rec.values], np.float32)
+            valid = np.ascontiguousarray(st["cdf_host"][rec.valid], np.float32)
+            o.cdf_arrays += [vals, valid]
+            r.values, r.valid = _p(vals), _p(valid)
+            o.cdf_lanes.append(r)
+        if o.cdf_lanes:
+            o._push_cdf()
         return o
 
     # ------------------------------------------------------------------ step
@@ -320,7 +416,8 @@ class OracleSolver:
         arr = (_abi.Collider * max(1, len(self.cols)))(*self.cols)
         t = C.c_double(self.time)
         rc = lib.gbmpm_oracle_tick(C.byref(p), C.byref(self.model), arr, len(self.cols), _p(self.wrench),
-                                   C.byref(t), float(dt), int(substeps), 1 if self.fused else 0, int(self.threads))
+                                   C.byref(t), float(dt), int(substeps), 1 if self.fused else 0, int(self.threads),
+                                   self.cdf_state if self.cdf_lanes else None, _p(self.cdf_wrench_acc))
         if rc != 0:
             raise RuntimeError(f"oracle tick failed ({rc}): {lib.gbmpm_oracle_last_error().decode()}")
         self.cols = [arr[i] for i in range(len(self.cols))]

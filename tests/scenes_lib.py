@@ -136,3 +136,32 @@ def free_blob(cls, n_grid=40):
     s = make(cls, n_grid, 0.4).load_particles(pos, vol)
     s.set_material(dough())
     return s
+
+
+# ---- CPIC (CDF) scenes: a 32^3 grid over 0.4 m, water at 2 particles per cell
+# edge (tests/test_cdf_transfers.py:14-40)
+CDF_NG, CDF_LIM = 32, 0.4
+CDF_DX = CDF_LIM / CDF_NG
+
+
+def cdf_water(x0, x1, y0, y1, z0, z1):
+    hp = CDF_DX / 2
+    ax = [np.arange(a + hp / 2, b, hp) for a, b in ((x0, x1), (y0, y1), (z0, z1))]
+    return np.stack(np.meshgrid(*ax, indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+
+
+def cdf_solver(cls, pos, g=(0.0, 0.0, 0.0), fused=True, floor=True):
+    s = make(cls, CDF_NG, CDF_LIM, fused=fused).load_particles(pos, np.full(len(pos), (CDF_DX / 2) ** 3,
+                                                                             np.float32))
+    s.set_material(newtonian(eta=0.5, density=1000.0, bulk_modulus=5.0e4), g=list(g))
+    if floor:
+        s.add_plane((0, 0, 3 * CDF_DX), (0, 0, 1), "slip")
+    s.add_domain_walls()
+    return s
+
+
+def set_velocity(s, vel):
+    if type(s).__name__ == "OracleSolver":
+        s.a["v"][:] = vel
+    else:
+        s.set_v(vel)

@@ -88,10 +88,3 @@ def test_material_range_and_mu_lam(cuda):
     np.testing.assert_allclose(mu[100:], 5e4 / 2.6, rtol=1e-6)
     with pytest.raises(NotImplementedError):
         s.set_material_range(0, 10, __import__("mpm_engine_gb300").tabulated_viscous([1.0, 2.0]))
-
-
-def test_cdf_collider_is_reported_missing(cuda):
-    from mpm_engine_gb300 import Solver
-    s, _ = blob_scene(Solver, "newtonian")
-    with pytest.raises(NotImplementedError):
-        s.add_cdf_collider(None, (0, 0, 0))

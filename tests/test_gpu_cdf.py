@@ -1,0 +1,167 @@
+"""CPIC thin-boundary (CDF) colliders on the CUDA engine, through the C ABI,
+against the CPU oracle.
+
+Stamps are decided on identical host-integrated poses with per-operation fp32
+rounding on both sides, so node tag and distance grids must agree bit for bit.
+Particle fields follow the engine's parity contract (1e-5 relative per substep,
+composed over k substeps); the per-lane reaction (float64 on the device, fp32 in
+the oracle) within 1e-3 of its largest component. Reference gates restated:
+tests/test_cdf_transfers.py:43-67 (the dam holds), tests/test_cdf_collider.py:73-86
+(guards), tests/test_cdf_stamp_skip.py:73-80 (a static pose stamps once).
+"""
+import numpy as np
+import pytest
+
+from mpm_engine_gb300.geometry import sheet_cdf
+from scenes_lib import CDF_DX, CDF_LIM, CDF_NG, cdf_solver, cdf_water, set_velocity, spin_velocity
+from test_gpu_parity import assert_close, rel_err
+
+pytestmark = pytest.mark.gpu
+
+DT, SUB = 2e-4, 10
+
+
+def _pair(oracle_lib, build, fused=True):
+    from mpm_engine_gb300 import Solver
+    s = build(Solver, fused)
+    o = oracle_lib.OracleSolver.from_state(s.export_state(), CDF_NG, CDF_LIM, fused=fused)
+    return s, o
+
+
+def _shelf(cls, fused):
+    """Water thrown down, spinning, onto a static horizontal sheet."""
+    pos = cdf_water(0.14, 0.26, 0.14, 0.26, 0.21, 0.27)
+    s = cdf_solver(cls, pos, g=(0.0, 0.0, -9.81), fused=fused)
+    set_velocity(s, spin_velocity(pos, lin=(0.1, 0.0, -0.6), omega=(0.0, 0.0, 4.0)))
+    s.add_cdf_collider(sheet_cdf("z"), center=(0.2, 0.2, 0.20), friction=0.3)
+    return s
+
+
+def _sweep(cls, fused):
+    """A tilted vertical sheet translating and turning into a resting block."""
+    pos = cdf_water(0.22, 0.30, 0.14, 0.26, 3 * CDF_DX, 3 * CDF_DX + 0.08)
+    s = cdf_solver(cls, pos, fused=fused)
+    half = 0.5 * np.deg2rad(10.0)
+    quat = (0.0, 0.0, float(np.sin(half)), float(np.cos(half)))
+    s.add_cdf_collider(sheet_cdf("x"), center=(0.18, 0.2, 0.2), quat=quat, velocity=(0.8, 0.0, 0.0),
+                       omega=(0.0, 0.0, 0.6), surface="slip")
+    return s
+
+
+def _check_grids(s, o, what):
+    tg, dg, ng = s.cdf_grids()
+    to, do, no = o.cdf_grids()
+    assert ng == no, f"{what}: {ng} stamps on the GPU, {no} in the oracle"
+    assert np.array_equal(tg, to), f"{what}: {int((tg != to).sum())} node tags differ"
+    assert np.array_equal(dg, do), f"{what}: owner distances differ"
+
+
+def _check_tags(s, o, what):
+    pt = s._t["cdf_tag"].cpu().numpy()
+    frac = float((pt != o.a["cdf_tag"]).mean())
+    assert frac <= 1e-3, f"{what}: {frac:.4%} of particle tags differ"
+
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_shelf_parity(cuda, oracle_lib, fused):
+    s, o = _pair(oracle_lib, _shelf, fused)
+    k = 0
+    for tick in range(5):
+        s.reset_cdf_wrench()
+        o.reset_cdf_wrench()
+        s.step(DT, SUB)
+        o.step(DT, SUB)
+        k += SUB
+        assert_close(s, o, k * 1e-5, f"shelf tick {tick}")
+        _check_grids(s, o, f"shelf tick {tick}")
+        _check_tags(s, o, f"shelf tick {tick}")
+        wg, wo = s.cdf_wrench(0, DT * SUB), o.cdf_wrench(0, DT * SUB)
+        for key in ("force", "torque"):
+            assert rel_err(wg[key], wo[key], 1e-9) < 1e-3, (tick, key, wg[key], wo[key])
+    assert s.cdf_wrench(0, DT * SUB)["force"][2] < 0.0
+
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_moving_turning_sheet_parity(cuda, oracle_lib, fused):
+    s, o = _pair(oracle_lib, _sweep, fused)
+    k = 0
+    for tick in range(4):
+        s.step(DT, SUB)
+        o.step(DT, SUB)
+        k += SUB
+        assert_close(s, o, k * 1e-5, f"sweep tick {tick}")
+        _check_grids(s, o, f"sweep tick {tick}")
+        _check_tags(s, o, f"sweep tick {tick}")
+    s._pull_cdf()
+    o._pull_cdf()
+    for a, b in zip(s._cdf, o.cdf_lanes):
+        assert list(a.center) == list(b.center) and list(a.quat) == list(b.quat)
+    assert s._cdf[0].center[0] > 0.18 + 0.8 * k * DT * 0.99
+
+
+def test_zero_thickness_dam_holds(cuda):
+    from mpm_engine_gb300 import Solver
+    pos = cdf_water(0.10, 0.16, 0.12, 0.28, 3 * CDF_DX, 3 * CDF_DX + 0.08)
+    s = cdf_solver(Solver, pos)
+    x_wall = 0.20
+    s.add_cdf_collider(sheet_cdf("x"), center=(x_wall, 0.2, 0.2))
+    v = s.v()
+    v[:, 0] += 1.0
+    s.set_v(v)
+    crossed, near = 0, False
+    for _ in range(30):
+        s.step(DT, SUB)
+        x = s.x()
+        crossed = max(crossed, int((x[:, 0] > x_wall).sum()))
+        near = near or bool((x[:, 0] > x_wall - 1.5 * CDF_DX).any())
+    assert near and crossed == 0, (near, crossed)
+
+
+def test_static_pose_stamps_once_and_sort_keeps_tags(cuda):
+    from mpm_engine_gb300 import Solver
+    s = _shelf(Solver, True)
+    for _ in range(5):
+        s.step(DT, SUB)
+    assert s.cdf_grids()[2] == 1
+    tags = s._t["cdf_tag"].cpu().numpy().copy()
+    x = s.x().copy()
+    assert (tags != 0).any()
+    assert s._sort_particles()
+    perm = s._t["perm"].cpu().numpy()[: len(x)]
+    assert np.array_equal(s.x(), x[perm])
+    assert np.array_equal(s._t["cdf_tag"].cpu().numpy(), tags[perm])
+
+
+def test_guards_and_api(cuda):
+    from mpm_engine_gb300 import BatchSolver, GridConfig, Solver
+    s = cdf_solver(Solver, cdf_water(0.08, 0.14, 0.08, 0.14, 0.08, 0.14))
+    cdf = sheet_cdf("z", size=0.3, band_cells=6.0)
+    with pytest.raises(ValueError, match="runtime band"):
+        s.add_cdf_collider(cdf, center=(0.2, 0.2, 0.2), band=10.0)
+    with pytest.warns(RuntimeWarning, match="below 1.5 dx"):
+        h = s.add_cdf_collider(cdf, center=(0.2, 0.2, 0.2), band=0.5 * CDF_DX)
+    with pytest.warns(RuntimeWarning, match="jumped the surface"):
+        s.set_cdf_pose(h, center=(0.2, 0.2, 0.35))
+    for _ in range(3):
+        s.add_cdf_collider(cdf, center=(0.2, 0.2, 0.2))
+    with pytest.raises(ValueError, match="at most"):
+        s.add_cdf_collider(cdf, center=(0.2, 0.2, 0.2))
+    with pytest.raises(NotImplementedError):
+        BatchSolver([s]).step(DT, 1)
+    s.step(DT, 2)
+    s.reset_cdf_wrench()
+    assert np.all(s.cdf_wrench(0, DT)["force"] == 0.0)
+    pos = cdf_water(0.10, 0.14, 0.10, 0.14, 0.10, 0.14)
+    p = Solver(grid=GridConfig(n_grid=CDF_NG, grid_lim=CDF_LIM), periodic_x=True)
+    p.load_particles(pos, np.full(len(pos), 1e-7, np.float32))
+    with pytest.raises(NotImplementedError):
+        p.add_cdf_collider(cdf, center=(0.2, 0.2, 0.2))
+
+
+def test_fast_sheet_warns_on_band_sweep(cuda):
+    from mpm_engine_gb300 import Solver
+    s = cdf_solver(Solver, cdf_water(0.14, 0.20, 0.14, 0.26, 3 * CDF_DX, 3 * CDF_DX + 0.05))
+    band = 2.0 * CDF_DX
+    s.add_cdf_collider(sheet_cdf("x"), center=(0.3, 0.2, 0.2), velocity=(2.0 * band / DT, 0.0, 0.0))
+    with pytest.warns(RuntimeWarning, match="sweeps"):
+        s.step(DT, 1)
