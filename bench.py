@@ -200,6 +200,30 @@ def dist_setup(args):
     return world, rank, local
 
 
+def captured_traffic(workload: str):
+    """DRAM bytes per launch of the fused particle kernel from the committed ncu
+    summary of this workload (profiles/k_particles_tiled_<workload>.txt), or None."""
+    name = workload.replace("^3", "")
+    f = REPO / "profiles" / f"k_particles_tiled_{name}.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            return float(line.split(":", 1)[1])
+    return None
+
+
+def replica_value(total_ms: float, units_per_step: float, steps: int, world: int, dist=None, device="cpu"):
+    """Whole-job throughput of N independent replicas: every rank's units over the
+    slowest rank's time (max all-reduce of the timed region). Returns (value, ms)."""
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([float(total_ms)], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return world * units_per_step * steps / (total_ms / 1e3), total_ms
+
+
 def run_reference(args):
     """CPU arm: the oracle restatement of the reference step, all host threads."""
     world, rank, _ = dist_setup(args)
@@ -291,11 +315,7 @@ def main():
     launches = s.launch_count() - launches0
     clk = clocks.stop()
     total_ms = sum(a.elapsed_time(b) for a, b in ev)
-    if dist:
-        t = torch.tensor([total_ms], device=f"cuda:{local}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * n * S * args.steps / (total_ms / 1e3)
+    value, total_ms = replica_value(total_ms, n * S, args.steps, world, dist, device=f"cuda:{local}")
     ms_per_step = total_ms / args.steps
 
     # dominant kernel duration: one frame with per-phase CUDA events (live launches)
@@ -313,8 +333,11 @@ def main():
     achieved = n * BYTES_PER_PARTICLE_SUBSTEP / (fused_ms / 1e3) / 1e9
     phases = {s._eng.lib.gbmpm_phase_name(i).decode(): round(msv[i] / max(cnt[i], 1), 5)
               for i in range(6) if cnt[i]}
+    traffic = captured_traffic(desc["workload"])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "k_particles_tiled (fused G2P2G)", "kernel_ms": fused_ms,
+                "traffic": traffic, "traffic_unit": "bytes per launch (ncu dram read + write, cold cache)",
+                "algorithmic_bytes_per_launch": n * BYTES_PER_PARTICLE_SUBSTEP,
+                "kernel": "k_particles_tiled (fused G2P2G)", "kernel_ms": fused_ms,
                 "grid_kernel_ms": grid_ms, "peak_kind": peak_kind, "phase_ms_per_launch": phases}
 
     e2e = None

@@ -2435,18 +2435,20 @@ void cdf_integrate(gbmpm_engine *e, double time, double dt, bool lag_prev) {
 // run live, on the direct kernel.
 void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cudaStream_t s, bool profile,
                  double t0 = 0.0, double dt = 0.0) {
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    if (profile) { cudaEventCreate(&ev0); cudaEventCreate(&ev1); }
+    // Profiling brackets every phase launch with an event pair and resolves the pairs
+    // once at the end of the tick: the host stays ahead of the GPU, so each pair
+    // measures the launch itself rather than host submission latency.
+    struct Mark { cudaEvent_t a, b; int phase; };
+    std::vector<Mark> marks;
     auto timed = [&](int phase, auto fn) {
         if (!profile) { fn(); return; }
-        cudaEventRecord(ev0, s);
+        Mark m{nullptr, nullptr, phase};
+        cudaEventCreate(&m.a);
+        cudaEventCreate(&m.b);
+        cudaEventRecord(m.a, s);
         fn();
-        cudaEventRecord(ev1, s);
-        cudaEventSynchronize(ev1);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ev0, ev1);
-        e->prof_ms[phase] += ms;
-        e->prof_n[phase] += 1;
+        cudaEventRecord(m.b, s);
+        marks.push_back(m);
     };
     const int *perm = nullptr;
     if (reorder) timed(5, [&] { perm = record_ws_begin(e, s); });
@@ -2489,7 +2491,17 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
             e->launches++;
         });
     }
-    if (profile) { cudaEventDestroy(ev0); cudaEventDestroy(ev1); }
+    if (profile) {
+        for (Mark &m : marks) {
+            cudaEventSynchronize(m.b);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, m.a, m.b);
+            e->prof_ms[m.phase] += ms;
+            e->prof_n[m.phase] += 1;
+            cudaEventDestroy(m.a);
+            cudaEventDestroy(m.b);
+        }
+    }
 }
 
 }  // namespace
