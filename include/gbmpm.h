@@ -221,6 +221,23 @@ int gbmpm_reset_cdf_wrench(gbmpm_engine *e, void *stream);
  * entries (either may be NULL), and the number of stamps so far (_cdf_stamp_count). */
 int gbmpm_cdf_grids(gbmpm_engine *e, int32_t *tag_out, float *d_out, int64_t *stamps, void *stream);
 
+/* ---- adjoint (no counterpart in the reference) ---------------------------------
+ * Adjoints of the particle state (x, v, C, F_trial, yield_stress; device arrays in
+ * the particle layout) and accumulated adjoints of the per-particle mu and lam. */
+typedef struct gbmpm_adj_grads {
+    float *x, *v, *C, *F_trial, *yield_stress;
+    float *mu, *lam;
+} gbmpm_adj_grads;
+
+/* Replays `substeps` split-schedule substeps forward from the bound state (the
+ * caller restores a checkpoint first), keeping each substep's starting state, then
+ * carries the adjoints in g from the end of the segment back to its start and adds
+ * each substep's contribution to g->mu and g->lam. Leaves the bound state at the
+ * segment's end and advances *time. Covers jelly (FCR) and von Mises particles and
+ * plane, cuboid and domain-wall colliders; anything else is GBMPM_ERR_UNSUPPORTED. */
+int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t substeps,
+                          const gbmpm_adj_grads *g, void *stream);
+
 /* Reaction impulse accumulated since the last reset: {fx, fy, fz, tx, ty, tz}. */
 int gbmpm_wrench(gbmpm_engine *e, int32_t collider, double out[6], void *stream);
 int gbmpm_reset_wrench(gbmpm_engine *e, int32_t collider, void *stream);

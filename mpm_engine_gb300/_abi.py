@@ -103,6 +103,10 @@ class Cdf(C.Structure):
     ]
 
 
+class AdjGrads(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ("x", "v", "C", "F_trial", "yield_stress", "mu", "lam")]
+
+
 # every entry point include/gbmpm.h declares, with its ctypes signature
 _SIGNATURES = {
     "gbmpm_last_error": (C.c_char_p, []),
@@ -123,6 +127,8 @@ _SIGNATURES = {
     "gbmpm_cdf_wrench": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_void_p]),
     "gbmpm_reset_cdf_wrench": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gbmpm_cdf_grids": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64), C.c_void_p]),
+    "gbmpm_adjoint_segment": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_double, C.c_int32,
+                                        C.POINTER(AdjGrads), C.c_void_p]),
     "gbmpm_sort_particles": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_int32), C.c_void_p,
                                        C.c_void_p]),
     "gbmpm_rebuild_active_blocks": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p]),

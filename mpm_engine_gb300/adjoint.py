@@ -1,0 +1,151 @@
+"""Differentiable rollouts: reverse-mode gradients through a Solver's substeps.
+
+The reference has no adjoint; gradient-based identification there is done by
+finite differences over serial rollouts. Here `rollout` runs a scene forward on
+the engine and returns its final positions and velocities as torch tensors whose
+gradients flow, through the engine's adjoint kernels, to the initial velocity
+field, Young's modulus, Poisson's ratio and the yield stress.
+
+Memory follows the usual checkpoint-and-recompute scheme: the forward keeps the
+state (x, v, C, F_trial, yield) and the collider poses every `checkpoint_every`
+substeps; the backward restores each checkpoint in reverse, replays that segment
+one substep at a time (the engine keeps every substep's starting state on the
+device) and carries the adjoints back through it (`gbmpm_adjoint_segment`).
+
+Scope: jelly (FCR) and von Mises particles (with or without hardening), plane,
+cuboid and domain-wall colliders, no periodic axis, rpic_damping = 0, particle
+order fixed during the rollout (sort_interval = 0).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from . import _abi
+from .solver import _torch
+
+_STATE = ("x", "v", "C", "F_trial", "yield_stress")
+
+
+def _snapshot(s):
+    s._pull_colliders()
+    cols = []
+    for rec in s._cols:
+        r = _abi.Collider()
+        C.memmove(C.byref(r), C.byref(rec), C.sizeof(_abi.Collider))
+        cols.append(r)
+    return {k: s._t[k].clone() for k in _STATE}, cols, s._time
+
+
+def _restore(s, snap):
+    state, cols, t = snap
+    for k in _STATE:
+        s._t[k].copy_(state[k])
+    s._cols = []
+    for rec in cols:
+        r = _abi.Collider()
+        C.memmove(C.byref(r), C.byref(rec), C.sizeof(_abi.Collider))
+        s._cols.append(r)
+    s._cols_dirty = True
+    s._time = t
+    s._sync_engine()
+
+
+def _check(s):
+    s._require_loaded()
+    if s.sort_interval:
+        raise ValueError("rollout needs a fixed particle order: set sort_interval = 0")
+    if s._cdf:
+        raise NotImplementedError("the adjoint does not cover CDF colliders")
+
+
+def _forward(s, dt, substeps, every):
+    ckpts = []
+    done = 0
+    while done < substeps:
+        k = min(every, substeps - done)
+        ckpts.append((_snapshot(s), k))
+        s.step(dt, k)
+        done += k
+    return ckpts
+
+
+def _backward(s, dt, ckpts, xb, vb):
+    torch = _torch()
+    n = s.n_particles
+    dev = s._t["x"].device
+    f = dict(device=dev, dtype=torch.float32)
+    g = {
+        "x": (xb.detach().to(**f).reshape(n, 3).clone() if xb is not None else torch.zeros(n, 3, **f)),
+        "v": (vb.detach().to(**f).reshape(n, 3).clone() if vb is not None else torch.zeros(n, 3, **f)),
+        "C": torch.zeros(n, 3, 3, **f), "F_trial": torch.zeros(n, 3, 3, **f),
+        "yield_stress": torch.zeros(n, **f), "mu": torch.zeros(n, **f), "lam": torch.zeros(n, **f),
+    }
+    rec = _abi.AdjGrads(**{k: g[k].data_ptr() for k in g})
+    lib, h = s._eng.lib, s._eng.h
+    for snap, k in reversed(ckpts):
+        _restore(s, snap)
+        t = C.c_double(s._time)
+        _abi.check(lib.gbmpm_adjoint_segment(h, C.byref(t), float(dt), int(k), C.byref(rec), s._stream()),
+                   "gbmpm_adjoint_segment")
+    return g
+
+
+class _Rollout(_torch().autograd.Function):
+    @staticmethod
+    def forward(ctx, v0, mu, lam, ys0, solver, dt, substeps, every):
+        s = solver
+        s._t["v"].copy_(v0.detach().reshape(-1, 3))
+        s._t["mu"].copy_(mu.detach())
+        s._t["lam"].copy_(lam.detach())
+        s._t["yield_stress"].copy_(ys0.detach())
+        ctx.solver, ctx.dt = s, dt
+        ctx.ckpts = _forward(s, dt, substeps, every)
+        x, v = s._t["x"].clone(), s._t["v"].clone()
+        ctx.final = _snapshot(s)
+        return x, v
+
+    @staticmethod
+    def backward(ctx, xb, vb):
+        s = ctx.solver
+        g = _backward(s, ctx.dt, ctx.ckpts, xb, vb)
+        _restore(s, ctx.final)
+        return g["v"], g["mu"], g["lam"], g["yield_stress"], None, None, None, None
+
+
+def mu_lam(E, nu):
+    """compute_mu_lam_from_E_nu (mpm_utils.py:583-588) on torch tensors."""
+    return E / (2.0 * (1.0 + nu)), E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+
+
+def rollout(solver, dt: float, substeps: int, *, v0=None, E=None, nu=None, yield_stress=None,
+            checkpoint_every: int = 20):
+    """Advance `solver` by `substeps` substeps of dt and return (x, v) at the end.
+
+    v0 ((N, 3)), E, nu and yield_stress (scalars or (N,) tensors) are the
+    differentiable inputs; any left as None keeps the scene's current value and is
+    not differentiated. E and nu set mu and lam of every particle through the
+    reference's formula. The solver is left at the end state of the rollout."""
+    torch = _torch()
+    _check(solver)
+    s = solver
+    n = s.n_particles
+    dev = s._t["x"].device
+    f = dict(device=dev, dtype=torch.float32)
+    v0 = s._t["v"].clone() if v0 is None else v0.to(**f)
+    if E is None and nu is None:
+        mu, lam = s._t["mu"].clone(), s._t["lam"].clone()
+    else:
+        if E is None or nu is None:
+            raise ValueError("E and nu are given together")
+        E = torch.as_tensor(E, **f) if not torch.is_tensor(E) else E.to(**f)
+        nu = torch.as_tensor(nu, **f) if not torch.is_tensor(nu) else nu.to(**f)
+        mu, lam = mu_lam(E, nu)
+        mu, lam = mu.expand(n), lam.expand(n)
+    if yield_stress is None:
+        ys = s._t["yield_stress"].clone()
+    else:
+        ys = (yield_stress if torch.is_tensor(yield_stress) else torch.as_tensor(yield_stress)).to(**f).expand(n)
+    return _Rollout.apply(v0, mu, lam, ys, s, float(dt), int(substeps), int(checkpoint_every))
+
+
+__all__ = ["mu_lam", "rollout"]

@@ -1,0 +1,693 @@
+// Reverse-mode adjoint of the explicit MLS/APIC substep (split schedule:
+// stress -> P2G -> grid update + colliders -> G2P) for the elastic (FCR, id 0) and
+// von Mises (id 1, optional hardening) materials, with plane, cuboid and domain-wall
+// colliders. The reference has no adjoint; the forward it differentiates is the one
+// restated by the rest of this file (mpm_utils.py:819-1158, mpm_solver_warp.py:
+// 1092-1281).
+//
+// One substep maps the particle state s = (x, v, C, F_trial, yield) to s' with
+// per-particle parameters (mu, lam). Given the adjoint of s' the kernels below
+// produce the adjoint of s and accumulate the adjoints of mu and lam:
+//
+//   forward recompute   k_adj_stress_fwd (F_trial -> F, Kirchhoff stress),
+//                       k_adj_p2g_fwd (scatter {m v, m}), k_adj_grid_fwd (normalize,
+//                       gravity, damping, colliders in list order)
+//   G2P adjoint         k_adj_g2p_bwd: x' = x + dt v', v' = sum w v_i,
+//                       C' = 4/dx^2 sum w v_i r_i^T, F_trial' = (I + dt L) F,
+//                       L = sum v_i grad(w_i)^T  -> grid v adjoint (scatter), F adjoint,
+//                       x adjoint through w, grad(w) (Hessian) and r_i = x_i - x_p
+//   grid adjoint        k_adj_grid_bwd: colliders in reverse order, then
+//                       v = mom/m + dt g  -> adjoints of mom and m per node
+//   P2G adjoint         k_adj_p2g_bwd: mom_i = sum w m (v + C r_i) + dt A grad(w_i),
+//                       A = -vol stress, m_i = sum w m  -> adjoints of v, C, x and the
+//                       stress; then the stress law and the return map back to
+//                       F_trial, yield, mu and lam.
+//
+// Every SVD-based map (the FCR rotation R = U V^T, the von Mises return
+// F = U diag(exp(eps')) V^T and the Hencky stress written as G(F) F^T) is an
+// isotropic matrix function G(F) = U diag(g(sigma)) V^T with g symmetric in sigma;
+// iso_adjoint propagates through all of them with the closed-form rotation terms
+// (g_i - g_j)/(s_i - s_j) and (g_i + g_j)/(s_i + s_j), using the coincident-value
+// limit of the first when two singular values (nearly) coincide.
+
+namespace gbmpm {
+
+struct AdjK {
+    // state at the start of the substep (caller layout: x[n][3], C[n][9] ...)
+    const float *x, *v, *C, *Ft, *ys;
+    const float *mass, *vol, *mu, *lam;
+    const int *mat, *sel;
+    int n;
+    // per-particle scratch: projected F, stress, adjoint of the projected F
+    float *Fp, *S, *Fpb;
+    // grid scratch (dense n^3): {mom, m}, {v}, {v adjoint}, {mom adjoint, m adjoint}
+    float4 *gmv, *gv, *gvb, *gmb;
+    int ng;
+    float dx, inv_dx, dt;
+    float grav[3];
+    float damp;
+    float hard1, xi1;   // von Mises hardening switch and xi (material table, id 1)
+    // adjoints: in = end of the substep, out = start of the substep
+    float *xb, *vb, *Cb, *Ftb, *ysb;
+    float *mub, *lamb;  // accumulated over substeps
+    // colliders of this substep
+    int ncol;
+    const ColDev *cols;
+    const PoseRec *poses;
+};
+
+// c = a^T b
+__device__ __forceinline__ void mTm(const float *a, const float *b, float *c) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) c[3 * i + j] = a[i] * b[j] + a[3 + i] * b[3 + j] + a[6 + i] * b[6 + j];
+}
+
+// Adjoint of G(F) = U diag(g) V^T at F = U diag(s) V^T, g symmetric in s with
+// Jacobian Jg[i][j] = dg_i/ds_j: adds to Fb the pull-back of Gb and returns the
+// diagonal of U^T Gb V (the adjoint of g) in yd.
+__device__ void iso_adjoint(const float *U, const float *s, const float *V, const float *g, const float (&Jg)[3][3],
+                            const float *Gb, float *Fb, float *yd) {
+    float T[9], Y[9], M[9];
+    mTm(U, Gb, T);
+    mm(T, V, Y);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) yd[i] = Y[4 * i];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) M[4 * j] = Jg[0][j] * Y[0] + Jg[1][j] * Y[4] + Jg[2][j] * Y[8];
+    const int P[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const int i = P[q][0], j = P[q][1];
+        const float d = s[i] - s[j], su = s[i] + s[j];
+        const float sc = fmaxf(fabsf(s[i]), fabsf(s[j]));
+        const float a = (fabsf(d) > 1e-3f * sc) ? (g[i] - g[j]) / d
+                                                : 0.5f * (Jg[i][i] - Jg[i][j] + Jg[j][j] - Jg[j][i]);
+        const float b = (fabsf(su) > 1e-6f) ? (g[i] + g[j]) / su : 0.0f;
+        const float ap = 0.5f * (a + b), am = 0.5f * (a - b);
+        const float yij = Y[3 * i + j], yji = Y[3 * j + i];
+        M[3 * i + j] = ap * yij + am * yji;
+        M[3 * j + i] = ap * yji + am * yij;
+    }
+    float W[9], R[9];
+    mm(U, M, W);
+    mmT(W, V, R);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Fb[i] += R[i];
+}
+
+// cofactor matrix: d det(F) / dF
+__device__ __forceinline__ void cofactor(const float *F, float *c) {
+    c[0] = F[4] * F[8] - F[5] * F[7];
+    c[1] = F[5] * F[6] - F[3] * F[8];
+    c[2] = F[3] * F[7] - F[4] * F[6];
+    c[3] = F[2] * F[7] - F[1] * F[8];
+    c[4] = F[0] * F[8] - F[2] * F[6];
+    c[5] = F[1] * F[6] - F[0] * F[7];
+    c[6] = F[1] * F[5] - F[2] * F[4];
+    c[7] = F[2] * F[3] - F[0] * F[5];
+    c[8] = F[0] * F[4] - F[1] * F[3];
+}
+
+// von Mises return map of one particle (mpm_utils.py:127-170) as the engine's
+// stress pass computes it; returns true on the plastic branch.
+__device__ bool vm_return(const float *Ft, float mu, float lam, float ys, float *U, float *sg, float *V, float *eps,
+                          float *Fp) {
+    svd3(Ft, U, sg, V);
+    eps[0] = logf(fmaxf(sg[0], 0.01f));
+    eps[1] = logf(fmaxf(sg[1], 0.01f));
+    eps[2] = logf(fmaxf(sg[2], 0.01f));
+    const float tr = eps[0] + eps[1] + eps[2];
+    const float temp = tr / 3.0f;
+    const float t0 = 2.0f * mu * eps[0] + lam * tr, t1 = 2.0f * mu * eps[1] + lam * tr, t2 = 2.0f * mu * eps[2] + lam * tr;
+    const float st = (t0 + t1 + t2) / 3.0f;
+    const float c0 = t0 - st, c1 = t1 - st, c2 = t2 - st;
+    if (!(sqrtf(c0 * c0 + c1 * c1 + c2 * c2) > ys)) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Fp[i] = Ft[i];
+        return false;
+    }
+    const float h0 = eps[0] - temp, h1 = eps[1] - temp, h2 = eps[2] - temp;
+    const float hn = sqrtf(h0 * h0 + h1 * h1 + h2 * h2) + 1e-6f;
+    const float r = (hn - ys / (2.0f * mu)) / hn;
+    udvt(U, expf(eps[0] - r * h0), expf(eps[1] - r * h1), expf(eps[2] - r * h2), V, Fp);
+    return true;
+}
+
+// Kirchhoff stress of the projected F (FCR for id 0, Hencky for id 1), symmetrized
+__device__ void adj_stress(int mat, const float *F, float mu, float lam, float *S) {
+    float U[9], V[9], sg[3], T[9];
+    svd3(F, U, sg, V);
+    if (mat == 0) {
+        float R[9], FR[9];
+        mmT(U, V, R);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) FR[i] = 2.0f * mu * (F[i] - R[i]);
+        mmT(FR, F, T);
+        const float J = det3(F);
+        const float dl = lam * J * (J - 1.0f);
+        T[0] += dl; T[4] += dl; T[8] += dl;
+    } else {
+        stress_hencky(U, sg, mu, lam, T);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) S[3 * i + j] = 0.5f * (T[3 * i + j] + T[3 * j + i]);
+}
+
+__global__ void k_adj_stress_fwd(AdjK k) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= k.n || (k.sel && k.sel[p] != 0)) return;
+    float Ft[9], Fp[9], S[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Ft[i] = k.Ft[9 * (size_t)p + i];
+    const int mat = k.mat[p];
+    const float mu = k.mu[p], lam = k.lam[p];
+    if (mat == 1) {
+        float U[9], V[9], sg[3], eps[3];
+        vm_return(Ft, mu, lam, k.ys[p], U, sg, V, eps, Fp);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Fp[i] = Ft[i];
+    }
+    adj_stress(mat, Fp, mu, lam, S);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) { k.Fp[9 * (size_t)p + i] = Fp[i]; k.S[9 * (size_t)p + i] = S[i]; }
+}
+
+// grad(w) and the Hessian of w with respect to x_p for node (i, j, kk)
+__device__ __forceinline__ void weight_derivs(const Stencil &s, float inv_dx, int i, int j, int kk, float &w, float *g,
+                                              float *H) {
+    const float dd[3] = {1.0f, -2.0f, 1.0f};
+    const float w0 = s.w[0][i], w1 = s.w[1][j], w2 = s.w[2][kk];
+    const float d0 = s.dw[0][i], d1 = s.dw[1][j], d2 = s.dw[2][kk];
+    w = w0 * w1 * w2;
+    g[0] = d0 * w1 * w2 * inv_dx;
+    g[1] = w0 * d1 * w2 * inv_dx;
+    g[2] = w0 * w1 * d2 * inv_dx;
+    const float i2 = inv_dx * inv_dx;
+    H[0] = dd[i] * w1 * w2 * i2;
+    H[4] = w0 * dd[j] * w2 * i2;
+    H[8] = w0 * w1 * dd[kk] * i2;
+    H[1] = H[3] = d0 * d1 * w2 * i2;
+    H[2] = H[6] = d0 * w1 * d2 * i2;
+    H[5] = H[7] = w0 * d1 * d2 * i2;
+}
+
+__global__ void k_adj_p2g_fwd(AdjK a, PK k) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.n || (a.sel && a.sel[p] != 0)) return;
+    float x[3] = {a.x[3 * p], a.x[3 * p + 1], a.x[3 * p + 2]};
+    float v[3] = {a.v[3 * p], a.v[3 * p + 1], a.v[3 * p + 2]};
+    float C[9], S[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) { C[i] = a.C[9 * (size_t)p + i]; S[i] = a.S[9 * (size_t)p + i]; }
+    Stencil s;
+    stencil(x, a.inv_dx, s);
+    if (!stencil_ok(s, a.ng, 0)) { set_status(k.status, GBMPM_FLAG_STENCIL_OOB); return; }
+    p2g_core(k, s, p, v, C, S, [&](int i, int j, int kk, float4 val) {
+        atomicAdd(a.gmv + ((size_t)(s.b[0] + i) * a.ng + (s.b[1] + j)) * a.ng + (s.b[2] + kk), val);
+    });
+}
+
+__device__ __forceinline__ GK adj_gk(const AdjK &a) {
+    GK g{};
+    g.ng = a.ng;
+    g.dx = a.dx;
+    g.dt = a.dt;
+    for (int i = 0; i < 3; ++i) g.g[i] = a.grav[i];
+    g.damp = a.damp;
+    return g;
+}
+
+// normalized, damped velocity before the colliders; m <= 1e-15 leaves zero
+__device__ __forceinline__ void grid_pre(const AdjK &a, float4 mv, float *v) {
+    v[0] = v[1] = v[2] = 0.0f;
+    if (mv.w > 1e-15f) {
+        const float inv = 1.0f / mv.w;
+        v[0] = mv.x * inv + a.dt * a.grav[0];
+        v[1] = mv.y * inv + a.dt * a.grav[1];
+        v[2] = mv.z * inv + a.dt * a.grav[2];
+    }
+    if (a.damp < 1.0f) { v[0] *= a.damp; v[1] *= a.damp; v[2] *= a.damp; }
+}
+
+__global__ void k_adj_grid_fwd(AdjK a) {
+    const size_t N = (size_t)a.ng * a.ng * a.ng;
+    const GK gk = adj_gk(a);
+    for (size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x; id < N; id += (size_t)gridDim.x * blockDim.x) {
+        const float4 mv = a.gmv[id];
+        if (mv.w == 0.0f) { a.gv[id] = make_float4(0.f, 0.f, 0.f, 0.f); continue; }
+        const int gz = (int)(id % a.ng), gy = (int)((id / a.ng) % a.ng), gx = (int)(id / ((size_t)a.ng * a.ng));
+        float v[3], acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        grid_pre(a, mv, v);
+        for (int c = 0; c < a.ncol; ++c)
+            if (mv.w > 0.0f && a.poses[c].mode != 0) collide(a.cols[c], a.poses[c], gx, gy, gz, mv.w, v, gk, acc);
+        a.gv[id] = make_float4(v[0], v[1], v[2], 0.0f);
+    }
+}
+
+__global__ void k_adj_g2p_bwd(AdjK a) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.n || (a.sel && a.sel[p] != 0)) return;
+    const float x[3] = {a.x[3 * p], a.x[3 * p + 1], a.x[3 * p + 2]};
+    float Fp[9], Ftb[9], Cb[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        Fp[i] = a.Fp[9 * (size_t)p + i];
+        Ftb[i] = a.Ftb[9 * (size_t)p + i];
+        Cb[i] = a.Cb[9 * (size_t)p + i];
+    }
+    float xb[3], vt[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        xb[d] = a.xb[3 * p + d];
+        vt[d] = a.vb[3 * p + d] + a.dt * xb[d];   // adjoint of v' (x' = x + dt v')
+    }
+    float Lb[9];   // adjoint of L: F_trial' = (I + dt L) F
+    mmT(Ftb, Fp, Lb);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Lb[i] *= a.dt;
+    Stencil s;
+    stencil(x, a.inv_dx, s);
+    if (!stencil_ok(s, a.ng, 0)) return;
+    const float c4 = 4.0f * a.inv_dx * a.inv_dx;
+    float L[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            for (int kk = 0; kk < 3; ++kk) {
+                const size_t id = ((size_t)(s.b[0] + i) * a.ng + (s.b[1] + j)) * a.ng + (s.b[2] + kk);
+                const float4 g4 = a.gv[id];
+                const float vi[3] = {g4.x, g4.y, g4.z};
+                float w, g[3], H[9];
+                weight_derivs(s, a.inv_dx, i, j, kk, w, g, H);
+                const float r[3] = {((float)i - s.fx[0]) * a.dx, ((float)j - s.fx[1]) * a.dx, ((float)kk - s.fx[2]) * a.dx};
+#pragma unroll
+                for (int u = 0; u < 3; ++u)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) L[3 * u + q] += vi[u] * g[q];
+                float vib[3], Cbr[3], CbTv[3], LbTv[3];
+#pragma unroll
+                for (int u = 0; u < 3; ++u) {
+                    Cbr[u] = Cb[3 * u] * r[0] + Cb[3 * u + 1] * r[1] + Cb[3 * u + 2] * r[2];
+                    CbTv[u] = Cb[u] * vi[0] + Cb[3 + u] * vi[1] + Cb[6 + u] * vi[2];
+                    LbTv[u] = Lb[u] * vi[0] + Lb[3 + u] * vi[1] + Lb[6 + u] * vi[2];
+                    vib[u] = w * vt[u] + c4 * w * Cbr[u] + (Lb[3 * u] * g[0] + Lb[3 * u + 1] * g[1] + Lb[3 * u + 2] * g[2]);
+                }
+                atomicAdd(a.gvb + id, make_float4(vib[0], vib[1], vib[2], 0.0f));
+                const float vv = vt[0] * vi[0] + vt[1] * vi[1] + vt[2] * vi[2];
+                const float vCr = vi[0] * Cbr[0] + vi[1] * Cbr[1] + vi[2] * Cbr[2];
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+                    xb[d] += (vv + c4 * vCr) * g[d] - c4 * w * CbTv[d] +
+                             (H[3 * d] * LbTv[0] + H[3 * d + 1] * LbTv[1] + H[3 * d + 2] * LbTv[2]);
+            }
+    // adjoint of the projected F: (I + dt L)^T F_trial'-adjoint
+    float A[9], Fb[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) A[i] = ((i % 4 == 0) ? 1.0f : 0.0f) + a.dt * L[i];
+    mTm(A, Ftb, Fb);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) a.Fpb[9 * (size_t)p + i] = Fb[i];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) a.xb[3 * p + d] = xb[d];
+}
+
+// Adjoint of one collider at one node: vb holds the adjoint of the collider's
+// output velocity on entry and of its input velocity vin on return.
+__device__ void collide_adj(const ColDev &c, const PoseRec &P, int gx, int gy, int gz, const float *vin, float *vb,
+                            const AdjK &a) {
+    const float dx = a.dx;
+    switch (c.kind) {
+    case GBMPM_COLLIDER_PLANE: {
+        const float o0 = (float)gx * dx - P.p[0], o1 = (float)gy * dx - P.p[1], o2 = (float)gz * dx - P.p[2];
+        const float dp = o0 * c.normal[0] + o1 * c.normal[1] + o2 * c.normal[2];
+        if (!(dp < 0.0f)) return;
+        if (c.surface == 0) { vb[0] = vb[1] = vb[2] = 0.0f; return; }
+        if (c.surface == 11) {
+            if ((float)gz * dx < 0.4f || (float)gz * dx > 0.53f) { vb[0] = vb[1] = vb[2] = 0.0f; }
+            else { vb[0] *= 0.3f; vb[1] = 0.0f; vb[2] *= 0.3f; }
+            return;
+        }
+        const float *n = c.normal;
+        const float nc = vin[0] * n[0] + vin[1] * n[1] + vin[2] * n[2];
+        const bool slip = c.surface == 1;
+        const float sub = slip ? nc : fminf(nc, 0.0f);
+        const float w[3] = {vin[0] - sub * n[0], vin[1] - sub * n[1], vin[2] - sub * n[2]};
+        const float len = sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        float wb[3] = {vb[0], vb[1], vb[2]}, ncb = 0.0f;
+        if (nc < 0.0f && len > 1e-20f) {
+            const float t = len + nc * c.friction;
+            if (t <= 0.0f) {
+                wb[0] = wb[1] = wb[2] = 0.0f;
+            } else {   // v = w + mu nc w/|w|
+                const float wh[3] = {w[0] / len, w[1] / len, w[2] / len};
+                const float whv = wh[0] * vb[0] + wh[1] * vb[1] + wh[2] * vb[2];
+                const float f = c.friction * nc / len;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) wb[d] = vb[d] + f * (vb[d] - wh[d] * whv);
+                ncb = c.friction * whv;
+            }
+        }
+        const float ds = (slip || nc < 0.0f) ? 1.0f : 0.0f;   // d sub / d nc
+        const float nw = n[0] * wb[0] + n[1] * wb[1] + n[2] * wb[2];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) vb[d] = wb[d] + n[d] * (ncb - ds * nw);
+        return;
+    }
+    case GBMPM_COLLIDER_BOX: {
+        if (P.mode == 2) { vb[0] = vb[1] = vb[2] = 0.0f; return; }
+        const float o0 = (float)gx * dx - P.p[0], o1 = (float)gy * dx - P.p[1], o2 = (float)gz * dx - P.p[2];
+        if (fabsf(o0) < c.size[0] && fabsf(o1) < c.size[1] && fabsf(o2) < c.size[2]) vb[0] = vb[1] = vb[2] = 0.0f;
+        return;
+    }
+    case GBMPM_COLLIDER_WALLS: {
+        const int pad = 3, n = a.ng;
+        if ((gx < pad && vin[0] < 0.0f) || (gx >= n - pad && vin[0] > 0.0f)) vb[0] = 0.0f;
+        if ((gy < pad && vin[1] < 0.0f) || (gy >= n - pad && vin[1] > 0.0f)) vb[1] = 0.0f;
+        if ((gz < pad && vin[2] < 0.0f) || (gz >= n - pad && vin[2] > 0.0f)) vb[2] = 0.0f;
+        return;
+    }
+    default:
+        return;
+    }
+}
+
+__global__ void k_adj_grid_bwd(AdjK a) {
+    const size_t N = (size_t)a.ng * a.ng * a.ng;
+    const GK gk = adj_gk(a);
+    for (size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x; id < N; id += (size_t)gridDim.x * blockDim.x) {
+        const float4 mv = a.gmv[id];
+        if (!(mv.w > 1e-15f)) { a.gmb[id] = make_float4(0.f, 0.f, 0.f, 0.f); continue; }
+        const int gz = (int)(id % a.ng), gy = (int)((id / a.ng) % a.ng), gx = (int)(id / ((size_t)a.ng * a.ng));
+        float vin[kMaxCol][3], v[3], acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        grid_pre(a, mv, v);
+        for (int c = 0; c < a.ncol; ++c) {
+            vin[c][0] = v[0]; vin[c][1] = v[1]; vin[c][2] = v[2];
+            if (a.poses[c].mode != 0) collide(a.cols[c], a.poses[c], gx, gy, gz, mv.w, v, gk, acc);
+        }
+        const float4 b4 = a.gvb[id];
+        float vb[3] = {b4.x, b4.y, b4.z};
+        for (int c = a.ncol - 1; c >= 0; --c)
+            if (a.poses[c].mode != 0) collide_adj(a.cols[c], a.poses[c], gx, gy, gz, vin[c], vb, a);
+        if (a.damp < 1.0f) { vb[0] *= a.damp; vb[1] *= a.damp; vb[2] *= a.damp; }
+        const float inv = 1.0f / mv.w;
+        const float mb = -(vb[0] * mv.x + vb[1] * mv.y + vb[2] * mv.z) * inv * inv;
+        a.gmb[id] = make_float4(vb[0] * inv, vb[1] * inv, vb[2] * inv, mb);
+    }
+}
+
+__global__ void k_adj_p2g_bwd(AdjK a) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.n || (a.sel && a.sel[p] != 0)) return;
+    const float x[3] = {a.x[3 * p], a.x[3 * p + 1], a.x[3 * p + 2]};
+    const float v[3] = {a.v[3 * p], a.v[3 * p + 1], a.v[3 * p + 2]};
+    float C[9], S[9], Fp[9], Ft[9], Fb[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        C[i] = a.C[9 * (size_t)p + i];
+        S[i] = a.S[9 * (size_t)p + i];
+        Fp[i] = a.Fp[9 * (size_t)p + i];
+        Ft[i] = a.Ft[9 * (size_t)p + i];
+        Fb[i] = a.Fpb[9 * (size_t)p + i];
+    }
+    const float m = a.mass[p], vol = a.vol[p], mu = a.mu[p], lam = a.lam[p], ys = a.ys[p];
+    const int mat = a.mat[p];
+    float xb[3] = {a.xb[3 * p], a.xb[3 * p + 1], a.xb[3 * p + 2]};
+    Stencil s;
+    stencil(x, a.inv_dx, s);
+    if (!stencil_ok(s, a.ng, 0)) return;
+    float A[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) A[i] = -vol * S[i];
+    float vb[3] = {0.f, 0.f, 0.f}, Cb[9] = {0.f}, Ab[9] = {0.f};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            for (int kk = 0; kk < 3; ++kk) {
+                const size_t id = ((size_t)(s.b[0] + i) * a.ng + (s.b[1] + j)) * a.ng + (s.b[2] + kk);
+                const float4 b4 = a.gmb[id];
+                const float mb[3] = {b4.x, b4.y, b4.z};
+                float w, g[3], H[9];
+                weight_derivs(s, a.inv_dx, i, j, kk, w, g, H);
+                const float r[3] = {((float)i - s.fx[0]) * a.dx, ((float)j - s.fx[1]) * a.dx, ((float)kk - s.fx[2]) * a.dx};
+                float q[3], CTm[3], ATm[3];
+#pragma unroll
+                for (int u = 0; u < 3; ++u) {
+                    q[u] = v[u] + C[3 * u] * r[0] + C[3 * u + 1] * r[1] + C[3 * u + 2] * r[2];
+                    CTm[u] = C[u] * mb[0] + C[3 + u] * mb[1] + C[6 + u] * mb[2];
+                    ATm[u] = A[u] * mb[0] + A[3 + u] * mb[1] + A[6 + u] * mb[2];
+                    vb[u] += w * m * mb[u];
+#pragma unroll
+                    for (int t = 0; t < 3; ++t) {
+                        Cb[3 * u + t] += w * m * mb[u] * r[t];
+                        Ab[3 * u + t] += a.dt * mb[u] * g[t];
+                    }
+                }
+                const float qm = q[0] * mb[0] + q[1] * mb[1] + q[2] * mb[2];
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+                    xb[d] += m * (qm + b4.w) * g[d] - w * m * CTm[d] +
+                             a.dt * (H[3 * d] * ATm[0] + H[3 * d + 1] * ATm[1] + H[3 * d + 2] * ATm[2]);
+            }
+    // stress adjoint: S = sym(tau), A = -vol S
+    float tb[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) tb[3 * i + j] = -0.5f * vol * (Ab[3 * i + j] + Ab[3 * j + i]);
+    float mub = 0.0f, lamb = 0.0f;
+    {
+        float U[9], V[9], sg[3], yd[3];
+        svd3(Fp, U, sg, V);
+        if (mat == 0) {   // tau = 2 mu (F - R) F^T + lam J (J - 1) I
+            float R[9], FR[9], T1[9], T2[9], cof[9];
+            mmT(U, V, R);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) FR[i] = Fp[i] - R[i];
+            mm(tb, Fp, T1);       // tau_b F
+            mTm(tb, FR, T2);      // tau_b^T (F - R)
+            float Rb[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                Fb[i] += 2.0f * mu * (T1[i] + T2[i]);
+                Rb[i] = -2.0f * mu * T1[i];
+            }
+            const float one[3] = {1.0f, 1.0f, 1.0f};
+            const float J0[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+            iso_adjoint(U, sg, V, one, J0, Rb, Fb, yd);
+            const float J = det3(Fp);
+            const float trb = tb[0] + tb[4] + tb[8];
+            cofactor(Fp, cof);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Fb[i] += lam * (2.0f * J - 1.0f) * trb * cof[i];
+            float FRF[9];
+            mmT(FR, Fp, FRF);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) mub += 2.0f * tb[i] * FRF[i];
+            lamb += J * (J - 1.0f) * trb;
+        } else {          // Hencky: tau = G F^T, G = U diag(h / s) V^T
+            float e[3], de[3], h[3], gg[3], Jg[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                e[i] = logf(fmaxf(sg[i], 1e-6f));
+                de[i] = (sg[i] > 1e-6f) ? 1.0f / sg[i] : 0.0f;
+            }
+            const float tr = e[0] + e[1] + e[2];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                h[i] = 2.0f * mu * e[i] + lam * tr;
+                gg[i] = (sg[i] > 1e-6f) ? h[i] / sg[i] : 0.0f;
+            }
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    const float dh = ((i == j) ? 2.0f * mu : 0.0f) * de[j] + lam * de[j];
+                    Jg[i][j] = (sg[i] > 1e-6f) ? (dh / sg[i] - ((i == j) ? h[i] / (sg[i] * sg[i]) : 0.0f)) : 0.0f;
+                }
+            float G[9], Gb[9], T1[9];
+            udvt(U, gg[0], gg[1], gg[2], V, G);
+            mm(tb, Fp, Gb);
+            mTm(tb, G, T1);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Fb[i] += T1[i];
+            iso_adjoint(U, sg, V, gg, Jg, Gb, Fb, yd);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+                if (sg[i] > 1e-6f) {
+                    mub += yd[i] * 2.0f * e[i] / sg[i];
+                    lamb += yd[i] * tr / sg[i];
+                }
+        }
+    }
+    // return-map adjoint: F (projected) -> F_trial, yield, mu
+    float Ftb[9];
+    float ysb_in = a.ysb[p], ysb = ysb_in;
+    if (mat == 1) {
+        float U[9], V[9], sg[3], e[3], Fq[9];
+        const bool plastic = vm_return(Ft, mu, lam, ys, U, sg, V, e, Fq);
+        if (!plastic) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Ftb[i] = Fb[i];
+        } else {
+            const float mean = (e[0] + e[1] + e[2]) / 3.0f;
+            const float eh[3] = {e[0] - mean, e[1] - mean, e[2] - mean};
+            const float nrm = sqrtf(eh[0] * eh[0] + eh[1] * eh[1] + eh[2] * eh[2]);
+            const float ehn = nrm + 1e-6f;
+            const float kap = ys / (2.0f * mu * ehn);
+            float de[3], ep[3], g[3], Jg[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                de[i] = (sg[i] > 0.01f) ? 1.0f / sg[i] : 0.0f;
+                ep[i] = e[i] - (1.0f - kap) * eh[i];
+                g[i] = expf(ep[i]);
+            }
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    const float dep = ((i == j) ? kap : 0.0f) + (1.0f - kap) / 3.0f -
+                                      (nrm > 0.0f ? kap / ehn * eh[i] * eh[j] / nrm : 0.0f);
+                    Jg[i][j] = g[i] * dep * de[j];
+                }
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Ftb[i] = 0.0f;
+            float yd[3];
+            iso_adjoint(U, sg, V, g, Jg, Fb, Ftb, yd);
+            ysb = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                ysb += yd[i] * g[i] * eh[i] / (2.0f * mu * ehn);
+                mub += yd[i] * g[i] * (-eh[i] * kap / mu);
+            }
+            if (a.hard1 > 0.5f) {   // yield' = yield + 2 mu xi (ehn - yield / (2 mu))
+                ysb += ysb_in * (1.0f - a.xi1);
+                mub += ysb_in * 2.0f * a.xi1 * ehn;
+                if (nrm > 0.0f) {
+                    float sb[3];
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) sb[i] = ysb_in * 2.0f * mu * a.xi1 * eh[i] / nrm * de[i];
+                    float T[9];
+                    udvt(U, sb[0], sb[1], sb[2], V, T);
+#pragma unroll
+                    for (int i = 0; i < 9; ++i) Ftb[i] += T[i];
+                }
+            } else {
+                ysb += ysb_in;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Ftb[i] = Fb[i];
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) { a.xb[3 * p + d] = xb[d]; a.vb[3 * p + d] = vb[d]; }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) { a.Cb[9 * (size_t)p + i] = Cb[i]; a.Ftb[9 * (size_t)p + i] = Ftb[i]; }
+    a.ysb[p] = ysb;
+    a.mub[p] += mub;
+    a.lamb[p] += lamb;
+}
+
+}  // namespace gbmpm
+
+// ------------------------------------------------------------- host side ----
+namespace {
+
+int adjoint_supported(gbmpm_engine *e) {
+    if (e->M.periodic_x) return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint does not wrap the periodic x axis");
+    if (e->M.rpic_damping != 0.0f) return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint needs rpic_damping == 0");
+    if (e->M.material_mask & ~3u)
+        return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint covers jelly (0) and von Mises (1) particles only");
+    if (e->cdf.n > 0) return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint does not cover CDF colliders");
+    for (const gbmpm_collider &c : e->cols)
+        if (c.kind != GBMPM_COLLIDER_PLANE && c.kind != GBMPM_COLLIDER_BOX && c.kind != GBMPM_COLLIDER_WALLS)
+            return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint covers plane, cuboid and domain-wall colliders only");
+    return GBMPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t substeps, const gbmpm_adj_grads *gr,
+                          void *stream) {
+    int rc = check_ready(e);
+    if (rc) return rc;
+    if (!time || !gr || substeps < 1 || substeps > GBMPM_MAX_SUBSTEPS || !(dt > 0.0))
+        return fail(GBMPM_ERR_ARG, "bad adjoint arguments");
+    if (!gr->x || !gr->v || !gr->C || !gr->F_trial || !gr->yield_stress || !gr->mu || !gr->lam)
+        return fail(GBMPM_ERR_ARG, "every adjoint array is required");
+    if ((rc = adjoint_supported(e))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const gbmpm_particles &P = e->P;
+    const int n = P.n, ng = e->G.n_grid, nc = (int)e->cols.size();
+    const size_t nn = (size_t)ng * ng * ng;
+    // segment storage: the state at the start of every substep, the collider records
+    // and clock it started with
+    const size_t per = (size_t)25 * n;   // x 3, v 3, C 9, F_trial 9, yield 1
+    GB_CUDA(e->adj_states.ensure(per * substeps));
+    GB_CUDA(e->adj_scratch.ensure((size_t)27 * n));
+    GB_CUDA(e->adj_grid.ensure(4 * nn));   // four float4 grids
+    GB_CUDA(e->adj_pose.ensure((size_t)std::max(1, nc) * substeps));
+    std::vector<PoseRec> poses((size_t)std::max(1, nc) * substeps);
+    std::vector<double> times(substeps);
+    const float dtf = (float)dt;
+    for (int i = 0; i < substeps; ++i) {
+        float *st = e->adj_states.ptr + per * i;
+        GB_CUDA(cudaMemcpyAsync(st, P.x, 3 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        GB_CUDA(cudaMemcpyAsync(st + 3 * (size_t)n, P.v, 3 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        GB_CUDA(cudaMemcpyAsync(st + 6 * (size_t)n, P.C, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        GB_CUDA(cudaMemcpyAsync(st + 15 * (size_t)n, P.F_trial, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        GB_CUDA(cudaMemcpyAsync(st + 24 * (size_t)n, P.yield_stress, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        times[i] = *time;
+        const float tf = (float)*time;
+        for (int c = 0; c < nc; ++c) poses[(size_t)i * std::max(1, nc) + c] = pose_of(e->cols[c], tf, dtf);
+        rc = gbmpm_tick(e, time, dt, 1, 0, stream);
+        if (rc) return rc;
+    }
+    GB_CUDA(cudaMemcpyAsync(e->adj_pose.ptr, poses.data(), poses.size() * sizeof(PoseRec), cudaMemcpyHostToDevice, s));
+    std::vector<ColDev> cd(std::max(1, nc));
+    for (int c = 0; c < nc; ++c) cd[c] = to_dev(e->cols[c]);
+    GB_CUDA(e->adj_cols.ensure(std::max(1, nc)));
+    GB_CUDA(cudaMemcpyAsync(e->adj_cols.ptr, cd.data(), cd.size() * sizeof(ColDev), cudaMemcpyHostToDevice, s));
+    float4 *grid = e->adj_grid.ptr;
+    const int pb = std::max(1, (n + 127) / 128);
+    const int gb = e->num_sms * 8;
+    for (int i = substeps - 1; i >= 0; --i) {
+        const float *st = e->adj_states.ptr + per * i;
+        AdjK a{};
+        a.x = st; a.v = st + 3 * (size_t)n; a.C = st + 6 * (size_t)n; a.Ft = st + 15 * (size_t)n;
+        a.ys = st + 24 * (size_t)n;
+        a.mass = P.mass; a.vol = P.vol; a.mu = P.mu; a.lam = P.lam; a.mat = P.material; a.sel = P.selection;
+        a.n = n;
+        a.Fp = e->adj_scratch.ptr; a.S = a.Fp + 9 * (size_t)n; a.Fpb = a.S + 9 * (size_t)n;
+        a.gmv = grid; a.gv = grid + nn; a.gvb = grid + 2 * nn; a.gmb = grid + 3 * nn;
+        a.ng = ng; a.dx = e->M.dx; a.inv_dx = e->M.inv_dx; a.dt = dtf;
+        for (int d = 0; d < 3; ++d) a.grav[d] = e->M.gravity[d];
+        a.damp = e->M.grid_v_damping_scale;
+        a.hard1 = e->M.hardening[1]; a.xi1 = e->M.xi[1];
+        a.xb = gr->x; a.vb = gr->v; a.Cb = gr->C; a.Ftb = gr->F_trial; a.ysb = gr->yield_stress;
+        a.mub = gr->mu; a.lamb = gr->lam;
+        a.ncol = nc; a.cols = e->adj_cols.ptr; a.poses = e->adj_pose.ptr + (size_t)i * std::max(1, nc);
+        // the engine's P2G building block reads its inputs through a PK
+        gbmpm_particles Ps = P;
+        Ps.x = const_cast<float *>(a.x); Ps.v = const_cast<float *>(a.v); Ps.C = const_cast<float *>(a.C);
+        PK k = make_pk(e, Ps, dtf, 0);
+        k.cdf_on = 0;
+        GB_CUDA(cudaMemsetAsync(grid, 0, 4 * nn * sizeof(float4), s));
+        k_adj_stress_fwd<<<pb, 128, 0, s>>>(a);
+        k_adj_p2g_fwd<<<pb, 128, 0, s>>>(a, k);
+        k_adj_grid_fwd<<<gb, 256, 0, s>>>(a);
+        k_adj_g2p_bwd<<<pb, 128, 0, s>>>(a);
+        k_adj_grid_bwd<<<gb, 256, 0, s>>>(a);
+        k_adj_p2g_bwd<<<pb, 128, 0, s>>>(a);
+        e->launches += 6;
+    }
+    GB_CUDA(cudaGetLastError());
+    return GBMPM_OK;
+}
+
+}  // extern "C"

@@ -2017,6 +2017,11 @@ struct gbmpm_engine {
     DevBuf<float> c_d, c_d_prev;
     DevBuf<double> c_wrench;
     int c_ng = 0;
+    // adjoint segment storage and scratch (allocated by the first adjoint call)
+    DevBuf<float> adj_states, adj_scratch;
+    DevBuf<float4> adj_grid;
+    DevBuf<PoseRec> adj_pose;
+    DevBuf<ColDev> adj_cols;
     // profiling
     double prof_ms[GBMPM_NUM_PHASES] = {0};
     int64_t prof_n[GBMPM_NUM_PHASES] = {0};
@@ -2238,6 +2243,21 @@ void integrate_pose(gbmpm_collider &c, double time, double dt) {
     }
 }
 
+// A collider's pose record for a substep starting at time tf: live inside its
+// window; a cuboid with reset == 1 zeroes its nodes for 15 substeps after it ends.
+PoseRec pose_of(const gbmpm_collider &col, float tf, float dtf) {
+    PoseRec r;
+    std::memset(&r, 0, sizeof r);
+    bool live = tf >= col.start_time && tf < col.end_time;
+    if (col.kind == GBMPM_COLLIDER_BOX && !live && col.reset == 1)
+        r.mode = (tf < col.end_time + 15.0f * dtf) ? 2 : 0;
+    else r.mode = live ? 1 : 0;
+    for (int a = 0; a < 3; ++a) r.p[a] = col.point[a];
+    for (int a = 0; a < 9; ++a) r.r[a] = col.rot[a];
+    for (int a = 0; a < 4; ++a) r.q[a] = col.quat[a];
+    return r;
+}
+
 // Builds the [S][ncol] pose table for a tick and advances the host collider
 // records and clock exactly as S calls of _apply_grid_bc + time += dt would.
 void build_pose_table(gbmpm_engine *e, double &time, double dt, int S) {
@@ -2246,18 +2266,7 @@ void build_pose_table(gbmpm_engine *e, double &time, double dt, int S) {
     float dtf = (float)dt;
     for (int s = 0; s < S; ++s) {
         float tf = (float)time;
-        for (int c = 0; c < nc; ++c) {
-            gbmpm_collider &col = e->cols[c];
-            PoseRec &r = e->h_pose[(size_t)s * stride + c];
-            std::memset(&r, 0, sizeof r);
-            bool live = tf >= col.start_time && tf < col.end_time;
-            if (col.kind == GBMPM_COLLIDER_BOX && !live && col.reset == 1)
-                r.mode = (tf < col.end_time + 15.0f * dtf) ? 2 : 0;
-            else r.mode = live ? 1 : 0;
-            for (int a = 0; a < 3; ++a) r.p[a] = col.point[a];
-            for (int a = 0; a < 9; ++a) r.r[a] = col.rot[a];
-            for (int a = 0; a < 4; ++a) r.q[a] = col.quat[a];
-        }
+        for (int c = 0; c < nc; ++c) e->h_pose[(size_t)s * stride + c] = pose_of(e->cols[c], tf, dtf);
         for (int c = 0; c < nc; ++c) integrate_pose(e->cols[c], time, dt);
         time = time + dt;
     }
@@ -2544,6 +2553,8 @@ void gbmpm_engine_destroy(gbmpm_engine *e) {
     e->ws_idx[1].release(); e->ws_hist.release();
     e->c_tag.release(); e->c_tag_prev.release(); e->c_block.release(); e->c_d.release(); e->c_d_prev.release();
     e->c_wrench.release();
+    e->adj_states.release(); e->adj_scratch.release(); e->adj_grid.release(); e->adj_pose.release();
+    e->adj_cols.release();
     delete e;
 }
 
@@ -3268,3 +3279,5 @@ int gbmpm_guard_noalloc(const float *x, const float *v, int32_t n, float out[7],
 }
 
 }  // extern "C"
+
+#include "adjoint.cuh"

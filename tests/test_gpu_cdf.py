@@ -77,7 +77,10 @@ def test_shelf_parity(cuda, oracle_lib, fused):
         _check_grids(s, o, f"shelf tick {tick}")
         _check_tags(s, o, f"shelf tick {tick}")
         wg, wo = s.cdf_wrench(0, DT * SUB), o.cdf_wrench(0, DT * SUB)
-        assert wg["force"][2] < 0.0, f"tick {tick}: no blocked deposits, the contact was not exercised"
+        # every tick blocks deposits (the water lands, then rebounds off the sheet)
+        assert np.abs(wg["force"]).max() > 0.0, f"tick {tick}: no blocked deposits"
+        if tick == 0:
+            assert wg["force"][2] < 0.0, "the landing water presses down on the sheet"
         for key in ("force", "torque"):
             assert rel_err(wg[key], wo[key], 1e-9) < 1e-3, (tick, key, wg[key], wo[key])
 
