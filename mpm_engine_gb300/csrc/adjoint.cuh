@@ -625,16 +625,16 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
     const gbmpm_particles &P = e->P;
     const int n = P.n, ng = e->G.n_grid, nc = (int)e->cols.size();
     const size_t nn = (size_t)ng * ng * ng;
-    // segment storage: the state at the start of every substep, the collider records
-    // and clock it started with
+    // segment storage: the state at the start of every substep
     const size_t per = (size_t)25 * n;   // x 3, v 3, C 9, F_trial 9, yield 1
     GB_CUDA(e->adj_states.ensure(per * substeps));
     GB_CUDA(e->adj_scratch.ensure((size_t)27 * n));
     GB_CUDA(e->adj_grid.ensure(4 * nn));   // four float4 grids
-    GB_CUDA(e->adj_pose.ensure((size_t)std::max(1, nc) * substeps));
-    std::vector<PoseRec> poses((size_t)std::max(1, nc) * substeps);
-    std::vector<double> times(substeps);
     const float dtf = (float)dt;
+    // forward replay on the split schedule: one pose table for the whole segment
+    // (the adjoint kernels read the same table), no host synchronization per substep
+    bool reorder = false;
+    if ((rc = prepare_tick(e, time, dt, substeps, 0, s, reorder))) return rc;
     for (int i = 0; i < substeps; ++i) {
         float *st = e->adj_states.ptr + per * i;
         GB_CUDA(cudaMemcpyAsync(st, P.x, 3 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
@@ -642,17 +642,8 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
         GB_CUDA(cudaMemcpyAsync(st + 6 * (size_t)n, P.C, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         GB_CUDA(cudaMemcpyAsync(st + 15 * (size_t)n, P.F_trial, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         GB_CUDA(cudaMemcpyAsync(st + 24 * (size_t)n, P.yield_stress, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-        times[i] = *time;
-        const float tf = (float)*time;
-        for (int c = 0; c < nc; ++c) poses[(size_t)i * std::max(1, nc) + c] = pose_of(e->cols[c], tf, dtf);
-        rc = gbmpm_tick(e, time, dt, 1, 0, stream);
-        if (rc) return rc;
+        record_tick(e, dtf, 1, false, false, s, false, 0.0, 0.0, i);
     }
-    GB_CUDA(cudaMemcpyAsync(e->adj_pose.ptr, poses.data(), poses.size() * sizeof(PoseRec), cudaMemcpyHostToDevice, s));
-    std::vector<ColDev> cd(std::max(1, nc));
-    for (int c = 0; c < nc; ++c) cd[c] = to_dev(e->cols[c]);
-    GB_CUDA(e->adj_cols.ensure(std::max(1, nc)));
-    GB_CUDA(cudaMemcpyAsync(e->adj_cols.ptr, cd.data(), cd.size() * sizeof(ColDev), cudaMemcpyHostToDevice, s));
     float4 *grid = e->adj_grid.ptr;
     const int pb = std::max(1, (n + 127) / 128);
     const int gb = e->num_sms * 8;
@@ -671,7 +662,7 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
         a.hard1 = e->M.hardening[1]; a.xi1 = e->M.xi[1];
         a.xb = gr->x; a.vb = gr->v; a.Cb = gr->C; a.Ftb = gr->F_trial; a.ysb = gr->yield_stress;
         a.mub = gr->mu; a.lamb = gr->lam;
-        a.ncol = nc; a.cols = e->adj_cols.ptr; a.poses = e->adj_pose.ptr + (size_t)i * std::max(1, nc);
+        a.ncol = nc; a.cols = e->d_cols.ptr; a.poses = e->d_pose.ptr + (size_t)i * std::max(1, nc);
         // the engine's P2G building block reads its inputs through a PK
         gbmpm_particles Ps = P;
         Ps.x = const_cast<float *>(a.x); Ps.v = const_cast<float *>(a.v); Ps.C = const_cast<float *>(a.C);

@@ -2020,8 +2020,6 @@ struct gbmpm_engine {
     // adjoint segment storage and scratch (allocated by the first adjoint call)
     DevBuf<float> adj_states, adj_scratch;
     DevBuf<float4> adj_grid;
-    DevBuf<PoseRec> adj_pose;
-    DevBuf<ColDev> adj_cols;
     // profiling
     double prof_ms[GBMPM_NUM_PHASES] = {0};
     int64_t prof_n[GBMPM_NUM_PHASES] = {0};
@@ -2443,7 +2441,7 @@ void cdf_integrate(gbmpm_engine *e, double time, double dt, bool lag_prev) {
 // launches (t0 = the tick's start time, dt its float64 substep), so such ticks
 // run live, on the direct kernel.
 void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cudaStream_t s, bool profile,
-                 double t0 = 0.0, double dt = 0.0) {
+                 double t0 = 0.0, double dt = 0.0, int pose_offset = 0) {
     // Profiling brackets every phase launch with an event pair and resolves the pairs
     // once at the end of the tick: the host stays ahead of the GPU, so each pair
     // measures the launch itself rather than host submission latency.
@@ -2478,7 +2476,7 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
                        (cdf ? PASS_STORE_VC : 0);
             timed(2, [&] { launch_particles(e, k, mode, reorder, s); });
         }
-        timed(3, [&] { launch_grid(e, dtf, sub, list, s); });
+        timed(3, [&] { launch_grid(e, dtf, pose_offset + sub, list, s); });
         if (cdf) cdf_integrate(e, tc, dt, fused);
         tc = tc + dt;
         if (!fused) {
@@ -2553,8 +2551,7 @@ void gbmpm_engine_destroy(gbmpm_engine *e) {
     e->ws_idx[1].release(); e->ws_hist.release();
     e->c_tag.release(); e->c_tag_prev.release(); e->c_block.release(); e->c_d.release(); e->c_d_prev.release();
     e->c_wrench.release();
-    e->adj_states.release(); e->adj_scratch.release(); e->adj_grid.release(); e->adj_pose.release();
-    e->adj_cols.release();
+    e->adj_states.release(); e->adj_scratch.release(); e->adj_grid.release();
     delete e;
 }
 
