@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--no-adjoint", action="store_true")
     return ap.parse_args()
 
 
@@ -191,6 +192,61 @@ def batched_measure(n_scenes: int, ticks: int, substeps: int = 100, dt: float = 
             "scenes": n_scenes, "particles_total": n_part, "ticks": ticks, "dt": dt,
             "particle_substeps_per_s": n_part * substeps * ticks / t_batch,
             "gpu_launches": batch.launch_count() - launches0}
+
+
+def adjoint_measure(n_scenes: int = 32, n_particles: int = 50_000, n_grid: int = 48, substeps: int = 400,
+                    every: int = 20, dt: float = 1.0e-5, device: str = "cuda:0", seed: int = 0):
+    """Batched forward+adjoint workload: n_scenes von Mises cubes of about
+    n_particles (8 per cell, jittered) on n_grid^3 grids, squeezed by a plate at
+    0.05 m/s; per scene seeded E log-uniform [1e4, 1e6], nu in [0.2, 0.45], yield
+    log-uniform [1e2, 1e4]. One scene = a rollout of `substeps` substeps and its
+    reverse pass (checkpoints every `every` substeps) for L = sum(a x) + sum(b v).
+    Plain runs the scenes one after another; batched runs all forwards in one CUDA
+    graph per segment and the reverse passes on one stream per scene."""
+    import torch
+    from mpm_engine_gb300 import Solver, adjoint
+    from mpm_engine_gb300.materials import vonmises
+    from mpm_engine_gb300.scenes import squeeze_scene
+    rng = np.random.default_rng(seed)
+    scenes = []
+    for i in range(n_scenes):
+        E = float(np.exp(rng.uniform(np.log(1e4), np.log(1e6))))
+        nu = float(rng.uniform(0.2, 0.45))
+        ys = float(np.exp(rng.uniform(np.log(1e2), np.log(1e4))))
+        s, _ = squeeze_scene(Solver, n_particles, n_grid, vonmises(E=E, nu=nu, yield_stress=ys, density=1000.0),
+                             seed=i, device=device)
+        scenes.append(s)
+    starts = [adjoint._snapshot(s) for s in scenes]
+    weights = [(torch.randn(s.n_particles, 3, device=device), torch.randn(s.n_particles, 3, device=device))
+               for s in scenes]
+
+    def run(batched, k):
+        for s, st in zip(scenes, starts):
+            adjoint._restore(s, st)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if batched:
+            r = adjoint.BatchRollout(scenes, dt, k, every, batched=True)
+            r.forward()
+            r.backward([w[0] for w in weights], [w[1] for w in weights])
+        else:
+            for s, w in zip(scenes, weights):
+                r = adjoint.BatchRollout([s], dt, k, every, batched=False)
+                r.forward()
+                r.backward([w[0]], [w[1]])
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    run(True, 2 * every)     # warm-up: scratch, graphs
+    run(False, 2 * every)
+    t_plain = run(False, substeps)
+    t_batch = run(True, substeps)
+    n_total = sum(s.n_particles for s in scenes)
+    return {"metric": "batched forward+adjoint scenes/s", "unit": f"scenes/s ({substeps} substeps each)",
+            "value": n_scenes / t_batch, "plain_value": n_scenes / t_plain, "speedup_vs_plain": t_plain / t_batch,
+            "scenes": n_scenes, "particles_total": n_total, "grid": f"{n_grid}^3", "substeps": substeps,
+            "checkpoint_every": every, "dt": dt,
+            "particle_substeps_per_s": n_total * substeps / t_batch}
 
 
 def dist_setup(args):
@@ -364,6 +420,10 @@ def main():
     if not args.no_batched:
         batched = batched_measure(args.batch_scenes, ticks=max(2, min(args.steps, 4)), device=f"cuda:{local}")
 
+    adj = None
+    if not args.no_adjoint:
+        adj = adjoint_measure(device=f"cuda:{local}")
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(s.export_state(), desc, args.cpu_seconds)
@@ -375,7 +435,7 @@ def main():
                 "config": {**desc, "l2": "256 MB buffer written between timed steps", "parallelism":
                            "replicas" if world > 1 else "single"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk, "batched": batched}
+                "clocks": clk, "batched": batched, "batched_adjoint": adj}
         print(json.dumps(line))
     if dist:
         dist.barrier()

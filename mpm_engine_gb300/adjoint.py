@@ -148,4 +148,78 @@ def rollout(solver, dt: float, substeps: int, *, v0=None, E=None, nu=None, yield
     return _Rollout.apply(v0, mu, lam, ys, s, float(dt), int(substeps), int(checkpoint_every))
 
 
-__all__ = ["mu_lam", "rollout"]
+class BatchRollout:
+    """Forward and reverse passes of many independent scenes (the batched
+    identification workload). Each scene is a loaded Solver whose current state
+    and parameters define its rollout. With `batched` the forward advances all
+    scenes in one CUDA graph per segment (BatchSolver) and the reverse pass runs
+    each scene's segments on its own stream; otherwise scenes run one after
+    another, as serial rollouts would."""
+
+    def __init__(self, solvers, dt: float, substeps: int, checkpoint_every: int = 20, batched: bool = True):
+        torch = _torch()
+        from .solver import BatchSolver
+        self.solvers = list(solvers)
+        for s in self.solvers:
+            _check(s)
+        self.dt, self.substeps, self.every = float(dt), int(substeps), int(checkpoint_every)
+        self.batched = batched
+        self.batch = BatchSolver(self.solvers) if batched else None
+        self.streams = [torch.cuda.Stream(device=s._t["x"].device) for s in self.solvers] if batched else None
+        self.ckpts = None
+
+    def forward(self):
+        """Runs every rollout; returns [(x, v)] at the end."""
+        if not self.batched:
+            self.ckpts = [_forward(s, self.dt, self.substeps, self.every) for s in self.solvers]
+        else:
+            self.ckpts = [[] for _ in self.solvers]
+            done = 0
+            while done < self.substeps:
+                k = min(self.every, self.substeps - done)
+                for i, s in enumerate(self.solvers):
+                    self.ckpts[i].append((_snapshot(s), k))
+                self.batch.step(self.dt, k)
+                done += k
+        self.final = [_snapshot(s) for s in self.solvers]
+        return [(s._t["x"].clone(), s._t["v"].clone()) for s in self.solvers]
+
+    def backward(self, xbs, vbs):
+        """Adjoints of the rollouts' starting states and parameters for the given
+        adjoints of their final (x, v): [{'v', 'x', 'C', 'F_trial', 'yield_stress',
+        'mu', 'lam'}]. Leaves every solver at its rollout's end state."""
+        torch = _torch()
+        if self.ckpts is None:
+            raise RuntimeError("forward must run first")
+        if not self.batched:
+            out = [_backward(s, self.dt, ck, xb, vb) for s, ck, xb, vb in zip(self.solvers, self.ckpts, xbs, vbs)]
+        else:
+            torch.cuda.synchronize()
+            gs, recs = [], []
+            for s, xb, vb in zip(self.solvers, xbs, vbs):
+                n = s.n_particles
+                f = dict(device=s._t["x"].device, dtype=torch.float32)
+                g = {"x": xb.detach().to(**f).reshape(n, 3).clone(), "v": vb.detach().to(**f).reshape(n, 3).clone(),
+                     "C": torch.zeros(n, 3, 3, **f), "F_trial": torch.zeros(n, 3, 3, **f),
+                     "yield_stress": torch.zeros(n, **f), "mu": torch.zeros(n, **f), "lam": torch.zeros(n, **f)}
+                gs.append(g)
+                recs.append(_abi.AdjGrads(**{k: g[k].data_ptr() for k in g}))
+            torch.cuda.synchronize()
+            nseg = len(self.ckpts[0])
+            for j in reversed(range(nseg)):
+                for i, s in enumerate(self.solvers):
+                    snap, k = self.ckpts[i][j]
+                    with torch.cuda.stream(self.streams[i]):
+                        _restore(s, snap)
+                        t = C.c_double(s._time)
+                        _abi.check(s._eng.lib.gbmpm_adjoint_segment(s._eng.h, C.byref(t), self.dt, int(k),
+                                                                    C.byref(recs[i]), s._stream()),
+                                   "gbmpm_adjoint_segment")
+            torch.cuda.synchronize()
+            out = gs
+        for s, snap in zip(self.solvers, self.final):
+            _restore(s, snap)
+        return out
+
+
+__all__ = ["BatchRollout", "mu_lam", "rollout"]

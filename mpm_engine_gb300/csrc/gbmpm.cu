@@ -1973,6 +1973,7 @@ struct gbmpm_engine {
     gbmpm_model M{};
     bool bound = false, modeled = false;
     std::vector<gbmpm_collider> cols;
+    std::vector<ColDev> h_cols;   // the descriptor table last uploaded to d_cols
     // device scratch
     DevBuf<MatTables> d_tab;
     DevBuf<ColDev> d_cols;
@@ -2617,8 +2618,15 @@ int gbmpm_set_colliders(gbmpm_engine *e, const gbmpm_collider *c, int32_t n) {
     e->cols.assign(c, c + n);
     std::vector<ColDev> d(std::max(1, n));
     for (int i = 0; i < n; ++i) d[i] = to_dev(c[i]);
-    GB_CUDA(e->d_cols.ensure(d.size()));
-    GB_CUDA(cudaMemcpy(e->d_cols.ptr, d.data(), d.size() * sizeof(ColDev), cudaMemcpyHostToDevice));
+    // descriptors hold no pose, so a pose-only update leaves the device table as it
+    // is (kernels of earlier ticks may still be reading it)
+    bool same = e->h_cols.size() == d.size() && e->d_cols.ptr &&
+                std::memcmp(e->h_cols.data(), d.data(), d.size() * sizeof(ColDev)) == 0;
+    if (!same) {
+        GB_CUDA(e->d_cols.ensure(d.size()));
+        GB_CUDA(cudaMemcpy(e->d_cols.ptr, d.data(), d.size() * sizeof(ColDev), cudaMemcpyHostToDevice));
+        e->h_cols = d;
+    }
     if (e->d_wrench.n < (size_t)kMaxCol * 6) {
         std::vector<double> keep(e->d_wrench.n);
         if (e->d_wrench.ptr && e->d_wrench.n)

@@ -90,20 +90,24 @@ class Case:
         h = rel if which == "v0" else rel * {"E": self.E, "nu": self.nu, "ys": self.ys}[which]
         return (at(1.0) - at(-1.0)) / (2.0 * h)
 
-    def fd_oracle(self, O, which, rel=1e-2):
+    def fd_oracle(self, O, which, rel=1e-2, direction=None):
         from mpm_engine_gb300.host import mu_lam_from_E_nu_f32
 
         def at(sg):
             p = {"E": self.E, "nu": self.nu, "ys": self.ys}
-            p[which] = p[which] * (1.0 + sg * rel)
+            if which != "v0":
+                p[which] = p[which] * (1.0 + sg * rel)
             o = O.from_state(self.state, NG, 0.4)
             mu, lam = mu_lam_from_E_nu_f32(np.full(N, p["E"], np.float32), np.full(N, p["nu"], np.float32))
             o.a["mu"][:] = mu
             o.a["lam"][:] = lam
             o.a["yield_stress"][:] = np.float32(p["ys"])
+            if which == "v0":
+                o.a["v"][:] = (o.a["v"].astype(np.float64) + sg * rel * direction).astype(np.float32)
             o.step(DT, K)
             return _loss_np(o.a["x"], o.a["v"])
-        return (at(1.0) - at(-1.0)) / (2.0 * rel * {"E": self.E, "nu": self.nu, "ys": self.ys}[which])
+        h = rel if which == "v0" else rel * {"E": self.E, "nu": self.nu, "ys": self.ys}[which]
+        return (at(1.0) - at(-1.0)) / (2.0 * h)
 
 
 def _close(ad, fd, tol, what):
@@ -123,7 +127,9 @@ def test_gradients_match_gpu_finite_differences(cuda, key, kw):
         _close(g[p], c.fd_gpu(p), 0.02, f"{key} d/d{p}")
     d = torch.randn(c.v0.shape, generator=torch.Generator().manual_seed(7)).to(c.dev)
     d = d / d.norm()
-    _close(float((g["v0"] * d).sum()), c.fd_gpu("v0", rel=1e-2, direction=d), 0.02, f"{key} d/dv0")
+    # a unit direction over all N x 3 components moves each by ~0.015 per unit step;
+    # a step of 0.1 m/s keeps the response linear and well above atomic-order noise
+    _close(float((g["v0"] * d).sum()), c.fd_gpu("v0", rel=1e-1, direction=d), 0.02, f"{key} d/dv0")
 
 
 @pytest.mark.parametrize("key,kw", [CASES[0], CASES[3]])
@@ -132,6 +138,11 @@ def test_gradients_match_oracle_finite_differences(cuda, oracle_lib, key, kw):
     g = c.grads()
     for p in ("E", "nu") + (("ys",) if key.startswith("metal") else ()):
         _close(g[p], c.fd_oracle(oracle_lib.OracleSolver, p), 0.02, f"{key} d/d{p} (oracle)")
+    d = np.random.default_rng(11).standard_normal((N, 3))
+    d /= np.linalg.norm(d)
+    gv = g["v0"].double().cpu().numpy()
+    _close(float((gv * d).sum()), c.fd_oracle(oracle_lib.OracleSolver, "v0", rel=1e-1, direction=d), 0.02,
+           f"{key} d/dv0 (oracle)")
 
 
 def test_long_rollout_checkpoint_interval_does_not_change_gradients(cuda):
