@@ -221,6 +221,16 @@ int gbmpm_reset_cdf_wrench(gbmpm_engine *e, void *stream);
  * entries (either may be NULL), and the number of stamps so far (_cdf_stamp_count). */
 int gbmpm_cdf_grids(gbmpm_engine *e, int32_t *tag_out, float *d_out, int64_t *stamps, void *stream);
 
+/* Stress-integral reaction on a kinematic box (box_contact_wrench,
+ * coupling/wrench.py:15-46) over the bound particles: out = {fx, fy, fz, tx, ty, tz,
+ * contacts, sum of current volume, inverted particles}. layer <= 0 takes
+ * 3 mean(vol)^(1/3). Volume and Cauchy stress follow the inversion policy
+ * (0 warn: |det F|, 1 nan, 2 raise: GBMPM_ERR_STATE when any particle is inverted;
+ * core/solver.py:559-598). The caller zeroes the result when contacts < 3. */
+int gbmpm_contact_wrench(gbmpm_engine *e, const double box_center[3], const double box_half[3],
+                         double layer, int32_t compressive_only, int32_t policy, double out[9],
+                         void *stream);
+
 /* ---- adjoint (no counterpart in the reference) ---------------------------------
  * Adjoints of the particle state (x, v, C, F_trial, yield_stress; device arrays in
  * the particle layout) and accumulated adjoints of the per-particle mu and lam. */

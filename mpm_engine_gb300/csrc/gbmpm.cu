@@ -265,7 +265,11 @@ __device__ __forceinline__ void stress_update(const PK &k, int p, int mat, const
         float Dd[9], gd;
         dev_rate(L, Dd, gd);
         float eta_app;
-        if (mat == 10) eta_app = T.pv[mat] + k.ys[p] / gd + T.hardening[mat] * powf(gd, T.softening[mat] - 1.0f);
+        if (mat == 10) {
+            // tau_y / gd and K gd^(n-1) are exactly zero when tau_y or K is zero
+            const float ys = k.ys[p], Kp = T.hardening[mat];
+            eta_app = T.pv[mat] + (ys != 0.0f ? ys / gd : 0.0f) + (Kp != 0.0f ? Kp * powf(gd, T.softening[mat] - 1.0f) : 0.0f);
+        }
         else eta_app = table_lerp(k.eta, k.eta_n, k.eta_smin, k.eta_smax, logf(gd) * 0.43429448190325176f);
         float two_eta = 2.0f * eta_app;
 #pragma unroll
@@ -1083,8 +1087,12 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
         set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
         want = false;
     }
-    // ---- scatter record: per-axis weights w[3][3] and dw[3][3], the affine momentum
-    // base m v - m C fx dx, m C dx, the stress term A = -vol dt/dx stress, and m
+    // ---- scatter record (40 floats, 16-byte aligned): [0..11] the x and y weights and
+    // derivatives a lane indexes by its node line (wx[3], wy[3], dwx[3], dwy[3]);
+    // [12..39] what every lane of a particle reads, packed for seven float4 loads:
+    // wz[3], m | dwz[3], b0 | b1, b2, c00, c01 | c02, c10, c11, c12 | c20, c21, c22,
+    // A00 | A01, A02, A10, A11 | A12, A20, A21, A22, with b = m v - m C fx dx the
+    // affine momentum base, c = m C dx and A = -vol dt/dx stress
     if (want) {
         float Cr[9];
 #pragma unroll
@@ -1101,17 +1109,22 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
         const float fs = -k.vol[p] * k.dt * k.inv_dx;
         float rec[kRec];
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int o = 0; o < 3; ++o) { rec[3 * a + o] = s.w[a][o]; rec[9 + 3 * a + o] = s.dw[a][o]; }
+        for (int o = 0; o < 3; ++o) {
+            rec[o] = s.w[0][o];
+            rec[3 + o] = s.w[1][o];
+            rec[6 + o] = s.dw[0][o];
+            rec[9 + o] = s.dw[1][o];
+            rec[12 + o] = s.w[2][o];
+            rec[16 + o] = s.dw[2][o];
+        }
+        rec[15] = m;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             float c0 = m * Cr[3 * a] * k.dx, c1 = m * Cr[3 * a + 1] * k.dx, c2 = m * Cr[3 * a + 2] * k.dx;
-            rec[18 + a] = m * v[a] - (c0 * s.fx[0] + c1 * s.fx[1] + c2 * s.fx[2]);
-            rec[21 + 3 * a] = c0; rec[22 + 3 * a] = c1; rec[23 + 3 * a] = c2;
-            rec[30 + 3 * a] = fs * S[3 * a]; rec[31 + 3 * a] = fs * S[3 * a + 1]; rec[32 + 3 * a] = fs * S[3 * a + 2];
+            rec[19 + a] = m * v[a] - (c0 * s.fx[0] + c1 * s.fx[1] + c2 * s.fx[2]);
+            rec[22 + 3 * a] = c0; rec[23 + 3 * a] = c1; rec[24 + 3 * a] = c2;
+            rec[31 + 3 * a] = fs * S[3 * a]; rec[32 + 3 * a] = fs * S[3 * a + 1]; rec[33 + 3 * a] = fs * S[3 * a + 2];
         }
-        rec[39] = m;
         float4 *dst = reinterpret_cast<float4 *>(s_mem + t * kRec);
 #pragma unroll
         for (int q = 0; q < kRec / 4; ++q) dst[q] = make_float4(rec[4 * q], rec[4 * q + 1], rec[4 * q + 2], rec[4 * q + 3]);
@@ -1149,17 +1162,25 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
         if (lane < 27) {
             for (int q = q0 + g3; q < q1; q += 3) {
                 const float *r = s_mem + q * kRec;
-                const float wxi = r[li], wyj = r[3 + lj], dwxi = r[9 + li], dwyj = r[12 + lj];
+                const float wxi = r[li], wyj = r[3 + lj], dwxi = r[6 + li], dwyj = r[9 + lj];
+                const float4 *r4 = reinterpret_cast<const float4 *>(r);
+                float inv[28];
+#pragma unroll
+                for (int h = 0; h < 7; ++h) {
+                    const float4 f4 = r4[3 + h];
+                    inv[4 * h] = f4.x; inv[4 * h + 1] = f4.y; inv[4 * h + 2] = f4.z; inv[4 * h + 3] = f4.w;
+                }
+                // inv[i] = rec[12 + i]
                 const float u = wxi * wyj, ux = dwxi * wyj, uy = wxi * dwyj;
-                const float wz0 = r[6], wz1 = r[7], wz2 = r[8], dz0 = r[15], dz1 = r[16], dz2 = r[17];
-                const float m = r[39];
+                const float wz0 = inv[0], wz1 = inv[1], wz2 = inv[2], dz0 = inv[4], dz1 = inv[5], dz2 = inv[6];
+                const float m = inv[3];
                 float P[3], Q[3], R[3];
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
-                    P[a] = u * (r[18 + a] + r[21 + 3 * a] * fi + r[22 + 3 * a] * fj) + r[30 + 3 * a] * ux +
-                           r[31 + 3 * a] * uy;
-                    Q[a] = u * r[23 + 3 * a];
-                    R[a] = u * r[32 + 3 * a];
+                    P[a] = u * (inv[7 + a] + inv[10 + 3 * a] * fi + inv[11 + 3 * a] * fj) + inv[19 + 3 * a] * ux +
+                           inv[20 + 3 * a] * uy;
+                    Q[a] = u * inv[12 + 3 * a];
+                    R[a] = u * inv[21 + 3 * a];
                 }
                 const float um = u * m;
 #pragma unroll
@@ -2082,7 +2103,8 @@ void launch_particles(gbmpm_engine *e, const PK &k, int mode, bool tiled, cudaSt
         const bool solids = has_solids(e->M);
         if (solids && e->tile_occ >= 3) k_particles_tiled<true, 3><<<grid, kTileThreads, 0, s>>>(k, mode);
         else if (solids) k_particles_tiled<true, 2><<<grid, kTileThreads, 0, s>>>(k, mode);
-        else if (e->tile_occ >= 3) k_particles_tiled<false, 3><<<grid, kTileThreads, 0, s>>>(k, mode);
+        else if (e->tile_occ >= 4) k_particles_tiled<false, 4><<<grid, kTileThreads, 0, s>>>(k, mode);
+        else if (e->tile_occ == 3) k_particles_tiled<false, 3><<<grid, kTileThreads, 0, s>>>(k, mode);
         else k_particles_tiled<false, 2><<<grid, kTileThreads, 0, s>>>(k, mode);
     } else {
         int grid = std::max(1, (k.n + kParticleThreads - 1) / kParticleThreads);
@@ -3284,5 +3306,119 @@ int gbmpm_guard_noalloc(const float *x, const float *v, int32_t n, float out[7],
 }
 
 }  // extern "C"
+
+// ================================================ stress-integral contact wrench
+// box_contact_wrench (coupling/wrench.py:15-46) on the device: the reaction on a
+// kinematic box from the Cauchy traction of the particles in a layer of thickness T
+// under its bottom face, F = -sum sigma.e_z vol / T, torque about the box centre.
+// Current volume and Cauchy stress follow the inversion policy of
+// Solver.vol() / Solver.cauchy() (core/solver.py:559-598).
+namespace gbmpm {
+
+struct CWArgs {
+    const float *x, *F, *S, *vol0;
+    const int *sel;
+    int n;
+    double c[3], h[3];
+    double layer;        // > 0: given thickness; otherwise 3 mean(vol)^(1/3)
+    int compressive, policy;   // policy 0 warn (|J|), 1 nan, 2 raise
+    double *acc;         // [0..5] force, torque; [6] contacts; [7] sum vol; [8] invalid count
+};
+
+__device__ __forceinline__ void cw_jacobian(const CWArgs &a, int p, double &Jv, double &Jc, bool &bad) {
+    float F[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) F[i] = a.F[9 * (size_t)p + i];
+    const float J = det3(F);
+    bad = !isfinite(J) || J <= 0.0f;
+    if (a.policy == 1) Jv = bad ? (double)NAN : (double)J;
+    else Jv = isfinite(J) ? (double)fabsf(J) : (double)NAN;
+    Jc = (a.policy == 0) ? (Jv < 1e-9 ? 1e-9 : Jv) : Jv;   // NaN stays NaN
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void k_cw_volume(CWArgs a) {
+    double sv = 0.0, nb = 0.0;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+        double Jv, Jc;
+        bool bad;
+        cw_jacobian(a, p, Jv, Jc, bad);
+        sv += (double)a.vol0[p] * Jv;
+        nb += bad ? 1.0 : 0.0;
+    }
+    sv = warp_sum_d(sv);
+    nb = warp_sum_d(nb);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(a.acc + 7, sv);
+        atomicAdd(a.acc + 8, nb);
+    }
+}
+
+__global__ void k_cw_layer(CWArgs a) {
+    const double T = a.layer > 0.0 ? a.layer : 3.0 * cbrt(a.acc[7] / (double)a.n);
+    const double bottom = a.c[2] - a.h[2];
+    double f[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+        const double x0 = a.x[3 * (size_t)p], x1 = a.x[3 * (size_t)p + 1], x2 = a.x[3 * (size_t)p + 2];
+        if (!(fabs(x0 - a.c[0]) < a.h[0] && fabs(x1 - a.c[1]) < a.h[1] && x2 > bottom - T && x2 < bottom + 0.5 * T))
+            continue;
+        double Jv, Jc;
+        bool bad;
+        cw_jacobian(a, p, Jv, Jc, bad);
+        const float *S = a.S + 9 * (size_t)p;
+        const double s02 = (double)S[2] / Jc, s12 = (double)S[5] / Jc, s22 = (double)S[8] / Jc;
+        if (a.compressive && !(s22 < 0.0)) continue;
+        const double w = (double)a.vol0[p] * Jv / T;
+        const double fp[3] = {-s02 * w, -s12 * w, -s22 * w};
+        const double r[3] = {x0 - a.c[0], x1 - a.c[1], x2 - a.c[2]};
+        f[0] += fp[0]; f[1] += fp[1]; f[2] += fp[2];
+        f[3] += r[1] * fp[2] - r[2] * fp[1];
+        f[4] += r[2] * fp[0] - r[0] * fp[2];
+        f[5] += r[0] * fp[1] - r[1] * fp[0];
+        f[6] += 1.0;
+    }
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        const double v = warp_sum_d(f[i]);
+        if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(a.acc + i, v);
+    }
+}
+
+}  // namespace gbmpm
+
+extern "C" int gbmpm_contact_wrench(gbmpm_engine *e, const double box_center[3], const double box_half[3],
+                                    double layer, int32_t compressive_only, int32_t policy, double out[9],
+                                    void *stream) {
+    if (!e || !box_center || !box_half || !out) return fail(GBMPM_ERR_ARG, "null argument");
+    if (!e->bound) return fail(GBMPM_ERR_STATE, "buffers not bound");
+    if (policy < 0 || policy > 2) return fail(GBMPM_ERR_ARG, "policy must be 0 (warn), 1 (nan) or 2 (raise)");
+    cudaStream_t s = (cudaStream_t)stream;
+    GB_CUDA(e->d_tmp.ensure(18));   // nine doubles
+    CWArgs a{};
+    a.x = e->P.x; a.F = e->P.F; a.S = e->P.stress; a.vol0 = e->P.vol; a.sel = e->P.selection; a.n = e->P.n;
+    for (int i = 0; i < 3; ++i) { a.c[i] = box_center[i]; a.h[i] = box_half[i]; }
+    a.layer = layer;
+    a.compressive = compressive_only ? 1 : 0;
+    a.policy = policy;
+    a.acc = reinterpret_cast<double *>(e->d_tmp.ptr);
+    GB_CUDA(cudaMemsetAsync(a.acc, 0, 9 * sizeof(double), s));
+    if (a.n > 0) {
+        const int grid = std::min((a.n + 255) / 256, e->num_sms * 4);
+        k_cw_volume<<<grid, 256, 0, s>>>(a);
+        k_cw_layer<<<grid, 256, 0, s>>>(a);
+        e->launches += 2;
+    }
+    GB_CUDA(cudaMemcpyAsync(out, a.acc, 9 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    if (policy == 2 && out[8] > 0.0)
+        return fail(GBMPM_ERR_STATE, std::to_string((long long)out[8]) +
+                                         " particles have non-finite or non-positive det(F); current volume and "
+                                         "Cauchy stress are undefined for an inverted configuration");
+    return GBMPM_OK;
+}
 
 #include "adjoint.cuh"

@@ -703,6 +703,35 @@ class Solver:
             _abi.check(self._eng.lib.gbmpm_reset_cdf_wrench(self._eng.h, self._stream()), "gbmpm_reset_cdf_wrench")
         return self
 
+    def contact_wrench(self, box_center, box_half, layer_cells: float | None = None, dx: float | None = None,
+                       compressive_only: bool = True) -> dict:
+        """Stress-integral reaction on a box end-effector, computed on the device
+        (box_contact_wrench, coupling/wrench.py:15-46, over x, cauchy() and vol()):
+        {'force', 'torque', 'n_contact', 'Fz'}. Only 9 numbers cross to the host."""
+        self._require_loaded()
+        policy = {"warn": 0, "nan": 1, "raise": 2}[self.inversion_policy]
+        layer = float(layer_cells) * float(dx) if (layer_cells and dx) else 0.0
+        c = (C.c_double * 3)(*[float(v) for v in box_center])
+        h = (C.c_double * 3)(*[float(v) for v in box_half])
+        out = (C.c_double * 9)()
+        rc = self._eng.lib.gbmpm_contact_wrench(self._eng.h, c, h, layer, 1 if compressive_only else 0, policy, out,
+                                                self._stream())
+        if rc == _abi.ERR_STATE and policy == 2:
+            raise RuntimeError(self._eng.lib.gbmpm_last_error().decode())
+        _abi.check(rc, "gbmpm_contact_wrench")
+        if out[8] > 0 and policy == 0 and not getattr(self, "_warned_inverted", False):
+            self._warned_inverted = True
+            warnings.warn(f"{int(out[8])} particles have non-finite or non-positive det(F); current volume and "
+                          f"Cauchy stress are undefined for an inverted configuration; using |det(F)| for "
+                          f"compatibility. Set inversion_policy='raise' to reject or 'nan' to mark these particles.",
+                          RuntimeWarning, stacklevel=2)
+        n_contact = int(out[6])
+        if n_contact < 3:
+            return {"force": np.zeros(3), "torque": np.zeros(3), "n_contact": 0, "Fz": 0.0}
+        force = np.array(out[0:3], dtype=float)
+        return {"force": force, "torque": np.array(out[3:6], dtype=float), "n_contact": n_contact,
+                "Fz": float(force[2])}
+
     def cdf_grids(self):
         """(tag, distance) node grids of the last CPIC stamp as host arrays, and the
         number of stamps so far."""

@@ -127,6 +127,26 @@ _KEYS = ("x", "v", "C", "F", "F_trial", "L", "stress", "mass", "vol", "density",
          "material", "selection", "cov", "init_cov", "cdf_tag")
 
 
+def box_contact_wrench(x, cauchy, vol, box_center, box_half, layer_cells=None, dx=None, compressive_only=True):
+    """Stress-integral reaction on a box (coupling/wrench.py:15-46), restated in numpy."""
+    cx, cy, cz = box_center
+    hx, hy, hz = box_half
+    h = float(np.mean(vol) ** (1.0 / 3.0))
+    T = (layer_cells * dx) if (layer_cells and dx) else 3.0 * h
+    bottom = cz - hz
+    under = (np.abs(x[:, 0] - cx) < hx) & (np.abs(x[:, 1] - cy) < hy)
+    contact = under & (x[:, 2] > bottom - T) & (x[:, 2] < bottom + 0.5 * T)
+    if compressive_only:
+        contact &= cauchy[:, 2, 2] < 0.0
+    if contact.sum() < 3:
+        return {"force": np.zeros(3), "torque": np.zeros(3), "n_contact": 0, "Fz": 0.0}
+    f_per = -cauchy[contact][:, :, 2] * (vol[contact, None] / T)
+    force = f_per.sum(0)
+    r = x[contact] - np.array(box_center)
+    torque = np.cross(r, f_per).sum(0)
+    return {"force": force, "torque": torque, "n_contact": int(contact.sum()), "Fz": float(force[2])}
+
+
 class OracleSolver:
     """numpy twin of mpm_engine_gb300.Solver's host side, stepping the C++ oracle."""
 
