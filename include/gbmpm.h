@@ -221,6 +221,14 @@ int gbmpm_reset_cdf_wrench(gbmpm_engine *e, void *stream);
  * entries (either may be NULL), and the number of stamps so far (_cdf_stamp_count). */
 int gbmpm_cdf_grids(gbmpm_engine *e, int32_t *tag_out, float *d_out, int64_t *stamps, void *stream);
 
+/* Current volume vol0 * J, Cauchy stress = stress / J and J = det(F) per particle
+ * (Solver.vol / Solver.cauchy, core/solver.py:559-598) into caller device buffers
+ * (any may be NULL). policy 0 warn: |J| (Cauchy divides by max(|J|, 1e-9));
+ * 1 nan and 2 raise: NaN for inverted particles. *n_inverted (host, may be NULL:
+ * then nothing synchronizes) receives the count of non-finite or non-positive J. */
+int gbmpm_compute_cauchy(gbmpm_engine *e, float *cauchy_out, float *vol_out, float *J_out, int32_t policy,
+                         int32_t *n_inverted, void *stream);
+
 /* Stress-integral reaction on a kinematic box (box_contact_wrench,
  * coupling/wrench.py:15-46) over the bound particles: out = {fx, fy, fz, tx, ty, tz,
  * contacts, sum of current volume, inverted particles}. layer <= 0 takes

@@ -127,6 +127,8 @@ _SIGNATURES = {
     "gbmpm_cdf_wrench": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_void_p]),
     "gbmpm_reset_cdf_wrench": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gbmpm_cdf_grids": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64), C.c_void_p]),
+    "gbmpm_compute_cauchy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                       C.POINTER(C.c_int32), C.c_void_p]),
     "gbmpm_contact_wrench": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double,
                                        C.c_int32, C.c_int32, C.POINTER(C.c_double), C.c_void_p]),
     "gbmpm_adjoint_segment": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_double, C.c_int32,

@@ -3390,6 +3390,51 @@ __global__ void k_cw_layer(CWArgs a) {
 
 }  // namespace gbmpm
 
+namespace gbmpm {
+// Current volume, Cauchy stress and det(F) per particle (Solver.vol / cauchy,
+// core/solver.py:559-598): policy 0 warn (|J|, Cauchy divides by max(|J|, 1e-9)),
+// 1 nan and 2 raise (NaN for inverted particles); counts the inverted ones.
+__global__ void k_export_cauchy(const float *F, const float *S, const float *vol0, int n, int policy, float *cauchy,
+                                float *vol, float *Jout, int *bad_count) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float Fp[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Fp[i] = F[9 * (size_t)p + i];
+    const float J = det3(Fp);
+    const bool bad = !isfinite(J) || J <= 0.0f;
+    if (bad) atomicAdd(bad_count, 1);
+    float Jv = (policy == 0) ? (isfinite(J) ? fabsf(J) : NAN) : (bad ? NAN : J);
+    float Jc = (policy == 0 && Jv < 1e-9f) ? 1e-9f : Jv;
+    if (Jout) Jout[p] = J;
+    if (vol) vol[p] = vol0[p] * Jv;
+    if (cauchy) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) cauchy[9 * (size_t)p + i] = S[9 * (size_t)p + i] / Jc;
+    }
+}
+}  // namespace gbmpm
+
+extern "C" int gbmpm_compute_cauchy(gbmpm_engine *e, float *cauchy_out, float *vol_out, float *J_out, int32_t policy,
+                                    int32_t *n_inverted, void *stream) {
+    if (!e) return fail(GBMPM_ERR_ARG, "null engine");
+    if (!e->bound) return fail(GBMPM_ERR_STATE, "buffers not bound");
+    if (policy < 0 || policy > 2) return fail(GBMPM_ERR_ARG, "policy must be 0 (warn), 1 (nan) or 2 (raise)");
+    cudaStream_t s = (cudaStream_t)stream;
+    GB_CUDA(e->d_flagbuf.ensure(1));
+    GB_CUDA(cudaMemsetAsync(e->d_flagbuf.ptr, 0, sizeof(int), s));
+    if (e->P.n > 0) {
+        k_export_cauchy<<<(e->P.n + 255) / 256, 256, 0, s>>>(e->P.F, e->P.stress, e->P.vol, e->P.n, policy, cauchy_out,
+                                                             vol_out, J_out, e->d_flagbuf.ptr);
+        e->launches++;
+    }
+    if (n_inverted) {
+        GB_CUDA(cudaMemcpyAsync(n_inverted, e->d_flagbuf.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+        GB_CUDA(cudaStreamSynchronize(s));
+    }
+    return GBMPM_OK;
+}
+
 extern "C" int gbmpm_contact_wrench(gbmpm_engine *e, const double box_center[3], const double box_half[3],
                                     double layer, int32_t compressive_only, int32_t policy, double out[9],
                                     void *stream) {

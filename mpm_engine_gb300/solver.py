@@ -978,15 +978,46 @@ class Solver:
         J[bad] = np.nan
         return J
 
+    def _device_exports(self, cauchy: bool, vol: bool):
+        """Cauchy stress and current volume computed on the device under the
+        inversion policy; raises or warns as _checked_jacobian does."""
+        if self.inversion_policy not in {"warn", "raise", "nan"}:
+            raise ValueError("inversion_policy must be 'warn', 'raise', or 'nan'")
+        torch = _torch()
+        n = self._n
+        dev = self._t["x"].device
+        c = torch.empty(n, 3, 3, device=dev, dtype=torch.float32) if cauchy else None
+        v = torch.empty(n, device=dev, dtype=torch.float32) if vol else None
+        bad = C.c_int32(0)
+        policy = {"warn": 0, "nan": 1, "raise": 2}[self.inversion_policy]
+        _abi.check(self._eng.lib.gbmpm_compute_cauchy(self._eng.h, None if c is None else c.data_ptr(),
+                                                      None if v is None else v.data_ptr(), None, policy,
+                                                      C.byref(bad), self._stream()), "gbmpm_compute_cauchy")
+        if bad.value:
+            message = (f"{bad.value} particles have non-finite or non-positive det(F); current volume "
+                       "and Cauchy stress are undefined for an inverted configuration")
+            if self.inversion_policy == "raise":
+                raise RuntimeError(message)
+            if self.inversion_policy == "warn" and not getattr(self, "_warned_inverted", False):
+                self._warned_inverted = True
+                warnings.warn(f"{message}; using |det(F)| for compatibility. Set inversion_policy='raise' to "
+                              "reject or 'nan' to mark these particles.", RuntimeWarning, stacklevel=3)
+        return c, v
+
+    def vol_torch(self):
+        """Current volume vol0 * det(F) as a device tensor (inversion policy applied)."""
+        return self._device_exports(False, True)[1]
+
+    def cauchy_torch(self):
+        """Cauchy stress = Kirchhoff / det(F) as a device tensor (inversion policy applied)."""
+        return self._device_exports(True, False)[0]
+
     def vol(self) -> np.ndarray:
-        return self._vol0 * self._checked_jacobian()
+        return self.vol_torch().cpu().numpy()
 
     def cauchy(self) -> np.ndarray:
         """Cauchy stress = Kirchhoff / det(F) under the inversion policy."""
-        J = self._checked_jacobian()
-        if self.inversion_policy == "warn":
-            J = np.clip(J, 1e-9, None)
-        return self.stress() / J[:, None, None]
+        return self.cauchy_torch().cpu().numpy()
 
     def _cov_tensor(self):
         if self._t.get("cov") is None:

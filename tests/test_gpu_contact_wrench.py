@@ -64,3 +64,26 @@ def test_contact_wrench_inversion_policy(cuda):
     s.inversion_policy = "warn"
     with pytest.warns(RuntimeWarning, match="inverted"):
         s.contact_wrench(center, half)
+
+
+def test_device_cauchy_and_volume_match_reference_formula(cuda):
+    """Solver.cauchy()/vol() now computed on the device (core/solver.py:559-598)."""
+    from mpm_engine_gb300 import Solver
+    s, center, half, dx = _press(Solver)
+    s.step(2e-5, 50)
+    F, S = s.F().astype(np.float64), s.stress().astype(np.float64)
+    J = np.linalg.det(F)
+    want_c = S / np.clip(np.abs(J), 1e-9, None)[:, None, None]
+    want_v = s._vol0.astype(np.float64) * np.abs(J)
+    got_c, got_v = s.cauchy(), s.vol()
+    assert np.abs(got_c - want_c).max() <= 1e-5 * np.abs(want_c).max()
+    np.testing.assert_allclose(got_v, want_v, rtol=1e-5)
+    F32 = s.F()
+    F32[3] = -np.eye(3, dtype=np.float32)
+    s._t["F"].copy_(__import__("torch").from_numpy(F32))
+    s.inversion_policy = "nan"
+    v = s.vol()
+    assert np.isnan(v[3]) and np.isfinite(np.delete(v, 3)).all()
+    s.inversion_policy = "raise"
+    with pytest.raises(RuntimeError, match="non-positive det"):
+        s.cauchy()
