@@ -1994,7 +1994,9 @@ struct gbmpm_engine {
     gbmpm_model M{};
     bool bound = false, modeled = false;
     std::vector<gbmpm_collider> cols;
-    std::vector<ColDev> h_cols;   // the descriptor table last uploaded to d_cols
+    std::vector<ColDev> h_cols;   // the collider descriptor table (device copy: d_cols)
+    ColDev *h_coldev = nullptr;   // pinned staging for its stream-ordered upload
+    bool cols_upload = false;     // h_cols changed since the last upload
     // device scratch
     DevBuf<MatTables> d_tab;
     DevBuf<ColDev> d_cols;
@@ -2024,6 +2026,7 @@ struct gbmpm_engine {
     int bd = 0;
     int num_sms = 148;
     int tile_occ = 3;       // resident CTAs per SM the tiled particle kernel is compiled for
+    int grid_ctas = 2;      // grid-update CTAs per SM
     // graph cache
     cudaGraphExec_t graph = nullptr;
     int g_substeps = -1, g_flags = -1;
@@ -2201,7 +2204,9 @@ void launch_grid(gbmpm_engine *e, float dt, int substep, int list, cudaStream_t 
     g.blk_count_read = e->d_count.ptr + list;
     g.blk_count_reset = e->d_count.ptr + (list ^ 1);
     g.bd = e->bd;
-    int grid = e->num_sms * 8;
+    // one wave of CTAs looping over the active blocks: the per-CTA setup (collider
+    // tables into shared memory, two barriers) is paid once per SM slot, not per item
+    int grid = e->num_sms * e->grid_ctas;
     k_grid<<<grid, kGridThreads, 0, s>>>(g);
     e->launches++;
 }
@@ -2551,6 +2556,7 @@ int gbmpm_engine_create(gbmpm_engine **out) {
     if (cudaGetDevice(&e->device) != cudaSuccess) { delete e; return fail(GBMPM_ERR_CUDA, "no CUDA device"); }
     cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, e->device);
     if (const char *occ = std::getenv("GBMPM_TILE_OCC")) e->tile_occ = std::atoi(occ);
+    if (const char *gc = std::getenv("GBMPM_GRID_CTAS")) e->grid_ctas = std::max(1, std::min(8, std::atoi(gc)));
     if (cudaEventCreateWithFlags(&e->pose_done, cudaEventDisableTiming) != cudaSuccess) {
         delete e;
         return fail(GBMPM_ERR_CUDA, "event create failed");
@@ -2565,6 +2571,7 @@ void gbmpm_engine_destroy(gbmpm_engine *e) {
     if (e->graph) cudaGraphExecDestroy(e->graph);
     if (e->pose_done) cudaEventDestroy(e->pose_done);
     if (e->h_pose) cudaFreeHost(e->h_pose);
+    if (e->h_coldev) cudaFreeHost(e->h_coldev);
     e->d_tab.release(); e->d_cols.release(); e->d_pose.release(); e->d_wrench.release();
     e->d_flag.release(); e->d_list.release(); e->d_count.release(); e->d_status.release();
     e->d_guard.release(); e->d_keys[0].release(); e->d_keys[1].release(); e->d_skeys.release(); e->d_kminmax.release(); e->d_idx[0].release();
@@ -2640,14 +2647,14 @@ int gbmpm_set_colliders(gbmpm_engine *e, const gbmpm_collider *c, int32_t n) {
     e->cols.assign(c, c + n);
     std::vector<ColDev> d(std::max(1, n));
     for (int i = 0; i < n; ++i) d[i] = to_dev(c[i]);
-    // descriptors hold no pose, so a pose-only update leaves the device table as it
-    // is (kernels of earlier ticks may still be reading it)
-    bool same = e->h_cols.size() == d.size() && e->d_cols.ptr &&
-                std::memcmp(e->h_cols.data(), d.data(), d.size() * sizeof(ColDev)) == 0;
-    if (!same) {
-        GB_CUDA(e->d_cols.ensure(d.size()));
-        GB_CUDA(cudaMemcpy(e->d_cols.ptr, d.data(), d.size() * sizeof(ColDev), cudaMemcpyHostToDevice));
+    // The device table (fixed capacity, so its address never changes) is refreshed
+    // on the stream of the next tick; a captured tick graph reads it at run time, so
+    // only a change of the collider count needs a new capture.
+    if (!e->h_coldev) GB_CUDA(cudaMallocHost(&e->h_coldev, kMaxCol * sizeof(ColDev)));
+    GB_CUDA(e->d_cols.ensure(kMaxCol));
+    if (e->h_cols.size() != d.size() || std::memcmp(e->h_cols.data(), d.data(), d.size() * sizeof(ColDev)) != 0) {
         e->h_cols = d;
+        e->cols_upload = true;
     }
     if (e->d_wrench.n < (size_t)kMaxCol * 6) {
         std::vector<double> keep(e->d_wrench.n);
@@ -2660,7 +2667,7 @@ int gbmpm_set_colliders(gbmpm_engine *e, const gbmpm_collider *c, int32_t n) {
     }
     if ((size_t)n > old)
         GB_CUDA(cudaMemset(e->d_wrench.ptr + old * 6, 0, (n - old) * 6 * sizeof(double)));
-    mark_dirty(e);
+    if ((size_t)n != old) mark_dirty(e);
     return GBMPM_OK;
 }
 
@@ -2791,6 +2798,12 @@ int prepare_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int
     GB_CUDA(e->d_pose.ensure(need));
     if (e->d_pose.ptr != old_dev) mark_dirty(e);
     GB_CUDA(cudaEventSynchronize(e->pose_done));
+    if (e->cols_upload) {   // the staging buffer is free once the previous upload is done
+        std::memcpy(e->h_coldev, e->h_cols.data(), e->h_cols.size() * sizeof(ColDev));
+        GB_CUDA(cudaMemcpyAsync(e->d_cols.ptr, e->h_coldev, e->h_cols.size() * sizeof(ColDev),
+                                cudaMemcpyHostToDevice, s));
+        e->cols_upload = false;
+    }
     build_pose_table(e, *time, dt, substeps);
     GB_CUDA(cudaMemcpyAsync(e->d_pose.ptr, e->h_pose, need * sizeof(PoseRec), cudaMemcpyHostToDevice, s));
     GB_CUDA(cudaEventRecord(e->pose_done, s));
