@@ -1128,7 +1128,7 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
         float4 *dst = reinterpret_cast<float4 *>(s_mem + t * kRec);
 #pragma unroll
         for (int q = 0; q < kRec / 4; ++q) dst[q] = make_float4(rec[4 * q], rec[4 * q + 1], rec[4 * q + 2], rec[4 * q + 3]);
-        s_key[t] = (s.b[0] * k.ng + s.b[1]) * k.ng + s.b[2];
+        s_key[t] = (s.b[0] << 20) | (s.b[1] << 10) | s.b[2];   // n_grid <= 1024 on this path
     } else {
         s_key[t] = -1 - t;   // a dead slot forms its own, skipped run
     }
@@ -1160,6 +1160,7 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
 #pragma unroll
         for (int kk = 0; kk < 3; ++kk) acc[kk][0] = acc[kk][1] = acc[kk][2] = acc[kk][3] = 0.f;
         if (lane < 27) {
+#pragma unroll 2
             for (int q = q0 + g3; q < q1; q += 3) {
                 const float *r = s_mem + q * kRec;
                 const float wxi = r[li], wyj = r[3 + lj], dwxi = r[6 + li], dwyj = r[9 + lj];
@@ -1203,15 +1204,19 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
                 acc[kk][c] += x9 + x18;
             }
         if (lane < 9) {
-            const int bz = key % k.ng, rr = key / k.ng, by = rr % k.ng, bx = rr / k.ng;
+            const int bx = key >> 20, by = (key >> 10) & 1023, bz = key & 1023;
             const int gx = bx + li, gy = by + lj;
+            int marked = -1;   // 4^3 block (z index) this lane marked last
 #pragma unroll
             for (int kk = 0; kk < 3; ++kk) {
                 if (acc[kk][0] != 0.f || acc[kk][1] != 0.f || acc[kk][2] != 0.f || acc[kk][3] != 0.f) {
                     const int gz = bz + kk;
                     atomicAdd(k.gmv + ((size_t)gx * k.ng + gy) * k.ng + gz,
                               make_float4(acc[kk][0], acc[kk][1], acc[kk][2], acc[kk][3]));
-                    mark_block(k, gx >> 2, gy >> 2, gz >> 2);
+                    if ((gz >> 2) != marked) {
+                        mark_block(k, gx >> 2, gy >> 2, gz >> 2);
+                        marked = gz >> 2;
+                    }
                 }
             }
         }
@@ -2807,7 +2812,7 @@ int prepare_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int
     build_pose_table(e, *time, dt, substeps);
     GB_CUDA(cudaMemcpyAsync(e->d_pose.ptr, e->h_pose, need * sizeof(PoseRec), cudaMemcpyHostToDevice, s));
     GB_CUDA(cudaEventRecord(e->pose_done, s));
-    reorder = (flags & GBMPM_TICK_REORDER) && !e->M.periodic_x && e->P.n > 0;
+    reorder = (flags & GBMPM_TICK_REORDER) && !e->M.periodic_x && e->P.n > 0 && e->G.n_grid <= 1024;
     if (reorder && e->ws_n != e->P.n) {
         GB_CUDA(ensure_ws(e));
         mark_dirty(e);
