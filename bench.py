@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["pour", "pour_hb", "dam"], default="pour")
+    ap.add_argument("--workload", choices=["pour", "pour_hb", "pour_cdf", "dam"], default="pour")
     ap.add_argument("--n-grid", type=int, default=192)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-cdf", action="store_true")
     return ap.parse_args()
 
 
@@ -117,19 +118,24 @@ def build_workload(name: str, n_grid: int, solver_cls, **kw):
     """Returns (solver, frame(i) callable, particles, substeps per step, description)."""
     from mpm_engine_gb300 import newtonian
     from mpm_engine_gb300.scenes import dam_break_lattice, pour_scene
-    if name in ("pour", "pour_hb"):
+    if name in ("pour", "pour_hb", "pour_cdf"):
         mat = None
         if name == "pour_hb":
             mat = newtonian(eta=0.0, density=1400.0, bulk_modulus=9.0e5).with_yield(50.0).with_powerlaw(K=20.0, n=0.6)
-        s, src, rcv, traj, S, dt = pour_scene(solver_cls, n_grid=n_grid, material=mat, **kw)
+        glass = "cdf" if name == "pour_cdf" else "cup"
+        s, src, rcv, traj, S, dt = pour_scene(solver_cls, n_grid=n_grid, material=mat, glass=glass, **kw)
 
         def frame(i, s=s):
             t = i / 60.0
             c, q, v, w = traj.command(t, 1.0 / 60.0)
-            s.set_cup(src, center=c, quat=q, velocity=v, omega=w)
+            if glass == "cdf":
+                s.set_cdf_pose(src, center=c, quat=(q[1], q[2], q[3], q[0]), velocity=v, omega=w)
+            else:
+                s.set_cup(src, center=c, quat=q, velocity=v, omega=w)
             s.step(dt, S)
 
-        desc = {"workload": f"pour_{'honey' if name == 'pour' else 'herschel_bulkley'}_{n_grid}^3",
+        label = {"pour": "honey", "pour_hb": "herschel_bulkley", "pour_cdf": "honey_cdf_glasses"}[name]
+        desc = {"workload": f"pour_{label}_{n_grid}^3",
                 "particles": s.n_particles, "substeps_per_step": S, "dt": dt, "grid_lim": 0.7}
         return s, frame, s.n_particles, S, desc
     if name == "dam":
@@ -192,6 +198,27 @@ def batched_measure(n_scenes: int, ticks: int, substeps: int = 100, dt: float = 
             "scenes": n_scenes, "particles_total": n_part, "ticks": ticks, "dt": dt,
             "particle_substeps_per_s": n_part * substeps * ticks / t_batch,
             "gpu_launches": batch.launch_count() - launches0}
+
+
+def cdf_pour_measure(n_grid: int = 192, frames: int = 3, warmup: int = 2, device: str = "cuda:0"):
+    """The pour with both glasses as CPIC (CDF) sheets, the reference's costly case:
+    ms per 1/60 s frame (live ticks; the source glass restamps every substep)."""
+    import torch
+    from mpm_engine_gb300 import Solver
+    s, frame, n, S, desc = build_workload("pour_cdf", n_grid, Solver, device=device)
+    for i in range(warmup):
+        frame(i)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for i in range(frames):
+        frame(warmup + i)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / frames
+    return {"workload": desc["workload"], "particles": n, "substeps_per_frame": S, "ms_per_frame": ms,
+            "particle_substeps_per_s": n * S / (ms / 1e3), "frames": frames,
+            "cdf_stamps": s.cdf_grids()[2]}
 
 
 def adjoint_measure(n_scenes: int = 32, n_particles: int = 50_000, n_grid: int = 48, substeps: int = 400,
@@ -420,6 +447,10 @@ def main():
     if not args.no_batched:
         batched = batched_measure(args.batch_scenes, ticks=max(2, min(args.steps, 4)), device=f"cuda:{local}")
 
+    cdf = None
+    if not args.no_cdf and args.workload == "pour":
+        cdf = cdf_pour_measure(args.n_grid, device=f"cuda:{local}")
+
     adj = None
     if not args.no_adjoint:
         adj = adjoint_measure(device=f"cuda:{local}")
@@ -435,7 +466,7 @@ def main():
                 "config": {**desc, "l2": "256 MB buffer written between timed steps", "parallelism":
                            "replicas" if world > 1 else "single"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk, "batched": batched, "batched_adjoint": adj}
+                "clocks": clk, "batched": batched, "batched_adjoint": adj, "pour_cdf": cdf}
         print(json.dumps(line))
     if dist:
         dist.barrier()

@@ -90,6 +90,44 @@ def sheet_cdf(normal: str = "z", size: float = 0.5, res: int = 64, band_cells: f
     return CDFData(values=side * dist, valid=valid, origin=origin, cell=float(cell), band=float(band))
 
 
+def revolved_open_cdf(profile_rz, res: int = 96, band_cells: float = 3.0, margin_cells: float = 4.0) -> CDFData:
+    """CDF of the open surface of revolution of an (r, z) polyline about the z axis,
+    on the grid build_surface_cdf uses for its revolved mesh (mesh_sdf.py:412-480):
+    exact distance to the surface (the distance in the meridian plane), side from
+    the normal of the nearest segment (the tangent turned +90 degrees in (r, z), so
+    a profile traced floor-then-wall gives +1 inside the cavity), valid within
+    `band` of the surface and farther than `band` from the open rim (the last
+    polyline vertex; the first lies on the axis)."""
+    P = np.asarray(profile_rz, dtype=np.float64)
+    rmax = float(P[:, 0].max())
+    zmin, zmax = float(P[:, 1].min()), float(P[:, 1].max())
+    span = max(2.0 * rmax, zmax - zmin)
+    cell = span / (res - 1 - 2 * margin_cells)
+    band = band_cells * cell
+    L = cell * (res - 1)
+    center = np.array([0.0, 0.0, 0.5 * (zmin + zmax)])
+    origin = center - 0.5 * L
+    ax = [origin[d] + cell * np.arange(res) for d in range(3)]
+    X, Y, Z = np.meshgrid(ax[0], ax[1], ax[2], indexing="ij")
+    R = np.sqrt(X * X + Y * Y)
+    best = np.full(R.shape, np.inf)
+    side = np.ones(R.shape)
+    for a, b in zip(P[:-1], P[1:]):
+        t = b - a
+        tl2 = float(t @ t)
+        u = np.clip(((R - a[0]) * t[0] + (Z - a[1]) * t[1]) / tl2, 0.0, 1.0)
+        cr, cz = a[0] + u * t[0], a[1] + u * t[1]
+        d = np.sqrt((R - cr) ** 2 + (Z - cz) ** 2)
+        n = np.array([-t[1], t[0]]) / np.sqrt(tl2)
+        s_seg = np.where((R - cr) * n[0] + (Z - cz) * n[1] >= 0.0, 1.0, -1.0)
+        closer = d < best
+        best = np.where(closer, d, best)
+        side = np.where(closer, s_seg, side)
+    rim = np.sqrt((R - P[-1, 0]) ** 2 + (Z - P[-1, 1]) ** 2)
+    valid = ((best <= band) & (rim > band)).astype(np.float64)
+    return CDFData(values=side * best, valid=valid, origin=origin, cell=float(cell), band=float(band))
+
+
 def save_sdf(sdf: SDFData, path) -> None:
     path = Path(path)
     path.parent.mkdir(parents=True, exist_ok=True)
@@ -124,4 +162,5 @@ def analytic_sdf(kind: str, res: int = 48, half_extent=(0.05, 0.05, 0.05), radiu
     return SDFData(values=vals, grads=grads, origin=origin, cell=float(cell), sdf_max=float(vals.max()))
 
 
-__all__ = ["CDFData", "SDFData", "analytic_sdf", "load_cdf", "load_sdf", "save_cdf", "save_sdf", "sheet_cdf"]
+__all__ = ["CDFData", "SDFData", "analytic_sdf", "load_cdf", "load_sdf", "revolved_open_cdf", "save_cdf", "save_sdf",
+           "sheet_cdf"]

@@ -148,3 +148,23 @@ def cup_fill(profile: GlassProfile, h: float, fill_fraction: float = 0.80, clear
 
 __all__ = ["GlassProfile", "angular_velocity_between", "cup_fill", "glass_sdf_local", "quat_from_axis_angle", "quat_mul", "quat_to_mat",
            "world_to_local"]
+
+
+def glass_cavity_profile(profile: GlassProfile | None = None) -> np.ndarray:
+    """Open (r, z) polyline of the glass cavity surface, floor disk then inner wall
+    up to the rim (glass_cavity_profile, colliders/glass.py:162-183): the CPIC sheet
+    traces the cavity so CDF and SDF contact geometry coincide."""
+    p = GlassProfile() if profile is None else profile
+    return np.array([(0.0, p.inner_floor_z), (p.inner_radius, p.inner_floor_z), (p.inner_radius, p.rim_z)])
+
+
+def glass_cdf(dx: float, profile: GlassProfile | None = None, res: int = 96):
+    """The glass as a CDF collider field, with a built band wide enough for a runtime
+    band of 2 dx (examples/pour_franka.py:249-262)."""
+    from .geometry import revolved_open_cdf
+    prof = glass_cavity_profile(profile)
+    span = max(2.0 * float(prof[:, 0].max()), float(prof[:, 1].max() - prof[:, 1].min()))
+    cell = span / (res - 1 - 8)
+    band_cells = max(3.0, float(np.ceil(2.2 * dx / cell)))
+    return revolved_open_cdf(prof, res=res, band_cells=band_cells)
+

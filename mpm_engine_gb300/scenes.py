@@ -81,12 +81,14 @@ class PourTrajectory:
         return POUR_SOURCE, q0, (0.0, 0.0, 0.0), angular_velocity_between(q0, q1, dt_tick)
 
 
-def pour_scene(solver_cls, n_grid: int = 192, material=None, **solver_kw):
+def pour_scene(solver_cls, n_grid: int = 192, material=None, glass: str = "cup", **solver_kw):
     """The reference pour geometry: default GlassProfile filled to 80 % with cup_fill at
     h = dx/2 (340,489 particles at 192^3, grid_lim 0.7), a separable floor (mu 0.3),
-    domain walls, a source and a receiver glass (friction 0.05). Returns
-    (solver, source handle, receiver handle, trajectory, substeps per 1/60 s frame, dt)."""
-    from .glass import GlassProfile, cup_fill
+    domain walls, a source and a receiver glass (friction 0.05), as revolved-SDF cups
+    or, with glass="cdf", as CPIC sheets of the cavity (examples/pour_franka.py:266-291).
+    Returns (solver, source handle, receiver handle, trajectory, substeps per 1/60 s
+    frame, dt)."""
+    from .glass import GlassProfile, cup_fill, glass_cdf
     from .solver import GridConfig
     prof = GlassProfile()
     grid = GridConfig(n_grid=n_grid, grid_lim=POUR_GRID_LIM)
@@ -97,8 +99,14 @@ def pour_scene(solver_cls, n_grid: int = 192, material=None, **solver_kw):
     s.add_plane((0, 0, POUR_FLOOR_Z), (0, 0, 1), "separate", friction=0.3)
     s.add_domain_walls()
     traj = PourTrajectory()
-    src = s.add_cup(prof, POUR_SOURCE, tuple(traj.quat(0.0)), friction=0.05)
-    rcv = s.add_cup(prof, POUR_RECEIVER, (1.0, 0.0, 0.0, 0.0), friction=0.05)
+    if glass == "cdf":
+        cdf = glass_cdf(grid.dx, prof)
+        q = traj.quat(0.0)
+        src = s.add_cdf_collider(cdf, POUR_SOURCE, quat=(q[1], q[2], q[3], q[0]), friction=0.05)
+        rcv = s.add_cdf_collider(cdf, POUR_RECEIVER, friction=0.05)
+    else:
+        src = s.add_cup(prof, POUR_SOURCE, tuple(traj.quat(0.0)), friction=0.05)
+        rcv = s.add_cup(prof, POUR_RECEIVER, (1.0, 0.0, 0.0, 0.0), friction=0.05)
     substeps = pour_substeps(HONEY, grid.dx)
     return s, src, rcv, traj, substeps, (1.0 / 60.0) / substeps
 
