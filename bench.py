@@ -200,9 +200,10 @@ def batched_measure(n_scenes: int, ticks: int, substeps: int = 100, dt: float = 
             "gpu_launches": batch.launch_count() - launches0}
 
 
-def cdf_pour_measure(n_grid: int = 192, frames: int = 3, warmup: int = 2, device: str = "cuda:0"):
+def cdf_pour_measure(n_grid: int = 192, frames: int = 4, warmup: int = 24, device: str = "cuda:0"):
     """The pour with both glasses as CPIC (CDF) sheets, the reference's costly case:
-    ms per 1/60 s frame (live ticks; the source glass restamps every substep)."""
+    ms per 1/60 s frame, timed mid-tilt (from t = 0.4 s), where the source glass
+    restamps every substep (live ticks)."""
     import torch
     from mpm_engine_gb300 import Solver
     s, frame, n, S, desc = build_workload("pour_cdf", n_grid, Solver, device=device)

@@ -179,10 +179,12 @@ def test_cdf_pour_holds_and_matches_oracle(cuda, oracle_lib):
     from mpm_engine_gb300.glass import GlassProfile
     from mpm_engine_gb300.scenes import POUR_SOURCE, pour_scene
     s, src, rcv, traj, S, dt = pour_scene(Solver, n_grid=96, glass="cdf")
-    c, q, v, w = traj.command(0.5, 1.0 / 60.0)
-    s.set_cdf_pose(src, center=c, quat=(q[1], q[2], q[3], q[0]), velocity=v, omega=w)
     o = oracle_lib.OracleSolver.from_state(s.export_state(), 96, 0.7)
     o.threads = 16
+    # the same pose command on both sides, so their lane bookkeeping stays identical
+    c, q, v, w = traj.command(0.5, 1.0 / 60.0)
+    for solver in (s, o):
+        solver.set_cdf_pose(src, center=c, quat=(q[1], q[2], q[3], q[0]), velocity=v, omega=w)
     k = 0
     for _ in range(2):
         s.step(dt, 10)
