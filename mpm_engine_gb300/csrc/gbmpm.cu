@@ -87,7 +87,7 @@ struct PK {
     const int *ctag, *ctag_prev, *cblock;
     const float *cd, *cd_prev;
     int *ptag;
-    double *cwrench;   // [4][6] blocked-deposit reaction
+    double *cwrench;   // [CTA][4][6] per-CTA partial sums of the blocked-deposit reaction
     float grav[3];
     CdfLanes lanes;
 };
@@ -693,32 +693,65 @@ __device__ __forceinline__ bool cdf_near(const PK &k, const Stencil &s) {
     return false;
 }
 
-// cdf_particle_tag: per lane, the particle is valid when any stencil node is, and
-// its side is the sign of the weighted signed distance of the valid nodes.
-__device__ int cdf_vote(const PK &k, const Stencil &s, bool prev) {
-    const int *T = prev ? k.ctag_prev : k.ctag;
-    const float *D = prev ? k.cd_prev : k.cd;
-    float votes[4] = {0.f, 0.f, 0.f, 0.f};
-    int seen = 0;
+// One pass over the 27 stencil nodes of a stamp: caches the node tags (node index
+// (i*3 + j)*3 + kk) and forms cdf_particle_tag's lane votes, the weighted signed
+// distances of the valid nodes (mpm_utils.py:678-713); with `ghost`, it also forms
+// the owner-lane sums of cdf_particle_ghost (:733-771) in the same node order.
+struct CdfScan {
+    int tag[27];
+    float votes[4];
+    int seen;
+    float d_hat, n_acc[3], best_w;
+    int lane_p;
+};
+
+template <bool GHOST>
+__device__ __forceinline__ void cdf_scan(const PK &k, const Stencil &s, const int *T, const float *D, CdfScan &c) {
+    c.votes[0] = c.votes[1] = c.votes[2] = c.votes[3] = 0.f;
+    c.seen = 0;
+    c.d_hat = 0.f;
+    c.n_acc[0] = c.n_acc[1] = c.n_acc[2] = 0.f;
+    c.best_w = 0.f;
+    c.lane_p = 0;
+#pragma unroll
     for (int i = 0; i < 3; ++i)
+#pragma unroll
         for (int j = 0; j < 3; ++j)
+#pragma unroll
             for (int kk = 0; kk < 3; ++kk) {
-                size_t id = node_id(k, s, i, j, kk);
-                int t = T[id];
+                const size_t id = node_id(k, s, i, j, kk);
+                const int t = T[id];
+                c.tag[(i * 3 + j) * 3 + kk] = t;
                 if (t == 0) continue;
-                float w = s.w[0][i] * s.w[1][j] * s.w[2][kk];
-                float dd = D[id];
+                const float w = s.w[0][i] * s.w[1][j] * s.w[2][kk];
+                const float dd = D[id];
 #pragma unroll
                 for (int l = 0; l < 4; ++l)
                     if ((t >> (2 * l)) & 1) {
-                        seen |= 1 << (2 * l);
-                        votes[l] += w * dd * (((t >> (2 * l + 1)) & 1) ? 1.0f : -1.0f);
+                        c.seen |= 1 << (2 * l);
+                        c.votes[l] += w * dd * (((t >> (2 * l + 1)) & 1) ? 1.0f : -1.0f);
                     }
+                if (GHOST) {
+                    const int own = (t >> kCdfOwnerShift) & 3;
+                    if (((t >> (2 * own)) & 1) == 0) continue;
+                    const float sgn = ((t >> (2 * own + 1)) & 1) ? 1.0f : -1.0f;
+                    c.d_hat += w * sgn * dd;
+                    const float dw[3] = {s.dw[0][i] * s.w[1][j] * s.w[2][kk], s.w[0][i] * s.dw[1][j] * s.w[2][kk],
+                                         s.w[0][i] * s.w[1][j] * s.dw[2][kk]};
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) c.n_acc[a] += dw[a] * k.inv_dx * sgn * dd;
+                    if (w > c.best_w) { c.best_w = w; c.lane_p = own; }
+                }
             }
+}
+
+// the particle tag from the votes: valid per lane where a valid node was seen, side
+// from the sign of the vote
+__device__ __forceinline__ int cdf_vote_tag(const CdfScan &c) {
     int pc = 0;
 #pragma unroll
     for (int l = 0; l < 4; ++l)
-        if ((seen >> (2 * l)) & 1) pc |= (1 << (2 * l)) | ((votes[l] >= 0.0f ? 1 : 0) << (2 * l + 1));
+        if ((c.seen >> (2 * l)) & 1) pc |= (1 << (2 * l)) | ((c.votes[l] >= 0.0f ? 1 : 0) << (2 * l + 1));
     return pc;
 }
 
@@ -734,44 +767,25 @@ __device__ __forceinline__ int cdf_persist(int old, int fresh) {
     return pc;
 }
 
-// cdf_particle_ghost: the velocity the particle reads from nodes across the
-// surface. Surface normal and distance come from the owner-lane distance field
-// at the previous stamp; the tangential part follows the surface type (sticky,
-// slip, separable Coulomb with a capped impulse) plus a separation push when the
+// cdf_particle_ghost (mpm_utils.py:733-816): the velocity the particle reads from
+// nodes across the surface. Surface normal and distance come from the owner-lane
+// sums of the scan; the tangential part follows the surface type (sticky, slip,
+// separable Coulomb with a capped impulse) plus a separation push when the
 // particle sits within 0.05 dx of the surface.
-__device__ void cdf_ghost(const PK &k, const Stencil &s, const float *xp, const float *vp, int pc, const float *grav,
+__device__ void cdf_ghost(const PK &k, const CdfScan &c, const float *xp, const float *vp, int pc, const float *grav,
                           float *ghost) {
-    float d_hat = 0.0f, n_acc[3] = {0.f, 0.f, 0.f}, best_w = 0.0f;
-    int lane_p = 0;
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j)
-            for (int kk = 0; kk < 3; ++kk) {
-                size_t id = node_id(k, s, i, j, kk);
-                int t = k.ctag_prev[id];
-                if (t == 0) continue;
-                int own = (t >> kCdfOwnerShift) & 3;
-                if (((t >> (2 * own)) & 1) == 0) continue;
-                float w = s.w[0][i] * s.w[1][j] * s.w[2][kk];
-                float sgn = ((t >> (2 * own + 1)) & 1) ? 1.0f : -1.0f;
-                float dd = k.cd_prev[id];
-                d_hat += w * sgn * dd;
-                float dw[3] = {s.dw[0][i] * s.w[1][j] * s.w[2][kk], s.w[0][i] * s.dw[1][j] * s.w[2][kk],
-                               s.w[0][i] * s.w[1][j] * s.dw[2][kk]};
-#pragma unroll
-                for (int a = 0; a < 3; ++a) n_acc[a] += dw[a] * k.inv_dx * sgn * dd;
-                if (w > best_w) { best_w = w; lane_p = own; }
-            }
     float vf[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) { vf[a] = vp[a] + grav[a] * k.dt; ghost[a] = vf[a]; }
-    float nl = sqrtf(n_acc[0] * n_acc[0] + n_acc[1] * n_acc[1] + n_acc[2] * n_acc[2]);
+    const float nl = sqrtf(c.n_acc[0] * c.n_acc[0] + c.n_acc[1] * c.n_acc[1] + c.n_acc[2] * c.n_acc[2]);
     if (!(nl > 1.0e-12f)) return;
+    const int lane_p = c.lane_p;
     const float side = ((pc >> (2 * lane_p + 1)) & 1) ? 1.0f : -1.0f;
     float n[3], vs[3], vrel[3];
     const float *cp = k.lanes.c_prev[lane_p], *vl = k.lanes.v_prev[lane_p], *wl = k.lanes.w_prev[lane_p];
     float rel[3] = {xp[0] - cp[0], xp[1] - cp[1], xp[2] - cp[2]};
 #pragma unroll
-    for (int a = 0; a < 3; ++a) n[a] = n_acc[a] / nl * side;
+    for (int a = 0; a < 3; ++a) n[a] = c.n_acc[a] / nl * side;
     vs[0] = vl[0] + (wl[1] * rel[2] - wl[2] * rel[1]);
     vs[1] = vl[1] + (wl[2] * rel[0] - wl[0] * rel[2]);
     vs[2] = vl[2] + (wl[0] * rel[1] - wl[1] * rel[0]);
@@ -781,18 +795,18 @@ __device__ void cdf_ghost(const PK &k, const Stencil &s, const float *xp, const 
     float vt[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) vt[a] = vrel[a] - n[a] * vn;
-    float c = 0.0f;
-    const float d_side = d_hat * side, eps = 0.05f * k.dx;
-    if (d_side < eps) c = fminf((eps - d_side) / k.dt, 0.5f * k.dx / k.dt);
+    float cc = 0.0f;
+    const float d_side = c.d_hat * side, eps = 0.05f * k.dx;
+    if (d_side < eps) cc = fminf((eps - d_side) / k.dt, 0.5f * k.dx / k.dt);
     const int stype = k.lanes.type[lane_p];
     if (stype == 0) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) ghost[a] = vs[a] + n[a] * c;
+        for (int a = 0; a < 3; ++a) ghost[a] = vs[a] + n[a] * cc;
     } else if (stype == 1) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) ghost[a] = vs[a] + vt[a] + n[a] * c;
+        for (int a = 0; a < 3; ++a) ghost[a] = vs[a] + vt[a] + n[a] * cc;
     } else {
-        const float dvn = fmaxf(-vn, 0.0f) + c;
+        const float dvn = fmaxf(-vn, 0.0f) + cc;
         const float tl = sqrtf(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
         if (tl > 1.0e-12f && dvn > 0.0f) {
             const float sc = fmaxf(0.0f, tl - k.lanes.fric[lane_p] * dvn) / tl;
@@ -801,7 +815,7 @@ __device__ void cdf_ghost(const PK &k, const Stencil &s, const float *xp, const 
         }
         const float vnp = fmaxf(vn, 0.0f);
 #pragma unroll
-        for (int a = 0; a < 3; ++a) ghost[a] = vs[a] + vt[a] + n[a] * vnp + n[a] * c;
+        for (int a = 0; a < 3; ++a) ghost[a] = vs[a] + vt[a] + n[a] * vnp + n[a] * cc;
     }
 }
 
@@ -809,18 +823,18 @@ __device__ void cdf_ghost(const PK &k, const Stencil &s, const float *xp, const 
 // withheld from the grid and added to the owner lane's reaction (force and torque
 // about the lane centre, summed per thread in float64 before one flush per lane).
 __device__ void cdf_deposit_all(const PK &k, const Stencil &s, int p, const float *v, const float *C, const float *S,
-                                int pc) {
+                                int pc, const int *tags) {
     double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     int acc_own = -1;
     auto flush = [&]() {
         if (acc_own < 0) return;
-        double *w = k.cwrench + 6 * acc_own;
+        double *w = k.cwrench + ((size_t)blockIdx.x * GBMPM_MAX_CDF + acc_own) * 6;
 #pragma unroll
         for (int a = 0; a < 6; ++a) { atomicAdd(w + a, acc[a]); acc[a] = 0.0; }
     };
     p2g_core(k, s, p, v, C, S, [&](int i, int j, int kk, float4 val) {
         size_t id = node_id(k, s, i, j, kk);
-        int nt = __ldg(k.ctag + id);
+        int nt = tags[(i * 3 + j) * 3 + kk];
         if (cdf_incompatible(pc, nt)) {
             int own = (nt >> kCdfOwnerShift) & 3;
             if (own != acc_own) { flush(); acc_own = own; }
@@ -866,9 +880,13 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
             set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
             return;
         }
+        CdfScan cs;
         if (k.cdf_on) {
             int pc = 0;
-            if (cdf_near(k, s)) pc = cdf_persist(k.ptag[p], cdf_vote(k, s, true));
+            if (cdf_near(k, s)) {
+                cdf_scan<true>(k, s, k.ctag_prev, k.cd_prev, cs);
+                pc = cdf_persist(k.ptag[p], cdf_vote_tag(cs));
+            }
             k.ptag[p] = pc;
             ptag = pc;
         }
@@ -876,10 +894,10 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
             const float *vi = k.v + 3 * (size_t)p;
             const float vp[3] = {vi[0], vi[1], vi[2]};
             float gh[3];
-            cdf_ghost(k, s, x, vp, ptag, k.grav, gh);
+            cdf_ghost(k, cs, x, vp, ptag, k.grav, gh);
             const float4 g4 = make_float4(gh[0], gh[1], gh[2], 0.0f);
             g2p_core(k, s, [&](int i, int j, int kk) {
-                return cdf_incompatible(ptag, k.ctag_prev[node_id(k, s, i, j, kk)]) ? g4 : global_fetch(k, s, i, j, kk);
+                return cdf_incompatible(ptag, cs.tag[(i * 3 + j) * 3 + kk]) ? g4 : global_fetch(k, s, i, j, kk);
             }, v, C, L);
         } else {
             g2p_core(k, s, [&](int i, int j, int kk) { return global_fetch(k, s, i, j, kk); }, v, C, L);
@@ -926,8 +944,12 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
             return;
         }
         int pc = 0;
-        if (k.cdf_on && cdf_near(k, s)) pc = cdf_persist(ptag, cdf_vote(k, s, false));
-        if (pc != 0) cdf_deposit_all(k, s, p, v, C, S, pc);
+        CdfScan cs;
+        if (k.cdf_on && cdf_near(k, s)) {
+            cdf_scan<false>(k, s, k.ctag, k.cd, cs);
+            pc = cdf_persist(ptag, cdf_vote_tag(cs));
+        }
+        if (pc != 0) cdf_deposit_all(k, s, p, v, C, S, pc, cs.tag);
         else global_deposit_all(k, s, p, v, C, S);
     }
 }
@@ -1360,6 +1382,22 @@ __device__ __forceinline__ void qrot_inv_rn(const float *q, const float *x, floa
         float td = __fmul_rn(__fmul_rn(q[a], d), 2.0f);
         out[a] = __fadd_rn(__fsub_rn(ta, tb), td);
     }
+}
+
+// Folds the per-CTA partial reactions into the per-lane totals and clears them:
+// one warp per component.
+__global__ void k_cdf_wrench_fold(double *partial, int nctas, double *total) {
+    const int comp = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;   // lane * 6 + axis
+    if (comp >= 6 * GBMPM_MAX_CDF) return;
+    const int l = threadIdx.x & 31;
+    double acc = 0.0;
+    for (int c = l; c < nctas; c += 32) {
+        double *q = partial + (size_t)c * 6 * GBMPM_MAX_CDF + comp;
+        acc += *q;
+        *q = 0.0;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (l == 0) total[comp] += acc;
 }
 
 __device__ __forceinline__ bool box_node(const CdfBox &b, long long idx, int &x, int &y, int &z) {
@@ -2045,7 +2083,9 @@ struct gbmpm_engine {
     CdfHost cdf;
     DevBuf<int> c_tag, c_tag_prev, c_block;
     DevBuf<float> c_d, c_d_prev;
-    DevBuf<double> c_wrench;
+    DevBuf<double> c_wrench;        // [4][6] reaction per lane (float64)
+    DevBuf<double> c_partial;       // [CTA][4][6] per-CTA partials the transfer passes add into
+    size_t c_partial_ctas = 0;
     int c_ng = 0;
     // adjoint segment storage and scratch (allocated by the first adjoint call)
     DevBuf<float> adj_states, adj_scratch;
@@ -2089,7 +2129,7 @@ PK make_pk(gbmpm_engine *e, const gbmpm_particles &P, float dt, int list) {
         k.ctag = e->c_tag.ptr; k.ctag_prev = e->c_tag_prev.ptr; k.cblock = e->c_block.ptr;
         k.cd = e->c_d.ptr; k.cd_prev = e->c_d_prev.ptr;
         k.ptag = P.cdf_tag;
-        k.cwrench = e->c_wrench.ptr;
+        k.cwrench = e->c_partial.ptr;
         std::memcpy(k.lanes.c_cur, H.c_cur, sizeof H.c_cur);
         std::memcpy(k.lanes.c_prev, H.c_prev, sizeof H.c_prev);
         std::memcpy(k.lanes.v_prev, H.v_prev, sizeof H.v_prev);
@@ -2311,6 +2351,13 @@ int check_ready(gbmpm_engine *e) {
 }
 
 // ---- CPIC (CDF) host driver ----------------------------------------------------
+void fold_cdf_wrench(gbmpm_engine *e, cudaStream_t s) {
+    if (!e->c_partial_ctas || !e->c_wrench.ptr) return;
+    k_cdf_wrench_fold<<<(6 * GBMPM_MAX_CDF + 7) / 8, 256, 0, s>>>(e->c_partial.ptr, (int)e->c_partial_ctas,
+                                                                  e->c_wrench.ptr);
+    e->launches++;
+}
+
 int cdf_grid_blocks(gbmpm_engine *e, long long work) {
     long long want = (work + 255) / 256;
     return (int)std::max<long long>(1, std::min<long long>(want, (long long)e->num_sms * 8));
@@ -2585,7 +2632,7 @@ void gbmpm_engine_destroy(gbmpm_engine *e) {
     e->ws_buf.release(); e->ws_keys[0].release(); e->ws_keys[1].release(); e->ws_idx[0].release();
     e->ws_idx[1].release(); e->ws_hist.release();
     e->c_tag.release(); e->c_tag_prev.release(); e->c_block.release(); e->c_d.release(); e->c_d_prev.release();
-    e->c_wrench.release();
+    e->c_wrench.release(); e->c_partial.release();
     e->adj_states.release(); e->adj_scratch.release(); e->adj_grid.release();
     delete e;
 }
@@ -2757,6 +2804,7 @@ int gbmpm_cdf_wrench(gbmpm_engine *e, int32_t lane, double out[6], void *stream)
     if (!e || !out) return fail(GBMPM_ERR_ARG, "null argument");
     if (lane < 0 || lane >= e->cdf.n) return fail(GBMPM_ERR_ARG, "CDF lane out of range");
     cudaStream_t s = (cudaStream_t)stream;
+    fold_cdf_wrench(e, s);
     GB_CUDA(cudaMemcpyAsync(out, e->c_wrench.ptr + 6 * lane, 6 * sizeof(double), cudaMemcpyDeviceToHost, s));
     GB_CUDA(cudaStreamSynchronize(s));
     return GBMPM_OK;
@@ -2777,6 +2825,9 @@ int gbmpm_reset_cdf_wrench(gbmpm_engine *e, void *stream) {
     if (!e) return fail(GBMPM_ERR_ARG, "null argument");
     if (e->cdf.n == 0) return GBMPM_OK;
     GB_CUDA(cudaMemsetAsync(e->c_wrench.ptr, 0, 6 * GBMPM_MAX_CDF * sizeof(double), (cudaStream_t)stream));
+    if (e->c_partial_ctas)
+        GB_CUDA(cudaMemsetAsync(e->c_partial.ptr, 0, e->c_partial_ctas * 6 * GBMPM_MAX_CDF * sizeof(double),
+                                (cudaStream_t)stream));
     return GBMPM_OK;
 }
 
@@ -2833,6 +2884,14 @@ int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32
     if (cdf) {
         int rc = check_ready(e);
         if (rc) return rc;
+        const size_t ctas = (size_t)std::max(1, (e->P.n + kParticleThreads - 1) / kParticleThreads);
+        if (e->c_partial_ctas < ctas) {
+            GB_CUDA(cudaStreamSynchronize(s));
+            if (e->c_partial_ctas) fold_cdf_wrench(e, s);
+            GB_CUDA(e->c_partial.ensure(ctas * 6 * GBMPM_MAX_CDF));
+            GB_CUDA(cudaMemsetAsync(e->c_partial.ptr, 0, ctas * 6 * GBMPM_MAX_CDF * sizeof(double), s));
+            e->c_partial_ctas = ctas;
+        }
         if (e->c_ng != e->M.n_grid) return fail(GBMPM_ERR_STATE, "CDF grids were sized for another n_grid");
         if (e->M.periodic_x) return fail(GBMPM_ERR_UNSUPPORTED, "CDF colliders do not wrap the periodic x axis");
         if (e->P.n > 0 && !e->P.cdf_tag) return fail(GBMPM_ERR_ARG, "CDF colliders need particles.cdf_tag");
