@@ -240,19 +240,22 @@ int gbmpm_contact_wrench(gbmpm_engine *e, const double box_center[3], const doub
                          void *stream);
 
 /* ---- adjoint (no counterpart in the reference) ---------------------------------
- * Adjoints of the particle state (x, v, C, F_trial, yield_stress; device arrays in
- * the particle layout) and accumulated adjoints of the per-particle mu and lam. */
+ * Adjoints of the particle state (x, v, C, F_trial, yield_stress, L; device arrays
+ * in the particle layout) and accumulated per-particle adjoints of mu, lam and of
+ * the Newtonian viscosity (its sum is the gradient of the per-type value). */
 typedef struct gbmpm_adj_grads {
     float *x, *v, *C, *F_trial, *yield_stress;
     float *mu, *lam;
+    float *L, *viscosity;
 } gbmpm_adj_grads;
 
 /* Replays `substeps` split-schedule substeps forward from the bound state (the
  * caller restores a checkpoint first), keeping each substep's starting state, then
  * carries the adjoints in g from the end of the segment back to its start and adds
- * each substep's contribution to g->mu and g->lam. Leaves the bound state at the
- * segment's end and advances *time. Covers jelly (FCR) and von Mises particles and
- * plane, cuboid and domain-wall colliders; anything else is GBMPM_ERR_UNSUPPORTED. */
+ * each substep's contribution to g->mu, g->lam and g->viscosity. Leaves the bound
+ * state at the segment's end and advances *time. Covers jelly (FCR), von Mises,
+ * water and Newtonian (Bingham, Herschel-Bulkley) particles and every grid
+ * collider; CDF lanes, periodic x and other materials are GBMPM_ERR_UNSUPPORTED. */
 int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t substeps,
                           const gbmpm_adj_grads *g, void *stream);
 

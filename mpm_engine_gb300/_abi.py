@@ -104,7 +104,7 @@ class Cdf(C.Structure):
 
 
 class AdjGrads(C.Structure):
-    _fields_ = [(k, C.c_void_p) for k in ("x", "v", "C", "F_trial", "yield_stress", "mu", "lam")]
+    _fields_ = [(k, C.c_void_p) for k in ("x", "v", "C", "F_trial", "yield_stress", "mu", "lam", "L", "viscosity")]
 
 
 # every entry point include/gbmpm.h declares, with its ctypes signature

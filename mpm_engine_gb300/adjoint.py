@@ -4,7 +4,8 @@ The reference has no adjoint; gradient-based identification there is done by
 finite differences over serial rollouts. Here `rollout` runs a scene forward on
 the engine and returns its final positions and velocities as torch tensors whose
 gradients flow, through the engine's adjoint kernels, to the initial velocity
-field, Young's modulus, Poisson's ratio and the yield stress.
+field, Young's modulus, Poisson's ratio, the yield stress and the Newtonian
+viscosity.
 
 Memory follows the usual checkpoint-and-recompute scheme: the forward keeps the
 state (x, v, C, F_trial, yield) and the collider poses every `checkpoint_every`
@@ -12,9 +13,10 @@ substeps; the backward restores each checkpoint in reverse, replays that segment
 one substep at a time (the engine keeps every substep's starting state on the
 device) and carries the adjoints back through it (`gbmpm_adjoint_segment`).
 
-Scope: jelly (FCR) and von Mises particles (with or without hardening), plane,
-cuboid and domain-wall colliders, no periodic axis, rpic_damping = 0, particle
-order fixed during the rollout (sort_interval = 0).
+Scope: jelly (FCR), von Mises (with or without hardening), water and Newtonian
+(Bingham, Herschel-Bulkley) particles; plane, cuboid, domain-wall, revolved-SDF cup
+and mesh-SDF colliders; no periodic axis, rpic_damping = 0, particle order fixed
+during the rollout (sort_interval = 0).
 """
 from __future__ import annotations
 
@@ -23,7 +25,7 @@ import ctypes as C
 from . import _abi
 from .solver import _torch
 
-_STATE = ("x", "v", "C", "F_trial", "yield_stress")
+_STATE = ("x", "v", "C", "F_trial", "L", "yield_stress")
 
 
 def _snapshot(s):
@@ -79,6 +81,7 @@ def _backward(s, dt, ckpts, xb, vb):
         "v": (vb.detach().to(**f).reshape(n, 3).clone() if vb is not None else torch.zeros(n, 3, **f)),
         "C": torch.zeros(n, 3, 3, **f), "F_trial": torch.zeros(n, 3, 3, **f),
         "yield_stress": torch.zeros(n, **f), "mu": torch.zeros(n, **f), "lam": torch.zeros(n, **f),
+        "L": torch.zeros(n, 3, 3, **f), "viscosity": torch.zeros(n, **f),
     }
     rec = _abi.AdjGrads(**{k: g[k].data_ptr() for k in g})
     lib, h = s._eng.lib, s._eng.h
@@ -90,14 +93,19 @@ def _backward(s, dt, ckpts, xb, vb):
     return g
 
 
+NEWTONIAN = 10   # material id whose per-type viscosity `viscosity` sets
+
+
 class _Rollout(_torch().autograd.Function):
     @staticmethod
-    def forward(ctx, v0, mu, lam, ys0, solver, dt, substeps, every):
+    def forward(ctx, v0, mu, lam, ys0, eta, solver, dt, substeps, every):
         s = solver
         s._t["v"].copy_(v0.detach().reshape(-1, 3))
         s._t["mu"].copy_(mu.detach())
         s._t["lam"].copy_(lam.detach())
         s._t["yield_stress"].copy_(ys0.detach())
+        s._model.plastic_viscosity[NEWTONIAN] = float(eta)
+        s._model_dirty = True
         ctx.solver, ctx.dt = s, dt
         ctx.ckpts = _forward(s, dt, substeps, every)
         x, v = s._t["x"].clone(), s._t["v"].clone()
@@ -109,7 +117,7 @@ class _Rollout(_torch().autograd.Function):
         s = ctx.solver
         g = _backward(s, ctx.dt, ctx.ckpts, xb, vb)
         _restore(s, ctx.final)
-        return g["v"], g["mu"], g["lam"], g["yield_stress"], None, None, None, None
+        return g["v"], g["mu"], g["lam"], g["yield_stress"], g["viscosity"].sum(), None, None, None, None
 
 
 def mu_lam(E, nu):
@@ -117,14 +125,15 @@ def mu_lam(E, nu):
     return E / (2.0 * (1.0 + nu)), E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
 
 
-def rollout(solver, dt: float, substeps: int, *, v0=None, E=None, nu=None, yield_stress=None,
+def rollout(solver, dt: float, substeps: int, *, v0=None, E=None, nu=None, yield_stress=None, viscosity=None,
             checkpoint_every: int = 20):
     """Advance `solver` by `substeps` substeps of dt and return (x, v) at the end.
 
-    v0 ((N, 3)), E, nu and yield_stress (scalars or (N,) tensors) are the
-    differentiable inputs; any left as None keeps the scene's current value and is
-    not differentiated. E and nu set mu and lam of every particle through the
-    reference's formula. The solver is left at the end state of the rollout."""
+    v0 ((N, 3)), E, nu and yield_stress (scalars or (N,) tensors) and viscosity (the
+    Newtonian plastic viscosity, a scalar) are the differentiable inputs; any left
+    as None keeps the scene's current value and is not differentiated. E and nu set
+    mu and lam of every particle through the reference's formula. The solver is
+    left at the end state of the rollout."""
     torch = _torch()
     _check(solver)
     s = solver
@@ -145,7 +154,11 @@ def rollout(solver, dt: float, substeps: int, *, v0=None, E=None, nu=None, yield
         ys = s._t["yield_stress"].clone()
     else:
         ys = (yield_stress if torch.is_tensor(yield_stress) else torch.as_tensor(yield_stress)).to(**f).expand(n)
-    return _Rollout.apply(v0, mu, lam, ys, s, float(dt), int(substeps), int(checkpoint_every))
+    if viscosity is None:
+        eta = torch.tensor(float(s._model.plastic_viscosity[NEWTONIAN]), **f)
+    else:
+        eta = (viscosity if torch.is_tensor(viscosity) else torch.as_tensor(viscosity)).to(**f)
+    return _Rollout.apply(v0, mu, lam, ys, eta, s, float(dt), int(substeps), int(checkpoint_every))
 
 
 class BatchRollout:
@@ -186,8 +199,9 @@ class BatchRollout:
 
     def backward(self, xbs, vbs):
         """Adjoints of the rollouts' starting states and parameters for the given
-        adjoints of their final (x, v): [{'v', 'x', 'C', 'F_trial', 'yield_stress',
-        'mu', 'lam'}]. Leaves every solver at its rollout's end state."""
+        adjoints of their final (x, v): [{'v', 'x', 'C', 'F_trial', 'L',
+        'yield_stress', 'mu', 'lam', 'viscosity'}]. Leaves every solver at its
+        rollout's end state."""
         torch = _torch()
         if self.ckpts is None:
             raise RuntimeError("forward must run first")
@@ -201,7 +215,8 @@ class BatchRollout:
                 f = dict(device=s._t["x"].device, dtype=torch.float32)
                 g = {"x": xb.detach().to(**f).reshape(n, 3).clone(), "v": vb.detach().to(**f).reshape(n, 3).clone(),
                      "C": torch.zeros(n, 3, 3, **f), "F_trial": torch.zeros(n, 3, 3, **f),
-                     "yield_stress": torch.zeros(n, **f), "mu": torch.zeros(n, **f), "lam": torch.zeros(n, **f)}
+                     "yield_stress": torch.zeros(n, **f), "mu": torch.zeros(n, **f), "lam": torch.zeros(n, **f),
+                     "L": torch.zeros(n, 3, 3, **f), "viscosity": torch.zeros(n, **f)}
                 gs.append(g)
                 recs.append(_abi.AdjGrads(**{k: g[k].data_ptr() for k in g}))
             torch.cuda.synchronize()

@@ -1,12 +1,14 @@
 // Reverse-mode adjoint of the explicit MLS/APIC substep (split schedule:
-// stress -> P2G -> grid update + colliders -> G2P) for the elastic (FCR, id 0) and
-// von Mises (id 1, optional hardening) materials, with plane, cuboid and domain-wall
-// colliders. The reference has no adjoint; the forward it differentiates is the one
+// stress -> P2G -> grid update + colliders -> G2P) for the elastic (FCR, id 0), von
+// Mises (id 1, optional hardening), water (id 6) and Newtonian / Bingham /
+// Herschel-Bulkley (id 10) materials, with plane, cuboid, domain-wall, revolved-SDF
+// cup and mesh-SDF colliders. The reference has no adjoint; the forward it differentiates is the one
 // restated by the rest of this file (mpm_utils.py:819-1158, mpm_solver_warp.py:
 // 1092-1281).
 //
-// One substep maps the particle state s = (x, v, C, F_trial, yield) to s' with
-// per-particle parameters (mu, lam). Given the adjoint of s' the kernels below
+// One substep maps the particle state s = (x, v, C, F_trial, L, yield) to s' with
+// per-particle parameters (mu, lam) and the per-type viscosity (L feeds the viscous
+// stress of the next substep). Given the adjoint of s' the kernels below
 // produce the adjoint of s and accumulate the adjoints of mu and lam:
 //
 //   forward recompute   k_adj_stress_fwd (F_trial -> F, Kirchhoff stress),
@@ -34,7 +36,8 @@ namespace gbmpm {
 
 struct AdjK {
     // state at the start of the substep (caller layout: x[n][3], C[n][9] ...)
-    const float *x, *v, *C, *Ft, *ys;
+    const float *x, *v, *C, *Ft, *Lst, *ys;
+    const MatTables *tab;
     const float *mass, *vol, *mu, *lam;
     const int *mat, *sel;
     int n;
@@ -48,8 +51,8 @@ struct AdjK {
     float damp;
     float hard1, xi1;   // von Mises hardening switch and xi (material table, id 1)
     // adjoints: in = end of the substep, out = start of the substep
-    float *xb, *vb, *Cb, *Ftb, *ysb;
-    float *mub, *lamb;  // accumulated over substeps
+    float *xb, *vb, *Cb, *Ftb, *Lb, *ysb;
+    float *mub, *lamb, *pvb;   // accumulated over substeps (pvb: Newtonian viscosity)
     // colliders of this substep
     int ncol;
     const ColDev *cols;
@@ -157,6 +160,34 @@ __device__ void adj_stress(int mat, const float *F, float mu, float lam, float *
         for (int j = 0; j < 3; ++j) S[3 * i + j] = 0.5f * (T[3 * i + j] + T[3 * j + i]);
 }
 
+// Fluid stress (water id 6; Newtonian / Bingham / Herschel-Bulkley id 10) as the
+// engine's stress pass computes it: F reset to J^(1/3) I, tau = J (p I + 2 eta dev D).
+struct FluidTerms {
+    float Jt, Jc, J, pr, gd, eta, Dd[9];
+};
+__device__ void fluid_stress(const AdjK &k, int p, int mat, const float *Ft, const float *L, FluidTerms &f, float *Fp,
+                             float *S) {
+    const MatTables &T = *k.tab;
+    f.Jt = det3(Ft);
+    f.Jc = powf(f.Jt, 1.0f / 3.0f);
+    f.J = f.Jc * f.Jc * f.Jc;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Fp[i] = (i % 4 == 0) ? f.Jc : 0.0f;
+    f.pr = eos_pressure(f.J, T.bulk[mat]);
+    if (mat == 6) {
+        f.gd = 1.0f; f.eta = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) { f.Dd[i] = 0.0f; S[i] = (i % 4 == 0) ? f.J * f.pr : 0.0f; }
+        return;
+    }
+    dev_rate(L, f.Dd, f.gd);
+    const float ys = k.ys[p], Kp = T.hardening[mat];
+    f.eta = T.pv[mat] + (ys != 0.0f ? ys / f.gd : 0.0f) + (Kp != 0.0f ? Kp * powf(f.gd, T.softening[mat] - 1.0f) : 0.0f);
+    const float two_eta = 2.0f * f.eta;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) S[i] = f.J * (((i % 4 == 0) ? f.pr : 0.0f) + two_eta * f.Dd[i]);
+}
+
 __global__ void k_adj_stress_fwd(AdjK k) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= k.n || (k.sel && k.sel[p] != 0)) return;
@@ -165,6 +196,16 @@ __global__ void k_adj_stress_fwd(AdjK k) {
     for (int i = 0; i < 9; ++i) Ft[i] = k.Ft[9 * (size_t)p + i];
     const int mat = k.mat[p];
     const float mu = k.mu[p], lam = k.lam[p];
+    if (mat == 6 || mat == 10) {
+        float L[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) L[i] = k.Lst[9 * (size_t)p + i];
+        FluidTerms f;
+        fluid_stress(k, p, mat, Ft, L, f, Fp, S);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) { k.Fp[9 * (size_t)p + i] = Fp[i]; k.S[9 * (size_t)p + i] = S[i]; }
+        return;
+    }
     if (mat == 1) {
         float U[9], V[9], sg[3], eps[3];
         vm_return(Ft, mu, lam, k.ys[p], U, sg, V, eps, Fp);
@@ -266,10 +307,10 @@ __global__ void k_adj_g2p_bwd(AdjK a) {
         xb[d] = a.xb[3 * p + d];
         vt[d] = a.vb[3 * p + d] + a.dt * xb[d];   // adjoint of v' (x' = x + dt v')
     }
-    float Lb[9];   // adjoint of L: F_trial' = (I + dt L) F
+    float Lb[9];   // adjoint of L: the state's L' (viscous stress next substep) and F_trial' = (I + dt L) F
     mmT(Ftb, Fp, Lb);
 #pragma unroll
-    for (int i = 0; i < 9; ++i) Lb[i] *= a.dt;
+    for (int i = 0; i < 9; ++i) Lb[i] = Lb[i] * a.dt + a.Lb[9 * (size_t)p + i];
     Stencil s;
     stencil(x, a.inv_dx, s);
     if (!stencil_ok(s, a.ng, 0)) return;
@@ -313,6 +354,29 @@ __global__ void k_adj_g2p_bwd(AdjK a) {
     for (int i = 0; i < 9; ++i) a.Fpb[9 * (size_t)p + i] = Fb[i];
 #pragma unroll
     for (int d = 0; d < 3; ++d) a.xb[3 * p + d] = xb[d];
+}
+
+// Adjoint of the separable contact response v = v_s + v_t max(0, |v_t| + mu v_n)/|v_t|
+// applied when v_n = v_r . n < 0 (identity otherwise), with v_r = v - v_s and
+// v_t = v_r - v_n n; vb: adjoint of the output in, of the input velocity out.
+__device__ __forceinline__ void coulomb_adj(const float *vr, const float *n, float mu, float tl_eps, float *vb) {
+    const float vn = vr[0] * n[0] + vr[1] * n[1] + vr[2] * n[2];
+    if (!(vn < 0.0f)) return;
+    const float vt[3] = {vr[0] - vn * n[0], vr[1] - vn * n[1], vr[2] - vn * n[2]};
+    const float tl = sqrtf(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
+    float tb[3] = {vb[0], vb[1], vb[2]}, nb = 0.0f;
+    if (tl > tl_eps) {
+        if (tl + mu * vn <= 0.0f) { vb[0] = vb[1] = vb[2] = 0.0f; return; }
+        const float th[3] = {vt[0] / tl, vt[1] / tl, vt[2] / tl};
+        const float thv = th[0] * vb[0] + th[1] * vb[1] + th[2] * vb[2];
+        const float f = mu * vn / tl;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) tb[d] = vb[d] + f * (vb[d] - th[d] * thv);
+        nb = mu * thv;
+    }
+    const float ntb = n[0] * tb[0] + n[1] * tb[1] + n[2] * tb[2];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) vb[d] = tb[d] - n[d] * ntb + n[d] * nb;
 }
 
 // Adjoint of one collider at one node: vb holds the adjoint of the collider's
@@ -361,6 +425,61 @@ __device__ void collide_adj(const ColDev &c, const PoseRec &P, int gx, int gy, i
         if (P.mode == 2) { vb[0] = vb[1] = vb[2] = 0.0f; return; }
         const float o0 = (float)gx * dx - P.p[0], o1 = (float)gy * dx - P.p[1], o2 = (float)gz * dx - P.p[2];
         if (fabsf(o0) < c.size[0] && fabsf(o1) < c.size[1] && fabsf(o2) < c.size[2]) vb[0] = vb[1] = vb[2] = 0.0f;
+        return;
+    }
+    case GBMPM_COLLIDER_CUP: {   // mpm_solver_warp.py:2161-2225
+        const float rel[3] = {(float)gx * dx - P.p[0], (float)gy * dx - P.p[1], (float)gz * dx - P.p[2]};
+        const float *R = P.r;
+        const float l0 = R[0] * rel[0] + R[3] * rel[1] + R[6] * rel[2];
+        const float l1 = R[1] * rel[0] + R[4] * rel[1] + R[7] * rel[2];
+        const float l2 = R[2] * rel[0] + R[5] * rel[1] + R[8] * rel[2];
+        const float sdf = glass_sdf(l0, l1, l2, c);
+        if (!(sdf < c.band_c)) return;
+        if (!(sdf > -c.sticky)) { vb[0] = vb[1] = vb[2] = 0.0f; return; }   // grabbed: v = v_solid
+        const float h = 0.25f * dx;
+        float n0 = glass_sdf(l0 + h, l1, l2, c) - glass_sdf(l0 - h, l1, l2, c);
+        float n1 = glass_sdf(l0, l1 + h, l2, c) - glass_sdf(l0, l1 - h, l2, c);
+        float n2 = glass_sdf(l0, l1, l2 + h, c) - glass_sdf(l0, l1, l2 - h, c);
+        const float nl = sqrtf(n0 * n0 + n1 * n1 + n2 * n2);
+        if (!(nl > 1.0e-12f)) return;
+        n0 /= nl; n1 /= nl; n2 /= nl;
+        const float n[3] = {R[0] * n0 + R[1] * n1 + R[2] * n2, R[3] * n0 + R[4] * n1 + R[5] * n2,
+                            R[6] * n0 + R[7] * n1 + R[8] * n2};
+        const float vs[3] = {c.vel[0] + (c.omega[1] * rel[2] - c.omega[2] * rel[1]),
+                             c.vel[1] + (c.omega[2] * rel[0] - c.omega[0] * rel[2]),
+                             c.vel[2] + (c.omega[0] * rel[1] - c.omega[1] * rel[0])};
+        const float vr[3] = {vin[0] - vs[0], vin[1] - vs[1], vin[2] - vs[2]};
+        coulomb_adj(vr, n, c.friction, 1.0e-20f, vb);
+        return;
+    }
+    case GBMPM_COLLIDER_SDF: {   // mpm_solver_warp.py:2680-2736
+        const float rel[3] = {(float)gx * dx - P.p[0], (float)gy * dx - P.p[1], (float)gz * dx - P.p[2]};
+        float body[3];
+        qrot(P.q, rel, body, true);
+        const float f0 = (body[0] - c.origin[0]) / c.cell, f1 = (body[1] - c.origin[1]) / c.cell,
+                    f2 = (body[2] - c.origin[2]) / c.cell;
+        const float rf = (float)c.sdf_res - 1.0f;
+        if (!(f0 >= 0.0f && f1 >= 0.0f && f2 >= 0.0f && f0 <= rf && f1 <= rf && f2 <= rf)) return;
+        if (!(trilerp(c.sdf_val, c.sdf_res, f0, f1, f2, 1, 0) <= c.band)) return;
+        float g[3] = {trilerp(c.sdf_grad, c.sdf_res, f0, f1, f2, 3, 0), trilerp(c.sdf_grad, c.sdf_res, f0, f1, f2, 3, 1),
+                      trilerp(c.sdf_grad, c.sdf_res, f0, f1, f2, 3, 2)};
+        const float gl = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+        if (!(gl > 1.0e-12f)) return;
+        g[0] /= gl; g[1] /= gl; g[2] /= gl;
+        float n[3];
+        qrot(P.q, g, n, false);
+        if (c.surface == 0) { vb[0] = vb[1] = vb[2] = 0.0f; return; }
+        if (c.surface == 1) {   // v = v_s + (v_r - (v_r . n) n)
+            const float nb = n[0] * vb[0] + n[1] * vb[1] + n[2] * vb[2];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) vb[d] -= nb * n[d];
+            return;
+        }
+        const float vs[3] = {c.vel[0] + (c.omega[1] * rel[2] - c.omega[2] * rel[1]),
+                             c.vel[1] + (c.omega[2] * rel[0] - c.omega[0] * rel[2]),
+                             c.vel[2] + (c.omega[0] * rel[1] - c.omega[1] * rel[0])};
+        const float vr[3] = {vin[0] - vs[0], vin[1] - vs[1], vin[2] - vs[2]};
+        coulomb_adj(vr, n, c.friction, 1.0e-12f, vb);
         return;
     }
     case GBMPM_COLLIDER_WALLS: {
@@ -457,8 +576,52 @@ __global__ void k_adj_p2g_bwd(AdjK a) {
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) tb[3 * i + j] = -0.5f * vol * (Ab[3 * i + j] + Ab[3 * j + i]);
-    float mub = 0.0f, lamb = 0.0f;
-    {
+    float mub = 0.0f, lamb = 0.0f, pvb = 0.0f;
+    float Lb[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // adjoint of the state's L
+    float Ftb[9];
+    float ysb_in = a.ysb[p], ysb = ysb_in;
+    if (mat == 6 || mat == 10) {
+        // tau = J (p I + 2 eta dev D) with J = Jc^3, Jc = det(F_trial)^(1/3), F = Jc I,
+        // p = -K (J^-1.1 - 1), D = sym(L), eta = eta_p + tau_y / gd + K_p gd^(n - 1)
+        const MatTables &T = *a.tab;
+        float L[9], Sx[9], Fq[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) L[i] = a.Lst[9 * (size_t)p + i];
+        FluidTerms f;
+        fluid_stress(a, p, mat, Ft, L, f, Fq, Sx);
+        const float trb = tb[0] + tb[4] + tb[8];
+        const float dpr = 1.1f * T.bulk[mat] * powf(f.J, -2.1f);
+        float Jb = trb * f.pr + f.J * trb * dpr;
+        if (mat == 10) {
+            float tD = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) tD += tb[i] * f.Dd[i];
+            Jb += 2.0f * f.eta * tD;
+            const float etab = 2.0f * f.J * tD;
+            const float ys_p = a.ys[p], Kp = T.hardening[mat], np_ = T.softening[mat];
+            const float detadgd = -ys_p / (f.gd * f.gd) + (Kp != 0.0f ? Kp * (np_ - 1.0f) * powf(f.gd, np_ - 2.0f) : 0.0f);
+            const float gdb = etab * detadgd;
+            float Ddb[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Ddb[i] = 2.0f * f.J * f.eta * tb[i] + gdb * 2.0f * f.Dd[i] / f.gd;
+            // L adjoint: sym(dev(Ddb))
+            const float tr3 = (Ddb[0] + Ddb[4] + Ddb[8]) / 3.0f;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                    Lb[3 * i + j] = 0.5f * (Ddb[3 * i + j] + Ddb[3 * j + i]) - ((i == j) ? tr3 : 0.0f);
+            ysb = ysb_in + etab / f.gd;
+            pvb = etab;
+        }
+        // back through J = Jc^3, F = Jc I and Jc = det(F_trial)^(1/3)
+        const float Jcb = 3.0f * f.Jc * f.Jc * Jb + (Fb[0] + Fb[4] + Fb[8]);
+        const float Jtb = Jcb * f.Jc / (3.0f * f.Jt);
+        float cof[9];
+        cofactor(Ft, cof);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Ftb[i] = Jtb * cof[i];
+    } else {
         float U[9], V[9], sg[3], yd[3];
         svd3(Fp, U, sg, V);
         if (mat == 0) {   // tau = 2 mu (F - R) F^T + lam J (J - 1) I
@@ -522,9 +685,7 @@ __global__ void k_adj_p2g_bwd(AdjK a) {
                 }
         }
     }
-    // return-map adjoint: F (projected) -> F_trial, yield, mu
-    float Ftb[9];
-    float ysb_in = a.ysb[p], ysb = ysb_in;
+    // return-map adjoint: F (projected) -> F_trial, yield, mu (fluids done above)
     if (mat == 1) {
         float U[9], V[9], sg[3], e[3], Fq[9];
         const bool plastic = vm_return(Ft, mu, lam, ys, U, sg, V, e, Fq);
@@ -578,17 +739,22 @@ __global__ void k_adj_p2g_bwd(AdjK a) {
                 ysb += ysb_in;
             }
         }
-    } else {
+    } else if (mat != 6 && mat != 10) {   // jelly: F = F_trial
 #pragma unroll
         for (int i = 0; i < 9; ++i) Ftb[i] = Fb[i];
     }
 #pragma unroll
     for (int d = 0; d < 3; ++d) { a.xb[3 * p + d] = xb[d]; a.vb[3 * p + d] = vb[d]; }
 #pragma unroll
-    for (int i = 0; i < 9; ++i) { a.Cb[9 * (size_t)p + i] = Cb[i]; a.Ftb[9 * (size_t)p + i] = Ftb[i]; }
+    for (int i = 0; i < 9; ++i) {
+        a.Cb[9 * (size_t)p + i] = Cb[i];
+        a.Ftb[9 * (size_t)p + i] = Ftb[i];
+        a.Lb[9 * (size_t)p + i] = Lb[i];
+    }
     a.ysb[p] = ysb;
     a.mub[p] += mub;
     a.lamb[p] += lamb;
+    a.pvb[p] += pvb;
 }
 
 }  // namespace gbmpm
@@ -599,12 +765,11 @@ namespace {
 int adjoint_supported(gbmpm_engine *e) {
     if (e->M.periodic_x) return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint does not wrap the periodic x axis");
     if (e->M.rpic_damping != 0.0f) return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint needs rpic_damping == 0");
-    if (e->M.material_mask & ~3u)
-        return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint covers jelly (0) and von Mises (1) particles only");
+    const uint32_t covered = (1u << 0) | (1u << 1) | (1u << 6) | (1u << 10);
+    if (e->M.material_mask & ~covered)
+        return fail(GBMPM_ERR_UNSUPPORTED,
+                    "the adjoint covers jelly (0), von Mises (1), water (6) and Newtonian (10) particles only");
     if (e->cdf.n > 0) return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint does not cover CDF colliders");
-    for (const gbmpm_collider &c : e->cols)
-        if (c.kind != GBMPM_COLLIDER_PLANE && c.kind != GBMPM_COLLIDER_BOX && c.kind != GBMPM_COLLIDER_WALLS)
-            return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint covers plane, cuboid and domain-wall colliders only");
     return GBMPM_OK;
 }
 
@@ -618,15 +783,17 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
     if (rc) return rc;
     if (!time || !gr || substeps < 1 || substeps > GBMPM_MAX_SUBSTEPS || !(dt > 0.0))
         return fail(GBMPM_ERR_ARG, "bad adjoint arguments");
-    if (!gr->x || !gr->v || !gr->C || !gr->F_trial || !gr->yield_stress || !gr->mu || !gr->lam)
+    if (!gr->x || !gr->v || !gr->C || !gr->F_trial || !gr->yield_stress || !gr->mu || !gr->lam || !gr->L ||
+        !gr->viscosity)
         return fail(GBMPM_ERR_ARG, "every adjoint array is required");
+    if (!e->P.L) return fail(GBMPM_ERR_ARG, "the adjoint needs particles.L");
     if ((rc = adjoint_supported(e))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     const gbmpm_particles &P = e->P;
     const int n = P.n, ng = e->G.n_grid, nc = (int)e->cols.size();
     const size_t nn = (size_t)ng * ng * ng;
     // segment storage: the state at the start of every substep
-    const size_t per = (size_t)25 * n;   // x 3, v 3, C 9, F_trial 9, yield 1
+    const size_t per = (size_t)34 * n;   // x 3, v 3, C 9, F_trial 9, L 9, yield 1
     GB_CUDA(e->adj_states.ensure(per * substeps));
     GB_CUDA(e->adj_scratch.ensure((size_t)27 * n));
     GB_CUDA(e->adj_grid.ensure(4 * nn));   // four float4 grids
@@ -641,7 +808,8 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
         GB_CUDA(cudaMemcpyAsync(st + 3 * (size_t)n, P.v, 3 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         GB_CUDA(cudaMemcpyAsync(st + 6 * (size_t)n, P.C, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         GB_CUDA(cudaMemcpyAsync(st + 15 * (size_t)n, P.F_trial, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-        GB_CUDA(cudaMemcpyAsync(st + 24 * (size_t)n, P.yield_stress, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        GB_CUDA(cudaMemcpyAsync(st + 24 * (size_t)n, P.L, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        GB_CUDA(cudaMemcpyAsync(st + 33 * (size_t)n, P.yield_stress, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         record_tick(e, dtf, 1, false, false, s, false, 0.0, 0.0, i);
     }
     float4 *grid = e->adj_grid.ptr;
@@ -651,7 +819,8 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
         const float *st = e->adj_states.ptr + per * i;
         AdjK a{};
         a.x = st; a.v = st + 3 * (size_t)n; a.C = st + 6 * (size_t)n; a.Ft = st + 15 * (size_t)n;
-        a.ys = st + 24 * (size_t)n;
+        a.Lst = st + 24 * (size_t)n; a.ys = st + 33 * (size_t)n;
+        a.tab = e->d_tab.ptr;
         a.mass = P.mass; a.vol = P.vol; a.mu = P.mu; a.lam = P.lam; a.mat = P.material; a.sel = P.selection;
         a.n = n;
         a.Fp = e->adj_scratch.ptr; a.S = a.Fp + 9 * (size_t)n; a.Fpb = a.S + 9 * (size_t)n;
@@ -660,8 +829,8 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
         for (int d = 0; d < 3; ++d) a.grav[d] = e->M.gravity[d];
         a.damp = e->M.grid_v_damping_scale;
         a.hard1 = e->M.hardening[1]; a.xi1 = e->M.xi[1];
-        a.xb = gr->x; a.vb = gr->v; a.Cb = gr->C; a.Ftb = gr->F_trial; a.ysb = gr->yield_stress;
-        a.mub = gr->mu; a.lamb = gr->lam;
+        a.xb = gr->x; a.vb = gr->v; a.Cb = gr->C; a.Ftb = gr->F_trial; a.Lb = gr->L; a.ysb = gr->yield_stress;
+        a.mub = gr->mu; a.lamb = gr->lam; a.pvb = gr->viscosity;
         a.ncol = nc; a.cols = e->d_cols.ptr; a.poses = e->d_pose.ptr + (size_t)i * std::max(1, nc);
         // the engine's P2G building block reads its inputs through a PK
         gbmpm_particles Ps = P;

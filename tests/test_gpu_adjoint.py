@@ -21,13 +21,25 @@ pytestmark = pytest.mark.gpu
 DT, PRE, K, EVERY = 1.0e-4, 20, 4, 2
 N, NG = 1500, 32
 
+# a Bingham fluid gentle enough for dt = 1e-4 on this grid (its apparent viscosity
+# tops out at eta + tau_y / 0.02 = 102 Pa s, inside the explicit viscous limit)
+MATS = dict(MATERIALS, bingham_soft=lambda: __import__("mpm_engine_gb300").newtonian(
+    eta=2.0, density=1000.0, bulk_modulus=2.0e5).with_yield(2.0))
 
-def _scene(cls, key, floor="sticky", plate=False):
+
+def _scene(cls, key, floor="sticky", plate=False, cup=False, sphere=False):
+    from mpm_engine_gb300.geometry import analytic_sdf
+    from scenes_lib import SMALL_CUP
     pts, vol = blob(n=N, lo=0.12, size=0.08)
     s = make(cls, NG, 0.4).load_particles(pts, vol)
-    s.set_material(MATERIALS[key](), g=[0.0, 0.0, -9.8])
+    s.set_material(MATS[key](), g=[0.0, 0.0, -9.8])
     dx = 0.4 / NG
-    s.add_plane((0, 0, 0.121), (0, 0, 1), floor, friction=0.0 if floor == "sticky" else 0.3)
+    if cup:       # the blob lands on the cup's floor and presses its walls
+        s.add_cup(SMALL_CUP, (0.16, 0.16, 0.155), friction=0.3)
+    elif sphere:  # the blob lands on a mesh-SDF sphere
+        s.add_sdf_collider(analytic_sdf("sphere", radius=0.03), center=(0.16, 0.16, 0.095), friction=0.3)
+    else:
+        s.add_plane((0, 0, 0.121), (0, 0, 1), floor, friction=0.0 if floor == "sticky" else 0.3)
     s.add_domain_walls()
     if plate:
         s.add_box((0.16, 0.16, 0.20 + dx), (0.06, 0.06, dx), velocity=(0.0, 0.0, -0.5))
@@ -54,18 +66,21 @@ class Case:
         self.s = _scene(Solver, key, **kw)
         self.snap = adjoint._snapshot(self.s)
         self.state = self.s.export_state()
-        m = MATERIALS[key]()
+        m = MATS[key]()
         self.E, self.nu, self.ys = float(m.E), float(m.nu), float(m.yield_stress)
+        self.eta = float(self.s._model.plastic_viscosity[10])
         self.v0 = self.s._t["v"].clone()
         dev = self.v0.device
         self.dev = dev
         self.a, self.b = (torch.from_numpy(w).to(dev) for w in _weights())
 
-    def rollout(self, v0, E, nu, ys, grad=False):
+    def rollout(self, v0, E, nu, ys, eta=None, grad=False):
         import torch
         from mpm_engine_gb300 import adjoint
         adjoint._restore(self.s, self.snap)
-        x, v = adjoint.rollout(self.s, DT, K, v0=v0, E=E, nu=nu, yield_stress=ys, checkpoint_every=EVERY)
+        eta = self.eta if eta is None else eta
+        x, v = adjoint.rollout(self.s, DT, K, v0=v0, E=E, nu=nu, yield_stress=ys, viscosity=eta,
+                               checkpoint_every=EVERY)
         L = (x.double() * self.a).sum() + (v.double() * self.b).sum()
         if grad:
             L.backward()
@@ -75,19 +90,22 @@ class Case:
         import torch
         t = lambda x: torch.tensor(x, device=self.dev, requires_grad=True)  # noqa: E731
         v0 = self.v0.clone().requires_grad_(True)
-        E, nu, ys = t(self.E), t(self.nu), t(self.ys)
-        self.rollout(v0, E, nu, ys, grad=True)
-        return {"v0": v0.grad, "E": float(E.grad), "nu": float(nu.grad), "ys": float(ys.grad)}
+        E, nu, ys, eta = t(self.E), t(self.nu), t(self.ys), t(self.eta)
+        self.rollout(v0, E, nu, ys, eta, grad=True)
+        return {"v0": v0.grad, "E": float(E.grad), "nu": float(nu.grad), "ys": float(ys.grad),
+                "eta": float(eta.grad)}
 
     def fd_gpu(self, which, rel=1e-2, direction=None):
+        base = {"v0": self.v0, "E": self.E, "nu": self.nu, "ys": self.ys, "eta": self.eta}
+
         def at(sg):
-            p = {"v0": self.v0, "E": self.E, "nu": self.nu, "ys": self.ys}
+            p = dict(base)
             if which == "v0":
                 p["v0"] = self.v0 + sg * rel * direction
             else:
                 p[which] = p[which] * (1.0 + sg * rel)
-            return self.rollout(p["v0"], p["E"], p["nu"], p["ys"])
-        h = rel if which == "v0" else rel * {"E": self.E, "nu": self.nu, "ys": self.ys}[which]
+            return self.rollout(p["v0"], p["E"], p["nu"], p["ys"], p["eta"])
+        h = rel if which == "v0" else rel * base[which]
         return (at(1.0) - at(-1.0)) / (2.0 * h)
 
     def fd_oracle(self, O, which, rel=1e-2, direction=None):
@@ -145,6 +163,24 @@ def test_gradients_match_oracle_finite_differences(cuda, oracle_lib, key, kw):
            f"{key} d/dv0 (oracle)")
 
 
+@pytest.mark.parametrize("key,kw,params", [
+    ("newtonian", {"cup": True}, ("eta",)),
+    ("bingham_soft", {"cup": True}, ("eta", "ys")),
+    ("jelly", {"sphere": True}, ("E", "nu")),
+])
+def test_fluid_cup_and_sdf_gradients_match_finite_differences(cuda, key, kw, params):
+    """The Newtonian family (viscosity, Bingham yield) in a revolved-SDF cup, and
+    jelly on a mesh-SDF sphere."""
+    import torch
+    c = Case(key, **kw)
+    g = c.grads()
+    for p in params:
+        _close(g[p], c.fd_gpu(p), 0.02, f"{key} d/d{p}")
+    d = torch.randn(c.v0.shape, generator=torch.Generator().manual_seed(5)).to(c.dev)
+    d = d / d.norm()
+    _close(float((g["v0"] * d).sum()), c.fd_gpu("v0", rel=1e-1, direction=d), 0.02, f"{key} d/dv0")
+
+
 def test_long_rollout_checkpoint_interval_does_not_change_gradients(cuda):
     import torch
     from mpm_engine_gb300 import Solver, adjoint
@@ -166,7 +202,7 @@ def test_unsupported_scenes_are_refused(cuda):
     from mpm_engine_gb300 import Solver, adjoint
     pts, vol = blob(n=500)
     s = make(Solver, 32, 0.4).load_particles(pts, vol)
-    s.set_material(MATERIALS["newtonian"]())
+    s.set_material(MATERIALS["mu_i"]())
     with pytest.raises(NotImplementedError):
         x, v = adjoint.rollout(s, DT, 4, v0=torch.zeros(len(pts), 3, device="cuda", requires_grad=True))
         x.sum().backward()
