@@ -160,11 +160,19 @@ def glass_cavity_profile(profile: GlassProfile | None = None) -> np.ndarray:
 
 def glass_cdf(dx: float, profile: GlassProfile | None = None, res: int = 96):
     """The glass as a CDF collider field, with a built band wide enough for a runtime
-    band of 2 dx (examples/pour_franka.py:249-262)."""
+    band of 2 dx (examples/pour_franka.py:249-262). The field's margin around the
+    surface is widened to cover the band: with the recipe's fixed 4-cell margin a
+    coarse grid's band reaches past the field below the glass floor, nodes there are
+    never tagged and material seeps through."""
     from .geometry import revolved_open_cdf
     prof = glass_cavity_profile(profile)
     span = max(2.0 * float(prof[:, 0].max()), float(prof[:, 1].max() - prof[:, 1].min()))
-    cell = span / (res - 1 - 8)
+    margin = 4.0
+    for _ in range(3):
+        cell = span / (res - 1 - 2 * margin)
+        band_cells = max(3.0, float(np.ceil(2.2 * dx / cell)))
+        margin = max(4.0, band_cells + 1.0)
+    cell = span / (res - 1 - 2 * margin)
     band_cells = max(3.0, float(np.ceil(2.2 * dx / cell)))
-    return revolved_open_cdf(prof, res=res, band_cells=band_cells)
+    return revolved_open_cdf(prof, res=res, band_cells=band_cells, margin_cells=margin)
 

@@ -110,9 +110,10 @@ class Case:
 
     def fd_oracle(self, O, which, rel=1e-2, direction=None):
         from mpm_engine_gb300.host import mu_lam_from_E_nu_f32
+        base = {"E": self.E, "nu": self.nu, "ys": self.ys, "eta": self.eta}
 
         def at(sg):
-            p = {"E": self.E, "nu": self.nu, "ys": self.ys}
+            p = dict(base)
             if which != "v0":
                 p[which] = p[which] * (1.0 + sg * rel)
             o = O.from_state(self.state, NG, 0.4)
@@ -120,11 +121,12 @@ class Case:
             o.a["mu"][:] = mu
             o.a["lam"][:] = lam
             o.a["yield_stress"][:] = np.float32(p["ys"])
+            o.model.plastic_viscosity[10] = np.float32(p["eta"])
             if which == "v0":
                 o.a["v"][:] = (o.a["v"].astype(np.float64) + sg * rel * direction).astype(np.float32)
             o.step(DT, K)
             return _loss_np(o.a["x"], o.a["v"])
-        h = rel if which == "v0" else rel * {"E": self.E, "nu": self.nu, "ys": self.ys}[which]
+        h = rel if which == "v0" else rel * base[which]
         return (at(1.0) - at(-1.0)) / (2.0 * h)
 
 
@@ -168,14 +170,18 @@ def test_gradients_match_oracle_finite_differences(cuda, oracle_lib, key, kw):
     ("bingham_soft", {"cup": True}, ("eta", "ys")),
     ("jelly", {"sphere": True}, ("E", "nu")),
 ])
-def test_fluid_cup_and_sdf_gradients_match_finite_differences(cuda, key, kw, params):
+def test_fluid_cup_and_sdf_gradients_match_finite_differences(cuda, oracle_lib, key, kw, params):
     """The Newtonian family (viscosity, Bingham yield) in a revolved-SDF cup, and
-    jelly on a mesh-SDF sphere."""
+    jelly on a mesh-SDF sphere. The fluid parameters move the loss by ~1e-5 per
+    percent, the size of the GPU forward's atomic-order noise, so they are checked
+    against deterministic oracle differences at 10 % (the response is linear in
+    them to well under 1 % over 4 substeps)."""
     import torch
     c = Case(key, **kw)
     g = c.grads()
     for p in params:
-        _close(g[p], c.fd_gpu(p), 0.02, f"{key} d/d{p}")
+        fd = c.fd_oracle(oracle_lib.OracleSolver, p, rel=1e-1) if p in ("eta", "ys") else c.fd_gpu(p)
+        _close(g[p], fd, 0.02, f"{key} d/d{p}")
     d = torch.randn(c.v0.shape, generator=torch.Generator().manual_seed(5)).to(c.dev)
     d = d / d.norm()
     _close(float((g["v0"] * d).sum()), c.fd_gpu("v0", rel=1e-1, direction=d), 0.02, f"{key} d/dv0")
