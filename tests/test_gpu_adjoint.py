@@ -25,12 +25,17 @@ N, NG = 1500, 32
 # tops out at eta + tau_y / 0.02 = 102 Pa s, inside the explicit viscous limit)
 MATS = dict(MATERIALS, bingham_soft=lambda: __import__("mpm_engine_gb300").newtonian(
     eta=2.0, density=1000.0, bulk_modulus=2.0e5).with_yield(2.0))
+# yield-dominated Bingham (eta_app up to 500 Pa s): explicit limit needs dt <= 5e-5
+MATS["bingham_yield"] = lambda: __import__("mpm_engine_gb300").newtonian(
+    eta=0.2, density=1000.0, bulk_modulus=2.0e5).with_yield(10.0)
+DT_OF = {"bingham_yield": 4.0e-5}
 
 
-def _scene(cls, key, floor="sticky", plate=False, cup=False, sphere=False):
+def _scene(cls, key, floor="sticky", plate=False, cup=False, sphere=False, drop=0.0):
     from mpm_engine_gb300.geometry import analytic_sdf
     from scenes_lib import SMALL_CUP
     pts, vol = blob(n=N, lo=0.12, size=0.08)
+    pts[:, 2] -= drop
     s = make(cls, NG, 0.4).load_particles(pts, vol)
     s.set_material(MATS[key](), g=[0.0, 0.0, -9.8])
     dx = 0.4 / NG
@@ -44,7 +49,7 @@ def _scene(cls, key, floor="sticky", plate=False, cup=False, sphere=False):
     if plate:
         s.add_box((0.16, 0.16, 0.20 + dx), (0.06, 0.06, dx), velocity=(0.0, 0.0, -0.5))
     s.set_v(spin_velocity(pts, lin=(0.3, 0.2, -1.0), omega=(0.0, 2.0, 5.0)))
-    s.step(DT, PRE)
+    s.step(DT_OF.get(key, DT), PRE)
     return s
 
 
@@ -63,6 +68,7 @@ class Case:
         import torch
         from mpm_engine_gb300 import Solver, adjoint
         self.key, self.kw = key, kw
+        self.dt = DT_OF.get(key, DT)
         self.s = _scene(Solver, key, **kw)
         self.snap = adjoint._snapshot(self.s)
         self.state = self.s.export_state()
@@ -79,7 +85,7 @@ class Case:
         from mpm_engine_gb300 import adjoint
         adjoint._restore(self.s, self.snap)
         eta = self.eta if eta is None else eta
-        x, v = adjoint.rollout(self.s, DT, K, v0=v0, E=E, nu=nu, yield_stress=ys, viscosity=eta,
+        x, v = adjoint.rollout(self.s, self.dt, K, v0=v0, E=E, nu=nu, yield_stress=ys, viscosity=eta,
                                checkpoint_every=EVERY)
         L = (x.double() * self.a).sum() + (v.double() * self.b).sum()
         if grad:
@@ -124,7 +130,7 @@ class Case:
             o.model.plastic_viscosity[10] = np.float32(p["eta"])
             if which == "v0":
                 o.a["v"][:] = (o.a["v"].astype(np.float64) + sg * rel * direction).astype(np.float32)
-            o.step(DT, K)
+            o.step(self.dt, K)
             return _loss_np(o.a["x"], o.a["v"])
         h = rel if which == "v0" else rel * base[which]
         return (at(1.0) - at(-1.0)) / (2.0 * h)
@@ -166,22 +172,24 @@ def test_gradients_match_oracle_finite_differences(cuda, oracle_lib, key, kw):
 
 
 @pytest.mark.parametrize("key,kw,params", [
-    ("newtonian", {"cup": True}, ("eta",)),
-    ("bingham_soft", {"cup": True}, ("eta", "ys")),
-    ("jelly", {"sphere": True}, ("E", "nu")),
+    ("newtonian", {"cup": True}, {"eta": (1e-1, 0.02)}),
+    ("bingham_yield", {"cup": True, "drop": 0.0045}, {"ys": (3e-2, 0.10)}),
+    ("jelly", {"sphere": True}, {"E": (1e-2, 0.02), "nu": (1e-2, 0.02)}),
 ])
 def test_fluid_cup_and_sdf_gradients_match_finite_differences(cuda, oracle_lib, key, kw, params):
     """The Newtonian family (viscosity, Bingham yield) in a revolved-SDF cup, and
     jelly on a mesh-SDF sphere. The fluid parameters move the loss by ~1e-5 per
     percent, the size of the GPU forward's atomic-order noise, so they are checked
-    against deterministic oracle differences at 10 % (the response is linear in
-    them to well under 1 % over 4 substeps)."""
+    against deterministic oracle differences. Even those carry fp32 noise here (the
+    stiff equation of state turns rounding of J into pressure noise, and contact
+    branches flip): oracle differences of the Bingham yield derivative spread by
+    about 5 % between 1 % and 3 % steps, hence its 10 % bound."""
     import torch
     c = Case(key, **kw)
     g = c.grads()
-    for p in params:
-        fd = c.fd_oracle(oracle_lib.OracleSolver, p, rel=1e-1) if p in ("eta", "ys") else c.fd_gpu(p)
-        _close(g[p], fd, 0.02, f"{key} d/d{p}")
+    for p, (rel, tol) in params.items():
+        fd = c.fd_oracle(oracle_lib.OracleSolver, p, rel=rel) if p in ("eta", "ys") else c.fd_gpu(p, rel=rel)
+        _close(g[p], fd, tol, f"{key} d/d{p}")
     d = torch.randn(c.v0.shape, generator=torch.Generator().manual_seed(5)).to(c.dev)
     d = d / d.norm()
     _close(float((g["v0"] * d).sum()), c.fd_gpu("v0", rel=1e-1, direction=d), 0.02, f"{key} d/dv0")

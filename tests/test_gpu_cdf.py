@@ -184,8 +184,10 @@ def test_cdf_pour_holds_and_matches_oracle(cuda, oracle_lib):
     s, src, rcv, traj, S, dt = pour_scene(Solver, n_grid=96, glass="cdf")
     o = oracle_lib.OracleSolver.from_state(s.export_state(), 96, 0.7)
     o.threads = 16
-    # the same pose command on both sides, so their lane bookkeeping stays identical
-    c, q, v, w = traj.command(0.5, 1.0 / 60.0)
+    # the same pose command on both sides, so their lane bookkeeping stays identical;
+    # the trajectory then continues from there (a jump back would teleport the sheet)
+    t0 = 0.15
+    c, q, v, w = traj.command(t0, 1.0 / 60.0)
     for solver in (s, o):
         solver.set_cdf_pose(src, center=c, quat=(q[1], q[2], q[3], q[0]), velocity=v, omega=w)
     k = 0
@@ -195,8 +197,8 @@ def test_cdf_pour_holds_and_matches_oracle(cuda, oracle_lib):
         k += 10
         assert_close(s, o, k * 2e-5, f"cdf pour after {k} substeps")
         _check_grids(s, o, f"cdf pour after {k} substeps")
-    for i in range(6):
-        c, q, v, w = traj.command(i / 60.0, 1.0 / 60.0)
+    for i in range(1, 7):
+        c, q, v, w = traj.command(t0 + i / 60.0, 1.0 / 60.0)
         s.set_cdf_pose(src, center=c, quat=(q[1], q[2], q[3], q[0]), velocity=v, omega=w)
         s.step(dt, S)
     prof = GlassProfile()
