@@ -192,7 +192,13 @@ def test_fluid_cup_and_sdf_gradients_match_finite_differences(cuda, oracle_lib, 
         _close(g[p], fd, tol, f"{key} d/d{p}")
     d = torch.randn(c.v0.shape, generator=torch.Generator().manual_seed(5)).to(c.dev)
     d = d / d.norm()
-    _close(float((g["v0"] * d).sum()), c.fd_gpu("v0", rel=1e-1, direction=d), 0.02, f"{key} d/dv0")
+    if key.startswith("bingham"):
+        # a yield-dominated stress behaves like tau_y D/|D| at low strain rate, so the
+        # velocity step must stay small: 1e-2 m/s against the deterministic oracle
+        fd = c.fd_oracle(oracle_lib.OracleSolver, "v0", rel=1e-2, direction=d.double().cpu().numpy())
+    else:
+        fd = c.fd_gpu("v0", rel=1e-1, direction=d)
+    _close(float((g["v0"] * d).sum()), fd, 0.02, f"{key} d/dv0")
 
 
 def test_long_rollout_checkpoint_interval_does_not_change_gradients(cuda):
