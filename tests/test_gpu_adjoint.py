@@ -195,10 +195,13 @@ def test_fluid_cup_and_sdf_gradients_match_finite_differences(cuda, oracle_lib, 
     if key.startswith("bingham"):
         # a yield-dominated stress behaves like tau_y D/|D| at low strain rate, so the
         # velocity step must stay small: 1e-2 m/s against the deterministic oracle
+        # (its fp32 differences spread by about 5 %, as for the yield derivative)
         fd = c.fd_oracle(oracle_lib.OracleSolver, "v0", rel=1e-2, direction=d.double().cpu().numpy())
+        tol = 0.05
     else:
         fd = c.fd_gpu("v0", rel=1e-1, direction=d)
-    _close(float((g["v0"] * d).sum()), fd, 0.02, f"{key} d/dv0")
+        tol = 0.02
+    _close(float((g["v0"] * d).sum()), fd, tol, f"{key} d/dv0")
 
 
 def test_long_rollout_checkpoint_interval_does_not_change_gradients(cuda):
