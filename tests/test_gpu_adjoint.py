@@ -173,7 +173,7 @@ def test_gradients_match_oracle_finite_differences(cuda, oracle_lib, key, kw):
 
 @pytest.mark.parametrize("key,kw,params", [
     ("newtonian", {"cup": True}, {"eta": (1e-1, 0.02)}),
-    ("bingham_yield", {"cup": True, "drop": 0.0045}, {"ys": (3e-2, 0.10)}),
+    ("bingham_yield", {"cup": True, "drop": 0.0045}, {"ys": (3e-2, 0.15)}),
     ("jelly", {"sphere": True}, {"E": (1e-2, 0.02), "nu": (1e-2, 0.02)}),
 ])
 def test_fluid_cup_and_sdf_gradients_match_finite_differences(cuda, oracle_lib, key, kw, params):
@@ -183,7 +183,9 @@ def test_fluid_cup_and_sdf_gradients_match_finite_differences(cuda, oracle_lib, 
     against deterministic oracle differences. Even those carry fp32 noise here (the
     stiff equation of state turns rounding of J into pressure noise, and contact
     branches flip): oracle differences of the Bingham yield derivative spread by
-    about 5 % between 1 % and 3 % steps, hence its 10 % bound."""
+    about 5 % between 1 % and 3 % steps and by about 10 % between pre-rolled states
+    (the pre-roll runs on the GPU, whose float atomics reorder), hence its 15 %
+    bound; it pins sign and magnitude, not the last digits."""
     import torch
     c = Case(key, **kw)
     g = c.grads()
