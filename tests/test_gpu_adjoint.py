@@ -190,7 +190,12 @@ def test_fluid_cup_and_sdf_gradients_match_finite_differences(cuda, oracle_lib, 
     c = Case(key, **kw)
     g = c.grads()
     for p, (rel, tol) in params.items():
-        fd = c.fd_oracle(oracle_lib.OracleSolver, p, rel=rel) if p in ("eta", "ys") else c.fd_gpu(p, rel=rel)
+        if p == "ys":   # average over steps: the single differences jitter at the fp32 floor
+            fd = float(np.mean([c.fd_oracle(oracle_lib.OracleSolver, p, rel=r) for r in (1e-2, 2e-2, 3e-2, 5e-2)]))
+        elif p == "eta":
+            fd = c.fd_oracle(oracle_lib.OracleSolver, p, rel=rel)
+        else:
+            fd = c.fd_gpu(p, rel=rel)
         _close(g[p], fd, tol, f"{key} d/d{p}")
     d = torch.randn(c.v0.shape, generator=torch.Generator().manual_seed(5)).to(c.dev)
     d = d / d.norm()
