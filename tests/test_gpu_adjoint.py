@@ -25,13 +25,17 @@ N, NG = 1500, 32
 # tops out at eta + tau_y / 0.02 = 102 Pa s, inside the explicit viscous limit)
 MATS = dict(MATERIALS, bingham_soft=lambda: __import__("mpm_engine_gb300").newtonian(
     eta=2.0, density=1000.0, bulk_modulus=2.0e5).with_yield(2.0))
-# yield-dominated Bingham (eta_app up to 500 Pa s): explicit limit needs dt <= 5e-5
+# fluids for a free, straining blob: a soft equation of state keeps pressure rounding
+# (K (J^-1.1 - 1) near J = 1) below the viscous and yield stresses under test; the
+# Bingham one is yield-dominated (eta_app up to 500 Pa s, explicit limit 5e-5 s)
+MATS["newtonian_soft"] = lambda: __import__("mpm_engine_gb300").newtonian(
+    eta=2.0, density=1000.0, bulk_modulus=2.0e4)
 MATS["bingham_yield"] = lambda: __import__("mpm_engine_gb300").newtonian(
-    eta=0.2, density=1000.0, bulk_modulus=2.0e5).with_yield(10.0)
+    eta=0.2, density=1000.0, bulk_modulus=2.0e4).with_yield(10.0)
 DT_OF = {"bingham_yield": 4.0e-5}
 
 
-def _scene(cls, key, floor="sticky", plate=False, cup=False, sphere=False, drop=0.0):
+def _scene(cls, key, floor="sticky", plate=False, cup=False, sphere=False, drop=0.0, free=False):
     from mpm_engine_gb300.geometry import analytic_sdf
     from scenes_lib import SMALL_CUP
     pts, vol = blob(n=N, lo=0.12, size=0.08)
@@ -39,7 +43,9 @@ def _scene(cls, key, floor="sticky", plate=False, cup=False, sphere=False, drop=
     s = make(cls, NG, 0.4).load_particles(pts, vol)
     s.set_material(MATS[key](), g=[0.0, 0.0, -9.8])
     dx = 0.4 / NG
-    if cup:       # the blob lands on the cup's floor and presses its walls
+    if free:      # no contact within the rollout: a straining flow loads the stress
+        pass
+    elif cup:     # the blob lands on the cup's floor and presses its walls
         s.add_cup(SMALL_CUP, (0.16, 0.16, 0.155), friction=0.3)
     elif sphere:  # the blob lands on a mesh-SDF sphere
         s.add_sdf_collider(analytic_sdf("sphere", radius=0.03), center=(0.16, 0.16, 0.095), friction=0.3)
@@ -48,7 +54,11 @@ def _scene(cls, key, floor="sticky", plate=False, cup=False, sphere=False, drop=
     s.add_domain_walls()
     if plate:
         s.add_box((0.16, 0.16, 0.20 + dx), (0.06, 0.06, dx), velocity=(0.0, 0.0, -0.5))
-    s.set_v(spin_velocity(pts, lin=(0.3, 0.2, -1.0), omega=(0.0, 2.0, 5.0)))
+    vel = spin_velocity(pts, lin=(0.3, 0.2, -1.0), omega=(0.0, 2.0, 5.0))
+    if free:      # plus shear and extension, 4/s
+        A = np.array([[2.0, 2.0, 0.0], [2.0, -2.0, 1.0], [0.0, 1.0, 0.0]], np.float32)
+        vel = vel + (pts - pts.mean(axis=0)) @ A.T
+    s.set_v(vel.astype(np.float32))
     s.step(DT_OF.get(key, DT), PRE)
     return s
 
@@ -171,43 +181,32 @@ def test_gradients_match_oracle_finite_differences(cuda, oracle_lib, key, kw):
            f"{key} d/dv0 (oracle)")
 
 
-@pytest.mark.parametrize("key,kw,params", [
-    ("newtonian", {"cup": True}, {"eta": (1e-1, 0.02)}),
-    ("bingham_yield", {"cup": True, "drop": 0.0045}, {"ys": (3e-2, 0.15)}),
-    ("jelly", {"sphere": True}, {"E": (1e-2, 0.02), "nu": (1e-2, 0.02)}),
+@pytest.mark.parametrize("key,kw,params,tol", [
+    ("jelly", {"cup": True}, ("E", "nu"), 0.02),
+    ("jelly", {"sphere": True}, ("E", "nu"), 0.02),
+    ("newtonian_soft", {"free": True}, ("eta",), 0.03),
+    ("bingham_yield", {"free": True}, ("ys",), 0.05),
 ])
-def test_fluid_cup_and_sdf_gradients_match_finite_differences(cuda, oracle_lib, key, kw, params):
-    """The Newtonian family (viscosity, Bingham yield) in a revolved-SDF cup, and
-    jelly on a mesh-SDF sphere. The fluid parameters move the loss by ~1e-5 per
-    percent, the size of the GPU forward's atomic-order noise, so they are checked
-    against deterministic oracle differences. Even those carry fp32 noise here (the
-    stiff equation of state turns rounding of J into pressure noise, and contact
-    branches flip): oracle differences of the Bingham yield derivative spread by
-    about 5 % between 1 % and 3 % steps and by about 10 % between pre-rolled states
-    (the pre-roll runs on the GPU, whose float atomics reorder), hence its 15 %
-    bound; it pins sign and magnitude, not the last digits."""
+def test_fluid_cup_and_sdf_gradients_match_finite_differences(cuda, oracle_lib, key, kw, params, tol):
+    """The revolved-SDF cup and mesh-SDF colliders with a jelly blob landing on them,
+    and the Newtonian family (viscosity, Bingham yield) in a free straining flow.
+    A fluid landing in a cup is chaotic at fp32 level (stiff pressure and contact
+    branches scatter its finite differences by 10-20 % from run to run), so the
+    fluid laws are checked without contact; their parameters move the loss by about
+    1e-5 per percent, near the GPU's atomic-order noise, so they are checked against
+    deterministic oracle differences. Their fp32 differences spread by about 2 %
+    (Newtonian viscosity) and 3-6 % (Bingham yield) across step sizes, which sets
+    those bounds; the viscosity of the yield-dominated fluid is too weak an input
+    (eta << tau_y / strain rate) to resolve and is left to the Newtonian case."""
     import torch
     c = Case(key, **kw)
     g = c.grads()
-    for p, (rel, tol) in params.items():
-        if p == "ys":   # average over steps: the single differences jitter at the fp32 floor
-            fd = float(np.mean([c.fd_oracle(oracle_lib.OracleSolver, p, rel=r) for r in (1e-2, 2e-2, 3e-2, 5e-2)]))
-        elif p == "eta":
-            fd = c.fd_oracle(oracle_lib.OracleSolver, p, rel=rel)
-        else:
-            fd = c.fd_gpu(p, rel=rel)
+    for p in params:
+        fd = c.fd_oracle(oracle_lib.OracleSolver, p, rel=3e-2) if p in ("eta", "ys") else c.fd_gpu(p)
         _close(g[p], fd, tol, f"{key} d/d{p}")
     d = torch.randn(c.v0.shape, generator=torch.Generator().manual_seed(5)).to(c.dev)
     d = d / d.norm()
-    if key.startswith("bingham"):
-        # a yield-dominated stress behaves like tau_y D/|D| at low strain rate, so the
-        # velocity step must stay small: 1e-2 m/s against the deterministic oracle
-        # (its fp32 differences spread by about 5 %, as for the yield derivative)
-        fd = c.fd_oracle(oracle_lib.OracleSolver, "v0", rel=1e-2, direction=d.double().cpu().numpy())
-        tol = 0.05
-    else:
-        fd = c.fd_gpu("v0", rel=1e-1, direction=d)
-        tol = 0.02
+    fd = c.fd_oracle(oracle_lib.OracleSolver, "v0", rel=1e-2, direction=d.double().cpu().numpy())
     _close(float((g["v0"] * d).sum()), fd, tol, f"{key} d/dv0")
 
 
