@@ -1169,63 +1169,58 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
     if (head) s_seg[off + __popc(bal & ((1u << lane) - 1u))] = t;
     if (t == 0) s_seg[total] = kTileThreads;
     __syncthreads();
-    // ---- runs: lane = (particle group g, node line (i,j)); each lane sums three
-    // nodes k = 0..2 of its line for particles q0+g, q0+g+3, ...; the three groups
-    // are folded with shuffles and lanes 0..8 deposit
+    // ---- runs: a warp takes three runs at once, one per 9-lane group; lane
+    // (group, node line (i,j)) sums the three nodes k = 0..2 of its line over its
+    // run's particles and deposits them itself
     const int g3 = lane / 9, li = (lane % 9) / 3, lj = lane % 3;
     const float fi = (float)li, fj = (float)lj;
-    for (int sg = warp; sg < total; sg += kTileThreads / 32) {
-        const int q0 = s_seg[sg], q1 = s_seg[sg + 1];
-        const int key = s_key[q0];
-        if (key < 0) continue;   // uniform across the warp
+    for (int sg0 = warp * 3; sg0 < total; sg0 += 3 * (kTileThreads / 32)) {
+        const int sg = sg0 + g3;
+        int q0 = 0, q1 = 0, key = -1;
+        if (lane < 27 && sg < total) {
+            q0 = s_seg[sg];
+            q1 = s_seg[sg + 1];
+            key = s_key[q0];
+        }
+        if (key < 0) q1 = q0;   // dead slot or idle lane: no particles
         float acc[3][4];
 #pragma unroll
         for (int kk = 0; kk < 3; ++kk) acc[kk][0] = acc[kk][1] = acc[kk][2] = acc[kk][3] = 0.f;
-        if (lane < 27) {
 #pragma unroll 2
-            for (int q = q0 + g3; q < q1; q += 3) {
-                const float *r = s_mem + q * kRec;
-                const float wxi = r[li], wyj = r[3 + lj], dwxi = r[6 + li], dwyj = r[9 + lj];
-                const float4 *r4 = reinterpret_cast<const float4 *>(r);
-                float inv[28];
+        for (int q = q0; q < q1; ++q) {
+            const float *r = s_mem + q * kRec;
+            const float wxi = r[li], wyj = r[3 + lj], dwxi = r[6 + li], dwyj = r[9 + lj];
+            const float4 *r4 = reinterpret_cast<const float4 *>(r);
+            float inv[28];
 #pragma unroll
-                for (int h = 0; h < 7; ++h) {
-                    const float4 f4 = r4[3 + h];
-                    inv[4 * h] = f4.x; inv[4 * h + 1] = f4.y; inv[4 * h + 2] = f4.z; inv[4 * h + 3] = f4.w;
-                }
-                // inv[i] = rec[12 + i]
-                const float u = wxi * wyj, ux = dwxi * wyj, uy = wxi * dwyj;
-                const float wz0 = inv[0], wz1 = inv[1], wz2 = inv[2], dz0 = inv[4], dz1 = inv[5], dz2 = inv[6];
-                const float m = inv[3];
-                float P[3], Q[3], R[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    P[a] = u * (inv[7 + a] + inv[10 + 3 * a] * fi + inv[11 + 3 * a] * fj) + inv[19 + 3 * a] * ux +
-                           inv[20 + 3 * a] * uy;
-                    Q[a] = u * inv[12 + 3 * a];
-                    R[a] = u * inv[21 + 3 * a];
-                }
-                const float um = u * m;
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    acc[0][a] += wz0 * P[a] + dz0 * R[a];
-                    acc[1][a] += wz1 * (P[a] + Q[a]) + dz1 * R[a];
-                    acc[2][a] += wz2 * (P[a] + 2.0f * Q[a]) + dz2 * R[a];
-                }
-                acc[0][3] += wz0 * um;
-                acc[1][3] += wz1 * um;
-                acc[2][3] += wz2 * um;
+            for (int h = 0; h < 7; ++h) {
+                const float4 f4 = r4[3 + h];
+                inv[4 * h] = f4.x; inv[4 * h + 1] = f4.y; inv[4 * h + 2] = f4.z; inv[4 * h + 3] = f4.w;
             }
+            // inv[i] = rec[12 + i]
+            const float u = wxi * wyj, ux = dwxi * wyj, uy = wxi * dwyj;
+            const float wz0 = inv[0], wz1 = inv[1], wz2 = inv[2], dz0 = inv[4], dz1 = inv[5], dz2 = inv[6];
+            const float m = inv[3];
+            float P[3], Q[3], R[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                P[a] = u * (inv[7 + a] + inv[10 + 3 * a] * fi + inv[11 + 3 * a] * fj) + inv[19 + 3 * a] * ux +
+                       inv[20 + 3 * a] * uy;
+                Q[a] = u * inv[12 + 3 * a];
+                R[a] = u * inv[21 + 3 * a];
+            }
+            const float um = u * m;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                acc[0][a] += wz0 * P[a] + dz0 * R[a];
+                acc[1][a] += wz1 * (P[a] + Q[a]) + dz1 * R[a];
+                acc[2][a] += wz2 * (P[a] + 2.0f * Q[a]) + dz2 * R[a];
+            }
+            acc[0][3] += wz0 * um;
+            acc[1][3] += wz1 * um;
+            acc[2][3] += wz2 * um;
         }
-#pragma unroll
-        for (int kk = 0; kk < 3; ++kk)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                float x9 = __shfl_down_sync(0xffffffffu, acc[kk][c], 9);
-                float x18 = __shfl_down_sync(0xffffffffu, acc[kk][c], 18);
-                acc[kk][c] += x9 + x18;
-            }
-        if (lane < 9) {
+        if (q1 > q0) {
             const int bx = key >> 20, by = (key >> 10) & 1023, bz = key & 1023;
             const int gx = bx + li, gy = by + lj;
             int marked = -1;   // 4^3 block (z index) this lane marked last
