@@ -970,7 +970,11 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
 constexpr int kTileThreads = 256;
 constexpr int kGatherCap = 1536;          // nodes in the shared gather tile (24 KB)
 constexpr int kRec = 40;                  // floats per particle scatter record (10 float4)
-constexpr int kSmemFloats = (kGatherCap * 4 > kTileThreads * kRec) ? kGatherCap * 4 : kTileThreads * kRec;
+// record stride in shared memory: 44 floats = 176 B, so the 16-byte stores of eight
+// consecutive lanes land on disjoint bank groups (a 160 B stride pairs them up)
+constexpr int kRecStride = 44;
+constexpr int kSmemFloats =
+    (kGatherCap * 4 > kTileThreads * kRecStride) ? kGatherCap * 4 : kTileThreads * kRecStride;
 
 struct TileBox {
     int lo[3], e[3];
@@ -1147,7 +1151,7 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
             rec[22 + 3 * a] = c0; rec[23 + 3 * a] = c1; rec[24 + 3 * a] = c2;
             rec[31 + 3 * a] = fs * S[3 * a]; rec[32 + 3 * a] = fs * S[3 * a + 1]; rec[33 + 3 * a] = fs * S[3 * a + 2];
         }
-        float4 *dst = reinterpret_cast<float4 *>(s_mem + t * kRec);
+        float4 *dst = reinterpret_cast<float4 *>(s_mem + t * kRecStride);
 #pragma unroll
         for (int q = 0; q < kRec / 4; ++q) dst[q] = make_float4(rec[4 * q], rec[4 * q + 1], rec[4 * q + 2], rec[4 * q + 3]);
         s_key[t] = (s.b[0] << 20) | (s.b[1] << 10) | s.b[2];   // n_grid <= 1024 on this path
@@ -1188,7 +1192,7 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
         for (int kk = 0; kk < 3; ++kk) acc[kk][0] = acc[kk][1] = acc[kk][2] = acc[kk][3] = 0.f;
 #pragma unroll 2
         for (int q = q0; q < q1; ++q) {
-            const float *r = s_mem + q * kRec;
+            const float *r = s_mem + q * kRecStride;
             const float wxi = r[li], wyj = r[3 + lj], dwxi = r[6 + li], dwyj = r[9 + lj];
             const float4 *r4 = reinterpret_cast<const float4 *>(r);
             float inv[28];
