@@ -1025,10 +1025,15 @@ __device__ __forceinline__ void bspline_o(float fx, int o, float &w, float &dw) 
     dw = (o == 0) ? -t0 : ((o == 1) ? -2.0f * t1 : t2);
 }
 
-template <bool SOLIDS, int MINB>
+// CDF adds the CPIC branches of the direct kernel: the gather reads the ghost
+// velocity at nodes incompatible with the particle, and scatter runs are keyed by
+// (base cell, particle tag) so each run deposits under one mask, its blocked nodes
+// becoming the owner lane's reaction.
+template <bool SOLIDS, int MINB, bool CDF = false>
 __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, int mode) {
     __shared__ __align__(16) float s_mem[kSmemFloats];
     __shared__ int s_key[kTileThreads];
+    __shared__ int s_pc[CDF ? kTileThreads : 1];
     __shared__ int s_seg[kTileThreads + 1];
     __shared__ int s_wcnt[kTileThreads / 32];
     __shared__ int s_red[kTileThreads / 32][6];
@@ -1045,6 +1050,7 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
     if (live) fld_load<true, 3>(k.x, k.n, p, x);
     float v[3] = {0.f, 0.f, 0.f}, C[9], L[9], Ft[9], S[9];
     bool gathered = false;
+    int ptag = 0;   // CPIC particle tag carried from the gather into the scatter
     if (mode & PASS_G2P) {
         bool want = live && mat != 7 && mat != 8;
         Stencil s;
@@ -1053,6 +1059,27 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
             set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
             want = false;
             live = false;
+        }
+        // CPIC: tag from the previous stamp (persisted), and the ghost velocity
+        CdfScan cs;
+        float4 g4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (CDF && want) {
+            int pc = 0;
+            if (cdf_near(k, s)) {
+                cdf_scan<true>(k, s, k.ctag_prev, k.cd_prev, cs);
+                float old;
+                fld_load<true, 1>(reinterpret_cast<float *>(k.ptag), k.n, p, &old);
+                pc = cdf_persist(__float_as_int(old), cdf_vote_tag(cs));
+            }
+            const float pcf = __int_as_float(pc);
+            fld_store<true, 1>(reinterpret_cast<float *>(k.ptag), k.n, p, &pcf);
+            ptag = pc;
+            if (pc != 0) {
+                float vp[3], gh[3];
+                fld_load<true, 3>(k.v, k.n, p, vp);
+                cdf_ghost(k, cs, x, vp, pc, k.grav, gh);
+                g4 = make_float4(gh[0], gh[1], gh[2], 0.0f);
+            }
         }
         TileBox box;
         block_box(s.b, want, box, s_red);
@@ -1066,13 +1093,24 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
             __syncthreads();
             if (want) {
                 const int o0 = s.b[0] - box.lo[0], o1 = s.b[1] - box.lo[1], o2 = s.b[2] - box.lo[2];
-                g2p_core(k, s, [&](int i, int j, int kk) {
-                    return s_tile[((o0 + i) * box.e[1] + (o1 + j)) * box.e[2] + (o2 + kk)];
-                }, v, C, L);
+                if (CDF && ptag != 0)
+                    g2p_core(k, s, [&](int i, int j, int kk) {
+                        return cdf_incompatible(ptag, cs.tag[(i * 3 + j) * 3 + kk])
+                                   ? g4 : s_tile[((o0 + i) * box.e[1] + (o1 + j)) * box.e[2] + (o2 + kk)];
+                    }, v, C, L);
+                else
+                    g2p_core(k, s, [&](int i, int j, int kk) {
+                        return s_tile[((o0 + i) * box.e[1] + (o1 + j)) * box.e[2] + (o2 + kk)];
+                    }, v, C, L);
             }
             __syncthreads();
         } else if (want) {
-            g2p_core(k, s, [&](int i, int j, int kk) { return global_fetch(k, s, i, j, kk); }, v, C, L);
+            if (CDF && ptag != 0)
+                g2p_core(k, s, [&](int i, int j, int kk) {
+                    return cdf_incompatible(ptag, cs.tag[(i * 3 + j) * 3 + kk]) ? g4 : global_fetch(k, s, i, j, kk);
+                }, v, C, L);
+            else
+                g2p_core(k, s, [&](int i, int j, int kk) { return global_fetch(k, s, i, j, kk); }, v, C, L);
         }
         if (want) {
             g2p_finish<true>(k, p, x, v, L, Ft);
@@ -1104,6 +1142,11 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
         if (!gathered) {
             fld_load<true, 3>(k.v, k.n, p, v);
             fld_load<true, 9>(k.C, k.n, p, C);
+            if (CDF) {
+                float old;
+                fld_load<true, 1>(reinterpret_cast<float *>(k.ptag), k.n, p, &old);
+                ptag = __float_as_int(old);
+            }
         }
     }
     Stencil s;
@@ -1113,6 +1156,13 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
         set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
         want = false;
     }
+    int pcs = 0;   // CPIC tag of this particle at the current stamp
+    if (CDF && want && cdf_near(k, s)) {
+        CdfScan cs;
+        cdf_scan<false>(k, s, k.ctag, k.cd, cs);
+        pcs = cdf_persist(ptag, cdf_vote_tag(cs));
+    }
+    if (CDF) s_pc[t] = pcs;
     // ---- scatter record (40 floats, 16-byte aligned): [0..11] the x and y weights and
     // derivatives a lane indexes by its node line (wx[3], wy[3], dwx[3], dwy[3]);
     // [12..39] what every lane of a particle reads, packed for seven float4 loads:
@@ -1159,8 +1209,8 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
         s_key[t] = -1 - t;   // a dead slot forms its own, skipped run
     }
     __syncthreads();
-    // ---- runs of equal base node: compact the run heads
-    const bool head = (t == 0) || (s_key[t] != s_key[t - 1]);
+    // ---- runs of equal base node (and CPIC tag): compact the run heads
+    const bool head = (t == 0) || (s_key[t] != s_key[t - 1]) || (CDF && s_pc[t] != s_pc[t - 1]);
     const unsigned bal = __ballot_sync(0xffffffffu, head);
     if (lane == 0) s_wcnt[warp] = __popc(bal);
     __syncthreads();
@@ -1227,9 +1277,28 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
         if (q1 > q0) {
             const int bx = key >> 20, by = (key >> 10) & 1023, bz = key & 1023;
             const int gx = bx + li, gy = by + lj;
+            const int pcr = CDF ? s_pc[q0] : 0;
             int marked = -1;   // 4^3 block (z index) this lane marked last
 #pragma unroll
             for (int kk = 0; kk < 3; ++kk) {
+                if (CDF && pcr != 0) {
+                    const size_t id = ((size_t)gx * k.ng + gy) * k.ng + (bz + kk);
+                    const int nt = __ldg(k.ctag + id);
+                    if (cdf_incompatible(pcr, nt)) {   // blocked: the owner lane's reaction
+                        const int own = (nt >> kCdfOwnerShift) & 3;
+                        const float *cc = k.lanes.c_cur[own];
+                        const float r[3] = {(float)gx * k.dx - cc[0], (float)gy * k.dx - cc[1],
+                                            (float)(bz + kk) * k.dx - cc[2]};
+                        double *w = k.cwrench + ((size_t)blockIdx.x * GBMPM_MAX_CDF + own) * 6;
+                        atomicAdd(w + 0, (double)acc[kk][0]);
+                        atomicAdd(w + 1, (double)acc[kk][1]);
+                        atomicAdd(w + 2, (double)acc[kk][2]);
+                        atomicAdd(w + 3, (double)(r[1] * acc[kk][2] - r[2] * acc[kk][1]));
+                        atomicAdd(w + 4, (double)(r[2] * acc[kk][0] - r[0] * acc[kk][2]));
+                        atomicAdd(w + 5, (double)(r[0] * acc[kk][1] - r[1] * acc[kk][0]));
+                        continue;
+                    }
+                }
                 if (acc[kk][0] != 0.f || acc[kk][1] != 0.f || acc[kk][2] != 0.f || acc[kk][3] != 0.f) {
                     const int gz = bz + kk;
                     atomicAdd(k.gmv + ((size_t)gx * k.ng + gy) * k.ng + gz,
@@ -2145,6 +2214,13 @@ bool has_solids(const gbmpm_model &m) {
 }
 
 void launch_particles(gbmpm_engine *e, const PK &k, int mode, bool tiled, cudaStream_t s) {
+    if (tiled && k.cdf_on) {
+        int grid = std::max(1, (k.n + kTileThreads - 1) / kTileThreads);
+        if (has_solids(e->M)) k_particles_tiled<true, 2, true><<<grid, kTileThreads, 0, s>>>(k, mode);
+        else k_particles_tiled<false, 2, true><<<grid, kTileThreads, 0, s>>>(k, mode);
+        e->launches++;
+        return;
+    }
     if (tiled) {
         int grid = std::max(1, (k.n + kTileThreads - 1) / kTileThreads);
         const bool solids = has_solids(e->M);
@@ -2178,6 +2254,7 @@ cudaError_t ensure_ws(gbmpm_engine *e) {
         {reinterpret_cast<float *>(P.material), 1, 0, reinterpret_cast<float **>(&W.material)},
         {reinterpret_cast<float *>(P.selection), 1, 0, reinterpret_cast<float **>(&W.selection)},
         {cov ? P.cov : nullptr, 6, 1, &W.cov},
+        {e->cdf.n > 0 ? reinterpret_cast<float *>(P.cdf_tag) : nullptr, 1, 1, reinterpret_cast<float **>(&W.cdf_tag)},
     };
     size_t total = 0;
     for (const Spec &sp : spec) if (sp.ext) total += (size_t)sp.w * n;
@@ -2539,7 +2616,7 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
     const int *perm = nullptr;
     if (reorder) timed(5, [&] { perm = record_ws_begin(e, s); });
     const gbmpm_particles &P = reorder ? e->W : e->P;
-    const bool cdf = e->cdf.n > 0 && !reorder;
+    const bool cdf = e->cdf.n > 0;
     double tc = t0;
     for (int sub = 0; sub < S; ++sub) {
         int list = sub & 1;
@@ -2788,6 +2865,7 @@ int gbmpm_set_cdf(gbmpm_engine *e, const gbmpm_cdf *lanes, int32_t n) {
         if (moved) H.dirty[l] = true;
         if (moved || synced) { H.sync_lane(l); H.lane_prev_stale = true; }
     }
+    if (H.n == 0 && n > 0) e->ws_n = -1;   // the working set gains the particle tag
     H.n = n;
     return GBMPM_OK;
 }
@@ -2894,7 +2972,7 @@ int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32
         if (e->c_ng != e->M.n_grid) return fail(GBMPM_ERR_STATE, "CDF grids were sized for another n_grid");
         if (e->M.periodic_x) return fail(GBMPM_ERR_UNSUPPORTED, "CDF colliders do not wrap the periodic x axis");
         if (e->P.n > 0 && !e->P.cdf_tag) return fail(GBMPM_ERR_ARG, "CDF colliders need particles.cdf_tag");
-        flags &= ~(GBMPM_TICK_GRAPH | GBMPM_TICK_REORDER);
+        flags &= ~GBMPM_TICK_GRAPH;
     }
     const double t0 = time ? *time : 0.0;
     bool reorder = false;
