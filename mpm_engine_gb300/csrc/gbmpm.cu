@@ -88,6 +88,7 @@ struct PK {
     const float *cd, *cd_prev;
     int *ptag;
     double *cwrench;   // [CTA][4][6] per-CTA partial sums of the blocked-deposit reaction
+    float *ccache;     // tiled kernel: the scatter scan of each particle, SoA x5 (see k_particles_tiled)
     float grav[3];
     CdfLanes lanes;
 };
@@ -1034,6 +1035,7 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
     __shared__ __align__(16) float s_mem[kSmemFloats];
     __shared__ int s_key[kTileThreads];
     __shared__ int s_pc[CDF ? kTileThreads : 1];
+    __shared__ int s_mask[CDF ? kTileThreads : 1];
     __shared__ int s_seg[kTileThreads + 1];
     __shared__ int s_wcnt[kTileThreads / 32];
     __shared__ int s_red[kTileThreads / 32][6];
@@ -1060,24 +1062,27 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
             want = false;
             live = false;
         }
-        // CPIC: tag from the previous stamp (persisted), and the ghost velocity
-        CdfScan cs;
+        // CPIC: the gather's scan (previous stamp at this position) is the scan the
+        // last scatter made (current stamp then, at the same position), so its
+        // result comes from the cache: the tag, the mask of incompatible stencil
+        // nodes and the owner-lane sums of the ghost velocity.
+        int gmask = 0;
         float4 g4 = make_float4(0.f, 0.f, 0.f, 0.f);
         if (CDF && want) {
-            int pc = 0;
-            if (cdf_near(k, s)) {
-                cdf_scan<true>(k, s, k.ctag_prev, k.cd_prev, cs);
-                float old;
-                fld_load<true, 1>(reinterpret_cast<float *>(k.ptag), k.n, p, &old);
-                pc = cdf_persist(__float_as_int(old), cdf_vote_tag(cs));
-            }
-            const float pcf = __int_as_float(pc);
-            fld_store<true, 1>(reinterpret_cast<float *>(k.ptag), k.n, p, &pcf);
-            ptag = pc;
-            if (pc != 0) {
-                float vp[3], gh[3];
+            float old;
+            fld_load<true, 1>(reinterpret_cast<float *>(k.ptag), k.n, p, &old);
+            ptag = __float_as_int(old);
+            if (ptag != 0) {
+                CdfScan cs;
+                float cch[5], vp[3], gh[3];
+                fld_load<true, 5>(k.ccache, k.n, p, cch);
+                const int mb = __float_as_int(cch[0]);
+                gmask = mb & 0x7ffffff;
+                cs.lane_p = (mb >> 27) & 3;
+                cs.d_hat = cch[1];
+                cs.n_acc[0] = cch[2]; cs.n_acc[1] = cch[3]; cs.n_acc[2] = cch[4];
                 fld_load<true, 3>(k.v, k.n, p, vp);
-                cdf_ghost(k, cs, x, vp, pc, k.grav, gh);
+                cdf_ghost(k, cs, x, vp, ptag, k.grav, gh);
                 g4 = make_float4(gh[0], gh[1], gh[2], 0.0f);
             }
         }
@@ -1093,9 +1098,9 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
             __syncthreads();
             if (want) {
                 const int o0 = s.b[0] - box.lo[0], o1 = s.b[1] - box.lo[1], o2 = s.b[2] - box.lo[2];
-                if (CDF && ptag != 0)
+                if (CDF && gmask != 0)
                     g2p_core(k, s, [&](int i, int j, int kk) {
-                        return cdf_incompatible(ptag, cs.tag[(i * 3 + j) * 3 + kk])
+                        return ((gmask >> ((i * 3 + j) * 3 + kk)) & 1)
                                    ? g4 : s_tile[((o0 + i) * box.e[1] + (o1 + j)) * box.e[2] + (o2 + kk)];
                     }, v, C, L);
                 else
@@ -1105,9 +1110,9 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
             }
             __syncthreads();
         } else if (want) {
-            if (CDF && ptag != 0)
+            if (CDF && gmask != 0)
                 g2p_core(k, s, [&](int i, int j, int kk) {
-                    return cdf_incompatible(ptag, cs.tag[(i * 3 + j) * 3 + kk]) ? g4 : global_fetch(k, s, i, j, kk);
+                    return ((gmask >> ((i * 3 + j) * 3 + kk)) & 1) ? g4 : global_fetch(k, s, i, j, kk);
                 }, v, C, L);
             else
                 g2p_core(k, s, [&](int i, int j, int kk) { return global_fetch(k, s, i, j, kk); }, v, C, L);
@@ -1156,13 +1161,24 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
         set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
         want = false;
     }
-    int pcs = 0;   // CPIC tag of this particle at the current stamp
-    if (CDF && want && cdf_near(k, s)) {
-        CdfScan cs;
-        cdf_scan<false>(k, s, k.ctag, k.cd, cs);
-        pcs = cdf_persist(ptag, cdf_vote_tag(cs));
+    int pcs = 0, pmask = 0;   // CPIC tag at the current stamp, mask of incompatible nodes
+    if (CDF && want) {
+        if (cdf_near(k, s)) {
+            CdfScan cs;
+            cdf_scan<true>(k, s, k.ctag, k.cd, cs);
+            pcs = cdf_persist(ptag, cdf_vote_tag(cs));
+            if (pcs != 0) {
+#pragma unroll
+                for (int q = 0; q < 27; ++q) pmask |= (cdf_incompatible(pcs, cs.tag[q]) ? 1 : 0) << q;
+                const float cch[5] = {__int_as_float(pmask | (cs.lane_p << 27)), cs.d_hat, cs.n_acc[0],
+                                      cs.n_acc[1], cs.n_acc[2]};
+                fld_store<true, 5>(k.ccache, k.n, p, cch);
+            }
+        }
+        const float pcf = __int_as_float(pcs);
+        fld_store<true, 1>(reinterpret_cast<float *>(k.ptag), k.n, p, &pcf);
     }
-    if (CDF) s_pc[t] = pcs;
+    if (CDF) { s_pc[t] = pcs; s_mask[t] = pmask; }
     // ---- scatter record (40 floats, 16-byte aligned): [0..11] the x and y weights and
     // derivatives a lane indexes by its node line (wx[3], wy[3], dwx[3], dwy[3]);
     // [12..39] what every lane of a particle reads, packed for seven float4 loads:
@@ -1277,14 +1293,13 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
         if (q1 > q0) {
             const int bx = key >> 20, by = (key >> 10) & 1023, bz = key & 1023;
             const int gx = bx + li, gy = by + lj;
-            const int pcr = CDF ? s_pc[q0] : 0;
+            const int lmask = CDF ? (s_mask[q0] >> ((li * 3 + lj) * 3)) & 7 : 0;   // the run's mask, this line
             int marked = -1;   // 4^3 block (z index) this lane marked last
 #pragma unroll
             for (int kk = 0; kk < 3; ++kk) {
-                if (CDF && pcr != 0) {
-                    const size_t id = ((size_t)gx * k.ng + gy) * k.ng + (bz + kk);
-                    const int nt = __ldg(k.ctag + id);
-                    if (cdf_incompatible(pcr, nt)) {   // blocked: the owner lane's reaction
+                if (CDF && lmask != 0) {
+                    if ((lmask >> kk) & 1) {   // blocked: the owner lane's reaction
+                        const int nt = __ldg(k.ctag + ((size_t)gx * k.ng + gy) * k.ng + (bz + kk));
                         const int own = (nt >> kCdfOwnerShift) & 3;
                         const float *cc = k.lanes.c_cur[own];
                         const float r[3] = {(float)gx * k.dx - cc[0], (float)gy * k.dx - cc[1],
@@ -1543,6 +1558,94 @@ __global__ void k_cdf_stamp(CdfStamp a) {
             t = (t & ~(3 << kCdfOwnerShift)) | (a.lane << kCdfOwnerShift);
         }
         a.tag[id] = t;
+    }
+}
+
+__device__ __forceinline__ bool in_box(const CdfBox &b, int x, int y, int z) {
+    return x >= b.lo[0] && x < b.hi[0] && y >= b.lo[1] && y < b.hi[1] && z >= b.lo[2] && z < b.hi[2];
+}
+
+// One lane's stamp of node (x,y,z) into the node's running (tag, distance): the
+// arithmetic of k_cdf_stamp on registers.
+__device__ __forceinline__ void stamp_node(const CdfStamp &a, int x, int y, int z, int &t, float &d) {
+    const float rf = (float)a.res - 1.0f;
+    const float rel[3] = {__fsub_rn(__fmul_rn((float)x, a.dx), a.center[0]),
+                          __fsub_rn(__fmul_rn((float)y, a.dx), a.center[1]),
+                          __fsub_rn(__fmul_rn((float)z, a.dx), a.center[2])};
+    float body[3];
+    qrot_inv_rn(a.quat, rel, body);
+    const float f0 = __fdiv_rn(__fsub_rn(body[0], a.origin[0]), a.cell);
+    const float f1 = __fdiv_rn(__fsub_rn(body[1], a.origin[1]), a.cell);
+    const float f2 = __fdiv_rn(__fsub_rn(body[2], a.origin[2]), a.cell);
+    if (f0 < 0.0f || f1 < 0.0f || f2 < 0.0f || f0 > rf || f1 > rf || f2 > rf) return;
+    if (trilerp_rn(a.valid, a.res, f0, f1, f2) < 0.999f) return;
+    const float dd = trilerp_rn(a.values, a.res, f0, f1, f2);
+    const float ud = fabsf(dd);
+    if (ud > a.band) return;
+    t |= (1 << (2 * a.lane)) | ((dd >= 0.0f ? 1 : 0) << (2 * a.lane + 1));
+    if (ud < d) {
+        d = ud;
+        t = (t & ~(3 << kCdfOwnerShift)) | (a.lane << kCdfOwnerShift);
+    }
+}
+
+// The whole restamp of a substep in one launch, one warp per 4^3 block of `bb`
+// (two nodes a lane): the previous grids catch up with the current ones over
+// `stale`; nodes of `box` are cleared and stamped by every listed lane in lane
+// order (the nearest lane owns a node, the first on a tie); with `post_copy` the
+// previous grids then take the new stamp over `box`; blocks of `mb` get their
+// mask, the OR of current and previous tags over the block's nodes. Equivalent to
+// copy_prev(stale), clear(box), stamp(lane) for each lane, [copy_prev(box)],
+// block_mask(mb) in sequence, as each node depends on itself alone.
+struct CdfRestamp {
+    CdfStamp lane[GBMPM_MAX_CDF];   // per lane: field, pose and its clip of `box`
+    int nl, post_copy, ng, nb;
+    CdfBox box, stale, bb, mb;
+    int *tag, *tag_prev, *block;
+    float *d, *d_prev;
+};
+
+__global__ void k_cdf_restamp(CdfRestamp a) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    const int e1 = a.bb.hi[1] - a.bb.lo[1], e2 = a.bb.hi[2] - a.bb.lo[2];
+    const long long nblk = (long long)(a.bb.hi[0] - a.bb.lo[0]) * e1 * e2;
+    const int ng = a.ng;
+    for (long long w = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); w < nblk; w += (long long)gridDim.x * wpb) {
+        const int bi = a.bb.lo[0] + (int)(w / ((long long)e1 * e2));
+        const int r = (int)(w % ((long long)e1 * e2));
+        const int bj = a.bb.lo[1] + r / e2, bk = a.bb.lo[2] + r % e2;
+        int occ = 0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int n = lane + 32 * h;
+            const int x = (bi << 2) + (n >> 4), y = (bj << 2) + ((n >> 2) & 3), z = (bk << 2) + (n & 3);
+            if (x >= ng || y >= ng || z >= ng) continue;
+            const size_t id = ((size_t)x * ng + y) * ng + z;
+            int t = a.tag[id], tp = a.tag_prev[id];
+            float d = a.d[id];
+            if (in_box(a.stale, x, y, z)) {
+                a.tag_prev[id] = t;
+                a.d_prev[id] = d;
+                tp = t;
+            }
+            if (in_box(a.box, x, y, z)) {
+                t = 0;
+                d = 1.0e9f;
+                for (int l = 0; l < a.nl; ++l)
+                    if (in_box(a.lane[l].box, x, y, z)) stamp_node(a.lane[l], x, y, z, t, d);
+                a.tag[id] = t;
+                a.d[id] = d;
+                if (a.post_copy) {
+                    a.tag_prev[id] = t;
+                    a.d_prev[id] = d;
+                    tp = t;
+                }
+            }
+            occ |= t | tp;
+        }
+        occ = __reduce_or_sync(0xffffffffu, occ);
+        if (lane == 0 && in_box(a.mb, bi, bj, bk)) a.block[((size_t)bi * a.nb + bj) * a.nb + bk] = occ;
     }
 }
 
@@ -2137,6 +2240,8 @@ struct gbmpm_engine {
     int bd = 0;
     int num_sms = 148;
     int tile_occ = 3;       // resident CTAs per SM the tiled particle kernel is compiled for
+    int cdf_occ = 2;        // the same for its CPIC variant
+    bool cdf_fused_stamp = true;   // one restamp launch a substep (else the five-kernel sequence)
     int grid_ctas = 2;      // grid-update CTAs per SM
     // graph cache
     cudaGraphExec_t graph = nullptr;
@@ -2153,6 +2258,7 @@ struct gbmpm_engine {
     DevBuf<float> c_d, c_d_prev;
     DevBuf<double> c_wrench;        // [4][6] reaction per lane (float64)
     DevBuf<double> c_partial;       // [CTA][4][6] per-CTA partials the transfer passes add into
+    DevBuf<float> c_cache;          // [5][n] the tiled scatter's scan, read by the next gather
     size_t c_partial_ctas = 0;
     int c_ng = 0;
     // adjoint segment storage and scratch (allocated by the first adjoint call)
@@ -2198,6 +2304,7 @@ PK make_pk(gbmpm_engine *e, const gbmpm_particles &P, float dt, int list) {
         k.cd = e->c_d.ptr; k.cd_prev = e->c_d_prev.ptr;
         k.ptag = P.cdf_tag;
         k.cwrench = e->c_partial.ptr;
+        k.ccache = e->c_cache.ptr;
         std::memcpy(k.lanes.c_cur, H.c_cur, sizeof H.c_cur);
         std::memcpy(k.lanes.c_prev, H.c_prev, sizeof H.c_prev);
         std::memcpy(k.lanes.v_prev, H.v_prev, sizeof H.v_prev);
@@ -2216,8 +2323,14 @@ bool has_solids(const gbmpm_model &m) {
 void launch_particles(gbmpm_engine *e, const PK &k, int mode, bool tiled, cudaStream_t s) {
     if (tiled && k.cdf_on) {
         int grid = std::max(1, (k.n + kTileThreads - 1) / kTileThreads);
-        if (has_solids(e->M)) k_particles_tiled<true, 2, true><<<grid, kTileThreads, 0, s>>>(k, mode);
-        else k_particles_tiled<false, 2, true><<<grid, kTileThreads, 0, s>>>(k, mode);
+        const bool solids = has_solids(e->M);
+        if (e->cdf_occ >= 3) {
+            if (solids) k_particles_tiled<true, 3, true><<<grid, kTileThreads, 0, s>>>(k, mode);
+            else k_particles_tiled<false, 3, true><<<grid, kTileThreads, 0, s>>>(k, mode);
+        } else {
+            if (solids) k_particles_tiled<true, 2, true><<<grid, kTileThreads, 0, s>>>(k, mode);
+            else k_particles_tiled<false, 2, true><<<grid, kTileThreads, 0, s>>>(k, mode);
+        }
         e->launches++;
         return;
     }
@@ -2494,14 +2607,18 @@ void cdf_copy_prev_box(gbmpm_engine *e, const int *b, cudaStream_t s) {
 void cdf_stamp(gbmpm_engine *e, double time, bool lag_prev, cudaStream_t s) {
     CdfHost &H = e->cdf;
     if (H.n == 0) return;
-    if (H.stale_set) { cdf_copy_prev_box(e, H.stale_box, s); H.stale_set = false; }
+    // a pending catch-up of the previous grids folds into the restamp launch
+    int stale[6] = {0, 0, 0, 0, 0, 0};
+    const bool had_stale = H.stale_set;
+    if (had_stale) { std::memcpy(stale, H.stale_box, sizeof stale); H.stale_set = false; }
+    auto flush_stale = [&]() { if (had_stale) cdf_copy_prev_box(e, stale, s); };
     for (int l = 0; l < H.n; ++l) {
         bool act = time >= (double)H.rec[l].start_time && time < (double)H.rec[l].end_time;
         if (act != H.active[l]) { H.active[l] = act; H.dirty[l] = true; }
     }
     bool any = false;
     for (int l = 0; l < H.n; ++l) any = any || H.dirty[l];
-    if (!any) return;
+    if (!any) { flush_stale(); return; }
     int box[6] = {INT32_MAX, INT32_MAX, INT32_MAX, INT32_MIN, INT32_MIN, INT32_MIN};
     bool have = false;
     auto grow = [&](const int *b) {
@@ -2518,9 +2635,55 @@ void cdf_stamp(gbmpm_engine *e, double time, bool lag_prev, cudaStream_t s) {
         if (ok) std::memcpy(H.prev_box[l], b, sizeof b);
     }
     for (int l = 0; l < H.n; ++l) H.dirty[l] = false;
-    if (!have) return;
+    if (!have) { flush_stale(); return; }
     H.stamps++;
     const int ng = e->c_ng;
+    if (e->cdf_fused_stamp) {
+        CdfRestamp a{};
+        a.ng = ng;
+        a.nb = (ng + 3) / 4;
+        a.box = to_box(box);
+        a.stale = had_stale ? to_box(stale) : CdfBox{{0, 0, 0}, {0, 0, 0}};
+        a.post_copy = lag_prev ? 0 : 1;
+        a.tag = e->c_tag.ptr; a.tag_prev = e->c_tag_prev.ptr; a.block = e->c_block.ptr;
+        a.d = e->c_d.ptr; a.d_prev = e->c_d_prev.ptr;
+        const float tf = (float)time;
+        for (int l = 0; l < H.n; ++l) {
+            const gbmpm_cdf &r = H.rec[l];
+            int lb[6], clip[6];
+            if (!cdf_lane_box(r, e->M, lb)) continue;
+            bool empty = false;
+            for (int i = 0; i < 3; ++i) {
+                clip[i] = std::max(box[i], lb[i]);
+                clip[3 + i] = std::min(box[3 + i], lb[3 + i]);
+                if (clip[3 + i] <= clip[i]) empty = true;
+            }
+            if (empty || tf < r.start_time || tf >= r.end_time) continue;
+            CdfStamp &c = a.lane[a.nl++];
+            c.values = r.values; c.valid = r.valid; c.res = r.res; c.lane = l; c.ng = ng;
+            for (int i = 0; i < 3; ++i) { c.origin[i] = r.origin[i]; c.center[i] = r.center[i]; }
+            for (int i = 0; i < 4; ++i) c.quat[i] = r.quat[i];
+            c.cell = r.cell; c.band = r.band; c.dx = e->M.dx;
+            c.box = to_box(clip);
+        }
+        // blocks to visit: those of the stamp box and of the stale box
+        int vb[6] = {box[0] >> 2, box[1] >> 2, box[2] >> 2, ((box[3] - 1) >> 2) + 1, ((box[4] - 1) >> 2) + 1,
+                     ((box[5] - 1) >> 2) + 1};
+        a.mb = to_box(vb);
+        if (had_stale && stale[3] > stale[0] && stale[4] > stale[1] && stale[5] > stale[2])
+            for (int i = 0; i < 3; ++i) {
+                vb[i] = std::min(vb[i], stale[i] >> 2);
+                vb[3 + i] = std::max(vb[3 + i], ((stale[3 + i] - 1) >> 2) + 1);
+            }
+        a.bb = to_box(vb);
+        const long long nblk = (long long)(vb[3] - vb[0]) * (vb[4] - vb[1]) * (vb[5] - vb[2]);
+        const int ctas = (int)std::max<long long>(1, std::min<long long>((nblk + 7) / 8, (long long)e->num_sms * 8));
+        k_cdf_restamp<<<ctas, 256, 0, s>>>(a);
+        e->launches++;
+        if (lag_prev) { H.stale_set = true; std::memcpy(H.stale_box, box, sizeof box); }
+        return;
+    }
+    flush_stale();
     long long vol = (long long)(box[3] - box[0]) * (box[4] - box[1]) * (box[5] - box[2]);
     k_cdf_clear<<<cdf_grid_blocks(e, vol), 256, 0, s>>>(e->c_tag.ptr, e->c_d.ptr, to_box(box), ng);
     e->launches++;
@@ -2684,6 +2847,8 @@ int gbmpm_engine_create(gbmpm_engine **out) {
     if (cudaGetDevice(&e->device) != cudaSuccess) { delete e; return fail(GBMPM_ERR_CUDA, "no CUDA device"); }
     cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, e->device);
     if (const char *occ = std::getenv("GBMPM_TILE_OCC")) e->tile_occ = std::atoi(occ);
+    if (const char *occ = std::getenv("GBMPM_CDF_OCC")) e->cdf_occ = std::atoi(occ);
+    if (const char *fs = std::getenv("GBMPM_CDF_SPLIT_STAMP")) e->cdf_fused_stamp = std::atoi(fs) == 0;
     if (const char *gc = std::getenv("GBMPM_GRID_CTAS")) e->grid_ctas = std::max(1, std::min(8, std::atoi(gc)));
     if (cudaEventCreateWithFlags(&e->pose_done, cudaEventDisableTiming) != cudaSuccess) {
         delete e;
@@ -2708,7 +2873,7 @@ void gbmpm_engine_destroy(gbmpm_engine *e) {
     e->ws_buf.release(); e->ws_keys[0].release(); e->ws_keys[1].release(); e->ws_idx[0].release();
     e->ws_idx[1].release(); e->ws_hist.release();
     e->c_tag.release(); e->c_tag_prev.release(); e->c_block.release(); e->c_d.release(); e->c_d_prev.release();
-    e->c_wrench.release(); e->c_partial.release();
+    e->c_wrench.release(); e->c_partial.release(); e->c_cache.release();
     e->adj_states.release(); e->adj_scratch.release(); e->adj_grid.release();
     delete e;
 }
@@ -2969,6 +3134,7 @@ int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32
             GB_CUDA(cudaMemsetAsync(e->c_partial.ptr, 0, ctas * 6 * GBMPM_MAX_CDF * sizeof(double), s));
             e->c_partial_ctas = ctas;
         }
+        GB_CUDA(e->c_cache.ensure(5 * (size_t)std::max(1, e->P.n)));
         if (e->c_ng != e->M.n_grid) return fail(GBMPM_ERR_STATE, "CDF grids were sized for another n_grid");
         if (e->M.periodic_x) return fail(GBMPM_ERR_UNSUPPORTED, "CDF colliders do not wrap the periodic x axis");
         if (e->P.n > 0 && !e->P.cdf_tag) return fail(GBMPM_ERR_ARG, "CDF colliders need particles.cdf_tag");
