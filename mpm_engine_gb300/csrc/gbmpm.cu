@@ -701,7 +701,7 @@ __device__ __forceinline__ bool cdf_near(const PK &k, const Stencil &s) {
 struct CdfScan {
     int tag[27];
     float votes[4];
-    int seen;
+    int side1[4], side0[4];   // per lane: stencil nodes (bit (i*3 + j)*3 + kk) valid on side +, side -
     float d_hat, n_acc[3], best_w;
     int lane_p;
 };
@@ -709,7 +709,8 @@ struct CdfScan {
 template <bool GHOST>
 __device__ __forceinline__ void cdf_scan(const PK &k, const Stencil &s, const int *T, const float *D, CdfScan &c) {
     c.votes[0] = c.votes[1] = c.votes[2] = c.votes[3] = 0.f;
-    c.seen = 0;
+#pragma unroll
+    for (int l = 0; l < 4; ++l) c.side1[l] = c.side0[l] = 0;
     c.d_hat = 0.f;
     c.n_acc[0] = c.n_acc[1] = c.n_acc[2] = 0.f;
     c.best_w = 0.f;
@@ -726,11 +727,14 @@ __device__ __forceinline__ void cdf_scan(const PK &k, const Stencil &s, const in
                 if (t == 0) continue;
                 const float w = s.w[0][i] * s.w[1][j] * s.w[2][kk];
                 const float dd = D[id];
+                const int nbit = 1 << ((i * 3 + j) * 3 + kk);
 #pragma unroll
                 for (int l = 0; l < 4; ++l)
                     if ((t >> (2 * l)) & 1) {
-                        c.seen |= 1 << (2 * l);
-                        c.votes[l] += w * dd * (((t >> (2 * l + 1)) & 1) ? 1.0f : -1.0f);
+                        const bool plus = (t >> (2 * l + 1)) & 1;
+                        c.votes[l] += w * dd * (plus ? 1.0f : -1.0f);
+                        if (plus) c.side1[l] |= nbit;
+                        else c.side0[l] |= nbit;
                     }
                 if (GHOST) {
                     const int own = (t >> kCdfOwnerShift) & 3;
@@ -752,8 +756,17 @@ __device__ __forceinline__ int cdf_vote_tag(const CdfScan &c) {
     int pc = 0;
 #pragma unroll
     for (int l = 0; l < 4; ++l)
-        if ((c.seen >> (2 * l)) & 1) pc |= (1 << (2 * l)) | ((c.votes[l] >= 0.0f ? 1 : 0) << (2 * l + 1));
+        if ((c.side1[l] | c.side0[l]) != 0) pc |= (1 << (2 * l)) | ((c.votes[l] >= 0.0f ? 1 : 0) << (2 * l + 1));
     return pc;
+}
+
+// the stencil nodes incompatible with tag pc (cdf_incompatible of each node's tag)
+__device__ __forceinline__ int cdf_mask(int pc, const CdfScan &c) {
+    int m = 0;
+#pragma unroll
+    for (int l = 0; l < 4; ++l)
+        if ((pc >> (2 * l)) & 1) m |= ((pc >> (2 * l + 1)) & 1) ? c.side0[l] : c.side1[l];
+    return m;
 }
 
 // cdf_persist_tag: a lane the particle already carried keeps its side
@@ -1098,24 +1111,18 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
             __syncthreads();
             if (want) {
                 const int o0 = s.b[0] - box.lo[0], o1 = s.b[1] - box.lo[1], o2 = s.b[2] - box.lo[2];
-                if (CDF && gmask != 0)
-                    g2p_core(k, s, [&](int i, int j, int kk) {
-                        return ((gmask >> ((i * 3 + j) * 3 + kk)) & 1)
-                                   ? g4 : s_tile[((o0 + i) * box.e[1] + (o1 + j)) * box.e[2] + (o2 + kk)];
-                    }, v, C, L);
-                else
-                    g2p_core(k, s, [&](int i, int j, int kk) {
-                        return s_tile[((o0 + i) * box.e[1] + (o1 + j)) * box.e[2] + (o2 + kk)];
-                    }, v, C, L);
+                // one copy of the unrolled gather serves masked and unmasked particles
+                g2p_core(k, s, [&](int i, int j, int kk) {
+                    const float4 t4 = s_tile[((o0 + i) * box.e[1] + (o1 + j)) * box.e[2] + (o2 + kk)];
+                    return (CDF && ((gmask >> ((i * 3 + j) * 3 + kk)) & 1)) ? g4 : t4;
+                }, v, C, L);
             }
             __syncthreads();
         } else if (want) {
-            if (CDF && gmask != 0)
-                g2p_core(k, s, [&](int i, int j, int kk) {
-                    return ((gmask >> ((i * 3 + j) * 3 + kk)) & 1) ? g4 : global_fetch(k, s, i, j, kk);
-                }, v, C, L);
-            else
-                g2p_core(k, s, [&](int i, int j, int kk) { return global_fetch(k, s, i, j, kk); }, v, C, L);
+            g2p_core(k, s, [&](int i, int j, int kk) {
+                const float4 t4 = global_fetch(k, s, i, j, kk);
+                return (CDF && ((gmask >> ((i * 3 + j) * 3 + kk)) & 1)) ? g4 : t4;
+            }, v, C, L);
         }
         if (want) {
             g2p_finish<true>(k, p, x, v, L, Ft);
@@ -1168,8 +1175,7 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
             cdf_scan<true>(k, s, k.ctag, k.cd, cs);
             pcs = cdf_persist(ptag, cdf_vote_tag(cs));
             if (pcs != 0) {
-#pragma unroll
-                for (int q = 0; q < 27; ++q) pmask |= (cdf_incompatible(pcs, cs.tag[q]) ? 1 : 0) << q;
+                pmask = cdf_mask(pcs, cs);
                 const float cch[5] = {__int_as_float(pmask | (cs.lane_p << 27)), cs.d_hat, cs.n_acc[0],
                                       cs.n_acc[1], cs.n_acc[2]};
                 fld_store<true, 5>(k.ccache, k.n, p, cch);
@@ -2240,7 +2246,7 @@ struct gbmpm_engine {
     int bd = 0;
     int num_sms = 148;
     int tile_occ = 3;       // resident CTAs per SM the tiled particle kernel is compiled for
-    int cdf_occ = 2;        // the same for its CPIC variant
+    int cdf_occ = 3;        // the same for its CPIC variant
     bool cdf_fused_stamp = true;   // one restamp launch a substep (else the five-kernel sequence)
     int grid_ctas = 2;      // grid-update CTAs per SM
     // graph cache
