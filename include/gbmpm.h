@@ -308,6 +308,35 @@ int64_t gbmpm_batch_launch_count(gbmpm_batch *b);
 int gbmpm_guard_noalloc(const float *x, const float *v, int32_t n, float out[7], int32_t *nonfinite,
                         void *stream);
 
+/* Mesh -> distance-field searches (warpmpm.geometry.mesh_sdf,
+ * src/warpmpm/geometry/mesh_sdf.py), engine-free. Every array is device memory,
+ * float64, row-major; work is ordered on `stream`. The query points are either
+ * `points` [n][3] or, with points == NULL, the res^3 nodes origin + cell * (i, j, k)
+ * of a cubic field grid, i slowest (the meshgrid "ij" order of build_sdf :341-348).
+ *
+ * gbmpm_field_nearest: per point the nearest of the samples [n_samples][3] (the
+ *   cKDTree query of _unsigned_distance :314-326 and build_surface_cdf :451-466):
+ *   dist_out[p] = sqrt((dx^2 + dy^2) + dz^2) in float64, index_out[p] the sample,
+ *   the lowest index on a tie.
+ * gbmpm_field_winding: per point the generalized winding number over the faces
+ *   tri [n_faces][3 vertices][3] (_winding_number :210-233). Summed in float32
+ *   except where within the float32 error of +-0.5, or everywhere with precise != 0.
+ * gbmpm_field_tri_distance: per point the exact distance to the nearest face
+ *   (_point_triangle_distance_exact :236-289). */
+typedef struct gbmpm_field_points {
+    const double *points;   /* device [n][3], or NULL for the grid */
+    int64_t n;
+    double origin[3];
+    double cell;
+    int32_t res;
+} gbmpm_field_points;
+int gbmpm_field_nearest(const gbmpm_field_points *pts, const double *samples, int64_t n_samples, double *dist_out,
+                        int64_t *index_out, void *stream);
+int gbmpm_field_winding(const gbmpm_field_points *pts, const double *tri, int64_t n_faces, int32_t precise,
+                        double *wn_out, void *stream);
+int gbmpm_field_tri_distance(const gbmpm_field_points *pts, const double *tri, int64_t n_faces, double *dist_out,
+                             void *stream);
+
 /* Number of kernels this engine has launched (graph replays count each node). */
 int64_t gbmpm_launch_count(gbmpm_engine *e);
 

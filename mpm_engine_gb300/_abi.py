@@ -107,6 +107,12 @@ class AdjGrads(C.Structure):
     _fields_ = [(k, C.c_void_p) for k in ("x", "v", "C", "F_trial", "yield_stress", "mu", "lam", "L", "viscosity")]
 
 
+class FieldPoints(C.Structure):
+    """gbmpm_field_points: explicit device points, or the res^3 grid (points = None)."""
+    _fields_ = [("points", C.c_void_p), ("n", C.c_int64), ("origin", C.c_double * 3), ("cell", C.c_double),
+                ("res", C.c_int32)]
+
+
 # every entry point include/gbmpm.h declares, with its ctypes signature
 _SIGNATURES = {
     "gbmpm_last_error": (C.c_char_p, []),
@@ -148,6 +154,9 @@ _SIGNATURES = {
                                    C.c_void_p]),
     "gbmpm_batch_guard": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.c_void_p]),
     "gbmpm_batch_launch_count": (C.c_int64, [C.c_void_p]),
+    "gbmpm_field_nearest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gbmpm_field_winding": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p]),
+    "gbmpm_field_tri_distance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
 }
 
 PACKAGE_DIR = Path(__file__).resolve().parent

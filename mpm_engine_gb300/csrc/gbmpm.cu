@@ -3793,3 +3793,4 @@ extern "C" int gbmpm_contact_wrench(gbmpm_engine *e, const double box_center[3],
 }
 
 #include "adjoint.cuh"
+#include "meshfield.cuh"
