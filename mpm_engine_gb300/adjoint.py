@@ -8,15 +8,18 @@ field, Young's modulus, Poisson's ratio, the yield stress and the Newtonian
 viscosity.
 
 Memory follows the usual checkpoint-and-recompute scheme: the forward keeps the
-state (x, v, C, F_trial, yield) and the collider poses every `checkpoint_every`
-substeps; the backward restores each checkpoint in reverse, replays that segment
+state (x, v, C, F_trial, L, yield, and mu, lam, which softening can zero) and the
+collider poses every `checkpoint_every` substeps; the backward restores each checkpoint in reverse, replays that segment
 one substep at a time (the engine keeps every substep's starting state on the
 device) and carries the adjoints back through it (`gbmpm_adjoint_segment`).
 
-Scope: jelly (FCR), von Mises (with or without hardening), water and Newtonian
-(Bingham, Herschel-Bulkley) particles; plane, cuboid, domain-wall, revolved-SDF cup
-and mesh-SDF colliders; no periodic axis, rpic_damping = 0, particle order fixed
-during the rollout (sort_interval = 0).
+Scope: jelly (FCR), von Mises (with or without hardening, with or without
+softening), Drucker-Prager sand, mu(I) and tabulated mu(I) granular flow, water,
+Newtonian (Bingham, Herschel-Bulkley) and tabulated viscous particles; plane,
+cuboid, domain-wall, revolved-SDF cup and mesh-SDF colliders; no periodic axis,
+rpic_damping = 0, particle order fixed during the rollout (sort_interval = 0). Not
+covered: mu(I)-Phi(I) (its packing state Jp would join the adjoint state) and CDF
+colliders.
 """
 from __future__ import annotations
 
@@ -25,7 +28,7 @@ import ctypes as C
 from . import _abi
 from .solver import _torch
 
-_STATE = ("x", "v", "C", "F_trial", "L", "yield_stress")
+_STATE = ("x", "v", "C", "F_trial", "L", "yield_stress", "mu", "lam")
 
 
 def _snapshot(s):

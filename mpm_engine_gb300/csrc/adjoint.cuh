@@ -38,8 +38,11 @@ struct AdjK {
     // state at the start of the substep (caller layout: x[n][3], C[n][9] ...)
     const float *x, *v, *C, *Ft, *Lst, *ys;
     const MatTables *tab;
-    const float *mass, *vol, *mu, *lam;
+    const float *mass, *vol, *mu, *lam;   // mu, lam: the state at the start of the substep
     const int *mat, *sel;
+    const float *eta_tab;                 // viscosity / mu(I) table of the tabulated laws (ids 12, 13)
+    int eta_n;
+    float eta_smin, eta_smax;
     int n;
     // per-particle scratch: projected F, stress, adjoint of the projected F
     float *Fp, *S, *Fpb;
@@ -138,11 +141,188 @@ __device__ bool vm_return(const float *Ft, float mu, float lam, float ys, float 
     return true;
 }
 
-// Kirchhoff stress of the projected F (FCR for id 0, Hencky for id 1), symmetrized
+// slope of table_lerp in its argument (0 where the lookup is clamped)
+__device__ __forceinline__ float table_slope(const float *tab, int n, float smin, float smax, float s) {
+    const float idx = (s - smin) / (smax - smin) * (float)(n - 1);
+    if (!(idx > 0.0f && idx < (float)(n - 1) - 1.0e-6f)) return 0.0f;
+    const int i0 = (int)floorf(idx);
+    return (tab[i0 + 1] - tab[i0]) * (float)(n - 1) / (smax - smin);
+}
+
+// Drucker-Prager return map (mpm_utils.py:543-580) as the engine's stress pass
+// computes it: 0 elastic (F = F_trial), 1 apex (F = U V^T), 2 onto the cone.
+__device__ int dp_return(const float *Ft, float mu, float lam, float alpha, float *U, float *sg, float *V, float *e,
+                         float *h, float &hn, float *Fp) {
+    svd3(Ft, U, sg, V);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) e[i] = logf(fmaxf(fabsf(sg[i]), 1e-14f));
+    const float tr = e[0] + e[1] + e[2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) h[i] = e[i] - tr / 3.0f;
+    hn = sqrtf(h[0] * h[0] + h[1] * h[1] + h[2] * h[2]);
+    const float dg = hn + (3.0f * lam + 2.0f * mu) / (2.0f * mu) * tr * alpha;
+    if (dg <= 0.0f) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Fp[i] = Ft[i];
+        return 0;
+    }
+    if (tr > 0.0f) {
+        udvt(U, 1.0f, 1.0f, 1.0f, V, Fp);
+        return 1;
+    }
+    const float r = dg / hn;
+    udvt(U, expf(e[0] - h[0] * r), expf(e[1] - h[1] * r), expf(e[2] - h[2] * r), V, Fp);
+    return 2;
+}
+
+// mu(I) return map (ids 9 and 13; mpm_utils.py:246-522) as the engine's stress pass
+// computes it: 0 below the yield surface (F = F_trial), 1 tension (F = U V^T), 2
+// flow with the rate gdp from the bisection. MuI keeps what the adjoint needs.
+struct MuI {
+    float s[3], e[3], d[3], dn, tr, mean, J, pK, tbK, pC, Ic, gdp, sc;
+};
+__device__ int mui_return(const AdjK &a, int mat, const float *Ft, float mu, float lam, float *U, float *sg, float *V,
+                          MuI &m, float *Fp) {
+    const MatTables &T = *a.tab;
+    svd3(Ft, U, sg, V);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        m.s[i] = fmaxf(fabsf(sg[i]), 1e-6f);
+        m.e[i] = logf(m.s[i]);
+    }
+    m.tr = m.e[0] + m.e[1] + m.e[2];
+    m.mean = m.tr / 3.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) m.d[i] = m.e[i] - m.mean;
+    m.dn = sqrtf(m.d[0] * m.d[0] + m.d[1] * m.d[1] + m.d[2] * m.d[2]);
+    m.J = m.s[0] * m.s[1] * m.s[2];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Fp[i] = Ft[i];
+    if (m.tr >= 0.0f) {
+        udvt(U, 1.0f, 1.0f, 1.0f, V, Fp);
+        return 1;
+    }
+    m.pK = -(2.0f * mu / 3.0f + lam) * m.tr;
+    m.tbK = 2.0f * mu * m.dn / sqrtf(2.0f);
+    m.pC = m.pK / m.J;
+    const float thr = (mat == 13) ? a.eta_tab[0] : T.mu_s[mat];
+    if (!(m.tbK > thr * m.pK)) return 0;
+    m.Ic = T.d[mat] * sqrtf(T.rho_s[mat] / m.pC);
+    m.gdp = (mat == 13) ? mu_i_bisect<true>(m.tbK, mu, a.dt, m.pK, m.Ic, 0.0f, 0.0f, 0.0f, a.eta_tab, a.eta_n,
+                                            a.eta_smin, a.eta_smax)
+                        : mu_i_bisect<false>(m.tbK, mu, a.dt, m.pK, m.Ic, T.mu_s[mat], T.dmu[mat], T.I0[mat],
+                                             a.eta_tab, a.eta_n, a.eta_smin, a.eta_smax);
+    m.sc = (m.tbK - mu * a.dt * m.gdp) / fmaxf(m.tbK, 1e-20f);
+    udvt(U, expf(m.d[0] * m.sc + m.mean), expf(m.d[1] * m.sc + m.mean), expf(m.d[2] * m.sc + m.mean), V, Fp);
+    return 2;
+}
+
+// Reverse of the mu(I) flow branch: from gb (adjoint of the returned singular
+// values g) to sb (adjoint of the trial singular values) and the mu, lam adjoints.
+// The rate gdp is the root of f = tbK - mu dt gdp - mu_I(gdp Ic) pK, so its
+// sensitivities follow from the implicit function theorem: d gdp = -df / f_gdp.
+__device__ void mui_reverse(const AdjK &a, int mat, const MuI &m, const float *sg, float mu, float lam, const float *gb,
+                            float *sb, float &mub, float &lamb) {
+    const MatTables &T = *a.tab;
+    float epb[3], db[3];
+    float scb = 0.0f, meanb = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        epb[i] = gb[i] * expf(m.d[i] * m.sc + m.mean);
+        db[i] = epb[i] * m.sc;
+        scb += epb[i] * m.d[i];
+        meanb += epb[i];
+    }
+    // sc = (tbK - mu dt gdp) / tbK (tbK > 0 on this branch)
+    float tbKb = scb * mu * a.dt * m.gdp / (m.tbK * m.tbK);
+    const float gdpb = -scb * mu * a.dt / m.tbK;
+    mub += -scb * a.dt * m.gdp / m.tbK;
+    const float I = m.gdp * m.Ic;
+    float muI, dmuI;
+    if (mat == 13) {
+        muI = mu_of_i<true>(I, 0.0f, 0.0f, 0.0f, a.eta_tab, a.eta_n, a.eta_smin, a.eta_smax);
+        dmuI = (I > 1e-12f) ? table_slope(a.eta_tab, a.eta_n, a.eta_smin, a.eta_smax,
+                                           logf(I) * 0.43429448190325176f) * 0.43429448190325176f / I
+                            : 0.0f;
+    } else {
+        muI = mu_of_i<false>(I, T.mu_s[mat], T.dmu[mat], T.I0[mat], nullptr, 0, 0.0f, 0.0f);
+        dmuI = T.dmu[mat] * T.I0[mat] / ((I + T.I0[mat]) * (I + T.I0[mat]));
+    }
+    const float fg = -mu * a.dt - dmuI * m.Ic * m.pK;
+    const float kf = (fg != 0.0f) ? -gdpb / fg : 0.0f;
+    tbKb += kf;
+    mub += kf * (-a.dt * m.gdp);
+    float pKb = kf * (-muI);
+    const float Icb = kf * (-dmuI * m.gdp * m.pK);
+    // Ic = d sqrt(rho_s / pC), pC = pK / J
+    const float pCb = Icb * (-0.5f * m.Ic / m.pC);
+    pKb += pCb / m.J;
+    const float Jb = -pCb * m.pK / (m.J * m.J);
+    // pK = -(2 mu / 3 + lam) tr, tbK = 2 mu dn / sqrt 2
+    mub += pKb * (-2.0f * m.tr / 3.0f) + tbKb * 2.0f * m.dn / sqrtf(2.0f);
+    lamb += pKb * (-m.tr);
+    const float trb = pKb * (-(2.0f * mu / 3.0f + lam)) + meanb / 3.0f;
+    const float dnb = tbKb * 2.0f * mu / sqrtf(2.0f);
+    if (m.dn > 0.0f) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) db[i] += dnb * m.d[i] / m.dn;
+    }
+    const float dsum = (db[0] + db[1] + db[2]) / 3.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float eb = db[i] - dsum + trb;
+        const float s_b = eb / m.s[i] + Jb * m.J / m.s[i];
+        sb[i] = (fabsf(sg[i]) > 1e-6f) ? (sg[i] > 0.0f ? s_b : -s_b) : 0.0f;
+    }
+}
+
+// The return map of a solid particle and the (mu, lam) its stress then uses: von
+// Mises with softening (id 5) zeroes both once the yield stress is used up. Returns
+// the yield stress after the substep in *ys_out.
+__device__ void solid_return(const AdjK &a, int mat, const float *Ft, float mu, float lam, float ys, float *Fp,
+                             float &mus, float &lams, float &ys_out) {
+    const MatTables &T = *a.tab;
+    float U[9], V[9], sg[3], e[3];
+    mus = mu;
+    lams = lam;
+    ys_out = ys;
+    if (mat == 1 || mat == 5) {
+        if (mat == 5 && ys <= 0.0f) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Fp[i] = Ft[i];
+            return;
+        }
+        if (!vm_return(Ft, mu, lam, ys, U, sg, V, e, Fp)) return;
+        const float mean = (e[0] + e[1] + e[2]) / 3.0f;
+        const float h0 = e[0] - mean, h1 = e[1] - mean, h2 = e[2] - mean;
+        const float hn = sqrtf(h0 * h0 + h1 * h1 + h2 * h2) + 1e-6f;
+        const float dg = hn - ys / (2.0f * mu);
+        float y = ys;
+        if (mat == 5) {
+            const float r = dg / hn;
+            const float rh0 = r * h0, rh1 = r * h1, rh2 = r * h2;
+            y = y - T.softening[mat] * sqrtf(rh0 * rh0 + rh1 * rh1 + rh2 * rh2);
+            if (y <= 0.0f) { mus = 0.0f; lams = 0.0f; }
+        }
+        if (T.hardening[mat] > 0.5f) y = y + 2.0f * mus * T.xi[mat] * dg;
+        ys_out = y;
+    } else if (mat == 2) {
+        float h[3], hn;
+        dp_return(Ft, mu, lam, T.alpha[mat], U, sg, V, e, h, hn, Fp);
+    } else if (mat == 9 || mat == 13) {
+        MuI m;
+        mui_return(a, mat, Ft, mu, lam, U, sg, V, m, Fp);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Fp[i] = Ft[i];
+    }
+}
+
+// Kirchhoff stress of the projected F (FCR for ids 0 and 5, Hencky otherwise), symmetrized
 __device__ void adj_stress(int mat, const float *F, float mu, float lam, float *S) {
     float U[9], V[9], sg[3], T[9];
     svd3(F, U, sg, V);
-    if (mat == 0) {
+    if (mat == 0 || mat == 5) {
         float R[9], FR[9];
         mmT(U, V, R);
 #pragma unroll
@@ -181,8 +361,13 @@ __device__ void fluid_stress(const AdjK &k, int p, int mat, const float *Ft, con
         return;
     }
     dev_rate(L, f.Dd, f.gd);
-    const float ys = k.ys[p], Kp = T.hardening[mat];
-    f.eta = T.pv[mat] + (ys != 0.0f ? ys / f.gd : 0.0f) + (Kp != 0.0f ? Kp * powf(f.gd, T.softening[mat] - 1.0f) : 0.0f);
+    if (mat == 12) {
+        f.eta = table_lerp(k.eta_tab, k.eta_n, k.eta_smin, k.eta_smax, logf(f.gd) * 0.43429448190325176f);
+    } else {
+        const float ys = k.ys[p], Kp = T.hardening[mat];
+        f.eta = T.pv[mat] + (ys != 0.0f ? ys / f.gd : 0.0f) +
+                (Kp != 0.0f ? Kp * powf(f.gd, T.softening[mat] - 1.0f) : 0.0f);
+    }
     const float two_eta = 2.0f * f.eta;
 #pragma unroll
     for (int i = 0; i < 9; ++i) S[i] = f.J * (((i % 4 == 0) ? f.pr : 0.0f) + two_eta * f.Dd[i]);
@@ -196,7 +381,7 @@ __global__ void k_adj_stress_fwd(AdjK k) {
     for (int i = 0; i < 9; ++i) Ft[i] = k.Ft[9 * (size_t)p + i];
     const int mat = k.mat[p];
     const float mu = k.mu[p], lam = k.lam[p];
-    if (mat == 6 || mat == 10) {
+    if (mat == 6 || mat == 10 || mat == 12) {
         float L[9];
 #pragma unroll
         for (int i = 0; i < 9; ++i) L[i] = k.Lst[9 * (size_t)p + i];
@@ -206,14 +391,9 @@ __global__ void k_adj_stress_fwd(AdjK k) {
         for (int i = 0; i < 9; ++i) { k.Fp[9 * (size_t)p + i] = Fp[i]; k.S[9 * (size_t)p + i] = S[i]; }
         return;
     }
-    if (mat == 1) {
-        float U[9], V[9], sg[3], eps[3];
-        vm_return(Ft, mu, lam, k.ys[p], U, sg, V, eps, Fp);
-    } else {
-#pragma unroll
-        for (int i = 0; i < 9; ++i) Fp[i] = Ft[i];
-    }
-    adj_stress(mat, Fp, mu, lam, S);
+    float mus, lams, ys_out;
+    solid_return(k, mat, Ft, mu, lam, k.ys[p], Fp, mus, lams, ys_out);
+    adj_stress(mat, Fp, mus, lams, S);
 #pragma unroll
     for (int i = 0; i < 9; ++i) { k.Fp[9 * (size_t)p + i] = Fp[i]; k.S[9 * (size_t)p + i] = S[i]; }
 }
@@ -580,7 +760,15 @@ __global__ void k_adj_p2g_bwd(AdjK a) {
     float Lb[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // adjoint of the state's L
     float Ftb[9];
     float ysb_in = a.ysb[p], ysb = ysb_in;
-    if (mat == 6 || mat == 10) {
+    // the (mu, lam) the stress used, and whether mu and lam are still the
+    // parameters (von Mises with softening zeroes them once its yield is used up)
+    float mus = mu, lams = lam, ys_next = ys;
+    if (mat != 6 && mat != 10 && mat != 12) {
+        float Fq[9];
+        solid_return(a, mat, Ft, mu, lam, ys, Fq, mus, lams, ys_next);
+    }
+    const bool params_live = (mu != 0.0f);
+    if (mat == 6 || mat == 10 || mat == 12) {
         // tau = J (p I + 2 eta dev D) with J = Jc^3, Jc = det(F_trial)^(1/3), F = Jc I,
         // p = -K (J^-1.1 - 1), D = sym(L), eta = eta_p + tau_y / gd + K_p gd^(n - 1)
         const MatTables &T = *a.tab;
@@ -592,14 +780,18 @@ __global__ void k_adj_p2g_bwd(AdjK a) {
         const float trb = tb[0] + tb[4] + tb[8];
         const float dpr = 1.1f * T.bulk[mat] * powf(f.J, -2.1f);
         float Jb = trb * f.pr + f.J * trb * dpr;
-        if (mat == 10) {
+        if (mat == 10 || mat == 12) {
             float tD = 0.0f;
 #pragma unroll
             for (int i = 0; i < 9; ++i) tD += tb[i] * f.Dd[i];
             Jb += 2.0f * f.eta * tD;
             const float etab = 2.0f * f.J * tD;
             const float ys_p = a.ys[p], Kp = T.hardening[mat], np_ = T.softening[mat];
-            const float detadgd = -ys_p / (f.gd * f.gd) + (Kp != 0.0f ? Kp * (np_ - 1.0f) * powf(f.gd, np_ - 2.0f) : 0.0f);
+            const float detadgd =
+                (mat == 12)
+                    ? table_slope(a.eta_tab, a.eta_n, a.eta_smin, a.eta_smax, logf(f.gd) * 0.43429448190325176f) *
+                          0.43429448190325176f / f.gd
+                    : -ys_p / (f.gd * f.gd) + (Kp != 0.0f ? Kp * (np_ - 1.0f) * powf(f.gd, np_ - 2.0f) : 0.0f);
             const float gdb = etab * detadgd;
             float Ddb[9];
 #pragma unroll
@@ -611,8 +803,10 @@ __global__ void k_adj_p2g_bwd(AdjK a) {
 #pragma unroll
                 for (int j = 0; j < 3; ++j)
                     Lb[3 * i + j] = 0.5f * (Ddb[3 * i + j] + Ddb[3 * j + i]) - ((i == j) ? tr3 : 0.0f);
-            ysb = ysb_in + etab / f.gd;
-            pvb = etab;
+            if (mat == 10) {
+                ysb = ysb_in + etab / f.gd;
+                pvb = etab;
+            }
         }
         // back through J = Jc^3, F = Jc I and Jc = det(F_trial)^(1/3)
         const float Jcb = 3.0f * f.Jc * f.Jc * Jb + (Fb[0] + Fb[4] + Fb[8]);
@@ -624,7 +818,9 @@ __global__ void k_adj_p2g_bwd(AdjK a) {
     } else {
         float U[9], V[9], sg[3], yd[3];
         svd3(Fp, U, sg, V);
-        if (mat == 0) {   // tau = 2 mu (F - R) F^T + lam J (J - 1) I
+        const float mu = mus, lam = lams;   // the stress's moduli (zero once softened away)
+        float mub_s = 0.0f, lamb_s = 0.0f;
+        if (mat == 0 || mat == 5) {   // tau = 2 mu (F - R) F^T + lam J (J - 1) I
             float R[9], FR[9], T1[9], T2[9], cof[9];
             mmT(U, V, R);
 #pragma unroll
@@ -648,8 +844,8 @@ __global__ void k_adj_p2g_bwd(AdjK a) {
             float FRF[9];
             mmT(FR, Fp, FRF);
 #pragma unroll
-            for (int i = 0; i < 9; ++i) mub += 2.0f * tb[i] * FRF[i];
-            lamb += J * (J - 1.0f) * trb;
+            for (int i = 0; i < 9; ++i) mub_s += 2.0f * tb[i] * FRF[i];
+            lamb_s += J * (J - 1.0f) * trb;
         } else {          // Hencky: tau = G F^T, G = U diag(h / s) V^T
             float e[3], de[3], h[3], gg[3], Jg[3][3];
 #pragma unroll
@@ -680,13 +876,19 @@ __global__ void k_adj_p2g_bwd(AdjK a) {
 #pragma unroll
             for (int i = 0; i < 3; ++i)
                 if (sg[i] > 1e-6f) {
-                    mub += yd[i] * 2.0f * e[i] / sg[i];
-                    lamb += yd[i] * tr / sg[i];
+                    mub_s += yd[i] * 2.0f * e[i] / sg[i];
+                    lamb_s += yd[i] * tr / sg[i];
                 }
+        }
+        // the stress used the parameters unless softening zeroed them
+        if (params_live && mus != 0.0f) {
+            mub += mub_s;
+            lamb += lamb_s;
         }
     }
     // return-map adjoint: F (projected) -> F_trial, yield, mu (fluids done above)
-    if (mat == 1) {
+    if ((mat == 1 || mat == 5) && !(mat == 5 && ys <= 0.0f)) {
+        const MatTables &T = *a.tab;
         float U[9], V[9], sg[3], e[3], Fq[9];
         const bool plastic = vm_return(Ft, mu, lam, ys, U, sg, V, e, Fq);
         if (!plastic) {
@@ -718,28 +920,106 @@ __global__ void k_adj_p2g_bwd(AdjK a) {
             float yd[3];
             iso_adjoint(U, sg, V, g, Jg, Fb, Ftb, yd);
             ysb = 0.0f;
+            float mub_r = 0.0f;
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
                 ysb += yd[i] * g[i] * eh[i] / (2.0f * mu * ehn);
-                mub += yd[i] * g[i] * (-eh[i] * kap / mu);
+                mub_r += yd[i] * g[i] * (-eh[i] * kap / mu);
             }
-            if (a.hard1 > 0.5f) {   // yield' = yield + 2 mu xi (ehn - yield / (2 mu))
-                ysb += ysb_in * (1.0f - a.xi1);
-                mub += ysb_in * 2.0f * a.xi1 * ehn;
-                if (nrm > 0.0f) {
-                    float sb[3];
+            // yield after the substep: y1 = y - soft |r h| (id 5; r h = (1 - kap) h),
+            // then + 2 mu' xi (ehn - y / (2 mu)) with hardening (mu' = 0 once softened away)
+            const float soft = (mat == 5) ? T.softening[mat] : 0.0f;
+            const bool hard = T.hardening[mat] > 0.5f && mus != 0.0f;
+            const float xi = T.xi[mat];
+            float ydy = 1.0f + soft * nrm / (2.0f * mu * ehn);
+            float ydmu = -soft * nrm * ys / (2.0f * mu * mu * ehn);
+            float ydn = -soft * (1.0f - ys / (2.0f * mu) * 1e-6f / (ehn * ehn));
+            if (hard) {
+                ydy += -xi;
+                ydmu += 2.0f * xi * ehn;
+                ydn += 2.0f * mu * xi;
+            }
+            ysb += ysb_in * ydy;
+            mub_r += ysb_in * ydmu;
+            if (nrm > 0.0f && ydn != 0.0f) {
+                float sb[3];
 #pragma unroll
-                    for (int i = 0; i < 3; ++i) sb[i] = ysb_in * 2.0f * mu * a.xi1 * eh[i] / nrm * de[i];
-                    float T[9];
-                    udvt(U, sb[0], sb[1], sb[2], V, T);
+                for (int i = 0; i < 3; ++i) sb[i] = ysb_in * ydn * eh[i] / nrm * de[i];
+                float Tm[9];
+                udvt(U, sb[0], sb[1], sb[2], V, Tm);
 #pragma unroll
-                    for (int i = 0; i < 9; ++i) Ftb[i] += T[i];
+                for (int i = 0; i < 9; ++i) Ftb[i] += Tm[i];
+            }
+            if (params_live) mub += mub_r;
+        }
+    } else if (mat == 2) {   // Drucker-Prager: e' = e - (dg / |h|) h, dg = |h| + c tr, c = alpha (3 lam + 2 mu) / (2 mu)
+        const MatTables &T = *a.tab;
+        float U[9], V[9], sg[3], e[3], h[3], hn, Fq[9];
+        const int br = dp_return(Ft, mu, lam, T.alpha[mat], U, sg, V, e, h, hn, Fq);
+        if (br == 0) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Ftb[i] = Fb[i];
+        } else {
+            float g[3], Jg[3][3], yd[3];
+            const float alpha = T.alpha[mat];
+            const float c = alpha * (3.0f * lam + 2.0f * mu) / (2.0f * mu);
+            const float tr = e[0] + e[1] + e[2];
+            float hh[3], de[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                hh[i] = (br == 2) ? h[i] / hn : 0.0f;
+                de[i] = (fabsf(sg[i]) > 1e-14f) ? 1.0f / sg[i] : 0.0f;
+                g[i] = (br == 2) ? expf(e[i] - h[i] * ((hn + c * tr) / hn)) : 1.0f;
+            }
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    const float P = ((i == j) ? 1.0f : 0.0f) - 1.0f / 3.0f;
+                    const float dep = 1.0f / 3.0f - c * (hh[i] + tr * (P - hh[i] * hh[j]) / hn);
+                    Jg[i][j] = (br == 2) ? g[i] * dep * de[j] : 0.0f;
                 }
-            } else {
-                ysb += ysb_in;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Ftb[i] = 0.0f;
+            iso_adjoint(U, sg, V, g, Jg, Fb, Ftb, yd);
+            if (br == 2 && params_live) {
+                float cb = 0.0f;
+#pragma unroll
+                for (int i = 0; i < 3; ++i) cb += yd[i] * g[i] * (-tr * hh[i]);
+                mub += cb * alpha * (-3.0f * lam / (2.0f * mu * mu));
+                lamb += cb * alpha * (3.0f / (2.0f * mu));
             }
         }
-    } else if (mat != 6 && mat != 10) {   // jelly: F = F_trial
+    } else if (mat == 9 || mat == 13) {   // mu(I)
+        float U[9], V[9], sg[3], Fq[9];
+        MuI m;
+        const int br = mui_return(a, mat, Ft, mu, lam, U, sg, V, m, Fq);
+        if (br == 0) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Ftb[i] = Fb[i];
+        } else {
+            float g[3], Jg[3][3], yd[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) g[i] = (br == 2) ? expf(m.d[i] * m.sc + m.mean) : 1.0f;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                float unit[3] = {0.0f, 0.0f, 0.0f}, row[3], dm = 0.0f, dl = 0.0f;
+                unit[i] = 1.0f;
+                if (br == 2) mui_reverse(a, mat, m, sg, mu, lam, unit, row, dm, dl);
+#pragma unroll
+                for (int j = 0; j < 3; ++j) Jg[i][j] = (br == 2) ? row[j] : 0.0f;
+            }
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Ftb[i] = 0.0f;
+            iso_adjoint(U, sg, V, g, Jg, Fb, Ftb, yd);
+            if (br == 2 && params_live) {
+                float sbd[3], dm = 0.0f, dl = 0.0f;
+                mui_reverse(a, mat, m, sg, mu, lam, yd, sbd, dm, dl);
+                mub += dm;
+                lamb += dl;
+            }
+        }
+    } else if (mat != 6 && mat != 10 && mat != 12) {   // jelly, and id 5 once softened away: F = F_trial
 #pragma unroll
         for (int i = 0; i < 9; ++i) Ftb[i] = Fb[i];
     }
@@ -765,10 +1045,12 @@ namespace {
 int adjoint_supported(gbmpm_engine *e) {
     if (e->M.periodic_x) return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint does not wrap the periodic x axis");
     if (e->M.rpic_damping != 0.0f) return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint needs rpic_damping == 0");
-    const uint32_t covered = (1u << 0) | (1u << 1) | (1u << 6) | (1u << 10);
+    const uint32_t covered = (1u << 0) | (1u << 1) | (1u << 2) | (1u << 5) | (1u << 6) | (1u << 9) | (1u << 10) |
+                             (1u << 12) | (1u << 13);
     if (e->M.material_mask & ~covered)
         return fail(GBMPM_ERR_UNSUPPORTED,
-                    "the adjoint covers jelly (0), von Mises (1), water (6) and Newtonian (10) particles only");
+                    "the adjoint covers jelly (0), von Mises (1), sand (2), softening von Mises (5), water (6), "
+                    "mu(I) (9, 13), Newtonian (10) and tabulated viscous (12) particles; not mu(I)-Phi(I) (11)");
     if (e->cdf.n > 0) return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint does not cover CDF colliders");
     return GBMPM_OK;
 }
@@ -793,7 +1075,7 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
     const int n = P.n, ng = e->G.n_grid, nc = (int)e->cols.size();
     const size_t nn = (size_t)ng * ng * ng;
     // segment storage: the state at the start of every substep
-    const size_t per = (size_t)34 * n;   // x 3, v 3, C 9, F_trial 9, L 9, yield 1
+    const size_t per = (size_t)36 * n;   // x 3, v 3, C 9, F_trial 9, L 9, yield 1, mu 1, lam 1
     GB_CUDA(e->adj_states.ensure(per * substeps));
     GB_CUDA(e->adj_scratch.ensure((size_t)27 * n));
     GB_CUDA(e->adj_grid.ensure(4 * nn));   // four float4 grids
@@ -810,6 +1092,8 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
         GB_CUDA(cudaMemcpyAsync(st + 15 * (size_t)n, P.F_trial, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         GB_CUDA(cudaMemcpyAsync(st + 24 * (size_t)n, P.L, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         GB_CUDA(cudaMemcpyAsync(st + 33 * (size_t)n, P.yield_stress, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        GB_CUDA(cudaMemcpyAsync(st + 34 * (size_t)n, P.mu, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        GB_CUDA(cudaMemcpyAsync(st + 35 * (size_t)n, P.lam, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         record_tick(e, dtf, 1, false, false, s, false, 0.0, 0.0, i);
     }
     float4 *grid = e->adj_grid.ptr;
@@ -821,7 +1105,10 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
         a.x = st; a.v = st + 3 * (size_t)n; a.C = st + 6 * (size_t)n; a.Ft = st + 15 * (size_t)n;
         a.Lst = st + 24 * (size_t)n; a.ys = st + 33 * (size_t)n;
         a.tab = e->d_tab.ptr;
-        a.mass = P.mass; a.vol = P.vol; a.mu = P.mu; a.lam = P.lam; a.mat = P.material; a.sel = P.selection;
+        a.mass = P.mass; a.vol = P.vol; a.mu = st + 34 * (size_t)n; a.lam = st + 35 * (size_t)n;
+        a.mat = P.material; a.sel = P.selection;
+        a.eta_tab = e->M.eta_table; a.eta_n = e->M.eta_table_n;
+        a.eta_smin = e->M.eta_table_smin; a.eta_smax = e->M.eta_table_smax;
         a.n = n;
         a.Fp = e->adj_scratch.ptr; a.S = a.Fp + 9 * (size_t)n; a.Fpb = a.S + 9 * (size_t)n;
         a.gmv = grid; a.gv = grid + nn; a.gvb = grid + 2 * nn; a.gmb = grid + 3 * nn;

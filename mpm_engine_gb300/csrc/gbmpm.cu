@@ -216,21 +216,31 @@ __device__ __forceinline__ void stress_hencky(const float *U, const float *sig, 
     udvt(U, 2.0f * mu * e0 + lam * tr, 2.0f * mu * e1 + lam * tr, 2.0f * mu * e2 + lam * tr, U, out);
 }
 
+// the friction law mu(I): mu_s + dmu I / (I + I0), or the table over log10 I
+template <bool TAB>
+__device__ __forceinline__ float mu_of_i(float Im, float mu_s, float dmu, float I0, const float *tab, int tn, float smin,
+                                         float smax) {
+    if (!TAB) return mu_s + dmu * Im / (Im + I0);
+    return table_lerp(tab, tn, smin, smax, logf(fmaxf(Im, 1e-12f)) * 0.43429448190325176f);
+}
+
 // the 48-step bisection on g(gdp) = tau_bar - G dt gdp - mu(I) p (mpm_utils.py:300-312)
 template <bool TAB>
 __device__ __forceinline__ float mu_i_bisect(float tbK, float G, float dt, float pK, float Ic, float mu_s, float dmu,
-                                             float I0, const PK &k) {
+                                             float I0, const float *tab, int tn, float smin, float smax) {
     float lo = 0.0f, hi = tbK / (G * dt);
     for (int it = 0; it < 48; ++it) {
         float mid = 0.5f * (lo + hi);
-        float Im = mid * Ic;
-        float mu_mid;
-        if (!TAB) mu_mid = mu_s + dmu * Im / (Im + I0);
-        else mu_mid = table_lerp(k.eta, k.eta_n, k.eta_smin, k.eta_smax, logf(fmaxf(Im, 1e-12f)) * 0.43429448190325176f);
+        float mu_mid = mu_of_i<TAB>(mid * Ic, mu_s, dmu, I0, tab, tn, smin, smax);
         float g = tbK - G * dt * mid - mu_mid * pK;
         if (g > 0.0f) lo = mid; else hi = mid;
     }
     return 0.5f * (lo + hi);
+}
+template <bool TAB>
+__device__ __forceinline__ float mu_i_bisect(float tbK, float G, float dt, float pK, float Ic, float mu_s, float dmu,
+                                             float I0, const PK &k) {
+    return mu_i_bisect<TAB>(tbK, G, dt, pK, Ic, mu_s, dmu, I0, k.eta, k.eta_n, k.eta_smin, k.eta_smax);
 }
 
 // Return map F_trial -> F and Kirchhoff stress for one particle

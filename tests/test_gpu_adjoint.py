@@ -14,7 +14,7 @@ differences scatter by about 10 %, so long horizons are checked for consistency
 import numpy as np
 import pytest
 
-from scenes_lib import MATERIALS, blob, make, spin_velocity
+from scenes_lib import MATERIALS, NAME_PARAMS, blob, make, spin_velocity
 
 pytestmark = pytest.mark.gpu
 
@@ -33,6 +33,33 @@ MATS["newtonian_soft"] = lambda: __import__("mpm_engine_gb300").newtonian(
 MATS["bingham_yield"] = lambda: __import__("mpm_engine_gb300").newtonian(
     eta=0.2, density=1000.0, bulk_modulus=2.0e4).with_yield(10.0)
 DT_OF = {"bingham_yield": 4.0e-5}
+# the remaining laws: Drucker-Prager sand, von Mises with softening, mu(I) and its
+# tabulated form (by engine name and parameters), and a tabulated viscous fluid
+MATS["sand"] = ("sand", NAME_PARAMS["sand"])
+MATS["plasticine"] = ("plasticine", NAME_PARAMS["plasticine"])
+MATS["mu_i_table"] = ("tabulated_mu_i", dict(E=1.0e5, nu=0.3, density=2500.0, eta_table=[0.38, 0.45, 0.55, 0.64],
+                                             eta_table_smin=-4.0, eta_table_smax=0.0, grain_diameter=1.0e-3,
+                                             grain_density=2650.0))
+MATS["tabulated_soft"] = lambda: __import__("mpm_engine_gb300").tabulated_viscous(
+    [8.0, 4.0, 2.0, 1.0, 0.5], smin=-1.0, smax=2.0, density=1000.0, bulk_modulus=2.0e4)
+
+
+def _set_material(s, key):
+    m = MATS[key]
+    if isinstance(m, tuple):
+        s.set_material(m[0], g=[0.0, 0.0, -9.8], **m[1])
+    else:
+        s.set_material(m(), g=[0.0, 0.0, -9.8])
+
+
+def _mat_params(key):
+    """(E, nu, yield) of a test material."""
+    m = MATS[key]
+    if isinstance(m, tuple):
+        kw = m[1]
+        return float(kw.get("E", 1e5)), float(kw.get("nu", 0.3)), float(kw.get("yield_stress", 0.0))
+    m = m()
+    return float(m.E), float(m.nu), float(m.yield_stress)
 
 
 def _scene(cls, key, floor="sticky", plate=False, cup=False, sphere=False, drop=0.0, free=False):
@@ -41,7 +68,7 @@ def _scene(cls, key, floor="sticky", plate=False, cup=False, sphere=False, drop=
     pts, vol = blob(n=N, lo=0.12, size=0.08)
     pts[:, 2] -= drop
     s = make(cls, NG, 0.4).load_particles(pts, vol)
-    s.set_material(MATS[key](), g=[0.0, 0.0, -9.8])
+    _set_material(s, key)
     dx = 0.4 / NG
     if free:      # no contact within the rollout: a straining flow loads the stress
         pass
@@ -82,8 +109,7 @@ class Case:
         self.s = _scene(Solver, key, **kw)
         self.snap = adjoint._snapshot(self.s)
         self.state = self.s.export_state()
-        m = MATS[key]()
-        self.E, self.nu, self.ys = float(m.E), float(m.nu), float(m.yield_stress)
+        self.E, self.nu, self.ys = _mat_params(key)
         self.eta = float(self.s._model.plastic_viscosity[10])
         self.v0 = self.s._t["v"].clone()
         dev = self.v0.device
@@ -210,6 +236,30 @@ def test_fluid_cup_and_sdf_gradients_match_finite_differences(cuda, oracle_lib, 
     _close(float((g["v0"] * d).sum()), fd, tol, f"{key} d/dv0")
 
 
+@pytest.mark.parametrize("key,kw,params,tol", [
+    ("sand", {}, ("E", "nu"), 0.03),
+    ("plasticine", {"plate": True}, ("E", "nu", "ys"), 0.03),
+    ("mu_i", {}, ("E", "nu"), 0.05),
+    ("mu_i_table", {}, ("E", "nu"), 0.05),
+    ("tabulated_soft", {"free": True}, (), 0.03),
+])
+def test_granular_softening_and_tabulated_gradients(cuda, oracle_lib, key, kw, params, tol):
+    """Drucker-Prager sand and mu(I) (closed-form and tabulated) landing on a sticky
+    floor, softening von Mises pressed by a plate, and a tabulated viscous fluid in a
+    free straining flow, against deterministic oracle differences. The mu(I) laws
+    switch branch where a particle's volumetric strain changes sign (tension resets
+    F to its rotation), which makes their differences the noisiest, hence 5 %."""
+    import torch
+    c = Case(key, **kw)
+    g = c.grads()
+    for p in params:
+        _close(g[p], c.fd_oracle(oracle_lib.OracleSolver, p), tol, f"{key} d/d{p}")
+    d = torch.randn(c.v0.shape, generator=torch.Generator().manual_seed(9)).to(c.dev)
+    d = d / d.norm()
+    fd = c.fd_oracle(oracle_lib.OracleSolver, "v0", rel=1e-2, direction=d.double().cpu().numpy())
+    _close(float((g["v0"] * d).sum()), fd, tol, f"{key} d/dv0")
+
+
 def test_long_rollout_checkpoint_interval_does_not_change_gradients(cuda):
     import torch
     from mpm_engine_gb300 import Solver, adjoint
@@ -231,7 +281,7 @@ def test_unsupported_scenes_are_refused(cuda):
     from mpm_engine_gb300 import Solver, adjoint
     pts, vol = blob(n=500)
     s = make(Solver, 32, 0.4).load_particles(pts, vol)
-    s.set_material(MATERIALS["mu_i"]())
+    s.set_material(MATERIALS["mu_i_phi"]())
     with pytest.raises(NotImplementedError):
         x, v = adjoint.rollout(s, DT, 4, v0=torch.zeros(len(pts), 3, device="cuda", requires_grad=True))
         x.sum().backward()
