@@ -81,6 +81,9 @@ typedef struct {
     int32_t *material, *selection;      /* [n] */
     float *cov, *init_cov;              /* [n][6] upper triangle xx,xy,xz,yy,yz,zz, or NULL */
     int32_t *cdf_tag;                   /* [n] persisted CPIC side bits (warp_utils.py:124-129), or NULL */
+    int32_t *rigid_id;                  /* [n] body of a material-8 particle (mpm_solver_warp.py:366-371), or NULL */
+    float *x_ref;                       /* [n][3] body-frame position of a rigid particle, or NULL */
+    int32_t *mod_mask;                  /* [n] bit m set: particle modifier m acts on the particle, or NULL */
 } gbmpm_particles;
 
 /* Dense n^3 grid, index ((ix*n)+iy)*n+iz (Warp 3-D array order).
@@ -307,6 +310,50 @@ int64_t gbmpm_batch_launch_count(gbmpm_batch *b);
  * address; make it before any stream capture. Synchronizes the stream. */
 int gbmpm_guard_noalloc(const float *x, const float *v, int32_t n, float out[7], int32_t *nonfinite,
                         void *stream);
+
+/* Rigid bodies (MPM_Simulator_WARP.finalize_rigid_bodies / _p2g2p_tail,
+ * mpm_solver_warp.py:818-987, 1338-1367; kernels mpm_utils.py:1369-1493). The
+ * material-8 particles of body b (particles.rigid_id) move with it: after every
+ * G2P the body gathers the grid momentum of its particles, integrates (v_cm = P/M,
+ * omega = I_world^-1 L, x_cm += dt v_cm, R re-orthogonalised by polar
+ * decomposition), takes restitution impulses from the rigid surfaces (add_plane
+ * with restitution > 0; the host loop of _apply_rigid_restitution, here on the
+ * device) and writes back x, v = v_cm + omega x r, C = skew(omega), F = I. R and the
+ * inverse body inertia are row-major. gbmpm_set_rigid replaces bodies and surfaces;
+ * gbmpm_get_rigid reads the bodies back (synchronizing the stream). */
+typedef struct gbmpm_rigid_body {
+    float x_cm[3], v_cm[3], omega[3];
+    float R[9];
+    float mass;
+    float inv_inertia[9];
+} gbmpm_rigid_body;
+typedef struct gbmpm_rigid_surface {
+    double point[3], normal[3];         /* normal of unit length */
+    double friction, restitution;
+    double start_time, end_time;
+} gbmpm_rigid_surface;
+#define GBMPM_MAX_RIGID_SURFACES 8
+int gbmpm_set_rigid(gbmpm_engine *e, const gbmpm_rigid_body *bodies, int32_t n_bodies,
+                    const gbmpm_rigid_surface *surfaces, int32_t n_surfaces);
+int gbmpm_get_rigid(gbmpm_engine *e, gbmpm_rigid_body *bodies, int32_t n_bodies, void *stream);
+
+/* Particle modifiers (add_impulse_on_particles, enforce_particle_velocity_translation,
+ * enforce_particle_velocity_rotation; mpm_solver_warp.py:2385-2540), applied to the
+ * particles whose particles.mod_mask has bit m set, before the stress and P2G of
+ * every substep whose start time t (float32) lies in [start_time, end_time): first
+ * every impulse (v += force / m * dt), then every velocity override, each kind in
+ * list order. kind 1 sets v = vec; kind 2 sets the rotation field about the axis
+ * through `point` along `normal` (rotation_scale, translation_scale, with the
+ * reference's horizontal axes axis1, axis2). At most 32 modifiers. */
+typedef struct gbmpm_modifier {
+    int32_t kind;                       /* 0 impulse, 1 velocity translation, 2 velocity rotation */
+    float start_time, end_time;
+    float vec[3];                       /* kind 0: force; kind 1: velocity */
+    float point[3], normal[3], axis1[3], axis2[3];
+    float rotation_scale, translation_scale;
+} gbmpm_modifier;
+#define GBMPM_MAX_MODIFIERS 32
+int gbmpm_set_modifiers(gbmpm_engine *e, const gbmpm_modifier *mods, int32_t n);
 
 /* Mesh -> distance-field searches (warpmpm.geometry.mesh_sdf,
  * src/warpmpm/geometry/mesh_sdf.py), engine-free. Every array is device memory,

@@ -50,6 +50,7 @@ class Particles(C.Structure):
         ("material", C.c_void_p), ("selection", C.c_void_p),
         ("cov", C.c_void_p), ("init_cov", C.c_void_p),
         ("cdf_tag", C.c_void_p),
+        ("rigid_id", C.c_void_p), ("x_ref", C.c_void_p), ("mod_mask", C.c_void_p),
     ]
 
 
@@ -103,6 +104,28 @@ class Cdf(C.Structure):
     ]
 
 
+class RigidBody(C.Structure):
+    """gbmpm_rigid_body: R and the body-frame inverse inertia row-major."""
+    _fields_ = [("x_cm", C.c_float * 3), ("v_cm", C.c_float * 3), ("omega", C.c_float * 3), ("R", C.c_float * 9),
+                ("mass", C.c_float), ("inv_inertia", C.c_float * 9)]
+
+
+class RigidSurface(C.Structure):
+    _fields_ = [("point", C.c_double * 3), ("normal", C.c_double * 3), ("friction", C.c_double),
+                ("restitution", C.c_double), ("start_time", C.c_double), ("end_time", C.c_double)]
+
+
+class Modifier(C.Structure):
+    """gbmpm_modifier: kind 0 impulse, 1 velocity translation, 2 velocity rotation."""
+    _fields_ = [("kind", C.c_int32), ("start_time", C.c_float), ("end_time", C.c_float), ("vec", C.c_float * 3),
+                ("point", C.c_float * 3), ("normal", C.c_float * 3), ("axis1", C.c_float * 3),
+                ("axis2", C.c_float * 3), ("rotation_scale", C.c_float), ("translation_scale", C.c_float)]
+
+
+MAX_RIGID_SURFACES = 8
+MAX_MODIFIERS = 32
+
+
 class AdjGrads(C.Structure):
     _fields_ = [(k, C.c_void_p) for k in ("x", "v", "C", "F_trial", "yield_stress", "mu", "lam", "L", "viscosity")]
 
@@ -154,6 +177,9 @@ _SIGNATURES = {
                                    C.c_void_p]),
     "gbmpm_batch_guard": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.c_void_p]),
     "gbmpm_batch_launch_count": (C.c_int64, [C.c_void_p]),
+    "gbmpm_set_rigid": (C.c_int, [C.c_void_p, C.POINTER(RigidBody), C.c_int32, C.POINTER(RigidSurface), C.c_int32]),
+    "gbmpm_get_rigid": (C.c_int, [C.c_void_p, C.POINTER(RigidBody), C.c_int32, C.c_void_p]),
+    "gbmpm_set_modifiers": (C.c_int, [C.c_void_p, C.POINTER(Modifier), C.c_int32]),
     "gbmpm_field_nearest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gbmpm_field_winding": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p]),
     "gbmpm_field_tri_distance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),

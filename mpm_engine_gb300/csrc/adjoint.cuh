@@ -1052,6 +1052,8 @@ int adjoint_supported(gbmpm_engine *e) {
                     "the adjoint covers jelly (0), von Mises (1), sand (2), softening von Mises (5), water (6), "
                     "mu(I) (9, 13), Newtonian (10) and tabulated viscous (12) particles; not mu(I)-Phi(I) (11)");
     if (e->cdf.n > 0) return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint does not cover CDF colliders");
+    if (e->n_bodies > 0 || e->n_mods > 0)
+        return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint does not cover rigid bodies or particle modifiers");
     return GBMPM_OK;
 }
 

@@ -89,6 +89,13 @@ struct PK {
     int *ptag;
     double *cwrench;   // [CTA][4][6] per-CTA partial sums of the blocked-deposit reaction
     float *ccache;     // tiled kernel: the scatter scan of each particle, SoA x5 (see k_particles_tiled)
+    // particle modifiers (bit m of mod_mask selects modifier m) and rigid bodies
+    int n_mods;
+    const gbmpm_modifier *mods;
+    const int *mod_mask;
+    const double *sub_time;   // start time of every substep of the tick
+    int sub;                  // the substep whose P2G this pass performs
+    int rigid_defer;          // material-8 particles leave their P2G to the rigid pass
     float grav[3];
     CdfLanes lanes;
 };
@@ -879,6 +886,45 @@ __device__ void cdf_deposit_all(const PK &k, const Stencil &s, int p, const floa
     mark_stencil_blocks(k, s);
 }
 
+// Particle modifiers before the stress and P2G of a substep (the pre-P2G operations
+// and velocity modifiers of p2g2p, mpm_solver_warp.py:1182-1196; kernels
+// :2385-2540): impulses first, then velocity overrides, each in list order, on the
+// float32 time window [start, end). Returns true when v changed.
+__device__ bool apply_modifiers(const PK &k, int mask, const float *x, float mass, float *v) {
+    const float t = (float)k.sub_time[k.sub];
+    bool changed = false;
+    for (int pass = 0; pass < 2; ++pass)
+        for (int m = 0; m < k.n_mods; ++m) {
+            if (!((mask >> m) & 1)) continue;
+            const gbmpm_modifier &d = k.mods[m];
+            if ((d.kind == 0) != (pass == 0)) continue;
+            if (!(t >= d.start_time && t < d.end_time)) continue;
+            changed = true;
+            if (d.kind == 0) {
+                const float imp[3] = {d.vec[0] / mass, d.vec[1] / mass, d.vec[2] / mass};
+#pragma unroll
+                for (int a = 0; a < 3; ++a) v[a] = v[a] + imp[a] * k.dt;
+            } else if (d.kind == 1) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) v[a] = d.vec[a];
+            } else {
+                const float off[3] = {x[0] - d.point[0], x[1] - d.point[1], x[2] - d.point[2]};
+                const float on = off[0] * d.normal[0] + off[1] * d.normal[1] + off[2] * d.normal[2];
+                const float hz[3] = {off[0] - on * d.normal[0], off[1] - on * d.normal[1], off[2] - on * d.normal[2]};
+                const float hd = sqrtf(hz[0] * hz[0] + hz[1] * hz[1] + hz[2] * hz[2]);
+                const float cosine = (off[0] * d.axis1[0] + off[1] * d.axis1[1] + off[2] * d.axis1[2]) / hd;
+                float theta = acosf(fminf(fmaxf(cosine, -1.0f), 1.0f));
+                if (!(off[0] * d.axis2[0] + off[1] * d.axis2[1] + off[2] * d.axis2[2] > 0.0f)) theta = -theta;
+                const float a1 = -hd * sinf(theta) * d.rotation_scale;
+                const float a2 = hd * cosf(theta) * d.rotation_scale;
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+                    v[a] = a1 * d.axis1[a] + a2 * d.axis2[a] + d.translation_scale * d.normal[a];
+            }
+        }
+    return changed;
+}
+
 // ---- direct kernel: one thread per particle, global gather and atomics ------
 // One kernel serves every particle pass of the schedule; `mode` selects the
 // stages (G2P, STRESS, P2G): the fused interior pass is G2P|STRESS|P2G, the tick
@@ -961,6 +1007,14 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
             v[0] = vi[0]; v[1] = vi[1]; v[2] = vi[2];
             mat_load(k.C + 9 * (size_t)p, C);
         }
+        if (k.n_mods && k.mod_mask) {
+            const int mm = k.mod_mask[p];
+            if (mm && apply_modifiers(k, mm, x, k.mass[p], v)) {
+                float *vo = k.v + 3 * (size_t)p;
+                vo[0] = v[0]; vo[1] = v[1]; vo[2] = v[2];
+            }
+        }
+        if (k.rigid_defer && mat == 8) return;   // deposits after the rigid update
         Stencil s;
         stencil(x, k.inv_dx, s);
         if (!stencil_ok(s, k.ng, k.periodic_x)) {
@@ -1171,9 +1225,13 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
             }
         }
     }
+    if (live && k.n_mods && k.mod_mask) {
+        const int mm = k.mod_mask[p];
+        if (mm && apply_modifiers(k, mm, x, k.mass[p], v)) fld_store<true, 3>(k.v, k.n, p, v);
+    }
     Stencil s;
     stencil(x, k.inv_dx, s);
-    bool want = live;
+    bool want = live && !(k.rigid_defer && mat == 8);   // rigid particles deposit after the rigid update
     if (want && !stencil_ok(s, k.ng, k.periodic_x)) {
         set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
         want = false;
@@ -2147,6 +2205,8 @@ __global__ void k_compute_cov(const float *Ft, const float *c0, int n, float *ou
 
 }  // namespace gbmpm
 
+#include "rigid.cuh"
+
 // ====================================================================== host
 using namespace gbmpm;
 
@@ -2280,6 +2340,17 @@ struct gbmpm_engine {
     // adjoint segment storage and scratch (allocated by the first adjoint call)
     DevBuf<float> adj_states, adj_scratch;
     DevBuf<float4> adj_grid;
+    // rigid bodies and particle modifiers
+    int n_bodies = 0;
+    std::vector<gbmpm_rigid_surface> rsurf;
+    DevBuf<gbmpm_rigid_body> d_bodies;
+    DevBuf<double> d_racc;                  // [body][6] gathered momentum, angular momentum
+    DevBuf<unsigned long long> d_rkey;      // [body][2] contact keys (distance, particle)
+    int n_mods = 0;
+    DevBuf<gbmpm_modifier> d_mods;
+    double *h_time = nullptr;               // pinned staging of d_time
+    size_t h_time_cap = 0;
+    DevBuf<double> d_time;                  // start time of every substep of the tick
     // profiling
     double prof_ms[GBMPM_NUM_PHASES] = {0};
     int64_t prof_n[GBMPM_NUM_PHASES] = {0};
@@ -2312,6 +2383,12 @@ PK make_pk(gbmpm_engine *e, const gbmpm_particles &P, float dt, int list) {
     k.blk_count = e->d_count.ptr + list;
     k.status = e->d_status.ptr;
     for (int a = 0; a < 3; ++a) k.grav[a] = e->M.gravity[a];
+    k.n_mods = (e->n_mods > 0 && P.mod_mask) ? e->n_mods : 0;
+    k.mods = e->d_mods.ptr;
+    k.mod_mask = P.mod_mask;
+    k.sub_time = e->d_time.ptr;
+    k.sub = 0;
+    k.rigid_defer = 0;
     if (e->cdf.n > 0 && P.cdf_tag) {
         const CdfHost &H = e->cdf;
         k.cdf_on = 1;
@@ -2384,6 +2461,10 @@ cudaError_t ensure_ws(gbmpm_engine *e) {
         {reinterpret_cast<float *>(P.selection), 1, 0, reinterpret_cast<float **>(&W.selection)},
         {cov ? P.cov : nullptr, 6, 1, &W.cov},
         {e->cdf.n > 0 ? reinterpret_cast<float *>(P.cdf_tag) : nullptr, 1, 1, reinterpret_cast<float **>(&W.cdf_tag)},
+        {e->n_bodies > 0 ? reinterpret_cast<float *>(P.rigid_id) : nullptr, 1, 0,
+         reinterpret_cast<float **>(&W.rigid_id)},
+        {e->n_bodies > 0 ? P.x_ref : nullptr, 3, 0, &W.x_ref},
+        {e->n_mods > 0 ? reinterpret_cast<float *>(P.mod_mask) : nullptr, 1, 0, reinterpret_cast<float **>(&W.mod_mask)},
     };
     size_t total = 0;
     for (const Spec &sp : spec) if (sp.ext) total += (size_t)sp.w * n;
@@ -2771,6 +2852,38 @@ void cdf_integrate(gbmpm_engine *e, double time, double dt, bool lag_prev) {
     if (!lag_prev && H.lane_prev_stale) H.copy_lane_prev();
 }
 
+// The rigid tail of substep `tail_sub` (gather, integrate, one contact per active
+// rigid surface, write-back); with `deposit` the rigid particles' P2G of substep
+// `sub` follows. perm maps working-set rows to the caller's particle order.
+void record_rigid(gbmpm_engine *e, const gbmpm_particles &P, float dtf, int tail_sub, int sub, int list, bool deposit,
+                  bool soa, const int *perm, cudaStream_t s) {
+    if (P.n == 0) return;
+    PK k = make_pk(e, P, dtf, list);   // the deposit marks the block list the next grid pass reads
+    k.sub = sub;
+    const int pb = (int)std::max<long long>(1, std::min<long long>((P.n + 255) / 256, (long long)e->num_sms * 8));
+    const int nb = e->n_bodies, bb = (nb + 63) / 64;
+    const int *rid = P.rigid_id;
+    if (soa) k_rigid_gather<true><<<pb, 256, 0, s>>>(k, rid, e->d_bodies.ptr, e->d_racc.ptr);
+    else k_rigid_gather<false><<<pb, 256, 0, s>>>(k, rid, e->d_bodies.ptr, e->d_racc.ptr);
+    k_rigid_integrate<<<bb, 64, 0, s>>>(e->d_bodies.ptr, nb, e->d_racc.ptr, dtf);
+    e->launches += 2;
+    for (const gbmpm_rigid_surface &sf : e->rsurf) {
+        for (int stage = 0; stage < 2; ++stage) {
+            if (soa)
+                k_rigid_contact<true><<<pb, 256, 0, s>>>(k, rid, P.x_ref, e->d_bodies.ptr, sf, e->d_rkey.ptr, stage, perm);
+            else
+                k_rigid_contact<false><<<pb, 256, 0, s>>>(k, rid, P.x_ref, e->d_bodies.ptr, sf, e->d_rkey.ptr, stage,
+                                                          nullptr);
+        }
+        if (soa) k_rigid_impulse<true><<<bb, 64, 0, s>>>(k, e->d_bodies.ptr, nb, P.x_ref, e->d_rkey.ptr, sf, tail_sub);
+        else k_rigid_impulse<false><<<bb, 64, 0, s>>>(k, e->d_bodies.ptr, nb, P.x_ref, e->d_rkey.ptr, sf, tail_sub);
+        e->launches += 3;
+    }
+    if (soa) k_rigid_update<true><<<pb, 256, 0, s>>>(k, rid, P.x_ref, e->d_bodies.ptr, deposit ? 1 : 0);
+    else k_rigid_update<false><<<pb, 256, 0, s>>>(k, rid, P.x_ref, e->d_bodies.ptr, deposit ? 1 : 0);
+    e->launches++;
+}
+
 // Records the launches of one tick on stream s.
 // With CPIC lanes the host stamps and integrates lane poses between the
 // launches (t0 = the tick's start time, dt its float64 substep), so such ticks
@@ -2796,11 +2909,13 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
     if (reorder) timed(5, [&] { perm = record_ws_begin(e, s); });
     const gbmpm_particles &P = reorder ? e->W : e->P;
     const bool cdf = e->cdf.n > 0;
+    const bool rigid = e->n_bodies > 0 && P.rigid_id && P.x_ref;
     double tc = t0;
     for (int sub = 0; sub < S; ++sub) {
         int list = sub & 1;
         if (cdf) cdf_stamp(e, tc, fused, s);
         PK k = make_pk(e, P, dtf, list);
+        k.sub = pose_offset + sub;
         bool last_stress = fused ? (sub == S - 1) : true;
         if (!fused || sub == 0) {
             int mode = PASS_STRESS | PASS_P2G | (last_stress ? PASS_STORE_ALL : 0);
@@ -2809,7 +2924,10 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
             // a CPIC ghost velocity starts from the particle's previous velocity
             int mode = PASS_G2P | PASS_STRESS | PASS_P2G | (last_stress ? PASS_STORE_ALL : 0) |
                        (cdf ? PASS_STORE_VC : 0);
+            k.rigid_defer = rigid ? 1 : 0;
             timed(2, [&] { launch_particles(e, k, mode, reorder, s); });
+            // the rigid tail of the previous substep, then its rigid particles' P2G
+            if (rigid) record_rigid(e, P, dtf, pose_offset + sub - 1, pose_offset + sub, list, true, reorder, perm, s);
         }
         timed(3, [&] { launch_grid(e, dtf, pose_offset + sub, list, s); });
         if (cdf) cdf_integrate(e, tc, dt, fused);
@@ -2817,6 +2935,7 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
         if (!fused) {
             PK kg = make_pk(e, P, dtf, list);
             timed(4, [&] { launch_particles(e, kg, PASS_G2P | PASS_RESET_LISTS, reorder, s); });
+            if (rigid) record_rigid(e, P, dtf, pose_offset + sub, pose_offset + sub, list, false, reorder, perm, s);
         }
     }
     if (fused) {
@@ -2826,6 +2945,7 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
         }
         PK k = make_pk(e, P, dtf, 0);
         timed(4, [&] { launch_particles(e, k, PASS_G2P | PASS_RESET_LISTS, reorder, s); });
+        if (rigid) record_rigid(e, P, dtf, pose_offset + S - 1, pose_offset + S - 1, 0, false, reorder, perm, s);
     }
     if (reorder) {
         timed(5, [&] {
@@ -2881,6 +3001,8 @@ void gbmpm_engine_destroy(gbmpm_engine *e) {
     if (e->pose_done) cudaEventDestroy(e->pose_done);
     if (e->h_pose) cudaFreeHost(e->h_pose);
     if (e->h_coldev) cudaFreeHost(e->h_coldev);
+    if (e->h_time) cudaFreeHost(e->h_time);
+    e->d_bodies.release(); e->d_racc.release(); e->d_rkey.release(); e->d_mods.release(); e->d_time.release();
     e->d_tab.release(); e->d_cols.release(); e->d_pose.release(); e->d_wrench.release();
     e->d_flag.release(); e->d_list.release(); e->d_count.release(); e->d_status.release();
     e->d_guard.release(); e->d_keys[0].release(); e->d_keys[1].release(); e->d_skeys.release(); e->d_kminmax.release(); e->d_idx[0].release();
@@ -2992,6 +3114,60 @@ int gbmpm_get_colliders(gbmpm_engine *e, gbmpm_collider *c, int32_t n) {
 // append lanes or change existing ones. A lane whose centre or quaternion changed
 // is restamped at the next substep; any pose or rate change refreshes the lane
 // arrays the transfer passes read.
+int gbmpm_set_rigid(gbmpm_engine *e, const gbmpm_rigid_body *bodies, int32_t n_bodies,
+                    const gbmpm_rigid_surface *surfaces, int32_t n_surfaces) {
+    if (!e || n_bodies < 0 || n_surfaces < 0 || (n_bodies > 0 && !bodies) || (n_surfaces > 0 && !surfaces))
+        return fail(GBMPM_ERR_ARG, "bad rigid-body arguments");
+    if (n_surfaces > GBMPM_MAX_RIGID_SURFACES)
+        return fail(GBMPM_ERR_ARG, "at most " + std::to_string(GBMPM_MAX_RIGID_SURFACES) + " rigid surfaces");
+    if (!e->bound) return fail(GBMPM_ERR_STATE, "buffers not bound (call gbmpm_bind)");
+    if (n_bodies > 0 && e->P.n > 0 && (!e->P.rigid_id || !e->P.x_ref))
+        return fail(GBMPM_ERR_ARG, "rigid bodies need particles.rigid_id and particles.x_ref");
+    for (int b = 0; b < n_bodies; ++b)
+        if (!(bodies[b].mass > 0.0f)) return fail(GBMPM_ERR_ARG, "rigid body " + std::to_string(b) + " has no mass");
+    GB_CUDA(cudaDeviceSynchronize());
+    if (n_bodies > 0) {
+        GB_CUDA(e->d_bodies.ensure(n_bodies));
+        GB_CUDA(e->d_racc.ensure(6 * (size_t)n_bodies));
+        GB_CUDA(e->d_rkey.ensure(2 * (size_t)n_bodies));
+        GB_CUDA(cudaMemcpy(e->d_bodies.ptr, bodies, n_bodies * sizeof(gbmpm_rigid_body), cudaMemcpyHostToDevice));
+        GB_CUDA(cudaMemset(e->d_racc.ptr, 0, 6 * (size_t)n_bodies * sizeof(double)));
+        GB_CUDA(cudaMemset(e->d_rkey.ptr, 0xff, 2 * (size_t)n_bodies * sizeof(unsigned long long)));
+    }
+    e->rsurf.assign(surfaces, surfaces + n_surfaces);
+    if ((e->n_bodies == 0) != (n_bodies == 0)) e->ws_n = -1;   // the working set gains or drops the rigid fields
+    e->n_bodies = n_bodies;
+    mark_dirty(e);
+    return GBMPM_OK;
+}
+
+int gbmpm_get_rigid(gbmpm_engine *e, gbmpm_rigid_body *bodies, int32_t n_bodies, void *stream) {
+    if (!e || !bodies || n_bodies < 0 || n_bodies > e->n_bodies) return fail(GBMPM_ERR_ARG, "bad rigid-body read");
+    if (n_bodies == 0) return GBMPM_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    GB_CUDA(cudaMemcpyAsync(bodies, e->d_bodies.ptr, n_bodies * sizeof(gbmpm_rigid_body), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    return GBMPM_OK;
+}
+
+int gbmpm_set_modifiers(gbmpm_engine *e, const gbmpm_modifier *mods, int32_t n) {
+    if (!e || n < 0 || (n > 0 && !mods)) return fail(GBMPM_ERR_ARG, "bad modifier arguments");
+    if (n > GBMPM_MAX_MODIFIERS) return fail(GBMPM_ERR_ARG, "at most 32 particle modifiers");
+    if (!e->bound) return fail(GBMPM_ERR_STATE, "buffers not bound (call gbmpm_bind)");
+    if (n > 0 && e->P.n > 0 && !e->P.mod_mask) return fail(GBMPM_ERR_ARG, "particle modifiers need particles.mod_mask");
+    for (int m = 0; m < n; ++m)
+        if (mods[m].kind < 0 || mods[m].kind > 2) return fail(GBMPM_ERR_ARG, "modifier kind must be 0, 1 or 2");
+    GB_CUDA(cudaDeviceSynchronize());
+    if (n > 0) {
+        GB_CUDA(e->d_mods.ensure(n));
+        GB_CUDA(cudaMemcpy(e->d_mods.ptr, mods, n * sizeof(gbmpm_modifier), cudaMemcpyHostToDevice));
+    }
+    if ((e->n_mods == 0) != (n == 0)) e->ws_n = -1;
+    e->n_mods = n;
+    mark_dirty(e);
+    return GBMPM_OK;
+}
+
 int gbmpm_set_cdf(gbmpm_engine *e, const gbmpm_cdf *lanes, int32_t n) {
     if (!e || (n > 0 && !lanes)) return fail(GBMPM_ERR_ARG, "null argument");
     if (!e->modeled) return fail(GBMPM_ERR_STATE, "model not set (call gbmpm_set_model)");
@@ -3118,6 +3294,21 @@ int prepare_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int
                                 cudaMemcpyHostToDevice, s));
         e->cols_upload = false;
     }
+    // substep start times (modifier and rigid-surface windows), as the tick advances them
+    if (e->h_time_cap < (size_t)substeps) {
+        if (e->h_time) cudaFreeHost(e->h_time);
+        e->h_time = nullptr;
+        GB_CUDA(cudaMallocHost(&e->h_time, (size_t)substeps * sizeof(double)));
+        e->h_time_cap = substeps;
+    }
+    double *old_time = e->d_time.ptr;
+    GB_CUDA(e->d_time.ensure(substeps));
+    if (e->d_time.ptr != old_time) mark_dirty(e);
+    {
+        double t = *time;
+        for (int i = 0; i < substeps; ++i) { e->h_time[i] = t; t = t + dt; }
+    }
+    GB_CUDA(cudaMemcpyAsync(e->d_time.ptr, e->h_time, (size_t)substeps * sizeof(double), cudaMemcpyHostToDevice, s));
     build_pose_table(e, *time, dt, substeps);
     GB_CUDA(cudaMemcpyAsync(e->d_pose.ptr, e->h_pose, need * sizeof(PoseRec), cudaMemcpyHostToDevice, s));
     GB_CUDA(cudaEventRecord(e->pose_done, s));
@@ -3296,8 +3487,9 @@ int gbmpm_sort_particles(gbmpm_engine *e, double dx, int32_t *sorted_out, int32_
     for (float *a : f1) GB_CUDA(permute(a, 1));
     float *c6[] = {P.init_cov, P.cov};
     for (float *a : c6) GB_CUDA(permute(a, 6));
-    int *i1[] = {P.selection, P.material, P.cdf_tag};
+    int *i1[] = {P.selection, P.material, P.cdf_tag, P.rigid_id, P.mod_mask};
     for (int *a : i1) GB_CUDA(permute(reinterpret_cast<float *>(a), 1));
+    GB_CUDA(permute(P.x_ref, 3));
     if (perm_out) GB_CUDA(cudaMemcpyAsync(perm_out, perm, (size_t)n * sizeof(int), cudaMemcpyDeviceToDevice, s));
     if (sorted_out) *sorted_out = 1;
     return GBMPM_OK;

@@ -237,3 +237,111 @@ def material_mask_bit(name) -> int:
 
 def is_finite_number(x) -> bool:
     return isinstance(x, (int, float)) and math.isfinite(float(x))
+
+
+# ---- rigid bodies and particle modifiers ----------------------------------------
+def rigid_bodies(x, mass, material, rigid_id):
+    """Bodies of the material-8 particles grouped by rigid_id (finalize_rigid_bodies,
+    mpm_solver_warp.py:834-879): mass, centre of mass (float32 sums as the reference
+    forms them), body-frame inverse inertia (float64 sum, inverted, stored float32),
+    identity orientation, at rest; plus each rigid particle's body-frame position
+    x - x_cm. Returns (list of _abi.RigidBody, x_ref float32 [n][3])."""
+    x = np.asarray(x, np.float32)
+    m = np.asarray(mass, np.float32)
+    rigid = np.asarray(material) == 8
+    rid = np.asarray(rigid_id)
+    x_ref = np.zeros_like(x)
+    if not rigid.any():
+        return [], x_ref
+    out = []
+    for b in range(int(rid[rigid].max()) + 1):
+        idx = np.nonzero(rigid & (rid == b))[0]
+        if len(idx) == 0:
+            raise ValueError(f"rigid body {b} has no particles (obj_id values must be 0 .. n-1)")
+        mb = m[idx]
+        M = np.float32(mb.sum())
+        com = ((x[idx] * mb[:, None]).sum(axis=0) / M).astype(np.float32)
+        r = (x[idx] - com).astype(np.float32)
+        x_ref[idx] = r
+        r64, m64 = r.astype(np.float64), mb.astype(np.float64)
+        inertia = np.eye(3) * (m64 * (r64 * r64).sum(axis=1)).sum() - np.einsum("p,pi,pj->ij", m64, r64, r64)
+        inv = np.linalg.inv(inertia).astype(np.float32)
+        rec = _abi.RigidBody()
+        rec.x_cm[:] = tuple(float(c) for c in com)
+        rec.R[:] = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0)
+        rec.mass = float(M)
+        rec.inv_inertia[:] = tuple(float(c) for c in inv.reshape(-1))
+        out.append(rec)
+    return out, x_ref
+
+
+def rigid_surface(point, normal, friction, restitution, start_time=0.0, end_time=999.0):
+    """add_surface_collider's rigid contact record (mpm_solver_warp.py:1880-1927)."""
+    n = np.asarray(normal, dtype=np.float64)
+    n = n / np.sqrt((n * n).sum())
+    rec = _abi.RigidSurface()
+    rec.point[:] = tuple(float(c) for c in point)
+    rec.normal[:] = tuple(float(c) for c in n)
+    rec.friction, rec.restitution = float(friction), float(restitution)
+    rec.start_time, rec.end_time = float(start_time), float(end_time)
+    return rec
+
+
+def impulse_modifier(force, dt, num_dt, start_time):
+    """add_impulse_on_particles (mpm_solver_warp.py:2385-2427): active for num_dt
+    substeps from start_time."""
+    rec = _abi.Modifier()
+    rec.kind = 0
+    rec.start_time = float(start_time)
+    rec.end_time = float(start_time + dt * num_dt)
+    rec.vec[:] = tuple(float(c) for c in force)
+    return rec
+
+
+def translation_modifier(velocity, start_time, end_time):
+    """enforce_particle_velocity_translation (mpm_solver_warp.py:2431-2469)."""
+    rec = _abi.Modifier()
+    rec.kind = 1
+    rec.start_time, rec.end_time = float(start_time), float(end_time)
+    rec.vec[:] = tuple(float(c) for c in velocity)
+    return rec
+
+
+def rotation_modifier(point, normal, rotation_scale, translation_scale, start_time, end_time):
+    """enforce_particle_velocity_rotation (mpm_solver_warp.py:2475-2539): the unit axis
+    and the two horizontal axes the reference derives from (1, 1, 1) (or
+    (0.72, 0.37, -0.67) when that is nearly along the axis), in float32."""
+    n = np.asarray(normal, dtype=np.float32)
+    n = (n * np.float32(1.0 / np.sqrt(np.float32((n.astype(np.float64) ** 2).sum())))).astype(np.float32)
+    h1 = np.array([1.0, 1.0, 1.0], np.float32)
+    if abs(float(np.dot(n, h1))) < 0.01:
+        h1 = np.array([0.72, 0.37, -0.67], np.float32)
+    h1 = (h1 - np.float32(np.dot(h1, n)) * n).astype(np.float32)
+    h1 = (h1 * np.float32(1.0 / np.linalg.norm(h1))).astype(np.float32)
+    h2 = np.cross(h1, n).astype(np.float32)
+    rec = _abi.Modifier()
+    rec.kind = 2
+    rec.start_time, rec.end_time = float(start_time), float(end_time)
+    rec.point[:] = tuple(float(c) for c in point)
+    rec.normal[:] = tuple(float(c) for c in n)
+    rec.axis1[:] = tuple(float(c) for c in h1)
+    rec.axis2[:] = tuple(float(c) for c in h2)
+    rec.rotation_scale, rec.translation_scale = float(rotation_scale), float(translation_scale)
+    return rec
+
+
+def box_mask(x, point, size):
+    """Particles with |x - point| < size on every axis (the modifiers' box selection,
+    mpm_utils.py:1321-1345)."""
+    x = np.asarray(x, np.float32)
+    return (np.abs(x - np.asarray(point, np.float32)) < np.asarray(size, np.float32)).all(axis=1)
+
+
+def cylinder_mask(x, point, unit_normal, half_height, radius):
+    """Particles inside the cylinder about the axis (mpm_utils.py:1349-1362)."""
+    x = np.asarray(x, np.float32)
+    n = np.asarray(unit_normal, np.float32)
+    off = x - np.asarray(point, np.float32)
+    along = off @ n
+    horiz = np.linalg.norm(off - along[:, None] * n, axis=1)
+    return (np.abs(along) < np.float32(half_height)) & (horiz < np.float32(radius))

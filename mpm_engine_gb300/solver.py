@@ -138,6 +138,16 @@ class _ModelView:
     cdf_mask_off = 0
 
 
+class _HostArray:
+    """A host array behind Warp's `.numpy()` accessor."""
+
+    def __init__(self, a):
+        self._a = a
+
+    def numpy(self):
+        return self._a
+
+
 class _SimShim:
     """The parts of MPM_Simulator_WARP that tests and scripts touch through
     `Solver._sim` (mpm_solver_warp.py), mapped onto this engine."""
@@ -162,6 +172,52 @@ class _SimShim:
     @property
     def n_particles(self) -> int:
         return self._s._n
+
+    # rigid-body arrays of MPM_Simulator_WARP (mpm_solver_warp.py:495-504), read from the engine
+    def _rigid_field(self, name, shape):
+        s = self._s
+        recs = s._rigid_bodies() if s._n_bodies else []
+        return _HostArray(np.array([np.array(getattr(r, name)[:], np.float32).reshape(shape) for r in recs],
+                                   np.float32).reshape((len(recs),) + shape))
+
+    @property
+    def rigid_mass(self):
+        recs = self._s._rigid_bodies() if self._s._n_bodies else []
+        return _HostArray(np.array([r.mass for r in recs], np.float32))
+
+    @property
+    def rigid_x_cm(self):
+        return self._rigid_field("x_cm", (3,))
+
+    @property
+    def rigid_v_cm(self):
+        return self._rigid_field("v_cm", (3,))
+
+    @property
+    def rigid_omega(self):
+        return self._rigid_field("omega", (3,))
+
+    @property
+    def rigid_orientation(self):
+        return self._rigid_field("R", (3, 3))
+
+    def finalize_rigid_bodies(self, device=None):
+        self._s.finalize_rigid_bodies()
+
+    def set_rigid_body_velocity(self, body_id, v_cm=(0, 0, 0), omega=(0, 0, 0), device=None):
+        self._s.set_rigid_body_velocity(body_id, v_cm, omega)
+
+    def add_impulse_on_particles(self, force, dt, point=(1, 1, 1), size=(1, 1, 1), num_dt=1, start_time=0.0,
+                                 device=None):
+        self._s.add_impulse_on_particles(force, dt, point, size, num_dt, start_time)
+
+    def enforce_particle_velocity_translation(self, point, size, velocity, start_time, end_time, device=None):
+        self._s.enforce_particle_velocity_translation(point, size, velocity, start_time, end_time)
+
+    def enforce_particle_velocity_rotation(self, point, normal, half_height_and_radius, rotation_scale,
+                                           translation_scale, start_time, end_time, device=None):
+        self._s.enforce_particle_velocity_rotation(point, normal, half_height_and_radius, rotation_scale,
+                                                   translation_scale, start_time, end_time)
 
     @property
     def time(self) -> float:
@@ -248,6 +304,8 @@ class Solver:
         self._cdf_guard: dict = {}
         self._cdf_keep: list = []      # device copies of the lanes' fields
         self._rigid_surfaces: list = []
+        self._n_bodies = 0
+        self._mods: list = []          # particle modifier records, in registration order
         self._update_cov = False
 
     # ------------------------------------------------------------------ setup
@@ -298,6 +356,8 @@ class Solver:
             "material": torch.zeros(n, device=dev, dtype=torch.int32),
             "selection": torch.zeros(n, device=dev, dtype=torch.int32),
             "cdf_tag": torch.zeros(n, device=dev, dtype=torch.int32),
+            "rigid_id": torch.zeros(n, device=dev, dtype=torch.int32), "x_ref": torch.zeros(n, 3, **f),
+            "mod_mask": torch.zeros(n, device=dev, dtype=torch.int32),
             "init_cov": None, "cov": None,
         }
         if cov6 is not None:
@@ -328,7 +388,8 @@ class Solver:
         p = _abi.Particles()
         p.n = self._n
         for k in ("x", "v", "C", "F", "F_trial", "L", "stress", "mass", "vol", "density", "Jp", "mu", "lam",
-                  "yield_stress", "material", "selection", "cov", "init_cov", "cdf_tag"):
+                  "yield_stress", "material", "selection", "cov", "init_cov", "cdf_tag", "rigid_id", "x_ref",
+                  "mod_mask"):
             setattr(p, k, self._ptr(k))
         g = _abi.Grid()
         g.n_grid = int(self.grid.n_grid)
@@ -392,6 +453,8 @@ class Solver:
             m.rpic_damping = host.f32(kw["rpic_damping"])
         if "grid_v_damping_scale" in kw:
             m.grid_v_damping_scale = host.f32(kw["grid_v_damping_scale"])
+        if "obj_id" in kw:   # rigid body of material-8 particles (mpm_solver_warp.py:1755-1758)
+            t["rigid_id"][sl] = int(kw["obj_id"])
         if "additional_material_params" in kw:
             raise NotImplementedError("regional additional_material_params are not supported")
         self._model_dirty = True
@@ -433,8 +496,106 @@ class Solver:
         self._apply_params({"material": name, **params, **overrides}, lo=int(start), hi=int(end))
         return self
 
+    # ------------------------------------------------------------- rigid bodies
     def finalize_rigid_bodies(self) -> Solver:
-        raise NotImplementedError("rigid bodies are not part of this engine")
+        """Each rigid body's mass, centre of mass and body-frame inverse inertia from
+        the particles assigned material "rigid" and their obj_id, and every rigid
+        particle's body-frame position (finalize_rigid_bodies, mpm_solver_warp.py:
+        834-879). Bodies start at rest with identity orientation. Call after every
+        set_material_range and before the first step."""
+        self._require_loaded()
+        torch = _torch()
+        t = self._t
+        recs, x_ref = host.rigid_bodies(t["x"].cpu().numpy(), t["mass"].cpu().numpy(), t["material"].cpu().numpy(),
+                                        t["rigid_id"].cpu().numpy())
+        if not recs:
+            return self
+        t["x_ref"].copy_(torch.from_numpy(x_ref))
+        self._n_bodies = len(recs)
+        self._sim.n_rigid_bodies = len(recs)
+        self._push_rigid((_abi.RigidBody * len(recs))(*recs))
+        return self
+
+    def _surface_records(self):
+        arr = (_abi.RigidSurface * max(1, len(self._rigid_surfaces)))()
+        for i, rec in enumerate(self._rigid_surfaces):
+            arr[i] = rec
+        return arr
+
+    def _push_rigid(self, bodies=None) -> None:
+        if self._n_bodies == 0:
+            return
+        if bodies is None:
+            bodies = self._rigid_bodies()
+        _abi.check(self._eng.lib.gbmpm_set_rigid(self._eng.h, bodies, self._n_bodies, self._surface_records(),
+                                                 len(self._rigid_surfaces)), "gbmpm_set_rigid")
+
+    def _rigid_bodies(self):
+        arr = (_abi.RigidBody * self._n_bodies)()
+        _abi.check(self._eng.lib.gbmpm_get_rigid(self._eng.h, arr, self._n_bodies, self._stream()), "gbmpm_get_rigid")
+        return arr
+
+    def rigid_state(self, body: int = 0) -> dict:
+        """State of one rigid body: com (3,), v (3,), omega (3,), R (3, 3)
+        (core/solver.py:200-210)."""
+        if not 0 <= body < self._n_bodies:
+            raise IndexError(f"no rigid body {body}")
+        r = self._rigid_bodies()[body]
+        return {"com": np.array(r.x_cm[:], np.float32), "v": np.array(r.v_cm[:], np.float32),
+                "omega": np.array(r.omega[:], np.float32), "R": np.array(r.R[:], np.float32).reshape(3, 3)}
+
+    def set_rigid_body_velocity(self, body_id: int, v_cm=(0.0, 0.0, 0.0), omega=(0.0, 0.0, 0.0)) -> Solver:
+        """Linear and angular velocity of one rigid body (mpm_solver_warp.py:881-885)."""
+        bodies = self._rigid_bodies()
+        bodies[body_id].v_cm[:] = tuple(float(c) for c in v_cm)
+        bodies[body_id].omega[:] = tuple(float(c) for c in omega)
+        self._push_rigid(bodies)
+        return self
+
+    # ------------------------------------------------------- particle modifiers
+    def _add_modifier(self, rec, mask) -> None:
+        if len(self._mods) >= _abi.MAX_MODIFIERS:
+            raise ValueError(f"at most {_abi.MAX_MODIFIERS} particle modifiers")
+        bit = len(self._mods)
+        self._t["mod_mask"] |= (mask.to(_torch().int32) << bit)
+        self._mods.append(rec)
+        arr = (_abi.Modifier * len(self._mods))(*self._mods)
+        _abi.check(self._eng.lib.gbmpm_set_modifiers(self._eng.h, arr, len(self._mods)), "gbmpm_set_modifiers")
+
+    def _mask(self, mask_np):
+        return _torch().from_numpy(mask_np).to(self._t["x"].device)
+
+    def add_impulse_on_particles(self, force, dt, point=(1, 1, 1), size=(1, 1, 1), num_dt: int = 1,
+                                 start_time: float = 0.0) -> Solver:
+        """For num_dt substeps from start_time, v += force / m * dt on the particles
+        within the box |x - point| < size, chosen now (mpm_solver_warp.py:2385-2427)."""
+        self._require_loaded()
+        rec = host.impulse_modifier(force, dt, num_dt, start_time)
+        self._add_modifier(rec, self._mask(host.box_mask(self.x(), point, size)))
+        self._sim.pre_p2g_operations.append(rec)
+        return self
+
+    def enforce_particle_velocity_translation(self, point, size, velocity, start_time, end_time) -> Solver:
+        """Between start_time and end_time, v = velocity on the particles within the box
+        |x - point| < size, chosen now (mpm_solver_warp.py:2431-2469)."""
+        self._require_loaded()
+        rec = host.translation_modifier(velocity, start_time, end_time)
+        self._add_modifier(rec, self._mask(host.box_mask(self.x(), point, size)))
+        self._sim.particle_velocity_modifiers.append(rec)
+        return self
+
+    def enforce_particle_velocity_rotation(self, point, normal, half_height_and_radius, rotation_scale,
+                                           translation_scale, start_time, end_time) -> Solver:
+        """Between start_time and end_time, the particles within the cylinder about the
+        axis through `point` along `normal` (half height, radius), chosen now, turn at
+        rotation_scale about the axis and move at translation_scale along it
+        (mpm_solver_warp.py:2475-2539)."""
+        self._require_loaded()
+        rec = host.rotation_modifier(point, normal, rotation_scale, translation_scale, start_time, end_time)
+        mask = host.cylinder_mask(self.x(), point, rec.normal[:], half_height_and_radius[0], half_height_and_radius[1])
+        self._add_modifier(rec, self._mask(mask))
+        self._sim.particle_velocity_modifiers.append(rec)
+        return self
 
     # -------------------------------------------------------------- colliders
     def _add_collider(self, rec, slots: int = 1) -> int:
@@ -476,7 +637,10 @@ class Solver:
         if restitution != 0.0:
             if not (0.0 < restitution <= 1.0):
                 raise ValueError("restitution must be between 0 (exclusive) and 1 (inclusive).")
-            self._rigid_surfaces.append((tuple(point), tuple(normal), friction, restitution))
+            if len(self._rigid_surfaces) >= _abi.MAX_RIGID_SURFACES:
+                raise ValueError(f"at most {_abi.MAX_RIGID_SURFACES} rigid contact surfaces")
+            self._rigid_surfaces.append(host.rigid_surface(point, normal, friction, restitution))
+            self._push_rigid()
         self._pull_colliders()
         self._add_collider(rec)
         return self
@@ -1073,7 +1237,8 @@ class Solver:
         out = {k: (None if v is None else v.detach().cpu().numpy().copy())
                for k, v in self._t.items() if k in ("x", "v", "C", "F", "F_trial", "L", "stress", "mass", "vol",
                                                     "density", "Jp", "mu", "lam", "yield_stress", "material",
-                                                    "selection", "cov", "init_cov", "cdf_tag")}
+                                                    "selection", "cov", "init_cov", "cdf_tag", "rigid_id", "x_ref",
+                                                    "mod_mask")}
         model = _abi.Model()
         C.memmove(C.byref(model), C.byref(self._model), C.sizeof(_abi.Model))
         out["model"] = model
@@ -1094,6 +1259,9 @@ class Solver:
             lanes.append(r)
         out["cdf_lanes"] = lanes
         out["cdf_host"] = {t.data_ptr(): t.cpu().numpy().copy() for t in self._cdf_keep}
+        out["rigid_bodies"] = list(self._rigid_bodies()) if self._n_bodies else []
+        out["rigid_surfaces"] = list(self._surface_records())[:len(self._rigid_surfaces)]
+        out["modifiers"] = list(self._mods)
         out["time"] = self._time
         return out
 

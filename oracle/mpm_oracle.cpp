@@ -34,6 +34,7 @@
 #include <cstring>
 #include <numeric>
 #include <vector>
+#include <functional>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -1367,11 +1368,217 @@ void grid_update(Grid& G, const gbmpm_model* M, gbmpm_collider* cols, int ncol, 
     }
 }
 
+// ---- rigid bodies and particle modifiers (split pipeline order) ----------------
+struct RigidState {
+    std::vector<gbmpm_rigid_body> bodies;
+    std::vector<gbmpm_rigid_surface> surf;
+    std::vector<gbmpm_modifier> mods;
+};
+RigidState g_rigid;
+
+// pre-P2G operations and velocity modifiers (mpm_solver_warp.py:1182-1196,
+// 2385-2540) on every selected particle whose mod_mask bit is set: impulses first,
+// then velocity overrides, each in list order, on the float32 window [start, end)
+void apply_modifiers(const gbmpm_particles* P, int p, float time_f, float dt) {
+    const int mask = P->mod_mask ? P->mod_mask[p] : 0;
+    if (!mask) return;
+    float* v = P->v + 3 * (size_t)p;
+    const float* x = P->x + 3 * (size_t)p;
+    for (int pass = 0; pass < 2; ++pass)
+        for (size_t m = 0; m < g_rigid.mods.size(); ++m) {
+            const gbmpm_modifier& d = g_rigid.mods[m];
+            if (!((mask >> m) & 1) || (d.kind == 0) != (pass == 0)) continue;
+            if (!(time_f >= d.start_time && time_f < d.end_time)) continue;
+            if (d.kind == 0) {
+                const float mass = P->mass[p];
+                for (int a = 0; a < 3; ++a) v[a] = v[a] + (d.vec[a] / mass) * dt;
+            } else if (d.kind == 1) {
+                for (int a = 0; a < 3; ++a) v[a] = d.vec[a];
+            } else {
+                float off[3], hz[3];
+                for (int a = 0; a < 3; ++a) off[a] = x[a] - d.point[a];
+                const float on = off[0] * d.normal[0] + off[1] * d.normal[1] + off[2] * d.normal[2];
+                for (int a = 0; a < 3; ++a) hz[a] = off[a] - on * d.normal[a];
+                const float hd = std::sqrt(hz[0] * hz[0] + hz[1] * hz[1] + hz[2] * hz[2]);
+                const float cosine = (off[0] * d.axis1[0] + off[1] * d.axis1[1] + off[2] * d.axis1[2]) / hd;
+                float theta = std::acos(std::min(std::max(cosine, -1.0f), 1.0f));
+                if (!(off[0] * d.axis2[0] + off[1] * d.axis2[1] + off[2] * d.axis2[2] > 0.0f)) theta = -theta;
+                const float a1 = -hd * std::sin(theta) * d.rotation_scale;
+                const float a2 = hd * std::cos(theta) * d.rotation_scale;
+                for (int a = 0; a < 3; ++a) v[a] = a1 * d.axis1[a] + a2 * d.axis2[a] + d.translation_scale * d.normal[a];
+            }
+        }
+}
+
+inline void rmul(const float* a, const float* b, float* c) {   // row-major 3x3 product
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) c[3 * i + j] = a[3 * i] * b[j] + a[3 * i + 1] * b[3 + j] + a[3 * i + 2] * b[6 + j];
+}
+inline void rmulT(const float* a, const float* b, float* c) {  // a b^T
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) c[3 * i + j] = a[3 * i] * b[3 * j] + a[3 * i + 1] * b[3 * j + 1] + a[3 * i + 2] * b[3 * j + 2];
+}
+
+// the rigid tail of one substep (_p2g2p_tail, mpm_solver_warp.py:1338-1367):
+// rigid_g2p_accumulate, rigid_body_integrate, _apply_rigid_restitution (deepest
+// particle by float64 distance, lowest index on a tie) and rigid_particle_update
+void rigid_tail(const gbmpm_particles* P, const gbmpm_model* M, Grid& G, double time, float dt,
+                const std::function<bool(int)>& sel) {
+    const int nb = (int)g_rigid.bodies.size();
+    if (nb == 0) return;
+    std::vector<double> acc(6 * (size_t)nb, 0.0);
+    for (int p = 0; p < P->n; ++p) {
+        if (!sel(p) || P->material[p] != 8) continue;
+        Weights W;
+        bspline(P->x + 3 * (size_t)p, M->inv_dx, W);
+        float vi[3] = {0.0f, 0.0f, 0.0f};
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                for (int k = 0; k < 3; ++k) {
+                    const float w = W.w[0][i] * W.w[1][j] * W.w[2][k];
+                    const size_t id = G.idx(W.base[0] + i, W.base[1] + j, W.base[2] + k);
+                    for (int a = 0; a < 3; ++a) vi[a] = vi[a] + G.vout[3 * id + a] * w;
+                }
+        const int b = P->rigid_id[p];
+        const float m = P->mass[p];
+        const float* x = P->x + 3 * (size_t)p;
+        const float r[3] = {x[0] - g_rigid.bodies[b].x_cm[0], x[1] - g_rigid.bodies[b].x_cm[1],
+                            x[2] - g_rigid.bodies[b].x_cm[2]};
+        const float pm[3] = {vi[0] * m, vi[1] * m, vi[2] * m};
+        const float am[3] = {r[1] * pm[2] - r[2] * pm[1], r[2] * pm[0] - r[0] * pm[2], r[0] * pm[1] - r[1] * pm[0]};
+        for (int a = 0; a < 3; ++a) { acc[6 * b + a] += pm[a]; acc[6 * b + 3 + a] += am[a]; }
+    }
+    for (int b = 0; b < nb; ++b) {
+        gbmpm_rigid_body& r = g_rigid.bodies[b];
+        float v[3], w[3], T1[9], Iw[9];
+        for (int a = 0; a < 3; ++a) v[a] = (float)acc[6 * b + a] / r.mass;
+        rmul(r.R, r.inv_inertia, T1);
+        rmulT(T1, r.R, Iw);
+        const float L[3] = {(float)acc[6 * b + 3], (float)acc[6 * b + 4], (float)acc[6 * b + 5]};
+        for (int i = 0; i < 3; ++i) w[i] = Iw[3 * i] * L[0] + Iw[3 * i + 1] * L[1] + Iw[3 * i + 2] * L[2];
+        for (int a = 0; a < 3; ++a) r.x_cm[a] = r.x_cm[a] + v[a] * dt;
+        const float Wk[9] = {0.0f, -w[2], w[1], w[2], 0.0f, -w[0], -w[1], w[0], 0.0f};
+        float WR[9], Rn[9];
+        rmul(Wk, r.R, WR);
+        for (int i = 0; i < 9; ++i) Rn[i] = r.R[i] + WR[i] * dt;
+        M3 Rm = load33(Rn), U, V;
+        V3 sg;
+        svd3_impl(Rm, U, sg, V);
+        store33(r.R, mmul(U, mT(V)));
+        for (int a = 0; a < 3; ++a) { r.v_cm[a] = v[a]; r.omega[a] = w[a]; }
+        for (const gbmpm_rigid_surface& sf : g_rigid.surf) {
+            if (!(time >= sf.start_time && time < sf.end_time)) continue;
+            double dmin = 0.0;
+            int pmin = -1;
+            for (int p = 0; p < P->n; ++p) {
+                if (!sel(p) || P->material[p] != 8 || P->rigid_id[p] != b) continue;
+                const float* xr = P->x_ref + 3 * (size_t)p;
+                double d = 0.0;
+                for (int i = 0; i < 3; ++i) {
+                    const float xw = r.x_cm[i] + (r.R[3 * i] * xr[0] + r.R[3 * i + 1] * xr[1] + r.R[3 * i + 2] * xr[2]);
+                    d += ((double)xw - sf.point[i]) * sf.normal[i];
+                }
+                if (pmin < 0 || d < dmin) { dmin = d; pmin = p; }
+            }
+            if (pmin < 0 || !(dmin < 0.0)) continue;
+            const double* n = sf.normal;
+            const float* xr = P->x_ref + 3 * (size_t)pmin;
+            double xc[3];
+            for (int i = 0; i < 3; ++i) {
+                const float xw = r.x_cm[i] + (r.R[3 * i] * xr[0] + r.R[3 * i + 1] * xr[1] + r.R[3 * i + 2] * xr[2]);
+                const double push = -dmin * n[i];
+                xc[i] = (double)xw + push;
+                r.x_cm[i] = (float)((double)r.x_cm[i] + push);
+            }
+            float Iwf[9];
+            rmul(r.R, r.inv_inertia, T1);
+            rmulT(T1, r.R, Iwf);
+            auto mv = [&](const double* a, double* o) {
+                for (int i = 0; i < 3; ++i) o[i] = (double)Iwf[3 * i] * a[0] + (double)Iwf[3 * i + 1] * a[1] + (double)Iwf[3 * i + 2] * a[2];
+            };
+            auto cross = [](const double* a, const double* c, double* o) {
+                o[0] = a[1] * c[2] - a[2] * c[1];
+                o[1] = a[2] * c[0] - a[0] * c[2];
+                o[2] = a[0] * c[1] - a[1] * c[0];
+            };
+            double rr[3], om[3], vc[3], tmp[3];
+            for (int i = 0; i < 3; ++i) { rr[i] = xc[i] - (double)r.x_cm[i]; om[i] = r.omega[i]; }
+            cross(om, rr, tmp);
+            for (int i = 0; i < 3; ++i) vc[i] = (double)r.v_cm[i] + tmp[i];
+            const double vn = vc[0] * n[0] + vc[1] * n[1] + vc[2] * n[2];
+            if (!(vn < 0.0)) continue;
+            const double Mb = r.mass;
+            double rxn[3], q[3], qq[3], dw[3];
+            cross(rr, n, rxn);
+            mv(rxn, q);
+            cross(q, rr, qq);
+            const double Jn = -(1.0 + sf.restitution) * vn / (1.0 / Mb + (qq[0] * n[0] + qq[1] * n[1] + qq[2] * n[2]));
+            const double jr[3] = {Jn * rxn[0], Jn * rxn[1], Jn * rxn[2]};
+            mv(jr, dw);
+            for (int i = 0; i < 3; ++i) {
+                r.v_cm[i] = (float)((double)r.v_cm[i] + (Jn / Mb) * n[i]);
+                r.omega[i] = (float)((double)r.omega[i] + dw[i]);
+            }
+            if (sf.friction > 0.0) {
+                double vt[3];
+                for (int i = 0; i < 3; ++i) vt[i] = vc[i] - vn * n[i];
+                const double vtm = std::sqrt(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
+                if (vtm > 1e-10) {
+                    const double th[3] = {vt[0] / vtm, vt[1] / vtm, vt[2] / vtm};
+                    double rxt[3], q2[3], qq2[3];
+                    cross(rr, th, rxt);
+                    mv(rxt, q2);
+                    cross(q2, rr, qq2);
+                    const double dent = 1.0 / Mb + (qq2[0] * th[0] + qq2[1] * th[1] + qq2[2] * th[2]);
+                    const double Jt = std::min(vtm / dent, sf.friction * Jn);
+                    const double jt[3] = {Jt * rxt[0], Jt * rxt[1], Jt * rxt[2]};
+                    mv(jt, dw);
+                    for (int i = 0; i < 3; ++i) {
+                        r.v_cm[i] = (float)((double)r.v_cm[i] - (Jt / Mb) * th[i]);
+                        r.omega[i] = (float)((double)r.omega[i] - dw[i]);
+                    }
+                }
+            }
+        }
+    }
+    for (int p = 0; p < P->n; ++p) {
+        if (!sel(p) || P->material[p] != 8) continue;
+        const gbmpm_rigid_body& r = g_rigid.bodies[P->rigid_id[p]];
+        const float* xr = P->x_ref + 3 * (size_t)p;
+        float* x = P->x + 3 * (size_t)p;
+        float* v = P->v + 3 * (size_t)p;
+        for (int i = 0; i < 3; ++i)
+            x[i] = r.x_cm[i] + (r.R[3 * i] * xr[0] + r.R[3 * i + 1] * xr[1] + r.R[3 * i + 2] * xr[2]);
+        const float rr[3] = {x[0] - r.x_cm[0], x[1] - r.x_cm[1], x[2] - r.x_cm[2]};
+        v[0] = r.v_cm[0] + (r.omega[1] * rr[2] - r.omega[2] * rr[1]);
+        v[1] = r.v_cm[1] + (r.omega[2] * rr[0] - r.omega[0] * rr[2]);
+        v[2] = r.v_cm[2] + (r.omega[0] * rr[1] - r.omega[1] * rr[0]);
+        const float Cm[9] = {0.0f, -r.omega[2], r.omega[1], r.omega[2], 0.0f, -r.omega[0], -r.omega[1], r.omega[0], 0.0f};
+        const float I[9] = {1.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 1.0f};
+        std::memcpy(P->C + 9 * (size_t)p, Cm, sizeof Cm);
+        std::memcpy(P->F + 9 * (size_t)p, I, sizeof I);
+    }
+}
+
 }  // namespace
 
 extern "C" {
 
 const char* gbmpm_oracle_last_error(void) { return g_err; }
+
+int gbmpm_oracle_set_rigid(const gbmpm_rigid_body* bodies, int32_t nb, const gbmpm_rigid_surface* surf, int32_t ns) {
+    g_rigid.bodies.assign(bodies, bodies + nb);
+    g_rigid.surf.assign(surf, surf + ns);
+    return GBMPM_OK;
+}
+int gbmpm_oracle_get_rigid(gbmpm_rigid_body* bodies, int32_t nb) {
+    for (int b = 0; b < nb && b < (int)g_rigid.bodies.size(); ++b) bodies[b] = g_rigid.bodies[b];
+    return GBMPM_OK;
+}
+int gbmpm_oracle_set_modifiers(const gbmpm_modifier* mods, int32_t n) {
+    g_rigid.mods.assign(mods, mods + n);
+    return GBMPM_OK;
+}
 
 // sizes and field offsets of the include/gbmpm.h records, so tests can check
 // the ctypes mirror against the C compiler's layout
@@ -1476,15 +1683,23 @@ int gbmpm_oracle_tick(const gbmpm_particles* P, const gbmpm_model* M, gbmpm_coll
     }
     const int n = P->n;
     auto sel = [&](int p) { return !P->selection || P->selection[p] == 0; };
+    const std::function<bool(int)> self_fn = sel;
+    // rigid bodies and particle modifiers run the split pipeline, as Solver.step does
+    // (core/solver.py:440-453)
+    const bool rigid = !g_rigid.bodies.empty() && P->rigid_id && P->x_ref;
+    const bool mods = !g_rigid.mods.empty() && P->mod_mask;
+    if (rigid || mods) fused = 0;
     int prev_lo[3], prev_hi[3];
     for (int s = 0; s < substeps; ++s) {
         float tf = (float)*time;
+        const double t_sub = *time;
         for (int a = 0; a < 3; ++a) { prev_lo[a] = G.lo[a]; prev_hi[a] = G.hi[a]; }
         if (S) cdf_stamp(*S, M, *time, fused != 0);
         if (!fused || s == 0) {
             // zero_grid over the previous touched box, stress, p2g
             if (prev_hi[0] > prev_lo[0]) zero_box(G, prev_lo, prev_hi, true, true);
             if (!fused && s > 0) { /* split pipeline: g2p already ran at the end of s-1 */ }
+            if (mods) for (int p = 0; p < n; ++p) if (sel(p)) apply_modifiers(P, p, tf, dtf);
             par_for(n, par, [&](int p) { if (sel(p)) stress_particle(c, p); });
             track_box(G, P, M);
             par_for(n, par, [&](int p) { if (sel(p)) p2g_particle(c, p); });
@@ -1511,6 +1726,7 @@ int gbmpm_oracle_tick(const gbmpm_particles* P, const gbmpm_model* M, gbmpm_coll
                 int mat = P->material[p];
                 if (mat != 7 && mat != 8) g2p_particle(c, p);
             });
+            if (rigid) rigid_tail(P, M, G, t_sub, dtf, self_fn);
         }
     }
     if (fused) {

@@ -79,12 +79,21 @@ def load():
     lib.gbmpm_oracle_cov.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
     lib.gbmpm_oracle_last_error.restype = C.c_char_p
     lib.gbmpm_oracle_abi_layout.argtypes = [C.c_void_p]
+    lib.gbmpm_oracle_set_rigid.argtypes = [P(_abi.RigidBody), C.c_int32, P(_abi.RigidSurface), C.c_int32]
+    lib.gbmpm_oracle_get_rigid.argtypes = [P(_abi.RigidBody), C.c_int32]
+    lib.gbmpm_oracle_set_modifiers.argtypes = [P(_abi.Modifier), C.c_int32]
     _lib = lib
     return lib
 
 
 def _p(a):
     return None if a is None else a.ctypes.data
+
+
+def _copy(cls, rec):
+    r = cls()
+    C.memmove(C.byref(r), C.byref(rec), C.sizeof(cls))
+    return r
 
 
 def abi_layout() -> list[int]:
@@ -124,7 +133,7 @@ def blocks(x: np.ndarray, inv_dx: float, n_grid: int, prev: np.ndarray | None = 
 
 
 _KEYS = ("x", "v", "C", "F", "F_trial", "L", "stress", "mass", "vol", "density", "Jp", "mu", "lam", "yield_stress",
-         "material", "selection", "cov", "init_cov", "cdf_tag")
+         "material", "selection", "cov", "init_cov", "cdf_tag", "rigid_id", "x_ref", "mod_mask")
 
 
 def box_contact_wrench(x, cauchy, vol, box_center, box_half, layer_cells=None, dx=None, compressive_only=True):
@@ -173,6 +182,9 @@ class OracleSolver:
         self.cdf_arrays: list = []
         self.cdf_state = None
         self.cdf_wrench_acc = np.zeros((4, 6), np.float32)
+        self.rigid_bodies: list = []
+        self.rigid_surfaces: list = []
+        self.modifiers: list = []
 
     def __del__(self):
         if getattr(self, "cdf_state", None):
@@ -189,7 +201,8 @@ class OracleSolver:
                   "mass": z(n), "vol": np.asarray(vol, np.float32).copy(), "density": z(n), "Jp": z(n),
                   "mu": z(n), "lam": z(n), "yield_stress": z(n), "material": np.zeros(n, np.int32),
                   "selection": np.zeros(n, np.int32), "cov": None, "init_cov": None,
-                  "cdf_tag": np.zeros(n, np.int32)}
+                  "cdf_tag": np.zeros(n, np.int32), "rigid_id": np.zeros(n, np.int32), "x_ref": z(n, 3),
+                  "mod_mask": np.zeros(n, np.int32)}
         if cov is not None:
             c6 = np.ascontiguousarray(cov, np.float32).reshape(n, 6)
             self.a["init_cov"] = c6.copy()
@@ -225,6 +238,8 @@ class OracleSolver:
             m.eta_table_smax = host.f32(kw["eta_table_smax"])
         if "g" in kw and not ranged:
             m.gravity[:] = tuple(host.f32(g) for g in kw["g"])
+        if "obj_id" in kw:
+            a["rigid_id"][sl] = int(kw["obj_id"])
         if "density" in kw:
             a["density"][sl] = np.float32(kw["density"])
             a["mass"][sl] = a["density"][sl] * a["vol"][sl]
@@ -268,6 +283,39 @@ class OracleSolver:
 
     def add_plane(self, point, normal, surface="sticky", friction=0.0, restitution=0.0):
         self._add(host.plane_collider(point, normal, surface, friction))
+        if restitution != 0.0:
+            self.rigid_surfaces.append(host.rigid_surface(point, normal, friction, restitution))
+        return self
+
+    def finalize_rigid_bodies(self):
+        self.rigid_bodies, x_ref = host.rigid_bodies(self.a["x"], self.a["mass"], self.a["material"],
+                                                     self.a["rigid_id"])
+        self.a["x_ref"][:] = x_ref
+        return self
+
+    def set_rigid_body_velocity(self, body_id, v_cm=(0.0, 0.0, 0.0), omega=(0.0, 0.0, 0.0)):
+        self.rigid_bodies[body_id].v_cm[:] = tuple(float(c) for c in v_cm)
+        self.rigid_bodies[body_id].omega[:] = tuple(float(c) for c in omega)
+        return self
+
+    def _add_modifier(self, rec, mask):
+        self.a["mod_mask"] |= (mask.astype(np.int32) << len(self.modifiers))
+        self.modifiers.append(rec)
+
+    def add_impulse_on_particles(self, force, dt, point=(1, 1, 1), size=(1, 1, 1), num_dt=1, start_time=0.0):
+        self._add_modifier(host.impulse_modifier(force, dt, num_dt, start_time), host.box_mask(self.a["x"], point, size))
+        return self
+
+    def enforce_particle_velocity_translation(self, point, size, velocity, start_time, end_time):
+        self._add_modifier(host.translation_modifier(velocity, start_time, end_time),
+                           host.box_mask(self.a["x"], point, size))
+        return self
+
+    def enforce_particle_velocity_rotation(self, point, normal, half_height_and_radius, rotation_scale,
+                                           translation_scale, start_time, end_time):
+        rec = host.rotation_modifier(point, normal, rotation_scale, translation_scale, start_time, end_time)
+        self._add_modifier(rec, host.cylinder_mask(self.a["x"], point, rec.normal[:], half_height_and_radius[0],
+                                                   half_height_and_radius[1]))
         return self
 
     def add_box(self, center, half_size, velocity=(0.0, 0.0, 0.0), start_time=0.0, end_time=1.0e9):
@@ -408,8 +456,14 @@ class OracleSolver:
         o.handles = list(st.get("handles", range(len(o.cols))))
         o.wrench = np.zeros((len(o.cols), 6), np.float32)
         o.time = float(st["time"])
-        if o.a.get("cdf_tag") is None:
-            o.a["cdf_tag"] = np.zeros(len(o.a["x"]), np.int32)
+        n = len(o.a["x"])
+        for k, shape, dt in (("cdf_tag", (n,), np.int32), ("rigid_id", (n,), np.int32), ("x_ref", (n, 3), np.float32),
+                             ("mod_mask", (n,), np.int32)):
+            if o.a.get(k) is None:
+                o.a[k] = np.zeros(shape, dt)
+        o.rigid_bodies = [_copy(_abi.RigidBody, r) for r in st.get("rigid_bodies", [])]
+        o.rigid_surfaces = [_copy(_abi.RigidSurface, r) for r in st.get("rigid_surfaces", [])]
+        o.modifiers = [_copy(_abi.Modifier, r) for r in st.get("modifiers", [])]
         for rec in st.get("cdf_lanes", []):
             r = _abi.Cdf()
             C.memmove(C.byref(r), C.byref(rec), C.sizeof(_abi.Cdf))
@@ -431,18 +485,31 @@ class OracleSolver:
         return p
 
     def step(self, dt, substeps=1):
+        """One control tick; scenes with rigid bodies or particle modifiers run the
+        split pipeline, as the reference's Solver.step does."""
         lib = load()
         p = self._particles()
+        nb, ns, nm = len(self.rigid_bodies), len(self.rigid_surfaces), len(self.modifiers)
+        bodies = (_abi.RigidBody * max(1, nb))(*self.rigid_bodies)
+        lib.gbmpm_oracle_set_rigid(bodies, nb, (_abi.RigidSurface * max(1, ns))(*self.rigid_surfaces), ns)
+        lib.gbmpm_oracle_set_modifiers((_abi.Modifier * max(1, nm))(*self.modifiers), nm)
         arr = (_abi.Collider * max(1, len(self.cols)))(*self.cols)
         t = C.c_double(self.time)
         rc = lib.gbmpm_oracle_tick(C.byref(p), C.byref(self.model), arr, len(self.cols), _p(self.wrench),
                                    C.byref(t), float(dt), int(substeps), 1 if self.fused else 0, int(self.threads),
                                    self.cdf_state if self.cdf_lanes else None, _p(self.cdf_wrench_acc))
+        lib.gbmpm_oracle_get_rigid(bodies, nb)
+        self.rigid_bodies = [_copy(_abi.RigidBody, bodies[i]) for i in range(nb)]
         if rc != 0:
             raise RuntimeError(f"oracle tick failed ({rc}): {lib.gbmpm_oracle_last_error().decode()}")
         self.cols = [arr[i] for i in range(len(self.cols))]
         self.time = t.value
         return self
+
+    def rigid_state(self, body: int = 0) -> dict:
+        r = self.rigid_bodies[body]
+        return {"com": np.array(r.x_cm[:], np.float32), "v": np.array(r.v_cm[:], np.float32),
+                "omega": np.array(r.omega[:], np.float32), "R": np.array(r.R[:], np.float32).reshape(3, 3)}
 
     def x(self):
         return self.a["x"]

@@ -165,3 +165,56 @@ def set_velocity(s, vel):
         s.a["v"][:] = vel
     else:
         s.set_v(vel)
+
+
+def tilted_cube(center, edge, spacing, ax=0.5, ay=0.35):
+    """Lattice points of a cube rotated by ax about x then ay about y (radians), so
+    its lowest point is one corner."""
+    k = np.arange(int(round(edge / spacing))) * spacing
+    k = k - k.mean()
+    p = np.stack(np.meshgrid(k, k, k, indexing="ij"), -1).reshape(-1, 3)
+    cx, sx, cy, sy = np.cos(ax), np.sin(ax), np.cos(ay), np.sin(ay)
+    Rx = np.array([[1, 0, 0], [0, cx, -sx], [0, sx, cx]])
+    Ry = np.array([[cy, 0, sy], [0, 1, 0], [-sy, 0, cy]])
+    return (p @ (Ry @ Rx).T + np.asarray(center)).astype(np.float32)
+
+
+def rigid_scene(cls, water=True, fused=True, restitution=0.3, n_grid=32, grid_lim=0.4, height=None):
+    """A tilted rigid cube (obj_id 0, density 500) thrown, spinning, at a slip floor
+    that is also a restitution surface, optionally above a water slab, inside
+    domain walls (the two-way coupling of warpmpm.vehicle at test scale)."""
+    dx = grid_lim / n_grid
+    h = dx / 2
+    floor = 3 * dx
+    cube = tilted_cube((0.2, 0.2, floor + (height if height is not None else (0.09 if water else 0.05))), 0.06, h)
+    parts = [cube]
+    if water:
+        ax = np.arange(0.08, 0.32, h)
+        w = np.stack(np.meshgrid(ax, ax, np.arange(floor + 0.5 * h, floor + 0.04, h), indexing="ij"), -1)
+        w = w.reshape(-1, 3) + np.random.default_rng(1).uniform(-0.2 * h, 0.2 * h, (w.size // 3, 3))
+        parts.insert(0, w.astype(np.float32))
+    pos = np.concatenate(parts).astype(np.float32)
+    n_w = len(pos) - len(cube)
+    s = make(cls, n_grid, grid_lim, fused=fused).load_particles(pos, np.full(len(pos), h ** 3, np.float32))
+    s.set_material(newtonian(eta=0.5, density=1000.0, bulk_modulus=4.0e4))
+    s.set_material_range(n_w, len(pos), "rigid", obj_id=0, density=500.0)
+    s.finalize_rigid_bodies()
+    s.add_plane((0, 0, floor), (0, 0, 1), "slip", friction=0.2, restitution=restitution)
+    s.add_domain_walls()
+    set_rigid_motion(s, n_w, (0.3, -0.1, -1.0), (0.0, 2.0, 1.0))
+    return s, n_w
+
+
+def set_rigid_motion(s, n_w, v_cm, omega):
+    """Body velocity and the matching particle velocities v_cm + omega x r: the
+    body's own velocity alone is replaced by its particles' momentum at the first
+    substep (the rigid tail gathers it from the grid they deposit to)."""
+    s.set_rigid_body_velocity(0, v_cm, omega)
+    x = np.asarray(s.x(), np.float64)
+    com = np.asarray(s.rigid_state(0)["com"], np.float64)
+    v = np.array(s.v(), np.float32)
+    v[n_w:] = (np.asarray(v_cm) + np.cross(np.asarray(omega), x[n_w:] - com)).astype(np.float32)
+    if hasattr(s, "set_v"):
+        s.set_v(v)
+    else:
+        s.a["v"][:] = v
