@@ -243,13 +243,15 @@ int gbmpm_contact_wrench(gbmpm_engine *e, const double box_center[3], const doub
                          void *stream);
 
 /* ---- adjoint (no counterpart in the reference) ---------------------------------
- * Adjoints of the particle state (x, v, C, F_trial, yield_stress, L; device arrays
- * in the particle layout) and accumulated per-particle adjoints of mu, lam and of
- * the Newtonian viscosity (its sum is the gradient of the per-type value). */
+ * Adjoints of the particle state (x, v, C, F_trial, yield_stress, L, and Jp, the
+ * mu(I)-Phi(I) packing state; device arrays in the particle layout) and accumulated
+ * per-particle adjoints of mu, lam and of the Newtonian viscosity (its sum is the
+ * gradient of the per-type value). */
 typedef struct gbmpm_adj_grads {
     float *x, *v, *C, *F_trial, *yield_stress;
     float *mu, *lam;
     float *L, *viscosity;
+    float *Jp;
 } gbmpm_adj_grads;
 
 /* Replays `substeps` split-schedule substeps forward from the bound state (the

@@ -127,7 +127,8 @@ MAX_MODIFIERS = 32
 
 
 class AdjGrads(C.Structure):
-    _fields_ = [(k, C.c_void_p) for k in ("x", "v", "C", "F_trial", "yield_stress", "mu", "lam", "L", "viscosity")]
+    _fields_ = [(k, C.c_void_p) for k in ("x", "v", "C", "F_trial", "yield_stress", "mu", "lam", "L", "viscosity",
+                                          "Jp")]
 
 
 class FieldPoints(C.Structure):

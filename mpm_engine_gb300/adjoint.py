@@ -14,12 +14,12 @@ one substep at a time (the engine keeps every substep's starting state on the
 device) and carries the adjoints back through it (`gbmpm_adjoint_segment`).
 
 Scope: jelly (FCR), von Mises (with or without hardening, with or without
-softening), Drucker-Prager sand, mu(I) and tabulated mu(I) granular flow, water,
-Newtonian (Bingham, Herschel-Bulkley) and tabulated viscous particles; plane,
-cuboid, domain-wall, revolved-SDF cup and mesh-SDF colliders; no periodic axis,
-rpic_damping = 0, particle order fixed during the rollout (sort_interval = 0). Not
-covered: mu(I)-Phi(I) (its packing state Jp would join the adjoint state) and CDF
-colliders.
+softening), Drucker-Prager sand, mu(I), tabulated mu(I) and mu(I)-Phi(I) granular
+flow (its packing state Jp carried as adjoint state), water, Newtonian (Bingham,
+Herschel-Bulkley) and tabulated viscous particles; plane, cuboid, domain-wall,
+revolved-SDF cup and mesh-SDF colliders; no periodic axis, rpic_damping = 0,
+particle order fixed during the rollout (sort_interval = 0). Not covered: CDF
+colliders, rigid bodies and particle modifiers.
 """
 from __future__ import annotations
 
@@ -28,7 +28,7 @@ import ctypes as C
 from . import _abi
 from .solver import _torch
 
-_STATE = ("x", "v", "C", "F_trial", "L", "yield_stress", "mu", "lam")
+_STATE = ("x", "v", "C", "F_trial", "L", "yield_stress", "mu", "lam", "Jp")
 
 
 def _snapshot(s):
@@ -84,7 +84,7 @@ def _backward(s, dt, ckpts, xb, vb):
         "v": (vb.detach().to(**f).reshape(n, 3).clone() if vb is not None else torch.zeros(n, 3, **f)),
         "C": torch.zeros(n, 3, 3, **f), "F_trial": torch.zeros(n, 3, 3, **f),
         "yield_stress": torch.zeros(n, **f), "mu": torch.zeros(n, **f), "lam": torch.zeros(n, **f),
-        "L": torch.zeros(n, 3, 3, **f), "viscosity": torch.zeros(n, **f),
+        "L": torch.zeros(n, 3, 3, **f), "viscosity": torch.zeros(n, **f), "Jp": torch.zeros(n, **f),
     }
     rec = _abi.AdjGrads(**{k: g[k].data_ptr() for k in g})
     lib, h = s._eng.lib, s._eng.h
@@ -219,7 +219,7 @@ class BatchRollout:
                 g = {"x": xb.detach().to(**f).reshape(n, 3).clone(), "v": vb.detach().to(**f).reshape(n, 3).clone(),
                      "C": torch.zeros(n, 3, 3, **f), "F_trial": torch.zeros(n, 3, 3, **f),
                      "yield_stress": torch.zeros(n, **f), "mu": torch.zeros(n, **f), "lam": torch.zeros(n, **f),
-                     "L": torch.zeros(n, 3, 3, **f), "viscosity": torch.zeros(n, **f)}
+                     "L": torch.zeros(n, 3, 3, **f), "viscosity": torch.zeros(n, **f), "Jp": torch.zeros(n, **f)}
                 gs.append(g)
                 recs.append(_abi.AdjGrads(**{k: g[k].data_ptr() for k in g}))
             torch.cuda.synchronize()

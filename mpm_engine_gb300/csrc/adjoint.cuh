@@ -36,7 +36,7 @@ namespace gbmpm {
 
 struct AdjK {
     // state at the start of the substep (caller layout: x[n][3], C[n][9] ...)
-    const float *x, *v, *C, *Ft, *Lst, *ys;
+    const float *x, *v, *C, *Ft, *Lst, *ys, *Jp;
     const MatTables *tab;
     const float *mass, *vol, *mu, *lam;   // mu, lam: the state at the start of the substep
     const int *mat, *sel;
@@ -54,7 +54,7 @@ struct AdjK {
     float damp;
     float hard1, xi1;   // von Mises hardening switch and xi (material table, id 1)
     // adjoints: in = end of the substep, out = start of the substep
-    float *xb, *vb, *Cb, *Ftb, *Lb, *ysb;
+    float *xb, *vb, *Cb, *Ftb, *Lb, *ysb, *Jpb;
     float *mub, *lamb, *pvb;   // accumulated over substeps (pvb: Newtonian viscosity)
     // colliders of this substep
     int ncol;
@@ -276,16 +276,132 @@ __device__ void mui_reverse(const AdjK &a, int mat, const MuI &m, const float *s
     }
 }
 
+// mu(I)-Phi(I) return map (id 11; mpm_utils.py:375-522) as the engine's stress pass
+// computes it, with the packing state Jp: 0 no compaction pressure (F = U e^mean V^T),
+// 1 below the yield surface (F = F_trial), 2 flow (rate gdp from the bisection, Jp
+// relaxing toward the critical-state value). MuIPhi keeps what the adjoint needs.
+struct MuIPhi {
+    float s[3], e[3], d[3], dn, mean, J, Jr, K, pc, pK, tbK, Ic, gdp, Ir, dgam, jcs, q, sc;
+    bool jr_clamped;
+};
+__device__ int muiphi_return(const AdjK &a, const float *Ft, float mu, float jp, float *U, float *sg, float *V,
+                             MuIPhi &m, float *Fp, float &jp_new) {
+    const MatTables &T = *a.tab;
+    const int mat = 11;
+    svd3(Ft, U, sg, V);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        m.s[i] = fmaxf(fabsf(sg[i]), 1e-6f);
+        m.e[i] = logf(m.s[i]);
+    }
+    m.mean = (m.e[0] + m.e[1] + m.e[2]) / 3.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) m.d[i] = m.e[i] - m.mean;
+    m.dn = sqrtf(m.d[0] * m.d[0] + m.d[1] * m.d[1] + m.d[2] * m.d[2]);
+    m.J = m.s[0] * m.s[1] * m.s[2];
+    m.jr_clamped = jp < 0.5f;
+    m.Jr = m.jr_clamped ? 1.0f : jp;
+    m.K = T.E[mat] / (3.0f * (1.0f - 2.0f * T.nu[mat]));
+    m.pc = fmaxf(m.K * (m.Jr / fmaxf(m.J, 1e-6f) - 1.0f), 0.0f);
+    jp_new = m.Jr;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Fp[i] = Ft[i];
+    if (m.pc <= 0.0f) {
+        const float si = expf(m.mean);
+        udvt(U, si, si, si, V, Fp);
+        return 0;
+    }
+    m.pK = m.pc * m.J;
+    m.tbK = 2.0f * mu * m.dn / sqrtf(2.0f);
+    if (!(m.tbK > T.mu_s[mat] * m.pK)) return 1;
+    m.Ic = T.d[mat] * sqrtf(T.rho_s[mat] / m.pc);
+    m.gdp = mu_i_bisect<false>(m.tbK, mu, a.dt, m.pK, m.Ic, T.mu_s[mat], T.dmu[mat], T.I0[mat], a.eta_tab, a.eta_n,
+                               a.eta_smin, a.eta_smax);
+    m.Ir = m.gdp * m.Ic;
+    m.dgam = fminf(8.0f * m.gdp * a.dt, 1.0f);
+    m.q = 1.0f - T.phi_chi[mat] * m.Ir / (m.Ir + T.I0[mat]);
+    m.jcs = 1.0f / fmaxf(m.q, 1e-3f);
+    jp_new = m.Jr + m.dgam * (m.jcs - m.Jr);
+    m.sc = (m.tbK - mu * a.dt * m.gdp) / fmaxf(m.tbK, 1e-20f);
+    udvt(U, expf(m.d[0] * m.sc + m.mean), expf(m.d[1] * m.sc + m.mean), expf(m.d[2] * m.sc + m.mean), V, Fp);
+    return 2;
+}
+
+// Reverse of the mu(I)-Phi(I) flow branch: from gb (adjoint of the returned singular
+// values) and jpb (adjoint of the new Jp) to sb (adjoint of the trial singular
+// values), mu and the clamped old Jp (jrb). gdp is the root of
+// f = tbK - mu dt gdp - mu_I(gdp Ic) pK, differentiated implicitly.
+__device__ void muiphi_reverse(const AdjK &a, const MuIPhi &m, const float *sg, float mu, const float *gb, float jpb,
+                               float *sb, float &mub, float &jrb) {
+    const MatTables &T = *a.tab;
+    const int mat = 11;
+    float db[3], scb = 0.0f, meanb = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float epb = gb[i] * expf(m.d[i] * m.sc + m.mean);
+        db[i] = epb * m.sc;
+        scb += epb * m.d[i];
+        meanb += epb;
+    }
+    float tbKb = scb * mu * a.dt * m.gdp / (m.tbK * m.tbK);
+    float gdpb = -scb * mu * a.dt / m.tbK;
+    mub += -scb * a.dt * m.gdp / m.tbK;
+    // Jp' = Jr + dgam (jcs - Jr), dgam = min(8 gdp dt, 1), jcs = 1 / max(q, 1e-3)
+    jrb += jpb * (1.0f - m.dgam);
+    const float dgamb = jpb * (m.jcs - m.Jr), jcsb = jpb * m.dgam;
+    if (8.0f * m.gdp * a.dt < 1.0f) gdpb += dgamb * 8.0f * a.dt;
+    float Irb = 0.0f;
+    if (m.q > 1e-3f) {
+        const float qb = -jcsb / (m.q * m.q);
+        Irb = qb * (-T.phi_chi[mat] * T.I0[mat] / ((m.Ir + T.I0[mat]) * (m.Ir + T.I0[mat])));
+    }
+    gdpb += Irb * m.Ic;
+    float Icb = Irb * m.gdp;
+    const float muI = mu_of_i<false>(m.Ir, T.mu_s[mat], T.dmu[mat], T.I0[mat], nullptr, 0, 0.0f, 0.0f);
+    const float dmuI = T.dmu[mat] * T.I0[mat] / ((m.Ir + T.I0[mat]) * (m.Ir + T.I0[mat]));
+    const float fg = -mu * a.dt - dmuI * m.Ic * m.pK;
+    const float kf = (fg != 0.0f) ? -gdpb / fg : 0.0f;
+    tbKb += kf;
+    mub += kf * (-a.dt * m.gdp);
+    const float pKb = kf * (-muI);
+    Icb += kf * (-dmuI * m.gdp * m.pK);
+    // Ic = d sqrt(rho_s / pc), pK = pc J, pc = K (Jr / J - 1)
+    float pcb = Icb * (-0.5f * m.Ic / m.pc) + pKb * m.J;
+    float Jb = pKb * m.pc;
+    jrb += pcb * m.K / m.J;
+    Jb += pcb * (-m.K * m.Jr / (m.J * m.J));
+    // tbK = 2 mu dn / sqrt 2
+    mub += tbKb * 2.0f * m.dn / sqrtf(2.0f);
+    const float dnb = tbKb * 2.0f * mu / sqrtf(2.0f);
+    if (m.dn > 0.0f) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) db[i] += dnb * m.d[i] / m.dn;
+    }
+    const float dsum = (db[0] + db[1] + db[2]) / 3.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float eb = db[i] - dsum + meanb / 3.0f;
+        const float s_b = eb / m.s[i] + Jb * m.J / m.s[i];
+        sb[i] = (fabsf(sg[i]) > 1e-6f) ? (sg[i] > 0.0f ? s_b : -s_b) : 0.0f;
+    }
+}
+
 // The return map of a solid particle and the (mu, lam) its stress then uses: von
 // Mises with softening (id 5) zeroes both once the yield stress is used up. Returns
 // the yield stress after the substep in *ys_out.
-__device__ void solid_return(const AdjK &a, int mat, const float *Ft, float mu, float lam, float ys, float *Fp,
-                             float &mus, float &lams, float &ys_out) {
+__device__ void solid_return(const AdjK &a, int mat, const float *Ft, float mu, float lam, float ys, float jp,
+                             float *Fp, float &mus, float &lams, float &ys_out, float &jp_out) {
     const MatTables &T = *a.tab;
     float U[9], V[9], sg[3], e[3];
     mus = mu;
     lams = lam;
     ys_out = ys;
+    jp_out = jp;
+    if (mat == 11) {
+        MuIPhi m;
+        muiphi_return(a, Ft, mu, jp, U, sg, V, m, Fp, jp_out);
+        return;
+    }
     if (mat == 1 || mat == 5) {
         if (mat == 5 && ys <= 0.0f) {
 #pragma unroll
@@ -316,6 +432,28 @@ __device__ void solid_return(const AdjK &a, int mat, const float *Ft, float mu, 
 #pragma unroll
         for (int i = 0; i < 9; ++i) Fp[i] = Ft[i];
     }
+}
+
+// mu(I)-Phi(I) stress (mpm_utils.py:525-540): U diag(2 mu (e - mean) - pc Jc) U^T,
+// e = log max(sigma, 1e-6), pc = max(K (Jr / J - 1), 0) with the new Jp, symmetrized
+__device__ void muiphi_stress(const AdjK &a, const float *F, float mu, float jp, float *S) {
+    const MatTables &T = *a.tab;
+    float U[9], V[9], sg[3], Tm[9];
+    const float J = det3(F);
+    svd3(F, U, sg, V);
+    const float Jr = (jp < 0.5f) ? 1.0f : jp;
+    const float K = T.E[11] / (3.0f * (1.0f - 2.0f * T.nu[11]));
+    const float pc = fmaxf(K * (Jr / fmaxf(J, 1e-6f) - 1.0f), 0.0f);
+    const float s0 = fmaxf(sg[0], 1e-6f), s1 = fmaxf(sg[1], 1e-6f), s2 = fmaxf(sg[2], 1e-6f);
+    const float e0 = logf(s0), e1 = logf(s1), e2 = logf(s2);
+    const float Jc = s0 * s1 * s2;
+    const float mean = (e0 + e1 + e2) / 3.0f;
+    const float iso = -pc * Jc;
+    udvt(U, 2.0f * mu * (e0 - mean) + iso, 2.0f * mu * (e1 - mean) + iso, 2.0f * mu * (e2 - mean) + iso, U, Tm);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) S[3 * i + j] = 0.5f * (Tm[3 * i + j] + Tm[3 * j + i]);
 }
 
 // Kirchhoff stress of the projected F (FCR for ids 0 and 5, Hencky otherwise), symmetrized
@@ -391,9 +529,10 @@ __global__ void k_adj_stress_fwd(AdjK k) {
         for (int i = 0; i < 9; ++i) { k.Fp[9 * (size_t)p + i] = Fp[i]; k.S[9 * (size_t)p + i] = S[i]; }
         return;
     }
-    float mus, lams, ys_out;
-    solid_return(k, mat, Ft, mu, lam, k.ys[p], Fp, mus, lams, ys_out);
-    adj_stress(mat, Fp, mus, lams, S);
+    float mus, lams, ys_out, jp_out;
+    solid_return(k, mat, Ft, mu, lam, k.ys[p], k.Jp[p], Fp, mus, lams, ys_out, jp_out);
+    if (mat == 11) muiphi_stress(k, Fp, mus, jp_out, S);
+    else adj_stress(mat, Fp, mus, lams, S);
 #pragma unroll
     for (int i = 0; i < 9; ++i) { k.Fp[9 * (size_t)p + i] = Fp[i]; k.S[9 * (size_t)p + i] = S[i]; }
 }
@@ -762,11 +901,12 @@ __global__ void k_adj_p2g_bwd(AdjK a) {
     float ysb_in = a.ysb[p], ysb = ysb_in;
     // the (mu, lam) the stress used, and whether mu and lam are still the
     // parameters (von Mises with softening zeroes them once its yield is used up)
-    float mus = mu, lams = lam, ys_next = ys;
+    float mus = mu, lams = lam, ys_next = ys, jp_next = a.Jp[p];
     if (mat != 6 && mat != 10 && mat != 12) {
         float Fq[9];
-        solid_return(a, mat, Ft, mu, lam, ys, Fq, mus, lams, ys_next);
+        solid_return(a, mat, Ft, mu, lam, ys, a.Jp[p], Fq, mus, lams, ys_next, jp_next);
     }
+    float jpb_new = a.Jpb[p];   // adjoint of Jp after the substep; the stress adds to it
     const bool params_live = (mu != 0.0f);
     if (mat == 6 || mat == 10 || mat == 12) {
         // tau = J (p I + 2 eta dev D) with J = Jc^3, Jc = det(F_trial)^(1/3), F = Jc I,
@@ -820,7 +960,46 @@ __global__ void k_adj_p2g_bwd(AdjK a) {
         svd3(Fp, U, sg, V);
         const float mu = mus, lam = lams;   // the stress's moduli (zero once softened away)
         float mub_s = 0.0f, lamb_s = 0.0f;
-        if (mat == 0 || mat == 5) {   // tau = 2 mu (F - R) F^T + lam J (J - 1) I
+        if (mat == 11) {   // tau = G F^T, G = U diag(h / s) V^T, h = 2 mu (e - mean) - pc Jc
+            const MatTables &T = *a.tab;
+            const float Jr = (jp_next < 0.5f) ? 1.0f : jp_next;
+            const float K = T.E[11] / (3.0f * (1.0f - 2.0f * T.nu[11]));
+            const float pc = fmaxf(K * (Jr / fmaxf(det3(Fp), 1e-6f) - 1.0f), 0.0f);
+            float e[3], de[3], h[3], gg[3], Jg[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                e[i] = logf(fmaxf(sg[i], 1e-6f));
+                de[i] = (sg[i] > 1e-6f) ? 1.0f / sg[i] : 0.0f;
+            }
+            const float mean = (e[0] + e[1] + e[2]) / 3.0f;
+            const float Jc = fmaxf(sg[0], 1e-6f) * fmaxf(sg[1], 1e-6f) * fmaxf(sg[2], 1e-6f);
+            const float kp = (pc > 0.0f) ? K : 0.0f;   // d(pc Jc)/dJr; d(pc Jc)/ds_j = -K Jc / s_j
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                h[i] = 2.0f * mu * (e[i] - mean) - pc * Jc;
+                gg[i] = (sg[i] > 1e-6f) ? h[i] / sg[i] : 0.0f;
+            }
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    const float dh = 2.0f * mu * (((i == j) ? 1.0f : 0.0f) - 1.0f / 3.0f) * de[j] + kp * Jc * de[j];
+                    Jg[i][j] = (sg[i] > 1e-6f) ? (dh / sg[i] - ((i == j) ? h[i] / (sg[i] * sg[i]) : 0.0f)) : 0.0f;
+                }
+            float G[9], Gb[9], T1[9];
+            udvt(U, gg[0], gg[1], gg[2], V, G);
+            mm(tb, Fp, Gb);
+            mTm(tb, G, T1);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Fb[i] += T1[i];
+            iso_adjoint(U, sg, V, gg, Jg, Gb, Fb, yd);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+                if (sg[i] > 1e-6f) {
+                    mub_s += yd[i] * 2.0f * (e[i] - mean) / sg[i];
+                    if (!(jp_next < 0.5f)) jpb_new += yd[i] * (-kp) / sg[i];
+                }
+        } else if (mat == 0 || mat == 5) {   // tau = 2 mu (F - R) F^T + lam J (J - 1) I
             float R[9], FR[9], T1[9], T2[9], cof[9];
             mmT(U, V, R);
 #pragma unroll
@@ -1019,6 +1198,58 @@ __global__ void k_adj_p2g_bwd(AdjK a) {
                 lamb += dl;
             }
         }
+    } else if (mat == 11) {   // mu(I)-Phi(I), with the packing state Jp
+        float U[9], V[9], sg[3], Fq[9], jpn;
+        MuIPhi m;
+        const int br = muiphi_return(a, Ft, mu, a.Jp[p], U, sg, V, m, Fq, jpn);
+        float jrb = 0.0f;
+        if (br == 1) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Ftb[i] = Fb[i];
+            jrb = jpb_new;
+        } else {
+            float g[3], Jg[3][3], yd[3];
+            if (br == 0) {   // g = exp(mean) = (s0 s1 s2)^(1/3)
+                const float gi = expf(m.mean);
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    g[i] = gi;
+#pragma unroll
+                    for (int j = 0; j < 3; ++j)
+                        Jg[i][j] = (fabsf(sg[j]) > 1e-6f) ? gi / (3.0f * sg[j]) : 0.0f;
+                }
+                jrb = jpb_new;
+            } else {
+#pragma unroll
+                for (int i = 0; i < 3; ++i) g[i] = expf(m.d[i] * m.sc + m.mean);
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    float unit[3] = {0.0f, 0.0f, 0.0f}, row[3], dm = 0.0f, dj = 0.0f;
+                    unit[i] = 1.0f;
+                    muiphi_reverse(a, m, sg, mu, unit, 0.0f, row, dm, dj);
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) Jg[i][j] = row[j];
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Ftb[i] = 0.0f;
+            iso_adjoint(U, sg, V, g, Jg, Fb, Ftb, yd);
+            if (br == 2) {
+                // mu and the old Jp through both g and the new Jp; the trial singular
+                // values through the new Jp (the g part went through iso_adjoint)
+                float sbd[3], dm = 0.0f;
+                muiphi_reverse(a, m, sg, mu, yd, jpb_new, sbd, dm, jrb);
+                float sbj[3], dmx = 0.0f, djx = 0.0f;
+                const float z[3] = {0.0f, 0.0f, 0.0f};
+                muiphi_reverse(a, m, sg, mu, z, jpb_new, sbj, dmx, djx);
+                float Tm[9];
+                udvt(U, sbj[0], sbj[1], sbj[2], V, Tm);
+#pragma unroll
+                for (int i = 0; i < 9; ++i) Ftb[i] += Tm[i];
+                if (params_live) mub += dm;
+            }
+        }
+        jpb_new = m.jr_clamped ? 0.0f : jrb;
     } else if (mat != 6 && mat != 10 && mat != 12) {   // jelly, and id 5 once softened away: F = F_trial
 #pragma unroll
         for (int i = 0; i < 9; ++i) Ftb[i] = Fb[i];
@@ -1032,6 +1263,7 @@ __global__ void k_adj_p2g_bwd(AdjK a) {
         a.Lb[9 * (size_t)p + i] = Lb[i];
     }
     a.ysb[p] = ysb;
+    if (mat == 11) a.Jpb[p] = jpb_new;
     a.mub[p] += mub;
     a.lamb[p] += lamb;
     a.pvb[p] += pvb;
@@ -1046,11 +1278,11 @@ int adjoint_supported(gbmpm_engine *e) {
     if (e->M.periodic_x) return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint does not wrap the periodic x axis");
     if (e->M.rpic_damping != 0.0f) return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint needs rpic_damping == 0");
     const uint32_t covered = (1u << 0) | (1u << 1) | (1u << 2) | (1u << 5) | (1u << 6) | (1u << 9) | (1u << 10) |
-                             (1u << 12) | (1u << 13);
+                             (1u << 11) | (1u << 12) | (1u << 13);
     if (e->M.material_mask & ~covered)
         return fail(GBMPM_ERR_UNSUPPORTED,
                     "the adjoint covers jelly (0), von Mises (1), sand (2), softening von Mises (5), water (6), "
-                    "mu(I) (9, 13), Newtonian (10) and tabulated viscous (12) particles; not mu(I)-Phi(I) (11)");
+                    "mu(I) (9, 11, 13), Newtonian (10) and tabulated viscous (12) particles");
     if (e->cdf.n > 0) return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint does not cover CDF colliders");
     if (e->n_bodies > 0 || e->n_mods > 0)
         return fail(GBMPM_ERR_UNSUPPORTED, "the adjoint does not cover rigid bodies or particle modifiers");
@@ -1068,7 +1300,7 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
     if (!time || !gr || substeps < 1 || substeps > GBMPM_MAX_SUBSTEPS || !(dt > 0.0))
         return fail(GBMPM_ERR_ARG, "bad adjoint arguments");
     if (!gr->x || !gr->v || !gr->C || !gr->F_trial || !gr->yield_stress || !gr->mu || !gr->lam || !gr->L ||
-        !gr->viscosity)
+        !gr->viscosity || !gr->Jp)
         return fail(GBMPM_ERR_ARG, "every adjoint array is required");
     if (!e->P.L) return fail(GBMPM_ERR_ARG, "the adjoint needs particles.L");
     if ((rc = adjoint_supported(e))) return rc;
@@ -1077,7 +1309,7 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
     const int n = P.n, ng = e->G.n_grid, nc = (int)e->cols.size();
     const size_t nn = (size_t)ng * ng * ng;
     // segment storage: the state at the start of every substep
-    const size_t per = (size_t)36 * n;   // x 3, v 3, C 9, F_trial 9, L 9, yield 1, mu 1, lam 1
+    const size_t per = (size_t)37 * n;   // x 3, v 3, C 9, F_trial 9, L 9, yield 1, mu 1, lam 1, Jp 1
     GB_CUDA(e->adj_states.ensure(per * substeps));
     GB_CUDA(e->adj_scratch.ensure((size_t)27 * n));
     GB_CUDA(e->adj_grid.ensure(4 * nn));   // four float4 grids
@@ -1096,6 +1328,7 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
         GB_CUDA(cudaMemcpyAsync(st + 33 * (size_t)n, P.yield_stress, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         GB_CUDA(cudaMemcpyAsync(st + 34 * (size_t)n, P.mu, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         GB_CUDA(cudaMemcpyAsync(st + 35 * (size_t)n, P.lam, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        GB_CUDA(cudaMemcpyAsync(st + 36 * (size_t)n, P.Jp, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         record_tick(e, dtf, 1, false, false, s, false, 0.0, 0.0, i);
     }
     float4 *grid = e->adj_grid.ptr;
@@ -1105,7 +1338,7 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
         const float *st = e->adj_states.ptr + per * i;
         AdjK a{};
         a.x = st; a.v = st + 3 * (size_t)n; a.C = st + 6 * (size_t)n; a.Ft = st + 15 * (size_t)n;
-        a.Lst = st + 24 * (size_t)n; a.ys = st + 33 * (size_t)n;
+        a.Lst = st + 24 * (size_t)n; a.ys = st + 33 * (size_t)n; a.Jp = st + 36 * (size_t)n;
         a.tab = e->d_tab.ptr;
         a.mass = P.mass; a.vol = P.vol; a.mu = st + 34 * (size_t)n; a.lam = st + 35 * (size_t)n;
         a.mat = P.material; a.sel = P.selection;
@@ -1119,7 +1352,7 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
         a.damp = e->M.grid_v_damping_scale;
         a.hard1 = e->M.hardening[1]; a.xi1 = e->M.xi[1];
         a.xb = gr->x; a.vb = gr->v; a.Cb = gr->C; a.Ftb = gr->F_trial; a.Lb = gr->L; a.ysb = gr->yield_stress;
-        a.mub = gr->mu; a.lamb = gr->lam; a.pvb = gr->viscosity;
+        a.mub = gr->mu; a.lamb = gr->lam; a.pvb = gr->viscosity; a.Jpb = gr->Jp;
         a.ncol = nc; a.cols = e->d_cols.ptr; a.poses = e->d_pose.ptr + (size_t)i * std::max(1, nc);
         // the engine's P2G building block reads its inputs through a PK
         gbmpm_particles Ps = P;

@@ -11,7 +11,7 @@ class FakeSolver:
     def __init__(self, n=5):
         self._t = {"x": torch.zeros(n, 3), "v": torch.zeros(n, 3), "C": torch.zeros(n, 3, 3),
                    "F_trial": torch.eye(3).repeat(n, 1, 1), "L": torch.zeros(n, 3, 3),
-                   "yield_stress": torch.zeros(n), "mu": torch.ones(n), "lam": torch.ones(n)}
+                   "yield_stress": torch.zeros(n), "mu": torch.ones(n), "lam": torch.ones(n), "Jp": torch.ones(n)}
         self._cols = [_abi.Collider()]
         self._cols_dirty = False
         self._time = 0.0
