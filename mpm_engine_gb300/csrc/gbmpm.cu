@@ -141,6 +141,19 @@ __device__ __forceinline__ void mat_store(float *p, const float (&m)[9]) {
 #pragma unroll
     for (int i = 0; i < 9; ++i) p[i] = m[i];
 }
+// Programmatic dependent launch. The particle passes and the grid pass are launched
+// with programmatic stream serialization, so a pass may start while the kernel
+// before it finishes: pdl_wait() blocks until that kernel has completed and its
+// writes are visible, and must come before anything touching its outputs;
+// pdl_trigger() lets the next pass start launching. Each pass triggers only after
+// its own wait, so the code a pass runs before waiting only ever overlaps a kernel
+// that is past its own wait (the grid pass while the particle pass loads its
+// particles, or the particle pass's last wave while the grid pass stages its
+// collider records), and never reads what that kernel writes. Without the launch
+// attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Particle fields are either the caller's records (AoS: W floats per particle)
 // or the engine's working copy (SoA: component c of particle p at c*n + p, so a
 // warp's access to one component is one coalesced line).
@@ -1116,15 +1129,15 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
     __shared__ int s_seg[kTileThreads + 1];
     __shared__ int s_wcnt[kTileThreads / 32];
     __shared__ int s_red[kTileThreads / 32][6];
-    if ((mode & PASS_RESET_LISTS) && blockIdx.x == 0 && threadIdx.x == 0) {
-        k.blk_count[0] = 0;
-        k.blk_count[1] = 0;
-    }
     const int t = threadIdx.x;
     const int lane = t & 31, warp = t >> 5;
     const int p = blockIdx.x * kTileThreads + t;
     bool live = p < k.n && !(k.sel && k.sel[p] != 0);
     const int mat = live ? k.mat[p] : 0;
+    if (!(mode & PASS_G2P)) {   // without a gather, x and the stress inputs are what the previous pass wrote
+        pdl_wait();
+        pdl_trigger();
+    }
     float x[3] = {0.f, 0.f, 0.f};
     if (live) fld_load<true, 3>(k.x, k.n, p, x);
     float v[3] = {0.f, 0.f, 0.f}, C[9], L[9], Ft[9], S[9];
@@ -1165,6 +1178,12 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
         }
         TileBox box;
         block_box(s.b, want, box, s_red);
+        pdl_wait();   // the grid velocities come from the grid pass before this one
+        pdl_trigger();
+        if ((mode & PASS_RESET_LISTS) && blockIdx.x == 0 && threadIdx.x == 0) {
+            k.blk_count[0] = 0;
+            k.blk_count[1] = 0;
+        }
         float4 *s_tile = reinterpret_cast<float4 *>(s_mem);
         if (box.fits) {
             const int e12 = box.e[1] * box.e[2];
@@ -1213,6 +1232,8 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
         if (mode & PASS_STORE_ALL) fld_store<true, 9>(k.S, k.n, p, S);
     }
     if (!(mode & PASS_P2G)) return;
+    pdl_wait();   // the scatter target and block lists are the grid pass's (no-op after the gather's wait)
+    pdl_trigger();
     if (live) {
         if (!(mode & PASS_STRESS)) fld_load<true, 9>(k.S, k.n, p, S);
         if (!gathered) {
@@ -1899,6 +1920,8 @@ __global__ void __launch_bounds__(kGridThreads) k_grid(GK k) {
     const int t = threadIdx.x;
     for (int i = t; i < k.ncol; i += blockDim.x) { s_cols[i] = k.cols[i]; s_pose[i] = k.poses[i]; }
     for (int i = t; i < k.ncol * 6; i += blockDim.x) s_acc[i / 6][i % 6] = 0.0f;
+    pdl_wait();   // the particle pass before this one deposits into gmv and fills the block list
+    pdl_trigger();
     if (blockIdx.x == 0 && t == 0) *k.blk_count_reset = 0;
     __syncthreads();
     const int count = *k.blk_count_read;
@@ -2317,6 +2340,7 @@ struct gbmpm_engine {
     int num_sms = 148;
     int tile_occ = 3;       // resident CTAs per SM the tiled particle kernel is compiled for
     int cdf_occ = 3;        // the same for its CPIC variant
+    bool pdl = true;        // programmatic dependent launch of the particle and grid passes
     bool cdf_fused_stamp = true;   // one restamp launch a substep (else the five-kernel sequence)
     int grid_ctas = 2;      // grid-update CTAs per SM
     // graph cache
@@ -2413,16 +2437,36 @@ bool has_solids(const gbmpm_model &m) {
     return (m.material_mask & ~fluid) != 0;
 }
 
+// Launch with programmatic stream serialization (see pdl_wait) when enabled.
+template <typename... P, typename... A>
+void launch_pdl(gbmpm_engine *e, void (*kern)(P...), int grid, int block, cudaStream_t s, A... args) {
+    if (!e->pdl) {
+        kern<<<grid, block, 0, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 void launch_particles(gbmpm_engine *e, const PK &k, int mode, bool tiled, cudaStream_t s) {
     if (tiled && k.cdf_on) {
         int grid = std::max(1, (k.n + kTileThreads - 1) / kTileThreads);
         const bool solids = has_solids(e->M);
         if (e->cdf_occ >= 3) {
-            if (solids) k_particles_tiled<true, 3, true><<<grid, kTileThreads, 0, s>>>(k, mode);
-            else k_particles_tiled<false, 3, true><<<grid, kTileThreads, 0, s>>>(k, mode);
+            if (solids) launch_pdl(e, k_particles_tiled<true, 3, true>, grid, kTileThreads, s, k, mode);
+            else launch_pdl(e, k_particles_tiled<false, 3, true>, grid, kTileThreads, s, k, mode);
         } else {
-            if (solids) k_particles_tiled<true, 2, true><<<grid, kTileThreads, 0, s>>>(k, mode);
-            else k_particles_tiled<false, 2, true><<<grid, kTileThreads, 0, s>>>(k, mode);
+            if (solids) launch_pdl(e, k_particles_tiled<true, 2, true>, grid, kTileThreads, s, k, mode);
+            else launch_pdl(e, k_particles_tiled<false, 2, true>, grid, kTileThreads, s, k, mode);
         }
         e->launches++;
         return;
@@ -2430,11 +2474,11 @@ void launch_particles(gbmpm_engine *e, const PK &k, int mode, bool tiled, cudaSt
     if (tiled) {
         int grid = std::max(1, (k.n + kTileThreads - 1) / kTileThreads);
         const bool solids = has_solids(e->M);
-        if (solids && e->tile_occ >= 3) k_particles_tiled<true, 3><<<grid, kTileThreads, 0, s>>>(k, mode);
-        else if (solids) k_particles_tiled<true, 2><<<grid, kTileThreads, 0, s>>>(k, mode);
-        else if (e->tile_occ >= 4) k_particles_tiled<false, 4><<<grid, kTileThreads, 0, s>>>(k, mode);
-        else if (e->tile_occ == 3) k_particles_tiled<false, 3><<<grid, kTileThreads, 0, s>>>(k, mode);
-        else k_particles_tiled<false, 2><<<grid, kTileThreads, 0, s>>>(k, mode);
+        if (solids && e->tile_occ >= 3) launch_pdl(e, k_particles_tiled<true, 3>, grid, kTileThreads, s, k, mode);
+        else if (solids) launch_pdl(e, k_particles_tiled<true, 2>, grid, kTileThreads, s, k, mode);
+        else if (e->tile_occ >= 4) launch_pdl(e, k_particles_tiled<false, 4>, grid, kTileThreads, s, k, mode);
+        else if (e->tile_occ == 3) launch_pdl(e, k_particles_tiled<false, 3>, grid, kTileThreads, s, k, mode);
+        else launch_pdl(e, k_particles_tiled<false, 2>, grid, kTileThreads, s, k, mode);
     } else {
         int grid = std::max(1, (k.n + kParticleThreads - 1) / kParticleThreads);
         if (has_solids(e->M)) k_particles<true><<<grid, kParticleThreads, 0, s>>>(k, mode);
@@ -2538,7 +2582,7 @@ void launch_grid(gbmpm_engine *e, float dt, int substep, int list, cudaStream_t 
     // one wave of CTAs looping over the active blocks: the per-CTA setup (collider
     // tables into shared memory, two barriers) is paid once per SM slot, not per item
     int grid = e->num_sms * e->grid_ctas;
-    k_grid<<<grid, kGridThreads, 0, s>>>(g);
+    launch_pdl(e, k_grid, grid, kGridThreads, s, g);
     e->launches++;
 }
 
@@ -2984,6 +3028,7 @@ int gbmpm_engine_create(gbmpm_engine **out) {
     cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, e->device);
     if (const char *occ = std::getenv("GBMPM_TILE_OCC")) e->tile_occ = std::atoi(occ);
     if (const char *occ = std::getenv("GBMPM_CDF_OCC")) e->cdf_occ = std::atoi(occ);
+    if (const char *pd = std::getenv("GBMPM_NO_PDL")) e->pdl = std::atoi(pd) == 0;
     if (const char *fs = std::getenv("GBMPM_CDF_SPLIT_STAMP")) e->cdf_fused_stamp = std::atoi(fs) == 0;
     if (const char *gc = std::getenv("GBMPM_GRID_CTAS")) e->grid_ctas = std::max(1, std::min(8, std::atoi(gc)));
     if (cudaEventCreateWithFlags(&e->pose_done, cudaEventDisableTiming) != cudaSuccess) {
