@@ -2369,7 +2369,7 @@ struct gbmpm_engine {
     std::vector<gbmpm_rigid_surface> rsurf;
     DevBuf<gbmpm_rigid_body> d_bodies;
     DevBuf<double> d_racc;                  // [body][6] gathered momentum, angular momentum
-    DevBuf<unsigned long long> d_rkey;      // [body][2] contact keys (distance, particle)
+    DevBuf<unsigned long long> d_rkey;      // [body][surface][2] contact keys (distance, particle)
     int n_mods = 0;
     DevBuf<gbmpm_modifier> d_mods;
     double *h_time = nullptr;               // pinned staging of d_time
@@ -2911,7 +2911,10 @@ void record_rigid(gbmpm_engine *e, const gbmpm_particles &P, float dtf, int tail
     else k_rigid_gather<false><<<pb, 256, 0, s>>>(k, rid, e->d_bodies.ptr, e->d_racc.ptr);
     k_rigid_integrate<<<bb, 64, 0, s>>>(e->d_bodies.ptr, nb, e->d_racc.ptr, dtf);
     e->launches += 2;
-    for (const gbmpm_rigid_surface &sf : e->rsurf) {
+    if (!e->rsurf.empty()) {
+        RigidSurfaces sf{};
+        sf.n = (int)e->rsurf.size();
+        for (int q = 0; q < sf.n; ++q) sf.s[q] = e->rsurf[q];
         for (int stage = 0; stage < 2; ++stage) {
             if (soa)
                 k_rigid_contact<true><<<pb, 256, 0, s>>>(k, rid, P.x_ref, e->d_bodies.ptr, sf, e->d_rkey.ptr, stage, perm);
@@ -3174,10 +3177,11 @@ int gbmpm_set_rigid(gbmpm_engine *e, const gbmpm_rigid_body *bodies, int32_t n_b
     if (n_bodies > 0) {
         GB_CUDA(e->d_bodies.ensure(n_bodies));
         GB_CUDA(e->d_racc.ensure(6 * (size_t)n_bodies));
-        GB_CUDA(e->d_rkey.ensure(2 * (size_t)n_bodies));
+        GB_CUDA(e->d_rkey.ensure(2 * (size_t)n_bodies * GBMPM_MAX_RIGID_SURFACES));
         GB_CUDA(cudaMemcpy(e->d_bodies.ptr, bodies, n_bodies * sizeof(gbmpm_rigid_body), cudaMemcpyHostToDevice));
         GB_CUDA(cudaMemset(e->d_racc.ptr, 0, 6 * (size_t)n_bodies * sizeof(double)));
-        GB_CUDA(cudaMemset(e->d_rkey.ptr, 0xff, 2 * (size_t)n_bodies * sizeof(unsigned long long)));
+        GB_CUDA(cudaMemset(e->d_rkey.ptr, 0xff, 2 * (size_t)n_bodies * GBMPM_MAX_RIGID_SURFACES *
+                                                   sizeof(unsigned long long)));
     }
     e->rsurf.assign(surfaces, surfaces + n_surfaces);
     if ((e->n_bodies == 0) != (n_bodies == 0)) e->ws_n = -1;   // the working set gains or drops the rigid fields

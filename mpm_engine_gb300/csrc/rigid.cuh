@@ -5,10 +5,10 @@
 //
 // After the G2P of substep n the bodies gather the grid momentum of their particles
 // (k_rigid_gather), integrate (k_rigid_integrate), take one impulse per active
-// rigid surface at their deepest particle (k_rigid_contact twice: the minimum
-// signed distance, then the lowest particle index at that distance, as numpy's
-// argmin picks; then k_rigid_impulse), and write x, v, C = skew(omega), F = I back
-// to their particles (k_rigid_update).
+// rigid surface at their deepest particle (k_rigid_contact twice for all surfaces:
+// the minimum signed distance, then the lowest particle index at that distance, as
+// numpy's argmin picks; then k_rigid_impulse, surface after surface), and write x,
+// v, C = skew(omega), F = I back to their particles (k_rigid_update).
 //
 // In fused ticks the G2P of substep n and the P2G of substep n+1 are one pass, so
 // rigid particles sit out that pass's scatter (PK.rigid_defer) and k_rigid_update
@@ -17,41 +17,78 @@
 
 namespace gbmpm {
 
-// rigid_g2p_accumulate (mpm_utils.py:1369-1414): the grid velocity at each rigid
-// particle; its momentum and angular momentum about the body's centre of mass are
-// summed per body in float64
+struct RigidSurfaces {   // the rigid contact surfaces, by value
+    gbmpm_rigid_surface s[GBMPM_MAX_RIGID_SURFACES];
+    int n;
+};
+
+// A warp whose rigid particles all belong to one body (the usual case: particles
+// arrive block-sorted) reduces with shuffles and makes one atomic per warp;
+// otherwise each particle makes its own. The loops below step whole warps.
+__device__ __forceinline__ bool warp_one_body(bool on, int b, int &b0) {
+    const unsigned act = __ballot_sync(0xffffffffu, on);
+    if (!act) { b0 = -1; return true; }
+    b0 = __shfl_sync(0xffffffffu, b, __ffs(act) - 1);
+    return __all_sync(0xffffffffu, !on || b == b0);
+}
+
+// grid velocity at a rigid particle's position (the gather of rigid_g2p_accumulate)
+__device__ __forceinline__ void rigid_velocity(const PK &k, const Stencil &s, float *vi) {
+    vi[0] = vi[1] = vi[2] = 0.0f;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            for (int kk = 0; kk < 3; ++kk) {
+                const float w = s.w[0][i] * s.w[1][j] * s.w[2][kk];
+                const float4 g = global_fetch(k, s, i, j, kk);
+                vi[0] = vi[0] + g.x * w;
+                vi[1] = vi[1] + g.y * w;
+                vi[2] = vi[2] + g.z * w;
+            }
+}
+
+// rigid_g2p_accumulate (mpm_utils.py:1369-1414): each rigid particle's momentum
+// and angular momentum about its body's centre of mass, summed per body in float64
 template <bool SOA>
 __global__ void k_rigid_gather(PK k, const int *rid, const gbmpm_rigid_body *B, double *acc) {
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < k.n; p += gridDim.x * blockDim.x) {
-        if ((k.sel && k.sel[p] != 0) || k.mat[p] != 8) continue;
-        float x[3];
-        fld_load<SOA, 3>(k.x, k.n, p, x);
-        Stencil s;
-        stencil(x, k.inv_dx, s);
-        if (!stencil_ok(s, k.ng, k.periodic_x)) {
-            set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
-            continue;
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x - lane; base < k.n; base += stride) {
+        const int p = base + lane;
+        bool on = p < k.n && !(k.sel && k.sel[p] != 0) && k.mat[p] == 8;
+        const int b = on ? rid[p] : -1;
+        double c6[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        if (on) {
+            float x[3], vi[3];
+            fld_load<SOA, 3>(k.x, k.n, p, x);
+            Stencil s;
+            stencil(x, k.inv_dx, s);
+            if (stencil_ok(s, k.ng, k.periodic_x)) {
+                rigid_velocity(k, s, vi);
+                const float m = k.mass[p];
+                const float r[3] = {x[0] - B[b].x_cm[0], x[1] - B[b].x_cm[1], x[2] - B[b].x_cm[2]};
+                const float pm[3] = {vi[0] * m, vi[1] * m, vi[2] * m};
+                c6[0] = pm[0]; c6[1] = pm[1]; c6[2] = pm[2];
+                c6[3] = r[1] * pm[2] - r[2] * pm[1];
+                c6[4] = r[2] * pm[0] - r[0] * pm[2];
+                c6[5] = r[0] * pm[1] - r[1] * pm[0];
+            } else {
+                set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
+                on = false;
+            }
         }
-        float vi[3] = {0.0f, 0.0f, 0.0f};
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j)
-                for (int kk = 0; kk < 3; ++kk) {
-                    const float w = s.w[0][i] * s.w[1][j] * s.w[2][kk];
-                    const float4 g = global_fetch(k, s, i, j, kk);
-                    vi[0] = vi[0] + g.x * w;
-                    vi[1] = vi[1] + g.y * w;
-                    vi[2] = vi[2] + g.z * w;
-                }
-        const int b = rid[p];
-        const float m = k.mass[p];
-        const float r[3] = {x[0] - B[b].x_cm[0], x[1] - B[b].x_cm[1], x[2] - B[b].x_cm[2]};
-        const float pm[3] = {vi[0] * m, vi[1] * m, vi[2] * m};
-        const float am[3] = {r[1] * pm[2] - r[2] * pm[1], r[2] * pm[0] - r[0] * pm[2], r[0] * pm[1] - r[1] * pm[0]};
-        double *a = acc + 6 * (size_t)b;
+        int b0;
+        if (warp_one_body(on, b, b0)) {
+            if (b0 < 0) continue;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            atomicAdd(a + c, (double)pm[c]);
-            atomicAdd(a + 3 + c, (double)am[c]);
+            for (int c = 0; c < 6; ++c) {
+                double v = c6[c];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                if (lane == 0) atomicAdd(acc + 6 * (size_t)b0 + c, v);
+            }
+        } else if (on) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) atomicAdd(acc + 6 * (size_t)b + c, c6[c]);
         }
     }
 }
@@ -117,55 +154,67 @@ __device__ __forceinline__ double rigid_plane_dist(const PK &k, int p, const flo
     return d;
 }
 
-// stage 0: the smallest distance per body; stage 1: the lowest particle index (in
-// the caller's particle order, through perm) at that distance, with the pass index
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w < v ? w : v;
+    }
+    return v;
+}
+
+// Deepest particle of every body under every rigid surface, in two passes over the
+// particles for all surfaces at once: stage 0 the smallest signed distance per
+// (body, surface), stage 1 the lowest particle index (in the caller's order, through
+// perm) at that distance, with the pass row. The distances use the pose after
+// integration; the pushes of earlier surfaces move a body's particles together,
+// which leaves each surface's deepest particle unchanged (the reference likewise
+// shifts its world positions by each push). Keys: [body][surface][2].
 template <bool SOA>
 __global__ void k_rigid_contact(PK k, const int *rid, const float *x_ref, const gbmpm_rigid_body *B,
-                                gbmpm_rigid_surface sf, unsigned long long *key, int stage, const int *perm) {
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < k.n; p += gridDim.x * blockDim.x) {
-        if ((k.sel && k.sel[p] != 0) || k.mat[p] != 8) continue;
-        const int b = rid[p];
-        const unsigned long long dk = dkey(rigid_plane_dist<SOA>(k, p, x_ref, B[b], sf));
-        if (stage == 0) {
-            atomicMin(key + 2 * (size_t)b, dk);
-        } else if (dk == key[2 * (size_t)b]) {
-            const unsigned long long orig = (unsigned long long)(perm ? perm[p] : p);
-            atomicMin(key + 2 * (size_t)b + 1, (orig << 32) | (unsigned long long)(unsigned)p);
+                                RigidSurfaces sf, unsigned long long *key, int stage, const int *perm) {
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x - lane; base < k.n; base += stride) {
+        const int p = base + lane;
+        const bool on = p < k.n && !(k.sel && k.sel[p] != 0) && k.mat[p] == 8;
+        const int b = on ? rid[p] : -1;
+        int b0;
+        const bool one = warp_one_body(on, b, b0);
+        if (b0 < 0) continue;
+        for (int q = 0; q < sf.n; ++q) {
+            unsigned long long v = ~0ull;
+            unsigned long long *kq = nullptr;
+            if (on) {
+                kq = key + 2 * ((size_t)b * sf.n + q);
+                const unsigned long long dk = dkey(rigid_plane_dist<SOA>(k, p, x_ref, B[b], sf.s[q]));
+                if (stage == 0) v = dk;
+                else if (dk == kq[0])
+                    v = ((unsigned long long)(perm ? perm[p] : p) << 32) | (unsigned long long)(unsigned)p;
+            }
+            if (one) {
+                v = warp_min_u64(v);
+                if (lane == 0 && v != ~0ull) atomicMin(key + 2 * ((size_t)b0 * sf.n + q) + stage, v);
+            } else if (on && v != ~0ull) {
+                atomicMin(kq + stage, v);
+            }
         }
     }
 }
 
-// one restitution contact per body (_apply_rigid_restitution, mpm_solver_warp.py:
-// 915-975): push the body out by the deepest penetration, then a normal impulse
-// -(1 + e) v_n / (1/M + ((I^-1 (r x n)) x r) . n) and a Coulomb-capped tangential
-// one, in float64 with the body state rounded to float32 as the reference stores
-// it; resets the keys for the next surface
+// The restitution contacts of one body, surface after surface
+// (_apply_rigid_restitution, mpm_solver_warp.py:915-975): where the deepest
+// particle, shifted by the pushes so far, penetrates, push the body out by that
+// depth, then apply a normal impulse -(1 + e) v_n / (1/M + ((I^-1 (r x n)) x r) . n)
+// and a Coulomb-capped tangential one, in float64 with the body state rounded to
+// float32 as the reference stores it. Resets the keys for the next substep.
 template <bool SOA>
 __global__ void k_rigid_impulse(PK k, gbmpm_rigid_body *B, int nb, const float *x_ref, unsigned long long *key,
-                                gbmpm_rigid_surface sf, int tail_sub) {
+                                RigidSurfaces sfs, int tail_sub) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nb) return;
-    unsigned long long *kb = key + 2 * (size_t)b;
-    const unsigned long long k0 = kb[0], k1 = kb[1];
-    kb[0] = ~0ull;
-    kb[1] = ~0ull;
-    const double t = k.sub_time[tail_sub];
-    if (!(t >= sf.start_time && t < sf.end_time) || k0 == ~0ull) return;
-    const double dmin = dunkey(k0);
-    if (!(dmin < 0.0)) return;
-    const int p = (int)(unsigned)(k1 & 0xffffffffull);
     gbmpm_rigid_body r = B[b];
-    const double n[3] = {sf.normal[0], sf.normal[1], sf.normal[2]};
-    float xr[3];
-    fld_load<SOA, 3>(x_ref, k.n, p, xr);
-    double xc[3], push[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const float xw = r.x_cm[i] + (r.R[3 * i] * xr[0] + r.R[3 * i + 1] * xr[1] + r.R[3 * i + 2] * xr[2]);
-        push[i] = -dmin * n[i];
-        xc[i] = (double)xw + push[i];
-        r.x_cm[i] = (float)((double)r.x_cm[i] + push[i]);
-    }
+    const float xc0[3] = {r.x_cm[0], r.x_cm[1], r.x_cm[2]};   // the pose the distances were measured at
     float T1[9], Iwf[9];
     m33(r.R, r.inv_inertia, T1);
     mmT(T1, r.R, Iwf);
@@ -181,19 +230,43 @@ __global__ void k_rigid_impulse(PK k, gbmpm_rigid_body *B, int nb, const float *
 #pragma unroll
         for (int i = 0; i < 3; ++i) o[i] = Iw[3 * i] * v[0] + Iw[3 * i + 1] * v[1] + Iw[3 * i + 2] * v[2];
     };
-    double rr[3], om[3], vc[3], tmp[3];
+    const double t = k.sub_time[tail_sub];
+    double pacc[3] = {0.0, 0.0, 0.0};   // pushes so far
+    for (int q = 0; q < sfs.n; ++q) {
+        unsigned long long *kb = key + 2 * ((size_t)b * sfs.n + q);
+        const unsigned long long k0 = kb[0], k1 = kb[1];
+        kb[0] = ~0ull;
+        kb[1] = ~0ull;
+        const gbmpm_rigid_surface &sf = sfs.s[q];
+        if (!(t >= sf.start_time && t < sf.end_time) || k0 == ~0ull) continue;
+        const double n[3] = {sf.normal[0], sf.normal[1], sf.normal[2]};
+        const double dmin = dunkey(k0) + (pacc[0] * n[0] + pacc[1] * n[1] + pacc[2] * n[2]);
+        if (!(dmin < 0.0)) continue;
+        const int p = (int)(unsigned)(k1 & 0xffffffffull);
+        float xr[3];
+        fld_load<SOA, 3>(x_ref, k.n, p, xr);
+        double xc[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) { rr[i] = xc[i] - (double)r.x_cm[i]; om[i] = (double)r.omega[i]; }
-    cross(om, rr, tmp);
+        for (int i = 0; i < 3; ++i) {
+            const float xw = xc0[i] + (r.R[3 * i] * xr[0] + r.R[3 * i + 1] * xr[1] + r.R[3 * i + 2] * xr[2]);
+            const double push = -dmin * n[i];
+            pacc[i] += push;
+            xc[i] = (double)xw + pacc[i];
+            r.x_cm[i] = (float)((double)r.x_cm[i] + push);
+        }
+        double rr[3], om[3], vc[3], tmp[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) vc[i] = (double)r.v_cm[i] + tmp[i];
-    const double vn = vc[0] * n[0] + vc[1] * n[1] + vc[2] * n[2];
-    if (vn < 0.0) {
+        for (int i = 0; i < 3; ++i) { rr[i] = xc[i] - (double)r.x_cm[i]; om[i] = (double)r.omega[i]; }
+        cross(om, rr, tmp);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) vc[i] = (double)r.v_cm[i] + tmp[i];
+        const double vn = vc[0] * n[0] + vc[1] * n[1] + vc[2] * n[2];
+        if (!(vn < 0.0)) continue;
         const double M = (double)r.mass;
-        double rxn[3], q[3], qq[3];
+        double rxn[3], qv[3], qq[3];
         cross(rr, n, rxn);
-        mv(rxn, q);
-        cross(q, rr, qq);
+        mv(rxn, qv);
+        cross(qv, rr, qq);
         const double den = 1.0 / M + (qq[0] * n[0] + qq[1] * n[1] + qq[2] * n[2]);
         const double Jn = -(1.0 + sf.restitution) * vn / den;
         double dw[3];

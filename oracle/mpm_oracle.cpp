@@ -1466,6 +1466,11 @@ void rigid_tail(const gbmpm_particles* P, const gbmpm_model* M, Grid& G, double 
         svd3_impl(Rm, U, sg, V);
         store33(r.R, mmul(U, mT(V)));
         for (int a = 0; a < 3; ++a) { r.v_cm[a] = v[a]; r.omega[a] = w[a]; }
+        // world positions once, from the integrated pose; each surface's deepest
+        // particle is taken there and shifted by the pushes of the surfaces before
+        // it (the reference adds each push to its world positions)
+        const float xc0[3] = {r.x_cm[0], r.x_cm[1], r.x_cm[2]};
+        double pacc[3] = {0.0, 0.0, 0.0};
         for (const gbmpm_rigid_surface& sf : g_rigid.surf) {
             if (!(time >= sf.start_time && time < sf.end_time)) continue;
             double dmin = 0.0;
@@ -1475,19 +1480,22 @@ void rigid_tail(const gbmpm_particles* P, const gbmpm_model* M, Grid& G, double 
                 const float* xr = P->x_ref + 3 * (size_t)p;
                 double d = 0.0;
                 for (int i = 0; i < 3; ++i) {
-                    const float xw = r.x_cm[i] + (r.R[3 * i] * xr[0] + r.R[3 * i + 1] * xr[1] + r.R[3 * i + 2] * xr[2]);
+                    const float xw = xc0[i] + (r.R[3 * i] * xr[0] + r.R[3 * i + 1] * xr[1] + r.R[3 * i + 2] * xr[2]);
                     d += ((double)xw - sf.point[i]) * sf.normal[i];
                 }
                 if (pmin < 0 || d < dmin) { dmin = d; pmin = p; }
             }
-            if (pmin < 0 || !(dmin < 0.0)) continue;
+            if (pmin < 0) continue;
+            dmin += pacc[0] * sf.normal[0] + pacc[1] * sf.normal[1] + pacc[2] * sf.normal[2];
+            if (!(dmin < 0.0)) continue;
             const double* n = sf.normal;
             const float* xr = P->x_ref + 3 * (size_t)pmin;
             double xc[3];
             for (int i = 0; i < 3; ++i) {
-                const float xw = r.x_cm[i] + (r.R[3 * i] * xr[0] + r.R[3 * i + 1] * xr[1] + r.R[3 * i + 2] * xr[2]);
+                const float xw = xc0[i] + (r.R[3 * i] * xr[0] + r.R[3 * i + 1] * xr[1] + r.R[3 * i + 2] * xr[2]);
                 const double push = -dmin * n[i];
-                xc[i] = (double)xw + push;
+                pacc[i] += push;
+                xc[i] = (double)xw + pacc[i];
                 r.x_cm[i] = (float)((double)r.x_cm[i] + push);
             }
             float Iwf[9];
