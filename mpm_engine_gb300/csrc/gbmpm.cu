@@ -2370,6 +2370,8 @@ struct gbmpm_engine {
     DevBuf<gbmpm_rigid_body> d_bodies;
     DevBuf<double> d_racc;                  // [body][6] gathered momentum, angular momentum
     DevBuf<unsigned long long> d_rkey;      // [body][surface][2] contact keys (distance, particle)
+    DevBuf<int> d_rlist, d_rcount;          // this tick's rigid particles (k_rigid_list) and their count
+    int n_rigid = 0;                        // rigid particles when the bodies were set (grid sizing)
     int n_mods = 0;
     DevBuf<gbmpm_modifier> d_mods;
     double *h_time = nullptr;               // pinned staging of d_time
@@ -2904,11 +2906,12 @@ void record_rigid(gbmpm_engine *e, const gbmpm_particles &P, float dtf, int tail
     if (P.n == 0) return;
     PK k = make_pk(e, P, dtf, list);   // the deposit marks the block list the next grid pass reads
     k.sub = sub;
-    const int pb = (int)std::max<long long>(1, std::min<long long>((P.n + 255) / 256, (long long)e->num_sms * 8));
+    const long long nr = std::max(32, e->n_rigid);
+    const int pb = (int)std::max<long long>(1, std::min<long long>((nr + 255) / 256, (long long)e->num_sms * 8));
     const int nb = e->n_bodies, bb = (nb + 63) / 64;
-    const int *rid = P.rigid_id;
-    if (soa) k_rigid_gather<true><<<pb, 256, 0, s>>>(k, rid, e->d_bodies.ptr, e->d_racc.ptr);
-    else k_rigid_gather<false><<<pb, 256, 0, s>>>(k, rid, e->d_bodies.ptr, e->d_racc.ptr);
+    const int *rid = P.rigid_id, *rl = e->d_rlist.ptr, *rc = e->d_rcount.ptr;
+    if (soa) k_rigid_gather<true><<<pb, 256, 0, s>>>(k, rl, rc, rid, e->d_bodies.ptr, e->d_racc.ptr);
+    else k_rigid_gather<false><<<pb, 256, 0, s>>>(k, rl, rc, rid, e->d_bodies.ptr, e->d_racc.ptr);
     k_rigid_integrate<<<bb, 64, 0, s>>>(e->d_bodies.ptr, nb, e->d_racc.ptr, dtf);
     e->launches += 2;
     if (!e->rsurf.empty()) {
@@ -2917,17 +2920,18 @@ void record_rigid(gbmpm_engine *e, const gbmpm_particles &P, float dtf, int tail
         for (int q = 0; q < sf.n; ++q) sf.s[q] = e->rsurf[q];
         for (int stage = 0; stage < 2; ++stage) {
             if (soa)
-                k_rigid_contact<true><<<pb, 256, 0, s>>>(k, rid, P.x_ref, e->d_bodies.ptr, sf, e->d_rkey.ptr, stage, perm);
+                k_rigid_contact<true><<<pb, 256, 0, s>>>(k, rl, rc, rid, P.x_ref, e->d_bodies.ptr, sf, e->d_rkey.ptr,
+                                                         stage, perm);
             else
-                k_rigid_contact<false><<<pb, 256, 0, s>>>(k, rid, P.x_ref, e->d_bodies.ptr, sf, e->d_rkey.ptr, stage,
-                                                          nullptr);
+                k_rigid_contact<false><<<pb, 256, 0, s>>>(k, rl, rc, rid, P.x_ref, e->d_bodies.ptr, sf, e->d_rkey.ptr,
+                                                          stage, nullptr);
         }
         if (soa) k_rigid_impulse<true><<<bb, 64, 0, s>>>(k, e->d_bodies.ptr, nb, P.x_ref, e->d_rkey.ptr, sf, tail_sub);
         else k_rigid_impulse<false><<<bb, 64, 0, s>>>(k, e->d_bodies.ptr, nb, P.x_ref, e->d_rkey.ptr, sf, tail_sub);
         e->launches += 3;
     }
-    if (soa) k_rigid_update<true><<<pb, 256, 0, s>>>(k, rid, P.x_ref, e->d_bodies.ptr, deposit ? 1 : 0);
-    else k_rigid_update<false><<<pb, 256, 0, s>>>(k, rid, P.x_ref, e->d_bodies.ptr, deposit ? 1 : 0);
+    if (soa) k_rigid_update<true><<<pb, 256, 0, s>>>(k, rl, rc, rid, P.x_ref, e->d_bodies.ptr, deposit ? 1 : 0);
+    else k_rigid_update<false><<<pb, 256, 0, s>>>(k, rl, rc, rid, P.x_ref, e->d_bodies.ptr, deposit ? 1 : 0);
     e->launches++;
 }
 
@@ -2957,6 +2961,12 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
     const gbmpm_particles &P = reorder ? e->W : e->P;
     const bool cdf = e->cdf.n > 0;
     const bool rigid = e->n_bodies > 0 && P.rigid_id && P.x_ref;
+    if (rigid && P.n > 0) {   // this tick's rigid particles, in its particle order
+        cudaMemsetAsync(e->d_rcount.ptr, 0, sizeof(int), s);
+        const int g = (int)std::max<long long>(1, std::min<long long>((P.n + 255) / 256, (long long)e->num_sms * 8));
+        k_rigid_list<<<g, 256, 0, s>>>(P.material, P.selection, P.n, e->d_rlist.ptr, e->d_rcount.ptr);
+        e->launches++;
+    }
     double tc = t0;
     for (int sub = 0; sub < S; ++sub) {
         int list = sub & 1;
@@ -3051,6 +3061,7 @@ void gbmpm_engine_destroy(gbmpm_engine *e) {
     if (e->h_coldev) cudaFreeHost(e->h_coldev);
     if (e->h_time) cudaFreeHost(e->h_time);
     e->d_bodies.release(); e->d_racc.release(); e->d_rkey.release(); e->d_mods.release(); e->d_time.release();
+    e->d_rlist.release(); e->d_rcount.release();
     e->d_tab.release(); e->d_cols.release(); e->d_pose.release(); e->d_wrench.release();
     e->d_flag.release(); e->d_list.release(); e->d_count.release(); e->d_status.release();
     e->d_guard.release(); e->d_keys[0].release(); e->d_keys[1].release(); e->d_skeys.release(); e->d_kminmax.release(); e->d_idx[0].release();
@@ -3179,6 +3190,14 @@ int gbmpm_set_rigid(gbmpm_engine *e, const gbmpm_rigid_body *bodies, int32_t n_b
         GB_CUDA(e->d_racc.ensure(6 * (size_t)n_bodies));
         GB_CUDA(e->d_rkey.ensure(2 * (size_t)n_bodies * GBMPM_MAX_RIGID_SURFACES));
         GB_CUDA(cudaMemcpy(e->d_bodies.ptr, bodies, n_bodies * sizeof(gbmpm_rigid_body), cudaMemcpyHostToDevice));
+        GB_CUDA(e->d_rlist.ensure(std::max(1, e->P.n)));
+        GB_CUDA(e->d_rcount.ensure(1));
+        GB_CUDA(cudaMemset(e->d_rcount.ptr, 0, sizeof(int)));
+        if (e->P.n > 0) {   // how many particles are rigid now: sizes the rigid passes' grids
+            k_rigid_list<<<std::max(1, std::min((e->P.n + 255) / 256, e->num_sms * 8)), 256>>>(
+                e->P.material, e->P.selection, e->P.n, e->d_rlist.ptr, e->d_rcount.ptr);
+            GB_CUDA(cudaMemcpy(&e->n_rigid, e->d_rcount.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+        }
         GB_CUDA(cudaMemset(e->d_racc.ptr, 0, 6 * (size_t)n_bodies * sizeof(double)));
         GB_CUDA(cudaMemset(e->d_rkey.ptr, 0xff, 2 * (size_t)n_bodies * GBMPM_MAX_RIGID_SURFACES *
                                                    sizeof(unsigned long long)));

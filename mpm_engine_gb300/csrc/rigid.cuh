@@ -22,6 +22,23 @@ struct RigidSurfaces {   // the rigid contact surfaces, by value
     int n;
 };
 
+// The rigid particles of the tick's particle order, compacted once per tick so the
+// rigid passes visit them alone (order within the list is arbitrary; nothing the
+// passes compute depends on it beyond float summation order).
+__global__ void k_rigid_list(const int *mat, const int *sel, int n, int *list, int *count) {
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x - lane; base < n; base += gridDim.x * blockDim.x) {
+        const int p = base + lane;
+        const bool on = p < n && !(sel && sel[p] != 0) && mat[p] == 8;
+        const unsigned act = __ballot_sync(0xffffffffu, on);
+        if (!act) continue;
+        int first = 0;
+        if (lane == 0) first = atomicAdd(count, __popc(act));
+        first = __shfl_sync(0xffffffffu, first, 0);
+        if (on) list[first + __popc(act & ((1u << lane) - 1u))] = p;
+    }
+}
+
 // A warp whose rigid particles all belong to one body (the usual case: particles
 // arrive block-sorted) reduces with shuffles and makes one atomic per warp;
 // otherwise each particle makes its own. The loops below step whole warps.
@@ -49,12 +66,14 @@ __device__ __forceinline__ void rigid_velocity(const PK &k, const Stencil &s, fl
 // rigid_g2p_accumulate (mpm_utils.py:1369-1414): each rigid particle's momentum
 // and angular momentum about its body's centre of mass, summed per body in float64
 template <bool SOA>
-__global__ void k_rigid_gather(PK k, const int *rid, const gbmpm_rigid_body *B, double *acc) {
+__global__ void k_rigid_gather(PK k, const int *rlist, const int *rcount, const int *rid, const gbmpm_rigid_body *B,
+                               double *acc) {
     const int lane = threadIdx.x & 31;
     const int stride = gridDim.x * blockDim.x;
-    for (int base = blockIdx.x * blockDim.x + threadIdx.x - lane; base < k.n; base += stride) {
-        const int p = base + lane;
-        bool on = p < k.n && !(k.sel && k.sel[p] != 0) && k.mat[p] == 8;
+    const int cnt = *rcount;
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x - lane; base < cnt; base += stride) {
+        bool on = base + lane < cnt;
+        const int p = on ? rlist[base + lane] : 0;
         const int b = on ? rid[p] : -1;
         double c6[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         if (on) {
@@ -171,13 +190,15 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v)
 // which leaves each surface's deepest particle unchanged (the reference likewise
 // shifts its world positions by each push). Keys: [body][surface][2].
 template <bool SOA>
-__global__ void k_rigid_contact(PK k, const int *rid, const float *x_ref, const gbmpm_rigid_body *B,
-                                RigidSurfaces sf, unsigned long long *key, int stage, const int *perm) {
+__global__ void k_rigid_contact(PK k, const int *rlist, const int *rcount, const int *rid, const float *x_ref,
+                                const gbmpm_rigid_body *B, RigidSurfaces sf, unsigned long long *key, int stage,
+                                const int *perm) {
     const int lane = threadIdx.x & 31;
     const int stride = gridDim.x * blockDim.x;
-    for (int base = blockIdx.x * blockDim.x + threadIdx.x - lane; base < k.n; base += stride) {
-        const int p = base + lane;
-        const bool on = p < k.n && !(k.sel && k.sel[p] != 0) && k.mat[p] == 8;
+    const int cnt = *rcount;
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x - lane; base < cnt; base += stride) {
+        const bool on = base + lane < cnt;
+        const int p = on ? rlist[base + lane] : 0;
         const int b = on ? rid[p] : -1;
         int b0;
         const bool one = warp_one_body(on, b, b0);
@@ -307,9 +328,11 @@ __global__ void k_rigid_impulse(PK k, gbmpm_rigid_body *B, int nb, const float *
 // omega x r, C = skew(omega), F = I; with `deposit` the particle's P2G follows
 // (a rigid particle carries no stress)
 template <bool SOA>
-__global__ void k_rigid_update(PK k, const int *rid, const float *x_ref, const gbmpm_rigid_body *B, int deposit) {
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < k.n; p += gridDim.x * blockDim.x) {
-        if ((k.sel && k.sel[p] != 0) || k.mat[p] != 8) continue;
+__global__ void k_rigid_update(PK k, const int *rlist, const int *rcount, const int *rid, const float *x_ref,
+                               const gbmpm_rigid_body *B, int deposit) {
+    const int cnt = *rcount;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+        const int p = rlist[i];
         const gbmpm_rigid_body &r = B[rid[p]];
         float xr[3], x[3], v[3];
         fld_load<SOA, 3>(x_ref, k.n, p, xr);
