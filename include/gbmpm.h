@@ -223,6 +223,14 @@ int gbmpm_reset_cdf_wrench(gbmpm_engine *e, void *stream);
  * mpm_solver_warp.py:2906-2915), copied into caller device buffers of n_grid^3
  * entries (either may be NULL), and the number of stamps so far (_cdf_stamp_count). */
 int gbmpm_cdf_grids(gbmpm_engine *e, int32_t *tag_out, float *d_out, int64_t *stamps, void *stream);
+/* Stamp every CDF lane now, at `time` (MPM_Simulator_WARP._stamp_cdf called
+ * directly, mpm_solver_warp.py:3040-3098); the previous grids take the new stamp. */
+int gbmpm_cdf_restamp(gbmpm_engine *e, double time, void *stream);
+/* on != 0: restamp every lane at every substep instead of only the lanes that moved
+ * or changed activity (the _cdf_force_stamp switch, :3046-3052). */
+int gbmpm_cdf_force_stamp(gbmpm_engine *e, int32_t on);
+/* 1 when a captured tick graph is ready for replay. */
+int32_t gbmpm_graph_state(gbmpm_engine *e);
 
 /* Current volume vol0 * J, Cauchy stress = stress / J and J = det(F) per particle
  * (Solver.vol / Solver.cauchy, core/solver.py:559-598) into caller device buffers

@@ -178,6 +178,9 @@ _SIGNATURES = {
                                    C.c_void_p]),
     "gbmpm_batch_guard": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.c_void_p]),
     "gbmpm_batch_launch_count": (C.c_int64, [C.c_void_p]),
+    "gbmpm_cdf_restamp": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p]),
+    "gbmpm_cdf_force_stamp": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gbmpm_graph_state": (C.c_int32, [C.c_void_p]),
     "gbmpm_set_rigid": (C.c_int, [C.c_void_p, C.POINTER(RigidBody), C.c_int32, C.POINTER(RigidSurface), C.c_int32]),
     "gbmpm_get_rigid": (C.c_int, [C.c_void_p, C.POINTER(RigidBody), C.c_int32, C.c_void_p]),
     "gbmpm_set_modifiers": (C.c_int, [C.c_void_p, C.POINTER(Modifier), C.c_int32]),

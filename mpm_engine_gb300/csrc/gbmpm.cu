@@ -2281,6 +2281,7 @@ struct CdfHost {
     bool stale_set = false;     // tag_prev lags tag inside stale_box
     int stale_box[6] = {};
     bool lane_prev_stale = false;
+    bool force = false;         // restamp every lane every substep (no dirty-lane skip)
     int64_t stamps = 0;
     void sync_lane(int l) {    // _sync_cdf_lane (mpm_solver_warp.py:2883-2905)
         for (int a = 0; a < 3; ++a) {
@@ -2759,6 +2760,8 @@ void cdf_stamp(gbmpm_engine *e, double time, bool lag_prev, cudaStream_t s) {
         bool act = time >= (double)H.rec[l].start_time && time < (double)H.rec[l].end_time;
         if (act != H.active[l]) { H.active[l] = act; H.dirty[l] = true; }
     }
+    if (H.force)
+        for (int l = 0; l < H.n; ++l) H.dirty[l] = true;
     bool any = false;
     for (int l = 0; l < H.n; ++l) any = any || H.dirty[l];
     if (!any) { flush_stale(); return; }
@@ -3322,6 +3325,23 @@ int gbmpm_cdf_grids(gbmpm_engine *e, int32_t *tag_out, float *d_out, int64_t *st
     if (d_out) GB_CUDA(cudaMemcpyAsync(d_out, e->c_d.ptr, N * sizeof(float), cudaMemcpyDeviceToDevice, s));
     return GBMPM_OK;
 }
+
+int gbmpm_cdf_restamp(gbmpm_engine *e, double time, void *stream) {
+    if (!e) return fail(GBMPM_ERR_ARG, "null argument");
+    if (e->cdf.n == 0) return GBMPM_OK;
+    for (int l = 0; l < e->cdf.n; ++l) e->cdf.dirty[l] = true;
+    cdf_stamp(e, time, false, (cudaStream_t)stream);
+    GB_CUDA(cudaGetLastError());
+    return GBMPM_OK;
+}
+
+int gbmpm_cdf_force_stamp(gbmpm_engine *e, int32_t on) {
+    if (!e) return fail(GBMPM_ERR_ARG, "null argument");
+    e->cdf.force = on != 0;
+    return GBMPM_OK;
+}
+
+int32_t gbmpm_graph_state(gbmpm_engine *e) { return (e && e->graph) ? 1 : 0; }
 
 int gbmpm_reset_cdf_wrench(gbmpm_engine *e, void *stream) {
     if (!e) return fail(GBMPM_ERR_ARG, "null argument");

@@ -92,6 +92,16 @@ class _DeviceArray:
         self._t.zero_()
 
 
+class _HostArray:
+    """A host array behind Warp's `.numpy()` accessor."""
+
+    def __init__(self, a):
+        self._a = a
+
+    def numpy(self):
+        return self._a
+
+
 class _StateView:
     def __init__(self, s: Solver):
         self._s = s
@@ -101,6 +111,9 @@ class _StateView:
         key = name[len("particle_"):] if name.startswith("particle_") else None
         if key in t:
             return _DeviceArray(t[key])
+        if name in ("grid_cdf_tag", "grid_cdf_d"):   # the CPIC node grids (mpm_solver_warp.py:94-183)
+            tag, d, _ = self._s.cdf_grids()
+            return _HostArray(tag if name == "grid_cdf_tag" else d)
         raise AttributeError(name)
 
 
@@ -138,16 +151,6 @@ class _ModelView:
     cdf_mask_off = 0
 
 
-class _HostArray:
-    """A host array behind Warp's `.numpy()` accessor."""
-
-    def __init__(self, a):
-        self._a = a
-
-    def numpy(self):
-        return self._a
-
-
 class _SimShim:
     """The parts of MPM_Simulator_WARP that tests and scripts touch through
     `Solver._sim` (mpm_solver_warp.py), mapped onto this engine."""
@@ -172,6 +175,40 @@ class _SimShim:
     @property
     def n_particles(self) -> int:
         return self._s._n
+
+    @property
+    def _graph_A(self):
+        """Non-None once the engine holds a captured tick graph."""
+        s = self._s
+        return "tick graph" if s._eng is not None and s._eng.lib.gbmpm_graph_state(s._eng.h) else None
+
+    @property
+    def collider_aabbs(self):
+        """One callable per collider record, in order, giving the grid node box
+        ((lo), (dims)) the collider can reach, or None when it lies outside the grid
+        (the restricted-launch boxes of mpm_solver_warp.py:1283-1336). The engine
+        applies colliders over the active blocks only, so the boxes are informational."""
+        return [lambda rec=rec: self._s._collider_box(rec) for rec in self._s._cols]
+
+    def _stamp_cdf(self, dt=None, device=None):
+        """Stamp every CDF lane now (mpm_solver_warp.py:3040-3098)."""
+        s = self._s
+        s._sync_engine()
+        _abi.check(s._eng.lib.gbmpm_cdf_restamp(s._eng.h, float(s._time), s._stream()), "gbmpm_cdf_restamp")
+
+    @property
+    def _cdf_force_stamp(self):
+        return self._s._cdf_force
+
+    @_cdf_force_stamp.setter
+    def _cdf_force_stamp(self, on):
+        s = self._s
+        s._cdf_force = bool(on)
+        _abi.check(s._eng.lib.gbmpm_cdf_force_stamp(s._eng.h, 1 if on else 0), "gbmpm_cdf_force_stamp")
+
+    @property
+    def _cdf_stamp_count(self):
+        return self._s.cdf_grids()[2]
 
     # rigid-body arrays of MPM_Simulator_WARP (mpm_solver_warp.py:495-504), read from the engine
     def _rigid_field(self, name, shape):
@@ -306,6 +343,7 @@ class Solver:
         self._rigid_surfaces: list = []
         self._n_bodies = 0
         self._mods: list = []          # particle modifier records, in registration order
+        self._cdf_force = False
         self._update_cov = False
 
     # ------------------------------------------------------------------ setup
@@ -515,6 +553,24 @@ class Solver:
         self._sim.n_rigid_bodies = len(recs)
         self._push_rigid((_abi.RigidBody * len(recs))(*recs))
         return self
+
+    def _collider_box(self, rec):
+        """Grid node box a collider record can reach, or None outside the grid."""
+        ng, dx = int(self.grid.n_grid), float(self.grid.dx)
+        c = np.array(rec.point[:], np.float64)
+        if rec.kind == _abi.COLLIDER_SDF:
+            ext = host.sdf_r_max(np.array(rec.sdf_origin[:]), float(rec.sdf_cell), int(rec.sdf_res)) + float(rec.band)
+        elif rec.kind == _abi.COLLIDER_CUP:
+            ext = float(rec.outer_radius) + float(rec.half_height) + float(rec.contact_band)
+        elif rec.kind == _abi.COLLIDER_BOX:
+            ext = np.abs(np.array(rec.size[:], np.float64))
+        else:
+            return (0, 0, 0), (ng, ng, ng)
+        lo = np.maximum(np.floor((c - ext) / dx).astype(int) - 2, 0)
+        hi = np.minimum(np.ceil((c + ext) / dx).astype(int) + 3, ng)
+        if np.any(hi <= lo):
+            return None
+        return tuple(int(v) for v in lo), tuple(int(v) for v in hi - lo)
 
     def _surface_records(self):
         arr = (_abi.RigidSurface * max(1, len(self._rigid_surfaces)))()
