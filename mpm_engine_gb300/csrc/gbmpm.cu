@@ -154,6 +154,14 @@ __device__ __forceinline__ void mat_store(float *p, const float (&m)[9]) {
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// 4-byte asynchronous global -> shared copy; cp.async.wait_all makes the calling
+// thread's copies complete and visible to that thread
+__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // Particle fields are either the caller's records (AoS: W floats per particle)
 // or the engine's working copy (SoA: component c of particle p at c*n + p, so a
 // warp's access to one component is one coalesced line).
@@ -581,9 +589,11 @@ __device__ __forceinline__ void g2p_core(const PK &k, const Stencil &s, Fetch fe
     }
 }
 
-// advection, F_trial and covariance after the gather
+// advection, F_trial and covariance after the gather; Fpre, when given, holds the
+// particle's F (already fetched) instead of the field
 template <bool SOA>
-__device__ __forceinline__ void g2p_finish(const PK &k, int p, float *x, const float *v, const float *L, float *Ft) {
+__device__ __forceinline__ void g2p_finish(const PK &k, int p, float *x, const float *v, const float *L, float *Ft,
+                                           const float *Fpre = nullptr) {
     float xn[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) xn[a] = x[a] + k.dt * v[a];
@@ -595,7 +605,12 @@ __device__ __forceinline__ void g2p_finish(const PK &k, int p, float *x, const f
 #pragma unroll
     for (int a = 0; a < 3; ++a) x[a] = xn[a];
     float Fo[9], A[9];
-    fld_load<SOA, 9>(k.F, k.n, p, Fo);
+    if (Fpre) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Fo[i] = Fpre[i];
+    } else {
+        fld_load<SOA, 9>(k.F, k.n, p, Fo);
+    }
 #pragma unroll
     for (int i = 0; i < 9; ++i) A[i] = ((i % 4 == 0) ? 1.0f : 0.0f) + L[i] * k.dt;
     mm(A, Fo, Ft);
@@ -1066,6 +1081,7 @@ constexpr int kRec = 40;                  // floats per particle scatter record 
 constexpr int kRecStride = 44;
 constexpr int kSmemFloats =
     (kGatherCap * 4 > kTileThreads * kRecStride) ? kGatherCap * 4 : kTileThreads * kRecStride;
+static_assert(kGatherCap * 4 + 11 * kTileThreads <= kSmemFloats, "prefetch slots fit past the gather tile");
 
 struct TileBox {
     int lo[3], e[3];
@@ -1129,6 +1145,12 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
     __shared__ int s_seg[kTileThreads + 1];
     __shared__ int s_wcnt[kTileThreads / 32];
     __shared__ int s_red[kTileThreads / 32][6];
+    // F, mass and volume of a gather pass's particle, fetched asynchronously at the
+    // start so that their L2 round trip overlaps the tile box, the tile load and the
+    // gather (a gather pass starts before its wait: nothing still running writes
+    // them). The slots lie past the gather tile, in the record area, and are read
+    // into registers before the barrier that ends the gather.
+    float(*s_pf)[kTileThreads] = reinterpret_cast<float(*)[kTileThreads]>(s_mem + kGatherCap * 4);
     const int t = threadIdx.x;
     const int lane = t & 31, warp = t >> 5;
     const int p = blockIdx.x * kTileThreads + t;
@@ -1138,9 +1160,19 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
         pdl_wait();
         pdl_trigger();
     }
+    const bool pf = (mode & PASS_G2P) && live;
+    if (pf) {
+#pragma unroll
+        for (int c = 0; c < 9; ++c) cp_async4(&s_pf[c][t], k.F + (size_t)c * k.n + p);
+        if (mode & PASS_P2G) {
+            cp_async4(&s_pf[9][t], k.mass + p);
+            cp_async4(&s_pf[10][t], k.vol + p);
+        }
+    }
     float x[3] = {0.f, 0.f, 0.f};
     if (live) fld_load<true, 3>(k.x, k.n, p, x);
     float v[3] = {0.f, 0.f, 0.f}, C[9], L[9], Ft[9], S[9];
+    float Fpf[9], mpf = 0.f, vpf = 0.f;
     bool gathered = false;
     int ptag = 0;   // CPIC particle tag carried from the gather into the scatter
     if (mode & PASS_G2P) {
@@ -1185,6 +1217,16 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
             k.blk_count[1] = 0;
         }
         float4 *s_tile = reinterpret_cast<float4 *>(s_mem);
+        // the prefetched fields, taken into registers before the record area is reused
+        auto take_prefetch = [&]() {
+            if (pf) {
+                cp_async_wait_all();
+#pragma unroll
+                for (int c = 0; c < 9; ++c) Fpf[c] = s_pf[c][t];
+                mpf = s_pf[9][t];
+                vpf = s_pf[10][t];
+            }
+        };
         if (box.fits) {
             const int e12 = box.e[1] * box.e[2];
             for (int q = t; q < box.vol; q += kTileThreads) {
@@ -1200,15 +1242,19 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
                     return (CDF && ((gmask >> ((i * 3 + j) * 3 + kk)) & 1)) ? g4 : t4;
                 }, v, C, L);
             }
+            take_prefetch();
             __syncthreads();
-        } else if (want) {
-            g2p_core(k, s, [&](int i, int j, int kk) {
-                const float4 t4 = global_fetch(k, s, i, j, kk);
-                return (CDF && ((gmask >> ((i * 3 + j) * 3 + kk)) & 1)) ? g4 : t4;
-            }, v, C, L);
+        } else {   // box.fits is uniform over the CTA, so is this branch and its barrier
+            if (want)
+                g2p_core(k, s, [&](int i, int j, int kk) {
+                    const float4 t4 = global_fetch(k, s, i, j, kk);
+                    return (CDF && ((gmask >> ((i * 3 + j) * 3 + kk)) & 1)) ? g4 : t4;
+                }, v, C, L);
+            take_prefetch();
+            __syncthreads();
         }
         if (want) {
-            g2p_finish<true>(k, p, x, v, L, Ft);
+            g2p_finish<true>(k, p, x, v, L, Ft, Fpf);
             gathered = true;
             fld_store<true, 3>(k.x, k.n, p, x);
             if (!(mode & (PASS_STRESS | PASS_P2G)) || (mode & PASS_STORE_VC)) {
@@ -1292,8 +1338,8 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, in
                     Cr[3 * i + j] = (k.rpic < -0.001f) ? 0.0f
                                     : (1.0f - k.rpic) * C[3 * i + j] + k.rpic / 2.0f * (C[3 * i + j] - C[3 * j + i]);
         }
-        const float m = k.mass[p];
-        const float fs = -k.vol[p] * k.dt * k.inv_dx;
+        const float m = (pf && (mode & PASS_P2G)) ? mpf : k.mass[p];
+        const float fs = -((pf && (mode & PASS_P2G)) ? vpf : k.vol[p]) * k.dt * k.inv_dx;
         float rec[kRec];
 #pragma unroll
         for (int o = 0; o < 3; ++o) {
