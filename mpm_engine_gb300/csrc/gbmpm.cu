@@ -1968,14 +1968,20 @@ __global__ void __launch_bounds__(kGridThreads) k_grid(GK k) {
     for (int i = t; i < k.ncol * 6; i += blockDim.x) s_acc[i / 6][i % 6] = 0.0f;
     pdl_wait();   // the particle pass before this one deposits into gmv and fills the block list
     pdl_trigger();
+    const int per = blockDim.x / 64;
+    const int stride = gridDim.x * per;
+    const int first = blockIdx.x * per + t / 64;
+    // the count and this thread's first list entry are read together: the list holds
+    // bd^3 entries, and an entry at or past the count is never used
+    const int count = *k.blk_count_read;
+    int b_next = (first < k.bd * k.bd * k.bd) ? k.blk_list[first] : 0;
     if (blockIdx.x == 0 && t == 0) *k.blk_count_reset = 0;
     __syncthreads();
-    const int count = *k.blk_count_read;
-    const int per = blockDim.x / 64;
     const int lane = t & 31;
-    for (int item = blockIdx.x * per + t / 64; item < count; item += gridDim.x * per) {
+    for (int item = first; item < count; item += stride) {
         bool valid = true;
-        int b = k.blk_list[item];
+        int b = b_next;
+        if (item + stride < count) b_next = k.blk_list[item + stride];   // next iteration's entry, in flight now
         int bz = b % k.bd, r = b / k.bd, by = r % k.bd, bx = r / k.bd;
         int cell = t & 63;
         int gx = bx * 4 + (cell >> 4), gy = by * 4 + ((cell >> 2) & 3), gz = bz * 4 + (cell & 3);
