@@ -1073,8 +1073,8 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
 //    the run's contributions to that node from broadcast shared reads, and issue
 //    one red.global.add.v4.f32. Global atomics drop from 27 per particle to 27 per
 //    run, and no shared-memory atomics are needed.
-constexpr int kTileThreads = 256;
-constexpr int kGatherCap = 1536;          // nodes in the shared gather tile (24 KB)
+constexpr int kTileThreads = 128;
+constexpr int kGatherCap = 768;           // nodes in the shared gather tile (12 KB)
 constexpr int kRec = 40;                  // floats per particle scatter record (10 float4)
 // record stride in shared memory: 44 floats = 176 B, so the 16-byte stores of eight
 // consecutive lanes land on disjoint bank groups (a 160 B stride pairs them up)
@@ -1137,7 +1137,7 @@ __device__ __forceinline__ void bspline_o(float fx, int o, float &w, float &dw) 
 // (base cell, particle tag) so each run deposits under one mask, its blocked nodes
 // becoming the owner lane's reaction.
 template <bool SOLIDS, int MINB, bool CDF = false>
-__global__ void __launch_bounds__(kTileThreads, MINB) k_particles_tiled(PK k, int mode) {
+__global__ void __launch_bounds__(kTileThreads, MINB * 256 / kTileThreads) k_particles_tiled(PK k, int mode) {
     __shared__ __align__(16) float s_mem[kSmemFloats];
     __shared__ int s_key[kTileThreads];
     __shared__ int s_pc[CDF ? kTileThreads : 1];
