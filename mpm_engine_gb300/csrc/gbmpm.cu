@@ -1061,27 +1061,38 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
 }
 
 // ---- tiled kernel: block-sorted particles, shared-memory gather tile, run-wise scatter
-// Particles arrive sorted by (4^3 block, cell); a CTA owns kTileThreads
+// Particles arrive sorted by (4^3 block, cell); a CTA owns Tile<CDF>::threads
 // consecutive particles, one per thread.
 //  * Gather: the CTA reduces the bounding box of its stencils; when it holds at
-//    most kGatherCap nodes the grid velocity of that box is copied to shared
-//    memory and the 27-node gathers read it there (neighbouring threads share
-//    nodes, so most reads are broadcasts).
-//  * Scatter: each particle leaves a 25-float record in shared memory. Runs of
+//    most Tile<CDF>::gather_cap nodes the grid velocity of that box is copied to
+//    shared memory and the 27-node gathers read it there (neighbouring threads
+//    share nodes, so most reads are broadcasts).
+//  * Scatter: each particle leaves a 40-float record in shared memory. Runs of
 //    consecutive particles whose stencils share the same base node (the same
-//    cell) are scattered together: 27 lanes of a warp take one node each, sum
-//    the run's contributions to that node from broadcast shared reads, and issue
-//    one red.global.add.v4.f32. Global atomics drop from 27 per particle to 27 per
-//    run, and no shared-memory atomics are needed.
+//    cell) are scattered together, three runs per warp: nine lanes take one
+//    (i, j) node line each, sum the run's contributions to its three nodes from
+//    shared reads, and issue one red.global.add.v4.f32 per node. Global atomics
+//    drop from 27 per particle to 27 per run, and no shared-memory atomics are
+//    needed.
+// The plain pass runs 128-thread CTAs (six per SM); the CPIC pass, whose larger
+// body runs best with fewer, wider CTAs, 256 (three per SM).
 constexpr int kTileThreads = 128;
-constexpr int kGatherCap = 768;           // nodes in the shared gather tile (12 KB)
+constexpr int kTileThreadsCdf = 256;
 constexpr int kRec = 40;                  // floats per particle scatter record (10 float4)
 // record stride in shared memory: 44 floats = 176 B, so the 16-byte stores of eight
 // consecutive lanes land on disjoint bank groups (a 160 B stride pairs them up)
 constexpr int kRecStride = 44;
-constexpr int kSmemFloats =
-    (kGatherCap * 4 > kTileThreads * kRecStride) ? kGatherCap * 4 : kTileThreads * kRecStride;
-static_assert(kGatherCap * 4 + 11 * kTileThreads <= kSmemFloats, "prefetch slots fit past the gather tile");
+template <bool CDF>
+struct Tile {
+    static constexpr int threads = CDF ? kTileThreadsCdf : kTileThreads;
+    static constexpr int gather_cap = 6 * threads;   // nodes in the shared gather tile (16 B each)
+    static constexpr int smem_floats =
+        (gather_cap * 4 > threads * kRecStride) ? gather_cap * 4 : threads * kRecStride;
+    static_assert(gather_cap * 4 + 11 * threads <= smem_floats, "prefetch slots fit past the gather tile");
+};
+// the CPIC reaction partials are indexed by CTA; they are sized for the narrower of
+// the direct and the tiled CPIC launches
+constexpr int kCdfCtaThreads = kParticleThreads < kTileThreadsCdf ? kParticleThreads : kTileThreadsCdf;
 
 struct TileBox {
     int lo[3], e[3];
@@ -1089,7 +1100,8 @@ struct TileBox {
     bool fits;
 };
 
-__device__ __forceinline__ void block_box(const int *b, bool valid, TileBox &box, int (*s_red)[6]) {
+template <int TH>
+__device__ __forceinline__ void block_box(const int *b, bool valid, TileBox &box, int (*s_red)[6], int cap) {
     int v[6];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -1108,7 +1120,7 @@ __device__ __forceinline__ void block_box(const int *b, bool valid, TileBox &box
     int r[6];
 #pragma unroll
     for (int a = 0; a < 6; ++a) r[a] = INT_MAX;
-    for (int ww = 0; ww < kTileThreads / 32; ++ww)
+    for (int ww = 0; ww < TH / 32; ++ww)
 #pragma unroll
         for (int a = 0; a < 6; ++a) r[a] = min(r[a], s_red[ww][a]);
     __syncthreads();
@@ -1121,7 +1133,7 @@ __device__ __forceinline__ void block_box(const int *b, bool valid, TileBox &box
         vol *= (long long)box.e[a];
     }
     box.vol = any ? (int)min(vol, (long long)INT_MAX) : 0;
-    box.fits = any && vol <= kGatherCap;
+    box.fits = any && vol <= cap;
 }
 
 // quadratic B-spline weight and its derivative for node offset o of one axis
@@ -1137,8 +1149,11 @@ __device__ __forceinline__ void bspline_o(float fx, int o, float &w, float &dw) 
 // (base cell, particle tag) so each run deposits under one mask, its blocked nodes
 // becoming the owner lane's reaction.
 template <bool SOLIDS, int MINB, bool CDF = false>
-__global__ void __launch_bounds__(kTileThreads, MINB * 256 / kTileThreads) k_particles_tiled(PK k, int mode) {
-    __shared__ __align__(16) float s_mem[kSmemFloats];
+__global__ void __launch_bounds__(Tile<CDF>::threads, MINB * 256 / Tile<CDF>::threads)
+    k_particles_tiled(PK k, int mode) {
+    constexpr int kTileThreads = Tile<CDF>::threads;
+    constexpr int kGatherCap = Tile<CDF>::gather_cap;
+    __shared__ __align__(16) float s_mem[Tile<CDF>::smem_floats];
     __shared__ int s_key[kTileThreads];
     __shared__ int s_pc[CDF ? kTileThreads : 1];
     __shared__ int s_mask[CDF ? kTileThreads : 1];
@@ -1209,7 +1224,7 @@ __global__ void __launch_bounds__(kTileThreads, MINB * 256 / kTileThreads) k_par
             }
         }
         TileBox box;
-        block_box(s.b, want, box, s_red);
+        block_box<kTileThreads>(s.b, want, box, s_red, kGatherCap);
         pdl_wait();   // the grid velocities come from the grid pass before this one
         pdl_trigger();
         if ((mode & PASS_RESET_LISTS) && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -2514,26 +2529,28 @@ void launch_pdl(gbmpm_engine *e, void (*kern)(P...), int grid, int block, cudaSt
 
 void launch_particles(gbmpm_engine *e, const PK &k, int mode, bool tiled, cudaStream_t s) {
     if (tiled && k.cdf_on) {
-        int grid = std::max(1, (k.n + kTileThreads - 1) / kTileThreads);
+        constexpr int th = Tile<true>::threads;
+        int grid = std::max(1, (k.n + th - 1) / th);
         const bool solids = has_solids(e->M);
         if (e->cdf_occ >= 3) {
-            if (solids) launch_pdl(e, k_particles_tiled<true, 3, true>, grid, kTileThreads, s, k, mode);
-            else launch_pdl(e, k_particles_tiled<false, 3, true>, grid, kTileThreads, s, k, mode);
+            if (solids) launch_pdl(e, k_particles_tiled<true, 3, true>, grid, th, s, k, mode);
+            else launch_pdl(e, k_particles_tiled<false, 3, true>, grid, th, s, k, mode);
         } else {
-            if (solids) launch_pdl(e, k_particles_tiled<true, 2, true>, grid, kTileThreads, s, k, mode);
-            else launch_pdl(e, k_particles_tiled<false, 2, true>, grid, kTileThreads, s, k, mode);
+            if (solids) launch_pdl(e, k_particles_tiled<true, 2, true>, grid, th, s, k, mode);
+            else launch_pdl(e, k_particles_tiled<false, 2, true>, grid, th, s, k, mode);
         }
         e->launches++;
         return;
     }
     if (tiled) {
-        int grid = std::max(1, (k.n + kTileThreads - 1) / kTileThreads);
+        constexpr int th = Tile<false>::threads;
+        int grid = std::max(1, (k.n + th - 1) / th);
         const bool solids = has_solids(e->M);
-        if (solids && e->tile_occ >= 3) launch_pdl(e, k_particles_tiled<true, 3>, grid, kTileThreads, s, k, mode);
-        else if (solids) launch_pdl(e, k_particles_tiled<true, 2>, grid, kTileThreads, s, k, mode);
-        else if (e->tile_occ >= 4) launch_pdl(e, k_particles_tiled<false, 4>, grid, kTileThreads, s, k, mode);
-        else if (e->tile_occ == 3) launch_pdl(e, k_particles_tiled<false, 3>, grid, kTileThreads, s, k, mode);
-        else launch_pdl(e, k_particles_tiled<false, 2>, grid, kTileThreads, s, k, mode);
+        if (solids && e->tile_occ >= 3) launch_pdl(e, k_particles_tiled<true, 3>, grid, th, s, k, mode);
+        else if (solids) launch_pdl(e, k_particles_tiled<true, 2>, grid, th, s, k, mode);
+        else if (e->tile_occ >= 4) launch_pdl(e, k_particles_tiled<false, 4>, grid, th, s, k, mode);
+        else if (e->tile_occ == 3) launch_pdl(e, k_particles_tiled<false, 3>, grid, th, s, k, mode);
+        else launch_pdl(e, k_particles_tiled<false, 2>, grid, th, s, k, mode);
     } else {
         int grid = std::max(1, (k.n + kParticleThreads - 1) / kParticleThreads);
         if (has_solids(e->M)) k_particles<true><<<grid, kParticleThreads, 0, s>>>(k, mode);
@@ -3473,7 +3490,7 @@ int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32
     if (cdf) {
         int rc = check_ready(e);
         if (rc) return rc;
-        const size_t ctas = (size_t)std::max(1, (e->P.n + kParticleThreads - 1) / kParticleThreads);
+        const size_t ctas = (size_t)std::max(1, (e->P.n + kCdfCtaThreads - 1) / kCdfCtaThreads);
         if (e->c_partial_ctas < ctas) {
             GB_CUDA(cudaStreamSynchronize(s));
             if (e->c_partial_ctas) fold_cdf_wrench(e, s);
