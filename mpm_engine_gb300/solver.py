@@ -1150,6 +1150,10 @@ class Solver:
         """Stream-ordered copy of the positions into a caller (pinned host) tensor."""
         out.copy_(self._t["x"], non_blocking=True)
 
+    def v_into(self, out) -> None:
+        """Stream-ordered copy of the velocities into a caller (pinned host) tensor."""
+        out.copy_(self._t["v"], non_blocking=True)
+
     # ---------------------------------------------------------------- exports
     def x(self) -> np.ndarray:
         return self._t["x"].cpu().numpy()
