@@ -161,6 +161,11 @@ __device__ __forceinline__ void cp_async4(float *dst, const float *src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// 16-byte asynchronous global -> shared copy (both addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(src) : "memory");
+}
 
 // Particle fields are either the caller's records (AoS: W floats per particle)
 // or the engine's working copy (SoA: component c of particle p at c*n + p, so a
@@ -1243,11 +1248,16 @@ __global__ void __launch_bounds__(Tile<CDF>::threads, MINB * 256 / Tile<CDF>::th
             }
         };
         if (box.fits) {
-            const int e12 = box.e[1] * box.e[2];
-            for (int q = t; q < box.vol; q += kTileThreads) {
-                int qx = q / e12, r = q - qx * e12, qy = r / box.e[2], qz = r - qy * box.e[2];
-                s_tile[q] = __ldg(k.gv + ((size_t)(box.lo[0] + qx) * k.ng + (box.lo[1] + qy)) * k.ng + (box.lo[2] + qz));
+            // one thread per (x, y) row of the box: the row's nodes are contiguous in
+            // the grid and in the tile, and all its 16-byte copies are in flight at once
+            const int rows = box.e[0] * box.e[1];
+            for (int r = t; r < rows; r += kTileThreads) {
+                const int qx = r / box.e[1], qy = r - qx * box.e[1];
+                const float4 *src = k.gv + ((size_t)(box.lo[0] + qx) * k.ng + (box.lo[1] + qy)) * k.ng + box.lo[2];
+                float4 *dst = s_tile + r * box.e[2];
+                for (int qz = 0; qz < box.e[2]; ++qz) cp_async16(dst + qz, src + qz);
             }
+            cp_async_wait_all();
             __syncthreads();
             if (want) {
                 const int o0 = s.b[0] - box.lo[0], o1 = s.b[1] - box.lo[1], o2 = s.b[2] - box.lo[2];
