@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["pour", "pour_hb", "pour_cdf", "dam"], default="pour")
+    ap.add_argument("--workload", choices=["pour", "pour_hb", "pour_cdf", "dam", "press"], default="pour")
     ap.add_argument("--n-grid", type=int, default=192)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-cdf", action="store_true")
     ap.add_argument("--no-flood", action="store_true")
+    ap.add_argument("--no-press", action="store_true")
     return ap.parse_args()
 
 
@@ -159,6 +160,18 @@ def build_workload(name: str, n_grid: int, solver_cls, **kw):
             s.step(dt, S)
 
         desc = {"workload": f"dam_break_{n_grid}^3", "particles": s.n_particles, "substeps_per_step": S, "dt": dt,
+                "grid_lim": 1.0}
+        return s, frame, s.n_particles, S, desc
+    if name == "press":
+        # the granular press as the main workload: one step = one 20-substep tick
+        from mpm_engine_gb300.scenes import press_scene
+        s, plate, center, half, dt = press_scene(solver_cls, n_grid=n_grid, **kw)
+        S = 20
+
+        def frame(i, s=s):
+            s.step(dt, S)
+
+        desc = {"workload": f"press_mu_i_{n_grid}^3", "particles": s.n_particles, "substeps_per_step": S, "dt": dt,
                 "grid_lim": 1.0}
         return s, frame, s.n_particles, S, desc
     raise SystemExit(f"unknown workload {name}")
@@ -340,6 +353,97 @@ def dist_setup(args):
     return world, rank, local
 
 
+def fp32_sgemm_tflops(device: str = "cuda:0", n: int = 8192, reps: int = 5) -> float:
+    """FP32 issue ceiling measured on this GPU: cuBLAS SGEMM with TF32 off (CUDA-core
+    FMAs), n^3 x 2 FLOP per product, best of `reps` after one warm-up."""
+    import torch
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        a = torch.randn(n, n, device=device)
+        b = torch.randn(n, n, device=device)
+        torch.mm(a, b)
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.mm(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        return 2.0 * n ** 3 / (best / 1e3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def captured_value(name: str, key: str):
+    """A `key: value` line of a committed ncu summary under profiles/, or None."""
+    f = REPO / "profiles" / name
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith(key + ":"):
+            return float(line.split(":", 1)[1])
+    return None
+
+
+def press_measure(n_grid: int = 256, ticks: int = 100, substeps: int = 20, device: str = "cuda:0"):
+    """The granular press: a seeded random-height heap of mu(I) grains (about 2 M
+    particles at 256^3) pressed by a plate at 0.1 m/s, sparse blocks, a particle sort
+    every 8 ticks, `ticks` ticks of `substeps` substeps (2000 in all). After every
+    tick the plate's stress-integral contact wrench (box_contact_wrench,
+    coupling/wrench.py:15-46) is reduced on the device and read back, as the
+    reference's press loop records it. Sparse mode runs the split passes, as in the
+    reference. The substep is graded against both ceilings. HBM: N x 212 B (x, v, C and
+    F read and written, mass, volume, mu, lambda and yield) plus 56 B per active node.
+    FP32: N x the FLOPs per particle-substep that ncu counted over the three
+    particle passes, against a cuBLAS SGEMM with TF32 off."""
+    import torch
+    from mpm_engine_gb300 import Solver
+    from mpm_engine_gb300.scenes import press_scene
+    s, plate, center, half, dt = press_scene(Solver, n_grid=n_grid, device=device)
+    n = s.n_particles
+    vz = -0.1
+    t = 0.0
+
+    def tick():
+        nonlocal t
+        s.step(dt, substeps)
+        t += dt * substeps
+        c = (center[0], center[1], center[2] + vz * t)
+        return s.contact_wrench(c, half, layer_cells=2.0, dx=s.grid.dx)
+
+    for _ in range(2):
+        tick()
+    torch.cuda.synchronize()
+    fz = []
+    t0 = time.perf_counter()
+    for _ in range(ticks):
+        fz.append(float(tick()["Fz"]))
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    us_substep = el / (ticks * substeps) * 1e6
+    active_nodes = int(s._sim._block_counts[0]) * 64
+    bytes_substep = n * 212.0 + active_nodes * 56.0
+    hbm_peak, _ = peaks()
+    hbm = bytes_substep / (us_substep / 1e6) / 1e9
+    flops_p = captured_value("particle_passes_press_mu_i_256.txt", "fp32_flops_per_particle_substep")
+    fp32_peak = fp32_sgemm_tflops(device)
+    fp32 = None if flops_p is None else n * flops_p / (us_substep / 1e6) / 1e12
+    rl = {"hbm": {"achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak,
+                  "bytes_per_substep": bytes_substep, "active_nodes": active_nodes},
+          "fp32": {"achieved": fp32, "peak": fp32_peak, "unit": "TFLOP/s",
+                   "frac": None if fp32 is None else fp32 / fp32_peak, "flops_per_particle_substep": flops_p,
+                   "peak_kind": "measured: cuBLAS SGEMM, TF32 off"}}
+    fr = [v["frac"] for v in rl.values() if v["frac"] is not None]
+    rl["binding"] = max((k for k in ("hbm", "fp32") if rl[k]["frac"] is not None), key=lambda k: rl[k]["frac"])
+    return {"workload": f"press_mu_i_{n_grid}^3", "particles": n, "substeps": ticks * substeps, "dt": dt,
+            "us_per_substep": us_substep, "particle_substeps_per_s": n * ticks * substeps / el,
+            "plate_Fz_last_N": fz[-1], "roofline": rl, "pipeline": "split (sparse)", "max_frac": max(fr)}
+
+
 def captured_traffic(workload: str):
     """DRAM bytes per launch of the fused particle kernel from the committed ncu
     summary of this workload (profiles/k_particles_tiled_<workload>.txt), or None."""
@@ -454,7 +558,17 @@ def main():
     torch.cuda.synchronize()
     launches = s.launch_count() - launches0
     clk = clocks.stop()
-    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    frame_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(frame_ms)
+    phases_of_pour = None
+    if args.workload.startswith("pour"):
+        # the source glass stands upright until t = 0.1 s (frame 6), then tilts
+        idx = [args.warmup + k for k in range(args.steps)]
+        up = [m for i, m in zip(idx, frame_ms) if i / 60.0 < 0.1]
+        tilt = [m for i, m in zip(idx, frame_ms) if i / 60.0 >= 0.1]
+        phases_of_pour = {"upright_ms_per_frame": sum(up) / len(up) if up else None,
+                          "tilting_ms_per_frame": sum(tilt) / len(tilt) if tilt else None,
+                          "frames": [idx[0], idx[-1]]}
     value, total_ms = replica_value(total_ms, n * S, args.steps, world, dist, device=f"cuda:{local}")
     ms_per_step = total_ms / args.steps
 
@@ -470,11 +584,13 @@ def main():
     fused_ms = msv[2] / max(cnt[2], 1)
     grid_ms = msv[3] / max(cnt[3], 1)
     peak, peak_kind = peaks()
-    achieved = n * BYTES_PER_PARTICLE_SUBSTEP / (fused_ms / 1e3) / 1e9
+    # split-pipeline workloads (the sparse press) have no fused pass to grade here
+    achieved = n * BYTES_PER_PARTICLE_SUBSTEP / (fused_ms / 1e3) / 1e9 if fused_ms > 0 else None
     phases = {s._eng.lib.gbmpm_phase_name(i).decode(): round(msv[i] / max(cnt[i], 1), 5)
               for i in range(6) if cnt[i]}
     traffic = captured_traffic(desc["workload"])
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved is not None else None,
                 "traffic": traffic, "traffic_unit": "bytes per launch (ncu dram read + write, cold cache)",
                 "algorithmic_bytes_per_launch": n * BYTES_PER_PARTICLE_SUBSTEP,
                 "kernel": "k_particles_tiled (fused G2P2G)", "kernel_ms": fused_ms,
@@ -528,6 +644,10 @@ def main():
     if not args.no_flood and args.workload == "pour":
         flood = flood_measure(device=f"cuda:{local}")
 
+    press = None
+    if not args.no_press and args.workload == "pour":
+        press = press_measure(device=f"cuda:{local}")
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(s.export_state(), desc, args.cpu_seconds)
@@ -539,8 +659,8 @@ def main():
                 "config": {**desc, "l2": "256 MB buffer written between timed steps", "parallelism":
                            "replicas" if world > 1 else "single"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk, "batched": batched, "batched_adjoint": adj, "pour_cdf": cdf,
-                "flood_vehicle": flood}
+                "clocks": clk, "pour_phases": phases_of_pour, "batched": batched, "batched_adjoint": adj,
+                "pour_cdf": cdf, "flood_vehicle": flood, "press": press}
         print(json.dumps(line))
     if dist:
         dist.barrier()

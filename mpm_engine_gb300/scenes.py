@@ -111,6 +111,63 @@ def pour_scene(solver_cls, n_grid: int = 192, material=None, glass: str = "cup",
     return s, src, rcv, traj, substeps, (1.0 / 60.0) / substeps
 
 
+# ---- granular press: a seeded random-height heap of mu(I) grains under a plate ----------
+PRESS_GRANULAR = dict(mu_s=0.38, delta_mu=0.26, I0=0.28, density=2500.0, E=1.0e6, nu=0.3)
+
+
+def press_heap(n_grid: int = 256, grid_lim: float = 1.0, seed: int = 0):
+    """Heap of grains at 8 particles per cell (spacing dx/2, +-h/4 seeded jitter) over
+    the square footprint [0.25, 0.75]^2 x grid_lim, standing on the floor 3 cells up.
+    Its height at (x, y) is 0.06 grid_lim plus a seeded smooth field of amplitude
+    0.025 grid_lim (six random plane waves), so the plate meets the peaks first. At
+    256^3 on the unit cube this is about 2.0 M particles. Returns (pos, vol, floor_z)."""
+    dx = grid_lim / n_grid
+    h = 0.5 * dx
+    floor = 3 * dx
+    rng = np.random.default_rng(seed)
+    k = rng.uniform(1.0, 4.0, (6, 2)) * (2.0 * np.pi / (0.5 * grid_lim)) * rng.choice([-1.0, 1.0], (6, 2))
+    phase = rng.uniform(0.0, 2.0 * np.pi, 6)
+    ax = np.arange(0.25 * grid_lim + 0.5 * h, 0.75 * grid_lim, h)
+    X, Y = np.meshgrid(ax, ax, indexing="ij")
+    field = sum(np.cos(k[i, 0] * X + k[i, 1] * Y + phase[i]) for i in range(6)) / np.sqrt(6.0)
+    height = grid_lim * (0.06 + 0.025 * np.clip(field, -1.5, 1.5) / 1.5)
+    layers = np.floor(height / h).astype(np.int64)
+    reps = layers.reshape(-1)
+    xy = np.repeat(np.stack([X.reshape(-1), Y.reshape(-1)], -1), reps, axis=0)
+    z = floor + 0.5 * h + h * (np.arange(reps.sum()) - np.repeat(np.cumsum(reps) - reps, reps))
+    pts = np.concatenate([xy, z[:, None]], axis=1)
+    pts = pts + rng.uniform(-0.25 * h, 0.25 * h, size=pts.shape)
+    pos = pts.astype(np.float32)
+    return pos, np.full(len(pos), h ** 3, dtype=np.float32), floor
+
+
+def press_scene(solver_cls, n_grid: int = 256, grid_lim: float = 1.0, plate_speed: float = 0.1, seed: int = 0,
+                **solver_kw):
+    """The granular press: `press_heap` of mu(I) grains (mu_s 0.38, delta_mu 0.26,
+    I0 0.28, rho 2500, E 1e6, nu 0.3) on a sticky floor inside domain walls, pressed
+    by a kinematic plate (half size 0.2 x 0.2 x 2 dx) descending at `plate_speed`
+    from just above the highest grain. Runs with sparse blocks and a particle sort
+    every 8 ticks. dt is the elastic CFL bound 0.3 dx / c_p. Returns (solver, plate
+    handle, plate centre at t = 0, plate half size, dt)."""
+    from .materials import granular
+    from .solver import GridConfig
+    grid = GridConfig(n_grid=n_grid, grid_lim=grid_lim)
+    pos, vol, floor = press_heap(n_grid, grid_lim, seed)
+    kw = dict(sparse=True, sort_interval=8)
+    kw.update(solver_kw)
+    s = solver_cls(grid=grid, **kw).load_particles(pos, vol)
+    s.set_material(granular(**PRESS_GRANULAR))
+    s.add_plane((0, 0, floor), (0, 0, 1), "sticky")
+    s.add_domain_walls()
+    dx = grid.dx
+    center = (0.5 * grid_lim, 0.5 * grid_lim, float(pos[:, 2].max()) + 3 * dx)
+    half = (0.2 * grid_lim, 0.2 * grid_lim, 2 * dx)
+    plate = s.add_box(center, half, velocity=(0.0, 0.0, -plate_speed))
+    E, nu, rho = PRESS_GRANULAR["E"], PRESS_GRANULAR["nu"], PRESS_GRANULAR["density"]
+    c_p = float(np.sqrt(E * (1 - nu) / ((1 + nu) * (1 - 2 * nu)) / rho))
+    return s, plate, center, half, 0.3 * dx / c_p
+
+
 # ---- batched dough-squeeze scenes ---------------------------------------------------
 def squeeze_scene(solver_cls, n_particles: int, n_grid: int, material, grid_lim: float = 0.3,
                   plate_speed: float = 0.05, seed: int = 0, **solver_kw):
@@ -165,5 +222,5 @@ def squeeze_from_spec(solver_cls, spec: dict, **solver_kw):
     return squeeze_scene(solver_cls, spec["n_particles"], spec["n_grid"], mat, seed=spec["seed"], **solver_kw)
 
 
-__all__ = ["HONEY", "PourTrajectory", "block", "dam_break_lattice", "dough", "pour_scene", "pour_substeps",
-           "squeeze_batch_specs", "squeeze_from_spec", "squeeze_scene"]
+__all__ = ["HONEY", "PRESS_GRANULAR", "PourTrajectory", "block", "dam_break_lattice", "dough", "pour_scene",
+           "pour_substeps", "press_heap", "press_scene", "squeeze_batch_specs", "squeeze_from_spec", "squeeze_scene"]
