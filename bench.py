@@ -518,9 +518,20 @@ def cpu_baseline(st, desc, seconds: float):
     o.step(desc["dt"], m)
     el = time.perf_counter() - t0
     n = len(st["x"])
+    # one thread as well: Warp's CPU kernels run single-threaded, so this is the
+    # closer analogue of the reference's own CPU path (about a quarter of the time)
+    o.threads = 1
+    t0 = time.perf_counter()
+    o.step(desc["dt"], 1)
+    per1 = time.perf_counter() - t0
+    m1 = max(1, int(0.25 * seconds / max(per1, 1e-6)))
+    t0 = time.perf_counter()
+    o.step(desc["dt"], m1)
+    el1 = time.perf_counter() - t0
     return {"value": n * m / el, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{m} substeps of the {desc['workload']} frame state after warm-up "
-                      f"({n} particles; CPU restatement of the reference step, not Warp)"}
+                      f"({n} particles; CPU restatement of the reference step, not Warp)",
+            "single_thread": {"value": n * m1 / el1, "cores": 1, "sample": f"{m1} further substeps"}}
 
 
 def main():
