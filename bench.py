@@ -177,22 +177,28 @@ def build_workload(name: str, n_grid: int, solver_cls, **kw):
     raise SystemExit(f"unknown workload {name}")
 
 
-def batched_measure(n_scenes: int, ticks: int, substeps: int = 100, dt: float = 1.0e-5, device: str = "cuda:0"):
+def batched_measure(n_scenes: int, ticks: int, substeps: int = 100, dt: float = 1.0e-5, device: str = "cuda:0",
+                    rank: int = 0, world: int = 1):
     """Batched forward workload: n_scenes seeded dough-squeeze scenes (8k..120k
     particles, 48^3..128^3 grids, per-scene E, nu, yield, von Mises or elastic,
     plate at 0.05 m/s). One scene-tick = `substeps` substeps of one scene. The plain
     path steps the Solvers one after another (the reference's serial rollouts); the
-    batched path advances all scenes in one CUDA graph."""
+    batched path advances all scenes in one CUDA graph. With several ranks the
+    scenes are sharded whole (sharding.partition, balanced by particle count): each
+    rank builds and steps only its share, and the rates are every rank's
+    scene-ticks over the slowest rank's time."""
     import torch
-    from mpm_engine_gb300 import BatchSolver, Solver
+    from mpm_engine_gb300 import Solver
     from mpm_engine_gb300.scenes import squeeze_batch_specs, squeeze_from_spec
+    from mpm_engine_gb300.sharding import ShardedBatch, sharded_throughput
     specs = squeeze_batch_specs(n_scenes)
-    scenes = [squeeze_from_spec(Solver, sp, device=device)[0] for sp in specs]
-    n_part = sum(sc.n_particles for sc in scenes)
-    batch = BatchSolver(scenes)
+    shard = ShardedBatch(lambda i: squeeze_from_spec(Solver, specs[i], device=device)[0],
+                         [sp["n_particles"] for sp in specs], rank, world)
+    scenes, batch = shard.scenes, shard.batch
+    n_local = len(scenes)
     for sc in scenes:                      # warm-up: capture each scene's own graph
         sc.step(dt, substeps)
-    batch.step(dt, substeps)               # warm-up: capture the batch graph
+    shard.step(dt, substeps)               # warm-up: capture the batch graph
     torch.cuda.synchronize()
 
     def timed(fn):
@@ -203,15 +209,19 @@ def batched_measure(n_scenes: int, ticks: int, substeps: int = 100, dt: float = 
         return time.perf_counter() - t0
 
     t_plain = timed(lambda: [sc.step(dt, substeps) for sc in scenes])
-    launches0 = batch.launch_count()
-    t_batch = timed(lambda: batch.step(dt, substeps))
-    rate_b = n_scenes * ticks / t_batch
-    rate_p = n_scenes * ticks / t_plain
+    launches0 = batch.launch_count() if batch else 0
+    t_batch = timed(lambda: shard.step(dt, substeps))
+    launches = (batch.launch_count() if batch else 0) - launches0
+    red = "cuda" if world > 1 and torch.distributed.get_backend() == "nccl" else "cpu"
+    rate_b, _, _ = sharded_throughput(n_local * ticks, t_batch, device=red)
+    rate_p, _, _ = sharded_throughput(n_local * ticks, t_plain, device=red)
+    rate_pp, n_part, _ = sharded_throughput(shard.particles() * substeps * ticks, t_batch, device=red)
+    n_part /= substeps * ticks
     return {"metric": "batched forward scene-ticks/s", "unit": f"scene-ticks/s ({substeps} substeps each)",
             "value": rate_b, "plain_value": rate_p, "speedup_vs_plain": rate_b / rate_p,
-            "scenes": n_scenes, "particles_total": n_part, "ticks": ticks, "dt": dt,
-            "particle_substeps_per_s": n_part * substeps * ticks / t_batch,
-            "gpu_launches": batch.launch_count() - launches0}
+            "scenes": n_scenes, "particles_total": int(n_part), "ticks": ticks, "dt": dt,
+            "particle_substeps_per_s": rate_pp, "gpu_launches": launches,
+            "sharding": {"ranks": world, "scenes_on_rank0": n_local} if world > 1 else None}
 
 
 def cdf_pour_measure(n_grid: int = 192, frames: int = 4, warmup: int = 24, device: str = "cuda:0"):
@@ -641,7 +651,8 @@ def main():
 
     batched = None
     if not args.no_batched:
-        batched = batched_measure(args.batch_scenes, ticks=max(2, min(args.steps, 4)), device=f"cuda:{local}")
+        batched = batched_measure(args.batch_scenes, ticks=max(2, min(args.steps, 4)), device=f"cuda:{local}",
+                                  rank=rank, world=world)
 
     cdf = None
     if not args.no_cdf and args.workload == "pour":
