@@ -350,7 +350,8 @@ __device__ __forceinline__ void stress_update(const PK &k, int p, int mat, const
                         y = y - T.softening[mat] * sqrtf(rh0 * rh0 + rh1 * rh1 + rh2 * rh2);
                         if (y <= 0.0f) { mu = 0.0f; lam = 0.0f; k.mu[p] = 0.0f; k.lam[p] = 0.0f; }
                     }
-                    udvt(U, expf(e0), expf(e1), expf(e2), V, F);
+                    sig[0] = expf(e0); sig[1] = expf(e1); sig[2] = expf(e2);
+                    udvt(U, sig[0], sig[1], sig[2], V, F);
                     if (T.hardening[mat] > 0.5f) y = y + 2.0f * mu * T.xi[mat] * dg;
                     k.ys[p] = y;
                     done = true;
@@ -372,10 +373,12 @@ __device__ __forceinline__ void stress_update(const PK &k, int p, int mat, const
 #pragma unroll
                 for (int i = 0; i < 9; ++i) F[i] = Ft[i];
             } else if (tr > 0.0f) {
+                sig[0] = sig[1] = sig[2] = 1.0f;
                 udvt(U, 1.0f, 1.0f, 1.0f, V, F);
             } else {
                 float r = dg / hn;
-                udvt(U, expf(e0 - h0 * r), expf(e1 - h1 * r), expf(e2 - h2 * r), V, F);
+                sig[0] = expf(e0 - h0 * r); sig[1] = expf(e1 - h1 * r); sig[2] = expf(e2 - h2 * r);
+                udvt(U, sig[0], sig[1], sig[2], V, F);
             }
         } else if (mat == 9 || mat == 13 || mat == 11) {  // mu(I) family (mpm_utils.py:246-522)
             svd3(Ft, U, sig, V);
@@ -390,6 +393,7 @@ __device__ __forceinline__ void stress_update(const PK &k, int p, int mat, const
             for (int i = 0; i < 9; ++i) F[i] = Ft[i];
             if (mat != 11) {
                 if (tr >= 0.0f) {
+                    sig[0] = sig[1] = sig[2] = 1.0f;
                     udvt(U, 1.0f, 1.0f, 1.0f, V, F);
                 } else {
                     float pK = -(2.0f * mu / 3.0f + lam) * tr;
@@ -402,7 +406,8 @@ __device__ __forceinline__ void stress_update(const PK &k, int p, int mat, const
                                                 : mu_i_bisect<false>(tbK, mu, k.dt, pK, Ic, T.mu_s[mat], T.dmu[mat],
                                                                      T.I0[mat], k);
                         float sc = (tbK - mu * k.dt * gdp) / fmaxf(tbK, 1e-20f);
-                        udvt(U, expf(d0 * sc + mean), expf(d1 * sc + mean), expf(d2 * sc + mean), V, F);
+                        sig[0] = expf(d0 * sc + mean); sig[1] = expf(d1 * sc + mean); sig[2] = expf(d2 * sc + mean);
+                        udvt(U, sig[0], sig[1], sig[2], V, F);
                     }
                 }
             } else {
@@ -413,6 +418,7 @@ __device__ __forceinline__ void stress_update(const PK &k, int p, int mat, const
                 float jp_new = Jr;
                 if (pc <= 0.0f) {
                     float si = expf(mean);
+                    sig[0] = sig[1] = sig[2] = si;
                     udvt(U, si, si, si, V, F);
                 } else {
                     float pK = pc * J;
@@ -425,7 +431,8 @@ __device__ __forceinline__ void stress_update(const PK &k, int p, int mat, const
                         float jcs = 1.0f / fmaxf(1.0f - T.phi_chi[mat] * Ir / (Ir + T.I0[mat]), 1e-3f);
                         jp_new = Jr + dgam * (jcs - Jr);
                         float sc = (tbK - mu * k.dt * gdp) / fmaxf(tbK, 1e-20f);
-                        udvt(U, expf(d0 * sc + mean), expf(d1 * sc + mean), expf(d2 * sc + mean), V, F);
+                        sig[0] = expf(d0 * sc + mean); sig[1] = expf(d1 * sc + mean); sig[2] = expf(d2 * sc + mean);
+                        udvt(U, sig[0], sig[1], sig[2], V, F);
                     }
                 }
                 k.Jp[p] = jp_new;
@@ -434,9 +441,13 @@ __device__ __forceinline__ void stress_update(const PK &k, int p, int mat, const
 #pragma unroll
             for (int i = 0; i < 9; ++i) F[i] = Ft[i];
         }
-        // ---- stress of the returned F
+        // ---- stress of the returned F. Every return map above leaves (U, sig, V) a
+        // singular value decomposition of the F it returns: F_trial's own when it
+        // returns F_trial (bit for bit what a second svd3 gives), else U diag(sig) V^T
+        // with the projected values, whose descending order the projections keep. So
+        // only the maps without an SVD of their own (FCR jelly) factor F here.
         float J = det3(F);
-        svd3(F, U, sig, V);
+        if (!(mat == 1 || mat == 5 || mat == 2 || mat == 9 || mat == 13 || mat == 11)) svd3(F, U, sig, V);
         if (mat == 0 || mat == 5) {  // FCR (mpm_utils.py:8-15)
             float R[9], FR[9];
             mmT(U, V, R);
