@@ -1433,7 +1433,7 @@ __global__ void __launch_bounds__(Tile<CDF>::threads, MINB * 256 / Tile<CDF>::th
         float acc[3][4];
 #pragma unroll
         for (int kk = 0; kk < 3; ++kk) acc[kk][0] = acc[kk][1] = acc[kk][2] = acc[kk][3] = 0.f;
-#pragma unroll 2
+#pragma unroll 1   // unrolling by two measured slower (22.01 against 21.87 ms per pour frame, 56.5 against 54.9 CPIC)
         for (int q = q0; q < q1; ++q) {
             const float *r = s_mem + q * kRecStride;
             const float wxi = r[li], wyj = r[3 + lj], dwxi = r[6 + li], dwyj = r[9 + lj];
