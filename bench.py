@@ -16,6 +16,18 @@ all host threads, a bounded sample of the same frame per step.
 Under torchrun (N > 1) every rank runs an independent replica of the scene on its
 own GPU (the path has no cross-GPU exchange); value sums all ranks' work over the
 slowest rank's time.
+
+Beside the headline the line carries:
+- `roofline`: the fused particle pass against the measured HBM copy;
+- `e2e`: the same frames through the public API with host inputs and outputs;
+- `cpu_baseline`: the oracle on all host cores and on one thread;
+- `pour_phases`: the upright and the tilting frames;
+- `batched` and `batched_adjoint`: many scenes in one graph, sharded whole
+  across ranks;
+- `pour_cdf`: the pour with CPIC glasses;
+- `flood_vehicle`: rigid-body coupling;
+- `press`: the granular press, graded against FP32 and HBM.
+Each can be switched off with its --no-* flag.
 """
 from __future__ import annotations
 
