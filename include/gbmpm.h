@@ -229,6 +229,11 @@ int gbmpm_cdf_restamp(gbmpm_engine *e, double time, void *stream);
 /* on != 0: restamp every lane at every substep instead of only the lanes that moved
  * or changed activity (the _cdf_force_stamp switch, :3046-3052). */
 int gbmpm_cdf_force_stamp(gbmpm_engine *e, int32_t on);
+/* off != 0: every particle scans its 27 stencil nodes for CPIC tags instead of
+ * skipping stencils that touch no tagged 4^3 block (model.cdf_mask_off,
+ * kernels/warp_utils.py:84, read at kernels/mpm_utils.py:856, 980). The skip is
+ * exact, so results do not change. */
+int gbmpm_cdf_mask_off(gbmpm_engine *e, int32_t off);
 /* 1 when a captured tick graph is ready for replay. */
 int32_t gbmpm_graph_state(gbmpm_engine *e);
 

@@ -180,6 +180,7 @@ _SIGNATURES = {
     "gbmpm_batch_launch_count": (C.c_int64, [C.c_void_p]),
     "gbmpm_cdf_restamp": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p]),
     "gbmpm_cdf_force_stamp": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gbmpm_cdf_mask_off": (C.c_int, [C.c_void_p, C.c_int32]),
     "gbmpm_graph_state": (C.c_int32, [C.c_void_p]),
     "gbmpm_set_rigid": (C.c_int, [C.c_void_p, C.POINTER(RigidBody), C.c_int32, C.POINTER(RigidSurface), C.c_int32]),
     "gbmpm_get_rigid": (C.c_int, [C.c_void_p, C.POINTER(RigidBody), C.c_int32, C.c_void_p]),

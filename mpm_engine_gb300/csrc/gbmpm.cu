@@ -747,7 +747,10 @@ __device__ __forceinline__ size_t node_id(const PK &k, const Stencil &s, int i, 
 }
 
 // cdf_stencil_near: a 4^3 block under the stencil holds tags now or at the last stamp
+// k.cblock is null when the early-out is switched off (model.cdf_mask_off,
+// mpm_utils.py:856, 980): every particle then takes the full 27-node scan
 __device__ __forceinline__ bool cdf_near(const PK &k, const Stencil &s) {
+    if (!k.cblock) return true;
     for (int bi = s.b[0] >> 2; bi <= (s.b[0] + 2) >> 2; ++bi)
         for (int bj = s.b[1] >> 2; bj <= (s.b[1] + 2) >> 2; ++bj)
             for (int bk = s.b[2] >> 2; bk <= (s.b[2] + 2) >> 2; ++bk)
@@ -2370,6 +2373,7 @@ struct CdfHost {
     int stale_box[6] = {};
     bool lane_prev_stale = false;
     bool force = false;         // restamp every lane every substep (no dirty-lane skip)
+    bool mask_off = false;      // scan every particle's stencil, no block-mask early-out
     int64_t stamps = 0;
     void sync_lane(int l) {    // _sync_cdf_lane (mpm_solver_warp.py:2883-2905)
         for (int a = 0; a < 3; ++a) {
@@ -2508,7 +2512,7 @@ PK make_pk(gbmpm_engine *e, const gbmpm_particles &P, float dt, int list) {
         const CdfHost &H = e->cdf;
         k.cdf_on = 1;
         k.cnb = (e->c_ng + 3) / 4;
-        k.ctag = e->c_tag.ptr; k.ctag_prev = e->c_tag_prev.ptr; k.cblock = e->c_block.ptr;
+        k.ctag = e->c_tag.ptr; k.ctag_prev = e->c_tag_prev.ptr; k.cblock = e->cdf.mask_off ? nullptr : e->c_block.ptr;
         k.cd = e->c_d.ptr; k.cd_prev = e->c_d_prev.ptr;
         k.ptag = P.cdf_tag;
         k.cwrench = e->c_partial.ptr;
@@ -3428,6 +3432,12 @@ int gbmpm_cdf_restamp(gbmpm_engine *e, double time, void *stream) {
 int gbmpm_cdf_force_stamp(gbmpm_engine *e, int32_t on) {
     if (!e) return fail(GBMPM_ERR_ARG, "null argument");
     e->cdf.force = on != 0;
+    return GBMPM_OK;
+}
+
+int gbmpm_cdf_mask_off(gbmpm_engine *e, int32_t off) {
+    if (!e) return fail(GBMPM_ERR_ARG, "null argument");
+    e->cdf.mask_off = off != 0;   // ticks with CDF lanes launch live, so the next launch sees it
     return GBMPM_OK;
 }
 

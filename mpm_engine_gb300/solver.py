@@ -148,7 +148,18 @@ class _ModelView:
     n_grid = property(lambda self: self._get("n_grid"))
     dx = property(lambda self: self._get("dx"))
     inv_dx = property(lambda self: self._get("inv_dx"))
-    cdf_mask_off = 0
+
+    @property
+    def cdf_mask_off(self) -> int:
+        """1: every particle scans its stencil for CPIC tags (no block-mask early-out)."""
+        return 1 if self._s._cdf_mask_off else 0
+
+    @cdf_mask_off.setter
+    def cdf_mask_off(self, v):
+        s = self._s
+        s._cdf_mask_off = bool(v)
+        if s._eng is not None:
+            _abi.check(s._eng.lib.gbmpm_cdf_mask_off(s._eng.h, 1 if v else 0), "gbmpm_cdf_mask_off")
 
 
 class _SimShim:
@@ -344,6 +355,7 @@ class Solver:
         self._n_bodies = 0
         self._mods: list = []          # particle modifier records, in registration order
         self._cdf_force = False
+        self._cdf_mask_off = False
         self._update_cov = False
 
     # ------------------------------------------------------------------ setup
@@ -414,6 +426,10 @@ class Solver:
         self._model.eta_table = t["eta_table"].data_ptr()
         self._eng = _Engine()
         self._bind()
+        if self._cdf_force:
+            _abi.check(self._eng.lib.gbmpm_cdf_force_stamp(self._eng.h, 1), "gbmpm_cdf_force_stamp")
+        if self._cdf_mask_off:
+            _abi.check(self._eng.lib.gbmpm_cdf_mask_off(self._eng.h, 1), "gbmpm_cdf_mask_off")
         self._model_dirty = True
         self._sim = _SimShim(self)
         return self

@@ -135,7 +135,7 @@ class Case:
         L = (x.double() * self.a).sum() + (v.double() * self.b).sum()
         if grad:
             L.backward()
-        return float(L)
+        return float(L.detach())
 
     def grads(self):
         import torch

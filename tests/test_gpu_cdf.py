@@ -207,3 +207,29 @@ def test_cdf_pour_holds_and_matches_oracle(cuda, oracle_lib):
     inside = r < prof.inner_radius - 2 * 0.7 / 96
     assert np.isfinite(x).all()
     assert (x[inside, 2] > prof.inner_floor_z - 1.5 * 0.7 / 96).all(), "honey leaked through the glass floor"
+
+
+@pytest.mark.parametrize("fused", [True, False])
+@pytest.mark.parametrize("moving", [False, True])
+def test_block_mask_skip_changes_nothing(cuda, fused, moving):
+    """The block-mask early-out of the CPIC scan (tests/test_cdf_mask.py:37-75): a
+    column on a sheet plus a blob far from any sheet, stepped with the early-out on
+    and with every particle scanning its stencil (model.cdf_mask_off = 1). The skip
+    is exact; two GPU runs agree to float-atomic rounding."""
+    from mpm_engine_gb300 import Solver
+    out = []
+    for off in (0, 1):
+        pos = np.concatenate([cdf_water(0.14, 0.26, 0.14, 0.26, 0.21, 0.27),
+                              cdf_water(0.06, 0.12, 0.06, 0.12, 0.08, 0.14)])
+        s = cdf_solver(Solver, pos, g=(0.0, 0.0, -9.81), fused=fused)
+        h = s.add_cdf_collider(sheet_cdf("z"), center=(0.2, 0.2, 0.20), friction=0.3)
+        s._sim.mpm_model.cdf_mask_off = off
+        assert s._sim.mpm_model.cdf_mask_off == off
+        if moving:
+            s.set_cdf_pose(h, velocity=(0.0, 0.0, 0.01))
+        for _ in range(8 if moving else 5):
+            s.step(DT, SUB)
+        out.append((s.x(), s.v()))
+    np.testing.assert_allclose(out[1][0], out[0][0], rtol=1e-5, atol=1e-6)
+    vs = float(np.abs(out[0][1]).max())
+    np.testing.assert_allclose(out[1][1], out[0][1], rtol=0, atol=1e-4 * vs + 1e-7)
