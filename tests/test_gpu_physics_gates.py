@@ -10,7 +10,10 @@ These tests pose the same scenes and apply the same acceptance bounds:
   (tests/test_tabulated_material.py:20-68);
 - sparse active blocks against the dense path (tests/test_sparse_blocks.py:20-73);
 - periodic-x transfers: a block crossing the wrap, and a mu(I) chute developing
-  the Bagnold profile (tests/test_periodic_chute.py:20-98).
+  the Bagnold profile (tests/test_periodic_chute.py:20-98);
+- a settled column's base pressure (tests/test_engine.py:109-131);
+- von Mises hardening evolving the yield stress
+  (tests/test_material_review_fixes.py:16-60).
 
 The reference runs them on Warp's deterministic CPU backend. Here they run on the
 GPU, so the one bitwise comparison (sparse against dense) becomes a rounding
@@ -277,3 +280,47 @@ def test_mu_i_chute_develops_the_bagnold_profile(cuda):
     he = float(np.quantile(zr, 0.99))
     bag = he ** 1.5 - (he - np.minimum(zc, he)) ** 1.5
     assert float(np.corrcoef(prof, bag)[0, 1]) > 0.99
+
+
+# ---- a settled column carries hydrostatic-order pressure at its base -------------------
+def test_static_column_pressure_grows_with_depth(cuda):
+    """A dough block settling on a sticky floor (tests/test_engine.py:109-131): the
+    lowest third carries more compressive pressure -tr(sigma)/3 than the top third,
+    and within an order of magnitude of rho g h."""
+    from mpm_engine_gb300 import Solver
+    from mpm_engine_gb300.scenes import block, dough
+    g = _grid(48)
+    pos, vol, floor = block(g, size=(0.08, 0.08, 0.12), ppc=2)
+    s = Solver(grid=g).load_particles(pos, vol)
+    s.set_material(dough())
+    s.add_plane((0, 0, floor), (0, 0, 1), "sticky")
+    s.step(2.0e-5, 2000)
+    x, c = s.x(), s.cauchy()
+    p = -(c[:, 0, 0] + c[:, 1, 1] + c[:, 2, 2]) / 3.0
+    z = x[:, 2]
+    lo, hi = z < np.quantile(z, 0.33), z > np.quantile(z, 0.67)
+    assert p[lo].mean() > p[hi].mean() and p[lo].mean() > 0.0
+    p_hydro = 1000.0 * GRAV * float(z.max() - z.min())
+    assert 0.1 * p_hydro < p[lo].mean() < 10.0 * p_hydro, (p[lo].mean(), p_hydro)
+
+
+# ---- von Mises hardening evolves the yield stress --------------------------------------
+def _squeeze_yield(xi):
+    """A von Mises block crushed 12 mm by a plate (tests/test_material_review_fixes.py
+    :16-49); returns the per-particle yield stress after sustained plastic flow."""
+    from mpm_engine_gb300 import Solver, vonmises
+    g = _grid()
+    h = g.dx / 2
+    pos = _fill(0.16, 0.24, 0.16, 0.24, 0.16, 0.24, h)
+    s = Solver(grid=g).load_particles(pos, np.full(len(pos), h ** 3, np.float32))
+    s.set_material(vonmises(E=5.0e5, nu=0.3, yield_stress=2.0e3, hardening_xi=xi), g=[0.0, 0.0, 0.0])
+    s.add_plane((0, 0, 0.16), (0, 0, 1), "sticky")
+    s.add_box(center=(0.2, 0.2, 0.30), half_size=(0.1, 0.1, 0.06), velocity=(0.0, 0.0, -0.2))
+    for _ in range(30):
+        s.step(2e-4, 10)
+    return s._sim.mpm_model.yield_stress.numpy()
+
+
+def test_von_mises_hardening_evolves_the_yield(cuda):
+    assert float(_squeeze_yield(0.0).max()) == pytest.approx(2.0e3)
+    assert float(_squeeze_yield(5.0e4).max()) > 2.1e3
