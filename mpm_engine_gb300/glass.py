@@ -4,7 +4,10 @@ Same public behaviour as warpmpm.colliders.glass (src/warpmpm/colliders/glass.py
 `GlassProfile` (defaults 0.089 m outer radius, 0.020 m wall, 0.24 m height, 0.050 m
 base, 0.012 m fillet), the revolved SDF `glass_sdf_local` that the cup collider
 kernel evaluates, and `cup_fill`, whose jittered lattice defines the 340,489-particle
-pour at 192^3 / grid_lim 0.7. Quaternions here are w x y z.
+pour at 192^3 / grid_lim 0.7. The host helpers that pour scripts use around the step
+are here too: `glass_sdf` at a pose, `cavity_mask` (liquid held), `solid_mask`
+(leak audit), `project_out_of_solid`, `write_glass_obj` (the render mesh) and the
+quaternion conversions. Quaternions here are w x y z.
 """
 from __future__ import annotations
 
@@ -30,6 +33,43 @@ def quat_mul(a, b) -> np.ndarray:
                      aw * bx + ax * bw + ay * bz - az * by,
                      aw * by - ax * bz + ay * bw + az * bx,
                      aw * bz + ax * by - ay * bx + az * bw], dtype=np.float64)
+
+
+def quat_conj(q) -> np.ndarray:
+    """Conjugate (the inverse rotation for a unit quaternion), w x y z."""
+    w, x, y, z = (float(c) for c in q)
+    return np.array([w, -x, -y, -z], dtype=np.float64)
+
+
+def quat_from_mat(m) -> np.ndarray:
+    """Unit w x y z quaternion of a rotation matrix. Shepperd's method: take the
+    square root of whichever of 1 + trace and 1 + 2 m_ii - trace is largest (the
+    best-conditioned component), then the other three components from the
+    off-diagonal sums and differences."""
+    m = np.asarray(m, dtype=np.float64)
+    t = float(m[0, 0] + m[1, 1] + m[2, 2])
+    if t > 0.0:
+        k = 0
+    elif m[0, 0] > m[1, 1] and m[0, 0] > m[2, 2]:
+        k = 1
+    elif m[1, 1] > m[2, 2]:
+        k = 2
+    else:
+        k = 3
+    if k == 0:
+        r = 2.0 * np.sqrt(t + 1.0)
+        q = [0.25 * r, (m[2, 1] - m[1, 2]) / r, (m[0, 2] - m[2, 0]) / r, (m[1, 0] - m[0, 1]) / r]
+    elif k == 1:
+        r = 2.0 * np.sqrt(max(1.0 + m[0, 0] - m[1, 1] - m[2, 2], 1e-12))
+        q = [(m[2, 1] - m[1, 2]) / r, 0.25 * r, (m[0, 1] + m[1, 0]) / r, (m[0, 2] + m[2, 0]) / r]
+    elif k == 2:
+        r = 2.0 * np.sqrt(max(1.0 + m[1, 1] - m[0, 0] - m[2, 2], 1e-12))
+        q = [(m[0, 2] - m[2, 0]) / r, (m[0, 1] + m[1, 0]) / r, 0.25 * r, (m[1, 2] + m[2, 1]) / r]
+    else:
+        r = 2.0 * np.sqrt(max(1.0 + m[2, 2] - m[0, 0] - m[1, 1], 1e-12))
+        q = [(m[1, 0] - m[0, 1]) / r, (m[0, 2] + m[2, 0]) / r, (m[1, 2] + m[2, 1]) / r, 0.25 * r]
+    q = np.asarray(q, dtype=np.float64)
+    return q / np.linalg.norm(q)
 
 
 def quat_from_axis_angle(axis, angle: float) -> np.ndarray:
@@ -120,6 +160,111 @@ def glass_sdf_local(points_local, profile: GlassProfile):
     cavity = _capped_cylinder(r, z, profile.inner_radius - fr, profile.inner_floor_z + fr,
                               profile.half_height + profile.outer_radius) - fr
     return np.maximum(outer, -cavity)
+
+
+def glass_sdf(points_world, pos, quat, profile: GlassProfile):
+    """glass_sdf_local of world points for the glass at (pos, w x y z quat)."""
+    return glass_sdf_local(world_to_local(points_world, pos, quat), profile)
+
+
+def cavity_mask(points_world, pos, quat, profile: GlassProfile, pad: float = 0.0,
+                brim_clearance: float = 0.0) -> np.ndarray:
+    """Points held in the open cavity: within the cavity radius at their height (plus
+    `pad`), at or above the floor (1 mm slack) and at most `brim_clearance` below the
+    rim (colliders/glass.py:218-230)."""
+    loc = world_to_local(points_world, pos, quat)
+    r = np.hypot(loc[:, 0], loc[:, 1])
+    z = loc[:, 2]
+    return (r < profile.inner_radius_at_z(z) + pad) & (z >= profile.inner_floor_z - 1e-3) & \
+        (z <= profile.rim_z - brim_clearance)
+
+
+def solid_mask(points_world, pos, quat, profile: GlassProfile, tol: float = 0.0) -> np.ndarray:
+    """Points embedded in the glass material deeper than `tol`."""
+    return glass_sdf(points_world, pos, quat, profile) < -tol
+
+
+def project_out_of_solid(x, v, pos, quat, profile: GlassProfile, clearance: float = 0.0, solid_velocity=None):
+    """Moves every point embedded in the glass out along the SDF gradient (central
+    differences, step 1e-5 m) to `clearance` outside the surface. It then removes the
+    inward normal part of its velocity relative to the wall, whose velocity is
+    v_lin + omega x (x - pos) when `solid_velocity` = (v_lin, omega) is given, else
+    zero (colliders/glass.py:238-290). Returns (x_new, v_new, number moved); the
+    inputs are not modified."""
+    x = np.array(x, dtype=np.float64)
+    v = np.array(v, dtype=np.float64)
+    d = glass_sdf(x, pos, quat, profile)
+    bad = d < 0.0
+    nb = int(bad.sum())
+    if nb == 0:
+        return x, v, 0
+    R = quat_to_mat(quat)
+    p0 = np.asarray(pos, dtype=np.float64)
+    loc = world_to_local(x[bad], pos, quat)
+    eps = 1e-5
+    g = np.empty_like(loc)
+    for a in range(3):
+        e = np.zeros(3)
+        e[a] = eps
+        g[:, a] = glass_sdf_local(loc + e, profile) - glass_sdf_local(loc - e, profile)
+    n = g / np.maximum(np.linalg.norm(g, axis=1, keepdims=True), 1e-12)
+    x[bad] = (loc + (clearance - d[bad])[:, None] * n) @ R.T + p0
+    nw = n @ R.T
+    if solid_velocity is None:
+        vw = np.zeros((nb, 3))
+    else:
+        vl, om = (np.asarray(c, dtype=np.float64) for c in solid_velocity)
+        vw = vl + np.cross(om, x[bad] - p0)
+    rel = v[bad] - vw
+    vn = np.einsum("ij,ij->i", rel, nw)
+    v[bad] = vw + rel - nw * np.minimum(vn, 0.0)[:, None]
+    return x, v, nb
+
+
+def write_glass_obj(profile: GlassProfile, path, segments: int = 48, fillet_segments: int = 8):
+    """Writes the glass as a watertight, outward-wound triangle mesh (OBJ) in its
+    local frame: outer wall, rim annulus, inner wall, fillet strips down to the
+    cavity floor, a bottom cap and a floor disc (colliders/glass.py:293-354).
+    Returns the path."""
+    from pathlib import Path
+    path = Path(path)
+    path.parent.mkdir(parents=True, exist_ok=True)
+    n = int(segments)
+    th = np.arange(n) * (2.0 * np.pi / n)
+    c, s_ = np.cos(th), np.sin(th)
+    ro, ri = profile.outer_radius, profile.inner_radius
+    zb, zr, zf = -profile.half_height, profile.rim_z, profile.inner_floor_z
+    fr = min(max(profile.fillet_radius, 0.0), ri - 1e-6)
+
+    def ring(rad, z):
+        return np.column_stack([rad * c, rad * s_, np.full(n, z)])
+
+    if fr > 0.0:
+        phi = np.linspace(0.0, 0.5 * np.pi, fillet_segments + 1)
+        fil = [ring(ri - fr + fr * np.sin(a), zf + fr * (1.0 - np.cos(a))) for a in phi]
+    else:
+        fil = [ring(ri, zf)]
+    rings = [ring(ro, zb), ring(ro, zr), ring(ri, zr)] + fil
+    start = [k * n for k in range(len(rings))]
+    verts = np.vstack(rings + [np.array([[0.0, 0.0, zb], [0.0, 0.0, zf]])])
+    cb, cf = len(verts) - 2, len(verts) - 1
+    ob, ot, it = start[0], start[1], start[2]
+    fs = start[3:]
+    tris = []
+    for i in range(n):
+        j = (i + 1) % n
+        tris += [(ob + i, ob + j, ot + j), (ob + i, ot + j, ot + i)]            # outer wall
+        tris += [(ot + i, ot + j, it + j), (ot + i, it + j, it + i)]            # rim
+        tris += [(fs[-1] + i, it + i, it + j), (fs[-1] + i, it + j, fs[-1] + j)]  # inner wall
+        for a, b in zip(fs[:-1], fs[1:]):                                       # fillet
+            tris += [(a + i, b + i, b + j), (a + i, b + j, a + j)]
+        tris.append((cb, ob + j, ob + i))                                       # bottom cap
+        tris.append((cf, fs[0] + i, fs[0] + j))                                 # cavity floor
+    with path.open("w", encoding="utf-8") as f:
+        f.write(f"# glass: R_o={ro} R_i={ri} h={profile.height} base={profile.base_thickness} fillet={fr}\n")
+        f.writelines(f"v {p[0]:.6f} {p[1]:.6f} {p[2]:.6f}\n" for p in verts)
+        f.writelines(f"f {a + 1} {b + 1} {d + 1}\n" for a, b, d in tris)
+    return path
 
 
 def cup_fill(profile: GlassProfile, h: float, fill_fraction: float = 0.80, clearance: float | None = None,
