@@ -1306,6 +1306,68 @@ class Solver:
         return 0 if self._eng is None else int(self._eng.lib.gbmpm_launch_count(self._eng.h))
 
     # ------------------------------------------------------------ test access
+    # per-particle arrays a checkpoint carries: everything the step reads or writes
+    _CHECKPOINT_FIELDS = ("x", "v", "C", "F", "F_trial", "L", "stress", "mass", "vol", "density", "Jp", "mu", "lam",
+                          "yield_stress", "material", "selection", "cov", "init_cov", "cdf_tag", "rigid_id", "x_ref",
+                          "mod_mask")
+
+    def state_dict(self) -> dict:
+        """Checkpoint of the simulation. It holds device copies of every per-particle
+        array, the clock and tick counters, the collider poses and the rigid bodies'
+        states. The reference has no full-state checkpoint; its pour script caches
+        x and v only (examples/pour_franka.py:367-387)."""
+        self._require_loaded()
+        self._pull_colliders()
+        cols = []
+        for rec in self._cols:
+            r = _abi.Collider()
+            C.memmove(C.byref(r), C.byref(rec), C.sizeof(_abi.Collider))
+            cols.append(r)
+        bodies = []
+        if self._n_bodies:
+            arr = self._rigid_bodies()
+            for i in range(self._n_bodies):
+                b = _abi.RigidBody()
+                C.memmove(C.byref(b), C.byref(arr[i]), C.sizeof(_abi.RigidBody))
+                bodies.append(b)
+        return {"particles": {k: t.detach().clone() for k, t in self._t.items()
+                              if k in self._CHECKPOINT_FIELDS and t is not None},
+                "vol0": None if self._vol0 is None else np.array(self._vol0, copy=True),
+                "time": self._time, "step": self._step, "tick": self._tick, "colliders": cols,
+                "rigid_bodies": bodies, "n_particles": self._n, "n_grid": self.grid.n_grid}
+
+    def load_state_dict(self, state: dict) -> Solver:
+        """Restores a `state_dict` of this scene (same particles, grid and colliders).
+        The arrays are copied in place, so buffer addresses and captured tick graphs
+        stay valid; the working copy, the grid and the active blocks are rebuilt by
+        the next tick from these arrays. Scenes with CDF lanes are refused: their
+        per-particle scan cache and stamp history are not part of the checkpoint."""
+        self._require_loaded()
+        if state.get("n_particles") != self._n or state.get("n_grid") != self.grid.n_grid:
+            raise ValueError("state_dict is of another scene (particle count or grid differs)")
+        if self._cdf:
+            raise NotImplementedError("load_state_dict does not restore CDF (CPIC) lane state")
+        if len(state["colliders"]) != len(self._cols) or len(state["rigid_bodies"]) != self._n_bodies:
+            raise ValueError("state_dict has another collider or rigid-body set")
+        for k, t in state["particles"].items():
+            if self._t.get(k) is None:
+                raise ValueError(f"state_dict carries '{k}', which this scene does not allocate")
+            self._t[k].copy_(t)
+        self._cols = []
+        for rec in state["colliders"]:
+            r = _abi.Collider()
+            C.memmove(C.byref(r), C.byref(rec), C.sizeof(_abi.Collider))
+            self._cols.append(r)
+        self._cols_dirty = True
+        if self._n_bodies:
+            arr = (_abi.RigidBody * self._n_bodies)(*state["rigid_bodies"])
+            self._push_rigid(arr)
+        if state.get("vol0") is not None:
+            self._vol0 = np.array(state["vol0"], copy=True)
+        self._time, self._step, self._tick = state["time"], state["step"], state["tick"]
+        self._sync_engine()
+        return self
+
     def export_state(self) -> dict:
         """Host copies of the engine inputs (particles, model, colliders, clock) used to
         replay the same scene elsewhere."""
