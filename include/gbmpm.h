@@ -234,8 +234,13 @@ int gbmpm_cdf_force_stamp(gbmpm_engine *e, int32_t on);
  * kernels/warp_utils.py:84, read at kernels/mpm_utils.py:856, 980). The skip is
  * exact, so results do not change. */
 int gbmpm_cdf_mask_off(gbmpm_engine *e, int32_t off);
-/* 1 when a captured tick graph is ready for replay. */
+/* 1 when a captured tick graph is ready for replay, 0 when none is, -1 after a
+ * capture failed: ticks then launch live for the rest of the run, as the
+ * reference falls back (kernels/mpm_solver_warp.py:1118-1125). */
 int32_t gbmpm_graph_state(gbmpm_engine *e);
+/* Test hook for failure handling: the next capture is discarded as if it had failed.
+ * Nothing invalid reaches the GPU. */
+int gbmpm_debug_fail_next_capture(gbmpm_engine *e);
 
 /* Current volume vol0 * J, Cauchy stress = stress / J and J = det(F) per particle
  * (Solver.vol / Solver.cauchy, core/solver.py:559-598) into caller device buffers

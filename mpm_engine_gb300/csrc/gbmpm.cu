@@ -2431,6 +2431,8 @@ struct gbmpm_engine {
     cudaEvent_t pose_done = nullptr;
     int bd = 0;
     int num_sms = 148;
+    bool graph_failed = false;          // a capture failed: live launches for the rest of the run
+    bool fake_capture_failure = false;  // test hook: treat the next capture as failed
     int tile_occ = 3;       // resident CTAs per SM the tiled particle kernel is compiled for
     int cdf_occ = 3;        // the same for its CPIC variant
     bool pdl = true;        // programmatic dependent launch of the particle and grid passes
@@ -3441,7 +3443,16 @@ int gbmpm_cdf_mask_off(gbmpm_engine *e, int32_t off) {
     return GBMPM_OK;
 }
 
-int32_t gbmpm_graph_state(gbmpm_engine *e) { return (e && e->graph) ? 1 : 0; }
+int32_t gbmpm_graph_state(gbmpm_engine *e) {
+    if (!e) return 0;
+    return e->graph_failed ? -1 : (e->graph ? 1 : 0);
+}
+
+int gbmpm_debug_fail_next_capture(gbmpm_engine *e) {
+    if (!e) return fail(GBMPM_ERR_ARG, "null argument");
+    e->fake_capture_failure = true;
+    return GBMPM_OK;
+}
 
 int gbmpm_reset_cdf_wrench(gbmpm_engine *e, void *stream) {
     if (!e) return fail(GBMPM_ERR_ARG, "null argument");
@@ -3543,7 +3554,7 @@ int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32
     const bool profile = (flags & GBMPM_TICK_PROFILE) != 0;
     const bool use_graph = (flags & GBMPM_TICK_GRAPH) && !profile;
     const float dtf = (float)dt;
-    if (!use_graph) {
+    if (!use_graph || e->graph_failed) {
         record_tick(e, dtf, substeps, fused, reorder, s, profile, t0, dt);
         GB_CUDA(cudaGetLastError());
         return GBMPM_OK;
@@ -3562,10 +3573,23 @@ int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32
         e->launches = before;
         cudaError_t ce = cudaStreamEndCapture(cap, &g);
         cudaStreamDestroy(cap);
-        if (ce != cudaSuccess) return fail(GBMPM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
-        ce = cudaGraphInstantiate(&e->graph, g, 0);
-        cudaGraphDestroy(g);
-        if (ce != cudaSuccess) { e->graph = nullptr; return fail(GBMPM_ERR_CUDA, "graph instantiate failed"); }
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&e->graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (ce == cudaSuccess && e->fake_capture_failure) {   // test hook: this capture counts as failed
+            cudaGraphExecDestroy(e->graph);
+            ce = cudaErrorStreamCaptureInvalidated;
+        }
+        e->fake_capture_failure = false;
+        if (ce != cudaSuccess) {
+            // as the reference does on a failed capture (mpm_solver_warp.py:1118-1125): no
+            // graphs for the rest of the run, this tick and the next ones launched live
+            e->graph = nullptr;
+            e->graph_failed = true;
+            (void)cudaGetLastError();
+            record_tick(e, dtf, substeps, fused, reorder, s, profile, t0, dt);
+            GB_CUDA(cudaGetLastError());
+            return GBMPM_OK;
+        }
         e->g_substeps = substeps; e->g_flags = flags; e->g_dt = dt; e->g_stream = s;
         e->dirty = false;
     }

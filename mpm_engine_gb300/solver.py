@@ -191,7 +191,7 @@ class _SimShim:
     def _graph_A(self):
         """Non-None once the engine holds a captured tick graph."""
         s = self._s
-        return "tick graph" if s._eng is not None and s._eng.lib.gbmpm_graph_state(s._eng.h) else None
+        return "tick graph" if s._eng is not None and s._eng.lib.gbmpm_graph_state(s._eng.h) > 0 else None
 
     @property
     def collider_aabbs(self):
@@ -1077,6 +1077,10 @@ class Solver:
         t = C.c_double(self._time)
         _abi.check(self._eng.lib.gbmpm_tick(self._eng.h, C.byref(t), float(dt), int(substeps), flags,
                                             self._stream()), "gbmpm_tick")
+        if flags & _abi.TICK_GRAPH and self._eng.lib.gbmpm_graph_state(self._eng.h) < 0:
+            # the capture failed and the engine ran this tick live; like the reference,
+            # stay on live launches (mpm_solver_warp.py:1118-1125)
+            self._sim.use_cuda_graph = False
         self._time = t.value
         self._step += substeps
         return self

@@ -88,3 +88,23 @@ def test_material_range_and_mu_lam(cuda):
     np.testing.assert_allclose(mu[100:], 5e4 / 2.6, rtol=1e-6)
     with pytest.raises(NotImplementedError):
         s.set_material_range(0, 10, __import__("mpm_engine_gb300").tabulated_viscous([1.0, 2.0]))
+
+
+def test_failed_capture_falls_back_to_live_launches(cuda):
+    """The reference drops its graphs and keeps stepping live when a capture fails
+    (kernels/mpm_solver_warp.py:1118-1125). The failure is made on the host: the
+    engine's test hook discards the next capture as failed, so nothing invalid runs
+    on the GPU. The run continues live and agrees with a graph run to rounding."""
+    from scenes_lib import blob_scene
+    from mpm_engine_gb300 import Solver
+    a, _ = blob_scene(Solver, "jelly", v0=True)
+    b, _ = blob_scene(Solver, "jelly", v0=True)
+    assert a._sim.use_cuda_graph
+    a._eng.lib.gbmpm_debug_fail_next_capture(a._eng.h)
+    for _ in range(5):
+        a.step(2.0e-4, 4)
+        b.step(2.0e-4, 4)
+    assert a._sim.use_cuda_graph is False and a._sim._graph_A is None
+    assert a._eng.lib.gbmpm_graph_state(a._eng.h) == -1
+    assert b._sim._graph_A is not None
+    np.testing.assert_allclose(a.x(), b.x(), rtol=1e-5, atol=1e-6)
