@@ -2644,7 +2644,7 @@ const int *record_ws_begin(gbmpm_engine *e, cudaStream_t s) {
     e->launches++;
     unsigned long long maxkey = ((unsigned long long)e->bd * e->bd * e->bd << 6) - 1ull;
     int bits = 0;
-    while ((maxkey >> bits) != 0ull) ++bits;
+    while (bits < 64 && (maxkey >> bits) != 0ull) ++bits;
     int cur = 0;
     for (int shift = 0; shift < bits; shift += kRadixBits) {
         k_radix_hist<<<ntiles, kSortThreads, 0, s>>>(e->ws_keys[cur].ptr, n, shift, e->ws_hist.ptr, ntiles);
