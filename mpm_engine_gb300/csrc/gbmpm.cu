@@ -214,2108 +214,10 @@ __device__ __forceinline__ void udvt(const float *U, float d0, float d1, float d
 
 __device__ __forceinline__ void set_status(unsigned *st, unsigned bit) { atomicOr(st, bit); }
 
-// ------------------------------------------------------- material laws -----
-// Kirchhoff stress of the viscous laws (mpm_utils.py:17-85)
-__device__ __forceinline__ void dev_rate(const float *L, float *Dd, float &gd) {
-    float D[9];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) D[3 * i + j] = 0.5f * (L[3 * i + j] + L[3 * j + i]);
-    float trd = (D[0] + D[4] + D[8]) / 3.0f;
-    float dd = 0.0f;
-#pragma unroll
-    for (int i = 0; i < 9; ++i) {
-        Dd[i] = D[i] - ((i % 4 == 0) ? trd : 0.0f);
-        dd += Dd[i] * Dd[i];
-    }
-    gd = sqrtf(2.0f * dd + 0.02f * 0.02f);
-}
-
-__device__ __forceinline__ float eos_pressure(float J, float bulk) { return -bulk * (powf(J, -1.1f) - 1.0f); }
-
-__device__ __forceinline__ float table_lerp(const float *tab, int n, float smin, float smax, float s) {
-    float idx = (s - smin) / (smax - smin) * (float)(n - 1);
-    idx = fminf(fmaxf(idx, 0.0f), (float)(n - 1) - 1.0e-6f);
-    int i0 = (int)floorf(idx);
-    float fr = idx - (float)i0;
-    return tab[i0] * (1.0f - fr) + tab[i0 + 1] * fr;
-}
-
-// Hencky stress U diag(2 mu eps + lam tr eps) U^T (mpm_utils.py:228-243)
-__device__ __forceinline__ void stress_hencky(const float *U, const float *sig, float mu, float lam, float *out) {
-    float e0 = logf(fmaxf(sig[0], 1e-6f)), e1 = logf(fmaxf(sig[1], 1e-6f)), e2 = logf(fmaxf(sig[2], 1e-6f));
-    float tr = e0 + e1 + e2;
-    udvt(U, 2.0f * mu * e0 + lam * tr, 2.0f * mu * e1 + lam * tr, 2.0f * mu * e2 + lam * tr, U, out);
-}
-
-// the friction law mu(I): mu_s + dmu I / (I + I0), or the table over log10 I
-template <bool TAB>
-__device__ __forceinline__ float mu_of_i(float Im, float mu_s, float dmu, float I0, const float *tab, int tn, float smin,
-                                         float smax) {
-    if (!TAB) return mu_s + dmu * Im / (Im + I0);
-    return table_lerp(tab, tn, smin, smax, logf(fmaxf(Im, 1e-12f)) * 0.43429448190325176f);
-}
-
-// the 48-step bisection on g(gdp) = tau_bar - G dt gdp - mu(I) p (mpm_utils.py:300-312)
-template <bool TAB>
-__device__ __forceinline__ float mu_i_bisect(float tbK, float G, float dt, float pK, float Ic, float mu_s, float dmu,
-                                             float I0, const float *tab, int tn, float smin, float smax) {
-    float lo = 0.0f, hi = tbK / (G * dt);
-    for (int it = 0; it < 48; ++it) {
-        float mid = 0.5f * (lo + hi);
-        float mu_mid = mu_of_i<TAB>(mid * Ic, mu_s, dmu, I0, tab, tn, smin, smax);
-        float g = tbK - G * dt * mid - mu_mid * pK;
-        if (g > 0.0f) lo = mid; else hi = mid;
-    }
-    return 0.5f * (lo + hi);
-}
-template <bool TAB>
-__device__ __forceinline__ float mu_i_bisect(float tbK, float G, float dt, float pK, float Ic, float mu_s, float dmu,
-                                             float I0, const PK &k) {
-    return mu_i_bisect<TAB>(tbK, G, dt, pK, Ic, mu_s, dmu, I0, k.eta, k.eta_n, k.eta_smin, k.eta_smax);
-}
-
-// Return map F_trial -> F and Kirchhoff stress for one particle
-// (stress_update_particle, mpm_utils.py:1056-1149).
-template <bool SOLIDS>
-__device__ __forceinline__ void stress_update(const PK &k, int p, int mat, const float *Ft, const float *L, float *F,
-                                              float *S) {
-    const MatTables &T = *k.tab;
-    if (!SOLIDS || mat == 6 || mat == 10 || mat == 12 || mat == 7 || mat == 8) {
-        float J;
-        if (mat == 7 || mat == 8) {
-#pragma unroll
-            for (int i = 0; i < 9; ++i) F[i] = (i % 4 == 0) ? 1.0f : 0.0f;
-            J = 1.0f;
-        } else {
-            float Jt = det3(Ft);
-            float Jc = powf(Jt, 1.0f / 3.0f);
-#pragma unroll
-            for (int i = 0; i < 9; ++i) F[i] = (i % 4 == 0) ? Jc : 0.0f;
-            J = Jc * Jc * Jc;
-        }
-        if (mat == 7 || mat == 8) {
-#pragma unroll
-            for (int i = 0; i < 9; ++i) S[i] = 0.0f;
-            return;
-        }
-        float pr = eos_pressure(J, T.bulk[mat]);
-        if (mat == 6) {
-#pragma unroll
-            for (int i = 0; i < 9; ++i) S[i] = (i % 4 == 0) ? J * pr : 0.0f;
-            return;
-        }
-        float Dd[9], gd;
-        dev_rate(L, Dd, gd);
-        float eta_app;
-        if (mat == 10) {
-            // tau_y / gd and K gd^(n-1) are exactly zero when tau_y or K is zero
-            const float ys = k.ys[p], Kp = T.hardening[mat];
-            eta_app = T.pv[mat] + (ys != 0.0f ? ys / gd : 0.0f) + (Kp != 0.0f ? Kp * powf(gd, T.softening[mat] - 1.0f) : 0.0f);
-        }
-        else eta_app = table_lerp(k.eta, k.eta_n, k.eta_smin, k.eta_smax, logf(gd) * 0.43429448190325176f);
-        float two_eta = 2.0f * eta_app;
-#pragma unroll
-        for (int i = 0; i < 9; ++i) S[i] = J * (((i % 4 == 0) ? pr : 0.0f) + two_eta * Dd[i]);
-        return;
-    }
-    if constexpr (SOLIDS) {
-        float U[9], V[9], sig[3];
-        float mu = k.mu[p], lam = k.lam[p];
-        // ---- return mapping
-        if (mat == 1 || mat == 5) {  // von Mises (mpm_utils.py:127-225)
-            svd3(Ft, U, sig, V);
-            float e0 = logf(fmaxf(sig[0], 0.01f)), e1 = logf(fmaxf(sig[1], 0.01f)), e2 = logf(fmaxf(sig[2], 0.01f));
-            float tr = e0 + e1 + e2;
-            float temp = tr / 3.0f;
-            float t0 = 2.0f * mu * e0 + lam * tr, t1 = 2.0f * mu * e1 + lam * tr, t2 = 2.0f * mu * e2 + lam * tr;
-            float st = (t0 + t1 + t2) / 3.0f;
-            float c0 = t0 - st, c1 = t1 - st, c2 = t2 - st;
-            float y = k.ys[p];
-            bool done = false;
-            if (sqrtf(c0 * c0 + c1 * c1 + c2 * c2) > y) {
-                if (mat == 5 && y <= 0.0f) {
-#pragma unroll
-                    for (int i = 0; i < 9; ++i) F[i] = Ft[i];
-                    done = true;
-                } else {
-                    float h0 = e0 - temp, h1 = e1 - temp, h2 = e2 - temp;
-                    float hn = sqrtf(h0 * h0 + h1 * h1 + h2 * h2) + 1e-6f;
-                    float dg = hn - y / (2.0f * mu);
-                    float r = dg / hn;
-                    e0 -= r * h0; e1 -= r * h1; e2 -= r * h2;
-                    if (mat == 5) {
-                        float rh0 = r * h0, rh1 = r * h1, rh2 = r * h2;
-                        y = y - T.softening[mat] * sqrtf(rh0 * rh0 + rh1 * rh1 + rh2 * rh2);
-                        if (y <= 0.0f) { mu = 0.0f; lam = 0.0f; k.mu[p] = 0.0f; k.lam[p] = 0.0f; }
-                    }
-                    sig[0] = expf(e0); sig[1] = expf(e1); sig[2] = expf(e2);
-                    udvt(U, sig[0], sig[1], sig[2], V, F);
-                    if (T.hardening[mat] > 0.5f) y = y + 2.0f * mu * T.xi[mat] * dg;
-                    k.ys[p] = y;
-                    done = true;
-                }
-            }
-            if (!done) {
-#pragma unroll
-                for (int i = 0; i < 9; ++i) F[i] = Ft[i];
-            }
-        } else if (mat == 2) {  // Drucker-Prager sand (mpm_utils.py:543-580)
-            svd3(Ft, U, sig, V);
-            float e0 = logf(fmaxf(fabsf(sig[0]), 1e-14f)), e1 = logf(fmaxf(fabsf(sig[1]), 1e-14f)),
-                  e2 = logf(fmaxf(fabsf(sig[2]), 1e-14f));
-            float tr = e0 + e1 + e2;
-            float h0 = e0 - tr / 3.0f, h1 = e1 - tr / 3.0f, h2 = e2 - tr / 3.0f;
-            float hn = sqrtf(h0 * h0 + h1 * h1 + h2 * h2);
-            float dg = hn + (3.0f * lam + 2.0f * mu) / (2.0f * mu) * tr * T.alpha[mat];
-            if (dg <= 0.0f) {
-#pragma unroll
-                for (int i = 0; i < 9; ++i) F[i] = Ft[i];
-            } else if (tr > 0.0f) {
-                sig[0] = sig[1] = sig[2] = 1.0f;
-                udvt(U, 1.0f, 1.0f, 1.0f, V, F);
-            } else {
-                float r = dg / hn;
-                sig[0] = expf(e0 - h0 * r); sig[1] = expf(e1 - h1 * r); sig[2] = expf(e2 - h2 * r);
-                udvt(U, sig[0], sig[1], sig[2], V, F);
-            }
-        } else if (mat == 9 || mat == 13 || mat == 11) {  // mu(I) family (mpm_utils.py:246-522)
-            svd3(Ft, U, sig, V);
-            float s0 = fmaxf(fabsf(sig[0]), 1e-6f), s1 = fmaxf(fabsf(sig[1]), 1e-6f), s2 = fmaxf(fabsf(sig[2]), 1e-6f);
-            float e0 = logf(s0), e1 = logf(s1), e2 = logf(s2);
-            float tr = e0 + e1 + e2;
-            float mean = tr / 3.0f;
-            float d0 = e0 - mean, d1 = e1 - mean, d2 = e2 - mean;
-            float dn = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
-            float J = s0 * s1 * s2;
-#pragma unroll
-            for (int i = 0; i < 9; ++i) F[i] = Ft[i];
-            if (mat != 11) {
-                if (tr >= 0.0f) {
-                    sig[0] = sig[1] = sig[2] = 1.0f;
-                    udvt(U, 1.0f, 1.0f, 1.0f, V, F);
-                } else {
-                    float pK = -(2.0f * mu / 3.0f + lam) * tr;
-                    float tbK = 2.0f * mu * dn / sqrtf(2.0f);
-                    float pC = pK / J;
-                    float thr = (mat == 13) ? k.eta[0] : T.mu_s[mat];
-                    if (tbK > thr * pK) {
-                        float Ic = T.d[mat] * sqrtf(T.rho_s[mat] / pC);
-                        float gdp = (mat == 13) ? mu_i_bisect<true>(tbK, mu, k.dt, pK, Ic, 0, 0, 0, k)
-                                                : mu_i_bisect<false>(tbK, mu, k.dt, pK, Ic, T.mu_s[mat], T.dmu[mat],
-                                                                     T.I0[mat], k);
-                        float sc = (tbK - mu * k.dt * gdp) / fmaxf(tbK, 1e-20f);
-                        sig[0] = expf(d0 * sc + mean); sig[1] = expf(d1 * sc + mean); sig[2] = expf(d2 * sc + mean);
-                        udvt(U, sig[0], sig[1], sig[2], V, F);
-                    }
-                }
-            } else {
-                float Jr = k.Jp[p];
-                if (Jr < 0.5f) Jr = 1.0f;
-                float K = T.E[mat] / (3.0f * (1.0f - 2.0f * T.nu[mat]));
-                float pc = fmaxf(K * (Jr / fmaxf(J, 1e-6f) - 1.0f), 0.0f);
-                float jp_new = Jr;
-                if (pc <= 0.0f) {
-                    float si = expf(mean);
-                    sig[0] = sig[1] = sig[2] = si;
-                    udvt(U, si, si, si, V, F);
-                } else {
-                    float pK = pc * J;
-                    float tbK = 2.0f * mu * dn / sqrtf(2.0f);
-                    if (tbK > T.mu_s[mat] * pK) {
-                        float Ic = T.d[mat] * sqrtf(T.rho_s[mat] / pc);
-                        float gdp = mu_i_bisect<false>(tbK, mu, k.dt, pK, Ic, T.mu_s[mat], T.dmu[mat], T.I0[mat], k);
-                        float Ir = gdp * Ic;
-                        float dgam = fminf(8.0f * gdp * k.dt, 1.0f);
-                        float jcs = 1.0f / fmaxf(1.0f - T.phi_chi[mat] * Ir / (Ir + T.I0[mat]), 1e-3f);
-                        jp_new = Jr + dgam * (jcs - Jr);
-                        float sc = (tbK - mu * k.dt * gdp) / fmaxf(tbK, 1e-20f);
-                        sig[0] = expf(d0 * sc + mean); sig[1] = expf(d1 * sc + mean); sig[2] = expf(d2 * sc + mean);
-                        udvt(U, sig[0], sig[1], sig[2], V, F);
-                    }
-                }
-                k.Jp[p] = jp_new;
-            }
-        } else {  // jelly (0) and any unknown id: F = F_trial
-#pragma unroll
-            for (int i = 0; i < 9; ++i) F[i] = Ft[i];
-        }
-        // ---- stress of the returned F. Every return map above leaves (U, sig, V) a
-        // singular value decomposition of the F it returns: F_trial's own when it
-        // returns F_trial (bit for bit what a second svd3 gives), else U diag(sig) V^T
-        // with the projected values, whose descending order the projections keep. So
-        // only the maps without an SVD of their own (FCR jelly) factor F here.
-        float J = det3(F);
-        if (!(mat == 1 || mat == 5 || mat == 2 || mat == 9 || mat == 13 || mat == 11)) svd3(F, U, sig, V);
-        if (mat == 0 || mat == 5) {  // FCR (mpm_utils.py:8-15)
-            float R[9], FR[9];
-            mmT(U, V, R);
-#pragma unroll
-            for (int i = 0; i < 9; ++i) FR[i] = 2.0f * mu * (F[i] - R[i]);
-            mmT(FR, F, S);
-            float dl = lam * J * (J - 1.0f);
-            S[0] += dl; S[4] += dl; S[8] += dl;
-        } else if (mat == 1 || mat == 9 || mat == 13) {
-            stress_hencky(U, sig, mu, lam, S);
-        } else if (mat == 2) {  // Drucker-Prager stress (mpm_utils.py:109-124)
-            float l0 = logf(sig[0]), l1 = logf(sig[1]), l2 = logf(sig[2]);
-            float ls = l0 + l1 + l2;
-            float c0 = (2.0f * mu * l0 + lam * ls) / sig[0];
-            float c1 = (2.0f * mu * l1 + lam * ls) / sig[1];
-            float c2 = (2.0f * mu * l2 + lam * ls) / sig[2];
-            float T1[9];
-            udvt(U, c0, c1, c2, V, T1);
-            mmT(T1, F, S);
-        } else if (mat == 11) {  // mu(I)-Phi(I) stress (mpm_utils.py:525-540)
-            float Jr = k.Jp[p];
-            if (Jr < 0.5f) Jr = 1.0f;
-            float K = T.E[mat] / (3.0f * (1.0f - 2.0f * T.nu[mat]));
-            float pc = fmaxf(K * (Jr / fmaxf(J, 1e-6f) - 1.0f), 0.0f);
-            float s0 = fmaxf(sig[0], 1e-6f), s1 = fmaxf(sig[1], 1e-6f), s2 = fmaxf(sig[2], 1e-6f);
-            float e0 = logf(s0), e1 = logf(s1), e2 = logf(s2);
-            float Jc = s0 * s1 * s2;
-            float mean = (e0 + e1 + e2) / 3.0f;
-            float iso = -pc * Jc;
-            udvt(U, 2.0f * mu * (e0 - mean) + iso, 2.0f * mu * (e1 - mean) + iso, 2.0f * mu * (e2 - mean) + iso, U, S);
-        } else {
-#pragma unroll
-            for (int i = 0; i < 9; ++i) S[i] = 0.0f;
-        }
-        // symmetrize (mpm_utils.py:1148)
-        float s01 = 0.5f * (S[1] + S[3]), s02 = 0.5f * (S[2] + S[6]), s12 = 0.5f * (S[5] + S[7]);
-        S[1] = S[3] = s01; S[2] = S[6] = s02; S[5] = S[7] = s12;
-    }
-}
-
-// ------------------------------------------------------ particle pass ------
-struct Stencil {
-    int b[3];
-    float fx[3];
-    float w[3][3], dw[3][3];
-};
-
-__device__ __forceinline__ void stencil(const float *x, float inv_dx, Stencil &s) {
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        float gp = x[a] * inv_dx;
-        s.b[a] = (int)floorf(gp - 0.5f);
-        float fx = gp - (float)s.b[a];
-        s.fx[a] = fx;
-        float wa = 1.5f - fx, wb = fx - 1.0f, wc = fx - 0.5f;
-        s.w[a][0] = 0.5f * (wa * wa);
-        s.w[a][1] = 0.75f - wb * wb;
-        s.w[a][2] = 0.5f * (wc * wc);
-        s.dw[a][0] = fx - 1.5f;
-        s.dw[a][1] = -2.0f * wb;
-        s.dw[a][2] = wc;
-    }
-}
-
-// true when the 3x3x3 stencil lies inside the grid (x wraps when periodic)
-__device__ __forceinline__ bool stencil_ok(const Stencil &s, int ng, int periodic_x) {
-    bool ok = true;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        if (a == 0 && periodic_x) continue;
-        ok = ok && s.b[a] >= 0 && s.b[a] + 2 < ng;
-    }
-    return ok;
-}
-
-__device__ __forceinline__ int wrap(int i, int n) { return ((i % n) + n) % n; }
-
-__device__ __forceinline__ void mark_block(const PK &k, int bx, int by, int bz) {
-    int b = (bx * k.bd + by) * k.bd + bz;
-    if (k.blk_flag[b] == 0 && atomicExch(&k.blk_flag[b], 1) == 0) {
-        int i = atomicAdd(k.blk_count, 1);
-        k.blk_list[i] = b;
-    }
-}
-
-// ---- building blocks shared by the direct and the tiled particle kernels ----
-
-// G2P for one particle (g2p_particle, mpm_utils.py:944-1043) with the grid
-// velocity supplied by `fetch(ix, iy, iz)` (global memory or a shared tile).
-// The 27-node sums v = sum w g, C = 4/dx sum w g (x_i - x_p)^T / dx and
-// L = sum g grad(w)^T are evaluated axis by axis (z, then y, then x): the
-// quadratic weights are separable, so the 7 moment sums cost 441 FMAs instead of
-// 27 x 21.
-template <class Fetch>
-__device__ __forceinline__ void g2p_core(const PK &k, const Stencil &s, Fetch fetch, float *v, float *C, float *L) {
-    float zw[3], zd[3], zg[3];
-#pragma unroll
-    for (int kk = 0; kk < 3; ++kk) {
-        zw[kk] = s.w[2][kk];
-        zd[kk] = s.w[2][kk] * ((float)kk - s.fx[2]);
-        zg[kk] = s.dw[2][kk];
-    }
-    float V0[3] = {0.f, 0.f, 0.f}, SX[3] = {0.f, 0.f, 0.f}, SY[3] = {0.f, 0.f, 0.f}, SZ[3] = {0.f, 0.f, 0.f};
-    float GX[3] = {0.f, 0.f, 0.f}, GY[3] = {0.f, 0.f, 0.f}, GZ[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        float B0[3] = {0.f, 0.f, 0.f}, BY[3] = {0.f, 0.f, 0.f}, BDY[3] = {0.f, 0.f, 0.f};
-        float BZ[3] = {0.f, 0.f, 0.f}, BDZ[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            float A0[3] = {0.f, 0.f, 0.f}, AZ[3] = {0.f, 0.f, 0.f}, ADZ[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-            for (int kk = 0; kk < 3; ++kk) {
-                float4 g = fetch(i, j, kk);
-                const float gv[3] = {g.x, g.y, g.z};
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    A0[a] += zw[kk] * gv[a];
-                    AZ[a] += zd[kk] * gv[a];
-                    ADZ[a] += zg[kk] * gv[a];
-                }
-            }
-            const float wy = s.w[1][j], wyd = s.w[1][j] * ((float)j - s.fx[1]), dwy = s.dw[1][j];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                B0[a] += wy * A0[a];
-                BY[a] += wyd * A0[a];
-                BDY[a] += dwy * A0[a];
-                BZ[a] += wy * AZ[a];
-                BDZ[a] += wy * ADZ[a];
-            }
-        }
-        const float wx = s.w[0][i], wxd = s.w[0][i] * ((float)i - s.fx[0]), dwx = s.dw[0][i];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            V0[a] += wx * B0[a];
-            SX[a] += wxd * B0[a];
-            SY[a] += wx * BY[a];
-            SZ[a] += wx * BZ[a];
-            GX[a] += dwx * B0[a];
-            GY[a] += wx * BDY[a];
-            GZ[a] += wx * BDZ[a];
-        }
-    }
-    const float c4 = k.inv_dx * 4.0f;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        v[a] = V0[a];
-        C[3 * a + 0] = SX[a] * c4;
-        C[3 * a + 1] = SY[a] * c4;
-        C[3 * a + 2] = SZ[a] * c4;
-        L[3 * a + 0] = GX[a] * k.inv_dx;
-        L[3 * a + 1] = GY[a] * k.inv_dx;
-        L[3 * a + 2] = GZ[a] * k.inv_dx;
-    }
-}
-
-// advection, F_trial and covariance after the gather; Fpre, when given, holds the
-// particle's F (already fetched) instead of the field
-template <bool SOA>
-__device__ __forceinline__ void g2p_finish(const PK &k, int p, float *x, const float *v, const float *L, float *Ft,
-                                           const float *Fpre = nullptr) {
-    float xn[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) xn[a] = x[a] + k.dt * v[a];
-    if (k.periodic_x) {
-        float lx = (float)k.ng * k.dx;
-        if (xn[0] < 0.0f) xn[0] += lx;
-        if (xn[0] >= lx) xn[0] -= lx;
-    }
-#pragma unroll
-    for (int a = 0; a < 3; ++a) x[a] = xn[a];
-    float Fo[9], A[9];
-    if (Fpre) {
-#pragma unroll
-        for (int i = 0; i < 9; ++i) Fo[i] = Fpre[i];
-    } else {
-        fld_load<SOA, 9>(k.F, k.n, p, Fo);
-    }
-#pragma unroll
-    for (int i = 0; i < 9; ++i) A[i] = ((i % 4 == 0) ? 1.0f : 0.0f) + L[i] * k.dt;
-    mm(A, Fo, Ft);
-    if (k.update_cov && k.cov) {
-        float c6[6];
-        fld_load<SOA, 6>(k.cov, k.n, p, c6);
-        float cn[9] = {c6[0], c6[1], c6[2], c6[1], c6[3], c6[4], c6[2], c6[4], c6[5]};
-        float a1[9], a2[9];
-        mm(L, cn, a1);
-        mmT(cn, L, a2);
-        c6[0] = cn[0] + k.dt * (a1[0] + a2[0]);
-        c6[1] = cn[1] + k.dt * (a1[1] + a2[1]);
-        c6[2] = cn[2] + k.dt * (a1[2] + a2[2]);
-        c6[3] = cn[4] + k.dt * (a1[4] + a2[4]);
-        c6[4] = cn[5] + k.dt * (a1[5] + a2[5]);
-        c6[5] = cn[8] + k.dt * (a1[8] + a2[8]);
-        fld_store<SOA, 6>(k.cov, k.n, p, c6);
-    }
-}
-
-// P2G for one particle (p2g_particle, mpm_utils.py:819-916): every node
-// contribution {m v_i, m} goes through `deposit(i, j, kk, float4)`.
-template <class Deposit>
-__device__ __forceinline__ void p2g_core(const PK &k, const Stencil &s, int p, const float *v, const float *Cin,
-                                         const float *S, Deposit deposit) {
-    float C[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) C[i] = Cin[i];
-    if (k.rpic != 0.0f) {
-        float Cn[9];
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-                Cn[3 * i + j] = (1.0f - k.rpic) * C[3 * i + j] + k.rpic / 2.0f * (C[3 * i + j] - C[3 * j + i]);
-#pragma unroll
-        for (int i = 0; i < 9; ++i) C[i] = (k.rpic < -0.001f) ? 0.0f : Cn[i];
-    }
-    const float m = k.mass[p];
-    const float fs = -k.vol[p] * k.dt * k.inv_dx;
-    float A[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) A[i] = fs * S[i];
-    float mCdx[9], base[3];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) mCdx[i] = m * C[i] * k.dx;
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-        base[a] = m * v[a] - (mCdx[3 * a] * s.fx[0] + mCdx[3 * a + 1] * s.fx[1] + mCdx[3 * a + 2] * s.fx[2]);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            float wij = s.w[0][i] * s.w[1][j];
-            float dwi_j = s.dw[0][i] * s.w[1][j];
-            float wi_dj = s.w[0][i] * s.dw[1][j];
-#pragma unroll
-            for (int kk = 0; kk < 3; ++kk) {
-                float wt = wij * s.w[2][kk];
-                float gx = dwi_j * s.w[2][kk], gy = wi_dj * s.w[2][kk], gz = wij * s.dw[2][kk];
-                float mom[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    float aff = base[a] + mCdx[3 * a] * (float)i + mCdx[3 * a + 1] * (float)j + mCdx[3 * a + 2] * (float)kk;
-                    mom[a] = wt * aff + (A[3 * a] * gx + A[3 * a + 1] * gy + A[3 * a + 2] * gz);
-                }
-                deposit(i, j, kk, make_float4(mom[0], mom[1], mom[2], wt * m));
-            }
-        }
-    }
-}
-
-__device__ __forceinline__ void mark_stencil_blocks(const PK &k, const Stencil &s) {
-    int by0 = s.b[1] >> 2, by1 = (s.b[1] + 2) >> 2;
-    int bz0 = s.b[2] >> 2, bz1 = (s.b[2] + 2) >> 2;
-    if (k.periodic_x) {
-        for (int i = 0; i < 3; ++i) {
-            int bxi = wrap(s.b[0] + i, k.ng) >> 2;
-            for (int by = by0; by <= by1; ++by)
-                for (int bz = bz0; bz <= bz1; ++bz) mark_block(k, bxi, by, bz);
-        }
-    } else {
-        int bx0 = s.b[0] >> 2, bx1 = (s.b[0] + 2) >> 2;
-        for (int bx = bx0; bx <= bx1; ++bx)
-            for (int by = by0; by <= by1; ++by)
-                for (int bz = bz0; bz <= bz1; ++bz) mark_block(k, bx, by, bz);
-    }
-}
-
-__device__ __forceinline__ void global_deposit_all(const PK &k, const Stencil &s, int p, const float *v,
-                                                   const float *C, const float *S) {
-    p2g_core(k, s, p, v, C, S, [&](int i, int j, int kk, float4 val) {
-        int ix = s.b[0] + i;
-        if (k.periodic_x) ix = wrap(ix, k.ng);
-        atomicAdd(k.gmv + ((size_t)ix * k.ng + (s.b[1] + j)) * k.ng + (s.b[2] + kk), val);
-    });
-    mark_stencil_blocks(k, s);
-}
-
-__device__ __forceinline__ float4 global_fetch(const PK &k, const Stencil &s, int i, int j, int kk) {
-    int ix = s.b[0] + i;
-    if (k.periodic_x) ix = wrap(ix, k.ng);
-    return __ldg(k.gv + ((size_t)ix * k.ng + (s.b[1] + j)) * k.ng + (s.b[2] + kk));
-}
-
-// ---- CPIC (CDF) transfer helpers (mpm_utils.py:648-816) ----------------------
-// Node tags: bit 2l = lane l valid here, bit 2l+1 = the node's side of lane l,
-// bits 8..9 = the lane nearest the node (owner).
-constexpr int kCdfOwnerShift = 8;
-
-// cdf_pair_incompatible: some lane is valid at both ends with opposite sides
-__device__ __forceinline__ bool cdf_incompatible(int pc, int nt) {
-    return ((pc & nt & 0x55) & ((pc ^ nt) >> 1)) != 0;
-}
-
-__device__ __forceinline__ size_t node_id(const PK &k, const Stencil &s, int i, int j, int kk) {
-    return ((size_t)(s.b[0] + i) * k.ng + (s.b[1] + j)) * k.ng + (s.b[2] + kk);
-}
-
-// cdf_stencil_near: a 4^3 block under the stencil holds tags now or at the last stamp
-// k.cblock is null when the early-out is switched off (model.cdf_mask_off,
-// mpm_utils.py:856, 980): every particle then takes the full 27-node scan
-__device__ __forceinline__ bool cdf_near(const PK &k, const Stencil &s) {
-    if (!k.cblock) return true;
-    for (int bi = s.b[0] >> 2; bi <= (s.b[0] + 2) >> 2; ++bi)
-        for (int bj = s.b[1] >> 2; bj <= (s.b[1] + 2) >> 2; ++bj)
-            for (int bk = s.b[2] >> 2; bk <= (s.b[2] + 2) >> 2; ++bk)
-                if (__ldg(k.cblock + ((size_t)bi * k.cnb + bj) * k.cnb + bk) != 0) return true;
-    return false;
-}
-
-// One pass over the 27 stencil nodes of a stamp: caches the node tags (node index
-// (i*3 + j)*3 + kk) and forms cdf_particle_tag's lane votes, the weighted signed
-// distances of the valid nodes (mpm_utils.py:678-713); with `ghost`, it also forms
-// the owner-lane sums of cdf_particle_ghost (:733-771) in the same node order.
-struct CdfScan {
-    int tag[27];
-    float votes[4];
-    int side1[4], side0[4];   // per lane: stencil nodes (bit (i*3 + j)*3 + kk) valid on side +, side -
-    float d_hat, n_acc[3], best_w;
-    int lane_p;
-};
-
-template <bool GHOST>
-__device__ __forceinline__ void cdf_scan(const PK &k, const Stencil &s, const int *T, const float *D, CdfScan &c) {
-    c.votes[0] = c.votes[1] = c.votes[2] = c.votes[3] = 0.f;
-#pragma unroll
-    for (int l = 0; l < 4; ++l) c.side1[l] = c.side0[l] = 0;
-    c.d_hat = 0.f;
-    c.n_acc[0] = c.n_acc[1] = c.n_acc[2] = 0.f;
-    c.best_w = 0.f;
-    c.lane_p = 0;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-#pragma unroll
-            for (int kk = 0; kk < 3; ++kk) {
-                const size_t id = node_id(k, s, i, j, kk);
-                const int t = T[id];
-                c.tag[(i * 3 + j) * 3 + kk] = t;
-                if (t == 0) continue;
-                const float w = s.w[0][i] * s.w[1][j] * s.w[2][kk];
-                const float dd = D[id];
-                const int nbit = 1 << ((i * 3 + j) * 3 + kk);
-#pragma unroll
-                for (int l = 0; l < 4; ++l)
-                    if ((t >> (2 * l)) & 1) {
-                        const bool plus = (t >> (2 * l + 1)) & 1;
-                        c.votes[l] += w * dd * (plus ? 1.0f : -1.0f);
-                        if (plus) c.side1[l] |= nbit;
-                        else c.side0[l] |= nbit;
-                    }
-                if (GHOST) {
-                    const int own = (t >> kCdfOwnerShift) & 3;
-                    if (((t >> (2 * own)) & 1) == 0) continue;
-                    const float sgn = ((t >> (2 * own + 1)) & 1) ? 1.0f : -1.0f;
-                    c.d_hat += w * sgn * dd;
-                    const float dw[3] = {s.dw[0][i] * s.w[1][j] * s.w[2][kk], s.w[0][i] * s.dw[1][j] * s.w[2][kk],
-                                         s.w[0][i] * s.w[1][j] * s.dw[2][kk]};
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) c.n_acc[a] += dw[a] * k.inv_dx * sgn * dd;
-                    if (w > c.best_w) { c.best_w = w; c.lane_p = own; }
-                }
-            }
-}
-
-// the particle tag from the votes: valid per lane where a valid node was seen, side
-// from the sign of the vote
-__device__ __forceinline__ int cdf_vote_tag(const CdfScan &c) {
-    int pc = 0;
-#pragma unroll
-    for (int l = 0; l < 4; ++l)
-        if ((c.side1[l] | c.side0[l]) != 0) pc |= (1 << (2 * l)) | ((c.votes[l] >= 0.0f ? 1 : 0) << (2 * l + 1));
-    return pc;
-}
-
-// the stencil nodes incompatible with tag pc (cdf_incompatible of each node's tag)
-__device__ __forceinline__ int cdf_mask(int pc, const CdfScan &c) {
-    int m = 0;
-#pragma unroll
-    for (int l = 0; l < 4; ++l)
-        if ((pc >> (2 * l)) & 1) m |= ((pc >> (2 * l + 1)) & 1) ? c.side0[l] : c.side1[l];
-    return m;
-}
-
-// cdf_persist_tag: a lane the particle already carried keeps its side
-__device__ __forceinline__ int cdf_persist(int old, int fresh) {
-    int pc = 0;
-#pragma unroll
-    for (int l = 0; l < 4; ++l)
-        if ((fresh >> (2 * l)) & 1) {
-            int side_bit = 1 << (2 * l + 1);
-            pc |= (1 << (2 * l)) | (((old >> (2 * l)) & 1) ? (old & side_bit) : (fresh & side_bit));
-        }
-    return pc;
-}
-
-// cdf_particle_ghost (mpm_utils.py:733-816): the velocity the particle reads from
-// nodes across the surface. Surface normal and distance come from the owner-lane
-// sums of the scan; the tangential part follows the surface type (sticky, slip,
-// separable Coulomb with a capped impulse) plus a separation push when the
-// particle sits within 0.05 dx of the surface.
-__device__ void cdf_ghost(const PK &k, const CdfScan &c, const float *xp, const float *vp, int pc, const float *grav,
-                          float *ghost) {
-    float vf[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) { vf[a] = vp[a] + grav[a] * k.dt; ghost[a] = vf[a]; }
-    const float nl = sqrtf(c.n_acc[0] * c.n_acc[0] + c.n_acc[1] * c.n_acc[1] + c.n_acc[2] * c.n_acc[2]);
-    if (!(nl > 1.0e-12f)) return;
-    const int lane_p = c.lane_p;
-    const float side = ((pc >> (2 * lane_p + 1)) & 1) ? 1.0f : -1.0f;
-    float n[3], vs[3], vrel[3];
-    const float *cp = k.lanes.c_prev[lane_p], *vl = k.lanes.v_prev[lane_p], *wl = k.lanes.w_prev[lane_p];
-    float rel[3] = {xp[0] - cp[0], xp[1] - cp[1], xp[2] - cp[2]};
-#pragma unroll
-    for (int a = 0; a < 3; ++a) n[a] = c.n_acc[a] / nl * side;
-    vs[0] = vl[0] + (wl[1] * rel[2] - wl[2] * rel[1]);
-    vs[1] = vl[1] + (wl[2] * rel[0] - wl[0] * rel[2]);
-    vs[2] = vl[2] + (wl[0] * rel[1] - wl[1] * rel[0]);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) vrel[a] = vf[a] - vs[a];
-    const float vn = vrel[0] * n[0] + vrel[1] * n[1] + vrel[2] * n[2];
-    float vt[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) vt[a] = vrel[a] - n[a] * vn;
-    float cc = 0.0f;
-    const float d_side = c.d_hat * side, eps = 0.05f * k.dx;
-    if (d_side < eps) cc = fminf((eps - d_side) / k.dt, 0.5f * k.dx / k.dt);
-    const int stype = k.lanes.type[lane_p];
-    if (stype == 0) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) ghost[a] = vs[a] + n[a] * cc;
-    } else if (stype == 1) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) ghost[a] = vs[a] + vt[a] + n[a] * cc;
-    } else {
-        const float dvn = fmaxf(-vn, 0.0f) + cc;
-        const float tl = sqrtf(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
-        if (tl > 1.0e-12f && dvn > 0.0f) {
-            const float sc = fmaxf(0.0f, tl - k.lanes.fric[lane_p] * dvn) / tl;
-#pragma unroll
-            for (int a = 0; a < 3; ++a) vt[a] *= sc;
-        }
-        const float vnp = fmaxf(vn, 0.0f);
-#pragma unroll
-        for (int a = 0; a < 3; ++a) ghost[a] = vs[a] + vt[a] + n[a] * vnp + n[a] * cc;
-    }
-}
-
-// P2G with the CPIC mask: deposits into nodes incompatible with the particle are
-// withheld from the grid and added to the owner lane's reaction (force and torque
-// about the lane centre, summed per thread in float64 before one flush per lane).
-__device__ void cdf_deposit_all(const PK &k, const Stencil &s, int p, const float *v, const float *C, const float *S,
-                                int pc, const int *tags) {
-    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    int acc_own = -1;
-    auto flush = [&]() {
-        if (acc_own < 0) return;
-        double *w = k.cwrench + ((size_t)blockIdx.x * GBMPM_MAX_CDF + acc_own) * 6;
-#pragma unroll
-        for (int a = 0; a < 6; ++a) { atomicAdd(w + a, acc[a]); acc[a] = 0.0; }
-    };
-    p2g_core(k, s, p, v, C, S, [&](int i, int j, int kk, float4 val) {
-        size_t id = node_id(k, s, i, j, kk);
-        int nt = tags[(i * 3 + j) * 3 + kk];
-        if (cdf_incompatible(pc, nt)) {
-            int own = (nt >> kCdfOwnerShift) & 3;
-            if (own != acc_own) { flush(); acc_own = own; }
-            const float *cc = k.lanes.c_cur[own];
-            float r[3] = {(float)(s.b[0] + i) * k.dx - cc[0], (float)(s.b[1] + j) * k.dx - cc[1],
-                          (float)(s.b[2] + kk) * k.dx - cc[2]};
-            acc[0] += (double)val.x;
-            acc[1] += (double)val.y;
-            acc[2] += (double)val.z;
-            acc[3] += (double)(r[1] * val.z - r[2] * val.y);
-            acc[4] += (double)(r[2] * val.x - r[0] * val.z);
-            acc[5] += (double)(r[0] * val.y - r[1] * val.x);
-            return;
-        }
-        atomicAdd(k.gmv + id, val);
-    });
-    flush();
-    mark_stencil_blocks(k, s);
-}
-
-// Particle modifiers before the stress and P2G of a substep (the pre-P2G operations
-// and velocity modifiers of p2g2p, mpm_solver_warp.py:1182-1196; kernels
-// :2385-2540): impulses first, then velocity overrides, each in list order, on the
-// float32 time window [start, end). Returns true when v changed.
-__device__ bool apply_modifiers(const PK &k, int mask, const float *x, float mass, float *v) {
-    const float t = (float)k.sub_time[k.sub];
-    bool changed = false;
-    for (int pass = 0; pass < 2; ++pass)
-        for (int m = 0; m < k.n_mods; ++m) {
-            if (!((mask >> m) & 1)) continue;
-            const gbmpm_modifier &d = k.mods[m];
-            if ((d.kind == 0) != (pass == 0)) continue;
-            if (!(t >= d.start_time && t < d.end_time)) continue;
-            changed = true;
-            if (d.kind == 0) {
-                const float imp[3] = {d.vec[0] / mass, d.vec[1] / mass, d.vec[2] / mass};
-#pragma unroll
-                for (int a = 0; a < 3; ++a) v[a] = v[a] + imp[a] * k.dt;
-            } else if (d.kind == 1) {
-#pragma unroll
-                for (int a = 0; a < 3; ++a) v[a] = d.vec[a];
-            } else {
-                const float off[3] = {x[0] - d.point[0], x[1] - d.point[1], x[2] - d.point[2]};
-                const float on = off[0] * d.normal[0] + off[1] * d.normal[1] + off[2] * d.normal[2];
-                const float hz[3] = {off[0] - on * d.normal[0], off[1] - on * d.normal[1], off[2] - on * d.normal[2]};
-                const float hd = sqrtf(hz[0] * hz[0] + hz[1] * hz[1] + hz[2] * hz[2]);
-                const float cosine = (off[0] * d.axis1[0] + off[1] * d.axis1[1] + off[2] * d.axis1[2]) / hd;
-                float theta = acosf(fminf(fmaxf(cosine, -1.0f), 1.0f));
-                if (!(off[0] * d.axis2[0] + off[1] * d.axis2[1] + off[2] * d.axis2[2] > 0.0f)) theta = -theta;
-                const float a1 = -hd * sinf(theta) * d.rotation_scale;
-                const float a2 = hd * cosf(theta) * d.rotation_scale;
-#pragma unroll
-                for (int a = 0; a < 3; ++a)
-                    v[a] = a1 * d.axis1[a] + a2 * d.axis2[a] + d.translation_scale * d.normal[a];
-            }
-        }
-    return changed;
-}
-
-// ---- direct kernel: one thread per particle, global gather and atomics ------
-// One kernel serves every particle pass of the schedule; `mode` selects the
-// stages (G2P, STRESS, P2G): the fused interior pass is G2P|STRESS|P2G, the tick
-// prologue STRESS|P2G and the epilogue G2P.
-template <bool SOLIDS>
-__global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) {
-    if ((mode & PASS_RESET_LISTS) && blockIdx.x == 0 && threadIdx.x == 0) {
-        k.blk_count[0] = 0;
-        k.blk_count[1] = 0;
-    }
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= k.n) return;
-    if (k.sel && k.sel[p] != 0) return;
-    const int mat = k.mat[p];
-    float x[3] = {k.x[3 * p], k.x[3 * p + 1], k.x[3 * p + 2]};
-    float v[3], C[9], L[9], Ft[9], S[9];
-    bool gathered = false;
-    int ptag = 0;   // CPIC particle tag carried from G2P into P2G
-    if ((mode & PASS_G2P) && mat != 7 && mat != 8) {
-        Stencil s;
-        stencil(x, k.inv_dx, s);
-        if (!stencil_ok(s, k.ng, k.periodic_x)) {
-            set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
-            return;
-        }
-        CdfScan cs;
-        if (k.cdf_on) {
-            int pc = 0;
-            if (cdf_near(k, s)) {
-                cdf_scan<true>(k, s, k.ctag_prev, k.cd_prev, cs);
-                pc = cdf_persist(k.ptag[p], cdf_vote_tag(cs));
-            }
-            k.ptag[p] = pc;
-            ptag = pc;
-        }
-        if (ptag != 0) {
-            const float *vi = k.v + 3 * (size_t)p;
-            const float vp[3] = {vi[0], vi[1], vi[2]};
-            float gh[3];
-            cdf_ghost(k, cs, x, vp, ptag, k.grav, gh);
-            const float4 g4 = make_float4(gh[0], gh[1], gh[2], 0.0f);
-            g2p_core(k, s, [&](int i, int j, int kk) {
-                return cdf_incompatible(ptag, cs.tag[(i * 3 + j) * 3 + kk]) ? g4 : global_fetch(k, s, i, j, kk);
-            }, v, C, L);
-        } else {
-            g2p_core(k, s, [&](int i, int j, int kk) { return global_fetch(k, s, i, j, kk); }, v, C, L);
-        }
-        g2p_finish<false>(k, p, x, v, L, Ft);
-        gathered = true;
-    } else if (k.cdf_on && (mode & PASS_P2G)) {
-        ptag = k.ptag[p];
-    }
-    if (gathered) {
-        float *xo = k.x + 3 * (size_t)p;
-        xo[0] = x[0]; xo[1] = x[1]; xo[2] = x[2];
-        if (!(mode & (PASS_STRESS | PASS_P2G)) || (mode & PASS_STORE_VC)) {
-            float *vo = k.v + 3 * (size_t)p;
-            vo[0] = v[0]; vo[1] = v[1]; vo[2] = v[2];
-            mat_store(k.C + 9 * (size_t)p, C);
-        }
-        if (!(mode & PASS_STRESS)) {
-            mat_store(k.L + 9 * (size_t)p, L);
-            mat_store(k.Ft + 9 * (size_t)p, Ft);
-        }
-    }
-    if (mode & PASS_STRESS) {
-        if (!gathered) {
-            mat_load(k.Ft + 9 * (size_t)p, Ft);
-            mat_load(k.L + 9 * (size_t)p, L);
-        }
-        float Fn[9];
-        stress_update<SOLIDS>(k, p, mat, Ft, L, Fn, S);
-        mat_store(k.F + 9 * (size_t)p, Fn);
-        if (mode & PASS_STORE_ALL) mat_store(k.S + 9 * (size_t)p, S);
-    }
-    if (mode & PASS_P2G) {
-        if (!(mode & PASS_STRESS)) mat_load(k.S + 9 * (size_t)p, S);
-        if (!gathered) {
-            const float *vi = k.v + 3 * (size_t)p;
-            v[0] = vi[0]; v[1] = vi[1]; v[2] = vi[2];
-            mat_load(k.C + 9 * (size_t)p, C);
-        }
-        if (k.n_mods && k.mod_mask) {
-            const int mm = k.mod_mask[p];
-            if (mm && apply_modifiers(k, mm, x, k.mass[p], v)) {
-                float *vo = k.v + 3 * (size_t)p;
-                vo[0] = v[0]; vo[1] = v[1]; vo[2] = v[2];
-            }
-        }
-        if (k.rigid_defer && mat == 8) return;   // deposits after the rigid update
-        Stencil s;
-        stencil(x, k.inv_dx, s);
-        if (!stencil_ok(s, k.ng, k.periodic_x)) {
-            set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
-            return;
-        }
-        int pc = 0;
-        CdfScan cs;
-        if (k.cdf_on && cdf_near(k, s)) {
-            cdf_scan<false>(k, s, k.ctag, k.cd, cs);
-            pc = cdf_persist(ptag, cdf_vote_tag(cs));
-        }
-        if (pc != 0) cdf_deposit_all(k, s, p, v, C, S, pc, cs.tag);
-        else global_deposit_all(k, s, p, v, C, S);
-    }
-}
-
-// ---- tiled kernel: block-sorted particles, shared-memory gather tile, run-wise scatter
-// Particles arrive sorted by (4^3 block, cell); a CTA owns Tile<CDF>::threads
-// consecutive particles, one per thread.
-//  * Gather: the CTA reduces the bounding box of its stencils; when it holds at
-//    most Tile<CDF>::gather_cap nodes the grid velocity of that box is copied to
-//    shared memory and the 27-node gathers read it there (neighbouring threads
-//    share nodes, so most reads are broadcasts).
-//  * Scatter: each particle leaves a 40-float record in shared memory. Runs of
-//    consecutive particles whose stencils share the same base node (the same
-//    cell) are scattered together, three runs per warp: nine lanes take one
-//    (i, j) node line each, sum the run's contributions to its three nodes from
-//    shared reads, and issue one red.global.add.v4.f32 per node. Global atomics
-//    drop from 27 per particle to 27 per run, and no shared-memory atomics are
-//    needed.
-// The plain pass runs 128-thread CTAs (six per SM); the CPIC pass, whose larger
-// body runs best with fewer, wider CTAs, 256 (three per SM).
-constexpr int kTileThreads = 128;
-constexpr int kTileThreadsCdf = 256;
-constexpr int kRec = 40;                  // floats per particle scatter record (10 float4)
-// record stride in shared memory: 44 floats = 176 B, so the 16-byte stores of eight
-// consecutive lanes land on disjoint bank groups (a 160 B stride pairs them up)
-constexpr int kRecStride = 44;
-template <bool CDF>
-struct Tile {
-    static constexpr int threads = CDF ? kTileThreadsCdf : kTileThreads;
-    static constexpr int gather_cap = 6 * threads;   // nodes in the shared gather tile (16 B each)
-    static constexpr int smem_floats =
-        (gather_cap * 4 > threads * kRecStride) ? gather_cap * 4 : threads * kRecStride;
-    static_assert(gather_cap * 4 + 11 * threads <= smem_floats, "prefetch slots fit past the gather tile");
-};
-// the CPIC reaction partials are indexed by CTA; they are sized for the narrower of
-// the direct and the tiled CPIC launches
-constexpr int kCdfCtaThreads = kParticleThreads < kTileThreadsCdf ? kParticleThreads : kTileThreadsCdf;
-
-struct TileBox {
-    int lo[3], e[3];
-    int vol;
-    bool fits;
-};
-
-template <int TH>
-__device__ __forceinline__ void block_box(const int *b, bool valid, TileBox &box, int (*s_red)[6], int cap) {
-    int v[6];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        v[a] = valid ? b[a] : INT_MAX;
-        v[3 + a] = valid ? -b[a] : INT_MAX;   // max as min of negatives
-    }
-#pragma unroll
-    for (int a = 0; a < 6; ++a)
-        for (int o = 16; o > 0; o >>= 1) v[a] = min(v[a], __shfl_xor_sync(0xffffffffu, v[a], o));
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) {
-#pragma unroll
-        for (int a = 0; a < 6; ++a) s_red[w][a] = v[a];
-    }
-    __syncthreads();
-    int r[6];
-#pragma unroll
-    for (int a = 0; a < 6; ++a) r[a] = INT_MAX;
-    for (int ww = 0; ww < TH / 32; ++ww)
-#pragma unroll
-        for (int a = 0; a < 6; ++a) r[a] = min(r[a], s_red[ww][a]);
-    __syncthreads();
-    bool any = r[0] != INT_MAX;
-    long long vol = 1;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        box.lo[a] = any ? r[a] : 0;
-        box.e[a] = any ? (-r[3 + a]) - r[a] + 3 : 0;
-        vol *= (long long)box.e[a];
-    }
-    box.vol = any ? (int)min(vol, (long long)INT_MAX) : 0;
-    box.fits = any && vol <= cap;
-}
-
-// quadratic B-spline weight and its derivative for node offset o of one axis
-__device__ __forceinline__ void bspline_o(float fx, int o, float &w, float &dw) {
-    float t0 = 1.5f - fx, t1 = fx - 1.0f, t2 = fx - 0.5f;
-    float w0 = 0.5f * (t0 * t0), w1 = 0.75f - t1 * t1, w2 = 0.5f * (t2 * t2);
-    w = (o == 0) ? w0 : ((o == 1) ? w1 : w2);
-    dw = (o == 0) ? -t0 : ((o == 1) ? -2.0f * t1 : t2);
-}
-
-// CDF adds the CPIC branches of the direct kernel: the gather reads the ghost
-// velocity at nodes incompatible with the particle, and scatter runs are keyed by
-// (base cell, particle tag) so each run deposits under one mask, its blocked nodes
-// becoming the owner lane's reaction.
-template <bool SOLIDS, int MINB, bool CDF = false>
-__global__ void __launch_bounds__(Tile<CDF>::threads, MINB * 256 / Tile<CDF>::threads)
-    k_particles_tiled(PK k, int mode) {
-    constexpr int kTileThreads = Tile<CDF>::threads;
-    constexpr int kGatherCap = Tile<CDF>::gather_cap;
-    __shared__ __align__(16) float s_mem[Tile<CDF>::smem_floats];
-    __shared__ int s_key[kTileThreads];
-    __shared__ int s_pc[CDF ? kTileThreads : 1];
-    __shared__ int s_mask[CDF ? kTileThreads : 1];
-    __shared__ int s_seg[kTileThreads + 1];
-    __shared__ int s_wcnt[kTileThreads / 32];
-    __shared__ int s_red[kTileThreads / 32][6];
-    // F, mass and volume of a gather pass's particle, fetched asynchronously at the
-    // start so that their L2 round trip overlaps the tile box, the tile load and the
-    // gather (a gather pass starts before its wait: nothing still running writes
-    // them). The slots lie past the gather tile, in the record area, and are read
-    // into registers before the barrier that ends the gather.
-    float(*s_pf)[kTileThreads] = reinterpret_cast<float(*)[kTileThreads]>(s_mem + kGatherCap * 4);
-    const int t = threadIdx.x;
-    const int lane = t & 31, warp = t >> 5;
-    const int p = blockIdx.x * kTileThreads + t;
-    bool live = p < k.n && !(k.sel && k.sel[p] != 0);
-    const int mat = live ? k.mat[p] : 0;
-    if (!(mode & PASS_G2P)) {   // without a gather, x and the stress inputs are what the previous pass wrote
-        pdl_wait();
-        pdl_trigger();
-    }
-    const bool pf = (mode & PASS_G2P) && live;
-    if (pf) {
-#pragma unroll
-        for (int c = 0; c < 9; ++c) cp_async4(&s_pf[c][t], k.F + (size_t)c * k.n + p);
-        if (mode & PASS_P2G) {
-            cp_async4(&s_pf[9][t], k.mass + p);
-            cp_async4(&s_pf[10][t], k.vol + p);
-        }
-    }
-    float x[3] = {0.f, 0.f, 0.f};
-    if (live) fld_load<true, 3>(k.x, k.n, p, x);
-    float v[3] = {0.f, 0.f, 0.f}, C[9], L[9], Ft[9], S[9];
-    float Fpf[9], mpf = 0.f, vpf = 0.f;
-    bool gathered = false;
-    int ptag = 0;   // CPIC particle tag carried from the gather into the scatter
-    if (mode & PASS_G2P) {
-        bool want = live && mat != 7 && mat != 8;
-        Stencil s;
-        stencil(x, k.inv_dx, s);
-        if (want && !stencil_ok(s, k.ng, k.periodic_x)) {
-            set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
-            want = false;
-            live = false;
-        }
-        // CPIC: the gather's scan (previous stamp at this position) is the scan the
-        // last scatter made (current stamp then, at the same position), so its
-        // result comes from the cache: the tag, the mask of incompatible stencil
-        // nodes and the owner-lane sums of the ghost velocity.
-        int gmask = 0;
-        float4 g4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (CDF && want) {
-            float old;
-            fld_load<true, 1>(reinterpret_cast<float *>(k.ptag), k.n, p, &old);
-            ptag = __float_as_int(old);
-            if (ptag != 0) {
-                CdfScan cs;
-                float cch[5], vp[3], gh[3];
-                fld_load<true, 5>(k.ccache, k.n, p, cch);
-                const int mb = __float_as_int(cch[0]);
-                gmask = mb & 0x7ffffff;
-                cs.lane_p = (mb >> 27) & 3;
-                cs.d_hat = cch[1];
-                cs.n_acc[0] = cch[2]; cs.n_acc[1] = cch[3]; cs.n_acc[2] = cch[4];
-                fld_load<true, 3>(k.v, k.n, p, vp);
-                cdf_ghost(k, cs, x, vp, ptag, k.grav, gh);
-                g4 = make_float4(gh[0], gh[1], gh[2], 0.0f);
-            }
-        }
-        TileBox box;
-        block_box<kTileThreads>(s.b, want, box, s_red, kGatherCap);
-        pdl_wait();   // the grid velocities come from the grid pass before this one
-        pdl_trigger();
-        if ((mode & PASS_RESET_LISTS) && blockIdx.x == 0 && threadIdx.x == 0) {
-            k.blk_count[0] = 0;
-            k.blk_count[1] = 0;
-        }
-        float4 *s_tile = reinterpret_cast<float4 *>(s_mem);
-        // the prefetched fields, taken into registers before the record area is reused
-        auto take_prefetch = [&]() {
-            if (pf) {
-                cp_async_wait_all();
-#pragma unroll
-                for (int c = 0; c < 9; ++c) Fpf[c] = s_pf[c][t];
-                mpf = s_pf[9][t];
-                vpf = s_pf[10][t];
-            }
-        };
-        if (box.fits) {
-            // one thread per (x, y) row of the box: the row's nodes are contiguous in
-            // the grid and in the tile, and all its 16-byte copies are in flight at once
-            const int rows = box.e[0] * box.e[1];
-            for (int r = t; r < rows; r += kTileThreads) {
-                const int qx = r / box.e[1], qy = r - qx * box.e[1];
-                const float4 *src = k.gv + ((size_t)(box.lo[0] + qx) * k.ng + (box.lo[1] + qy)) * k.ng + box.lo[2];
-                float4 *dst = s_tile + r * box.e[2];
-                for (int qz = 0; qz < box.e[2]; ++qz) cp_async16(dst + qz, src + qz);
-            }
-            cp_async_wait_all();
-            __syncthreads();
-            if (want) {
-                const int o0 = s.b[0] - box.lo[0], o1 = s.b[1] - box.lo[1], o2 = s.b[2] - box.lo[2];
-                // one copy of the unrolled gather serves masked and unmasked particles
-                g2p_core(k, s, [&](int i, int j, int kk) {
-                    const float4 t4 = s_tile[((o0 + i) * box.e[1] + (o1 + j)) * box.e[2] + (o2 + kk)];
-                    return (CDF && ((gmask >> ((i * 3 + j) * 3 + kk)) & 1)) ? g4 : t4;
-                }, v, C, L);
-            }
-            take_prefetch();
-            __syncthreads();
-        } else {   // box.fits is uniform over the CTA, so is this branch and its barrier
-            if (want)
-                g2p_core(k, s, [&](int i, int j, int kk) {
-                    const float4 t4 = global_fetch(k, s, i, j, kk);
-                    return (CDF && ((gmask >> ((i * 3 + j) * 3 + kk)) & 1)) ? g4 : t4;
-                }, v, C, L);
-            take_prefetch();
-            __syncthreads();
-        }
-        if (want) {
-            g2p_finish<true>(k, p, x, v, L, Ft, Fpf);
-            gathered = true;
-            fld_store<true, 3>(k.x, k.n, p, x);
-            if (!(mode & (PASS_STRESS | PASS_P2G)) || (mode & PASS_STORE_VC)) {
-                fld_store<true, 3>(k.v, k.n, p, v);
-                fld_store<true, 9>(k.C, k.n, p, C);
-            }
-            if (!(mode & PASS_STRESS)) {
-                fld_store<true, 9>(k.L, k.n, p, L);
-                fld_store<true, 9>(k.Ft, k.n, p, Ft);
-            }
-        }
-    }
-    if ((mode & PASS_STRESS) && live) {
-        if (!gathered) {
-            fld_load<true, 9>(k.Ft, k.n, p, Ft);
-            fld_load<true, 9>(k.L, k.n, p, L);
-        }
-        float Fn[9];
-        stress_update<SOLIDS>(k, p, mat, Ft, L, Fn, S);
-        fld_store<true, 9>(k.F, k.n, p, Fn);
-        if (mode & PASS_STORE_ALL) fld_store<true, 9>(k.S, k.n, p, S);
-    }
-    if (!(mode & PASS_P2G)) return;
-    pdl_wait();   // the scatter target and block lists are the grid pass's (no-op after the gather's wait)
-    pdl_trigger();
-    if (live) {
-        if (!(mode & PASS_STRESS)) fld_load<true, 9>(k.S, k.n, p, S);
-        if (!gathered) {
-            fld_load<true, 3>(k.v, k.n, p, v);
-            fld_load<true, 9>(k.C, k.n, p, C);
-            if (CDF) {
-                float old;
-                fld_load<true, 1>(reinterpret_cast<float *>(k.ptag), k.n, p, &old);
-                ptag = __float_as_int(old);
-            }
-        }
-    }
-    if (live && k.n_mods && k.mod_mask) {
-        const int mm = k.mod_mask[p];
-        if (mm && apply_modifiers(k, mm, x, k.mass[p], v)) fld_store<true, 3>(k.v, k.n, p, v);
-    }
-    Stencil s;
-    stencil(x, k.inv_dx, s);
-    bool want = live && !(k.rigid_defer && mat == 8);   // rigid particles deposit after the rigid update
-    if (want && !stencil_ok(s, k.ng, k.periodic_x)) {
-        set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
-        want = false;
-    }
-    int pcs = 0, pmask = 0;   // CPIC tag at the current stamp, mask of incompatible nodes
-    if (CDF && want) {
-        if (cdf_near(k, s)) {
-            CdfScan cs;
-            cdf_scan<true>(k, s, k.ctag, k.cd, cs);
-            pcs = cdf_persist(ptag, cdf_vote_tag(cs));
-            if (pcs != 0) {
-                pmask = cdf_mask(pcs, cs);
-                const float cch[5] = {__int_as_float(pmask | (cs.lane_p << 27)), cs.d_hat, cs.n_acc[0],
-                                      cs.n_acc[1], cs.n_acc[2]};
-                fld_store<true, 5>(k.ccache, k.n, p, cch);
-            }
-        }
-        const float pcf = __int_as_float(pcs);
-        fld_store<true, 1>(reinterpret_cast<float *>(k.ptag), k.n, p, &pcf);
-    }
-    if (CDF) { s_pc[t] = pcs; s_mask[t] = pmask; }
-    // ---- scatter record (40 floats, 16-byte aligned): [0..11] the x and y weights and
-    // derivatives a lane indexes by its node line (wx[3], wy[3], dwx[3], dwy[3]);
-    // [12..39] what every lane of a particle reads, packed for seven float4 loads:
-    // wz[3], m | dwz[3], b0 | b1, b2, c00, c01 | c02, c10, c11, c12 | c20, c21, c22,
-    // A00 | A01, A02, A10, A11 | A12, A20, A21, A22, with b = m v - m C fx dx the
-    // affine momentum base, c = m C dx and A = -vol dt/dx stress
-    if (want) {
-        float Cr[9];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) Cr[i] = C[i];
-        if (k.rpic != 0.0f) {
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j)
-                    Cr[3 * i + j] = (k.rpic < -0.001f) ? 0.0f
-                                    : (1.0f - k.rpic) * C[3 * i + j] + k.rpic / 2.0f * (C[3 * i + j] - C[3 * j + i]);
-        }
-        const float m = (pf && (mode & PASS_P2G)) ? mpf : k.mass[p];
-        const float fs = -((pf && (mode & PASS_P2G)) ? vpf : k.vol[p]) * k.dt * k.inv_dx;
-        float rec[kRec];
-#pragma unroll
-        for (int o = 0; o < 3; ++o) {
-            rec[o] = s.w[0][o];
-            rec[3 + o] = s.w[1][o];
-            rec[6 + o] = s.dw[0][o];
-            rec[9 + o] = s.dw[1][o];
-            rec[12 + o] = s.w[2][o];
-            rec[16 + o] = s.dw[2][o];
-        }
-        rec[15] = m;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            float c0 = m * Cr[3 * a] * k.dx, c1 = m * Cr[3 * a + 1] * k.dx, c2 = m * Cr[3 * a + 2] * k.dx;
-            rec[19 + a] = m * v[a] - (c0 * s.fx[0] + c1 * s.fx[1] + c2 * s.fx[2]);
-            rec[22 + 3 * a] = c0; rec[23 + 3 * a] = c1; rec[24 + 3 * a] = c2;
-            rec[31 + 3 * a] = fs * S[3 * a]; rec[32 + 3 * a] = fs * S[3 * a + 1]; rec[33 + 3 * a] = fs * S[3 * a + 2];
-        }
-        float4 *dst = reinterpret_cast<float4 *>(s_mem + t * kRecStride);
-#pragma unroll
-        for (int q = 0; q < kRec / 4; ++q) dst[q] = make_float4(rec[4 * q], rec[4 * q + 1], rec[4 * q + 2], rec[4 * q + 3]);
-        s_key[t] = (s.b[0] << 20) | (s.b[1] << 10) | s.b[2];   // n_grid <= 1024 on this path
-    } else {
-        s_key[t] = -1 - t;   // a dead slot forms its own, skipped run
-    }
-    __syncthreads();
-    // ---- runs of equal base node (and CPIC tag): compact the run heads
-    const bool head = (t == 0) || (s_key[t] != s_key[t - 1]) || (CDF && s_pc[t] != s_pc[t - 1]);
-    const unsigned bal = __ballot_sync(0xffffffffu, head);
-    if (lane == 0) s_wcnt[warp] = __popc(bal);
-    __syncthreads();
-    int off = 0, total = 0;
-    for (int w = 0; w < kTileThreads / 32; ++w) {
-        int c = s_wcnt[w];
-        if (w < warp) off += c;
-        total += c;
-    }
-    if (head) s_seg[off + __popc(bal & ((1u << lane) - 1u))] = t;
-    if (t == 0) s_seg[total] = kTileThreads;
-    __syncthreads();
-    // ---- runs: a warp takes three runs at once, one per 9-lane group; lane
-    // (group, node line (i,j)) sums the three nodes k = 0..2 of its line over its
-    // run's particles and deposits them itself
-    const int g3 = lane / 9, li = (lane % 9) / 3, lj = lane % 3;
-    const float fi = (float)li, fj = (float)lj;
-    for (int sg0 = warp * 3; sg0 < total; sg0 += 3 * (kTileThreads / 32)) {
-        const int sg = sg0 + g3;
-        int q0 = 0, q1 = 0, key = -1;
-        if (lane < 27 && sg < total) {
-            q0 = s_seg[sg];
-            q1 = s_seg[sg + 1];
-            key = s_key[q0];
-        }
-        if (key < 0) q1 = q0;   // dead slot or idle lane: no particles
-        float acc[3][4];
-#pragma unroll
-        for (int kk = 0; kk < 3; ++kk) acc[kk][0] = acc[kk][1] = acc[kk][2] = acc[kk][3] = 0.f;
-#pragma unroll 1   // unrolling by two measured slower (22.01 against 21.87 ms per pour frame, 56.5 against 54.9 CPIC)
-        for (int q = q0; q < q1; ++q) {
-            const float *r = s_mem + q * kRecStride;
-            const float wxi = r[li], wyj = r[3 + lj], dwxi = r[6 + li], dwyj = r[9 + lj];
-            const float4 *r4 = reinterpret_cast<const float4 *>(r);
-            float inv[28];
-#pragma unroll
-            for (int h = 0; h < 7; ++h) {
-                const float4 f4 = r4[3 + h];
-                inv[4 * h] = f4.x; inv[4 * h + 1] = f4.y; inv[4 * h + 2] = f4.z; inv[4 * h + 3] = f4.w;
-            }
-            // inv[i] = rec[12 + i]
-            const float u = wxi * wyj, ux = dwxi * wyj, uy = wxi * dwyj;
-            const float wz0 = inv[0], wz1 = inv[1], wz2 = inv[2], dz0 = inv[4], dz1 = inv[5], dz2 = inv[6];
-            const float m = inv[3];
-            float P[3], Q[3], R[3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                P[a] = u * (inv[7 + a] + inv[10 + 3 * a] * fi + inv[11 + 3 * a] * fj) + inv[19 + 3 * a] * ux +
-                       inv[20 + 3 * a] * uy;
-                Q[a] = u * inv[12 + 3 * a];
-                R[a] = u * inv[21 + 3 * a];
-            }
-            const float um = u * m;
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                acc[0][a] += wz0 * P[a] + dz0 * R[a];
-                acc[1][a] += wz1 * (P[a] + Q[a]) + dz1 * R[a];
-                acc[2][a] += wz2 * (P[a] + 2.0f * Q[a]) + dz2 * R[a];
-            }
-            acc[0][3] += wz0 * um;
-            acc[1][3] += wz1 * um;
-            acc[2][3] += wz2 * um;
-        }
-        if (q1 > q0) {
-            const int bx = key >> 20, by = (key >> 10) & 1023, bz = key & 1023;
-            const int gx = bx + li, gy = by + lj;
-            const int lmask = CDF ? (s_mask[q0] >> ((li * 3 + lj) * 3)) & 7 : 0;   // the run's mask, this line
-            int marked = -1;   // 4^3 block (z index) this lane marked last
-#pragma unroll
-            for (int kk = 0; kk < 3; ++kk) {
-                if (CDF && lmask != 0) {
-                    if ((lmask >> kk) & 1) {   // blocked: the owner lane's reaction
-                        const int nt = __ldg(k.ctag + ((size_t)gx * k.ng + gy) * k.ng + (bz + kk));
-                        const int own = (nt >> kCdfOwnerShift) & 3;
-                        const float *cc = k.lanes.c_cur[own];
-                        const float r[3] = {(float)gx * k.dx - cc[0], (float)gy * k.dx - cc[1],
-                                            (float)(bz + kk) * k.dx - cc[2]};
-                        double *w = k.cwrench + ((size_t)blockIdx.x * GBMPM_MAX_CDF + own) * 6;
-                        atomicAdd(w + 0, (double)acc[kk][0]);
-                        atomicAdd(w + 1, (double)acc[kk][1]);
-                        atomicAdd(w + 2, (double)acc[kk][2]);
-                        atomicAdd(w + 3, (double)(r[1] * acc[kk][2] - r[2] * acc[kk][1]));
-                        atomicAdd(w + 4, (double)(r[2] * acc[kk][0] - r[0] * acc[kk][2]));
-                        atomicAdd(w + 5, (double)(r[0] * acc[kk][1] - r[1] * acc[kk][0]));
-                        continue;
-                    }
-                }
-                if (acc[kk][0] != 0.f || acc[kk][1] != 0.f || acc[kk][2] != 0.f || acc[kk][3] != 0.f) {
-                    const int gz = bz + kk;
-                    atomicAdd(k.gmv + ((size_t)gx * k.ng + gy) * k.ng + gz,
-                              make_float4(acc[kk][0], acc[kk][1], acc[kk][2], acc[kk][3]));
-                    if ((gz >> 2) != marked) {
-                        mark_block(k, gx >> 2, gy >> 2, gz >> 2);
-                        marked = gz >> 2;
-                    }
-                }
-            }
-        }
-    }
-}
-
-// ---- per-tick working set: block-sorted copy of the particles --------------
-// key = (4^3 block of the stencil base, cell within the block); positions are
-// clamped into the grid so every particle gets a key.
-__global__ void k_cell_keys(const float *x, int n, float inv_dx, int ng, int bd, unsigned long long *keys,
-                            int *idx) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    int b[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        float g = x[3 * (size_t)p + a] * inv_dx - 0.5f;
-        int c = isfinite(g) ? (int)floorf(fminf(fmaxf(g, 0.0f), (float)(ng - 1))) : 0;
-        b[a] = c;
-    }
-    unsigned blk = (unsigned)(((b[0] >> 2) * bd + (b[1] >> 2)) * bd + (b[2] >> 2));
-    unsigned cell = (unsigned)(((b[0] & 3) << 4) | ((b[1] & 3) << 2) | (b[2] & 3));
-    keys[p] = ((unsigned long long)blk << 6) | cell;
-    idx[p] = p;
-}
-
-struct WsField {
-    float *ext;
-    float *ws;
-    int width;
-    int back;   // copied back to the caller's buffer at the end of the tick
-};
-constexpr int kMaxWsFields = 20;
-struct WsTable {
-    WsField f[kMaxWsFields];
-    int nf;
-};
-
-// caller AoS records -> working-copy SoA components, in block-sorted order
-__global__ void k_ws_gather(WsTable T, const int *perm, int n) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const size_t src = (size_t)perm[i];
-    for (int f = 0; f < T.nf; ++f) {
-        const int w = T.f[f].width;
-        const float *a = T.f[f].ext + src * w;
-        float *b = T.f[f].ws + i;
-        for (int c = 0; c < w; ++c) b[(size_t)c * n] = a[c];
-    }
-}
-
-__global__ void k_ws_scatter(WsTable T, const int *perm, int n) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const size_t dst = (size_t)perm[i];
-    for (int f = 0; f < T.nf; ++f) {
-        if (!T.f[f].back) continue;
-        const int w = T.f[f].width;
-        const float *a = T.f[f].ws + i;
-        float *b = T.f[f].ext + dst * w;
-        for (int c = 0; c < w; ++c) b[c] = a[(size_t)c * n];
-    }
-}
-
-// -------------------------------------------------------- grid pass --------
-// capped_cylinder_sdf / revolved_glass_sdf (mpm_solver_warp.py:29-57)
-__device__ __forceinline__ float capped_cyl(float r, float z, float rad, float z0, float z1) {
-    float zc = 0.5f * (z0 + z1), hh = 0.5f * (z1 - z0);
-    float dr = r - rad, dz = fabsf(z - zc) - hh;
-    float dro = fmaxf(dr, 0.0f), dzo = fmaxf(dz, 0.0f);
-    return sqrtf(dro * dro + dzo * dzo) + fminf(fmaxf(dr, dz), 0.0f);
-}
-__device__ __forceinline__ float glass_sdf(float l0, float l1, float l2, const ColDev &c) {
-    float r = sqrtf(l0 * l0 + l1 * l1);
-    float d_outer = capped_cyl(r, l2, c.outer_r, -c.half_h, c.half_h);
-    float d_cav = capped_cyl(r, l2, c.inner_r - c.fillet, c.floor_z + c.fillet, c.half_h + c.outer_r) - c.fillet;
-    return fmaxf(d_outer, -d_cav);
-}
-__device__ __forceinline__ float trilerp(const float *vals, int res, float f0, float f1, float f2, int stride,
-                                         int comp) {
-    float fi = fminf(fmaxf(f0, 0.0f), (float)res - 1.0001f);
-    float fj = fminf(fmaxf(f1, 0.0f), (float)res - 1.0001f);
-    float fk = fminf(fmaxf(f2, 0.0f), (float)res - 1.0001f);
-    int i = (int)floorf(fi), j = (int)floorf(fj), kk = (int)floorf(fk);
-    float tx = fi - (float)i, ty = fj - (float)j, tz = fk - (float)kk;
-    auto at = [&](int a, int b, int c) { return __ldg(vals + ((((size_t)a * res + b) * res + c) * stride + comp)); };
-    float c00 = at(i, j, kk) * (1.0f - tx) + at(i + 1, j, kk) * tx;
-    float c01 = at(i, j, kk + 1) * (1.0f - tx) + at(i + 1, j, kk + 1) * tx;
-    float c10 = at(i, j + 1, kk) * (1.0f - tx) + at(i + 1, j + 1, kk) * tx;
-    float c11 = at(i, j + 1, kk + 1) * (1.0f - tx) + at(i + 1, j + 1, kk + 1) * tx;
-    float c0 = c00 * (1.0f - ty) + c10 * ty;
-    float c1 = c01 * (1.0f - ty) + c11 * ty;
-    return c0 * (1.0f - tz) + c1 * tz;
-}
-// quaternion rotation x(2w^2-1) +/- 2w (q x x) + 2 q (q . x)
-__device__ __forceinline__ void qrot(const float *q, const float *x, float *out, bool inv) {
-    float w = q[3];
-    float c = 2.0f * w * w - 1.0f;
-    float cx = q[1] * x[2] - q[2] * x[1], cy = q[2] * x[0] - q[0] * x[2], cz = q[0] * x[1] - q[1] * x[0];
-    float d = q[0] * x[0] + q[1] * x[1] + q[2] * x[2];
-    float sgn = inv ? -2.0f * w : 2.0f * w;
-    out[0] = x[0] * c + cx * sgn + q[0] * d * 2.0f;
-    out[1] = x[1] * c + cy * sgn + q[1] * d * 2.0f;
-    out[2] = x[2] * c + cz * sgn + q[2] * d * 2.0f;
-}
-
-// ---- CPIC (CDF) stamping (mpm_solver_warp.py:94-183) ---------------------------
-// The stamp decides node tags by thresholds on interpolated fields, so its
-// arithmetic is spelled out with round-to-nearest intrinsics: no contraction into
-// FMAs, every operation rounded once, as in the fp32 statement of the algorithm.
-struct CdfBox {
-    int lo[3], hi[3];   // node range [lo, hi)
-};
-
-__device__ __forceinline__ float trilerp_rn(const float *vals, int res, float f0, float f1, float f2) {
-    const float top = (float)res - 1.0001f;
-    float fi = fminf(fmaxf(f0, 0.0f), top), fj = fminf(fmaxf(f1, 0.0f), top), fk = fminf(fmaxf(f2, 0.0f), top);
-    int i = (int)floorf(fi), j = (int)floorf(fj), kk = (int)floorf(fk);
-    float tx = __fsub_rn(fi, (float)i), ty = __fsub_rn(fj, (float)j), tz = __fsub_rn(fk, (float)kk);
-    auto at = [&](int a, int b, int c) { return __ldg(vals + (((size_t)a * res + b) * res + c)); };
-    auto lerp = [](float a, float b, float t) { return __fadd_rn(__fmul_rn(a, __fsub_rn(1.0f, t)), __fmul_rn(b, t)); };
-    float c00 = lerp(at(i, j, kk), at(i + 1, j, kk), tx);
-    float c01 = lerp(at(i, j, kk + 1), at(i + 1, j, kk + 1), tx);
-    float c10 = lerp(at(i, j + 1, kk), at(i + 1, j + 1, kk), tx);
-    float c11 = lerp(at(i, j + 1, kk + 1), at(i + 1, j + 1, kk + 1), tx);
-    return lerp(lerp(c00, c10, ty), lerp(c01, c11, ty), tz);
-}
-
-// inverse quaternion rotation x(2w^2-1) - 2w (q x x) + 2 q (q . x), rounded per operation
-__device__ __forceinline__ void qrot_inv_rn(const float *q, const float *x, float *out) {
-    const float w = q[3];
-    const float c = __fsub_rn(__fmul_rn(__fmul_rn(2.0f, w), w), 1.0f);
-    const float cr[3] = {__fsub_rn(__fmul_rn(q[1], x[2]), __fmul_rn(q[2], x[1])),
-                         __fsub_rn(__fmul_rn(q[2], x[0]), __fmul_rn(q[0], x[2])),
-                         __fsub_rn(__fmul_rn(q[0], x[1]), __fmul_rn(q[1], x[0]))};
-    const float d = __fadd_rn(__fadd_rn(__fmul_rn(q[0], x[0]), __fmul_rn(q[1], x[1])), __fmul_rn(q[2], x[2]));
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        float ta = __fmul_rn(x[a], c);
-        float tb = __fmul_rn(__fmul_rn(cr[a], w), 2.0f);
-        float td = __fmul_rn(__fmul_rn(q[a], d), 2.0f);
-        out[a] = __fadd_rn(__fsub_rn(ta, tb), td);
-    }
-}
-
-// Folds the per-CTA partial reactions into the per-lane totals and clears them:
-// one warp per component.
-__global__ void k_cdf_wrench_fold(double *partial, int nctas, double *total) {
-    const int comp = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;   // lane * 6 + axis
-    if (comp >= 6 * GBMPM_MAX_CDF) return;
-    const int l = threadIdx.x & 31;
-    double acc = 0.0;
-    for (int c = l; c < nctas; c += 32) {
-        double *q = partial + (size_t)c * 6 * GBMPM_MAX_CDF + comp;
-        acc += *q;
-        *q = 0.0;
-    }
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (l == 0) total[comp] += acc;
-}
-
-__device__ __forceinline__ bool box_node(const CdfBox &b, long long idx, int &x, int &y, int &z) {
-    const long long ny = b.hi[1] - b.lo[1], nz = b.hi[2] - b.lo[2];
-    z = b.lo[2] + (int)(idx % nz);
-    long long r = idx / nz;
-    y = b.lo[1] + (int)(r % ny);
-    x = b.lo[0] + (int)(r / ny);
-    return x < b.hi[0];
-}
-
-__device__ __forceinline__ long long box_volume(const CdfBox &b) {
-    return (long long)(b.hi[0] - b.lo[0]) * (b.hi[1] - b.lo[1]) * (b.hi[2] - b.lo[2]);
-}
-
-// cdf_zero_tags over a box
-__global__ void k_cdf_clear(int *tag, float *d, CdfBox b, int ng) {
-    const long long total = box_volume(b);
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        int x, y, z;
-        if (!box_node(b, i, x, y, z)) break;
-        size_t id = ((size_t)x * ng + y) * ng + z;
-        tag[id] = 0;
-        d[id] = 1.0e9f;
-    }
-}
-
-// cdf_copy_prev over a box
-__global__ void k_cdf_copy_prev(const int *tag, const float *d, int *tag_prev, float *d_prev, CdfBox b, int ng) {
-    const long long total = box_volume(b);
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        int x, y, z;
-        if (!box_node(b, i, x, y, z)) break;
-        size_t id = ((size_t)x * ng + y) * ng + z;
-        tag_prev[id] = tag[id];
-        d_prev[id] = d[id];
-    }
-}
-
-struct CdfStamp {
-    const float *values, *valid;
-    int res, lane, ng;
-    float origin[3], cell, center[3], quat[4], band;
-    float dx;
-    CdfBox box;
-    int *tag;
-    float *d;
-};
-
-// cdf_stamp for one lane: a node within `band` of the surface, where the field is
-// valid, gains the lane's valid bit and side bit; the nearest lane owns the node.
-__global__ void k_cdf_stamp(CdfStamp a) {
-    const long long total = box_volume(a.box);
-    const float rf = (float)a.res - 1.0f;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        int x, y, z;
-        if (!box_node(a.box, i, x, y, z)) break;
-        const float rel[3] = {__fsub_rn(__fmul_rn((float)x, a.dx), a.center[0]),
-                              __fsub_rn(__fmul_rn((float)y, a.dx), a.center[1]),
-                              __fsub_rn(__fmul_rn((float)z, a.dx), a.center[2])};
-        float body[3];
-        qrot_inv_rn(a.quat, rel, body);
-        const float f0 = __fdiv_rn(__fsub_rn(body[0], a.origin[0]), a.cell);
-        const float f1 = __fdiv_rn(__fsub_rn(body[1], a.origin[1]), a.cell);
-        const float f2 = __fdiv_rn(__fsub_rn(body[2], a.origin[2]), a.cell);
-        if (f0 < 0.0f || f1 < 0.0f || f2 < 0.0f || f0 > rf || f1 > rf || f2 > rf) continue;
-        if (trilerp_rn(a.valid, a.res, f0, f1, f2) < 0.999f) continue;
-        const float dd = trilerp_rn(a.values, a.res, f0, f1, f2);
-        const float ud = fabsf(dd);
-        if (ud > a.band) continue;
-        const size_t id = ((size_t)x * a.ng + y) * a.ng + z;
-        int t = a.tag[id] | (1 << (2 * a.lane)) | ((dd >= 0.0f ? 1 : 0) << (2 * a.lane + 1));
-        if (ud < a.d[id]) {
-            a.d[id] = ud;
-            t = (t & ~(3 << kCdfOwnerShift)) | (a.lane << kCdfOwnerShift);
-        }
-        a.tag[id] = t;
-    }
-}
-
-__device__ __forceinline__ bool in_box(const CdfBox &b, int x, int y, int z) {
-    return x >= b.lo[0] && x < b.hi[0] && y >= b.lo[1] && y < b.hi[1] && z >= b.lo[2] && z < b.hi[2];
-}
-
-// One lane's stamp of node (x,y,z) into the node's running (tag, distance): the
-// arithmetic of k_cdf_stamp on registers.
-__device__ __forceinline__ void stamp_node(const CdfStamp &a, int x, int y, int z, int &t, float &d) {
-    const float rf = (float)a.res - 1.0f;
-    const float rel[3] = {__fsub_rn(__fmul_rn((float)x, a.dx), a.center[0]),
-                          __fsub_rn(__fmul_rn((float)y, a.dx), a.center[1]),
-                          __fsub_rn(__fmul_rn((float)z, a.dx), a.center[2])};
-    float body[3];
-    qrot_inv_rn(a.quat, rel, body);
-    const float f0 = __fdiv_rn(__fsub_rn(body[0], a.origin[0]), a.cell);
-    const float f1 = __fdiv_rn(__fsub_rn(body[1], a.origin[1]), a.cell);
-    const float f2 = __fdiv_rn(__fsub_rn(body[2], a.origin[2]), a.cell);
-    if (f0 < 0.0f || f1 < 0.0f || f2 < 0.0f || f0 > rf || f1 > rf || f2 > rf) return;
-    if (trilerp_rn(a.valid, a.res, f0, f1, f2) < 0.999f) return;
-    const float dd = trilerp_rn(a.values, a.res, f0, f1, f2);
-    const float ud = fabsf(dd);
-    if (ud > a.band) return;
-    t |= (1 << (2 * a.lane)) | ((dd >= 0.0f ? 1 : 0) << (2 * a.lane + 1));
-    if (ud < d) {
-        d = ud;
-        t = (t & ~(3 << kCdfOwnerShift)) | (a.lane << kCdfOwnerShift);
-    }
-}
-
-// The whole restamp of a substep in one launch, one warp per 4^3 block of `bb`
-// (two nodes a lane): the previous grids catch up with the current ones over
-// `stale`; nodes of `box` are cleared and stamped by every listed lane in lane
-// order (the nearest lane owns a node, the first on a tie); with `post_copy` the
-// previous grids then take the new stamp over `box`; blocks of `mb` get their
-// mask, the OR of current and previous tags over the block's nodes. Equivalent to
-// copy_prev(stale), clear(box), stamp(lane) for each lane, [copy_prev(box)],
-// block_mask(mb) in sequence, as each node depends on itself alone.
-struct CdfRestamp {
-    CdfStamp lane[GBMPM_MAX_CDF];   // per lane: field, pose and its clip of `box`
-    int nl, post_copy, ng, nb;
-    CdfBox box, stale, bb, mb;
-    int *tag, *tag_prev, *block;
-    float *d, *d_prev;
-};
-
-__global__ void k_cdf_restamp(CdfRestamp a) {
-    const int lane = threadIdx.x & 31;
-    const int wpb = blockDim.x >> 5;
-    const int e1 = a.bb.hi[1] - a.bb.lo[1], e2 = a.bb.hi[2] - a.bb.lo[2];
-    const long long nblk = (long long)(a.bb.hi[0] - a.bb.lo[0]) * e1 * e2;
-    const int ng = a.ng;
-    for (long long w = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); w < nblk; w += (long long)gridDim.x * wpb) {
-        const int bi = a.bb.lo[0] + (int)(w / ((long long)e1 * e2));
-        const int r = (int)(w % ((long long)e1 * e2));
-        const int bj = a.bb.lo[1] + r / e2, bk = a.bb.lo[2] + r % e2;
-        int occ = 0;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int n = lane + 32 * h;
-            const int x = (bi << 2) + (n >> 4), y = (bj << 2) + ((n >> 2) & 3), z = (bk << 2) + (n & 3);
-            if (x >= ng || y >= ng || z >= ng) continue;
-            const size_t id = ((size_t)x * ng + y) * ng + z;
-            int t = a.tag[id], tp = a.tag_prev[id];
-            float d = a.d[id];
-            if (in_box(a.stale, x, y, z)) {
-                a.tag_prev[id] = t;
-                a.d_prev[id] = d;
-                tp = t;
-            }
-            if (in_box(a.box, x, y, z)) {
-                t = 0;
-                d = 1.0e9f;
-                for (int l = 0; l < a.nl; ++l)
-                    if (in_box(a.lane[l].box, x, y, z)) stamp_node(a.lane[l], x, y, z, t, d);
-                a.tag[id] = t;
-                a.d[id] = d;
-                if (a.post_copy) {
-                    a.tag_prev[id] = t;
-                    a.d_prev[id] = d;
-                    tp = t;
-                }
-            }
-            occ |= t | tp;
-        }
-        occ = __reduce_or_sync(0xffffffffu, occ);
-        if (lane == 0 && in_box(a.mb, bi, bj, bk)) a.block[((size_t)bi * a.nb + bj) * a.nb + bk] = occ;
-    }
-}
-
-// cdf_block_mask over a box of 4^3 blocks: OR of the current and previous tags
-__global__ void k_cdf_block_mask(const int *tag, const int *tag_prev, int *block, CdfBox bb, int nb, int ng) {
-    const long long total = box_volume(bb);
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        int bi, bj, bk;
-        if (!box_node(bb, i, bi, bj, bk)) break;
-        int occ = 0;
-        for (int a = 0; a < 4; ++a)
-            for (int b = 0; b < 4; ++b)
-                for (int c = 0; c < 4; ++c) {
-                    int ci = (bi << 2) + a, cj = (bj << 2) + b, ck = (bk << 2) + c;
-                    if (ci < ng && cj < ng && ck < ng) {
-                        size_t id = ((size_t)ci * ng + cj) * ng + ck;
-                        occ |= tag[id] | tag_prev[id];
-                    }
-                }
-        block[((size_t)bi * nb + bj) * nb + bk] = occ;
-    }
-}
-
-// Applies collider c to node (gx,gy,gz) of mass m (> 0); adds the reaction
-// impulse and torque into acc[6].
-__device__ __forceinline__ void collide(const ColDev &c, const PoseRec &P, int gx, int gy, int gz, float m,
-                                        float *v, const GK &k, float *acc) {
-    const float dx = k.dx;
-    switch (c.kind) {
-    case GBMPM_COLLIDER_PLANE: {  // mpm_solver_warp.py:1929-1992
-        float o0 = (float)gx * dx - P.p[0], o1 = (float)gy * dx - P.p[1], o2 = (float)gz * dx - P.p[2];
-        float dp = o0 * c.normal[0] + o1 * c.normal[1] + o2 * c.normal[2];
-        if (dp < 0.0f) {
-            if (c.surface == 0) {
-                v[0] = v[1] = v[2] = 0.0f;
-            } else if (c.surface == 11) {
-                if ((float)gz * dx < 0.4f || (float)gz * dx > 0.53f) { v[0] = v[1] = v[2] = 0.0f; }
-                else { v[0] *= 0.3f; v[1] = 0.0f; v[2] *= 0.3f; }
-            } else {
-                float nc = v[0] * c.normal[0] + v[1] * c.normal[1] + v[2] * c.normal[2];
-                float sub = (c.surface == 1) ? nc : fminf(nc, 0.0f);
-                float w0 = v[0] - sub * c.normal[0], w1 = v[1] - sub * c.normal[1], w2 = v[2] - sub * c.normal[2];
-                float len = sqrtf(w0 * w0 + w1 * w1 + w2 * w2);
-                if (nc < 0.0f && len > 1e-20f) {
-                    float sc = fmaxf(0.0f, len + nc * c.friction) / len;
-                    w0 *= sc; w1 *= sc; w2 *= sc;
-                }
-                v[0] = w0; v[1] = w1; v[2] = w2;
-            }
-        }
-        return;
-    }
-    case GBMPM_COLLIDER_BOX: {  // mpm_solver_warp.py:2053-2088
-        if (P.mode == 2) { v[0] = v[1] = v[2] = 0.0f; return; }
-        float o0 = (float)gx * dx - P.p[0], o1 = (float)gy * dx - P.p[1], o2 = (float)gz * dx - P.p[2];
-        if (fabsf(o0) < c.size[0] && fabsf(o1) < c.size[1] && fabsf(o2) < c.size[2]) {
-#pragma unroll
-            for (int a = 0; a < 3; ++a) { acc[a] += m * (v[a] - c.vel[a]); v[a] = c.vel[a]; }
-        }
-        return;
-    }
-    case GBMPM_COLLIDER_CUP: {  // mpm_solver_warp.py:2161-2225
-        float rel[3] = {(float)gx * dx - P.p[0], (float)gy * dx - P.p[1], (float)gz * dx - P.p[2]};
-        const float *R = P.r;
-        float l0 = R[0] * rel[0] + R[3] * rel[1] + R[6] * rel[2];
-        float l1 = R[1] * rel[0] + R[4] * rel[1] + R[7] * rel[2];
-        float l2 = R[2] * rel[0] + R[5] * rel[1] + R[8] * rel[2];
-        float sdf = glass_sdf(l0, l1, l2, c);
-        if (sdf < c.band_c) {
-            float vs[3] = {c.vel[0] + (c.omega[1] * rel[2] - c.omega[2] * rel[1]),
-                           c.vel[1] + (c.omega[2] * rel[0] - c.omega[0] * rel[2]),
-                           c.vel[2] + (c.omega[0] * rel[1] - c.omega[1] * rel[0])};
-            float vn_[3] = {vs[0], vs[1], vs[2]};
-            if (sdf > -c.sticky) {
-                vn_[0] = v[0]; vn_[1] = v[1]; vn_[2] = v[2];
-                float h = 0.25f * dx;
-                float n0 = glass_sdf(l0 + h, l1, l2, c) - glass_sdf(l0 - h, l1, l2, c);
-                float n1 = glass_sdf(l0, l1 + h, l2, c) - glass_sdf(l0, l1 - h, l2, c);
-                float n2 = glass_sdf(l0, l1, l2 + h, c) - glass_sdf(l0, l1, l2 - h, c);
-                float nl = sqrtf(n0 * n0 + n1 * n1 + n2 * n2);
-                if (nl > 1.0e-12f) {
-                    n0 /= nl; n1 /= nl; n2 /= nl;
-                    float n[3] = {R[0] * n0 + R[1] * n1 + R[2] * n2, R[3] * n0 + R[4] * n1 + R[5] * n2,
-                                  R[6] * n0 + R[7] * n1 + R[8] * n2};
-                    float vr[3] = {v[0] - vs[0], v[1] - vs[1], v[2] - vs[2]};
-                    float vn = vr[0] * n[0] + vr[1] * n[1] + vr[2] * n[2];
-                    if (vn < 0.0f) {
-                        float vt[3] = {vr[0] - vn * n[0], vr[1] - vn * n[1], vr[2] - vn * n[2]};
-                        float vtl = sqrtf(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
-                        if (vtl > 1.0e-20f) {
-                            float sc = fmaxf(vtl + c.friction * vn, 0.0f) / vtl;
-                            vt[0] *= sc; vt[1] *= sc; vt[2] *= sc;
-                        }
-                        vn_[0] = vs[0] + vt[0]; vn_[1] = vs[1] + vt[1]; vn_[2] = vs[2] + vt[2];
-                    }
-                }
-            }
-            float imp[3] = {m * (v[0] - vn_[0]), m * (v[1] - vn_[1]), m * (v[2] - vn_[2])};
-            acc[0] += imp[0]; acc[1] += imp[1]; acc[2] += imp[2];
-            acc[3] += rel[1] * imp[2] - rel[2] * imp[1];
-            acc[4] += rel[2] * imp[0] - rel[0] * imp[2];
-            acc[5] += rel[0] * imp[1] - rel[1] * imp[0];
-            v[0] = vn_[0]; v[1] = vn_[1]; v[2] = vn_[2];
-        }
-        return;
-    }
-    case GBMPM_COLLIDER_WALLS: {  // mpm_solver_warp.py:2294-2359
-        const int pad = 3;
-        const int n = k.ng;
-        if (gx < pad && v[0] < 0) v[0] = 0.0f;
-        if (gx >= n - pad && v[0] > 0) v[0] = 0.0f;
-        if (gy < pad && v[1] < 0) v[1] = 0.0f;
-        if (gy >= n - pad && v[1] > 0) v[1] = 0.0f;
-        if (gz < pad && v[2] < 0) v[2] = 0.0f;
-        if (gz >= n - pad && v[2] > 0) v[2] = 0.0f;
-        return;
-    }
-    case GBMPM_COLLIDER_SDF: {  // mpm_solver_warp.py:2680-2736
-        float rel[3] = {(float)gx * dx - P.p[0], (float)gy * dx - P.p[1], (float)gz * dx - P.p[2]};
-        float body[3];
-        qrot(P.q, rel, body, true);
-        float f0 = (body[0] - c.origin[0]) / c.cell, f1 = (body[1] - c.origin[1]) / c.cell,
-              f2 = (body[2] - c.origin[2]) / c.cell;
-        float rf = (float)c.sdf_res - 1.0f;
-        if (!(f0 >= 0.0f && f1 >= 0.0f && f2 >= 0.0f && f0 <= rf && f1 <= rf && f2 <= rf)) return;
-        float sd = trilerp(c.sdf_val, c.sdf_res, f0, f1, f2, 1, 0);
-        if (sd <= c.band) {
-            float g[3] = {trilerp(c.sdf_grad, c.sdf_res, f0, f1, f2, 3, 0), trilerp(c.sdf_grad, c.sdf_res, f0, f1, f2, 3, 1),
-                          trilerp(c.sdf_grad, c.sdf_res, f0, f1, f2, 3, 2)};
-            float gl = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-            if (gl > 1.0e-12f) {
-                g[0] /= gl; g[1] /= gl; g[2] /= gl;
-                float n[3];
-                qrot(P.q, g, n, false);
-                float vs[3] = {c.vel[0] + (c.omega[1] * rel[2] - c.omega[2] * rel[1]),
-                               c.vel[1] + (c.omega[2] * rel[0] - c.omega[0] * rel[2]),
-                               c.vel[2] + (c.omega[0] * rel[1] - c.omega[1] * rel[0])};
-                float vr[3] = {v[0] - vs[0], v[1] - vs[1], v[2] - vs[2]};
-                float vn = vr[0] * n[0] + vr[1] * n[1] + vr[2] * n[2];
-                float nv[3] = {v[0], v[1], v[2]};
-                if (c.surface == 0) {
-                    nv[0] = vs[0]; nv[1] = vs[1]; nv[2] = vs[2];
-                } else if (c.surface == 1) {
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) nv[a] = vs[a] + (vr[a] - vn * n[a]);
-                } else if (vn < 0.0f) {
-                    float vt[3] = {vr[0] - vn * n[0], vr[1] - vn * n[1], vr[2] - vn * n[2]};
-                    float tl = sqrtf(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
-                    if (tl > 1.0e-12f) {
-                        float sc = fmaxf(0.0f, tl + c.friction * vn) / tl;
-                        vt[0] *= sc; vt[1] *= sc; vt[2] *= sc;
-                    }
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) nv[a] = vs[a] + vt[a];
-                }
-                float imp[3] = {m * (v[0] - nv[0]), m * (v[1] - nv[1]), m * (v[2] - nv[2])};
-                acc[0] += imp[0]; acc[1] += imp[1]; acc[2] += imp[2];
-                acc[3] += rel[1] * imp[2] - rel[2] * imp[1];
-                acc[4] += rel[2] * imp[0] - rel[0] * imp[2];
-                acc[5] += rel[0] * imp[1] - rel[1] * imp[0];
-                v[0] = nv[0]; v[1] = nv[1]; v[2] = nv[2];
-            }
-        }
-        return;
-    }
-    default: return;
-    }
-}
-
-// Grid pass over the active-block list: normalize + gravity (mpm_utils.py:927-941),
-// damping (:1287-1295), every collider in list order, then clear the scatter
-// target and the block flags for the next particle pass.
-__global__ void __launch_bounds__(kGridThreads) k_grid(GK k) {
-    __shared__ ColDev s_cols[kMaxCol];
-    __shared__ PoseRec s_pose[kMaxCol];
-    __shared__ float s_acc[kMaxCol][6];
-    const int t = threadIdx.x;
-    for (int i = t; i < k.ncol; i += blockDim.x) { s_cols[i] = k.cols[i]; s_pose[i] = k.poses[i]; }
-    for (int i = t; i < k.ncol * 6; i += blockDim.x) s_acc[i / 6][i % 6] = 0.0f;
-    pdl_wait();   // the particle pass before this one deposits into gmv and fills the block list
-    pdl_trigger();
-    const int per = blockDim.x / 64;
-    const int stride = gridDim.x * per;
-    const int first = blockIdx.x * per + t / 64;
-    // the count and this thread's first list entry are read together: the list holds
-    // bd^3 entries, and an entry at or past the count is never used
-    const int count = *k.blk_count_read;
-    int b_next = (first < k.bd * k.bd * k.bd) ? k.blk_list[first] : 0;
-    if (blockIdx.x == 0 && t == 0) *k.blk_count_reset = 0;
-    __syncthreads();
-    const int lane = t & 31;
-    for (int item = first; item < count; item += stride) {
-        bool valid = true;
-        int b = b_next;
-        if (item + stride < count) b_next = k.blk_list[item + stride];   // next iteration's entry, in flight now
-        int bz = b % k.bd, r = b / k.bd, by = r % k.bd, bx = r / k.bd;
-        int cell = t & 63;
-        int gx = bx * 4 + (cell >> 4), gy = by * 4 + ((cell >> 2) & 3), gz = bz * 4 + (cell & 3);
-        valid = valid && gx < k.ng && gy < k.ng && gz < k.ng;
-        float m = 0.0f;
-        float v[3] = {0.f, 0.f, 0.f};
-        size_t id = 0;
-        if (valid) {
-            id = ((size_t)gx * k.ng + gy) * k.ng + gz;
-            float4 mv = k.gmv[id];
-            m = mv.w;
-            if (m > 1e-15f) {
-                float inv = 1.0f / m;
-                v[0] = mv.x * inv + k.dt * k.g[0];
-                v[1] = mv.y * inv + k.dt * k.g[1];
-                v[2] = mv.z * inv + k.dt * k.g[2];
-            }
-            if (k.damp < 1.0f) { v[0] *= k.damp; v[1] *= k.damp; v[2] *= k.damp; }
-        }
-        for (int c = 0; c < k.ncol; ++c) {
-            float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            if (valid && m > 0.0f && s_pose[c].mode != 0) collide(s_cols[c], s_pose[c], gx, gy, gz, m, v, k, acc);
-            int kind = s_cols[c].kind;
-            if (kind == GBMPM_COLLIDER_BOX || kind == GBMPM_COLLIDER_CUP || kind == GBMPM_COLLIDER_SDF) {
-                bool any = __any_sync(0xffffffffu, acc[0] != 0.f || acc[1] != 0.f || acc[2] != 0.f || acc[3] != 0.f ||
-                                                       acc[4] != 0.f || acc[5] != 0.f);
-                if (any) {
-#pragma unroll
-                    for (int a = 0; a < 6; ++a) {
-                        float x = acc[a];
-#pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-                        if (lane == 0) atomicAdd(&s_acc[c][a], x);
-                    }
-                }
-            }
-        }
-        if (valid) {
-            k.gv[id] = make_float4(v[0], v[1], v[2], 0.0f);
-            k.gmv[id] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (cell == 0) k.blk_flag[b] = 0;
-        }
-    }
-    __syncthreads();
-    for (int i = t; i < k.ncol * 6; i += blockDim.x) {
-        float a = s_acc[i / 6][i % 6];
-        if (a != 0.0f) atomicAdd(&k.wrench[i], (double)a);
-    }
-}
-
-// ------------------------------------------------- guard / reductions ------
-__device__ __forceinline__ float warp_min(float x) {
-    for (int o = 16; o > 0; o >>= 1) x = fminf(x, __shfl_xor_sync(0xffffffffu, x, o));
-    return x;
-}
-__device__ __forceinline__ float warp_max(float x) {
-    for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
-    return x;
-}
-__device__ __forceinline__ void atomic_min_f(float *a, float v) {
-    if (v >= 0.0f) atomicMin((int *)a, __float_as_int(v));
-    else atomicMax((unsigned *)a, __float_as_uint(v));
-}
-__device__ __forceinline__ void atomic_max_f(float *a, float v) {
-    if (v >= 0.0f) atomicMax((int *)a, __float_as_int(v));
-    else atomicMin((unsigned *)a, __float_as_uint(v));
-}
-
-__global__ void k_guard_init(float *out) {
-    if (threadIdx.x < 3) out[threadIdx.x] = INFINITY;
-    else if (threadIdx.x < 6) out[threadIdx.x] = -INFINITY;
-    else if (threadIdx.x == 6) out[6] = 0.0f;
-}
-
-__global__ void k_guard(const float *x, const float *v, int n, float *out, unsigned *status) {
-    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY}, vm = 0.0f;
-    bool bad = false;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            float xa = x[3 * p + a];
-            if (!isfinite(xa)) bad = true;
-            lo[a] = fminf(lo[a], xa);
-            hi[a] = fmaxf(hi[a], xa);
-            vm = fmaxf(vm, fabsf(v[3 * p + a]));
-        }
-    }
-    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(status, GBMPM_FLAG_NONFINITE);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) { lo[a] = warp_min(lo[a]); hi[a] = warp_max(hi[a]); }
-    vm = warp_max(vm);
-    if ((threadIdx.x & 31) == 0) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) { atomic_min_f(out + a, lo[a]); atomic_max_f(out + 3 + a, hi[a]); }
-        atomic_max_f(out + 6, vm);
-    }
-}
-
-// ------------------------------------------------------- block sort --------
-// key = ((bx nb + by) nb + bz), b = floor(x/dx - 0.5) >> 2 in float64
-// (core/solver.py:458-465). The pass stores the signed key, flags any descent
-// (the reference skips the permutation when keys are already non-decreasing)
-// and reduces min/max so the radix sort only walks the bits the keys span.
-__global__ void k_sort_keys(const float *x, int n, double dx, long long nb, long long *keys, int *idx,
-                            int *unsorted, long long *kminmax) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    long long key = 0;
-    bool valid = p < n;
-    if (valid) {
-        long long b[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) b[a] = ((long long)floor((double)x[3 * p + a] / dx - 0.5)) >> 2;
-        key = (b[0] * nb + b[1]) * nb + b[2];
-        keys[p] = key;
-        idx[p] = p;
-        if (p > 0) {
-            long long bp[3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) bp[a] = ((long long)floor((double)x[3 * (p - 1) + a] / dx - 0.5)) >> 2;
-            long long kp = (bp[0] * nb + bp[1]) * nb + bp[2];
-            if (kp > key) *unsorted = 1;
-        }
-    }
-    long long lo = valid ? key : LLONG_MAX, hi = valid ? key : LLONG_MIN;
-    for (int o = 16; o > 0; o >>= 1) {
-        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-    }
-    if ((threadIdx.x & 31) == 0) { atomicMin(&kminmax[0], lo); atomicMax(&kminmax[1], hi); }
-}
-
-__global__ void k_sort_minmax_init(long long *kminmax) {
-    kminmax[0] = LLONG_MAX;
-    kminmax[1] = LLONG_MIN;
-}
-
-// signed key -> unsigned offset from the minimum (order preserving)
-__global__ void k_sort_rebase(const long long *keys, int n, const long long *kminmax, unsigned long long *out) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < n) out[p] = (unsigned long long)(keys[p] - kminmax[0]);
-}
-
-constexpr int kRadixBits = 8;
-constexpr int kRadixBins = 1 << kRadixBits;
-constexpr int kSortTile = 4096;          // elements per tile
-constexpr int kSortThreads = 256;        // 16 rounds of 256 elements
-
-// per-tile digit histogram, stored bin-major: hist[bin * ntiles + tile]
-__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned long long *keys, int n, int shift,
-                                                             unsigned *hist, int ntiles) {
-    __shared__ unsigned h[kRadixBins];
-    for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) h[i] = 0;
-    __syncthreads();
-    int base = blockIdx.x * kSortTile;
-    for (int i = threadIdx.x; i < kSortTile; i += blockDim.x) {
-        int e = base + i;
-        if (e < n) atomicAdd(&h[(keys[e] >> shift) & (kRadixBins - 1)], 1u);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) hist[(size_t)i * ntiles + blockIdx.x] = h[i];
-}
-
-// exclusive scan of hist in place, one CTA: each thread scans a contiguous
-// chunk, the chunk totals are scanned in shared memory, then chunks are rebased
-__global__ void __launch_bounds__(1024) k_radix_scan(unsigned *hist, int total) {
-    __shared__ unsigned s[1024];
-    const int t = threadIdx.x;
-    const int chunk = (total + 1023) / 1024;
-    const int beg = min(t * chunk, total), end = min(beg + chunk, total);
-    unsigned sum = 0;
-    for (int i = beg; i < end; ++i) sum += hist[i];
-    s[t] = sum;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        unsigned v = t >= off ? s[t - off] : 0;
-        __syncthreads();
-        s[t] += v;
-        __syncthreads();
-    }
-    unsigned run = s[t] - sum;
-    for (int i = beg; i < end; ++i) {
-        unsigned v = hist[i];
-        hist[i] = run;
-        run += v;
-    }
-}
-
-// stable scatter: elements of a tile are ranked in index order per digit
-__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned long long *keys_in, const int *idx_in,
-                                                                unsigned long long *keys_out, int *idx_out, int n,
-                                                                int shift, const unsigned *hist, int ntiles) {
-    __shared__ unsigned offs[kRadixBins];
-    __shared__ unsigned warp_cnt[kSortThreads / 32][kRadixBins];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) offs[i] = hist[(size_t)i * ntiles + blockIdx.x];
-    int base = blockIdx.x * kSortTile;
-    for (int round = 0; round < kSortTile / kSortThreads; ++round) {
-        for (int i = threadIdx.x; i < (kSortThreads / 32) * kRadixBins; i += blockDim.x)
-            (&warp_cnt[0][0])[i] = 0;
-        __syncthreads();
-        int e = base + round * kSortThreads + threadIdx.x;
-        bool valid = e < n;
-        unsigned long long key = valid ? keys_in[e] : 0ull;
-        unsigned d = valid ? (unsigned)((key >> shift) & (kRadixBins - 1)) : 0xffffffffu;
-        unsigned peers = __match_any_sync(0xffffffffu, d);
-        int rank_in_warp = __popc(peers & ((1u << lane) - 1u));
-        int leader = 31 - __clz(peers);
-        if (valid && lane == leader) warp_cnt[warp][d] = __popc(peers);
-        __syncthreads();
-        if (valid) {
-            unsigned before = 0;
-            for (int w = 0; w < warp; ++w) before += warp_cnt[w][d];
-            unsigned pos = offs[d] + before + rank_in_warp;
-            keys_out[pos] = key;
-            idx_out[pos] = idx_in[e];
-        }
-        __syncthreads();
-        for (int b2 = threadIdx.x; b2 < kRadixBins; b2 += blockDim.x) {
-            unsigned tot = 0;
-            for (int w = 0; w < kSortThreads / 32; ++w) tot += warp_cnt[w][b2];
-            offs[b2] += tot;
-        }
-        __syncthreads();
-    }
-}
-
-template <int W>
-__global__ void k_gather_rows(const float *src, const int *perm, float *dst, int n) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float *s = src + (size_t)perm[i] * W;
-    float *d = dst + (size_t)i * W;
-#pragma unroll
-    for (int a = 0; a < W; ++a) d[a] = s[a];
-}
-
-// ------------------------------------------------- active blocks ----------
-// blocks_mark / blocks_dilate / blocks_compact (mpm_utils.py:1506-1544)
-__global__ void k_blocks_mark(const float *x, int n, float inv_dx, int bd, int *raw) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    int b[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        int v = (int)(x[3 * p + a] * inv_dx - 0.5f);
-        b[a] = min(max(v >> 2, 0), bd - 1);
-    }
-    raw[((size_t)b[0] * bd + b[1]) * bd + b[2]] = 1;
-}
-__global__ void k_blocks_dilate(const int *raw, int bd, int *cur, const int *prev, int *counts) {
-    int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= bd * bd * bd) return;
-    int z = id % bd, r = id / bd, y = r % bd, x = r / bd;
-    int on = 0;
-    for (int i = -1; i <= 1; ++i)
-        for (int j = -1; j <= 1; ++j)
-            for (int kk = -1; kk <= 1; ++kk) {
-                int xi = min(max(x + i, 0), bd - 1), yj = min(max(y + j, 0), bd - 1), zk = min(max(z + kk, 0), bd - 1);
-                if (raw[((size_t)xi * bd + yj) * bd + zk] == 1) on = 1;
-            }
-    cur[id] = on;
-    if (on) atomicAdd(&counts[0], 1);
-    if (on || prev[id] == 1) atomicAdd(&counts[1], 1);
-}
-
-// ----------------------------------------------------------- exports -------
-__global__ void k_compute_R(const float *Ft, int n, float *R_out) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    float F[9], U[9], V[9], s[3], R[9];
-    mat_load(Ft + 9 * (size_t)p, F);
-    svd3(F, U, s, V);
-    if (det3(U) < 0.0f) { U[2] = -U[2]; U[5] = -U[5]; U[8] = -U[8]; }
-    if (det3(V) < 0.0f) { V[2] = -V[2]; V[5] = -V[5]; V[8] = -V[8]; }
-    mmT(U, V, R);
-    float *o = R_out + 9 * (size_t)p;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) o[3 * i + j] = R[3 * j + i];
-}
-__global__ void k_compute_cov(const float *Ft, const float *c0, int n, float *out) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    float F[9], I0[9], T[9], r[9];
-    mat_load(Ft + 9 * (size_t)p, F);
-    const float *c = c0 + 6 * (size_t)p;
-    I0[0] = c[0]; I0[1] = c[1]; I0[2] = c[2];
-    I0[3] = c[1]; I0[4] = c[3]; I0[5] = c[4];
-    I0[6] = c[2]; I0[7] = c[4]; I0[8] = c[5];
-    mm(F, I0, T);
-    mmT(T, F, r);
-    float *o = out + 6 * (size_t)p;
-    o[0] = r[0]; o[1] = r[1]; o[2] = r[2]; o[3] = r[4]; o[4] = r[5]; o[5] = r[8];
-}
+#include "materials.cuh"
+#include "particle_pass.cuh"
+#include "grid_pass.cuh"
+#include "bookkeeping.cuh"
 
 }  // namespace gbmpm
 
