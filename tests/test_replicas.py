@@ -47,3 +47,13 @@ def test_single_rank_value_is_its_own():
     import bench
     value, ms = bench.replica_value(50.0, units_per_step=10.0, steps=2, world=1)
     assert ms == 50.0 and value == pytest.approx(10.0 * 2 / 0.05)
+
+
+def test_bench_reads_its_committed_profile_figures():
+    """The roofline's DRAM traffic and the press's FLOP count come from the ncu
+    summaries under profiles/: a renamed file or line would leave them null."""
+    import bench
+    assert bench.captured_traffic("pour_honey_192^3") > 0
+    assert bench.captured_traffic("pour_honey_cdf_glasses_192^3") > 0
+    flops = bench.captured_value("particle_passes_press_mu_i_256.txt", "fp32_flops_per_particle_substep")
+    assert flops is not None and 1000 < flops < 10000
