@@ -319,6 +319,11 @@ void gbmpm_batch_destroy(gbmpm_batch *b);
 int gbmpm_batch_tick(gbmpm_batch *b, double *times, double dt, int32_t substeps, int32_t flags, void *stream);
 int gbmpm_batch_guard(gbmpm_batch *b, float *out, uint32_t *status, void *stream);
 int64_t gbmpm_batch_launch_count(gbmpm_batch *b);
+/* As gbmpm_graph_state for the batch graph: 1 ready, 0 none, -1 after a failed
+ * capture (the scenes then tick live, one after another, for the rest of the run). */
+int32_t gbmpm_batch_graph_state(gbmpm_batch *b);
+/* Test hook: the batch's next capture is discarded as if it had failed. */
+int gbmpm_batch_debug_fail_next_capture(gbmpm_batch *b);
 
 /* Edge-guard reduction that allocates nothing (no counterpart in the reference).
  * For callers that cannot call cudaMalloc: a process whose device memory is owned

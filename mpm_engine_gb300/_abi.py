@@ -183,6 +183,8 @@ _SIGNATURES = {
     "gbmpm_cdf_mask_off": (C.c_int, [C.c_void_p, C.c_int32]),
     "gbmpm_graph_state": (C.c_int32, [C.c_void_p]),
     "gbmpm_debug_fail_next_capture": (C.c_int, [C.c_void_p]),
+    "gbmpm_batch_graph_state": (C.c_int32, [C.c_void_p]),
+    "gbmpm_batch_debug_fail_next_capture": (C.c_int, [C.c_void_p]),
     "gbmpm_set_rigid": (C.c_int, [C.c_void_p, C.POINTER(RigidBody), C.c_int32, C.POINTER(RigidSurface), C.c_int32]),
     "gbmpm_get_rigid": (C.c_int, [C.c_void_p, C.POINTER(RigidBody), C.c_int32, C.c_void_p]),
     "gbmpm_set_modifiers": (C.c_int, [C.c_void_p, C.POINTER(Modifier), C.c_int32]),

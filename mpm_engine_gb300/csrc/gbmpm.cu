@@ -1686,6 +1686,8 @@ struct gbmpm_batch {
     double g_dt = 0.0;
     int64_t graph_launches = 0;
     int64_t launches = 0;
+    bool graph_failed = false;          // a capture failed: live launches from then on
+    bool fake_capture_failure = false;  // test hook: treat the next capture as failed
 };
 
 extern "C" {
@@ -1737,9 +1739,12 @@ int gbmpm_batch_tick(gbmpm_batch *b, double *times, double dt, int32_t substeps,
     }
     const bool fused = (flags & GBMPM_TICK_FUSED) != 0;
     const float dtf = (float)dt;
-    if (!(flags & GBMPM_TICK_GRAPH)) {
+    auto live = [&]() {
         for (int i = 0; i < n; ++i)
             if (b->engines[i]->P.n > 0) record_tick(b->engines[i], dtf, substeps, fused, reorder[i], s, false);
+    };
+    if (!(flags & GBMPM_TICK_GRAPH) || b->graph_failed) {
+        live();
         GB_CUDA(cudaGetLastError());
         return GBMPM_OK;
     }
@@ -1767,16 +1772,40 @@ int gbmpm_batch_tick(gbmpm_batch *b, double *times, double dt, int32_t substeps,
         }
         cudaError_t ce = cudaStreamEndCapture(cap, &g);
         cudaStreamDestroy(cap);
-        if (ce != cudaSuccess) return fail(GBMPM_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(ce));
-        ce = cudaGraphInstantiate(&b->graph, g, 0);
-        cudaGraphDestroy(g);
-        if (ce != cudaSuccess) { b->graph = nullptr; return fail(GBMPM_ERR_CUDA, "batch graph instantiate failed"); }
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&b->graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (ce == cudaSuccess && b->fake_capture_failure) {   // test hook: this capture counts as failed
+            cudaGraphExecDestroy(b->graph);
+            ce = cudaErrorStreamCaptureInvalidated;
+        }
+        b->fake_capture_failure = false;
+        if (ce != cudaSuccess) {
+            // as a single scene does: this tick and the following ones run live, scene
+            // after scene on the caller's stream
+            b->graph = nullptr;
+            b->graph_failed = true;
+            (void)cudaGetLastError();
+            live();
+            GB_CUDA(cudaGetLastError());
+            return GBMPM_OK;
+        }
         for (int i = 0; i < n; ++i) b->versions[i] = b->engines[i]->version;
         b->g_substeps = substeps; b->g_flags = flags; b->g_dt = dt;
         b->graph_launches = total;
     }
     GB_CUDA(cudaGraphLaunch(b->graph, s));
     b->launches += b->graph_launches;
+    return GBMPM_OK;
+}
+
+int32_t gbmpm_batch_graph_state(gbmpm_batch *b) {
+    if (!b) return 0;
+    return b->graph_failed ? -1 : (b->graph ? 1 : 0);
+}
+
+int gbmpm_batch_debug_fail_next_capture(gbmpm_batch *b) {
+    if (!b) return fail(GBMPM_ERR_ARG, "null argument");
+    b->fake_capture_failure = true;
     return GBMPM_OK;
 }
 

@@ -1473,6 +1473,8 @@ class BatchSolver:
         times = (C.c_double * n)(*[s._time for s in self.solvers])
         _abi.check(self.lib.gbmpm_batch_tick(self.h, times, float(dt), int(substeps), flags, stream),
                    "gbmpm_batch_tick")
+        if flags & _abi.TICK_GRAPH and self.lib.gbmpm_batch_graph_state(self.h) < 0:
+            self.use_graph = False   # the capture failed; the engine ran this tick live
         for i, s in enumerate(self.solvers):
             s._time = times[i]
             s._step += substeps

@@ -75,3 +75,20 @@ def test_batch_squeeze_workload_runs(cuda):
         b.step(1.0e-5, 50)
     for s in scenes:
         assert np.isfinite(s.x()).all()
+
+
+def test_batch_capture_failure_falls_back_to_live_launches(cuda):
+    """As for one scene: the test hook discards the batch's capture as failed, the
+    batch keeps stepping live (scene after scene), and the scenes advance as a
+    graph batch of the same scenes does, to rounding."""
+    from mpm_engine_gb300 import BatchSolver, Solver
+    a, b = _scenes(Solver), _scenes(Solver)
+    ba, bb = BatchSolver(a), BatchSolver(b)
+    ba.lib.gbmpm_batch_debug_fail_next_capture(ba.h)
+    for _ in range(4):
+        ba.step(2.0e-4, 4)
+        bb.step(2.0e-4, 4)
+    assert ba.use_graph is False and ba.lib.gbmpm_batch_graph_state(ba.h) == -1
+    assert bb.lib.gbmpm_batch_graph_state(bb.h) == 1
+    for sa, sb in zip(a, b):
+        np.testing.assert_allclose(sa.x(), sb.x(), rtol=1e-5, atol=1e-6)
