@@ -17,7 +17,9 @@
 // (uv.lock:1159-1160), which is not installed here, so step-level parity is
 // unpinned: it is anchored on the reference's physics-gate assertions
 // (tests/test_engine.py, test_analytic_benchmarks.py, test_pour.py,
-// test_sdf_collider.py, test_material_review_fixes.py), restated in tests/.
+// test_sdf_collider.py, test_material_review_fixes.py, test_periodic_chute.py,
+// test_tabulated_material.py, test_sparse_blocks.py, test_particle_sort.py,
+// test_cdf_mask.py), restated in tests/ on this oracle and on the CUDA engine.
 //
 // svd3: warp's svd3 is not vendored. This file uses its own method: a cyclic
 // Jacobi eigen-solve of F^T F in float64, descending sort, then a Givens QR of
