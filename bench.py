@@ -26,7 +26,9 @@ Beside the headline the line carries:
   across ranks;
 - `pour_cdf`: the pour with CPIC glasses;
 - `flood_vehicle`: rigid-body coupling;
-- `press`: the granular press, graded against FP32 and HBM.
+- `press`: the granular press, graded against FP32 and HBM;
+- `dam` and `pour_hb`: the 64^3 dam break (362,250 particles, 100 substeps a step)
+  and the pour with the Herschel-Bulkley fluid, timed like the headline.
 Each can be switched off with its --no-* flag.
 """
 from __future__ import annotations
@@ -71,6 +73,7 @@ def parse():
     ap.add_argument("--no-cdf", action="store_true")
     ap.add_argument("--no-flood", action="store_true")
     ap.add_argument("--no-press", action="store_true")
+    ap.add_argument("--no-others", action="store_true", help="skip the dam-break and Herschel-Bulkley pour lines")
     return ap.parse_args()
 
 
@@ -139,14 +142,14 @@ def build_workload(name: str, n_grid: int, solver_cls, **kw):
         glass = "cdf" if name == "pour_cdf" else "cup"
         s, src, rcv, traj, S, dt = pour_scene(solver_cls, n_grid=n_grid, material=mat, glass=glass, **kw)
 
-        def frame(i, s=s):
+        def frame(i, s=s, n=None):
             t = i / 60.0
             c, q, v, w = traj.command(t, 1.0 / 60.0)
             if glass == "cdf":
                 s.set_cdf_pose(src, center=c, quat=(q[1], q[2], q[3], q[0]), velocity=v, omega=w)
             else:
                 s.set_cup(src, center=c, quat=q, velocity=v, omega=w)
-            s.step(dt, S)
+            s.step(dt, S if n is None else n)
 
         label = {"pour": "honey", "pour_hb": "herschel_bulkley", "pour_cdf": "honey_cdf_glasses"}[name]
         desc = {"workload": f"pour_{label}_{n_grid}^3",
@@ -168,8 +171,8 @@ def build_workload(name: str, n_grid: int, solver_cls, **kw):
         s.add_domain_walls()
         S, dt = 100, 1.0e-4
 
-        def frame(i, s=s):
-            s.step(dt, S)
+        def frame(i, s=s, n=None):
+            s.step(dt, S if n is None else n)
 
         desc = {"workload": f"dam_break_{n_grid}^3", "particles": s.n_particles, "substeps_per_step": S, "dt": dt,
                 "grid_lim": 1.0}
@@ -180,8 +183,8 @@ def build_workload(name: str, n_grid: int, solver_cls, **kw):
         s, plate, center, half, dt = press_scene(solver_cls, n_grid=n_grid, **kw)
         S = 20
 
-        def frame(i, s=s):
-            s.step(dt, S)
+        def frame(i, s=s, n=None):
+            s.step(dt, S if n is None else n)
 
         desc = {"workload": f"press_mu_i_{n_grid}^3", "particles": s.n_particles, "substeps_per_step": S, "dt": dt,
                 "grid_lim": 1.0}
@@ -234,6 +237,33 @@ def batched_measure(n_scenes: int, ticks: int, substeps: int = 100, dt: float = 
             "scenes": n_scenes, "particles_total": int(n_part), "ticks": ticks, "dt": dt,
             "particle_substeps_per_s": rate_pp, "gpu_launches": launches,
             "sharding": {"ranks": world, "scenes_on_rank0": n_local} if world > 1 else None}
+
+
+def workload_measure(name: str, n_grid: int, frames: int = 4, warmup: int = 3, device: str = "cuda:0"):
+    """Another configuration timed like the headline (CUDA events per frame, 256 MB
+    written between frames to flush L2): ms per step and particle-substeps/s."""
+    import torch
+    from mpm_engine_gb300 import Solver
+    s, frame, n, S, desc = build_workload(name, n_grid, Solver, device=device)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=device)
+    for i in range(warmup):
+        frame(i)
+    torch.cuda.synchronize()
+    ms = []
+    for k in range(frames):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        frame(warmup + k)
+        b.record()
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    per = sum(ms) / len(ms)
+    out = {**desc, "ms_per_step": per, "particle_substeps_per_s": n * S / (per / 1e3), "frames": [warmup,
+           warmup + frames - 1]}
+    del s, frame, flush
+    torch.cuda.empty_cache()
+    return out
 
 
 def cdf_pour_measure(n_grid: int = 192, frames: int = 4, warmup: int = 24, device: str = "cuda:0"):
@@ -490,8 +520,31 @@ def replica_value(total_ms: float, units_per_step: float, steps: int, world: int
     return world * units_per_step * steps / (total_ms / 1e3), total_ms
 
 
+def start_state(args):
+    """The scene state at the first timed frame of the GPU arm (after `warmup`
+    frames), reached on the GPU engine; None without a GPU."""
+    import torch
+    if not torch.cuda.is_available():
+        return None
+    from mpm_engine_gb300 import Solver
+    from mpm_engine_gb300.build import build_native
+    build_native()
+    g, gframe, _, _, _ = build_workload(args.workload, args.n_grid, Solver, device="cuda:0")
+    for i in range(args.warmup):
+        gframe(i)
+    torch.cuda.synchronize()
+    st = g.export_state()
+    del g, gframe
+    torch.cuda.empty_cache()
+    return st
+
+
 def run_reference(args):
-    """CPU arm: the oracle restatement of the reference step, all host threads."""
+    """CPU arm: the oracle restatement of the reference step, all host threads, on
+    the frames the GPU arm times. The GPU engine advances the scene through the
+    warm-up frames (setup only); from that state the oracle steps the timed frames,
+    each step a bounded sample of that frame's substeps under the frame's own
+    collider commands."""
     world, rank, _ = dist_setup(args)
     if rank != 0:
         return
@@ -499,25 +552,33 @@ def run_reference(args):
     build()
     threads = os.cpu_count() or 1
     s, frame, n, S, desc = build_workload(args.workload, args.n_grid, OracleSolver, threads=threads)
+    st = start_state(args)
+    same = st is not None
+    if same:   # the frame callable drives the oracle built from the GPU arm's state
+        s = OracleSolver.from_state(st, args.n_grid, desc["grid_lim"], threads=threads)
     # bounded sample per step: calibrate substeps so the whole run stays within minutes
+    first = args.warmup if same else 0
     t0 = time.perf_counter()
-    s.step(s_dt(desc), 1)
+    frame(first, s=s, n=1)
     per = time.perf_counter() - t0
     m = max(1, min(S, int(args.cpu_seconds / max(per, 1e-6) / max(args.steps + args.warmup, 1))))
-    for _ in range(args.warmup):
-        s.step(s_dt(desc), m)
+    if not same:
+        for i in range(args.warmup):
+            frame(i, s=s, n=m)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        s.step(s_dt(desc), m)
+    for k in range(args.steps):
+        frame(first + k, s=s, n=m)
     el = time.perf_counter() - t0
     value = n * m * args.steps / el
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": {**desc, "sample_substeps_per_step": m, "l2": "n/a (host CPU)"},
+            "config": {**desc, "sample_substeps_per_step": m, "l2": "n/a (host CPU)",
+                       "frames": [first, first + args.steps - 1],
+                       "start_state": "the GPU arm's state after its warm-up frames" if same else "frame 0"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{m} substeps of the {desc['workload']} scene per step (CPU restatement "
-                                       f"of the reference step, not Warp)"},
+                             "sample": f"{m} substeps of each of frames {first}..{first + args.steps - 1} of the "
+                                       f"{desc['workload']} scene (CPU restatement of the reference step, not Warp)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -614,8 +675,15 @@ def main():
     cnt = (C.c_int64 * 6)()
     s._eng.lib.gbmpm_profile(s._eng.h, msv, cnt, 0)
     s.profile = False
-    fused_ms = msv[2] / max(cnt[2], 1)
+    # The profiled frame brackets every launch with events, so its per-launch times
+    # carry launch gaps and lose the programmatic overlap of consecutive passes. The
+    # fused pass's in-graph duration is the graph-timed frame apportioned by the
+    # profiled frame's shares: ms_per_step x (fused time / all phases) / fused launches.
+    live_fused_ms = msv[2] / max(cnt[2], 1)
     grid_ms = msv[3] / max(cnt[3], 1)
+    total_prof = sum(msv[i] for i in range(6))
+    fused_share = msv[2] / total_prof if total_prof > 0 else 0.0
+    fused_ms = ms_per_step * fused_share / cnt[2] if cnt[2] else 0.0
     peak, peak_kind = peaks()
     # split-pipeline workloads (the sparse press) have no fused pass to grade here
     achieved = n * BYTES_PER_PARTICLE_SUBSTEP / (fused_ms / 1e3) / 1e9 if fused_ms > 0 else None
@@ -627,6 +695,9 @@ def main():
                 "traffic": traffic, "traffic_unit": "bytes per launch (ncu dram read + write, cold cache)",
                 "algorithmic_bytes_per_launch": n * BYTES_PER_PARTICLE_SUBSTEP,
                 "kernel": "k_particles_tiled (fused G2P2G)", "kernel_ms": fused_ms,
+                "kernel_ms_how": "graph-timed ms_per_step x the fused pass's share of a profiled frame / its "
+                                 "launches per frame",
+                "fused_share": fused_share, "live_kernel_ms": live_fused_ms,
                 "grid_kernel_ms": grid_ms, "peak_kind": peak_kind, "phase_ms_per_launch": phases}
 
     e2e = None
@@ -666,6 +737,11 @@ def main():
         batched = batched_measure(args.batch_scenes, ticks=max(2, min(args.steps, 4)), device=f"cuda:{local}",
                                   rank=rank, world=world)
 
+    others = None
+    if not args.no_others and args.workload == "pour":
+        others = {"dam": workload_measure("dam", 64, device=f"cuda:{local}"),
+                  "pour_hb": workload_measure("pour_hb", args.n_grid, device=f"cuda:{local}")}
+
     cdf = None
     if not args.no_cdf and args.workload == "pour":
         cdf = cdf_pour_measure(args.n_grid, device=f"cuda:{local}")
@@ -694,6 +770,7 @@ def main():
                            "replicas" if world > 1 else "single"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clk, "pour_phases": phases_of_pour, "batched": batched, "batched_adjoint": adj,
+                "dam": others and others["dam"], "pour_hb": others and others["pour_hb"],
                 "pour_cdf": cdf, "flood_vehicle": flood, "press": press}
         print(json.dumps(line))
     if dist:

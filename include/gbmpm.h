@@ -331,8 +331,9 @@ int gbmpm_batch_debug_fail_next_capture(gbmpm_batch *b);
  * synchronization. Same out[7] as gbmpm_guard, over device arrays x, v of [n][3]
  * floats, plus *nonfinite = 1 when a position is not finite. Scratch is a 33 KB
  * static device array, so n <= 4194304 (larger n: GBMPM_ERR_ARG). Calls that
- * overlap on the GPU race on that array. The first call on a device looks up its
- * address; make it before any stream capture. Synchronizes the stream. */
+ * overlap on the GPU race on that array. Every call looks up the array's address
+ * in the current context (no cached pointer survives a device reset) and
+ * synchronizes the stream. */
 int gbmpm_guard_noalloc(const float *x, const float *v, int32_t n, float out[7], int32_t *nonfinite,
                         void *stream);
 
@@ -411,6 +412,13 @@ int gbmpm_field_tri_distance(const gbmpm_field_points *pts, const double *tri, i
 
 /* Number of kernels this engine has launched (graph replays count each node). */
 int64_t gbmpm_launch_count(gbmpm_engine *e);
+/* Test hook (no counterpart in the reference): deposits the current particle state
+ * (stored stress, v, C; no stress update) into the grid with the P2G kernel,
+ * returns out[4] = {sum m, sum m vx, sum m vy, sum m vz} over every grid node in
+ * float64, then clears the grid and the block bookkeeping again. Checks that P2G
+ * conserves mass and momentum (the B-spline weights sum to 1, the APIC and stress
+ * terms sum to 0). Synchronizes the stream. */
+int gbmpm_debug_deposit_sums(gbmpm_engine *e, double dt, double out[4], void *stream);
 
 #ifdef __cplusplus
 }

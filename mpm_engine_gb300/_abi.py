@@ -172,6 +172,7 @@ _SIGNATURES = {
     "gbmpm_guard_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_float),
                                       C.POINTER(C.c_int32), C.c_void_p]),
     "gbmpm_launch_count": (C.c_int64, [C.c_void_p]),
+    "gbmpm_debug_deposit_sums": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_double), C.c_void_p]),
     "gbmpm_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]),
     "gbmpm_batch_destroy": (None, [C.c_void_p]),
     "gbmpm_batch_tick": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_double, C.c_int32, C.c_int32,

@@ -249,3 +249,26 @@ __global__ void k_compute_cov(const float *Ft, const float *c0, int n, float *ou
     float *o = out + 6 * (size_t)p;
     o[0] = r[0]; o[1] = r[1]; o[2] = r[2]; o[3] = r[4]; o[4] = r[5]; o[5] = r[8];
 }
+
+// ---- test hook: sums of a deposit over the whole grid ----------------------------
+// Sum of m and m v over every node of mv[n^3] in float64 (per-CTA partials folded
+// with float64 atomics into out[4] = {m, m vx, m vy, m vz}).
+__global__ void __launch_bounds__(256) k_grid_sums(const float4 *mv, long long nodes, double *out) {
+    double a[4] = {0.0, 0.0, 0.0, 0.0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nodes; i += (long long)gridDim.x * blockDim.x) {
+        const float4 g = mv[i];
+        a[0] += (double)g.w; a[1] += (double)g.x; a[2] += (double)g.y; a[3] += (double)g.z;
+    }
+    __shared__ double s[4][8];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        for (int o = 16; o > 0; o >>= 1) a[c] += __shfl_xor_sync(0xffffffffu, a[c], o);
+        if ((threadIdx.x & 31) == 0) s[c][threadIdx.x >> 5] = a[c];
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[threadIdx.x][w];
+        atomicAdd(out + threadIdx.x, t);
+    }
+}

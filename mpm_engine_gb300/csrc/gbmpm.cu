@@ -1468,7 +1468,11 @@ int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32
         cudaStream_t cap;
         GB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
         cudaGraph_t g = nullptr;
-        GB_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        cudaError_t be = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (be != cudaSuccess) {
+            cudaStreamDestroy(cap);
+            return fail(GBMPM_ERR_CUDA, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(be));
+        }
         int64_t before = e->launches;
         record_tick(e, dtf, substeps, fused, reorder, cap, false);
         e->graph_launches = e->launches - before;
@@ -1667,6 +1671,36 @@ int gbmpm_profile(gbmpm_engine *e, double ms_out[GBMPM_NUM_PHASES], int64_t coun
 
 int64_t gbmpm_launch_count(gbmpm_engine *e) { return e ? e->launches : 0; }
 
+int gbmpm_debug_deposit_sums(gbmpm_engine *e, double dt, double out[4], void *stream) {
+    int rc = check_ready(e);
+    if (rc) return rc;
+    if (!out || !(dt > 0.0)) return fail(GBMPM_ERR_ARG, "bad argument");
+    if (e->cdf.n > 0 || e->n_bodies > 0) return fail(GBMPM_ERR_UNSUPPORTED, "deposit sums cover plain scenes");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t nodes = (size_t)e->G.n_grid * e->G.n_grid * e->G.n_grid;
+    const size_t nb = (size_t)e->bd * e->bd * e->bd;
+    GB_CUDA(e->d_tmp.ensure(8));
+    double *d_out = reinterpret_cast<double *>(e->d_tmp.ptr);
+    GB_CUDA(cudaMemsetAsync(d_out, 0, 4 * sizeof(double), s));
+    if (e->P.n > 0) {
+        // the P2G of the stored stress, velocity and affine velocity (no stress update,
+        // so the particle state is left as it is), on the direct path
+        PK k = make_pk(e, e->P, (float)dt, 0);
+        const bool pdl = e->pdl;
+        e->pdl = false;
+        launch_particles(e, k, PASS_P2G, false, s);
+        e->pdl = pdl;
+    }
+    k_grid_sums<<<e->num_sms * 4, 256, 0, s>>>(reinterpret_cast<const float4 *>(e->G.mv), (long long)nodes, d_out);
+    // undo: the grid and the block bookkeeping return to their between-tick state
+    GB_CUDA(cudaMemsetAsync(e->G.mv, 0, nodes * sizeof(float4), s));
+    GB_CUDA(cudaMemsetAsync(e->d_flag.ptr, 0, nb * sizeof(int), s));
+    GB_CUDA(cudaMemsetAsync(e->d_count.ptr, 0, 2 * sizeof(int), s));
+    GB_CUDA(cudaMemcpyAsync(out, d_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    return GBMPM_OK;
+}
+
 }  // extern "C"
 
 // ============================================================ batched scenes
@@ -1755,23 +1789,32 @@ int gbmpm_batch_tick(gbmpm_batch *b, double *times, double dt, int32_t substeps,
         cudaStream_t cap;
         GB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
         cudaGraph_t g = nullptr;
-        GB_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-        GB_CUDA(cudaEventRecord(b->fork, cap));
+        cudaError_t be = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (be != cudaSuccess) {
+            cudaStreamDestroy(cap);
+            return fail(GBMPM_ERR_CUDA, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(be));
+        }
+        // inside the capture the first error is kept rather than returned at once, so
+        // the capture is always ended and its stream released; a failed capture then
+        // takes the live fallback below
+        cudaError_t first = cudaEventRecord(b->fork, cap);
+        auto keep = [&](cudaError_t err) { if (first == cudaSuccess) first = err; };
         int64_t total = 0;
-        for (int i = 0; i < n; ++i) {
+        for (int i = 0; i < n && first == cudaSuccess; ++i) {
             gbmpm_engine *e = b->engines[i];
-            GB_CUDA(cudaStreamWaitEvent(b->streams[i], b->fork, 0));
-            if (e->P.n > 0) {
+            keep(cudaStreamWaitEvent(b->streams[i], b->fork, 0));
+            if (e->P.n > 0 && first == cudaSuccess) {
                 int64_t before = e->launches;
                 record_tick(e, dtf, substeps, fused, reorder[i], b->streams[i], false);
                 total += e->launches - before;
                 e->launches = before;
             }
-            GB_CUDA(cudaEventRecord(b->joins[i], b->streams[i]));
-            GB_CUDA(cudaStreamWaitEvent(cap, b->joins[i], 0));
+            keep(cudaEventRecord(b->joins[i], b->streams[i]));
+            keep(cudaStreamWaitEvent(cap, b->joins[i], 0));
         }
         cudaError_t ce = cudaStreamEndCapture(cap, &g);
         cudaStreamDestroy(cap);
+        if (ce == cudaSuccess && first != cudaSuccess) ce = first;
         if (ce == cudaSuccess) ce = cudaGraphInstantiate(&b->graph, g, 0);
         if (g) cudaGraphDestroy(g);
         if (ce == cudaSuccess && b->fake_capture_failure) {   // test hook: this capture counts as failed
@@ -1858,10 +1901,10 @@ int64_t gbmpm_batch_launch_count(gbmpm_batch *b) { return b ? b->launches : 0; }
 //    two threads) race on it and must be serialized by the caller;
 //  * nothing in the array needs to start at zero: each call writes every slot
 //    it later reads.
-//  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress); make that first call before any stream capture.
-
-#include <mutex>
+//  * every call looks up the array's device address in the current context
+//    (cudaGetSymbolAddress, which allocates nothing). The address is not cached:
+//    after cudaDeviceReset, or on another context of the same device, the module
+//    can load at another address, and a cached pointer would be stale.
 
 namespace noalloc {
 
@@ -1873,10 +1916,6 @@ constexpr long long kMaxParticles = (long long)kMaxBlocks * kThreads * kPerThrea
 
 // per-block partial results, then the final record at slot kMaxBlocks (33 KB)
 static __device__ __align__(256) float g_guard_scratch[(kMaxBlocks + 1) * kSlot];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-float *g_scratch_ptr[kMaxDevices] = {nullptr};
 
 __device__ __forceinline__ float wmin(float x) {
     for (int o = 16; o > 0; o >>= 1) x = fminf(x, __shfl_xor_sync(0xffffffffu, x, o));
@@ -1931,19 +1970,13 @@ __global__ void __launch_bounds__(32) k_guard_final(float *scratch, int nblocks)
     scratch[kMaxBlocks * kSlot + a] = acc;
 }
 
-// device address of the scratch array for the current device, looked up once
+// device address of the scratch array in the current context, looked up on every
+// call (the lookup allocates nothing)
 int scratch_for_current_device(float **out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return fail(GBMPM_ERR_CUDA, "no current CUDA device");
-    if (dev < 0 || dev >= kMaxDevices) return fail(GBMPM_ERR_ARG, "device ordinal out of range");
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_ptr[dev]) {
-        float *ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_guard_scratch);
-        if (e != cudaSuccess || !ptr) return fail(GBMPM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_scratch_ptr[dev] = ptr;
-    }
-    *out = g_scratch_ptr[dev];
+    float *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_guard_scratch);
+    if (e != cudaSuccess || !ptr) return fail(GBMPM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    *out = ptr;
     return GBMPM_OK;
 }
 
@@ -1967,8 +2000,12 @@ int gbmpm_guard_noalloc(const float *x, const float *v, int32_t n, float out[7],
     const int nblocks = n > 0 ? (int)((n + (long long)kThreads * kPerThread - 1) / ((long long)kThreads * kPerThread)) : 0;
     if (nblocks > 0) k_guard_partials<<<nblocks, kThreads, 0, s>>>(x, v, n, scratch);
     k_guard_final<<<1, 32, 0, s>>>(scratch, nblocks);
+    // a launch that failed leaves the previous call's record in the array: report
+    // the failure instead of copying that record back
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(GBMPM_ERR_CUDA, std::string("gbmpm_guard_noalloc launch: ") + cudaGetErrorString(e));
     float h[kSlot];
-    cudaError_t e = cudaMemcpyAsync(h, scratch + kMaxBlocks * kSlot, kSlot * sizeof(float), cudaMemcpyDeviceToHost, s);
+    e = cudaMemcpyAsync(h, scratch + kMaxBlocks * kSlot, kSlot * sizeof(float), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return fail(GBMPM_ERR_CUDA, std::string("gbmpm_guard_noalloc: ") + cudaGetErrorString(e));
     for (int i = 0; i < 7; ++i) out[i] = h[i];

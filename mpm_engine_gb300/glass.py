@@ -6,8 +6,7 @@ base, 0.012 m fillet), the revolved SDF `glass_sdf_local` that the cup collider
 kernel evaluates, and `cup_fill`, whose jittered lattice defines the 340,489-particle
 pour at 192^3 / grid_lim 0.7. The host helpers that pour scripts use around the step
 are here too: `glass_sdf` at a pose, `cavity_mask` (liquid held), `solid_mask`
-(leak audit), `project_out_of_solid`, `write_glass_obj` (the render mesh) and the
-quaternion conversions. Quaternions here are w x y z.
+(leak audit), `project_out_of_solid` and the quaternion conversions. Quaternions here are w x y z.
 """
 from __future__ import annotations
 
@@ -219,52 +218,6 @@ def project_out_of_solid(x, v, pos, quat, profile: GlassProfile, clearance: floa
     vn = np.einsum("ij,ij->i", rel, nw)
     v[bad] = vw + rel - nw * np.minimum(vn, 0.0)[:, None]
     return x, v, nb
-
-
-def write_glass_obj(profile: GlassProfile, path, segments: int = 48, fillet_segments: int = 8):
-    """Writes the glass as a watertight, outward-wound triangle mesh (OBJ) in its
-    local frame: outer wall, rim annulus, inner wall, fillet strips down to the
-    cavity floor, a bottom cap and a floor disc (colliders/glass.py:293-354).
-    Returns the path."""
-    from pathlib import Path
-    path = Path(path)
-    path.parent.mkdir(parents=True, exist_ok=True)
-    n = int(segments)
-    th = np.arange(n) * (2.0 * np.pi / n)
-    c, s_ = np.cos(th), np.sin(th)
-    ro, ri = profile.outer_radius, profile.inner_radius
-    zb, zr, zf = -profile.half_height, profile.rim_z, profile.inner_floor_z
-    fr = min(max(profile.fillet_radius, 0.0), ri - 1e-6)
-
-    def ring(rad, z):
-        return np.column_stack([rad * c, rad * s_, np.full(n, z)])
-
-    if fr > 0.0:
-        phi = np.linspace(0.0, 0.5 * np.pi, fillet_segments + 1)
-        fil = [ring(ri - fr + fr * np.sin(a), zf + fr * (1.0 - np.cos(a))) for a in phi]
-    else:
-        fil = [ring(ri, zf)]
-    rings = [ring(ro, zb), ring(ro, zr), ring(ri, zr)] + fil
-    start = [k * n for k in range(len(rings))]
-    verts = np.vstack(rings + [np.array([[0.0, 0.0, zb], [0.0, 0.0, zf]])])
-    cb, cf = len(verts) - 2, len(verts) - 1
-    ob, ot, it = start[0], start[1], start[2]
-    fs = start[3:]
-    tris = []
-    for i in range(n):
-        j = (i + 1) % n
-        tris += [(ob + i, ob + j, ot + j), (ob + i, ot + j, ot + i)]            # outer wall
-        tris += [(ot + i, ot + j, it + j), (ot + i, it + j, it + i)]            # rim
-        tris += [(fs[-1] + i, it + i, it + j), (fs[-1] + i, it + j, fs[-1] + j)]  # inner wall
-        for a, b in zip(fs[:-1], fs[1:]):                                       # fillet
-            tris += [(a + i, b + i, b + j), (a + i, b + j, a + j)]
-        tris.append((cb, ob + j, ob + i))                                       # bottom cap
-        tris.append((cf, fs[0] + i, fs[0] + j))                                 # cavity floor
-    with path.open("w", encoding="utf-8") as f:
-        f.write(f"# glass: R_o={ro} R_i={ri} h={profile.height} base={profile.base_thickness} fillet={fr}\n")
-        f.writelines(f"v {p[0]:.6f} {p[1]:.6f} {p[2]:.6f}\n" for p in verts)
-        f.writelines(f"f {a + 1} {b + 1} {d + 1}\n" for a, b, d in tris)
-    return path
 
 
 def cup_fill(profile: GlassProfile, h: float, fill_fraction: float = 0.80, clearance: float | None = None,

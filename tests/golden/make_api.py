@@ -3,7 +3,7 @@
 default values. The file is parsed with `ast`; nothing is imported, so Warp is not
 needed.
 
-    python tests/golden/make_api.py [reference_root]
+    python tests/golden/make_api.py <reference_root>
 """
 import ast
 import json
@@ -51,4 +51,6 @@ def main(ref_root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit(f"usage: python {Path(__file__).name} <reference checkout root>")
+    main(sys.argv[1])

@@ -2,13 +2,12 @@
 (src/warpmpm/colliders/glass.py) on seeded inputs, for tests/test_glass_tools_host.py.
 The module is pure numpy and is loaded from its file, so Warp is not needed.
 
-    python tests/golden/make_glass_tools.py [reference_root]
+    python tests/golden/make_glass_tools.py <reference_root>
 """
 from __future__ import annotations
 
 import importlib.util
 import sys
-import tempfile
 from pathlib import Path
 
 import numpy as np
@@ -55,16 +54,11 @@ def main(ref_root: str) -> None:
     for tag, sv in (("static", None), ("moving", (np.array([0.1, -0.05, 0.02]), np.array([0.0, 1.5, -0.4])))):
         xn, vn, nb = g.project_out_of_solid(pts, v, pos, quat, prof, clearance=0.001, solid_velocity=sv)
         out[f"proj_{tag}_x"], out[f"proj_{tag}_v"], out[f"proj_{tag}_n"] = xn, vn, np.int64(nb)
-    # render meshes
-    with tempfile.TemporaryDirectory() as d:
-        thin = g.GlassProfile(outer_radius=0.06, inner_radius=0.05, height=0.16, base_thickness=0.02,
-                              fillet_radius=0.0)
-        for tag, p, kw in (("default", prof, {}), ("thin", thin, {"segments": 20, "fillet_segments": 3})):
-            path = g.write_glass_obj(p, Path(d) / f"{tag}.obj", **kw)
-            out[f"obj_{tag}"] = np.array(Path(path).read_text())
     np.savez_compressed(OUT / "glass_tools.npz", **out)
     print(OUT / "glass_tools.npz")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit(f"usage: python {Path(__file__).name} <reference checkout root>")
+    main(sys.argv[1])

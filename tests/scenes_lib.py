@@ -55,6 +55,16 @@ NAME_PARAMS = {
 }
 
 
+# laws named by engine name and per-type parameters, compared outside the
+# all-materials sweep: tabulated mu(I) (id 13, mpm_utils.py:327-407), whose friction
+# coefficient is a table over log10 I
+EXTRA_MATERIALS = {
+    "tabulated_mu_i": ("tabulated_mu_i", dict(E=1.0e5, nu=0.3, density=2500.0, eta_table=[0.38, 0.45, 0.55, 0.64],
+                                               eta_table_smin=-4.0, eta_table_smax=0.0, grain_diameter=1.0e-3,
+                                               grain_density=2650.0)),
+}
+
+
 def spin_velocity(pts, lin=(0.3, 0.1, -0.4), omega=(0.0, 1.0, 3.0)):
     """A translating, spinning initial velocity field v0 = lin + omega x (x - centroid)."""
     c = pts.mean(axis=0)
@@ -62,20 +72,24 @@ def spin_velocity(pts, lin=(0.3, 0.1, -0.4), omega=(0.0, 1.0, 3.0)):
 
 
 def blob_scene(cls, material_key, n_grid=48, grid_lim=0.4, fused=True, cup=False, box=False, n=2000, v0=False,
-               **kw):
+               cov=None, cov_mode="step", **kw):
     """A blob on a separable floor with domain walls (the fused-pipeline test
     scene, tests/test_fused_pipeline.py:27-56), optionally thrown with a spinning
-    initial velocity, with a moving cup or a descending plate."""
+    initial velocity, with a moving cup or a descending plate, optionally carrying a
+    per-particle covariance (load_particles' cov and cov_mode)."""
     pts, vol = blob(n=n)
-    s = make(cls, n_grid, grid_lim, fused=fused, **kw).load_particles(pts, vol)
+    s = make(cls, n_grid, grid_lim, fused=fused, **kw)
+    s = s.load_particles(pts, vol) if cov is None else s.load_particles(pts, vol, cov=cov, cov_mode=cov_mode)
     if v0:
         vel = spin_velocity(pts)
         if cls.__name__ == "OracleSolver":
             s.a["v"][:] = vel
         else:
             s.set_v(vel)
-    mat = MATERIALS[material_key]
-    if isinstance(mat, str):
+    mat = MATERIALS[material_key] if material_key in MATERIALS else EXTRA_MATERIALS[material_key]
+    if isinstance(mat, tuple):
+        s.set_material(mat[0], **mat[1])
+    elif isinstance(mat, str):
         s.set_material(mat, **NAME_PARAMS[mat])
     else:
         s.set_material(mat())

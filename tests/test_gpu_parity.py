@@ -297,3 +297,84 @@ def test_R_and_cov_exports_match_oracle(cuda, oracle_lib):
     c_ref = np.zeros((len(Ft), 6), np.float32)
     oracle_lib.load().gbmpm_oracle_cov(Ft.ctypes.data, cov.ctypes.data, len(Ft), c_ref.ctypes.data)
     np.testing.assert_allclose(s.cov(), c_ref, rtol=1e-5, atol=1e-12)
+
+
+def _cov_field(n, seed=2):
+    """Symmetric positive-definite covariances, 6-packed (xx, xy, xz, yy, yz, zz)."""
+    rng = np.random.default_rng(seed)
+    A = rng.normal(0.0, 1.0e-3, (n, 3, 3)).astype(np.float64)
+    S = A @ np.transpose(A, (0, 2, 1)) + 1.0e-7 * np.eye(3)
+    return S[:, [0, 0, 0, 1, 1, 2], [0, 1, 2, 1, 2, 2]].astype(np.float32)
+
+
+@pytest.mark.parametrize("key", ["jelly", "newtonian", "metal"])
+def test_cov_step_parity(cuda, oracle_lib, key):
+    """load_particles(cov=..., cov_mode="step") (core/solver.py:148-156): the
+    covariance advects every substep, cov += dt (L cov + cov L^T) (update_cov,
+    mpm_utils.py:613-633), beside x, v, C and F. Per substep within 1e-5 relative,
+    the covariance against its own scale."""
+    from mpm_engine_gb300 import Solver
+    cov = _cov_field(2000)
+    s, _ = blob_scene(Solver, key, v0=True, cov=cov, cov_mode="step")
+    assert s._update_cov
+    o = oracle_lib.OracleSolver.from_state(s.export_state(), s.grid.n_grid, s.grid.grid_lim)
+    assert o.model.update_cov_with_F == 1
+    c0 = s.cov().copy()
+    for i in range(4):
+        s.step(2.0e-4, 1)
+        o.step(2.0e-4, 1)
+        assert_close(s, o, 1e-5, f"{key} with covariance, substep {i}")
+        assert rel_err(s.cov(), o.a["cov"], 1e-12) <= 1e-5, f"{key} covariance, substep {i}"
+    s.step(2.0e-4, 8)
+    o.step(2.0e-4, 8)
+    assert_close(s, o, 12e-5, f"{key} with covariance after a fused 8-substep tick")
+    assert rel_err(s.cov(), o.a["cov"], 1e-12) <= 12e-5
+    assert np.abs(s.cov() - c0).max() > 1e-3 * np.abs(c0).max()   # the covariance did advect
+
+
+def test_tabulated_mu_i_forward_parity(cuda, oracle_lib):
+    """Tabulated mu(I) (id 13; mpm_utils.py:327-407): the mu(I) return map with the
+    friction coefficient interpolated from a table over log10 I, pre-strained so every
+    grain is under pressure and flowing. Per substep within 1e-5 relative, and the
+    composed bound after a fused 8-substep tick."""
+    from mpm_engine_gb300 import Solver
+    s, _ = blob_scene(Solver, "tabulated_mu_i", v0=True)
+    prestrain(s)
+    assert int(s._t["material"][0]) == 13
+    o = oracle_lib.OracleSolver.from_state(s.export_state(), s.grid.n_grid, s.grid.grid_lim)
+    for i in range(4):
+        s.step(2.0e-4, 1)
+        o.step(2.0e-4, 1)
+        assert_close(s, o, 1e-5, f"tabulated mu(I) substep {i}")
+    s.step(2.0e-4, 8)
+    o.step(2.0e-4, 8)
+    assert_close(s, o, 12e-5, "tabulated mu(I) after a fused 8-substep tick")
+
+
+@pytest.mark.parametrize("key", ["newtonian", "jelly", "metal"])
+def test_p2g_conserves_mass_and_momentum(cuda, key):
+    """The P2G deposit of a thrown, spinning blob in mid-flight: the grid's summed
+    mass equals the particles' summed mass within 1e-6 relative, and its summed
+    momentum the particles' momentum within 1e-6 of sum m |v| (the quadratic weights
+    sum to one; the APIC term sum_i w_i (x_i - x_p) and the stress term sum_i grad w_i
+    vanish). Sums in float64 on both sides."""
+    import ctypes as C
+    from mpm_engine_gb300 import Solver, _abi
+    s, _ = blob_scene(Solver, key, v0=True)
+    s.step(2.0e-4, 6)
+    out = (C.c_double * 4)()
+    _abi.check(s._eng.lib.gbmpm_debug_deposit_sums(s._eng.h, 2.0e-4, out, s._stream()), "deposit sums")
+    m = s._t["mass"].double().cpu().numpy()
+    v = s.v().astype(np.float64)
+    m_sum = float(m.sum())
+    p_sum = (m[:, None] * v).sum(0)
+    assert abs(out[0] - m_sum) <= 1e-6 * m_sum, (out[0], m_sum)
+    scale = float((m * np.linalg.norm(v, axis=1)).sum())
+    assert np.abs(np.array(out[1:]) - p_sum).max() <= 1e-6 * scale, (list(out[1:]), p_sum)
+    # the hook leaves the grid as a tick leaves it: the next steps still match a
+    # scene that never called it
+    s2, _ = blob_scene(Solver, key, v0=True)
+    s2.step(2.0e-4, 6)
+    s.step(2.0e-4, 4)
+    s2.step(2.0e-4, 4)
+    np.testing.assert_allclose(s.x(), s2.x(), rtol=0, atol=1e-6)

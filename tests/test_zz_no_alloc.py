@@ -80,3 +80,29 @@ def test_noalloc_guard_rejects_oversize(cuda):
     rc = lib.gbmpm_guard_noalloc(None, None, 4194305, out, None, None)
     assert rc == _abi.ERR_ARG
     assert b"4194304" in lib.gbmpm_last_error()
+
+
+def test_noalloc_guard_empty_and_full_size(cuda):
+    """n = 0 (only the final fold runs, over no partials) and n at the limit (every
+    partial slot of the static array in use)."""
+    torch = cuda
+    from mpm_engine_gb300 import _abi
+    lib = _abi.load()
+    out = (C.c_float * 7)()
+    bad = C.c_int32(-1)
+    _abi.check(lib.gbmpm_guard_noalloc(None, None, 0, out, C.byref(bad), None))
+    got = np.array(out[:], np.float32)
+    assert np.all(got[:3] == np.inf) and np.all(got[3:6] == -np.inf)
+    assert got[6] == 0.0 and bad.value == 0
+    n = 4_194_304
+    g = torch.Generator(device="cuda").manual_seed(11)
+    x = torch.rand(n, 3, device="cuda", generator=g) * 0.3 + 0.05
+    v = torch.randn(n, 3, device="cuda", generator=g)
+    x[n - 1] = torch.tensor([0.01, 0.39, 0.02], device="cuda")   # extremes in the last slice
+    v[n - 1, 1] = -7.5
+    for _ in range(2):
+        got, bad = _guard_noalloc(lib, x, v)
+        want, want_bad = _guard_engine(lib, torch, x, v)
+        np.testing.assert_array_equal(got, want)
+        assert bad == want_bad == 0
+        assert got[6] == 7.5
