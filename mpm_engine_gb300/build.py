@@ -1,7 +1,7 @@
 """In-tree build of the native library (nvcc, sm_103a only).
 
-Outputs mpm_engine_gb300/_build/libgbmpm.so. The build is a single nvcc call;
-nothing is installed into site-packages.
+Outputs mpm_engine_gb300/_build/libgbmpm.so: one nvcc per translation unit, run in
+parallel, then one link. Nothing is installed into site-packages.
 """
 from __future__ import annotations
 
@@ -29,20 +29,39 @@ def sources() -> list[Path]:
 
 
 def build_native(verbose: bool = False, force: bool = False) -> Path:
+    """Compiles every csrc/*.cu to an object in parallel (one nvcc per translation
+    unit, sm_103a), then links them into libgbmpm.so."""
     OUT_DIR.mkdir(parents=True, exist_ok=True)
     out = OUT_DIR / "libgbmpm.so"
     deps = sources() + sorted(CSRC.glob("*.cuh")) + [REPO / "include" / "gbmpm.h"]
     if out.exists() and not force and all(out.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return out
-    cmd = [nvcc_path(), GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-           "-I", str(REPO / "include"), "-o", str(out)] + [str(s) for s in sources()]
+    nvcc = nvcc_path()
+    common = [GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(REPO / "include")]
     if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-    res = subprocess.run(cmd, capture_output=True, text=True)
+        common.append("-Xptxas=-v")
+    procs = []
+    objs = []
+    for src in sources():
+        obj = OUT_DIR / (src.stem + ".o")
+        objs.append(obj)
+        cmd = [nvcc] + common + ["-c", "-o", str(obj), str(src)]
+        procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+    logs = []
+    failed = []
+    for src, pr in procs:
+        text, _ = pr.communicate()
+        logs.append(text)
+        if pr.returncode != 0:
+            failed.append(f"{src.name}:\n{text}")
+    if failed:
+        raise RuntimeError("nvcc failed:\n" + "\n".join(failed))
+    res = subprocess.run([nvcc, GENCODE, "-shared", "-o", str(out)] + [str(o) for o in objs],
+                         capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError("nvcc failed:\n" + res.stdout + res.stderr)
+        raise RuntimeError("nvcc link failed:\n" + res.stdout + res.stderr)
     if verbose:
-        print(res.stdout + res.stderr)
+        print("\n".join(logs) + res.stdout + res.stderr)
     return out
 
 

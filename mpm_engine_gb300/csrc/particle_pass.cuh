@@ -366,7 +366,7 @@ __device__ __forceinline__ int cdf_persist(int old, int fresh) {
 // sums of the scan; the tangential part follows the surface type (sticky, slip,
 // separable Coulomb with a capped impulse) plus a separation push when the
 // particle sits within 0.05 dx of the surface.
-__device__ void cdf_ghost(const PK &k, const CdfScan &c, const float *xp, const float *vp, int pc, const float *grav,
+static __device__ void cdf_ghost(const PK &k, const CdfScan &c, const float *xp, const float *vp, int pc, const float *grav,
                           float *ghost) {
     float vf[3];
 #pragma unroll
@@ -416,7 +416,7 @@ __device__ void cdf_ghost(const PK &k, const CdfScan &c, const float *xp, const 
 // P2G with the CPIC mask: deposits into nodes incompatible with the particle are
 // withheld from the grid and added to the owner lane's reaction (force and torque
 // about the lane centre, summed per thread in float64 before one flush per lane).
-__device__ void cdf_deposit_all(const PK &k, const Stencil &s, int p, const float *v, const float *C, const float *S,
+static __device__ void cdf_deposit_all(const PK &k, const Stencil &s, int p, const float *v, const float *C, const float *S,
                                 int pc, const int *tags) {
     double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     int acc_own = -1;
@@ -453,7 +453,7 @@ __device__ void cdf_deposit_all(const PK &k, const Stencil &s, int p, const floa
 // and velocity modifiers of p2g2p, mpm_solver_warp.py:1182-1196; kernels
 // :2385-2540): impulses first, then velocity overrides, each in list order, on the
 // float32 time window [start, end). Returns true when v changed.
-__device__ bool apply_modifiers(const PK &k, int mask, const float *x, float mass, float *v) {
+static __device__ bool apply_modifiers(const PK &k, int mask, const float *x, float mass, float *v) {
     const float t = (float)k.sub_time[k.sub];
     bool changed = false;
     for (int pass = 0; pass < 2; ++pass)

@@ -170,9 +170,10 @@ def press_scene(solver_cls, n_grid: int = 256, grid_lim: float = 1.0, plate_spee
 
 # ---- batched dough-squeeze scenes ---------------------------------------------------
 def squeeze_scene(solver_cls, n_particles: int, n_grid: int, material, grid_lim: float = 0.3,
-                  plate_speed: float = 0.05, seed: int = 0, **solver_kw):
+                  plate_speed: float = 0.05, seed: int = 0, plate_gap: float = 1.0, **solver_kw):
     """A cubic block of about `n_particles` (8 per cell, jittered) resting on a sticky
-    floor 3 cells up, squeezed by a kinematic plate descending at `plate_speed`.
+    floor 3 cells up, squeezed by a kinematic plate descending at `plate_speed` whose
+    lower face starts `plate_gap` cells above the block (negative: pressed into it).
     Returns (solver, plate handle)."""
     from .solver import GridConfig
     grid = GridConfig(n_grid=n_grid, grid_lim=grid_lim)
@@ -191,7 +192,7 @@ def squeeze_scene(solver_cls, n_particles: int, n_grid: int, material, grid_lim:
     s.add_plane((0, 0, floor), (0, 0, 1), "sticky")
     s.add_domain_walls()
     top = floor + edge
-    plate = s.add_box((c, c, top + 2 * dx), (0.6 * edge + 2 * dx, 0.6 * edge + 2 * dx, dx),
+    plate = s.add_box((c, c, top + (plate_gap + 1.0) * dx), (0.6 * edge + 2 * dx, 0.6 * edge + 2 * dx, dx),
                       velocity=(0.0, 0.0, -plate_speed))
     return s, plate
 

@@ -21,6 +21,14 @@
 // test_tabulated_material.py, test_sparse_blocks.py, test_particle_sort.py,
 // test_cdf_mask.py), restated in tests/ on this oracle and on the CUDA engine.
 //
+// Precision: the restated arithmetic is written over the scalar type Real, float
+// by default (the reference's fp32 and operation order: the parity checker). The
+// same source built with -DORACLE_REAL=double is a second library with the
+// rounding taken out: its particle arrays, grid and accumulators are float64, and
+// the tests use it as a noise-free forward for finite-difference checks of the
+// engine's adjoint (literal constants keep their fp32 values, so both builds
+// describe the same model).
+//
 // svd3: warp's svd3 is not vendored. This file uses its own method: a cyclic
 // Jacobi eigen-solve of F^T F in float64, descending sort, then a Givens QR of
 // F V, giving U and V proper rotations and sigma_3 carrying the sign of det F
@@ -41,31 +49,72 @@
 #include <omp.h>
 #endif
 
+#ifndef ORACLE_REAL
+#define ORACLE_REAL float
+#endif
+
 namespace {
 
-struct V3 { float v[3]; float& operator[](int i) { return v[i]; } float operator[](int i) const { return v[i]; } };
-struct M3 { float m[3][3]; };
+using Real = ORACLE_REAL;
 
-inline V3 mkv(float a, float b, float c) { V3 r; r.v[0] = a; r.v[1] = b; r.v[2] = c; return r; }
+// The particle arrays in the oracle's precision: gbmpm_particles with Real fields
+// (the caller's arrays are float32 or float64 to match the build).
+struct RP {
+    int32_t n;
+    Real *x, *v;
+    Real *C, *F, *F_trial, *L, *stress;
+    Real *mass, *vol, *density, *Jp;
+    Real *mu, *lam, *yield_stress;
+    int32_t *material, *selection;
+    Real *cov, *init_cov;
+    int32_t *cdf_tag;
+    int32_t *rigid_id;
+    Real *x_ref;
+    int32_t *mod_mask;
+};
+inline RP to_rp(const gbmpm_particles& P) {
+    auto r = [](float* f) { return reinterpret_cast<Real*>(f); };
+    RP o;
+    o.n = P.n;
+    o.x = r(P.x); o.v = r(P.v); o.C = r(P.C); o.F = r(P.F); o.F_trial = r(P.F_trial); o.L = r(P.L);
+    o.stress = r(P.stress); o.mass = r(P.mass); o.vol = r(P.vol); o.density = r(P.density); o.Jp = r(P.Jp);
+    o.mu = r(P.mu); o.lam = r(P.lam); o.yield_stress = r(P.yield_stress);
+    o.material = P.material; o.selection = P.selection; o.cov = r(P.cov); o.init_cov = r(P.init_cov);
+    o.cdf_tag = P.cdf_tag; o.rigid_id = P.rigid_id; o.x_ref = r(P.x_ref); o.mod_mask = P.mod_mask;
+    return o;
+}
+
+struct V3 { Real v[3]; Real& operator[](int i) { return v[i]; } Real operator[](int i) const { return v[i]; } };
+struct M3 { Real m[3][3]; };
+
+inline V3 mkv(Real a, Real b, Real c) { V3 r; r.v[0] = a; r.v[1] = b; r.v[2] = c; return r; }
 inline M3 zero33() { M3 r; std::memset(&r, 0, sizeof r); return r; }
 inline M3 ident33() { M3 r = zero33(); r.m[0][0] = r.m[1][1] = r.m[2][2] = 1.0f; return r; }
-inline M3 diag33(float a, float b, float c) { M3 r = zero33(); r.m[0][0] = a; r.m[1][1] = b; r.m[2][2] = c; return r; }
-inline M3 load33(const float* p) { M3 r; std::memcpy(&r, p, 36); return r; }
-inline void store33(float* p, const M3& a) { std::memcpy(p, &a, 36); }
-inline V3 load3(const float* p) { return mkv(p[0], p[1], p[2]); }
-inline void store3(float* p, const V3& a) { p[0] = a[0]; p[1] = a[1]; p[2] = a[2]; }
+inline M3 diag33(Real a, Real b, Real c) { M3 r = zero33(); r.m[0][0] = a; r.m[1][1] = b; r.m[2][2] = c; return r; }
+// loads and stores from either precision: the particle arrays are Real, collider
+// and rigid-body records float
+template <class T> inline M3 load33(const T* p) {
+    M3 r;
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) r.m[i][j] = (Real)p[3 * i + j];
+    return r;
+}
+template <class T> inline void store33(T* p, const M3& a) {
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) p[3 * i + j] = (T)a.m[i][j];
+}
+template <class T> inline V3 load3(const T* p) { return mkv((Real)p[0], (Real)p[1], (Real)p[2]); }
+template <class T> inline void store3(T* p, const V3& a) { p[0] = (T)a[0]; p[1] = (T)a[1]; p[2] = (T)a[2]; }
 
 inline V3 vadd(V3 a, V3 b) { return mkv(a[0] + b[0], a[1] + b[1], a[2] + b[2]); }
 inline V3 vsub(V3 a, V3 b) { return mkv(a[0] - b[0], a[1] - b[1], a[2] - b[2]); }
-inline V3 vscale(V3 a, float s) { return mkv(a[0] * s, a[1] * s, a[2] * s); }
-inline V3 vdivs(V3 a, float s) { return mkv(a[0] / s, a[1] / s, a[2] / s); }
-inline float vdot(V3 a, V3 b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
-inline float vlen(V3 a) { return std::sqrt(vdot(a, a)); }
+inline V3 vscale(V3 a, Real s) { return mkv(a[0] * s, a[1] * s, a[2] * s); }
+inline V3 vdivs(V3 a, Real s) { return mkv(a[0] / s, a[1] / s, a[2] / s); }
+inline Real vdot(V3 a, V3 b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+inline Real vlen(V3 a) { return std::sqrt(vdot(a, a)); }
 inline V3 vcross(V3 a, V3 b) {
     return mkv(a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]);
 }
 inline V3 vnormalize(V3 a) {
-    float l = vlen(a);
+    Real l = vlen(a);
     if (l > 0.0f) return vdivs(a, l);
     return mkv(0, 0, 0);
 }
@@ -94,14 +143,14 @@ inline M3 madd(const M3& a, const M3& b) {
 inline M3 msub(const M3& a, const M3& b) {
     M3 r; for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) r.m[i][j] = a.m[i][j] - b.m[i][j]; return r;
 }
-inline M3 mscale(const M3& a, float s) {
+inline M3 mscale(const M3& a, Real s) {
     M3 r; for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) r.m[i][j] = a.m[i][j] * s; return r;
 }
 inline M3 outer(V3 a, V3 b) {
     M3 r; for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) r.m[i][j] = a[i] * b[j]; return r;
 }
 // warp determinant(mat33) = dot(row0, cross(row1, row2))
-inline float mdet(const M3& a) {
+inline Real mdet(const M3& a) {
     V3 r0 = mkv(a.m[0][0], a.m[0][1], a.m[0][2]);
     V3 r1 = mkv(a.m[1][0], a.m[1][1], a.m[1][2]);
     V3 r2 = mkv(a.m[2][0], a.m[2][1], a.m[2][2]);
@@ -183,123 +232,123 @@ void svd3_impl(const M3& Fin, M3& U, V3& s, M3& V) {
         }
     }
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) { U.m[i][j] = (float)Q[i][j]; V.m[i][j] = (float)Vs[i][j]; }
-    s[0] = (float)W[0][0]; s[1] = (float)W[1][1]; s[2] = (float)W[2][2];
+        for (int j = 0; j < 3; ++j) { U.m[i][j] = (Real)Q[i][j]; V.m[i][j] = (Real)Vs[i][j]; }
+    s[0] = (Real)W[0][0]; s[1] = (Real)W[1][1]; s[2] = (Real)W[2][2];
 }
 
 // ------------------------------------------------------------ model view ---
 struct Model {
     const gbmpm_model* m;
-    float dx, inv_dx;
+    Real dx, inv_dx;
 };
 
 struct Parts {
-    const gbmpm_particles* p;
+    const RP* p;
 };
 
 // --------------------------------------------------------- stress laws -----
 // kirchoff_stress_FCR (mpm_utils.py:8-15)
-M3 stress_fcr(const M3& F, const M3& U, const M3& V, float J, float mu, float lam) {
+M3 stress_fcr(const M3& F, const M3& U, const M3& V, Real J, Real mu, Real lam) {
     M3 R = mmul(U, mT(V));
     M3 t = mmul(mscale(msub(F, R), 2.0f * mu), mT(F));
-    float d = lam * J * (J - 1.0f);
+    Real d = lam * J * (J - 1.0f);
     M3 id = ident33();
     return madd(t, mscale(id, d));
 }
 // kirchoff_stress_water (mpm_utils.py:17-25)
-M3 stress_water(float J, float bulk) {
-    const float gamma = 1.1f;
-    float pressure = -bulk * (std::pow(J, -gamma) - 1.0f);
+M3 stress_water(Real J, Real bulk) {
+    const Real gamma = 1.1f;
+    Real pressure = -bulk * (std::pow(J, -gamma) - 1.0f);
     M3 c = mscale(ident33(), pressure);
     return mscale(c, J);
 }
 // deviatoric strain rate shared by the newtonian and tabulated laws (mpm_utils.py:40-49)
-void dev_rate(const M3& L, M3& Ddev, float& gd) {
-    const float eps = 0.02f;
+void dev_rate(const M3& L, M3& Ddev, Real& gd) {
+    const Real eps = 0.02f;
     M3 D = mscale(madd(L, mT(L)), 0.5f);
-    float trd = (D.m[0][0] + D.m[1][1] + D.m[2][2]) / 3.0f;
+    Real trd = (D.m[0][0] + D.m[1][1] + D.m[2][2]) / 3.0f;
     Ddev = msub(D, mscale(ident33(), trd));
-    float dd = 0.0f;
+    Real dd = 0.0f;
     for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) dd = dd + Ddev.m[i][j] * Ddev.m[i][j];
     gd = std::sqrt(2.0f * dd + eps * eps);
 }
 // kirchoff_stress_newtonian (mpm_utils.py:27-54)
-M3 stress_newtonian(float J, float bulk, const M3& L, float eta, float tau_y, float pk, float pn) {
-    const float gamma = 1.1f;
-    float pressure = -bulk * (std::pow(J, -gamma) - 1.0f);
-    M3 Ddev; float gd;
+M3 stress_newtonian(Real J, Real bulk, const M3& L, Real eta, Real tau_y, Real pk, Real pn) {
+    const Real gamma = 1.1f;
+    Real pressure = -bulk * (std::pow(J, -gamma) - 1.0f);
+    M3 Ddev; Real gd;
     dev_rate(L, Ddev, gd);
-    float eta_app = eta + tau_y / gd + pk * std::pow(gd, pn - 1.0f);
+    Real eta_app = eta + tau_y / gd + pk * std::pow(gd, pn - 1.0f);
     M3 c = madd(mscale(ident33(), pressure), mscale(Ddev, 2.0f * eta_app));
     return mscale(c, J);
 }
 // kirchoff_stress_tabulated (mpm_utils.py:56-85)
-M3 stress_tabulated(float J, float bulk, const M3& L, const float* table, float smin, float smax, int n) {
-    const float gamma = 1.1f;
-    float pressure = -bulk * (std::pow(J, -gamma) - 1.0f);
-    M3 Ddev; float gd;
+M3 stress_tabulated(Real J, Real bulk, const M3& L, const float* table, Real smin, Real smax, int n) {
+    const Real gamma = 1.1f;
+    Real pressure = -bulk * (std::pow(J, -gamma) - 1.0f);
+    M3 Ddev; Real gd;
     dev_rate(L, Ddev, gd);
-    float s = std::log(gd) * 0.43429448190325176f;
-    float idx = (s - smin) / (smax - smin) * (float)(n - 1);
-    idx = std::min(std::max(idx, 0.0f), (float)(n - 1) - 1.0e-6f);
+    Real s = std::log(gd) * 0.43429448190325176f;
+    Real idx = (s - smin) / (smax - smin) * (Real)(n - 1);
+    idx = std::min<Real>(std::max<Real>(idx, 0.0f), (Real)(n - 1) - 1.0e-6f);
     int i0 = (int)std::floor(idx);
-    float frac = idx - (float)i0;
-    float eta_app = table[i0] * (1.0f - frac) + table[i0 + 1] * frac;
+    Real frac = idx - (Real)i0;
+    Real eta_app = table[i0] * (1.0f - frac) + table[i0 + 1] * frac;
     M3 c = madd(mscale(ident33(), pressure), mscale(Ddev, 2.0f * eta_app));
     return mscale(c, J);
 }
 // kirchoff_stress_drucker_prager (mpm_utils.py:109-124)
-M3 stress_dp(const M3& F, const M3& U, const M3& V, V3 sig, float mu, float lam) {
-    float l0 = std::log(sig[0]), l1 = std::log(sig[1]), l2 = std::log(sig[2]);
-    float lsum = l0 + l1 + l2;
-    float c0 = 2.0f * mu * std::log(sig[0]) * (1.0f / sig[0]) + lam * lsum * (1.0f / sig[0]);
-    float c1 = 2.0f * mu * std::log(sig[1]) * (1.0f / sig[1]) + lam * lsum * (1.0f / sig[1]);
-    float c2 = 2.0f * mu * std::log(sig[2]) * (1.0f / sig[2]) + lam * lsum * (1.0f / sig[2]);
+M3 stress_dp(const M3& F, const M3& U, const M3& V, V3 sig, Real mu, Real lam) {
+    Real l0 = std::log(sig[0]), l1 = std::log(sig[1]), l2 = std::log(sig[2]);
+    Real lsum = l0 + l1 + l2;
+    Real c0 = 2.0f * mu * std::log(sig[0]) * (1.0f / sig[0]) + lam * lsum * (1.0f / sig[0]);
+    Real c1 = 2.0f * mu * std::log(sig[1]) * (1.0f / sig[1]) + lam * lsum * (1.0f / sig[1]);
+    Real c2 = 2.0f * mu * std::log(sig[2]) * (1.0f / sig[2]) + lam * lsum * (1.0f / sig[2]);
     return mmul(mmul(mmul(U, diag33(c0, c1, c2)), mT(V)), mT(F));
 }
 // kirchoff_stress_hencky (mpm_utils.py:228-243)
-M3 stress_hencky(const M3& U, V3 sig, float mu, float lam) {
-    float e0 = std::log(std::max(sig[0], 1e-6f)), e1 = std::log(std::max(sig[1], 1e-6f)),
-          e2 = std::log(std::max(sig[2], 1e-6f));
-    float tr = e0 + e1 + e2;
+M3 stress_hencky(const M3& U, V3 sig, Real mu, Real lam) {
+    Real e0 = std::log(std::max<Real>(sig[0], 1e-6f)), e1 = std::log(std::max<Real>(sig[1], 1e-6f)),
+          e2 = std::log(std::max<Real>(sig[2], 1e-6f));
+    Real tr = e0 + e1 + e2;
     M3 t = diag33(2.0f * mu * e0 + lam * tr, 2.0f * mu * e1 + lam * tr, 2.0f * mu * e2 + lam * tr);
     return mmul(mmul(U, t), mT(U));
 }
 // mu_i_phi_pressure (mpm_utils.py:421-430)
-float mu_i_phi_pressure(const gbmpm_model* m, int mat, float J, float Jp_ref) {
-    float K = m->E[mat] / (3.0f * (1.0f - 2.0f * m->nu[mat]));
-    float p = K * (Jp_ref / std::max(J, 1e-6f) - 1.0f);
-    return std::max(p, 0.0f);
+Real mu_i_phi_pressure(const gbmpm_model* m, int mat, Real J, Real Jp_ref) {
+    Real K = m->E[mat] / (3.0f * (1.0f - 2.0f * m->nu[mat]));
+    Real p = K * (Jp_ref / std::max<Real>(J, 1e-6f) - 1.0f);
+    return std::max<Real>(p, 0.0f);
 }
 // kirchoff_stress_mu_i_phi (mpm_utils.py:525-540)
-M3 stress_mu_i_phi(const M3& U, V3 sig, float G, float p_comp) {
-    float s0 = std::max(sig[0], 1e-6f), s1 = std::max(sig[1], 1e-6f), s2 = std::max(sig[2], 1e-6f);
-    float e0 = std::log(s0), e1 = std::log(s1), e2 = std::log(s2);
-    float J = s0 * s1 * s2;
-    float mean = (e0 + e1 + e2) / 3.0f;
-    float iso = -p_comp * J;
+M3 stress_mu_i_phi(const M3& U, V3 sig, Real G, Real p_comp) {
+    Real s0 = std::max<Real>(sig[0], 1e-6f), s1 = std::max<Real>(sig[1], 1e-6f), s2 = std::max<Real>(sig[2], 1e-6f);
+    Real e0 = std::log(s0), e1 = std::log(s1), e2 = std::log(s2);
+    Real J = s0 * s1 * s2;
+    Real mean = (e0 + e1 + e2) / 3.0f;
+    Real iso = -p_comp * J;
     M3 t = diag33(2.0f * G * (e0 - mean) + iso, 2.0f * G * (e1 - mean) + iso, 2.0f * G * (e2 - mean) + iso);
     return mmul(mmul(U, t), mT(U));
 }
 
 // ------------------------------------------------------- return maps -------
 // von_mises_return_mapping (mpm_utils.py:127-170); with_damage (:172-225)
-M3 rm_von_mises(const M3& Ft, const gbmpm_particles* P, const gbmpm_model* m, int p, int mat, bool damage) {
+M3 rm_von_mises(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat, bool damage) {
     M3 U, V; V3 so;
     svd3_impl(Ft, U, so, V);
-    V3 sig = mkv(std::max(so[0], 0.01f), std::max(so[1], 0.01f), std::max(so[2], 0.01f));
+    V3 sig = mkv(std::max<Real>(so[0], 0.01f), std::max<Real>(so[1], 0.01f), std::max<Real>(so[2], 0.01f));
     V3 eps = mkv(std::log(sig[0]), std::log(sig[1]), std::log(sig[2]));
-    float temp = (eps[0] + eps[1] + eps[2]) / 3.0f;
-    float mu = P->mu[p], lam = P->lam[p];
-    float tr = eps[0] + eps[1] + eps[2];
+    Real temp = (eps[0] + eps[1] + eps[2]) / 3.0f;
+    Real mu = P->mu[p], lam = P->lam[p];
+    Real tr = eps[0] + eps[1] + eps[2];
     V3 tau = vadd(vscale(eps, 2.0f * mu), vscale(mkv(1, 1, 1), lam * tr));
-    float sum_tau = tau[0] + tau[1] + tau[2];
+    Real sum_tau = tau[0] + tau[1] + tau[2];
     V3 cond = mkv(tau[0] - sum_tau / 3.0f, tau[1] - sum_tau / 3.0f, tau[2] - sum_tau / 3.0f);
     if (vlen(cond) > P->yield_stress[p]) {
         if (damage && P->yield_stress[p] <= 0) return Ft;
         V3 eh = vsub(eps, mkv(temp, temp, temp));
-        float ehn = vlen(eh) + 1e-6f;
-        float dg = ehn - P->yield_stress[p] / (2.0f * mu);
+        Real ehn = vlen(eh) + 1e-6f;
+        Real dg = ehn - P->yield_stress[p] / (2.0f * mu);
         eps = vsub(eps, vscale(eh, dg / ehn));
         if (damage) {
             P->yield_stress[p] = P->yield_stress[p] - m->softening[mat] * vlen(vscale(eh, dg / ehn));
@@ -315,52 +364,52 @@ M3 rm_von_mises(const M3& Ft, const gbmpm_particles* P, const gbmpm_model* m, in
 }
 
 // mu_i_return_mapping (mpm_utils.py:246-324) and the tabulated variant (:327-407)
-M3 rm_mu_i(const M3& Ft, const gbmpm_particles* P, const gbmpm_model* m, int p, int mat, float dt, bool tab) {
+M3 rm_mu_i(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat, Real dt, bool tab) {
     M3 U, V; V3 sig;
     svd3_impl(Ft, U, sig, V);
-    V3 sc = mkv(std::max(std::fabs(sig[0]), 1e-6f), std::max(std::fabs(sig[1]), 1e-6f),
-                std::max(std::fabs(sig[2]), 1e-6f));
+    V3 sc = mkv(std::max<Real>(std::fabs(sig[0]), 1e-6f), std::max<Real>(std::fabs(sig[1]), 1e-6f),
+                std::max<Real>(std::fabs(sig[2]), 1e-6f));
     V3 eps = mkv(std::log(sc[0]), std::log(sc[1]), std::log(sc[2]));
-    float tr = eps[0] + eps[1] + eps[2];
+    Real tr = eps[0] + eps[1] + eps[2];
     M3 Fe = Ft;
     if (tr >= 0.0f) {
         Fe = mmul(U, mT(V));
     } else {
-        float G = P->mu[p], lam = P->lam[p];
-        float J = sc[0] * sc[1] * sc[2];
-        float mean = tr / 3.0f;
-        float d0 = eps[0] - mean, d1 = eps[1] - mean, d2 = eps[2] - mean;
-        float dn = std::sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-        float pK = -(2.0f * G / 3.0f + lam) * tr;
-        float tbK = 2.0f * G * dn / std::sqrt(2.0f);
-        float pC = pK / J;
-        float mu_s = m->muI_mu_s[mat], dmu = m->muI_delta_mu[mat], I0 = m->muI_I0[mat];
-        float thresh = tab ? m->eta_table[0] : mu_s;
+        Real G = P->mu[p], lam = P->lam[p];
+        Real J = sc[0] * sc[1] * sc[2];
+        Real mean = tr / 3.0f;
+        Real d0 = eps[0] - mean, d1 = eps[1] - mean, d2 = eps[2] - mean;
+        Real dn = std::sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+        Real pK = -(2.0f * G / 3.0f + lam) * tr;
+        Real tbK = 2.0f * G * dn / std::sqrt(2.0f);
+        Real pC = pK / J;
+        Real mu_s = m->muI_mu_s[mat], dmu = m->muI_delta_mu[mat], I0 = m->muI_I0[mat];
+        Real thresh = tab ? m->eta_table[0] : mu_s;
         if (tbK > thresh * pK) {
-            float Ic = m->muI_d[mat] * std::sqrt(m->muI_rho_s[mat] / pC);
-            float lo = 0.0f, hi = tbK / (G * dt);
+            Real Ic = m->muI_d[mat] * std::sqrt(m->muI_rho_s[mat] / pC);
+            Real lo = 0.0f, hi = tbK / (G * dt);
             for (int it = 0; it < 48; ++it) {
-                float mid = 0.5f * (lo + hi);
-                float Im = mid * Ic;
-                float mu_mid;
+                Real mid = 0.5f * (lo + hi);
+                Real Im = mid * Ic;
+                Real mu_mid;
                 if (!tab) {
                     mu_mid = mu_s + dmu * Im / (Im + I0);
                 } else {
-                    float s = std::log(std::max(Im, 1e-12f)) * 0.43429448190325176f;
-                    float idx = (s - m->eta_table_smin) / (m->eta_table_smax - m->eta_table_smin) *
-                                (float)(m->eta_table_n - 1);
-                    idx = std::min(std::max(idx, 0.0f), (float)(m->eta_table_n - 1) - 1.0e-6f);
+                    Real s = std::log(std::max<Real>(Im, 1e-12f)) * 0.43429448190325176f;
+                    Real idx = (s - m->eta_table_smin) / (m->eta_table_smax - m->eta_table_smin) *
+                                (Real)(m->eta_table_n - 1);
+                    idx = std::min<Real>(std::max<Real>(idx, 0.0f), (Real)(m->eta_table_n - 1) - 1.0e-6f);
                     int i0 = (int)std::floor(idx);
-                    float fr = idx - (float)i0;
+                    Real fr = idx - (Real)i0;
                     mu_mid = m->eta_table[i0] * (1.0f - fr) + m->eta_table[i0 + 1] * fr;
                 }
-                float g = tbK - G * dt * mid - mu_mid * pK;
+                Real g = tbK - G * dt * mid - mu_mid * pK;
                 if (g > 0.0f) lo = mid; else hi = mid;
             }
-            float gdp = 0.5f * (lo + hi);
-            float tbn = tbK - G * dt * gdp;
-            float scale = tbn / std::max(tbK, 1e-20f);
-            float e0 = d0 * scale + mean, e1 = d1 * scale + mean, e2 = d2 * scale + mean;
+            Real gdp = 0.5f * (lo + hi);
+            Real tbn = tbK - G * dt * gdp;
+            Real scale = tbn / std::max<Real>(tbK, 1e-20f);
+            Real e0 = d0 * scale + mean, e1 = d1 * scale + mean, e2 = d2 * scale + mean;
             Fe = mmul(mmul(U, diag33(std::exp(e0), std::exp(e1), std::exp(e2))), mT(V));
         }
     }
@@ -368,56 +417,56 @@ M3 rm_mu_i(const M3& Ft, const gbmpm_particles* P, const gbmpm_model* m, int p, 
 }
 
 // j_cs_of_I (mpm_utils.py:410-418)
-float j_cs_of_I(const gbmpm_model* m, int mat, float I) {
-    float I0 = m->muI_I0[mat], chi = m->muI_phi_chi[mat];
-    float denom = std::max(1.0f - chi * I / (I + I0), 1e-3f);
+Real j_cs_of_I(const gbmpm_model* m, int mat, Real I) {
+    Real I0 = m->muI_I0[mat], chi = m->muI_phi_chi[mat];
+    Real denom = std::max<Real>(1.0f - chi * I / (I + I0), 1e-3f);
     return 1.0f / denom;
 }
 
 // mu_i_phi_return_mapping (mpm_utils.py:433-522)
-M3 rm_mu_i_phi(const M3& Ft, const gbmpm_particles* P, const gbmpm_model* m, int p, int mat, float dt) {
+M3 rm_mu_i_phi(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat, Real dt) {
     M3 U, V; V3 sig;
     svd3_impl(Ft, U, sig, V);
-    V3 sc = mkv(std::max(std::fabs(sig[0]), 1e-6f), std::max(std::fabs(sig[1]), 1e-6f),
-                std::max(std::fabs(sig[2]), 1e-6f));
+    V3 sc = mkv(std::max<Real>(std::fabs(sig[0]), 1e-6f), std::max<Real>(std::fabs(sig[1]), 1e-6f),
+                std::max<Real>(std::fabs(sig[2]), 1e-6f));
     V3 eps = mkv(std::log(sc[0]), std::log(sc[1]), std::log(sc[2]));
-    float J = sc[0] * sc[1] * sc[2];
-    float tr = eps[0] + eps[1] + eps[2];
-    float mean = tr / 3.0f;
-    float d0 = eps[0] - mean, d1 = eps[1] - mean, d2 = eps[2] - mean;
-    float dn = std::sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-    float G = P->mu[p];
-    float Jp_ref = P->Jp[p];
+    Real J = sc[0] * sc[1] * sc[2];
+    Real tr = eps[0] + eps[1] + eps[2];
+    Real mean = tr / 3.0f;
+    Real d0 = eps[0] - mean, d1 = eps[1] - mean, d2 = eps[2] - mean;
+    Real dn = std::sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    Real G = P->mu[p];
+    Real Jp_ref = P->Jp[p];
     if (Jp_ref < 0.5f) Jp_ref = 1.0f;
-    float pc = mu_i_phi_pressure(m, mat, J, Jp_ref);
-    const float beta = 8.0f;
+    Real pc = mu_i_phi_pressure(m, mat, J, Jp_ref);
+    const Real beta = 8.0f;
     M3 Fe = Ft;
     P->Jp[p] = Jp_ref;
     if (pc <= 0.0f) {
-        float si = std::exp(mean);
+        Real si = std::exp(mean);
         Fe = mmul(mmul(U, diag33(si, si, si)), mT(V));
     } else {
-        float pK = pc * J;
-        float tbK = 2.0f * G * dn / std::sqrt(2.0f);
-        float mu_s = m->muI_mu_s[mat], dmu = m->muI_delta_mu[mat], I0 = m->muI_I0[mat];
+        Real pK = pc * J;
+        Real tbK = 2.0f * G * dn / std::sqrt(2.0f);
+        Real mu_s = m->muI_mu_s[mat], dmu = m->muI_delta_mu[mat], I0 = m->muI_I0[mat];
         if (tbK > mu_s * pK) {
-            float Ic = m->muI_d[mat] * std::sqrt(m->muI_rho_s[mat] / pc);
-            float lo = 0.0f, hi = tbK / (G * dt);
+            Real Ic = m->muI_d[mat] * std::sqrt(m->muI_rho_s[mat] / pc);
+            Real lo = 0.0f, hi = tbK / (G * dt);
             for (int it = 0; it < 48; ++it) {
-                float mid = 0.5f * (lo + hi);
-                float Im = mid * Ic;
-                float mu_mid = mu_s + dmu * Im / (Im + I0);
-                float g = tbK - G * dt * mid - mu_mid * pK;
+                Real mid = 0.5f * (lo + hi);
+                Real Im = mid * Ic;
+                Real mu_mid = mu_s + dmu * Im / (Im + I0);
+                Real g = tbK - G * dt * mid - mu_mid * pK;
                 if (g > 0.0f) lo = mid; else hi = mid;
             }
-            float gdp = 0.5f * (lo + hi);
-            float Ir = gdp * Ic;
-            float dgam = std::min(beta * gdp * dt, 1.0f);
-            float jcs = j_cs_of_I(m, mat, Ir);
+            Real gdp = 0.5f * (lo + hi);
+            Real Ir = gdp * Ic;
+            Real dgam = std::min<Real>(beta * gdp * dt, 1.0f);
+            Real jcs = j_cs_of_I(m, mat, Ir);
             P->Jp[p] = Jp_ref + dgam * (jcs - Jp_ref);
-            float tbn = tbK - G * dt * gdp;
-            float scale = tbn / std::max(tbK, 1e-20f);
-            float e0 = d0 * scale + mean, e1 = d1 * scale + mean, e2 = d2 * scale + mean;
+            Real tbn = tbK - G * dt * gdp;
+            Real scale = tbn / std::max<Real>(tbK, 1e-20f);
+            Real e0 = d0 * scale + mean, e1 = d1 * scale + mean, e2 = d2 * scale + mean;
             Fe = mmul(mmul(U, diag33(std::exp(e0), std::exp(e1), std::exp(e2))), mT(V));
         }
     }
@@ -425,16 +474,16 @@ M3 rm_mu_i_phi(const M3& Ft, const gbmpm_particles* P, const gbmpm_model* m, int
 }
 
 // sand_return_mapping (mpm_utils.py:543-580)
-M3 rm_sand(const M3& Ft, const gbmpm_particles* P, const gbmpm_model* m, int p, int mat) {
+M3 rm_sand(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat) {
     M3 U, V; V3 sig;
     svd3_impl(Ft, U, sig, V);
-    V3 eps = mkv(std::log(std::max(std::fabs(sig[0]), 1e-14f)), std::log(std::max(std::fabs(sig[1]), 1e-14f)),
-                 std::log(std::max(std::fabs(sig[2]), 1e-14f)));
-    float tr = eps[0] + eps[1] + eps[2];
+    V3 eps = mkv(std::log(std::max<Real>(std::fabs(sig[0]), 1e-14f)), std::log(std::max<Real>(std::fabs(sig[1]), 1e-14f)),
+                 std::log(std::max<Real>(std::fabs(sig[2]), 1e-14f)));
+    Real tr = eps[0] + eps[1] + eps[2];
     V3 eh = vsub(eps, mkv(tr / 3.0f, tr / 3.0f, tr / 3.0f));
-    float ehn = vlen(eh);
-    float mu = P->mu[p], lam = P->lam[p];
-    float dg = ehn + (3.0f * lam + 2.0f * mu) / (2.0f * mu) * tr * m->alpha[mat];
+    Real ehn = vlen(eh);
+    Real mu = P->mu[p], lam = P->lam[p];
+    Real dg = ehn + (3.0f * lam + 2.0f * mu) / (2.0f * mu) * tr * m->alpha[mat];
     M3 Fe = Ft;
     if (dg <= 0) Fe = Ft;
     if (dg > 0 && tr > 0) Fe = mmul(U, mT(V));
@@ -452,11 +501,11 @@ constexpr int kOwnerMask = 3 << kOwnerShift;
 struct CdfState {
     int n_grid = 0, nb = 0, n = 0;
     std::vector<int32_t> tag, tag_prev, block;
-    std::vector<float> d, d_prev;
+    std::vector<Real> d, d_prev;
     gbmpm_cdf rec[GBMPM_MAX_CDF];
-    float c_cur[4][3] = {}, v_cur[4][3] = {}, w_cur[4][3] = {};
-    float c_prev[4][3] = {}, v_prev[4][3] = {}, w_prev[4][3] = {};
-    float fric[4] = {};
+    Real c_cur[4][3] = {}, v_cur[4][3] = {}, w_cur[4][3] = {};
+    Real c_prev[4][3] = {}, v_prev[4][3] = {}, w_prev[4][3] = {};
+    Real fric[4] = {};
     int type[4] = {};
     bool dirty[4] = {}, active[4] = {}, has_prev_box[4] = {};
     int prev_box[4][6] = {};
@@ -492,23 +541,23 @@ bool cdf_stencil_near(const CdfState& S, const int* b);
 struct Weights;
 int cdf_particle_tag(const CdfState& S, const Weights& W, bool use_prev);
 int cdf_persist(int old, int fresh);
-V3 cdf_ghost(const CdfState& S, const gbmpm_model* M, float dt, V3 xp, V3 vp, int pc, const Weights& W);
+V3 cdf_ghost(const CdfState& S, const gbmpm_model* M, Real dt, V3 xp, V3 vp, int pc, const Weights& W);
 
 // ----------------------------------------------------- particle stages -----
 struct Weights {
     int base[3];
-    float fx[3];
-    float w[3][3];   // w[axis][i]
-    float dw[3][3];
+    Real fx[3];
+    Real w[3][3];   // w[axis][i]
+    Real dw[3][3];
 };
 
-inline void bspline(const float* x, float inv_dx, Weights& W) {
+inline void bspline(const Real* x, Real inv_dx, Weights& W) {
     for (int a = 0; a < 3; ++a) {
-        float gp = x[a] * inv_dx;
+        Real gp = x[a] * inv_dx;
         W.base[a] = (int)std::floor(gp - 0.5f);
-        W.fx[a] = gp - (float)W.base[a];
-        float fx = W.fx[a];
-        float wa = 1.5f - fx, wb = fx - 1.0f, wc = fx - 0.5f;
+        W.fx[a] = gp - (Real)W.base[a];
+        Real fx = W.fx[a];
+        Real wa = 1.5f - fx, wb = fx - 1.0f, wc = fx - 0.5f;
         W.w[a][0] = wa * wa * 0.5f;
         W.w[a][1] = (0.0f - wb * wb) + 0.75f;
         W.w[a][2] = wc * wc * 0.5f;
@@ -519,7 +568,7 @@ inline void bspline(const float* x, float inv_dx, Weights& W) {
 }
 
 // compute_dweight (mpm_utils.py:601-610)
-inline V3 dweight(const Weights& W, int i, int j, int k, float inv_dx) {
+inline V3 dweight(const Weights& W, int i, int j, int k, Real inv_dx) {
     V3 d = mkv(W.dw[0][i] * W.w[1][j] * W.w[2][k], W.w[0][i] * W.dw[1][j] * W.w[2][k],
                W.w[0][i] * W.w[1][j] * W.dw[2][k]);
     return vscale(d, inv_dx);
@@ -527,7 +576,7 @@ inline V3 dweight(const Weights& W, int i, int j, int k, float inv_dx) {
 
 struct Grid {
     int n = 0;
-    std::vector<float> m, vin, vout;   // m[n^3], vin/vout[n^3][3]
+    std::vector<Real> m, vin, vout;   // m[n^3], vin/vout[n^3][3]
     // box of nodes written since the last zero: [lo, hi) per axis
     int lo[3], hi[3];
     int plo[3], phi[3];
@@ -546,21 +595,21 @@ struct Grid {
 thread_local const char* g_err = "";
 
 struct Ctx {
-    const gbmpm_particles* P;
+    const RP* P;
     const gbmpm_model* M;
     Grid* G;
-    float dt;
+    Real dt;
     bool atomic;   // parallel mode
     int oob;
     CdfState* cdf = nullptr;     // CPIC lanes (null or n == 0: feature off)
-    float* cdf_wrench = nullptr; // [4][6] blocked-deposit reaction
+    Real* cdf_wrench = nullptr; // [4][6] blocked-deposit reaction
 };
 
 inline int wrapx(int ix, int n) { return ((ix % n) + n) % n; }
 
 // p2g_particle (mpm_utils.py:819-916), CDF branch omitted (no CDF colliders)
 void p2g_particle(Ctx& c, int p) {
-    const gbmpm_particles* P = c.P;
+    const RP* P = c.P;
     const gbmpm_model* M = c.M;
     Grid& G = *c.G;
     M3 stress = load33(P->stress + 9 * (size_t)p);
@@ -573,10 +622,10 @@ void p2g_particle(Ctx& c, int p) {
         if (b0 < 0 || b1 >= n) { c.oob = 1; return; }
     }
     M3 C = load33(P->C + 9 * (size_t)p);
-    float r = M->rpic_damping;
+    Real r = M->rpic_damping;
     C = madd(mscale(C, 1.0f - r), mscale(msub(C, mT(C)), r / 2.0f));
     if (r < -0.001f) C = zero33();
-    float mass = P->mass[p], vol = P->vol[p];
+    Real mass = P->mass[p], vol = P->vol[p];
     V3 v = load3(P->v + 3 * (size_t)p);
     M3 fs = mscale(stress, -vol);
     int pc = 0;
@@ -585,22 +634,22 @@ void p2g_particle(Ctx& c, int p) {
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j)
             for (int k = 0; k < 3; ++k) {
-                V3 dpos = vscale(vsub(mkv((float)i, (float)j, (float)k), mkv(W.fx[0], W.fx[1], W.fx[2])), M->dx);
+                V3 dpos = vscale(vsub(mkv((Real)i, (Real)j, (Real)k), mkv(W.fx[0], W.fx[1], W.fx[2])), M->dx);
                 int ix = W.base[0] + i, iy = W.base[1] + j, iz = W.base[2] + k;
                 if (M->periodic_x) ix = wrapx(ix, n);
-                float weight = W.w[0][i] * W.w[1][j] * W.w[2][k];
+                Real weight = W.w[0][i] * W.w[1][j] * W.w[2][k];
                 V3 dwt = dweight(W, i, j, k, M->inv_dx);
                 V3 ef = mvmul(fs, dwt);
                 V3 add = vadd(vscale(vadd(v, mvmul(C, dpos)), weight * mass), vscale(ef, c.dt));
                 size_t id = G.idx(ix, iy, iz);
-                float dm = weight * mass;
+                Real dm = weight * mass;
                 if (pc != 0) {
                     int nt = c.cdf->tag[id];
                     if (cdf_incompatible(pc, nt)) {   // blocked deposit = reaction on the sheet
                         int own = (nt >> kOwnerShift) & 3;
-                        V3 xw = mkv((float)ix * M->dx, (float)iy * M->dx, (float)iz * M->dx);
+                        V3 xw = mkv((Real)ix * M->dx, (Real)iy * M->dx, (Real)iz * M->dx);
                         V3 tq = vcross(vsub(xw, load3(c.cdf->c_cur[own])), add);
-                        float* acc = c.cdf_wrench + 6 * own;
+                        Real* acc = c.cdf_wrench + 6 * own;
                         for (int a = 0; a < 3; ++a) {
                             if (c.atomic) {
 #pragma omp atomic
@@ -634,8 +683,8 @@ void p2g_particle(Ctx& c, int p) {
 }
 
 // update_cov (mpm_utils.py:613-633)
-void update_cov(const gbmpm_particles* P, int p, const M3& gv, float dt) {
-    float* c6 = P->cov + 6 * (size_t)p;
+void update_cov(const RP* P, int p, const M3& gv, Real dt) {
+    Real* c6 = P->cov + 6 * (size_t)p;
     M3 cn;
     cn.m[0][0] = c6[0]; cn.m[0][1] = c6[1]; cn.m[0][2] = c6[2];
     cn.m[1][0] = c6[1]; cn.m[1][1] = c6[3]; cn.m[1][2] = c6[4];
@@ -647,7 +696,7 @@ void update_cov(const gbmpm_particles* P, int p, const M3& gv, float dt) {
 
 // g2p_particle (mpm_utils.py:944-1043), CDF branch omitted
 void g2p_particle(Ctx& c, int p) {
-    const gbmpm_particles* P = c.P;
+    const RP* P = c.P;
     const gbmpm_model* M = c.M;
     Grid& G = *c.G;
     Weights W;
@@ -673,8 +722,8 @@ void g2p_particle(Ctx& c, int p) {
             for (int k = 0; k < 3; ++k) {
                 int ix = W.base[0] + i, iy = W.base[1] + j, iz = W.base[2] + k;
                 if (M->periodic_x) ix = wrapx(ix, n);
-                V3 dpos = vsub(mkv((float)i, (float)j, (float)k), mkv(W.fx[0], W.fx[1], W.fx[2]));
-                float weight = W.w[0][i] * W.w[1][j] * W.w[2][k];
+                V3 dpos = vsub(mkv((Real)i, (Real)j, (Real)k), mkv(W.fx[0], W.fx[1], W.fx[2]));
+                Real weight = W.w[0][i] * W.w[1][j] * W.w[2][k];
                 size_t id = G.idx(ix, iy, iz);
                 V3 gv = load3(&G.vout[3 * id]);
                 if (pc != 0 && cdf_incompatible(pc, c.cdf->tag_prev[id])) gv = ghost;
@@ -687,7 +736,7 @@ void g2p_particle(Ctx& c, int p) {
     V3 x = load3(P->x + 3 * (size_t)p);
     V3 xn = vadd(x, vscale(nv, c.dt));
     if (M->periodic_x) {
-        float lx = (float)n * M->dx;
+        Real lx = (Real)n * M->dx;
         if (xn[0] < 0.0f) xn[0] = xn[0] + lx;
         if (xn[0] >= lx) xn[0] = xn[0] - lx;
     }
@@ -701,7 +750,7 @@ void g2p_particle(Ctx& c, int p) {
 
 // stress_update_particle (mpm_utils.py:1056-1149)
 void stress_particle(Ctx& c, int p) {
-    const gbmpm_particles* P = c.P;
+    const RP* P = c.P;
     const gbmpm_model* M = c.M;
     int mat = P->material[p];
     M3 Ft = load33(P->F_trial + 9 * (size_t)p);
@@ -713,14 +762,14 @@ void stress_particle(Ctx& c, int p) {
     else if (mat == 13) F = rm_mu_i(Ft, P, M, p, mat, c.dt, true);
     else if (mat == 11) F = rm_mu_i_phi(Ft, P, M, p, mat, c.dt);
     else if (mat == 6 || mat == 10 || mat == 12) {
-        float J = mdet(Ft);
-        float Jc = std::pow(J, 1.0f / 3.0f);
+        Real J = mdet(Ft);
+        Real Jc = std::pow(J, 1.0f / 3.0f);
         F = diag33(Jc, Jc, Jc);
     } else if (mat == 7 || mat == 8) F = ident33();
     else F = Ft;
     store33(P->F + 9 * (size_t)p, F);
 
-    float J = mdet(F);
+    Real J = mdet(F);
     M3 U = zero33(), V = zero33(); V3 sig = mkv(0, 0, 0);
     M3 st = zero33();
     if (mat != 6 && mat != 7 && mat != 8 && mat != 10 && mat != 12) svd3_impl(F, U, sig, V);
@@ -736,9 +785,9 @@ void stress_particle(Ctx& c, int p) {
                               M->eta_table_smax, M->eta_table_n);
     if (mat == 9 || mat == 13) st = stress_hencky(U, sig, P->mu[p], P->lam[p]);
     if (mat == 11) {
-        float Jr = P->Jp[p];
+        Real Jr = P->Jp[p];
         if (Jr < 0.5f) Jr = 1.0f;
-        float pc = mu_i_phi_pressure(M, mat, J, Jr);
+        Real pc = mu_i_phi_pressure(M, mat, J, Jr);
         st = stress_mu_i_phi(U, sig, P->mu[p], pc);
     }
     st = mscale(madd(st, mT(st)), 0.5f);
@@ -748,44 +797,44 @@ void stress_particle(Ctx& c, int p) {
 
 // ------------------------------------------------------------ colliders -----
 // capped_cylinder_sdf / revolved_glass_sdf (mpm_solver_warp.py:29-57)
-float capped_cyl(float r, float z, float rad, float z0, float z1) {
-    float zc = 0.5f * (z0 + z1), hh = 0.5f * (z1 - z0);
-    float dr = r - rad, dz = std::fabs(z - zc) - hh;
-    float dro = std::max(dr, 0.0f), dzo = std::max(dz, 0.0f);
-    float outside = std::sqrt(dro * dro + dzo * dzo);
-    float inside = std::min(std::max(dr, dz), 0.0f);
+Real capped_cyl(Real r, Real z, Real rad, Real z0, Real z1) {
+    Real zc = 0.5f * (z0 + z1), hh = 0.5f * (z1 - z0);
+    Real dr = r - rad, dz = std::fabs(z - zc) - hh;
+    Real dro = std::max<Real>(dr, 0.0f), dzo = std::max<Real>(dz, 0.0f);
+    Real outside = std::sqrt(dro * dro + dzo * dzo);
+    Real inside = std::min<Real>(std::max<Real>(dr, dz), 0.0f);
     return outside + inside;
 }
-float glass_sdf(V3 l, const gbmpm_collider& c) {
-    float r = std::sqrt(l[0] * l[0] + l[1] * l[1]);
-    float d_outer = capped_cyl(r, l[2], c.outer_radius, -c.half_height, c.half_height);
-    float d_cav = capped_cyl(r, l[2], c.inner_radius - c.fillet_radius, c.inner_floor_z + c.fillet_radius,
+Real glass_sdf(V3 l, const gbmpm_collider& c) {
+    Real r = std::sqrt(l[0] * l[0] + l[1] * l[1]);
+    Real d_outer = capped_cyl(r, l[2], c.outer_radius, -c.half_height, c.half_height);
+    Real d_cav = capped_cyl(r, l[2], c.inner_radius - c.fillet_radius, c.inner_floor_z + c.fillet_radius,
                              c.half_height + c.outer_radius) - c.fillet_radius;
     return std::max(d_outer, -d_cav);
 }
 
 // sdf_trilerp (mpm_solver_warp.py:60-74)
-float trilerp(const float* vals, int res, V3 f, int stride, int comp) {
-    float fi = std::min(std::max(f[0], 0.0f), (float)res - 1.0001f);
-    float fj = std::min(std::max(f[1], 0.0f), (float)res - 1.0001f);
-    float fk = std::min(std::max(f[2], 0.0f), (float)res - 1.0001f);
+template <class T> Real trilerp(const T* vals, int res, V3 f, int stride, int comp) {
+    Real fi = std::min<Real>(std::max<Real>(f[0], 0.0f), (Real)res - 1.0001f);
+    Real fj = std::min<Real>(std::max<Real>(f[1], 0.0f), (Real)res - 1.0001f);
+    Real fk = std::min<Real>(std::max<Real>(f[2], 0.0f), (Real)res - 1.0001f);
     int i = (int)std::floor(fi), j = (int)std::floor(fj), k = (int)std::floor(fk);
-    float tx = fi - (float)i, ty = fj - (float)j, tz = fk - (float)k;
+    Real tx = fi - (Real)i, ty = fj - (Real)j, tz = fk - (Real)k;
     auto at = [&](int a, int b, int cc) { return vals[(((size_t)a * res + b) * res + cc) * stride + comp]; };
-    float c00 = at(i, j, k) * (1.0f - tx) + at(i + 1, j, k) * tx;
-    float c01 = at(i, j, k + 1) * (1.0f - tx) + at(i + 1, j, k + 1) * tx;
-    float c10 = at(i, j + 1, k) * (1.0f - tx) + at(i + 1, j + 1, k) * tx;
-    float c11 = at(i, j + 1, k + 1) * (1.0f - tx) + at(i + 1, j + 1, k + 1) * tx;
-    float c0 = c00 * (1.0f - ty) + c10 * ty;
-    float c1 = c01 * (1.0f - ty) + c11 * ty;
+    Real c00 = at(i, j, k) * (1.0f - tx) + at(i + 1, j, k) * tx;
+    Real c01 = at(i, j, k + 1) * (1.0f - tx) + at(i + 1, j, k + 1) * tx;
+    Real c10 = at(i, j + 1, k) * (1.0f - tx) + at(i + 1, j + 1, k) * tx;
+    Real c11 = at(i, j + 1, k + 1) * (1.0f - tx) + at(i + 1, j + 1, k + 1) * tx;
+    Real c0 = c00 * (1.0f - ty) + c10 * ty;
+    Real c1 = c01 * (1.0f - ty) + c11 * ty;
     return c0 * (1.0f - tz) + c1 * tz;
 }
 
 // warp quat_rotate / quat_rotate_inv: x(2w^2-1) +/- 2w(q x x) + 2q(q.x)
-V3 qrot(const float q[4], V3 x, bool inv) {
+template <class T> V3 qrot(const T q[4], V3 x, bool inv) {
     V3 qv = mkv(q[0], q[1], q[2]);
-    float w = q[3];
-    float c = 2.0f * w * w - 1.0f;
+    Real w = q[3];
+    Real c = 2.0f * w * w - 1.0f;
     V3 a = vscale(x, c);
     V3 b = vscale(vscale(vcross(qv, x), w), 2.0f);
     V3 d = vscale(vscale(qv, vdot(qv, x)), 2.0f);
@@ -793,19 +842,19 @@ V3 qrot(const float q[4], V3 x, bool inv) {
 }
 
 struct NodeCtx {
-    float time;
-    float dt;
+    Real time;
+    Real dt;
     const gbmpm_model* M;
 };
 
 // one collider applied to one node; returns true when the node was handled
-void collide_node(const gbmpm_collider& c, int gx, int gy, int gz, float m, float* vout, const NodeCtx& nc,
-                  float* acc /* force[3], torque[3] fp32 */, bool atomic) {
+void collide_node(const gbmpm_collider& c, int gx, int gy, int gz, Real m, Real* vout, const NodeCtx& nc,
+                  Real* acc /* force[3], torque[3] fp32 */, bool atomic) {
     const gbmpm_model* M = nc.M;
-    float dx = M->dx;
+    Real dx = M->dx;
     if (m <= 0.0f) return;   // mass gate (mpm_solver_warp.py:1942 and the other collide kernels)
     bool live = nc.time >= c.start_time && nc.time < c.end_time;
-    auto addacc = [&](int i, float v) {
+    auto addacc = [&](int i, Real v) {
         if (atomic) {
 #pragma omp atomic
             acc[i] += v;
@@ -816,14 +865,14 @@ void collide_node(const gbmpm_collider& c, int gx, int gy, int gz, float m, floa
     switch (c.kind) {
     case GBMPM_COLLIDER_PLANE: {  // mpm_solver_warp.py:1929-1992
         if (!live) return;
-        V3 off = mkv((float)gx * dx - c.point[0], (float)gy * dx - c.point[1], (float)gz * dx - c.point[2]);
+        V3 off = mkv((Real)gx * dx - c.point[0], (Real)gy * dx - c.point[1], (Real)gz * dx - c.point[2]);
         V3 n = mkv(c.normal[0], c.normal[1], c.normal[2]);
-        float dp = vdot(off, n);
+        Real dp = vdot(off, n);
         if (dp < 0.0f) {
             if (c.surface_type == 0) {
                 vout[0] = vout[1] = vout[2] = 0.0f;
             } else if (c.surface_type == 11) {
-                if ((float)gz * dx < 0.4f || (float)gz * dx > 0.53f) {
+                if ((Real)gz * dx < 0.4f || (Real)gz * dx > 0.53f) {
                     vout[0] = vout[1] = vout[2] = 0.0f;
                 } else {
                     V3 vi = load3(vout);
@@ -832,11 +881,11 @@ void collide_node(const gbmpm_collider& c, int gx, int gy, int gz, float m, floa
                 }
             } else {
                 V3 v = load3(vout);
-                float nc_ = vdot(v, n);
+                Real nc_ = vdot(v, n);
                 if (c.surface_type == 1) v = vsub(v, vscale(n, nc_));
-                else v = vsub(v, vscale(n, std::min(nc_, 0.0f)));
+                else v = vsub(v, vscale(n, std::min<Real>(nc_, 0.0f)));
                 if (nc_ < 0.0f && vlen(v) > 1e-20f) {
-                    float s = std::max(0.0f, vlen(v) + nc_ * c.friction);
+                    Real s = std::max<Real>(0.0f, vlen(v) + nc_ * c.friction);
                     v = vscale(vnormalize(v), s);
                 }
                 store3(vout, v);
@@ -846,7 +895,7 @@ void collide_node(const gbmpm_collider& c, int gx, int gy, int gz, float m, floa
     }
     case GBMPM_COLLIDER_BOX: {  // mpm_solver_warp.py:2053-2088
         if (live) {
-            V3 off = mkv((float)gx * dx - c.point[0], (float)gy * dx - c.point[1], (float)gz * dx - c.point[2]);
+            V3 off = mkv((Real)gx * dx - c.point[0], (Real)gy * dx - c.point[1], (Real)gz * dx - c.point[2]);
             if (std::fabs(off[0]) < c.size[0] && std::fabs(off[1]) < c.size[1] && std::fabs(off[2]) < c.size[2]) {
                 V3 vf = load3(vout);
                 V3 vb = mkv(c.velocity[0], c.velocity[1], c.velocity[2]);
@@ -861,11 +910,11 @@ void collide_node(const gbmpm_collider& c, int gx, int gy, int gz, float m, floa
     }
     case GBMPM_COLLIDER_CUP: {  // mpm_solver_warp.py:2161-2225
         if (!live) return;
-        V3 xn = mkv((float)gx * dx, (float)gy * dx, (float)gz * dx);
+        V3 xn = mkv((Real)gx * dx, (Real)gy * dx, (Real)gz * dx);
         V3 rel = vsub(xn, mkv(c.point[0], c.point[1], c.point[2]));
         M3 R = load33(c.rot);
         V3 local = mvmul(mT(R), rel);
-        float sdf = glass_sdf(local, c);
+        Real sdf = glass_sdf(local, c);
         if (sdf < c.contact_band) {
             V3 vs = vadd(mkv(c.velocity[0], c.velocity[1], c.velocity[2]),
                          vcross(mkv(c.omega[0], c.omega[1], c.omega[2]), rel));
@@ -873,19 +922,19 @@ void collide_node(const gbmpm_collider& c, int gx, int gy, int gz, float m, floa
             V3 vnew = vs;
             if (sdf > -c.sticky_depth) {
                 vnew = vin;
-                float h = 0.25f * dx;
+                Real h = 0.25f * dx;
                 V3 nl = mkv(glass_sdf(vadd(local, mkv(h, 0, 0)), c) - glass_sdf(vsub(local, mkv(h, 0, 0)), c),
                             glass_sdf(vadd(local, mkv(0, h, 0)), c) - glass_sdf(vsub(local, mkv(0, h, 0)), c),
                             glass_sdf(vadd(local, mkv(0, 0, h)), c) - glass_sdf(vsub(local, mkv(0, 0, h)), c));
-                float nl_len = vlen(nl);
+                Real nl_len = vlen(nl);
                 if (nl_len > 1.0e-12f) {
                     V3 n = mvmul(R, vdivs(nl, nl_len));
                     V3 vr = vsub(vin, vs);
-                    float vn = vdot(vr, n);
+                    Real vn = vdot(vr, n);
                     if (vn < 0.0f) {
                         V3 vt = vsub(vr, vscale(n, vn));
-                        float vtl = vlen(vt);
-                        if (vtl > 1.0e-20f) vt = vscale(vdivs(vt, vtl), std::max(vtl + c.friction * vn, 0.0f));
+                        Real vtl = vlen(vt);
+                        if (vtl > 1.0e-20f) vt = vscale(vdivs(vt, vtl), std::max<Real>(vtl + c.friction * vn, 0.0f));
                         vnew = vadd(vs, vt);
                     }
                 }
@@ -911,15 +960,15 @@ void collide_node(const gbmpm_collider& c, int gx, int gy, int gz, float m, floa
     }
     case GBMPM_COLLIDER_SDF: {  // mpm_solver_warp.py:2680-2736
         if (!live) return;
-        V3 xw = mkv((float)gx * dx, (float)gy * dx, (float)gz * dx);
+        V3 xw = mkv((Real)gx * dx, (Real)gy * dx, (Real)gz * dx);
         V3 rel = vsub(xw, mkv(c.point[0], c.point[1], c.point[2]));
         V3 body = qrot(c.quat, rel, true);
         V3 f = mkv((body[0] - c.sdf_origin[0]) / c.sdf_cell, (body[1] - c.sdf_origin[1]) / c.sdf_cell,
                    (body[2] - c.sdf_origin[2]) / c.sdf_cell);
-        float rf = (float)c.sdf_res - 1.0f;
+        Real rf = (Real)c.sdf_res - 1.0f;
         bool inside = f[0] >= 0.0f && f[1] >= 0.0f && f[2] >= 0.0f && f[0] <= rf && f[1] <= rf && f[2] <= rf;
         if (!inside) return;
-        float sd = trilerp(c.sdf_val, c.sdf_res, f, 1, 0);
+        Real sd = trilerp(c.sdf_val, c.sdf_res, f, 1, 0);
         if (sd <= c.band) {
             V3 g = mkv(trilerp(c.sdf_grad, c.sdf_res, f, 3, 0), trilerp(c.sdf_grad, c.sdf_res, f, 3, 1),
                        trilerp(c.sdf_grad, c.sdf_res, f, 3, 2));
@@ -929,14 +978,14 @@ void collide_node(const gbmpm_collider& c, int gx, int gy, int gz, float m, floa
                              vcross(mkv(c.omega[0], c.omega[1], c.omega[2]), rel));
                 V3 vf = load3(vout);
                 V3 vr = vsub(vf, vs);
-                float vn = vdot(vr, nw);
+                Real vn = vdot(vr, nw);
                 V3 vnew = vf;
                 if (c.surface_type == 0) vnew = vs;
                 else if (c.surface_type == 1) vnew = vadd(vs, vsub(vr, vscale(nw, vn)));
                 else if (vn < 0.0f) {
                     V3 vt = vsub(vr, vscale(nw, vn));
-                    float tl = vlen(vt);
-                    if (tl > 1.0e-12f) vt = vscale(vt, std::max(0.0f, tl + c.friction * vn) / tl);
+                    Real tl = vlen(vt);
+                    if (tl > 1.0e-12f) vt = vscale(vt, std::max<Real>(0.0f, tl + c.friction * vn) / tl);
                     vnew = vadd(vs, vt);
                 }
                 V3 imp = vscale(vsub(vf, vnew), m);
@@ -958,7 +1007,7 @@ void integrate_pose(gbmpm_collider& c, double time, double dt) {
     if (!live) return;
     if (c.kind == GBMPM_COLLIDER_BOX || c.kind == GBMPM_COLLIDER_CUP || c.kind == GBMPM_COLLIDER_SDF) {
         // box: mpm_solver_warp.py:2090-2096; cup: :2227-2233; sdf: :2756
-        for (int i = 0; i < 3; ++i) c.point[i] = (float)((double)c.point[i] + dt * (double)c.velocity[i]);
+        for (int i = 0; i < 3; ++i) c.point[i] = (Real)((double)c.point[i] + dt * (double)c.velocity[i]);
     }
     if (c.kind == GBMPM_COLLIDER_CUP) {  // Rodrigues on the float64 shadow (:2234-2254)
         double w[3] = {c.omega[0], c.omega[1], c.omega[2]};
@@ -984,7 +1033,7 @@ void integrate_pose(gbmpm_collider& c, double time, double dt) {
                     Rn[i][j] = acc;
                 }
             for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) { c.rot64[3 * i + j] = Rn[i][j]; c.rot[3 * i + j] = (float)Rn[i][j]; }
+                for (int j = 0; j < 3; ++j) { c.rot64[3 * i + j] = Rn[i][j]; c.rot[3 * i + j] = (Real)Rn[i][j]; }
         }
     }
     if (c.kind == GBMPM_COLLIDER_SDF) {  // _omega_step_quat (mpm_solver_warp.py:198-210)
@@ -1000,7 +1049,7 @@ void integrate_pose(gbmpm_collider& c, double time, double dt) {
                            d[3] * q[2] + d[0] * q[1] - d[1] * q[0] + d[2] * q[3],
                            d[3] * q[3] - d[0] * q[0] - d[1] * q[1] - d[2] * q[2]};
             double nr = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3]);
-            for (int i = 0; i < 4; ++i) c.quat[i] = (float)(r[i] / nr);
+            for (int i = 0; i < 4; ++i) c.quat[i] = (Real)(r[i] / nr);
         }
     }
 }
@@ -1023,20 +1072,20 @@ bool cdf_stencil_near(const CdfState& S, const int* b) {
 
 // cdf_particle_tag (mpm_utils.py:678-713)
 int cdf_particle_tag(const CdfState& S, const Weights& W, bool use_prev) {
-    float votes[4] = {0.f, 0.f, 0.f, 0.f};
+    Real votes[4] = {0.f, 0.f, 0.f, 0.f};
     int seen = 0;
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j)
             for (int k = 0; k < 3; ++k) {
                 size_t id = S.idx(W.base[0] + i, W.base[1] + j, W.base[2] + k);
                 int t = use_prev ? S.tag_prev[id] : S.tag[id];
-                float dd = use_prev ? S.d_prev[id] : S.d[id];
+                Real dd = use_prev ? S.d_prev[id] : S.d[id];
                 if (t == 0) continue;
-                float weight = W.w[0][i] * W.w[1][j] * W.w[2][k];
+                Real weight = W.w[0][i] * W.w[1][j] * W.w[2][k];
                 for (int lane = 0; lane < 4; ++lane)
                     if ((t >> (2 * lane)) & 1) {
                         seen |= 1 << (2 * lane);
-                        float sgn = ((t >> (2 * lane + 1)) & 1) ? 1.0f : -1.0f;
+                        Real sgn = ((t >> (2 * lane + 1)) & 1) ? 1.0f : -1.0f;
                         votes[lane] = votes[lane] + weight * dd * sgn;
                     }
             }
@@ -1061,10 +1110,10 @@ int cdf_persist(int old, int fresh) {
 }
 
 // cdf_particle_ghost (mpm_utils.py:733-816)
-V3 cdf_ghost(const CdfState& S, const gbmpm_model* M, float dt, V3 xp, V3 vp, int pc, const Weights& W) {
-    float d_hat = 0.0f;
+V3 cdf_ghost(const CdfState& S, const gbmpm_model* M, Real dt, V3 xp, V3 vp, int pc, const Weights& W) {
+    Real d_hat = 0.0f;
     V3 n_acc = mkv(0, 0, 0);
-    float best_w = 0.0f;
+    Real best_w = 0.0f;
     int lane_p = 0;
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j)
@@ -1074,9 +1123,9 @@ V3 cdf_ghost(const CdfState& S, const gbmpm_model* M, float dt, V3 xp, V3 vp, in
                 if (t == 0) continue;
                 int own = (t >> kOwnerShift) & 3;
                 if (((t >> (2 * own)) & 1) == 0) continue;
-                float weight = W.w[0][i] * W.w[1][j] * W.w[2][k];
-                float sgn = ((t >> (2 * own + 1)) & 1) ? 1.0f : -1.0f;
-                float dd = S.d_prev[id];
+                Real weight = W.w[0][i] * W.w[1][j] * W.w[2][k];
+                Real sgn = ((t >> (2 * own + 1)) & 1) ? 1.0f : -1.0f;
+                Real dd = S.d_prev[id];
                 d_hat = d_hat + weight * sgn * dd;
                 V3 dwt = dweight(W, i, j, k, M->inv_dx);
                 n_acc = vadd(n_acc, vscale(vscale(dwt, sgn), dd));
@@ -1087,16 +1136,16 @@ V3 cdf_ghost(const CdfState& S, const gbmpm_model* M, float dt, V3 xp, V3 vp, in
     V3 ghost = v_free;
     if (vlen(n_acc) > 1.0e-12f) {
         V3 n_hat = vnormalize(n_acc);
-        float side = ((pc >> (2 * lane_p + 1)) & 1) ? 1.0f : -1.0f;
+        Real side = ((pc >> (2 * lane_p + 1)) & 1) ? 1.0f : -1.0f;
         V3 n_par = vscale(n_hat, side);
         V3 rel = vsub(xp, load3(S.c_prev[lane_p]));
         V3 v_surf = vadd(load3(S.v_prev[lane_p]), vcross(load3(S.w_prev[lane_p]), rel));
         V3 v_rel = vsub(v_free, v_surf);
-        float vn = vdot(v_rel, n_par);
+        Real vn = vdot(v_rel, n_par);
         V3 v_tan = vsub(v_rel, vscale(n_par, vn));
-        float c = 0.0f;
-        float d_side = d_hat * side;
-        float eps = 0.05f * M->dx;
+        Real c = 0.0f;
+        Real d_side = d_hat * side;
+        Real eps = 0.05f * M->dx;
         if (d_side < eps) c = std::min((eps - d_side) / dt, 0.5f * M->dx / dt);
         int stype = S.type[lane_p];
         if (stype == 0) {
@@ -1104,13 +1153,13 @@ V3 cdf_ghost(const CdfState& S, const gbmpm_model* M, float dt, V3 xp, V3 vp, in
         } else if (stype == 1) {
             ghost = vadd(vadd(v_surf, v_tan), vscale(n_par, c));
         } else {
-            float dvn = std::max(-vn, 0.0f) + c;
-            float tlen = vlen(v_tan);
+            Real dvn = std::max<Real>(-vn, 0.0f) + c;
+            Real tlen = vlen(v_tan);
             if (tlen > 1.0e-12f && dvn > 0.0f) {
-                float sc = std::max(0.0f, tlen - S.fric[lane_p] * dvn) / tlen;
+                Real sc = std::max<Real>(0.0f, tlen - S.fric[lane_p] * dvn) / tlen;
                 v_tan = vscale(v_tan, sc);
             }
-            ghost = vadd(vadd(vadd(v_surf, v_tan), vscale(n_par, std::max(vn, 0.0f))), vscale(n_par, c));
+            ghost = vadd(vadd(vadd(v_surf, v_tan), vscale(n_par, std::max<Real>(vn, 0.0f))), vscale(n_par, c));
         }
     }
     return ghost;
@@ -1134,7 +1183,7 @@ bool cdf_lane_box(const gbmpm_cdf& r, const gbmpm_model* M, int* box) {
                     hi[i] = std::max(hi[i], p);
                 }
             }
-    double dx = (double)M->grid_lim / M->n_grid;   // python float grid_lim / n_grid
+    double dx = (double)M->grid_lim / M->n_grid;   // python Real grid_lim / n_grid
     for (int i = 0; i < 3; ++i) {
         int l = std::max(0, (int)std::floor(lo[i] / dx) - 2);
         int h = std::min(M->n_grid, (int)std::ceil(hi[i] / dx) + 2 + 1);
@@ -1146,22 +1195,22 @@ bool cdf_lane_box(const gbmpm_cdf& r, const gbmpm_model* M, int* box) {
 }
 
 // cdf_stamp kernel body (mpm_solver_warp.py:146-183) for one lane over a box
-void cdf_stamp_lane(CdfState& S, const gbmpm_model* M, const gbmpm_cdf& r, int lane, float time_f, const int* box) {
+void cdf_stamp_lane(CdfState& S, const gbmpm_model* M, const gbmpm_cdf& r, int lane, Real time_f, const int* box) {
     if (time_f < r.start_time || time_f >= r.end_time) return;
-    float rf = (float)r.res - 1.0f;
+    Real rf = (Real)r.res - 1.0f;
     for (int x = box[0]; x < box[3]; ++x)
         for (int y = box[1]; y < box[4]; ++y)
             for (int z = box[2]; z < box[5]; ++z) {
-                V3 xw = mkv((float)x * M->dx, (float)y * M->dx, (float)z * M->dx);
+                V3 xw = mkv((Real)x * M->dx, (Real)y * M->dx, (Real)z * M->dx);
                 V3 rel = vsub(xw, mkv(r.center[0], r.center[1], r.center[2]));
                 V3 body = qrot(r.quat, rel, true);
                 V3 f = mkv((body[0] - r.origin[0]) / r.cell, (body[1] - r.origin[1]) / r.cell,
                            (body[2] - r.origin[2]) / r.cell);
                 if (f[0] < 0.0f || f[1] < 0.0f || f[2] < 0.0f || f[0] > rf || f[1] > rf || f[2] > rf) continue;
-                float ok = trilerp(r.valid, r.res, f, 1, 0);
+                Real ok = trilerp(r.valid, r.res, f, 1, 0);
                 if (ok < 0.999f) continue;
-                float dd = trilerp(r.values, r.res, f, 1, 0);
-                float ud = std::fabs(dd);
+                Real dd = trilerp(r.values, r.res, f, 1, 0);
+                Real ud = std::fabs(dd);
                 if (ud > r.band) continue;
                 int side = dd >= 0.0f ? 1 : 0;
                 size_t id = S.idx(x, y, z);
@@ -1222,7 +1271,7 @@ void cdf_stamp(CdfState& S, const gbmpm_model* M, double time, bool lag_prev) {
                 S.tag[id] = 0;
                 S.d[id] = 1.0e9f;
             }
-    float tf = (float)time;
+    Real tf = (Real)time;
     for (int l = 0; l < S.n; ++l) {
         int lb[6];
         if (!cdf_lane_box(S.rec[l], M, lb)) continue;
@@ -1265,7 +1314,7 @@ void cdf_integrate(CdfState& S, double time, double dt, bool lag_prev) {
         if (r.velocity[0] == 0.0f && r.velocity[1] == 0.0f && r.velocity[2] == 0.0f && r.omega[0] == 0.0f &&
             r.omega[1] == 0.0f && r.omega[2] == 0.0f)
             continue;
-        for (int a = 0; a < 3; ++a) r.center[a] = (float)((double)r.center[a] + dt * (double)r.velocity[a]);
+        for (int a = 0; a < 3; ++a) r.center[a] = (Real)((double)r.center[a] + dt * (double)r.velocity[a]);
         double w[3] = {r.omega[0], r.omega[1], r.omega[2]};
         double sp = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
         if (!(sp * dt < 1e-12)) {
@@ -1277,7 +1326,7 @@ void cdf_integrate(CdfState& S, double time, double dt, bool lag_prev) {
                            dq[3] * q[2] + dq[0] * q[1] - dq[1] * q[0] + dq[2] * q[3],
                            dq[3] * q[3] - dq[0] * q[0] - dq[1] * q[1] - dq[2] * q[2]};
             double nr = std::sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2] + o[3] * o[3]);
-            for (int i = 0; i < 4; ++i) r.quat[i] = (float)(o[i] / nr);
+            for (int i = 0; i < 4; ++i) r.quat[i] = (Real)(o[i] / nr);
         }
         S.sync_lane(l);
         S.dirty[l] = true;
@@ -1301,14 +1350,14 @@ template <class Fn> void par_for(int n, bool par, Fn fn) {
     }
 }
 
-void track_box(Grid& G, const gbmpm_particles* P, const gbmpm_model* M) {
+void track_box(Grid& G, const RP* P, const gbmpm_model* M) {
     // nodes the coming scatter can touch: every selected particle's stencil
     G.reset_box();
     int lo[3] = {G.n, G.n, G.n}, hi[3] = {0, 0, 0};
     for (int p = 0; p < P->n; ++p) {
         if (P->selection && P->selection[p] != 0) continue;
         for (int a = 0; a < 3; ++a) {
-            float gp = P->x[3 * (size_t)p + a] * M->inv_dx;
+            Real gp = P->x[3 * (size_t)p + a] * M->inv_dx;
             int b = (int)std::floor(gp - 0.5f);
             if (a == 0 && M->periodic_x) { lo[0] = 0; hi[0] = G.n; continue; }
             lo[a] = std::min(lo[a], std::max(b, 0));
@@ -1330,8 +1379,8 @@ void zero_box(Grid& G, const int* lo, const int* hi, bool m_vin, bool vout) {
 
 // grid_normalization_and_gravity (mpm_utils.py:927-941), add_damping_via_grid
 // (:1287-1295) and the collider kernels, over the box of touched nodes
-void grid_update(Grid& G, const gbmpm_model* M, gbmpm_collider* cols, int ncol, float* wrench, float time_f,
-                 float dt, bool par) {
+void grid_update(Grid& G, const gbmpm_model* M, gbmpm_collider* cols, int ncol, Real* wrench, Real time_f,
+                 Real dt, bool par) {
     int nx = G.hi[0] - G.lo[0];
     if (nx <= 0) return;
     NodeCtx nc{time_f, dt, M};
@@ -1340,9 +1389,9 @@ void grid_update(Grid& G, const gbmpm_model* M, gbmpm_collider* cols, int ncol, 
         for (int y = G.lo[1]; y < G.hi[1]; ++y)
             for (int z = G.lo[2]; z < G.hi[2]; ++z) {
                 size_t id = G.idx(x, y, z);
-                float m = G.m[id];
+                Real m = G.m[id];
                 if (m > 1e-15f) {
-                    float inv = 1.0f / m;
+                    Real inv = 1.0f / m;
                     for (int a = 0; a < 3; ++a) G.vout[3 * id + a] = G.vin[3 * id + a] * inv + dt * M->gravity[a];
                 }
             }
@@ -1381,50 +1430,56 @@ RigidState g_rigid;
 // pre-P2G operations and velocity modifiers (mpm_solver_warp.py:1182-1196,
 // 2385-2540) on every selected particle whose mod_mask bit is set: impulses first,
 // then velocity overrides, each in list order, on the float32 window [start, end)
-void apply_modifiers(const gbmpm_particles* P, int p, float time_f, float dt) {
+void apply_modifiers(const RP* P, int p, Real time_f, Real dt) {
     const int mask = P->mod_mask ? P->mod_mask[p] : 0;
     if (!mask) return;
-    float* v = P->v + 3 * (size_t)p;
-    const float* x = P->x + 3 * (size_t)p;
+    Real* v = P->v + 3 * (size_t)p;
+    const Real* x = P->x + 3 * (size_t)p;
     for (int pass = 0; pass < 2; ++pass)
         for (size_t m = 0; m < g_rigid.mods.size(); ++m) {
             const gbmpm_modifier& d = g_rigid.mods[m];
             if (!((mask >> m) & 1) || (d.kind == 0) != (pass == 0)) continue;
             if (!(time_f >= d.start_time && time_f < d.end_time)) continue;
             if (d.kind == 0) {
-                const float mass = P->mass[p];
+                const Real mass = P->mass[p];
                 for (int a = 0; a < 3; ++a) v[a] = v[a] + (d.vec[a] / mass) * dt;
             } else if (d.kind == 1) {
                 for (int a = 0; a < 3; ++a) v[a] = d.vec[a];
             } else {
-                float off[3], hz[3];
+                Real off[3], hz[3];
                 for (int a = 0; a < 3; ++a) off[a] = x[a] - d.point[a];
-                const float on = off[0] * d.normal[0] + off[1] * d.normal[1] + off[2] * d.normal[2];
+                const Real on = off[0] * d.normal[0] + off[1] * d.normal[1] + off[2] * d.normal[2];
                 for (int a = 0; a < 3; ++a) hz[a] = off[a] - on * d.normal[a];
-                const float hd = std::sqrt(hz[0] * hz[0] + hz[1] * hz[1] + hz[2] * hz[2]);
-                const float cosine = (off[0] * d.axis1[0] + off[1] * d.axis1[1] + off[2] * d.axis1[2]) / hd;
-                float theta = std::acos(std::min(std::max(cosine, -1.0f), 1.0f));
+                const Real hd = std::sqrt(hz[0] * hz[0] + hz[1] * hz[1] + hz[2] * hz[2]);
+                const Real cosine = (off[0] * d.axis1[0] + off[1] * d.axis1[1] + off[2] * d.axis1[2]) / hd;
+                Real theta = std::acos(std::min<Real>(std::max<Real>(cosine, -1.0f), 1.0f));
                 if (!(off[0] * d.axis2[0] + off[1] * d.axis2[1] + off[2] * d.axis2[2] > 0.0f)) theta = -theta;
-                const float a1 = -hd * std::sin(theta) * d.rotation_scale;
-                const float a2 = hd * std::cos(theta) * d.rotation_scale;
+                const Real a1 = -hd * std::sin(theta) * d.rotation_scale;
+                const Real a2 = hd * std::cos(theta) * d.rotation_scale;
                 for (int a = 0; a < 3; ++a) v[a] = a1 * d.axis1[a] + a2 * d.axis2[a] + d.translation_scale * d.normal[a];
             }
         }
 }
 
-inline void rmul(const float* a, const float* b, float* c) {   // row-major 3x3 product
+template <class A, class B>
+inline void rmul(const A* a, const B* b, Real* c) {   // row-major 3x3 product
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) c[3 * i + j] = a[3 * i] * b[j] + a[3 * i + 1] * b[3 + j] + a[3 * i + 2] * b[6 + j];
+        for (int j = 0; j < 3; ++j)
+            c[3 * i + j] = (Real)a[3 * i] * (Real)b[j] + (Real)a[3 * i + 1] * (Real)b[3 + j] +
+                           (Real)a[3 * i + 2] * (Real)b[6 + j];
 }
-inline void rmulT(const float* a, const float* b, float* c) {  // a b^T
+template <class A, class B>
+inline void rmulT(const A* a, const B* b, Real* c) {  // a b^T
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) c[3 * i + j] = a[3 * i] * b[3 * j] + a[3 * i + 1] * b[3 * j + 1] + a[3 * i + 2] * b[3 * j + 2];
+        for (int j = 0; j < 3; ++j)
+            c[3 * i + j] = (Real)a[3 * i] * (Real)b[3 * j] + (Real)a[3 * i + 1] * (Real)b[3 * j + 1] +
+                           (Real)a[3 * i + 2] * (Real)b[3 * j + 2];
 }
 
 // the rigid tail of one substep (_p2g2p_tail, mpm_solver_warp.py:1338-1367):
 // rigid_g2p_accumulate, rigid_body_integrate, _apply_rigid_restitution (deepest
 // particle by float64 distance, lowest index on a tie) and rigid_particle_update
-void rigid_tail(const gbmpm_particles* P, const gbmpm_model* M, Grid& G, double time, float dt,
+void rigid_tail(const RP* P, const gbmpm_model* M, Grid& G, double time, Real dt,
                 const std::function<bool(int)>& sel) {
     const int nb = (int)g_rigid.bodies.size();
     if (nb == 0) return;
@@ -1433,34 +1488,34 @@ void rigid_tail(const gbmpm_particles* P, const gbmpm_model* M, Grid& G, double 
         if (!sel(p) || P->material[p] != 8) continue;
         Weights W;
         bspline(P->x + 3 * (size_t)p, M->inv_dx, W);
-        float vi[3] = {0.0f, 0.0f, 0.0f};
+        Real vi[3] = {0.0f, 0.0f, 0.0f};
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j)
                 for (int k = 0; k < 3; ++k) {
-                    const float w = W.w[0][i] * W.w[1][j] * W.w[2][k];
+                    const Real w = W.w[0][i] * W.w[1][j] * W.w[2][k];
                     const size_t id = G.idx(W.base[0] + i, W.base[1] + j, W.base[2] + k);
                     for (int a = 0; a < 3; ++a) vi[a] = vi[a] + G.vout[3 * id + a] * w;
                 }
         const int b = P->rigid_id[p];
-        const float m = P->mass[p];
-        const float* x = P->x + 3 * (size_t)p;
-        const float r[3] = {x[0] - g_rigid.bodies[b].x_cm[0], x[1] - g_rigid.bodies[b].x_cm[1],
+        const Real m = P->mass[p];
+        const Real* x = P->x + 3 * (size_t)p;
+        const Real r[3] = {x[0] - g_rigid.bodies[b].x_cm[0], x[1] - g_rigid.bodies[b].x_cm[1],
                             x[2] - g_rigid.bodies[b].x_cm[2]};
-        const float pm[3] = {vi[0] * m, vi[1] * m, vi[2] * m};
-        const float am[3] = {r[1] * pm[2] - r[2] * pm[1], r[2] * pm[0] - r[0] * pm[2], r[0] * pm[1] - r[1] * pm[0]};
+        const Real pm[3] = {vi[0] * m, vi[1] * m, vi[2] * m};
+        const Real am[3] = {r[1] * pm[2] - r[2] * pm[1], r[2] * pm[0] - r[0] * pm[2], r[0] * pm[1] - r[1] * pm[0]};
         for (int a = 0; a < 3; ++a) { acc[6 * b + a] += pm[a]; acc[6 * b + 3 + a] += am[a]; }
     }
     for (int b = 0; b < nb; ++b) {
         gbmpm_rigid_body& r = g_rigid.bodies[b];
-        float v[3], w[3], T1[9], Iw[9];
-        for (int a = 0; a < 3; ++a) v[a] = (float)acc[6 * b + a] / r.mass;
+        Real v[3], w[3], T1[9], Iw[9];
+        for (int a = 0; a < 3; ++a) v[a] = (Real)acc[6 * b + a] / r.mass;
         rmul(r.R, r.inv_inertia, T1);
         rmulT(T1, r.R, Iw);
-        const float L[3] = {(float)acc[6 * b + 3], (float)acc[6 * b + 4], (float)acc[6 * b + 5]};
+        const Real L[3] = {(Real)acc[6 * b + 3], (Real)acc[6 * b + 4], (Real)acc[6 * b + 5]};
         for (int i = 0; i < 3; ++i) w[i] = Iw[3 * i] * L[0] + Iw[3 * i + 1] * L[1] + Iw[3 * i + 2] * L[2];
         for (int a = 0; a < 3; ++a) r.x_cm[a] = r.x_cm[a] + v[a] * dt;
-        const float Wk[9] = {0.0f, -w[2], w[1], w[2], 0.0f, -w[0], -w[1], w[0], 0.0f};
-        float WR[9], Rn[9];
+        const Real Wk[9] = {0.0f, -w[2], w[1], w[2], 0.0f, -w[0], -w[1], w[0], 0.0f};
+        Real WR[9], Rn[9];
         rmul(Wk, r.R, WR);
         for (int i = 0; i < 9; ++i) Rn[i] = r.R[i] + WR[i] * dt;
         M3 Rm = load33(Rn), U, V;
@@ -1471,7 +1526,7 @@ void rigid_tail(const gbmpm_particles* P, const gbmpm_model* M, Grid& G, double 
         // world positions once, from the integrated pose; each surface's deepest
         // particle is taken there and shifted by the pushes of the surfaces before
         // it (the reference adds each push to its world positions)
-        const float xc0[3] = {r.x_cm[0], r.x_cm[1], r.x_cm[2]};
+        const Real xc0[3] = {r.x_cm[0], r.x_cm[1], r.x_cm[2]};
         double pacc[3] = {0.0, 0.0, 0.0};
         for (const gbmpm_rigid_surface& sf : g_rigid.surf) {
             if (!(time >= sf.start_time && time < sf.end_time)) continue;
@@ -1479,10 +1534,10 @@ void rigid_tail(const gbmpm_particles* P, const gbmpm_model* M, Grid& G, double 
             int pmin = -1;
             for (int p = 0; p < P->n; ++p) {
                 if (!sel(p) || P->material[p] != 8 || P->rigid_id[p] != b) continue;
-                const float* xr = P->x_ref + 3 * (size_t)p;
+                const Real* xr = P->x_ref + 3 * (size_t)p;
                 double d = 0.0;
                 for (int i = 0; i < 3; ++i) {
-                    const float xw = xc0[i] + (r.R[3 * i] * xr[0] + r.R[3 * i + 1] * xr[1] + r.R[3 * i + 2] * xr[2]);
+                    const Real xw = xc0[i] + (r.R[3 * i] * xr[0] + r.R[3 * i + 1] * xr[1] + r.R[3 * i + 2] * xr[2]);
                     d += ((double)xw - sf.point[i]) * sf.normal[i];
                 }
                 if (pmin < 0 || d < dmin) { dmin = d; pmin = p; }
@@ -1491,16 +1546,16 @@ void rigid_tail(const gbmpm_particles* P, const gbmpm_model* M, Grid& G, double 
             dmin += pacc[0] * sf.normal[0] + pacc[1] * sf.normal[1] + pacc[2] * sf.normal[2];
             if (!(dmin < 0.0)) continue;
             const double* n = sf.normal;
-            const float* xr = P->x_ref + 3 * (size_t)pmin;
+            const Real* xr = P->x_ref + 3 * (size_t)pmin;
             double xc[3];
             for (int i = 0; i < 3; ++i) {
-                const float xw = xc0[i] + (r.R[3 * i] * xr[0] + r.R[3 * i + 1] * xr[1] + r.R[3 * i + 2] * xr[2]);
+                const Real xw = xc0[i] + (r.R[3 * i] * xr[0] + r.R[3 * i + 1] * xr[1] + r.R[3 * i + 2] * xr[2]);
                 const double push = -dmin * n[i];
                 pacc[i] += push;
                 xc[i] = (double)xw + pacc[i];
-                r.x_cm[i] = (float)((double)r.x_cm[i] + push);
+                r.x_cm[i] = (Real)((double)r.x_cm[i] + push);
             }
-            float Iwf[9];
+            Real Iwf[9];
             rmul(r.R, r.inv_inertia, T1);
             rmulT(T1, r.R, Iwf);
             auto mv = [&](const double* a, double* o) {
@@ -1526,8 +1581,8 @@ void rigid_tail(const gbmpm_particles* P, const gbmpm_model* M, Grid& G, double 
             const double jr[3] = {Jn * rxn[0], Jn * rxn[1], Jn * rxn[2]};
             mv(jr, dw);
             for (int i = 0; i < 3; ++i) {
-                r.v_cm[i] = (float)((double)r.v_cm[i] + (Jn / Mb) * n[i]);
-                r.omega[i] = (float)((double)r.omega[i] + dw[i]);
+                r.v_cm[i] = (Real)((double)r.v_cm[i] + (Jn / Mb) * n[i]);
+                r.omega[i] = (Real)((double)r.omega[i] + dw[i]);
             }
             if (sf.friction > 0.0) {
                 double vt[3];
@@ -1544,8 +1599,8 @@ void rigid_tail(const gbmpm_particles* P, const gbmpm_model* M, Grid& G, double 
                     const double jt[3] = {Jt * rxt[0], Jt * rxt[1], Jt * rxt[2]};
                     mv(jt, dw);
                     for (int i = 0; i < 3; ++i) {
-                        r.v_cm[i] = (float)((double)r.v_cm[i] - (Jt / Mb) * th[i]);
-                        r.omega[i] = (float)((double)r.omega[i] - dw[i]);
+                        r.v_cm[i] = (Real)((double)r.v_cm[i] - (Jt / Mb) * th[i]);
+                        r.omega[i] = (Real)((double)r.omega[i] - dw[i]);
                     }
                 }
             }
@@ -1554,17 +1609,17 @@ void rigid_tail(const gbmpm_particles* P, const gbmpm_model* M, Grid& G, double 
     for (int p = 0; p < P->n; ++p) {
         if (!sel(p) || P->material[p] != 8) continue;
         const gbmpm_rigid_body& r = g_rigid.bodies[P->rigid_id[p]];
-        const float* xr = P->x_ref + 3 * (size_t)p;
-        float* x = P->x + 3 * (size_t)p;
-        float* v = P->v + 3 * (size_t)p;
+        const Real* xr = P->x_ref + 3 * (size_t)p;
+        Real* x = P->x + 3 * (size_t)p;
+        Real* v = P->v + 3 * (size_t)p;
         for (int i = 0; i < 3; ++i)
             x[i] = r.x_cm[i] + (r.R[3 * i] * xr[0] + r.R[3 * i + 1] * xr[1] + r.R[3 * i + 2] * xr[2]);
-        const float rr[3] = {x[0] - r.x_cm[0], x[1] - r.x_cm[1], x[2] - r.x_cm[2]};
+        const Real rr[3] = {x[0] - r.x_cm[0], x[1] - r.x_cm[1], x[2] - r.x_cm[2]};
         v[0] = r.v_cm[0] + (r.omega[1] * rr[2] - r.omega[2] * rr[1]);
         v[1] = r.v_cm[1] + (r.omega[2] * rr[0] - r.omega[0] * rr[2]);
         v[2] = r.v_cm[2] + (r.omega[0] * rr[1] - r.omega[1] * rr[0]);
-        const float Cm[9] = {0.0f, -r.omega[2], r.omega[1], r.omega[2], 0.0f, -r.omega[0], -r.omega[1], r.omega[0], 0.0f};
-        const float I[9] = {1.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 1.0f};
+        const Real Cm[9] = {0.0f, -r.omega[2], r.omega[1], r.omega[2], 0.0f, -r.omega[0], -r.omega[1], r.omega[0], 0.0f};
+        const Real I[9] = {1.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 1.0f};
         std::memcpy(P->C + 9 * (size_t)p, Cm, sizeof Cm);
         std::memcpy(P->F + 9 * (size_t)p, I, sizeof I);
     }
@@ -1605,13 +1660,13 @@ void gbmpm_oracle_abi_layout(int64_t* out) {
     out[9] = offsetof(gbmpm_model, material_mask);
 }
 
-void gbmpm_oracle_svd3(const float* F, float* U, float* s, float* V) {
+void gbmpm_oracle_svd3(const Real* F, Real* U, Real* s, Real* V) {
     M3 f = load33(F), u, v; V3 sg;
     svd3_impl(f, u, sg, v);
     store33(U, u); store33(V, v); s[0] = sg[0]; s[1] = sg[1]; s[2] = sg[2];
 }
 
-float gbmpm_oracle_glass_sdf(const gbmpm_collider* c, const float* local) {
+Real gbmpm_oracle_glass_sdf(const gbmpm_collider* c, const Real* local) {
     return glass_sdf(load3(local), *c);
 }
 
@@ -1629,10 +1684,10 @@ void* gbmpm_oracle_cdf_new(int32_t n_grid) {
 void gbmpm_oracle_cdf_free(void* st) { delete static_cast<CdfState*>(st); }
 int32_t gbmpm_oracle_cdf_stamp_count(void* st) { return static_cast<CdfState*>(st)->stamp_count; }
 // current node tags and owner distances (grid_cdf_tag / grid_cdf_d), n_grid^3 each
-void gbmpm_oracle_cdf_grids(void* st, int32_t* tag, float* d) {
+void gbmpm_oracle_cdf_grids(void* st, int32_t* tag, Real* d) {
     CdfState& S = *static_cast<CdfState*>(st);
     if (tag) std::memcpy(tag, S.tag.data(), S.tag.size() * sizeof(int32_t));
-    if (d) std::memcpy(d, S.d.data(), S.d.size() * sizeof(float));
+    if (d) std::memcpy(d, S.d.data(), S.d.size() * sizeof(Real));
 }
 
 // add_cdf_collider / set_cdf_pose (mpm_solver_warp.py:2819-2953): lanes beyond the
@@ -1669,10 +1724,14 @@ int gbmpm_oracle_cdf_get(void* st, gbmpm_cdf* lanes, int32_t n) {
     return GBMPM_OK;
 }
 
-int gbmpm_oracle_tick(const gbmpm_particles* P, const gbmpm_model* M, gbmpm_collider* cols, int32_t ncol,
-                      float* wrench, double* time, double dt, int32_t substeps, int32_t fused, int32_t threads,
-                      void* cdf_state, float* cdf_wrench) {
-    if (!P || !M || !time || substeps < 1) { g_err = "bad argument"; return GBMPM_ERR_ARG; }
+// The particle record's float pointers address Real arrays (float32, or float64 in
+// the double build); wrench and cdf_wrench are Real accumulators.
+int gbmpm_oracle_tick(const gbmpm_particles* Pin, const gbmpm_model* M, gbmpm_collider* cols, int32_t ncol,
+                      Real* wrench, double* time, double dt, int32_t substeps, int32_t fused, int32_t threads,
+                      void* cdf_state, Real* cdf_wrench) {
+    if (!Pin || !M || !time || substeps < 1) { g_err = "bad argument"; return GBMPM_ERR_ARG; }
+    const RP rp = to_rp(*Pin);
+    const RP* P = &rp;
     bool par = threads > 1;
 #ifdef _OPENMP
     if (par) omp_set_num_threads(threads);
@@ -1681,7 +1740,7 @@ int gbmpm_oracle_tick(const gbmpm_particles* P, const gbmpm_model* M, gbmpm_coll
 #endif
     Grid& G = g_oracle.G;
     G.resize(M->n_grid);
-    float dtf = (float)dt;
+    Real dtf = (Real)dt;
     Ctx c{P, M, &G, dtf, par, 0};
     CdfState* S = static_cast<CdfState*>(cdf_state);
     if (S && S->n > 0) {
@@ -1701,7 +1760,7 @@ int gbmpm_oracle_tick(const gbmpm_particles* P, const gbmpm_model* M, gbmpm_coll
     if (rigid || mods) fused = 0;
     int prev_lo[3], prev_hi[3];
     for (int s = 0; s < substeps; ++s) {
-        float tf = (float)*time;
+        Real tf = (Real)*time;
         const double t_sub = *time;
         for (int a = 0; a < 3; ++a) { prev_lo[a] = G.lo[a]; prev_hi[a] = G.hi[a]; }
         if (S) cdf_stamp(*S, M, *time, fused != 0);
@@ -1753,7 +1812,7 @@ int gbmpm_oracle_tick(const gbmpm_particles* P, const gbmpm_model* M, gbmpm_coll
 
 // Block-key sort permutation (core/solver.py:458-465): float64 floor, >> 2,
 // lexicographic key, stable argsort; returns 0 (perm untouched) when sorted.
-int32_t gbmpm_oracle_sort_perm(const float* x, int32_t n, double dx, int32_t n_grid, int64_t* keys_out,
+int32_t gbmpm_oracle_sort_perm(const Real* x, int32_t n, double dx, int32_t n_grid, int64_t* keys_out,
                                int32_t* perm_out) {
     std::vector<int64_t> keys(n);
     int64_t nb = (n_grid >> 2) + 2;
@@ -1779,7 +1838,7 @@ int32_t gbmpm_oracle_sort_perm(const float* x, int32_t n, double dx, int32_t n_g
 // Active blocks (mpm_utils.py:1506-1544): mark with fp32 int() truncation,
 // dilate by one block, count current and union-with-previous. prev/cur are
 // int32[bd^3] (cur is written); counts = {current, union}.
-void gbmpm_oracle_blocks(const float* x, int32_t n, float inv_dx, int32_t n_grid, const int32_t* prev, int32_t* cur,
+void gbmpm_oracle_blocks(const Real* x, int32_t n, Real inv_dx, int32_t n_grid, const int32_t* prev, int32_t* cur,
                          int32_t* counts) {
     int bd = (n_grid + 3) / 4;
     std::vector<int32_t> raw((size_t)bd * bd * bd, 0);
@@ -1815,7 +1874,7 @@ void gbmpm_oracle_blocks(const float* x, int32_t n, float inv_dx, int32_t n_grid
 }
 
 // compute_R_from_F (mpm_utils.py:1256-1285): stores R^T
-void gbmpm_oracle_R(const float* F_trial, int32_t n, float* R_out) {
+void gbmpm_oracle_R(const Real* F_trial, int32_t n, Real* R_out) {
     for (int p = 0; p < n; ++p) {
         M3 F = load33(F_trial + 9 * (size_t)p), U, V; V3 s;
         svd3_impl(F, U, s, V);
@@ -1826,16 +1885,16 @@ void gbmpm_oracle_R(const float* F_trial, int32_t n, float* R_out) {
 }
 
 // compute_cov_from_F (mpm_utils.py:1234-1253)
-void gbmpm_oracle_cov(const float* F_trial, const float* init_cov, int32_t n, float* cov_out) {
+void gbmpm_oracle_cov(const Real* F_trial, const Real* init_cov, int32_t n, Real* cov_out) {
     for (int p = 0; p < n; ++p) {
         M3 F = load33(F_trial + 9 * (size_t)p);
-        const float* c = init_cov + 6 * (size_t)p;
+        const Real* c = init_cov + 6 * (size_t)p;
         M3 I0;
         I0.m[0][0] = c[0]; I0.m[0][1] = c[1]; I0.m[0][2] = c[2];
         I0.m[1][0] = c[1]; I0.m[1][1] = c[3]; I0.m[1][2] = c[4];
         I0.m[2][0] = c[2]; I0.m[2][1] = c[4]; I0.m[2][2] = c[5];
         M3 r = mmul(mmul(F, I0), mT(F));
-        float* o = cov_out + 6 * (size_t)p;
+        Real* o = cov_out + 6 * (size_t)p;
         o[0] = r.m[0][0]; o[1] = r.m[0][1]; o[2] = r.m[0][2];
         o[3] = r.m[1][1]; o[4] = r.m[1][2]; o[5] = r.m[2][2];
     }

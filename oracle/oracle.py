@@ -29,31 +29,40 @@ from mpm_engine_gb300.glass import quat_to_mat  # noqa: E402
 from mpm_engine_gb300.materials import material_id  # noqa: E402
 
 LIB = HERE / "_build" / "libmpm_oracle.so"
+# the same source with the arithmetic in float64: a rounding-free forward for
+# finite-difference checks of the engine's adjoint (never a parity checker)
+LIB64 = HERE / "_build" / "libmpm_oracle64.so"
 SRC = HERE / "mpm_oracle.cpp"
-_lib = None
+_libs: dict = {}
 
 
 def build(force: bool = False) -> Path:
-    """g++ recipe: fp contraction off so every product and sum rounds as written."""
+    """g++ recipe: fp contraction off so every product and sum rounds as written.
+    Builds the float32 oracle and its float64 twin (-DORACLE_REAL=double) in parallel."""
     LIB.parent.mkdir(parents=True, exist_ok=True)
     deps = [SRC, REPO / "include" / "gbmpm.h"]
-    if LIB.exists() and not force and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
-        return LIB
-    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-           "-I", str(REPO / "include"), "-o", str(LIB), str(SRC)]
-    res = subprocess.run(cmd, capture_output=True, text=True)
-    if res.returncode != 0:
-        raise RuntimeError("oracle build failed:\n" + res.stdout + res.stderr)
+    procs = []
+    for out, real in ((LIB, "float"), (LIB64, "double")):
+        if out.exists() and not force and all(out.stat().st_mtime >= d.stat().st_mtime for d in deps):
+            continue
+        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
+               "-ffp-contract=off", f"-DORACLE_REAL={real}", "-I", str(REPO / "include"), "-o", str(out), str(SRC)]
+        procs.append(subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))
+    for pr in procs:
+        out, _ = pr.communicate()
+        if pr.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + out)
     return LIB
 
 
-def load():
-    global _lib
-    if _lib is not None:
-        return _lib
-    if not LIB.exists():
+def load(precision: int = 32):
+    """The oracle library: float32 (the parity checker) or its float64 twin."""
+    if precision in _libs:
+        return _libs[precision]
+    path = LIB64 if precision == 64 else LIB
+    if not path.exists():
         build()
-    lib = C.CDLL(str(LIB))
+    lib = C.CDLL(str(path))
     P = C.POINTER
     lib.gbmpm_oracle_tick.restype = C.c_int
     lib.gbmpm_oracle_tick.argtypes = [P(_abi.Particles), P(_abi.Model), P(_abi.Collider), C.c_int32, C.c_void_p,
@@ -82,7 +91,7 @@ def load():
     lib.gbmpm_oracle_set_rigid.argtypes = [P(_abi.RigidBody), C.c_int32, P(_abi.RigidSurface), C.c_int32]
     lib.gbmpm_oracle_get_rigid.argtypes = [P(_abi.RigidBody), C.c_int32]
     lib.gbmpm_oracle_set_modifiers.argtypes = [P(_abi.Modifier), C.c_int32]
-    _lib = lib
+    _libs[precision] = lib
     return lib
 
 
@@ -156,13 +165,23 @@ def box_contact_wrench(x, cauchy, vol, box_center, box_half, layer_cells=None, d
     return {"force": force, "torque": torque, "n_contact": int(contact.sum()), "Fz": float(force[2])}
 
 
+_FLOAT_KEYS = ("x", "v", "C", "F", "F_trial", "L", "stress", "mass", "vol", "density", "Jp", "mu", "lam",
+               "yield_stress", "cov", "init_cov", "x_ref")
+
+
 class OracleSolver:
-    """numpy twin of mpm_engine_gb300.Solver's host side, stepping the C++ oracle."""
+    """numpy twin of mpm_engine_gb300.Solver's host side, stepping the C++ oracle.
+    precision=64 steps the float64 build: particle arrays, grid and accumulators in
+    float64 (a finite-difference reference without rounding noise)."""
 
     def __init__(self, n_grid: int = 64, grid_lim: float = 0.4, fused: bool = True, threads: int = 1,
-                 periodic_x: bool = False, grid=None, **_ignored):
+                 periodic_x: bool = False, grid=None, precision: int = 32, **_ignored):
         if grid is not None:
             n_grid, grid_lim = grid.n_grid, grid.grid_lim
+        if precision not in (32, 64):
+            raise ValueError("precision is 32 or 64")
+        self.precision = precision
+        self.fdt = np.float64 if precision == 64 else np.float32
         self.n_grid, self.grid_lim = int(n_grid), float(grid_lim)
         self.dx = self.grid_lim / self.n_grid
         self.fused = fused
@@ -177,34 +196,35 @@ class OracleSolver:
         self.sdf_arrays: list = []
         self.time = 0.0
         self.mat_current = 0
-        self.wrench = np.zeros((0, 6), np.float32)
+        self.wrench = np.zeros((0, 6), self.fdt)
         self.cdf_lanes: list = []
         self.cdf_arrays: list = []
         self.cdf_state = None
-        self.cdf_wrench_acc = np.zeros((4, 6), np.float32)
+        self.cdf_wrench_acc = np.zeros((4, 6), self.fdt)
         self.rigid_bodies: list = []
         self.rigid_surfaces: list = []
         self.modifiers: list = []
 
     def __del__(self):
         if getattr(self, "cdf_state", None):
-            load().gbmpm_oracle_cdf_free(self.cdf_state)
+            load(self.precision).gbmpm_oracle_cdf_free(self.cdf_state)
             self.cdf_state = None
 
     # ----------------------------------------------------------------- setup
     def load_particles(self, pos, vol, cov=None, cov_mode="step"):
         n = len(pos)
-        eye = np.tile(np.eye(3, dtype=np.float32), (n, 1, 1))
-        z = lambda *s: np.zeros(s, np.float32)  # noqa: E731
-        self.a = {"x": np.ascontiguousarray(pos, np.float32).reshape(n, 3).copy(), "v": z(n, 3), "C": z(n, 3, 3),
-                  "F": eye.copy(), "F_trial": eye.copy(), "L": z(n, 3, 3), "stress": z(n, 3, 3),
-                  "mass": z(n), "vol": np.asarray(vol, np.float32).copy(), "density": z(n), "Jp": z(n),
+        fdt = self.fdt
+        eye = np.tile(np.eye(3, dtype=fdt), (n, 1, 1))
+        z = lambda *s: np.zeros(s, fdt)  # noqa: E731
+        self.a = {"x": np.ascontiguousarray(pos, np.float32).astype(fdt).reshape(n, 3).copy(), "v": z(n, 3),
+                  "C": z(n, 3, 3), "F": eye.copy(), "F_trial": eye.copy(), "L": z(n, 3, 3), "stress": z(n, 3, 3),
+                  "mass": z(n), "vol": np.asarray(vol, np.float32).astype(fdt).copy(), "density": z(n), "Jp": z(n),
                   "mu": z(n), "lam": z(n), "yield_stress": z(n), "material": np.zeros(n, np.int32),
                   "selection": np.zeros(n, np.int32), "cov": None, "init_cov": None,
                   "cdf_tag": np.zeros(n, np.int32), "rigid_id": np.zeros(n, np.int32), "x_ref": z(n, 3),
                   "mod_mask": np.zeros(n, np.int32)}
         if cov is not None:
-            c6 = np.ascontiguousarray(cov, np.float32).reshape(n, 6)
+            c6 = np.ascontiguousarray(cov, np.float32).astype(fdt).reshape(n, 6)
             self.a["init_cov"] = c6.copy()
             self.a["cov"] = c6.copy() if cov_mode == "step" else np.zeros_like(c6)
             self.model.update_cov_with_F = 1 if cov_mode == "step" else 0
@@ -278,7 +298,7 @@ class OracleSolver:
         first = len(self.handles)
         self.handles.append(len(self.cols) - 1)
         self.handles.extend([None] * (slots - 1))
-        self.wrench = np.zeros((len(self.cols), 6), np.float32)
+        self.wrench = np.zeros((len(self.cols), 6), self.fdt)
         return first
 
     def add_plane(self, point, normal, surface="sticky", friction=0.0, restitution=0.0):
@@ -365,7 +385,7 @@ class OracleSolver:
                                            start_time, end_time))
 
     def _push_cdf(self):
-        lib = load()
+        lib = load(self.precision)
         if self.cdf_state is None:
             self.cdf_state = lib.gbmpm_oracle_cdf_new(self.n_grid)
         arr = (_abi.Cdf * max(1, len(self.cdf_lanes)))(*self.cdf_lanes)
@@ -377,7 +397,7 @@ class OracleSolver:
         if self.cdf_state is None or not self.cdf_lanes:
             return
         arr = (_abi.Cdf * len(self.cdf_lanes))()
-        load().gbmpm_oracle_cdf_get(self.cdf_state, arr, len(self.cdf_lanes))
+        load(self.precision).gbmpm_oracle_cdf_get(self.cdf_state, arr, len(self.cdf_lanes))
         self.cdf_lanes = [arr[i] for i in range(len(self.cdf_lanes))]
 
     def add_cdf_collider(self, cdf, center, quat=(0.0, 0.0, 0.0, 1.0), velocity=(0.0, 0.0, 0.0),
@@ -418,10 +438,10 @@ class OracleSolver:
         """(tag, distance) node grids of the last stamp and the number of stamps so far."""
         ng = self.n_grid
         tag = np.zeros((ng, ng, ng), np.int32)
-        d = np.zeros((ng, ng, ng), np.float32)
+        d = np.zeros((ng, ng, ng), self.fdt)
         if self.cdf_state is None:
             return tag, d, 0
-        lib = load()
+        lib = load(self.precision)
         lib.gbmpm_oracle_cdf_grids(self.cdf_state, _p(tag), _p(d))
         return tag, d, int(lib.gbmpm_oracle_cdf_stamp_count(self.cdf_state))
 
@@ -438,9 +458,13 @@ class OracleSolver:
 
     # ------------------------------------------------------------ from GPU
     @classmethod
-    def from_state(cls, st: dict, n_grid: int, grid_lim: float, fused: bool = True, threads: int = 1):
-        o = cls(n_grid, grid_lim, fused=fused, threads=threads)
+    def from_state(cls, st: dict, n_grid: int, grid_lim: float, fused: bool = True, threads: int = 1,
+                   precision: int = 32):
+        o = cls(n_grid, grid_lim, fused=fused, threads=threads, precision=precision)
         o.a = {k: (None if st.get(k) is None else np.ascontiguousarray(st[k]).copy()) for k in _KEYS}
+        for k in _FLOAT_KEYS:
+            if o.a.get(k) is not None:
+                o.a[k] = np.ascontiguousarray(o.a[k], o.fdt)
         C.memmove(C.byref(o.model), C.byref(st["model"]), C.sizeof(_abi.Model))
         o.eta_table = np.ascontiguousarray(st["eta_table"], np.float32).copy()
         o.model.eta_table = _p(o.eta_table)
@@ -454,10 +478,10 @@ class OracleSolver:
                 r.sdf_val, r.sdf_grad = _p(val), _p(grad)
             o.cols.append(r)
         o.handles = list(st.get("handles", range(len(o.cols))))
-        o.wrench = np.zeros((len(o.cols), 6), np.float32)
+        o.wrench = np.zeros((len(o.cols), 6), o.fdt)
         o.time = float(st["time"])
         n = len(o.a["x"])
-        for k, shape, dt in (("cdf_tag", (n,), np.int32), ("rigid_id", (n,), np.int32), ("x_ref", (n, 3), np.float32),
+        for k, shape, dt in (("cdf_tag", (n,), np.int32), ("rigid_id", (n,), np.int32), ("x_ref", (n, 3), o.fdt),
                              ("mod_mask", (n,), np.int32)):
             if o.a.get(k) is None:
                 o.a[k] = np.zeros(shape, dt)
@@ -487,7 +511,7 @@ class OracleSolver:
     def step(self, dt, substeps=1):
         """One control tick; scenes with rigid bodies or particle modifiers run the
         split pipeline, as the reference's Solver.step does."""
-        lib = load()
+        lib = load(self.precision)
         p = self._particles()
         nb, ns, nm = len(self.rigid_bodies), len(self.rigid_surfaces), len(self.modifiers)
         bodies = (_abi.RigidBody * max(1, nb))(*self.rigid_bodies)

@@ -1,0 +1,169 @@
+"""The engine's adjoint against central finite differences of the float64 oracle.
+
+The float32 forward cannot resolve a finite difference at h = 1e-3 relative: over
+a few substeps the parameters move the loss by about 1e-6 of its size, the same
+order as the rounding of 4,500 float32 positions, so float32 differences scatter by
+percents. The oracle built with its arithmetic in float64 (oracle/, precision=64)
+steps the same scene from the same starting state with the rounding taken out.
+Central differences of it at h = 1e-3 relative have a truncation error of order
+h^2 and no visible noise, so they measure the adjoint itself.
+
+Bound: the adjoint's gradient (float32 kernels along the float32 trajectory, the
+loss summed in float64) within 1e-3 relative of the float64 differences, for
+dL/dE, dL/dnu, dL/dyield, dL/dviscosity and a unit direction of dL/dv0.
+"""
+import numpy as np
+import pytest
+
+from test_gpu_adjoint import K, N, NG, Case, _loss_np
+
+pytestmark = pytest.mark.gpu
+
+H = 1.0e-3
+TOL = 1.0e-3
+
+
+def fd64(c, which, rel=H, direction=None, k=K):
+    """Central difference of the loss of a k-substep rollout of the float64 oracle
+    from the case's starting state: parameters perturbed by +-rel relative (v0 by
+    +-rel along a unit direction), mu and lambda formed from E and nu in float64."""
+    from oracle.oracle import OracleSolver
+    base = {"E": c.E, "nu": c.nu, "ys": c.ys, "eta": c.eta}
+
+    def at(sg):
+        p = dict(base)
+        if which != "v0":
+            p[which] = p[which] * (1.0 + sg * rel)
+        o = OracleSolver.from_state(c.state, NG, 0.4, precision=64, threads=8)
+        E, nu = float(p["E"]), float(p["nu"])
+        o.a["mu"][:] = E / (2.0 * (1.0 + nu))
+        o.a["lam"][:] = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+        o.a["yield_stress"][:] = p["ys"]
+        o.model.plastic_viscosity[10] = p["eta"]
+        eta_used = float(o.model.plastic_viscosity[10])   # the model record holds float32
+        if which == "v0":
+            o.a["v"][:] = o.a["v"] + sg * rel * direction
+        o.step(c.dt, k)
+        return _loss_np(o.a["x"], o.a["v"]), eta_used
+    (lp, ep), (lm, em) = at(1.0), at(-1.0)
+    if which == "v0":
+        h = rel
+    elif which == "eta":
+        h = 0.5 * (ep - em)
+    else:
+        h = rel * base[which]
+    return (lp - lm) / (2.0 * h)
+
+
+def check(c, params, tol=TOL, seed=7):
+    import torch
+    g = c.grads()
+    errs = {}
+    for p in params:
+        fd = fd64(c, p)
+        errs[p] = abs(g[p] - fd) / abs(fd)
+    d = torch.randn(c.v0.shape, generator=torch.Generator().manual_seed(seed)).double()
+    d = (d / d.norm()).numpy()
+    fd = fd64(c, "v0", direction=d)
+    ad = float((g["v0"].double().cpu().numpy() * d).sum())
+    errs["v0"] = abs(ad - fd) / abs(fd)
+    print(c.key, c.kw, {k: f"{e:.2e}" for k, e in errs.items()})
+    bad = {k: e for k, e in errs.items() if not e <= tol}
+    assert not bad, f"{c.key} {c.kw}: relative gradient errors {bad} exceed {tol}"
+
+
+@pytest.mark.parametrize("key,kw,params", [
+    ("jelly", {}, ("E", "nu")),
+    ("jelly", {"floor": "separate", "plate": True}, ("E", "nu")),
+    ("metal", {}, ("E", "nu", "ys")),
+    ("metal_hardening", {"plate": True}, ("E", "nu", "ys")),
+    ("jelly", {"cup": True}, ("E", "nu")),
+    ("jelly", {"sphere": True}, ("E", "nu")),
+])
+def test_elastic_and_von_mises_gradients_match_float64_differences(cuda, key, kw, params):
+    check(Case(key, **kw), params)
+
+
+@pytest.mark.parametrize("key,kw,params", [
+    ("sand", {}, ("E", "nu")),
+    ("plasticine", {"plate": True}, ("E", "nu", "ys")),
+    ("mu_i", {}, ("E", "nu")),
+    ("mu_i_table", {}, ("E", "nu")),
+])
+def test_granular_and_softening_gradients_match_float64_differences(cuda, key, kw, params):
+    check(Case(key, **kw), params)
+
+
+@pytest.mark.parametrize("key,kw,params", [
+    ("newtonian_soft", {"free": True}, ("eta",)),
+    ("bingham_yield", {"free": True}, ("ys",)),
+    ("tabulated_soft", {"free": True}, ()),
+])
+def test_fluid_gradients_match_float64_differences(cuda, key, kw, params):
+    check(Case(key, **kw), params)
+
+
+def test_mu_i_phi_gradients_match_float64_differences(cuda):
+    check(Case("mu_i_phi", free=True, pre=0, prestrain=True), ("E", "nu"))
+
+
+def test_identification_scene_full_length(cuda):
+    """One scene of the batched identification workload at its full length: a
+    von Mises cube of about 50k particles on a 48^3 grid, resting on a sticky floor
+    and squeezed by a plate pressed into its top at 0.05 m/s, 400 substeps of 1e-5 s
+    with checkpoints every 20. The loss is the squared distance of the final
+    positions to a seeded target rollout (the same scene with E, nu and the yield
+    stress 30 %, 5 % and 30 % higher) plus a seeded projection of the final
+    velocities. dL/dE, dL/dnu, dL/dyield and a unit direction of dL/dv0 against
+    central differences of the float64 oracle at h = 1e-3 relative."""
+    import torch
+    from mpm_engine_gb300 import Solver, adjoint
+    from mpm_engine_gb300.materials import vonmises
+    from mpm_engine_gb300.scenes import squeeze_scene
+    from oracle.oracle import OracleSolver
+    E0, nu0, ys0, dt, K5, every = 1.0e5, 0.3, 500.0, 1.0e-5, 400, 20
+
+    def scene(E, nu, ys):
+        s, _ = squeeze_scene(Solver, 50_000, 48, vonmises(E=E, nu=nu, yield_stress=ys, density=1000.0),
+                             seed=3, plate_gap=-0.5)
+        return s
+
+    tgt = scene(1.3 * E0, 1.05 * nu0, 1.3 * ys0)
+    tgt.step(dt, K5)
+    x_t = tgt._t["x"].double().clone()
+    s = scene(E0, nu0, ys0)
+    n = s.n_particles
+    st = s.export_state()
+    b = torch.from_numpy(np.random.default_rng(8).standard_normal((n, 3))).to(x_t.device)
+    dev = x_t.device
+    t = lambda x: torch.tensor(x, device=dev, dtype=torch.float32, requires_grad=True)  # noqa: E731
+    v0 = s._t["v"].clone().requires_grad_(True)
+    E, nu, ys = t(E0), t(nu0), t(ys0)
+    x, v = adjoint.rollout(s, dt, K5, v0=v0, E=E, nu=nu, yield_stress=ys, checkpoint_every=every)
+    L = ((x.double() - x_t) ** 2).sum() + (v.double() * b).sum()
+    L.backward()
+    g = {"E": float(E.grad), "nu": float(nu.grad), "ys": float(ys.grad)}
+    xt = x_t.cpu().numpy()
+    bn = b.cpu().numpy()
+
+    def loss64(E_, nu_, ys_, dv=None):
+        o = OracleSolver.from_state(st, 48, 0.3, precision=64, threads=16)
+        o.a["mu"][:] = E_ / (2.0 * (1.0 + nu_))
+        o.a["lam"][:] = E_ * nu_ / ((1.0 + nu_) * (1.0 - 2.0 * nu_))
+        o.a["yield_stress"][:] = ys_
+        if dv is not None:
+            o.a["v"][:] = o.a["v"] + dv
+        o.step(dt, K5)
+        return float(((o.a["x"] - xt) ** 2).sum() + (o.a["v"] * bn).sum())
+
+    fd = {"E": (loss64(E0 * (1 + H), nu0, ys0) - loss64(E0 * (1 - H), nu0, ys0)) / (2 * H * E0),
+          "nu": (loss64(E0, nu0 * (1 + H), ys0) - loss64(E0, nu0 * (1 - H), ys0)) / (2 * H * nu0),
+          "ys": (loss64(E0, nu0, ys0 * (1 + H)) - loss64(E0, nu0, ys0 * (1 - H))) / (2 * H * ys0)}
+    d = np.random.default_rng(12).standard_normal((n, 3))
+    d /= np.linalg.norm(d)
+    fd["v0"] = (loss64(E0, nu0, ys0, H * d) - loss64(E0, nu0, ys0, -H * d)) / (2 * H)
+    g["v0"] = float((v0.grad.double().cpu().numpy() * d).sum())
+    errs = {k: abs(g[k] - fd[k]) / abs(fd[k]) for k in fd}
+    print("identification scene, 400 substeps:", {k: (g[k], fd[k], f"{errs[k]:.2e}") for k in fd})
+    bad = {k: e for k, e in errs.items() if not e <= TOL}
+    assert not bad, f"identification scene: relative gradient errors {bad} exceed {TOL}"

@@ -43,12 +43,26 @@ def fields_oracle(o):
     return {"x": o.a["x"], "v": o.a["v"], "C": o.a["C"], "F": o.a["F"]}
 
 
+def worst(s, o, key):
+    """Where field `key` differs most: particle index, |difference|, and that
+    particle's position and oracle velocity (for failure messages)."""
+    g, r = fields_gpu(s)[key], fields_oracle(o)[key]
+    n = len(r)
+    d = np.abs(np.asarray(g, np.float64).reshape(n, -1) - np.asarray(r, np.float64).reshape(n, -1)).max(axis=1)
+    p = int(np.argmax(d))
+    above = int((d > 0.5 * d[p]).sum())
+    return {"particle": p, "diff": float(d[p]), "x": o.a["x"][p].tolist(), "v": o.a["v"][p].tolist(),
+            "particles_above_half_max": above}
+
+
 def assert_close(s, o, tol, what=""):
     g, r = fields_gpu(s), fields_oracle(o)
     floors = dict(FLOOR, C=c_floor(o))
     errs = {k: rel_err(g[k], r[k], floors[k]) for k in g}
     bad = {k: e for k, e in errs.items() if not e <= tol}
-    assert not bad, f"{what}: relative errors {errs} exceed {tol}"
+    if bad:
+        where = {k: worst(s, o, k) for k in bad}
+        raise AssertionError(f"{what}: relative errors {errs} exceed {tol}; worst particles {where}")
     return errs
 
 
