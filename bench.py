@@ -211,6 +211,12 @@ def batched_measure(n_scenes: int, ticks: int, substeps: int = 100, dt: float = 
                          [sp["n_particles"] for sp in specs], rank, world)
     scenes, batch = shard.scenes, shard.batch
     n_local = len(scenes)
+    tuned = None
+    if batch is not None:                  # the project's autotuner picks the launch shape
+        tuned = batch.autotune(dt, substeps, ticks=1)
+        tuned = {"choice": dict(zip(("single_launch", "tile_threads", "tile_occ", "grid_ctas_per_sm"),
+                                    tuned["tuning"])), "cached": tuned["cached"],
+                 "ms_per_tick_by_candidate": tuned["ms_per_tick"]}
     for sc in scenes:                      # warm-up: capture each scene's own graph
         sc.step(dt, substeps)
     shard.step(dt, substeps)               # warm-up: capture the batch graph
@@ -235,7 +241,8 @@ def batched_measure(n_scenes: int, ticks: int, substeps: int = 100, dt: float = 
     return {"metric": "batched forward scene-ticks/s", "unit": f"scene-ticks/s ({substeps} substeps each)",
             "value": rate_b, "plain_value": rate_p, "speedup_vs_plain": rate_b / rate_p,
             "scenes": n_scenes, "particles_total": int(n_part), "ticks": ticks, "dt": dt,
-            "particle_substeps_per_s": rate_pp, "gpu_launches": launches,
+            "particle_substeps_per_s": rate_pp, "gpu_launches": launches, "substeps_timed": ticks * substeps,
+            "autotuned": tuned,
             "sharding": {"ranks": world, "scenes_on_rank0": n_local} if world > 1 else None}
 
 
@@ -734,8 +741,7 @@ def main():
 
     batched = None
     if not args.no_batched:
-        batched = batched_measure(args.batch_scenes, ticks=max(2, min(args.steps, 4)), device=f"cuda:{local}",
-                                  rank=rank, world=world)
+        batched = batched_measure(args.batch_scenes, ticks=10, device=f"cuda:{local}", rank=rank, world=world)
 
     others = None
     if not args.no_others and args.workload == "pour":

@@ -264,12 +264,21 @@ int gbmpm_contact_wrench(gbmpm_engine *e, const double box_center[3], const doub
  * Adjoints of the particle state (x, v, C, F_trial, yield_stress, L, and Jp, the
  * mu(I)-Phi(I) packing state; device arrays in the particle layout) and accumulated
  * per-particle adjoints of mu, lam and of the Newtonian viscosity (its sum is the
- * gradient of the per-type value). */
+ * gradient of the per-type value).
+ * Collider trajectories (optional, NULL to skip): collider_force holds, for every
+ * substep of the segment, the adjoint of each collider's force accumulator
+ * ([substeps][n_colliders][3]; the reaction that gbmpm_wrench and the reference's
+ * tool_force read, core/solver.py:415-427), and collider_velocity accumulates the
+ * adjoint of each kinematic cuboid's velocity ([n_colliders][3]; the velocity
+ * add_box / set_box give, which moves the box and sets the velocity of the nodes it
+ * covers, mpm_solver_warp.py:2053-2096). */
 typedef struct gbmpm_adj_grads {
     float *x, *v, *C, *F_trial, *yield_stress;
     float *mu, *lam;
     float *L, *viscosity;
     float *Jp;
+    const float *collider_force;
+    float *collider_velocity;
 } gbmpm_adj_grads;
 
 /* Replays `substeps` split-schedule substeps forward from the bound state (the
@@ -319,6 +328,21 @@ void gbmpm_batch_destroy(gbmpm_batch *b);
 int gbmpm_batch_tick(gbmpm_batch *b, double *times, double dt, int32_t substeps, int32_t flags, void *stream);
 int gbmpm_batch_guard(gbmpm_batch *b, float *out, uint32_t *status, void *stream);
 int64_t gbmpm_batch_launch_count(gbmpm_batch *b);
+/* Schedule and launch shape of the batch's fused ticks (no counterpart in the
+ * reference, which steps scenes one after another). With single_launch (the
+ * default) a tick whose scenes all run the fused schedule on their block-sorted
+ * working sets, with no CPIC lanes, rigid bodies or particle modifiers, launches
+ * each particle pass and each grid pass once over every scene; otherwise each
+ * scene's own tick is a branch of the batch graph. tile_threads (64, 128 or 256
+ * particles per CTA) and tile_occ (2 or 3 resident 256-thread equivalents per SM)
+ * select the particle-pass kernel; grid_ctas (1 to 8 per SM) sizes the grid pass,
+ * shared out over the scenes by particle count. The autotuner
+ * (mpm_engine_gb300.autotune) sets these. */
+int gbmpm_batch_set_tuning(gbmpm_batch *b, int32_t single_launch, int32_t tile_threads, int32_t tile_occ,
+                           int32_t grid_ctas);
+/* out = {single_launch, tile_threads, tile_occ, grid_ctas, last captured graph
+ * runs the single-launch schedule (0/1)}. */
+int gbmpm_batch_get_tuning(gbmpm_batch *b, int32_t out[5]);
 /* As gbmpm_graph_state for the batch graph: 1 ready, 0 none, -1 after a failed
  * capture (the scenes then tick live, one after another, for the rest of the run). */
 int32_t gbmpm_batch_graph_state(gbmpm_batch *b);
@@ -412,6 +436,13 @@ int gbmpm_field_tri_distance(const gbmpm_field_points *pts, const double *tri, i
 
 /* Number of kernels this engine has launched (graph replays count each node). */
 int64_t gbmpm_launch_count(gbmpm_engine *e);
+/* Launch shape of one scene's passes (no counterpart in the reference): tile_occ
+ * (2 to 4 resident 256-thread equivalents per SM; 4 only for scenes without
+ * SVD-based laws) selects the tiled particle kernel, grid_ctas (1 to 8 per SM) the
+ * grid-update launch. Set by the autotuner (mpm_engine_gb300.autotune). */
+int gbmpm_set_tuning(gbmpm_engine *e, int32_t tile_occ, int32_t grid_ctas);
+/* out = {tile_occ, grid_ctas}. */
+int gbmpm_get_tuning(gbmpm_engine *e, int32_t out[2]);
 /* Test hook (no counterpart in the reference): deposits the current particle state
  * (stored stress, v, C; no stress update) into the grid with the P2G kernel,
  * returns out[4] = {sum m, sum m vx, sum m vy, sum m vz} over every grid node in

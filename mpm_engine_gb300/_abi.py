@@ -128,7 +128,7 @@ MAX_MODIFIERS = 32
 
 class AdjGrads(C.Structure):
     _fields_ = [(k, C.c_void_p) for k in ("x", "v", "C", "F_trial", "yield_stress", "mu", "lam", "L", "viscosity",
-                                          "Jp")]
+                                          "Jp", "collider_force", "collider_velocity")]
 
 
 class FieldPoints(C.Structure):
@@ -172,6 +172,8 @@ _SIGNATURES = {
     "gbmpm_guard_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_float),
                                       C.POINTER(C.c_int32), C.c_void_p]),
     "gbmpm_launch_count": (C.c_int64, [C.c_void_p]),
+    "gbmpm_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "gbmpm_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "gbmpm_debug_deposit_sums": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_double), C.c_void_p]),
     "gbmpm_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]),
     "gbmpm_batch_destroy": (None, [C.c_void_p]),
@@ -179,6 +181,8 @@ _SIGNATURES = {
                                    C.c_void_p]),
     "gbmpm_batch_guard": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.c_void_p]),
     "gbmpm_batch_launch_count": (C.c_int64, [C.c_void_p]),
+    "gbmpm_batch_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "gbmpm_batch_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "gbmpm_cdf_restamp": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p]),
     "gbmpm_cdf_force_stamp": (C.c_int, [C.c_void_p, C.c_int32]),
     "gbmpm_cdf_mask_off": (C.c_int, [C.c_void_p, C.c_int32]),

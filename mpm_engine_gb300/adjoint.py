@@ -5,7 +5,11 @@ finite differences over serial rollouts. Here `rollout` runs a scene forward on
 the engine and returns its final positions and velocities as torch tensors whose
 gradients flow, through the engine's adjoint kernels, to the initial velocity
 field, Young's modulus, Poisson's ratio, the yield stress and the Newtonian
-viscosity.
+viscosity. With a kinematic cuboid (`plate`, an add_box handle) the rollout also
+returns the cuboid's reaction-force trace, one force per checkpoint segment (what
+tool_force reads after each segment, core/solver.py:415-427), and differentiates
+the cuboid's trajectory: its velocity, which moves the box and drives the nodes it
+covers, is an input like the material parameters.
 
 Memory follows the usual checkpoint-and-recompute scheme: the forward keeps the
 state (x, v, C, F_trial, L, yield, and mu, lam, which softening can zero) and the
@@ -24,6 +28,8 @@ colliders, rigid bodies and particle modifiers.
 from __future__ import annotations
 
 import ctypes as C
+
+import numpy as np
 
 from . import _abi
 from .solver import _torch
@@ -63,18 +69,24 @@ def _check(s):
         raise NotImplementedError("the adjoint does not cover CDF colliders")
 
 
-def _forward(s, dt, substeps, every):
-    ckpts = []
+def _forward(s, dt, substeps, every, plate=None):
+    """Runs the rollout, keeping a checkpoint per segment; with a plate handle also
+    returns the plate's reaction force over each segment ([segments][3] float64)."""
+    ckpts, forces = [], []
     done = 0
     while done < substeps:
         k = min(every, substeps - done)
         ckpts.append((_snapshot(s), k))
+        if plate is not None:
+            s.reset_tool_force(plate)
         s.step(dt, k)
+        if plate is not None:
+            forces.append(s.tool_force(plate, dt * k))
         done += k
-    return ckpts
+    return (ckpts, forces) if plate is not None else ckpts
 
 
-def _backward(s, dt, ckpts, xb, vb):
+def _backward(s, dt, ckpts, xb, vb, plate=None, force_bar=None):
     torch = _torch()
     n = s.n_particles
     dev = s._t["x"].device
@@ -88,11 +100,26 @@ def _backward(s, dt, ckpts, xb, vb):
     }
     rec = _abi.AdjGrads(**{k: g[k].data_ptr() for k in g})
     lib, h = s._eng.lib, s._eng.h
-    for snap, k in reversed(ckpts):
+    ncol = max(1, len(s._cols))
+    col = s._col(plate) if plate is not None else None
+    if col is not None:
+        g["collider_velocity"] = torch.zeros(ncol, 3, **f)
+        rec.collider_velocity = g["collider_velocity"].data_ptr()
+    for j in reversed(range(len(ckpts))):
+        snap, k = ckpts[j]
         _restore(s, snap)
+        if col is not None:
+            # the segment's force is sum_substeps sum_nodes m (v_free - v_box) / (dt k)
+            # stream-ordered: the segment's kernels read fb before a later allocation reuses it
+            fb = torch.zeros(k, ncol, 3, **f)
+            if force_bar is not None:
+                fb[:, col, :] = force_bar[j].to(**f) / (dt * k)
+            rec.collider_force = fb.data_ptr()
         t = C.c_double(s._time)
         _abi.check(lib.gbmpm_adjoint_segment(h, C.byref(t), float(dt), int(k), C.byref(rec), s._stream()),
                    "gbmpm_adjoint_segment")
+    if col is not None:
+        g["plate_velocity"] = g["collider_velocity"][col].clone()
     return g
 
 
@@ -101,7 +128,8 @@ NEWTONIAN = 10   # material id whose per-type viscosity `viscosity` sets
 
 class _Rollout(_torch().autograd.Function):
     @staticmethod
-    def forward(ctx, v0, mu, lam, ys0, eta, solver, dt, substeps, every):
+    def forward(ctx, v0, mu, lam, ys0, eta, plate_v, solver, dt, substeps, every, plate):
+        torch = _torch()
         s = solver
         s._t["v"].copy_(v0.detach().reshape(-1, 3))
         s._t["mu"].copy_(mu.detach())
@@ -109,18 +137,27 @@ class _Rollout(_torch().autograd.Function):
         s._t["yield_stress"].copy_(ys0.detach())
         s._model.plastic_viscosity[NEWTONIAN] = float(eta)
         s._model_dirty = True
-        ctx.solver, ctx.dt = s, dt
-        ctx.ckpts = _forward(s, dt, substeps, every)
+        if plate is not None:
+            s.set_box(plate, velocity=tuple(float(c) for c in plate_v.detach().cpu()))
+        ctx.solver, ctx.dt, ctx.plate = s, dt, plate
+        if plate is not None:
+            ctx.ckpts, forces = _forward(s, dt, substeps, every, plate)
+            F = torch.tensor(np.array(forces), dtype=torch.float64, device=v0.device)
+        else:
+            ctx.ckpts = _forward(s, dt, substeps, every)
+            F = torch.zeros(0, 3, dtype=torch.float64, device=v0.device)
         x, v = s._t["x"].clone(), s._t["v"].clone()
         ctx.final = _snapshot(s)
-        return x, v
+        return x, v, F
 
     @staticmethod
-    def backward(ctx, xb, vb):
+    def backward(ctx, xb, vb, Fb):
         s = ctx.solver
-        g = _backward(s, ctx.dt, ctx.ckpts, xb, vb)
+        g = _backward(s, ctx.dt, ctx.ckpts, xb, vb, ctx.plate, Fb if ctx.plate is not None else None)
         _restore(s, ctx.final)
-        return g["v"], g["mu"], g["lam"], g["yield_stress"], g["viscosity"].sum(), None, None, None, None
+        pvb = g.get("plate_velocity")
+        return (g["v"], g["mu"], g["lam"], g["yield_stress"], g["viscosity"].sum(), pvb, None, None, None, None,
+                None)
 
 
 def mu_lam(E, nu):
@@ -129,14 +166,21 @@ def mu_lam(E, nu):
 
 
 def rollout(solver, dt: float, substeps: int, *, v0=None, E=None, nu=None, yield_stress=None, viscosity=None,
-            checkpoint_every: int = 20):
+            checkpoint_every: int = 20, plate=None, plate_velocity=None):
     """Advance `solver` by `substeps` substeps of dt and return (x, v) at the end.
 
     v0 ((N, 3)), E, nu and yield_stress (scalars or (N,) tensors) and viscosity (the
     Newtonian plastic viscosity, a scalar) are the differentiable inputs; any left
     as None keeps the scene's current value and is not differentiated. E and nu set
     mu and lam of every particle through the reference's formula. The solver is
-    left at the end state of the rollout."""
+    left at the end state of the rollout.
+
+    With `plate` (an add_box handle) the call returns (x, v, F): F is the plate's
+    reaction force over each checkpoint segment ((segments, 3) float64, the
+    tool_force of that segment), and `plate_velocity` ((3,), default the plate's
+    current velocity) is differentiable: it moves the plate through the rollout and
+    drives the grid nodes inside it. Gradients reach it through the positions and
+    velocities and through the force trace."""
     torch = _torch()
     _check(solver)
     s = solver
@@ -161,7 +205,16 @@ def rollout(solver, dt: float, substeps: int, *, v0=None, E=None, nu=None, yield
         eta = torch.tensor(float(s._model.plastic_viscosity[NEWTONIAN]), **f)
     else:
         eta = (viscosity if torch.is_tensor(viscosity) else torch.as_tensor(viscosity)).to(**f)
-    return _Rollout.apply(v0, mu, lam, ys, eta, s, float(dt), int(substeps), int(checkpoint_every))
+    if plate is None:
+        pv = torch.zeros(3, **f)
+    else:
+        rec = s._cols[s._col(plate)]
+        if rec.kind != _abi.COLLIDER_BOX:
+            raise ValueError("plate must be an add_box handle")
+        pv = (torch.tensor(list(rec.velocity), **f) if plate_velocity is None else
+              (plate_velocity if torch.is_tensor(plate_velocity) else torch.as_tensor(plate_velocity)).to(**f))
+    x, v, F = _Rollout.apply(v0, mu, lam, ys, eta, pv, s, float(dt), int(substeps), int(checkpoint_every), plate)
+    return (x, v) if plate is None else (x, v, F)
 
 
 class BatchRollout:

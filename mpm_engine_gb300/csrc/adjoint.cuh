@@ -60,6 +60,11 @@ struct AdjK {
     int ncol;
     const ColDev *cols;
     const PoseRec *poses;
+    // kinematic cuboids: adjoint of each collider's force accumulator at this
+    // substep ([ncol][3], or null) and the accumulated adjoint of each collider's
+    // velocity ([ncol][3], or null)
+    const float *col_force_b;
+    float *col_vel_b;
 };
 
 // c = a^T b
@@ -487,7 +492,7 @@ __device__ void fluid_stress(const AdjK &k, int p, int mat, const float *Ft, con
                              float *S) {
     const MatTables &T = *k.tab;
     f.Jt = det3(Ft);
-    f.Jc = powf(f.Jt, 1.0f / 3.0f);
+    f.Jc = pow_near1(f.Jt, 1.0f / 3.0f);
     f.J = f.Jc * f.Jc * f.Jc;
 #pragma unroll
     for (int i = 0; i < 9; ++i) Fp[i] = (i % 4 == 0) ? f.Jc : 0.0f;
@@ -699,9 +704,11 @@ __device__ __forceinline__ void coulomb_adj(const float *vr, const float *n, flo
 }
 
 // Adjoint of one collider at one node: vb holds the adjoint of the collider's
-// output velocity on entry and of its input velocity vin on return.
+// output velocity on entry and of its input velocity vin on return. A kinematic
+// cuboid also takes fb, the adjoint of its force accumulator (acc += m (vin - vel)),
+// and adds to velb (its velocity's adjoint) and mb (the node mass's adjoint).
 __device__ void collide_adj(const ColDev &c, const PoseRec &P, int gx, int gy, int gz, const float *vin, float *vb,
-                            const AdjK &a) {
+                            const AdjK &a, float m, const float *fb, float *velb, float &mb) {
     const float dx = a.dx;
     switch (c.kind) {
     case GBMPM_COLLIDER_PLANE: {
@@ -740,10 +747,18 @@ __device__ void collide_adj(const ColDev &c, const PoseRec &P, int gx, int gy, i
         for (int d = 0; d < 3; ++d) vb[d] = wb[d] + n[d] * (ncb - ds * nw);
         return;
     }
-    case GBMPM_COLLIDER_BOX: {
+    case GBMPM_COLLIDER_BOX: {   // v = vel, acc += m (vin - vel) inside (mpm_solver_warp.py:2053-2088)
         if (P.mode == 2) { vb[0] = vb[1] = vb[2] = 0.0f; return; }
         const float o0 = (float)gx * dx - P.p[0], o1 = (float)gy * dx - P.p[1], o2 = (float)gz * dx - P.p[2];
-        if (fabsf(o0) < c.size[0] && fabsf(o1) < c.size[1] && fabsf(o2) < c.size[2]) vb[0] = vb[1] = vb[2] = 0.0f;
+        if (fabsf(o0) < c.size[0] && fabsf(o1) < c.size[1] && fabsf(o2) < c.size[2]) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const float f = fb ? fb[d] : 0.0f;
+                velb[d] += vb[d] - f * m;
+                mb += f * (vin[d] - c.vel[d]);
+                vb[d] = f * m;
+            }
+        }
         return;
     }
     case GBMPM_COLLIDER_CUP: {   // mpm_solver_warp.py:2161-2225
@@ -828,11 +843,21 @@ __global__ void k_adj_grid_bwd(AdjK a) {
         }
         const float4 b4 = a.gvb[id];
         float vb[3] = {b4.x, b4.y, b4.z};
-        for (int c = a.ncol - 1; c >= 0; --c)
-            if (a.poses[c].mode != 0) collide_adj(a.cols[c], a.poses[c], gx, gy, gz, vin[c], vb, a);
+        float mb_col = 0.0f;
+        for (int c = a.ncol - 1; c >= 0; --c) {
+            if (a.poses[c].mode == 0) continue;
+            float velb[3] = {0.f, 0.f, 0.f};
+            collide_adj(a.cols[c], a.poses[c], gx, gy, gz, vin[c], vb, a, mv.w,
+                        a.col_force_b ? a.col_force_b + 3 * c : nullptr, velb, mb_col);
+            if (a.col_vel_b && a.cols[c].kind == GBMPM_COLLIDER_BOX &&
+                (velb[0] != 0.0f || velb[1] != 0.0f || velb[2] != 0.0f)) {
+#pragma unroll
+                for (int d = 0; d < 3; ++d) atomicAdd(a.col_vel_b + 3 * c + d, velb[d]);
+            }
+        }
         if (a.damp < 1.0f) { vb[0] *= a.damp; vb[1] *= a.damp; vb[2] *= a.damp; }
         const float inv = 1.0f / mv.w;
-        const float mb = -(vb[0] * mv.x + vb[1] * mv.y + vb[2] * mv.z) * inv * inv;
+        const float mb = -(vb[0] * mv.x + vb[1] * mv.y + vb[2] * mv.z) * inv * inv + mb_col;
         a.gmb[id] = make_float4(vb[0] * inv, vb[1] * inv, vb[2] * inv, mb);
     }
 }
@@ -1353,6 +1378,8 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
         a.hard1 = e->M.hardening[1]; a.xi1 = e->M.xi[1];
         a.xb = gr->x; a.vb = gr->v; a.Cb = gr->C; a.Ftb = gr->F_trial; a.Lb = gr->L; a.ysb = gr->yield_stress;
         a.mub = gr->mu; a.lamb = gr->lam; a.pvb = gr->viscosity; a.Jpb = gr->Jp;
+        a.col_force_b = gr->collider_force ? gr->collider_force + (size_t)i * 3 * std::max(1, nc) : nullptr;
+        a.col_vel_b = gr->collider_velocity;
         a.ncol = nc; a.cols = e->d_cols.ptr; a.poses = e->d_pose.ptr + (size_t)i * std::max(1, nc);
         // the engine's P2G building block reads its inputs through a PK
         gbmpm_particles Ps = P;

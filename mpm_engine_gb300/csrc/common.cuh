@@ -198,6 +198,26 @@ __device__ __forceinline__ void udvt(const float *U, float d0, float d1, float d
 
 __device__ __forceinline__ void set_status(unsigned *st, unsigned bit) { atomicOr(st, bit); }
 
+// Launch with programmatic stream serialization (see pdl_wait) when `pdl` is set.
+template <typename... P, typename... A>
+inline void launch_kernel(bool pdl, void (*kern)(P...), int grid, int block, cudaStream_t s, A... args) {
+    if (!pdl) {
+        kern<<<grid, block, 0, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 // The particle-pass launcher (particles.cu): picks the direct or the tiled kernel
 // and its specialisation (solids compiled in or out, resident CTAs per SM, CPIC).
 struct ParticleLaunch {
@@ -208,5 +228,26 @@ struct ParticleLaunch {
     int cdf_occ;     // the same for its CPIC variant
 };
 void launch_particle_pass(const ParticleLaunch &L, const PK &k, int mode, cudaStream_t s);
+
+// Batched scenes: one particle pass over many scenes. CTA b of the launch takes
+// tile ctas[b].tile of scene ctas[b].scene (particles_batch_*.cu).
+struct BatchCta {
+    int scene, tile;
+};
+struct BatchLaunch {
+    int threads;     // particles per tile (CTA width): 64, 128 or 256
+    int occ;         // resident 256-thread equivalents per SM the kernel is compiled for: 2 or 3
+    bool solids;     // SVD-based laws present in some scene
+    bool pdl;
+};
+void launch_particle_batch_fluid(const BatchLaunch &L, const PK *table, const BatchCta *ctas, int nctas, int mode,
+                                 int list, int sub, cudaStream_t s);
+void launch_particle_batch_solid(const BatchLaunch &L, const PK *table, const BatchCta *ctas, int nctas, int mode,
+                                 int list, int sub, cudaStream_t s);
+inline void launch_particle_batch(const BatchLaunch &L, const PK *table, const BatchCta *ctas, int nctas, int mode,
+                                  int list, int sub, cudaStream_t s) {
+    if (L.solids) launch_particle_batch_solid(L, table, ctas, nctas, mode, list, sub, s);
+    else launch_particle_batch_fluid(L, table, ctas, nctas, mode, list, sub, s);
+}
 
 }  // namespace gbmpm

@@ -258,21 +258,7 @@ bool has_solids(const gbmpm_model &m) {
 // Launch with programmatic stream serialization (see pdl_wait) when enabled.
 template <typename... P, typename... A>
 void launch_pdl(gbmpm_engine *e, void (*kern)(P...), int grid, int block, cudaStream_t s, A... args) {
-    if (!e->pdl) {
-        kern<<<grid, block, 0, s>>>(args...);
-        return;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kern, args...);
+    launch_kernel(e->pdl, kern, grid, block, s, args...);
 }
 
 void launch_particles(gbmpm_engine *e, const PK &k, int mode, bool tiled, cudaStream_t s) {
@@ -355,7 +341,7 @@ const int *record_ws_begin(gbmpm_engine *e, cudaStream_t s) {
     return e->ws_idx[cur].ptr;
 }
 
-void launch_grid(gbmpm_engine *e, float dt, int substep, int list, cudaStream_t s) {
+GK make_gk(gbmpm_engine *e, float dt, int substep, int list) {
     GK g{};
     g.gmv = reinterpret_cast<float4 *>(e->G.mv);
     g.gv = reinterpret_cast<float4 *>(e->G.v);
@@ -373,6 +359,11 @@ void launch_grid(gbmpm_engine *e, float dt, int substep, int list, cudaStream_t 
     g.blk_count_read = e->d_count.ptr + list;
     g.blk_count_reset = e->d_count.ptr + (list ^ 1);
     g.bd = e->bd;
+    return g;
+}
+
+void launch_grid(gbmpm_engine *e, float dt, int substep, int list, cudaStream_t s) {
+    GK g = make_gk(e, dt, substep, list);
     // one wave of CTAs looping over the active blocks: the per-CTA setup (collider
     // tables into shared memory, two barriers) is paid once per SM slot, not per item
     int grid = e->num_sms * e->grid_ctas;
@@ -1464,6 +1455,23 @@ int gbmpm_profile(gbmpm_engine *e, double ms_out[GBMPM_NUM_PHASES], int64_t coun
 
 int64_t gbmpm_launch_count(gbmpm_engine *e) { return e ? e->launches : 0; }
 
+int gbmpm_set_tuning(gbmpm_engine *e, int32_t tile_occ, int32_t grid_ctas) {
+    if (!e) return fail(GBMPM_ERR_ARG, "null argument");
+    if (tile_occ < 2 || tile_occ > 4 || grid_ctas < 1 || grid_ctas > 8)
+        return fail(GBMPM_ERR_ARG, "tile_occ is 2 to 4; grid_ctas 1 to 8");
+    e->tile_occ = tile_occ;
+    e->grid_ctas = grid_ctas;
+    mark_dirty(e);
+    return GBMPM_OK;
+}
+
+int gbmpm_get_tuning(gbmpm_engine *e, int32_t out[2]) {
+    if (!e || !out) return fail(GBMPM_ERR_ARG, "null argument");
+    out[0] = e->tile_occ;
+    out[1] = e->grid_ctas;
+    return GBMPM_OK;
+}
+
 int gbmpm_debug_deposit_sums(gbmpm_engine *e, double dt, double out[4], void *stream) {
     int rc = check_ready(e);
     if (rc) return rc;
@@ -1507,7 +1515,7 @@ struct gbmpm_batch {
     std::vector<uint64_t> versions;
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> joins;
-    cudaEvent_t fork = nullptr;
+    cudaEvent_t fork = nullptr, fork2 = nullptr;
     cudaGraphExec_t graph = nullptr;
     int g_substeps = -1, g_flags = -1;
     double g_dt = 0.0;
@@ -1515,7 +1523,135 @@ struct gbmpm_batch {
     int64_t launches = 0;
     bool graph_failed = false;          // a capture failed: live launches from then on
     bool fake_capture_failure = false;  // test hook: treat the next capture as failed
+    // The single-launch schedule (fused ticks whose scenes all run the tiled path):
+    // every particle pass and every grid pass is one launch over all scenes, each
+    // CTA finding its scene and tile in the tables below.
+    bool single_launch = true;          // use it when every scene qualifies
+    int tile_threads = 128;             // particles per CTA of the batched particle pass
+    int tile_occ = 3;                   // its resident 256-thread equivalents per SM
+    int grid_ctas = 2;                  // grid-update CTAs per SM, shared out by particle count
+    int tuning_version = 0;             // bumped by gbmpm_batch_set_tuning
+    bool g_single = false;              // the cached graph runs the single-launch schedule
+    int g_tuning = -1;
+    DevBuf<PK> d_pk;                    // per-scene particle-pass records
+    DevBuf<GK> d_gk;                    // per-scene grid-pass records
+    DevBuf<BatchCta> d_pcta;            // particle-pass CTA -> (scene, tile)
+    DevBuf<int4> d_gcta;                // grid-pass CTA -> (scene, CTA of the scene, CTAs of the scene)
+    int n_pcta = 0, n_gcta = 0;
+    bool any_solids = false;
+    std::vector<uint64_t> t_versions;   // engine versions the tables were built for
+    float t_dt = -1.0f;
+    int t_tuning = -1;
+    std::vector<const int *> perms;     // each scene's working-set permutation, for the scatter back
 };
+
+namespace {
+
+// Every scene of the batch runs the fused schedule on its block-sorted working set,
+// with no feature that adds launches between the passes (CPIC lanes, rigid bodies,
+// particle modifiers).
+bool batch_single_launch_ok(const gbmpm_batch *b, bool fused, const std::vector<char> &reorder) {
+    if (!b->single_launch || !fused) return false;
+    for (size_t i = 0; i < b->engines.size(); ++i) {
+        const gbmpm_engine *e = b->engines[i];
+        if (!reorder[i] || e->P.n == 0 || e->cdf.n > 0 || e->n_bodies > 0 || e->n_mods > 0) return false;
+    }
+    return true;
+}
+
+// Builds and uploads the per-scene records and CTA maps when an engine, the
+// substep or the tuning changed since the last build. The stream is synchronized
+// first: a replay of the previous graph may still be reading the old tables.
+int batch_tables(gbmpm_batch *b, float dtf, cudaStream_t s) {
+    const int n = (int)b->engines.size();
+    bool same = b->t_dt == dtf && b->t_tuning == b->tuning_version && (int)b->t_versions.size() == n;
+    for (int i = 0; i < n && same; ++i) same = b->t_versions[i] == b->engines[i]->version;
+    if (same) return GBMPM_OK;
+    GB_CUDA(cudaStreamSynchronize(s));
+    std::vector<PK> pk(n);
+    std::vector<GK> gk(n);
+    std::vector<BatchCta> pc;
+    std::vector<int4> gc;
+    long long total = 0;
+    for (gbmpm_engine *e : b->engines) total += e->P.n;
+    const int th = b->tile_threads;
+    const int gtotal = std::max(n, b->engines[0]->num_sms * b->grid_ctas);
+    b->any_solids = false;
+    for (int i = 0; i < n; ++i) {
+        gbmpm_engine *e = b->engines[i];
+        pk[i] = make_pk(e, e->W, dtf, 0);
+        gk[i] = make_gk(e, dtf, 0, 0);
+        b->any_solids = b->any_solids || has_solids(e->M);
+        const int tiles = (e->P.n + th - 1) / th;
+        for (int t = 0; t < tiles; ++t) pc.push_back(BatchCta{i, t});
+        const int g = std::max(1, (int)std::llround((double)gtotal * (double)e->P.n / (double)std::max(1LL, total)));
+        for (int c = 0; c < g; ++c) gc.push_back(make_int4(i, c, g, 0));
+    }
+    GB_CUDA(b->d_pk.ensure(n));
+    GB_CUDA(b->d_gk.ensure(n));
+    GB_CUDA(b->d_pcta.ensure(pc.size()));
+    GB_CUDA(b->d_gcta.ensure(gc.size()));
+    GB_CUDA(cudaMemcpy(b->d_pk.ptr, pk.data(), n * sizeof(PK), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(b->d_gk.ptr, gk.data(), n * sizeof(GK), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(b->d_pcta.ptr, pc.data(), pc.size() * sizeof(BatchCta), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(b->d_gcta.ptr, gc.data(), gc.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    b->n_pcta = (int)pc.size();
+    b->n_gcta = (int)gc.size();
+    b->t_versions.resize(n);
+    for (int i = 0; i < n; ++i) b->t_versions[i] = b->engines[i]->version;
+    b->t_dt = dtf;
+    b->t_tuning = b->tuning_version;
+    return GBMPM_OK;
+}
+
+// Records one fused tick of every scene: each scene's working-set sort and gather on
+// its own branch, then per substep one particle pass and one grid pass over all
+// scenes on s, then each scene's scatter back on its branch. Returns the first
+// error of an event call (the launches report through cudaGetLastError).
+cudaError_t batch_record_single_launch(gbmpm_batch *b, float dtf, int S, cudaStream_t s) {
+    (void)dtf;
+    const int n = (int)b->engines.size();
+    cudaError_t first = cudaEventRecord(b->fork, s);
+    auto keep = [&](cudaError_t err) { if (first == cudaSuccess) first = err; };
+    b->perms.assign(n, nullptr);
+    int64_t launches = 0;
+    for (int i = 0; i < n; ++i) {
+        gbmpm_engine *e = b->engines[i];
+        keep(cudaStreamWaitEvent(b->streams[i], b->fork, 0));
+        const int64_t before = e->launches;
+        b->perms[i] = record_ws_begin(e, b->streams[i]);
+        launches += e->launches - before;
+        e->launches = before;
+        keep(cudaEventRecord(b->joins[i], b->streams[i]));
+        keep(cudaStreamWaitEvent(s, b->joins[i], 0));
+    }
+    const bool pdl = b->engines[0]->pdl;
+    const BatchLaunch L{b->tile_threads, b->tile_occ, b->any_solids, pdl};
+    for (int sub = 0; sub < S; ++sub) {
+        const int list = sub & 1;
+        int mode = (sub == 0) ? (PASS_STRESS | PASS_P2G) : (PASS_G2P | PASS_STRESS | PASS_P2G);
+        if (sub == S - 1) mode |= PASS_STORE_ALL;
+        launch_particle_batch(L, b->d_pk.ptr, b->d_pcta.ptr, b->n_pcta, mode, list, sub, s);
+        launch_kernel(pdl, k_grid_batch, b->n_gcta, kGridThreads, s, (const GK *)b->d_gk.ptr,
+                      (const int4 *)b->d_gcta.ptr, sub, list);
+        launches += 2;
+    }
+    launch_particle_batch(L, b->d_pk.ptr, b->d_pcta.ptr, b->n_pcta, PASS_G2P | PASS_RESET_LISTS, 0, 0, s);
+    launches += 1;
+    keep(cudaEventRecord(b->fork2, s));
+    for (int i = 0; i < n; ++i) {
+        gbmpm_engine *e = b->engines[i];
+        keep(cudaStreamWaitEvent(b->streams[i], b->fork2, 0));
+        k_ws_scatter<<<(e->P.n + 255) / 256, 256, 0, b->streams[i]>>>(e->ws_table, b->perms[i], e->P.n);
+        launches += 1;
+        keep(cudaEventRecord(b->joins[i], b->streams[i]));
+        keep(cudaStreamWaitEvent(s, b->joins[i], 0));
+    }
+    b->launches += launches;
+    return first;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -1531,6 +1667,7 @@ int gbmpm_batch_create(gbmpm_engine *const *engines, int32_t n, gbmpm_batch **ou
     b->streams.assign(n, nullptr);
     b->joins.assign(n, nullptr);
     cudaError_t err = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&b->fork2, cudaEventDisableTiming);
     for (int i = 0; i < n && err == cudaSuccess; ++i) {
         err = cudaStreamCreateWithFlags(&b->streams[i], cudaStreamNonBlocking);
         if (err == cudaSuccess) err = cudaEventCreateWithFlags(&b->joins[i], cudaEventDisableTiming);
@@ -1546,6 +1683,8 @@ void gbmpm_batch_destroy(gbmpm_batch *b) {
     for (cudaStream_t st : b->streams) if (st) cudaStreamDestroy(st);
     for (cudaEvent_t ev : b->joins) if (ev) cudaEventDestroy(ev);
     if (b->fork) cudaEventDestroy(b->fork);
+    if (b->fork2) cudaEventDestroy(b->fork2);
+    b->d_pk.release(); b->d_gk.release(); b->d_pcta.release(); b->d_gcta.release();
     delete b;
 }
 
@@ -1566,16 +1705,28 @@ int gbmpm_batch_tick(gbmpm_batch *b, double *times, double dt, int32_t substeps,
     }
     const bool fused = (flags & GBMPM_TICK_FUSED) != 0;
     const float dtf = (float)dt;
-    auto live = [&]() {
-        for (int i = 0; i < n; ++i)
-            if (b->engines[i]->P.n > 0) record_tick(b->engines[i], dtf, substeps, fused, reorder[i], s, false);
+    const bool single = batch_single_launch_ok(b, fused, reorder);
+    if (single) {
+        int rt = batch_tables(b, dtf, s);
+        if (rt) return rt;
+    }
+    auto live = [&]() -> int {
+        if (single) {
+            GB_CUDA(batch_record_single_launch(b, dtf, substeps, s));
+        } else {
+            for (int i = 0; i < n; ++i)
+                if (b->engines[i]->P.n > 0) record_tick(b->engines[i], dtf, substeps, fused, reorder[i], s, false);
+        }
+        return GBMPM_OK;
     };
     if (!(flags & GBMPM_TICK_GRAPH) || b->graph_failed) {
-        live();
+        int rl = live();
+        if (rl) return rl;
         GB_CUDA(cudaGetLastError());
         return GBMPM_OK;
     }
-    bool reuse = b->graph && b->g_substeps == substeps && b->g_flags == flags && b->g_dt == dt;
+    bool reuse = b->graph && b->g_substeps == substeps && b->g_flags == flags && b->g_dt == dt &&
+                 b->g_single == single && b->g_tuning == b->tuning_version;
     for (int i = 0; i < n && reuse; ++i) reuse = b->versions[i] == b->engines[i]->version;
     if (!reuse) {
         if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
@@ -1590,10 +1741,18 @@ int gbmpm_batch_tick(gbmpm_batch *b, double *times, double dt, int32_t substeps,
         // inside the capture the first error is kept rather than returned at once, so
         // the capture is always ended and its stream released; a failed capture then
         // takes the live fallback below
-        cudaError_t first = cudaEventRecord(b->fork, cap);
+        cudaError_t first = cudaSuccess;
         auto keep = [&](cudaError_t err) { if (first == cudaSuccess) first = err; };
         int64_t total = 0;
-        for (int i = 0; i < n && first == cudaSuccess; ++i) {
+        if (single) {
+            const int64_t before = b->launches;
+            keep(batch_record_single_launch(b, dtf, substeps, cap));
+            total = b->launches - before;
+            b->launches = before;
+        } else {
+            keep(cudaEventRecord(b->fork, cap));
+        }
+        for (int i = 0; i < n && first == cudaSuccess && !single; ++i) {
             gbmpm_engine *e = b->engines[i];
             keep(cudaStreamWaitEvent(b->streams[i], b->fork, 0));
             if (e->P.n > 0 && first == cudaSuccess) {
@@ -1621,12 +1780,14 @@ int gbmpm_batch_tick(gbmpm_batch *b, double *times, double dt, int32_t substeps,
             b->graph = nullptr;
             b->graph_failed = true;
             (void)cudaGetLastError();
-            live();
+            int rl = live();
+            if (rl) return rl;
             GB_CUDA(cudaGetLastError());
             return GBMPM_OK;
         }
         for (int i = 0; i < n; ++i) b->versions[i] = b->engines[i]->version;
         b->g_substeps = substeps; b->g_flags = flags; b->g_dt = dt;
+        b->g_single = single; b->g_tuning = b->tuning_version;
         b->graph_launches = total;
     }
     GB_CUDA(cudaGraphLaunch(b->graph, s));
@@ -1673,6 +1834,30 @@ int gbmpm_batch_guard(gbmpm_batch *b, float *out, uint32_t *status, void *stream
 }
 
 int64_t gbmpm_batch_launch_count(gbmpm_batch *b) { return b ? b->launches : 0; }
+
+int gbmpm_batch_set_tuning(gbmpm_batch *b, int32_t single_launch, int32_t tile_threads, int32_t tile_occ,
+                           int32_t grid_ctas) {
+    if (!b) return fail(GBMPM_ERR_ARG, "null argument");
+    if (!(tile_threads == 64 || tile_threads == 128 || tile_threads == 256) || tile_occ < 2 || tile_occ > 3 ||
+        grid_ctas < 1 || grid_ctas > 8)
+        return fail(GBMPM_ERR_ARG, "tile_threads is 64, 128 or 256; tile_occ 2 or 3; grid_ctas 1 to 8");
+    b->single_launch = single_launch != 0;
+    b->tile_threads = tile_threads;
+    b->tile_occ = tile_occ;
+    b->grid_ctas = grid_ctas;
+    b->tuning_version++;
+    return GBMPM_OK;
+}
+
+int gbmpm_batch_get_tuning(gbmpm_batch *b, int32_t out[5]) {
+    if (!b || !out) return fail(GBMPM_ERR_ARG, "null argument");
+    out[0] = b->single_launch ? 1 : 0;
+    out[1] = b->tile_threads;
+    out[2] = b->tile_occ;
+    out[3] = b->grid_ctas;
+    out[4] = b->g_single ? 1 : 0;
+    return GBMPM_OK;
+}
 
 }  // extern "C"
 

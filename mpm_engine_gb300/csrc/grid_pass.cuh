@@ -494,7 +494,9 @@ __device__ __forceinline__ void collide(const ColDev &c, const PoseRec &P, int g
 // Grid pass over the active-block list: normalize + gravity (mpm_utils.py:927-941),
 // damping (:1287-1295), every collider in list order, then clear the scatter
 // target and the block flags for the next particle pass.
-__global__ void __launch_bounds__(kGridThreads) k_grid(GK k) {
+// The grid update over a scene's active-block list, by CTA `cta` of the `nctas`
+// CTAs given to that scene.
+__device__ __forceinline__ void grid_update(const GK &k, int cta, int nctas) {
     __shared__ ColDev s_cols[kMaxCol];
     __shared__ PoseRec s_pose[kMaxCol];
     __shared__ float s_acc[kMaxCol][6];
@@ -504,13 +506,13 @@ __global__ void __launch_bounds__(kGridThreads) k_grid(GK k) {
     pdl_wait();   // the particle pass before this one deposits into gmv and fills the block list
     pdl_trigger();
     const int per = blockDim.x / 64;
-    const int stride = gridDim.x * per;
-    const int first = blockIdx.x * per + t / 64;
+    const int stride = nctas * per;
+    const int first = cta * per + t / 64;
     // the count and this thread's first list entry are read together: the list holds
     // bd^3 entries, and an entry at or past the count is never used
     const int count = *k.blk_count_read;
     int b_next = (first < k.bd * k.bd * k.bd) ? k.blk_list[first] : 0;
-    if (blockIdx.x == 0 && t == 0) *k.blk_count_reset = 0;
+    if (cta == 0 && t == 0) *k.blk_count_reset = 0;
     __syncthreads();
     const int lane = t & 31;
     for (int item = first; item < count; item += stride) {
@@ -565,4 +567,27 @@ __global__ void __launch_bounds__(kGridThreads) k_grid(GK k) {
         float a = s_acc[i / 6][i % 6];
         if (a != 0.0f) atomicAdd(&k.wrench[i], (double)a);
     }
+}
+
+__global__ void __launch_bounds__(kGridThreads) k_grid(GK k) { grid_update(k, blockIdx.x, gridDim.x); }
+
+// Batched scenes: CTA b updates scene ctas[b].x as CTA ctas[b].y of ctas[b].z.
+// The per-scene record holds the tick's first pose row, block list 0 and the
+// count pair; `substep` and `list` select this pass's.
+__global__ void __launch_bounds__(kGridThreads) k_grid_batch(const GK *table, const int4 *ctas, int substep, int list) {
+    __shared__ GK s_g;
+    const int4 c = ctas[blockIdx.x];
+    const int *src = reinterpret_cast<const int *>(table + c.x);
+    int *d = reinterpret_cast<int *>(&s_g);
+    for (int i = threadIdx.x; i < (int)(sizeof(GK) / 4); i += blockDim.x) d[i] = src[i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int *counts = s_g.blk_count_read;
+        s_g.poses += (size_t)substep * (s_g.ncol > 0 ? s_g.ncol : 1);
+        s_g.blk_list += (size_t)list * s_g.bd * s_g.bd * s_g.bd;
+        s_g.blk_count_read = counts + list;
+        s_g.blk_count_reset = counts + (list ^ 1);
+    }
+    __syncthreads();
+    grid_update(s_g, c.y, c.z);
 }

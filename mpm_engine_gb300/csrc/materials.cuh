@@ -23,7 +23,19 @@ __device__ __forceinline__ void dev_rate(const float *L, float *Dd, float &gd) {
     gd = sqrtf(2.0f * dd + 0.02f * 0.02f);
 }
 
-__device__ __forceinline__ float eos_pressure(float J, float bulk) { return -bulk * (powf(J, -1.1f) - 1.0f); }
+// x^y for x near 1 (the volume ratios of the fluid laws), as 1 + expm1(y log1p(x - 1)).
+// x - 1 is exact for x in [0.5, 2], and the small term carries about one ulp of its
+// own size, far below the final rounding next to 1: the result is the correctly
+// rounded power except in rare near-ties, as an accurate C library's powf gives it.
+// Near 1 a powf with a few ulps of error would differ from that rounding often, and
+// the stiff equation of state (K (J^-1.1 - 1), K ~ 1e6 Pa) turns each ulp into a
+// visible pressure difference. Away from [0.5, 2] this is powf.
+__device__ __forceinline__ float pow_near1(float x, float y) {
+    if (!(x > 0.5f && x < 2.0f)) return powf(x, y);
+    return 1.0f + expm1f(y * log1pf(x - 1.0f));
+}
+
+__device__ __forceinline__ float eos_pressure(float J, float bulk) { return -bulk * (pow_near1(J, -1.1f) - 1.0f); }
 
 __device__ __forceinline__ float table_lerp(const float *tab, int n, float smin, float smax, float s) {
     float idx = (s - smin) / (smax - smin) * (float)(n - 1);
@@ -81,7 +93,7 @@ __device__ __forceinline__ void stress_update(const PK &k, int p, int mat, const
             J = 1.0f;
         } else {
             float Jt = det3(Ft);
-            float Jc = powf(Jt, 1.0f / 3.0f);
+            float Jc = pow_near1(Jt, 1.0f / 3.0f);
 #pragma unroll
             for (int i = 0; i < 9; ++i) F[i] = (i % 4 == 0) ? Jc : 0.0f;
             J = Jc * Jc * Jc;

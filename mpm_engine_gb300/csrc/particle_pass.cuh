@@ -617,14 +617,16 @@ constexpr int kRec = 40;                  // floats per particle scatter record 
 // record stride in shared memory: 44 floats = 176 B, so the 16-byte stores of eight
 // consecutive lanes land on disjoint bank groups (a 160 B stride pairs them up)
 constexpr int kRecStride = 44;
-template <bool CDF>
-struct Tile {
-    static constexpr int threads = CDF ? kTileThreadsCdf : kTileThreads;
-    static constexpr int gather_cap = 6 * threads;   // nodes in the shared gather tile (16 B each)
-    static constexpr int smem_floats =
-        (gather_cap * 4 > threads * kRecStride) ? gather_cap * 4 : threads * kRecStride;
-    static_assert(gather_cap * 4 + 11 * threads <= smem_floats, "prefetch slots fit past the gather tile");
+// shared-memory shape of a tile of TH particles
+template <int TH>
+struct TileShape {
+    static constexpr int threads = TH;
+    static constexpr int gather_cap = 6 * TH;   // nodes in the shared gather tile (16 B each)
+    static constexpr int smem_floats = (gather_cap * 4 > TH * kRecStride) ? gather_cap * 4 : TH * kRecStride;
+    static_assert(gather_cap * 4 + 11 * TH <= smem_floats, "prefetch slots fit past the gather tile");
 };
+template <bool CDF>
+struct Tile : TileShape<CDF ? kTileThreadsCdf : kTileThreads> {};
 // the CPIC reaction partials are indexed by CTA; they are sized for the narrower of
 // the direct and the tiled CPIC launches
 constexpr int kCdfCtaThreads = kParticleThreads < kTileThreadsCdf ? kParticleThreads : kTileThreadsCdf;
@@ -679,16 +681,16 @@ __device__ __forceinline__ void bspline_o(float fx, int o, float &w, float &dw) 
     dw = (o == 0) ? -t0 : ((o == 1) ? -2.0f * t1 : t2);
 }
 
-// CDF adds the CPIC branches of the direct kernel: the gather reads the ghost
-// velocity at nodes incompatible with the particle, and scatter runs are keyed by
-// (base cell, particle tag) so each run deposits under one mask, its blocked nodes
-// becoming the owner lane's reaction.
-template <bool SOLIDS, int MINB, bool CDF = false>
-__global__ void __launch_bounds__(Tile<CDF>::threads, MINB * 256 / Tile<CDF>::threads)
-    k_particles_tiled(PK k, int mode) {
-    constexpr int kTileThreads = Tile<CDF>::threads;
-    constexpr int kGatherCap = Tile<CDF>::gather_cap;
-    __shared__ __align__(16) float s_mem[Tile<CDF>::smem_floats];
+// One tile of TH consecutive particles of the sorted working set (`tile` is its
+// index; the kernels below map CTAs to tiles). CDF adds the CPIC branches of the
+// direct kernel: the gather reads the ghost velocity at nodes incompatible with the
+// particle, and scatter runs are keyed by (base cell, particle tag) so each run
+// deposits under one mask, its blocked nodes becoming the owner lane's reaction.
+template <bool SOLIDS, bool CDF, int TH>
+__device__ __forceinline__ void particles_tile(const PK &k, int mode, int tile) {
+    constexpr int kTileThreads = TH;
+    constexpr int kGatherCap = TileShape<TH>::gather_cap;
+    __shared__ __align__(16) float s_mem[TileShape<TH>::smem_floats];
     __shared__ int s_key[kTileThreads];
     __shared__ int s_pc[CDF ? kTileThreads : 1];
     __shared__ int s_mask[CDF ? kTileThreads : 1];
@@ -703,7 +705,7 @@ __global__ void __launch_bounds__(Tile<CDF>::threads, MINB * 256 / Tile<CDF>::th
     float(*s_pf)[kTileThreads] = reinterpret_cast<float(*)[kTileThreads]>(s_mem + kGatherCap * 4);
     const int t = threadIdx.x;
     const int lane = t & 31, warp = t >> 5;
-    const int p = blockIdx.x * kTileThreads + t;
+    const int p = tile * kTileThreads + t;
     bool live = p < k.n && !(k.sel && k.sel[p] != 0);
     const int mat = live ? k.mat[p] : 0;
     if (!(mode & PASS_G2P)) {   // without a gather, x and the stress inputs are what the previous pass wrote
@@ -762,7 +764,7 @@ __global__ void __launch_bounds__(Tile<CDF>::threads, MINB * 256 / Tile<CDF>::th
         block_box<kTileThreads>(s.b, want, box, s_red, kGatherCap);
         pdl_wait();   // the grid velocities come from the grid pass before this one
         pdl_trigger();
-        if ((mode & PASS_RESET_LISTS) && blockIdx.x == 0 && threadIdx.x == 0) {
+        if ((mode & PASS_RESET_LISTS) && tile == 0 && threadIdx.x == 0) {
             k.blk_count[0] = 0;
             k.blk_count[1] = 0;
         }
@@ -1000,7 +1002,7 @@ __global__ void __launch_bounds__(Tile<CDF>::threads, MINB * 256 / Tile<CDF>::th
                         const float *cc = k.lanes.c_cur[own];
                         const float r[3] = {(float)gx * k.dx - cc[0], (float)gy * k.dx - cc[1],
                                             (float)(bz + kk) * k.dx - cc[2]};
-                        double *w = k.cwrench + ((size_t)blockIdx.x * GBMPM_MAX_CDF + own) * 6;
+                        double *w = k.cwrench + ((size_t)tile * GBMPM_MAX_CDF + own) * 6;
                         atomicAdd(w + 0, (double)acc[kk][0]);
                         atomicAdd(w + 1, (double)acc[kk][1]);
                         atomicAdd(w + 2, (double)acc[kk][2]);
@@ -1022,4 +1024,38 @@ __global__ void __launch_bounds__(Tile<CDF>::threads, MINB * 256 / Tile<CDF>::th
             }
         }
     }
+}
+
+// The tiled particle pass of one scene: CTA b takes tile b.
+template <bool SOLIDS, int MINB, bool CDF = false>
+__global__ void __launch_bounds__(Tile<CDF>::threads, MINB * 256 / Tile<CDF>::threads)
+    k_particles_tiled(PK k, int mode) {
+    particles_tile<SOLIDS, CDF, Tile<CDF>::threads>(k, mode, blockIdx.x);
+}
+
+// ---- batched scenes: one launch runs the same pass over many scenes ---------
+// Scene s contributes ceil(n_s / TH) tiles; CTA b takes tile ctas[b].tile of scene
+// ctas[b].scene, whose pass record (its working set, grid, block lists, material
+// tables) it copies from the per-scene table into shared memory. The record holds
+// block list 0 and the tick's first substep; `list` and `sub` select this pass's.
+__device__ __forceinline__ void load_scene_pk(PK &dst, const PK *table, int scene, int list, int sub) {
+    const int *src = reinterpret_cast<const int *>(table + scene);
+    int *d = reinterpret_cast<int *>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(PK) / 4); i += blockDim.x) d[i] = src[i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        dst.blk_list += (size_t)list * dst.bd * dst.bd * dst.bd;
+        dst.blk_count += list;
+        dst.sub += sub;
+    }
+    __syncthreads();
+}
+
+template <bool SOLIDS, int MINB, int TH>
+__global__ void __launch_bounds__(TH, MINB * 256 / TH)
+    k_particles_batch(const PK *table, const BatchCta *ctas, int mode, int list, int sub) {
+    __shared__ PK s_k;
+    const BatchCta c = ctas[blockIdx.x];
+    load_scene_pk(s_k, table, c.scene, list, sub);
+    particles_tile<SOLIDS, false, TH>(s_k, mode, c.tile);
 }

@@ -1106,6 +1106,13 @@ class Solver:
         self._vol0 = self._vol0[p]
         return True
 
+    def autotune(self, dt: float, substeps: int, ticks: int = 2, use_cache: bool = True) -> dict:
+        """Picks the fastest launch shape of this scene's passes
+        (mpm_engine_gb300.autotune); the scene's state is restored after the search."""
+        from .autotune import tune_solver
+        self._require_loaded()
+        return tune_solver(self, dt, substeps, ticks=ticks, use_cache=use_cache)
+
     def profile_report(self) -> str:
         """Per-phase device time collected while profile=True (CUDA events, live launches)."""
         if self._eng is None:
@@ -1483,3 +1490,22 @@ class BatchSolver:
 
     def launch_count(self) -> int:
         return int(self.lib.gbmpm_batch_launch_count(self.h))
+
+    def autotune(self, dt: float, substeps: int, ticks: int = 2, use_cache: bool = True) -> dict:
+        """Picks the fastest launch shape for these scenes (mpm_engine_gb300.autotune):
+        every candidate is timed on the scenes' own state, which is restored after."""
+        from .autotune import tune_batch
+        return tune_batch(self, dt, substeps, ticks=ticks, use_cache=use_cache)
+
+    @property
+    def tuning(self) -> dict:
+        """The launch shape in use: single-launch schedule, particles per CTA,
+        resident CTAs per SM, grid CTAs per SM."""
+        from .autotune import batch_tuning
+        return batch_tuning(self)
+
+    def set_tuning(self, single_launch: bool = True, tile_threads: int = 128, tile_occ: int = 3,
+                   grid_ctas_per_sm: int = 2) -> BatchSolver:
+        from .autotune import set_batch_tuning
+        set_batch_tuning(self, (int(single_launch), tile_threads, tile_occ, grid_ctas_per_sm))
+        return self

@@ -113,57 +113,150 @@ def test_identification_scene_full_length(cuda):
     and squeezed by a plate pressed into its top at 0.05 m/s, 400 substeps of 1e-5 s
     with checkpoints every 20. The loss is the squared distance of the final
     positions to a seeded target rollout (the same scene with E, nu and the yield
-    stress 30 %, 5 % and 30 % higher) plus a seeded projection of the final
-    velocities. dL/dE, dL/dnu, dL/dyield and a unit direction of dL/dv0 against
-    central differences of the float64 oracle at h = 1e-3 relative."""
+    stress 30 %, 5 % and 30 % higher), plus the squared distance of the plate's
+    reaction-force trace (one force per 20-substep segment) to the target's, plus a
+    seeded projection of the final velocities. dL/dE, dL/dnu, dL/dyield, dL/d(plate
+    velocity, z) and a unit direction of dL/dv0 against central differences of the
+    float64 oracle at h = 1e-3 relative."""
     import torch
     from mpm_engine_gb300 import Solver, adjoint
     from mpm_engine_gb300.materials import vonmises
     from mpm_engine_gb300.scenes import squeeze_scene
     from oracle.oracle import OracleSolver
-    E0, nu0, ys0, dt, K5, every = 1.0e5, 0.3, 500.0, 1.0e-5, 400, 20
+    E0, nu0, ys0, dt, K5, every = 1.0e5, 0.3, 100.0, 1.0e-5, 400, 20
 
     def scene(E, nu, ys):
         s, _ = squeeze_scene(Solver, 50_000, 48, vonmises(E=E, nu=nu, yield_stress=ys, density=1000.0),
                              seed=3, plate_gap=-0.5)
         return s
 
+    nseg = K5 // every
     tgt = scene(1.3 * E0, 1.05 * nu0, 1.3 * ys0)
-    tgt.step(dt, K5)
+    ht = _plate_handle(tgt)
+    F_t = []
+    for _ in range(nseg):
+        tgt.reset_tool_force(ht)
+        tgt.step(dt, every)
+        F_t.append(tgt.tool_force(ht, dt * every))
+    F_t = np.array(F_t)
     x_t = tgt._t["x"].double().clone()
     s = scene(E0, nu0, ys0)
+    hp = _plate_handle(s)
+    vel0 = np.array(s._cols[s._col(hp)].velocity[:], np.float64)
     n = s.n_particles
     st = s.export_state()
     b = torch.from_numpy(np.random.default_rng(8).standard_normal((n, 3))).to(x_t.device)
     dev = x_t.device
+    F_tt = torch.from_numpy(F_t).to(dev)
     t = lambda x: torch.tensor(x, device=dev, dtype=torch.float32, requires_grad=True)  # noqa: E731
     v0 = s._t["v"].clone().requires_grad_(True)
-    E, nu, ys = t(E0), t(nu0), t(ys0)
-    x, v = adjoint.rollout(s, dt, K5, v0=v0, E=E, nu=nu, yield_stress=ys, checkpoint_every=every)
-    L = ((x.double() - x_t) ** 2).sum() + (v.double() * b).sum()
+    E, nu, ys, pv = t(E0), t(nu0), t(ys0), t(vel0.tolist())
+    x, v, F = adjoint.rollout(s, dt, K5, v0=v0, E=E, nu=nu, yield_stress=ys, checkpoint_every=every, plate=hp,
+                              plate_velocity=pv)
+    L = ((x.double() - x_t) ** 2).sum() + ((F - F_tt) ** 2).sum() + (v.double() * b).sum()
     L.backward()
-    g = {"E": float(E.grad), "nu": float(nu.grad), "ys": float(ys.grad)}
+    g = {"E": float(E.grad), "nu": float(nu.grad), "ys": float(ys.grad), "plate_vz": float(pv.grad[2])}
     xt = x_t.cpu().numpy()
     bn = b.cpu().numpy()
 
-    def loss64(E_, nu_, ys_, dv=None):
+    def loss64(E_, nu_, ys_, dv=None, vel=vel0):
         o = OracleSolver.from_state(st, 48, 0.3, precision=64, threads=16)
         o.a["mu"][:] = E_ / (2.0 * (1.0 + nu_))
         o.a["lam"][:] = E_ * nu_ / ((1.0 + nu_) * (1.0 - 2.0 * nu_))
         o.a["yield_stress"][:] = ys_
+        o.set_box(hp, velocity=tuple(vel))
         if dv is not None:
             o.a["v"][:] = o.a["v"] + dv
-        o.step(dt, K5)
-        return float(((o.a["x"] - xt) ** 2).sum() + (o.a["v"] * bn).sum())
+        Fs = []
+        for _ in range(nseg):
+            o.reset_wrench(hp)
+            o.step(dt, every)
+            Fs.append(o.wrench_of(hp, dt * every)["force"])
+        val = float(((o.a["x"] - xt) ** 2).sum() + ((np.array(Fs) - F_t) ** 2).sum() + (o.a["v"] * bn).sum())
+        return val, float(o.cols[o.handles[hp]].velocity[2])
 
-    fd = {"E": (loss64(E0 * (1 + H), nu0, ys0) - loss64(E0 * (1 - H), nu0, ys0)) / (2 * H * E0),
-          "nu": (loss64(E0, nu0 * (1 + H), ys0) - loss64(E0, nu0 * (1 - H), ys0)) / (2 * H * nu0),
-          "ys": (loss64(E0, nu0, ys0 * (1 + H)) - loss64(E0, nu0, ys0 * (1 - H))) / (2 * H * ys0)}
+    fd = {"E": (loss64(E0 * (1 + H), nu0, ys0)[0] - loss64(E0 * (1 - H), nu0, ys0)[0]) / (2 * H * E0),
+          "nu": (loss64(E0, nu0 * (1 + H), ys0)[0] - loss64(E0, nu0 * (1 - H), ys0)[0]) / (2 * H * nu0),
+          "ys": (loss64(E0, nu0, ys0 * (1 + H))[0] - loss64(E0, nu0, ys0 * (1 - H))[0]) / (2 * H * ys0)}
+    e = np.array([0.0, 0.0, H * abs(vel0[2])])
+    (lp, vp), (lm, vm) = loss64(E0, nu0, ys0, vel=vel0 + e), loss64(E0, nu0, ys0, vel=vel0 - e)
+    fd["plate_vz"] = (lp - lm) / (vp - vm)
     d = np.random.default_rng(12).standard_normal((n, 3))
     d /= np.linalg.norm(d)
-    fd["v0"] = (loss64(E0, nu0, ys0, H * d) - loss64(E0, nu0, ys0, -H * d)) / (2 * H)
+    fd["v0"] = (loss64(E0, nu0, ys0, H * d)[0] - loss64(E0, nu0, ys0, -H * d)[0]) / (2 * H)
     g["v0"] = float((v0.grad.double().cpu().numpy() * d).sum())
+    assert all(fd[k] != 0.0 for k in fd), f"a parameter does not move the loss: {fd}"
     errs = {k: abs(g[k] - fd[k]) / abs(fd[k]) for k in fd}
     print("identification scene, 400 substeps:", {k: (g[k], fd[k], f"{errs[k]:.2e}") for k in fd})
     bad = {k: e for k, e in errs.items() if not e <= TOL}
     assert not bad, f"identification scene: relative gradient errors {bad} exceed {TOL}"
+
+
+def _plate_handle(s):
+    """The handle of the scene's add_box plate."""
+    from mpm_engine_gb300 import _abi
+    for h, i in enumerate(s._handles):
+        if i is not None and s._cols[i].kind == _abi.COLLIDER_BOX:
+            return h
+    raise AssertionError("no plate")
+
+
+@pytest.mark.parametrize("key", ["jelly", "metal_hardening"])
+def test_plate_trajectory_and_force_trace_gradients(cuda, key):
+    """Collider trajectories: a blob pressed by a descending plate (a kinematic
+    cuboid) over K substeps in segments of 2. The loss adds a seeded projection of
+    the plate's reaction-force trace (one force per segment, as tool_force reads
+    it) to the particle terms; its gradient with respect to the plate's velocity,
+    E and nu is checked against central differences of the float64 oracle."""
+    import torch
+    from mpm_engine_gb300 import adjoint
+    from oracle.oracle import OracleSolver
+    from test_gpu_adjoint import EVERY, _weights
+    c = Case(key, plate=True)
+    s = c.s
+    h = _plate_handle(s)
+    nseg = (K + EVERY - 1) // EVERY
+    wf = torch.from_numpy(np.random.default_rng(21).standard_normal((nseg, 3))).to(c.dev)
+    vel0 = np.array(s._cols[s._col(h)].velocity[:], np.float64)
+    dev = c.dev
+    t = lambda x: torch.tensor(x, device=dev, dtype=torch.float32, requires_grad=True)  # noqa: E731
+    adjoint._restore(s, c.snap)
+    pv, E, nu = t(vel0.tolist()), t(c.E), t(c.nu)
+    x, v, F = adjoint.rollout(s, c.dt, K, E=E, nu=nu, checkpoint_every=EVERY, plate=h, plate_velocity=pv)
+    assert F.shape == (nseg, 3) and float(F.abs().max()) > 0.0
+    L = (x.double() * c.a).sum() + (v.double() * c.b).sum() + (F * wf).sum()
+    L.backward()
+    g = {"E": float(E.grad), "nu": float(nu.grad)}
+    g.update({f"plate_v{d}": float(pv.grad[d]) for d in range(3)})
+    a, b = _weights()
+    wfn = wf.cpu().numpy()
+    hh = {"E": H * c.E, "nu": H * c.nu, "plate_v": H * max(1.0, float(np.abs(vel0).max()))}
+
+    def loss64(E_, nu_, vel):
+        o = OracleSolver.from_state(c.state, NG, 0.4, precision=64, threads=8)
+        o.a["mu"][:] = E_ / (2.0 * (1.0 + nu_))
+        o.a["lam"][:] = E_ * nu_ / ((1.0 + nu_) * (1.0 - 2.0 * nu_))
+        o.set_box(h, velocity=tuple(vel))
+        vel_used = np.array(o.cols[o.handles[h]].velocity[:], np.float64)   # the record holds float32
+        Fs = []
+        left = K
+        while left > 0:
+            k = min(EVERY, left)
+            o.reset_wrench(h)
+            o.step(c.dt, k)
+            Fs.append(o.wrench_of(h, c.dt * k)["force"])
+            left -= k
+        val = float((o.a["x"] * a).sum() + (o.a["v"] * b).sum() + (np.array(Fs) * wfn).sum())
+        return val, vel_used
+
+    fd = {"E": (loss64(c.E + hh["E"], c.nu, vel0)[0] - loss64(c.E - hh["E"], c.nu, vel0)[0]) / (2 * hh["E"]),
+          "nu": (loss64(c.E, c.nu + hh["nu"], vel0)[0] - loss64(c.E, c.nu - hh["nu"], vel0)[0]) / (2 * hh["nu"])}
+    for d in range(3):
+        e = np.zeros(3)
+        e[d] = hh["plate_v"]
+        (lp, vp), (lm, vm) = loss64(c.E, c.nu, vel0 + e), loss64(c.E, c.nu, vel0 - e)
+        fd[f"plate_v{d}"] = (lp - lm) / (vp[d] - vm[d])
+    errs = {k: abs(g[k] - fd[k]) / max(abs(fd[k]), 1e-12) for k in fd}
+    print(key, "plate:", {k: (g[k], fd[k], f"{errs[k]:.2e}") for k in fd})
+    bad = {k: e for k, e in errs.items() if not e <= TOL}
+    assert not bad, f"{key} with plate: relative gradient errors {bad} exceed {TOL}"

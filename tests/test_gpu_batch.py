@@ -92,3 +92,111 @@ def test_batch_capture_failure_falls_back_to_live_launches(cuda):
     assert bb.lib.gbmpm_batch_graph_state(bb.h) == 1
     for sa, sb in zip(a, b):
         np.testing.assert_allclose(sa.x(), sb.x(), rtol=1e-5, atol=1e-6)
+
+
+SHAPES = [(1, 64, 2, 2), (1, 64, 3, 2), (1, 128, 2, 2), (1, 128, 3, 1), (1, 256, 2, 4), (1, 256, 3, 2)]
+
+
+@pytest.mark.parametrize("tuning", SHAPES)
+def test_single_launch_shapes_match_oracle(cuda, oracle_lib, tuning):
+    """The single-launch schedule: every particle pass and every grid pass is one
+    launch over all four scenes (different grids, particle counts and laws), each CTA
+    finding its scene and tile in the batch's tables. Every compiled launch shape
+    (particles per CTA, resident CTAs per SM, grid CTAs per SM) keeps every scene
+    within the parity bound of the oracle (1e-5 per substep, composed)."""
+    from mpm_engine_gb300 import BatchSolver, Solver
+    from test_gpu_parity import assert_close
+    scenes = _scenes(Solver)
+    oracles = [oracle_lib.OracleSolver.from_state(s.export_state(), s.grid.n_grid, s.grid.grid_lim) for s in scenes]
+    b = BatchSolver(scenes).set_tuning(*tuning)
+    for _ in range(2):
+        b.step(2.0e-4, 5)
+        for o in oracles:
+            o.step(2.0e-4, 5)
+    tun = b.tuning
+    assert tun["last_graph_single_launch"] and tun["tile_threads"] == tuning[1]
+    for s, o in zip(scenes, oracles):
+        assert_close(s, o, 10 * 1e-5, f"single-launch batch {tuning}")
+
+
+def test_single_launch_equals_branch_schedule_and_counts_launches(cuda):
+    """The same scenes under the single-launch schedule and under one graph branch
+    per scene agree to float-atomic rounding; the single-launch tick issues two
+    launches per substep for all scenes instead of two per scene."""
+    from mpm_engine_gb300 import BatchSolver, Solver
+    a, c = _scenes(Solver), _scenes(Solver)
+    ba = BatchSolver(a).set_tuning(single_launch=True)
+    bc = BatchSolver(c).set_tuning(single_launch=False)
+    for _ in range(3):
+        ba.step(2.0e-4, 6)
+        bc.step(2.0e-4, 6)
+    assert ba.tuning["last_graph_single_launch"] and not bc.tuning["last_graph_single_launch"]
+    for sa, sc in zip(a, c):
+        assert np.abs(sa.x() - sc.x()).max() <= 18e-5 * np.abs(sc.x()).max()
+        assert np.abs(sa.v() - sc.v()).max() <= 18e-5 * np.abs(sc.v()).max()
+    n0, m0 = ba.launch_count(), bc.launch_count()
+    ba.step(2.0e-4, 6)
+    bc.step(2.0e-4, 6)
+    single, branch = ba.launch_count() - n0, bc.launch_count() - m0
+    # both sort and scatter each scene's working set; the substeps' 2 x 6 passes and
+    # the closing G2P are issued once instead of once per scene
+    assert branch - single == (len(a) - 1) * (2 * 6 + 1), (single, branch)
+
+
+def test_batch_with_modifiers_takes_the_branch_schedule(cuda):
+    """A scene with particle modifiers adds launches between the passes, so the batch
+    falls back to one branch per scene and still advances every scene as it would
+    alone."""
+    from mpm_engine_gb300 import BatchSolver, Solver
+    alone, batched = _scenes(Solver), _scenes(Solver)
+    for group in (alone, batched):
+        group[0].add_impulse_on_particles((0.0, 0.0, 1.0e-4), 2.0e-4, point=(0.1, 0.1, 0.1), size=(0.2, 0.2, 0.2))
+    b = BatchSolver(batched)
+    for _ in range(2):
+        for s in alone:
+            s.step(2.0e-4, 5)
+        b.step(2.0e-4, 5)
+    assert not b.tuning["last_graph_single_launch"]
+    for a, s in zip(alone, batched):
+        assert np.abs(s.x() - a.x()).max() <= 10e-5 * np.abs(a.x()).max()
+
+
+def test_autotune_keeps_state_picks_a_candidate_and_caches(cuda, tmp_path, monkeypatch):
+    """The autotuner times each candidate launch shape on the batch's own scenes,
+    restores the scenes to their state before the search, keeps the fastest and
+    caches it: a second batch of the same kind reads the choice from the cache."""
+    from mpm_engine_gb300 import BatchSolver, Solver, autotune
+    monkeypatch.setenv("GBMPM_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    monkeypatch.setattr(autotune, "_memory", {})
+    scenes, ref = _scenes(Solver), _scenes(Solver)
+    x0 = [s.x().copy() for s in scenes]
+    b = BatchSolver(scenes)
+    cands = [(1, 128, 3, 2), (1, 64, 2, 2), (0, 128, 3, 2)]
+    res = autotune.tune_batch(b, 2.0e-4, 5, ticks=1, candidates=cands)
+    assert not res["cached"] and tuple(res["tuning"]) in cands and len(res["ms_per_tick"]) == 3
+    for s, x in zip(scenes, x0):
+        np.testing.assert_array_equal(s.x(), x)
+    t = b.tuning
+    assert (int(t["single_launch"]), t["tile_threads"], t["tile_occ"], t["grid_ctas_per_sm"]) == tuple(res["tuning"])
+    # the tuned batch steps as an untuned one does, to rounding
+    rb = BatchSolver(ref)
+    b.step(2.0e-4, 5)
+    rb.step(2.0e-4, 5)
+    for s, r in zip(scenes, ref):
+        assert np.abs(s.x() - r.x()).max() <= 5e-5 * np.abs(r.x()).max()
+    assert (tmp_path / "tune.json").exists()
+    monkeypatch.setattr(autotune, "_memory", {})
+    again = autotune.tune_batch(BatchSolver(_scenes(Solver)), 2.0e-4, 5, ticks=1, candidates=cands)
+    assert again["cached"] and again["tuning"] == res["tuning"]
+
+
+def test_solver_autotune(cuda, tmp_path, monkeypatch):
+    from mpm_engine_gb300 import Solver, autotune
+    monkeypatch.setenv("GBMPM_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    monkeypatch.setattr(autotune, "_memory", {})
+    s = _scenes(Solver)[0]
+    x0 = s.x().copy()
+    res = s.autotune(2.0e-4, 5, ticks=1)
+    assert tuple(res["tuning"]) in autotune.SOLVER_CANDIDATES
+    np.testing.assert_array_equal(s.x(), x0)
+    assert autotune.solver_tuning(s)["tile_occ"] == res["tuning"][0]

@@ -79,7 +79,18 @@ def test_pour_full_size_1000_substeps(cuda, oracle_lib, material):
     sides under the same tilting cup commands (the frame boundaries fall where the
     benchmark's do), compared at the end: x, v, C and F within 1e-3 relative. Both
     the reference honey and the Herschel-Bulkley fluid (yield stress 50 Pa,
-    consistency 20 Pa s^n, n = 0.6, density 1400). Mass is unchanged on both sides."""
+    consistency 20 Pa s^n, n = 0.6, density 1400). Mass is unchanged on both sides.
+
+    A second oracle run from the same state, whose multithreaded deposits add in
+    another order, measures the restatement's own spread over the 1,000 substeps.
+    The Herschel-Bulkley fluid's unyielded regions are stiff (the regularised
+    viscosity tau_y / 0.02 is far above the explicit step's limit there), and the
+    sign of their shear rate flips with rounding, so their velocities and affine
+    fields are chaotic at the level of tau_y dt / (rho dx) ~ 4e-4 m/s: two oracle runs
+    differ there by several 1e-3 of the velocity scale. For such a field the bound
+    is twice the oracle's own spread instead of 1e-3 (GPU and oracle are two
+    rounding-perturbed runs of the same map, as the two oracle runs are); positions
+    and F are held to 1e-3 outright."""
     from mpm_engine_gb300 import newtonian
     mat = None
     if material == "herschel_bulkley":
@@ -109,14 +120,17 @@ def test_pour_full_size_1000_substeps(cuda, oracle_lib, material):
         o2.step(dt, k)
         left -= k
         frame += 1
-    from test_gpu_parity import FLOOR, c_floor, fields_oracle
+    from test_gpu_parity import FLOOR, c_floor, fields_gpu, fields_oracle
     f1, f2 = fields_oracle(o), fields_oracle(o2)
     floors = dict(FLOOR, C=c_floor(o))
     spread = {k: rel_err(f2[k], f1[k], floors[k]) for k in f1}
     print(f"{material} pour 192^3, 1000 substeps: oracle against itself (deposit order) {spread}")
-    errs = assert_close(s, o, 1e-3, f"{material} pour at 192^3 after 1000 substeps "
-                                    f"(oracle against itself: {spread})")
+    fg = fields_gpu(s)
+    errs = {k: rel_err(fg[k], f1[k], floors[k]) for k in f1}
     print(f"{material} pour 192^3, 1000 substeps: relative errors {errs}")
+    bound = {k: max(1e-3, 2.0 * spread[k]) if k in ("v", "C") else 1e-3 for k in f1}
+    bad = {k: (errs[k], bound[k]) for k in f1 if not errs[k] <= bound[k]}
+    assert not bad, f"{material} pour after 1000 substeps: (error, bound) {bad}; oracle spread {spread}"
     np.testing.assert_array_equal(s._t["mass"].cpu().numpy(), o.a["mass"])
 
 
