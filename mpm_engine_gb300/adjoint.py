@@ -105,16 +105,18 @@ def _backward(s, dt, ckpts, xb, vb, plate=None, force_bar=None):
     if col is not None:
         g["collider_velocity"] = torch.zeros(ncol, 3, **f)
         rec.collider_velocity = g["collider_velocity"].data_ptr()
+        # one buffer for every segment, so the engine's captured segment graph (keyed
+        # on the adjoint arrays) is reused; each segment rewrites it in stream order
+        fb = torch.zeros(max(k for _, k in ckpts), ncol, 3, **f)
+        rec.collider_force = fb.data_ptr()
     for j in reversed(range(len(ckpts))):
         snap, k = ckpts[j]
         _restore(s, snap)
         if col is not None:
             # the segment's force is sum_substeps sum_nodes m (v_free - v_box) / (dt k)
-            # stream-ordered: the segment's kernels read fb before a later allocation reuses it
-            fb = torch.zeros(k, ncol, 3, **f)
+            fb.zero_()
             if force_bar is not None:
-                fb[:, col, :] = force_bar[j].to(**f) / (dt * k)
-            rec.collider_force = fb.data_ptr()
+                fb[:k, col, :] = force_bar[j].to(**f) / (dt * k)
         t = C.c_double(s._time)
         _abi.check(lib.gbmpm_adjoint_segment(h, C.byref(t), float(dt), int(k), C.byref(rec), s._stream()),
                    "gbmpm_adjoint_segment")

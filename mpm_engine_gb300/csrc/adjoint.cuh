@@ -1314,46 +1314,28 @@ int adjoint_supported(gbmpm_engine *e) {
     return GBMPM_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t substeps, const gbmpm_adj_grads *gr,
-                          void *stream) {
-    int rc = check_ready(e);
-    if (rc) return rc;
-    if (!time || !gr || substeps < 1 || substeps > GBMPM_MAX_SUBSTEPS || !(dt > 0.0))
-        return fail(GBMPM_ERR_ARG, "bad adjoint arguments");
-    if (!gr->x || !gr->v || !gr->C || !gr->F_trial || !gr->yield_stress || !gr->mu || !gr->lam || !gr->L ||
-        !gr->viscosity || !gr->Jp)
-        return fail(GBMPM_ERR_ARG, "every adjoint array is required");
-    if (!e->P.L) return fail(GBMPM_ERR_ARG, "the adjoint needs particles.L");
-    if ((rc = adjoint_supported(e))) return rc;
-    cudaStream_t s = (cudaStream_t)stream;
+// Records one adjoint segment on stream s: the forward replay that keeps every
+// substep's starting state, then the reverse substeps. Returns the first error of a
+// copy or memset call (kernel launches report through cudaGetLastError).
+cudaError_t record_adjoint_segment(gbmpm_engine *e, float dtf, int substeps, const gbmpm_adj_grads *gr,
+                                   cudaStream_t s) {
     const gbmpm_particles &P = e->P;
     const int n = P.n, ng = e->G.n_grid, nc = (int)e->cols.size();
     const size_t nn = (size_t)ng * ng * ng;
-    // segment storage: the state at the start of every substep
-    const size_t per = (size_t)37 * n;   // x 3, v 3, C 9, F_trial 9, L 9, yield 1, mu 1, lam 1, Jp 1
-    GB_CUDA(e->adj_states.ensure(per * substeps));
-    GB_CUDA(e->adj_scratch.ensure((size_t)27 * n));
-    GB_CUDA(e->adj_grid.ensure(4 * nn));   // four float4 grids
-    const float dtf = (float)dt;
-    // forward replay on the split schedule: one pose table for the whole segment
-    // (the adjoint kernels read the same table), no host synchronization per substep
-    bool reorder = false;
-    if ((rc = prepare_tick(e, time, dt, substeps, 0, s, reorder))) return rc;
+    const size_t per = (size_t)37 * n;
+    cudaError_t first = cudaSuccess;
+    auto keep = [&](cudaError_t err) { if (first == cudaSuccess) first = err; };
     for (int i = 0; i < substeps; ++i) {
         float *st = e->adj_states.ptr + per * i;
-        GB_CUDA(cudaMemcpyAsync(st, P.x, 3 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-        GB_CUDA(cudaMemcpyAsync(st + 3 * (size_t)n, P.v, 3 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-        GB_CUDA(cudaMemcpyAsync(st + 6 * (size_t)n, P.C, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-        GB_CUDA(cudaMemcpyAsync(st + 15 * (size_t)n, P.F_trial, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-        GB_CUDA(cudaMemcpyAsync(st + 24 * (size_t)n, P.L, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-        GB_CUDA(cudaMemcpyAsync(st + 33 * (size_t)n, P.yield_stress, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-        GB_CUDA(cudaMemcpyAsync(st + 34 * (size_t)n, P.mu, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-        GB_CUDA(cudaMemcpyAsync(st + 35 * (size_t)n, P.lam, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-        GB_CUDA(cudaMemcpyAsync(st + 36 * (size_t)n, P.Jp, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        keep(cudaMemcpyAsync(st, P.x, 3 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        keep(cudaMemcpyAsync(st + 3 * (size_t)n, P.v, 3 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        keep(cudaMemcpyAsync(st + 6 * (size_t)n, P.C, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        keep(cudaMemcpyAsync(st + 15 * (size_t)n, P.F_trial, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        keep(cudaMemcpyAsync(st + 24 * (size_t)n, P.L, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        keep(cudaMemcpyAsync(st + 33 * (size_t)n, P.yield_stress, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        keep(cudaMemcpyAsync(st + 34 * (size_t)n, P.mu, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        keep(cudaMemcpyAsync(st + 35 * (size_t)n, P.lam, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        keep(cudaMemcpyAsync(st + 36 * (size_t)n, P.Jp, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         record_tick(e, dtf, 1, false, false, s, false, 0.0, 0.0, i);
     }
     float4 *grid = e->adj_grid.ptr;
@@ -1386,7 +1368,7 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
         Ps.x = const_cast<float *>(a.x); Ps.v = const_cast<float *>(a.v); Ps.C = const_cast<float *>(a.C);
         PK k = make_pk(e, Ps, dtf, 0);
         k.cdf_on = 0;
-        GB_CUDA(cudaMemsetAsync(grid, 0, 4 * nn * sizeof(float4), s));
+        keep(cudaMemsetAsync(grid, 0, 4 * nn * sizeof(float4), s));
         k_adj_stress_fwd<<<pb, 128, 0, s>>>(a);
         k_adj_p2g_fwd<<<pb, 128, 0, s>>>(a, k);
         k_adj_grid_fwd<<<gb, 256, 0, s>>>(a);
@@ -1395,6 +1377,82 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
         k_adj_p2g_bwd<<<pb, 128, 0, s>>>(a);
         e->launches += 6;
     }
+    return first;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t substeps, const gbmpm_adj_grads *gr,
+                          void *stream) {
+    int rc = check_ready(e);
+    if (rc) return rc;
+    if (!time || !gr || substeps < 1 || substeps > GBMPM_MAX_SUBSTEPS || !(dt > 0.0))
+        return fail(GBMPM_ERR_ARG, "bad adjoint arguments");
+    if (!gr->x || !gr->v || !gr->C || !gr->F_trial || !gr->yield_stress || !gr->mu || !gr->lam || !gr->L ||
+        !gr->viscosity || !gr->Jp)
+        return fail(GBMPM_ERR_ARG, "every adjoint array is required");
+    if (!e->P.L) return fail(GBMPM_ERR_ARG, "the adjoint needs particles.L");
+    if ((rc = adjoint_supported(e))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const gbmpm_particles &P = e->P;
+    const int n = P.n, ng = e->G.n_grid, nc = (int)e->cols.size();
+    const size_t nn = (size_t)ng * ng * ng;
+    // segment storage: the state at the start of every substep
+    const size_t per = (size_t)37 * n;   // x 3, v 3, C 9, F_trial 9, L 9, yield 1, mu 1, lam 1, Jp 1
+    GB_CUDA(e->adj_states.ensure(per * substeps));
+    GB_CUDA(e->adj_scratch.ensure((size_t)27 * n));
+    GB_CUDA(e->adj_grid.ensure(4 * nn));   // four float4 grids
+    const float dtf = (float)dt;
+    // forward replay on the split schedule: one pose table for the whole segment
+    // (the adjoint kernels read the same table), no host synchronization per substep.
+    // The tables are uploaded here, outside the segment's graph, which reads them.
+    bool reorder = false;
+    uint64_t version0 = e->version;
+    if ((rc = prepare_tick(e, time, dt, substeps, 0, s, reorder))) return rc;
+    const bool same = e->adj_graph && e->adj_g_substeps == substeps && e->adj_g_dt == dt &&
+                      e->adj_g_version == e->version && version0 == e->version &&
+                      std::memcmp(&e->adj_g_grads, gr, sizeof *gr) == 0;
+    if (same) {
+        GB_CUDA(cudaGraphLaunch(e->adj_graph, s));
+        e->launches += e->adj_graph_launches;
+        return GBMPM_OK;
+    }
+    if (e->adj_graph) { cudaGraphExecDestroy(e->adj_graph); e->adj_graph = nullptr; }
+    if (!e->graph_failed) {
+        cudaStream_t cap;
+        GB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaError_t be = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (be != cudaSuccess) {
+            cudaStreamDestroy(cap);
+            return fail(GBMPM_ERR_CUDA, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(be));
+        }
+        const int64_t before = e->launches;
+        cudaError_t ce = record_adjoint_segment(e, dtf, substeps, gr, cap);
+        e->adj_graph_launches = e->launches - before;
+        e->launches = before;
+        cudaGraph_t graph = nullptr;
+        cudaError_t ee = cudaStreamEndCapture(cap, &graph);
+        cudaStreamDestroy(cap);
+        if (ce == cudaSuccess) ce = ee;
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&e->adj_graph, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (ce == cudaSuccess) {
+            e->adj_g_substeps = substeps;
+            e->adj_g_dt = dt;
+            e->adj_g_version = e->version;
+            e->adj_g_grads = *gr;
+            GB_CUDA(cudaGraphLaunch(e->adj_graph, s));
+            e->launches += e->adj_graph_launches;
+            return GBMPM_OK;
+        }
+        // as a failed tick capture: launched live from here on
+        e->adj_graph = nullptr;
+        e->graph_failed = true;
+        (void)cudaGetLastError();
+    }
+    GB_CUDA(record_adjoint_segment(e, dtf, substeps, gr, s));
     GB_CUDA(cudaGetLastError());
     return GBMPM_OK;
 }

@@ -180,6 +180,15 @@ struct gbmpm_engine {
     // adjoint segment storage and scratch (allocated by the first adjoint call)
     DevBuf<float> adj_states, adj_scratch;
     DevBuf<float4> adj_grid;
+    // the launches of one adjoint segment, captured once and replayed while the
+    // segment's shape and buffers stay the same (key: substeps, dt, adjoint arrays,
+    // engine version)
+    cudaGraphExec_t adj_graph = nullptr;
+    int adj_g_substeps = -1;
+    double adj_g_dt = 0.0;
+    gbmpm_adj_grads adj_g_grads{};
+    uint64_t adj_g_version = 0;
+    int64_t adj_graph_launches = 0;
     // rigid bodies and particle modifiers
     int n_bodies = 0;
     std::vector<gbmpm_rigid_surface> rsurf;
@@ -838,6 +847,7 @@ int gbmpm_engine_create(gbmpm_engine **out) {
 }
 
 void gbmpm_engine_destroy(gbmpm_engine *e) {
+    if (e && e->adj_graph) { cudaGraphExecDestroy(e->adj_graph); e->adj_graph = nullptr; }
     if (!e) return;
     cudaDeviceSynchronize();
     if (e->graph) cudaGraphExecDestroy(e->graph);
