@@ -183,9 +183,25 @@ __device__ __forceinline__ void mmT(const float *a, const float *b, float *c) {
         for (int j = 0; j < 3; ++j)
             c[3 * i + j] = a[3 * i] * b[3 * j] + a[3 * i + 1] * b[3 * j + 1] + a[3 * i + 2] * b[3 * j + 2];
 }
+// det(m) as row0 . (row1 x row2), every product and sum rounded on its own in
+// that order (the reference's determinant, and the oracle's): the fluid laws feed
+// J into a stiff equation of state, K (J^-1.1 - 1) with K ~ 1e6 Pa, where one ulp of
+// J is 0.1 Pa, so J is formed exactly as the restatement forms it
 __device__ __forceinline__ float det3(const float *m) {
-    return m[0] * (m[4] * m[8] - m[5] * m[7]) + m[1] * (m[5] * m[6] - m[3] * m[8]) +
-           m[2] * (m[3] * m[7] - m[4] * m[6]);
+    const float c0 = __fsub_rn(__fmul_rn(m[4], m[8]), __fmul_rn(m[5], m[7]));
+    const float c1 = __fsub_rn(__fmul_rn(m[5], m[6]), __fmul_rn(m[3], m[8]));
+    const float c2 = __fsub_rn(__fmul_rn(m[3], m[7]), __fmul_rn(m[4], m[6]));
+    return __fadd_rn(__fadd_rn(__fmul_rn(m[0], c0), __fmul_rn(m[1], c1)), __fmul_rn(m[2], c2));
+}
+// c = a b with each product and sum rounded on its own, k ascending (the reference's
+// mat33 product): used for F_trial = (I + dt L) F, whose determinant is J
+__device__ __forceinline__ void mm_rn(const float *a, const float *b, float *c) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            c[3 * i + j] = __fadd_rn(__fadd_rn(__fmul_rn(a[3 * i], b[j]), __fmul_rn(a[3 * i + 1], b[3 + j])),
+                                     __fmul_rn(a[3 * i + 2], b[6 + j]));
 }
 // U diag(d) V^T
 __device__ __forceinline__ void udvt(const float *U, float d0, float d1, float d2, const float *V, float *out) {

@@ -60,16 +60,22 @@ __device__ __forceinline__ float mu_of_i(float Im, float mu_s, float dmu, float 
     return table_lerp(tab, tn, smin, smax, logf(fmaxf(Im, 1e-12f)) * 0.43429448190325176f);
 }
 
-// the 48-step bisection on g(gdp) = tau_bar - G dt gdp - mu(I) p (mpm_utils.py:300-312)
+// the 48-step bisection on g(gdp) = tau_bar - G dt gdp - mu(I) p (mpm_utils.py:300-312).
+// Once the midpoint rounds to one end of the bracket, the step it takes leaves the
+// bracket where every later step leaves it too (the midpoint repeats, so does the
+// comparison), and the loop stops there: the result is bit for bit that of all 48
+// steps, which fp32 exhausts after about 24 + log2(hi / root) of them.
 template <bool TAB>
 __device__ __forceinline__ float mu_i_bisect(float tbK, float G, float dt, float pK, float Ic, float mu_s, float dmu,
                                              float I0, const float *tab, int tn, float smin, float smax) {
     float lo = 0.0f, hi = tbK / (G * dt);
     for (int it = 0; it < 48; ++it) {
-        float mid = 0.5f * (lo + hi);
+        const float mid = 0.5f * (lo + hi);
+        const bool at_end = mid == lo || mid == hi;
         float mu_mid = mu_of_i<TAB>(mid * Ic, mu_s, dmu, I0, tab, tn, smin, smax);
         float g = tbK - G * dt * mid - mu_mid * pK;
         if (g > 0.0f) lo = mid; else hi = mid;
+        if (at_end) break;
     }
     return 0.5f * (lo + hi);
 }

@@ -41,12 +41,30 @@ __device__ __forceinline__ bool stencil_ok(const Stencil &s, int ng, int periodi
 
 __device__ __forceinline__ int wrap(int i, int n) { return ((i % n) + n) % n; }
 
-__device__ __forceinline__ void mark_block(const PK &k, int bx, int by, int bz) {
-    int b = (bx * k.bd + by) * k.bd + bz;
+__device__ __forceinline__ void mark_block_id(const PK &k, int b) {
     if (k.blk_flag[b] == 0 && atomicExch(&k.blk_flag[b], 1) == 0) {
         int i = atomicAdd(k.blk_count, 1);
         k.blk_list[i] = b;
     }
+}
+__device__ __forceinline__ void mark_block(const PK &k, int bx, int by, int bz) {
+    mark_block_id(k, (bx * k.bd + by) * k.bd + bz);
+}
+
+// The tiled scatter marks its 4^3 blocks in a per-CTA set in shared memory (open
+// addressing over kMarkSlots slots) and checks the global flags once per distinct
+// block at the end of the CTA: the scatter loop then never waits on a global load.
+// A full set marks directly.
+constexpr int kMarkSlots = 64;
+__device__ __forceinline__ void defer_mark(const PK &k, int *s_blk, int bx, int by, int bz) {
+    const int b = (bx * k.bd + by) * k.bd + bz;
+    unsigned h = ((unsigned)b * 2654435761u) >> 26;
+    for (int i = 0; i < kMarkSlots; ++i) {
+        const int old = atomicCAS(&s_blk[h], -1, b);
+        if (old == -1 || old == b) return;
+        h = (h + 1) & (kMarkSlots - 1);
+    }
+    mark_block_id(k, b);
 }
 
 // ---- building blocks shared by the direct and the tiled particle kernels ----
@@ -148,7 +166,7 @@ __device__ __forceinline__ void g2p_finish(const PK &k, int p, float *x, const f
                                            const float *Fpre = nullptr) {
     float xn[3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) xn[a] = x[a] + k.dt * v[a];
+    for (int a = 0; a < 3; ++a) xn[a] = __fadd_rn(x[a], __fmul_rn(v[a], k.dt));   // x + v dt, as the reference rounds it
     if (k.periodic_x) {
         float lx = (float)k.ng * k.dx;
         if (xn[0] < 0.0f) xn[0] += lx;
@@ -163,9 +181,14 @@ __device__ __forceinline__ void g2p_finish(const PK &k, int p, float *x, const f
     } else {
         fld_load<SOA, 9>(k.F, k.n, p, Fo);
     }
+    // F_trial = (I + dt L) F with the reference's roundings (L dt, then 1 +, then the
+    // product): its determinant drives the fluids' stiff pressure
 #pragma unroll
-    for (int i = 0; i < 9; ++i) A[i] = ((i % 4 == 0) ? 1.0f : 0.0f) + L[i] * k.dt;
-    mm(A, Fo, Ft);
+    for (int i = 0; i < 9; ++i) {
+        const float ld = __fmul_rn(L[i], k.dt);
+        A[i] = (i % 4 == 0) ? __fadd_rn(1.0f, ld) : ld;
+    }
+    mm_rn(A, Fo, Ft);
     if (k.update_cov && k.cov) {
         float c6[6];
         fld_load<SOA, 6>(k.cov, k.n, p, c6);
@@ -633,10 +656,10 @@ __global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) 
 // body runs best with fewer, wider CTAs, 256 (three per SM).
 constexpr int kTileThreads = 128;
 constexpr int kTileThreadsCdf = 256;
-constexpr int kRec = 60;                  // floats per particle scatter record (15 float4)
-// record stride in shared memory: 60 floats = 240 B, so the 16-byte stores of eight
-// consecutive lanes land on disjoint bank groups (word offsets 60 t mod 32 step by 28)
-constexpr int kRecStride = 60;
+constexpr int kRec = 40;                  // floats per particle scatter record (10 float4)
+// record stride in shared memory: 44 floats = 176 B, so the 16-byte stores of eight
+// consecutive lanes land on disjoint bank groups (a 160 B stride pairs them up)
+constexpr int kRecStride = 44;
 // shared-memory shape of a tile of TH particles
 template <int TH>
 struct TileShape {
@@ -717,6 +740,7 @@ __device__ __forceinline__ void particles_tile(const PK &k, int mode, int tile) 
     __shared__ int s_seg[kTileThreads + 1];
     __shared__ int s_wcnt[kTileThreads / 32];
     __shared__ int s_red[kTileThreads / 32][6];
+    __shared__ int s_blk[kMarkSlots];   // distinct blocks this CTA's scatter deposits into
     // F, mass and volume of a gather pass's particle, fetched asynchronously at the
     // start so that their L2 round trip overlaps the tile box, the tile load and the
     // gather (a gather pass starts before its wait: nothing still running writes
@@ -897,15 +921,12 @@ __device__ __forceinline__ void particles_tile(const PK &k, int mode, int tile) 
         fld_store<true, 1>(reinterpret_cast<float *>(k.ptag), k.n, p, &pcf);
     }
     if (CDF) { s_pc[t] = pcs; s_mask[t] = pmask; }
-    // ---- scatter record (kRec floats, 16-byte aligned), laid out for paired loads:
-    // [0..23] what a lane indexes by its node line (i, j), each value duplicated into a
-    // pair: wx[i] at 2i, dwx[i] at 6 + 2i, wy[j] at 12 + 2j, dwy[j] at 18 + 2j;
-    // [24..59] what every lane of a particle reads, as nine float4: (b0, b1, c00, c10),
-    // (c01, c11, c02, c12), (A00, A10, A01, A11), (A02, A12, b2, c20),
-    // (c21, c22, A20, A21), (A22, m, -, -), (wz0, wz0, wz1, wz1), (wz2, wz2, dwz0, dwz0),
-    // (dwz1, dwz1, dwz2, dwz2), with b = m v - m C fx dx the affine momentum base,
-    // c = m C dx (c[a][b] row a) and A = -vol dt/dx stress: the (x, y) rows of b, c and
-    // A sit side by side so the lane forms both components with one paired operation
+    // ---- scatter record (40 floats, 16-byte aligned): [0..11] the x and y weights and
+    // derivatives a lane indexes by its node line (wx[3], wy[3], dwx[3], dwy[3]);
+    // [12..39] what every lane of a particle reads, packed for seven float4 loads:
+    // wz[3], m | dwz[3], b0 | b1, b2, c00, c01 | c02, c10, c11, c12 | c20, c21, c22,
+    // A00 | A01, A02, A10, A11 | A12, A20, A21, A22, with b = m v - m C fx dx the
+    // affine momentum base, c = m C dx and A = -vol dt/dx stress
     if (want) {
         float Cr[9];
 #pragma unroll
@@ -920,33 +941,32 @@ __device__ __forceinline__ void particles_tile(const PK &k, int mode, int tile) 
         }
         const float m = (pf && (mode & PASS_P2G)) ? mpf : k.mass[p];
         const float fs = -((pf && (mode & PASS_P2G)) ? vpf : k.vol[p]) * k.dt * k.inv_dx;
-        float b[3], c[9], A[9];
+        float rec[kRec];
+#pragma unroll
+        for (int o = 0; o < 3; ++o) {
+            rec[o] = s.w[0][o];
+            rec[3 + o] = s.w[1][o];
+            rec[6 + o] = s.dw[0][o];
+            rec[9 + o] = s.dw[1][o];
+            rec[12 + o] = s.w[2][o];
+            rec[16 + o] = s.dw[2][o];
+        }
+        rec[15] = m;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            c[3 * a] = m * Cr[3 * a] * k.dx; c[3 * a + 1] = m * Cr[3 * a + 1] * k.dx; c[3 * a + 2] = m * Cr[3 * a + 2] * k.dx;
-            b[a] = m * v[a] - (c[3 * a] * s.fx[0] + c[3 * a + 1] * s.fx[1] + c[3 * a + 2] * s.fx[2]);
-            A[3 * a] = fs * S[3 * a]; A[3 * a + 1] = fs * S[3 * a + 1]; A[3 * a + 2] = fs * S[3 * a + 2];
+            float c0 = m * Cr[3 * a] * k.dx, c1 = m * Cr[3 * a + 1] * k.dx, c2 = m * Cr[3 * a + 2] * k.dx;
+            rec[19 + a] = m * v[a] - (c0 * s.fx[0] + c1 * s.fx[1] + c2 * s.fx[2]);
+            rec[22 + 3 * a] = c0; rec[23 + 3 * a] = c1; rec[24 + 3 * a] = c2;
+            rec[31 + 3 * a] = fs * S[3 * a]; rec[32 + 3 * a] = fs * S[3 * a + 1]; rec[33 + 3 * a] = fs * S[3 * a + 2];
         }
         float4 *dst = reinterpret_cast<float4 *>(s_mem + t * kRecStride);
-        dst[0] = make_float4(s.w[0][0], s.w[0][0], s.w[0][1], s.w[0][1]);
-        dst[1] = make_float4(s.w[0][2], s.w[0][2], s.dw[0][0], s.dw[0][0]);
-        dst[2] = make_float4(s.dw[0][1], s.dw[0][1], s.dw[0][2], s.dw[0][2]);
-        dst[3] = make_float4(s.w[1][0], s.w[1][0], s.w[1][1], s.w[1][1]);
-        dst[4] = make_float4(s.w[1][2], s.w[1][2], s.dw[1][0], s.dw[1][0]);
-        dst[5] = make_float4(s.dw[1][1], s.dw[1][1], s.dw[1][2], s.dw[1][2]);
-        dst[6] = make_float4(b[0], b[1], c[0], c[3]);
-        dst[7] = make_float4(c[1], c[4], c[2], c[5]);
-        dst[8] = make_float4(A[0], A[3], A[1], A[4]);
-        dst[9] = make_float4(A[2], A[5], b[2], c[6]);
-        dst[10] = make_float4(c[7], c[8], A[6], A[7]);
-        dst[11] = make_float4(A[8], m, 0.0f, 0.0f);
-        dst[12] = make_float4(s.w[2][0], s.w[2][0], s.w[2][1], s.w[2][1]);
-        dst[13] = make_float4(s.w[2][2], s.w[2][2], s.dw[2][0], s.dw[2][0]);
-        dst[14] = make_float4(s.dw[2][1], s.dw[2][1], s.dw[2][2], s.dw[2][2]);
+#pragma unroll
+        for (int q = 0; q < kRec / 4; ++q) dst[q] = make_float4(rec[4 * q], rec[4 * q + 1], rec[4 * q + 2], rec[4 * q + 3]);
         s_key[t] = (s.b[0] << 20) | (s.b[1] << 10) | s.b[2];   // n_grid <= 1024 on this path
     } else {
         s_key[t] = -1 - t;   // a dead slot forms its own, skipped run
     }
+    for (int i = t; i < kMarkSlots; i += kTileThreads) s_blk[i] = -1;
     __syncthreads();
     // ---- runs of equal base node (and CPIC tag): compact the run heads
     const bool head = (t == 0) || (s_key[t] != s_key[t - 1]) || (CDF && s_pc[t] != s_pc[t - 1]);
@@ -967,7 +987,6 @@ __device__ __forceinline__ void particles_tile(const PK &k, int mode, int tile) 
     // run's particles and deposits them itself
     const int g3 = lane / 9, li = (lane % 9) / 3, lj = lane % 3;
     const float fi = (float)li, fj = (float)lj;
-    const float2 fi2 = f2(fi, fi), fj2 = f2(fj, fj);
     for (int sg0 = warp * 3; sg0 < total; sg0 += 3 * (kTileThreads / 32)) {
         const int sg = sg0 + g3;
         int q0 = 0, q1 = 0, key = -1;
@@ -977,45 +996,43 @@ __device__ __forceinline__ void particles_tile(const PK &k, int mode, int tile) 
             key = s_key[q0];
         }
         if (key < 0) q1 = q0;   // dead slot or idle lane: no particles
-        // the line's three nodes: (x, y) momentum pairs, z momentum, mass
-        float2 a0 = f2(0.f, 0.f), a1 = f2(0.f, 0.f), a2 = f2(0.f, 0.f);
-        float az[3] = {0.f, 0.f, 0.f}, am[3] = {0.f, 0.f, 0.f};
+        float acc[3][4];
+#pragma unroll
+        for (int kk = 0; kk < 3; ++kk) acc[kk][0] = acc[kk][1] = acc[kk][2] = acc[kk][3] = 0.f;
 #pragma unroll 1   // unrolling by two measured slower (22.01 against 21.87 ms per pour frame, 56.5 against 54.9 CPIC)
         for (int q = q0; q < q1; ++q) {
             const float *r = s_mem + q * kRecStride;
+            const float wxi = r[li], wyj = r[3 + lj], dwxi = r[6 + li], dwyj = r[9 + lj];
             const float4 *r4 = reinterpret_cast<const float4 *>(r);
-            const float2 wxi = *reinterpret_cast<const float2 *>(r + 2 * li);
-            const float2 dwxi = *reinterpret_cast<const float2 *>(r + 6 + 2 * li);
-            const float2 wyj = *reinterpret_cast<const float2 *>(r + 12 + 2 * lj);
-            const float2 dwyj = *reinterpret_cast<const float2 *>(r + 18 + 2 * lj);
-            const float4 s0 = r4[6], s1 = r4[7], s2 = r4[8], s3 = r4[9], s4 = r4[10], s5 = r4[11];
-            const float4 s6 = r4[12], s7 = r4[13], s8 = r4[14];
-            // u = wx wy, ux = dwx wy, uy = wx dwy, each as a duplicated pair
-            const float2 uu = mul2(wxi, wyj), ux = mul2(dwxi, wyj), uy = mul2(wxi, dwyj);
-            const float u = uu.x;
-            // P = u (b + c0 i + c1 j) + A0 ux + A1 uy, Q = u c2, R = u A2; (x, y) paired
-            float2 Pxy = fma2(f2(s1.x, s1.y), fj2, fma2(f2(s0.z, s0.w), fi2, f2(s0.x, s0.y)));
-            Pxy = fma2(f2(s2.z, s2.w), uy, fma2(f2(s2.x, s2.y), ux, mul2(Pxy, uu)));
-            const float2 Qxy = mul2(f2(s1.z, s1.w), uu), Rxy = mul2(f2(s3.x, s3.y), uu);
-            float Pz = fmaf(s4.x, fj, fmaf(s3.w, fi, s3.z));
-            Pz = fmaf(s4.w, uy.x, fmaf(s4.z, ux.x, u * Pz));
-            const float Qz = u * s4.y, Rz = u * s5.x, um = u * s5.y;
-            const float2 wz0 = f2(s6.x, s6.y), wz1 = f2(s6.z, s6.w), wz2 = f2(s7.x, s7.y);
-            const float2 dz0 = f2(s7.z, s7.w), dz1 = f2(s8.x, s8.y), dz2 = f2(s8.z, s8.w);
-            // node kk of the line: wz[kk] (P + kk Q) + dwz[kk] R, and m wz[kk] u
-            const float2 P1 = add2(Pxy, Qxy), P2 = add2(P1, Qxy);
-            const float P1z = Pz + Qz, P2z = P1z + Qz;
-            a0 = fma2(dz0, Rxy, fma2(wz0, Pxy, a0));
-            a1 = fma2(dz1, Rxy, fma2(wz1, P1, a1));
-            a2 = fma2(dz2, Rxy, fma2(wz2, P2, a2));
-            az[0] = fmaf(dz0.x, Rz, fmaf(wz0.x, Pz, az[0]));
-            az[1] = fmaf(dz1.x, Rz, fmaf(wz1.x, P1z, az[1]));
-            az[2] = fmaf(dz2.x, Rz, fmaf(wz2.x, P2z, az[2]));
-            am[0] = fmaf(wz0.x, um, am[0]);
-            am[1] = fmaf(wz1.x, um, am[1]);
-            am[2] = fmaf(wz2.x, um, am[2]);
+            float inv[28];
+#pragma unroll
+            for (int h = 0; h < 7; ++h) {
+                const float4 f4 = r4[3 + h];
+                inv[4 * h] = f4.x; inv[4 * h + 1] = f4.y; inv[4 * h + 2] = f4.z; inv[4 * h + 3] = f4.w;
+            }
+            // inv[i] = rec[12 + i]
+            const float u = wxi * wyj, ux = dwxi * wyj, uy = wxi * dwyj;
+            const float wz0 = inv[0], wz1 = inv[1], wz2 = inv[2], dz0 = inv[4], dz1 = inv[5], dz2 = inv[6];
+            const float m = inv[3];
+            float P[3], Q[3], R[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                P[a] = u * (inv[7 + a] + inv[10 + 3 * a] * fi + inv[11 + 3 * a] * fj) + inv[19 + 3 * a] * ux +
+                       inv[20 + 3 * a] * uy;
+                Q[a] = u * inv[12 + 3 * a];
+                R[a] = u * inv[21 + 3 * a];
+            }
+            const float um = u * m;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                acc[0][a] += wz0 * P[a] + dz0 * R[a];
+                acc[1][a] += wz1 * (P[a] + Q[a]) + dz1 * R[a];
+                acc[2][a] += wz2 * (P[a] + 2.0f * Q[a]) + dz2 * R[a];
+            }
+            acc[0][3] += wz0 * um;
+            acc[1][3] += wz1 * um;
+            acc[2][3] += wz2 * um;
         }
-        float acc[3][4] = {{a0.x, a0.y, az[0], am[0]}, {a1.x, a1.y, az[1], am[1]}, {a2.x, a2.y, az[2], am[2]}};
         if (q1 > q0) {
             const int bx = key >> 20, by = (key >> 10) & 1023, bz = key & 1023;
             const int gx = bx + li, gy = by + lj;
@@ -1045,12 +1062,18 @@ __device__ __forceinline__ void particles_tile(const PK &k, int mode, int tile) 
                     atomicAdd(k.gmv + ((size_t)gx * k.ng + gy) * k.ng + gz,
                               make_float4(acc[kk][0], acc[kk][1], acc[kk][2], acc[kk][3]));
                     if ((gz >> 2) != marked) {
-                        mark_block(k, gx >> 2, gy >> 2, gz >> 2);
+                        defer_mark(k, s_blk, gx >> 2, gy >> 2, gz >> 2);
                         marked = gz >> 2;
                     }
                 }
             }
         }
+    }
+    // the distinct blocks of this CTA's deposits, each checked against the global flags once
+    __syncthreads();
+    for (int i = t; i < kMarkSlots; i += kTileThreads) {
+        const int b = s_blk[i];
+        if (b >= 0) mark_block_id(k, b);
     }
 }
 

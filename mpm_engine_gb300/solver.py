@@ -1044,8 +1044,13 @@ class Solver:
                     f"velocity/omega, or raise band (and the SDF margin).", RuntimeWarning, stacklevel=3)
 
     def _tick_flags(self) -> int:
+        # Sparse ticks stay on the fused schedule. The reference drops to the split one
+        # in sparse mode (core/solver.py:441-444) because its active-block lists are
+        # rebuilt per phase; here every particle pass marks the blocks it deposits into
+        # and the grid pass visits exactly those, on either schedule, and the two
+        # schedules compute the same substep (fused == split in the oracle, bit for bit).
         flags = 0
-        if self.fused and not self.sparse:
+        if self.fused:
             flags |= _abi.TICK_FUSED
         if self.profile:
             flags |= _abi.TICK_PROFILE
