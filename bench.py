@@ -376,22 +376,32 @@ def adjoint_measure(n_scenes: int = 32, n_particles: int = 50_000, n_grid: int =
     weights = [(torch.randn(s.n_particles, 3, device=device), torch.randn(s.n_particles, 3, device=device))
                for s in scenes]
 
+    split = {}
+
     def run(batched, k):
         for s, st in zip(scenes, starts):
             adjoint._restore(s, st)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        t_fwd = 0.0
         if batched:
             r = adjoint.BatchRollout(scenes, dt, k, every, batched=True)
             r.forward()
+            torch.cuda.synchronize()
+            t_fwd = time.perf_counter() - t0
             r.backward([w[0] for w in weights], [w[1] for w in weights])
         else:
             for s, w in zip(scenes, weights):
+                t1 = time.perf_counter()
                 r = adjoint.BatchRollout([s], dt, k, every, batched=False)
                 r.forward()
+                torch.cuda.synchronize()
+                t_fwd += time.perf_counter() - t1
                 r.backward([w[0]], [w[1]])
         torch.cuda.synchronize()
-        return time.perf_counter() - t0
+        el = time.perf_counter() - t0
+        split["batched" if batched else "plain"] = {"forward_s": t_fwd, "backward_s": el - t_fwd}
+        return el
 
     run(True, 2 * every)     # warm-up: scratch, graphs
     run(False, 2 * every)
@@ -401,7 +411,7 @@ def adjoint_measure(n_scenes: int = 32, n_particles: int = 50_000, n_grid: int =
     return {"metric": "batched forward+adjoint scenes/s", "unit": f"scenes/s ({substeps} substeps each)",
             "value": n_scenes / t_batch, "plain_value": n_scenes / t_plain, "speedup_vs_plain": t_plain / t_batch,
             "scenes": n_scenes, "particles_total": n_total, "grid": f"{n_grid}^3", "substeps": substeps,
-            "checkpoint_every": every, "dt": dt,
+            "checkpoint_every": every, "dt": dt, "seconds": split,
             "particle_substeps_per_s": n_total * substeps / t_batch}
 
 
