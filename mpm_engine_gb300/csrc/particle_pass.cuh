@@ -41,30 +41,12 @@ __device__ __forceinline__ bool stencil_ok(const Stencil &s, int ng, int periodi
 
 __device__ __forceinline__ int wrap(int i, int n) { return ((i % n) + n) % n; }
 
-__device__ __forceinline__ void mark_block_id(const PK &k, int b) {
+__device__ __forceinline__ void mark_block(const PK &k, int bx, int by, int bz) {
+    int b = (bx * k.bd + by) * k.bd + bz;
     if (k.blk_flag[b] == 0 && atomicExch(&k.blk_flag[b], 1) == 0) {
         int i = atomicAdd(k.blk_count, 1);
         k.blk_list[i] = b;
     }
-}
-__device__ __forceinline__ void mark_block(const PK &k, int bx, int by, int bz) {
-    mark_block_id(k, (bx * k.bd + by) * k.bd + bz);
-}
-
-// The tiled scatter marks its 4^3 blocks in a per-CTA set in shared memory (open
-// addressing over kMarkSlots slots) and checks the global flags once per distinct
-// block at the end of the CTA: the scatter loop then never waits on a global load.
-// A full set marks directly.
-constexpr int kMarkSlots = 64;
-__device__ __forceinline__ void defer_mark(const PK &k, int *s_blk, int bx, int by, int bz) {
-    const int b = (bx * k.bd + by) * k.bd + bz;
-    unsigned h = ((unsigned)b * 2654435761u) >> 26;
-    for (int i = 0; i < kMarkSlots; ++i) {
-        const int old = atomicCAS(&s_blk[h], -1, b);
-        if (old == -1 || old == b) return;
-        h = (h + 1) & (kMarkSlots - 1);
-    }
-    mark_block_id(k, b);
 }
 
 // ---- building blocks shared by the direct and the tiled particle kernels ----
@@ -740,7 +722,6 @@ __device__ __forceinline__ void particles_tile(const PK &k, int mode, int tile) 
     __shared__ int s_seg[kTileThreads + 1];
     __shared__ int s_wcnt[kTileThreads / 32];
     __shared__ int s_red[kTileThreads / 32][6];
-    __shared__ int s_blk[kMarkSlots];   // distinct blocks this CTA's scatter deposits into
     // F, mass and volume of a gather pass's particle, fetched asynchronously at the
     // start so that their L2 round trip overlaps the tile box, the tile load and the
     // gather (a gather pass starts before its wait: nothing still running writes
@@ -966,7 +947,6 @@ __device__ __forceinline__ void particles_tile(const PK &k, int mode, int tile) 
     } else {
         s_key[t] = -1 - t;   // a dead slot forms its own, skipped run
     }
-    for (int i = t; i < kMarkSlots; i += kTileThreads) s_blk[i] = -1;
     __syncthreads();
     // ---- runs of equal base node (and CPIC tag): compact the run heads
     const bool head = (t == 0) || (s_key[t] != s_key[t - 1]) || (CDF && s_pc[t] != s_pc[t - 1]);
@@ -1062,18 +1042,12 @@ __device__ __forceinline__ void particles_tile(const PK &k, int mode, int tile) 
                     atomicAdd(k.gmv + ((size_t)gx * k.ng + gy) * k.ng + gz,
                               make_float4(acc[kk][0], acc[kk][1], acc[kk][2], acc[kk][3]));
                     if ((gz >> 2) != marked) {
-                        defer_mark(k, s_blk, gx >> 2, gy >> 2, gz >> 2);
+                        mark_block(k, gx >> 2, gy >> 2, gz >> 2);
                         marked = gz >> 2;
                     }
                 }
             }
         }
-    }
-    // the distinct blocks of this CTA's deposits, each checked against the global flags once
-    __syncthreads();
-    for (int i = t; i < kMarkSlots; i += kTileThreads) {
-        const int b = s_blk[i];
-        if (b >= 0) mark_block_id(k, b);
     }
 }
 
