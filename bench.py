@@ -510,7 +510,7 @@ def press_measure(n_grid: int = 256, ticks: int = 100, substeps: int = 20, devic
     rl["binding"] = max((k for k in ("hbm", "fp32") if rl[k]["frac"] is not None), key=lambda k: rl[k]["frac"])
     return {"workload": f"press_mu_i_{n_grid}^3", "particles": n, "substeps": ticks * substeps, "dt": dt,
             "us_per_substep": us_substep, "particle_substeps_per_s": n * ticks * substeps / el,
-            "plate_Fz_last_N": fz[-1], "roofline": rl, "pipeline": "split (sparse)", "max_frac": max(fr)}
+            "plate_Fz_last_N": fz[-1], "roofline": rl, "pipeline": "fused (sparse)", "max_frac": max(fr)}
 
 
 def captured_traffic(workload: str):

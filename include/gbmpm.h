@@ -175,6 +175,10 @@ typedef struct {
 #define GBMPM_TICK_PROFILE 4    /* per-phase CUDA-event timing, live launches */
 #define GBMPM_TICK_REORDER 8    /* run the tick on a block-sorted working copy with shared-memory
                                    grid tiles (results equal up to float summation order) */
+#define GBMPM_TICK_DETERMINISTIC 16  /* deterministic passes: every operation rounded once, P2G summed
+                                        per node in particle order (sorted records, no float atomics);
+                                        bit-reproducible; jelly, water and Newtonian materials with
+                                        plane, box and wall colliders (else GBMPM_ERR_UNSUPPORTED) */
 
 #define GBMPM_NUM_PHASES 6      /* stress, p2g, g2p2g_fused, grid_update, g2p, sort+gather/scatter */
 

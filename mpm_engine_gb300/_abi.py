@@ -29,6 +29,7 @@ TICK_FUSED = 1
 TICK_GRAPH = 2
 TICK_PROFILE = 4
 TICK_REORDER = 8
+TICK_DETERMINISTIC = 16
 
 COLLIDER_PLANE = 0
 COLLIDER_BOX = 1

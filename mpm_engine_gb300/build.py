@@ -24,6 +24,11 @@ def nvcc_path() -> str:
     raise RuntimeError("nvcc not found (CUDA toolkit required to build libgbmpm.so)")
 
 
+# deterministic.cu states its arithmetic operation by operation: no product may be
+# contracted into an FMA there
+PER_TU_FLAGS = {"deterministic.cu": ["--fmad=false"]}
+
+
 def sources() -> list[Path]:
     return sorted(CSRC.glob("*.cu"))
 
@@ -45,7 +50,8 @@ def build_native(verbose: bool = False, force: bool = False) -> Path:
     for src in sources():
         obj = OUT_DIR / (src.stem + ".o")
         objs.append(obj)
-        cmd = [nvcc] + common + ["-c", "-o", str(obj), str(src)]
+        extra = PER_TU_FLAGS.get(src.name, [])
+        cmd = [nvcc] + common + extra + ["-c", "-o", str(obj), str(src)]
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
     logs = []
     failed = []

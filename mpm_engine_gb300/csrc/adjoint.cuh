@@ -711,9 +711,10 @@ __device__ void collide_adj(const ColDev &c, const PoseRec &P, int gx, int gy, i
                             const AdjK &a, float m, const float *fb, float *velb, float &mb) {
     const float dx = a.dx;
     switch (c.kind) {
-    case GBMPM_COLLIDER_PLANE: {
-        const float o0 = (float)gx * dx - P.p[0], o1 = (float)gy * dx - P.p[1], o2 = (float)gz * dx - P.p[2];
-        const float dp = o0 * c.normal[0] + o1 * c.normal[1] + o2 * c.normal[2];
+    case GBMPM_COLLIDER_PLANE: {   // the forward's contact test, rounded as it rounds it
+        const float o0 = __fsub_rn(__fmul_rn((float)gx, dx), P.p[0]), o1 = __fsub_rn(__fmul_rn((float)gy, dx), P.p[1]),
+                    o2 = __fsub_rn(__fmul_rn((float)gz, dx), P.p[2]);
+        const float dp = dot3_rn(o0, c.normal[0], o1, c.normal[1], o2, c.normal[2]);
         if (!(dp < 0.0f)) return;
         if (c.surface == 0) { vb[0] = vb[1] = vb[2] = 0.0f; return; }
         if (c.surface == 11) {
@@ -722,14 +723,15 @@ __device__ void collide_adj(const ColDev &c, const PoseRec &P, int gx, int gy, i
             return;
         }
         const float *n = c.normal;
-        const float nc = vin[0] * n[0] + vin[1] * n[1] + vin[2] * n[2];
+        const float nc = dot3_rn(vin[0], n[0], vin[1], n[1], vin[2], n[2]);
         const bool slip = c.surface == 1;
         const float sub = slip ? nc : fminf(nc, 0.0f);
-        const float w[3] = {vin[0] - sub * n[0], vin[1] - sub * n[1], vin[2] - sub * n[2]};
-        const float len = sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        const float w[3] = {__fsub_rn(vin[0], __fmul_rn(n[0], sub)), __fsub_rn(vin[1], __fmul_rn(n[1], sub)),
+                            __fsub_rn(vin[2], __fmul_rn(n[2], sub))};
+        const float len = __fsqrt_rn(dot3_rn(w[0], w[0], w[1], w[1], w[2], w[2]));
         float wb[3] = {vb[0], vb[1], vb[2]}, ncb = 0.0f;
         if (nc < 0.0f && len > 1e-20f) {
-            const float t = len + nc * c.friction;
+            const float t = __fadd_rn(len, __fmul_rn(nc, c.friction));
             if (t <= 0.0f) {
                 wb[0] = wb[1] = wb[2] = 0.0f;
             } else {   // v = w + mu nc w/|w|
@@ -749,7 +751,8 @@ __device__ void collide_adj(const ColDev &c, const PoseRec &P, int gx, int gy, i
     }
     case GBMPM_COLLIDER_BOX: {   // v = vel, acc += m (vin - vel) inside (mpm_solver_warp.py:2053-2088)
         if (P.mode == 2) { vb[0] = vb[1] = vb[2] = 0.0f; return; }
-        const float o0 = (float)gx * dx - P.p[0], o1 = (float)gy * dx - P.p[1], o2 = (float)gz * dx - P.p[2];
+        const float o0 = __fsub_rn(__fmul_rn((float)gx, dx), P.p[0]), o1 = __fsub_rn(__fmul_rn((float)gy, dx), P.p[1]),
+                    o2 = __fsub_rn(__fmul_rn((float)gz, dx), P.p[2]);
         if (fabsf(o0) < c.size[0] && fabsf(o1) < c.size[1] && fabsf(o2) < c.size[2]) {
 #pragma unroll
             for (int d = 0; d < 3; ++d) {

@@ -245,6 +245,15 @@ struct ParticleLaunch {
 };
 void launch_particle_pass(const ParticleLaunch &L, const PK &k, int mode, cudaStream_t s);
 
+// Deterministic particle passes (deterministic.cu): every operation rounded once,
+// P2G as per-node sums in particle order. det_launch_p2g writes 27 records a
+// particle; the caller sorts them by key (stable) and hands them to det_launch_segsum.
+void det_launch_g2p(const PK &k, bool reset_lists, cudaStream_t s);
+void det_launch_stress(const PK &k, cudaStream_t s);
+void det_launch_p2g(const PK &k, unsigned long long *key, int *idx, float4 *val, cudaStream_t s);
+void det_launch_segsum(const PK &k, const unsigned long long *key, const int *idx, const float4 *val, int n_rec,
+                       cudaStream_t s);
+
 // Batched scenes: one particle pass over many scenes. CTA b of the launch takes
 // tile ctas[b].tile of scene ctas[b].scene (particles_batch_*.cu).
 struct BatchCta {

@@ -1,0 +1,428 @@
+// The deterministic particle passes (GBMPM_TICK_DETERMINISTIC).
+//
+// Every operation here rounds once: this translation unit is compiled with
+// --fmad=false, so no product is contracted into an FMA, and each expression is
+// written in the operation order of the fp32 statement of the reference's kernels
+// (mpm_utils.py). Powers go through double and are rounded once, and the SVD runs
+// in double. The P2G deposits are not added with atomics: each particle writes its
+// 27 contributions as records keyed by node, a stable radix sort groups them by
+// node in particle order, and one thread per node adds its group in that order.
+//
+// So a tick on this path is bit-for-bit reproducible run to run, and it equals, bit
+// for bit, a single-threaded CPU statement of the same arithmetic in the same order.
+// It is a verification mode: simple one-thread-per-item kernels over the caller's
+// particle order, several times slower than the tiled path.
+//
+// Scope: jelly (FCR, id 0), water (id 6) and the Newtonian / Bingham /
+// Herschel-Bulkley law (id 10), with plane, box and wall colliders; the host
+// rejects other materials and CDF lanes, rigid bodies and particle modifiers.
+#include "common.cuh"
+
+namespace gbmpm {
+namespace {
+
+constexpr int kDetThreads = 256;
+
+// ---- 3x3 algebra, row-major float[9], in the reference's operation order ----
+
+// warp mat*mat: t[i][j] = ((0 + a[i][0] b[0][j]) + a[i][1] b[1][j]) + a[i][2] b[2][j]
+__device__ __forceinline__ void d_mmul(const float *a, const float *b, float *t) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) acc = acc + a[3 * i + k] * b[3 * k + j];
+            t[3 * i + j] = acc;
+        }
+}
+__device__ __forceinline__ void d_trans(const float *a, float *t) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) t[3 * i + j] = a[3 * j + i];
+}
+// warp mat*vec: r[i] = (a[i][0] b0 + a[i][1] b1) + a[i][2] b2
+__device__ __forceinline__ void d_mvmul(const float *a, const float *b, float *r) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) r[i] = a[3 * i] * b[0] + a[3 * i + 1] * b[1] + a[3 * i + 2] * b[2];
+}
+// warp determinant: dot(row0, cross(row1, row2))
+__device__ __forceinline__ float d_det(const float *a) {
+    const float c0 = a[4] * a[8] - a[5] * a[7];
+    const float c1 = a[5] * a[6] - a[3] * a[8];
+    const float c2 = a[3] * a[7] - a[4] * a[6];
+    return a[0] * c0 + a[1] * c1 + a[2] * c2;
+}
+// wp.pow in fp32 as its correctly rounded value: evaluated in double, rounded once
+__device__ __forceinline__ float d_pow(float x, float y) { return (float)pow((double)x, (double)y); }
+
+// ---- SVD: this project's cyclic Jacobi eigen-solve of F^T F, then a Givens QR of
+// F V, in double throughout (the tiled path's method, without its FP32 first try)
+__device__ void d_svd3(const float *F, float *U, float *s, float *Vo) {
+    double A[3][3], B[3][3], V[3][3], W[3][3], Q[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) A[i][j] = (double)F[3 * i + j];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double acc = 0.0;
+            for (int k = 0; k < 3; ++k) acc = acc + A[k][i] * A[k][j];
+            B[i][j] = acc;
+            V[i][j] = (i == j) ? 1.0 : 0.0;
+        }
+    for (int sweep = 0; sweep < 40; ++sweep) {
+        const double off = B[0][1] * B[0][1] + B[0][2] * B[0][2] + B[1][2] * B[1][2];
+        const double dia = B[0][0] * B[0][0] + B[1][1] * B[1][1] + B[2][2] * B[2][2];
+        if (off <= 1e-32 * dia || off == 0.0) break;
+        for (int p = 0; p < 2; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                if (B[p][q] == 0.0) continue;
+                const double theta = (B[q][q] - B[p][p]) / (2.0 * B[p][q]);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+                for (int k = 0; k < 3; ++k) {   // B = J^T B J
+                    const double bkp = B[k][p], bkq = B[k][q];
+                    B[k][p] = c * bkp - sn * bkq;
+                    B[k][q] = sn * bkp + c * bkq;
+                }
+                for (int k = 0; k < 3; ++k) {
+                    const double bpk = B[p][k], bqk = B[q][k];
+                    B[p][k] = c * bpk - sn * bqk;
+                    B[q][k] = sn * bpk + c * bqk;
+                }
+                for (int k = 0; k < 3; ++k) {
+                    const double vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - sn * vkq;
+                    V[k][q] = sn * vkp + c * vkq;
+                }
+            }
+    }
+    // eigenvalues descending, a stable insertion sort (equal values keep their order)
+    int ord[3] = {0, 1, 2};
+    for (int i = 1; i < 3; ++i) {
+        const int val = ord[i];
+        int j = i;
+        while (j > 0 && B[val][val] > B[ord[j - 1]][ord[j - 1]]) { ord[j] = ord[j - 1]; --j; }
+        ord[j] = val;
+    }
+    double Vs[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Vs[i][j] = V[i][ord[j]];
+    const double dv = Vs[0][0] * (Vs[1][1] * Vs[2][2] - Vs[1][2] * Vs[2][1]) -
+                      Vs[0][1] * (Vs[1][0] * Vs[2][2] - Vs[1][2] * Vs[2][0]) +
+                      Vs[0][2] * (Vs[1][0] * Vs[2][1] - Vs[1][1] * Vs[2][0]);
+    if (dv < 0)
+        for (int i = 0; i < 3; ++i) Vs[i][2] = -Vs[i][2];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double acc = 0.0;
+            for (int k = 0; k < 3; ++k) acc = acc + A[i][k] * Vs[k][j];
+            W[i][j] = acc;
+            Q[i][j] = (i == j) ? 1.0 : 0.0;
+        }
+    const int pr[3][2] = {{0, 1}, {0, 2}, {1, 2}};   // zero W[1][0], W[2][0], W[2][1]
+    for (int g = 0; g < 3; ++g) {
+        const int a = pr[g][0], b = pr[g][1], col = (g < 2) ? 0 : 1;
+        const double x = W[a][col], y = W[b][col];
+        const double r = sqrt(x * x + y * y);
+        double c = 1.0, sn = 0.0;
+        if (r > 0.0) { c = x / r; sn = y / r; }
+        for (int k = 0; k < 3; ++k) {
+            const double wa = W[a][k], wb = W[b][k];
+            W[a][k] = c * wa + sn * wb;
+            W[b][k] = -sn * wa + c * wb;
+        }
+        for (int k = 0; k < 3; ++k) {
+            const double qa = Q[k][a], qb = Q[k][b];
+            Q[k][a] = c * qa + sn * qb;
+            Q[k][b] = -sn * qa + c * qb;
+        }
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) { U[3 * i + j] = (float)Q[i][j]; Vo[3 * i + j] = (float)Vs[i][j]; }
+    s[0] = (float)W[0][0]; s[1] = (float)W[1][1]; s[2] = (float)W[2][2];
+}
+
+// ---- quadratic B-spline weights (p2g_particle / g2p_particle, mpm_utils.py:830-850)
+struct DetStencil {
+    int base[3];
+    float fx[3], w[3][3], dw[3][3];   // w[axis][node]
+};
+__device__ __forceinline__ void d_stencil(const float *x, float inv_dx, DetStencil &S) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float gp = x[a] * inv_dx;
+        S.base[a] = (int)floorf(gp - 0.5f);
+        const float fx = gp - (float)S.base[a];
+        S.fx[a] = fx;
+        const float wa = 1.5f - fx, wb = fx - 1.0f, wc = fx - 0.5f;
+        S.w[a][0] = wa * wa * 0.5f;
+        S.w[a][1] = (0.0f - wb * wb) + 0.75f;
+        S.w[a][2] = wc * wc * 0.5f;
+        S.dw[a][0] = fx - 1.5f;
+        S.dw[a][1] = -2.0f * (fx - 1.0f);
+        S.dw[a][2] = fx - 0.5f;
+    }
+}
+__device__ __forceinline__ bool d_inside(const DetStencil &S, int ng, int periodic_x) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (a == 0 && periodic_x) continue;
+        if (S.base[a] < 0 || S.base[a] + 2 >= ng) return false;
+    }
+    return true;
+}
+__device__ __forceinline__ int d_wrap(int i, int n) { return ((i % n) + n) % n; }
+// compute_dweight (mpm_utils.py:601-610)
+__device__ __forceinline__ void d_dweight(const DetStencil &S, int i, int j, int k, float inv_dx, float *d) {
+    d[0] = S.dw[0][i] * S.w[1][j] * S.w[2][k] * inv_dx;
+    d[1] = S.w[0][i] * S.dw[1][j] * S.w[2][k] * inv_dx;
+    d[2] = S.w[0][i] * S.w[1][j] * S.dw[2][k] * inv_dx;
+}
+
+// ---- G2P (g2p_particle, mpm_utils.py:944-1043): v, C, x, L and F_trial --------
+__global__ void __launch_bounds__(kDetThreads) k_det_g2p(PK k, int reset_lists) {
+    if (reset_lists && blockIdx.x == 0 && threadIdx.x == 0) {
+        k.blk_count[0] = 0;
+        k.blk_count[1] = 0;
+    }
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= k.n) return;
+    if (k.sel && k.sel[p] != 0) return;
+    const float x[3] = {k.x[3 * p], k.x[3 * p + 1], k.x[3 * p + 2]};
+    DetStencil S;
+    d_stencil(x, k.inv_dx, S);
+    if (!d_inside(S, k.ng, k.periodic_x)) { set_status(k.status, GBMPM_FLAG_STENCIL_OOB); return; }
+    float nv[3] = {0.0f, 0.0f, 0.0f}, nC[9], nF[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) { nC[i] = 0.0f; nF[i] = 0.0f; }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            for (int kk = 0; kk < 3; ++kk) {
+                int ix = S.base[0] + i;
+                if (k.periodic_x) ix = d_wrap(ix, k.ng);
+                const int iy = S.base[1] + j, iz = S.base[2] + kk;
+                const float dpos[3] = {(float)i - S.fx[0], (float)j - S.fx[1], (float)kk - S.fx[2]};
+                const float weight = S.w[0][i] * S.w[1][j] * S.w[2][kk];
+                const float4 g4 = k.gv[((size_t)ix * k.ng + iy) * k.ng + iz];
+                const float gv[3] = {g4.x, g4.y, g4.z};
+#pragma unroll
+                for (int a = 0; a < 3; ++a) nv[a] = nv[a] + gv[a] * weight;
+                const float sc = weight * k.inv_dx * 4.0f;
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+#pragma unroll
+                    for (int b = 0; b < 3; ++b) nC[3 * a + b] = nC[3 * a + b] + gv[a] * dpos[b] * sc;
+                float dwt[3];
+                d_dweight(S, i, j, kk, k.inv_dx, dwt);
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+#pragma unroll
+                    for (int b = 0; b < 3; ++b) nF[3 * a + b] = nF[3 * a + b] + gv[a] * dwt[b];
+            }
+    float xn[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) xn[a] = x[a] + nv[a] * k.dt;
+    if (k.periodic_x) {
+        const float lx = (float)k.ng * k.dx;
+        if (xn[0] < 0.0f) xn[0] = xn[0] + lx;
+        if (xn[0] >= lx) xn[0] = xn[0] - lx;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { k.v[3 * p + a] = nv[a]; k.x[3 * p + a] = xn[a]; }
+    float A[9], Fo[9], Ft[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        k.C[9 * (size_t)p + i] = nC[i];
+        k.L[9 * (size_t)p + i] = nF[i];
+        A[i] = ((i % 4 == 0) ? 1.0f : 0.0f) + nF[i] * k.dt;
+        Fo[i] = k.F[9 * (size_t)p + i];
+    }
+    d_mmul(A, Fo, Ft);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) k.Ft[9 * (size_t)p + i] = Ft[i];
+    if (k.update_cov && k.cov) {   // update_cov (mpm_utils.py:613-633)
+        float *c6 = k.cov + 6 * (size_t)p;
+        const float cn[9] = {c6[0], c6[1], c6[2], c6[1], c6[3], c6[4], c6[2], c6[4], c6[5]};
+        float gT[9], a1[9], a2[9];
+        d_trans(nF, gT);
+        d_mmul(nF, cn, a1);
+        d_mmul(cn, gT, a2);
+        float nn[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) nn[i] = cn[i] + (a1[i] + a2[i]) * k.dt;
+        c6[0] = nn[0]; c6[1] = nn[1]; c6[2] = nn[2]; c6[3] = nn[4]; c6[4] = nn[5]; c6[5] = nn[8];
+    }
+}
+
+// ---- stress (stress_update_particle, mpm_utils.py:1056-1149) --------------------
+__global__ void __launch_bounds__(kDetThreads) k_det_stress(PK k) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= k.n) return;
+    if (k.sel && k.sel[p] != 0) return;
+    const int mat = k.mat[p];
+    float Ft[9], F[9], st[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Ft[i] = k.Ft[9 * (size_t)p + i];
+    if (mat == 6 || mat == 10) {   // the fluids keep only the volume: F = J^(1/3) I
+        const float Jc = d_pow(d_det(Ft), 1.0f / 3.0f);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) F[i] = (i % 4 == 0) ? Jc : 0.0f;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) F[i] = Ft[i];
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) k.F[9 * (size_t)p + i] = F[i];
+    const float J = d_det(F);
+    const MatTables &T = *k.tab;
+    if (mat == 0) {   // kirchoff_stress_FCR (mpm_utils.py:8-15)
+        float U[9], sg[3], V[9], Vt[9], R[9], D[9], FT[9];
+        d_svd3(F, U, sg, V);
+        d_trans(V, Vt);
+        d_mmul(U, Vt, R);
+        const float mu = k.mu[p], lam = k.lam[p];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) D[i] = (F[i] - R[i]) * (2.0f * mu);
+        d_trans(F, FT);
+        d_mmul(D, FT, st);
+        const float d = lam * J * (J - 1.0f);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) st[i] = st[i] + ((i % 4 == 0) ? 1.0f : 0.0f) * d;
+    } else {
+        const float gamma = 1.1f;
+        const float pressure = -T.bulk[mat] * (d_pow(J, -gamma) - 1.0f);
+        float c[9];
+        if (mat == 6) {   // kirchoff_stress_water (mpm_utils.py:17-25)
+#pragma unroll
+            for (int i = 0; i < 9; ++i) c[i] = ((i % 4 == 0) ? 1.0f : 0.0f) * pressure;
+        } else {          // kirchoff_stress_newtonian (mpm_utils.py:27-54)
+            const float *L = k.L + 9 * (size_t)p;
+            float D[9], Dd[9];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) D[3 * i + j] = (L[3 * i + j] + L[3 * j + i]) * 0.5f;
+            const float trd = (D[0] + D[4] + D[8]) / 3.0f;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Dd[i] = D[i] - ((i % 4 == 0) ? 1.0f : 0.0f) * trd;
+            float dd = 0.0f;
+            for (int i = 0; i < 9; ++i) dd = dd + Dd[i] * Dd[i];
+            const float eps = 0.02f;
+            const float gd = sqrtf(2.0f * dd + eps * eps);
+            const float eta_app = T.pv[mat] + k.ys[p] / gd + T.hardening[mat] * d_pow(gd, T.softening[mat] - 1.0f);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) c[i] = ((i % 4 == 0) ? 1.0f : 0.0f) * pressure + Dd[i] * (2.0f * eta_app);
+        }
+#pragma unroll
+        for (int i = 0; i < 9; ++i) st[i] = c[i] * J;
+    }
+    float stT[9];
+    d_trans(st, stT);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) k.S[9 * (size_t)p + i] = (st[i] + stT[i]) * 0.5f;
+}
+
+// ---- P2G records (p2g_particle, mpm_utils.py:819-916) ---------------------------
+// Record p * 27 + (i * 9 + j * 3 + k) holds the deposit of particle p into node
+// (base + (i, j, k)): key = node index, val = (momentum and force impulse, mass).
+// A particle that deposits nothing keys its records past the last node.
+__global__ void __launch_bounds__(kDetThreads) k_det_p2g(PK k, unsigned long long *key, int *idx, float4 *val) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= k.n) return;
+    const unsigned long long none = (unsigned long long)k.ng * k.ng * k.ng;
+    const size_t r0 = (size_t)p * 27;
+    auto skip = [&]() {
+        for (int s = 0; s < 27; ++s) { key[r0 + s] = none; idx[r0 + s] = (int)(r0 + s); }
+    };
+    if (k.sel && k.sel[p] != 0) { skip(); return; }
+    const float x[3] = {k.x[3 * p], k.x[3 * p + 1], k.x[3 * p + 2]};
+    DetStencil S;
+    d_stencil(x, k.inv_dx, S);
+    if (!d_inside(S, k.ng, k.periodic_x)) {
+        set_status(k.status, GBMPM_FLAG_STENCIL_OOB);
+        skip();
+        return;
+    }
+    float C0[9], CT[9], C[9], fs[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) C0[i] = k.C[9 * (size_t)p + i];
+    d_trans(C0, CT);
+    const float r = k.rpic;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) C[i] = C0[i] * (1.0f - r) + (C0[i] - CT[i]) * (r / 2.0f);
+    if (r < -0.001f) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) C[i] = 0.0f;
+    }
+    const float mass = k.mass[p], vol = k.vol[p];
+    const float v[3] = {k.v[3 * p], k.v[3 * p + 1], k.v[3 * p + 2]};
+#pragma unroll
+    for (int i = 0; i < 9; ++i) fs[i] = k.S[9 * (size_t)p + i] * -vol;
+    int s = 0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            for (int kk = 0; kk < 3; ++kk, ++s) {
+                const float dpos[3] = {((float)i - S.fx[0]) * k.dx, ((float)j - S.fx[1]) * k.dx,
+                                       ((float)kk - S.fx[2]) * k.dx};
+                int ix = S.base[0] + i;
+                if (k.periodic_x) ix = d_wrap(ix, k.ng);
+                const int iy = S.base[1] + j, iz = S.base[2] + kk;
+                const float weight = S.w[0][i] * S.w[1][j] * S.w[2][kk];
+                float dwt[3], ef[3], cd[3];
+                d_dweight(S, i, j, kk, k.inv_dx, dwt);
+                d_mvmul(fs, dwt, ef);
+                d_mvmul(C, dpos, cd);
+                const float wm = weight * mass;
+                float add[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) add[a] = (v[a] + cd[a]) * wm + ef[a] * k.dt;
+                key[r0 + s] = ((unsigned long long)ix * k.ng + iy) * k.ng + iz;
+                idx[r0 + s] = (int)(r0 + s);
+                val[r0 + s] = make_float4(add[0], add[1], add[2], weight * mass);
+            }
+}
+
+// ---- per-node sums in particle order ---------------------------------------------
+// After the stable sort by node, the records of one node are contiguous and in
+// particle order; the thread at the first record of a node adds them from zero,
+// as the serial deposit loop does, writes the node and marks its 4^3 block.
+__global__ void __launch_bounds__(kDetThreads) k_det_segsum(PK k, const unsigned long long *key, const int *idx,
+                                                            const float4 *val, int n_rec) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_rec) return;
+    const unsigned long long node = key[i];
+    const unsigned long long none = (unsigned long long)k.ng * k.ng * k.ng;
+    if (node >= none || (i > 0 && key[i - 1] == node)) return;
+    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int j = i; j < n_rec && key[j] == node; ++j) {
+        const float4 d = val[idx[j]];
+        acc.x = acc.x + d.x;
+        acc.y = acc.y + d.y;
+        acc.z = acc.z + d.z;
+        acc.w = acc.w + d.w;
+    }
+    k.gmv[node] = acc;
+    const int gz = (int)(node % k.ng), gy = (int)((node / k.ng) % k.ng), gx = (int)(node / ((size_t)k.ng * k.ng));
+    const int b = ((gx >> 2) * k.bd + (gy >> 2)) * k.bd + (gz >> 2);
+    if (k.blk_flag[b] == 0 && atomicExch(&k.blk_flag[b], 1) == 0) k.blk_list[atomicAdd(k.blk_count, 1)] = b;
+}
+
+inline int det_grid(long long n) { return (int)std::max<long long>(1, (n + kDetThreads - 1) / kDetThreads); }
+
+}  // namespace
+
+void det_launch_g2p(const PK &k, bool reset_lists, cudaStream_t s) {
+    k_det_g2p<<<det_grid(k.n), kDetThreads, 0, s>>>(k, reset_lists ? 1 : 0);
+}
+void det_launch_stress(const PK &k, cudaStream_t s) { k_det_stress<<<det_grid(k.n), kDetThreads, 0, s>>>(k); }
+void det_launch_p2g(const PK &k, unsigned long long *key, int *idx, float4 *val, cudaStream_t s) {
+    k_det_p2g<<<det_grid(k.n), kDetThreads, 0, s>>>(k, key, idx, val);
+}
+void det_launch_segsum(const PK &k, const unsigned long long *key, const int *idx, const float4 *val, int n_rec,
+                       cudaStream_t s) {
+    k_det_segsum<<<det_grid(n_rec), kDetThreads, 0, s>>>(k, key, idx, val, n_rec);
+}
+
+}  // namespace gbmpm

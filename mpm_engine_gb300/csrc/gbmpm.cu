@@ -157,6 +157,11 @@ struct gbmpm_engine {
     int tile_occ = 3;       // resident CTAs per SM the tiled particle kernel is compiled for
     int cdf_occ = 3;        // the same for its CPIC variant
     bool pdl = true;        // programmatic dependent launch of the particle and grid passes
+    bool det = false;       // this tick runs the deterministic passes (GBMPM_TICK_DETERMINISTIC)
+    DevBuf<unsigned long long> det_key[2];   // P2G records of the deterministic passes, sorted by node
+    DevBuf<int> det_idx[2];
+    DevBuf<float4> det_val;
+    DevBuf<unsigned> det_hist;
     bool cdf_fused_stamp = true;   // one restamp launch a substep (else the five-kernel sequence)
     int grid_ctas = 2;      // grid-update CTAs per SM
     // graph cache
@@ -270,7 +275,35 @@ void launch_pdl(gbmpm_engine *e, void (*kern)(P...), int grid, int block, cudaSt
     launch_kernel(e->pdl, kern, grid, block, s, args...);
 }
 
+// The deterministic passes: G2P, stress, then P2G as 27 records a particle, a stable
+// radix sort of the records by node (so each node's records stay in particle
+// order) and one in-order sum per node.
+void det_pass(gbmpm_engine *e, const PK &k, int mode, cudaStream_t s) {
+    if (mode & PASS_G2P) { det_launch_g2p(k, (mode & PASS_RESET_LISTS) != 0, s); e->launches++; }
+    if (mode & PASS_STRESS) { det_launch_stress(k, s); e->launches++; }
+    if (!(mode & PASS_P2G)) return;
+    const int nrec = 27 * k.n;
+    det_launch_p2g(k, e->det_key[0].ptr, e->det_idx[0].ptr, e->det_val.ptr, s);
+    const unsigned long long none = (unsigned long long)k.ng * k.ng * k.ng;   // key of an empty record
+    int bits = 0;
+    while (bits < 64 && (none >> bits) != 0ull) ++bits;
+    const int ntiles = (nrec + kSortTile - 1) / kSortTile;
+    int cur = 0;
+    for (int shift = 0; shift < bits; shift += kRadixBits) {
+        k_radix_hist<<<ntiles, kSortThreads, 0, s>>>(e->det_key[cur].ptr, nrec, shift, e->det_hist.ptr, ntiles);
+        k_radix_scan<<<1, 1024, 0, s>>>(e->det_hist.ptr, ntiles * kRadixBins);
+        k_radix_scatter<<<ntiles, kSortThreads, 0, s>>>(e->det_key[cur].ptr, e->det_idx[cur].ptr,
+                                                         e->det_key[cur ^ 1].ptr, e->det_idx[cur ^ 1].ptr, nrec,
+                                                         shift, e->det_hist.ptr, ntiles);
+        e->launches += 3;
+        cur ^= 1;
+    }
+    det_launch_segsum(k, e->det_key[cur].ptr, e->det_idx[cur].ptr, e->det_val.ptr, nrec, s);
+    e->launches += 2;
+}
+
 void launch_particles(gbmpm_engine *e, const PK &k, int mode, bool tiled, cudaStream_t s) {
+    if (e->det) { det_pass(e, k, mode, s); return; }
     ParticleLaunch L{tiled, has_solids(e->M), e->pdl, e->tile_occ, e->cdf_occ};
     launch_particle_pass(L, k, mode, s);
     e->launches++;
@@ -867,6 +900,8 @@ void gbmpm_engine_destroy(gbmpm_engine *e) {
     e->c_tag.release(); e->c_tag_prev.release(); e->c_block.release(); e->c_d.release(); e->c_d_prev.release();
     e->c_wrench.release(); e->c_partial.release(); e->c_cache.release();
     e->adj_states.release(); e->adj_scratch.release(); e->adj_grid.release();
+    e->det_key[0].release(); e->det_key[1].release(); e->det_idx[0].release(); e->det_idx[1].release();
+    e->det_val.release(); e->det_hist.release();
     delete e;
 }
 
@@ -1207,7 +1242,25 @@ int prepare_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int
     build_pose_table(e, *time, dt, substeps);
     GB_CUDA(cudaMemcpyAsync(e->d_pose.ptr, e->h_pose, need * sizeof(PoseRec), cudaMemcpyHostToDevice, s));
     GB_CUDA(cudaEventRecord(e->pose_done, s));
-    reorder = (flags & GBMPM_TICK_REORDER) && !e->M.periodic_x && e->P.n > 0 && e->G.n_grid <= 1024;
+    e->det = (flags & GBMPM_TICK_DETERMINISTIC) != 0;
+    if (e->det) {
+        // jelly (0), water (6) and the Newtonian law (10) only; on the caller's particle order
+        const uint32_t det_mats = (1u << 0) | (1u << 6) | (1u << 10);
+        if (e->M.material_mask & ~det_mats)
+            return fail(GBMPM_ERR_UNSUPPORTED, "deterministic ticks support jelly, water and Newtonian materials");
+        if (e->cdf.n > 0 || e->n_bodies > 0 || e->n_mods > 0)
+            return fail(GBMPM_ERR_UNSUPPORTED,
+                        "deterministic ticks support no CDF colliders, rigid bodies or particle modifiers");
+        const size_t nrec = (size_t)27 * std::max(1, e->P.n);
+        if (nrec > (size_t)INT32_MAX) return fail(GBMPM_ERR_ARG, "too many particles for a deterministic tick");
+        const unsigned long long *old_key = e->det_key[0].ptr;
+        GB_CUDA(e->det_key[0].ensure(nrec)); GB_CUDA(e->det_key[1].ensure(nrec));
+        GB_CUDA(e->det_idx[0].ensure(nrec)); GB_CUDA(e->det_idx[1].ensure(nrec));
+        GB_CUDA(e->det_val.ensure(nrec));
+        GB_CUDA(e->det_hist.ensure((nrec + kSortTile - 1) / kSortTile * kRadixBins));
+        if (e->det_key[0].ptr != old_key) mark_dirty(e);
+    }
+    reorder = !e->det && (flags & GBMPM_TICK_REORDER) && !e->M.periodic_x && e->P.n > 0 && e->G.n_grid <= 1024;
     if (reorder && e->ws_n != e->P.n) {
         GB_CUDA(ensure_ws(e));
         mark_dirty(e);
@@ -1701,6 +1754,8 @@ void gbmpm_batch_destroy(gbmpm_batch *b) {
 int gbmpm_batch_tick(gbmpm_batch *b, double *times, double dt, int32_t substeps, int32_t flags, void *stream) {
     if (!b || !times) return fail(GBMPM_ERR_ARG, "bad batch tick arguments");
     if (flags & GBMPM_TICK_PROFILE) return fail(GBMPM_ERR_UNSUPPORTED, "profiling is per engine (gbmpm_tick)");
+    if (flags & GBMPM_TICK_DETERMINISTIC)
+        return fail(GBMPM_ERR_UNSUPPORTED, "deterministic ticks are per engine (gbmpm_tick)");
     cudaStream_t s = (cudaStream_t)stream;
     const int n = (int)b->engines.size();
     for (int i = 0; i < n; ++i)

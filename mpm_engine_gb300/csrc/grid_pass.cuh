@@ -63,17 +63,26 @@ __global__ void k_ws_scatter(WsTable T, const int *perm, int n) {
 }
 
 // -------------------------------------------------------- grid pass --------
-// capped_cylinder_sdf / revolved_glass_sdf (mpm_solver_warp.py:29-57)
+// capped_cylinder_sdf / revolved_glass_sdf (mpm_solver_warp.py:29-57). The cup's
+// contact normal is a central difference of this SDF over half a cell, which
+// cancels all but about 1e-2 of its value: so every operation here and in the cup
+// branch rounds once (no contraction into FMAs), in the order the fp32 statement of
+// the collider writes it, and the normal carries no rounding of its own.
+__device__ __forceinline__ float dot3_rn(float a0, float b0, float a1, float b1, float a2, float b2) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a0, b0), __fmul_rn(a1, b1)), __fmul_rn(a2, b2));
+}
 __device__ __forceinline__ float capped_cyl(float r, float z, float rad, float z0, float z1) {
-    float zc = 0.5f * (z0 + z1), hh = 0.5f * (z1 - z0);
-    float dr = r - rad, dz = fabsf(z - zc) - hh;
-    float dro = fmaxf(dr, 0.0f), dzo = fmaxf(dz, 0.0f);
-    return sqrtf(dro * dro + dzo * dzo) + fminf(fmaxf(dr, dz), 0.0f);
+    const float zc = __fmul_rn(0.5f, __fadd_rn(z0, z1)), hh = __fmul_rn(0.5f, __fsub_rn(z1, z0));
+    const float dr = __fsub_rn(r, rad), dz = __fsub_rn(fabsf(__fsub_rn(z, zc)), hh);
+    const float dro = fmaxf(dr, 0.0f), dzo = fmaxf(dz, 0.0f);
+    return __fadd_rn(__fsqrt_rn(__fadd_rn(__fmul_rn(dro, dro), __fmul_rn(dzo, dzo))), fminf(fmaxf(dr, dz), 0.0f));
 }
 __device__ __forceinline__ float glass_sdf(float l0, float l1, float l2, const ColDev &c) {
-    float r = sqrtf(l0 * l0 + l1 * l1);
-    float d_outer = capped_cyl(r, l2, c.outer_r, -c.half_h, c.half_h);
-    float d_cav = capped_cyl(r, l2, c.inner_r - c.fillet, c.floor_z + c.fillet, c.half_h + c.outer_r) - c.fillet;
+    const float r = __fsqrt_rn(__fadd_rn(__fmul_rn(l0, l0), __fmul_rn(l1, l1)));
+    const float d_outer = capped_cyl(r, l2, c.outer_r, -c.half_h, c.half_h);
+    const float d_cav = __fsub_rn(capped_cyl(r, l2, __fsub_rn(c.inner_r, c.fillet), __fadd_rn(c.floor_z, c.fillet),
+                                             __fadd_rn(c.half_h, c.outer_r)),
+                                  c.fillet);
     return fmaxf(d_outer, -d_cav);
 }
 __device__ __forceinline__ float trilerp(const float *vals, int res, float f0, float f1, float f2, int stride,
@@ -351,9 +360,11 @@ __device__ __forceinline__ void collide(const ColDev &c, const PoseRec &P, int g
                                         float *v, const GK &k, float *acc) {
     const float dx = k.dx;
     switch (c.kind) {
-    case GBMPM_COLLIDER_PLANE: {  // mpm_solver_warp.py:1929-1992
-        float o0 = (float)gx * dx - P.p[0], o1 = (float)gy * dx - P.p[1], o2 = (float)gz * dx - P.p[2];
-        float dp = o0 * c.normal[0] + o1 * c.normal[1] + o2 * c.normal[2];
+    case GBMPM_COLLIDER_PLANE: {  // mpm_solver_warp.py:1929-1992 (each operation rounded once, as written)
+        const float o0 = __fsub_rn(__fmul_rn((float)gx, dx), P.p[0]), o1 = __fsub_rn(__fmul_rn((float)gy, dx), P.p[1]),
+                    o2 = __fsub_rn(__fmul_rn((float)gz, dx), P.p[2]);
+        const float *n = c.normal;
+        const float dp = dot3_rn(o0, n[0], o1, n[1], o2, n[2]);
         if (dp < 0.0f) {
             if (c.surface == 0) {
                 v[0] = v[1] = v[2] = 0.0f;
@@ -361,22 +372,26 @@ __device__ __forceinline__ void collide(const ColDev &c, const PoseRec &P, int g
                 if ((float)gz * dx < 0.4f || (float)gz * dx > 0.53f) { v[0] = v[1] = v[2] = 0.0f; }
                 else { v[0] *= 0.3f; v[1] = 0.0f; v[2] *= 0.3f; }
             } else {
-                float nc = v[0] * c.normal[0] + v[1] * c.normal[1] + v[2] * c.normal[2];
-                float sub = (c.surface == 1) ? nc : fminf(nc, 0.0f);
-                float w0 = v[0] - sub * c.normal[0], w1 = v[1] - sub * c.normal[1], w2 = v[2] - sub * c.normal[2];
-                float len = sqrtf(w0 * w0 + w1 * w1 + w2 * w2);
-                if (nc < 0.0f && len > 1e-20f) {
-                    float sc = fmaxf(0.0f, len + nc * c.friction) / len;
-                    w0 *= sc; w1 *= sc; w2 *= sc;
+                const float nc = dot3_rn(v[0], n[0], v[1], n[1], v[2], n[2]);
+                const float sub = (c.surface == 1) ? nc : fminf(nc, 0.0f);
+                float w[3] = {__fsub_rn(v[0], __fmul_rn(n[0], sub)), __fsub_rn(v[1], __fmul_rn(n[1], sub)),
+                              __fsub_rn(v[2], __fmul_rn(n[2], sub))};
+                const float len = __fsqrt_rn(dot3_rn(w[0], w[0], w[1], w[1], w[2], w[2]));
+                if (nc < 0.0f && len > 1e-20f) {   // the unit tangent times the Coulomb-reduced speed
+                    const float t = __fadd_rn(len, __fmul_rn(nc, c.friction));
+                    const float sp = (0.0f < t) ? t : 0.0f;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) w[a] = __fmul_rn(__fdiv_rn(w[a], len), sp);
                 }
-                v[0] = w0; v[1] = w1; v[2] = w2;
+                v[0] = w[0]; v[1] = w[1]; v[2] = w[2];
             }
         }
         return;
     }
     case GBMPM_COLLIDER_BOX: {  // mpm_solver_warp.py:2053-2088
         if (P.mode == 2) { v[0] = v[1] = v[2] = 0.0f; return; }
-        float o0 = (float)gx * dx - P.p[0], o1 = (float)gy * dx - P.p[1], o2 = (float)gz * dx - P.p[2];
+        const float o0 = __fsub_rn(__fmul_rn((float)gx, dx), P.p[0]), o1 = __fsub_rn(__fmul_rn((float)gy, dx), P.p[1]),
+                    o2 = __fsub_rn(__fmul_rn((float)gz, dx), P.p[2]);
         if (fabsf(o0) < c.size[0] && fabsf(o1) < c.size[1] && fabsf(o2) < c.size[2]) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) { acc[a] += m * (v[a] - c.vel[a]); v[a] = c.vel[a]; }
@@ -384,42 +399,48 @@ __device__ __forceinline__ void collide(const ColDev &c, const PoseRec &P, int g
         return;
     }
     case GBMPM_COLLIDER_CUP: {  // mpm_solver_warp.py:2161-2225
-        float rel[3] = {(float)gx * dx - P.p[0], (float)gy * dx - P.p[1], (float)gz * dx - P.p[2]};
+        const float rel[3] = {__fsub_rn(__fmul_rn((float)gx, dx), P.p[0]), __fsub_rn(__fmul_rn((float)gy, dx), P.p[1]),
+                              __fsub_rn(__fmul_rn((float)gz, dx), P.p[2])};
         const float *R = P.r;
-        float l0 = R[0] * rel[0] + R[3] * rel[1] + R[6] * rel[2];
-        float l1 = R[1] * rel[0] + R[4] * rel[1] + R[7] * rel[2];
-        float l2 = R[2] * rel[0] + R[5] * rel[1] + R[8] * rel[2];
-        float sdf = glass_sdf(l0, l1, l2, c);
+        const float l0 = dot3_rn(R[0], rel[0], R[3], rel[1], R[6], rel[2]);
+        const float l1 = dot3_rn(R[1], rel[0], R[4], rel[1], R[7], rel[2]);
+        const float l2 = dot3_rn(R[2], rel[0], R[5], rel[1], R[8], rel[2]);
+        const float sdf = glass_sdf(l0, l1, l2, c);
         if (sdf < c.band_c) {
-            float vs[3] = {c.vel[0] + (c.omega[1] * rel[2] - c.omega[2] * rel[1]),
-                           c.vel[1] + (c.omega[2] * rel[0] - c.omega[0] * rel[2]),
-                           c.vel[2] + (c.omega[0] * rel[1] - c.omega[1] * rel[0])};
+            const float *o = c.omega;
+            const float vs[3] = {__fadd_rn(c.vel[0], __fsub_rn(__fmul_rn(o[1], rel[2]), __fmul_rn(o[2], rel[1]))),
+                                 __fadd_rn(c.vel[1], __fsub_rn(__fmul_rn(o[2], rel[0]), __fmul_rn(o[0], rel[2]))),
+                                 __fadd_rn(c.vel[2], __fsub_rn(__fmul_rn(o[0], rel[1]), __fmul_rn(o[1], rel[0])))};
             float vn_[3] = {vs[0], vs[1], vs[2]};
             if (sdf > -c.sticky) {
                 vn_[0] = v[0]; vn_[1] = v[1]; vn_[2] = v[2];
-                float h = 0.25f * dx;
-                float n0 = glass_sdf(l0 + h, l1, l2, c) - glass_sdf(l0 - h, l1, l2, c);
-                float n1 = glass_sdf(l0, l1 + h, l2, c) - glass_sdf(l0, l1 - h, l2, c);
-                float n2 = glass_sdf(l0, l1, l2 + h, c) - glass_sdf(l0, l1, l2 - h, c);
-                float nl = sqrtf(n0 * n0 + n1 * n1 + n2 * n2);
+                const float h = __fmul_rn(0.25f, dx);
+                float n0 = __fsub_rn(glass_sdf(__fadd_rn(l0, h), l1, l2, c), glass_sdf(__fsub_rn(l0, h), l1, l2, c));
+                float n1 = __fsub_rn(glass_sdf(l0, __fadd_rn(l1, h), l2, c), glass_sdf(l0, __fsub_rn(l1, h), l2, c));
+                float n2 = __fsub_rn(glass_sdf(l0, l1, __fadd_rn(l2, h), c), glass_sdf(l0, l1, __fsub_rn(l2, h), c));
+                const float nl = __fsqrt_rn(dot3_rn(n0, n0, n1, n1, n2, n2));
                 if (nl > 1.0e-12f) {
-                    n0 /= nl; n1 /= nl; n2 /= nl;
-                    float n[3] = {R[0] * n0 + R[1] * n1 + R[2] * n2, R[3] * n0 + R[4] * n1 + R[5] * n2,
-                                  R[6] * n0 + R[7] * n1 + R[8] * n2};
-                    float vr[3] = {v[0] - vs[0], v[1] - vs[1], v[2] - vs[2]};
-                    float vn = vr[0] * n[0] + vr[1] * n[1] + vr[2] * n[2];
+                    n0 = __fdiv_rn(n0, nl); n1 = __fdiv_rn(n1, nl); n2 = __fdiv_rn(n2, nl);
+                    const float n[3] = {dot3_rn(R[0], n0, R[1], n1, R[2], n2), dot3_rn(R[3], n0, R[4], n1, R[5], n2),
+                                        dot3_rn(R[6], n0, R[7], n1, R[8], n2)};
+                    const float vr[3] = {__fsub_rn(v[0], vs[0]), __fsub_rn(v[1], vs[1]), __fsub_rn(v[2], vs[2])};
+                    const float vn = dot3_rn(vr[0], n[0], vr[1], n[1], vr[2], n[2]);
                     if (vn < 0.0f) {
-                        float vt[3] = {vr[0] - vn * n[0], vr[1] - vn * n[1], vr[2] - vn * n[2]};
-                        float vtl = sqrtf(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
-                        if (vtl > 1.0e-20f) {
-                            float sc = fmaxf(vtl + c.friction * vn, 0.0f) / vtl;
-                            vt[0] *= sc; vt[1] *= sc; vt[2] *= sc;
+                        float vt[3] = {__fsub_rn(vr[0], __fmul_rn(n[0], vn)), __fsub_rn(vr[1], __fmul_rn(n[1], vn)),
+                                       __fsub_rn(vr[2], __fmul_rn(n[2], vn))};
+                        const float vtl = __fsqrt_rn(dot3_rn(vt[0], vt[0], vt[1], vt[1], vt[2], vt[2]));
+                        if (vtl > 1.0e-20f) {   // the unit tangent times the Coulomb-reduced speed
+                            const float sp = fmaxf(__fadd_rn(vtl, __fmul_rn(c.friction, vn)), 0.0f);
+#pragma unroll
+                            for (int a = 0; a < 3; ++a) vt[a] = __fmul_rn(__fdiv_rn(vt[a], vtl), sp);
                         }
-                        vn_[0] = vs[0] + vt[0]; vn_[1] = vs[1] + vt[1]; vn_[2] = vs[2] + vt[2];
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) vn_[a] = __fadd_rn(vs[a], vt[a]);
                     }
                 }
             }
-            float imp[3] = {m * (v[0] - vn_[0]), m * (v[1] - vn_[1]), m * (v[2] - vn_[2])};
+            const float imp[3] = {__fmul_rn(__fsub_rn(v[0], vn_[0]), m), __fmul_rn(__fsub_rn(v[1], vn_[1]), m),
+                                  __fmul_rn(__fsub_rn(v[2], vn_[2]), m)};
             acc[0] += imp[0]; acc[1] += imp[1]; acc[2] += imp[2];
             acc[3] += rel[1] * imp[2] - rel[2] * imp[1];
             acc[4] += rel[2] * imp[0] - rel[0] * imp[2];
@@ -531,10 +552,11 @@ __device__ __forceinline__ void grid_update(const GK &k, int cta, int nctas) {
             float4 mv = k.gmv[id];
             m = mv.w;
             if (m > 1e-15f) {
-                float inv = 1.0f / m;
-                v[0] = mv.x * inv + k.dt * k.g[0];
-                v[1] = mv.y * inv + k.dt * k.g[1];
-                v[2] = mv.z * inv + k.dt * k.g[2];
+                // each product and sum rounded once, as the fp32 statement writes it
+                const float inv = 1.0f / m;
+                v[0] = __fadd_rn(__fmul_rn(mv.x, inv), __fmul_rn(k.dt, k.g[0]));
+                v[1] = __fadd_rn(__fmul_rn(mv.y, inv), __fmul_rn(k.dt, k.g[1]));
+                v[2] = __fadd_rn(__fmul_rn(mv.z, inv), __fmul_rn(k.dt, k.g[2]));
             }
             if (k.damp < 1.0f) { v[0] *= k.damp; v[1] *= k.damp; v[2] *= k.damp; }
         }

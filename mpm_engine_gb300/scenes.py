@@ -170,18 +170,19 @@ def press_scene(solver_cls, n_grid: int = 256, grid_lim: float = 1.0, plate_spee
 
 # ---- batched dough-squeeze scenes ---------------------------------------------------
 def squeeze_scene(solver_cls, n_particles: int, n_grid: int, material, grid_lim: float = 0.3,
-                  plate_speed: float = 0.05, seed: int = 0, plate_gap: float = 1.0, **solver_kw):
+                  plate_speed: float = 0.05, seed: int = 0, plate_gap: float = 1.0, floor_cells: float = 3.0,
+                  **solver_kw):
     """A cubic block of about `n_particles` (8 per cell, jittered) resting on a sticky
-    floor 3 cells up, squeezed by a kinematic plate descending at `plate_speed` whose
-    lower face starts `plate_gap` cells above the block (negative: pressed into it).
-    Returns (solver, plate handle)."""
+    floor `floor_cells` cells up, squeezed by a kinematic plate descending at
+    `plate_speed` whose lower face starts `plate_gap` cells above the block (negative:
+    pressed into it). Returns (solver, plate handle)."""
     from .solver import GridConfig
     grid = GridConfig(n_grid=n_grid, grid_lim=grid_lim)
     dx = grid.dx
     h = 0.5 * dx
     side = max(4, int(round((n_particles ** (1.0 / 3.0)))))
     edge = side * h
-    floor = 3 * dx
+    floor = floor_cells * dx
     c = 0.5 * grid_lim
     ax = np.arange(side) * h + 0.5 * h
     pts = np.stack(np.meshgrid(ax + c - 0.5 * edge, ax + c - 0.5 * edge, ax + floor, indexing="ij"),

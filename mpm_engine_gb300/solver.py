@@ -328,6 +328,9 @@ class Solver:
     profile: bool = False
     inversion_policy: str = "warn"
     periodic_x: bool = False
+    # deterministic passes: every operation rounded once and P2G summed per node in
+    # particle order, so runs repeat bit for bit (jelly, water, Newtonian; slower)
+    deterministic: bool = False
     _sim: Any = field(default=None, init=False, repr=False)
     _step: int = field(default=0, init=False, repr=False)
     _tick: int = field(default=0, init=False, repr=False)
@@ -1058,6 +1061,8 @@ class Solver:
             flags |= _abi.TICK_GRAPH
         if self._sim.reorder:
             flags |= _abi.TICK_REORDER
+        if self.deterministic:
+            flags |= _abi.TICK_DETERMINISTIC
         return flags
 
     def step(self, dt: float, substeps: int = 1) -> Solver:
@@ -1438,8 +1443,9 @@ class BatchSolver:
             raise ValueError("BatchSolver needs at least one Solver")
         for s in self.solvers:
             s._require_loaded()
-            if s.sort_interval or s.sparse or s.profile:
-                raise ValueError("sort_interval, sparse and profile are per-Solver features; not in a batch")
+            if s.sort_interval or s.sparse or s.profile or s.deterministic:
+                raise ValueError("sort_interval, sparse, profile and deterministic are per-Solver features; "
+                                 "not in a batch")
         if len({s.fused for s in self.solvers}) != 1:
             raise ValueError("all scenes of a batch must share the fused setting")
         self.lib = _abi.load()

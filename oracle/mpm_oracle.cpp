@@ -119,6 +119,12 @@ inline V3 vnormalize(V3 a) {
     return mkv(0, 0, 0);
 }
 
+// wp.pow in fp32 as its correctly rounded value: the power is evaluated in double
+// and rounded once to Real. That is the correctly rounded powf except when the
+// exact power lies within about one double ulp of a float rounding boundary (a
+// chance near 2^-28 per call), so every libm, and a GPU doing the same, agree.
+inline Real powr(Real x, Real y) { return (Real)std::pow((double)x, (double)y); }
+
 // warp mat*mat: t[i][j] += a[i][k]*b[k][j], k ascending from zero
 inline M3 mmul(const M3& a, const M3& b) {
     M3 t = zero33();
@@ -217,7 +223,7 @@ void svd3_impl(const M3& Fin, M3& U, V3& s, M3& V) {
     for (int g = 0; g < 3; ++g) {
         int a = pr[g][0], b = pr[g][1], col = (g < 2) ? 0 : 1;
         double x = W[a][col], y = W[b][col];
-        double r = std::hypot(x, y);
+        double r = std::sqrt(x * x + y * y);   // O(1) entries: no overflow guard needed
         double c = 1.0, sn = 0.0;
         if (r > 0.0) { c = x / r; sn = y / r; }
         for (int k = 0; k < 3; ++k) {  // rows a, b of W: G W
@@ -258,7 +264,7 @@ M3 stress_fcr(const M3& F, const M3& U, const M3& V, Real J, Real mu, Real lam) 
 // kirchoff_stress_water (mpm_utils.py:17-25)
 M3 stress_water(Real J, Real bulk) {
     const Real gamma = 1.1f;
-    Real pressure = -bulk * (std::pow(J, -gamma) - 1.0f);
+    Real pressure = -bulk * (powr(J, -gamma) - 1.0f);
     M3 c = mscale(ident33(), pressure);
     return mscale(c, J);
 }
@@ -275,17 +281,17 @@ void dev_rate(const M3& L, M3& Ddev, Real& gd) {
 // kirchoff_stress_newtonian (mpm_utils.py:27-54)
 M3 stress_newtonian(Real J, Real bulk, const M3& L, Real eta, Real tau_y, Real pk, Real pn) {
     const Real gamma = 1.1f;
-    Real pressure = -bulk * (std::pow(J, -gamma) - 1.0f);
+    Real pressure = -bulk * (powr(J, -gamma) - 1.0f);
     M3 Ddev; Real gd;
     dev_rate(L, Ddev, gd);
-    Real eta_app = eta + tau_y / gd + pk * std::pow(gd, pn - 1.0f);
+    Real eta_app = eta + tau_y / gd + pk * powr(gd, pn - 1.0f);
     M3 c = madd(mscale(ident33(), pressure), mscale(Ddev, 2.0f * eta_app));
     return mscale(c, J);
 }
 // kirchoff_stress_tabulated (mpm_utils.py:56-85)
 M3 stress_tabulated(Real J, Real bulk, const M3& L, const float* table, Real smin, Real smax, int n) {
     const Real gamma = 1.1f;
-    Real pressure = -bulk * (std::pow(J, -gamma) - 1.0f);
+    Real pressure = -bulk * (powr(J, -gamma) - 1.0f);
     M3 Ddev; Real gd;
     dev_rate(L, Ddev, gd);
     Real s = std::log(gd) * 0.43429448190325176f;
@@ -763,7 +769,7 @@ void stress_particle(Ctx& c, int p) {
     else if (mat == 11) F = rm_mu_i_phi(Ft, P, M, p, mat, c.dt);
     else if (mat == 6 || mat == 10 || mat == 12) {
         Real J = mdet(Ft);
-        Real Jc = std::pow(J, 1.0f / 3.0f);
+        Real Jc = powr(J, 1.0f / 3.0f);
         F = diag33(Jc, Jc, Jc);
     } else if (mat == 7 || mat == 8) F = ident33();
     else F = Ft;

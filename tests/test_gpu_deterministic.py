@@ -1,0 +1,116 @@
+"""Deterministic ticks (Solver(deterministic=True)) against the oracle, bit for bit.
+
+The deterministic passes round every operation once, in the order of the fp32
+statement of the reference's kernels, and sum the P2G deposits of each node in
+particle order (sorted records, no float atomics). The oracle run on one thread
+deposits in particle order too. So the two must agree exactly, not within a
+tolerance: x, v, C, F and the stress, compared with np.array_equal after every
+check point. Both sides evaluate powers in double rounded once to float and run
+the SVD in double; they could differ only where a double result falls within a
+double ulp or two of a float rounding boundary (a chance near 2^-28 per power).
+
+The reference's own precedent for bitwise checks is fused == split on one device
+(tests/test_fused_pipeline.py:59-75).
+"""
+import numpy as np
+import pytest
+
+from scenes_lib import MATERIALS, make, spin_velocity
+
+pytestmark = pytest.mark.gpu
+
+NG, LIM = 32, 0.4
+DX = LIM / NG
+
+
+def scene(cls, key, fused=True, n=3000, seed=5, **kw):
+    """A thrown, spinning blob whose lower part starts inside the floor's contact
+    band (a separable floor with friction, 0.3 cells off its node row), inside
+    domain walls, under a descending plate that reaches the blob's top."""
+    rng = np.random.default_rng(seed)
+    pts = (rng.random((n, 3)) * np.array([0.09, 0.09, 0.06]) + np.array([0.15, 0.15, 3.1 * DX])).astype(np.float32)
+    vol = np.full(n, 1.0e-7, np.float32)
+    s = make(cls, NG, LIM, fused=fused, **kw).load_particles(pts, vol)
+    vel = spin_velocity(pts, lin=(0.3, 0.1, -0.6), omega=(0.0, 2.0, 4.0))
+    if cls.__name__ == "OracleSolver":
+        s.a["v"][:] = vel
+    else:
+        s.set_v(vel)
+    mat = MATERIALS[key]
+    if isinstance(mat, str):
+        from scenes_lib import NAME_PARAMS
+        s.set_material(mat, **NAME_PARAMS[mat])
+    else:
+        s.set_material(mat())
+    s.add_plane((0, 0, 3.3 * DX), (0, 0, 1), "separate", friction=0.3)
+    s.add_domain_walls()
+    s.add_box((0.196, 0.196, 3.1 * DX + 0.06 + 0.3 * DX + 0.01), (0.07, 0.07, 0.01), velocity=(0.0, 0.0, -1.5))
+    return s
+
+
+def fields(side):
+    if hasattr(side, "a"):
+        a = side.a
+        return {"x": a["x"], "v": a["v"], "C": a["C"], "F": a["F"], "stress": a["stress"]}
+    t = side._t
+    return {k: t[k].detach().cpu().numpy() for k in ("x", "v", "C", "F", "stress")}
+
+
+def assert_bitwise(s, o, what):
+    g, r = fields(s), fields(o)
+    bad = {}
+    for k in g:
+        a = np.asarray(g[k], np.float32).reshape(len(r["x"]), -1)
+        b = np.asarray(r[k], np.float32).reshape(len(r["x"]), -1)
+        if not np.array_equal(a.view(np.uint32), b.view(np.uint32)):
+            diff = np.abs(a.astype(np.float64) - b.astype(np.float64)).max(axis=1)
+            bad[k] = {"particles": int((a.view(np.uint32) != b.view(np.uint32)).any(axis=1).sum()),
+                      "max_abs": float(diff.max()), "first": int(np.argmax(diff > 0) if diff.max() > 0 else -1)}
+    assert not bad, f"{what}: not bitwise equal: {bad}"
+
+
+@pytest.mark.parametrize("key,fused", [("newtonian", True), ("jelly", True), ("water", True),
+                                       ("herschel_bulkley", True), ("newtonian", False), ("jelly", False)])
+def test_deterministic_ticks_equal_oracle_bitwise(cuda, oracle_lib, key, fused):
+    from mpm_engine_gb300 import Solver
+    s = scene(Solver, key, fused=fused, deterministic=True)
+    o = oracle_lib.OracleSolver.from_state(s.export_state(), NG, LIM, fused=fused, threads=1)
+    dt = 1.0e-4
+    k = 0
+    for n in (1, 4, 15, 30):
+        s.step(dt, n)
+        o.step(dt, n)
+        k += n
+        assert_bitwise(s, o, f"{key} ({'fused' if fused else 'split'}) after {k} substeps")
+
+
+def test_deterministic_ticks_repeat_bitwise_and_match_the_fast_path(cuda):
+    """Two deterministic runs from one state, one through a captured CUDA graph and
+    one launched live, give the same bits; the tiled path from the same state stays
+    within the parity contract (k x 1e-5) of them."""
+    from mpm_engine_gb300 import Solver
+    from test_gpu_parity import assert_close
+
+    a = scene(Solver, "jelly", deterministic=True)   # the scenes are built identically
+    b = scene(Solver, "jelly", deterministic=True)
+    b._sim.use_cuda_graph = False
+    c = scene(Solver, "jelly")
+    for side in (a, b, c):
+        side.step(1.0e-4, 10)
+    fa, fb = fields(a), fields(b)
+    for k in fa:
+        assert np.array_equal(np.asarray(fa[k]).view(np.uint32), np.asarray(fb[k]).view(np.uint32)), k
+
+    class _View:   # the deterministic run, read as the parity helpers read the oracle
+        def __init__(self, f):
+            self.a = f
+            self.dx = DX
+    view = _View({"x": a.x(), "v": a.v(), "C": a.C(), "F": a.F()})
+    assert_close(c, view, 10 * 1e-5, "tiled path against the deterministic passes after 10 substeps")
+
+
+def test_deterministic_ticks_reject_unsupported_materials(cuda):
+    from mpm_engine_gb300 import Solver
+    s = scene(Solver, "metal", deterministic=True)
+    with pytest.raises(NotImplementedError, match="deterministic"):
+        s.step(1.0e-4, 1)
