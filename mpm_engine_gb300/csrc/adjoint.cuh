@@ -215,8 +215,7 @@ __device__ int mui_return(const AdjK &a, int mat, const float *Ft, float mu, flo
     m.Ic = T.d[mat] * sqrtf(T.rho_s[mat] / m.pC);
     m.gdp = (mat == 13) ? mu_i_bisect<true>(m.tbK, mu, a.dt, m.pK, m.Ic, 0.0f, 0.0f, 0.0f, a.eta_tab, a.eta_n,
                                             a.eta_smin, a.eta_smax)
-                        : mu_i_bisect<false>(m.tbK, mu, a.dt, m.pK, m.Ic, T.mu_s[mat], T.dmu[mat], T.I0[mat],
-                                             a.eta_tab, a.eta_n, a.eta_smin, a.eta_smax);
+                        : mu_i_root(m.tbK, mu, a.dt, m.pK, m.Ic, T.mu_s[mat], T.dmu[mat], T.I0[mat]);
     m.sc = (m.tbK - mu * a.dt * m.gdp) / fmaxf(m.tbK, 1e-20f);
     udvt(U, expf(m.d[0] * m.sc + m.mean), expf(m.d[1] * m.sc + m.mean), expf(m.d[2] * m.sc + m.mean), V, Fp);
     return 2;
@@ -320,8 +319,7 @@ __device__ int muiphi_return(const AdjK &a, const float *Ft, float mu, float jp,
     m.tbK = 2.0f * mu * m.dn / sqrtf(2.0f);
     if (!(m.tbK > T.mu_s[mat] * m.pK)) return 1;
     m.Ic = T.d[mat] * sqrtf(T.rho_s[mat] / m.pc);
-    m.gdp = mu_i_bisect<false>(m.tbK, mu, a.dt, m.pK, m.Ic, T.mu_s[mat], T.dmu[mat], T.I0[mat], a.eta_tab, a.eta_n,
-                               a.eta_smin, a.eta_smax);
+    m.gdp = mu_i_root(m.tbK, mu, a.dt, m.pK, m.Ic, T.mu_s[mat], T.dmu[mat], T.I0[mat]);
     m.Ir = m.gdp * m.Ic;
     m.dgam = fminf(8.0f * m.gdp * a.dt, 1.0f);
     m.q = 1.0f - T.phi_chi[mat] * m.Ir / (m.Ir + T.I0[mat]);

@@ -139,7 +139,7 @@ IDENT_PLATE_GAP = -0.37   # plate face 0.37 cells into the block, between node r
 
 
 def identification_errors(floor_cells=IDENT_FLOOR_CELLS, plate_gap=IDENT_PLATE_GAP, steps=STEPS, tol=TOL,
-                          ys0=100.0, reference="f64"):
+                          ys0=100.0, reference="f64", linearized=True):
     """One scene of the batched identification workload at its full length: a von
     Mises cube of about 50k particles on a 48^3 grid, resting on a sticky floor and
     squeezed by a plate pressed into its top at 0.05 m/s, 400 substeps of 1e-5 s with
@@ -197,6 +197,16 @@ def identification_errors(floor_cells=IDENT_FLOOR_CELLS, plate_gap=IDENT_PLATE_G
          "v0": float((v0.grad.double().cpu().numpy() * d).sum())}
     xt = x_t.cpu().numpy()
     bn = b.cpu().numpy()
+    # the loss linearised at the engine's trajectory: the same cotangents the adjoint
+    # starts from, 2 (x - x_target) and 2 (F - F_target), as fixed weights
+    wx = 2.0 * (x.detach().double() - x_t).cpu().numpy()
+    wF = 2.0 * (F.detach().double() - F_tt).cpu().numpy()
+
+    def value(xo, Fo, vo):
+        xo, Fo, vo = (np.asarray(a, np.float64) for a in (xo, Fo, vo))
+        if linearized:
+            return float((wx * xo).sum() + (wF * Fo).sum() + (bn * vo).sum())
+        return float(((xo - xt) ** 2).sum() + ((Fo - F_t) ** 2).sum() + (vo * bn).sum())
 
     def loss32(E_, nu_, ys_, dv=None, vel=vel0):
         adjoint._restore(s, snap)
@@ -207,8 +217,7 @@ def identification_errors(floor_cells=IDENT_FLOOR_CELLS, plate_gap=IDENT_PLATE_G
             x_, v_, F_ = adjoint.rollout(s, dt, K5, v0=v_init, E=torch.tensor(E_, **f), nu=torch.tensor(nu_, **f),
                                          yield_stress=torch.tensor(ys_, **f), checkpoint_every=every, plate=hp,
                                          plate_velocity=pvel)
-        val = float(((x_.double() - x_t) ** 2).sum() + ((F_ - F_tt) ** 2).sum() + (v_.double() * b).sum())
-        return val, float(pvel[2])
+        return value(x_.cpu().numpy(), F_.cpu().numpy(), v_.cpu().numpy()), float(pvel[2])
 
     def loss64(E_, nu_, ys_, dv=None, vel=vel0):
         if reference == "f32":
@@ -225,8 +234,7 @@ def identification_errors(floor_cells=IDENT_FLOOR_CELLS, plate_gap=IDENT_PLATE_G
             o.reset_wrench(hp)
             o.step(dt, every)
             Fs.append(o.wrench_of(hp, dt * every)["force"])
-        val = float(((o.a["x"] - xt) ** 2).sum() + ((np.array(Fs) - F_t) ** 2).sum() + (o.a["v"] * bn).sum())
-        return val, float(o.cols[o.handles[hp]].velocity[2])
+        return value(o.a["x"], np.array(Fs), o.a["v"]), float(o.cols[o.handles[hp]].velocity[2])
 
     def fd(p, h):
         if p == "E":

@@ -186,7 +186,8 @@ def _press(**kw):
 
 def test_press_full_size_parity_per_substep(cuda, oracle_lib):
     """The granular press at its measured size (1,978,257 mu(I) grains on 256^3,
-    sparse mode: the split passes, as the reference runs it), held to the parity
+    sparse mode; the engine runs it on the fused schedule and the oracle on the split
+    one, as the reference does, and the two schedules compute the same substep), held to the parity
     contract of the small granular scenes. Those scenes start pre-strained and thrown,
     and so does this one. The heap is pre-strained to F0 = [[0.97, 0.1, 0],
     [0, 0.97, 0], [0, 0, 0.97]], which puts every grain clearly in one branch of the
