@@ -352,31 +352,52 @@ def flood_measure(n_grid: int = 128, frames: int = 3, warmup: int = 2, device: s
 
 def adjoint_measure(n_scenes: int = 32, n_particles: int = 50_000, n_grid: int = 48, substeps: int = 400,
                     every: int = 20, dt: float = 1.0e-5, device: str = "cuda:0", seed: int = 0):
-    """Batched forward+adjoint workload: n_scenes von Mises cubes of about
-    n_particles (8 per cell, jittered) on n_grid^3 grids, squeezed by a plate at
-    0.05 m/s; per scene seeded E log-uniform [1e4, 1e6], nu in [0.2, 0.45], yield
-    log-uniform [1e2, 1e4]. One scene = a rollout of `substeps` substeps and its
-    reverse pass (checkpoints every `every` substeps) for L = sum(a x) + sum(b v).
-    Plain runs the scenes one after another; batched runs all forwards in one CUDA
-    graph per segment and the reverse passes on one stream per scene."""
+    """Batched forward+adjoint workload (the identification loss): n_scenes von Mises
+    cubes of about n_particles (8 per cell, jittered) on n_grid^3 grids, squeezed by
+    a plate at 0.05 m/s; per scene seeded E log-uniform [1e4, 1e6], nu in
+    [0.2, 0.45], yield log-uniform [1e2, 1e4]. Each scene has a seeded target rollout
+    (E, nu and the yield 30 %, 5 % and 30 % higher; run once, untimed). One scene =
+    a rollout of `substeps` substeps with checkpoints every `every`, the loss
+    L = |x - x_target|^2 + |F - F_target|^2 over the final positions and the plate's
+    per-segment reaction-force trace, and the reverse pass to v0, E, nu, the yield
+    and the plate's velocity. Plain runs the scenes one after another; batched runs
+    all forwards in one CUDA graph per segment and the reverse passes on one stream
+    per scene."""
     import torch
     from mpm_engine_gb300 import Solver, adjoint
     from mpm_engine_gb300.materials import vonmises
     from mpm_engine_gb300.scenes import squeeze_scene
     rng = np.random.default_rng(seed)
-    scenes = []
+    params = []
     for i in range(n_scenes):
         E = float(np.exp(rng.uniform(np.log(1e4), np.log(1e6))))
         nu = float(rng.uniform(0.2, 0.45))
         ys = float(np.exp(rng.uniform(np.log(1e2), np.log(1e4))))
-        s, _ = squeeze_scene(Solver, n_particles, n_grid, vonmises(E=E, nu=nu, yield_stress=ys, density=1000.0),
-                             seed=i, device=device)
-        scenes.append(s)
-    starts = [adjoint._snapshot(s) for s in scenes]
-    weights = [(torch.randn(s.n_particles, 3, device=device), torch.randn(s.n_particles, 3, device=device))
-               for s in scenes]
+        params.append((E, nu, ys))
 
+    def build(scale):
+        out, handles = [], []
+        for i, (E, nu, ys) in enumerate(params):
+            s, h = squeeze_scene(Solver, n_particles, n_grid,
+                                 vonmises(E=E * scale[0], nu=nu * scale[1], yield_stress=ys * scale[2],
+                                          density=1000.0), seed=i, device=device)
+            out.append(s)
+            handles.append(h)
+        return out, handles
+
+    targets, th = build((1.3, 1.05, 1.3))
+    tr = adjoint.BatchRollout(targets, dt, substeps, every, batched=True, plates=th)
+    target_out = tr.forward()
+    x_t = [o[0].double() for o in target_out]
+    F_t = [o[2] for o in target_out]
+    del tr, targets
+    scenes, handles = build((1.0, 1.0, 1.0))
+    starts = [adjoint._snapshot(s) for s in scenes]
     split = {}
+
+    def cotangents(outs):
+        return ([2.0 * (o[0].double() - xt) for o, xt in zip(outs, x_t)], [None] * len(outs),
+                [2.0 * (o[2] - ft) for o, ft in zip(outs, F_t)])
 
     def run(batched, k):
         for s, st in zip(scenes, starts):
@@ -385,19 +406,28 @@ def adjoint_measure(n_scenes: int = 32, n_particles: int = 50_000, n_grid: int =
         t0 = time.perf_counter()
         t_fwd = 0.0
         if batched:
-            r = adjoint.BatchRollout(scenes, dt, k, every, batched=True)
-            r.forward()
+            r = adjoint.BatchRollout(scenes, dt, k, every, batched=True, plates=handles)
+            outs = r.forward()
             torch.cuda.synchronize()
             t_fwd = time.perf_counter() - t0
-            r.backward([w[0] for w in weights], [w[1] for w in weights])
+            if k == substeps:
+                xb, vb, fb = cotangents(outs)
+            else:   # warm-up: any cotangent
+                xb, vb, fb = [o[0] for o in outs], [None] * len(outs), [o[2] for o in outs]
+            r.backward(xb, vb, fb)
         else:
-            for s, w in zip(scenes, weights):
+            for i, s in enumerate(scenes):
                 t1 = time.perf_counter()
-                r = adjoint.BatchRollout([s], dt, k, every, batched=False)
-                r.forward()
+                r = adjoint.BatchRollout([s], dt, k, every, batched=False, plates=[handles[i]])
+                out = r.forward()[0]
                 torch.cuda.synchronize()
                 t_fwd += time.perf_counter() - t1
-                r.backward([w[0]], [w[1]])
+                if k == substeps:
+                    xb = 2.0 * (out[0].double() - x_t[i])
+                    fb = 2.0 * (out[2] - F_t[i])
+                else:
+                    xb, fb = out[0], out[2]
+                r.backward([xb], [None], [fb])
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
         split["batched" if batched else "plain"] = {"forward_s": t_fwd, "backward_s": el - t_fwd}
@@ -411,7 +441,9 @@ def adjoint_measure(n_scenes: int = 32, n_particles: int = 50_000, n_grid: int =
     return {"metric": "batched forward+adjoint scenes/s", "unit": f"scenes/s ({substeps} substeps each)",
             "value": n_scenes / t_batch, "plain_value": n_scenes / t_plain, "speedup_vs_plain": t_plain / t_batch,
             "scenes": n_scenes, "particles_total": n_total, "grid": f"{n_grid}^3", "substeps": substeps,
-            "checkpoint_every": every, "dt": dt, "seconds": split,
+            "checkpoint_every": every, "dt": dt,
+            "loss": "|x - x_target|^2 + |plate force trace - target trace|^2 (seeded target rollouts)",
+            "gradients": ["v0", "mu and lam (so E and nu)", "yield_stress", "plate_velocity"], "seconds": split,
             "particle_substeps_per_s": n_total * substeps / t_batch}
 
 

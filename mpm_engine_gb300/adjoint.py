@@ -86,7 +86,9 @@ def _forward(s, dt, substeps, every, plate=None):
     return (ckpts, forces) if plate is not None else ckpts
 
 
-def _backward(s, dt, ckpts, xb, vb, plate=None, force_bar=None):
+def _adj_setup(s, xb, vb, plate, kmax):
+    """The adjoint arrays of one scene's reverse pass (seeded with the final-state
+    adjoints xb, vb) and their ABI record; with a plate also its collider buffers."""
     torch = _torch()
     n = s.n_particles
     dev = s._t["x"].device
@@ -99,30 +101,44 @@ def _backward(s, dt, ckpts, xb, vb, plate=None, force_bar=None):
         "L": torch.zeros(n, 3, 3, **f), "viscosity": torch.zeros(n, **f), "Jp": torch.zeros(n, **f),
     }
     rec = _abi.AdjGrads(**{k: g[k].data_ptr() for k in g})
-    lib, h = s._eng.lib, s._eng.h
     ncol = max(1, len(s._cols))
     col = s._col(plate) if plate is not None else None
+    fb = None
     if col is not None:
         g["collider_velocity"] = torch.zeros(ncol, 3, **f)
         rec.collider_velocity = g["collider_velocity"].data_ptr()
         # one buffer for every segment, so the engine's captured segment graph (keyed
         # on the adjoint arrays) is reused; each segment rewrites it in stream order
-        fb = torch.zeros(max(k for _, k in ckpts), ncol, 3, **f)
+        fb = torch.zeros(kmax, ncol, 3, **f)
         rec.collider_force = fb.data_ptr()
-    for j in reversed(range(len(ckpts))):
-        snap, k = ckpts[j]
-        _restore(s, snap)
-        if col is not None:
-            # the segment's force is sum_substeps sum_nodes m (v_free - v_box) / (dt k)
-            fb.zero_()
-            if force_bar is not None:
-                fb[:k, col, :] = force_bar[j].to(**f) / (dt * k)
-        t = C.c_double(s._time)
-        _abi.check(lib.gbmpm_adjoint_segment(h, C.byref(t), float(dt), int(k), C.byref(rec), s._stream()),
-                   "gbmpm_adjoint_segment")
+    return g, rec, fb, col
+
+
+def _adj_segment(s, dt, rec, snap, k, fb, col, force_bar_j):
+    """Replays one checkpoint segment and runs its reverse substeps (stream order)."""
+    _restore(s, snap)
+    if col is not None:
+        # the segment's force is sum_substeps sum_nodes m (v_free - v_box) / (dt k)
+        fb.zero_()
+        if force_bar_j is not None:
+            fb[:k, col, :] = force_bar_j.to(device=fb.device, dtype=fb.dtype) / (dt * k)
+    t = C.c_double(s._time)
+    _abi.check(s._eng.lib.gbmpm_adjoint_segment(s._eng.h, C.byref(t), float(dt), int(k), C.byref(rec), s._stream()),
+               "gbmpm_adjoint_segment")
+
+
+def _adj_finish(g, col):
     if col is not None:
         g["plate_velocity"] = g["collider_velocity"][col].clone()
     return g
+
+
+def _backward(s, dt, ckpts, xb, vb, plate=None, force_bar=None):
+    g, rec, fb, col = _adj_setup(s, xb, vb, plate, max(k for _, k in ckpts))
+    for j in reversed(range(len(ckpts))):
+        snap, k = ckpts[j]
+        _adj_segment(s, dt, rec, snap, k, fb, col, None if force_bar is None else force_bar[j])
+    return _adj_finish(g, col)
 
 
 NEWTONIAN = 10   # material id whose per-type viscosity `viscosity` sets
@@ -225,14 +241,20 @@ class BatchRollout:
     and parameters define its rollout. With `batched` the forward advances all
     scenes in one CUDA graph per segment (BatchSolver) and the reverse pass runs
     each scene's segments on its own stream; otherwise scenes run one after
-    another, as serial rollouts would."""
+    another, as serial rollouts would. `plates` (one add_box handle or None per
+    scene) adds each plate's reaction-force trace to the outputs, one force per
+    checkpoint segment, and its adjoint to the reverse pass."""
 
-    def __init__(self, solvers, dt: float, substeps: int, checkpoint_every: int = 20, batched: bool = True):
+    def __init__(self, solvers, dt: float, substeps: int, checkpoint_every: int = 20, batched: bool = True,
+                 plates=None):
         torch = _torch()
         from .solver import BatchSolver
         self.solvers = list(solvers)
         for s in self.solvers:
             _check(s)
+        self.plates = list(plates) if plates is not None else [None] * len(self.solvers)
+        if len(self.plates) != len(self.solvers):
+            raise ValueError("one plate handle (or None) per scene")
         self.dt, self.substeps, self.every = float(dt), int(substeps), int(checkpoint_every)
         self.batched = batched
         self.batch = BatchSolver(self.solvers) if batched else None
@@ -240,9 +262,17 @@ class BatchRollout:
         self.ckpts = None
 
     def forward(self):
-        """Runs every rollout; returns [(x, v)] at the end."""
+        """Runs every rollout; returns [(x, v)] at the end, or [(x, v, F)] with the
+        force trace F ((segments, 3) float64) of the scenes that have a plate."""
+        torch = _torch()
+        forces = [[] for _ in self.solvers]
         if not self.batched:
-            self.ckpts = [_forward(s, self.dt, self.substeps, self.every) for s in self.solvers]
+            self.ckpts = []
+            for i, s in enumerate(self.solvers):
+                r = _forward(s, self.dt, self.substeps, self.every, self.plates[i])
+                if self.plates[i] is not None:
+                    r, forces[i] = r
+                self.ckpts.append(r)
         else:
             self.ckpts = [[] for _ in self.solvers]
             done = 0
@@ -250,46 +280,49 @@ class BatchRollout:
                 k = min(self.every, self.substeps - done)
                 for i, s in enumerate(self.solvers):
                     self.ckpts[i].append((_snapshot(s), k))
+                    if self.plates[i] is not None:
+                        s.reset_tool_force(self.plates[i])
                 self.batch.step(self.dt, k)
+                for i, s in enumerate(self.solvers):
+                    if self.plates[i] is not None:
+                        forces[i].append(s.tool_force(self.plates[i], self.dt * k))
                 done += k
         self.final = [_snapshot(s) for s in self.solvers]
-        return [(s._t["x"].clone(), s._t["v"].clone()) for s in self.solvers]
+        out = []
+        for i, s in enumerate(self.solvers):
+            xv = (s._t["x"].clone(), s._t["v"].clone())
+            if self.plates[i] is not None:
+                xv = xv + (torch.tensor(np.array(forces[i]), dtype=torch.float64, device=s._t["x"].device),)
+            out.append(xv)
+        return out
 
-    def backward(self, xbs, vbs):
+    def backward(self, xbs, vbs, force_bars=None):
         """Adjoints of the rollouts' starting states and parameters for the given
-        adjoints of their final (x, v): [{'v', 'x', 'C', 'F_trial', 'L',
-        'yield_stress', 'mu', 'lam', 'viscosity'}]. Leaves every solver at its
+        adjoints of their final (x, v) and of their force traces: [{'v', 'x', 'C',
+        'F_trial', 'L', 'yield_stress', 'mu', 'lam', 'viscosity'}, plus
+        'plate_velocity' where a scene has a plate]. Leaves every solver at its
         rollout's end state."""
         torch = _torch()
         if self.ckpts is None:
             raise RuntimeError("forward must run first")
+        fbars = list(force_bars) if force_bars is not None else [None] * len(self.solvers)
         if not self.batched:
-            out = [_backward(s, self.dt, ck, xb, vb) for s, ck, xb, vb in zip(self.solvers, self.ckpts, xbs, vbs)]
+            out = [_backward(s, self.dt, ck, xb, vb, pl, fbar)
+                   for s, ck, xb, vb, pl, fbar in zip(self.solvers, self.ckpts, xbs, vbs, self.plates, fbars)]
         else:
             torch.cuda.synchronize()
-            gs, recs = [], []
-            for s, xb, vb in zip(self.solvers, xbs, vbs):
-                n = s.n_particles
-                f = dict(device=s._t["x"].device, dtype=torch.float32)
-                g = {"x": xb.detach().to(**f).reshape(n, 3).clone(), "v": vb.detach().to(**f).reshape(n, 3).clone(),
-                     "C": torch.zeros(n, 3, 3, **f), "F_trial": torch.zeros(n, 3, 3, **f),
-                     "yield_stress": torch.zeros(n, **f), "mu": torch.zeros(n, **f), "lam": torch.zeros(n, **f),
-                     "L": torch.zeros(n, 3, 3, **f), "viscosity": torch.zeros(n, **f), "Jp": torch.zeros(n, **f)}
-                gs.append(g)
-                recs.append(_abi.AdjGrads(**{k: g[k].data_ptr() for k in g}))
+            setups = [_adj_setup(s, xb, vb, pl, max(k for _, k in ck))
+                      for s, ck, xb, vb, pl in zip(self.solvers, self.ckpts, xbs, vbs, self.plates)]
             torch.cuda.synchronize()
             nseg = len(self.ckpts[0])
             for j in reversed(range(nseg)):
                 for i, s in enumerate(self.solvers):
                     snap, k = self.ckpts[i][j]
+                    g, rec, fb, col = setups[i]
                     with torch.cuda.stream(self.streams[i]):
-                        _restore(s, snap)
-                        t = C.c_double(s._time)
-                        _abi.check(s._eng.lib.gbmpm_adjoint_segment(s._eng.h, C.byref(t), self.dt, int(k),
-                                                                    C.byref(recs[i]), s._stream()),
-                                   "gbmpm_adjoint_segment")
+                        _adj_segment(s, self.dt, rec, snap, k, fb, col, None if fbars[i] is None else fbars[i][j])
             torch.cuda.synchronize()
-            out = gs
+            out = [_adj_finish(g, col) for g, rec, fb, col in setups]
         for s, snap in zip(self.solvers, self.final):
             _restore(s, snap)
         return out

@@ -65,7 +65,25 @@ struct AdjK {
     // velocity ([ncol][3], or null)
     const float *col_force_b;
     float *col_vel_b;
+    // node box of the segment ({lo x, y, z, hi x, y, z}, inclusive): every stencil of
+    // the segment's particles lies inside it, so the grid kernels visit only it
+    const int *box;
 };
+
+// the index-th node of the segment's box
+__device__ __forceinline__ bool box_node(const int *box, size_t index, int ng, int &gx, int &gy, int &gz, size_t &id) {
+    const int ex = box[3] - box[0] + 1, ey = box[4] - box[1] + 1, ez = box[5] - box[2] + 1;
+    if (ex <= 0 || ey <= 0 || ez <= 0 || index >= (size_t)ex * ey * ez) return false;
+    gz = box[2] + (int)(index % ez);
+    gy = box[1] + (int)((index / ez) % ey);
+    gx = box[0] + (int)(index / ((size_t)ez * ey));
+    id = ((size_t)gx * ng + gy) * ng + gz;
+    return true;
+}
+__device__ __forceinline__ size_t box_count(const int *box) {
+    const int ex = box[3] - box[0] + 1, ey = box[4] - box[1] + 1, ez = box[5] - box[2] + 1;
+    return (ex <= 0 || ey <= 0 || ez <= 0) ? 0 : (size_t)ex * ey * ez;
+}
 
 // c = a^T b
 __device__ __forceinline__ void mTm(const float *a, const float *b, float *c) {
@@ -597,13 +615,58 @@ __device__ __forceinline__ void grid_pre(const AdjK &a, float4 mv, float *v) {
     if (a.damp < 1.0f) { v[0] *= a.damp; v[1] *= a.damp; v[2] *= a.damp; }
 }
 
+// The segment's node box: every particle stencil of every saved substep state
+// (base cell to base + 2 per axis), as an inclusive node range clamped to the grid.
+__global__ void k_adj_box_init(int *box, int ng) {
+    if (threadIdx.x == 0) { box[0] = box[1] = box[2] = ng; box[3] = box[4] = box[5] = -1; }
+}
+__global__ void k_adj_box(const float *states, size_t per, int n, int substeps, float inv_dx, int ng, int *box) {
+    int lo[3] = {ng, ng, ng}, hi[3] = {-1, -1, -1};
+    const size_t total = (size_t)n * substeps;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = t / n, p = t % n;
+        const float *x = states + per * i + 3 * p;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int b = (int)floorf(x[d] * inv_dx - 0.5f);
+            lo[d] = min(lo[d], max(b, 0));
+            hi[d] = max(hi[d], min(b + 2, ng - 1));
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[d] = min(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+            hi[d] = max(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) { atomicMin(box + d, lo[d]); atomicMax(box + 3 + d, hi[d]); }
+    }
+}
+// zero the accumulated grids (momentum and mass, the velocity adjoint) inside the box
+__global__ void k_adj_zero_box(AdjK a) {
+    const size_t N = box_count(a.box);
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < N; t += (size_t)gridDim.x * blockDim.x) {
+        int gx, gy, gz;
+        size_t id;
+        if (!box_node(a.box, t, a.ng, gx, gy, gz, id)) break;
+        a.gmv[id] = make_float4(0.f, 0.f, 0.f, 0.f);
+        a.gvb[id] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
 __global__ void k_adj_grid_fwd(AdjK a) {
-    const size_t N = (size_t)a.ng * a.ng * a.ng;
+    const size_t N = box_count(a.box);
     const GK gk = adj_gk(a);
-    for (size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x; id < N; id += (size_t)gridDim.x * blockDim.x) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < N; t += (size_t)gridDim.x * blockDim.x) {
+        int gx, gy, gz;
+        size_t id;
+        if (!box_node(a.box, t, a.ng, gx, gy, gz, id)) break;
         const float4 mv = a.gmv[id];
         if (mv.w == 0.0f) { a.gv[id] = make_float4(0.f, 0.f, 0.f, 0.f); continue; }
-        const int gz = (int)(id % a.ng), gy = (int)((id / a.ng) % a.ng), gx = (int)(id / ((size_t)a.ng * a.ng));
         float v[3], acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         grid_pre(a, mv, v);
         for (int c = 0; c < a.ncol; ++c)
@@ -830,12 +893,14 @@ __device__ void collide_adj(const ColDev &c, const PoseRec &P, int gx, int gy, i
 }
 
 __global__ void k_adj_grid_bwd(AdjK a) {
-    const size_t N = (size_t)a.ng * a.ng * a.ng;
+    const size_t N = box_count(a.box);
     const GK gk = adj_gk(a);
-    for (size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x; id < N; id += (size_t)gridDim.x * blockDim.x) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < N; t += (size_t)gridDim.x * blockDim.x) {
+        int gx, gy, gz;
+        size_t id;
+        if (!box_node(a.box, t, a.ng, gx, gy, gz, id)) break;
         const float4 mv = a.gmv[id];
         if (!(mv.w > 1e-15f)) { a.gmb[id] = make_float4(0.f, 0.f, 0.f, 0.f); continue; }
-        const int gz = (int)(id % a.ng), gy = (int)((id / a.ng) % a.ng), gx = (int)(id / ((size_t)a.ng * a.ng));
         float vin[kMaxCol][3], v[3], acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         grid_pre(a, mv, v);
         for (int c = 0; c < a.ncol; ++c) {
@@ -1341,7 +1406,14 @@ cudaError_t record_adjoint_segment(gbmpm_engine *e, float dtf, int substeps, con
     }
     float4 *grid = e->adj_grid.ptr;
     const int pb = std::max(1, (n + 127) / 128);
-    const int gb = e->num_sms * 8;
+    // the grid kernels stride over the segment's node box; sized for the whole grid
+    // at most, so that the scenes of a batch run side by side
+    const int gb = (int)std::max<size_t>(1, std::min<size_t>((size_t)e->num_sms * 2, (nn + 255) / 256));
+    int *box = e->adj_box.ptr;
+    k_adj_box_init<<<1, 32, 0, s>>>(box, ng);
+    k_adj_box<<<std::max(1, std::min(e->num_sms * 4, (int)(((size_t)n * substeps + 255) / 256))), 256, 0, s>>>(
+        e->adj_states.ptr, per, n, substeps, e->M.inv_dx, ng, box);
+    e->launches += 2;
     for (int i = substeps - 1; i >= 0; --i) {
         const float *st = e->adj_states.ptr + per * i;
         AdjK a{};
@@ -1364,19 +1436,20 @@ cudaError_t record_adjoint_segment(gbmpm_engine *e, float dtf, int substeps, con
         a.col_force_b = gr->collider_force ? gr->collider_force + (size_t)i * 3 * std::max(1, nc) : nullptr;
         a.col_vel_b = gr->collider_velocity;
         a.ncol = nc; a.cols = e->d_cols.ptr; a.poses = e->d_pose.ptr + (size_t)i * std::max(1, nc);
+        a.box = box;
         // the engine's P2G building block reads its inputs through a PK
         gbmpm_particles Ps = P;
         Ps.x = const_cast<float *>(a.x); Ps.v = const_cast<float *>(a.v); Ps.C = const_cast<float *>(a.C);
         PK k = make_pk(e, Ps, dtf, 0);
         k.cdf_on = 0;
-        keep(cudaMemsetAsync(grid, 0, 4 * nn * sizeof(float4), s));
+        k_adj_zero_box<<<gb, 256, 0, s>>>(a);
         k_adj_stress_fwd<<<pb, 128, 0, s>>>(a);
         k_adj_p2g_fwd<<<pb, 128, 0, s>>>(a, k);
         k_adj_grid_fwd<<<gb, 256, 0, s>>>(a);
         k_adj_g2p_bwd<<<pb, 128, 0, s>>>(a);
         k_adj_grid_bwd<<<gb, 256, 0, s>>>(a);
         k_adj_p2g_bwd<<<pb, 128, 0, s>>>(a);
-        e->launches += 6;
+        e->launches += 7;
     }
     return first;
 }
@@ -1404,7 +1477,11 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
     const size_t per = (size_t)37 * n;   // x 3, v 3, C 9, F_trial 9, L 9, yield 1, mu 1, lam 1, Jp 1
     GB_CUDA(e->adj_states.ensure(per * substeps));
     GB_CUDA(e->adj_scratch.ensure((size_t)27 * n));
+    float4 *old_grid = e->adj_grid.ptr;
     GB_CUDA(e->adj_grid.ensure(4 * nn));   // four float4 grids
+    if (e->adj_grid.ptr != old_grid)        // zero once; then each substep zeroes its box
+        GB_CUDA(cudaMemsetAsync(e->adj_grid.ptr, 0, 4 * nn * sizeof(float4), s));
+    GB_CUDA(e->adj_box.ensure(6));
     const float dtf = (float)dt;
     // forward replay on the split schedule: one pose table for the whole segment
     // (the adjoint kernels read the same table), no host synchronization per substep.

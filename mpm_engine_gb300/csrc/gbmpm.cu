@@ -185,6 +185,7 @@ struct gbmpm_engine {
     // adjoint segment storage and scratch (allocated by the first adjoint call)
     DevBuf<float> adj_states, adj_scratch;
     DevBuf<float4> adj_grid;
+    DevBuf<int> adj_box;     // the adjoint segment's node box
     // the launches of one adjoint segment, captured once and replayed while the
     // segment's shape and buffers stay the same (key: substeps, dt, adjoint arrays,
     // engine version)
@@ -899,7 +900,7 @@ void gbmpm_engine_destroy(gbmpm_engine *e) {
     e->ws_idx[1].release(); e->ws_hist.release();
     e->c_tag.release(); e->c_tag_prev.release(); e->c_block.release(); e->c_d.release(); e->c_d_prev.release();
     e->c_wrench.release(); e->c_partial.release(); e->c_cache.release();
-    e->adj_states.release(); e->adj_scratch.release(); e->adj_grid.release();
+    e->adj_states.release(); e->adj_scratch.release(); e->adj_grid.release(); e->adj_box.release();
     e->det_key[0].release(); e->det_key[1].release(); e->det_idx[0].release(); e->det_idx[1].release();
     e->det_val.release(); e->det_hist.release();
     delete e;
