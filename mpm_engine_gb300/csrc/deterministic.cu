@@ -3,8 +3,8 @@
 // Every operation here rounds once: this translation unit is compiled with
 // --fmad=false, so no product is contracted into an FMA, and each expression is
 // written in the operation order of the fp32 statement of the reference's kernels
-// (mpm_utils.py). Powers go through double and are rounded once, and the SVD runs
-// in double. The P2G deposits are not added with atomics: each particle writes its
+// (mpm_utils.py). Logarithms, exponentials and powers are evaluated in double by this
+// file's own method and rounded once, and the SVD runs in double. The P2G deposits are not added with atomics: each particle writes its
 // 27 contributions as records keyed by node, a stable radix sort groups them by
 // node in particle order, and one thread per node adds its group in that order.
 //
@@ -13,9 +13,8 @@
 // It is a verification mode: simple one-thread-per-item kernels over the caller's
 // particle order, several times slower than the tiled path.
 //
-// Scope: jelly (FCR, id 0), water (id 6) and the Newtonian / Bingham /
-// Herschel-Bulkley law (id 10), with plane, box and wall colliders; the host
-// rejects other materials and CDF lanes, rigid bodies and particle modifiers.
+// Scope: every material law (ids 0-2, 5, 6, 9-13), with the grid pass's colliders;
+// the host rejects rigid bodies (7, 8), CDF lanes and particle modifiers.
 #include "common.cuh"
 
 namespace gbmpm {
@@ -55,8 +54,38 @@ __device__ __forceinline__ float d_det(const float *a) {
     const float c2 = a[3] * a[7] - a[4] * a[6];
     return a[0] * c0 + a[1] * c1 + a[2] * c2;
 }
-// wp.pow in fp32 as its correctly rounded value: evaluated in double, rounded once
-__device__ __forceinline__ float d_pow(float x, float y) { return (float)pow((double)x, (double)y); }
+// wp.log, wp.exp and wp.pow in fp32 as their correctly rounded values: evaluated in
+// double by this file's own method, operation by operation, and rounded once. The
+// CPU statement of the same method returns the same double, bit for bit.
+//   log x = k ln2 + 2 atanh(s), x = m 2^k with m in [1/sqrt 2, sqrt 2), s = (m - 1)/(m + 1),
+//           the atanh series to s^23 (|s| <= 0.1716: the next term is below 1e-18);
+//   exp x = 2^k exp(r), k = round(x / ln2), r = x - k ln2 (|r| <= 0.35), the Taylor
+//           series to r^17 in Horner form (the next term is below 1e-22).
+// Measured against the host libm over 2e6 arguments: 3.7e-16 and 9.4e-16 relative.
+__device__ __forceinline__ double d_dlog(double x) {
+    if (!(x > 0.0) || isinf(x)) return (x == 0.0) ? -HUGE_VAL : (isinf(x) ? x : (double)NAN);
+    int k = 0;
+    double m = frexp(x, &k);
+    if (m < 0.70710678118654752440) { m = m * 2.0; k = k - 1; }
+    const double s = (m - 1.0) / (m + 1.0);
+    const double s2 = s * s;
+    double t = 1.0 / 23.0;
+    for (int j = 21; j >= 1; j -= 2) t = 1.0 / (double)j + s2 * t;
+    return (double)k * 0.69314718055994530942 + 2.0 * s * t;
+}
+__device__ __forceinline__ double d_dexp(double x) {
+    if (x != x) return x;
+    if (x > 709.0) return HUGE_VAL;
+    if (x < -745.0) return 0.0;
+    const double kd = floor(x * 1.44269504088896340736 + 0.5);
+    const double r = x - kd * 0.69314718055994530942;
+    double t = 1.0;
+    for (int j = 17; j >= 1; --j) t = 1.0 + r * t / (double)j;
+    return ldexp(t, (int)kd);
+}
+__device__ __forceinline__ float d_log(float x) { return (float)d_dlog((double)x); }
+__device__ __forceinline__ float d_exp(float x) { return (float)d_dexp((double)x); }
+__device__ __forceinline__ float d_pow(float x, float y) { return (float)d_dexp((double)y * d_dlog((double)x)); }
 
 // ---- SVD: this project's cyclic Jacobi eigen-solve of F^T F, then a Givens QR of
 // F V, in double throughout (the tiled path's method, without its FP32 first try)
@@ -142,6 +171,181 @@ __device__ void d_svd3(const float *F, float *U, float *s, float *Vo) {
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) { U[3 * i + j] = (float)Q[i][j]; Vo[3 * i + j] = (float)Vs[i][j]; }
     s[0] = (float)W[0][0]; s[1] = (float)W[1][1]; s[2] = (float)W[2][2];
+}
+
+// U diag(d0, d1, d2) W^T as the reference writes it: full 3x3 products with the zeros
+__device__ __forceinline__ void d_udwt(const float *U, float d0, float d1, float d2, const float *W, float *out) {
+    const float D[9] = {d0, 0.0f, 0.0f, 0.0f, d1, 0.0f, 0.0f, 0.0f, d2};
+    float UD[9], WT[9];
+    d_mmul(U, D, UD);
+    d_trans(W, WT);
+    d_mmul(UD, WT, out);
+}
+__device__ __forceinline__ float d_len3(float a, float b, float c) { return sqrtf(a * a + b * b + c * c); }
+__device__ __forceinline__ float d_max(float a, float b) { return (a < b) ? b : a; }   // std::max
+__device__ __forceinline__ float d_min(float a, float b) { return (b < a) ? b : a; }   // std::min
+
+// a table over [smin, smax] sampled at n points, linear in between (mpm_utils.py:62-70)
+__device__ __forceinline__ float d_table(const float *tab, int n, float smin, float smax, float s) {
+    float idx = (s - smin) / (smax - smin) * (float)(n - 1);
+    idx = d_min(d_max(idx, 0.0f), (float)(n - 1) - 1.0e-6f);
+    const int i0 = (int)floorf(idx);
+    const float fr = idx - (float)i0;
+    return tab[i0] * (1.0f - fr) + tab[i0 + 1] * fr;
+}
+
+// ---- return maps (mpm_utils.py:127-580); each may update the particle's yield, mu,
+// lam or Jp as the reference's do
+// von_mises_return_mapping (:127-170), with_damage (:172-225)
+__device__ void d_rm_von_mises(const PK &k, int p, int mat, bool damage, const float *Ft, float *Fe) {
+    const MatTables &T = *k.tab;
+    float U[9], so[3], V[9];
+    d_svd3(Ft, U, so, V);
+    const float sig[3] = {d_max(so[0], 0.01f), d_max(so[1], 0.01f), d_max(so[2], 0.01f)};
+    float eps[3] = {d_log(sig[0]), d_log(sig[1]), d_log(sig[2])};
+    const float temp = (eps[0] + eps[1] + eps[2]) / 3.0f;
+    const float mu = k.mu[p], lam = k.lam[p];
+    const float tr = eps[0] + eps[1] + eps[2];
+    float tau[3];
+    for (int a = 0; a < 3; ++a) tau[a] = eps[a] * (2.0f * mu) + 1.0f * (lam * tr);
+    const float sum_tau = tau[0] + tau[1] + tau[2];
+    const float cond[3] = {tau[0] - sum_tau / 3.0f, tau[1] - sum_tau / 3.0f, tau[2] - sum_tau / 3.0f};
+    for (int i = 0; i < 9; ++i) Fe[i] = Ft[i];
+    float ys = k.ys[p];
+    if (!(d_len3(cond[0], cond[1], cond[2]) > ys)) return;
+    if (damage && ys <= 0) return;
+    const float eh[3] = {eps[0] - temp, eps[1] - temp, eps[2] - temp};
+    const float ehn = d_len3(eh[0], eh[1], eh[2]) + 1e-6f;
+    const float dg = ehn - ys / (2.0f * mu);
+    const float f = dg / ehn;
+    for (int a = 0; a < 3; ++a) eps[a] = eps[a] - eh[a] * f;
+    if (damage) {
+        ys = ys - T.softening[mat] * d_len3(eh[0] * f, eh[1] * f, eh[2] * f);
+        if (ys <= 0) { k.mu[p] = 0.0f; k.lam[p] = 0.0f; }
+    }
+    d_udwt(U, d_exp(eps[0]), d_exp(eps[1]), d_exp(eps[2]), V, Fe);
+    if (T.hardening[mat] > 0.5f) ys = ys + 2.0f * k.mu[p] * T.xi[mat] * dg;
+    k.ys[p] = ys;
+}
+
+// the 48-step bisection of mu_i_return_mapping (:300-312), as the reference runs it
+__device__ float d_mu_i_bisect(const PK &k, bool tab, float tbK, float G, float pK, float Ic, float mu_s, float dmu,
+                               float I0) {
+    float lo = 0.0f, hi = tbK / (G * k.dt);
+    for (int it = 0; it < 48; ++it) {
+        const float mid = 0.5f * (lo + hi);
+        const float Im = mid * Ic;
+        float mu_mid;
+        if (!tab) mu_mid = mu_s + dmu * Im / (Im + I0);
+        else mu_mid = d_table(k.eta, k.eta_n, k.eta_smin, k.eta_smax, d_log(d_max(Im, 1e-12f)) * 0.43429448190325176f);
+        const float g = tbK - G * k.dt * mid - mu_mid * pK;
+        if (g > 0.0f) lo = mid; else hi = mid;
+    }
+    return 0.5f * (lo + hi);
+}
+
+// mu_i_return_mapping (:246-324) and its tabulated variant (:327-407)
+__device__ void d_rm_mu_i(const PK &k, int p, int mat, bool tab, const float *Ft, float *Fe) {
+    const MatTables &T = *k.tab;
+    float U[9], sig[3], V[9];
+    d_svd3(Ft, U, sig, V);
+    const float sc[3] = {d_max(fabsf(sig[0]), 1e-6f), d_max(fabsf(sig[1]), 1e-6f), d_max(fabsf(sig[2]), 1e-6f)};
+    const float eps[3] = {d_log(sc[0]), d_log(sc[1]), d_log(sc[2])};
+    const float tr = eps[0] + eps[1] + eps[2];
+    for (int i = 0; i < 9; ++i) Fe[i] = Ft[i];
+    if (tr >= 0.0f) {
+        float VT[9];
+        d_trans(V, VT);
+        d_mmul(U, VT, Fe);
+        return;
+    }
+    const float G = k.mu[p], lam = k.lam[p];
+    const float J = sc[0] * sc[1] * sc[2];
+    const float mean = tr / 3.0f;
+    const float d0 = eps[0] - mean, d1 = eps[1] - mean, d2 = eps[2] - mean;
+    const float dn = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+    const float pK = -(2.0f * G / 3.0f + lam) * tr;
+    const float tbK = 2.0f * G * dn / sqrtf(2.0f);
+    const float pC = pK / J;
+    const float mu_s = T.mu_s[mat], dmu = T.dmu[mat], I0 = T.I0[mat];
+    const float thresh = tab ? k.eta[0] : mu_s;
+    if (!(tbK > thresh * pK)) return;
+    const float Ic = T.d[mat] * sqrtf(T.rho_s[mat] / pC);
+    const float gdp = d_mu_i_bisect(k, tab, tbK, G, pK, Ic, mu_s, dmu, I0);
+    const float tbn = tbK - G * k.dt * gdp;
+    const float scale = tbn / d_max(tbK, 1e-20f);
+    d_udwt(U, d_exp(d0 * scale + mean), d_exp(d1 * scale + mean), d_exp(d2 * scale + mean), V, Fe);
+}
+
+// mu_i_phi_pressure (:421-430), j_cs_of_I (:410-418)
+__device__ __forceinline__ float d_mu_i_phi_pressure(const MatTables &T, int mat, float J, float Jr) {
+    const float K = T.E[mat] / (3.0f * (1.0f - 2.0f * T.nu[mat]));
+    const float pr = K * (Jr / d_max(J, 1e-6f) - 1.0f);
+    return d_max(pr, 0.0f);
+}
+
+// mu_i_phi_return_mapping (:433-522)
+__device__ void d_rm_mu_i_phi(const PK &k, int p, int mat, const float *Ft, float *Fe) {
+    const MatTables &T = *k.tab;
+    float U[9], sig[3], V[9];
+    d_svd3(Ft, U, sig, V);
+    const float sc[3] = {d_max(fabsf(sig[0]), 1e-6f), d_max(fabsf(sig[1]), 1e-6f), d_max(fabsf(sig[2]), 1e-6f)};
+    const float eps[3] = {d_log(sc[0]), d_log(sc[1]), d_log(sc[2])};
+    const float J = sc[0] * sc[1] * sc[2];
+    const float tr = eps[0] + eps[1] + eps[2];
+    const float mean = tr / 3.0f;
+    const float d0 = eps[0] - mean, d1 = eps[1] - mean, d2 = eps[2] - mean;
+    const float dn = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+    const float G = k.mu[p];
+    float Jr = k.Jp[p];
+    if (Jr < 0.5f) Jr = 1.0f;
+    const float pc = d_mu_i_phi_pressure(T, mat, J, Jr);
+    const float beta = 8.0f;
+    for (int i = 0; i < 9; ++i) Fe[i] = Ft[i];
+    k.Jp[p] = Jr;
+    if (pc <= 0.0f) {
+        const float si = d_exp(mean);
+        d_udwt(U, si, si, si, V, Fe);
+        return;
+    }
+    const float pK = pc * J;
+    const float tbK = 2.0f * G * dn / sqrtf(2.0f);
+    const float mu_s = T.mu_s[mat], dmu = T.dmu[mat], I0 = T.I0[mat];
+    if (!(tbK > mu_s * pK)) return;
+    const float Ic = T.d[mat] * sqrtf(T.rho_s[mat] / pc);
+    const float gdp = d_mu_i_bisect(k, false, tbK, G, pK, Ic, mu_s, dmu, I0);
+    const float Ir = gdp * Ic;
+    const float dgam = d_min(beta * gdp * k.dt, 1.0f);
+    const float denom = d_max(1.0f - T.phi_chi[mat] * Ir / (Ir + I0), 1e-3f);
+    const float jcs = 1.0f / denom;
+    k.Jp[p] = Jr + dgam * (jcs - Jr);
+    const float tbn = tbK - G * k.dt * gdp;
+    const float scale = tbn / d_max(tbK, 1e-20f);
+    d_udwt(U, d_exp(d0 * scale + mean), d_exp(d1 * scale + mean), d_exp(d2 * scale + mean), V, Fe);
+}
+
+// sand_return_mapping (:543-580)
+__device__ void d_rm_sand(const PK &k, int p, int mat, const float *Ft, float *Fe) {
+    const MatTables &T = *k.tab;
+    float U[9], sig[3], V[9];
+    d_svd3(Ft, U, sig, V);
+    const float eps[3] = {d_log(d_max(fabsf(sig[0]), 1e-14f)), d_log(d_max(fabsf(sig[1]), 1e-14f)),
+                          d_log(d_max(fabsf(sig[2]), 1e-14f))};
+    const float tr = eps[0] + eps[1] + eps[2];
+    const float eh[3] = {eps[0] - tr / 3.0f, eps[1] - tr / 3.0f, eps[2] - tr / 3.0f};
+    const float ehn = d_len3(eh[0], eh[1], eh[2]);
+    const float mu = k.mu[p], lam = k.lam[p];
+    const float dg = ehn + (3.0f * lam + 2.0f * mu) / (2.0f * mu) * tr * T.alpha[mat];
+    for (int i = 0; i < 9; ++i) Fe[i] = Ft[i];
+    if (dg > 0 && tr > 0) {
+        float VT[9];
+        d_trans(V, VT);
+        d_mmul(U, VT, Fe);
+    }
+    if (dg > 0 && tr <= 0) {
+        const float f = dg / ehn;
+        d_udwt(U, d_exp(eps[0] - eh[0] * f), d_exp(eps[1] - eh[1] * f), d_exp(eps[2] - eh[2] * f), V, Fe);
+    }
 }
 
 // ---- quadratic B-spline weights (p2g_particle / g2p_particle, mpm_utils.py:830-850)
@@ -257,70 +461,112 @@ __global__ void __launch_bounds__(kDetThreads) k_det_g2p(PK k, int reset_lists) 
 }
 
 // ---- stress (stress_update_particle, mpm_utils.py:1056-1149) --------------------
+// the fluids' pressure and deviatoric rate (mpm_utils.py:17-85)
+__device__ __forceinline__ float d_eos(float J, float bulk) { return -bulk * (d_pow(J, -1.1f) - 1.0f); }
+__device__ __forceinline__ void d_dev_rate(const float *L, float *Dd, float &gd) {
+    float D[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) D[3 * i + j] = (L[3 * i + j] + L[3 * j + i]) * 0.5f;
+    const float trd = (D[0] + D[4] + D[8]) / 3.0f;
+    for (int i = 0; i < 9; ++i) Dd[i] = D[i] - ((i % 4 == 0) ? 1.0f : 0.0f) * trd;
+    float dd = 0.0f;
+    for (int i = 0; i < 9; ++i) dd = dd + Dd[i] * Dd[i];
+    const float eps = 0.02f;
+    gd = sqrtf(2.0f * dd + eps * eps);
+}
+// Hencky (mpm_utils.py:228-243): U diag(2 mu e + lam tr e) U^T
+__device__ void d_stress_hencky(const float *U, const float *sig, float mu, float lam, float *st) {
+    const float e0 = d_log(d_max(sig[0], 1e-6f)), e1 = d_log(d_max(sig[1], 1e-6f)), e2 = d_log(d_max(sig[2], 1e-6f));
+    const float tr = e0 + e1 + e2;
+    d_udwt(U, 2.0f * mu * e0 + lam * tr, 2.0f * mu * e1 + lam * tr, 2.0f * mu * e2 + lam * tr, U, st);
+}
+// Drucker-Prager (mpm_utils.py:109-124): U diag(c) V^T F^T
+__device__ void d_stress_dp(const float *F, const float *U, const float *V, const float *sig, float mu, float lam,
+                            float *st) {
+    const float l0 = d_log(sig[0]), l1 = d_log(sig[1]), l2 = d_log(sig[2]);
+    const float lsum = l0 + l1 + l2;
+    float c[3];
+    for (int a = 0; a < 3; ++a)
+        c[a] = 2.0f * mu * d_log(sig[a]) * (1.0f / sig[a]) + lam * lsum * (1.0f / sig[a]);
+    float UDV[9], FT[9];
+    d_udwt(U, c[0], c[1], c[2], V, UDV);
+    d_trans(F, FT);
+    d_mmul(UDV, FT, st);
+}
+// mu(I)-Phi(I) (mpm_utils.py:525-540)
+__device__ void d_stress_mu_i_phi(const float *U, const float *sig, float G, float pc, float *st) {
+    const float s0 = d_max(sig[0], 1e-6f), s1 = d_max(sig[1], 1e-6f), s2 = d_max(sig[2], 1e-6f);
+    const float e0 = d_log(s0), e1 = d_log(s1), e2 = d_log(s2);
+    const float J = s0 * s1 * s2;
+    const float mean = (e0 + e1 + e2) / 3.0f;
+    const float iso = -pc * J;
+    d_udwt(U, 2.0f * G * (e0 - mean) + iso, 2.0f * G * (e1 - mean) + iso, 2.0f * G * (e2 - mean) + iso, U, st);
+}
+
 __global__ void __launch_bounds__(kDetThreads) k_det_stress(PK k) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= k.n) return;
     if (k.sel && k.sel[p] != 0) return;
     const int mat = k.mat[p];
+    const MatTables &T = *k.tab;
     float Ft[9], F[9], st[9];
-#pragma unroll
     for (int i = 0; i < 9; ++i) Ft[i] = k.Ft[9 * (size_t)p + i];
-    if (mat == 6 || mat == 10) {   // the fluids keep only the volume: F = J^(1/3) I
+    // the return map (or the fluids' volumetric F)
+    if (mat == 1 || mat == 5) {
+        d_rm_von_mises(k, p, mat, mat == 5, Ft, F);
+    } else if (mat == 2) {
+        d_rm_sand(k, p, mat, Ft, F);
+    } else if (mat == 9 || mat == 13) {
+        d_rm_mu_i(k, p, mat, mat == 13, Ft, F);
+    } else if (mat == 11) {
+        d_rm_mu_i_phi(k, p, mat, Ft, F);
+    } else if (mat == 6 || mat == 10 || mat == 12) {   // the fluids keep only the volume: F = J^(1/3) I
         const float Jc = d_pow(d_det(Ft), 1.0f / 3.0f);
-#pragma unroll
         for (int i = 0; i < 9; ++i) F[i] = (i % 4 == 0) ? Jc : 0.0f;
     } else {
-#pragma unroll
         for (int i = 0; i < 9; ++i) F[i] = Ft[i];
     }
-#pragma unroll
     for (int i = 0; i < 9; ++i) k.F[9 * (size_t)p + i] = F[i];
     const float J = d_det(F);
-    const MatTables &T = *k.tab;
-    if (mat == 0) {   // kirchoff_stress_FCR (mpm_utils.py:8-15)
-        float U[9], sg[3], V[9], Vt[9], R[9], D[9], FT[9];
-        d_svd3(F, U, sg, V);
+    float U[9], sg[3], V[9];
+    if (mat != 6 && mat != 10 && mat != 12) d_svd3(F, U, sg, V);
+    const float mu = k.mu[p], lam = k.lam[p];
+    if (mat == 0 || mat == 5) {   // kirchoff_stress_FCR (mpm_utils.py:8-15)
+        float Vt[9], R[9], D[9], FT[9];
         d_trans(V, Vt);
         d_mmul(U, Vt, R);
-        const float mu = k.mu[p], lam = k.lam[p];
-#pragma unroll
         for (int i = 0; i < 9; ++i) D[i] = (F[i] - R[i]) * (2.0f * mu);
         d_trans(F, FT);
         d_mmul(D, FT, st);
         const float d = lam * J * (J - 1.0f);
-#pragma unroll
         for (int i = 0; i < 9; ++i) st[i] = st[i] + ((i % 4 == 0) ? 1.0f : 0.0f) * d;
-    } else {
-        const float gamma = 1.1f;
-        const float pressure = -T.bulk[mat] * (d_pow(J, -gamma) - 1.0f);
+    } else if (mat == 1 || mat == 9 || mat == 13) {
+        d_stress_hencky(U, sg, mu, lam, st);
+    } else if (mat == 2) {
+        d_stress_dp(F, U, V, sg, mu, lam, st);
+    } else if (mat == 11) {
+        float Jr = k.Jp[p];
+        if (Jr < 0.5f) Jr = 1.0f;
+        d_stress_mu_i_phi(U, sg, mu, d_mu_i_phi_pressure(T, mat, J, Jr), st);
+    } else {   // the fluids (mpm_utils.py:17-85)
+        const float pressure = d_eos(J, T.bulk[mat]);
         float c[9];
-        if (mat == 6) {   // kirchoff_stress_water (mpm_utils.py:17-25)
-#pragma unroll
+        if (mat == 6) {   // water
             for (int i = 0; i < 9; ++i) c[i] = ((i % 4 == 0) ? 1.0f : 0.0f) * pressure;
-        } else {          // kirchoff_stress_newtonian (mpm_utils.py:27-54)
-            const float *L = k.L + 9 * (size_t)p;
-            float D[9], Dd[9];
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) D[3 * i + j] = (L[3 * i + j] + L[3 * j + i]) * 0.5f;
-            const float trd = (D[0] + D[4] + D[8]) / 3.0f;
-#pragma unroll
-            for (int i = 0; i < 9; ++i) Dd[i] = D[i] - ((i % 4 == 0) ? 1.0f : 0.0f) * trd;
-            float dd = 0.0f;
-            for (int i = 0; i < 9; ++i) dd = dd + Dd[i] * Dd[i];
-            const float eps = 0.02f;
-            const float gd = sqrtf(2.0f * dd + eps * eps);
-            const float eta_app = T.pv[mat] + k.ys[p] / gd + T.hardening[mat] * d_pow(gd, T.softening[mat] - 1.0f);
-#pragma unroll
+        } else {          // Newtonian / Bingham / Herschel-Bulkley, tabulated viscosity
+            float Dd[9], gd;
+            d_dev_rate(k.L + 9 * (size_t)p, Dd, gd);
+            float eta_app;
+            if (mat == 10)
+                eta_app = T.pv[mat] + k.ys[p] / gd + T.hardening[mat] * d_pow(gd, T.softening[mat] - 1.0f);
+            else
+                eta_app = d_table(k.eta, k.eta_n, k.eta_smin, k.eta_smax, d_log(gd) * 0.43429448190325176f);
             for (int i = 0; i < 9; ++i) c[i] = ((i % 4 == 0) ? 1.0f : 0.0f) * pressure + Dd[i] * (2.0f * eta_app);
         }
-#pragma unroll
         for (int i = 0; i < 9; ++i) st[i] = c[i] * J;
     }
     float stT[9];
     d_trans(st, stT);
-#pragma unroll
     for (int i = 0; i < 9; ++i) k.S[9 * (size_t)p + i] = (st[i] + stT[i]) * 0.5f;
 }
 

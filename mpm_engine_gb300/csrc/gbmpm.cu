@@ -1245,10 +1245,11 @@ int prepare_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int
     GB_CUDA(cudaEventRecord(e->pose_done, s));
     e->det = (flags & GBMPM_TICK_DETERMINISTIC) != 0;
     if (e->det) {
-        // jelly (0), water (6) and the Newtonian law (10) only; on the caller's particle order
-        const uint32_t det_mats = (1u << 0) | (1u << 6) | (1u << 10);
+        // every material law but the rigid bodies' (7, 8); on the caller's particle order
+        const uint32_t det_mats = (1u << 0) | (1u << 1) | (1u << 2) | (1u << 5) | (1u << 6) | (1u << 9) |
+                                  (1u << 10) | (1u << 11) | (1u << 12) | (1u << 13);
         if (e->M.material_mask & ~det_mats)
-            return fail(GBMPM_ERR_UNSUPPORTED, "deterministic ticks support jelly, water and Newtonian materials");
+            return fail(GBMPM_ERR_UNSUPPORTED, "deterministic ticks do not cover rigid-body materials");
         if (e->cdf.n > 0 || e->n_bodies > 0 || e->n_mods > 0)
             return fail(GBMPM_ERR_UNSUPPORTED,
                         "deterministic ticks support no CDF colliders, rigid bodies or particle modifiers");

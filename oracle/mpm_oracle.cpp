@@ -119,11 +119,40 @@ inline V3 vnormalize(V3 a) {
     return mkv(0, 0, 0);
 }
 
-// wp.pow in fp32 as its correctly rounded value: the power is evaluated in double
-// and rounded once to Real. That is the correctly rounded powf except when the
-// exact power lies within about one double ulp of a float rounding boundary (a
-// chance near 2^-28 per call), so every libm, and a GPU doing the same, agree.
-inline Real powr(Real x, Real y) { return (Real)std::pow((double)x, (double)y); }
+// wp.log, wp.exp and wp.pow in fp32 as their correctly rounded values: each is
+// evaluated in double by this file's own method and rounded once to Real. That is
+// the correctly rounded float except when the exact value lies within about 1e-16
+// of a float rounding boundary. The method is written here operation by operation
+// (no libm), so the deterministic GPU passes, which state the same operations in the
+// same order, return the same bits.
+//   log x = k ln2 + 2 atanh(s), x = m 2^k with m in [1/sqrt 2, sqrt 2), s = (m - 1)/(m + 1),
+//           the atanh series to s^23 (|s| <= 0.1716: the next term is below 1e-18);
+//   exp x = 2^k exp(r), k = round(x / ln2), r = x - k ln2 (|r| <= 0.35), the Taylor
+//           series to r^17 in Horner form (the next term is below 1e-22).
+inline double dlog(double x) {
+    if (!(x > 0.0) || x == HUGE_VAL) return (x == 0.0) ? -HUGE_VAL : (x == HUGE_VAL ? x : NAN);
+    int k = 0;
+    double m = std::frexp(x, &k);
+    if (m < 0.70710678118654752440) { m = m * 2.0; k = k - 1; }
+    const double s = (m - 1.0) / (m + 1.0);
+    const double s2 = s * s;
+    double t = 1.0 / 23.0;
+    for (int j = 21; j >= 1; j -= 2) t = 1.0 / (double)j + s2 * t;
+    return (double)k * 0.69314718055994530942 + 2.0 * s * t;
+}
+inline double dexp(double x) {
+    if (x != x) return x;
+    if (x > 709.0) return HUGE_VAL;
+    if (x < -745.0) return 0.0;
+    const double kd = std::floor(x * 1.44269504088896340736 + 0.5);
+    const double r = x - kd * 0.69314718055994530942;
+    double t = 1.0;
+    for (int j = 17; j >= 1; --j) t = 1.0 + r * t / (double)j;
+    return std::ldexp(t, (int)kd);
+}
+inline Real logr(Real x) { return (Real)dlog((double)x); }
+inline Real expr(Real x) { return (Real)dexp((double)x); }
+inline Real powr(Real x, Real y) { return (Real)dexp((double)y * dlog((double)x)); }
 
 // warp mat*mat: t[i][j] += a[i][k]*b[k][j], k ascending from zero
 inline M3 mmul(const M3& a, const M3& b) {
@@ -294,7 +323,7 @@ M3 stress_tabulated(Real J, Real bulk, const M3& L, const float* table, Real smi
     Real pressure = -bulk * (powr(J, -gamma) - 1.0f);
     M3 Ddev; Real gd;
     dev_rate(L, Ddev, gd);
-    Real s = std::log(gd) * 0.43429448190325176f;
+    Real s = logr(gd) * 0.43429448190325176f;
     Real idx = (s - smin) / (smax - smin) * (Real)(n - 1);
     idx = std::min<Real>(std::max<Real>(idx, 0.0f), (Real)(n - 1) - 1.0e-6f);
     int i0 = (int)std::floor(idx);
@@ -305,17 +334,17 @@ M3 stress_tabulated(Real J, Real bulk, const M3& L, const float* table, Real smi
 }
 // kirchoff_stress_drucker_prager (mpm_utils.py:109-124)
 M3 stress_dp(const M3& F, const M3& U, const M3& V, V3 sig, Real mu, Real lam) {
-    Real l0 = std::log(sig[0]), l1 = std::log(sig[1]), l2 = std::log(sig[2]);
+    Real l0 = logr(sig[0]), l1 = logr(sig[1]), l2 = logr(sig[2]);
     Real lsum = l0 + l1 + l2;
-    Real c0 = 2.0f * mu * std::log(sig[0]) * (1.0f / sig[0]) + lam * lsum * (1.0f / sig[0]);
-    Real c1 = 2.0f * mu * std::log(sig[1]) * (1.0f / sig[1]) + lam * lsum * (1.0f / sig[1]);
-    Real c2 = 2.0f * mu * std::log(sig[2]) * (1.0f / sig[2]) + lam * lsum * (1.0f / sig[2]);
+    Real c0 = 2.0f * mu * logr(sig[0]) * (1.0f / sig[0]) + lam * lsum * (1.0f / sig[0]);
+    Real c1 = 2.0f * mu * logr(sig[1]) * (1.0f / sig[1]) + lam * lsum * (1.0f / sig[1]);
+    Real c2 = 2.0f * mu * logr(sig[2]) * (1.0f / sig[2]) + lam * lsum * (1.0f / sig[2]);
     return mmul(mmul(mmul(U, diag33(c0, c1, c2)), mT(V)), mT(F));
 }
 // kirchoff_stress_hencky (mpm_utils.py:228-243)
 M3 stress_hencky(const M3& U, V3 sig, Real mu, Real lam) {
-    Real e0 = std::log(std::max<Real>(sig[0], 1e-6f)), e1 = std::log(std::max<Real>(sig[1], 1e-6f)),
-          e2 = std::log(std::max<Real>(sig[2], 1e-6f));
+    Real e0 = logr(std::max<Real>(sig[0], 1e-6f)), e1 = logr(std::max<Real>(sig[1], 1e-6f)),
+          e2 = logr(std::max<Real>(sig[2], 1e-6f));
     Real tr = e0 + e1 + e2;
     M3 t = diag33(2.0f * mu * e0 + lam * tr, 2.0f * mu * e1 + lam * tr, 2.0f * mu * e2 + lam * tr);
     return mmul(mmul(U, t), mT(U));
@@ -329,7 +358,7 @@ Real mu_i_phi_pressure(const gbmpm_model* m, int mat, Real J, Real Jp_ref) {
 // kirchoff_stress_mu_i_phi (mpm_utils.py:525-540)
 M3 stress_mu_i_phi(const M3& U, V3 sig, Real G, Real p_comp) {
     Real s0 = std::max<Real>(sig[0], 1e-6f), s1 = std::max<Real>(sig[1], 1e-6f), s2 = std::max<Real>(sig[2], 1e-6f);
-    Real e0 = std::log(s0), e1 = std::log(s1), e2 = std::log(s2);
+    Real e0 = logr(s0), e1 = logr(s1), e2 = logr(s2);
     Real J = s0 * s1 * s2;
     Real mean = (e0 + e1 + e2) / 3.0f;
     Real iso = -p_comp * J;
@@ -343,7 +372,7 @@ M3 rm_von_mises(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat,
     M3 U, V; V3 so;
     svd3_impl(Ft, U, so, V);
     V3 sig = mkv(std::max<Real>(so[0], 0.01f), std::max<Real>(so[1], 0.01f), std::max<Real>(so[2], 0.01f));
-    V3 eps = mkv(std::log(sig[0]), std::log(sig[1]), std::log(sig[2]));
+    V3 eps = mkv(logr(sig[0]), logr(sig[1]), logr(sig[2]));
     Real temp = (eps[0] + eps[1] + eps[2]) / 3.0f;
     Real mu = P->mu[p], lam = P->lam[p];
     Real tr = eps[0] + eps[1] + eps[2];
@@ -360,7 +389,7 @@ M3 rm_von_mises(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat,
             P->yield_stress[p] = P->yield_stress[p] - m->softening[mat] * vlen(vscale(eh, dg / ehn));
             if (P->yield_stress[p] <= 0) { P->mu[p] = 0.0f; P->lam[p] = 0.0f; }
         }
-        M3 se = diag33(std::exp(eps[0]), std::exp(eps[1]), std::exp(eps[2]));
+        M3 se = diag33(expr(eps[0]), expr(eps[1]), expr(eps[2]));
         M3 Fe = mmul(mmul(U, se), mT(V));
         if (m->hardening[mat] > 0.5f)
             P->yield_stress[p] = P->yield_stress[p] + 2.0f * P->mu[p] * m->xi[mat] * dg;
@@ -375,7 +404,7 @@ M3 rm_mu_i(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat, Real
     svd3_impl(Ft, U, sig, V);
     V3 sc = mkv(std::max<Real>(std::fabs(sig[0]), 1e-6f), std::max<Real>(std::fabs(sig[1]), 1e-6f),
                 std::max<Real>(std::fabs(sig[2]), 1e-6f));
-    V3 eps = mkv(std::log(sc[0]), std::log(sc[1]), std::log(sc[2]));
+    V3 eps = mkv(logr(sc[0]), logr(sc[1]), logr(sc[2]));
     Real tr = eps[0] + eps[1] + eps[2];
     M3 Fe = Ft;
     if (tr >= 0.0f) {
@@ -401,7 +430,7 @@ M3 rm_mu_i(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat, Real
                 if (!tab) {
                     mu_mid = mu_s + dmu * Im / (Im + I0);
                 } else {
-                    Real s = std::log(std::max<Real>(Im, 1e-12f)) * 0.43429448190325176f;
+                    Real s = logr(std::max<Real>(Im, 1e-12f)) * 0.43429448190325176f;
                     Real idx = (s - m->eta_table_smin) / (m->eta_table_smax - m->eta_table_smin) *
                                 (Real)(m->eta_table_n - 1);
                     idx = std::min<Real>(std::max<Real>(idx, 0.0f), (Real)(m->eta_table_n - 1) - 1.0e-6f);
@@ -416,7 +445,7 @@ M3 rm_mu_i(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat, Real
             Real tbn = tbK - G * dt * gdp;
             Real scale = tbn / std::max<Real>(tbK, 1e-20f);
             Real e0 = d0 * scale + mean, e1 = d1 * scale + mean, e2 = d2 * scale + mean;
-            Fe = mmul(mmul(U, diag33(std::exp(e0), std::exp(e1), std::exp(e2))), mT(V));
+            Fe = mmul(mmul(U, diag33(expr(e0), expr(e1), expr(e2))), mT(V));
         }
     }
     return Fe;
@@ -435,7 +464,7 @@ M3 rm_mu_i_phi(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat, 
     svd3_impl(Ft, U, sig, V);
     V3 sc = mkv(std::max<Real>(std::fabs(sig[0]), 1e-6f), std::max<Real>(std::fabs(sig[1]), 1e-6f),
                 std::max<Real>(std::fabs(sig[2]), 1e-6f));
-    V3 eps = mkv(std::log(sc[0]), std::log(sc[1]), std::log(sc[2]));
+    V3 eps = mkv(logr(sc[0]), logr(sc[1]), logr(sc[2]));
     Real J = sc[0] * sc[1] * sc[2];
     Real tr = eps[0] + eps[1] + eps[2];
     Real mean = tr / 3.0f;
@@ -449,7 +478,7 @@ M3 rm_mu_i_phi(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat, 
     M3 Fe = Ft;
     P->Jp[p] = Jp_ref;
     if (pc <= 0.0f) {
-        Real si = std::exp(mean);
+        Real si = expr(mean);
         Fe = mmul(mmul(U, diag33(si, si, si)), mT(V));
     } else {
         Real pK = pc * J;
@@ -473,7 +502,7 @@ M3 rm_mu_i_phi(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat, 
             Real tbn = tbK - G * dt * gdp;
             Real scale = tbn / std::max<Real>(tbK, 1e-20f);
             Real e0 = d0 * scale + mean, e1 = d1 * scale + mean, e2 = d2 * scale + mean;
-            Fe = mmul(mmul(U, diag33(std::exp(e0), std::exp(e1), std::exp(e2))), mT(V));
+            Fe = mmul(mmul(U, diag33(expr(e0), expr(e1), expr(e2))), mT(V));
         }
     }
     return Fe;
@@ -483,8 +512,8 @@ M3 rm_mu_i_phi(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat, 
 M3 rm_sand(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat) {
     M3 U, V; V3 sig;
     svd3_impl(Ft, U, sig, V);
-    V3 eps = mkv(std::log(std::max<Real>(std::fabs(sig[0]), 1e-14f)), std::log(std::max<Real>(std::fabs(sig[1]), 1e-14f)),
-                 std::log(std::max<Real>(std::fabs(sig[2]), 1e-14f)));
+    V3 eps = mkv(logr(std::max<Real>(std::fabs(sig[0]), 1e-14f)), logr(std::max<Real>(std::fabs(sig[1]), 1e-14f)),
+                 logr(std::max<Real>(std::fabs(sig[2]), 1e-14f)));
     Real tr = eps[0] + eps[1] + eps[2];
     V3 eh = vsub(eps, mkv(tr / 3.0f, tr / 3.0f, tr / 3.0f));
     Real ehn = vlen(eh);
@@ -495,7 +524,7 @@ M3 rm_sand(const M3& Ft, const RP* P, const gbmpm_model* m, int p, int mat) {
     if (dg > 0 && tr > 0) Fe = mmul(U, mT(V));
     if (dg > 0 && tr <= 0) {
         V3 H = vsub(eps, vscale(eh, dg / ehn));
-        Fe = mmul(mmul(U, diag33(std::exp(H[0]), std::exp(H[1]), std::exp(H[2]))), mT(V));
+        Fe = mmul(mmul(U, diag33(expr(H[0]), expr(H[1]), expr(H[2]))), mT(V));
     }
     return Fe;
 }

@@ -5,9 +5,9 @@ statement of the reference's kernels, and sum the P2G deposits of each node in
 particle order (sorted records, no float atomics). The oracle run on one thread
 deposits in particle order too. So the two must agree exactly, not within a
 tolerance: x, v, C, F and the stress, compared with np.array_equal after every
-check point. Both sides evaluate powers in double rounded once to float and run
-the SVD in double; they could differ only where a double result falls within a
-double ulp or two of a float rounding boundary (a chance near 2^-28 per power).
+check point, for every material law. Both sides evaluate logarithms, exponentials
+and powers in double by the same written-out method (no libm) and round them once,
+and run the SVD in double in the same order.
 
 The reference's own precedent for bitwise checks is fused == split on one device
 (tests/test_fused_pipeline.py:59-75).
@@ -15,7 +15,7 @@ The reference's own precedent for bitwise checks is fused == split on one device
 import numpy as np
 import pytest
 
-from scenes_lib import MATERIALS, make, spin_velocity
+from scenes_lib import EXTRA_MATERIALS, MATERIALS, NAME_PARAMS, make, spin_velocity
 
 pytestmark = pytest.mark.gpu
 
@@ -23,10 +23,16 @@ NG, LIM = 32, 0.4
 DX = LIM / NG
 
 
+GRANULAR = ("sand", "mu_i", "mu_i_phi", "tabulated_mu_i")
+PRESTRAIN_F0 = np.array([[0.97, 0.10, 0.0], [0.0, 0.97, 0.0], [0.0, 0.0, 0.97]], np.float32)
+
+
 def scene(cls, key, fused=True, n=3000, seed=5, **kw):
     """A thrown, spinning blob whose lower part starts inside the floor's contact
     band (a separable floor with friction, 0.3 cells off its node row), inside
-    domain walls, under a descending plate that reaches the blob's top."""
+    domain walls, under a descending plate that reaches the blob's top. Granular
+    blobs start compressed and sheared (F0 = 0.97 I plus shear), so that their return
+    maps flow from the first substep."""
     rng = np.random.default_rng(seed)
     pts = (rng.random((n, 3)) * np.array([0.09, 0.09, 0.06]) + np.array([0.15, 0.15, 3.1 * DX])).astype(np.float32)
     vol = np.full(n, 1.0e-7, np.float32)
@@ -36,12 +42,22 @@ def scene(cls, key, fused=True, n=3000, seed=5, **kw):
         s.a["v"][:] = vel
     else:
         s.set_v(vel)
-    mat = MATERIALS[key]
-    if isinstance(mat, str):
-        from scenes_lib import NAME_PARAMS
+    mat = MATERIALS[key] if key in MATERIALS else EXTRA_MATERIALS[key]
+    if isinstance(mat, tuple):
+        s.set_material(mat[0], **mat[1])
+    elif isinstance(mat, str):
         s.set_material(mat, **NAME_PARAMS[mat])
     else:
         s.set_material(mat())
+    if key in GRANULAR:
+        F0 = np.tile(PRESTRAIN_F0, (n, 1, 1))
+        if cls.__name__ == "OracleSolver":
+            s.a["F"][:] = F0.reshape(s.a["F"].shape)
+            s.a["F_trial"][:] = F0.reshape(s.a["F_trial"].shape)
+        else:
+            import torch
+            for f in ("F", "F_trial"):
+                s._t[f].copy_(torch.from_numpy(F0))
     s.add_plane((0, 0, 3.3 * DX), (0, 0, 1), "separate", friction=0.3)
     s.add_domain_walls()
     s.add_box((0.196, 0.196, 3.1 * DX + 0.06 + 0.3 * DX + 0.01), (0.07, 0.07, 0.01), velocity=(0.0, 0.0, -1.5))
@@ -69,8 +85,12 @@ def assert_bitwise(s, o, what):
     assert not bad, f"{what}: not bitwise equal: {bad}"
 
 
-@pytest.mark.parametrize("key,fused", [("newtonian", True), ("jelly", True), ("water", True),
-                                       ("herschel_bulkley", True), ("newtonian", False), ("jelly", False)])
+ALL = ["newtonian", "herschel_bulkley", "bingham", "water", "tabulated", "jelly", "metal", "metal_hardening",
+       "plasticine", "sand", "mu_i", "tabulated_mu_i", "mu_i_phi"]
+
+
+@pytest.mark.parametrize("key,fused", [(k, True) for k in ALL] +
+                         [("newtonian", False), ("jelly", False), ("metal_hardening", False), ("mu_i", False)])
 def test_deterministic_ticks_equal_oracle_bitwise(cuda, oracle_lib, key, fused):
     from mpm_engine_gb300 import Solver
     s = scene(Solver, key, fused=fused, deterministic=True)
@@ -109,8 +129,9 @@ def test_deterministic_ticks_repeat_bitwise_and_match_the_fast_path(cuda):
     assert_close(c, view, 10 * 1e-5, "tiled path against the deterministic passes after 10 substeps")
 
 
-def test_deterministic_ticks_reject_unsupported_materials(cuda):
+def test_deterministic_ticks_reject_particle_modifiers(cuda):
     from mpm_engine_gb300 import Solver
-    s = scene(Solver, "metal", deterministic=True)
+    s = scene(Solver, "jelly", deterministic=True)
+    s.add_impulse_on_particles((0.0, 0.0, 1.0e-3), 1.0e-4)
     with pytest.raises(NotImplementedError, match="deterministic"):
         s.step(1.0e-4, 1)
