@@ -518,7 +518,7 @@ static __device__ bool apply_modifiers(const PK &k, int mask, const float *x, fl
 // stages (G2P, STRESS, P2G): the fused interior pass is G2P|STRESS|P2G, the tick
 // prologue STRESS|P2G and the epilogue G2P.
 template <bool SOLIDS>
-__global__ void __launch_bounds__(kParticleThreads) k_particles(PK k, int mode) {
+__global__ void __launch_bounds__(kParticleThreads, 5) k_particles(PK k, int mode) {
     if ((mode & PASS_RESET_LISTS) && blockIdx.x == 0 && threadIdx.x == 0) {
         k.blk_count[0] = 0;
         k.blk_count[1] = 0;
