@@ -290,10 +290,23 @@ typedef struct gbmpm_adj_grads {
  * caller restores a checkpoint first), keeping each substep's starting state, then
  * carries the adjoints in g from the end of the segment back to its start and adds
  * each substep's contribution to g->mu, g->lam and g->viscosity. Leaves the bound
- * state at the segment's end and advances *time. Covers jelly (FCR), von Mises,
- * water and Newtonian (Bingham, Herschel-Bulkley) particles and every grid
- * collider; CDF lanes, periodic x and other materials are GBMPM_ERR_UNSUPPORTED. */
+ * state at the segment's end and advances *time. Covers every material law but the
+ * rigid bodies' and every grid collider; CDF lanes, rigid bodies, particle
+ * modifiers, periodic x and rpic_damping != 0 are GBMPM_ERR_UNSUPPORTED. */
 int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t substeps,
+                          const gbmpm_adj_grads *g, void *stream);
+
+/* The two halves of gbmpm_adjoint_segment, for callers that keep every substep's
+ * state instead of replaying the segment: gbmpm_adjoint_forward steps the segment
+ * from the bound state (advancing it and *time, as a tick on the split schedule
+ * does) and writes each substep's starting state into `states` (device memory,
+ * 37 x n floats per substep: x 3, v 3, C 9, F_trial 9, L 9, yield 1, mu 1, lam 1,
+ * Jp 1 per particle, field-major); gbmpm_adjoint_reverse runs the reverse
+ * substeps of that segment from `states`, with the collider poses and *time of the
+ * segment's start (the caller restores them, as for gbmpm_adjoint_segment). */
+int gbmpm_adjoint_forward(gbmpm_engine *e, double *time, double dt, int32_t substeps, float *states,
+                          void *stream);
+int gbmpm_adjoint_reverse(gbmpm_engine *e, double *time, double dt, int32_t substeps, const float *states,
                           const gbmpm_adj_grads *g, void *stream);
 
 /* Reaction impulse accumulated since the last reset: {fx, fy, fz, tx, ty, tz}. */

@@ -164,6 +164,10 @@ _SIGNATURES = {
                                        C.c_int32, C.c_int32, C.POINTER(C.c_double), C.c_void_p]),
     "gbmpm_adjoint_segment": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_double, C.c_int32,
                                         C.POINTER(AdjGrads), C.c_void_p]),
+    "gbmpm_adjoint_forward": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_double, C.c_int32, C.c_void_p,
+                                        C.c_void_p]),
+    "gbmpm_adjoint_reverse": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_double, C.c_int32, C.c_void_p,
+                                        C.POINTER(AdjGrads), C.c_void_p]),
     "gbmpm_sort_particles": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_int32), C.c_void_p,
                                        C.c_void_p]),
     "gbmpm_rebuild_active_blocks": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p]),

@@ -37,20 +37,22 @@ from .solver import _torch
 _STATE = ("x", "v", "C", "F_trial", "L", "yield_stress", "mu", "lam", "Jp")
 
 
-def _snapshot(s):
+def _snapshot(s, particles: bool = True):
+    """The scene's clock, collider poses and (with `particles`) particle state."""
     s._pull_colliders()
     cols = []
     for rec in s._cols:
         r = _abi.Collider()
         C.memmove(C.byref(r), C.byref(rec), C.sizeof(_abi.Collider))
         cols.append(r)
-    return {k: s._t[k].clone() for k in _STATE}, cols, s._time
+    return ({k: s._t[k].clone() for k in _STATE} if particles else None), cols, s._time
 
 
 def _restore(s, snap):
     state, cols, t = snap
-    for k in _STATE:
-        s._t[k].copy_(state[k])
+    if state is not None:
+        for k in _STATE:
+            s._t[k].copy_(state[k])
     s._cols = []
     for rec in cols:
         r = _abi.Collider()
@@ -69,17 +71,58 @@ def _check(s):
         raise NotImplementedError("the adjoint does not cover CDF colliders")
 
 
-def _forward(s, dt, substeps, every, plate=None):
-    """Runs the rollout, keeping a checkpoint per segment; with a plate handle also
-    returns the plate's reaction force over each segment ([segments][3] float64)."""
+STATE_FLOATS = 37   # floats a particle keeps per substep: x 3, v 3, C 9, F_trial 9, L 9, yield, mu, lam, Jp
+
+
+def state_bytes(n_particles: int, substeps: int) -> int:
+    """Device bytes that keeping every substep's state of a rollout takes."""
+    return STATE_FLOATS * 4 * int(n_particles) * int(substeps)
+
+
+def _keep_states(s, substeps, keep):
+    """Whether a rollout keeps every substep's state (None: when it takes less than
+    half of the free device memory) instead of replaying each segment backwards."""
+    if keep is not None:
+        return bool(keep)
+    torch = _torch()
+    free, _ = torch.cuda.mem_get_info(s._t["x"].device)
+    return state_bytes(s.n_particles, substeps) < 0.5 * free
+
+
+def _segment_forward(s, dt, k):
+    """Steps one segment on the split schedule, keeping each substep's starting state
+    (a device tensor of STATE_FLOATS x n x k floats); the bookkeeping is Solver.step's."""
+    torch = _torch()
+    if s._tick % max(1, s.guard_interval) == 0:
+        s._update_grid_box(dt, k)
+    s._tick += 1
+    s._pull_colliders()
+    s._sync_engine()
+    states = torch.empty(STATE_FLOATS * s.n_particles * k, dtype=torch.float32, device=s._t["x"].device)
+    t = C.c_double(s._time)
+    _abi.check(s._eng.lib.gbmpm_adjoint_forward(s._eng.h, C.byref(t), float(dt), int(k), states.data_ptr(),
+                                                s._stream()), "gbmpm_adjoint_forward")
+    s._time = t.value
+    s._step += k
+    return states
+
+
+def _forward(s, dt, substeps, every, plate=None, keep=False):
+    """Runs the rollout, keeping a checkpoint per segment (with `keep`, the segment's
+    every substep state instead of its starting particle state); with a plate handle
+    also returns the plate's reaction force over each segment ([segments][3] float64)."""
     ckpts, forces = [], []
     done = 0
     while done < substeps:
         k = min(every, substeps - done)
-        ckpts.append((_snapshot(s), k))
+        snap = _snapshot(s, particles=not keep)
         if plate is not None:
             s.reset_tool_force(plate)
-        s.step(dt, k)
+        if keep:
+            ckpts.append((snap, k, _segment_forward(s, dt, k)))
+        else:
+            s.step(dt, k)
+            ckpts.append((snap, k, None))
         if plate is not None:
             forces.append(s.tool_force(plate, dt * k))
         done += k
@@ -114,8 +157,9 @@ def _adj_setup(s, xb, vb, plate, kmax):
     return g, rec, fb, col
 
 
-def _adj_segment(s, dt, rec, snap, k, fb, col, force_bar_j):
-    """Replays one checkpoint segment and runs its reverse substeps (stream order)."""
+def _adj_segment(s, dt, rec, snap, k, fb, col, force_bar_j, states=None):
+    """Runs one checkpoint segment's reverse substeps (stream order): from its kept
+    states, or replaying the segment from its checkpoint first."""
     _restore(s, snap)
     if col is not None:
         # the segment's force is sum_substeps sum_nodes m (v_free - v_box) / (dt k)
@@ -123,8 +167,12 @@ def _adj_segment(s, dt, rec, snap, k, fb, col, force_bar_j):
         if force_bar_j is not None:
             fb[:k, col, :] = force_bar_j.to(device=fb.device, dtype=fb.dtype) / (dt * k)
     t = C.c_double(s._time)
-    _abi.check(s._eng.lib.gbmpm_adjoint_segment(s._eng.h, C.byref(t), float(dt), int(k), C.byref(rec), s._stream()),
-               "gbmpm_adjoint_segment")
+    if states is not None:
+        _abi.check(s._eng.lib.gbmpm_adjoint_reverse(s._eng.h, C.byref(t), float(dt), int(k), states.data_ptr(),
+                                                    C.byref(rec), s._stream()), "gbmpm_adjoint_reverse")
+    else:
+        _abi.check(s._eng.lib.gbmpm_adjoint_segment(s._eng.h, C.byref(t), float(dt), int(k), C.byref(rec),
+                                                    s._stream()), "gbmpm_adjoint_segment")
 
 
 def _adj_finish(g, col):
@@ -134,10 +182,10 @@ def _adj_finish(g, col):
 
 
 def _backward(s, dt, ckpts, xb, vb, plate=None, force_bar=None):
-    g, rec, fb, col = _adj_setup(s, xb, vb, plate, max(k for _, k in ckpts))
+    g, rec, fb, col = _adj_setup(s, xb, vb, plate, max(c[1] for c in ckpts))
     for j in reversed(range(len(ckpts))):
-        snap, k = ckpts[j]
-        _adj_segment(s, dt, rec, snap, k, fb, col, None if force_bar is None else force_bar[j])
+        snap, k, states = ckpts[j]
+        _adj_segment(s, dt, rec, snap, k, fb, col, None if force_bar is None else force_bar[j], states)
     return _adj_finish(g, col)
 
 
@@ -146,7 +194,7 @@ NEWTONIAN = 10   # material id whose per-type viscosity `viscosity` sets
 
 class _Rollout(_torch().autograd.Function):
     @staticmethod
-    def forward(ctx, v0, mu, lam, ys0, eta, plate_v, solver, dt, substeps, every, plate):
+    def forward(ctx, v0, mu, lam, ys0, eta, plate_v, solver, dt, substeps, every, plate, keep):
         torch = _torch()
         s = solver
         s._t["v"].copy_(v0.detach().reshape(-1, 3))
@@ -159,10 +207,10 @@ class _Rollout(_torch().autograd.Function):
             s.set_box(plate, velocity=tuple(float(c) for c in plate_v.detach().cpu()))
         ctx.solver, ctx.dt, ctx.plate = s, dt, plate
         if plate is not None:
-            ctx.ckpts, forces = _forward(s, dt, substeps, every, plate)
+            ctx.ckpts, forces = _forward(s, dt, substeps, every, plate, keep)
             F = torch.tensor(np.array(forces), dtype=torch.float64, device=v0.device)
         else:
-            ctx.ckpts = _forward(s, dt, substeps, every)
+            ctx.ckpts = _forward(s, dt, substeps, every, None, keep)
             F = torch.zeros(0, 3, dtype=torch.float64, device=v0.device)
         x, v = s._t["x"].clone(), s._t["v"].clone()
         ctx.final = _snapshot(s)
@@ -175,7 +223,7 @@ class _Rollout(_torch().autograd.Function):
         _restore(s, ctx.final)
         pvb = g.get("plate_velocity")
         return (g["v"], g["mu"], g["lam"], g["yield_stress"], g["viscosity"].sum(), pvb, None, None, None, None,
-                None)
+                None, None)
 
 
 def mu_lam(E, nu):
@@ -184,7 +232,7 @@ def mu_lam(E, nu):
 
 
 def rollout(solver, dt: float, substeps: int, *, v0=None, E=None, nu=None, yield_stress=None, viscosity=None,
-            checkpoint_every: int = 20, plate=None, plate_velocity=None):
+            checkpoint_every: int = 20, plate=None, plate_velocity=None, keep_states=None):
     """Advance `solver` by `substeps` substeps of dt and return (x, v) at the end.
 
     v0 ((N, 3)), E, nu and yield_stress (scalars or (N,) tensors) and viscosity (the
@@ -198,7 +246,11 @@ def rollout(solver, dt: float, substeps: int, *, v0=None, E=None, nu=None, yield
     tool_force of that segment), and `plate_velocity` ((3,), default the plate's
     current velocity) is differentiable: it moves the plate through the rollout and
     drives the grid nodes inside it. Gradients reach it through the positions and
-    velocities and through the force trace."""
+    velocities and through the force trace.
+
+    `keep_states` keeps every substep's state from the forward pass (state_bytes of
+    device memory) so that the reverse pass does not replay each segment; None keeps
+    them when they take less than half of the free device memory."""
     torch = _torch()
     _check(solver)
     s = solver
@@ -231,7 +283,9 @@ def rollout(solver, dt: float, substeps: int, *, v0=None, E=None, nu=None, yield
             raise ValueError("plate must be an add_box handle")
         pv = (torch.tensor(list(rec.velocity), **f) if plate_velocity is None else
               (plate_velocity if torch.is_tensor(plate_velocity) else torch.as_tensor(plate_velocity)).to(**f))
-    x, v, F = _Rollout.apply(v0, mu, lam, ys, eta, pv, s, float(dt), int(substeps), int(checkpoint_every), plate)
+    keep = _keep_states(s, substeps, keep_states)
+    x, v, F = _Rollout.apply(v0, mu, lam, ys, eta, pv, s, float(dt), int(substeps), int(checkpoint_every), plate,
+                             keep)
     return (x, v) if plate is None else (x, v, F)
 
 
@@ -243,10 +297,13 @@ class BatchRollout:
     each scene's segments on its own stream; otherwise scenes run one after
     another, as serial rollouts would. `plates` (one add_box handle or None per
     scene) adds each plate's reaction-force trace to the outputs, one force per
-    checkpoint segment, and its adjoint to the reverse pass."""
+    checkpoint segment, and its adjoint to the reverse pass. `keep_states` keeps
+    every substep's state from the forward pass (as in `rollout`), so that the
+    reverse pass does not replay the segments; the batched forward then runs each
+    scene's segments on its own stream."""
 
     def __init__(self, solvers, dt: float, substeps: int, checkpoint_every: int = 20, batched: bool = True,
-                 plates=None):
+                 plates=None, keep_states=None):
         torch = _torch()
         from .solver import BatchSolver
         self.solvers = list(solvers)
@@ -257,7 +314,11 @@ class BatchRollout:
             raise ValueError("one plate handle (or None) per scene")
         self.dt, self.substeps, self.every = float(dt), int(substeps), int(checkpoint_every)
         self.batched = batched
-        self.batch = BatchSolver(self.solvers) if batched else None
+        if keep_states is None:   # every scene's states within half of the free device memory
+            free, _ = torch.cuda.mem_get_info(self.solvers[0]._t["x"].device)
+            keep_states = sum(state_bytes(s.n_particles, self.substeps) for s in self.solvers) < 0.5 * free
+        self.keep = bool(keep_states)
+        self.batch = BatchSolver(self.solvers) if batched and not self.keep else None
         self.streams = [torch.cuda.Stream(device=s._t["x"].device) for s in self.solvers] if batched else None
         self.ckpts = None
 
@@ -269,17 +330,34 @@ class BatchRollout:
         if not self.batched:
             self.ckpts = []
             for i, s in enumerate(self.solvers):
-                r = _forward(s, self.dt, self.substeps, self.every, self.plates[i])
+                r = _forward(s, self.dt, self.substeps, self.every, self.plates[i], self.keep)
                 if self.plates[i] is not None:
                     r, forces[i] = r
                 self.ckpts.append(r)
+        elif self.keep:   # each scene's segment on its own stream, the states kept
+            self.ckpts = [[] for _ in self.solvers]
+            done = 0
+            while done < self.substeps:
+                k = min(self.every, self.substeps - done)
+                for i, s in enumerate(self.solvers):
+                    snap = _snapshot(s, particles=False)
+                    with torch.cuda.stream(self.streams[i]):
+                        if self.plates[i] is not None:
+                            s.reset_tool_force(self.plates[i])
+                        self.ckpts[i].append((snap, k, _segment_forward(s, self.dt, k)))
+                for i, s in enumerate(self.solvers):
+                    if self.plates[i] is not None:
+                        with torch.cuda.stream(self.streams[i]):
+                            forces[i].append(s.tool_force(self.plates[i], self.dt * k))
+                done += k
+            torch.cuda.synchronize()
         else:
             self.ckpts = [[] for _ in self.solvers]
             done = 0
             while done < self.substeps:
                 k = min(self.every, self.substeps - done)
                 for i, s in enumerate(self.solvers):
-                    self.ckpts[i].append((_snapshot(s), k))
+                    self.ckpts[i].append((_snapshot(s), k, None))
                     if self.plates[i] is not None:
                         s.reset_tool_force(self.plates[i])
                 self.batch.step(self.dt, k)
@@ -311,16 +389,17 @@ class BatchRollout:
                    for s, ck, xb, vb, pl, fbar in zip(self.solvers, self.ckpts, xbs, vbs, self.plates, fbars)]
         else:
             torch.cuda.synchronize()
-            setups = [_adj_setup(s, xb, vb, pl, max(k for _, k in ck))
+            setups = [_adj_setup(s, xb, vb, pl, max(c[1] for c in ck))
                       for s, ck, xb, vb, pl in zip(self.solvers, self.ckpts, xbs, vbs, self.plates)]
             torch.cuda.synchronize()
             nseg = len(self.ckpts[0])
             for j in reversed(range(nseg)):
                 for i, s in enumerate(self.solvers):
-                    snap, k = self.ckpts[i][j]
+                    snap, k, states = self.ckpts[i][j]
                     g, rec, fb, col = setups[i]
                     with torch.cuda.stream(self.streams[i]):
-                        _adj_segment(s, self.dt, rec, snap, k, fb, col, None if fbars[i] is None else fbars[i][j])
+                        _adj_segment(s, self.dt, rec, snap, k, fb, col, None if fbars[i] is None else fbars[i][j],
+                                     states)
             torch.cuda.synchronize()
             out = [_adj_finish(g, col) for g, rec, fb, col in setups]
         for s, snap in zip(self.solvers, self.final):
@@ -328,4 +407,4 @@ class BatchRollout:
         return out
 
 
-__all__ = ["BatchRollout", "mu_lam", "rollout"]
+__all__ = ["BatchRollout", "mu_lam", "rollout", "state_bytes"]

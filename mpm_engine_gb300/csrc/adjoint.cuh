@@ -1384,19 +1384,19 @@ int adjoint_supported(gbmpm_engine *e) {
     return GBMPM_OK;
 }
 
-// Records one adjoint segment on stream s: the forward replay that keeps every
-// substep's starting state, then the reverse substeps. Returns the first error of a
-// copy or memset call (kernel launches report through cudaGetLastError).
-cudaError_t record_adjoint_segment(gbmpm_engine *e, float dtf, int substeps, const gbmpm_adj_grads *gr,
-                                   cudaStream_t s) {
+// The forward part of an adjoint segment on stream s: `substeps` split-schedule
+// substeps from the bound state, each substep's starting state kept in `states`
+// (x 3, v 3, C 9, F_trial 9, L 9, yield 1, mu 1, lam 1, Jp 1 floats a particle, in
+// that order, per substep). Returns the first error of a copy call (kernel launches
+// report through cudaGetLastError).
+cudaError_t record_adjoint_forward(gbmpm_engine *e, float dtf, int substeps, float *states, cudaStream_t s) {
     const gbmpm_particles &P = e->P;
-    const int n = P.n, ng = e->G.n_grid, nc = (int)e->cols.size();
-    const size_t nn = (size_t)ng * ng * ng;
+    const int n = P.n;
     const size_t per = (size_t)37 * n;
     cudaError_t first = cudaSuccess;
     auto keep = [&](cudaError_t err) { if (first == cudaSuccess) first = err; };
     for (int i = 0; i < substeps; ++i) {
-        float *st = e->adj_states.ptr + per * i;
+        float *st = states + per * i;
         keep(cudaMemcpyAsync(st, P.x, 3 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         keep(cudaMemcpyAsync(st + 3 * (size_t)n, P.v, 3 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         keep(cudaMemcpyAsync(st + 6 * (size_t)n, P.C, 9 * sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
@@ -1408,6 +1408,17 @@ cudaError_t record_adjoint_segment(gbmpm_engine *e, float dtf, int substeps, con
         keep(cudaMemcpyAsync(st + 36 * (size_t)n, P.Jp, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         record_tick(e, dtf, 1, false, false, s, false, 0.0, 0.0, i);
     }
+    return first;
+}
+
+// The reverse part of an adjoint segment on stream s, from the states the forward
+// part kept: the adjoints in gr carried from the end of the segment to its start.
+cudaError_t record_adjoint_reverse(gbmpm_engine *e, float dtf, int substeps, const gbmpm_adj_grads *gr,
+                                   const float *states, cudaStream_t s) {
+    const gbmpm_particles &P = e->P;
+    const int n = P.n, ng = e->G.n_grid, nc = (int)e->cols.size();
+    const size_t nn = (size_t)ng * ng * ng;
+    const size_t per = (size_t)37 * n;
     float4 *grid = e->adj_grid.ptr;
     const int pb = std::max(1, (n + 127) / 128);
     // the grid kernels stride over the segment's node box; sized for the whole grid
@@ -1416,10 +1427,10 @@ cudaError_t record_adjoint_segment(gbmpm_engine *e, float dtf, int substeps, con
     int *box = e->adj_box.ptr;
     k_adj_box_init<<<1, 32, 0, s>>>(box, ng);
     k_adj_box<<<std::max(1, std::min(e->num_sms * 4, (int)(((size_t)n * substeps + 255) / 256))), 256, 0, s>>>(
-        e->adj_states.ptr, per, n, substeps, e->M.inv_dx, ng, box);
+        states, per, n, substeps, e->M.inv_dx, ng, box);
     e->launches += 2;
     for (int i = substeps - 1; i >= 0; --i) {
-        const float *st = e->adj_states.ptr + per * i;
+        const float *st = states + per * i;
         AdjK a{};
         a.x = st; a.v = st + 3 * (size_t)n; a.C = st + 6 * (size_t)n; a.Ft = st + 15 * (size_t)n;
         a.Lst = st + 24 * (size_t)n; a.ys = st + 33 * (size_t)n; a.Jp = st + 36 * (size_t)n;
@@ -1455,53 +1466,53 @@ cudaError_t record_adjoint_segment(gbmpm_engine *e, float dtf, int substeps, con
         k_adj_p2g_bwd<<<pb, 128, 0, s>>>(a);
         e->launches += 7;
     }
-    return first;
+    return cudaSuccess;
 }
 
-}  // namespace
-
-extern "C" {
-
-int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t substeps, const gbmpm_adj_grads *gr,
-                          void *stream) {
+// Argument checks and scratch shared by the adjoint entry points; uploads the
+// segment's pose table (the forward and the reverse parts read the same one).
+int adjoint_prepare(gbmpm_engine *e, double *time, double dt, int32_t substeps, const gbmpm_adj_grads *gr,
+                    bool need_grads, cudaStream_t s, uint64_t &version0) {
     int rc = check_ready(e);
     if (rc) return rc;
-    if (!time || !gr || substeps < 1 || substeps > GBMPM_MAX_SUBSTEPS || !(dt > 0.0))
+    if (!time || substeps < 1 || substeps > GBMPM_MAX_SUBSTEPS || !(dt > 0.0))
         return fail(GBMPM_ERR_ARG, "bad adjoint arguments");
-    if (!gr->x || !gr->v || !gr->C || !gr->F_trial || !gr->yield_stress || !gr->mu || !gr->lam || !gr->L ||
-        !gr->viscosity || !gr->Jp)
+    if (need_grads && (!gr || !gr->x || !gr->v || !gr->C || !gr->F_trial || !gr->yield_stress || !gr->mu ||
+                       !gr->lam || !gr->L || !gr->viscosity || !gr->Jp))
         return fail(GBMPM_ERR_ARG, "every adjoint array is required");
     if (!e->P.L) return fail(GBMPM_ERR_ARG, "the adjoint needs particles.L");
     if ((rc = adjoint_supported(e))) return rc;
-    cudaStream_t s = (cudaStream_t)stream;
-    const gbmpm_particles &P = e->P;
-    const int n = P.n, ng = e->G.n_grid, nc = (int)e->cols.size();
+    const int n = e->P.n, ng = e->G.n_grid;
     const size_t nn = (size_t)ng * ng * ng;
-    // segment storage: the state at the start of every substep
-    const size_t per = (size_t)37 * n;   // x 3, v 3, C 9, F_trial 9, L 9, yield 1, mu 1, lam 1, Jp 1
-    GB_CUDA(e->adj_states.ensure(per * substeps));
+    GB_CUDA(e->adj_states.ensure((size_t)37 * n * substeps));
     GB_CUDA(e->adj_scratch.ensure((size_t)27 * n));
     float4 *old_grid = e->adj_grid.ptr;
     GB_CUDA(e->adj_grid.ensure(4 * nn));   // four float4 grids
     if (e->adj_grid.ptr != old_grid)        // zero once; then each substep zeroes its box
         GB_CUDA(cudaMemsetAsync(e->adj_grid.ptr, 0, 4 * nn * sizeof(float4), s));
     GB_CUDA(e->adj_box.ensure(6));
-    const float dtf = (float)dt;
-    // forward replay on the split schedule: one pose table for the whole segment
-    // (the adjoint kernels read the same table), no host synchronization per substep.
-    // The tables are uploaded here, outside the segment's graph, which reads them.
+    // one pose table for the whole segment, uploaded here, outside the captured graph
     bool reorder = false;
-    uint64_t version0 = e->version;
-    if ((rc = prepare_tick(e, time, dt, substeps, 0, s, reorder))) return rc;
-    const bool same = e->adj_graph && e->adj_g_substeps == substeps && e->adj_g_dt == dt &&
-                      e->adj_g_version == e->version && version0 == e->version &&
-                      std::memcmp(&e->adj_g_grads, gr, sizeof *gr) == 0;
+    version0 = e->version;
+    return prepare_tick(e, time, dt, substeps, 0, s, reorder);
+}
+
+// Runs `rec` on stream s through the captured graph cached in `c` (captured anew
+// when the segment length, dt, the engine's buffers or the adjoint arrays changed),
+// or live after a failed capture, as ticks do.
+template <typename Rec>
+int run_adjoint_graph(gbmpm_engine *e, AdjGraph &c, int substeps, double dt, const gbmpm_adj_grads *gr,
+                      uint64_t version0, cudaStream_t s, Rec rec) {
+    gbmpm_adj_grads key{};
+    if (gr) key = *gr;
+    const bool same = c.g && c.substeps == substeps && c.dt == dt && c.version == e->version &&
+                      version0 == e->version && std::memcmp(&c.grads, &key, sizeof key) == 0;
     if (same) {
-        GB_CUDA(cudaGraphLaunch(e->adj_graph, s));
-        e->launches += e->adj_graph_launches;
+        GB_CUDA(cudaGraphLaunch(c.g, s));
+        e->launches += c.launches;
         return GBMPM_OK;
     }
-    if (e->adj_graph) { cudaGraphExecDestroy(e->adj_graph); e->adj_graph = nullptr; }
+    c.drop();
     if (!e->graph_failed) {
         cudaStream_t cap;
         GB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
@@ -1511,32 +1522,83 @@ int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t subs
             return fail(GBMPM_ERR_CUDA, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(be));
         }
         const int64_t before = e->launches;
-        cudaError_t ce = record_adjoint_segment(e, dtf, substeps, gr, cap);
-        e->adj_graph_launches = e->launches - before;
+        cudaError_t ce = rec(cap);
+        c.launches = e->launches - before;
         e->launches = before;
         cudaGraph_t graph = nullptr;
         cudaError_t ee = cudaStreamEndCapture(cap, &graph);
         cudaStreamDestroy(cap);
         if (ce == cudaSuccess) ce = ee;
-        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&e->adj_graph, graph, 0);
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&c.g, graph, 0);
         if (graph) cudaGraphDestroy(graph);
         if (ce == cudaSuccess) {
-            e->adj_g_substeps = substeps;
-            e->adj_g_dt = dt;
-            e->adj_g_version = e->version;
-            e->adj_g_grads = *gr;
-            GB_CUDA(cudaGraphLaunch(e->adj_graph, s));
-            e->launches += e->adj_graph_launches;
+            c.substeps = substeps;
+            c.dt = dt;
+            c.version = e->version;
+            c.grads = key;
+            GB_CUDA(cudaGraphLaunch(c.g, s));
+            e->launches += c.launches;
             return GBMPM_OK;
         }
         // as a failed tick capture: launched live from here on
-        e->adj_graph = nullptr;
+        c.g = nullptr;
         e->graph_failed = true;
         (void)cudaGetLastError();
     }
-    GB_CUDA(record_adjoint_segment(e, dtf, substeps, gr, s));
+    GB_CUDA(rec(s));
     GB_CUDA(cudaGetLastError());
     return GBMPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbmpm_adjoint_segment(gbmpm_engine *e, double *time, double dt, int32_t substeps, const gbmpm_adj_grads *gr,
+                          void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    uint64_t version0 = 0;
+    int rc = adjoint_prepare(e, time, dt, substeps, gr, true, s, version0);
+    if (rc) return rc;
+    const float dtf = (float)dt;
+    return run_adjoint_graph(e, e->adj_seg, substeps, dt, gr, version0, s, [&](cudaStream_t cs) {
+        cudaError_t ce = record_adjoint_forward(e, dtf, substeps, e->adj_states.ptr, cs);
+        cudaError_t cr = record_adjoint_reverse(e, dtf, substeps, gr, e->adj_states.ptr, cs);
+        return ce != cudaSuccess ? ce : cr;
+    });
+}
+
+int gbmpm_adjoint_forward(gbmpm_engine *e, double *time, double dt, int32_t substeps, float *states, void *stream) {
+    if (!states) return fail(GBMPM_ERR_ARG, "null states");
+    cudaStream_t s = (cudaStream_t)stream;
+    uint64_t version0 = 0;
+    int rc = adjoint_prepare(e, time, dt, substeps, nullptr, false, s, version0);
+    if (rc) return rc;
+    const float dtf = (float)dt;
+    // the captured graph writes the engine's segment storage; the copy to the
+    // caller's buffer follows it on the stream
+    rc = run_adjoint_graph(e, e->adj_fwd, substeps, dt, nullptr, version0, s, [&](cudaStream_t cs) {
+        return record_adjoint_forward(e, dtf, substeps, e->adj_states.ptr, cs);
+    });
+    if (rc) return rc;
+    GB_CUDA(cudaMemcpyAsync(states, e->adj_states.ptr, (size_t)37 * e->P.n * substeps * sizeof(float),
+                            cudaMemcpyDeviceToDevice, s));
+    return GBMPM_OK;
+}
+
+int gbmpm_adjoint_reverse(gbmpm_engine *e, double *time, double dt, int32_t substeps, const float *states,
+                          const gbmpm_adj_grads *gr, void *stream) {
+    if (!states) return fail(GBMPM_ERR_ARG, "null states");
+    cudaStream_t s = (cudaStream_t)stream;
+    uint64_t version0 = 0;
+    int rc = adjoint_prepare(e, time, dt, substeps, gr, true, s, version0);
+    if (rc) return rc;
+    GB_CUDA(cudaMemcpyAsync(e->adj_states.ptr, states, (size_t)37 * e->P.n * substeps * sizeof(float),
+                            cudaMemcpyDeviceToDevice, s));
+    const float dtf = (float)dt;
+    return run_adjoint_graph(e, e->adj_rev, substeps, dt, gr, version0, s, [&](cudaStream_t cs) {
+        return record_adjoint_reverse(e, dtf, substeps, gr, e->adj_states.ptr, cs);
+    });
 }
 
 }  // extern "C"

@@ -114,6 +114,20 @@ struct CdfHost {
 };
 }  // namespace
 
+// One captured adjoint graph and the arguments it was captured for.
+struct AdjGraph {
+    cudaGraphExec_t g = nullptr;
+    int substeps = -1;
+    double dt = 0.0;
+    uint64_t version = 0;
+    gbmpm_adj_grads grads{};
+    int64_t launches = 0;
+    void drop() {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
+};
+
 struct gbmpm_engine {
     int device = 0;
     gbmpm_particles P{};
@@ -189,12 +203,8 @@ struct gbmpm_engine {
     // the launches of one adjoint segment, captured once and replayed while the
     // segment's shape and buffers stay the same (key: substeps, dt, adjoint arrays,
     // engine version)
-    cudaGraphExec_t adj_graph = nullptr;
-    int adj_g_substeps = -1;
-    double adj_g_dt = 0.0;
-    gbmpm_adj_grads adj_g_grads{};
-    uint64_t adj_g_version = 0;
-    int64_t adj_graph_launches = 0;
+    // captured adjoint graphs: replay + reverse, forward with states kept, reverse alone
+    AdjGraph adj_seg, adj_fwd, adj_rev;
     // rigid bodies and particle modifiers
     int n_bodies = 0;
     std::vector<gbmpm_rigid_surface> rsurf;
@@ -881,7 +891,7 @@ int gbmpm_engine_create(gbmpm_engine **out) {
 }
 
 void gbmpm_engine_destroy(gbmpm_engine *e) {
-    if (e && e->adj_graph) { cudaGraphExecDestroy(e->adj_graph); e->adj_graph = nullptr; }
+    if (e) { e->adj_seg.drop(); e->adj_fwd.drop(); e->adj_rev.drop(); }
     if (!e) return;
     cudaDeviceSynchronize();
     if (e->graph) cudaGraphExecDestroy(e->graph);

@@ -35,8 +35,9 @@ def test_segments_cover_the_rollout():
     s = FakeSolver()
     ckpts = adjoint._forward(s, 0.5, 45, 20)
     assert s.steps == [20, 20, 5]
-    assert [k for _, k in ckpts] == [20, 20, 5]
-    assert [snap[2] for snap, _ in ckpts] == [0.0, 10.0, 20.0]
+    assert [c[1] for c in ckpts] == [20, 20, 5]
+    assert [c[0][2] for c in ckpts] == [0.0, 10.0, 20.0]
+    assert all(c[2] is None for c in ckpts)   # replayed backwards: no kept states
 
 
 def test_snapshot_restores_state_colliders_and_clock():
@@ -51,6 +52,20 @@ def test_snapshot_restores_state_colliders_and_clock():
     s._cols[0].point[0] = 7.0
     assert snap[1][0].point[0] == 0.0
     assert C.sizeof(snap[1][0]) == C.sizeof(_abi.Collider)
+
+
+def test_collider_only_snapshot_restores_clock_and_colliders():
+    s = FakeSolver()
+    snap = adjoint._snapshot(s, particles=False)
+    assert snap[0] is None
+    s.step(0.1, 3)
+    adjoint._restore(s, snap)
+    assert float(s._t["x"].abs().max()) == 1.0   # particles untouched
+    assert s._cols[0].point[0] == 0.0 and s._time == 0.0
+
+
+def test_state_bytes():
+    assert adjoint.state_bytes(50_000, 400) == 37 * 4 * 50_000 * 400
 
 
 def test_mu_lam_is_the_reference_formula():

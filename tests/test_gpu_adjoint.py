@@ -318,10 +318,12 @@ def test_unsupported_scenes_are_refused(cuda):
         x.sum().backward()
 
 
-def test_batch_rollout_with_plates_matches_scenes_run_one_by_one(cuda):
+@pytest.mark.parametrize("keep", [True, False])
+def test_batch_rollout_with_plates_matches_scenes_run_one_by_one(cuda, keep):
     """BatchRollout with plate force traces: batched (all forwards in one CUDA graph
-    per segment, each scene's reverse pass on its own stream) against the same scenes
-    rolled out and reversed one after another. Force traces within 1e-5 and every
+    per segment, each scene's reverse pass on its own stream; with kept states each
+    scene's forward on its own stream too) against the same scenes rolled out and
+    reversed one after another. Force traces within 1e-5 and every
     gradient (v0, mu, lam, yield, plate velocity) within 1e-3 relative: the two
     differ only in float atomic order, which can move a particle across the yield
     surface in one run and not the other."""
@@ -335,7 +337,7 @@ def test_batch_rollout_with_plates_matches_scenes_run_one_by_one(cuda):
         built = [squeeze_scene(Solver, 8000, 32, vonmises(E=E, nu=nu, yield_stress=ys, density=1000.0), seed=i,
                                plate_gap=-0.37, floor_cells=3.3) for i, (E, nu, ys) in enumerate(specs)]
         scenes, plates = [b[0] for b in built], [b[1] for b in built]
-        r = adjoint.BatchRollout(scenes, 1.0e-5, 40, 10, batched=batched, plates=plates)
+        r = adjoint.BatchRollout(scenes, 1.0e-5, 40, 10, batched=batched, plates=plates, keep_states=keep)
         outs = r.forward()
         rng = np.random.default_rng(4)
         xb = [torch.from_numpy(rng.standard_normal((s.n_particles, 3))).to(o[0].device) for s, o in zip(scenes, outs)]
@@ -352,3 +354,27 @@ def test_batch_rollout_with_plates_matches_scenes_run_one_by_one(cuda):
             if k in ("mu", "lam", "yield_stress"):
                 a, b = np.array([a.sum()]), np.array([b.sum()])
             assert np.abs(a - b).max() <= 1e-3 * np.abs(b).max() + 1e-30, (i, k, np.abs(a - b).max(), np.abs(b).max())
+
+
+@pytest.mark.parametrize("key", ["jelly", "metal_hardening"])
+def test_kept_states_and_replayed_segments_give_the_same_gradients(cuda, key):
+    """rollout(keep_states=True) keeps every substep's state from the forward pass;
+    keep_states=False replays each segment from its checkpoint in the reverse pass.
+    Both linearise along the split schedule's trajectory and differ only in float
+    atomic order: gradients within 1e-4 relative (1e-3 for the von Mises scene,
+    whose yield kinks rounding may move)."""
+    import torch
+    from mpm_engine_gb300 import Solver, adjoint
+    out = {}
+    for keep in (True, False):
+        s = _scene(Solver, key, plate=True)
+        v0 = s._t["v"].clone().requires_grad_(True)
+        E = torch.tensor(_mat_params(key)[0], device=v0.device, requires_grad=True)
+        x, v = adjoint.rollout(s, DT, 12, v0=v0, E=E, nu=0.3, checkpoint_every=5, keep_states=keep)
+        a, b = (torch.from_numpy(w).to(v0.device) for w in _weights())
+        ((x.double() * a).sum() + (v.double() * b).sum()).backward()
+        out[keep] = (v0.grad.double().cpu().numpy(), float(E.grad))
+    tol = 1e-4 if key == "jelly" else 1e-3
+    (gk, Ek), (gr, Er) = out[True], out[False]
+    assert np.abs(gk - gr).max() <= tol * np.abs(gr).max(), (np.abs(gk - gr).max(), np.abs(gr).max())
+    assert abs(Ek - Er) <= tol * abs(Er), (Ek, Er)
