@@ -114,6 +114,16 @@ struct CdfHost {
 };
 }  // namespace
 
+constexpr int kStages = 4;
+struct Staging {
+    PoseRec *pose = nullptr;
+    size_t pose_cap = 0;
+    double *time = nullptr;
+    size_t time_cap = 0;
+    ColDev *cols = nullptr;
+    cudaEvent_t done = nullptr;
+};
+
 // One captured adjoint graph and the arguments it was captured for.
 struct AdjGraph {
     cudaGraphExec_t g = nullptr;
@@ -136,7 +146,6 @@ struct gbmpm_engine {
     bool bound = false, modeled = false;
     std::vector<gbmpm_collider> cols;
     std::vector<ColDev> h_cols;   // the collider descriptor table (device copy: d_cols)
-    ColDev *h_coldev = nullptr;   // pinned staging for its stream-ordered upload
     bool cols_upload = false;     // h_cols changed since the last upload
     // device scratch
     DevBuf<MatTables> d_tab;
@@ -161,9 +170,11 @@ struct gbmpm_engine {
     gbmpm_particles W{};
     WsTable ws_table{};
     int ws_n = -1;
-    PoseRec *h_pose = nullptr;
-    size_t h_pose_cap = 0;
-    cudaEvent_t pose_done = nullptr;
+    // pinned staging of the per-tick uploads (pose table, substep times, collider
+    // table): a ring, so that the host waits on the upload of kStages ticks ago rather
+    // than on the last one, which is queued behind the last tick's work
+    Staging stage[kStages];
+    int stage_i = 0;
     int bd = 0;
     int num_sms = 148;
     bool graph_failed = false;          // a capture failed: live launches for the rest of the run
@@ -215,8 +226,6 @@ struct gbmpm_engine {
     int n_rigid = 0;                        // rigid particles when the bodies were set (grid sizing)
     int n_mods = 0;
     DevBuf<gbmpm_modifier> d_mods;
-    double *h_time = nullptr;               // pinned staging of d_time
-    size_t h_time_cap = 0;
     DevBuf<double> d_time;                  // start time of every substep of the tick
     // profiling
     double prof_ms[GBMPM_NUM_PHASES] = {0};
@@ -499,13 +508,13 @@ PoseRec pose_of(const gbmpm_collider &col, float tf, float dtf) {
 
 // Builds the [S][ncol] pose table for a tick and advances the host collider
 // records and clock exactly as S calls of _apply_grid_bc + time += dt would.
-void build_pose_table(gbmpm_engine *e, double &time, double dt, int S) {
+void build_pose_table(gbmpm_engine *e, PoseRec *out, double &time, double dt, int S) {
     int nc = (int)e->cols.size();
     int stride = std::max(1, nc);
     float dtf = (float)dt;
     for (int s = 0; s < S; ++s) {
         float tf = (float)time;
-        for (int c = 0; c < nc; ++c) e->h_pose[(size_t)s * stride + c] = pose_of(e->cols[c], tf, dtf);
+        for (int c = 0; c < nc; ++c) out[(size_t)s * stride + c] = pose_of(e->cols[c], tf, dtf);
         for (int c = 0; c < nc; ++c) integrate_pose(e->cols[c], time, dt);
         time = time + dt;
     }
@@ -882,9 +891,13 @@ int gbmpm_engine_create(gbmpm_engine **out) {
     if (const char *pd = std::getenv("GBMPM_NO_PDL")) e->pdl = std::atoi(pd) == 0;
     if (const char *fs = std::getenv("GBMPM_CDF_SPLIT_STAMP")) e->cdf_fused_stamp = std::atoi(fs) == 0;
     if (const char *gc = std::getenv("GBMPM_GRID_CTAS")) e->grid_ctas = std::max(1, std::min(8, std::atoi(gc)));
-    if (cudaEventCreateWithFlags(&e->pose_done, cudaEventDisableTiming) != cudaSuccess) {
-        delete e;
-        return fail(GBMPM_ERR_CUDA, "event create failed");
+    for (Staging &st : e->stage) {
+        if (cudaEventCreateWithFlags(&st.done, cudaEventDisableTiming) != cudaSuccess) {
+            for (Staging &o : e->stage)
+                if (o.done) cudaEventDestroy(o.done);
+            delete e;
+            return fail(GBMPM_ERR_CUDA, "event create failed");
+        }
     }
     *out = e;
     return GBMPM_OK;
@@ -895,10 +908,12 @@ void gbmpm_engine_destroy(gbmpm_engine *e) {
     if (!e) return;
     cudaDeviceSynchronize();
     if (e->graph) cudaGraphExecDestroy(e->graph);
-    if (e->pose_done) cudaEventDestroy(e->pose_done);
-    if (e->h_pose) cudaFreeHost(e->h_pose);
-    if (e->h_coldev) cudaFreeHost(e->h_coldev);
-    if (e->h_time) cudaFreeHost(e->h_time);
+    for (Staging &st : e->stage) {
+        if (st.done) cudaEventDestroy(st.done);
+        if (st.pose) cudaFreeHost(st.pose);
+        if (st.time) cudaFreeHost(st.time);
+        if (st.cols) cudaFreeHost(st.cols);
+    }
     e->d_bodies.release(); e->d_racc.release(); e->d_rkey.release(); e->d_mods.release(); e->d_time.release();
     e->d_rlist.release(); e->d_rcount.release();
     e->d_tab.release(); e->d_cols.release(); e->d_pose.release(); e->d_wrench.release();
@@ -981,7 +996,6 @@ int gbmpm_set_colliders(gbmpm_engine *e, const gbmpm_collider *c, int32_t n) {
     // The device table (fixed capacity, so its address never changes) is refreshed
     // on the stream of the next tick; a captured tick graph reads it at run time, so
     // only a change of the collider count needs a new capture.
-    if (!e->h_coldev) GB_CUDA(cudaMallocHost(&e->h_coldev, kMaxCol * sizeof(ColDev)));
     GB_CUDA(e->d_cols.ensure(kMaxCol));
     if (e->h_cols.size() != d.size() || std::memcmp(e->h_cols.data(), d.data(), d.size() * sizeof(ColDev)) != 0) {
         e->h_cols = d;
@@ -1219,40 +1233,43 @@ int prepare_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int
         return fail(GBMPM_ERR_ARG, "bad tick arguments");
     const int nc = (int)e->cols.size();
     const size_t need = (size_t)substeps * std::max(1, nc);
-    if (e->h_pose_cap < need) {
-        if (e->h_pose) { cudaEventSynchronize(e->pose_done); cudaFreeHost(e->h_pose); }
-        e->h_pose = nullptr;
-        GB_CUDA(cudaMallocHost(&e->h_pose, need * sizeof(PoseRec)));
-        e->h_pose_cap = need;
+    Staging &st = e->stage[e->stage_i];
+    e->stage_i = (e->stage_i + 1) % kStages;
+    GB_CUDA(cudaEventSynchronize(st.done));   // this slot's last upload (kStages ticks ago) has run
+    if (st.pose_cap < need) {
+        if (st.pose) cudaFreeHost(st.pose);
+        st.pose = nullptr;
+        GB_CUDA(cudaMallocHost(&st.pose, need * sizeof(PoseRec)));
+        st.pose_cap = need;
     }
+    if (!st.cols) GB_CUDA(cudaMallocHost(&st.cols, kMaxCol * sizeof(ColDev)));
     PoseRec *old_dev = e->d_pose.ptr;
     GB_CUDA(e->d_pose.ensure(need));
     if (e->d_pose.ptr != old_dev) mark_dirty(e);
-    GB_CUDA(cudaEventSynchronize(e->pose_done));
-    if (e->cols_upload) {   // the staging buffer is free once the previous upload is done
-        std::memcpy(e->h_coldev, e->h_cols.data(), e->h_cols.size() * sizeof(ColDev));
-        GB_CUDA(cudaMemcpyAsync(e->d_cols.ptr, e->h_coldev, e->h_cols.size() * sizeof(ColDev),
-                                cudaMemcpyHostToDevice, s));
+    if (e->cols_upload) {
+        std::memcpy(st.cols, e->h_cols.data(), e->h_cols.size() * sizeof(ColDev));
+        GB_CUDA(cudaMemcpyAsync(e->d_cols.ptr, st.cols, e->h_cols.size() * sizeof(ColDev), cudaMemcpyHostToDevice,
+                                s));
         e->cols_upload = false;
     }
     // substep start times (modifier and rigid-surface windows), as the tick advances them
-    if (e->h_time_cap < (size_t)substeps) {
-        if (e->h_time) cudaFreeHost(e->h_time);
-        e->h_time = nullptr;
-        GB_CUDA(cudaMallocHost(&e->h_time, (size_t)substeps * sizeof(double)));
-        e->h_time_cap = substeps;
+    if (st.time_cap < (size_t)substeps) {
+        if (st.time) cudaFreeHost(st.time);
+        st.time = nullptr;
+        GB_CUDA(cudaMallocHost(&st.time, (size_t)substeps * sizeof(double)));
+        st.time_cap = substeps;
     }
     double *old_time = e->d_time.ptr;
     GB_CUDA(e->d_time.ensure(substeps));
     if (e->d_time.ptr != old_time) mark_dirty(e);
     {
         double t = *time;
-        for (int i = 0; i < substeps; ++i) { e->h_time[i] = t; t = t + dt; }
+        for (int i = 0; i < substeps; ++i) { st.time[i] = t; t = t + dt; }
     }
-    GB_CUDA(cudaMemcpyAsync(e->d_time.ptr, e->h_time, (size_t)substeps * sizeof(double), cudaMemcpyHostToDevice, s));
-    build_pose_table(e, *time, dt, substeps);
-    GB_CUDA(cudaMemcpyAsync(e->d_pose.ptr, e->h_pose, need * sizeof(PoseRec), cudaMemcpyHostToDevice, s));
-    GB_CUDA(cudaEventRecord(e->pose_done, s));
+    GB_CUDA(cudaMemcpyAsync(e->d_time.ptr, st.time, (size_t)substeps * sizeof(double), cudaMemcpyHostToDevice, s));
+    build_pose_table(e, st.pose, *time, dt, substeps);
+    GB_CUDA(cudaMemcpyAsync(e->d_pose.ptr, st.pose, need * sizeof(PoseRec), cudaMemcpyHostToDevice, s));
+    GB_CUDA(cudaEventRecord(st.done, s));
     e->det = (flags & GBMPM_TICK_DETERMINISTIC) != 0;
     if (e->det) {
         // every material law but the rigid bodies' (7, 8); on the caller's particle order
