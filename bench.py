@@ -360,10 +360,10 @@ def adjoint_measure(n_scenes: int = 32, n_particles: int = 50_000, n_grid: int =
     a rollout of `substeps` substeps with checkpoints every `every`, the loss
     L = |x - x_target|^2 + |F - F_target|^2 over the final positions and the plate's
     per-segment reaction-force trace, and the reverse pass to v0, E, nu, the yield
-    and the plate's velocity. Every substep's state is kept from the forward pass
-    when the device holds them (3 GB a scene), so the reverse pass replays nothing.
-    Plain runs the scenes one after another; batched runs each scene's segments on
-    its own stream, forward and reverse."""
+    and the plate's velocity. Plain runs the scenes one after another, each keeping
+    every substep's state from its forward pass (3 GB a scene) so that its reverse
+    pass replays nothing; batched runs all forwards in one CUDA graph per segment and
+    the reverse passes, which replay their segments, on one stream per scene."""
     import torch
     from mpm_engine_gb300 import Solver, adjoint
     from mpm_engine_gb300.materials import vonmises
@@ -400,7 +400,7 @@ def adjoint_measure(n_scenes: int = 32, n_particles: int = 50_000, n_grid: int =
         return ([2.0 * (o[0].double() - xt) for o, xt in zip(outs, x_t)], [None] * len(outs),
                 [2.0 * (o[2] - ft) for o, ft in zip(outs, F_t)])
 
-    keep = [None]
+    keep = [None, None]
 
     def run(batched, k):
         for s, st in zip(scenes, starts):
@@ -423,6 +423,7 @@ def adjoint_measure(n_scenes: int = 32, n_particles: int = 50_000, n_grid: int =
             for i, s in enumerate(scenes):
                 t1 = time.perf_counter()
                 r = adjoint.BatchRollout([s], dt, k, every, batched=False, plates=[handles[i]])
+                keep[1] = r.keep
                 out = r.forward()[0]
                 torch.cuda.synchronize()
                 t_fwd += time.perf_counter() - t1
@@ -448,8 +449,9 @@ def adjoint_measure(n_scenes: int = 32, n_particles: int = 50_000, n_grid: int =
             "checkpoint_every": every, "dt": dt,
             "loss": "|x - x_target|^2 + |plate force trace - target trace|^2 (seeded target rollouts)",
             "gradients": ["v0", "mu and lam (so E and nu)", "yield_stress", "plate_velocity"],
-            "states": "every substep's state kept from the forward pass (no segment replay)" if keep[0] else
-                      "segments replayed from checkpoints in the reverse pass", "seconds": split,
+            "states": {"batched": "kept from the forward pass" if keep[0] else "segments replayed",
+                       "plain": "kept from the forward pass" if keep[1] else "segments replayed"},
+            "seconds": split,
             "particle_substeps_per_s": n_total * substeps / t_batch}
 
 
