@@ -521,8 +521,19 @@ __device__ __forceinline__ void grid_update(const GK &k, int cta, int nctas) {
     __shared__ ColDev s_cols[kMaxCol];
     __shared__ PoseRec s_pose[kMaxCol];
     __shared__ float s_acc[kMaxCol][6];
+    // a cup's glass lies inside the sphere of radius sqrt(outer_r^2 + half_h^2) about
+    // its centre, so its SDF exceeds the contact band at every node of a 4^3 block
+    // whose centre is farther than that radius plus the band plus the block's
+    // half-diagonal (1.5 sqrt(3) dx < 3 dx): such a block skips the cup, exactly
+    __shared__ float s_cull[kMaxCol];
     const int t = threadIdx.x;
-    for (int i = t; i < k.ncol; i += blockDim.x) { s_cols[i] = k.cols[i]; s_pose[i] = k.poses[i]; }
+    for (int i = t; i < k.ncol; i += blockDim.x) {
+        s_cols[i] = k.cols[i];
+        s_pose[i] = k.poses[i];
+        const ColDev &c = k.cols[i];
+        const float rc = sqrtf(c.outer_r * c.outer_r + c.half_h * c.half_h) + c.band_c + 3.0f * k.dx;
+        s_cull[i] = (c.kind == GBMPM_COLLIDER_CUP) ? rc * rc : -1.0f;
+    }
     for (int i = t; i < k.ncol * 6; i += blockDim.x) s_acc[i / 6][i % 6] = 0.0f;
     pdl_wait();   // the particle pass before this one deposits into gmv and fills the block list
     pdl_trigger();
@@ -560,7 +571,13 @@ __device__ __forceinline__ void grid_update(const GK &k, int cta, int nctas) {
             }
             if (k.damp < 1.0f) { v[0] *= k.damp; v[1] *= k.damp; v[2] *= k.damp; }
         }
+        const float cb[3] = {((float)(bx * 4) + 1.5f) * k.dx, ((float)(by * 4) + 1.5f) * k.dx,
+                             ((float)(bz * 4) + 1.5f) * k.dx};
         for (int c = 0; c < k.ncol; ++c) {
+            if (s_cull[c] > 0.0f) {   // uniform over the block, so over each warp
+                const float d0 = cb[0] - s_pose[c].p[0], d1 = cb[1] - s_pose[c].p[1], d2 = cb[2] - s_pose[c].p[2];
+                if (d0 * d0 + d1 * d1 + d2 * d2 > s_cull[c]) continue;
+            }
             float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (valid && m > 0.0f && s_pose[c].mode != 0) collide(s_cols[c], s_pose[c], gx, gy, gz, m, v, k, acc);
             int kind = s_cols[c].kind;
