@@ -1,7 +1,8 @@
 // svd3.cuh - 3x3 singular value decomposition for the particle return maps.
 //
 // Method (this project's own): cyclic Jacobi eigen-solve of the symmetric
-// B = F^T F with exact Givens rotations, a descending sort of the eigenvalues,
+// B = F^T F (the symmetric update of each rotation, which zeroes its pivot exactly),
+// a descending sort of the eigenvalues,
 // then a Givens QR of W = F V. U = Q and V are proper rotations; sigma = diag(R),
 // so sigma_1 >= sigma_2 >= |sigma_3| and sigma_3 carries the sign of det F. That
 // is the convention the material laws are written against (sigma_3 may be
@@ -24,28 +25,38 @@ template <>
 __device__ __forceinline__ double gb_sqrt<double>(double x) { return sqrt(x); }
 
 template <typename T>
-__device__ __forceinline__ void jacobi_rot(T (&B)[3][3], T (&V)[3][3], int p, int q) {
-    T bpq = B[p][q];
+__device__ __forceinline__ T gb_rsqrt(T x);
+template <>
+__device__ __forceinline__ float gb_rsqrt<float>(float x) { return __frsqrt_rn(x); }   // correctly rounded
+template <>
+__device__ __forceinline__ double gb_rsqrt<double>(double x) { return 1.0 / sqrt(x); }
+
+// One Jacobi rotation of the symmetric B in the (p, q) plane (r is the third index):
+// the rotation that zeroes B[p][q] is applied to the diagonal, to the two entries of
+// row r and, by symmetry, column r, and B[p][q] is set to zero (the classic
+// symmetric update: B'pp = Bpp - t Bpq, B'qq = Bqq + t Bpq, B'rp = c Brp - s Brq,
+// B'rq = s Brp + c Brq with t = sgn(theta) / (|theta| + sqrt(theta^2 + 1)),
+// theta = (Bqq - Bpp) / (2 Bpq), c = 1 / sqrt(t^2 + 1), s = t c); V accumulates
+// the rotation.
+template <typename T>
+__device__ __forceinline__ void jacobi_rot(T (&B)[3][3], T (&V)[3][3], int p, int q, int r) {
+    const T bpq = B[p][q];
     if (bpq == T(0)) return;
-    T theta = (B[q][q] - B[p][p]) / (T(2) * bpq);
-    T at = theta < T(0) ? -theta : theta;
+    const T theta = (B[q][q] - B[p][p]) / (T(2) * bpq);
+    const T at = theta < T(0) ? -theta : theta;
     T t;
     if (at > T(1e18)) t = T(0.5) / theta;
     else t = (theta >= T(0) ? T(1) : T(-1)) / (at + gb_sqrt<T>(theta * theta + T(1)));
-    T c = T(1) / gb_sqrt<T>(t * t + T(1));
-    T s = t * c;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        T bkp = B[k][p], bkq = B[k][q];
-        B[k][p] = c * bkp - s * bkq;
-        B[k][q] = s * bkp + c * bkq;
-    }
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        T bpk = B[p][k], bqk = B[q][k];
-        B[p][k] = c * bpk - s * bqk;
-        B[q][k] = s * bpk + c * bqk;
-    }
+    const T c = gb_rsqrt<T>(t * t + T(1));
+    const T s = t * c;
+    B[p][p] = B[p][p] - t * bpq;
+    B[q][q] = B[q][q] + t * bpq;
+    B[p][q] = T(0);
+    B[q][p] = T(0);
+    const T brp = B[r][p], brq = B[r][q];
+    const T nrp = c * brp - s * brq, nrq = s * brp + c * brq;
+    B[r][p] = nrp; B[p][r] = nrp;
+    B[r][q] = nrq; B[q][r] = nrq;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         T vkp = V[k][p], vkq = V[k][q];
@@ -101,9 +112,9 @@ __device__ __forceinline__ void svd3_t(const float* F, float* U, float* s, float
         T off = B[0][1] * B[0][1] + B[0][2] * B[0][2] + B[1][2] * B[1][2];
         T dia = B[0][0] * B[0][0] + B[1][1] * B[1][1] + B[2][2] * B[2][2];
         if (off <= tol * dia) break;
-        jacobi_rot<T>(B, V, 0, 1);
-        jacobi_rot<T>(B, V, 0, 2);
-        jacobi_rot<T>(B, V, 1, 2);
+        jacobi_rot<T>(B, V, 0, 1, 2);
+        jacobi_rot<T>(B, V, 0, 2, 1);
+        jacobi_rot<T>(B, V, 1, 2, 0);
     }
     // descending sort; each swap negates one column so V stays proper
     if (B[0][0] < B[1][1]) swap_col<T>(V, B, 0, 1);
