@@ -355,6 +355,55 @@ __device__ __forceinline__ void cdf_scan(const PK &k, const Stencil &s, const in
             }
 }
 
+// cdf_scan<true> without the node-tag cache, the stencil's x offset taken as a
+// rolled loop: the nodes are visited in the same order with the same arithmetic, so
+// every vote, mask and sum is the same, in a third of the unrolled body (the tiled
+// CPIC pass is bound by instruction fetch; it needs no node tags after the scan).
+__device__ __forceinline__ void cdf_scan_rolled(const PK &k, const Stencil &s, const int *T, const float *D,
+                                                CdfScan &c) {
+    c.votes[0] = c.votes[1] = c.votes[2] = c.votes[3] = 0.f;
+#pragma unroll
+    for (int l = 0; l < 4; ++l) c.side1[l] = c.side0[l] = 0;
+    c.d_hat = 0.f;
+    c.n_acc[0] = c.n_acc[1] = c.n_acc[2] = 0.f;
+    c.best_w = 0.f;
+    c.lane_p = 0;
+#pragma unroll 1
+    for (int i = 0; i < 3; ++i) {
+        const float wx = i == 0 ? s.w[0][0] : (i == 1 ? s.w[0][1] : s.w[0][2]);
+        const float dwx = i == 0 ? s.dw[0][0] : (i == 1 ? s.dw[0][1] : s.dw[0][2]);
+        const size_t row = (size_t)(s.b[0] + i) * k.ng;
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk) {
+                const size_t id = (row + (s.b[1] + j)) * k.ng + (s.b[2] + kk);
+                const int t = __ldg(T + id);
+                if (t == 0) continue;
+                const float w = wx * s.w[1][j] * s.w[2][kk];
+                const float dd = __ldg(D + id);
+                const int nbit = 1 << (9 * i + 3 * j + kk);
+#pragma unroll
+                for (int l = 0; l < 4; ++l)
+                    if ((t >> (2 * l)) & 1) {
+                        const bool plus = (t >> (2 * l + 1)) & 1;
+                        c.votes[l] += w * dd * (plus ? 1.0f : -1.0f);
+                        if (plus) c.side1[l] |= nbit;
+                        else c.side0[l] |= nbit;
+                    }
+                const int own = (t >> kCdfOwnerShift) & 3;
+                if (((t >> (2 * own)) & 1) == 0) continue;
+                const float sgn = ((t >> (2 * own + 1)) & 1) ? 1.0f : -1.0f;
+                c.d_hat += w * sgn * dd;
+                const float dw[3] = {dwx * s.w[1][j] * s.w[2][kk], wx * s.dw[1][j] * s.w[2][kk],
+                                     wx * s.w[1][j] * s.dw[2][kk]};
+#pragma unroll
+                for (int a = 0; a < 3; ++a) c.n_acc[a] += dw[a] * k.inv_dx * sgn * dd;
+                if (w > c.best_w) { c.best_w = w; c.lane_p = own; }
+            }
+    }
+}
+
 // the particle tag from the votes: valid per lane where a valid node was seen, side
 // from the sign of the vote
 __device__ __forceinline__ int cdf_vote_tag(const CdfScan &c) {
@@ -889,7 +938,7 @@ __device__ __forceinline__ void particles_tile(const PK &k, int mode, int tile) 
     if (CDF && want) {
         if (cdf_near(k, s)) {
             CdfScan cs;
-            cdf_scan<true>(k, s, k.ctag, k.cd, cs);
+            cdf_scan_rolled(k, s, k.ctag, k.cd, cs);
             pcs = cdf_persist(ptag, cdf_vote_tag(cs));
             if (pcs != 0) {
                 pmask = cdf_mask(pcs, cs);
