@@ -179,6 +179,8 @@ _SIGNATURES = {
     "gbmpm_launch_count": (C.c_int64, [C.c_void_p]),
     "gbmpm_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "gbmpm_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "gbmpm_set_resort": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gbmpm_get_resort": (C.c_int32, [C.c_void_p]),
     "gbmpm_debug_deposit_sums": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_double), C.c_void_p]),
     "gbmpm_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]),
     "gbmpm_batch_destroy": (None, [C.c_void_p]),

@@ -143,6 +143,16 @@ def set_solver_tuning(solver, tuning) -> None:
     _abi.check(solver._eng.lib.gbmpm_set_tuning(solver._eng.h, occ, gc), "gbmpm_set_tuning")
 
 
+def set_solver_resort(solver, substeps: int) -> None:
+    """Substeps between re-sorts of the solver's working copy inside a tick (0 sorts
+    once per tick). Long ticks keep the scatter's runs of one cell long this way."""
+    _abi.check(solver._eng.lib.gbmpm_set_resort(solver._eng.h, int(substeps)), "gbmpm_set_resort")
+
+
+def solver_resort(solver) -> int:
+    return int(solver._eng.lib.gbmpm_get_resort(solver._eng.h))
+
+
 def solver_tuning(solver) -> dict:
     out = (C.c_int32 * 2)()
     _abi.check(solver._eng.lib.gbmpm_get_tuning(solver._eng.h, out), "gbmpm_get_tuning")
@@ -175,5 +185,5 @@ def tune_solver(solver, dt: float, substeps: int, ticks: int = 2, candidates=Non
     return {**rec, "cached": False, "key": key}
 
 
-__all__ = ["batch_key", "batch_tuning", "cache_path", "set_batch_tuning", "set_solver_tuning", "solver_key",
-           "solver_tuning", "tune_batch", "tune_solver"]
+__all__ = ["batch_key", "batch_tuning", "cache_path", "set_batch_tuning", "set_solver_resort", "set_solver_tuning",
+           "solver_key", "solver_resort", "solver_tuning", "tune_batch", "tune_solver"]

@@ -170,6 +170,14 @@ struct gbmpm_engine {
     gbmpm_particles W{};
     WsTable ws_table{};
     int ws_n = -1;
+    // re-sorts inside a fused tick: every resort_every substeps (0: once per tick) the
+    // working copy is sorted again by its current cells into the second copy and back
+    int resort_every = 144;
+    DevBuf<float> ws_buf2;
+    gbmpm_particles W2{};
+    WsTable ws_table2{};
+    DevBuf<int> ws_perm[2];   // working row -> caller particle, composed over the re-sorts
+    int ws2_n = -1;
     // pinned staging of the per-tick uploads (pose table, substep times, collider
     // table): a ring, so that the host waits on the upload of kStages ticks ago rather
     // than on the last one, which is queued behind the last tick's work
@@ -330,8 +338,9 @@ void launch_particles(gbmpm_engine *e, const PK &k, int mode, bool tiled, cudaSt
 }
 
 // Allocates the block-sorted working copy and the table of fields the tick
-// gathers into it and scatters back (only fields a tick writes go back).
-cudaError_t ensure_ws(gbmpm_engine *e) {
+// gathers into it and scatters back (only fields a tick writes go back). With
+// `second`, also the second copy, with the same layout, that re-sorts write.
+cudaError_t ensure_ws(gbmpm_engine *e, bool second) {
     const gbmpm_particles &P = e->P;
     const int n = P.n;
     const bool cov = P.cov && e->M.update_cov_with_F;
@@ -356,18 +365,33 @@ cudaError_t ensure_ws(gbmpm_engine *e) {
     for (const Spec &sp : spec) if (sp.ext) total += (size_t)sp.w * n;
     cudaError_t err = e->ws_buf.ensure(total);
     if (err != cudaSuccess) return err;
+    if (second && (err = e->ws_buf2.ensure(total)) != cudaSuccess) return err;
     size_t off = 0;
     e->ws_table.nf = 0;
+    e->ws_table2.nf = 0;
+    std::vector<std::pair<size_t, size_t>> rebase;   // (member offset in gbmpm_particles, buffer offset)
     for (const Spec &sp : spec) {
         if (!sp.ext) { *sp.dst = nullptr; continue; }
         float *ws = e->ws_buf.ptr + off;
-        off += (size_t)sp.w * n;
         *sp.dst = ws;
         e->ws_table.f[e->ws_table.nf++] = WsField{sp.ext, ws, sp.w, sp.back};
+        if (second) {
+            e->ws_table2.f[e->ws_table2.nf++] = WsField{sp.ext, e->ws_buf2.ptr + off, sp.w, sp.back};
+            rebase.push_back({(size_t)(reinterpret_cast<char *>(sp.dst) - reinterpret_cast<char *>(&W)), off});
+        }
+        off += (size_t)sp.w * n;
     }
     W.density = nullptr;
     W.init_cov = nullptr;
     if (!cov) W.cov = nullptr;
+    if (second) {
+        e->W2 = W;
+        for (const auto &r : rebase)
+            *reinterpret_cast<float **>(reinterpret_cast<char *>(&e->W2) + r.first) = e->ws_buf2.ptr + r.second;
+        if ((err = e->ws_perm[0].ensure(n)) != cudaSuccess) return err;
+        if ((err = e->ws_perm[1].ensure(n)) != cudaSuccess) return err;
+    }
+    e->ws2_n = second ? n : -1;
     const int ntiles = (n + kSortTile - 1) / kSortTile;
     if ((err = e->ws_keys[0].ensure(n)) != cudaSuccess) return err;
     if ((err = e->ws_keys[1].ensure(n)) != cudaSuccess) return err;
@@ -378,12 +402,18 @@ cudaError_t ensure_ws(gbmpm_engine *e) {
     return cudaSuccess;
 }
 
-// Records the working-set sort + gather; returns the permutation buffer.
-const int *record_ws_begin(gbmpm_engine *e, cudaStream_t s) {
+// Records the stable sort of n rows by the cell keys of positions x (the caller's
+// records, or with soa the working copy's own components); returns the sorted row
+// indices (in ws_idx, which the next sort overwrites).
+const int *record_cell_sort(gbmpm_engine *e, const float *x, bool soa, cudaStream_t s) {
     const int n = e->P.n;
     const int ntiles = (n + kSortTile - 1) / kSortTile;
-    k_cell_keys<<<(n + 255) / 256, 256, 0, s>>>(e->P.x, n, e->M.inv_dx, e->G.n_grid, e->bd, e->ws_keys[0].ptr,
-                                                 e->ws_idx[0].ptr);
+    if (soa)
+        k_cell_keys<true><<<(n + 255) / 256, 256, 0, s>>>(x, n, e->M.inv_dx, e->G.n_grid, e->bd, e->ws_keys[0].ptr,
+                                                          e->ws_idx[0].ptr);
+    else
+        k_cell_keys<false><<<(n + 255) / 256, 256, 0, s>>>(x, n, e->M.inv_dx, e->G.n_grid, e->bd, e->ws_keys[0].ptr,
+                                                           e->ws_idx[0].ptr);
     e->launches++;
     unsigned long long maxkey = ((unsigned long long)e->bd * e->bd * e->bd << 6) - 1ull;
     int bits = 0;
@@ -398,9 +428,27 @@ const int *record_ws_begin(gbmpm_engine *e, cudaStream_t s) {
         e->launches += 3;
         cur ^= 1;
     }
-    k_ws_gather<<<(n + 255) / 256, 256, 0, s>>>(e->ws_table, e->ws_idx[cur].ptr, n);
-    e->launches++;
     return e->ws_idx[cur].ptr;
+}
+
+// Records the working-set sort + gather; returns the permutation buffer.
+const int *record_ws_begin(gbmpm_engine *e, cudaStream_t s) {
+    const int n = e->P.n;
+    const int *perm = record_cell_sort(e, e->P.x, false, s);
+    k_ws_gather<<<(n + 255) / 256, 256, 0, s>>>(e->ws_table, perm, n);
+    e->launches++;
+    return perm;
+}
+
+// Records a re-sort of the working copy inside a tick: `from` (positions x) is sorted
+// again by its current cells into `to`, and the row -> particle map perm_in into
+// perm_out.
+void record_ws_resort(gbmpm_engine *e, const float *x, const WsTable &from, const WsTable &to, const int *perm_in,
+                      int *perm_out, cudaStream_t s) {
+    const int n = e->P.n;
+    const int *idx = record_cell_sort(e, x, true, s);
+    k_ws_permute<<<(n + 255) / 256, 256, 0, s>>>(from, to, idx, perm_in, perm_out, n);
+    e->launches++;
 }
 
 GK make_gk(gbmpm_engine *e, float dt, int substep, int list) {
@@ -805,18 +853,46 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
     };
     const int *perm = nullptr;
     if (reorder) timed(5, [&] { perm = record_ws_begin(e, s); });
-    const gbmpm_particles &P = reorder ? e->W : e->P;
+    // the working copy the passes run on: a re-sort moves it to the other copy
+    const gbmpm_particles *cur = reorder ? &e->W : &e->P;
+    const WsTable *tab = &e->ws_table;
+    const gbmpm_particles &P0 = *cur;
     const bool cdf = e->cdf.n > 0;
-    const bool rigid = e->n_bodies > 0 && P.rigid_id && P.x_ref;
-    if (rigid && P.n > 0) {   // this tick's rigid particles, in its particle order
+    const bool rigid = e->n_bodies > 0 && P0.rigid_id && P0.x_ref;
+    if (rigid && P0.n > 0) {   // this tick's rigid particles, in its particle order
         cudaMemsetAsync(e->d_rcount.ptr, 0, sizeof(int), s);
-        const int g = (int)std::max<long long>(1, std::min<long long>((P.n + 255) / 256, (long long)e->num_sms * 8));
-        k_rigid_list<<<g, 256, 0, s>>>(P.material, P.selection, P.n, e->d_rlist.ptr, e->d_rcount.ptr);
+        const int g = (int)std::max<long long>(1, std::min<long long>((P0.n + 255) / 256, (long long)e->num_sms * 8));
+        k_rigid_list<<<g, 256, 0, s>>>(P0.material, P0.selection, P0.n, e->d_rlist.ptr, e->d_rcount.ptr);
         e->launches++;
     }
+    // Particles cross cells during a long tick and the scatter's runs of one cell
+    // break up; a fused tick without CPIC lanes, rigid bodies or modifiers sorts its
+    // working copy again every resort_every substeps, between a grid pass and the next
+    // fused pass.
+    const bool resort = reorder && fused && !cdf && !rigid && e->n_mods == 0 && e->resort_every > 0 &&
+                        S > e->resort_every && e->ws2_n == e->P.n;
+    int resorts = 0;
     double tc = t0;
     for (int sub = 0; sub < S; ++sub) {
         int list = sub & 1;
+        bool resorted = false;
+        if (resort && sub > 0 && sub % e->resort_every == 0) {
+            timed(5, [&] {
+                if (resorts == 0) {   // the tick's first map is in the sort buffers the re-sort reuses
+                    cudaMemcpyAsync(e->ws_perm[0].ptr, perm, (size_t)e->P.n * sizeof(int), cudaMemcpyDeviceToDevice, s);
+                }
+                const bool to2 = tab == &e->ws_table;
+                const WsTable *to = to2 ? &e->ws_table2 : &e->ws_table;
+                int *out = e->ws_perm[(resorts + 1) & 1].ptr;
+                record_ws_resort(e, cur->x, *tab, *to, e->ws_perm[resorts & 1].ptr, out, s);
+                tab = to;
+                cur = to2 ? &e->W2 : &e->W;
+                perm = out;
+            });
+            ++resorts;
+            resorted = true;
+        }
+        const gbmpm_particles &P = *cur;
         if (cdf) cdf_stamp(e, tc, fused, s);
         PK k = make_pk(e, P, dtf, list);
         k.sub = pose_offset + sub;
@@ -829,7 +905,12 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
             int mode = PASS_G2P | PASS_STRESS | PASS_P2G | (last_stress ? PASS_STORE_ALL : 0) |
                        (cdf ? PASS_STORE_VC : 0);
             k.rigid_defer = rigid ? 1 : 0;
+            // after a re-sort the pass waits for the whole permute in stream order: it
+            // loads particle rows before its programmatic wait
+            const bool pdl = e->pdl;
+            if (resorted) e->pdl = false;
             timed(2, [&] { launch_particles(e, k, mode, reorder, s); });
+            e->pdl = pdl;
             // the rigid tail of the previous substep, then its rigid particles' P2G
             if (rigid) record_rigid(e, P, dtf, pose_offset + sub - 1, pose_offset + sub, list, true, reorder, perm, s);
         }
@@ -847,13 +928,13 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
             cdf_copy_prev_box(e, e->cdf.stale_box, s);
             e->cdf.stale_set = false;
         }
-        PK k = make_pk(e, P, dtf, 0);
+        PK k = make_pk(e, *cur, dtf, 0);
         timed(4, [&] { launch_particles(e, k, PASS_G2P | PASS_RESET_LISTS, reorder, s); });
-        if (rigid) record_rigid(e, P, dtf, pose_offset + S - 1, pose_offset + S - 1, 0, false, reorder, perm, s);
+        if (rigid) record_rigid(e, *cur, dtf, pose_offset + S - 1, pose_offset + S - 1, 0, false, reorder, perm, s);
     }
     if (reorder) {
         timed(5, [&] {
-            k_ws_scatter<<<(e->P.n + 255) / 256, 256, 0, s>>>(e->ws_table, perm, e->P.n);
+            k_ws_scatter<<<(e->P.n + 255) / 256, 256, 0, s>>>(*tab, perm, e->P.n);
             e->launches++;
         });
     }
@@ -1226,7 +1307,7 @@ namespace {
 // Everything a tick needs before its launches: argument checks, the float64 pose
 // table for every substep (uploaded on stream s) and the working-set buffers.
 int prepare_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32_t flags, cudaStream_t s,
-                 bool &reorder) {
+                 bool &reorder, bool batched = false) {
     int rc = check_ready(e);
     if (rc) return rc;
     if (!time || substeps < 1 || substeps > GBMPM_MAX_SUBSTEPS || !(dt > 0.0))
@@ -1290,8 +1371,11 @@ int prepare_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int
         if (e->det_key[0].ptr != old_key) mark_dirty(e);
     }
     reorder = !e->det && (flags & GBMPM_TICK_REORDER) && !e->M.periodic_x && e->P.n > 0 && e->G.n_grid <= 1024;
-    if (reorder && e->ws_n != e->P.n) {
-        GB_CUDA(ensure_ws(e));
+    // the second working copy, for a tick long enough to re-sort inside (record_tick)
+    const bool second = reorder && !batched && (flags & GBMPM_TICK_FUSED) && e->resort_every > 0 &&
+                        substeps > e->resort_every && e->cdf.n == 0 && e->n_bodies == 0 && e->n_mods == 0;
+    if (reorder && (e->ws_n != e->P.n || (second && e->ws2_n != e->P.n))) {
+        GB_CUDA(ensure_ws(e, second || e->ws2_n == e->P.n));
         mark_dirty(e);
     }
     return GBMPM_OK;
@@ -1557,6 +1641,16 @@ int gbmpm_set_tuning(gbmpm_engine *e, int32_t tile_occ, int32_t grid_ctas) {
     return GBMPM_OK;
 }
 
+int gbmpm_set_resort(gbmpm_engine *e, int32_t substeps) {
+    if (!e) return fail(GBMPM_ERR_ARG, "null argument");
+    if (substeps < 0) return fail(GBMPM_ERR_ARG, "the re-sort interval is 0 (once per tick) or a substep count");
+    e->resort_every = substeps;
+    mark_dirty(e);
+    return GBMPM_OK;
+}
+
+int32_t gbmpm_get_resort(gbmpm_engine *e) { return e ? e->resort_every : -1; }
+
 int gbmpm_get_tuning(gbmpm_engine *e, int32_t out[2]) {
     if (!e || !out) return fail(GBMPM_ERR_ARG, "null argument");
     out[0] = e->tile_occ;
@@ -1793,7 +1887,7 @@ int gbmpm_batch_tick(gbmpm_batch *b, double *times, double dt, int32_t substeps,
     std::vector<char> reorder(n, 0);
     for (int i = 0; i < n; ++i) {
         bool r = false;
-        int rc = prepare_tick(b->engines[i], &times[i], dt, substeps, flags, s, r);
+        int rc = prepare_tick(b->engines[i], &times[i], dt, substeps, flags, s, r, true);
         if (rc) return rc;
         reorder[i] = r;
     }

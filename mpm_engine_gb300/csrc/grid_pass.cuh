@@ -6,7 +6,9 @@
 
 // ---- per-tick working set: block-sorted copy of the particles --------------
 // key = (4^3 block of the stencil base, cell within the block); positions are
-// clamped into the grid so every particle gets a key.
+// clamped into the grid so every particle gets a key. SOA reads the working copy's
+// own positions (a re-sort inside a tick), else the caller's records.
+template <bool SOA>
 __global__ void k_cell_keys(const float *x, int n, float inv_dx, int ng, int bd, unsigned long long *keys,
                             int *idx) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -14,7 +16,7 @@ __global__ void k_cell_keys(const float *x, int n, float inv_dx, int ng, int bd,
     int b[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        float g = x[3 * (size_t)p + a] * inv_dx - 0.5f;
+        float g = x[SOA ? (size_t)a * n + p : 3 * (size_t)p + a] * inv_dx - 0.5f;
         int c = isfinite(g) ? (int)floorf(fminf(fmaxf(g, 0.0f), (float)(ng - 1))) : 0;
         b[a] = c;
     }
@@ -47,6 +49,21 @@ __global__ void k_ws_gather(WsTable T, const int *perm, int n) {
         float *b = T.f[f].ws + i;
         for (int c = 0; c < w; ++c) b[(size_t)c * n] = a[c];
     }
+}
+
+// working copy -> the other working copy, re-sorted inside a tick: row i takes row
+// idx[i] of every field, and the map from working rows to caller particles follows
+__global__ void k_ws_permute(WsTable from, WsTable to, const int *idx, const int *perm_in, int *perm_out, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t src = (size_t)idx[i];
+    for (int f = 0; f < from.nf; ++f) {
+        const int w = from.f[f].width;
+        const float *a = from.f[f].ws + src;
+        float *b = to.f[f].ws + i;
+        for (int c = 0; c < w; ++c) b[(size_t)c * n] = a[(size_t)c * n];
+    }
+    perm_out[i] = perm_in[src];
 }
 
 __global__ void k_ws_scatter(WsTable T, const int *perm, int n) {

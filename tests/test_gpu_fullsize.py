@@ -9,7 +9,8 @@ size.
 - Per-substep parity with the oracle, composed over a few substeps, including both
   cups' wrench readouts. The oracle keeps up at this size: it does a few million
   particle-substeps per second on the host's cores.
-- Bit-exact block sort of the whole working set.
+- Bit-exact block sort of the whole working set, and the working copy re-sorted
+  inside a tick against the oracle.
 - Size-independent properties over many frames: every field finite, particles inside
   the grid, the cup fill's particle count and mass unchanged. Also, graph replay
   equals live launches to float-atomic rounding.
@@ -144,6 +145,40 @@ def test_pour_full_size_1000_substeps(cuda, oracle_lib, material):
     print(f"{material} pour 192^3, 1000 substeps: momentum {mom_err:.2e}, kinetic energy {ke_err:.2e}")
     assert mom_err <= 1e-3 and ke_err <= 1e-3, (material, mom_err, ke_err)
     np.testing.assert_array_equal(s._t["mass"].cpu().numpy(), o.a["mass"])
+
+
+@pytest.mark.parametrize("every,graph", [(3, True), (4, False)])
+def test_pour_full_size_resorts_inside_a_tick(cuda, oracle_lib, every, graph):
+    """One 12-substep tick whose working copy is sorted again every 3 substeps (three
+    re-sorts, ending on the second copy; captured as a graph) or every 4 (two, ending
+    on the first; live launches), from the frame-3 state of the pour: the particles
+    come back in the caller's order with every field within 12 x 1e-5 relative of
+    the oracle, which never reorders anything, and the mass unchanged."""
+    from mpm_engine_gb300.autotune import set_solver_resort, solver_resort
+    s, src, rcv, traj, S, dt = _pour()
+    assert solver_resort(s) == 144
+    for i in range(3):
+        _frame(s, src, traj, i, S, dt)
+    o = oracle_lib.OracleSolver.from_state(s.export_state(), N_GRID, 0.7, threads=16)
+    c, q, v, w = traj.command(3 / 60.0, 1.0 / 60.0)
+    for side in (s, o):
+        side.set_cup(src, center=c, quat=q, velocity=v, omega=w)
+    s._sim.use_cuda_graph = graph
+    set_solver_resort(s, every)
+    assert solver_resort(s) == every
+    launches = s.launch_count()
+    s.step(dt, 12)
+    resorted = s.launch_count() - launches
+    o.step(dt, 12)
+    errs = assert_close(s, o, 12 * 1e-5, f"pour at 192^3, re-sorted every {every} substeps")
+    print(f"pour 192^3, 12 substeps re-sorted every {every}: relative errors {errs}")
+    np.testing.assert_array_equal(s._t["mass"].cpu().numpy(), o.a["mass"])
+    # each re-sort is one key pass, three radix passes of three kernels (23 key bits
+    # at 192^3) and one permute, against the same tick sorted once
+    set_solver_resort(s, 0)
+    launches = s.launch_count()
+    s.step(dt, 12)
+    assert resorted - (s.launch_count() - launches) == (11 // every) * 11
 
 
 def test_pour_full_size_sort_bit_exact(cuda, oracle_lib):
