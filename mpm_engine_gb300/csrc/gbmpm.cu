@@ -213,6 +213,8 @@ struct gbmpm_engine {
     DevBuf<double> c_wrench;        // [4][6] reaction per lane (float64)
     DevBuf<double> c_partial;       // [CTA][4][6] per-CTA partials the transfer passes add into
     DevBuf<float> c_cache;          // [5][n] the tiled scatter's scan, read by the next gather
+    DevBuf<float> c_cache2;   // the scan cache of the second working copy (re-sorts)
+    float *c_cache_cur = nullptr;   // the scan cache of the copy the passes run on (null: c_cache)
     size_t c_partial_ctas = 0;
     int c_ng = 0;
     // adjoint segment storage and scratch (allocated by the first adjoint call)
@@ -281,7 +283,7 @@ PK make_pk(gbmpm_engine *e, const gbmpm_particles &P, float dt, int list) {
         k.cd = e->c_d.ptr; k.cd_prev = e->c_d_prev.ptr;
         k.ptag = P.cdf_tag;
         k.cwrench = e->c_partial.ptr;
-        k.ccache = e->c_cache.ptr;
+        k.ccache = e->c_cache_cur ? e->c_cache_cur : e->c_cache.ptr;
         std::memcpy(k.lanes.c_cur, H.c_cur, sizeof H.c_cur);
         std::memcpy(k.lanes.c_prev, H.c_prev, sizeof H.c_prev);
         std::memcpy(k.lanes.v_prev, H.v_prev, sizeof H.v_prev);
@@ -866,11 +868,15 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
         e->launches++;
     }
     // Particles cross cells during a long tick and the scatter's runs of one cell
-    // break up; a fused tick without CPIC lanes, rigid bodies or modifiers sorts its
-    // working copy again every resort_every substeps, between a grid pass and the next
-    // fused pass.
-    const bool resort = reorder && fused && !cdf && !rigid && e->n_mods == 0 && e->resort_every > 0 &&
-                        S > e->resort_every && e->ws2_n == e->P.n;
+    // break up; a fused tick without rigid bodies or modifiers sorts its working copy
+    // again every resort_every substeps, between a grid pass and the next fused pass.
+    // With CPIC lanes the per-row scan cache (written by a scatter, read by the next
+    // gather) moves with the rows.
+    e->c_cache_cur = nullptr;
+    const size_t ccache_n = 5 * (size_t)std::max(1, e->P.n);
+    const bool resort = reorder && fused && !rigid && e->n_mods == 0 && e->resort_every > 0 &&
+                        S > e->resort_every && e->ws2_n == e->P.n &&
+                        (!cdf || (e->c_cache2.ptr && e->c_cache2.n >= ccache_n && e->c_cache.n >= ccache_n));
     int resorts = 0;
     double tc = t0;
     for (int sub = 0; sub < S; ++sub) {
@@ -883,8 +889,14 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
                 }
                 const bool to2 = tab == &e->ws_table;
                 const WsTable *to = to2 ? &e->ws_table2 : &e->ws_table;
+                WsTable from_t = *tab, to_t = *to;
+                if (cdf) {   // the scan cache, 5 components a row
+                    from_t.f[from_t.nf++] = WsField{nullptr, to2 ? e->c_cache.ptr : e->c_cache2.ptr, 5, 0};
+                    to_t.f[to_t.nf++] = WsField{nullptr, to2 ? e->c_cache2.ptr : e->c_cache.ptr, 5, 0};
+                    e->c_cache_cur = to2 ? e->c_cache2.ptr : e->c_cache.ptr;
+                }
                 int *out = e->ws_perm[(resorts + 1) & 1].ptr;
-                record_ws_resort(e, cur->x, *tab, *to, e->ws_perm[resorts & 1].ptr, out, s);
+                record_ws_resort(e, cur->x, from_t, to_t, e->ws_perm[resorts & 1].ptr, out, s);
                 tab = to;
                 cur = to2 ? &e->W2 : &e->W;
                 perm = out;
@@ -938,6 +950,7 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
             e->launches++;
         });
     }
+    e->c_cache_cur = nullptr;   // each tick's first pass writes the scan cache afresh
     if (profile) {
         for (Mark &m : marks) {
             cudaEventSynchronize(m.b);
@@ -1005,7 +1018,7 @@ void gbmpm_engine_destroy(gbmpm_engine *e) {
     e->ws_buf.release(); e->ws_keys[0].release(); e->ws_keys[1].release(); e->ws_idx[0].release();
     e->ws_idx[1].release(); e->ws_hist.release();
     e->c_tag.release(); e->c_tag_prev.release(); e->c_block.release(); e->c_d.release(); e->c_d_prev.release();
-    e->c_wrench.release(); e->c_partial.release(); e->c_cache.release();
+    e->c_wrench.release(); e->c_partial.release(); e->c_cache.release(); e->c_cache2.release();
     e->adj_states.release(); e->adj_scratch.release(); e->adj_grid.release(); e->adj_box.release();
     e->det_key[0].release(); e->det_key[1].release(); e->det_idx[0].release(); e->det_idx[1].release();
     e->det_val.release(); e->det_hist.release();
@@ -1373,7 +1386,7 @@ int prepare_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int
     reorder = !e->det && (flags & GBMPM_TICK_REORDER) && !e->M.periodic_x && e->P.n > 0 && e->G.n_grid <= 1024;
     // the second working copy, for a tick long enough to re-sort inside (record_tick)
     const bool second = reorder && !batched && (flags & GBMPM_TICK_FUSED) && e->resort_every > 0 &&
-                        substeps > e->resort_every && e->cdf.n == 0 && e->n_bodies == 0 && e->n_mods == 0;
+                        substeps > e->resort_every && e->n_bodies == 0 && e->n_mods == 0;
     if (reorder && (e->ws_n != e->P.n || (second && e->ws2_n != e->P.n))) {
         GB_CUDA(ensure_ws(e, second || e->ws2_n == e->P.n));
         mark_dirty(e);
@@ -1403,6 +1416,8 @@ int gbmpm_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int32
             e->c_partial_ctas = ctas;
         }
         GB_CUDA(e->c_cache.ensure(5 * (size_t)std::max(1, e->P.n)));
+        if (e->resort_every > 0 && substeps > e->resort_every && (flags & GBMPM_TICK_FUSED))
+            GB_CUDA(e->c_cache2.ensure(5 * (size_t)std::max(1, e->P.n)));
         if (e->c_ng != e->M.n_grid) return fail(GBMPM_ERR_STATE, "CDF grids were sized for another n_grid");
         if (e->M.periodic_x) return fail(GBMPM_ERR_UNSUPPORTED, "CDF colliders do not wrap the periodic x axis");
         if (e->P.n > 0 && !e->P.cdf_tag) return fail(GBMPM_ERR_ARG, "CDF colliders need particles.cdf_tag");

@@ -32,7 +32,7 @@ struct WsField {
     int width;
     int back;   // copied back to the caller's buffer at the end of the tick
 };
-constexpr int kMaxWsFields = 20;
+constexpr int kMaxWsFields = 21;   // the 20 particle fields, plus the CPIC scan cache a re-sort carries
 struct WsTable {
     WsField f[kMaxWsFields];
     int nf;
