@@ -463,13 +463,15 @@ int gbmpm_set_tuning(gbmpm_engine *e, int32_t tile_occ, int32_t grid_ctas);
 int gbmpm_get_tuning(gbmpm_engine *e, int32_t out[2]);
 /* Re-sorts of the block-sorted working copy inside a tick (no counterpart in the
  * reference, whose particle order changes only through sort_interval): a fused tick
- * of more than `substeps` substeps, without CDF lanes, rigid bodies or particle
- * modifiers, sorts its working copy again by the particles' current cells every
- * `substeps` substeps, so the scatter's runs of one cell stay long as particles
- * move. 0 sorts once per tick. Default 144. The caller's particle order never
- * changes. */
+ * without rigid bodies or particle modifiers sorts its working copy again by the
+ * particles' current cells every `substeps` substeps, so the scatter's runs of one
+ * cell stay long as particles move; a re-sort that would leave less than half an
+ * interval of the tick is skipped. 0 sorts once per tick. GBMPM_RESORT_AUTO (the
+ * default) re-sorts ticks of S >= 100 substeps every max(50, S / 3) substeps. The
+ * caller's particle order never changes. */
+#define GBMPM_RESORT_AUTO (-1)
 int gbmpm_set_resort(gbmpm_engine *e, int32_t substeps);
-/* The re-sort interval (-1 for a null engine). */
+/* The re-sort setting (GBMPM_RESORT_AUTO, 0 or an interval; -2 for a null engine). */
 int32_t gbmpm_get_resort(gbmpm_engine *e);
 /* Test hook (no counterpart in the reference): deposits the current particle state
  * (stored stress, v, C; no stress update) into the grid with the P2G kernel,

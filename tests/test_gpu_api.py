@@ -108,3 +108,37 @@ def test_failed_capture_falls_back_to_live_launches(cuda):
     assert a._eng.lib.gbmpm_graph_state(a._eng.h) == -1
     assert b._sim._graph_A is not None
     np.testing.assert_allclose(a.x(), b.x(), rtol=1e-5, atol=1e-6)
+
+
+def test_resort_setting_and_automatic_interval(cuda):
+    """The working copy's re-sort interval (no counterpart in the reference). By
+    default a tick of S >= 100 substeps re-sorts every max(50, S / 3) substeps, none
+    leaving less than half an interval of the tick; 0 sorts once per tick; an
+    interval is taken as given; other negative settings are refused. Launch counts
+    tell the re-sorts apart (each one a key pass, three radix passes of three kernels
+    for 17 key bits at 48^3, and a permute), and every setting steps the blob alike."""
+    from mpm_engine_gb300 import Solver
+    from mpm_engine_gb300._abi import RESORT_AUTO
+    from mpm_engine_gb300.autotune import set_solver_resort, solver_resort
+    s, _ = blob_scene(Solver, "newtonian")
+    assert solver_resort(s) == RESORT_AUTO
+    with pytest.raises(ValueError):
+        set_solver_resort(s, -5)
+    state = s.state_dict()
+    counts, xs = {}, {}
+    for setting in (0, RESORT_AUTO, 30):
+        s.load_state_dict(state)
+        set_solver_resort(s, setting)
+        assert solver_resort(s) == setting
+        for S in (99, 100, 150):
+            n0 = s.launch_count()
+            s.step(1e-4, S)
+            counts[(setting, S)] = s.launch_count() - n0
+        xs[setting] = s.x()
+    extra = {key: counts[key] - counts[(0, key[1])] for key in counts}
+    # automatic: none at 99; at 50 of 100; at 50 and 100 of 150
+    assert (extra[(RESORT_AUTO, 99)], extra[(RESORT_AUTO, 100)], extra[(RESORT_AUTO, 150)]) == (0, 11, 22)
+    # every 30: 30 and 60 of 99 or 100 (90 would leave 9 or 10); 30 to 120 of 150
+    assert (extra[(30, 99)], extra[(30, 100)], extra[(30, 150)]) == (22, 22, 44)
+    for setting in (RESORT_AUTO, 30):
+        assert np.abs(xs[setting].astype(np.float64) - xs[0]).max() < 1e-4

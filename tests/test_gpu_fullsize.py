@@ -154,9 +154,10 @@ def test_pour_full_size_resorts_inside_a_tick(cuda, oracle_lib, every, graph):
     on the first; live launches), from the frame-3 state of the pour: the particles
     come back in the caller's order with every field within 12 x 1e-5 relative of
     the oracle, which never reorders anything, and the mass unchanged."""
+    from mpm_engine_gb300._abi import RESORT_AUTO
     from mpm_engine_gb300.autotune import set_solver_resort, solver_resort
     s, src, rcv, traj, S, dt = _pour()
-    assert solver_resort(s) == 144
+    assert solver_resort(s) == RESORT_AUTO
     for i in range(3):
         _frame(s, src, traj, i, S, dt)
     o = oracle_lib.OracleSolver.from_state(s.export_state(), N_GRID, 0.7, threads=16)
