@@ -467,8 +467,8 @@ int gbmpm_get_tuning(gbmpm_engine *e, int32_t out[2]);
  * particles' current cells every `substeps` substeps, so the scatter's runs of one
  * cell stay long as particles move; a re-sort that would leave less than half an
  * interval of the tick is skipped. 0 sorts once per tick. GBMPM_RESORT_AUTO (the
- * default) re-sorts ticks of S >= 100 substeps every max(50, S / 3) substeps. The
- * caller's particle order never changes. */
+ * default) re-sorts ticks of S >= 100 substeps of scenes of 150,000 particles or more
+ * every max(50, S / 3) substeps. The caller's particle order never changes. */
 #define GBMPM_RESORT_AUTO (-1)
 int gbmpm_set_resort(gbmpm_engine *e, int32_t substeps);
 /* The re-sort setting (GBMPM_RESORT_AUTO, 0 or an interval; -2 for a null engine). */

@@ -30,7 +30,9 @@ TICK_GRAPH = 2
 TICK_PROFILE = 4
 TICK_REORDER = 8
 TICK_DETERMINISTIC = 16
-RESORT_AUTO = -1   # gbmpm_set_resort: re-sort ticks of S >= 100 substeps every max(50, S / 3)
+# gbmpm_set_resort's automatic setting: ticks of S >= 100 substeps in scenes of 150,000
+# particles or more re-sort every max(50, S / 3) substeps
+RESORT_AUTO = -1
 
 COLLIDER_PLANE = 0
 COLLIDER_BOX = 1

@@ -146,7 +146,8 @@ def set_solver_tuning(solver, tuning) -> None:
 def set_solver_resort(solver, substeps: int) -> None:
     """Substeps between re-sorts of the solver's working copy inside a tick: 0 sorts
     once per tick, _abi.RESORT_AUTO (the default) every max(50, S / 3) substeps of a
-    tick of S >= 100. Long ticks keep the scatter's runs of one cell long this way."""
+    tick of S >= 100 in a scene of 150,000 particles or more. Long ticks keep the
+    scatter's runs of one cell long this way."""
     _abi.check(solver._eng.lib.gbmpm_set_resort(solver._eng.h, int(substeps)), "gbmpm_set_resort")
 
 

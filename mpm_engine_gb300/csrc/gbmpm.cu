@@ -435,12 +435,15 @@ const int *record_cell_sort(gbmpm_engine *e, const float *x, bool soa, cudaStrea
 }
 
 // Substeps between re-sorts of the working copy inside a tick of S substeps (0: none).
-// The automatic choice, from measurements of re-sort cost (about 0.15 ms at 340k
-// particles) against the longer scatter runs it buys: none below 100 substeps, else
-// every max(50, S / 3).
+// The automatic choice weighs a re-sort's cost (about 0.15 ms at 340k particles, its
+// eleven launches a fixed part of that) against the longer scatter runs it buys:
+// scenes of 150,000 particles or more (the 340k pour and the 362k dam break gained;
+// 64 scenes of 54k particles stepped one by one, one re-sort in each 100-substep
+// tick, ran 5 % slower), ticks of 100 substeps or more, every max(50, S / 3).
+constexpr int kResortMinParticles = 150000;
 int resort_interval(const gbmpm_engine *e, int S) {
     if (e->resort_every >= 0) return e->resort_every;
-    return S >= 100 ? std::max(50, S / 3) : 0;
+    return (S >= 100 && e->P.n >= kResortMinParticles) ? std::max(50, S / 3) : 0;
 }
 
 // Records the working-set sort + gather; returns the permutation buffer.

@@ -180,6 +180,14 @@ def test_pour_full_size_resorts_inside_a_tick(cuda, oracle_lib, every, graph):
     launches = s.launch_count()
     s.step(dt, 12)
     assert resorted - (s.launch_count() - launches) == (11 // every) * 11
+    if every == 3:   # the automatic interval at this size: a 150-substep tick re-sorts at 50 and 100
+        counts = []
+        for setting in (0, RESORT_AUTO):
+            set_solver_resort(s, setting)
+            launches = s.launch_count()
+            s.step(dt, 150)
+            counts.append(s.launch_count() - launches)
+        assert counts[1] - counts[0] == 2 * 11, counts
 
 
 def test_pour_full_size_sort_bit_exact(cuda, oracle_lib):
