@@ -882,9 +882,10 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
     }
     // Particles cross cells during a long tick and the scatter's runs of one cell
     // break up; a fused tick without rigid bodies or modifiers sorts its working copy
-    // again every resort_every substeps, between a grid pass and the next fused pass.
-    // With CPIC lanes the per-row scan cache (written by a scatter, read by the next
-    // gather) moves with the rows.
+    // again every `every` substeps (resort_interval), between a grid pass and the next
+    // fused pass, except where that would leave less than half an interval of the
+    // tick. With CPIC lanes the per-row scan cache (written by a scatter, read by the
+    // next gather) moves with the rows.
     e->c_cache_cur = nullptr;
     const size_t ccache_n = 5 * (size_t)std::max(1, e->P.n);
     const int every = resort_interval(e, S);
@@ -895,7 +896,6 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
     for (int sub = 0; sub < S; ++sub) {
         int list = sub & 1;
         bool resorted = false;
-        // (none that would leave less than half an interval to run)
         if (resort && sub > 0 && sub % every == 0 && 2 * (S - sub) >= every) {
             timed(5, [&] {
                 if (resorts == 0) {   // the tick's first map is in the sort buffers the re-sort reuses
