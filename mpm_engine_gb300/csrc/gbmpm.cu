@@ -1385,9 +1385,8 @@ int prepare_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int
                                   (1u << 10) | (1u << 11) | (1u << 12) | (1u << 13);
         if (e->M.material_mask & ~det_mats)
             return fail(GBMPM_ERR_UNSUPPORTED, "deterministic ticks do not cover rigid-body materials");
-        if (e->cdf.n > 0 || e->n_bodies > 0 || e->n_mods > 0)
-            return fail(GBMPM_ERR_UNSUPPORTED,
-                        "deterministic ticks support no CDF colliders, rigid bodies or particle modifiers");
+        if (e->cdf.n > 0 || e->n_bodies > 0)
+            return fail(GBMPM_ERR_UNSUPPORTED, "deterministic ticks support no CDF colliders or rigid bodies");
         const size_t nrec = (size_t)27 * std::max(1, e->P.n);
         if (nrec > (size_t)INT32_MAX) return fail(GBMPM_ERR_ARG, "too many particles for a deterministic tick");
         const unsigned long long *old_key = e->det_key[0].ptr;

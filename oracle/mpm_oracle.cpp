@@ -154,6 +154,50 @@ inline Real logr(Real x) { return (Real)dlog((double)x); }
 inline Real expr(Real x) { return (Real)dexp((double)x); }
 inline Real powr(Real x, Real y) { return (Real)dexp((double)y * dlog((double)x)); }
 
+// wp.sin, wp.cos and wp.acos of the particle rotation modifier, the same way:
+//   sin, cos: x = q pi/2 + r, q = round(x 2/pi) (|r| <= pi/4 for the angles the
+//             modifier forms), then the Taylor series of sin r to r^21 and of cos r to
+//             r^20 in nested form (the next terms are below 1e-23), and the quadrant;
+//   acos c = pi/2 - asin c for |c| <= 1/2, 2 asin sqrt((1 - c)/2) above 1/2 and
+//            pi - 2 asin sqrt((1 + c)/2) below -1/2, with the Taylor series of asin z
+//            (|z| <= 1/2) to z^51 in Horner form (the next term is below 1e-18).
+inline double dsincos(double x, bool want_cos) {
+    if (!(x == x) || x == HUGE_VAL || x == -HUGE_VAL) return NAN;
+    const double q = std::floor(x * 0.63661977236758134308 + 0.5);
+    const double r = x - q * 1.57079632679489661923;
+    const double r2 = r * r;
+    double ts = 1.0, tc = 1.0;
+    for (int k = 10; k >= 1; --k) {
+        ts = 1.0 - r2 * ts / (double)((2 * k) * (2 * k + 1));
+        tc = 1.0 - r2 * tc / (double)((2 * k - 1) * (2 * k));
+    }
+    const double sn = r * ts;
+    int n = (int)((long long)q & 3);
+    if (want_cos) n = (n + 1) & 3;   // cos x = sin(x + pi/2)
+    return n == 0 ? sn : (n == 1 ? tc : (n == 2 ? -sn : -tc));
+}
+inline double dasin_half(double z) {   // |z| <= 1/2
+    double coef[26];
+    double a = 1.0;   // (2n)! / (4^n (n!)^2)
+    for (int n = 0; n < 26; ++n) {
+        coef[n] = a / (double)(2 * n + 1);
+        a = a * (double)(2 * n + 1) / (double)(2 * n + 2);
+    }
+    const double z2 = z * z;
+    double t = coef[25];
+    for (int n = 24; n >= 0; --n) t = coef[n] + z2 * t;
+    return z * t;
+}
+inline double dacos(double c) {
+    if (!(c >= -1.0 && c <= 1.0)) return NAN;
+    if (c > 0.5) return 2.0 * dasin_half(std::sqrt((1.0 - c) * 0.5));
+    if (c < -0.5) return 3.14159265358979323846 - 2.0 * dasin_half(std::sqrt((1.0 + c) * 0.5));
+    return 1.57079632679489661923 - dasin_half(c);
+}
+inline Real sinr(Real x) { return (Real)dsincos((double)x, false); }
+inline Real cosr(Real x) { return (Real)dsincos((double)x, true); }
+inline Real acosr(Real c) { return (Real)dacos((double)c); }
+
 // warp mat*mat: t[i][j] += a[i][k]*b[k][j], k ascending from zero
 inline M3 mmul(const M3& a, const M3& b) {
     M3 t = zero33();
@@ -1487,10 +1531,10 @@ void apply_modifiers(const RP* P, int p, Real time_f, Real dt) {
                 for (int a = 0; a < 3; ++a) hz[a] = off[a] - on * d.normal[a];
                 const Real hd = std::sqrt(hz[0] * hz[0] + hz[1] * hz[1] + hz[2] * hz[2]);
                 const Real cosine = (off[0] * d.axis1[0] + off[1] * d.axis1[1] + off[2] * d.axis1[2]) / hd;
-                Real theta = std::acos(std::min<Real>(std::max<Real>(cosine, -1.0f), 1.0f));
+                Real theta = acosr(std::min<Real>(std::max<Real>(cosine, -1.0f), 1.0f));
                 if (!(off[0] * d.axis2[0] + off[1] * d.axis2[1] + off[2] * d.axis2[2] > 0.0f)) theta = -theta;
-                const Real a1 = -hd * std::sin(theta) * d.rotation_scale;
-                const Real a2 = hd * std::cos(theta) * d.rotation_scale;
+                const Real a1 = -hd * sinr(theta) * d.rotation_scale;
+                const Real a2 = hd * cosr(theta) * d.rotation_scale;
                 for (int a = 0; a < 3; ++a) v[a] = a1 * d.axis1[a] + a2 * d.axis2[a] + d.translation_scale * d.normal[a];
             }
         }
@@ -1678,6 +1722,13 @@ int gbmpm_oracle_get_rigid(gbmpm_rigid_body* bodies, int32_t nb) {
 int gbmpm_oracle_set_modifiers(const gbmpm_modifier* mods, int32_t n) {
     g_rigid.mods.assign(mods, mods + n);
     return GBMPM_OK;
+}
+
+// the oracle's own double sin (kind 0), cos (1) and acos (2) of n arguments, for the
+// tests that check them against the host's libm
+void gbmpm_oracle_trig(const double* x, int64_t n, int32_t kind, double* out) {
+    for (int64_t i = 0; i < n; ++i)
+        out[i] = kind == 2 ? dacos(x[i]) : dsincos(x[i], kind == 1);
 }
 
 // sizes and field offsets of the include/gbmpm.h records, so tests can check

@@ -91,6 +91,8 @@ def load(precision: int = 32):
     lib.gbmpm_oracle_set_rigid.argtypes = [P(_abi.RigidBody), C.c_int32, P(_abi.RigidSurface), C.c_int32]
     lib.gbmpm_oracle_get_rigid.argtypes = [P(_abi.RigidBody), C.c_int32]
     lib.gbmpm_oracle_set_modifiers.argtypes = [P(_abi.Modifier), C.c_int32]
+    lib.gbmpm_oracle_trig.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p]
+    lib.gbmpm_oracle_trig.restype = None
     _libs[precision] = lib
     return lib
 
@@ -109,6 +111,14 @@ def abi_layout() -> list[int]:
     out = np.zeros(10, np.int64)
     load().gbmpm_oracle_abi_layout(_p(out))
     return [int(v) for v in out]
+
+
+def trig(x: np.ndarray, kind: str) -> np.ndarray:
+    """The oracle's own double sin, cos or acos (the rotation modifier's functions)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    load().gbmpm_oracle_trig(_p(x), x.size, {"sin": 0, "cos": 1, "acos": 2}[kind], _p(out))
+    return out
 
 
 def svd3(F: np.ndarray):

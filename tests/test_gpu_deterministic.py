@@ -129,10 +129,34 @@ def test_deterministic_ticks_repeat_bitwise_and_match_the_fast_path(cuda):
     assert_close(c, view, 10 * 1e-5, "tiled path against the deterministic passes after 10 substeps")
 
 
-def test_deterministic_ticks_reject_particle_modifiers(cuda):
+@pytest.mark.parametrize("fused", [True, False])
+def test_deterministic_ticks_with_particle_modifiers_equal_oracle_bitwise(cuda, oracle_lib, fused):
+    """An impulse (active three substeps), a held velocity translation and a rotating
+    cylinder on the jelly blob. The rotation's acos, sin and cos are evaluated in
+    double by the written-out method both sides share, so the ticks stay bit for
+    bit equal to the oracle, which runs the reference's split pipeline."""
     from mpm_engine_gb300 import Solver
+    dt = 1.0e-4
+    s = scene(Solver, "jelly", fused=fused, deterministic=True)
+    s.add_impulse_on_particles((0.0, 0.0, 5.0e-4), dt, point=(0.17, 0.17, 0.06), size=(0.02, 0.02, 0.02), num_dt=3,
+                               start_time=2 * dt)
+    s.enforce_particle_velocity_translation((0.22, 0.22, 0.07), (0.015, 0.015, 0.015), (0.0, 0.3, 0.0), 0.0, 1.0)
+    s.enforce_particle_velocity_rotation((0.19, 0.19, 0.06), (0.3, 0.2, 1.0), (0.02, 0.025), 4.0, 0.1, 5 * dt, 1.0)
+    o = oracle_lib.OracleSolver.from_state(s.export_state(), NG, LIM, fused=fused, threads=1)
+    k = 0
+    for n in (1, 4, 15):
+        s.step(dt, n)
+        o.step(dt, n)
+        k += n
+        assert_bitwise(s, o, f"modifiers ({'fused' if fused else 'split'}) after {k} substeps")
+    assert abs(float(s.v()[:, 1].mean())) > 1e-3     # the translation drags the blob
+
+
+def test_deterministic_ticks_reject_cdf_colliders(cuda):
+    from mpm_engine_gb300 import Solver
+    from mpm_engine_gb300.geometry import sheet_cdf
     s = scene(Solver, "jelly", deterministic=True)
-    s.add_impulse_on_particles((0.0, 0.0, 1.0e-3), 1.0e-4)
+    s.add_cdf_collider(sheet_cdf("z"), center=(0.2, 0.2, 0.2))
     with pytest.raises(NotImplementedError, match="deterministic"):
         s.step(1.0e-4, 1)
 

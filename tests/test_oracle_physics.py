@@ -99,6 +99,24 @@ def test_svd_reconstructs_and_orders(oracle_lib):
         np.testing.assert_allclose(np.abs(s), np.linalg.svd(F.astype(np.float64))[1], rtol=2e-6, atol=1e-7)
 
 
+def test_own_sin_cos_acos_match_libm(oracle_lib):
+    """The oracle's written-out sin, cos and acos (the rotation modifier's; the
+    deterministic GPU passes state the same operations) against the host's libm, in
+    double over the angles and cosines the modifier forms, and rounded to float."""
+    rng = np.random.default_rng(11)
+    th = np.concatenate([rng.uniform(-np.pi, np.pi, 200000),
+                         [0.0, np.pi, -np.pi, np.pi / 2, -np.pi / 2, np.pi / 4, 1e-9, -3e-5]])
+    c = np.concatenate([rng.uniform(-1.0, 1.0, 200000), [-1.0, -0.5, 0.0, 0.5, 1.0, 1.0 - 1e-12, -1.0 + 1e-9]])
+    for kind, x, ref in (("sin", th, np.sin(th)), ("cos", th, np.cos(th)), ("acos", c, np.arccos(c))):
+        got = oracle_lib.trig(x, kind)
+        err = np.abs(got - ref)
+        assert err.max() < 1e-15, (kind, float(err.max()), float(x[np.argmax(err)]))
+        differ = np.float32(got) != np.float32(ref)
+        assert differ.mean() < 1e-4, (kind, int(differ.sum()))
+    assert np.isnan(oracle_lib.trig(np.array([1.5, np.nan]), "acos")).all()
+    assert np.isnan(oracle_lib.trig(np.array([np.inf, np.nan]), "sin")).all()
+
+
 @pytest.mark.parametrize("fused", [True, False])
 def test_interleaved_oracle_instances_do_not_interact(O, fused):
     """The oracle library keeps one grid for every instance (each substep clears the box
