@@ -177,8 +177,8 @@ typedef struct {
                                    grid tiles (results equal up to float summation order) */
 #define GBMPM_TICK_DETERMINISTIC 16  /* deterministic passes: every operation rounded once, P2G summed
                                         per node in particle order (sorted records, no float atomics);
-                                        bit-reproducible; every material law but the rigid bodies'
-                                        (rigid bodies, CDF lanes, particle modifiers:
+                                        bit-reproducible; every material law but the rigid bodies',
+                                        and the particle modifiers (rigid bodies, CDF lanes:
                                         GBMPM_ERR_UNSUPPORTED) */
 
 #define GBMPM_NUM_PHASES 6      /* stress, p2g, g2p2g_fused, grid_update, g2p, sort+gather/scatter */

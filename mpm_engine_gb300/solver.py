@@ -330,7 +330,7 @@ class Solver:
     periodic_x: bool = False
     # deterministic passes: every operation rounded once and P2G summed per node in
     # particle order, so runs repeat bit for bit (every material law but the rigid
-    # bodies'; slower than the fast path)
+    # bodies', and the particle modifiers; slower than the fast path)
     deterministic: bool = False
     _sim: Any = field(default=None, init=False, repr=False)
     _step: int = field(default=0, init=False, repr=False)
