@@ -463,10 +463,9 @@ int gbmpm_set_tuning(gbmpm_engine *e, int32_t tile_occ, int32_t grid_ctas);
 int gbmpm_get_tuning(gbmpm_engine *e, int32_t out[2]);
 /* Re-sorts of the block-sorted working copy inside a tick (no counterpart in the
  * reference, whose particle order changes only through sort_interval): a fused tick
- * without rigid bodies or particle modifiers sorts its working copy again by the
- * particles' current cells every `substeps` substeps, so the scatter's runs of one
- * cell stay long as particles move; a re-sort that would leave less than half an
- * interval of the tick is skipped. 0 sorts once per tick. GBMPM_RESORT_AUTO (the
+ * sorts its working copy again by the particles' current cells every `substeps`
+ * substeps, so the scatter's runs of one cell stay long as particles move; a re-sort
+ * that would leave less than half an interval of the tick is skipped. 0 sorts once per tick. GBMPM_RESORT_AUTO (the
  * default) re-sorts ticks of S >= 100 substeps of scenes of 150,000 particles or more
  * every max(50, S / 3) substeps. The caller's particle order never changes. */
 #define GBMPM_RESORT_AUTO (-1)

@@ -874,22 +874,24 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
     const gbmpm_particles &P0 = *cur;
     const bool cdf = e->cdf.n > 0;
     const bool rigid = e->n_bodies > 0 && P0.rigid_id && P0.x_ref;
-    if (rigid && P0.n > 0) {   // this tick's rigid particles, in its particle order
+    auto rigid_rows = [&](const gbmpm_particles &P) {   // this tick's rigid particles, in its particle order
         cudaMemsetAsync(e->d_rcount.ptr, 0, sizeof(int), s);
-        const int g = (int)std::max<long long>(1, std::min<long long>((P0.n + 255) / 256, (long long)e->num_sms * 8));
-        k_rigid_list<<<g, 256, 0, s>>>(P0.material, P0.selection, P0.n, e->d_rlist.ptr, e->d_rcount.ptr);
+        const int g = (int)std::max<long long>(1, std::min<long long>((P.n + 255) / 256, (long long)e->num_sms * 8));
+        k_rigid_list<<<g, 256, 0, s>>>(P.material, P.selection, P.n, e->d_rlist.ptr, e->d_rcount.ptr);
         e->launches++;
-    }
+    };
+    if (rigid && P0.n > 0) rigid_rows(P0);
     // Particles cross cells during a long tick and the scatter's runs of one cell
-    // break up; a fused tick without rigid bodies or modifiers sorts its working copy
-    // again every `every` substeps (resort_interval), between a grid pass and the next
-    // fused pass, except where that would leave less than half an interval of the
-    // tick. With CPIC lanes the per-row scan cache (written by a scatter, read by the
-    // next gather) moves with the rows.
+    // break up; a fused tick sorts its working copy again every `every` substeps
+    // (resort_interval), between a grid pass and the next fused pass, except where
+    // that would leave less than half an interval of the tick. Every per-particle
+    // field moves with the rows (the modifier masks among them); with CPIC lanes the
+    // per-row scan cache (written by a scatter, read by the next gather) moves too,
+    // and with rigid bodies the list of rigid rows is rebuilt.
     e->c_cache_cur = nullptr;
     const size_t ccache_n = 5 * (size_t)std::max(1, e->P.n);
     const int every = resort_interval(e, S);
-    const bool resort = reorder && fused && !rigid && e->n_mods == 0 && every > 0 && S > every && e->ws2_n == e->P.n &&
+    const bool resort = reorder && fused && every > 0 && S > every && e->ws2_n == e->P.n &&
                         (!cdf || (e->c_cache2.ptr && e->c_cache2.n >= ccache_n && e->c_cache.n >= ccache_n));
     int resorts = 0;
     double tc = t0;
@@ -914,6 +916,7 @@ void record_tick(gbmpm_engine *e, float dtf, int S, bool fused, bool reorder, cu
                 tab = to;
                 cur = to2 ? &e->W2 : &e->W;
                 perm = out;
+                if (rigid) rigid_rows(*cur);
             });
             ++resorts;
             resorted = true;
@@ -1399,8 +1402,7 @@ int prepare_tick(gbmpm_engine *e, double *time, double dt, int32_t substeps, int
     reorder = !e->det && (flags & GBMPM_TICK_REORDER) && !e->M.periodic_x && e->P.n > 0 && e->G.n_grid <= 1024;
     // the second working copy, for a tick long enough to re-sort inside (record_tick)
     const int every = resort_interval(e, substeps);
-    const bool second = reorder && !batched && (flags & GBMPM_TICK_FUSED) && every > 0 && substeps > every &&
-                        e->n_bodies == 0 && e->n_mods == 0;
+    const bool second = reorder && !batched && (flags & GBMPM_TICK_FUSED) && every > 0 && substeps > every;
     if (reorder && (e->ws_n != e->P.n || (second && e->ws2_n != e->P.n))) {
         GB_CUDA(ensure_ws(e, second || e->ws2_n == e->P.n));
         mark_dirty(e);

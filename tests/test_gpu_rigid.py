@@ -32,12 +32,17 @@ def _rigid_close(s, o, tol, what):
         assert err <= tol, f"{what}: rigid {k} relative error {err:.3g} > {tol}"
 
 
-@pytest.mark.parametrize("water", [False, True])
-def test_rigid_body_matches_oracle(cuda, oracle_lib, water):
+@pytest.mark.parametrize("water,resort", [(False, False), (True, False), (True, True)])
+def test_rigid_body_matches_oracle(cuda, oracle_lib, water, resort):
     """A tilted cube thrown, spinning, at a restitution floor (alone: 12 ticks, into
     the floor with the deepest-corner impulse) or into a water slab (6 ticks:
-    two-way coupling through the grid, the cube pushing the fluid)."""
+    two-way coupling through the grid, the cube pushing the fluid); with `resort`,
+    the working copy is sorted again at substeps 3 and 6 of each tick, and the list
+    of rigid rows is rebuilt after each re-sort."""
     s, o = _pair(cuda, oracle_lib, water=water)
+    if resort:
+        from mpm_engine_gb300.autotune import set_solver_resort
+        set_solver_resort(s, 3)
     for t in range(6 if water else 12):
         s.step(DT, SUB)
         o.step(DT, SUB)
@@ -77,12 +82,18 @@ def test_rigid_body_api_and_reference_views(cuda):
         s.rigid_state(1)
 
 
-def test_particle_modifiers_match_oracle(cuda, oracle_lib):
+@pytest.mark.parametrize("resort", [False, True])
+def test_particle_modifiers_match_oracle(cuda, oracle_lib, resort):
     """An impulse (active 3 substeps), a held translation and a rotating cylinder on
-    one jelly blob, GPU fused tick against the oracle's split pipeline."""
+    one jelly blob, GPU fused tick against the oracle's split pipeline; with
+    `resort`, the working copy (modifier masks included) is sorted again at
+    substeps 3 and 6 of each tick."""
     from mpm_engine_gb300 import Solver, elastic
+    from mpm_engine_gb300.autotune import set_solver_resort
     pts, vol = blob(n=3000, lo=0.12, size=0.12)
     s = make(Solver, 40, 0.4).load_particles(pts, vol)
+    if resort:
+        set_solver_resort(s, 3)
     s.set_material(elastic(E=2e4, nu=0.3, density=1000.0))
     s.add_domain_walls()
     s.add_impulse_on_particles((0.0, 0.0, 5.0e-4), DT, point=(0.15, 0.15, 0.15), size=(0.03, 0.03, 0.03), num_dt=3,
